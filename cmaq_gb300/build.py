@@ -1,0 +1,81 @@
+"""Build the CUDA chemistry library in-tree for sm_103a.
+
+    python -m cmaq_gb300.build
+
+Compiles every translation unit under ``cmaq_gb300/csrc`` (the C ABI, the grid kernels
+per mechanism and the generated device code, which is sharded into several files) as
+relocatable device code in parallel, then links ``cmaq_gb300/_build/libcmaqchem.so``.
+The solver code is compiled with ``-fmad=false``: every fused multiply-add in it is an
+explicit ``fma`` so its rounding matches the CPU oracle.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG / "csrc"
+BUILD = PKG / "_build"
+LIB = BUILD / "libcmaqchem.so"
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-rdc=true", "-fmad=false", "-lineinfo", "-Xcompiler", "-fPIC",
+              "-Xptxas", "-O3"]
+
+
+def _nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and Path(cand).exists():
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def sources() -> list[Path]:
+    return sorted(CSRC.glob("*.cu")) + sorted((CSRC / "gen").glob("*.cu"))
+
+
+def _headers() -> list[Path]:
+    return sorted(CSRC.glob("*.cuh")) + sorted((CSRC / "gen").glob("*.cuh")) + [PKG.parent / "include" / "cmaqchem.h"]
+
+
+def build(jobs: int | None = None, verbose: bool = False) -> Path:
+    BUILD.mkdir(exist_ok=True)
+    nvcc = _nvcc()
+    hdr_mtime = max(p.stat().st_mtime for p in _headers())
+    todo, objs = [], []
+    for src in sources():
+        rel = src.relative_to(CSRC).as_posix().replace("/", "__")
+        obj = BUILD / (rel[:-3] + ".o")
+        objs.append(obj)
+        if obj.exists() and obj.stat().st_mtime > max(src.stat().st_mtime, hdr_mtime):
+            continue
+        todo.append((src, obj))
+
+    def compile_one(item):
+        src, obj = item
+        cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-I", str(CSRC), "-c", str(src), "-o", str(obj) + ".tmp"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed on {src.name}:\n{r.stderr[-4000:]}")
+        os.replace(str(obj) + ".tmp", obj)
+        if verbose:
+            print("compiled", src.name, flush=True)
+
+    if todo:
+        with ThreadPoolExecutor(max_workers=jobs or os.cpu_count() or 4) as ex:
+            list(ex.map(compile_one, todo))
+    if todo or not LIB.exists():
+        cmd = [nvcc, *ARCH, "-shared", "-rdc=true", *[str(o) for o in objs], "-o", str(LIB) + ".tmp"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stderr[-4000:]}")
+        os.replace(str(LIB) + ".tmp", LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose=True))
+    sys.exit(0)

@@ -1,0 +1,151 @@
+// Generated by cmaq_gb300.mechgen.generate from CCTM/src/MECHS/cb6r5_ae7_aq/RXNS_DATA_MODULE.F90
+// and RXNS_FUNC_MODULE.F90 (sha256/16 4242f44b2527a299).  Do not edit.
+#pragma once
+#include <cuda_runtime.h>
+#ifndef CHEM_HD
+#define CHEM_HD __device__
+#endif
+namespace mech_cb6r5_ae7_aq {
+constexpr const char* NAME = "cb6r5_ae7_aq";
+constexpr int NSPEC = 149;
+constexpr int NRXNS = 349;
+constexpr int ISCHAN = 149;
+constexpr int NPHOTAB = 32;
+constexpr int NHETERO = 17;
+constexpr int WS_ELEMS = 4116;
+constexpr int OFF_Y = 0;
+constexpr int OFF_YP = 149;
+constexpr int OFF_YDOT = 298;
+constexpr int OFF_F0 = 447;
+constexpr int OFF_K1 = 596;
+constexpr int OFF_K2 = 745;
+constexpr int OFF_K3 = 894;
+constexpr int OFF_RKI = 1043;
+constexpr int OFF_RXRAT = 1392;
+constexpr int OFF_LU = 2277;
+constexpr int OFF_VDIAG = 3967;
+constexpr int IARRAY_DAY = 1689;
+constexpr int IARRAY_NIGHT = 1615;
+constexpr double FLOPS_STEP_DAY = 36947.0;
+constexpr double FLOPS_STEP_NIGHT = 34766.0;
+extern __constant__ int c_inew2old[149];
+extern __constant__ int c_iold2new[149];
+static const int h_inew2old[149] = {112, 113, 114, 116, 117, 118, 120, 121, 14, 15, 43, 50, 68, 86, 101, 104, 105, 106, 108, 109, 110, 5, 122, 124, 126, 127, 41, 42, 46, 47, 49, 56, 60, 62, 73, 77, 80, 87, 94, 103, 9, 107, 19, 115, 119, 123, 125, 132, 143, 145, 148, 58, 59, 12, 36, 83, 85, 89, 99, 100, 102, 25, 48, 147, 64, 65, 67, 72, 84, 13, 98, 27, 131, 138, 139, 140, 142, 11, 79, 54, 81, 93, 96, 51, 20, 28, 128, 129, 130, 66, 29, 137, 75, 141, 144, 146, 97, 70, 53, 135, 136, 91, 95, 63, 82, 111, 45, 55, 8, 74, 90, 52, 78, 69, 32, 133, 134, 61, 34, 76, 38, 57, 21, 71, 92, 40, 33, 37, 22, 23, 2, 10, 44, 39, 31, 3, 30, 1, 17, 16, 35, 26, 88, 24, 0, 4, 18, 7, 6};
+static const int h_iold2new[149] = {144, 137, 130, 135, 145, 21, 148, 147, 108, 40, 131, 77, 53, 69, 8, 9, 139, 138, 146, 42, 84, 122, 128, 129, 143, 61, 141, 71, 85, 90, 136, 134, 114, 126, 118, 140, 54, 127, 120, 133, 125, 26, 27, 10, 132, 106, 28, 29, 62, 30, 11, 83, 111, 98, 79, 107, 31, 121, 51, 52, 32, 117, 33, 103, 64, 65, 89, 66, 12, 113, 97, 123, 67, 34, 109, 92, 119, 35, 112, 78, 36, 80, 104, 55, 68, 56, 13, 37, 142, 57, 110, 101, 124, 81, 38, 102, 82, 96, 70, 58, 59, 14, 60, 39, 15, 16, 17, 41, 18, 19, 20, 105, 0, 1, 2, 43, 3, 4, 5, 44, 6, 7, 22, 45, 23, 46, 24, 25, 86, 87, 88, 72, 47, 115, 116, 99, 100, 91, 73, 74, 75, 93, 76, 48, 94, 49, 95, 63, 50};
+static const int h_cgrid_index[149] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18, 19, 20, 21, 22, 23, 24, 25, 26, 27, 28, 29, 30, 31, 34, 35, 36, 37, 38, 39, 40, 41, 42, 43, 44, 45, 46, 47, 48, 33, 32, 49, 50, 51, 52, 53, 54, 55, 56, 57, 58, 59, 60, 61, 62, 64, 65, 69, 67, 66, 70, 71, 72, 73, 74, 75, 76, 77, 78, 79, 80, 81, 82, 83, 84, 85, 86, 87, 88, 89, 90, 91, 92, 93, 94, 95, 96, 124, 125, 126, 123, 97, 98, 99, 100, 101, 141, 142, 143, 63, 131, 176, 179, 68, 180, 181, 205, 177, 206, 207, 144, 178, 145, 146, 182, 184, 183, 185, 112, 113, 102, 103, 104, 105, 106, 107, 108, 110, 111, 109, 114, 115, 116, 117, 118, 119, 120, 121, 122, 127, 128};
+static const int h_convert[149] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 0, 1, 1, 1, 0, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+static const double h_molwt[149] = {46.0, 30.0, 16.0, 48.0, 62.0, 16.0, 17.0, 33.0, 34.0, 108.0, 63.0, 47.0, 79.0, 64.0, 98.0, 98.0, 75.0, 47.0, 87.1, 121.0, 76.0, 60.0, 89.0, 44.0, 87.1, 135.0, 30.0, 48.0, 32.0, 90.1, 87.1, 87.1, 119.1, 135.1, 46.0, 28.0, 63.0, 58.1, 60.0, 58.0, 72.0, 30.1, 46.1, 72.1, 14.0, 58.1, 44.1, 89.1, 45.0, 29.0, 26.0, 28.0, 42.1, 56.1, 68.1, 117.1, 68.1, 70.1, 147.1, 118.1, 116.1, 115.0, 118.1, 149.1, 136.2, 136.2, 197.0, 136.2, 78.1, 108.1, 159.1, 84.0, 127.0, 92.1, 173.1, 141.0, 98.1, 106.2, 187.1, 155.0, 128.2, 187.2, 107.1, 124.1, 153.1, 161.0, 16.0, 71.0, 35.5, 52.5, 51.5, 64.5, 36.5, 81.5, 97.5, 179.0, 169.0, 158.0, 198.0, 204.0, 204.0, 112.0, 64.0, 64.0, 35.5, 35.5, 35.5, 118.1, 96.0, 168.2, 66.4, 231.0, 231.0, 168.0, 179.0, 206.0, 169.0, 158.0, 132.0, 248.0, 133.0, 273.0, 220.0, 220.0, 220.0, 220.0, 170.0, 170.0, 218.0, 230.0, 241.0, 253.0, 266.0, 136.0, 136.0, 135.0, 134.0, 135.0, 30.0, 44.0, 54.0, 56.1, 56.1, 92.0, 200.6, 200.6, 271.5, 62.0, 96.0};
+__device__ void rconst(double* __restrict__ ws, double temp_in, double press, double h2o, double seawater, int lsunlight, const double* __restrict__ rjv, const double* __restrict__ hetv);
+__device__ void feval_0(double* __restrict__ ws, int src, int dst);
+__device__ void explic_0(double* __restrict__ ws);
+__device__ void feval_1(double* __restrict__ ws, int src, int dst);
+__device__ void explic_1(double* __restrict__ ws);
+__device__ void jacdecomp_0_0(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_1(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_2(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_3(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_4(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_5(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_6(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_7(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_8(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_9(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_10(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_11(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_12(double* __restrict__ ws, double gdtinv);
+__device__ void solve_0_0(double* __restrict__ ws, int rhs);
+__device__ void solve_0_1(double* __restrict__ ws, int rhs);
+__device__ void solve_0_2(double* __restrict__ ws, int rhs);
+__device__ void jacdecomp_1_0(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_1(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_2(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_3(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_4(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_5(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_6(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_7(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_8(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_9(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_10(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_11(double* __restrict__ ws, double gdtinv);
+__device__ void solve_1_0(double* __restrict__ ws, int rhs);
+__device__ void solve_1_1(double* __restrict__ ws, int rhs);
+__device__ void solve_1_2(double* __restrict__ ws, int rhs);
+__device__ __forceinline__ void jacdecomp_0(double* __restrict__ ws, double gdtinv)
+{
+    jacdecomp_0_0(ws, gdtinv);
+    jacdecomp_0_1(ws, gdtinv);
+    jacdecomp_0_2(ws, gdtinv);
+    jacdecomp_0_3(ws, gdtinv);
+    jacdecomp_0_4(ws, gdtinv);
+    jacdecomp_0_5(ws, gdtinv);
+    jacdecomp_0_6(ws, gdtinv);
+    jacdecomp_0_7(ws, gdtinv);
+    jacdecomp_0_8(ws, gdtinv);
+    jacdecomp_0_9(ws, gdtinv);
+    jacdecomp_0_10(ws, gdtinv);
+    jacdecomp_0_11(ws, gdtinv);
+    jacdecomp_0_12(ws, gdtinv);
+}
+__device__ __forceinline__ void solve_0(double* __restrict__ ws, int rhs)
+{
+    solve_0_0(ws, rhs);
+    solve_0_1(ws, rhs);
+    solve_0_2(ws, rhs);
+}
+__device__ __forceinline__ void jacdecomp_1(double* __restrict__ ws, double gdtinv)
+{
+    jacdecomp_1_0(ws, gdtinv);
+    jacdecomp_1_1(ws, gdtinv);
+    jacdecomp_1_2(ws, gdtinv);
+    jacdecomp_1_3(ws, gdtinv);
+    jacdecomp_1_4(ws, gdtinv);
+    jacdecomp_1_5(ws, gdtinv);
+    jacdecomp_1_6(ws, gdtinv);
+    jacdecomp_1_7(ws, gdtinv);
+    jacdecomp_1_8(ws, gdtinv);
+    jacdecomp_1_9(ws, gdtinv);
+    jacdecomp_1_10(ws, gdtinv);
+    jacdecomp_1_11(ws, gdtinv);
+}
+__device__ __forceinline__ void solve_1(double* __restrict__ ws, int rhs)
+{
+    solve_1_0(ws, rhs);
+    solve_1_1(ws, rhs);
+    solve_1_2(ws, rhs);
+}
+struct Traits {
+    static constexpr int NSPEC = mech_cb6r5_ae7_aq::NSPEC;
+    static constexpr int NRXNS = mech_cb6r5_ae7_aq::NRXNS;
+    static constexpr int ISCHAN = mech_cb6r5_ae7_aq::ISCHAN;
+    static constexpr int NPHOTAB = mech_cb6r5_ae7_aq::NPHOTAB;
+    static constexpr int NHETERO = mech_cb6r5_ae7_aq::NHETERO;
+    static constexpr int WS_ELEMS = mech_cb6r5_ae7_aq::WS_ELEMS;
+    static constexpr int OFF_Y = mech_cb6r5_ae7_aq::OFF_Y;
+    static constexpr int OFF_YP = mech_cb6r5_ae7_aq::OFF_YP;
+    static constexpr int OFF_YDOT = mech_cb6r5_ae7_aq::OFF_YDOT;
+    static constexpr int OFF_F0 = mech_cb6r5_ae7_aq::OFF_F0;
+    static constexpr int OFF_K1 = mech_cb6r5_ae7_aq::OFF_K1;
+    static constexpr int OFF_K2 = mech_cb6r5_ae7_aq::OFF_K2;
+    static constexpr int OFF_K3 = mech_cb6r5_ae7_aq::OFF_K3;
+    static constexpr int OFF_RKI = mech_cb6r5_ae7_aq::OFF_RKI;
+    static constexpr int OFF_RXRAT = mech_cb6r5_ae7_aq::OFF_RXRAT;
+    static constexpr int OFF_LU = mech_cb6r5_ae7_aq::OFF_LU;
+    static constexpr int OFF_VDIAG = mech_cb6r5_ae7_aq::OFF_VDIAG;
+    static constexpr int IARRAY_DAY = mech_cb6r5_ae7_aq::IARRAY_DAY;
+    static constexpr int IARRAY_NIGHT = mech_cb6r5_ae7_aq::IARRAY_NIGHT;
+    static constexpr const char* name() { return mech_cb6r5_ae7_aq::NAME; }
+    static __device__ __forceinline__ int iold2new(int s) { return mech_cb6r5_ae7_aq::c_iold2new[s]; }
+    static __device__ __forceinline__ int inew2old(int i) { return mech_cb6r5_ae7_aq::c_inew2old[i]; }
+    static __device__ __forceinline__ void feval_0(double* ws, int s, int t) { mech_cb6r5_ae7_aq::feval_0(ws, s, t); }
+    static __device__ __forceinline__ void explic_0(double* ws) { mech_cb6r5_ae7_aq::explic_0(ws); }
+    static __device__ __forceinline__ void jacdecomp_0(double* ws, double g) { mech_cb6r5_ae7_aq::jacdecomp_0(ws, g); }
+    static __device__ __forceinline__ void solve_0(double* ws, int r) { mech_cb6r5_ae7_aq::solve_0(ws, r); }
+    static __device__ __forceinline__ void feval_1(double* ws, int s, int t) { mech_cb6r5_ae7_aq::feval_1(ws, s, t); }
+    static __device__ __forceinline__ void explic_1(double* ws) { mech_cb6r5_ae7_aq::explic_1(ws); }
+    static __device__ __forceinline__ void jacdecomp_1(double* ws, double g) { mech_cb6r5_ae7_aq::jacdecomp_1(ws, g); }
+    static __device__ __forceinline__ void solve_1(double* ws, int r) { mech_cb6r5_ae7_aq::solve_1(ws, r); }
+    static __device__ __forceinline__ void rconst(double* ws, double t, double p, double h, double sw, int sun,
+                                                  const double* rj, const double* het) { mech_cb6r5_ae7_aq::rconst(ws, t, p, h, sw, sun, rj, het); }
+};
+}  // namespace mech_cb6r5_ae7_aq

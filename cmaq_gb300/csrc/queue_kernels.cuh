@@ -1,0 +1,151 @@
+// Batched ("queue") scheduling of the per-cell ROS3 integration.
+//
+// The reference balances stiffness by a first pass that estimates each cell's
+// stiffness, heap-sorts the cells and re-blocks them (rbdriver.F:430-434, 683-724;
+// Jacobson 1994).  Here a persistent grid pulls cells from a device work queue: a lane
+// that finishes its cell takes the next one at once, so a warp is no longer held by
+// its slowest cell.  The queue is ordered by each cell's step attempts in the previous
+// call, most first (a counting sort over step-count bins), so long cells start early
+// and the tail is short.  Every cell is integrated exactly as in k_chem_ros3; the
+// schedule changes no result bit.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "chem_kernels.cuh"
+
+namespace chem {
+
+constexpr int QUEUE_BINS = 256;
+
+struct QueueArgs {
+    const int* order;                 // [ncell] cell indices in queue order, or nullptr for 0..ncell-1
+    unsigned long long* head;         // next queue position (zeroed before the launch)
+};
+
+template <class M>
+__global__ void __launch_bounds__(THREADS_PER_BLOCK, 1) k_chem_ros3_queue(GridArgs a, QueueArgs q)
+{
+    const int lane = threadIdx.x & 31;
+    const long long warp = (long long)blockIdx.x * WARPS_PER_BLOCK + (threadIdx.x >> 5);
+    double* ws = warp_ws<M>(a.ws, warp);
+    ros3::CellState s;
+    long long cell = -1;
+    bool sun = false;
+    bool drained = false;
+    unsigned long long acc_steps = 0, rej_steps = 0, failed = 0, sunlit = 0;
+    for (;;) {
+        // refill idle lanes with one atomic per warp
+        if (!drained) {
+            const unsigned need = __ballot_sync(0xffffffffu, cell < 0);
+            if (need) {
+                const int leader = __ffs(need) - 1;
+                unsigned long long base = 0;
+                if (lane == leader) base = atomicAdd(q.head, (unsigned long long)__popc(need));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (cell < 0) {
+                    const unsigned long long pos = base + __popc(need & ((1u << lane) - 1u));
+                    if (pos < (unsigned long long)a.ncell) {
+                        cell = q.order ? q.order[pos] : (long long)pos;
+                        sun = gather_cell<M>(a, cell, ws);
+                        ros3::start(s);
+                    }
+                }
+                drained = __any_sync(0xffffffffu, base + __popc(need) >= (unsigned long long)a.ncell);
+            }
+        }
+        const bool busy = cell >= 0;
+        if (!__any_sync(0xffffffffu, busy)) break;
+        const bool night = __all_sync(0xffffffffu, !busy || !sun);
+        if (busy) {
+            ros3::attempt<M>(ws, s, a.chemstep, a.tol, night, a.max_iter);
+            if (ros3::finished(s, a.chemstep)) {
+                scatter_cell<M>(a, cell, ws);
+                acc_steps += s.st.nsteps;
+                rej_steps += s.st.nfails;
+                failed += s.st.status != ros3::ST_OK;
+                sunlit += sun;
+                if (a.cell_status) a.cell_status[cell] = s.st.status;
+                if (a.cell_steps) a.cell_steps[cell] = s.st.nsteps + s.st.nfails;
+                cell = -1;
+            }
+        }
+    }
+    if (a.counters) {
+        for (int o = 16; o > 0; o >>= 1) {
+            acc_steps += __shfl_down_sync(0xffffffffu, acc_steps, o);
+            rej_steps += __shfl_down_sync(0xffffffffu, rej_steps, o);
+            failed += __shfl_down_sync(0xffffffffu, failed, o);
+            sunlit += __shfl_down_sync(0xffffffffu, sunlit, o);
+        }
+        if (lane == 0) {
+            atomicAdd(&a.counters[0], acc_steps);
+            atomicAdd(&a.counters[1], rej_steps);
+            atomicAdd(&a.counters[2], failed);
+            atomicAdd(&a.counters[3], sunlit);
+        }
+    }
+}
+
+// ---- queue ordering: counting sort of cells by previous step attempts, descending
+
+__device__ __forceinline__ int queue_bin(int steps)
+{
+    const int b = steps < 0 ? 0 : (steps >= QUEUE_BINS ? QUEUE_BINS - 1 : steps);
+    return QUEUE_BINS - 1 - b;   // bin 0 = most steps
+}
+
+static __global__ void k_queue_hist(const int* __restrict__ steps, long long ncell, unsigned int* __restrict__ hist)
+{
+    __shared__ unsigned int h[QUEUE_BINS];
+    for (int i = threadIdx.x; i < QUEUE_BINS; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < ncell;
+         c += (long long)gridDim.x * blockDim.x)
+        atomicAdd(&h[queue_bin(steps[c])], 1u);
+    __syncthreads();
+    for (int i = threadIdx.x; i < QUEUE_BINS; i += blockDim.x)
+        if (h[i]) atomicAdd(&hist[i], h[i]);
+}
+
+// exclusive scan of the histogram into per-bin write cursors (one block of QUEUE_BINS threads)
+static __global__ void k_queue_scan(const unsigned int* __restrict__ hist, unsigned long long* __restrict__ cursor)
+{
+    __shared__ unsigned long long v[QUEUE_BINS];
+    const int t = threadIdx.x;
+    v[t] = hist[t];
+    __syncthreads();
+    for (int o = 1; o < QUEUE_BINS; o <<= 1) {
+        const unsigned long long x = t >= o ? v[t - o] : 0ull;
+        __syncthreads();
+        v[t] += x;
+        __syncthreads();
+    }
+    cursor[t] = v[t] - hist[t];
+}
+
+static __global__ void k_queue_scatter(const int* __restrict__ steps, long long ncell,
+                                unsigned long long* __restrict__ cursor, int* __restrict__ order)
+{
+    __shared__ unsigned int cnt[QUEUE_BINS];
+    __shared__ unsigned long long base[QUEUE_BINS];
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long c0 = (long long)blockIdx.x * blockDim.x; c0 < ncell; c0 += stride) {
+        for (int i = threadIdx.x; i < QUEUE_BINS; i += blockDim.x) cnt[i] = 0;
+        __syncthreads();
+        const long long c = c0 + threadIdx.x;
+        int b = 0;
+        unsigned int rank = 0;
+        if (c < ncell) {
+            b = queue_bin(steps[c]);
+            rank = atomicAdd(&cnt[b], 1u);
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < QUEUE_BINS; i += blockDim.x)
+            base[i] = cnt[i] ? atomicAdd(&cursor[i], (unsigned long long)cnt[i]) : 0ull;
+        __syncthreads();
+        if (c < ncell) order[base[b] + rank] = (int)c;
+        __syncthreads();
+    }
+}
+
+}  // namespace chem

@@ -1,0 +1,359 @@
+"""Emit fully unrolled FP64 device code for one mechanism.
+
+Per-cell working storage lives in a per-warp block ``[element][lane]`` of global
+memory: element ``k`` of a cell is at ``ws[k * 32]`` from the cell's thread
+pointer, so each access of a warp is one contiguous 256-byte row and every
+offset is a compile-time immediate.
+
+Generated functions (namespace ``mech_<name>``; ``d`` = 0 day, 1 night):
+
+* ``rconst``          rate constants, restating CALC_RCONST (RXNS_FUNC_MODULE.F90)
+* ``feval_d``         YDOT = f(Y), reactions in the active order of rbfeval.F:80-151
+* ``explic_d``        per-reaction partial-derivative products of rbjacob.F:112-143
+* ``jacdecomp_d``     Jacobian (rbjacob.F), diagonal shift (rbsolver.F:377-381) and
+                      LU without pivoting (rbdecomp.F), fused and ordered by rows
+* ``solve_d``         forward / backward substitution (rbsolve.F)
+
+Every sum is accumulated in the reference's order and every ``x +/- a*b`` of the
+reference is a single ``fma``; the translation unit is compiled with
+``-fmad=false`` so no other contraction happens.  The CPU oracle applies the
+same rule, so both compute the same sums with the same roundings.
+"""
+from __future__ import annotations
+
+from .emit_common import RATE_HELPERS, c_double
+from .fortran_tables import Mechanism
+from .rate_expr import RateProgram
+from .sparse import SparseMech, flop_counts
+
+
+class Layout:
+    """Element offsets of the per-cell workspace."""
+
+    def __init__(self, m: Mechanism, sp: SparseMech):
+        ns, nr = m.nspec, m.nrxns
+        off = 0
+        self.y = off; off += ns
+        self.yp = off; off += ns
+        self.ydot = off; off += ns
+        self.f0 = off; off += ns
+        self.k1 = off; off += ns
+        self.k2 = off; off += ns
+        self.k3 = off; off += ns
+        self.rki = off; off += nr
+        self.rxrat = off; off += nr
+        # partial-derivative products of multi-reactant reactions
+        self.ex = {}
+        for r in sp.active[0]:
+            if m.nreact[r] >= 2:
+                for ial in range(m.nreact[r]):
+                    self.ex[(r, ial)] = off
+                    off += 1
+        self.lu = off; off += max(sp.iarray) + 1      # 1-based storage, slot 0 unused
+        self.vdiag = off; off += sp.ischan
+        self.total = off
+
+
+def _w(k: int) -> str:
+    return f"ws[{k * 32}]"
+
+
+def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src_hash: str) -> dict[str, str]:
+    """Return {file name: text}: one header with declarations and the kernel traits,
+    and several translation units of device functions that compile in parallel
+    (relocatable device code)."""
+    lay = Layout(m, sp)
+    ns, nr, n = m.nspec, m.nrxns, sp.ischan
+    ns_name = f"mech_{mech}"
+    banner = [f"// Generated by cmaq_gb300.mechgen.generate from CCTM/src/MECHS/{mech}/RXNS_DATA_MODULE.F90",
+              f"// and RXNS_FUNC_MODULE.F90 (sha256/16 {src_hash}).  Do not edit."]
+    units: dict[str, list[str]] = {}
+    units["rates"] = _rconst(m, prog, lay)
+    for d in range(2):
+        units["rates"] += _feval(m, sp, lay, d) + _explic(m, sp, lay, d)
+    decls: list[str] = ["__device__ void rconst(double* __restrict__ ws, double temp_in, double press, double h2o, "
+                        "double seawater, int lsunlight, const double* __restrict__ rjv, const double* __restrict__ hetv);"]
+    for d in range(2):
+        decls.append(f"__device__ void feval_{d}(double* __restrict__ ws, int src, int dst);")
+        decls.append(f"__device__ void explic_{d}(double* __restrict__ ws);")
+    wrappers: list[str] = []
+    for d in range(2):
+        chunks = _jacdecomp_chunks(m, sp, lay, d)
+        for ci, code in enumerate(chunks):
+            unit = f"lu{d}_{ci // 3}"
+            units.setdefault(unit, []).extend(code)
+            decls.append(f"__device__ void jacdecomp_{d}_{ci}(double* __restrict__ ws, double gdtinv);")
+        wrappers.append(f"__device__ __forceinline__ void jacdecomp_{d}(double* __restrict__ ws, double gdtinv)")
+        wrappers.append("{")
+        wrappers.extend(f"    jacdecomp_{d}_{ci}(ws, gdtinv);" for ci in range(len(chunks)))
+        wrappers.append("}")
+        schunks = _solve_chunks(sp, lay, d)
+        for ci, code in enumerate(schunks):
+            unit = f"solve{d}"
+            units.setdefault(unit, []).extend(code)
+            decls.append(f"__device__ void solve_{d}_{ci}(double* __restrict__ ws, int rhs);")
+        wrappers.append(f"__device__ __forceinline__ void solve_{d}(double* __restrict__ ws, int rhs)")
+        wrappers.append("{")
+        wrappers.extend(f"    solve_{d}_{ci}(ws, rhs);" for ci in range(len(schunks)))
+        wrappers.append("}")
+
+    h = banner + ["#pragma once", "#include <cuda_runtime.h>", "#ifndef CHEM_HD", "#define CHEM_HD __device__",
+                  "#endif", f"namespace {ns_name} {{", f'constexpr const char* NAME = "{mech}";']
+    consts = (("NSPEC", ns), ("NRXNS", nr), ("ISCHAN", n), ("NPHOTAB", m.nphotab),
+              ("NHETERO", m.nhetero), ("WS_ELEMS", lay.total), ("OFF_Y", lay.y), ("OFF_YP", lay.yp),
+              ("OFF_YDOT", lay.ydot), ("OFF_F0", lay.f0), ("OFF_K1", lay.k1), ("OFF_K2", lay.k2),
+              ("OFF_K3", lay.k3), ("OFF_RKI", lay.rki), ("OFF_RXRAT", lay.rxrat), ("OFF_LU", lay.lu),
+              ("OFF_VDIAG", lay.vdiag), ("IARRAY_DAY", sp.iarray[0]), ("IARRAY_NIGHT", sp.iarray[1]))
+    for k, v in consts:
+        h.append(f"constexpr int {k} = {v};")
+    h.append(f"constexpr double FLOPS_STEP_DAY = {float(flop_counts(m, sp, 0)['step_total'])};")
+    h.append(f"constexpr double FLOPS_STEP_NIGHT = {float(flop_counts(m, sp, 1)['step_total'])};")
+    h.append(f"extern __constant__ int c_inew2old[{ns}];")
+    h.append(f"extern __constant__ int c_iold2new[{ns}];")
+    h.append(f"static const int h_inew2old[{ns}] = {{{', '.join(map(str, sp.inew2old))}}};")
+    h.append(f"static const int h_iold2new[{ns}] = {{{', '.join(map(str, sp.iold2new))}}};")
+    h.append(f"static const int h_cgrid_index[{ns}] = {{{', '.join(str(x - 1) for x in m.cgrid_index)}}};")
+    h.append(f"static const int h_convert[{ns}] = {{{', '.join('1' if c else '0' for c in m.convert_conc)}}};")
+    h.append(f"static const double h_molwt[{ns}] = {{{', '.join(c_double(x) for x in m.molwt)}}};")
+    h.extend(decls)
+    h.extend(wrappers)
+    h.append("struct Traits {")
+    for k, _ in consts:
+        h.append(f"    static constexpr int {k} = {ns_name}::{k};")
+    h.append(f"    static constexpr const char* name() {{ return {ns_name}::NAME; }}")
+    h.append(f"    static __device__ __forceinline__ int iold2new(int s) {{ return {ns_name}::c_iold2new[s]; }}")
+    h.append(f"    static __device__ __forceinline__ int inew2old(int i) {{ return {ns_name}::c_inew2old[i]; }}")
+    for d in range(2):
+        h.append(f"    static __device__ __forceinline__ void feval_{d}(double* ws, int s, int t) {{ {ns_name}::feval_{d}(ws, s, t); }}")
+        h.append(f"    static __device__ __forceinline__ void explic_{d}(double* ws) {{ {ns_name}::explic_{d}(ws); }}")
+        h.append(f"    static __device__ __forceinline__ void jacdecomp_{d}(double* ws, double g) {{ {ns_name}::jacdecomp_{d}(ws, g); }}")
+        h.append(f"    static __device__ __forceinline__ void solve_{d}(double* ws, int r) {{ {ns_name}::solve_{d}(ws, r); }}")
+    h.append("    static __device__ __forceinline__ void rconst(double* ws, double t, double p, double h, double sw, int sun,")
+    h.append(f"                                                  const double* rj, const double* het) {{ {ns_name}::rconst(ws, t, p, h, sw, sun, rj, het); }}")
+    h.append("};")
+    h.append(f"}}  // namespace {ns_name}")
+    files = {f"{mech}_mech.cuh": "\n".join(h) + "\n"}
+    for unit, body in units.items():
+        t = banner + [f'#include "{mech}_mech.cuh"', "#include <math.h>", f"namespace {ns_name} {{"]
+        if unit == "rates":
+            t.append(RATE_HELPERS)
+            t.append(f"__constant__ int c_inew2old[{ns}] = {{{', '.join(map(str, sp.inew2old))}}};")
+            t.append(f"__constant__ int c_iold2new[{ns}] = {{{', '.join(map(str, sp.iold2new))}}};")
+        t.extend(body)
+        t.append(f"}}  // namespace {ns_name}")
+        files[f"{mech}_{unit}.cu"] = "\n".join(t) + "\n"
+    return files
+
+
+def _rconst(m: Mechanism, prog: RateProgram, lay: Layout) -> list[str]:
+    from .generate import rate_body
+    o = ["// Rate constants of one cell into ws[OFF_RKI + r] (CALC_RCONST, RXNS_FUNC_MODULE.F90).",
+         "__device__ __noinline__ void rconst(double* __restrict__ ws, double temp_in, double press, double h2o,",
+         "                                    double seawater, int lsunlight, const double* __restrict__ rjv,",
+         "                                    const double* __restrict__ hetv)",
+         "{"]
+    body = rate_body(m, prog, "c",
+                     rki=lambda k: _w(lay.rki + k),
+                     rj=lambda k: f"rjv[{k}]",
+                     het=lambda k: f"hetv[{k}]",
+                     indent="    ")
+    o.extend(body)
+    o.append("}")
+    return o
+
+
+def _feval(m: Mechanism, sp: SparseMech, lay: Layout, d: int) -> list[str]:
+    """ws[dst..] = f(ws[src..]) in two phases: reaction rates into ws (RXRAT of
+    rbfeval.F:88-127), then each species' rate of change summed over its loss and
+    production terms in the reference's reaction order (rbfeval.F:129-151)."""
+    contrib: dict[int, list] = {}
+    for r in sp.active[d]:
+        for i in range(m.nreact[r]):
+            contrib.setdefault(sp.irm2[r][i], []).append((r, None))
+        for p in range(m.nprdct[r]):
+            contrib.setdefault(sp.irm2[r][3 + p], []).append((r, m.sc[r][p]))
+    o = [f"// f(y) for the {'day' if d == 0 else 'night'} reaction list (rbfeval.F:80-151).",
+         f"__device__ __noinline__ void feval_{d}(double* __restrict__ ws, int src, int dst)",
+         "{",
+         "    const double* __restrict__ yin = ws + src * 32;",
+         "    double* __restrict__ yout = ws + dst * 32;"]
+    for r in sp.active[d]:
+        expr = _w(lay.rki + r)
+        for i in range(m.nreact[r]):
+            expr = f"({expr}) * yin[{sp.irm2[r][i] * 32}]"
+        o.append(f"    {_w(lay.rxrat + r)} = {expr};")
+    for s_ in range(sp.ischan):
+        terms = contrib.get(s_, [])
+        if not terms:
+            o.append(f"    yout[{s_ * 32}] = 0.0;")
+            continue
+        o.append("    {")
+        for t, (r, scv) in enumerate(terms):
+            rr = _w(lay.rxrat + r)
+            if t == 0:
+                o.append(f"      double a = {'-' + rr if scv is None else c_double(scv) + ' * ' + rr};")
+            elif scv is None:
+                o.append(f"      a = a - {rr};")
+            else:
+                o.append(f"      a = fma({c_double(scv)}, {rr}, a);")
+        o.append(f"      yout[{s_ * 32}] = a;")
+        o.append("    }")
+    o.append("}")
+    return o
+
+
+def _ex_ref(m: Mechanism, sp: SparseMech, lay: Layout, r: int, ial: int) -> str:
+    if m.nreact[r] == 1:
+        return _w(lay.rki + r)
+    return _w(lay.ex[(r, ial)])
+
+
+def _explic(m: Mechanism, sp: SparseMech, lay: Layout, d: int) -> list[str]:
+    o = [f"// Partial-derivative products of 2- and 3-reactant reactions (rbjacob.F:112-143).",
+         f"__device__ __noinline__ void explic_{d}(double* __restrict__ ws)",
+         "{",
+         f"    const double* __restrict__ y = ws + {lay.y * 32};"]
+    for r in sp.active[d]:
+        nre = m.nreact[r]
+        k = _w(lay.rki + r)
+        if nre == 2:
+            y1 = f"y[{sp.irm2[r][0] * 32}]"
+            y2 = f"y[{sp.irm2[r][1] * 32}]"
+            o.append(f"    {{ const double kk = {k}; {_w(lay.ex[(r, 0)])} = kk * {y2}; {_w(lay.ex[(r, 1)])} = kk * {y1}; }}")
+        elif nre == 3:
+            y1 = f"y[{sp.irm2[r][0] * 32}]"
+            y2 = f"y[{sp.irm2[r][1] * 32}]"
+            y3 = f"y[{sp.irm2[r][2] * 32}]"
+            o.append(f"    {{ const double kk = {k}; const double cr2 = kk * {y2};"
+                     f" {_w(lay.ex[(r, 0)])} = cr2 * {y3};"
+                     f" {_w(lay.ex[(r, 1)])} = (kk * {y1}) * {y3};"
+                     f" {_w(lay.ex[(r, 2)])} = cr2 * {y1}; }}")
+    o.append("}")
+    return o
+
+
+def _jac_terms(m: Mechanism, sp: SparseMech, d: int) -> dict[int, list[tuple]]:
+    """storage index -> ordered PD terms [(rxn, ial, coef or None, sign)]."""
+    terms: dict[int, list] = {}
+    for r in sp.active[d]:
+        for (iar, ial) in sp.loss_pd[d][r]:
+            terms.setdefault(iar, []).append((r, ial, None, -1))
+        for (iar, ial, ic) in sp.prod_pd[d][r]:
+            terms.setdefault(iar, []).append((r, ial, None if ic < 0 else m.sc[r][ic], +1))
+    return terms
+
+
+JAC_CHUNK_OPS = 700     # elimination ops per generated function; bounds ptxas time
+
+
+def _jacdecomp_chunks(m: Mechanism, sp: SparseMech, lay: Layout, d: int) -> list[list[str]]:
+    """Jacobian - I/(gamma h) and its LU factors, row by row.  Each entry receives the same
+    updates in the same order as the column-ordered elimination of rbdecomp.F; L is stored
+    scaled by 1/U(k,k) and VDIAG = 1/U(i,i).  Rows are grouped into functions of bounded size."""
+    n = sp.ischan
+    jpt = sp.jarraypt[d]
+    terms = _jac_terms(m, sp, d)
+    rows_code = []
+    for i in range(n):
+        lower = sp.lower[d][i]
+        upper = sp.upper[d][i]
+        cols = [j for (_, j) in lower] + [i] + [j for (_, j) in upper]
+        o = [f"    {{ // row {i}"]
+        nops = 0
+        for j in cols:
+            st = jpt[(i, j)]
+            tl = terms.get(st, [])
+            var = f"a{j}"
+            if not tl:
+                o.append(f"      double {var} = 0.0;")
+                continue
+            first = True
+            for (r, ial, coef, sign) in tl:
+                ex = _ex_ref(m, sp, lay, r, ial)
+                if first:
+                    if sign < 0:
+                        o.append(f"      double {var} = -{ex};")
+                    elif coef is None:
+                        o.append(f"      double {var} = {ex};")
+                    else:
+                        o.append(f"      double {var} = {c_double(coef)} * {ex};")
+                    first = False
+                elif sign < 0:
+                    o.append(f"      {var} = {var} - {ex};")
+                elif coef is None:
+                    o.append(f"      {var} = {var} + {ex};")
+                else:
+                    o.append(f"      {var} = fma({c_double(coef)}, {ex}, {var});")
+        o.append(f"      a{i} = a{i} - gdtinv;")
+        for (st_ik, k) in lower:
+            o.append(f"      a{k} = a{k} * vd[{k * 32}];")
+            o.append(f"      lu[{st_ik * 32}] = a{k};")
+            for (st_kj, j) in sp.upper[d][k]:
+                o.append(f"      a{j} = fma(-a{k}, lu[{st_kj * 32}], a{j});")
+                nops += 1
+        for (st_ij, j) in upper:
+            o.append(f"      lu[{st_ij * 32}] = a{j};")
+        o.append(f"      vd[{i * 32}] = 1.0 / a{i};")
+        o.append("    }")
+        rows_code.append((nops + len(cols), o))
+    # group rows into chunks
+    chunks, cur, cost = [], [], 0
+    for c, code in rows_code:
+        if cur and cost + c > JAC_CHUNK_OPS:
+            chunks.append(cur); cur, cost = [], 0
+        cur.append(code); cost += c
+    if cur:
+        chunks.append(cur)
+    out = []
+    for ci, ch in enumerate(chunks):
+        f = [f"__device__ __noinline__ void jacdecomp_{d}_{ci}(double* __restrict__ ws, double gdtinv)", "{",
+             f"    double* __restrict__ lu = ws + {lay.lu * 32};",
+             f"    double* __restrict__ vd = ws + {lay.vdiag * 32};"]
+        for code in ch:
+            f.extend(code)
+        f.append("}")
+        out.append(f)
+    return out
+
+
+SOLVE_CHUNK_TERMS = 800
+
+
+def _solve_chunks(sp: SparseMech, lay: Layout, d: int) -> list[list[str]]:
+    """Forward then backward substitution in place at ws[rhs] (rbsolve.F); each row
+    sums its terms in the reference's column order."""
+    n = sp.ischan
+    pieces = []
+    for i in range(n):
+        o = ["    {", f"      double x = b[{i * 32}];"]
+        for (st, j) in sp.lower[d][i]:
+            o.append(f"      x = fma(-lu[{st * 32}], b[{j * 32}], x);")
+        o.append(f"      b[{i * 32}] = x;")
+        o.append("    }")
+        pieces.append((len(sp.lower[d][i]) + 1, o))
+    for i in range(n - 1, -1, -1):
+        o = ["    {", f"      double x = b[{i * 32}];"]
+        for (st, j) in sp.upper[d][i]:
+            o.append(f"      x = fma(-lu[{st * 32}], b[{j * 32}], x);")
+        o.append(f"      b[{i * 32}] = x * vd[{i * 32}];")
+        o.append("    }")
+        pieces.append((len(sp.upper[d][i]) + 1, o))
+    chunks, cur, cost = [], [], 0
+    for c, code in pieces:
+        if cur and cost + c > SOLVE_CHUNK_TERMS:
+            chunks.append(cur); cur, cost = [], 0
+        cur.append(code); cost += c
+    if cur:
+        chunks.append(cur)
+    out = []
+    for ci, ch in enumerate(chunks):
+        f = [f"__device__ __noinline__ void solve_{d}_{ci}(double* __restrict__ ws, int rhs)", "{",
+             f"    const double* __restrict__ lu = ws + {lay.lu * 32};",
+             f"    const double* __restrict__ vd = ws + {lay.vdiag * 32};",
+             "    double* __restrict__ b = ws + rhs * 32;",
+             "    (void)vd;"]
+        for code in ch:
+            f.extend(code)
+        f.append("}")
+        out.append(f)
+    return out

@@ -1,0 +1,164 @@
+"""Seeded synthetic inputs for the chemistry operator.
+
+CMAQ's benchmark inputs (met, photolysis, initial conditions) are external data that
+are not available, so workloads use seeded synthetic fields with the benchmark's
+shapes and the value distributions below.  ``numpy.random.Generator(PCG64(seed))``;
+the same seed gives the same arrays on every machine.
+
+Per column:   surface temperature U(240, 310) K with a -6.5 K/km lapse (200 K floor);
+              pressure on sigma levels from 1013 to 100 hPa; solar zenith angle
+              U(sza_min, sza_max) deg; photolysis J_k = Jmax_k * max(cos SZA, 0);
+              OCEAN+SZONE = 0, except a fraction of columns at U(0, 1); SEAICE = 0.
+Per cell:     H2O U(1e-4, 2e-2) mol/mol; density from the ideal-gas law.
+Initial mixing ratios (ppmV): O3 U(10, 120) ppb; NO, NO2 log-uniform 0.01-100 ppb;
+              CO U(50, 300) ppb; radicals and short-lived intermediates log-uniform
+              1e-12 - 1e-10 ppm (near their quasi-steady state); other gases log-uniform 0.01-50 ppb; aerosol species
+              (CGRID in ug/m3) log-uniform 1e-4 - 1 ug/m3.  Optional plume columns
+              multiply NO, NO2 and VOCs by `plume_factor`.
+Heterogeneous rates are zero unless `het` is set (log-uniform 1e-6 - 1e-2 1/min).
+
+The Jmax table is a project choice of representative clear-sky values [1/min]; CMAQ
+holds no J climatology in source.
+"""
+from __future__ import annotations
+
+import json
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+MECH_DIR = Path(__file__).resolve().parent / "mechs"
+
+# representative clear-sky maxima, 1/min (project choice)
+JMAX = {
+    "NO2": 0.48, "O3_O3P": 0.024, "O3_O1D": 1.8e-3, "H2O2": 4.2e-4, "NO3NO2": 9.6, "NO3NO": 1.2,
+    "N2O5": 1.8e-3, "HONO": 0.096, "HNO3": 3.0e-5, "PNA": 3.0e-4, "PAN": 3.0e-5, "MEPX": 3.0e-4,
+    "NTR": 1.8e-4, "FORM_R": 1.8e-3, "FORM_M": 2.7e-3, "ALD2": 2.4e-4, "ALDX": 9.0e-4, "GLYD": 6.0e-4,
+    "GLY": 1.8e-3, "MGLY": 7.2e-3, "KET": 1.2e-4, "ACET": 3.0e-5, "ISPD": 1.2e-3, "HPALD": 6.0e-3,
+    "CL2": 0.12, "HOCL": 0.018, "FMCL": 6.0e-4, "CLNO2": 0.018, "CLONO2_1": 1.2e-3,
+    "CLONO2_2": 3.0e-3, "IC3ONO2": 1.8e-4, "ACRO": 1.8e-4,
+}
+JMAX_DEFAULT = 1.0e-3
+
+RADICALS = {"O", "O1D", "OH", "HO2", "NO3", "HO", "O3P", "CL", "CLO", "ROR", "CRO", "BZO2", "TO2",
+            "XLO2", "ISO2", "C2O3", "CXO3", "MEO2", "RO2", "XO2", "XO2H", "XO2N", "OPO3", "EPX2",
+            "HCO3", "BENZRO2", "TOLRO2", "XYLRO2", "PAHRO2", "CAT1", "CRON", "TERPNRO2", "ECH4"}
+
+
+def jmax_for(photab: str) -> float:
+    name = photab.upper()
+    for key in sorted(JMAX, key=len, reverse=True):
+        if name.startswith(key):
+            return JMAX[key]
+    return JMAX_DEFAULT
+
+
+def manifest(mech: str) -> dict:
+    return json.loads((MECH_DIR / mech / "manifest.json").read_text())
+
+
+@dataclass
+class GridInputs:
+    """Arrays in CMAQ's Fortran layouts, held as C-ordered numpy arrays of the reversed shape."""
+    mech: str
+    ncols: int
+    nrows: int
+    nlays: int
+    nspcsd: int
+    conc: np.ndarray        # (nspcsd, nlays, nrows, ncols) float32  = CONC(C, R, L, S)
+    ta: np.ndarray          # (nlays, nrows, ncols) float32
+    qv: np.ndarray
+    dens: np.ndarray
+    pres: np.ndarray
+    seaice: np.ndarray      # (nrows, ncols) float32
+    ocean_szone: np.ndarray
+    rj: np.ndarray          # (nphotab, nlays, nrows, ncols) float32
+    khetero: np.ndarray     # (nlays, nrows, ncols, nhet) float64 = KHETERO(NHET, C, R, L)
+    cgrid_index: np.ndarray  # (nspec,) int32, 1-based
+    seed: int
+
+    @property
+    def ncell(self) -> int:
+        return self.ncols * self.nrows * self.nlays
+
+
+def make_grid(mech: str = "cb6r5_ae7_aq", ncols: int = 20, nrows: int = 20, nlays: int = 10, seed: int = 2018,
+              sza_range=(0.0, 100.0), plume_fraction: float = 0.0, plume_factor: float = 10.0,
+              seawater_fraction: float = 0.1, het: bool = False) -> GridInputs:
+    man = manifest(mech)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    nspec = man["nspec"]
+    cgi = np.array([s["cgrid_index"] for s in man["species"]], dtype=np.int32)
+    nspcsd = int(cgi.max()) + 1
+    ncr = ncols * nrows
+    shape3 = (nlays, nrows, ncols)
+    # vertical structure
+    sig = (np.arange(nlays) + 0.5) / nlays
+    p_hpa = 1013.0 - (1013.0 - 100.0) * sig
+    z_km = 7.5 * np.log(1013.0 / p_hpa)
+    tsurf = rng.uniform(240.0, 310.0, size=(nrows, ncols))
+    ta = np.maximum(tsurf[None] - 6.5 * z_km[:, None, None], 200.0).astype(np.float32)
+    pres = np.broadcast_to((p_hpa * 100.0)[:, None, None], shape3).astype(np.float32)
+    h2o = rng.uniform(1.0e-4, 2.0e-2, size=shape3)
+    qv = (h2o * 18.0153 / 28.9628).astype(np.float32)
+    dens = (pres.astype(np.float64) / (287.05 * ta.astype(np.float64))).astype(np.float32)
+    # photolysis
+    sza = rng.uniform(sza_range[0], sza_range[1], size=(nrows, ncols))
+    cosz = np.maximum(np.cos(np.deg2rad(sza)), 0.0)
+    jm = np.array([jmax_for(p) for p in man["photab"]])
+    rj = (jm[:, None, None, None] * cosz[None, None, :, :] * np.ones((1, nlays, 1, 1))).astype(np.float32)
+    # seawater
+    osz = np.zeros(ncr)
+    sea_cols = rng.random(ncr) < seawater_fraction
+    osz[sea_cols] = rng.uniform(0.0, 1.0, size=int(sea_cols.sum()))
+    osz = osz.reshape(nrows, ncols).astype(np.float32)
+    seaice = np.zeros((nrows, ncols), np.float32)
+    # heterogeneous rates
+    nhet = man["nhetero"]
+    if het:
+        khet = np.exp(rng.uniform(np.log(1e-6), np.log(1e-2), size=shape3 + (nhet,)))
+    else:
+        khet = np.zeros(shape3 + (nhet,))
+    # concentrations
+    plume = rng.random((nrows, ncols)) < plume_fraction
+    conc = np.zeros((nspcsd,) + shape3, np.float32)
+
+    def logu(lo, hi):
+        return np.exp(rng.uniform(np.log(lo), np.log(hi), size=shape3))
+
+    voc_like = {"FORM", "ALD2", "ALDX", "PAR", "ETH", "OLE", "IOLE", "ISOP", "TERP", "TOL", "XYLMN", "BENZENE",
+                "ETHA", "ETOH", "MEOH", "ACET", "KET", "PRPA", "ETHY", "APIN", "NAPH", "SESQ", "CRES", "GLY",
+                "GLYD", "MGLY", "ISPD", "ACRO_PRIMARY", "TOLU", "DMS", "HC3", "HC5", "HC10", "OLT", "OLI", "API",
+                "LIM", "TOL", "XYM", "XYE", "BEN", "ETE", "ETH", "HCHO", "ACD", "ALD", "ACT", "MEK", "KET"}
+    for s, sp in enumerate(man["species"]):
+        name = sp["name"]
+        if sp["convert"]:
+            v = logu(1.0e-4, 1.0)                       # ug/m3
+        elif name == "O3":
+            v = rng.uniform(0.010, 0.120, size=shape3)
+        elif name in ("NO", "NO2"):
+            v = logu(1.0e-5, 0.1)
+        elif name == "CO":
+            v = rng.uniform(0.05, 0.30, size=shape3)
+        elif name in RADICALS:
+            v = logu(1.0e-12, 1.0e-10)
+        else:
+            v = logu(1.0e-5, 0.05) if name in voc_like else logu(1.0e-12, 0.05)
+        if plume.any() and (name in ("NO", "NO2") or name in voc_like):
+            v = np.where(plume[None], v * plume_factor, v)
+        conc[cgi[s] - 1] = v.astype(np.float32)
+    return GridInputs(mech=mech, ncols=ncols, nrows=nrows, nlays=nlays, nspcsd=nspcsd, conc=conc, ta=ta,
+                      qv=qv, dens=dens, pres=np.ascontiguousarray(pres), seaice=seaice, ocean_szone=osz,
+                      rj=np.ascontiguousarray(rj), khetero=np.ascontiguousarray(khet), cgrid_index=cgi,
+                      seed=seed)
+
+
+# --- configurations of the chemistry benchmark (CB6r5 unless stated)
+CONFIGS = {
+    "cpu4k": dict(ncols=20, nrows=20, nlays=10),                        # 4,000 cells
+    "conus": dict(ncols=459, nrows=299, nlays=35),                      # 4,803,315 cells
+    "conus_skewed": dict(ncols=459, nrows=299, nlays=35, plume_fraction=0.3),
+    "adjoint350k": dict(ncols=100, nrows=100, nlays=35),
+    "cracmm2_1m": dict(ncols=200, nrows=200, nlays=25, mech="cracmm2"),
+}

@@ -1,0 +1,134 @@
+/*
+ * cmaqchem.h -- C ABI of the GB300 gas-phase chemistry library (libcmaqchem.so).
+ *
+ * The library replaces the body of CMAQ's gas-chemistry operator
+ *
+ *     SUBROUTINE CHEM( CONC, JDATE, JTIME, TSTEP )
+ *         CCTM/src/gas/ros3/rbdriver.F:20-785          (ROS3 solver)
+ *         CCTM/src/gas/ebi_cb6r5_ae7_aq/hrdriver.F:20  (EBI solver)
+ *     called once per synchronisation step from CCTM/src/driver/sciproc.F:298
+ *
+ * The operator's implicit inputs, which the Fortran reads through modules, are
+ * explicit arguments here: the met fields that CHEM interpolates to the step
+ * midpoint (rbdriver.F:390-403), OCEAN + SZONE (rbdriver.F:253-259), the
+ * photolysis rates RJ of PHOT_MOD and the heterogeneous rates KHETERO of
+ * AEROSOL_CHEMISTRY (rbdriver.F:409, 499-511).
+ *
+ * Array layouts are the reference's Fortran layouts, so a Fortran caller passes
+ * its arrays unchanged (see the ISO_C_BINDING shim in INTEGRATION.md):
+ *     conc    CONC(NCOLS, NROWS, NLAYS, NSPCSD)   REAL(4)
+ *     ta, qv, dens, pres  (NCOLS, NROWS, NLAYS)   REAL(4)  K, kg/kg, kg/m3, Pa
+ *     seaice, ocean_szone (NCOLS, NROWS)          REAL(4)  fractions
+ *     rj      RJ(NCOLS, NROWS, NLAYS, NPHOTAB)    REAL(4)  1/min
+ *     khetero KHETERO(NHETERO, NCOLS, NROWS, NLAYS) REAL(8)
+ *
+ * Errors: the reference stops the run (M3EXIT) on a step-size underflow
+ * (rbsolver.F:532-585).  Here every call returns an int: 0 success, > 0 the
+ * number of cells whose integration failed (their last accepted state is written
+ * back and their status is available per cell), < 0 a fatal error whose text
+ * cmaqchem_last_error() returns.  A handle is not re-entrant; use one handle per
+ * thread.  No pointer passed in is retained after a call returns.
+ */
+#ifndef CMAQCHEM_H
+#define CMAQCHEM_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CMAQCHEM_SOLVER_ROS3 0
+#define CMAQCHEM_SOLVER_EBI 1
+
+/* How cells are scheduled on the GPU; every mode integrates each cell with its own
+ * step size (the reference with BLKSIZE = 1). */
+#define CMAQCHEM_SCHED_STATIC 0   /* fixed cell -> thread assignment ("plain") */
+#define CMAQCHEM_SCHED_QUEUE 1    /* persistent kernel, cells pulled from a work queue ("batched") */
+
+/* per-cell status bits */
+#define CMAQCHEM_CELL_DT_UNDERFLOW 1
+#define CMAQCHEM_CELL_MAXITER 2
+#define CMAQCHEM_CELL_NONFINITE 4
+
+typedef struct cmaqchem_handle cmaqchem_handle;
+
+typedef struct {
+    const char* mechanism;     /* "cb6r5_ae7_aq" or "cracmm2" (MECHNAME of RXNS_DATA) */
+    int solver;                /* CMAQCHEM_SOLVER_* */
+    int schedule;              /* CMAQCHEM_SCHED_* */
+    double rtol;               /* RTOL = REAL(GLBL_RTOL, 8) (rbinit.F:251; RUNTIME_VARS.F:178) */
+    double atol;               /* ATOL = REAL(GLBL_ATOL, 8) [ppmV] (rbinit.F:250; RUNTIME_VARS.F:177) */
+    int ncols, nrows, nlays;   /* local domain of this process (GRID_CONF) */
+    int nspcsd;                /* number of CGRID species (CGRID_SPCS) */
+    const int* cgrid_index;    /* [nspec] CGRID slot (1-based, as CGRID_INDEX) or NULL for the mechanism's table */
+    int device;                /* CUDA device ordinal */
+    int max_iter;              /* cap on ROS3 step attempts per cell and call (<= 0: 100000) */
+} cmaqchem_cfg;
+
+typedef struct {
+    long long accepted_steps;  /* summed over cells */
+    long long rejected_steps;
+    long long failed_cells;    /* cells with a non-zero status */
+    long long sunlit_cells;
+    double device_ms;          /* device time of the call's kernels */
+} cmaqchem_stats;
+
+typedef struct {
+    int nspec, nrxns, ischan, nphotab, nhetero;
+    int iarray_day, iarray_night;       /* stored LU entries (day / night pattern) */
+    double flops_step_day;              /* algorithmic FLOPs of one ROS3 step attempt of one cell */
+    double flops_step_night;
+} cmaqchem_mech_info;
+
+/* Replaces the first-call set-up of CHEM: RBINIT, RBSPARSE, RESET_SPECIES_POINTERS
+ * (rbdriver.F:226-371).  Allocates device tables and workspaces for the domain. */
+int cmaqchem_init(const cmaqchem_cfg* cfg, cmaqchem_handle** out);
+
+/* One CHEM call on host arrays (rbdriver.F:373-785): copies the inputs to the device,
+ * integrates every cell over TSTEP(2) and copies CONC back.  tstep = TSTEP(3) HHMMSS. */
+int cmaqchem_step(cmaqchem_handle* h, float* conc, const float* ta, const float* qv,
+                  const float* dens, const float* pres, const float* seaice,
+                  const float* ocean_szone, const float* rj, const double* khetero,
+                  int jdate, int jtime, const int tstep[3], cmaqchem_stats* stats);
+
+/* Same call on device-resident arrays (same layouts), enqueued on `stream`
+ * (a cudaStream_t, NULL for the default stream); returns after the stream is idle. */
+int cmaqchem_step_device(cmaqchem_handle* h, float* conc, const float* ta, const float* qv,
+                         const float* dens, const float* pres, const float* seaice,
+                         const float* ocean_szone, const float* rj, const double* khetero,
+                         int jdate, int jtime, const int tstep[3], void* stream,
+                         cmaqchem_stats* stats);
+
+/* Per-cell status of the last step call (CMAQCHEM_CELL_* bits) and step attempts,
+ * copied to host arrays of ncols*nrows*nlays ints (either may be NULL). */
+int cmaqchem_cell_stats(cmaqchem_handle* h, int* status, int* attempts);
+
+/* Solver-level entry replacing RBSOLVER (rbsolver.F:26) for cells with given rate
+ * constants, device arrays:  y[ischan][ncell] in the solver's species order, updated in
+ * place; rki[nrxns][ncell] (ppm, min units); night[ncell] = 1 for cells without
+ * sunlight (night reaction list, rbsparse.F:275-279).  Per-cell outputs may be NULL. */
+int cmaqchem_ros3_solve_device(cmaqchem_handle* h, long long ncell, double* y, const double* rki,
+                               const unsigned char* night, double chemstep_min, int* status,
+                               int* nsteps, int* nfails, void* stream);
+
+/* Rate constants only (CALC_RCONST, RXNS_FUNC_MODULE.F90) for the handle's grid, device
+ * arrays: rki[nrxns][ncell], sunlit[ncell]. */
+int cmaqchem_rconst_device(cmaqchem_handle* h, const float* conc, const float* ta, const float* qv,
+                           const float* dens, const float* pres, const float* seaice,
+                           const float* ocean_szone, const float* rj, const double* khetero,
+                           double* rki, unsigned char* sunlit, void* stream);
+
+/* Mechanism sizes and species order (replaces RXNS_DATA / RBDATA module queries).
+ * inew2old may be NULL, else it receives nspec ints (solver order -> mechanism order). */
+int cmaqchem_mech_info_get(const char* mechanism, cmaqchem_mech_info* info, int* inew2old);
+
+void cmaqchem_destroy(cmaqchem_handle* h);
+
+/* Text of the last error of the calling thread; returns its length. */
+int cmaqchem_last_error(char* buf, size_t len);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CMAQCHEM_H */

@@ -1,0 +1,52 @@
+"""Build the CPU oracle shared libraries (test infrastructure).
+
+    python oracle/build.py [mech ...]
+
+Compiles ``oracle/ros3_oracle.c`` once per mechanism into
+``oracle/_build/liboracle_<mech>.so`` with gcc.  ``-ffp-contract=off`` keeps the
+compiler from fusing operations beyond the explicit ``fma`` calls; no
+``-march`` flag, so the library builds the same on x86-64 and aarch64.
+
+The reference's own Fortran (CCTM/src/gas/ros3) cannot be built here: there is no
+Fortran compiler, so there is no ``oracle/_ref`` library.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+MECHS = ("cb6r5_ae7_aq", "cracmm2")
+
+
+def lib_path(mech: str) -> Path:
+    return HERE / "_build" / f"liboracle_{mech}.so"
+
+
+def build(mechs=MECHS, force: bool = False) -> list[Path]:
+    out_dir = HERE / "_build"
+    out_dir.mkdir(exist_ok=True)
+    src = HERE / "ros3_oracle.c"
+    procs, outs = [], []
+    for mech in mechs:
+        gen = HERE / "gen" / f"{mech}_mech.c"
+        out = lib_path(mech)
+        outs.append(out)
+        if (not force and out.exists() and out.stat().st_mtime > max(src.stat().st_mtime, gen.stat().st_mtime)):
+            continue
+        cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+               "-fno-fast-math", f'-DMECH_SOURCE="gen/{mech}_mech.c"', "-I", str(HERE),
+               str(src), "-o", str(out) + ".tmp", "-lm"]
+        procs.append((subprocess.Popen(cmd, cwd=HERE), out))
+    for p, out in procs:
+        if p.wait() != 0:
+            raise RuntimeError(f"oracle build failed for {out.name}")
+        os.replace(str(out) + ".tmp", out)
+    return outs
+
+
+if __name__ == "__main__":
+    for p in build(sys.argv[1:] or MECHS, force=True):
+        print(p)

@@ -1,0 +1,135 @@
+"""ctypes binding of the CPU oracle (test infrastructure only).
+
+Loads ``oracle/_build/liboracle_<mech>.so`` (see ``oracle/build.py``), a C
+restatement of CMAQ's ROS3 chemistry (CCTM/src/gas/ros3/*.F).  Tests, the smoke
+check and the CPU-baseline leg of the benchmark use it as the checker; nothing
+in the product imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from functools import lru_cache
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+
+
+class OracleChemArgs(C.Structure):
+    _fields_ = [("ncols", C.c_int), ("nrows", C.c_int), ("nlays", C.c_int), ("nspcsd", C.c_int),
+                ("conc", C.POINTER(C.c_float)), ("cgrid_index", C.POINTER(C.c_int)),
+                ("convert", C.POINTER(C.c_int)), ("ta", C.POINTER(C.c_float)), ("qv", C.POINTER(C.c_float)),
+                ("dens", C.POINTER(C.c_float)), ("pres", C.POINTER(C.c_float)),
+                ("seaice", C.POINTER(C.c_float)), ("ocean_szone", C.POINTER(C.c_float)),
+                ("rj", C.POINTER(C.c_float)), ("khetero", C.POINTER(C.c_double)),
+                ("tstep_sec", C.c_int), ("rtol", C.c_double), ("atol", C.c_double), ("blksize", C.c_int),
+                ("lreorder", C.c_int), ("max_iter", C.c_int), ("threads", C.c_int),
+                ("nsteps_total", C.c_longlong), ("nfails_total", C.c_longlong), ("nfailed_blocks", C.c_int)]
+
+
+def _p(a: np.ndarray, ct):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+@lru_cache(maxsize=None)
+def load(mech: str = "cb6r5_ae7_aq") -> C.CDLL:
+    import sys
+    sys.path.insert(0, str(HERE))
+    try:
+        import build as _b  # oracle/build.py
+    finally:
+        sys.path.pop(0)
+    path = _b.lib_path(mech)
+    if not path.exists():
+        _b.build([mech])
+    lib = C.CDLL(str(path))
+    dp, ip, fp, u8p = C.POINTER(C.c_double), C.POINTER(C.c_int), C.POINTER(C.c_float), C.POINTER(C.c_uint8)
+    lib.oracle_calc_rconst.argtypes = [C.c_int, dp, dp, dp, dp, dp, C.c_int, dp, dp]
+    lib.oracle_feval.argtypes = [C.c_int, C.c_int, dp, dp, dp]
+    lib.oracle_jac_decomp.argtypes = [C.c_int, C.c_int, dp, dp, C.c_double, dp, dp]
+    lib.oracle_rbsolver_block.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, dp, dp, ip]
+    lib.oracle_rbsolver_cells.argtypes = [C.c_long, C.c_double, C.c_double, C.c_double, C.c_int, dp, dp, u8p,
+                                          ip, ip, ip, C.c_int]
+    lib.oracle_chem.argtypes = [C.POINTER(OracleChemArgs)]
+    lib.oracle_mech_name.restype = C.c_char_p
+    return lib
+
+
+class Oracle:
+    def __init__(self, mech: str = "cb6r5_ae7_aq"):
+        self.mech = mech
+        self.lib = load(mech)
+        self.nspec = self.lib.oracle_nspec()
+        self.nrxns = self.lib.oracle_nrxns()
+        self.ischan = self.lib.oracle_ischan()
+        self.nphotab = self.lib.oracle_nphotab()
+        self.nhetero = self.lib.oracle_nhetero()
+        self.inew2old = np.zeros(self.nspec, np.int32)
+        self.iold2new = np.zeros(self.nspec, np.int32)
+        self.lib.oracle_inew2old(_p(self.inew2old, C.c_int))
+        self.lib.oracle_iold2new(_p(self.iold2new, C.c_int))
+
+    def rconst(self, temp, pres_atm, h2o_ppm, rj, het, sunlit: bool, seawater) -> np.ndarray:
+        n = len(temp)
+        a = [np.ascontiguousarray(x, dtype=np.float64) for x in (temp, pres_atm, h2o_ppm)]
+        rj = np.ascontiguousarray(rj, dtype=np.float64).reshape(self.nphotab, n)
+        het = np.ascontiguousarray(het, dtype=np.float64).reshape(max(self.nhetero, 1), n)
+        sw = np.ascontiguousarray(seawater, dtype=np.float64)
+        out = np.zeros((self.nrxns, n))
+        self.lib.oracle_calc_rconst(n, _p(a[0], C.c_double), _p(a[1], C.c_double), _p(a[2], C.c_double),
+                                    _p(rj, C.c_double), _p(het, C.c_double), int(bool(sunlit)),
+                                    _p(sw, C.c_double), _p(out, C.c_double))
+        return out
+
+    def feval(self, y, rki, ncsp: int = 0) -> np.ndarray:
+        y = np.ascontiguousarray(y, np.float64)
+        rki = np.ascontiguousarray(rki, np.float64)
+        n = y.shape[1]
+        out = np.zeros_like(y)
+        self.lib.oracle_feval(n, ncsp, _p(y, C.c_double), _p(rki, C.c_double), _p(out, C.c_double))
+        return out
+
+    def solve_cells(self, y, rki, night, chemstep: float, rtol: float, atol: float, max_iter: int = 100000,
+                    threads: int = 0):
+        """Per-cell ROS3 (BLKSIZE = 1) over chemstep minutes; y (nspec, n) new order, in place copy."""
+        y = np.array(y, dtype=np.float64, order="C", copy=True)
+        rki = np.ascontiguousarray(rki, np.float64)
+        night = np.ascontiguousarray(night, np.uint8)
+        n = y.shape[1]
+        ns, nf, st = (np.zeros(n, np.int32) for _ in range(3))
+        self.lib.oracle_rbsolver_cells(n, chemstep, rtol, atol, max_iter, _p(y, C.c_double), _p(rki, C.c_double),
+                                       _p(night, C.c_uint8), _p(ns, C.c_int), _p(nf, C.c_int), _p(st, C.c_int),
+                                       threads)
+        return y, ns, nf, st
+
+    def solve_block(self, y, rki, ncsp: int, chemstep: float, rtol: float, atol: float, max_iter: int = 100000):
+        y = np.array(y, dtype=np.float64, order="C", copy=True)
+        rki = np.ascontiguousarray(rki, np.float64)
+        stats = np.zeros(4, np.int32)
+        self.lib.oracle_rbsolver_block(y.shape[1], ncsp, chemstep, rtol, atol, max_iter, _p(y, C.c_double),
+                                       _p(rki, C.c_double), _p(stats, C.c_int))
+        return y, stats
+
+    def chem(self, g, tstep_sec: int = 300, rtol: float = 1e-3, atol: float = 1e-9, blksize: int = 50,
+             lreorder: bool = True, max_iter: int = 100000, threads: int = 0, conc=None):
+        """One CHEM call on a GridInputs-like object; returns (new conc, totals)."""
+        conc = np.array(g.conc if conc is None else conc, dtype=np.float32, order="C", copy=True)
+        man_cgi = np.ascontiguousarray(g.cgrid_index - 1, np.int32)
+        convert = np.ascontiguousarray(self.convert_flags(g.mech), np.int32)
+        keep = [conc, man_cgi, convert, g.ta, g.qv, g.dens, g.pres, g.seaice, g.ocean_szone, g.rj, g.khetero]
+        a = OracleChemArgs(g.ncols, g.nrows, g.nlays, g.nspcsd, _p(conc, C.c_float), _p(man_cgi, C.c_int),
+                           _p(convert, C.c_int), _p(g.ta, C.c_float), _p(g.qv, C.c_float), _p(g.dens, C.c_float),
+                           _p(g.pres, C.c_float), _p(g.seaice, C.c_float), _p(g.ocean_szone, C.c_float),
+                           _p(g.rj, C.c_float), _p(g.khetero, C.c_double), tstep_sec, rtol, atol, blksize,
+                           int(lreorder), max_iter, threads, 0, 0, 0)
+        rc = self.lib.oracle_chem(C.byref(a))
+        del keep
+        return conc, {"rc": rc, "nsteps": a.nsteps_total, "nfails": a.nfails_total,
+                      "nfailed_blocks": a.nfailed_blocks}
+
+    @staticmethod
+    def convert_flags(mech: str) -> np.ndarray:
+        import json
+        man = json.loads((HERE.parent / "cmaq_gb300" / "mechs" / mech / "manifest.json").read_text())
+        return np.array([1 if s["convert"] else 0 for s in man["species"]], np.int32)

@@ -1,0 +1,649 @@
+/*
+ * CPU oracle for the CMAQ ROS3 gas-chemistry path.  TEST INFRASTRUCTURE ONLY:
+ * tests, the smoke check and the CPU-baseline leg of the benchmark load this; the
+ * product path never does.
+ *
+ * A plain-C, table-driven restatement of the reference's vectorised ROS3 solver,
+ * following its loops one for one:
+ *   oracle_rbfeval   CCTM/src/gas/ros3/rbfeval.F:58-151
+ *   oracle_rbjacob   CCTM/src/gas/ros3/rbjacob.F:84-185
+ *   oracle_rbdecomp  CCTM/src/gas/ros3/rbdecomp.F:80-137
+ *   oracle_rbsolve   CCTM/src/gas/ros3/rbsolve.F:76-187
+ *   oracle_rbsolver  CCTM/src/gas/ros3/rbsolver.F:306-597 (block-shared step size)
+ *   oracle_chem      CCTM/src/gas/ros3/rbdriver.F:373-726 (gather, two-pass stiffness
+ *                    ordering with the heap sort of :683-724, write-back) and the block
+ *                    layout of CCTM/src/gas/ros3/rbinit.F:257-303
+ * Mechanism tables and CALC_RCONST come from the generated file MECH_SOURCE
+ * (restating RXNS_DATA_MODULE.F90 / RXNS_FUNC_MODULE.F90 and rbsparse.F).
+ *
+ * Floating-point rule shared with the device code: every "x +/- a*b" of the
+ * reference is one fused multiply-add (C99 fma), every other operation is rounded
+ * on its own (this file is compiled with -ffp-contract=off).  REAL(4) arithmetic of
+ * the reference's gather and write-back is done in float.
+ *
+ * Parity pinning: the reference publishes no golden vectors for this path and its
+ * Fortran cannot be compiled here, so this restatement is pinned by invariants and
+ * closed-form cases in the test suite (parity unpinned at reference-test level).
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#ifndef MECH_SOURCE
+#error "compile with -DMECH_SOURCE=\"gen/<mech>_mech.c\""
+#endif
+#include MECH_SOURCE
+
+/* ROS3 method constants (rbsolver.F:85-113; KPP ROS3, Sandu et al. 1997) */
+static const double GAM = 0.43586652150845899941601945119356;
+static const double C21 = -0.10156171083877702091975600115545e+01;
+static const double C31 = 0.40759956452537699824805835358067e+01;
+static const double C32 = 0.92076794298330791242156818474003e+01;
+static const double B1 = 0.10000000000000000000000000000000e+01;
+static const double B2 = 0.61697947043828245592553615689730e+01;
+static const double B3 = -0.42772256543218573326238373806514e+00;
+static const double D1 = 0.50000000000000000000000000000000e+00;
+static const double D2 = -0.29079558716805469821718236208017e+01;
+static const double D3 = 0.22354069897811569627360909276199e+00;
+#define GROW (1.0 / 3.00)
+#define RGAM (1.0 / GAM)
+static const double DTSTART = 0.5e-01, DTMIN = 1.0e-08, DTMAX = 1.0e+01, UROUND = 1.0e-18;
+static const double FACMAX = 1.0e+01, FACMIN = 1.0e-01, FACONE = 1.0e+00, CONMIN = 1.0e-30;
+
+/* per-cell status bits (shared meaning with the device code) */
+#define ST_DT_UNDERFLOW 1
+#define ST_MAXITER 2
+#define ST_NONFINITE 4
+
+typedef struct {
+    int ncells;          /* NUMCELLS */
+    int ld;              /* leading dimension (BLKSIZE) of all block arrays */
+    double* y;           /* Y(ld, NSPEC) new order */
+    double* rki;         /* RKI(ld, NRXNS) */
+    double* cc2;         /* CC2(ld, 0:MXARR-1) */
+    double* vdiag;       /* VDIAG(ld, ISCHAN) */
+    double* ydot, *k1, *k2, *k3, *yp, *err, *rxrat, *explic;
+} Block;
+
+static void block_alloc(Block* b, int ld)
+{
+    memset(b, 0, sizeof(*b));
+    b->ld = ld;
+    size_t ns = (size_t)MECH_NSPEC * ld, nr = (size_t)MECH_NRXNS * ld;
+    b->y = calloc(ns, sizeof(double));
+    b->rki = calloc(nr, sizeof(double));
+    b->cc2 = calloc((size_t)MECH_MXARR * ld, sizeof(double));
+    b->vdiag = calloc((size_t)MECH_ISCHAN * ld, sizeof(double));
+    b->ydot = calloc(ns, sizeof(double));
+    b->k1 = calloc(ns, sizeof(double));
+    b->k2 = calloc(ns, sizeof(double));
+    b->k3 = calloc(ns, sizeof(double));
+    b->yp = calloc(ns, sizeof(double));
+    b->err = calloc((size_t)ld, sizeof(double));
+    b->rxrat = calloc(nr, sizeof(double));
+    b->explic = calloc((size_t)3 * ld, sizeof(double));
+}
+
+static void block_free(Block* b)
+{
+    free(b->y); free(b->rki); free(b->cc2); free(b->vdiag); free(b->ydot); free(b->k1);
+    free(b->k2); free(b->k3); free(b->yp); free(b->err); free(b->rxrat); free(b->explic);
+}
+
+#define Y_(b, arr, c, s) ((arr)[(size_t)(s) * (b)->ld + (c)])
+
+/* rbfeval.F: YDOT = production - loss over the active reactions of NCSP */
+static void oracle_rbfeval(const Block* b, int ncsp, const double* yin, double* ydot)
+{
+    const int n = b->ncells, ld = b->ld;
+    for (int isp = 0; isp < MECH_ISCHAN; ++isp)
+        for (int c = 0; c < n; ++c) ydot[(size_t)isp * ld + c] = 0.0;
+    const int nu = mech_nuserat[ncsp];
+    for (int nrx = 0; nrx < nu; ++nrx) {
+        const int nrk = mech_nkuserat[ncsp * MECH_NRXNS + nrx];
+        const int* irm = &mech_irm2[nrk * (3 + MECH_MXPRD)];
+        double* rr = &b->rxrat[(size_t)nrk * ld];
+        const double* k = &b->rki[(size_t)nrk * ld];
+        switch (mech_nreact[nrk]) {
+        case 1:
+            for (int c = 0; c < n; ++c) rr[c] = k[c] * yin[(size_t)irm[0] * ld + c];
+            break;
+        case 2:
+            for (int c = 0; c < n; ++c)
+                rr[c] = k[c] * yin[(size_t)irm[0] * ld + c] * yin[(size_t)irm[1] * ld + c];
+            break;
+        case 3:
+            for (int c = 0; c < n; ++c)
+                rr[c] = k[c] * yin[(size_t)irm[0] * ld + c] * yin[(size_t)irm[1] * ld + c]
+                        * yin[(size_t)irm[2] * ld + c];
+            break;
+        default:
+            for (int c = 0; c < n; ++c) rr[c] = k[c];
+        }
+        for (int nr = 0; nr < mech_nreact[nrk]; ++nr) {
+            double* yd = &ydot[(size_t)irm[nr] * ld];
+            for (int c = 0; c < n; ++c) yd[c] = yd[c] - rr[c];
+        }
+        for (int np = 0; np < mech_nprdct[nrk]; ++np) {
+            double* yd = &ydot[(size_t)irm[3 + np] * ld];
+            const double sc = mech_sc[nrk * MECH_MXPRD + np];
+            for (int c = 0; c < n; ++c) yd[c] = fma(sc, rr[c], yd[c]);
+        }
+    }
+}
+
+/* rbjacob.F: Jacobian scattered into CC2 by the PD pointer lists */
+static void oracle_rbjacob(const Block* b, int ncsp, const double* yin)
+{
+    const int n = b->ncells, ld = b->ld;
+    const int iarry = mech_iarray[ncsp];
+    for (int iar = 0; iar <= iarry; ++iar)
+        for (int c = 0; c < n; ++c) b->cc2[(size_t)iar * ld + c] = 0.0;
+    double* ex = b->explic;
+    const int nu = mech_nuserat[ncsp];
+    for (int nrx = 0; nrx < nu; ++nrx) {
+        const int nrk = mech_nkuserat[ncsp * MECH_NRXNS + nrx];
+        const int* irm = &mech_irm2[nrk * (3 + MECH_MXPRD)];
+        const double* k = &b->rki[(size_t)nrk * ld];
+        const int nre = mech_nreact[nrk];
+        if (nre == 1) {
+            for (int c = 0; c < n; ++c) ex[c] = k[c];
+        } else if (nre == 2) {
+            for (int c = 0; c < n; ++c) {
+                ex[c] = k[c] * yin[(size_t)irm[1] * ld + c];
+                ex[ld + c] = k[c] * yin[(size_t)irm[0] * ld + c];
+            }
+        } else if (nre == 3) {
+            for (int c = 0; c < n; ++c) {
+                const double cr2 = k[c] * yin[(size_t)irm[1] * ld + c];
+                ex[c] = cr2 * yin[(size_t)irm[2] * ld + c];
+                ex[ld + c] = k[c] * yin[(size_t)irm[0] * ld + c] * yin[(size_t)irm[2] * ld + c];
+                ex[2 * ld + c] = cr2 * yin[(size_t)irm[0] * ld + c];
+            }
+        }
+        for (int t = mech_loss_ptr[ncsp][nrk]; t < mech_loss_ptr[ncsp][nrk + 1]; ++t) {
+            double* cc = &b->cc2[(size_t)mech_loss_iarp[ncsp][t] * ld];
+            const double* e = &ex[(size_t)mech_loss_ial[ncsp][t] * ld];
+            for (int c = 0; c < n; ++c) cc[c] = cc[c] - e[c];
+        }
+        for (int t = mech_prod_ptr[ncsp][nrk]; t < mech_prod_ptr[ncsp][nrk + 1]; ++t) {
+            double* cc = &b->cc2[(size_t)mech_prod_iarp[ncsp][t] * ld];
+            const double* e = &ex[(size_t)mech_prod_ial[ncsp][t] * ld];
+            const int ic = mech_prod_icoeff[ncsp][t];
+            if (ic < 0) {
+                for (int c = 0; c < n; ++c) cc[c] = cc[c] + e[c];
+            } else {
+                const double fracn = mech_sc[nrk * MECH_MXPRD + ic];
+                for (int c = 0; c < n; ++c) cc[c] = fma(fracn, e[c], cc[c]);
+            }
+        }
+    }
+}
+
+/* rbdecomp.F: column-by-column LU without pivoting, VDIAG = 1/diag, L scaled */
+static void oracle_rbdecomp(const Block* b, int ncsp)
+{
+    const int n = b->ncells, ld = b->ld;
+    double* cc2 = b->cc2;
+    for (int j = 0; j < MECH_ISCHAN; ++j) {
+        for (int ic = mech_dec_ptr[ncsp][j]; ic < mech_dec_ptr[ncsp][j + 1]; ++ic) {
+            double* ij = &cc2[(size_t)mech_dec_ij[ncsp][ic] * ld];
+            const double* ik = &cc2[(size_t)mech_dec_ik[ncsp][ic] * ld];
+            const double* kj = &cc2[(size_t)mech_dec_kj[ncsp][ic] * ld];
+            for (int c = 0; c < n; ++c) ij[c] = fma(-ik[c], kj[c], ij[c]);
+        }
+        const double* dg = &cc2[(size_t)mech_diag[ncsp][j] * ld];
+        double* vd = &b->vdiag[(size_t)j * ld];
+        for (int c = 0; c < n; ++c) vd[c] = 1.0 / dg[c];
+        for (int jc = mech_lsc_ptr[ncsp][j]; jc < mech_lsc_ptr[ncsp][j + 1]; ++jc) {
+            double* ija = &cc2[(size_t)mech_lsc_ij[ncsp][jc] * ld];
+            for (int c = 0; c < n; ++c) ija[c] = ija[c] * vd[c];
+        }
+    }
+}
+
+/* rbsolve.F: forward (L) then backward (U) substitution; IJ walks CC2 in storage order */
+static void oracle_rbsolve(const Block* b, int ncsp, double* rhs)
+{
+    const int n = b->ncells, ld = b->ld;
+    const int* kz = mech_kzero[ncsp];
+    int ij = 1;
+    for (int i = 0; i < MECH_ISCHAN; ++i) {
+        double* ri = &rhs[(size_t)i * ld];
+        for (int t = 0; t < mech_kzilch[ncsp][i]; ++t, ++ij) {
+            const double* cc = &b->cc2[(size_t)ij * ld];
+            const double* rj = &rhs[(size_t)kz[ij] * ld];
+            for (int c = 0; c < n; ++c) ri[c] = fma(-cc[c], rj[c], ri[c]);
+        }
+    }
+    for (int i = MECH_ISCHAN - 1; i >= 0; --i) {
+        double* ri = &rhs[(size_t)i * ld];
+        for (int t = 0; t < mech_mzilch[ncsp][i]; ++t, ++ij) {
+            const double* cc = &b->cc2[(size_t)ij * ld];
+            const double* rj = &rhs[(size_t)kz[ij] * ld];
+            for (int c = 0; c < n; ++c) ri[c] = fma(-cc[c], rj[c], ri[c]);
+        }
+        const double* vd = &b->vdiag[(size_t)i * ld];
+        for (int c = 0; c < n; ++c) ri[c] = ri[c] * vd[c];
+    }
+}
+
+typedef struct {
+    double rtol, atol;      /* RTOL(N) = ATOL(N) for all species (rbinit.F:250-253) */
+    double rnspec;          /* 1.0 / FLOAT(N_SPEC) in REAL(4) (rbsolver.F:256) */
+    int max_iter;           /* cap on step attempts per call (0 = none) */
+} SolverCfg;
+
+typedef struct {
+    int nsteps, nfails, nbad_starts, status;
+} SolverStats;
+
+static double fmax_keepnan(double a, double b) { return (b != b) ? b : fmax(a, b); }
+
+/* rbsolver.F time loop for one block: one DT shared by the block's cells; the step is
+ * accepted only if the largest cell error is <= 1.  With ordering != NULL only the
+ * stiffness estimate of pass 1 is accumulated (rbsolver.F:348-362). */
+static SolverStats oracle_rbsolver(Block* b, int ncsp, double chemstep, const SolverCfg* cfg,
+                                   double* ordering)
+{
+    SolverStats st = {0, 0, 0, 0};
+    const int n = b->ncells, ld = b->ld;
+    double dt = fmax(DTMIN, DTSTART);
+    double tnow = 0.0;
+    int lpass = 0;
+    for (long iter = 0; tnow < chemstep; ++iter) {
+        if (cfg->max_iter > 0 && iter >= cfg->max_iter) { st.status |= ST_MAXITER; break; }
+        oracle_rbfeval(b, ncsp, b->y, b->ydot);
+        if (ordering) {
+            for (int jspc = 0; jspc < MECH_ISCHAN; ++jspc) {
+                const double yloweps = cfg->atol / fmin(cfg->rtol, 0.003);
+                for (int c = 0; c < n; ++c) {
+                    const double e = Y_(b, b->ydot, c, jspc) / (Y_(b, b->y, c, jspc) + yloweps);
+                    ordering[c] = fma(e, e, ordering[c]);
+                }
+            }
+            return st;
+        }
+        double tend = tnow + dt;
+        if (tend > chemstep) { dt = chemstep - tnow; tend = chemstep; }
+        const double dtinv = 1.0 / dt;
+        const double gdtinv = dtinv * RGAM;
+        oracle_rbjacob(b, ncsp, b->y);
+        for (int j = 0; j < MECH_ISCHAN; ++j) {
+            double* dg = &b->cc2[(size_t)mech_diag[ncsp][j] * ld];
+            for (int c = 0; c < n; ++c) dg[c] = dg[c] - gdtinv;
+        }
+        oracle_rbdecomp(b, ncsp);
+        const size_t nsl = (size_t)MECH_NSPEC * ld;
+        for (size_t q = 0; q < nsl; ++q) b->k1[q] = -b->ydot[q];
+        oracle_rbsolve(b, ncsp, b->k1);
+        for (size_t q = 0; q < nsl; ++q) b->yp[q] = b->y[q] + b->k1[q];
+        oracle_rbfeval(b, ncsp, b->yp, b->ydot);
+        double x1 = C21 * dtinv;
+        for (size_t q = 0; q < nsl; ++q) b->k2[q] = fma(-x1, b->k1[q], -b->ydot[q]);
+        oracle_rbsolve(b, ncsp, b->k2);
+        x1 = C31 * dtinv;
+        const double x2 = C32 * dtinv;
+        for (size_t q = 0; q < nsl; ++q) b->k3[q] = fma(-x2, b->k2[q], fma(-x1, b->k1[q], -b->ydot[q]));
+        oracle_rbsolve(b, ncsp, b->k3);
+        for (size_t q = 0; q < nsl; ++q) {
+            double v = fma(B1, b->k1[q], b->y[q]);
+            v = fma(B2, b->k2[q], v);
+            b->yp[q] = fma(B3, b->k3[q], v);
+        }
+        for (int c = 0; c < n; ++c) b->err[c] = 0.0;
+        int finite = 1;
+        for (int s = 0; s < MECH_NSPEC; ++s)
+            for (int c = 0; c < n; ++c) {
+                const double yp = Y_(b, b->yp, c, s);
+                const double ytol = fma(cfg->rtol, fabs(yp), cfg->atol);
+                double e = D1 * Y_(b, b->k1, c, s);
+                e = fma(D2, Y_(b, b->k2, c, s), e);
+                e = fma(D3, Y_(b, b->k3, c, s), e);
+                const double q = e / ytol;
+                b->err[c] = fma(q, q, b->err[c]);
+                finite = finite && isfinite(yp);
+            }
+        double maxerr = 0.0;
+        for (int c = 0; c < n; ++c)
+            maxerr = fmax_keepnan(fmax(maxerr, UROUND), sqrt(b->err[c] * cfg->rnspec));
+        double dtfac = 0.9 / pow(maxerr, GROW);
+        if (maxerr <= 1.0) {
+            st.nsteps++;
+            for (size_t q = 0; q < nsl; ++q) b->y[q] = fmax(b->yp[q], CONMIN);
+            if (!finite) st.status |= ST_NONFINITE;
+            tnow = tend;
+            dtfac = lpass ? fmax(FACMIN, fmin(dtfac, FACMAX)) : fmax(FACMIN, fmin(dtfac, FACONE));
+            dt = fmin(DTMAX, fmax(DTMIN, dtfac * dt));
+            lpass = 1;
+        } else {
+            if (st.nfails == 0 && tnow == 0.0) st.nbad_starts++;
+            st.nfails++;
+            dt = FACMIN * dt;
+            lpass = 0;
+            if (dt < DTMIN) { st.status |= ST_DT_UNDERFLOW; break; }
+        }
+    }
+    return st;
+}
+
+/* ------------------------------------------------------------------ exported API */
+
+int oracle_nspec(void) { return MECH_NSPEC; }
+int oracle_nrxns(void) { return MECH_NRXNS; }
+int oracle_ischan(void) { return MECH_ISCHAN; }
+int oracle_nphotab(void) { return MECH_NPHOTAB; }
+int oracle_nhetero(void) { return MECH_NHETERO; }
+const char* oracle_mech_name(void) { return MECH_NAME; }
+void oracle_inew2old(int* out) { memcpy(out, mech_inew2old, sizeof(mech_inew2old)); }
+void oracle_iold2new(int* out) { memcpy(out, mech_iold2new, sizeof(mech_iold2new)); }
+
+/* CALC_RCONST for n cells; arrays cell-fastest with leading dimension n. */
+void oracle_calc_rconst(int n, const double* temp, const double* pres_atm, const double* h2o_ppm,
+                        const double* rj, const double* het, int lsunlight, const double* seawater,
+                        double* rki)
+{
+    mech_calc_rconst(n, n, temp, pres_atm, h2o_ppm, rj, het, lsunlight, seawater, rki);
+}
+
+/* f(y) for n cells (new species order, cell fastest). */
+void oracle_feval(int n, int ncsp, const double* y, const double* rki, double* ydot)
+{
+    Block b;
+    block_alloc(&b, n);
+    b.ncells = n;
+    memcpy(b.rki, rki, sizeof(double) * (size_t)MECH_NRXNS * n);
+    oracle_rbfeval(&b, ncsp, y, ydot);
+    block_free(&b);
+}
+
+/* LU factors of J - I*gdtinv for n cells: cc2[(iarray+1) * n] storage order, vdiag[ischan * n]. */
+void oracle_jac_decomp(int n, int ncsp, const double* y, const double* rki, double gdtinv,
+                       double* cc2_out, double* vdiag_out)
+{
+    Block b;
+    block_alloc(&b, n);
+    b.ncells = n;
+    memcpy(b.rki, rki, sizeof(double) * (size_t)MECH_NRXNS * n);
+    oracle_rbjacob(&b, ncsp, y);
+    for (int j = 0; j < MECH_ISCHAN; ++j) {
+        double* dg = &b.cc2[(size_t)mech_diag[ncsp][j] * n];
+        for (int c = 0; c < n; ++c) dg[c] = dg[c] - gdtinv;
+    }
+    oracle_rbdecomp(&b, ncsp);
+    memcpy(cc2_out, b.cc2, sizeof(double) * (size_t)(mech_iarray[ncsp] + 1) * n);
+    memcpy(vdiag_out, b.vdiag, sizeof(double) * (size_t)MECH_ISCHAN * n);
+    block_free(&b);
+}
+
+/* RBSOLVER on one block of n cells sharing a step size (BLKSIZE semantics).
+ * y[nspec*n] new order updated in place; stats[4] = nsteps, nfails, nbad_starts, status. */
+int oracle_rbsolver_block(int n, int ncsp, double chemstep, double rtol, double atol, int max_iter,
+                          double* y, const double* rki, int* stats)
+{
+    Block b;
+    block_alloc(&b, n);
+    b.ncells = n;
+    memcpy(b.y, y, sizeof(double) * (size_t)MECH_NSPEC * n);
+    memcpy(b.rki, rki, sizeof(double) * (size_t)MECH_NRXNS * n);
+    SolverCfg cfg = {rtol, atol, (double)(1.0f / (float)MECH_NSPEC), max_iter};
+    SolverStats st = oracle_rbsolver(&b, ncsp, chemstep, &cfg, NULL);
+    memcpy(y, b.y, sizeof(double) * (size_t)MECH_NSPEC * n);
+    block_free(&b);
+    if (stats) { stats[0] = st.nsteps; stats[1] = st.nfails; stats[2] = st.nbad_starts; stats[3] = st.status; }
+    return st.status;
+}
+
+/* Per-cell integration of many cells (BLKSIZE = 1): y[nspec*ncell], rki[nrxns*ncell] cell-fastest;
+ * night[c] selects the night reaction list.  OpenMP over cells when threads > 1. */
+int oracle_rbsolver_cells(long ncell, double chemstep, double rtol, double atol, int max_iter,
+                          double* y, const double* rki, const uint8_t* night, int* nsteps, int* nfails,
+                          int* status, int threads)
+{
+    int nbad = 0;
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel reduction(+ : nbad)
+#endif
+    {
+        Block b;
+        block_alloc(&b, 1);
+        b.ncells = 1;
+        SolverCfg cfg = {rtol, atol, (double)(1.0f / (float)MECH_NSPEC), max_iter};
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 16)
+#endif
+        for (long c = 0; c < ncell; ++c) {
+            for (int s = 0; s < MECH_NSPEC; ++s) b.y[s] = y[(size_t)s * ncell + c];
+            for (int r = 0; r < MECH_NRXNS; ++r) b.rki[r] = rki[(size_t)r * ncell + c];
+            SolverStats st = oracle_rbsolver(&b, night[c] ? 1 : 0, chemstep, &cfg, NULL);
+            for (int s = 0; s < MECH_NSPEC; ++s) y[(size_t)s * ncell + c] = b.y[s];
+            if (nsteps) nsteps[c] = st.nsteps;
+            if (nfails) nfails[c] = st.nfails;
+            if (status) status[c] = st.status;
+            nbad += st.status != 0;
+        }
+        block_free(&b);
+    }
+    return nbad;
+}
+
+/* ------------------------------------------------------------------ CHEM driver */
+
+typedef struct {
+    int ncols, nrows, nlays, nspcsd;
+    float* conc;                 /* CONC(ncols, nrows, nlays, nspcsd) Fortran order */
+    const int* cgrid_index;      /* [nspec] 0-based */
+    const int* convert;          /* [nspec] */
+    const float* ta, *qv, *dens, *pres;      /* (ncols, nrows, nlays) */
+    const float* seaice, *ocean_szone;       /* (ncols, nrows) */
+    const float* rj;             /* (ncols, nrows, nlays, nphotab) */
+    const double* khetero;       /* (nhet, ncols, nrows, nlays) */
+    int tstep_sec;               /* TIME2SEC(TSTEP(2)) */
+    double rtol, atol;           /* REAL(GLBL_RTOL, 8), REAL(GLBL_ATOL, 8) */
+    int blksize;                 /* BLKSIZE (50 in the reference) */
+    int lreorder;                /* LREORDER */
+    int max_iter;
+    int threads;
+    /* outputs */
+    long long nsteps_total, nfails_total;
+    int nfailed_blocks;
+} OracleChemArgs;
+
+/* Per-block gather (rbdriver.F:460-511), CALC_RCONST and day/night choice (:513-519). */
+static int gather_block(const OracleChemArgs* a, const int* ccol, const int* crow, const int* clev,
+                        const long* nordcell, long offset, int numcells, Block* b, double* blktemp,
+                        double* blkpres, double* blkh2o, double* blkdens, float* blksvol,
+                        double* blksea, double* rjblk, double* blkhet, const float* fwd)
+{
+    const float PA2ATM = 1.0f / 101325.0f;
+    const float MAOMV = 28.9628f / 18.0153f;
+    const float QV_TO_PPM = 1.0e+06f * MAOMV;
+    const long nxy = (long)a->ncols * a->nrows;
+    const long ncell = nxy * a->nlays;
+    for (int c = 0; c < numcells; ++c) {
+        const long cell = nordcell[offset + c];
+        const long g = ccol[cell] + (long)a->ncols * (crow[cell] + (long)a->nrows * clev[cell]);
+        const long col2 = ccol[cell] + (long)a->ncols * crow[cell];
+        blktemp[c] = (double)a->ta[g];
+        blkdens[c] = (double)a->dens[g];
+        blksvol[c] = 1.0f / a->dens[g];
+        blkpres[c] = (double)(PA2ATM * a->pres[g]);
+        blkh2o[c] = (double)fmaxf(QV_TO_PPM * a->qv[g], 0.0f);
+        blksea[c] = (double)fmaxf(0.0f, a->ocean_szone[col2] - a->seaice[col2]);
+    }
+    for (int isp = 0; isp < MECH_ISCHAN; ++isp) {
+        const int spc = a->cgrid_index[isp];
+        const int ispnew = mech_iold2new[isp];
+        for (int c = 0; c < numcells; ++c) {
+            const long cell = nordcell[offset + c];
+            const long g = ccol[cell] + (long)a->ncols * (crow[cell] + (long)a->nrows * clev[cell]);
+            const float cv = a->conc[(size_t)spc * ncell + g];
+            float v;
+            if (a->convert[isp]) v = fmaxf(fwd[isp] * blksvol[c] * cv, 1.0e-30f);
+            else v = fmaxf(cv, 1.0e-30f);
+            b->y[(size_t)ispnew * b->ld + c] = (double)v;
+        }
+    }
+    int lsun = 0;
+    for (int c = 0; c < numcells; ++c) {
+        const long cell = nordcell[offset + c];
+        const long g = ccol[cell] + (long)a->ncols * (crow[cell] + (long)a->nrows * clev[cell]);
+        for (int k = 0; k < MECH_NHETERO; ++k) blkhet[(size_t)k * b->ld + c] = a->khetero[(size_t)g * MECH_NHETERO + k];
+        for (int k = 0; k < MECH_NPHOTAB; ++k) {
+            const double v = (double)a->rj[(size_t)k * ncell + g];
+            rjblk[(size_t)k * b->ld + c] = v;
+            if (v > 0.0) lsun = 1;
+        }
+    }
+    b->ncells = numcells;
+    mech_calc_rconst(numcells, b->ld, blktemp, blkpres, blkh2o, rjblk, blkhet, lsun, blksea, b->rki);
+    return lsun ? 0 : 1;   /* NCSP: 0 = day, 1 = night */
+}
+
+/* One CHEM call (rbdriver.F) on the whole grid with the given BLKSIZE. */
+int oracle_chem(OracleChemArgs* a)
+{
+    const long nxy = (long)a->ncols * a->nrows;
+    const long noxyz = nxy * a->nlays;
+    const long ncell = noxyz;
+    const int blksize = a->blksize > 0 ? a->blksize : 50;
+    /* cell list ordered (LEV, COL, ROW) with ROW fastest (rbinit.F:269-281) */
+    int* ccol = malloc(sizeof(int) * noxyz);
+    int* crow = malloc(sizeof(int) * noxyz);
+    int* clev = malloc(sizeof(int) * noxyz);
+    long nc = 0;
+    for (int lev = 0; lev < a->nlays; ++lev)
+        for (int col = 0; col < a->ncols; ++col)
+            for (int row = 0; row < a->nrows; ++row) { ccol[nc] = col; crow[nc] = row; clev[nc] = lev; ++nc; }
+    /* blocks (rbinit.F:286-303) */
+    const long nblks = 1 + (noxyz - 1) / blksize;
+    long iavg = 1 + (noxyz - 1) / nblks;
+    if (iavg > blksize) iavg = blksize;
+    long* blkcno = malloc(sizeof(long) * nblks);
+    int* blklen = malloc(sizeof(int) * nblks);
+    long off = 0;
+    for (long k = 0; k < nblks - 1; ++k) { blkcno[k] = off; blklen[k] = (int)iavg; off += iavg; }
+    blkcno[nblks - 1] = off;
+    blklen[nblks - 1] = (int)(noxyz - (nblks - 1) * iavg);
+    /* units (rbinit.F:250-254) */
+    float fwd[MECH_NSPEC];
+    double rev[MECH_NSPEC];
+    for (int s = 0; s < MECH_NSPEC; ++s) {
+        fwd[s] = 1.0e-3f * 28.9628f / (float)mech_molwt[s];
+        rev[s] = (double)(1.0f / fwd[s]);
+    }
+    long* nordcell = malloc(sizeof(long) * noxyz);
+    for (long c = 0; c < noxyz; ++c) nordcell[c] = c;
+    double* errmx2 = calloc((size_t)noxyz, sizeof(double));
+    const double chemstep = (double)a->tstep_sec / 60.0;
+    int lordering = (a->lreorder && nblks > 1 && blksize > 1) ? 1 : 0;
+    long long tot_steps = 0, tot_fails = 0;
+    int nfailed = 0;
+    const SolverCfg cfg = {a->rtol, a->atol, (double)(1.0f / (float)MECH_NSPEC), a->max_iter};
+#ifdef _OPENMP
+    if (a->threads > 0) omp_set_num_threads(a->threads);
+#endif
+    for (int pass = 0; pass < 2; ++pass) {
+        const int ordering_pass = (pass == 0 && lordering);
+        if (pass == 0 && !lordering) continue;
+        if (!ordering_pass) memset(errmx2, 0, sizeof(double) * noxyz);
+#ifdef _OPENMP
+#pragma omp parallel reduction(+ : tot_steps, tot_fails, nfailed)
+#endif
+        {
+            Block b;
+            block_alloc(&b, blksize);
+            double* blktemp = malloc(sizeof(double) * blksize);
+            double* blkpres = malloc(sizeof(double) * blksize);
+            double* blkh2o = malloc(sizeof(double) * blksize);
+            double* blkdens = malloc(sizeof(double) * blksize);
+            float* blksvol = malloc(sizeof(float) * blksize);
+            double* blksea = malloc(sizeof(double) * blksize);
+            double* rjblk = malloc(sizeof(double) * blksize * MECH_NPHOTAB);
+            double* blkhet = malloc(sizeof(double) * blksize * (MECH_NHETERO > 0 ? MECH_NHETERO : 1));
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 1)
+#endif
+            for (long blk = 0; blk < nblks; ++blk) {
+                const int numcells = blklen[blk];
+                const long offset = blkcno[blk];
+                const int ncsp = gather_block(a, ccol, crow, clev, nordcell, offset, numcells, &b, blktemp,
+                                              blkpres, blkh2o, blkdens, blksvol, blksea, rjblk, blkhet, fwd);
+                if (ordering_pass) {
+                    oracle_rbsolver(&b, ncsp, chemstep, &cfg, &errmx2[offset]);
+                    continue;
+                }
+                SolverStats st = oracle_rbsolver(&b, ncsp, chemstep, &cfg, NULL);
+                tot_steps += st.nsteps;
+                tot_fails += st.nfails;
+                nfailed += st.status != 0;
+                /* write-back (rbdriver.F:577-595) */
+                for (int isp = 0; isp < MECH_ISCHAN; ++isp) {
+                    const int old = mech_inew2old[isp];
+                    const int spc = a->cgrid_index[old];
+                    for (int c = 0; c < numcells; ++c) {
+                        const long cell = nordcell[offset + c];
+                        const long g = ccol[cell] + (long)a->ncols * (crow[cell] + (long)a->nrows * clev[cell]);
+                        const double yv = b.y[(size_t)isp * b.ld + c];
+                        a->conc[(size_t)spc * ncell + g] =
+                            a->convert[old] ? (float)(rev[old] * blkdens[c] * yv) : (float)yv;
+                    }
+                }
+            }
+            block_free(&b);
+            free(blktemp); free(blkpres); free(blkh2o); free(blkdens); free(blksvol); free(blksea);
+            free(rjblk); free(blkhet);
+        }
+        if (ordering_pass) {
+            /* heap sort of cells by ERRMX2, ascending (rbdriver.F:683-724) */
+            long lval = noxyz / 2 + 1, irval = noxyz;
+            double vallow;
+            long jreord;
+            /* 1-based indexing helpers */
+            double* E = errmx2 - 1;
+            long* N = nordcell - 1;
+            for (;;) {
+                if (lval > 1) {
+                    lval = lval - 1;
+                    vallow = E[lval];
+                    jreord = N[lval];
+                } else {
+                    vallow = E[irval];
+                    jreord = N[irval];
+                    E[irval] = E[1];
+                    N[irval] = N[1];
+                    irval = irval - 1;
+                    if (irval == 1) {
+                        E[irval] = vallow;
+                        N[irval] = jreord;
+                        break;
+                    }
+                }
+                long ipar = lval, jpar = lval + lval;
+                while (jpar <= irval) {
+                    if (jpar < irval && E[jpar] < E[jpar + 1]) jpar = jpar + 1;
+                    if (vallow < E[jpar]) {
+                        E[ipar] = E[jpar];
+                        N[ipar] = N[jpar];
+                        ipar = jpar;
+                        jpar = jpar + jpar;
+                    } else {
+                        jpar = irval + 1;
+                    }
+                }
+                E[ipar] = vallow;
+                N[ipar] = jreord;
+            }
+        }
+    }
+    a->nsteps_total = tot_steps;
+    a->nfails_total = tot_fails;
+    a->nfailed_blocks = nfailed;
+    free(ccol); free(crow); free(clev); free(blkcno); free(blklen); free(nordcell); free(errmx2);
+    return nfailed;
+}
