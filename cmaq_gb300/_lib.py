@@ -1,0 +1,91 @@
+"""ctypes binding of libcmaqchem.so (include/cmaqchem.h).
+
+The library is built in-tree by ``python -m cmaq_gb300.build``; loading fails loudly
+when it is missing -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from functools import lru_cache
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "_build" / "libcmaqchem.so"
+
+SOLVER_ROS3, SOLVER_EBI = 0, 1
+SCHED_STATIC, SCHED_QUEUE = 0, 1
+CELL_DT_UNDERFLOW, CELL_MAXITER, CELL_NONFINITE = 1, 2, 4
+
+
+class ChemError(RuntimeError):
+    pass
+
+
+class Cfg(C.Structure):
+    _fields_ = [("mechanism", C.c_char_p), ("solver", C.c_int), ("schedule", C.c_int), ("rtol", C.c_double),
+                ("atol", C.c_double), ("ncols", C.c_int), ("nrows", C.c_int), ("nlays", C.c_int),
+                ("nspcsd", C.c_int), ("cgrid_index", C.POINTER(C.c_int)), ("device", C.c_int),
+                ("max_iter", C.c_int)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("accepted_steps", C.c_longlong), ("rejected_steps", C.c_longlong),
+                ("failed_cells", C.c_longlong), ("sunlit_cells", C.c_longlong), ("sunlit_attempts", C.c_longlong),
+                ("device_ms", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class MechInfo(C.Structure):
+    _fields_ = [("nspec", C.c_int), ("nrxns", C.c_int), ("ischan", C.c_int), ("nphotab", C.c_int),
+                ("nhetero", C.c_int), ("iarray_day", C.c_int), ("iarray_night", C.c_int),
+                ("flops_step_day", C.c_double), ("flops_step_night", C.c_double)]
+
+
+@lru_cache(maxsize=None)
+def lib() -> C.CDLL:
+    if not LIB_PATH.exists():
+        raise ChemError(f"{LIB_PATH} is not built; run `python -m cmaq_gb300.build` (needs nvcc)")
+    L = C.CDLL(str(LIB_PATH))
+    vp, fp, dp, ip, u8p = C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_double), C.POINTER(C.c_int), C.c_void_p
+    L.cmaqchem_init.argtypes = [C.POINTER(Cfg), C.POINTER(vp)]
+    L.cmaqchem_step.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, C.c_int, C.c_int, ip, C.POINTER(Stats)]
+    L.cmaqchem_step_device.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, C.c_int, C.c_int, ip, vp,
+                                       C.POINTER(Stats)]
+    L.cmaqchem_cell_stats.argtypes = [vp, vp, vp]
+    L.cmaqchem_ros3_solve_device.argtypes = [vp, C.c_longlong, vp, vp, vp, C.c_double, vp, vp, vp, vp]
+    L.cmaqchem_rconst_device.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+    L.cmaqchem_mech_info_get.argtypes = [C.c_char_p, C.POINTER(MechInfo), ip]
+    L.cmaqchem_destroy.argtypes = [vp]
+    L.cmaqchem_destroy.restype = None
+    L.cmaqchem_last_error.argtypes = [C.c_char_p, C.c_size_t]
+    L.cmaqchem_diag_fp64_peak.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    return L
+
+
+def fp64_peak(device: int = 0) -> tuple[float, float]:
+    """Measured FP64 FMA throughput (TFLOP/s) and kernel time (ms) of `device`."""
+    tf, ms = C.c_double(), C.c_double()
+    if lib().cmaqchem_diag_fp64_peak(device, C.byref(tf), C.byref(ms)) != 0:
+        raise ChemError("FP64 peak measurement failed")
+    return tf.value, ms.value
+
+
+def last_error() -> str:
+    buf = C.create_string_buffer(4096)
+    lib().cmaqchem_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(rc: int) -> int:
+    if rc < 0:
+        raise ChemError(last_error())
+    return rc
+
+
+def mech_info(mechanism: str):
+    info = MechInfo()
+    check(lib().cmaqchem_mech_info_get(mechanism.encode(), C.byref(info), None))
+    order = (C.c_int * info.nspec)()
+    check(lib().cmaqchem_mech_info_get(mechanism.encode(), None, order))
+    return info, list(order)

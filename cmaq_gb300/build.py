@@ -38,7 +38,8 @@ def sources() -> list[Path]:
 
 
 def _headers() -> list[Path]:
-    return sorted(CSRC.glob("*.cuh")) + sorted((CSRC / "gen").glob("*.cuh")) + [PKG.parent / "include" / "cmaqchem.h"]
+    return (sorted(CSRC.glob("*.cuh")) + sorted((CSRC / "gen").glob("*.cuh"))
+            + sorted((PKG.parent / "include").glob("*.h")))
 
 
 def build(jobs: int | None = None, verbose: bool = False) -> Path:

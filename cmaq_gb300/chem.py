@@ -1,0 +1,222 @@
+"""Host-side chemistry operator: the GB300 counterpart of CMAQ's ``CHEM``.
+
+CMAQ calls ``CHEM(CGRID, JDATE, JTIME, TSTEP)`` once per synchronisation step
+(CCTM/src/driver/sciproc.F:298); the operator sets itself up on its first call
+(rbdriver.F:226-371) and reads met, photolysis and heterogeneous rates through
+modules.  Here:
+
+* :class:`ChemSolver` owns a library handle (the first-call state) and exposes
+  ``step`` (one CHEM call), the solver-level ``solve`` (RBSOLVER with given rate
+  constants) and ``rconst`` (CALC_RCONST);
+* :func:`CHEM` keeps the reference's call signature; the implicit inputs are set
+  with :func:`set_environment`, the analogue of the modules CHEM reads.
+
+Arrays are CMAQ's Fortran layouts held as C-ordered arrays of reversed shape
+(``conc[spc, lay, row, col]`` = ``CONC(col, row, lay, spc)``).  ``step`` accepts
+numpy arrays (copied to and from the GPU inside the call) or CUDA torch tensors
+(used in place).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import ChemError, check
+
+SCHEDULES = {"static": _lib.SCHED_STATIC, "plain": _lib.SCHED_STATIC, "queue": _lib.SCHED_QUEUE,
+             "batched": _lib.SCHED_QUEUE}
+
+
+def reference_tolerance(x: float) -> float:
+    """RB_RTOL / RB_ATOL are REAL(4) run-time settings widened to REAL(8) (rbinit.F:250-251)."""
+    return float(np.float32(x))
+
+
+def _is_torch(x) -> bool:
+    return hasattr(x, "data_ptr") and hasattr(x, "is_cuda")
+
+
+def _ptr(x):
+    if x is None:
+        return None
+    if _is_torch(x):
+        if not x.is_cuda:
+            raise ChemError("torch tensors passed to the chemistry operator must be on the GPU")
+        if not x.is_contiguous():
+            raise ChemError("torch tensors must be contiguous")
+        return C.c_void_p(x.data_ptr())
+    if not x.flags["C_CONTIGUOUS"]:
+        raise ChemError("numpy arrays must be C-contiguous")
+    return C.c_void_p(x.ctypes.data)
+
+
+def tstep_array(tstep) -> C.Array:
+    t = (C.c_int * 3)(*[int(v) for v in tstep])
+    return t
+
+
+class ChemSolver:
+    """One chemistry handle for a fixed local domain (first-call state of CHEM)."""
+
+    def __init__(self, mechanism: str = "cb6r5_ae7_aq", *, ncols: int, nrows: int, nlays: int, nspcsd: int,
+                 cgrid_index=None, rtol: float = 1.0e-3, atol: float = 1.0e-7, schedule: str = "queue",
+                 device: int = 0, max_iter: int = 0, reference_tolerances: bool = True):
+        if schedule not in SCHEDULES:
+            raise ChemError(f"unknown schedule {schedule!r}; use one of {sorted(SCHEDULES)}")
+        self.mechanism = mechanism
+        self.info, self.inew2old = _lib.mech_info(mechanism)
+        self.shape = (nlays, nrows, ncols)
+        self.nspcsd = nspcsd
+        self.rtol = reference_tolerance(rtol) if reference_tolerances else float(rtol)
+        self.atol = reference_tolerance(atol) if reference_tolerances else float(atol)
+        self._cgi = None
+        if cgrid_index is not None:
+            self._cgi = (C.c_int * self.info.nspec)(*[int(v) for v in cgrid_index])
+        cfg = _lib.Cfg(mechanism.encode(), _lib.SOLVER_ROS3, SCHEDULES[schedule], self.rtol, self.atol, ncols, nrows,
+                       nlays, nspcsd, self._cgi, device, max_iter)
+        h = C.c_void_p()
+        check(_lib.lib().cmaqchem_init(C.byref(cfg), C.byref(h)))
+        self._h = h
+        self.schedule = schedule
+
+    @property
+    def ncell(self) -> int:
+        n = 1
+        for s in self.shape:
+            n *= s
+        return n
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.lib().cmaqchem_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def step(self, conc, ta, qv, dens, pres, seaice, ocean_szone, rj, khetero, jdate: int = 2018182,
+             jtime: int = 0, tstep=(10000, 500, 500), stream=None) -> dict:
+        """One CHEM call (rbdriver.F).  Returns totals; ``failed_cells`` > 0 when some cells stopped
+        (their per-cell status is in :meth:`cell_stats`)."""
+        args = [conc, ta, qv, dens, pres, seaice, ocean_szone, rj, khetero]
+        on_gpu = [_is_torch(a) for a in args]
+        if any(on_gpu) and not all(on_gpu):
+            raise ChemError("pass either all numpy arrays (host) or all CUDA tensors (device)")
+        self._check_shapes(*args)
+        st = _lib.Stats()
+        ts = tstep_array(tstep)
+        ptrs = [_ptr(a) for a in args]
+        if all(on_gpu):
+            s = C.c_void_p(stream) if isinstance(stream, int) else (
+                C.c_void_p(stream.cuda_stream) if stream is not None else None)
+            rc = _lib.lib().cmaqchem_step_device(self._h, *ptrs, jdate, jtime, ts, s, C.byref(st))
+        else:
+            rc = _lib.lib().cmaqchem_step(self._h, *ptrs, jdate, jtime, ts, C.byref(st))
+        check(rc)
+        return st.as_dict()
+
+    def _check_shapes(self, conc, ta, qv, dens, pres, seaice, ocean_szone, rj, khetero):
+        L, R, Cc = self.shape
+        exp = {"conc": (self.nspcsd, L, R, Cc), "ta": (L, R, Cc), "qv": (L, R, Cc), "dens": (L, R, Cc),
+               "pres": (L, R, Cc), "seaice": (R, Cc), "ocean_szone": (R, Cc),
+               "rj": (self.info.nphotab, L, R, Cc), "khetero": (L, R, Cc, self.info.nhetero)}
+        got = dict(conc=conc, ta=ta, qv=qv, dens=dens, pres=pres, seaice=seaice, ocean_szone=ocean_szone, rj=rj,
+                   khetero=khetero)
+        for k, shp in exp.items():
+            a = got[k]
+            if tuple(a.shape) != shp:
+                raise ChemError(f"{k} has shape {tuple(a.shape)}, expected {shp}")
+            want = "float64" if k == "khetero" else "float32"
+            if want not in str(a.dtype):
+                raise ChemError(f"{k} must be {want}, got {a.dtype}")
+
+    def cell_stats(self):
+        status = np.zeros(self.shape, np.int32)
+        attempts = np.zeros(self.shape, np.int32)
+        check(_lib.lib().cmaqchem_cell_stats(self._h, C.c_void_p(status.ctypes.data),
+                                             C.c_void_p(attempts.ctypes.data)))
+        return status, attempts
+
+    def solve(self, y, rki, night, chemstep_min: float, with_stats: bool = False, stream=None):
+        """RBSOLVER on CUDA tensors: y [ischan, n] (solver species order) in place, rki [nrxns, n],
+        night [n] uint8.  Optional per-cell status / accepted / rejected step counts."""
+        import torch
+        n = y.shape[1]
+        st = ns = nf = None
+        if with_stats:
+            st, ns, nf = (torch.zeros(n, dtype=torch.int32, device=y.device) for _ in range(3))
+        s = C.c_void_p(stream.cuda_stream) if stream is not None else None
+        check(_lib.lib().cmaqchem_ros3_solve_device(self._h, n, _ptr(y), _ptr(rki), _ptr(night), chemstep_min,
+                                                    _ptr(st), _ptr(ns), _ptr(nf), s))
+        return (st, ns, nf) if with_stats else None
+
+    def rconst(self, conc, ta, qv, dens, pres, seaice, ocean_szone, rj, khetero):
+        """CALC_RCONST for every cell of the grid (CUDA tensors): returns rki [nrxns, ncell], sunlit [ncell]."""
+        import torch
+        dev = conc.device
+        rki = torch.empty((self.info.nrxns, self.ncell), dtype=torch.float64, device=dev)
+        sun = torch.empty(self.ncell, dtype=torch.uint8, device=dev)
+        check(_lib.lib().cmaqchem_rconst_device(self._h, *[_ptr(a) for a in (conc, ta, qv, dens, pres, seaice,
+                                                                            ocean_szone, rj, khetero)],
+                                                _ptr(rki), _ptr(sun), None))
+        return rki, sun
+
+
+# ------------------------------------------------------------------ reference-shaped entry point
+@dataclass
+class Environment:
+    """The inputs CHEM reads through modules: met (INTERPOLATE_VAR), OCEAN+SZONE, SEAICE,
+    photolysis rates (PHOT_MOD RJ) and heterogeneous rates (AEROSOL_CHEMISTRY KHETERO)."""
+    ta: object
+    qv: object
+    dens: object
+    pres: object
+    seaice: object
+    ocean_szone: object
+    rj: object
+    khetero: object
+    nspcsd: int
+    mechanism: str = "cb6r5_ae7_aq"
+    cgrid_index: object = None
+    rtol: float = 1.0e-3
+    atol: float = 1.0e-7
+    schedule: str = "queue"
+
+
+_ENV: Environment | None = None
+_SOLVER: ChemSolver | None = None
+
+
+def set_environment(env: Environment) -> None:
+    global _ENV, _SOLVER
+    _ENV = env
+    if _SOLVER is not None:
+        _SOLVER.close()
+        _SOLVER = None
+
+
+def CHEM(conc, jdate: int, jtime: int, tstep) -> dict:
+    """``CHEM(CGRID, JDATE, JTIME, TSTEP)``: integrate the gas chemistry of every cell over
+    TSTEP(2) and update ``conc`` in place.  The first call sets the solver up."""
+    global _SOLVER
+    if _ENV is None:
+        raise ChemError("CHEM: call set_environment() with the met, photolysis and heterogeneous inputs first")
+    e = _ENV
+    nlays, nrows, ncols = tuple(e.ta.shape)
+    if _SOLVER is None:
+        _SOLVER = ChemSolver(e.mechanism, ncols=ncols, nrows=nrows, nlays=nlays, nspcsd=e.nspcsd,
+                             cgrid_index=e.cgrid_index, rtol=e.rtol, atol=e.atol, schedule=e.schedule)
+    return _SOLVER.step(conc, e.ta, e.qv, e.dens, e.pres, e.seaice, e.ocean_szone, e.rj, e.khetero, jdate,
+                        jtime, tstep)

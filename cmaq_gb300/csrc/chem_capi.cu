@@ -223,7 +223,7 @@ extern "C" int cmaqchem_init(const cmaqchem_cfg* cfg, cmaqchem_handle** out)
         CK(cudaMalloc(&h->d_steps, sizeof(int) * h->ncell));
         CK(cudaMemset(h->d_status, 0, sizeof(int) * h->ncell));
         CK(cudaMemset(h->d_steps, 0, sizeof(int) * h->ncell));
-        CK(cudaMalloc(&h->d_counters, sizeof(unsigned long long) * 4));
+        CK(cudaMalloc(&h->d_counters, sizeof(unsigned long long) * 5));
         CK(cudaMalloc(&h->d_order, sizeof(int) * h->ncell));
         CK(cudaMalloc(&h->d_hist, sizeof(unsigned int) * chem::QUEUE_BINS));
         CK(cudaMalloc(&h->d_cursor, sizeof(unsigned long long) * chem::QUEUE_BINS));
@@ -255,7 +255,7 @@ static int step_device_impl(cmaqchem_handle* h, float* conc, const float* ta, co
     const double chemstep = (double)itmstep / 60.0;   // rbdriver.F:384-385
     CK(cudaSetDevice(h->device));
     chem::GridArgs a = grid_args(h, conc, ta, qv, dens, pres, seaice, osz, rj, khet, chemstep);
-    CK(cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned long long) * 4, s));
+    CK(cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned long long) * 5, s));
     CK(cudaEventRecord(h->ev0, s));
     if (h->cfg.schedule == CMAQCHEM_SCHED_QUEUE) {
         chem::QueueArgs q{nullptr, h->d_head};
@@ -276,7 +276,7 @@ static int step_device_impl(cmaqchem_handle* h, float* conc, const float* ta, co
         CK(h->ops->chem_static(a, h->nblocks, s));
     }
     CK(cudaEventRecord(h->ev1, s));
-    unsigned long long cnt[4];
+    unsigned long long cnt[5];
     CK(cudaMemcpyAsync(cnt, h->d_counters, sizeof(cnt), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     h->have_history = true;
@@ -287,6 +287,7 @@ static int step_device_impl(cmaqchem_handle* h, float* conc, const float* ta, co
         stats->rejected_steps = (long long)cnt[1];
         stats->failed_cells = (long long)cnt[2];
         stats->sunlit_cells = (long long)cnt[3];
+        stats->sunlit_attempts = (long long)cnt[4];
         stats->device_ms = ms;
     }
     return (int)cnt[2];

@@ -55,7 +55,8 @@ struct GridArgs {
     int max_iter;
     int* cell_status;              // [ncell] or nullptr
     int* cell_steps;               // [ncell] accepted + rejected step attempts, or nullptr
-    unsigned long long* counters;  // [4]: accepted steps, rejected steps, failed cells, sunlit cells
+    unsigned long long* counters;  // [5]: accepted steps, rejected steps, failed cells, sunlit cells,
+                                   //      step attempts of sunlit cells
 };
 
 template <class M>
@@ -119,7 +120,7 @@ __global__ void __launch_bounds__(THREADS_PER_BLOCK, 1) k_chem_ros3(GridArgs a)
     const long long nwarps = (long long)gridDim.x * WARPS_PER_BLOCK;
     const long long warp = (long long)blockIdx.x * WARPS_PER_BLOCK + (threadIdx.x >> 5);
     double* ws = warp_ws<M>(a.ws, warp);
-    unsigned long long acc_steps = 0, rej_steps = 0, failed = 0, sunlit = 0;
+    unsigned long long acc_steps = 0, rej_steps = 0, failed = 0, sunlit = 0, sun_att = 0;
     for (long long base = warp * 32; base < a.ncell; base += nwarps * 32) {
         const long long c = base + (threadIdx.x & 31);
         const bool active = c < a.ncell;
@@ -133,6 +134,7 @@ __global__ void __launch_bounds__(THREADS_PER_BLOCK, 1) k_chem_ros3(GridArgs a)
             rej_steps += st.nfails;
             failed += st.status != ros3::ST_OK;
             sunlit += sun;
+            if (sun) sun_att += st.nsteps + st.nfails;
             if (a.cell_status) a.cell_status[c] = st.status;
             if (a.cell_steps) a.cell_steps[c] = st.nsteps + st.nfails;
         }
@@ -144,12 +146,14 @@ __global__ void __launch_bounds__(THREADS_PER_BLOCK, 1) k_chem_ros3(GridArgs a)
             rej_steps += __shfl_down_sync(0xffffffffu, rej_steps, o);
             failed += __shfl_down_sync(0xffffffffu, failed, o);
             sunlit += __shfl_down_sync(0xffffffffu, sunlit, o);
+            sun_att += __shfl_down_sync(0xffffffffu, sun_att, o);
         }
         if ((threadIdx.x & 31) == 0) {
             atomicAdd(&a.counters[0], acc_steps);
             atomicAdd(&a.counters[1], rej_steps);
             atomicAdd(&a.counters[2], failed);
             atomicAdd(&a.counters[3], sunlit);
+            atomicAdd(&a.counters[4], sun_att);
         }
     }
 }

@@ -1,0 +1,57 @@
+// Measurement helpers (include/cmaqchem_diag.h).
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "../../include/cmaqchem_diag.h"
+
+namespace {
+
+constexpr int CHAINS = 8;
+
+// Each thread runs CHAINS independent dependent-FMA chains; the result is stored only
+// when it matches an impossible value, so the work cannot be removed.
+__global__ void k_fp64_fma(int iters, double b, double c, double* sink)
+{
+    double a[CHAINS];
+#pragma unroll
+    for (int k = 0; k < CHAINS; ++k) a[k] = (double)(threadIdx.x + k) * 1.0e-3;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < CHAINS; ++k) a[k] = fma(a[k], b, c);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < CHAINS; ++k) s += a[k];
+    if (s == -1.2345e300) sink[threadIdx.x] = s;
+}
+
+}  // namespace
+
+extern "C" int cmaqchem_diag_fp64_peak(int device, double* tflops, double* ms)
+{
+    if (cudaSetDevice(device) != cudaSuccess) return -1;
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+    double* sink = nullptr;
+    if (cudaMalloc(&sink, 1024 * sizeof(double)) != cudaSuccess) return -1;
+    const int threads = 256, blocks = nsm * 8, iters = 4096;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    k_fp64_fma<<<blocks, threads>>>(64, 0.999999, 1.0e-7, sink);   // warm-up
+    cudaEventRecord(e0);
+    k_fp64_fma<<<blocks, threads>>>(iters, 0.999999, 1.0e-7, sink);
+    cudaEventRecord(e1);
+    cudaError_t err = cudaEventSynchronize(e1);
+    float t = 0.0f;
+    cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(sink);
+    if (err != cudaSuccess) return -1;
+    const double flops = 2.0 * CHAINS * (double)iters * threads * blocks;
+    if (tflops) *tflops = flops / (t * 1.0e-3) / 1.0e12;
+    if (ms) *ms = t;
+    return 0;
+}

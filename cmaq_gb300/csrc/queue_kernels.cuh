@@ -32,7 +32,7 @@ __global__ void __launch_bounds__(THREADS_PER_BLOCK, 1) k_chem_ros3_queue(GridAr
     long long cell = -1;
     bool sun = false;
     bool drained = false;
-    unsigned long long acc_steps = 0, rej_steps = 0, failed = 0, sunlit = 0;
+    unsigned long long acc_steps = 0, rej_steps = 0, failed = 0, sunlit = 0, sun_att = 0;
     for (;;) {
         // refill idle lanes with one atomic per warp
         if (!drained) {
@@ -64,6 +64,7 @@ __global__ void __launch_bounds__(THREADS_PER_BLOCK, 1) k_chem_ros3_queue(GridAr
                 rej_steps += s.st.nfails;
                 failed += s.st.status != ros3::ST_OK;
                 sunlit += sun;
+                if (sun) sun_att += s.st.nsteps + s.st.nfails;
                 if (a.cell_status) a.cell_status[cell] = s.st.status;
                 if (a.cell_steps) a.cell_steps[cell] = s.st.nsteps + s.st.nfails;
                 cell = -1;
@@ -76,12 +77,14 @@ __global__ void __launch_bounds__(THREADS_PER_BLOCK, 1) k_chem_ros3_queue(GridAr
             rej_steps += __shfl_down_sync(0xffffffffu, rej_steps, o);
             failed += __shfl_down_sync(0xffffffffu, failed, o);
             sunlit += __shfl_down_sync(0xffffffffu, sunlit, o);
+            sun_att += __shfl_down_sync(0xffffffffu, sun_att, o);
         }
         if (lane == 0) {
             atomicAdd(&a.counters[0], acc_steps);
             atomicAdd(&a.counters[1], rej_steps);
             atomicAdd(&a.counters[2], failed);
             atomicAdd(&a.counters[3], sunlit);
+            atomicAdd(&a.counters[4], sun_att);
         }
     }
 }

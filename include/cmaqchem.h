@@ -71,6 +71,7 @@ typedef struct {
     long long rejected_steps;
     long long failed_cells;    /* cells with a non-zero status */
     long long sunlit_cells;
+    long long sunlit_attempts; /* step attempts (accepted + rejected) of sunlit cells */
     double device_ms;          /* device time of the call's kernels */
 } cmaqchem_stats;
 

@@ -1,0 +1,72 @@
+"""Shared helpers of the test suite: oracle-side gathers and GPU runs of one CHEM call."""
+from __future__ import annotations
+
+import numpy as np
+
+from cmaq_gb300.synthetic import GridInputs, manifest
+
+F32 = np.float32
+
+
+def gather_cells(g: GridInputs, o):
+    """Per-cell inputs gathered like rbdriver.F:460-511 (REAL(4) arithmetic), cells in CGRID order.
+
+    Returns y [nspec, n] (solver species order), rki [nrxns, n], night [n] via the oracle's CALC_RCONST."""
+    man = manifest(g.mech)
+    n = g.ncell
+    conc = g.conc.reshape(g.nspcsd, n)
+    dens = g.dens.reshape(n)
+    svol = (F32(1.0) / dens).astype(F32)
+    y = np.zeros((o.nspec, n))
+    for s, sp in enumerate(man["species"]):
+        v = conc[g.cgrid_index[s] - 1]
+        if sp["convert"]:
+            fwd = F32(F32(1.0e-3) * F32(28.9628)) / F32(sp["molwt"])
+            v = (F32(fwd) * svol).astype(F32) * v
+        y[o.iold2new[s]] = np.maximum(v.astype(F32), F32(1.0e-30)).astype(np.float64)
+    temp = g.ta.reshape(n).astype(np.float64)
+    pres = (F32(F32(1.0) / F32(101325.0)) * g.pres.reshape(n)).astype(F32).astype(np.float64)
+    qv2ppm = F32(F32(1.0e6) * F32(F32(28.9628) / F32(18.0153)))
+    h2o = np.maximum((qv2ppm * g.qv.reshape(n)).astype(F32), F32(0.0)).astype(np.float64)
+    col = np.arange(n) % (g.ncols * g.nrows)
+    sea = np.maximum(F32(0.0), (g.ocean_szone.reshape(-1) - g.seaice.reshape(-1)).astype(F32))[col].astype(np.float64)
+    rj = g.rj.reshape(o.nphotab, n).astype(np.float64)
+    het = g.khetero.reshape(n, -1).T.astype(np.float64)
+    sun = (rj > 0).any(axis=0)
+    rki = np.zeros((o.nrxns, n))
+    for lit in (True, False):
+        idx = np.where(sun == lit)[0]
+        if len(idx):
+            rki[:, idx] = o.rconst(temp[idx], pres[idx], h2o[idx], rj[:, idx], het[:, idx], lit, sea[idx])
+    return y, rki, (~sun).astype(np.uint8)
+
+
+def to_cuda(g: GridInputs):
+    import torch
+    t = {k: torch.from_numpy(np.ascontiguousarray(getattr(g, k))).cuda()
+         for k in ("conc", "ta", "qv", "dens", "pres", "seaice", "ocean_szone", "rj", "khetero")}
+    return t
+
+
+def gpu_chem(g: GridInputs, schedule="static", rtol=1e-3, atol=1e-9, tstep=(10000, 500, 500), nsteps=1,
+             solver=None):
+    """Run nsteps CHEM calls on the GPU; returns (conc numpy, stats list, solver)."""
+    from cmaq_gb300.chem import ChemSolver
+    t = to_cuda(g)
+    s = solver or ChemSolver(g.mech, ncols=g.ncols, nrows=g.nrows, nlays=g.nlays, nspcsd=g.nspcsd,
+                             cgrid_index=g.cgrid_index, rtol=rtol, atol=atol, schedule=schedule)
+    stats = []
+    for _ in range(nsteps):
+        stats.append(s.step(t["conc"], t["ta"], t["qv"], t["dens"], t["pres"], t["seaice"], t["ocean_szone"],
+                            t["rj"], t["khetero"], tstep=tstep))
+    return t["conc"].cpu().numpy(), stats, s
+
+
+def rel_err(a, b, floor=1e-10):
+    """Max relative difference over entries where either value exceeds `floor` (ppmV)."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    m = (np.abs(a) > floor) | (np.abs(b) > floor)
+    if not m.any():
+        return 0.0
+    return float(np.max(np.abs(a[m] - b[m]) / np.maximum(np.abs(b[m]), floor)))
