@@ -92,6 +92,11 @@ class Mechanism:
     third_body_conc: dict[str, float] = field(default_factory=dict)
     rxlabel: list[str] = field(default_factory=list)
     nspecial_rxn: int = 0
+    rtdat: list[list[float]] = field(default_factory=list)   # [rxn][3]
+    rfdat: list[list[float]] = field(default_factory=list)   # [falloff][5]
+    irrfall: list[int] = field(default_factory=list)          # 1-based reactions
+    iorder: list[int] = field(default_factory=list)
+    kunits: int = 0
 
 
 _TB = {"NRXWM": "M", "NRXWO2": "O2", "NRXWN2": "N2", "NRXWW": "H2O", "NRXWH2": "H2", "NRXWCH4": "CH4"}
@@ -199,6 +204,15 @@ def parse_rxns_data(text: str) -> Mechanism:
     sc_cols = [[fnum(v) for v in col("SC", str(k))] for k in range(1, mech.mxprd + 1)]
     mech.sc = [[sc_cols[k][r] for k in range(mech.mxprd)] for r in range(nr)]
     mech.rxlabel = [v.strip("'").strip() for v in col("RXLABEL")]
+    rt = [[fnum(v) for v in col("RTDAT", str(k))] for k in (1, 2, 3)]
+    mech.rtdat = [[rt[0][r], rt[1][r], rt[2][r]] for r in range(nr)]
+    nfall = int(params.get("NFALLOFF", "0"))
+    if nfall > 0:
+        rf = [[fnum(v) for v in col("RFDAT", str(k))] for k in (1, 2, 3, 4, 5)]
+        mech.rfdat = [[rf[k][i] for k in range(5)] for i in range(nfall)]
+        mech.irrfall = [int(v) for v in col("IRRFALL")][:nfall]
+    mech.iorder = [int(v) for v in col("IORDER")]
+    mech.kunits = int(params.get("KUNITS", "0"))
     mech.photab = [v.strip("'").strip() for v in arrays["PHOTAB"][("IRXXN",)]]
     mech.hetero = [v.strip("'").strip() for v in arrays["HETERO"][("IRXXN",)]]
     nmphot = pint("NMPHOT")

@@ -58,6 +58,10 @@ def manifest(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src_has
                        "sunlit_rate_block": r in photo_rx, "ktype": m.ktype[r]}
                       for r in range(m.nrxns)],
         "third_body": m.third_body, "third_body_conc": m.third_body_conc,
+        "rate_tables": {"ktype": m.ktype, "rtdat": m.rtdat, "rfdat": m.rfdat, "irrfall": m.irrfall,
+                        "iorder": m.iorder, "kunits": m.kunits, "iph": m.iph, "ihetero": m.ihetero,
+                        "rate_block": {str(r): ("photo" if r in prog.photo else "seawater" if r in
+                                                prog.seawater_cond else "thermal") for r in range(m.nrxns)}},
         "active": sp.active, "iarray": sp.iarray, "nnz_jac": sp.nnz_jac,
         "flops_per_step": {"day": flop_counts(m, sp, 0), "night": flop_counts(m, sp, 1)},
     }
@@ -244,17 +248,18 @@ def oracle_source(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, sr
     return "\n".join(L) + "\n"
 
 
-def write_outputs(cmaq_root: str, mech: str) -> dict:
+def write_outputs(cmaq_root: str, mech: str, out_root: Path = REPO) -> dict:
     m, prog, sp, src_hash = load(cmaq_root, mech)
     man = manifest(m, prog, sp, mech, src_hash)
-    mdir = REPO / "cmaq_gb300" / "mechs" / mech
+    REPO_ = Path(out_root)
+    mdir = REPO_ / "cmaq_gb300" / "mechs" / mech
     mdir.mkdir(parents=True, exist_ok=True)
     (mdir / "manifest.json").write_text(json.dumps(man, indent=1) + "\n")
-    odir = REPO / "oracle" / "gen"
+    odir = REPO_ / "oracle" / "gen"
     odir.mkdir(parents=True, exist_ok=True)
     (odir / f"{mech}_mech.c").write_text(oracle_source(m, prog, sp, mech, src_hash))
     from .emit_cuda import cuda_sources
-    cdir = REPO / "cmaq_gb300" / "csrc" / "gen"
+    cdir = REPO_ / "cmaq_gb300" / "csrc" / "gen"
     cdir.mkdir(parents=True, exist_ok=True)
     for old in cdir.glob(f"{mech}_*"):
         old.unlink()

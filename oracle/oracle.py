@@ -53,6 +53,8 @@ def load(mech: str = "cb6r5_ae7_aq") -> C.CDLL:
                                           ip, ip, ip, C.c_int]
     lib.oracle_chem.argtypes = [C.POINTER(OracleChemArgs)]
     lib.oracle_mech_name.restype = C.c_char_p
+    lib.oracle_set_dtmin.argtypes = [C.c_double]
+    lib.oracle_get_dtmin.restype = C.c_double
     return lib
 
 
@@ -69,6 +71,20 @@ class Oracle:
         self.iold2new = np.zeros(self.nspec, np.int32)
         self.lib.oracle_inew2old(_p(self.inew2old, C.c_int))
         self.lib.oracle_iold2new(_p(self.iold2new, C.c_int))
+
+    def tight(self):
+        """Context manager for the tight truth solution: DTMIN lowered to 1e-14 min."""
+        import contextlib
+
+        @contextlib.contextmanager
+        def cm():
+            old = self.lib.oracle_get_dtmin()
+            self.lib.oracle_set_dtmin(1.0e-14)
+            try:
+                yield self
+            finally:
+                self.lib.oracle_set_dtmin(old)
+        return cm()
 
     def rconst(self, temp, pres_atm, h2o_ppm, rj, het, sunlit: bool, seawater) -> np.ndarray:
         n = len(temp)

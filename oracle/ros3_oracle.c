@@ -51,7 +51,10 @@ static const double D2 = -0.29079558716805469821718236208017e+01;
 static const double D3 = 0.22354069897811569627360909276199e+00;
 #define GROW (1.0 / 3.00)
 #define RGAM (1.0 / GAM)
-static const double DTSTART = 0.5e-01, DTMIN = 1.0e-08, DTMAX = 1.0e+01, UROUND = 1.0e-18;
+static const double DTSTART = 0.5e-01, DTMAX = 1.0e+01, UROUND = 1.0e-18;
+/* DTMIN of rbsolver.F:105 (1.0e-8 min).  Only the tight truth solution lowers it, so that
+ * tolerances far below the reference's can resolve the initial radical transients. */
+static double DTMIN = 1.0e-08;
 static const double FACMAX = 1.0e+01, FACMIN = 1.0e-01, FACONE = 1.0e+00, CONMIN = 1.0e-30;
 
 /* per-cell status bits (shared meaning with the device code) */
@@ -332,6 +335,9 @@ static SolverStats oracle_rbsolver(Block* b, int ncsp, double chemstep, const So
 }
 
 /* ------------------------------------------------------------------ exported API */
+
+void oracle_set_dtmin(double dtmin) { DTMIN = dtmin > 0.0 ? dtmin : 1.0e-08; }
+double oracle_get_dtmin(void) { return DTMIN; }
 
 int oracle_nspec(void) { return MECH_NSPEC; }
 int oracle_nrxns(void) { return MECH_NRXNS; }
