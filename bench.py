@@ -1,0 +1,379 @@
+"""Benchmark: ROS3 CB6r5 grid-cells/s per 1-h chemistry step on GB300.
+
+One step = one CHEM call (a 5-min synchronisation step) over the whole grid; a
+1-hour chemistry step is 12 of them, so
+
+    value = cells / (12 * seconds per step)     [grid-cells/s per 1-h chem step]
+
+timed over K consecutive steps from the seeded initial state (K = 12 by default:
+exactly the first simulated hour).  Workload: cb6r5_ae7_aq on the CONUS-size grid
+459 x 299 x 35 (4,803,315 cells), rtol 1e-3, atol 1e-9 ppmV, FP64, seeded
+synthetic inputs (cmaq_gb300/synthetic.py); CGRID (4 GB) is larger than L2, so no
+L2 flush is needed between steps.
+
+Arms and extras
+* gb300 (default): the batched persistent kernel (work queue ordered by previous
+  step counts) on device-resident arrays -> ``value``; the plain per-cell kernel on
+  the same steps -> ``plain``; the host-pointer C ABI with copies inside the timed
+  region -> ``e2e``; the FP64 roofline of the solver kernel; a bounded CPU sample of
+  the reference algorithm (the C oracle, BLKSIZE 50 with the stiffness reordering)
+  on the host cores -> ``cpu_baseline``.
+* --impl reference: the reference algorithm (C oracle; the Fortran cannot be
+  compiled here) on all host cores, bounded sample per step.
+
+Multi-GPU (torchrun): every rank integrates its own grid of the same size (CMAQ
+gives each process its own subdomain; chemistry exchanges nothing), timing is the
+max over ranks and ``value`` counts all ranks' cells: weak scaling.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "ROS3 CB6r5 grid-cells/s per 1-h chem step"
+UNIT = "grid-cells/s per 1-h chem step"
+RTOL, ATOL = 1.0e-3, 1.0e-9
+TSTEP = (10000, 500, 500)          # TSTEP(3) HHMMSS: output 1 h, sync 5 min
+STEPS_PER_HOUR = 12
+
+WORKLOADS = {
+    "conus": dict(ncols=459, nrows=299, nlays=35),
+    "conus_skewed": dict(ncols=459, nrows=299, nlays=35, plume_fraction=0.3),
+    "small": dict(ncols=100, nrows=100, nlays=10),
+    "cpu4k": dict(ncols=20, nrows=20, nlays=10),
+}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            import tempfile
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.device)],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = float(p[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def make_inputs(workload: str, seed: int):
+    from cmaq_gb300.synthetic import make_grid
+    return make_grid(seed=seed, **WORKLOADS[workload])
+
+
+def flops_of(st: dict, info) -> float:
+    att = st["accepted_steps"] + st["rejected_steps"]
+    sun = st["sunlit_attempts"]
+    return sun * info.flops_step_day + (att - sun) * info.flops_step_night
+
+
+def run_device(g, schedule: str, steps: int, warmup: int, dist, device: int, sample_clocks: bool):
+    """K timed CHEM calls on device-resident arrays from the initial state."""
+    import torch
+    from cmaq_gb300.chem import ChemSolver
+    dev = {k: torch.from_numpy(np.ascontiguousarray(getattr(g, k))).to(f"cuda:{device}")
+           for k in ("conc", "ta", "qv", "dens", "pres", "seaice", "ocean_szone", "rj", "khetero")}
+    conc0 = dev["conc"].clone()
+    s = ChemSolver(g.mech, ncols=g.ncols, nrows=g.nrows, nlays=g.nlays, nspcsd=g.nspcsd, cgrid_index=g.cgrid_index,
+                   rtol=RTOL, atol=ATOL, schedule=schedule, device=device)
+    stream = torch.cuda.current_stream(device)
+    args = [dev[k] for k in ("conc", "ta", "qv", "dens", "pres", "seaice", "ocean_szone", "rj", "khetero")]
+    for _ in range(warmup):
+        s.step(*args, tstep=TSTEP, stream=stream)
+    # the warm-up steps leave the queue ordered by step counts; restart the hour from the initial state
+    dev["conc"].copy_(conc0)
+    torch.cuda.synchronize(device)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stats = []
+    clocks = ClockSampler(device) if sample_clocks else None
+    if clocks:
+        clocks.__enter__()
+    barrier(dist)
+    torch.cuda.synchronize(device)
+    t0 = time.perf_counter()
+    ev0.record(stream)
+    for _ in range(steps):
+        stats.append(s.step(*args, tstep=TSTEP, stream=stream))
+    ev1.record(stream)
+    torch.cuda.synchronize(device)
+    wall = time.perf_counter() - t0
+    barrier(dist)
+    if clocks:
+        clocks.__exit__()
+    ms = ev0.elapsed_time(ev1)
+    s.close()
+    del dev, conc0
+    torch.cuda.empty_cache()
+    return {"ms_total": ms, "wall_s": wall, "stats": stats, "clocks": clocks.summary() if clocks else None}
+
+
+def run_e2e(g, steps: int, warmup: int, dist, device: int):
+    """Same hour through the host-pointer C ABI (cmaqchem_step): every call copies CGRID, met,
+    photolysis and heterogeneous rates host->device and CGRID device->host."""
+    import torch
+    from cmaq_gb300.chem import ChemSolver
+
+    def pinned(a):
+        t = torch.empty(a.shape, dtype={np.float32: torch.float32, np.float64: torch.float64}[a.dtype.type],
+                        pin_memory=True)
+        t.numpy()[...] = a
+        return t.numpy()
+
+    h = {k: pinned(np.ascontiguousarray(getattr(g, k)))
+         for k in ("conc", "ta", "qv", "dens", "pres", "seaice", "ocean_szone", "rj", "khetero")}
+    conc0 = h["conc"].copy()
+    s = ChemSolver(g.mech, ncols=g.ncols, nrows=g.nrows, nlays=g.nlays, nspcsd=g.nspcsd, cgrid_index=g.cgrid_index,
+                   rtol=RTOL, atol=ATOL, schedule="queue", device=device)
+    args = [h[k] for k in ("conc", "ta", "qv", "dens", "pres", "seaice", "ocean_szone", "rj", "khetero")]
+    for _ in range(warmup):
+        s.step(*args, tstep=TSTEP)
+    h["conc"][...] = conc0
+    h2d = sum(a.nbytes for a in args)
+    d2h = h["conc"].nbytes
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        s.step(*args, tstep=TSTEP)
+    wall = time.perf_counter() - t0
+    barrier(dist)
+    s.close()
+    return {"wall_s": wall, "h2d": h2d, "d2h": d2h}
+
+
+def barrier(dist):
+    if dist is not None:
+        import torch.distributed as tdist
+        tdist.barrier()
+
+
+def max_over_ranks(x: float, dist) -> float:
+    if dist is None:
+        return x
+    import torch
+    import torch.distributed as tdist
+    t = torch.tensor([x], dtype=torch.float64, device=dist)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_reference(workload_cells: int, steps: int, warmup: int, threads: int, target_s: float = 20.0):
+    """The reference algorithm (C oracle: BLKSIZE 50, stiffness reordering) on host cores, on a
+    sample grid drawn from the same distributions; K calls from the initial state after W calls."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    from oracle import Oracle
+    from cmaq_gb300.synthetic import make_grid
+    o = Oracle("cb6r5_ae7_aq")
+    rt, at = float(np.float32(RTOL)), float(np.float32(ATOL))
+    # size the sample so that the timed calls take about target_s
+    ncols = 20
+    g = make_grid(ncols=ncols, nrows=10, nlays=10, seed=2018)
+    t0 = time.perf_counter()
+    c, _ = o.chem(g, blksize=50, rtol=rt, atol=at, threads=threads)
+    first = time.perf_counter() - t0
+    est_hour = first * 3.0            # later calls are cheaper than the first
+    scale = max(1, min(64, int(target_s / max(est_hour, 1e-3))))
+    g = make_grid(ncols=ncols * scale, nrows=10, nlays=10, seed=2018)
+    conc = g.conc.copy()
+    for _ in range(warmup):
+        conc, _ = o.chem(g, blksize=50, rtol=rt, atol=at, threads=threads, conc=conc)
+    conc = g.conc.copy()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        conc, _ = o.chem(g, blksize=50, rtol=rt, atol=at, threads=threads, conc=conc)
+    wall = time.perf_counter() - t0
+    value = g.ncell / (STEPS_PER_HOUR * wall / steps)
+    return {"value": value, "cells": g.ncell, "wall_s": wall, "steps": steps}
+
+
+def host_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=STEPS_PER_HOUR)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="conus", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain-kernel comparison")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    a = ap.parse_args()
+    world, rank, local = dist_env()
+
+    if a.impl == "reference":
+        if rank != 0:
+            return 0
+        thr = host_threads()
+        r = cpu_reference(0, a.steps, a.warmup, thr, target_s=60.0)
+        line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "impl": "reference", "n_gpus": a.gpus,
+                "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * r["wall_s"] / r["steps"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded; cmaq_gb300/synthetic.py)",
+                "config": {"workload": f"cb6r5_ae7_aq sample grid {r['cells']} cells (same distributions as "
+                                       "459x299x35), 12 x 5-min CHEM calls, rtol 1e-3 atol 1e-9",
+                           "algorithm": "reference ROS3 (BLKSIZE 50, stiffness reordering) restated in C; "
+                                        "the Fortran reference cannot be compiled on this image"},
+                "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": thr, "kind": "port",
+                                 "sample": f"{r['cells']} cells x {r['steps']} CHEM calls"},
+                "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as tdist
+        torch.cuda.set_device(local)
+        tdist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
+        dist = torch.device(f"cuda:{local}")
+    device = local if world > 1 else 0
+    torch.cuda.set_device(device)
+    from cmaq_gb300 import _lib
+    try:
+        _lib.lib()
+    except _lib.ChemError:
+        from cmaq_gb300 import build as cbuild
+        cbuild.build()
+        _lib.lib.cache_clear()
+    info, _ = _lib.mech_info("cb6r5_ae7_aq")
+    peak_tf, _ = _lib.fp64_peak(device)
+
+    g = make_inputs(a.workload, seed=2018 + rank)
+    ncell = g.ncell
+    batched = run_device(g, "queue", a.steps, a.warmup, dist, device, sample_clocks=(rank == 0))
+    ms_step = max_over_ranks(batched["ms_total"] / a.steps, dist)
+    value = world * ncell / (STEPS_PER_HOUR * ms_step / 1e3)
+    fl = sum(flops_of(s, info) for s in batched["stats"])
+    dev_ms = sum(s["device_ms"] for s in batched["stats"])
+    achieved_tf = fl / (dev_ms * 1e-3) / 1e12
+    attempts = sum(s["accepted_steps"] + s["rejected_steps"] for s in batched["stats"])
+
+    plain = None
+    if not a.no_plain:
+        p = run_device(g, "static", a.steps, a.warmup, dist, device, sample_clocks=False)
+        p_ms = max_over_ranks(p["ms_total"] / a.steps, dist)
+        p_fl = sum(flops_of(s, info) for s in p["stats"])
+        p_dev = sum(s["device_ms"] for s in p["stats"])
+        plain = {"value": world * ncell / (STEPS_PER_HOUR * p_ms / 1e3), "ms_per_step": p_ms,
+                 "achieved_tflops": p_fl / (p_dev * 1e-3) / 1e12}
+
+    e2e = None
+    if not a.no_e2e:
+        e = run_e2e(g, a.steps, min(a.warmup, 1), dist, device)
+        e_s = max_over_ranks(e["wall_s"] / a.steps, dist)
+        e2e = {"value": world * ncell / (STEPS_PER_HOUR * e_s), "unit": UNIT, "h2d_bytes_per_step": e["h2d"],
+               "d2h_bytes_per_step": e["d2h"], "ms_per_step": 1e3 * e_s,
+               "path": "cmaqchem_step (host pointers, pinned buffers; copies inside each call)"}
+
+    cpu = None
+    if rank == 0 and not a.no_cpu:
+        thr = host_threads()
+        r = cpu_reference(ncell, STEPS_PER_HOUR, 0, thr, target_s=15.0)
+        cpu = {"value": r["value"], "unit": UNIT, "cores": thr, "kind": "port",
+               "sample": f"{r['cells']} cells of the same distributions x {r['steps']} CHEM calls "
+                         f"(reference algorithm, BLKSIZE 50 + reordering, C restatement, {r['wall_s']:.1f} s)"}
+
+    traffic = None
+    tfile = ROOT / "profiles" / "traffic_per_step.json"
+    if tfile.exists():
+        try:
+            traffic = json.loads(tfile.read_text()).get(a.workload)
+        except Exception:
+            traffic = None
+    if rank == 0:
+        launches_per_step = 4 if a.warmup > 0 else 1   # queue ordering (hist, scan, scatter) + solve
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded; cmaq_gb300/synthetic.py)",
+            "config": {"workload": f"cb6r5_ae7_aq {g.ncols}x{g.nrows}x{g.nlays} ({ncell} cells per GPU), "
+                                   f"{a.steps} x 5-min CHEM calls from the initial state, rtol 1e-3, atol 1e-9 ppmV",
+                       "schedule": "batched (persistent, work queue ordered by previous step counts)",
+                       "cells": ncell, "step_attempts_per_cell": attempts / ncell / a.steps,
+                       "l2": "inputs larger than L2 (CGRID %.1f GB); no flush" % (g.conc.nbytes / 1e9),
+                       "parallelism": f"replicas x{world} (own grid per GPU)"},
+            "roofline": {"bound": "fp64", "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
+                         "frac": achieved_tf / peak_tf, "traffic": traffic,
+                         "peak_source": "measured live: FP64 FMA-chain kernel (no FP64 figure in "
+                                        "MEASURED_PEAKS.json)",
+                         "flops": "algorithmic FLOPs of the reference's ROS3 step per attempt x attempts"},
+            "plain": plain,
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "clocks": batched["clocks"],
+            "gpu_launches": launches_per_step * a.steps,
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        import torch.distributed as tdist
+        tdist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
