@@ -138,9 +138,11 @@ def run_device(g, schedule: str, steps: int, warmup: int, dist, device: int, sam
                    rtol=RTOL, atol=ATOL, schedule=schedule, device=device)
     stream = torch.cuda.current_stream(device)
     args = [dev[k] for k in ("conc", "ta", "qv", "dens", "pres", "seaice", "ocean_szone", "rj", "khetero")]
+    # every warm-up step is the hour's first CHEM call from the initial state, so the queue
+    # order the timed hour starts from comes from the same call
     for _ in range(warmup):
+        dev["conc"].copy_(conc0)
         s.step(*args, tstep=TSTEP, stream=stream)
-    # the warm-up steps leave the queue ordered by step counts; restart the hour from the initial state
     dev["conc"].copy_(conc0)
     torch.cuda.synchronize(device)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -186,6 +188,7 @@ def run_e2e(g, steps: int, warmup: int, dist, device: int):
                    rtol=RTOL, atol=ATOL, schedule="queue", device=device)
     args = [h[k] for k in ("conc", "ta", "qv", "dens", "pres", "seaice", "ocean_szone", "rj", "khetero")]
     for _ in range(warmup):
+        h["conc"][...] = conc0
         s.step(*args, tstep=TSTEP)
     h["conc"][...] = conc0
     h2d = sum(a.nbytes for a in args)
@@ -324,7 +327,7 @@ def main():
 
     e2e = None
     if not a.no_e2e:
-        e = run_e2e(g, a.steps, min(a.warmup, 1), dist, device)
+        e = run_e2e(g, a.steps, a.warmup, dist, device)
         e_s = max_over_ranks(e["wall_s"] / a.steps, dist)
         e2e = {"value": world * ncell / (STEPS_PER_HOUR * e_s), "unit": UNIT, "h2d_bytes_per_step": e["h2d"],
                "d2h_bytes_per_step": e["d2h"], "ms_per_step": 1e3 * e_s,

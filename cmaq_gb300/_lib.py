@@ -43,10 +43,12 @@ class MechInfo(C.Structure):
 
 
 @lru_cache(maxsize=None)
-def lib() -> C.CDLL:
-    if not LIB_PATH.exists():
-        raise ChemError(f"{LIB_PATH} is not built; run `python -m cmaq_gb300.build` (needs nvcc)")
-    L = C.CDLL(str(LIB_PATH))
+def lib(variant: str = "r255") -> C.CDLL:
+    """The library build of one register-cap variant (see cmaq_gb300/build.py)."""
+    path = LIB_PATH if variant == "r255" else LIB_PATH.parent / variant / "libcmaqchem.so"
+    if not path.exists():
+        raise ChemError(f"{path} is not built; run `python -m cmaq_gb300.build {variant}` (needs nvcc)")
+    L = C.CDLL(str(path))
     vp, fp, dp, ip, u8p = C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_double), C.POINTER(C.c_int), C.c_void_p
     L.cmaqchem_init.argtypes = [C.POINTER(Cfg), C.POINTER(vp)]
     L.cmaqchem_step.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, C.c_int, C.c_int, ip, C.POINTER(Stats)]
@@ -71,15 +73,15 @@ def fp64_peak(device: int = 0) -> tuple[float, float]:
     return tf.value, ms.value
 
 
-def last_error() -> str:
+def last_error(L: C.CDLL | None = None) -> str:
     buf = C.create_string_buffer(4096)
-    lib().cmaqchem_last_error(buf, len(buf))
+    (L or lib()).cmaqchem_last_error(buf, len(buf))
     return buf.value.decode(errors="replace")
 
 
-def check(rc: int) -> int:
+def check(rc: int, L: C.CDLL | None = None) -> int:
     if rc < 0:
-        raise ChemError(last_error())
+        raise ChemError(last_error(L))
     return rc
 
 

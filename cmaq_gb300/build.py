@@ -21,6 +21,8 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = BUILD / "libcmaqchem.so"
+# register-cap variants the autotuner can choose from: name -> -maxrregcount (None = no cap)
+VARIANTS = {"r255": None, "r168": 168, "r128": 128}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-rdc=true", "-fmad=false", "-lineinfo", "-Xcompiler", "-fPIC",
               "-Xptxas", "-O3"]
@@ -42,14 +44,24 @@ def _headers() -> list[Path]:
             + sorted((PKG.parent / "include").glob("*.h")))
 
 
-def build(jobs: int | None = None, verbose: bool = False) -> Path:
-    BUILD.mkdir(exist_ok=True)
+def lib_path(variant: str = "r255") -> Path:
+    return LIB if variant == "r255" else BUILD / variant / "libcmaqchem.so"
+
+
+def build(jobs: int | None = None, verbose: bool = False, variant: str = "r255") -> Path:
+    """Build one register-cap variant (``r255`` is the default library)."""
+    if variant not in VARIANTS:
+        raise ValueError(f"unknown variant {variant}")
+    out_dir = BUILD if variant == "r255" else BUILD / variant
+    out_dir.mkdir(parents=True, exist_ok=True)
+    lib = lib_path(variant)
+    extra = [] if VARIANTS[variant] is None else [f"-maxrregcount={VARIANTS[variant]}"]
     nvcc = _nvcc()
     hdr_mtime = max(p.stat().st_mtime for p in _headers())
     todo, objs = [], []
     for src in sources():
         rel = src.relative_to(CSRC).as_posix().replace("/", "__")
-        obj = BUILD / (rel[:-3] + ".o")
+        obj = out_dir / (rel[:-3] + ".o")
         objs.append(obj)
         if obj.exists() and obj.stat().st_mtime > max(src.stat().st_mtime, hdr_mtime):
             continue
@@ -57,7 +69,7 @@ def build(jobs: int | None = None, verbose: bool = False) -> Path:
 
     def compile_one(item):
         src, obj = item
-        cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-I", str(CSRC), "-c", str(src), "-o", str(obj) + ".tmp"]
+        cmd = [nvcc, *ARCH, *NVCC_FLAGS, *extra, "-I", str(CSRC), "-c", str(src), "-o", str(obj) + ".tmp"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {src.name}:\n{r.stderr[-4000:]}")
@@ -68,15 +80,16 @@ def build(jobs: int | None = None, verbose: bool = False) -> Path:
     if todo:
         with ThreadPoolExecutor(max_workers=jobs or os.cpu_count() or 4) as ex:
             list(ex.map(compile_one, todo))
-    if todo or not LIB.exists():
-        cmd = [nvcc, *ARCH, "-shared", "-rdc=true", *[str(o) for o in objs], "-o", str(LIB) + ".tmp"]
+    if todo or not lib.exists():
+        cmd = [nvcc, *ARCH, "-shared", "-rdc=true", *[str(o) for o in objs], "-o", str(lib) + ".tmp"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stderr[-4000:]}")
-        os.replace(str(LIB) + ".tmp", LIB)
-    return LIB
+        os.replace(str(lib) + ".tmp", lib)
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(verbose=True))
+    for v in (sys.argv[1:] or ["r255"]):
+        print(build(verbose=True, variant=v))
     sys.exit(0)

@@ -63,10 +63,12 @@ class ChemSolver:
 
     def __init__(self, mechanism: str = "cb6r5_ae7_aq", *, ncols: int, nrows: int, nlays: int, nspcsd: int,
                  cgrid_index=None, rtol: float = 1.0e-3, atol: float = 1.0e-7, schedule: str = "queue",
-                 device: int = 0, max_iter: int = 0, reference_tolerances: bool = True):
+                 device: int = 0, max_iter: int = 0, reference_tolerances: bool = True, variant: str = "r255"):
         if schedule not in SCHEDULES:
             raise ChemError(f"unknown schedule {schedule!r}; use one of {sorted(SCHEDULES)}")
         self.mechanism = mechanism
+        self.variant = variant
+        self._L = _lib.lib(variant)
         self.info, self.inew2old = _lib.mech_info(mechanism)
         self.shape = (nlays, nrows, ncols)
         self.nspcsd = nspcsd
@@ -78,7 +80,7 @@ class ChemSolver:
         cfg = _lib.Cfg(mechanism.encode(), _lib.SOLVER_ROS3, SCHEDULES[schedule], self.rtol, self.atol, ncols, nrows,
                        nlays, nspcsd, self._cgi, device, max_iter)
         h = C.c_void_p()
-        check(_lib.lib().cmaqchem_init(C.byref(cfg), C.byref(h)))
+        check(self._L.cmaqchem_init(C.byref(cfg), C.byref(h)), self._L)
         self._h = h
         self.schedule = schedule
 
@@ -91,7 +93,7 @@ class ChemSolver:
 
     def close(self):
         if getattr(self, "_h", None):
-            _lib.lib().cmaqchem_destroy(self._h)
+            self._L.cmaqchem_destroy(self._h)
             self._h = None
 
     def __del__(self):
@@ -121,10 +123,10 @@ class ChemSolver:
         if all(on_gpu):
             s = C.c_void_p(stream) if isinstance(stream, int) else (
                 C.c_void_p(stream.cuda_stream) if stream is not None else None)
-            rc = _lib.lib().cmaqchem_step_device(self._h, *ptrs, jdate, jtime, ts, s, C.byref(st))
+            rc = self._L.cmaqchem_step_device(self._h, *ptrs, jdate, jtime, ts, s, C.byref(st))
         else:
-            rc = _lib.lib().cmaqchem_step(self._h, *ptrs, jdate, jtime, ts, C.byref(st))
-        check(rc)
+            rc = self._L.cmaqchem_step(self._h, *ptrs, jdate, jtime, ts, C.byref(st))
+        check(rc, self._L)
         return st.as_dict()
 
     def _check_shapes(self, conc, ta, qv, dens, pres, seaice, ocean_szone, rj, khetero):
@@ -145,8 +147,8 @@ class ChemSolver:
     def cell_stats(self):
         status = np.zeros(self.shape, np.int32)
         attempts = np.zeros(self.shape, np.int32)
-        check(_lib.lib().cmaqchem_cell_stats(self._h, C.c_void_p(status.ctypes.data),
-                                             C.c_void_p(attempts.ctypes.data)))
+        check(self._L.cmaqchem_cell_stats(self._h, C.c_void_p(status.ctypes.data),
+                                          C.c_void_p(attempts.ctypes.data)), self._L)
         return status, attempts
 
     def solve(self, y, rki, night, chemstep_min: float, with_stats: bool = False, stream=None):
@@ -158,8 +160,8 @@ class ChemSolver:
         if with_stats:
             st, ns, nf = (torch.zeros(n, dtype=torch.int32, device=y.device) for _ in range(3))
         s = C.c_void_p(stream.cuda_stream) if stream is not None else None
-        check(_lib.lib().cmaqchem_ros3_solve_device(self._h, n, _ptr(y), _ptr(rki), _ptr(night), chemstep_min,
-                                                    _ptr(st), _ptr(ns), _ptr(nf), s))
+        check(self._L.cmaqchem_ros3_solve_device(self._h, n, _ptr(y), _ptr(rki), _ptr(night), chemstep_min,
+                                                 _ptr(st), _ptr(ns), _ptr(nf), s), self._L)
         return (st, ns, nf) if with_stats else None
 
     def rconst(self, conc, ta, qv, dens, pres, seaice, ocean_szone, rj, khetero):
@@ -168,9 +170,9 @@ class ChemSolver:
         dev = conc.device
         rki = torch.empty((self.info.nrxns, self.ncell), dtype=torch.float64, device=dev)
         sun = torch.empty(self.ncell, dtype=torch.uint8, device=dev)
-        check(_lib.lib().cmaqchem_rconst_device(self._h, *[_ptr(a) for a in (conc, ta, qv, dens, pres, seaice,
-                                                                            ocean_szone, rj, khetero)],
-                                                _ptr(rki), _ptr(sun), None))
+        check(self._L.cmaqchem_rconst_device(self._h, *[_ptr(a) for a in (conc, ta, qv, dens, pres, seaice,
+                                                                         ocean_szone, rj, khetero)],
+                                             _ptr(rki), _ptr(sun), None), self._L)
         return rki, sun
 
 
