@@ -62,6 +62,7 @@ def lib(variant: str = "r255") -> C.CDLL:
     L.cmaqchem_destroy.restype = None
     L.cmaqchem_last_error.argtypes = [C.c_char_p, C.c_size_t]
     L.cmaqchem_diag_fp64_peak.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.cmaqchem_diag_set_tuning.argtypes = [vp, C.c_char_p, C.c_int]
     return L
 
 

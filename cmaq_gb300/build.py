@@ -21,8 +21,9 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = BUILD / "libcmaqchem.so"
-# register-cap variants the autotuner can choose from: name -> -maxrregcount (None = no cap)
-VARIANTS = {"r255": None, "r168": 168, "r128": 128}
+# build variants the autotuner can choose from: name -> extra nvcc flags
+VARIANTS = {"r255": [], "r168": ["-maxrregcount=168"], "r128": ["-maxrregcount=128"],
+            "lucs": ["-DCHEM_LDLU(p)=__ldcs(p)"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-rdc=true", "-fmad=false", "-lineinfo", "-Xcompiler", "-fPIC",
               "-Xptxas", "-O3"]
@@ -55,7 +56,7 @@ def build(jobs: int | None = None, verbose: bool = False, variant: str = "r255")
     out_dir = BUILD if variant == "r255" else BUILD / variant
     out_dir.mkdir(parents=True, exist_ok=True)
     lib = lib_path(variant)
-    extra = [] if VARIANTS[variant] is None else [f"-maxrregcount={VARIANTS[variant]}"]
+    extra = list(VARIANTS[variant])
     nvcc = _nvcc()
     hdr_mtime = max(p.stat().st_mtime for p in _headers())
     todo, objs = [], []

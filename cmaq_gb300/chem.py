@@ -84,6 +84,11 @@ class ChemSolver:
         self._h = h
         self.schedule = schedule
 
+    def set_tuning(self, **knobs) -> None:
+        """Scheduling knobs (see include/cmaqchem_diag.h): night_pattern=0/1, lockstep=0/1."""
+        for k, v in knobs.items():
+            check(self._L.cmaqchem_diag_set_tuning(self._h, k.encode(), int(v)), self._L)
+
     @property
     def ncell(self) -> int:
         n = 1

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/cmaqchem.h"
+#include "../../include/cmaqchem_diag.h"
 #include "mech_ops.cuh"
 
 extern const MechOps mech_ops_cb6r5_ae7_aq;
@@ -52,6 +53,9 @@ int hhmmss_to_sec(int t)
 
 }  // namespace
 
+// error-text setter for the library's other translation units, not exported
+__attribute__((visibility("hidden"))) void cmaqchem_set_error(const std::string& msg) { g_err = msg; }
+
 struct cmaqchem_handle {
     const MechOps* ops = nullptr;
     cmaqchem_cfg cfg{};
@@ -74,6 +78,9 @@ struct cmaqchem_handle {
     unsigned long long* d_cursor = nullptr;
     unsigned long long* d_head = nullptr;
     bool have_history = false;
+    // tuning knobs (cmaqchem_diag_set_tuning)
+    int use_night = 1;
+    int lockstep = 0;
     // device staging of the host-pointer entry point, allocated on first use
     float *s_conc = nullptr, *s_ta = nullptr, *s_qv = nullptr, *s_dens = nullptr, *s_pres = nullptr;
     float *s_seaice = nullptr, *s_osz = nullptr, *s_rj = nullptr;
@@ -127,6 +134,7 @@ chem::GridArgs grid_args(cmaqchem_handle* h, float* conc, const float* ta, const
     a.cell_status = h->d_status;
     a.cell_steps = h->d_steps;
     a.counters = h->d_counters;
+    a.use_night = h->use_night;
     return a;
 }
 
@@ -244,6 +252,15 @@ extern "C" int cmaqchem_init(const cmaqchem_cfg* cfg, cmaqchem_handle** out)
 
 extern "C" void cmaqchem_destroy(cmaqchem_handle* h) { free_handle(h); }
 
+extern "C" int cmaqchem_diag_set_tuning(cmaqchem_handle* h, const char* key, int value)
+{
+    if (!h || !key) return fail("null argument");
+    if (strcmp(key, "night_pattern") == 0) h->use_night = value != 0;
+    else if (strcmp(key, "lockstep") == 0) h->lockstep = value != 0;
+    else return fail(std::string("unknown tuning key ") + key);
+    return 0;
+}
+
 static int step_device_impl(cmaqchem_handle* h, float* conc, const float* ta, const float* qv, const float* dens,
                             const float* pres, const float* seaice, const float* osz, const float* rj,
                             const double* khet, const int tstep[3], cudaStream_t s, cmaqchem_stats* stats)
@@ -271,7 +288,7 @@ static int step_device_impl(cmaqchem_handle* h, float* conc, const float* ta, co
             q.order = h->d_order;
         }
         CK(cudaMemsetAsync(h->d_head, 0, sizeof(unsigned long long), s));
-        CK(h->ops->chem_queue(a, q, h->nblocks, s));
+        CK(h->ops->chem_queue(a, q, h->lockstep != 0, h->nblocks, s));
     } else {
         CK(h->ops->chem_static(a, h->nblocks, s));
     }

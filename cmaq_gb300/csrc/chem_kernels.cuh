@@ -57,6 +57,7 @@ struct GridArgs {
     int* cell_steps;               // [ncell] accepted + rejected step attempts, or nullptr
     unsigned long long* counters;  // [5]: accepted steps, rejected steps, failed cells, sunlit cells,
                                    //      step attempts of sunlit cells
+    int use_night;                 // 1: all-dark warps use the night pattern; 0: day pattern always
 };
 
 template <class M>
@@ -126,7 +127,7 @@ __global__ void __launch_bounds__(THREADS_PER_BLOCK, 1) k_chem_ros3(GridArgs a)
         const bool active = c < a.ncell;
         bool sun = false;
         if (active) sun = gather_cell<M>(a, c, ws);
-        const bool night = __all_sync(0xffffffffu, !sun);
+        const bool night = a.use_night && __all_sync(0xffffffffu, !sun);
         if (active) {
             ros3::CellStats st = ros3::integrate<M>(ws, a.chemstep, a.tol, night, a.max_iter);
             scatter_cell<M>(a, c, ws);

@@ -5,6 +5,10 @@
 #ifndef CHEM_HD
 #define CHEM_HD __device__
 #endif
+// load of an LU factor or 1/U(i,i); a build may define it as a streaming load (__ldcs)
+#ifndef CHEM_LDLU
+#define CHEM_LDLU(p) (*(p))
+#endif
 namespace mech_cb6r5_ae7_aq {
 constexpr const char* NAME = "cb6r5_ae7_aq";
 constexpr int NSPEC = 149;
@@ -26,6 +30,12 @@ constexpr int OFF_LU = 2277;
 constexpr int OFF_VDIAG = 3967;
 constexpr int IARRAY_DAY = 1689;
 constexpr int IARRAY_NIGHT = 1615;
+constexpr int EBI_OFF_YC = 2277;
+constexpr int EBI_OFF_YC0 = 2426;
+constexpr int EBI_OFF_YCP = 2575;
+constexpr int EBI_OFF_PROD = 2724;
+constexpr int EBI_OFF_LOSS = 2873;
+constexpr int EBI_OFF_PNEG = 3022;
 constexpr double FLOPS_STEP_DAY = 36947.0;
 constexpr double FLOPS_STEP_NIGHT = 34766.0;
 extern __constant__ int c_inew2old[149];
@@ -71,6 +81,19 @@ __device__ void jacdecomp_1_11(double* __restrict__ ws, double gdtinv);
 __device__ void solve_1_0(double* __restrict__ ws, int rhs);
 __device__ void solve_1_1(double* __restrict__ ws, int rhs);
 __device__ void solve_1_2(double* __restrict__ ws, int rhs);
+constexpr int EBI_N_EBISP = 136;
+constexpr double EBI_DELTAT = 2.5;
+constexpr int EBI_NEBITER = 1000;
+constexpr int EBI_NPNEG = 1;
+extern __constant__ int c_ebi_ebisp[136];
+extern __constant__ double c_ebi_rtol[149];
+extern __constant__ int c_ebi_pneg[1];
+__device__ void ebi_hrrates(double* __restrict__ ws);
+__device__ void ebi_hrprodloss(double* __restrict__ ws);
+__device__ void ebi_hrg1(double* __restrict__ ws, double dtc);
+__device__ void ebi_hrg2(double* __restrict__ ws, double dtc);
+__device__ void ebi_hrg3(double* __restrict__ ws, double dtc);
+__device__ void ebi_hrg4(double* __restrict__ ws, double dtc);
 __device__ __forceinline__ void jacdecomp_0(double* __restrict__ ws, double gdtinv)
 {
     jacdecomp_0_0(ws, gdtinv);
@@ -134,6 +157,12 @@ struct Traits {
     static constexpr int OFF_VDIAG = mech_cb6r5_ae7_aq::OFF_VDIAG;
     static constexpr int IARRAY_DAY = mech_cb6r5_ae7_aq::IARRAY_DAY;
     static constexpr int IARRAY_NIGHT = mech_cb6r5_ae7_aq::IARRAY_NIGHT;
+    static constexpr int EBI_OFF_YC = mech_cb6r5_ae7_aq::EBI_OFF_YC;
+    static constexpr int EBI_OFF_YC0 = mech_cb6r5_ae7_aq::EBI_OFF_YC0;
+    static constexpr int EBI_OFF_YCP = mech_cb6r5_ae7_aq::EBI_OFF_YCP;
+    static constexpr int EBI_OFF_PROD = mech_cb6r5_ae7_aq::EBI_OFF_PROD;
+    static constexpr int EBI_OFF_LOSS = mech_cb6r5_ae7_aq::EBI_OFF_LOSS;
+    static constexpr int EBI_OFF_PNEG = mech_cb6r5_ae7_aq::EBI_OFF_PNEG;
     static constexpr const char* name() { return mech_cb6r5_ae7_aq::NAME; }
     static __device__ __forceinline__ int iold2new(int s) { return mech_cb6r5_ae7_aq::c_iold2new[s]; }
     static __device__ __forceinline__ int inew2old(int i) { return mech_cb6r5_ae7_aq::c_inew2old[i]; }

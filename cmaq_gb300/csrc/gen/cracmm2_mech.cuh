@@ -5,6 +5,10 @@
 #ifndef CHEM_HD
 #define CHEM_HD __device__
 #endif
+// load of an LU factor or 1/U(i,i); a build may define it as a streaming load (__ldcs)
+#ifndef CHEM_LDLU
+#define CHEM_LDLU(p) (*(p))
+#endif
 namespace mech_cracmm2 {
 constexpr const char* NAME = "cracmm2";
 constexpr int NSPEC = 189;
@@ -26,6 +30,12 @@ constexpr int OFF_LU = 3295;
 constexpr int OFF_VDIAG = 6580;
 constexpr int IARRAY_DAY = 3284;
 constexpr int IARRAY_NIGHT = 3199;
+constexpr int EBI_OFF_YC = 3295;
+constexpr int EBI_OFF_YC0 = 3484;
+constexpr int EBI_OFF_YCP = 3673;
+constexpr int EBI_OFF_PROD = 3862;
+constexpr int EBI_OFF_LOSS = 4051;
+constexpr int EBI_OFF_PNEG = 4240;
 constexpr double FLOPS_STEP_DAY = 79988.0;
 constexpr double FLOPS_STEP_NIGHT = 77148.0;
 extern __constant__ int c_inew2old[189];
@@ -104,6 +114,19 @@ __device__ void solve_1_1(double* __restrict__ ws, int rhs);
 __device__ void solve_1_2(double* __restrict__ ws, int rhs);
 __device__ void solve_1_3(double* __restrict__ ws, int rhs);
 __device__ void solve_1_4(double* __restrict__ ws, int rhs);
+constexpr int EBI_N_EBISP = 176;
+constexpr double EBI_DELTAT = 2.5;
+constexpr int EBI_NEBITER = 1000;
+constexpr int EBI_NPNEG = 0;
+extern __constant__ int c_ebi_ebisp[176];
+extern __constant__ double c_ebi_rtol[189];
+extern __constant__ int c_ebi_pneg[1];
+__device__ void ebi_hrrates(double* __restrict__ ws);
+__device__ void ebi_hrprodloss(double* __restrict__ ws);
+__device__ void ebi_hrg1(double* __restrict__ ws, double dtc);
+__device__ void ebi_hrg2(double* __restrict__ ws, double dtc);
+__device__ void ebi_hrg3(double* __restrict__ ws, double dtc);
+__device__ void ebi_hrg4(double* __restrict__ ws, double dtc);
 __device__ __forceinline__ void jacdecomp_0(double* __restrict__ ws, double gdtinv)
 {
     jacdecomp_0_0(ws, gdtinv);
@@ -200,6 +223,12 @@ struct Traits {
     static constexpr int OFF_VDIAG = mech_cracmm2::OFF_VDIAG;
     static constexpr int IARRAY_DAY = mech_cracmm2::IARRAY_DAY;
     static constexpr int IARRAY_NIGHT = mech_cracmm2::IARRAY_NIGHT;
+    static constexpr int EBI_OFF_YC = mech_cracmm2::EBI_OFF_YC;
+    static constexpr int EBI_OFF_YC0 = mech_cracmm2::EBI_OFF_YC0;
+    static constexpr int EBI_OFF_YCP = mech_cracmm2::EBI_OFF_YCP;
+    static constexpr int EBI_OFF_PROD = mech_cracmm2::EBI_OFF_PROD;
+    static constexpr int EBI_OFF_LOSS = mech_cracmm2::EBI_OFF_LOSS;
+    static constexpr int EBI_OFF_PNEG = mech_cracmm2::EBI_OFF_PNEG;
     static constexpr const char* name() { return mech_cracmm2::NAME; }
     static __device__ __forceinline__ int iold2new(int s) { return mech_cracmm2::c_iold2new[s]; }
     static __device__ __forceinline__ int inew2old(int i) { return mech_cracmm2::c_inew2old[i]; }

@@ -16,7 +16,8 @@ struct MechOps {
     const int* inew2old;      // [nspec]
     const int* iold2new;      // [nspec]
     cudaError_t (*chem_static)(const chem::GridArgs&, int nblocks, cudaStream_t);
-    cudaError_t (*chem_queue)(const chem::GridArgs&, const chem::QueueArgs&, int nblocks, cudaStream_t);
+    cudaError_t (*chem_queue)(const chem::GridArgs&, const chem::QueueArgs&, bool lockstep, int nblocks,
+                              cudaStream_t);
     cudaError_t (*solve)(const chem::SolveArgs&, int nblocks, cudaStream_t);
     cudaError_t (*rconst)(const chem::GridArgs&, double* rki, uint8_t* sunlit, int nblocks, cudaStream_t);
     cudaError_t (*occupancy)(int* blocks_per_sm);
@@ -30,9 +31,13 @@ struct MechOps {
         chem::k_chem_ros3<T_><<<nb, chem::THREADS_PER_BLOCK, 0, s>>>(a);                            \
         return cudaGetLastError();                                                                  \
     }                                                                                               \
-    cudaError_t chem_queue_(const chem::GridArgs& a, const chem::QueueArgs& q, int nb, cudaStream_t s) \
+    cudaError_t chem_queue_(const chem::GridArgs& a, const chem::QueueArgs& q, bool lockstep, int nb,   \
+                            cudaStream_t s)                                                         \
     {                                                                                               \
-        chem::k_chem_ros3_queue<T_><<<nb, chem::THREADS_PER_BLOCK, 0, s>>>(a, q);                   \
+        if (lockstep)                                                                               \
+            chem::k_chem_ros3_queue<T_, true><<<nb, chem::THREADS_PER_BLOCK, 0, s>>>(a, q);         \
+        else                                                                                        \
+            chem::k_chem_ros3_queue<T_, false><<<nb, chem::THREADS_PER_BLOCK, 0, s>>>(a, q);        \
         return cudaGetLastError();                                                                  \
     }                                                                                               \
     cudaError_t solve_(const chem::SolveArgs& a, int nb, cudaStream_t s)                            \
@@ -52,7 +57,7 @@ struct MechOps {
             &a, chem::k_chem_ros3<T_>, chem::THREADS_PER_BLOCK, 0);                                 \
         if (e != cudaSuccess) return e;                                                             \
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(                                          \
-            &b, chem::k_chem_ros3_queue<T_>, chem::THREADS_PER_BLOCK, 0);                           \
+            &b, chem::k_chem_ros3_queue<T_, false>, chem::THREADS_PER_BLOCK, 0);                    \
         *bps = a < b ? a : b;                                                                       \
         return e;                                                                                   \
     }                                                                                               \

@@ -22,7 +22,9 @@ struct QueueArgs {
     unsigned long long* head;         // next queue position (zeroed before the launch)
 };
 
-template <class M>
+// LOCKSTEP: the block's warps run each step attempt together, with barriers between its
+// phases (the block leaves the loop only when none of its warps holds a cell).
+template <class M, bool LOCKSTEP>
 __global__ void __launch_bounds__(THREADS_PER_BLOCK, 1) k_chem_ros3_queue(GridArgs a, QueueArgs q)
 {
     const int lane = threadIdx.x & 31;
@@ -54,10 +56,16 @@ __global__ void __launch_bounds__(THREADS_PER_BLOCK, 1) k_chem_ros3_queue(GridAr
             }
         }
         const bool busy = cell >= 0;
-        if (!__any_sync(0xffffffffu, busy)) break;
-        const bool night = __all_sync(0xffffffffu, !busy || !sun);
+        bool night;
+        if (LOCKSTEP) {
+            if (!__syncthreads_or(busy)) break;
+            night = __syncthreads_and(!busy || !sun) && a.use_night;
+        } else {
+            if (!__any_sync(0xffffffffu, busy)) break;
+            night = __all_sync(0xffffffffu, !busy || !sun) && a.use_night;
+        }
+        ros3::attempt_phased<M, LOCKSTEP>(ws, s, a.chemstep, a.tol, night, a.max_iter, busy);
         if (busy) {
-            ros3::attempt<M>(ws, s, a.chemstep, a.tol, night, a.max_iter);
             if (ros3::finished(s, a.chemstep)) {
                 scatter_cell<M>(a, cell, ws);
                 acc_steps += s.st.nsteps;

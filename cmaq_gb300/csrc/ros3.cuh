@@ -78,48 +78,65 @@ __device__ __forceinline__ bool finished(const CellState& s, double chemstep)
 // estimate, accept or reject, new step size.  Requires Y and RKI in ws.  `night` must be
 // warp-uniform: it selects the night reaction list and LU pattern, which give the same
 // numbers as the day pattern for a dark cell (the dropped reactions have zero rates)
-// with fewer operations.
-template <class M>
-__device__ void attempt(double* __restrict__ ws, CellState& s, double chemstep, Tol tol, bool night,
-                        int max_iter)
+// with fewer operations.  Every thread of the warp (of the block when SYNC) calls this;
+// lanes with active == false do no work.  With SYNC the block's warps pass a barrier
+// between phases, so they walk the (large) generated code together and share the
+// instruction cache.
+template <class M, bool SYNC>
+__device__ void attempt_phased(double* __restrict__ ws, CellState& s, double chemstep, Tol tol, bool night,
+                               int max_iter, bool active)
 {
-    if (s.iter >= max_iter) { s.st.status |= ST_MAXITER; return; }
-    s.iter++;
-    // f(Y) is unchanged after a rejected step; it is kept in F0
-    if (!s.have_f0) {
-        if (night) M::feval_1(ws, M::OFF_Y, M::OFF_F0); else M::feval_0(ws, M::OFF_Y, M::OFF_F0);
-        s.have_f0 = true;
+    bool go = active;
+    if (go && s.iter >= max_iter) { s.st.status |= ST_MAXITER; go = false; }
+    double dt = 0.0, tend = 0.0, dtinv = 0.0, gdtinv = 0.0;
+    if (go) {
+        s.iter++;
+        // f(Y) is unchanged after a rejected step; it is kept in F0
+        if (!s.have_f0) {
+            if (night) M::feval_1(ws, M::OFF_Y, M::OFF_F0); else M::feval_0(ws, M::OFF_Y, M::OFF_F0);
+            s.have_f0 = true;
+        }
+        dt = s.dt;
+        tend = s.tnow + dt;
+        if (tend > chemstep) { dt = chemstep - s.tnow; tend = chemstep; }
+        dtinv = 1.0 / dt;
+        gdtinv = dtinv * RGAM;
+        if (night) M::explic_1(ws); else M::explic_0(ws);
     }
-    double dt = s.dt;
-    double tend = s.tnow + dt;
-    if (tend > chemstep) { dt = chemstep - s.tnow; tend = chemstep; }
-    const double dtinv = 1.0 / dt;
-    const double gdtinv = dtinv * RGAM;
-    if (night) { M::explic_1(ws); M::jacdecomp_1(ws, gdtinv); }
-    else       { M::explic_0(ws); M::jacdecomp_0(ws, gdtinv); }
-    // stage 1
-    for (int n = 0; n < M::NSPEC; ++n) ws[(M::OFF_K1 + n) * 32] = -ws[(M::OFF_F0 + n) * 32];
-    if (night) M::solve_1(ws, M::OFF_K1); else M::solve_0(ws, M::OFF_K1);
-    // stage 2
-    for (int n = 0; n < M::NSPEC; ++n)
-        ws[(M::OFF_YP + n) * 32] = ws[(M::OFF_Y + n) * 32] + ws[(M::OFF_K1 + n) * 32];
-    if (night) M::feval_1(ws, M::OFF_YP, M::OFF_YDOT); else M::feval_0(ws, M::OFF_YP, M::OFF_YDOT);
-    {
+    if (SYNC) __syncthreads();
+    if (go) {
+        if (night) M::jacdecomp_1(ws, gdtinv); else M::jacdecomp_0(ws, gdtinv);
+    }
+    if (SYNC) __syncthreads();
+    if (go) {   // stage 1
+        for (int n = 0; n < M::NSPEC; ++n) ws[(M::OFF_K1 + n) * 32] = -ws[(M::OFF_F0 + n) * 32];
+        if (night) M::solve_1(ws, M::OFF_K1); else M::solve_0(ws, M::OFF_K1);
+    }
+    if (SYNC) __syncthreads();
+    if (go) {   // stage 2
+        for (int n = 0; n < M::NSPEC; ++n)
+            ws[(M::OFF_YP + n) * 32] = ws[(M::OFF_Y + n) * 32] + ws[(M::OFF_K1 + n) * 32];
+        if (night) M::feval_1(ws, M::OFF_YP, M::OFF_YDOT); else M::feval_0(ws, M::OFF_YP, M::OFF_YDOT);
         const double x1 = C21 * dtinv;
         for (int n = 0; n < M::NSPEC; ++n)
             ws[(M::OFF_K2 + n) * 32] = fma(-x1, ws[(M::OFF_K1 + n) * 32], -ws[(M::OFF_YDOT + n) * 32]);
     }
-    if (night) M::solve_1(ws, M::OFF_K2); else M::solve_0(ws, M::OFF_K2);
-    // stage 3
-    {
+    if (SYNC) __syncthreads();
+    if (go) {
+        if (night) M::solve_1(ws, M::OFF_K2); else M::solve_0(ws, M::OFF_K2);
+    }
+    if (SYNC) __syncthreads();
+    if (go) {   // stage 3
         const double x1 = C31 * dtinv;
         const double x2 = C32 * dtinv;
         for (int n = 0; n < M::NSPEC; ++n) {
             const double t = fma(-x1, ws[(M::OFF_K1 + n) * 32], -ws[(M::OFF_YDOT + n) * 32]);
             ws[(M::OFF_K3 + n) * 32] = fma(-x2, ws[(M::OFF_K2 + n) * 32], t);
         }
+        if (night) M::solve_1(ws, M::OFF_K3); else M::solve_0(ws, M::OFF_K3);
     }
-    if (night) M::solve_1(ws, M::OFF_K3); else M::solve_0(ws, M::OFF_K3);
+    if (SYNC) __syncthreads();
+    if (!go) return;
     // solution and error estimate
     double err = 0.0;
     bool finite = true;
@@ -158,6 +175,13 @@ __device__ void attempt(double* __restrict__ ws, CellState& s, double chemstep, 
         s.lpass = false;
         if (s.dt < DTMIN) s.st.status |= ST_DT_UNDERFLOW;
     }
+}
+
+template <class M>
+__device__ __forceinline__ void attempt(double* __restrict__ ws, CellState& s, double chemstep, Tol tol,
+                                        bool night, int max_iter)
+{
+    attempt_phased<M, false>(ws, s, chemstep, tol, night, max_iter, true);
 }
 
 // Integrate the cell in ws over chemstep minutes (the whole DO WHILE loop).

@@ -50,7 +50,10 @@ class Layout:
                     self.ex[(r, ial)] = off
                     off += 1
         self.lu = off; off += max(sp.iarray) + 1      # 1-based storage, slot 0 unused
+        # EBI species arrays overlay the LU region (the two solvers never share a cell state)
+        self.ebi_yc = self.lu
         self.vdiag = off; off += sp.ischan
+        off = max(off, self.ebi_yc + 6 * ns)
         self.total = off
 
 
@@ -58,7 +61,8 @@ def _w(k: int) -> str:
     return f"ws[{k * 32}]"
 
 
-def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src_hash: str) -> dict[str, str]:
+def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src_hash: str,
+                 ebi_decl: str = "") -> dict[str, str]:
     """Return {file name: text}: one header with declarations and the kernel traits,
     and several translation units of device functions that compile in parallel
     (relocatable device code)."""
@@ -98,12 +102,19 @@ def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src
         wrappers.append("}")
 
     h = banner + ["#pragma once", "#include <cuda_runtime.h>", "#ifndef CHEM_HD", "#define CHEM_HD __device__",
-                  "#endif", f"namespace {ns_name} {{", f'constexpr const char* NAME = "{mech}";']
+                  "#endif",
+                  "// load of an LU factor or 1/U(i,i); a build may define it as a streaming load (__ldcs)",
+                  "#ifndef CHEM_LDLU", "#define CHEM_LDLU(p) (*(p))", "#endif",
+                  f"namespace {ns_name} {{", f'constexpr const char* NAME = "{mech}";']
     consts = (("NSPEC", ns), ("NRXNS", nr), ("ISCHAN", n), ("NPHOTAB", m.nphotab),
               ("NHETERO", m.nhetero), ("WS_ELEMS", lay.total), ("OFF_Y", lay.y), ("OFF_YP", lay.yp),
               ("OFF_YDOT", lay.ydot), ("OFF_F0", lay.f0), ("OFF_K1", lay.k1), ("OFF_K2", lay.k2),
               ("OFF_K3", lay.k3), ("OFF_RKI", lay.rki), ("OFF_RXRAT", lay.rxrat), ("OFF_LU", lay.lu),
-              ("OFF_VDIAG", lay.vdiag), ("IARRAY_DAY", sp.iarray[0]), ("IARRAY_NIGHT", sp.iarray[1]))
+              ("OFF_VDIAG", lay.vdiag), ("IARRAY_DAY", sp.iarray[0]), ("IARRAY_NIGHT", sp.iarray[1]),
+              # EBI cell state reuses the workspace: YC, YC0, YCP, PROD, LOSS, PNEG after RKI/RXRAT
+              ("EBI_OFF_YC", lay.ebi_yc), ("EBI_OFF_YC0", lay.ebi_yc + ns), ("EBI_OFF_YCP", lay.ebi_yc + 2 * ns),
+              ("EBI_OFF_PROD", lay.ebi_yc + 3 * ns), ("EBI_OFF_LOSS", lay.ebi_yc + 4 * ns),
+              ("EBI_OFF_PNEG", lay.ebi_yc + 5 * ns))
     for k, v in consts:
         h.append(f"constexpr int {k} = {v};")
     h.append(f"constexpr double FLOPS_STEP_DAY = {float(flop_counts(m, sp, 0)['step_total'])};")
@@ -116,6 +127,8 @@ def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src
     h.append(f"static const int h_convert[{ns}] = {{{', '.join('1' if c else '0' for c in m.convert_conc)}}};")
     h.append(f"static const double h_molwt[{ns}] = {{{', '.join(c_double(x) for x in m.molwt)}}};")
     h.extend(decls)
+    if ebi_decl:
+        h.append(ebi_decl)
     h.extend(wrappers)
     h.append("struct Traits {")
     for k, _ in consts:
@@ -286,10 +299,10 @@ def _jacdecomp_chunks(m: Mechanism, sp: SparseMech, lay: Layout, d: int) -> list
                     o.append(f"      {var} = fma({c_double(coef)}, {ex}, {var});")
         o.append(f"      a{i} = a{i} - gdtinv;")
         for (st_ik, k) in lower:
-            o.append(f"      a{k} = a{k} * vd[{k * 32}];")
+            o.append(f"      a{k} = a{k} * CHEM_LDLU(vd + {k * 32});")
             o.append(f"      lu[{st_ik * 32}] = a{k};")
             for (st_kj, j) in sp.upper[d][k]:
-                o.append(f"      a{j} = fma(-a{k}, lu[{st_kj * 32}], a{j});")
+                o.append(f"      a{j} = fma(-a{k}, CHEM_LDLU(lu + {st_kj * 32}), a{j});")
                 nops += 1
         for (st_ij, j) in upper:
             o.append(f"      lu[{st_ij * 32}] = a{j};")
@@ -327,15 +340,15 @@ def _solve_chunks(sp: SparseMech, lay: Layout, d: int) -> list[list[str]]:
     for i in range(n):
         o = ["    {", f"      double x = b[{i * 32}];"]
         for (st, j) in sp.lower[d][i]:
-            o.append(f"      x = fma(-lu[{st * 32}], b[{j * 32}], x);")
+            o.append(f"      x = fma(-CHEM_LDLU(lu + {st * 32}), b[{j * 32}], x);")
         o.append(f"      b[{i * 32}] = x;")
         o.append("    }")
         pieces.append((len(sp.lower[d][i]) + 1, o))
     for i in range(n - 1, -1, -1):
         o = ["    {", f"      double x = b[{i * 32}];"]
         for (st, j) in sp.upper[d][i]:
-            o.append(f"      x = fma(-lu[{st * 32}], b[{j * 32}], x);")
-        o.append(f"      b[{i * 32}] = x * vd[{i * 32}];")
+            o.append(f"      x = fma(-CHEM_LDLU(lu + {st * 32}), b[{j * 32}], x);")
+        o.append(f"      b[{i * 32}] = x * CHEM_LDLU(vd + {i * 32});")
         o.append("    }")
         pieces.append((len(sp.upper[d][i]) + 1, o))
     chunks, cur, cost = [], [], 0

@@ -248,6 +248,57 @@ def oracle_source(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, sr
     return "\n".join(L) + "\n"
 
 
+def ebi_oracle_source(ebi: dict, mech: str, nspec: int) -> str:
+    from .ebi_translate import c_routines
+    L = [f"/* Generated by cmaq_gb300.mechgen.generate from CCTM/src/gas/ebi_{mech}/hr*.F.  Do not edit.",
+         " * EBI species list and tolerances (hrinit.F) and the translated straight-line routines",
+         " * HRRATES, HRPRODLOSS, HRG1-HRG4; species indices 0-based in mechanism order. */",
+         f"#define EBI_N_EBISP {len(ebi['ebisp'])}",
+         f"#define EBI_DELTAT {c_double(ebi['deltat'])}",
+         f"#define EBI_NEBITER {ebi['nebiter']}",
+         f"#define EBI_NPNEG {len(ebi['pneg_species'])}",
+         _arr("int", "ebi_ebisp", ebi["ebisp"]),
+         _arr("double", "ebi_rtol", [c_double(ebi["rtol"][i]) for i in range(nspec)]),
+         _arr("int", "ebi_pneg_species", ebi["pneg_species"] or [-1]),
+         c_routines(ebi, "static")]
+    return "\n".join(L)
+
+
+def ebi_cuda_source(ebi: dict, mech: str, nspec: int) -> tuple[str, str]:
+    """(declarations for the mechanism header, translation unit of device routines)."""
+    from .ebi_translate import c_routines
+    ns_name = f"mech_{mech}"
+    decl = [f"constexpr int EBI_N_EBISP = {len(ebi['ebisp'])};",
+            f"constexpr double EBI_DELTAT = {c_double(ebi['deltat'])};",
+            f"constexpr int EBI_NEBITER = {ebi['nebiter']};",
+            f"constexpr int EBI_NPNEG = {len(ebi['pneg_species'])};",
+            f"extern __constant__ int c_ebi_ebisp[{len(ebi['ebisp'])}];",
+            f"extern __constant__ double c_ebi_rtol[{nspec}];",
+            f"extern __constant__ int c_ebi_pneg[{max(1, len(ebi['pneg_species']))}];"]
+    for name in ebi["routines"]:
+        args = ", double dtc" if name.startswith("hrg") else ""
+        decl.append(f"__device__ void ebi_{name}(double* __restrict__ ws{args});")
+    tu = [f"// Generated by cmaq_gb300.mechgen.generate from CCTM/src/gas/ebi_{mech}/hr*.F.  Do not edit.",
+          "// Translated EBI routines HRRATES, HRPRODLOSS, HRG1-HRG4 on the per-cell workspace.",
+          f'#include "{mech}_mech.cuh"', "#include <math.h>", f"namespace {ns_name} {{",
+          f"__constant__ int c_ebi_ebisp[{len(ebi['ebisp'])}] = {{{', '.join(map(str, ebi['ebisp']))}}};",
+          f"__constant__ double c_ebi_rtol[{nspec}] = {{{', '.join(c_double(ebi['rtol'][i]) for i in range(nspec))}}};",
+          f"__constant__ int c_ebi_pneg[{max(1, len(ebi['pneg_species']))}] = "
+          f"{{{', '.join(map(str, ebi['pneg_species'] or [-1]))}}};",
+          "#define EBI_CELL_ARGS double* __restrict__ ws",
+          "#define EBI_YC(i) ws[(EBI_OFF_YC + (i)) * 32]",
+          "#define EBI_YC0(i) ws[(EBI_OFF_YC0 + (i)) * 32]",
+          "#define EBI_YCP(i) ws[(EBI_OFF_YCP + (i)) * 32]",
+          "#define EBI_RKI(r) ws[(OFF_RKI + (r)) * 32]",
+          "#define EBI_RXRAT(r) ws[(OFF_RXRAT + (r)) * 32]",
+          "#define EBI_PROD(i) ws[(EBI_OFF_PROD + (i)) * 32]",
+          "#define EBI_LOSS(i) ws[(EBI_OFF_LOSS + (i)) * 32]",
+          "#define EBI_PNEG(i) ws[(EBI_OFF_PNEG + (i)) * 32]",
+          c_routines(ebi, "__device__ __noinline__"),
+          f"}}  // namespace {ns_name}"]
+    return "\n".join(decl), "\n".join(tu) + "\n"
+
+
 def write_outputs(cmaq_root: str, mech: str, out_root: Path = REPO) -> dict:
     m, prog, sp, src_hash = load(cmaq_root, mech)
     man = manifest(m, prog, sp, mech, src_hash)
@@ -258,13 +309,18 @@ def write_outputs(cmaq_root: str, mech: str, out_root: Path = REPO) -> dict:
     odir = REPO_ / "oracle" / "gen"
     odir.mkdir(parents=True, exist_ok=True)
     (odir / f"{mech}_mech.c").write_text(oracle_source(m, prog, sp, mech, src_hash))
+    from .ebi_translate import parse_ebi
+    ebi = parse_ebi(Path(cmaq_root) / "CCTM" / "src" / "gas" / f"ebi_{mech}")
+    (odir / f"{mech}_ebi.c").write_text(ebi_oracle_source(ebi, mech, m.nspec))
     from .emit_cuda import cuda_sources
     cdir = REPO_ / "cmaq_gb300" / "csrc" / "gen"
     cdir.mkdir(parents=True, exist_ok=True)
     for old in cdir.glob(f"{mech}_*"):
         old.unlink()
-    for fname, text in cuda_sources(m, prog, sp, mech, src_hash).items():
+    ebi_decl, ebi_tu = ebi_cuda_source(ebi, mech, m.nspec)
+    for fname, text in cuda_sources(m, prog, sp, mech, src_hash, ebi_decl).items():
         (cdir / fname).write_text(text)
+    (cdir / f"{mech}_ebi.cu").write_text(ebi_tu)
     return man
 
 

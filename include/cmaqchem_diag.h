@@ -13,6 +13,13 @@ extern "C" {
  * on every SM: TFLOP/s (an FMA counts 2) and the kernel time in ms. */
 int cmaqchem_diag_fp64_peak(int device, double* tflops, double* ms);
 
+/* Scheduling knobs of a handle, for the autotuner: "night_pattern" (1: warps whose cells are
+ * all dark use the smaller night LU pattern; 0: the day pattern always, same numbers) and
+ * "lockstep" (1: the work-queue kernel runs each block's warps through a step attempt
+ * together, with barriers between its phases). */
+struct cmaqchem_handle;
+int cmaqchem_diag_set_tuning(struct cmaqchem_handle* h, const char* key, int value);
+
 #ifdef __cplusplus
 }
 #endif

@@ -29,16 +29,19 @@ def build(mechs=MECHS, force: bool = False) -> list[Path]:
     out_dir = HERE / "_build"
     out_dir.mkdir(exist_ok=True)
     src = HERE / "ros3_oracle.c"
+    src_ebi = HERE / "ebi_oracle.c"
     procs, outs = [], []
     for mech in mechs:
         gen = HERE / "gen" / f"{mech}_mech.c"
+        gen_ebi = HERE / "gen" / f"{mech}_ebi.c"
         out = lib_path(mech)
         outs.append(out)
-        if (not force and out.exists() and out.stat().st_mtime > max(src.stat().st_mtime, gen.stat().st_mtime)):
+        newest = max(p.stat().st_mtime for p in (src, src_ebi, gen, gen_ebi, HERE / "oracle.h"))
+        if not force and out.exists() and out.stat().st_mtime > newest:
             continue
         cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
-               "-fno-fast-math", f'-DMECH_SOURCE="gen/{mech}_mech.c"', "-I", str(HERE),
-               str(src), "-o", str(out) + ".tmp", "-lm"]
+               "-fno-fast-math", f'-DMECH_SOURCE="gen/{mech}_mech.c"', f'-DEBI_SOURCE="gen/{mech}_ebi.c"',
+               "-Wno-unused-function", "-I", str(HERE), str(src), str(src_ebi), "-o", str(out) + ".tmp", "-lm"]
         procs.append((subprocess.Popen(cmd, cwd=HERE), out))
     for p, out in procs:
         if p.wait() != 0:

@@ -53,6 +53,8 @@ def load(mech: str = "cb6r5_ae7_aq") -> C.CDLL:
                                           ip, ip, ip, C.c_int]
     lib.oracle_chem.argtypes = [C.POINTER(OracleChemArgs)]
     lib.oracle_mech_name.restype = C.c_char_p
+    lib.oracle_chem_ebi.argtypes = [C.POINTER(OracleChemArgs)]
+    lib.oracle_ebi_solve_cells.argtypes = [C.c_long, C.c_int, dp, dp, ip, C.POINTER(C.c_long), C.c_int]
     lib.oracle_set_dtmin.argtypes = [C.c_double]
     lib.oracle_get_dtmin.restype = C.c_double
     return lib
@@ -143,6 +145,32 @@ class Oracle:
         del keep
         return conc, {"rc": rc, "nsteps": a.nsteps_total, "nfails": a.nfails_total,
                       "nfailed_blocks": a.nfailed_blocks}
+
+    def chem_ebi(self, g, tstep_sec: int = 300, max_iter: int = 10000000, threads: int = 0, conc=None):
+        """One EBI CHEM call (hrdriver.F / hrsolver.F) on a GridInputs-like object."""
+        conc = np.array(g.conc if conc is None else conc, dtype=np.float32, order="C", copy=True)
+        man_cgi = np.ascontiguousarray(g.cgrid_index - 1, np.int32)
+        convert = np.ascontiguousarray(self.convert_flags(g.mech), np.int32)
+        keep = [conc, man_cgi, convert]
+        a = OracleChemArgs(g.ncols, g.nrows, g.nlays, g.nspcsd, _p(conc, C.c_float), _p(man_cgi, C.c_int),
+                           _p(convert, C.c_int), _p(g.ta, C.c_float), _p(g.qv, C.c_float), _p(g.dens, C.c_float),
+                           _p(g.pres, C.c_float), _p(g.seaice, C.c_float), _p(g.ocean_szone, C.c_float),
+                           _p(g.rj, C.c_float), _p(g.khetero, C.c_double), tstep_sec, 0.0, 0.0, 1, 0, max_iter,
+                           threads, 0, 0, 0)
+        rc = self.lib.oracle_chem_ebi(C.byref(a))
+        del keep
+        return conc, {"rc": rc, "iterations": a.nsteps_total, "nfailed": a.nfailed_blocks}
+
+    def ebi_solve_cells(self, yc, rki, tstep_sec: int = 300, threads: int = 0):
+        """EBI (HRSOLVER) for cells with given yc [nspec, n] (mechanism order) and rki [nrxns, n]."""
+        yc = np.array(yc, dtype=np.float64, order="C", copy=True)
+        rki = np.ascontiguousarray(rki, np.float64)
+        n = yc.shape[1]
+        st = np.zeros(n, np.int32)
+        it = np.zeros(n, np.int64)
+        self.lib.oracle_ebi_solve_cells(n, tstep_sec, _p(yc, C.c_double), _p(rki, C.c_double), _p(st, C.c_int),
+                                        it.ctypes.data_as(C.POINTER(C.c_long)), threads)
+        return yc, st, it
 
     @staticmethod
     def convert_flags(mech: str) -> np.ndarray:

@@ -37,6 +37,7 @@
 #error "compile with -DMECH_SOURCE=\"gen/<mech>_mech.c\""
 #endif
 #include MECH_SOURCE
+#include "oracle.h"
 
 /* ROS3 method constants (rbsolver.F:85-113; KPP ROS3, Sandu et al. 1997) */
 static const double GAM = 0.43586652150845899941601945119356;
@@ -57,10 +58,6 @@ static const double DTSTART = 0.5e-01, DTMAX = 1.0e+01, UROUND = 1.0e-18;
 static double DTMIN = 1.0e-08;
 static const double FACMAX = 1.0e+01, FACMIN = 1.0e-01, FACONE = 1.0e+00, CONMIN = 1.0e-30;
 
-/* per-cell status bits (shared meaning with the device code) */
-#define ST_DT_UNDERFLOW 1
-#define ST_MAXITER 2
-#define ST_NONFINITE 4
 
 typedef struct {
     int ncells;          /* NUMCELLS */
@@ -440,25 +437,7 @@ int oracle_rbsolver_cells(long ncell, double chemstep, double rtol, double atol,
 
 /* ------------------------------------------------------------------ CHEM driver */
 
-typedef struct {
-    int ncols, nrows, nlays, nspcsd;
-    float* conc;                 /* CONC(ncols, nrows, nlays, nspcsd) Fortran order */
-    const int* cgrid_index;      /* [nspec] 0-based */
-    const int* convert;          /* [nspec] */
-    const float* ta, *qv, *dens, *pres;      /* (ncols, nrows, nlays) */
-    const float* seaice, *ocean_szone;       /* (ncols, nrows) */
-    const float* rj;             /* (ncols, nrows, nlays, nphotab) */
-    const double* khetero;       /* (nhet, ncols, nrows, nlays) */
-    int tstep_sec;               /* TIME2SEC(TSTEP(2)) */
-    double rtol, atol;           /* REAL(GLBL_RTOL, 8), REAL(GLBL_ATOL, 8) */
-    int blksize;                 /* BLKSIZE (50 in the reference) */
-    int lreorder;                /* LREORDER */
-    int max_iter;
-    int threads;
-    /* outputs */
-    long long nsteps_total, nfails_total;
-    int nfailed_blocks;
-} OracleChemArgs;
+/* OracleChemArgs: oracle.h */
 
 /* Per-block gather (rbdriver.F:460-511), CALC_RCONST and day/night choice (:513-519). */
 static int gather_block(const OracleChemArgs* a, const int* ccol, const int* crow, const int* clev,
