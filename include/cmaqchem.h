@@ -126,6 +126,26 @@ int cmaqchem_mech_info_get(const char* mechanism, cmaqchem_mech_info* info, int*
 
 void cmaqchem_destroy(cmaqchem_handle* h);
 
+/* Allocation-free variant of cmaqchem_ros3_solve_device.  It has no counterpart in the
+ * reference.  It is for callers that cannot allocate device memory where they call the
+ * chemistry: host models that own the whole device footprint through their own memory
+ * pool, callers under a fixed device-memory budget, and loops that cannot accept the
+ * device-wide synchronisation of cudaMalloc / cudaFree.  No handle is needed and the
+ * call allocates nothing: the solver's workspace is a file-scope device array of
+ * CMAQCHEM_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until exit;
+ * the caller passes the device arrays y, rki, night and (optionally) status exactly as
+ * for cmaqchem_ros3_solve_device.  The first call on a device, with that device current,
+ * looks up the array's device address; make that first call before any stream capture.
+ * All calls share the array: calls whose kernels overlap on the GPU race and must be
+ * serialised by the caller.  ncell above CMAQCHEM_NOALLOC_MAX_CELLS is rejected, as is a
+ * mechanism whose per-block workspace does not fit the array.  Runs on the current
+ * device, returns 0 or -1 (text from cmaqchem_last_error). */
+#define CMAQCHEM_NOALLOC_SCRATCH_BYTES (64ull << 20)
+#define CMAQCHEM_NOALLOC_MAX_CELLS (1ll << 31)
+int cmaqchem_ros3_solve_noalloc(const char* mechanism, long long ncell, double* y, const double* rki,
+                                const unsigned char* night, double chemstep_min, double rtol,
+                                double atol, int* status, void* stream);
+
 /* Text of the last error of the calling thread; returns its length. */
 int cmaqchem_last_error(char* buf, size_t len);
 
