@@ -56,6 +56,11 @@ def lib(variant: str = "r255") -> C.CDLL:
                                        C.POINTER(Stats)]
     L.cmaqchem_cell_stats.argtypes = [vp, vp, vp]
     L.cmaqchem_ros3_solve_device.argtypes = [vp, C.c_longlong, vp, vp, vp, C.c_double, vp, vp, vp, vp]
+    L.cmaqchem_ebi_solve_device.argtypes = [vp, C.c_longlong, vp, vp, C.c_int, vp, vp, vp]
+    L.cmaqchem_adj_forward.argtypes = [vp, C.c_longlong, vp, vp, C.c_longlong, vp, vp, vp, C.c_int, C.c_double,
+                                       vp, vp, vp]
+    L.cmaqchem_adj_backward.argtypes = [vp, C.c_longlong, vp, vp, C.c_longlong, vp, vp, vp, C.c_int, C.c_double,
+                                        vp, vp, vp, vp, vp]
     L.cmaqchem_rconst_device.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     L.cmaqchem_mech_info_get.argtypes = [C.c_char_p, C.POINTER(MechInfo), ip]
     L.cmaqchem_destroy.argtypes = [vp]

@@ -26,6 +26,7 @@ import numpy as np
 from . import _lib
 from ._lib import ChemError, check
 
+SOLVERS = {"ros3": _lib.SOLVER_ROS3, "ebi": _lib.SOLVER_EBI}
 SCHEDULES = {"static": _lib.SCHED_STATIC, "plain": _lib.SCHED_STATIC, "queue": _lib.SCHED_QUEUE,
              "batched": _lib.SCHED_QUEUE}
 
@@ -63,7 +64,10 @@ class ChemSolver:
 
     def __init__(self, mechanism: str = "cb6r5_ae7_aq", *, ncols: int, nrows: int, nlays: int, nspcsd: int,
                  cgrid_index=None, rtol: float = 1.0e-3, atol: float = 1.0e-7, schedule: str = "queue",
-                 device: int = 0, max_iter: int = 0, reference_tolerances: bool = True, variant: str = "r255"):
+                 device: int = 0, max_iter: int = 0, reference_tolerances: bool = True, variant: str = "r255",
+                 solver: str = "ros3"):
+        if solver not in SOLVERS:
+            raise ChemError(f"unknown solver {solver!r}; use one of {sorted(SOLVERS)}")
         if schedule not in SCHEDULES:
             raise ChemError(f"unknown schedule {schedule!r}; use one of {sorted(SCHEDULES)}")
         self.mechanism = mechanism
@@ -77,7 +81,8 @@ class ChemSolver:
         self._cgi = None
         if cgrid_index is not None:
             self._cgi = (C.c_int * self.info.nspec)(*[int(v) for v in cgrid_index])
-        cfg = _lib.Cfg(mechanism.encode(), _lib.SOLVER_ROS3, SCHEDULES[schedule], self.rtol, self.atol, ncols, nrows,
+        self.solver = solver
+        cfg = _lib.Cfg(mechanism.encode(), SOLVERS[solver], SCHEDULES[schedule], self.rtol, self.atol, ncols, nrows,
                        nlays, nspcsd, self._cgi, device, max_iter)
         h = C.c_void_p()
         check(self._L.cmaqchem_init(C.byref(cfg), C.byref(h)), self._L)
@@ -85,7 +90,8 @@ class ChemSolver:
         self.schedule = schedule
 
     def set_tuning(self, **knobs) -> None:
-        """Scheduling knobs (see include/cmaqchem_diag.h): night_pattern=0/1, lockstep=0/1."""
+        """Scheduling knobs (see include/cmaqchem_diag.h): night_pattern=0/1, lockstep=0/1/2,
+        block_warps=2/4/8."""
         for k, v in knobs.items():
             check(self._L.cmaqchem_diag_set_tuning(self._h, k.encode(), int(v)), self._L)
 
@@ -168,6 +174,20 @@ class ChemSolver:
         check(self._L.cmaqchem_ros3_solve_device(self._h, n, _ptr(y), _ptr(rki), _ptr(night), chemstep_min,
                                                  _ptr(st), _ptr(ns), _ptr(nf), s), self._L)
         return (st, ns, nf) if with_stats else None
+
+    def ebi_solve(self, yc, rki, tstep_sec: int, with_stats: bool = False, stream=None):
+        """HRSOLVER on CUDA tensors: yc [nspec, n] (mechanism species order, ppm) in place,
+        rki [nrxns, n]; tstep_sec = synchronisation step.  Optional per-cell status and
+        Backward-Euler iteration counts."""
+        import torch
+        n = yc.shape[1]
+        st = it = None
+        if with_stats:
+            st, it = (torch.zeros(n, dtype=torch.int32, device=yc.device) for _ in range(2))
+        s = C.c_void_p(stream.cuda_stream) if stream is not None else None
+        check(self._L.cmaqchem_ebi_solve_device(self._h, n, _ptr(yc), _ptr(rki), int(tstep_sec), _ptr(st),
+                                                _ptr(it), s), self._L)
+        return (st, it) if with_stats else None
 
     def rconst(self, conc, ta, qv, dens, pres, seaice, ocean_szone, rj, khetero):
         """CALC_RCONST for every cell of the grid (CUDA tensors): returns rki [nrxns, ncell], sunlit [ncell]."""

@@ -69,6 +69,8 @@ struct cmaqchem_handle {
     int* d_convert = nullptr;
     float* d_fwd = nullptr;
     double* d_rev = nullptr;
+    float* d_ebi_fwd = nullptr;     // EBI driver's FORWARD_CONV / REVERSE_CONV (hrinit.F:90-93)
+    float* d_ebi_rev = nullptr;
     double* d_ws = nullptr;
     int* d_status = nullptr;
     int* d_steps = nullptr;
@@ -80,13 +82,31 @@ struct cmaqchem_handle {
     bool have_history = false;
     // tuning knobs (cmaqchem_diag_set_tuning)
     int use_night = 1;
-    int lockstep = 0;
+    int q_sync = 1;          // work-queue kernel: barriers between attempt phases
+    int q_wpb = 4;           // work-queue kernel: warps per block
+    int q_nblocks = 0;
+    size_t ws_warps = 0;     // workspace capacity in warps
     // device staging of the host-pointer entry point, allocated on first use
     float *s_conc = nullptr, *s_ta = nullptr, *s_qv = nullptr, *s_dens = nullptr, *s_pres = nullptr;
     float *s_seaice = nullptr, *s_osz = nullptr, *s_rj = nullptr;
     double* s_khet = nullptr;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // discrete adjoint (allocated on first use, grown as needed)
+    int adj_nblocks = 0;
+    double* d_adj_ws = nullptr;
+    double* d_tape_y = nullptr;
+    double* d_tape_h = nullptr;
+    size_t tape_cap = 0;               // entries
+    long long* d_tape_off = nullptr;   // [nsync][ncell]
+    size_t tape_off_cap = 0;
+    long long* d_tiles = nullptr;      // [nsync][ntiles] scan tile bases
+    long long* d_tape_tot = nullptr;   // [nsync]
+    size_t tiles_cap = 0, tot_cap = 0;
+    int* d_adj_order = nullptr;
+    int* d_adj_status = nullptr;
+    size_t adj_cell_cap = 0, adj_status_cap = 0;
+    unsigned long long* d_adj_counters = nullptr;
 };
 
 namespace {
@@ -95,15 +115,37 @@ void free_handle(cmaqchem_handle* h)
 {
     if (!h) return;
     cudaSetDevice(h->device);
-    void* ptrs[] = {h->d_cgrid_index, h->d_convert, h->d_fwd, h->d_rev, h->d_ws, h->d_status, h->d_steps,
+    void* ptrs[] = {h->d_cgrid_index, h->d_convert, h->d_fwd, h->d_rev, h->d_ebi_fwd, h->d_ebi_rev, h->d_ws, h->d_status, h->d_steps,
                     h->d_counters, h->d_order, h->d_hist, h->d_cursor, h->d_head, h->s_conc, h->s_ta,
-                    h->s_qv, h->s_dens, h->s_pres, h->s_seaice, h->s_osz, h->s_rj, h->s_khet};
+                    h->s_qv, h->s_dens, h->s_pres, h->s_seaice, h->s_osz, h->s_rj, h->s_khet,
+                    h->d_adj_ws, h->d_tape_y, h->d_tape_h, h->d_tape_off, h->d_tiles, h->d_tape_tot,
+                    h->d_adj_order, h->d_adj_status, h->d_adj_counters};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
+}
+
+// Grow the per-warp workspaces to `warps` (set-up calls only).
+int ensure_ws(cmaqchem_handle* h, size_t warps)
+{
+    if (warps <= h->ws_warps) return 0;
+    if (h->d_ws) CK(cudaFree(h->d_ws));
+    h->d_ws = nullptr;
+    CK(cudaMalloc(&h->d_ws, warps * (size_t)h->ops->ws_elems * 32 * sizeof(double)));
+    h->ws_warps = warps;
+    return 0;
+}
+
+// Grid of the work-queue kernel for the handle's knobs: one persistent wave.
+int configure_queue(cmaqchem_handle* h)
+{
+    int bps = 0;
+    CK(h->ops->queue_occupancy(h->q_sync, h->q_wpb, &bps));
+    h->q_nblocks = h->nsm * (bps > 0 ? bps : 1);
+    return ensure_ws(h, (size_t)h->q_nblocks * h->q_wpb);
 }
 
 chem::GridArgs grid_args(cmaqchem_handle* h, float* conc, const float* ta, const float* qv, const float* dens,
@@ -181,7 +223,7 @@ extern "C" int cmaqchem_init(const cmaqchem_cfg* cfg, cmaqchem_handle** out)
     *out = nullptr;
     const MechOps* m = find_mech(cfg->mechanism);
     if (!m) return fail(std::string("unknown mechanism ") + (cfg->mechanism ? cfg->mechanism : "(null)"));
-    if (cfg->solver != CMAQCHEM_SOLVER_ROS3) return fail("only the ROS3 solver is available in this build");
+    if (cfg->solver != CMAQCHEM_SOLVER_ROS3 && cfg->solver != CMAQCHEM_SOLVER_EBI) return fail("unknown solver");
     if (cfg->schedule != CMAQCHEM_SCHED_STATIC && cfg->schedule != CMAQCHEM_SCHED_QUEUE)
         return fail("unknown schedule");
     if (cfg->ncols <= 0 || cfg->nrows <= 0 || cfg->nlays <= 0) return fail("domain dimensions must be positive");
@@ -210,6 +252,13 @@ extern "C" int cmaqchem_init(const cmaqchem_cfg* cfg, cmaqchem_handle** out)
         fwd[s] = 1.0e-3f * 28.9628f / (float)m->molwt[s];
         rev[s] = (double)(1.0f / fwd[s]);
     }
+    // hrinit.F:90-93: the EBI driver forms its factors in REAL(8) from REAL(4) constants
+    // and the REAL(8) molecular weights, then stores them REAL(4)
+    std::vector<float> ebi_fwd(m->nspec), ebi_rev(m->nspec);
+    for (int s = 0; s < m->nspec; ++s) {
+        ebi_fwd[s] = (float)((double)(1.0e-3f * 28.9628f) / m->molwt[s]);
+        ebi_rev[s] = (float)((double)(1.0e+3f / 28.9628f) * m->molwt[s]);
+    }
     int rc = 0;
     auto setup = [&]() -> int {
         CK(cudaSetDevice(h->device));
@@ -217,8 +266,8 @@ extern "C" int cmaqchem_init(const cmaqchem_cfg* cfg, cmaqchem_handle** out)
         CK(m->occupancy(&h->bps));
         if (h->bps < 1) h->bps = 1;
         h->nblocks = h->nsm * h->bps;
-        const size_t nwarps = (size_t)h->nblocks * chem::WARPS_PER_BLOCK;
-        CK(cudaMalloc(&h->d_ws, nwarps * (size_t)m->ws_elems * 32 * sizeof(double)));
+        if (ensure_ws(h, (size_t)h->nblocks * chem::WARPS_PER_BLOCK)) return -1;
+        if (configure_queue(h)) return -1;
         CK(cudaMalloc(&h->d_cgrid_index, sizeof(int) * m->nspec));
         CK(cudaMalloc(&h->d_convert, sizeof(int) * m->nspec));
         CK(cudaMalloc(&h->d_fwd, sizeof(float) * m->nspec));
@@ -227,6 +276,10 @@ extern "C" int cmaqchem_init(const cmaqchem_cfg* cfg, cmaqchem_handle** out)
         CK(cudaMemcpy(h->d_convert, m->convert, sizeof(int) * m->nspec, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(h->d_fwd, fwd.data(), sizeof(float) * m->nspec, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(h->d_rev, rev.data(), sizeof(double) * m->nspec, cudaMemcpyHostToDevice));
+        CK(cudaMalloc(&h->d_ebi_fwd, sizeof(float) * m->nspec));
+        CK(cudaMalloc(&h->d_ebi_rev, sizeof(float) * m->nspec));
+        CK(cudaMemcpy(h->d_ebi_fwd, ebi_fwd.data(), sizeof(float) * m->nspec, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(h->d_ebi_rev, ebi_rev.data(), sizeof(float) * m->nspec, cudaMemcpyHostToDevice));
         CK(cudaMalloc(&h->d_status, sizeof(int) * h->ncell));
         CK(cudaMalloc(&h->d_steps, sizeof(int) * h->ncell));
         CK(cudaMemset(h->d_status, 0, sizeof(int) * h->ncell));
@@ -255,10 +308,23 @@ extern "C" void cmaqchem_destroy(cmaqchem_handle* h) { free_handle(h); }
 extern "C" int cmaqchem_diag_set_tuning(cmaqchem_handle* h, const char* key, int value)
 {
     if (!h || !key) return fail("null argument");
-    if (strcmp(key, "night_pattern") == 0) h->use_night = value != 0;
-    else if (strcmp(key, "lockstep") == 0) h->lockstep = value != 0;
-    else return fail(std::string("unknown tuning key ") + key);
-    return 0;
+    CK(cudaSetDevice(h->device));
+    if (strcmp(key, "night_pattern") == 0) {
+        h->use_night = value != 0;
+        return 0;
+    }
+    if (strcmp(key, "lockstep") == 0) {
+        if (value < 0 || value > 2) return fail("lockstep must be 0, 1 or 2");
+        if (value == 0 && h->q_wpb != 8) return fail("lockstep 0 needs block_warps 8");
+        h->q_sync = value;
+    } else if (strcmp(key, "block_warps") == 0) {
+        if (value != 2 && value != 4 && value != 8) return fail("block_warps must be 2, 4 or 8");
+        if (h->q_sync == 0 && value != 8) return fail("block_warps 2 or 4 needs lockstep 1 or 2");
+        h->q_wpb = value;
+    } else {
+        return fail(std::string("unknown tuning key ") + key);
+    }
+    return configure_queue(h);
 }
 
 static int step_device_impl(cmaqchem_handle* h, float* conc, const float* ta, const float* qv, const float* dens,
@@ -274,9 +340,10 @@ static int step_device_impl(cmaqchem_handle* h, float* conc, const float* ta, co
     chem::GridArgs a = grid_args(h, conc, ta, qv, dens, pres, seaice, osz, rj, khet, chemstep);
     CK(cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned long long) * 5, s));
     CK(cudaEventRecord(h->ev0, s));
-    if (h->cfg.schedule == CMAQCHEM_SCHED_QUEUE) {
+    const bool ebi_solver = h->cfg.solver == CMAQCHEM_SOLVER_EBI;
+    if (h->cfg.schedule == CMAQCHEM_SCHED_QUEUE || ebi_solver) {
         chem::QueueArgs q{nullptr, h->d_head};
-        if (h->have_history) {
+        if (h->have_history && h->cfg.schedule == CMAQCHEM_SCHED_QUEUE) {
             const int nb = 4 * h->nsm;
             CK(cudaMemsetAsync(h->d_hist, 0, sizeof(unsigned int) * chem::QUEUE_BINS, s));
             chem::k_queue_hist<<<nb, 256, 0, s>>>(h->d_steps, h->ncell, h->d_hist);
@@ -288,7 +355,15 @@ static int step_device_impl(cmaqchem_handle* h, float* conc, const float* ta, co
             q.order = h->d_order;
         }
         CK(cudaMemsetAsync(h->d_head, 0, sizeof(unsigned long long), s));
-        CK(h->ops->chem_queue(a, q, h->lockstep != 0, h->nblocks, s));
+        if (ebi_solver) {
+            chem::EbiArgs e{};
+            ebi::steps_for(itmstep, h->ops->ebi_deltat, &e.n_ebi_steps, &e.tmstep);
+            e.fwd = h->d_ebi_fwd;
+            e.rev = h->d_ebi_rev;
+            CK(h->ops->chem_ebi(a, q, e, h->nblocks, s));
+        } else {
+            CK(h->ops->chem_queue(a, q, h->q_sync, h->q_wpb, h->q_nblocks, s));
+        }
     } else {
         CK(h->ops->chem_static(a, h->nblocks, s));
     }
@@ -402,6 +477,30 @@ extern "C" int cmaqchem_ros3_solve_device(cmaqchem_handle* h, long long ncell, d
     return 0;
 }
 
+extern "C" int cmaqchem_ebi_solve_device(cmaqchem_handle* h, long long ncell, double* yc, const double* rki,
+                                         int tstep_sec, int* status, int* iterations, void* stream)
+{
+    if (!h) return fail("null handle");
+    if (ncell < 0) return fail("ncell must be >= 0");
+    if (ncell == 0) return 0;
+    if (!yc || !rki) return fail("null array argument");
+    if (tstep_sec <= 0) return fail("tstep_sec must be positive");
+    CK(cudaSetDevice(h->device));
+    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    chem::EbiSolveArgs a{};
+    a.yc = yc;
+    a.rki = rki;
+    a.ncell = ncell;
+    ebi::steps_for(tstep_sec, h->ops->ebi_deltat, &a.n_ebi_steps, &a.tmstep);
+    a.ws = h->d_ws;
+    a.max_iter = h->max_iter;
+    a.cell_status = status;
+    a.cell_iters = iterations;
+    CK(h->ops->ebi_solve(a, h->nblocks, s));
+    CK(cudaStreamSynchronize(s));
+    return 0;
+}
+
 extern "C" int cmaqchem_rconst_device(cmaqchem_handle* h, const float* conc, const float* ta, const float* qv,
                                       const float* dens, const float* pres, const float* seaice,
                                       const float* ocean_szone, const float* rj, const double* khetero,
@@ -417,4 +516,190 @@ extern "C" int cmaqchem_rconst_device(cmaqchem_handle* h, const float* conc, con
     CK(h->ops->rconst(a, rki, sunlit, h->nblocks, s));
     CK(cudaStreamSynchronize(s));
     return 0;
+}
+
+// ------------------------------------------------------------------ discrete adjoint
+
+namespace {
+
+template <class T>
+int grow(T** p, size_t* cap, size_t need)
+{
+    if (need <= *cap) return 0;
+    if (*p) CK(cudaFree(*p));
+    *p = nullptr;
+    *cap = 0;
+    CK(cudaMalloc(p, need * sizeof(T)));
+    *cap = need;
+    return 0;
+}
+
+int adj_setup(cmaqchem_handle* h, long long ncell)
+{
+    if (!h->d_adj_ws) {
+        int fb = 0, rb = 0;
+        CK(h->ops->adj_occupancy(&fb, &rb));
+        int bps = fb < rb ? fb : rb;
+        if (bps < 1) bps = 1;
+        h->adj_nblocks = h->nsm * bps;
+        CK(cudaMalloc(&h->d_adj_ws, (size_t)h->adj_nblocks * adj::WPB * h->ops->adj_ws_elems * 32 * sizeof(double)));
+        CK(cudaMalloc(&h->d_adj_counters, 3 * sizeof(unsigned long long)));
+    }
+    if (grow(&h->d_adj_order, &h->adj_cell_cap, (size_t)ncell)) return -1;
+    if (grow(&h->d_adj_status, &h->adj_status_cap, (size_t)ncell)) return -1;
+    return 0;
+}
+
+// queue order of the cells by step counts, most first
+int adj_order(cmaqchem_handle* h, const int* steps, long long ncell, cudaStream_t s)
+{
+    const int nb = 4 * h->nsm;
+    CK(cudaMemsetAsync(h->d_hist, 0, sizeof(unsigned int) * chem::QUEUE_BINS, s));
+    chem::k_queue_hist<<<nb, 256, 0, s>>>(steps, ncell, h->d_hist);
+    CK(cudaGetLastError());
+    chem::k_queue_scan<<<1, chem::QUEUE_BINS, 0, s>>>(h->d_hist, h->d_cursor);
+    CK(cudaGetLastError());
+    chem::k_queue_scatter<<<nb, 256, 0, s>>>(steps, ncell, h->d_cursor, h->d_adj_order);
+    CK(cudaGetLastError());
+    return 0;
+}
+
+adj::Args adj_args(cmaqchem_handle* h, long long ncell, const double* rki, const unsigned char* night,
+                   const double* kmult, const double* emis, double chemstep)
+{
+    adj::Args a{};
+    a.ncell = ncell;
+    a.chemstep = chemstep;
+    a.tol = ros3::Tol{h->cfg.rtol, h->cfg.atol, h->rnspec};
+    a.max_iter = h->max_iter;
+    a.ws = h->d_adj_ws;
+    a.rki = rki;
+    a.kmult = kmult;
+    a.emis = emis;
+    a.night = night;
+    a.head = h->d_head;
+    a.counters = h->d_adj_counters;
+    return a;
+}
+
+int adj_check(cmaqchem_handle* h, long long ncell, const void* y, const double* rki, const unsigned char* night,
+              int nsync, double chemstep, const void* ck, const int* nsteps)
+{
+    if (!h) return fail("null handle");
+    if (ncell <= 0) return fail("ncell must be positive");
+    if (ncell > (long long)INT32_MAX) return fail("ncell must fit in 32 bits");
+    if (!y || !rki || !night || !ck || !nsteps) return fail("null array argument");
+    if (nsync <= 0) return fail("nsync must be positive");
+    if (!(chemstep > 0.0)) return fail("chemstep must be positive");
+    return 0;
+}
+
+}  // namespace
+
+extern "C" int cmaqchem_adj_forward(cmaqchem_handle* h, long long ncell, double* y, const double* rki,
+                                    long long rki_sync_stride, const unsigned char* night, const double* kmult,
+                                    const double* emis, int nsync, double chemstep_min, double* checkpoints,
+                                    int* nsteps, void* stream)
+{
+    if (adj_check(h, ncell, y, rki, night, nsync, chemstep_min, checkpoints, nsteps)) return -1;
+    CK(cudaSetDevice(h->device));
+    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    if (adj_setup(h, ncell)) return -1;
+    CK(cudaMemsetAsync(h->d_adj_counters, 0, 3 * sizeof(unsigned long long), s));
+    const size_t plane = (size_t)h->ops->ischan * ncell;
+    for (int k = 0; k < nsync; ++k) {
+        double* ck = checkpoints + (size_t)k * plane;
+        CK(cudaMemcpyAsync(ck, y, plane * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        adj::Args a = adj_args(h, ncell, rki + (size_t)k * rki_sync_stride, night, kmult, emis, chemstep_min);
+        a.y_in = ck;
+        a.y_out = y;
+        a.nsteps = nsteps + (size_t)k * ncell;
+        a.status = h->d_adj_status;
+        if (k > 0) {
+            if (adj_order(h, nsteps + (size_t)(k - 1) * ncell, ncell, s)) return -1;
+            a.order = h->d_adj_order;
+        }
+        CK(cudaMemsetAsync(h->d_head, 0, sizeof(unsigned long long), s));
+        CK(h->ops->adj_forward(a, h->adj_nblocks, s));
+    }
+    unsigned long long cnt[3];
+    CK(cudaMemcpyAsync(cnt, h->d_adj_counters, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return (int)cnt[2];
+}
+
+extern "C" int cmaqchem_adj_backward(cmaqchem_handle* h, long long ncell, double* lambda, const double* rki,
+                                     long long rki_sync_stride, const unsigned char* night, const double* kmult,
+                                     const double* emis, int nsync, double chemstep_min, const double* checkpoints,
+                                     const int* nsteps, double* grad_logk, double* grad_emis, void* stream)
+{
+    if (adj_check(h, ncell, lambda, rki, night, nsync, chemstep_min, checkpoints, nsteps)) return -1;
+    if (!grad_logk) return fail("null array argument");
+    CK(cudaSetDevice(h->device));
+    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    if (adj_setup(h, ncell)) return -1;
+    // tape offsets of every synchronisation step
+    const int ntiles = (int)((ncell + adj::SCAN_TILE - 1) / adj::SCAN_TILE);
+    if (grow(&h->d_tape_off, &h->tape_off_cap, (size_t)nsync * ncell)) return -1;
+    if (grow(&h->d_tiles, &h->tiles_cap, (size_t)nsync * ntiles)) return -1;
+    if (grow(&h->d_tape_tot, &h->tot_cap, (size_t)nsync)) return -1;
+    for (int k = 0; k < nsync; ++k) {
+        const int* v = nsteps + (size_t)k * ncell;
+        long long* tiles = h->d_tiles + (size_t)k * ntiles;
+        adj::k_scan_tiles<<<ntiles, 256, 0, s>>>(v, ncell, tiles);
+        CK(cudaGetLastError());
+        adj::k_scan_tile_sums<<<1, 32, 0, s>>>(tiles, ntiles, h->d_tape_tot + k);
+        CK(cudaGetLastError());
+        adj::k_scan_apply<<<ntiles, 256, 0, s>>>(v, ncell, tiles, h->d_tape_off + (size_t)k * ncell);
+        CK(cudaGetLastError());
+    }
+    std::vector<long long> tot(nsync);
+    CK(cudaMemcpyAsync(tot.data(), h->d_tape_tot, sizeof(long long) * nsync, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    long long tmax = 1;
+    for (long long t : tot) {
+        if (t < 0) return fail("negative step count");
+        tmax = t > tmax ? t : tmax;
+    }
+    if ((size_t)tmax > h->tape_cap) {
+        if (h->d_tape_y) CK(cudaFree(h->d_tape_y));
+        if (h->d_tape_h) CK(cudaFree(h->d_tape_h));
+        h->d_tape_y = nullptr;
+        h->d_tape_h = nullptr;
+        h->tape_cap = 0;
+        const size_t bytes = (size_t)tmax * h->ops->ischan * sizeof(double);
+        cudaError_t e = cudaMalloc(&h->d_tape_y, bytes);
+        if (e != cudaSuccess)
+            return fail("adjoint tape of " + std::to_string(bytes >> 20) + " MiB does not fit: " +
+                        cudaGetErrorString(e));
+        CK(cudaMalloc(&h->d_tape_h, (size_t)tmax * sizeof(double)));
+        h->tape_cap = (size_t)tmax;
+    }
+    CK(cudaMemsetAsync(h->d_adj_counters, 0, 3 * sizeof(unsigned long long), s));
+    const size_t plane = (size_t)h->ops->ischan * ncell;
+    for (int k = nsync - 1; k >= 0; --k) {
+        adj::Args a = adj_args(h, ncell, rki + (size_t)k * rki_sync_stride, night, kmult, emis, chemstep_min);
+        a.nsteps = const_cast<int*>(nsteps) + (size_t)k * ncell;
+        a.tape_off = h->d_tape_off + (size_t)k * ncell;
+        a.tape_y = h->d_tape_y;
+        a.tape_h = h->d_tape_h;
+        if (adj_order(h, a.nsteps, ncell, s)) return -1;
+        a.order = h->d_adj_order;
+        // re-run the step from its checkpoint, recording the tape
+        a.y_in = checkpoints + (size_t)k * plane;
+        CK(cudaMemsetAsync(h->d_head, 0, sizeof(unsigned long long), s));
+        CK(h->ops->adj_forward(a, h->adj_nblocks, s));
+        // reverse sweep
+        a.lam = lambda;
+        a.grad_logk = grad_logk;
+        a.grad_emis = grad_emis;
+        CK(cudaMemsetAsync(h->d_head, 0, sizeof(unsigned long long), s));
+        CK(h->ops->adj_reverse(a, h->adj_nblocks, s));
+    }
+    unsigned long long cnt[3];
+    CK(cudaMemcpyAsync(cnt, h->d_adj_counters, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (cnt[0] != 0) return fail("the re-run of a step took more accepted steps than the forward pass recorded");
+    if (cnt[1] != (unsigned long long)ncell * nsync) return fail("reverse sweep did not visit every cell");
+    return (int)cnt[2];
 }

@@ -1,0 +1,1800 @@
+// Generated by cmaq_gb300.mechgen.generate from CCTM/src/MECHS/cb6r5_ae7_aq/RXNS_DATA_MODULE.F90
+// and RXNS_FUNC_MODULE.F90 (sha256/16 4242f44b2527a299).  Do not edit.
+#include "cb6r5_ae7_aq_mech.cuh"
+#include <math.h>
+namespace mech_cb6r5_ae7_aq {
+__device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int phioff, int outoff)
+{
+    const double* __restrict__ y = ws + yoff * 32;
+    const double* __restrict__ phi = ws + phioff * 32;
+    double* __restrict__ out = ws + outoff * 32;
+    {
+      double w = 1.0 * phi[4256];
+      w = fma(1.0, phi[3936], w);
+      w = fma(1.0, phi[4704], w);
+      w = fma(1.0, phi[4416], w);
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[3104];
+      w = w - phi[4448];
+      const double kw = ws[39136] * w;
+      out[3104] = fma(kw, y[4448], out[3104]);
+      out[4448] = fma(kw, y[3104], out[4448]);
+      ws[175616] = fma(kw * y[3104], y[4448], ws[175616]);
+    }
+    {
+      double w = -phi[3104];
+      w = w - phi[4704];
+      const double kw = ws[39168] * w;
+      out[3104] = fma(kw, y[4704], out[3104]);
+      out[4704] = fma(kw, y[3104], out[4704]);
+      ws[175648] = fma(kw * y[3104], y[4704], ws[175648]);
+    }
+    {
+      double w = 1.0 * phi[4256];
+      w = fma(1.0, phi[3936], w);
+      w = fma(1.0, phi[4704], w);
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[3104];
+      w = w - phi[4672];
+      const double kw = ws[39200] * w;
+      out[3104] = fma(kw, y[4672], out[3104]);
+      out[4672] = fma(kw, y[3104], out[4672]);
+      ws[175680] = fma(kw * y[3104], y[4672], ws[175680]);
+    }
+    {
+      double w = 0.18 * phi[3616];
+      w = fma(0.65, phi[3488], w);
+      w = fma(0.72, phi[4672], w);
+      w = fma(0.1, phi[3936], w);
+      w = fma(0.1, phi[4736], w);
+      w = fma(0.07, phi[4576], w);
+      w = fma(0.18, phi[4704], w);
+      w = fma(1.0, phi[2944], w);
+      w = w - phi[1088];
+      w = w - phi[4736];
+      const double kw = ws[39232] * w;
+      out[1088] = fma(kw, y[4736], out[1088]);
+      out[4736] = fma(kw, y[1088], out[4736]);
+      ws[175712] = fma(kw * y[1088], y[4736], ws[175712]);
+    }
+    {
+      double w = 0.86 * phi[4608];
+      w = fma(0.14, phi[4032], w);
+      w = fma(0.417, phi[4256], w);
+      w = fma(0.443, phi[4000], w);
+      w = fma(0.66, phi[3936], w);
+      w = fma(0.2, phi[3808], w);
+      w = fma(0.86, phi[4704], w);
+      w = w - phi[3488];
+      w = w - phi[4384];
+      const double kw = ws[39264] * w;
+      out[3488] = fma(kw, y[4384], out[3488]);
+      out[4384] = fma(kw, y[3488], out[4384]);
+      ws[175744] = fma(kw * y[3488], y[4384], ws[175744]);
+    }
+    {
+      double w = 0.48 * phi[4256];
+      w = fma(0.52, phi[4000], w);
+      w = fma(0.77, phi[3936], w);
+      w = fma(0.23, phi[3808], w);
+      w = fma(1.0, phi[4704], w);
+      w = fma(1.0, phi[4416], w);
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[3488];
+      w = w - phi[4448];
+      const double kw = ws[39296] * w;
+      out[3488] = fma(kw, y[4448], out[3488]);
+      out[4448] = fma(kw, y[3488], out[4448]);
+      ws[175776] = fma(kw * y[3488], y[4448], ws[175776]);
+    }
+    {
+      double w = -phi[3488];
+      w = w - phi[4704];
+      const double kw = ws[39328] * w;
+      out[3488] = fma(kw, y[4704], out[3488]);
+      out[4704] = fma(kw, y[3488], out[4704]);
+      ws[175808] = fma(kw * y[3488], y[4704], ws[175808]);
+    }
+    {
+      double w = 0.48 * phi[4256];
+      w = fma(0.52, phi[4000], w);
+      w = fma(0.77, phi[3936], w);
+      w = fma(0.23, phi[3808], w);
+      w = fma(1.0, phi[4704], w);
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[3488];
+      w = w - phi[4672];
+      const double kw = ws[39360] * w;
+      out[3488] = fma(kw, y[4672], out[3488]);
+      out[4672] = fma(kw, y[3488], out[4672]);
+      ws[175840] = fma(kw * y[3488], y[4672], ws[175840]);
+    }
+    {
+      double w = 0.155 * phi[3616];
+      w = fma(0.544, phi[3584], w);
+      w = fma(0.602, phi[4672], w);
+      w = fma(0.244, phi[3808], w);
+      w = fma(0.244, phi[4736], w);
+      w = fma(0.058, phi[4576], w);
+      w = fma(0.155, phi[4704], w);
+      w = fma(1.0, phi[2496], w);
+      w = w - phi[1120];
+      w = w - phi[4736];
+      const double kw = ws[39392] * w;
+      out[1120] = fma(kw, y[4736], out[1120]);
+      out[4736] = fma(kw, y[1120], out[4736]);
+      ws[175872] = fma(kw * y[1120], y[4736], ws[175872]);
+    }
+    {
+      double w = 0.155 * phi[3616];
+      w = fma(0.544, phi[3584], w);
+      w = fma(0.602, phi[4672], w);
+      w = fma(0.244, phi[3808], w);
+      w = fma(0.244, phi[4736], w);
+      w = fma(0.058, phi[4576], w);
+      w = fma(0.155, phi[4704], w);
+      w = fma(1.0, phi[2560], w);
+      w = w - phi[1152];
+      w = w - phi[4736];
+      const double kw = ws[39424] * w;
+      out[1152] = fma(kw, y[4736], out[1152]);
+      out[4736] = fma(kw, y[1152], out[4736]);
+      ws[175904] = fma(kw * y[1152], y[4736], ws[175904]);
+    }
+    {
+      double w = 0.86 * phi[4608];
+      w = fma(0.14, phi[4032], w);
+      w = fma(0.221, phi[4256], w);
+      w = fma(0.675, phi[4000], w);
+      w = fma(0.3, phi[3936], w);
+      w = fma(0.56, phi[3808], w);
+      w = fma(0.86, phi[4704], w);
+      w = w - phi[3584];
+      w = w - phi[4384];
+      const double kw = ws[39456] * w;
+      out[3584] = fma(kw, y[4384], out[3584]);
+      out[4384] = fma(kw, y[3584], out[4384]);
+      ws[175936] = fma(kw * y[3584], y[4384], ws[175936]);
+    }
+    {
+      double w = -phi[3584];
+      w = w - phi[4704];
+      const double kw = ws[39488] * w;
+      out[3584] = fma(kw, y[4704], out[3584]);
+      out[4704] = fma(kw, y[3584], out[4704]);
+      ws[175968] = fma(kw * y[3584], y[4704], ws[175968]);
+    }
+    {
+      double w = 0.26 * phi[4256];
+      w = fma(0.77, phi[4000], w);
+      w = fma(0.35, phi[3936], w);
+      w = fma(0.65, phi[3808], w);
+      w = fma(1.0, phi[4704], w);
+      w = fma(1.0, phi[4416], w);
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[3584];
+      w = w - phi[4448];
+      const double kw = ws[39520] * w;
+      out[3584] = fma(kw, y[4448], out[3584]);
+      out[4448] = fma(kw, y[3584], out[4448]);
+      ws[176000] = fma(kw * y[3584], y[4448], ws[176000]);
+    }
+    {
+      double w = 0.26 * phi[4256];
+      w = fma(0.77, phi[4000], w);
+      w = fma(0.35, phi[3936], w);
+      w = fma(0.65, phi[3808], w);
+      w = fma(1.0, phi[4704], w);
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[3584];
+      w = w - phi[4672];
+      const double kw = ws[39552] * w;
+      out[3584] = fma(kw, y[4672], out[3584]);
+      out[4672] = fma(kw, y[3584], out[4672]);
+      ws[176032] = fma(kw * y[3584], y[4672], ws[176032]);
+    }
+    {
+      double w = 0.025 * phi[4256];
+      w = fma(0.025, phi[3936], w);
+      w = fma(1.0, phi[4704], w);
+      w = fma(0.2, phi[3328], w);
+      w = fma(0.732, phi[1760], w);
+      w = fma(0.02, phi[4288], w);
+      w = fma(0.02, phi[4672], w);
+      w = w - phi[3616];
+      w = w - phi[4736];
+      const double kw = ws[39584] * w;
+      out[3616] = fma(kw, y[4736], out[3616]);
+      out[4736] = fma(kw, y[3616], out[4736]);
+      ws[176064] = fma(kw * y[3616], y[4736], ws[176064]);
+    }
+    {
+      double w = 0.3 * phi[3328];
+      w = fma(1.0, phi[4192], w);
+      w = fma(0.48, phi[4352], w);
+      w = fma(0.12, phi[4576], w);
+      w = fma(0.24, phi[4256], w);
+      w = fma(0.24, phi[4000], w);
+      w = fma(0.48, phi[3744], w);
+      w = fma(0.1, phi[4288], w);
+      w = fma(0.7, phi[4672], w);
+      w = w - phi[3616];
+      w = w - phi[4640];
+      const double kw = ws[39616] * w;
+      out[3616] = fma(kw, y[4640], out[3616]);
+      out[4640] = fma(kw, y[3616], out[4640]);
+      ws[176096] = fma(kw * y[3616], y[4640], ws[176096]);
+    }
+    {
+      double w = 1.0 * phi[2176];
+      w = w - phi[3328];
+      w = w - phi[4608];
+      const double kw = ws[39648] * w;
+      out[3328] = fma(kw, y[4608], out[3328]);
+      out[4608] = fma(kw, y[3328], out[4608]);
+      ws[176128] = fma(kw * y[3328], y[4608], ws[176128]);
+    }
+    {
+      double w = 1.0 * phi[3616];
+      w = w - phi[3328];
+      w = w - phi[4704];
+      const double kw = ws[39680] * w;
+      out[3328] = fma(kw, y[4704], out[3328]);
+      out[4704] = fma(kw, y[3328], out[4704]);
+      ws[176160] = fma(kw * y[3328], y[4704], ws[176160]);
+    }
+    {
+      double w = 1.0 * phi[4032];
+      w = fma(0.5, phi[3328], w);
+      w = w - phi[2176];
+      w = w - phi[4736];
+      const double kw = ws[39712] * w;
+      out[2176] = fma(kw, y[4736], out[2176]);
+      out[4736] = fma(kw, y[2176], out[4736]);
+      ws[176192] = fma(kw * y[2176], y[4736], ws[176192]);
+    }
+    {
+      double w = 1.0 * phi[4032];
+      w = fma(0.5, phi[3328], w);
+      w = fma(1.0, phi[4192], w);
+      w = w - phi[2176];
+      w = w - phi[4640];
+      const double kw = ws[39744] * w;
+      out[2176] = fma(kw, y[4640], out[2176]);
+      out[4640] = fma(kw, y[2176], out[4640]);
+      ws[176224] = fma(kw * y[2176], y[4640], ws[176224]);
+    }
+    {
+      double w = 1.0 * phi[2464];
+      w = fma(1.0, phi[4704], w);
+      w = fma(1.0, phi[4512], w);
+      w = fma(1.0, phi[3936], w);
+      w = w - phi[2176];
+      const double kw = ws[39776] * w;
+      out[2176] = out[2176] + kw;
+      ws[176256] = fma(kw, y[2176], ws[176256]);
+    }
+    {
+      double w = 0.4 * phi[4256];
+      w = fma(1.0, phi[4576], w);
+      w = fma(0.7, phi[4704], w);
+      w = fma(0.7, phi[4480], w);
+      w = fma(0.3, phi[4448], w);
+      w = w - phi[3808];
+      const double kw = ws[39808] * w;
+      out[3808] = out[3808] + kw;
+      ws[176288] = fma(kw, y[3808], ws[176288]);
+    }
+    {
+      double w = 1.0 * phi[4000];
+      w = fma(0.4, phi[4256], w);
+      w = fma(2.0, phi[4576], w);
+      w = fma(2.0, phi[4672], w);
+      w = w - phi[3808];
+      w = w - phi[4736];
+      const double kw = ws[39840] * w;
+      out[3808] = fma(kw, y[4736], out[3808]);
+      out[4736] = fma(kw, y[3808], out[4736]);
+      ws[176320] = fma(kw * y[3808], y[4736], ws[176320]);
+    }
+    {
+      double w = 1.2 * phi[4000];
+      w = fma(0.5, phi[4736], w);
+      w = fma(0.6, phi[4448], w);
+      w = fma(0.1, phi[4128], w);
+      w = fma(0.5, phi[4480], w);
+      w = fma(0.3, phi[4576], w);
+      w = fma(0.3, phi[4672], w);
+      w = w - phi[3808];
+      w = w - phi[4320];
+      const double kw = ws[39872] * w;
+      out[3808] = fma(kw, y[4320], out[3808]);
+      out[4320] = fma(kw, y[3808], out[4320]);
+      ws[176352] = fma(kw * y[3808], y[4320], ws[176352]);
+    }
+    {
+      double w = 0.5 * phi[4608];
+      w = fma(0.5, phi[4032], w);
+      w = fma(0.45, phi[4576], w);
+      w = fma(0.45, phi[4352], w);
+      w = fma(0.1, phi[4288], w);
+      w = fma(1.0, phi[4672], w);
+      w = fma(0.25, phi[3936], w);
+      w = fma(0.25, phi[4000], w);
+      w = w - phi[3808];
+      w = w - phi[4640];
+      const double kw = ws[39904] * w;
+      out[3808] = fma(kw, y[4640], out[3808]);
+      out[4640] = fma(kw, y[3808], out[4640]);
+      ws[176384] = fma(kw * y[3808], y[4640], ws[176384]);
+    }
+    {
+      double w = 1.0 * phi[3744];
+      w = fma(1.0, phi[4704], w);
+      w = fma(1.0, phi[4480], w);
+      w = w - phi[3936];
+      const double kw = ws[39936] * w;
+      out[3936] = out[3936] + kw;
+      ws[176416] = fma(kw, y[3936], ws[176416]);
+    }
+    {
+      double w = 0.6 * phi[3744];
+      w = fma(0.4, phi[4576], w);
+      w = fma(0.4, phi[4672], w);
+      w = fma(0.4, phi[4256], w);
+      w = w - phi[3936];
+      w = w - phi[4736];
+      const double kw = ws[39968] * w;
+      out[3936] = fma(kw, y[4736], out[3936]);
+      out[4736] = fma(kw, y[3936], out[4736]);
+      ws[176448] = fma(kw * y[3936], y[4736], ws[176448]);
+    }
+    {
+      double w = 1.4 * phi[4256];
+      w = fma(0.24, phi[4000], w);
+      w = fma(0.5, phi[4736], w);
+      w = fma(0.12, phi[4448], w);
+      w = fma(0.08, phi[4512], w);
+      w = fma(0.02, phi[4128], w);
+      w = fma(1.98, phi[4480], w);
+      w = fma(0.56, phi[4704], w);
+      w = w - phi[3936];
+      w = w - phi[4320];
+      const double kw = ws[40000] * w;
+      out[3936] = fma(kw, y[4320], out[3936]);
+      out[4320] = fma(kw, y[3936], out[4320]);
+      ws[176480] = fma(kw * y[3936], y[4320], ws[176480]);
+    }
+    {
+      double w = 1.0 * phi[3744];
+      w = fma(1.0, phi[4192], w);
+      w = w - phi[3936];
+      w = w - phi[4640];
+      const double kw = ws[40032] * w;
+      out[3936] = fma(kw, y[4640], out[3936]);
+      out[4640] = fma(kw, y[3936], out[4640]);
+      ws[176512] = fma(kw * y[3936], y[4640], ws[176512]);
+    }
+    {
+      double w = 0.14 * phi[4512];
+      w = fma(0.2, phi[4704], w);
+      w = fma(0.5, phi[3328], w);
+      w = w - phi[1760];
+      w = w - phi[4736];
+      const double kw = ws[40064] * w;
+      out[1760] = fma(kw, y[4736], out[1760]);
+      out[4736] = fma(kw, y[1760], out[4736]);
+      ws[176544] = fma(kw * y[1760], y[4736], ws[176544]);
+    }
+    {
+      double w = 1.0 * phi[3328];
+      w = fma(1.0, phi[4192], w);
+      w = w - phi[1760];
+      w = w - phi[4640];
+      const double kw = ws[40096] * w;
+      out[1760] = fma(kw, y[4640], out[1760]);
+      out[4640] = fma(kw, y[1760], out[4640]);
+      ws[176576] = fma(kw * y[1760], y[4640], ws[176576]);
+    }
+    {
+      double w = 1.0 * phi[4608];
+      w = fma(0.5, phi[4256], w);
+      w = fma(0.5, phi[4480], w);
+      w = fma(0.8, phi[4704], w);
+      w = fma(0.2, phi[4096], w);
+      w = w - phi[3744];
+      w = w - phi[4384];
+      const double kw = ws[40128] * w;
+      out[3744] = fma(kw, y[4384], out[3744]);
+      out[4384] = fma(kw, y[3744], out[4384]);
+      ws[176608] = fma(kw * y[3744], y[4384], ws[176608]);
+    }
+    {
+      double w = 1.0 * phi[1792];
+      w = w - phi[3744];
+      w = w - phi[4608];
+      const double kw = ws[40160] * w;
+      out[3744] = fma(kw, y[4608], out[3744]);
+      out[4608] = fma(kw, y[3744], out[4608]);
+      ws[176640] = fma(kw * y[3744], y[4608], ws[176640]);
+    }
+    {
+      double w = 1.0 * phi[3744];
+      w = fma(1.0, phi[4608], w);
+      w = w - phi[1792];
+      const double kw = ws[40192] * w;
+      out[1792] = out[1792] + kw;
+      ws[176672] = fma(kw, y[1792], ws[176672]);
+    }
+    {
+      double w = 0.37 * phi[2688];
+      w = fma(0.13, phi[3904], w);
+      w = fma(0.13, phi[4320], w);
+      w = fma(0.5, phi[4736], w);
+      w = fma(0.5, phi[4416], w);
+      w = fma(0.5, phi[4672], w);
+      w = w - phi[3744];
+      w = w - phi[4704];
+      const double kw = ws[40224] * w;
+      out[3744] = fma(kw, y[4704], out[3744]);
+      out[4704] = fma(kw, y[3744], out[4704]);
+      ws[176704] = fma(kw * y[3744], y[4704], ws[176704]);
+    }
+    {
+      double w = 1.0 * phi[4416];
+      w = fma(1.0, phi[4352], w);
+      w = fma(1.0, phi[4064], w);
+      w = fma(2.0, phi[4672], w);
+      w = w - phi[3744];
+      w = w - phi[4448];
+      const double kw = ws[40256] * w;
+      out[3744] = fma(kw, y[4448], out[3744]);
+      out[4448] = fma(kw, y[3744], out[4448]);
+      ws[176736] = fma(kw * y[3744], y[4448], ws[176736]);
+    }
+    {
+      double w = 0.8 * phi[4576];
+      w = fma(0.8, phi[4064], w);
+      w = fma(1.8, phi[4672], w);
+      w = fma(0.2, phi[3904], w);
+      w = w - phi[3744];
+      w = w - phi[4672];
+      const double kw = ws[40288] * w;
+      out[3744] = fma(kw, y[4672], out[3744]);
+      out[4672] = fma(kw, y[3744], out[4672]);
+      ws[176768] = fma(kw * y[3744], y[4672], ws[176768]);
+    }
+    {
+      double w = 0.5 * phi[4608];
+      w = fma(0.5, phi[4256], w);
+      w = fma(1.0, phi[4480], w);
+      w = fma(0.5, phi[4032], w);
+      w = w - phi[1792];
+      w = w - phi[4736];
+      const double kw = ws[40320] * w;
+      out[1792] = fma(kw, y[4736], out[1792]);
+      out[4736] = fma(kw, y[1792], out[4736]);
+      ws[176800] = fma(kw * y[1792], y[4736], ws[176800]);
+    }
+    {
+      double w = 1.0 * phi[4128];
+      w = fma(1.0, phi[4608], w);
+      w = w - phi[1952];
+      w = w - phi[4736];
+      const double kw = ws[40352] * w;
+      out[1952] = fma(kw, y[4736], out[1952]);
+      out[4736] = fma(kw, y[1952], out[4736]);
+      ws[176832] = fma(kw * y[1952], y[4736], ws[176832]);
+    }
+    {
+      double w = 1.0 * phi[4416];
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[416];
+      w = w - phi[4736];
+      const double kw = ws[40384] * w;
+      out[416] = fma(kw, y[4736], out[416]);
+      out[4736] = fma(kw, y[416], out[4736]);
+      ws[176864] = fma(kw * y[416], y[4736], ws[176864]);
+    }
+    {
+      double w = 1.0 * phi[4288];
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[928];
+      const double kw = ws[40416] * w;
+      out[928] = out[928] + kw;
+      ws[176896] = fma(kw, y[928], ws[176896]);
+    }
+}
+__device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int phioff, int outoff)
+{
+    const double* __restrict__ y = ws + yoff * 32;
+    const double* __restrict__ phi = ws + phioff * 32;
+    double* __restrict__ out = ws + outoff * 32;
+    {
+      double w = 0.732 * phi[3392];
+      w = fma(0.268, phi[4064], w);
+      w = fma(0.268, phi[4224], w);
+      w = fma(1.0, phi[4576], w);
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[928];
+      const double kw = ws[40448] * w;
+      out[928] = out[928] + kw;
+      ws[176928] = fma(kw, y[928], ws[176928]);
+    }
+    {
+      double w = 1.0 * phi[4288];
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[1984];
+      const double kw = ws[40480] * w;
+      out[1984] = out[1984] + kw;
+      ws[176960] = fma(kw, y[1984], ws[176960]);
+    }
+    {
+      double w = 0.126 * phi[4064];
+      w = fma(0.874, phi[960], w);
+      w = fma(0.126, phi[4576], w);
+      w = fma(0.874, phi[4352], w);
+      w = fma(1.0, phi[4672], w);
+      w = fma(-0.126, phi[4224], w);
+      w = w - phi[1984];
+      const double kw = ws[40512] * w;
+      out[1984] = out[1984] + kw;
+      ws[176992] = fma(kw, y[1984], ws[176992]);
+    }
+    {
+      double w = 1.0 * phi[4192];
+      w = w - phi[4608];
+      w = w - phi[4736];
+      const double kw = ws[40544] * w;
+      out[4608] = fma(kw, y[4736], out[4608]);
+      out[4736] = fma(kw, y[4608], out[4736]);
+      ws[177024] = fma(kw * y[4608], y[4736], ws[177024]);
+    }
+    {
+      double w = 2.0 * phi[4544];
+      w = w - phi[1184];
+      const double kw = ws[40576] * w;
+      out[1184] = out[1184] + kw;
+      ws[177056] = fma(kw, y[1184], ws[177056]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = fma(1.0, phi[4544], w);
+      w = w - phi[1824];
+      const double kw = ws[40608] * w;
+      out[1824] = out[1824] + kw;
+      ws[177088] = fma(kw, y[1824], ws[177088]);
+    }
+    {
+      double w = 1.0 * phi[3520];
+      w = w - phi[4544];
+      w = w - phi[4320];
+      const double kw = ws[40640] * w;
+      out[4544] = fma(kw, y[4320], out[4544]);
+      out[4320] = fma(kw, y[4544], out[4320]);
+      ws[177120] = fma(kw * y[4544], y[4320], ws[177120]);
+    }
+    {
+      double w = 0.3 * phi[1184];
+      w = fma(1.4, phi[4544], w);
+      w = w - phi[3520];
+      w = w - phi[3520];
+      const double kw = ws[40672] * w;
+      out[3520] = fma(kw, y[3520], out[3520]);
+      out[3520] = fma(kw, y[3520], out[3520]);
+      ws[177152] = fma(kw * y[3520], y[3520], ws[177152]);
+    }
+    {
+      double w = 1.0 * phi[4544];
+      w = fma(1.0, phi[4608], w);
+      w = w - phi[3520];
+      w = w - phi[4384];
+      const double kw = ws[40704] * w;
+      out[3520] = fma(kw, y[4384], out[3520]);
+      out[4384] = fma(kw, y[3520], out[4384]);
+      ws[177184] = fma(kw * y[3520], y[4384], ws[177184]);
+    }
+    {
+      double w = 1.0 * phi[1824];
+      w = w - phi[3520];
+      w = w - phi[4704];
+      const double kw = ws[40736] * w;
+      out[3520] = fma(kw, y[4704], out[3520]);
+      out[4704] = fma(kw, y[3520], out[4704]);
+      ws[177216] = fma(kw * y[3520], y[4704], ws[177216]);
+    }
+    {
+      double w = 1.0 * phi[4544];
+      w = fma(1.0, phi[4512], w);
+      w = fma(1.0, phi[4704], w);
+      w = w - phi[3520];
+      w = w - phi[4416];
+      const double kw = ws[40768] * w;
+      out[3520] = fma(kw, y[4416], out[3520]);
+      out[4416] = fma(kw, y[3520], out[4416]);
+      ws[177248] = fma(kw * y[3520], y[4416], ws[177248]);
+    }
+    {
+      double w = 1.0 * phi[4544];
+      w = fma(1.0, phi[4480], w);
+      w = w - phi[4736];
+      w = w - phi[3232];
+      const double kw = ws[40800] * w;
+      out[4736] = fma(kw, y[3232], out[4736]);
+      out[3232] = fma(kw, y[4736], out[3232]);
+      ws[177280] = fma(kw * y[4736], y[3232], ws[177280]);
+    }
+    {
+      double w = 1.0 * phi[4544];
+      w = fma(1.0, phi[4480], w);
+      w = fma(1.0, phi[4704], w);
+      w = w - phi[3232];
+      const double kw = ws[40832] * w;
+      out[3232] = out[3232] + kw;
+      ws[177312] = fma(kw, y[3232], ws[177312]);
+    }
+    {
+      double w = 1.0 * phi[3968];
+      w = fma(1.0, phi[4416], w);
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[4544];
+      const double kw = ws[40864] * w;
+      out[4544] = out[4544] + kw;
+      ws[177344] = fma(kw, y[4544], ws[177344]);
+    }
+    {
+      double w = 1.0 * phi[3968];
+      w = fma(1.0, phi[1984], w);
+      w = w - phi[4544];
+      w = w - phi[4224];
+      const double kw = ws[40896] * w;
+      out[4544] = fma(kw, y[4224], out[4544]);
+      out[4224] = fma(kw, y[4544], out[4224]);
+      ws[177376] = fma(kw * y[4544], y[4224], ws[177376]);
+    }
+    {
+      double w = 1.0 * phi[3968];
+      w = fma(1.0, phi[3392], w);
+      w = fma(0.97, phi[4576], w);
+      w = fma(0.03, phi[4288], w);
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[4544];
+      w = w - phi[896];
+      const double kw = ws[40928] * w;
+      out[4544] = fma(kw, y[896], out[4544]);
+      out[896] = fma(kw, y[4544], out[896]);
+      ws[177408] = fma(kw * y[4544], y[896], ws[177408]);
+    }
+    {
+      double w = 1.0 * phi[3968];
+      w = fma(0.991, phi[4128], w);
+      w = fma(0.991, phi[4576], w);
+      w = fma(0.009, phi[4288], w);
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[4544];
+      w = w - phi[832];
+      const double kw = ws[40960] * w;
+      out[4544] = fma(kw, y[832], out[4544]);
+      out[832] = fma(kw, y[4544], out[832]);
+      ws[177440] = fma(kw * y[4544], y[832], ws[177440]);
+    }
+    {
+      double w = 1.0 * phi[3232];
+      w = fma(2.0, phi[4352], w);
+      w = fma(1.0, phi[4704], w);
+      w = fma(1.0, phi[4512], w);
+      w = w - phi[4544];
+      w = w - phi[2656];
+      const double kw = ws[40992] * w;
+      out[4544] = fma(kw, y[2656], out[4544]);
+      out[2656] = fma(kw, y[4544], out[2656]);
+      ws[177472] = fma(kw * y[4544], y[2656], ws[177472]);
+    }
+    {
+      double w = 1.0 * phi[3232];
+      w = fma(0.33, phi[4128], w);
+      w = fma(0.67, phi[4064], w);
+      w = fma(2.0, phi[4352], w);
+      w = fma(1.0, phi[4704], w);
+      w = fma(-1.0, phi[4224], w);
+      w = w - phi[4544];
+      w = w - phi[3552];
+      const double kw = ws[41024] * w;
+      out[4544] = fma(kw, y[3552], out[4544]);
+      out[3552] = fma(kw, y[4544], out[3552]);
+      ws[177504] = fma(kw * y[4544], y[3552], ws[177504]);
+    }
+    {
+      double w = 0.3 * phi[3968];
+      w = fma(0.7, phi[3232], w);
+      w = fma(0.45, phi[4128], w);
+      w = fma(0.55, phi[4064], w);
+      w = fma(0.3, phi[3552], w);
+      w = fma(0.3, phi[4224], w);
+      w = fma(1.7, phi[4352], w);
+      w = fma(1.0, phi[4704], w);
+      w = w - phi[4544];
+      w = w - phi[3136];
+      const double kw = ws[41056] * w;
+      out[4544] = fma(kw, y[3136], out[4544]);
+      out[3136] = fma(kw, y[4544], out[3136]);
+      ws[177536] = fma(kw * y[4544], y[3136], ws[177536]);
+    }
+    {
+      double w = 1.0 * phi[3232];
+      w = fma(1.0, phi[3872], w);
+      w = fma(0.96, phi[4576], w);
+      w = fma(0.04, phi[4288], w);
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[4544];
+      w = w - phi[2528];
+      const double kw = ws[41088] * w;
+      out[4544] = fma(kw, y[2528], out[4544]);
+      out[2528] = fma(kw, y[4544], out[2528]);
+      ws[177568] = fma(kw * y[4544], y[2528], ws[177568]);
+    }
+    {
+      double w = 1.0 * phi[3968];
+      w = fma(1.0, phi[4704], w);
+      w = fma(1.0, phi[4480], w);
+      w = w - phi[4544];
+      w = w - phi[4512];
+      const double kw = ws[41120] * w;
+      out[4544] = fma(kw, y[4512], out[4544]);
+      out[4512] = fma(kw, y[4544], out[4512]);
+      ws[177600] = fma(kw * y[4544], y[4512], ws[177600]);
+    }
+    {
+      double w = 1.0 * phi[3968];
+      w = fma(1.0, phi[4448], w);
+      w = w - phi[4544];
+      w = w - phi[4128];
+      const double kw = ws[41152] * w;
+      out[4544] = fma(kw, y[4128], out[4544]);
+      out[4128] = fma(kw, y[4544], out[4128]);
+      ws[177632] = fma(kw * y[4544], y[4128], ws[177632]);
+    }
+    {
+      double w = 1.0 * phi[3968];
+      w = fma(1.0, phi[4096], w);
+      w = w - phi[4544];
+      w = w - phi[4064];
+      const double kw = ws[41184] * w;
+      out[4544] = fma(kw, y[4064], out[4544]);
+      out[4064] = fma(kw, y[4544], out[4064]);
+      ws[177664] = fma(kw * y[4544], y[4064], ws[177664]);
+    }
+    {
+      double w = 1.0 * phi[3968];
+      w = fma(1.0, phi[4704], w);
+      w = fma(1.0, phi[4512], w);
+      w = w - phi[4544];
+      w = w - phi[2720];
+      const double kw = ws[41216] * w;
+      out[4544] = fma(kw, y[2720], out[4544]);
+      out[2720] = fma(kw, y[4544], out[2720]);
+      ws[177696] = fma(kw * y[4544], y[2720], ws[177696]);
+    }
+    {
+      double w = 1.0 * phi[3968];
+      w = fma(1.0, phi[4704], w);
+      w = fma(1.0, phi[4128], w);
+      w = w - phi[4544];
+      w = w - phi[864];
+      const double kw = ws[41248] * w;
+      out[4544] = fma(kw, y[864], out[4544]);
+      out[864] = fma(kw, y[4544], out[864]);
+      ws[177728] = fma(kw * y[4544], y[864], ws[177728]);
+    }
+    {
+      double w = 1.0 * phi[4544];
+      w = w - phi[3968];
+      w = w - phi[4736];
+      const double kw = ws[41280] * w;
+      out[3968] = fma(kw, y[4736], out[3968]);
+      out[4736] = fma(kw, y[3968], out[4736]);
+      ws[177760] = fma(kw * y[3968], y[4736], ws[177760]);
+    }
+    {
+      double w = 1.0 * phi[3968];
+      w = fma(0.18, phi[3616], w);
+      w = fma(0.65, phi[3488], w);
+      w = fma(0.72, phi[4672], w);
+      w = fma(0.1, phi[3936], w);
+      w = fma(0.1, phi[4736], w);
+      w = fma(0.07, phi[4576], w);
+      w = fma(0.18, phi[4704], w);
+      w = fma(1.0, phi[2944], w);
+      w = w - phi[4544];
+      w = w - phi[1088];
+      const double kw = ws[41312] * w;
+      out[4544] = fma(kw, y[1088], out[4544]);
+      out[1088] = fma(kw, y[4544], out[1088]);
+      ws[177792] = fma(kw * y[4544], y[1088], ws[177792]);
+    }
+    {
+      double w = 1.0 * phi[3968];
+      w = fma(0.155, phi[3616], w);
+      w = fma(0.544, phi[3584], w);
+      w = fma(0.602, phi[4672], w);
+      w = fma(0.244, phi[3808], w);
+      w = fma(0.244, phi[4736], w);
+      w = fma(0.058, phi[4576], w);
+      w = fma(0.155, phi[4704], w);
+      w = fma(1.0, phi[2496], w);
+      w = w - phi[4544];
+      w = w - phi[1120];
+      const double kw = ws[41344] * w;
+      out[4544] = fma(kw, y[1120], out[4544]);
+      out[1120] = fma(kw, y[4544], out[1120]);
+      ws[177824] = fma(kw * y[4544], y[1120], ws[177824]);
+    }
+    {
+      double w = 1.0 * phi[3968];
+      w = fma(0.155, phi[3616], w);
+      w = fma(0.544, phi[3584], w);
+      w = fma(0.602, phi[4672], w);
+      w = fma(0.244, phi[3808], w);
+      w = fma(0.244, phi[4736], w);
+      w = fma(0.058, phi[4576], w);
+      w = fma(0.155, phi[4704], w);
+      w = fma(1.0, phi[2560], w);
+      w = w - phi[4544];
+      w = w - phi[1152];
+      const double kw = ws[41376] * w;
+      out[4544] = fma(kw, y[1152], out[4544]);
+      out[1152] = fma(kw, y[4544], out[1152]);
+      ws[177856] = fma(kw * y[4544], y[1152], ws[177856]);
+    }
+    {
+      double w = 1.0 * phi[4544];
+      w = fma(1.0, phi[4608], w);
+      w = w - phi[2592];
+      const double kw = ws[41408] * w;
+      out[2592] = out[2592] + kw;
+      ws[177888] = fma(kw, y[2592], ws[177888]);
+    }
+    {
+      double w = 1.0 * phi[1216];
+      w = w - phi[3520];
+      w = w - phi[4608];
+      const double kw = ws[41440] * w;
+      out[3520] = fma(kw, y[4608], out[3520]);
+      out[4608] = fma(kw, y[3520], out[4608]);
+      ws[177920] = fma(kw * y[3520], y[4608], ws[177920]);
+    }
+    {
+      double w = 1.0 * phi[3520];
+      w = fma(1.0, phi[4608], w);
+      w = w - phi[1216];
+      const double kw = ws[41472] * w;
+      out[1216] = out[1216] + kw;
+      ws[177952] = fma(kw, y[1216], ws[177952]);
+    }
+    {
+      double w = 1.0 * phi[4544];
+      w = fma(1.0, phi[4640], w);
+      w = w - phi[1216];
+      const double kw = ws[41504] * w;
+      out[1216] = out[1216] + kw;
+      ws[177984] = fma(kw, y[1216], ws[177984]);
+    }
+    {
+      double w = 1.0 * phi[1824];
+      w = fma(1.0, phi[4192], w);
+      w = w - phi[1216];
+      const double kw = ws[41536] * w;
+      out[1216] = out[1216] + kw;
+      ws[178016] = fma(kw, y[1216], ws[178016]);
+    }
+    {
+      double w = 1.0 * phi[1824];
+      w = fma(1.0, phi[4192], w);
+      w = w - phi[1216];
+      const double kw = ws[41568] * w;
+      out[1216] = out[1216] + kw;
+      ws[178048] = fma(kw, y[1216], ws[178048]);
+    }
+    {
+      double w = 1.0 * phi[4384];
+      w = fma(0.016, phi[3264], w);
+      w = fma(0.051, phi[2624], w);
+      w = fma(0.047, phi[3072], w);
+      w = w - phi[2944];
+      w = w - phi[4384];
+      const double kw = ws[41600] * w;
+      out[2944] = fma(kw, y[4384], out[2944]);
+      out[4384] = fma(kw, y[2944], out[4384]);
+      ws[178080] = fma(kw * y[2944], y[4384], ws[178080]);
+    }
+    {
+      double w = 1.0 * phi[4704];
+      w = fma(0.14, phi[2240], w);
+      w = w - phi[2944];
+      w = w - phi[4704];
+      const double kw = ws[41632] * w;
+      out[2944] = fma(kw, y[4704], out[2944]);
+      out[4704] = fma(kw, y[2944], out[4704]);
+      ws[178112] = fma(kw * y[2944], y[4704], ws[178112]);
+    }
+    {
+      double w = 1.0 * phi[4384];
+      w = fma(0.015, phi[3264], w);
+      w = fma(0.023, phi[2624], w);
+      w = fma(0.06, phi[3072], w);
+      w = w - phi[2496];
+      w = w - phi[4384];
+      const double kw = ws[41664] * w;
+      out[2496] = fma(kw, y[4384], out[2496]);
+      out[4384] = fma(kw, y[2496], out[4384]);
+      ws[178144] = fma(kw * y[2496], y[4384], ws[178144]);
+    }
+    {
+      double w = 1.0 * phi[4704];
+      w = fma(0.193, phi[2240], w);
+      w = w - phi[2496];
+      w = w - phi[4704];
+      const double kw = ws[41696] * w;
+      out[2496] = fma(kw, y[4704], out[2496]);
+      out[4704] = fma(kw, y[2496], out[4704]);
+      ws[178176] = fma(kw * y[2496], y[4704], ws[178176]);
+    }
+    {
+      double w = 1.0 * phi[4384];
+      w = fma(0.034, phi[3264], w);
+      w = fma(0.392, phi[3072], w);
+      w = w - phi[2144];
+      w = w - phi[4384];
+      const double kw = ws[41728] * w;
+      out[2144] = fma(kw, y[4384], out[2144]);
+      out[4384] = fma(kw, y[2144], out[4384]);
+      ws[178208] = fma(kw * y[2144], y[4384], ws[178208]);
+    }
+    {
+      double w = 1.0 * phi[4704];
+      w = fma(0.146, phi[2240], w);
+      w = w - phi[2144];
+      w = w - phi[4704];
+      const double kw = ws[41760] * w;
+      out[2144] = fma(kw, y[4704], out[2144]);
+      out[4704] = fma(kw, y[2144], out[4704]);
+      ws[178240] = fma(kw * y[2144], y[4704], ws[178240]);
+    }
+    {
+      double w = 1.0 * phi[4320];
+      w = fma(1.0, phi[1888], w);
+      w = w - phi[1856];
+      w = w - phi[4320];
+      const double kw = ws[41792] * w;
+      out[1856] = fma(kw, y[4320], out[1856]);
+      out[4320] = fma(kw, y[1856], out[4320]);
+      ws[178272] = fma(kw * y[1856], y[4320], ws[178272]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = fma(1.0, phi[1888], w);
+      w = w - phi[1856];
+      w = w - phi[4736];
+      const double kw = ws[41824] * w;
+      out[1856] = fma(kw, y[4736], out[1856]);
+      out[4736] = fma(kw, y[1856], out[4736]);
+      ws[178304] = fma(kw * y[1856], y[4736], ws[178304]);
+    }
+    {
+      double w = 1.0 * phi[4640];
+      w = fma(1.0, phi[1888], w);
+      w = w - phi[1856];
+      w = w - phi[4640];
+      const double kw = ws[41856] * w;
+      out[1856] = fma(kw, y[4640], out[1856]);
+      out[4640] = fma(kw, y[1856], out[4640]);
+      ws[178336] = fma(kw * y[1856], y[4640], ws[178336]);
+    }
+    {
+      double w = 1.0 * phi[4384];
+      w = fma(0.028, phi[3264], w);
+      w = fma(0.225, phi[2624], w);
+      w = fma(0.191, phi[3072], w);
+      w = w - phi[2560];
+      w = w - phi[4384];
+      const double kw = ws[41888] * w;
+      out[2560] = fma(kw, y[4384], out[2560]);
+      out[4384] = fma(kw, y[2560], out[4384]);
+      ws[178368] = fma(kw * y[2560], y[4384], ws[178368]);
+    }
+}
+__device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int phioff, int outoff)
+{
+    const double* __restrict__ y = ws + yoff * 32;
+    const double* __restrict__ phi = ws + phioff * 32;
+    double* __restrict__ out = ws + outoff * 32;
+    {
+      double w = 1.0 * phi[4704];
+      w = fma(0.473, phi[2240], w);
+      w = w - phi[2560];
+      w = w - phi[4704];
+      const double kw = ws[41920] * w;
+      out[2560] = fma(kw, y[4704], out[2560]);
+      out[4704] = fma(kw, y[2560], out[4704]);
+      ws[178400] = fma(kw * y[2560], y[4704], ws[178400]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = fma(0.006, phi[3264], w);
+      w = fma(0.052, phi[2624], w);
+      w = fma(0.081, phi[3072], w);
+      w = w - phi[448];
+      w = w - phi[4736];
+      const double kw = ws[41952] * w;
+      out[448] = fma(kw, y[4736], out[448]);
+      out[4736] = fma(kw, y[448], out[4736]);
+      ws[178432] = fma(kw * y[448], y[4736], ws[178432]);
+    }
+    {
+      double w = 1.0 * phi[4192];
+      w = w - phi[4032];
+      const double kw = ws[41984] * w;
+      out[4032] = out[4032] + kw;
+      ws[178464] = fma(kw, y[4032], ws[178464]);
+    }
+    {
+      double w = 1.0 * phi[4192];
+      w = fma(1.0, phi[1920], w);
+      w = w - phi[1280];
+      const double kw = ws[42016] * w;
+      out[1280] = out[1280] + kw;
+      ws[178496] = fma(kw, y[1280], ws[178496]);
+    }
+    {
+      double w = 1.0 * phi[4192];
+      w = fma(1.0, phi[1248], w);
+      w = w - phi[1280];
+      const double kw = ws[42048] * w;
+      out[1280] = out[1280] + kw;
+      ws[178528] = fma(kw, y[1280], ws[178528]);
+    }
+    {
+      double w = 1.0 * phi[4192];
+      w = w - phi[1920];
+      const double kw = ws[42080] * w;
+      out[1920] = out[1920] + kw;
+      ws[178560] = fma(kw, y[1920], ws[178560]);
+    }
+    {
+      double w = 1.0 * phi[4192];
+      w = w - phi[1248];
+      const double kw = ws[42112] * w;
+      out[1248] = out[1248] + kw;
+      ws[178592] = fma(kw, y[1248], ws[178592]);
+    }
+    {
+      double w = 1.0 * phi[2592];
+      w = w - phi[1920];
+      w = w - phi[480];
+      const double kw = ws[42144] * w;
+      out[1920] = fma(kw, y[480], out[1920]);
+      out[480] = fma(kw, y[1920], out[480]);
+      ws[178624] = fma(kw * y[1920], y[480], ws[178624]);
+    }
+    {
+      double w = 1.0 * phi[2592];
+      w = w - phi[1920];
+      w = w - phi[512];
+      const double kw = ws[42176] * w;
+      out[1920] = fma(kw, y[512], out[1920]);
+      out[512] = fma(kw, y[1920], out[512]);
+      ws[178656] = fma(kw * y[1920], y[512], ws[178656]);
+    }
+    {
+      double w = 1.0 * phi[2592];
+      w = w - phi[1248];
+      w = w - phi[544];
+      const double kw = ws[42208] * w;
+      out[1248] = fma(kw, y[544], out[1248]);
+      out[544] = fma(kw, y[1248], out[544]);
+      ws[178688] = fma(kw * y[1248], y[544], ws[178688]);
+    }
+    {
+      double w = 0.5 * phi[2464];
+      w = fma(0.5, phi[4192], w);
+      w = w - phi[4608];
+      const double kw = ws[42240] * w;
+      out[4608] = out[4608] + kw;
+      ws[178720] = fma(kw, y[4608], ws[178720]);
+    }
+    {
+      double w = -phi[4320];
+      const double kw = ws[42272] * w;
+      out[4320] = out[4320] + kw;
+      ws[178752] = fma(kw, y[4320], ws[178752]);
+    }
+    {
+      double w = 1.0 * phi[1312];
+      w = w - phi[1056];
+      const double kw = ws[42304] * w;
+      out[1056] = out[1056] + kw;
+      ws[178784] = fma(kw, y[1056], ws[178784]);
+    }
+    {
+      double w = 1.0 * phi[608];
+      w = w - phi[1312];
+      w = w - phi[576];
+      const double kw = ws[42336] * w;
+      out[1312] = fma(kw, y[576], out[1312]);
+      out[576] = fma(kw, y[1312], out[576]);
+      ws[178816] = fma(kw * y[1312], y[576], ws[178816]);
+    }
+    {
+      double w = 1.0 * phi[608];
+      w = w - phi[1312];
+      const double kw = ws[42368] * w;
+      out[1312] = out[1312] + kw;
+      ws[178848] = fma(kw, y[1312], ws[178848]);
+    }
+    {
+      double w = 1.0 * phi[640];
+      w = w - phi[4256];
+      const double kw = ws[42400] * w;
+      out[4256] = out[4256] + kw;
+      ws[178880] = fma(kw, y[4256], ws[178880]);
+    }
+    {
+      double w = 1.0 * phi[640];
+      w = w - phi[4000];
+      const double kw = ws[42432] * w;
+      out[4000] = out[4000] + kw;
+      ws[178912] = fma(kw, y[4000], ws[178912]);
+    }
+    {
+      double w = 1.0 * phi[4384];
+      w = fma(0.688, phi[3360], w);
+      w = w - phi[2848];
+      w = w - phi[4384];
+      const double kw = ws[42464] * w;
+      out[2848] = fma(kw, y[4384], out[2848]);
+      out[4384] = fma(kw, y[2848], out[4384]);
+      ws[178944] = fma(kw * y[2848], y[4384], ws[178944]);
+    }
+    {
+      double w = 1.0 * phi[4704];
+      w = fma(1.0, phi[3360], w);
+      w = w - phi[2848];
+      w = w - phi[4704];
+      const double kw = ws[42496] * w;
+      out[2848] = fma(kw, y[4704], out[2848]);
+      out[4704] = fma(kw, y[2848], out[4704]);
+      ws[178976] = fma(kw * y[2848], y[4704], ws[178976]);
+    }
+    {
+      double w = 1.0 * phi[4640];
+      w = fma(0.422, phi[3360], w);
+      w = w - phi[2848];
+      w = w - phi[4640];
+      const double kw = ws[42528] * w;
+      out[2848] = fma(kw, y[4640], out[2848]);
+      out[4640] = fma(kw, y[2848], out[4640]);
+      ws[179008] = fma(kw * y[2848], y[4640], ws[179008]);
+    }
+    {
+      double w = 1.0 * phi[4672];
+      w = fma(0.711, phi[3360], w);
+      w = w - phi[2848];
+      w = w - phi[4672];
+      const double kw = ws[42560] * w;
+      out[2848] = fma(kw, y[4672], out[2848]);
+      out[4672] = fma(kw, y[2848], out[4672]);
+      ws[179040] = fma(kw * y[2848], y[4672], ws[179040]);
+    }
+    {
+      double w = 1.0 * phi[4544];
+      w = fma(0.37, phi[3360], w);
+      w = w - phi[3360];
+      w = w - phi[4544];
+      const double kw = ws[42592] * w;
+      out[3360] = fma(kw, y[4544], out[3360]);
+      out[4544] = fma(kw, y[3360], out[4544]);
+      ws[179072] = fma(kw * y[3360], y[4544], ws[179072]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = fma(0.24, phi[3360], w);
+      w = w - phi[3360];
+      w = w - phi[4736];
+      const double kw = ws[42624] * w;
+      out[3360] = fma(kw, y[4736], out[3360]);
+      out[4736] = fma(kw, y[3360], out[4736]);
+      ws[179104] = fma(kw * y[3360], y[4736], ws[179104]);
+    }
+    {
+      double w = -phi[3360];
+      const double kw = ws[42656] * w;
+      out[3360] = out[3360] + kw;
+      ws[179136] = fma(kw, y[3360], ws[179136]);
+    }
+    {
+      double w = 1.0 * phi[32];
+      w = w - phi[0];
+      const double kw = ws[42688] * w;
+      out[0] = out[0] + kw;
+      ws[179168] = fma(kw, y[0], ws[179168]);
+    }
+    {
+      double w = 0.907 * phi[1376];
+      w = w - phi[64];
+      const double kw = ws[42720] * w;
+      out[64] = out[64] + kw;
+      ws[179200] = fma(kw, y[64], ws[179200]);
+    }
+    {
+      double w = 0.925 * phi[1376];
+      w = w - phi[96];
+      const double kw = ws[42752] * w;
+      out[96] = out[96] + kw;
+      ws[179232] = fma(kw, y[96], ws[179232]);
+    }
+    {
+      double w = 0.943 * phi[1376];
+      w = w - phi[128];
+      const double kw = ws[42784] * w;
+      out[128] = out[128] + kw;
+      ws[179264] = fma(kw, y[128], ws[179264]);
+    }
+    {
+      double w = 0.5 * phi[1408];
+      w = w - phi[160];
+      const double kw = ws[42816] * w;
+      out[160] = out[160] + kw;
+      ws[179296] = fma(kw, y[160], ws[179296]);
+    }
+    {
+      double w = 0.5 * phi[1408];
+      w = w - phi[192];
+      const double kw = ws[42848] * w;
+      out[192] = out[192] + kw;
+      ws[179328] = fma(kw, y[192], ws[179328]);
+    }
+    {
+      double w = 1.5 * phi[1408];
+      w = w - phi[224];
+      const double kw = ws[42880] * w;
+      out[224] = out[224] + kw;
+      ws[179360] = fma(kw, y[224], ws[179360]);
+    }
+    {
+      double w = 1.25 * phi[1440];
+      w = fma(1.0, phi[704], w);
+      w = fma(1.0, phi[4736], w);
+      w = w - phi[704];
+      w = w - phi[4736];
+      const double kw = ws[42912] * w;
+      out[704] = fma(kw, y[4736], out[704]);
+      out[4736] = fma(kw, y[704], out[4736]);
+      ws[179392] = fma(kw * y[704], y[4736], ws[179392]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = w - phi[1440];
+      w = w - phi[4736];
+      const double kw = ws[42944] * w;
+      out[1440] = fma(kw, y[4736], out[1440]);
+      out[4736] = fma(kw, y[1440], out[4736]);
+      ws[179424] = fma(kw * y[1440], y[4736], ws[179424]);
+    }
+    {
+      double w = 1.25 * phi[1472];
+      w = fma(1.0, phi[736], w);
+      w = fma(1.0, phi[4736], w);
+      w = w - phi[736];
+      w = w - phi[4736];
+      const double kw = ws[42976] * w;
+      out[736] = fma(kw, y[4736], out[736]);
+      out[4736] = fma(kw, y[736], out[4736]);
+      ws[179456] = fma(kw * y[736], y[4736], ws[179456]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = w - phi[1472];
+      w = w - phi[4736];
+      const double kw = ws[43008] * w;
+      out[1472] = fma(kw, y[4736], out[1472]);
+      out[4736] = fma(kw, y[1472], out[4736]);
+      ws[179488] = fma(kw * y[1472], y[4736], ws[179488]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = fma(1.0, phi[800], w);
+      w = w - phi[768];
+      w = w - phi[4736];
+      const double kw = ws[43040] * w;
+      out[768] = fma(kw, y[4736], out[768]);
+      out[4736] = fma(kw, y[768], out[4736]);
+      ws[179520] = fma(kw * y[768], y[4736], ws[179520]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = fma(0.4857, phi[2752], w);
+      w = fma(0.0062, phi[2784], w);
+      w = fma(0.0025, phi[2816], w);
+      w = fma(0.0026, phi[2304], w);
+      w = fma(0.0023, phi[1504], w);
+      w = fma(0.2944, phi[3680], w);
+      w = fma(0.2021, phi[3712], w);
+      w = fma(0.0019, phi[3168], w);
+      w = fma(0.0023, phi[3200], w);
+      w = w - phi[2752];
+      w = w - phi[4736];
+      const double kw = ws[43072] * w;
+      out[2752] = fma(kw, y[4736], out[2752]);
+      out[4736] = fma(kw, y[2752], out[4736]);
+      ws[179552] = fma(kw * y[2752], y[4736], ws[179552]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = fma(0.3003, phi[2752], w);
+      w = fma(0.2862, phi[2784], w);
+      w = fma(0.0041, phi[2816], w);
+      w = fma(0.0035, phi[2304], w);
+      w = fma(0.2239, phi[3680], w);
+      w = fma(0.182, phi[3712], w);
+      w = w - phi[2784];
+      w = w - phi[4736];
+      const double kw = ws[43104] * w;
+      out[2784] = fma(kw, y[4736], out[2784]);
+      out[4736] = fma(kw, y[2784], out[4736]);
+      ws[179584] = fma(kw * y[2784], y[4736], ws[179584]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = fma(0.3856, phi[2752], w);
+      w = fma(0.095, phi[2784], w);
+      w = fma(0.1373, phi[2816], w);
+      w = fma(0.0005, phi[2304], w);
+      w = fma(0.2051, phi[3680], w);
+      w = fma(0.1764, phi[3712], w);
+      w = w - phi[2816];
+      w = w - phi[4736];
+      const double kw = ws[43136] * w;
+      out[2816] = fma(kw, y[4736], out[2816]);
+      out[4736] = fma(kw, y[2816], out[4736]);
+      ws[179616] = fma(kw * y[2816], y[4736], ws[179616]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = fma(0.2181, phi[2752], w);
+      w = fma(0.3063, phi[2784], w);
+      w = fma(0.0153, phi[2816], w);
+      w = fma(0.1043, phi[2304], w);
+      w = fma(0.1893, phi[3680], w);
+      w = fma(0.1668, phi[3712], w);
+      w = w - phi[2304];
+      w = w - phi[4736];
+      const double kw = ws[43168] * w;
+      out[2304] = fma(kw, y[4736], out[2304]);
+      out[4736] = fma(kw, y[2304], out[4736]);
+      ws[179648] = fma(kw * y[2304], y[4736], ws[179648]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = fma(0.2412, phi[2752], w);
+      w = fma(0.2089, phi[2784], w);
+      w = fma(0.3, phi[2816], w);
+      w = fma(0.2028, phi[3680], w);
+      w = fma(0.0471, phi[3712], w);
+      w = w - phi[1504];
+      w = w - phi[4736];
+      const double kw = ws[43200] * w;
+      out[1504] = fma(kw, y[4736], out[1504]);
+      out[4736] = fma(kw, y[1504], out[4736]);
+      ws[179680] = fma(kw * y[1504], y[4736], ws[179680]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = fma(0.6664, phi[3680], w);
+      w = fma(0.0143, phi[3712], w);
+      w = fma(0.0123, phi[2912], w);
+      w = fma(0.1239, phi[3168], w);
+      w = fma(0.1831, phi[3200], w);
+      w = w - phi[3680];
+      w = w - phi[4736];
+      const double kw = ws[43232] * w;
+      out[3680] = fma(kw, y[4736], out[3680]);
+      out[4736] = fma(kw, y[3680], out[4736]);
+      ws[179712] = fma(kw * y[3680], y[4736], ws[179712]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = fma(0.2858, phi[3680], w);
+      w = fma(0.3931, phi[3712], w);
+      w = fma(0.0139, phi[2912], w);
+      w = fma(0.1027, phi[3168], w);
+      w = fma(0.2045, phi[3200], w);
+      w = w - phi[3712];
+      w = w - phi[4736];
+      const double kw = ws[43264] * w;
+      out[3712] = fma(kw, y[4736], out[3712]);
+      out[4736] = fma(kw, y[3712], out[4736]);
+      ws[179744] = fma(kw * y[3712], y[4736], ws[179744]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = fma(0.3303, phi[3680], w);
+      w = fma(0.2272, phi[3712], w);
+      w = fma(0.2607, phi[2912], w);
+      w = fma(0.0702, phi[3168], w);
+      w = fma(0.1116, phi[3200], w);
+      w = w - phi[2912];
+      w = w - phi[4736];
+      const double kw = ws[43296] * w;
+      out[2912] = fma(kw, y[4736], out[2912]);
+      out[4736] = fma(kw, y[2912], out[4736]);
+      ws[179776] = fma(kw * y[2912], y[4736], ws[179776]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = fma(0.3444, phi[3680], w);
+      w = fma(0.2749, phi[3712], w);
+      w = fma(0.0491, phi[2912], w);
+      w = fma(0.2577, phi[3168], w);
+      w = fma(0.0739, phi[3200], w);
+      w = w - phi[3168];
+      w = w - phi[4736];
+      const double kw = ws[43328] * w;
+      out[3168] = fma(kw, y[4736], out[3168]);
+      out[4736] = fma(kw, y[3168], out[4736]);
+      ws[179808] = fma(kw * y[3168], y[4736], ws[179808]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = fma(0.3886, phi[3680], w);
+      w = fma(0.2421, phi[3712], w);
+      w = fma(0.064, phi[2912], w);
+      w = fma(0.0385, phi[3168], w);
+      w = fma(0.2667, phi[3200], w);
+      w = w - phi[3200];
+      w = w - phi[4736];
+      const double kw = ws[43360] * w;
+      out[3200] = fma(kw, y[4736], out[3200]);
+      out[4736] = fma(kw, y[3200], out[4736]);
+      ws[179840] = fma(kw * y[3200], y[4736], ws[179840]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = w - phi[2336];
+      w = w - phi[4736];
+      const double kw = ws[43392] * w;
+      out[2336] = fma(kw, y[4736], out[2336]);
+      out[4736] = fma(kw, y[2336], out[4736]);
+      ws[179872] = fma(kw * y[2336], y[4736], ws[179872]);
+    }
+    {
+      double w = 1.0 * phi[4640];
+      w = w - phi[2336];
+      w = w - phi[4640];
+      const double kw = ws[43424] * w;
+      out[2336] = fma(kw, y[4640], out[2336]);
+      out[4640] = fma(kw, y[2336], out[4640]);
+      ws[179904] = fma(kw * y[2336], y[4640], ws[179904]);
+    }
+    {
+      double w = 1.0 * phi[4160];
+      w = w - phi[2336];
+      w = w - phi[4160];
+      const double kw = ws[43456] * w;
+      out[2336] = fma(kw, y[4160], out[2336]);
+      out[4160] = fma(kw, y[2336], out[4160]);
+      ws[179936] = fma(kw * y[2336], y[4160], ws[179936]);
+    }
+    {
+      double w = -phi[2336];
+      const double kw = ws[43488] * w;
+      out[2336] = out[2336] + kw;
+      ws[179968] = fma(kw, y[2336], ws[179968]);
+    }
+    {
+      double w = -phi[2336];
+      const double kw = ws[43520] * w;
+      out[2336] = out[2336] + kw;
+      ws[180000] = fma(kw, y[2336], ws[180000]);
+    }
+    {
+      double w = 1.0 * phi[4544];
+      w = w - phi[2336];
+      w = w - phi[4544];
+      const double kw = ws[43552] * w;
+      out[2336] = fma(kw, y[4544], out[2336]);
+      out[4544] = fma(kw, y[2336], out[4544]);
+      ws[180032] = fma(kw * y[2336], y[4544], ws[180032]);
+    }
+}
+__device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int phioff, int outoff)
+{
+    const double* __restrict__ y = ws + yoff * 32;
+    const double* __restrict__ phi = ws + phioff * 32;
+    double* __restrict__ out = ws + outoff * 32;
+    {
+      double w = 1.0 * phi[4736];
+      w = w - phi[2368];
+      w = w - phi[4736];
+      const double kw = ws[43584] * w;
+      out[2368] = fma(kw, y[4736], out[2368]);
+      out[4736] = fma(kw, y[2368], out[4736]);
+      ws[180064] = fma(kw * y[2368], y[4736], ws[180064]);
+    }
+    {
+      double w = 1.0 * phi[4640];
+      w = w - phi[2368];
+      w = w - phi[4640];
+      const double kw = ws[43616] * w;
+      out[2368] = fma(kw, y[4640], out[2368]);
+      out[4640] = fma(kw, y[2368], out[4640]);
+      ws[180096] = fma(kw * y[2368], y[4640], ws[180096]);
+    }
+    {
+      double w = 1.0 * phi[4160];
+      w = w - phi[2368];
+      w = w - phi[4160];
+      const double kw = ws[43648] * w;
+      out[2368] = fma(kw, y[4160], out[2368]);
+      out[4160] = fma(kw, y[2368], out[4160]);
+      ws[180128] = fma(kw * y[2368], y[4160], ws[180128]);
+    }
+    {
+      double w = -phi[2368];
+      const double kw = ws[43680] * w;
+      out[2368] = out[2368] + kw;
+      ws[180160] = fma(kw, y[2368], ws[180160]);
+    }
+    {
+      double w = 1.0 * phi[4544];
+      w = w - phi[2368];
+      w = w - phi[4544];
+      const double kw = ws[43712] * w;
+      out[2368] = fma(kw, y[4544], out[2368]);
+      out[4544] = fma(kw, y[2368], out[4544]);
+      ws[180192] = fma(kw * y[2368], y[4544], ws[180192]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = fma(0.58, phi[2976], w);
+      w = w - phi[2400];
+      w = w - phi[4736];
+      const double kw = ws[43744] * w;
+      out[2400] = fma(kw, y[4736], out[2400]);
+      out[4736] = fma(kw, y[2400], out[4736]);
+      ws[180224] = fma(kw * y[2400], y[4736], ws[180224]);
+    }
+    {
+      double w = 1.0 * phi[4320];
+      w = fma(0.52, phi[2976], w);
+      w = w - phi[2400];
+      w = w - phi[4320];
+      const double kw = ws[43776] * w;
+      out[2400] = fma(kw, y[4320], out[2400]);
+      out[4320] = fma(kw, y[2400], out[4320]);
+      ws[180256] = fma(kw * y[2400], y[4320], ws[180256]);
+    }
+    {
+      double w = 1.0 * phi[4640];
+      w = fma(0.045, phi[2976], w);
+      w = w - phi[2400];
+      w = w - phi[4640];
+      const double kw = ws[43808] * w;
+      out[2400] = fma(kw, y[4640], out[2400]);
+      out[4640] = fma(kw, y[2400], out[4640]);
+      ws[180288] = fma(kw * y[2400], y[4640], ws[180288]);
+    }
+    {
+      double w = 1.0 * phi[4544];
+      w = fma(0.58, phi[2976], w);
+      w = w - phi[2400];
+      w = w - phi[4544];
+      const double kw = ws[43840] * w;
+      out[2400] = fma(kw, y[4544], out[2400]);
+      out[4544] = fma(kw, y[2400], out[4544]);
+      ws[180320] = fma(kw * y[2400], y[4544], ws[180320]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = w - phi[2432];
+      w = w - phi[4736];
+      const double kw = ws[43872] * w;
+      out[2432] = fma(kw, y[4736], out[2432]);
+      out[4736] = fma(kw, y[2432], out[4736]);
+      ws[180352] = fma(kw * y[2432], y[4736], ws[180352]);
+    }
+    {
+      double w = 1.0 * phi[4320];
+      w = w - phi[2432];
+      w = w - phi[4320];
+      const double kw = ws[43904] * w;
+      out[2432] = fma(kw, y[4320], out[2432]);
+      out[4320] = fma(kw, y[2432], out[4320]);
+      ws[180384] = fma(kw * y[2432], y[4320], ws[180384]);
+    }
+    {
+      double w = 1.0 * phi[4640];
+      w = w - phi[2432];
+      w = w - phi[4640];
+      const double kw = ws[43936] * w;
+      out[2432] = fma(kw, y[4640], out[2432]);
+      out[4640] = fma(kw, y[2432], out[4640]);
+      ws[180416] = fma(kw * y[2432], y[4640], ws[180416]);
+    }
+    {
+      double w = -phi[2432];
+      const double kw = ws[43968] * w;
+      out[2432] = out[2432] + kw;
+      ws[180448] = fma(kw, y[2432], ws[180448]);
+    }
+    {
+      double w = 1.0 * phi[4544];
+      w = w - phi[2432];
+      w = w - phi[4544];
+      const double kw = ws[44000] * w;
+      out[2432] = fma(kw, y[4544], out[2432]);
+      out[4544] = fma(kw, y[2432], out[4544]);
+      ws[180480] = fma(kw * y[2432], y[4544], ws[180480]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = w - phi[2976];
+      w = w - phi[4736];
+      const double kw = ws[44032] * w;
+      out[2976] = fma(kw, y[4736], out[2976]);
+      out[4736] = fma(kw, y[2976], out[4736]);
+      ws[180512] = fma(kw * y[2976], y[4736], ws[180512]);
+    }
+    {
+      double w = 1.0 * phi[4320];
+      w = w - phi[2976];
+      w = w - phi[4320];
+      const double kw = ws[44064] * w;
+      out[2976] = fma(kw, y[4320], out[2976]);
+      out[4320] = fma(kw, y[2976], out[4320]);
+      ws[180544] = fma(kw * y[2976], y[4320], ws[180544]);
+    }
+    {
+      double w = 1.0 * phi[4640];
+      w = w - phi[2976];
+      w = w - phi[4640];
+      const double kw = ws[44096] * w;
+      out[2976] = fma(kw, y[4640], out[2976]);
+      out[4640] = fma(kw, y[2976], out[4640]);
+      ws[180576] = fma(kw * y[2976], y[4640], ws[180576]);
+    }
+    {
+      double w = -phi[2976];
+      const double kw = ws[44128] * w;
+      out[2976] = out[2976] + kw;
+      ws[180608] = fma(kw, y[2976], ws[180608]);
+    }
+    {
+      double w = 1.0 * phi[4544];
+      w = w - phi[2976];
+      w = w - phi[4544];
+      const double kw = ws[44160] * w;
+      out[2976] = fma(kw, y[4544], out[2976]);
+      out[4544] = fma(kw, y[2976], out[4544]);
+      ws[180640] = fma(kw * y[2976], y[4544], ws[180640]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = w - phi[1536];
+      w = w - phi[4736];
+      const double kw = ws[44192] * w;
+      out[1536] = fma(kw, y[4736], out[1536]);
+      out[4736] = fma(kw, y[1536], out[4736]);
+      ws[180672] = fma(kw * y[1536], y[4736], ws[180672]);
+    }
+    {
+      double w = 1.0 * phi[4544];
+      w = w - phi[1536];
+      w = w - phi[4544];
+      const double kw = ws[44224] * w;
+      out[1536] = fma(kw, y[4544], out[1536]);
+      out[4544] = fma(kw, y[1536], out[4544]);
+      ws[180704] = fma(kw * y[1536], y[4544], ws[180704]);
+    }
+    {
+      double w = 0.5 * phi[1568];
+      w = fma(0.5, phi[3040], w);
+      w = fma(1.0, phi[4320], w);
+      w = w - phi[3008];
+      w = w - phi[4320];
+      const double kw = ws[44256] * w;
+      out[3008] = fma(kw, y[4320], out[3008]);
+      out[4320] = fma(kw, y[3008], out[4320]);
+      ws[180736] = fma(kw * y[3008], y[4320], ws[180736]);
+    }
+    {
+      double w = 1.0 * phi[3040];
+      w = fma(1.0, phi[1184], w);
+      w = w - phi[3008];
+      w = w - phi[1184];
+      const double kw = ws[44288] * w;
+      out[3008] = fma(kw, y[1184], out[3008]);
+      out[1184] = fma(kw, y[3008], out[1184]);
+      ws[180768] = fma(kw * y[3008], y[1184], ws[180768]);
+    }
+    {
+      double w = 1.0 * phi[3040];
+      w = fma(1.0, phi[3456], w);
+      w = w - phi[3008];
+      w = w - phi[3456];
+      const double kw = ws[44320] * w;
+      out[3008] = fma(kw, y[3456], out[3008]);
+      out[3456] = fma(kw, y[3008], out[3456]);
+      ws[180800] = fma(kw * y[3008], y[3456], ws[180800]);
+    }
+    {
+      double w = 0.5 * phi[1568];
+      w = fma(0.5, phi[3040], w);
+      w = fma(1.0, phi[4736], w);
+      w = w - phi[3008];
+      w = w - phi[4736];
+      const double kw = ws[44352] * w;
+      out[3008] = fma(kw, y[4736], out[3008]);
+      out[4736] = fma(kw, y[3008], out[4736]);
+      ws[180832] = fma(kw * y[3008], y[4736], ws[180832]);
+    }
+    {
+      double w = 0.5 * phi[3008];
+      w = fma(0.5, phi[3040], w);
+      w = fma(1.0, phi[4544], w);
+      w = w - phi[3008];
+      w = w - phi[4544];
+      const double kw = ws[44384] * w;
+      out[3008] = fma(kw, y[4544], out[3008]);
+      out[4544] = fma(kw, y[3008], out[4544]);
+      ws[180864] = fma(kw * y[3008], y[4544], ws[180864]);
+    }
+    {
+      double w = 1.0 * phi[2208];
+      w = fma(1.0, phi[4416], w);
+      w = fma(1.0, phi[4512], w);
+      w = w - phi[2016];
+      w = w - phi[4736];
+      const double kw = ws[44416] * w;
+      out[2016] = fma(kw, y[4736], out[2016]);
+      out[4736] = fma(kw, y[2016], out[4736]);
+      ws[180896] = fma(kw * y[2016], y[4736], ws[180896]);
+    }
+    {
+      double w = 0.75 * phi[2208];
+      w = fma(0.25, phi[1600], w);
+      w = fma(1.0, phi[4416], w);
+      w = w - phi[2016];
+      w = w - phi[4736];
+      const double kw = ws[44448] * w;
+      out[2016] = fma(kw, y[4736], out[2016]);
+      out[4736] = fma(kw, y[2016], out[4736]);
+      ws[180928] = fma(kw * y[2016], y[4736], ws[180928]);
+    }
+    {
+      double w = 1.0 * phi[2208];
+      w = fma(1.0, phi[4192], w);
+      w = fma(1.0, phi[4416], w);
+      w = fma(1.0, phi[4512], w);
+      w = w - phi[2016];
+      w = w - phi[4640];
+      const double kw = ws[44480] * w;
+      out[2016] = fma(kw, y[4640], out[2016]);
+      out[4640] = fma(kw, y[2016], out[4640]);
+      ws[180960] = fma(kw * y[2016], y[4640], ws[180960]);
+    }
+    {
+      double w = 0.86 * phi[2208];
+      w = fma(1.0, phi[4416], w);
+      w = fma(0.45, phi[4512], w);
+      w = fma(0.45, phi[3968], w);
+      w = fma(0.14, phi[1600], w);
+      w = fma(0.55, phi[3520], w);
+      w = w - phi[2016];
+      w = w - phi[4544];
+      const double kw = ws[44512] * w;
+      out[2016] = fma(kw, y[4544], out[2016]);
+      out[4544] = fma(kw, y[2016], out[4544]);
+      ws[180992] = fma(kw * y[2016], y[4544], ws[180992]);
+    }
+}
+}  // namespace mech_cb6r5_ae7_aq

@@ -1,0 +1,2016 @@
+// Generated by cmaq_gb300.mechgen.generate from CCTM/src/MECHS/cb6r5_ae7_aq/RXNS_DATA_MODULE.F90
+// and RXNS_FUNC_MODULE.F90 (sha256/16 4242f44b2527a299).  Do not edit.
+#include "cb6r5_ae7_aq_mech.cuh"
+#include <math.h>
+namespace mech_cb6r5_ae7_aq {
+__device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int phioff, int outoff)
+{
+    const double* __restrict__ y = ws + yoff * 32;
+    const double* __restrict__ phi = ws + phioff * 32;
+    double* __restrict__ out = ws + outoff * 32;
+    {
+      double w = 1.0 * phi[4320];
+      w = w - phi[4160];
+      const double kw = ws[33408] * w;
+      out[4160] = out[4160] + kw;
+      ws[169888] = fma(kw, y[4160], ws[169888]);
+    }
+    {
+      double w = 1.0 * phi[4608];
+      w = w - phi[4320];
+      w = w - phi[4384];
+      const double kw = ws[33440] * w;
+      out[4320] = fma(kw, y[4384], out[4320]);
+      out[4384] = fma(kw, y[4320], out[4384]);
+      ws[169920] = fma(kw * y[4320], y[4384], ws[169920]);
+    }
+    {
+      double w = 1.0 * phi[4608];
+      w = w - phi[4160];
+      w = w - phi[4384];
+      const double kw = ws[33472] * w;
+      out[4160] = fma(kw, y[4384], out[4160]);
+      out[4384] = fma(kw, y[4160], out[4384]);
+      ws[169952] = fma(kw * y[4160], y[4384], ws[169952]);
+    }
+    {
+      double w = 1.0 * phi[4384];
+      w = w - phi[4160];
+      w = w - phi[4608];
+      const double kw = ws[33504] * w;
+      out[4160] = fma(kw, y[4608], out[4160]);
+      out[4608] = fma(kw, y[4160], out[4608]);
+      ws[169984] = fma(kw * y[4160], y[4608], ws[169984]);
+    }
+    {
+      double w = 1.0 * phi[4640];
+      w = w - phi[4160];
+      w = w - phi[4608];
+      const double kw = ws[33536] * w;
+      out[4160] = fma(kw, y[4608], out[4160]);
+      out[4608] = fma(kw, y[4160], out[4608]);
+      ws[170016] = fma(kw * y[4160], y[4608], ws[170016]);
+    }
+    {
+      double w = -phi[4160];
+      w = w - phi[4320];
+      const double kw = ws[33568] * w;
+      out[4160] = fma(kw, y[4320], out[4160]);
+      out[4320] = fma(kw, y[4160], out[4320]);
+      ws[170048] = fma(kw * y[4160], y[4320], ws[170048]);
+    }
+    {
+      double w = 1.0 * phi[4160];
+      w = w - phi[672];
+      const double kw = ws[33664] * w;
+      out[672] = out[672] + kw;
+      ws[170144] = fma(kw, y[672], ws[170144]);
+    }
+    {
+      double w = 2.0 * phi[4736];
+      w = w - phi[672];
+      const double kw = ws[33696] * w;
+      out[672] = out[672] + kw;
+      ws[170176] = fma(kw, y[672], ws[170176]);
+    }
+    {
+      double w = 1.0 * phi[4704];
+      w = w - phi[4320];
+      w = w - phi[4736];
+      const double kw = ws[33728] * w;
+      out[4320] = fma(kw, y[4736], out[4320]);
+      out[4736] = fma(kw, y[4320], out[4736]);
+      ws[170208] = fma(kw * y[4320], y[4736], ws[170208]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = w - phi[4320];
+      w = w - phi[4704];
+      const double kw = ws[33760] * w;
+      out[4320] = fma(kw, y[4704], out[4320]);
+      out[4704] = fma(kw, y[4320], out[4704]);
+      ws[170240] = fma(kw * y[4320], y[4704], ws[170240]);
+    }
+    {
+      double w = 1.0 * phi[4704];
+      w = w - phi[4736];
+      w = w - phi[4160];
+      const double kw = ws[33792] * w;
+      out[4736] = fma(kw, y[4160], out[4736]);
+      out[4160] = fma(kw, y[4736], out[4160]);
+      ws[170272] = fma(kw * y[4736], y[4160], ws[170272]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = w - phi[4704];
+      w = w - phi[4160];
+      const double kw = ws[33824] * w;
+      out[4704] = fma(kw, y[4160], out[4704]);
+      out[4160] = fma(kw, y[4704], out[4160]);
+      ws[170304] = fma(kw * y[4704], y[4160], ws[170304]);
+    }
+    {
+      double w = 1.0 * phi[4160];
+      w = w - phi[4736];
+      w = w - phi[4736];
+      const double kw = ws[33856] * w;
+      out[4736] = fma(kw, y[4736], out[4736]);
+      out[4736] = fma(kw, y[4736], out[4736]);
+      ws[170336] = fma(kw * y[4736], y[4736], ws[170336]);
+    }
+    {
+      double w = 1.0 * phi[3456];
+      w = w - phi[4736];
+      w = w - phi[4736];
+      const double kw = ws[33888] * w;
+      out[4736] = fma(kw, y[4736], out[4736]);
+      out[4736] = fma(kw, y[4736], out[4736]);
+      ws[170368] = fma(kw * y[4736], y[4736], ws[170368]);
+    }
+    {
+      double w = -phi[4736];
+      w = w - phi[4704];
+      const double kw = ws[33920] * w;
+      out[4736] = fma(kw, y[4704], out[4736]);
+      out[4704] = fma(kw, y[4736], out[4704]);
+      ws[170400] = fma(kw * y[4736], y[4704], ws[170400]);
+    }
+    {
+      double w = 1.0 * phi[3456];
+      w = w - phi[4704];
+      w = w - phi[4704];
+      const double kw = ws[33952] * w;
+      out[4704] = fma(kw, y[4704], out[4704]);
+      out[4704] = fma(kw, y[4704], out[4704]);
+      ws[170432] = fma(kw * y[4704], y[4704], ws[170432]);
+    }
+    {
+      double w = 1.0 * phi[3456];
+      w = w - phi[4704];
+      w = w - phi[4704];
+      const double kw = ws[33984] * w;
+      out[4704] = fma(kw, y[4704], out[4704]);
+      out[4704] = fma(kw, y[4704], out[4704]);
+      ws[170464] = fma(kw * y[4704], y[4704], ws[170464]);
+    }
+    {
+      double w = 1.0 * phi[4704];
+      w = w - phi[3456];
+      w = w - phi[4736];
+      const double kw = ws[34048] * w;
+      out[3456] = fma(kw, y[4736], out[3456]);
+      out[4736] = fma(kw, y[3456], out[4736]);
+      ws[170528] = fma(kw * y[3456], y[4736], ws[170528]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = fma(1.0, phi[4704], w);
+      w = w - phi[3456];
+      w = w - phi[4160];
+      const double kw = ws[34080] * w;
+      out[3456] = fma(kw, y[4160], out[3456]);
+      out[4160] = fma(kw, y[3456], out[4160]);
+      ws[170560] = fma(kw * y[3456], y[4160], ws[170560]);
+    }
+    {
+      double w = 2.0 * phi[4608];
+      w = w - phi[4384];
+      w = w - phi[4384];
+      const double kw = ws[34112] * w;
+      out[4384] = fma(kw, y[4384], out[4384]);
+      out[4384] = fma(kw, y[4384], out[4384]);
+      ws[170592] = fma(kw * y[4384], y[4384], ws[170592]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = fma(1.0, phi[4608], w);
+      w = w - phi[4704];
+      w = w - phi[4384];
+      const double kw = ws[34144] * w;
+      out[4704] = fma(kw, y[4384], out[4704]);
+      out[4384] = fma(kw, y[4704], out[4384]);
+      ws[170624] = fma(kw * y[4704], y[4384], ws[170624]);
+    }
+    {
+      double w = 1.0 * phi[4640];
+      w = w - phi[4608];
+      w = w - phi[4320];
+      const double kw = ws[34176] * w;
+      out[4608] = fma(kw, y[4320], out[4608]);
+      out[4320] = fma(kw, y[4608], out[4320]);
+      ws[170656] = fma(kw * y[4608], y[4320], ws[170656]);
+    }
+    {
+      double w = 2.0 * phi[4608];
+      w = w - phi[4640];
+      w = w - phi[4384];
+      const double kw = ws[34272] * w;
+      out[4640] = fma(kw, y[4384], out[4640]);
+      out[4384] = fma(kw, y[4640], out[4384]);
+      ws[170752] = fma(kw * y[4640], y[4384], ws[170752]);
+    }
+    {
+      double w = 1.0 * phi[4384];
+      w = fma(1.0, phi[4608], w);
+      w = w - phi[4640];
+      w = w - phi[4608];
+      const double kw = ws[34304] * w;
+      out[4640] = fma(kw, y[4608], out[4640]);
+      out[4608] = fma(kw, y[4640], out[4608]);
+      ws[170784] = fma(kw * y[4640], y[4608], ws[170784]);
+    }
+    {
+      double w = 1.0 * phi[4608];
+      w = w - phi[4640];
+      w = w - phi[4160];
+      const double kw = ws[34336] * w;
+      out[4640] = fma(kw, y[4160], out[4640]);
+      out[4160] = fma(kw, y[4640], out[4160]);
+      ws[170816] = fma(kw * y[4640], y[4160], ws[170816]);
+    }
+    {
+      double w = 1.0 * phi[4704];
+      w = fma(1.0, phi[4608], w);
+      w = w - phi[4640];
+      w = w - phi[4736];
+      const double kw = ws[34368] * w;
+      out[4640] = fma(kw, y[4736], out[4640]);
+      out[4736] = fma(kw, y[4640], out[4736]);
+      ws[170848] = fma(kw * y[4640], y[4736], ws[170848]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = fma(1.0, phi[4608], w);
+      w = w - phi[4640];
+      w = w - phi[4704];
+      const double kw = ws[34400] * w;
+      out[4640] = fma(kw, y[4704], out[4640]);
+      out[4704] = fma(kw, y[4640], out[4704]);
+      ws[170880] = fma(kw * y[4640], y[4704], ws[170880]);
+    }
+    {
+      double w = 1.0 * phi[4608];
+      w = w - phi[4640];
+      w = w - phi[4320];
+      const double kw = ws[34432] * w;
+      out[4640] = fma(kw, y[4320], out[4640]);
+      out[4320] = fma(kw, y[4640], out[4320]);
+      ws[170912] = fma(kw * y[4640], y[4320], ws[170912]);
+    }
+    {
+      double w = 2.0 * phi[4608];
+      w = w - phi[4640];
+      w = w - phi[4640];
+      const double kw = ws[34464] * w;
+      out[4640] = fma(kw, y[4640], out[4640]);
+      out[4640] = fma(kw, y[4640], out[4640]);
+      ws[170944] = fma(kw * y[4640], y[4640], ws[170944]);
+    }
+    {
+      double w = 1.0 * phi[1280];
+      w = w - phi[4640];
+      w = w - phi[4608];
+      const double kw = ws[34496] * w;
+      out[4640] = fma(kw, y[4608], out[4640]);
+      out[4608] = fma(kw, y[4640], out[4608]);
+      ws[170976] = fma(kw * y[4640], y[4608], ws[170976]);
+    }
+    {
+      double w = 1.0 * phi[4640];
+      w = fma(1.0, phi[4608], w);
+      w = w - phi[1280];
+      const double kw = ws[34528] * w;
+      out[1280] = out[1280] + kw;
+      ws[171008] = fma(kw, y[1280], ws[171008]);
+    }
+    {
+      double w = 2.0 * phi[4192];
+      w = w - phi[1280];
+      const double kw = ws[34592] * w;
+      out[1280] = out[1280] + kw;
+      ws[171072] = fma(kw, y[1280], ws[171072]);
+    }
+    {
+      double w = 1.0 * phi[2464];
+      w = w - phi[4384];
+      w = w - phi[4736];
+      const double kw = ws[34624] * w;
+      out[4384] = fma(kw, y[4736], out[4384]);
+      out[4736] = fma(kw, y[4384], out[4736]);
+      ws[171104] = fma(kw * y[4384], y[4736], ws[171104]);
+    }
+    {
+      double w = 2.0 * phi[2464];
+      w = w - phi[4384];
+      w = w - phi[4608];
+      const double kw = ws[34656] * w;
+      out[4384] = fma(kw, y[4608], out[4384]);
+      out[4608] = fma(kw, y[4384], out[4608]);
+      ws[171136] = fma(kw * y[4384], y[4608], ws[171136]);
+    }
+    {
+      double w = 1.0 * phi[4384];
+      w = fma(1.0, phi[4608], w);
+      w = w - phi[2464];
+      w = w - phi[2464];
+      const double kw = ws[34688] * w;
+      out[2464] = fma(kw, y[2464], out[2464]);
+      out[2464] = fma(kw, y[2464], out[2464]);
+      ws[171168] = fma(kw * y[2464], y[2464], ws[171168]);
+    }
+    {
+      double w = 1.0 * phi[4608];
+      w = w - phi[2464];
+      w = w - phi[4736];
+      const double kw = ws[34752] * w;
+      out[2464] = fma(kw, y[4736], out[2464]);
+      out[4736] = fma(kw, y[2464], out[4736]);
+      ws[171232] = fma(kw * y[2464], y[4736], ws[171232]);
+    }
+    {
+      double w = 1.0 * phi[4192];
+      w = w - phi[4608];
+      w = w - phi[4736];
+      const double kw = ws[34784] * w;
+      out[4608] = fma(kw, y[4736], out[4608]);
+      out[4736] = fma(kw, y[4608], out[4736]);
+      ws[171264] = fma(kw * y[4608], y[4736], ws[171264]);
+    }
+    {
+      double w = 1.0 * phi[4640];
+      w = w - phi[4192];
+      w = w - phi[4736];
+      const double kw = ws[34816] * w;
+      out[4192] = fma(kw, y[4736], out[4192]);
+      out[4736] = fma(kw, y[4192], out[4736]);
+      ws[171296] = fma(kw * y[4192], y[4736], ws[171296]);
+    }
+    {
+      double w = 1.0 * phi[1696];
+      w = w - phi[4704];
+      w = w - phi[4608];
+      const double kw = ws[34880] * w;
+      out[4704] = fma(kw, y[4608], out[4704]);
+      out[4608] = fma(kw, y[4704], out[4608]);
+      ws[171360] = fma(kw * y[4704], y[4608], ws[171360]);
+    }
+    {
+      double w = 1.0 * phi[4704];
+      w = fma(1.0, phi[4608], w);
+      w = w - phi[1696];
+      const double kw = ws[34912] * w;
+      out[1696] = out[1696] + kw;
+      ws[171392] = fma(kw, y[1696], ws[171392]);
+    }
+    {
+      double w = 1.0 * phi[4608];
+      w = w - phi[1696];
+      w = w - phi[4736];
+      const double kw = ws[34976] * w;
+      out[1696] = fma(kw, y[4736], out[1696]);
+      out[4736] = fma(kw, y[1696], out[4736]);
+      ws[171456] = fma(kw * y[1696], y[4736], ws[171456]);
+    }
+    {
+      double w = 1.0 * phi[256];
+      w = fma(1.0, phi[4704], w);
+      w = fma(1.0, phi[288], w);
+      w = w - phi[2208];
+      w = w - phi[4736];
+      const double kw = ws[35008] * w;
+      out[2208] = fma(kw, y[4736], out[2208]);
+      out[4736] = fma(kw, y[2208], out[4736]);
+      ws[171488] = fma(kw * y[2208], y[4736], ws[171488]);
+    }
+    {
+      double w = 1.0 * phi[4608];
+      w = fma(1.0, phi[4416], w);
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[4448];
+      w = w - phi[4384];
+      const double kw = ws[35040] * w;
+      out[4448] = fma(kw, y[4384], out[4448]);
+      out[4384] = fma(kw, y[4448], out[4384]);
+      ws[171520] = fma(kw * y[4448], y[4384], ws[171520]);
+    }
+    {
+      double w = 1.0 * phi[1344];
+      w = w - phi[4448];
+      w = w - phi[4608];
+      const double kw = ws[35072] * w;
+      out[4448] = fma(kw, y[4608], out[4448]);
+      out[4608] = fma(kw, y[4448], out[4608]);
+      ws[171552] = fma(kw * y[4448], y[4608], ws[171552]);
+    }
+    {
+      double w = 1.0 * phi[4608];
+      w = fma(1.0, phi[4448], w);
+      w = w - phi[1344];
+      const double kw = ws[35104] * w;
+      out[1344] = out[1344] + kw;
+      ws[171584] = fma(kw, y[1344], ws[171584]);
+    }
+    {
+      double w = 0.37 * phi[2688];
+      w = fma(0.13, phi[3904], w);
+      w = fma(0.13, phi[4320], w);
+      w = fma(0.5, phi[4416], w);
+      w = fma(0.5, phi[4672], w);
+      w = fma(0.5, phi[4736], w);
+      w = w - phi[4448];
+      w = w - phi[4704];
+      const double kw = ws[35168] * w;
+      out[4448] = fma(kw, y[4704], out[4448]);
+      out[4704] = fma(kw, y[4448], out[4704]);
+      ws[171648] = fma(kw * y[4448], y[4704], ws[171648]);
+    }
+    {
+      double w = 1.0 * phi[4416];
+      w = w - phi[4448];
+      w = w - phi[4672];
+      const double kw = ws[35200] * w;
+      out[4448] = fma(kw, y[4672], out[4448]);
+      out[4672] = fma(kw, y[4448], out[4672]);
+      ws[171680] = fma(kw * y[4448], y[4672], ws[171680]);
+    }
+    {
+      double w = 2.0 * phi[4416];
+      w = fma(2.0, phi[4672], w);
+      w = w - phi[4448];
+      w = w - phi[4448];
+      const double kw = ws[35232] * w;
+      out[4448] = fma(kw, y[4448], out[4448]);
+      out[4448] = fma(kw, y[4448], out[4448]);
+      ws[171712] = fma(kw * y[4448], y[4448], ws[171712]);
+    }
+    {
+      double w = 1.0 * phi[4416];
+      w = fma(1.0, phi[4128], w);
+      w = fma(1.0, phi[4576], w);
+      w = fma(2.0, phi[4672], w);
+      w = w - phi[4448];
+      w = w - phi[4096];
+      const double kw = ws[35264] * w;
+      out[4448] = fma(kw, y[4096], out[4448]);
+      out[4096] = fma(kw, y[4448], out[4096]);
+      ws[171744] = fma(kw * y[4448], y[4096], ws[171744]);
+    }
+    {
+      double w = 1.0 * phi[4608];
+      w = fma(1.0, phi[4128], w);
+      w = fma(1.0, phi[4576], w);
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[4096];
+      w = w - phi[4384];
+      const double kw = ws[35296] * w;
+      out[4096] = fma(kw, y[4384], out[4096]);
+      out[4384] = fma(kw, y[4096], out[4384]);
+      ws[171776] = fma(kw * y[4096], y[4384], ws[171776]);
+    }
+    {
+      double w = 1.0 * phi[1952];
+      w = w - phi[4096];
+      w = w - phi[4608];
+      const double kw = ws[35328] * w;
+      out[4096] = fma(kw, y[4608], out[4096]);
+      out[4608] = fma(kw, y[4096], out[4608]);
+      ws[171808] = fma(kw * y[4096], y[4608], ws[171808]);
+    }
+    {
+      double w = 1.0 * phi[4608];
+      w = fma(1.0, phi[4096], w);
+      w = w - phi[1952];
+      const double kw = ws[35360] * w;
+      out[1952] = out[1952] + kw;
+      ws[171840] = fma(kw, y[1952], ws[171840]);
+    }
+    {
+      double w = 0.37 * phi[2688];
+      w = fma(0.13, phi[3904], w);
+      w = fma(0.13, phi[4320], w);
+      w = fma(0.5, phi[4736], w);
+      w = fma(0.5, phi[4416], w);
+      w = fma(0.5, phi[4672], w);
+      w = w - phi[4096];
+      w = w - phi[4704];
+      const double kw = ws[35424] * w;
+      out[4096] = fma(kw, y[4704], out[4096]);
+      out[4704] = fma(kw, y[4096], out[4704]);
+      ws[171904] = fma(kw * y[4096], y[4704], ws[171904]);
+    }
+    {
+      double w = 1.0 * phi[4416];
+      w = w - phi[4096];
+      w = w - phi[4672];
+      const double kw = ws[35456] * w;
+      out[4096] = fma(kw, y[4672], out[4096]);
+      out[4672] = fma(kw, y[4096], out[4672]);
+      ws[171936] = fma(kw * y[4096], y[4672], ws[171936]);
+    }
+}
+__device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int phioff, int outoff)
+{
+    const double* __restrict__ y = ws + yoff * 32;
+    const double* __restrict__ phi = ws + phioff * 32;
+    double* __restrict__ out = ws + outoff * 32;
+    {
+      double w = 2.0 * phi[4416];
+      w = fma(2.0, phi[4672], w);
+      w = w - phi[4096];
+      w = w - phi[4096];
+      const double kw = ws[35488] * w;
+      out[4096] = fma(kw, y[4096], out[4096]);
+      out[4096] = fma(kw, y[4096], out[4096]);
+      ws[171968] = fma(kw * y[4096], y[4096], ws[171968]);
+    }
+    {
+      double w = 1.0 * phi[4384];
+      w = w - phi[4672];
+      w = w - phi[4384];
+      const double kw = ws[35520] * w;
+      out[4672] = fma(kw, y[4384], out[4672]);
+      out[4384] = fma(kw, y[4672], out[4384]);
+      ws[172000] = fma(kw * y[4672], y[4384], ws[172000]);
+    }
+    {
+      double w = 1.0 * phi[4704];
+      w = w - phi[4672];
+      w = w - phi[4704];
+      const double kw = ws[35552] * w;
+      out[4672] = fma(kw, y[4704], out[4672]);
+      out[4704] = fma(kw, y[4672], out[4704]);
+      ws[172032] = fma(kw * y[4672], y[4704], ws[172032]);
+    }
+    {
+      double w = -phi[4672];
+      w = w - phi[4672];
+      const double kw = ws[35584] * w;
+      out[4672] = fma(kw, y[4672], out[4672]);
+      out[4672] = fma(kw, y[4672], out[4672]);
+      ws[172064] = fma(kw * y[4672], y[4672], ws[172064]);
+    }
+    {
+      double w = 1.0 * phi[4512];
+      w = fma(1.0, phi[4704], w);
+      w = fma(1.0, phi[4608], w);
+      w = w - phi[4416];
+      w = w - phi[4384];
+      const double kw = ws[35616] * w;
+      out[4416] = fma(kw, y[4384], out[4416]);
+      out[4384] = fma(kw, y[4416], out[4384]);
+      ws[172096] = fma(kw * y[4416], y[4384], ws[172096]);
+    }
+    {
+      double w = 0.9 * phi[2272];
+      w = fma(0.1, phi[4512], w);
+      w = w - phi[4416];
+      w = w - phi[4704];
+      const double kw = ws[35648] * w;
+      out[4416] = fma(kw, y[4704], out[4416]);
+      out[4704] = fma(kw, y[4416], out[4704]);
+      ws[172128] = fma(kw * y[4416], y[4704], ws[172128]);
+    }
+    {
+      double w = 1.0 * phi[4512];
+      w = fma(0.9, phi[4704], w);
+      w = fma(0.9, phi[4416], w);
+      w = fma(0.1, phi[3904], w);
+      w = fma(0.9, phi[4672], w);
+      w = w - phi[4416];
+      w = w - phi[4448];
+      const double kw = ws[35680] * w;
+      out[4416] = fma(kw, y[4448], out[4416]);
+      out[4448] = fma(kw, y[4416], out[4448]);
+      ws[172160] = fma(kw * y[4416], y[4448], ws[172160]);
+    }
+    {
+      double w = 0.685 * phi[4512];
+      w = fma(0.315, phi[2720], w);
+      w = fma(0.37, phi[4704], w);
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[4416];
+      w = w - phi[4672];
+      const double kw = ws[35712] * w;
+      out[4416] = fma(kw, y[4672], out[4416]);
+      out[4672] = fma(kw, y[4416], out[4672]);
+      ws[172192] = fma(kw * y[4416], y[4672], ws[172192]);
+    }
+    {
+      double w = 1.0 * phi[4608];
+      w = fma(1.0, phi[4704], w);
+      w = w - phi[4576];
+      w = w - phi[4384];
+      const double kw = ws[35744] * w;
+      out[4576] = fma(kw, y[4384], out[4576]);
+      out[4384] = fma(kw, y[4576], out[4384]);
+      ws[172224] = fma(kw * y[4576], y[4384], ws[172224]);
+    }
+    {
+      double w = 1.0 * phi[2880];
+      w = w - phi[4576];
+      w = w - phi[4704];
+      const double kw = ws[35776] * w;
+      out[4576] = fma(kw, y[4704], out[4576]);
+      out[4704] = fma(kw, y[4576], out[4704]);
+      ws[172256] = fma(kw * y[4576], y[4704], ws[172256]);
+    }
+    {
+      double w = 0.8 * phi[4704];
+      w = fma(0.8, phi[4416], w);
+      w = fma(0.2, phi[3904], w);
+      w = fma(0.8, phi[4672], w);
+      w = w - phi[4576];
+      w = w - phi[4448];
+      const double kw = ws[35808] * w;
+      out[4576] = fma(kw, y[4448], out[4576]);
+      out[4448] = fma(kw, y[4576], out[4448]);
+      ws[172288] = fma(kw * y[4576], y[4448], ws[172288]);
+    }
+    {
+      double w = 0.6 * phi[4704];
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[4576];
+      w = w - phi[4672];
+      const double kw = ws[35840] * w;
+      out[4576] = fma(kw, y[4672], out[4576]);
+      out[4672] = fma(kw, y[4576], out[4672]);
+      ws[172320] = fma(kw * y[4576], y[4672], ws[172320]);
+    }
+    {
+      double w = 1.0 * phi[4608];
+      w = w - phi[4352];
+      w = w - phi[4384];
+      const double kw = ws[35872] * w;
+      out[4352] = fma(kw, y[4384], out[4352]);
+      out[4384] = fma(kw, y[4352], out[4384]);
+      ws[172352] = fma(kw * y[4352], y[4384], ws[172352]);
+    }
+    {
+      double w = 1.0 * phi[2880];
+      w = w - phi[4352];
+      w = w - phi[4704];
+      const double kw = ws[35904] * w;
+      out[4352] = fma(kw, y[4704], out[4352]);
+      out[4704] = fma(kw, y[4352], out[4704]);
+      ws[172384] = fma(kw * y[4352], y[4704], ws[172384]);
+    }
+    {
+      double w = 0.8 * phi[4416];
+      w = fma(0.2, phi[3904], w);
+      w = fma(0.8, phi[4672], w);
+      w = w - phi[4352];
+      w = w - phi[4448];
+      const double kw = ws[35936] * w;
+      out[4352] = fma(kw, y[4448], out[4352]);
+      out[4448] = fma(kw, y[4352], out[4448]);
+      ws[172416] = fma(kw * y[4352], y[4448], ws[172416]);
+    }
+    {
+      double w = 1.0 * phi[4672];
+      w = w - phi[4352];
+      w = w - phi[4672];
+      const double kw = ws[35968] * w;
+      out[4352] = fma(kw, y[4672], out[4352]);
+      out[4672] = fma(kw, y[4352], out[4672]);
+      ws[172448] = fma(kw * y[4352], y[4672], ws[172448]);
+    }
+    {
+      double w = 0.5 * phi[3648];
+      w = fma(0.5, phi[4032], w);
+      w = w - phi[4288];
+      w = w - phi[4384];
+      const double kw = ws[36000] * w;
+      out[4288] = fma(kw, y[4384], out[4288]);
+      out[4384] = fma(kw, y[4288], out[4384]);
+      ws[172480] = fma(kw * y[4288], y[4384], ws[172480]);
+    }
+    {
+      double w = 1.0 * phi[2880];
+      w = w - phi[4288];
+      w = w - phi[4704];
+      const double kw = ws[36032] * w;
+      out[4288] = fma(kw, y[4704], out[4288]);
+      out[4704] = fma(kw, y[4288], out[4704]);
+      ws[172512] = fma(kw * y[4288], y[4704], ws[172512]);
+    }
+    {
+      double w = 0.8 * phi[4704];
+      w = fma(0.8, phi[4416], w);
+      w = fma(0.2, phi[3904], w);
+      w = fma(0.8, phi[4672], w);
+      w = w - phi[4288];
+      w = w - phi[4448];
+      const double kw = ws[36064] * w;
+      out[4288] = fma(kw, y[4448], out[4288]);
+      out[4448] = fma(kw, y[4288], out[4448]);
+      ws[172544] = fma(kw * y[4288], y[4448], ws[172544]);
+    }
+    {
+      double w = 1.0 * phi[4672];
+      w = w - phi[4288];
+      w = w - phi[4672];
+      const double kw = ws[36096] * w;
+      out[4288] = fma(kw, y[4672], out[4288]);
+      out[4672] = fma(kw, y[4288], out[4672]);
+      ws[172576] = fma(kw * y[4288], y[4672], ws[172576]);
+    }
+    {
+      double w = 0.6 * phi[4416];
+      w = fma(0.6, phi[4672], w);
+      w = fma(0.4, phi[4512], w);
+      w = fma(0.4, phi[4736], w);
+      w = w - phi[2272];
+      w = w - phi[4736];
+      const double kw = ws[36128] * w;
+      out[2272] = fma(kw, y[4736], out[2272]);
+      out[4736] = fma(kw, y[2272], out[4736]);
+      ws[172608] = fma(kw * y[2272], y[4736], ws[172608]);
+    }
+    {
+      double w = 0.54 * phi[4576];
+      w = fma(0.06, phi[4288], w);
+      w = fma(0.6, phi[4672], w);
+      w = fma(0.4, phi[4736], w);
+      w = w - phi[2880];
+      w = w - phi[4736];
+      const double kw = ws[36192] * w;
+      out[2880] = fma(kw, y[4736], out[2880]);
+      out[4736] = fma(kw, y[2880], out[4736]);
+      ws[172672] = fma(kw * y[2880], y[4736], ws[172672]);
+    }
+    {
+      double w = 1.0 * phi[4032];
+      w = w - phi[3648];
+      w = w - phi[4736];
+      const double kw = ws[36256] * w;
+      out[3648] = fma(kw, y[4736], out[3648]);
+      out[4736] = fma(kw, y[3648], out[4736]);
+      ws[172736] = fma(kw * y[3648], y[4736], ws[172736]);
+    }
+    {
+      double w = 1.0 * phi[4704];
+      w = w - phi[3776];
+      w = w - phi[4736];
+      const double kw = ws[36320] * w;
+      out[3776] = fma(kw, y[4736], out[3776]);
+      out[4736] = fma(kw, y[3776], out[4736]);
+      ws[172800] = fma(kw * y[3776], y[4736], ws[172800]);
+    }
+    {
+      double w = 1.0 * phi[4416];
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[3904];
+      w = w - phi[4736];
+      const double kw = ws[36352] * w;
+      out[3904] = fma(kw, y[4736], out[3904]);
+      out[4736] = fma(kw, y[3904], out[4736]);
+      ws[172832] = fma(kw * y[3904], y[4736], ws[172832]);
+    }
+    {
+      double w = 1.0 * phi[4448];
+      w = w - phi[2688];
+      w = w - phi[4736];
+      const double kw = ws[36384] * w;
+      out[2688] = fma(kw, y[4736], out[2688]);
+      out[4736] = fma(kw, y[2688], out[4736]);
+      ws[172864] = fma(kw * y[2688], y[4736], ws[172864]);
+    }
+    {
+      double w = 1.0 * phi[4704];
+      w = fma(1.0, phi[4480], w);
+      w = w - phi[4512];
+      w = w - phi[4736];
+      const double kw = ws[36416] * w;
+      out[4512] = fma(kw, y[4736], out[4512]);
+      out[4736] = fma(kw, y[4512], out[4736]);
+      ws[172896] = fma(kw * y[4512], y[4736], ws[172896]);
+    }
+    {
+      double w = 1.0 * phi[4736];
+      w = fma(1.0, phi[4704], w);
+      w = fma(1.0, phi[4480], w);
+      w = w - phi[4512];
+      w = w - phi[4160];
+      const double kw = ws[36512] * w;
+      out[4512] = fma(kw, y[4160], out[4512]);
+      out[4160] = fma(kw, y[4512], out[4160]);
+      ws[172992] = fma(kw * y[4512], y[4160], ws[172992]);
+    }
+    {
+      double w = 1.0 * phi[4192];
+      w = fma(1.0, phi[4704], w);
+      w = fma(1.0, phi[4480], w);
+      w = w - phi[4512];
+      w = w - phi[4640];
+      const double kw = ws[36544] * w;
+      out[4512] = fma(kw, y[4640], out[4512]);
+      out[4640] = fma(kw, y[4512], out[4640]);
+      ws[173024] = fma(kw * y[4512], y[4640], ws[173024]);
+    }
+    {
+      double w = 1.0 * phi[1728];
+      w = w - phi[4512];
+      w = w - phi[4704];
+      const double kw = ws[36576] * w;
+      out[4512] = fma(kw, y[4704], out[4512]);
+      out[4704] = fma(kw, y[4512], out[4704]);
+      ws[173056] = fma(kw * y[4512], y[4704], ws[173056]);
+    }
+    {
+      double w = 1.0 * phi[4512];
+      w = fma(1.0, phi[4704], w);
+      w = w - phi[1728];
+      const double kw = ws[36608] * w;
+      out[1728] = out[1728] + kw;
+      ws[173088] = fma(kw, y[1728], ws[173088]);
+    }
+    {
+      double w = 1.0 * phi[3776];
+      w = fma(1.0, phi[4608], w);
+      w = fma(1.0, phi[4704], w);
+      w = w - phi[1728];
+      w = w - phi[4384];
+      const double kw = ws[36640] * w;
+      out[1728] = fma(kw, y[4384], out[1728]);
+      out[4384] = fma(kw, y[1728], out[4384]);
+      ws[173120] = fma(kw * y[1728], y[4384], ws[173120]);
+    }
+    {
+      double w = 0.5 * phi[2272];
+      w = fma(0.5, phi[3776], w);
+      w = fma(0.2, phi[4736], w);
+      w = fma(0.2, phi[4704], w);
+      w = w - phi[1728];
+      w = w - phi[4704];
+      const double kw = ws[36672] * w;
+      out[1728] = fma(kw, y[4704], out[1728]);
+      out[4704] = fma(kw, y[1728], out[4704]);
+      ws[173152] = fma(kw * y[1728], y[4704], ws[173152]);
+    }
+    {
+      double w = 1.0 * phi[4448];
+      w = fma(1.0, phi[4736], w);
+      w = w - phi[4128];
+      w = w - phi[4160];
+      const double kw = ws[36704] * w;
+      out[4128] = fma(kw, y[4160], out[4128]);
+      out[4160] = fma(kw, y[4128], out[4160]);
+      ws[173184] = fma(kw * y[4128], y[4160], ws[173184]);
+    }
+    {
+      double w = 1.0 * phi[4448];
+      w = w - phi[4128];
+      w = w - phi[4736];
+      const double kw = ws[36736] * w;
+      out[4128] = fma(kw, y[4736], out[4128]);
+      out[4736] = fma(kw, y[4128], out[4736]);
+      ws[173216] = fma(kw * y[4128], y[4736], ws[173216]);
+    }
+    {
+      double w = 1.0 * phi[4448];
+      w = fma(1.0, phi[4192], w);
+      w = w - phi[4128];
+      w = w - phi[4640];
+      const double kw = ws[36768] * w;
+      out[4128] = fma(kw, y[4640], out[4128]);
+      out[4640] = fma(kw, y[4128], out[4640]);
+      ws[173248] = fma(kw * y[4128], y[4640], ws[173248]);
+    }
+    {
+      double w = 1.0 * phi[4096];
+      w = fma(1.0, phi[4736], w);
+      w = w - phi[4064];
+      w = w - phi[4160];
+      const double kw = ws[36832] * w;
+      out[4064] = fma(kw, y[4160], out[4064]);
+      out[4160] = fma(kw, y[4064], out[4160]);
+      ws[173312] = fma(kw * y[4064], y[4160], ws[173312]);
+    }
+    {
+      double w = 1.0 * phi[4096];
+      w = w - phi[4064];
+      w = w - phi[4736];
+      const double kw = ws[36864] * w;
+      out[4064] = fma(kw, y[4736], out[4064]);
+      out[4736] = fma(kw, y[4064], out[4736]);
+      ws[173344] = fma(kw * y[4064], y[4736], ws[173344]);
+    }
+    {
+      double w = 1.0 * phi[4096];
+      w = fma(1.0, phi[4192], w);
+      w = w - phi[4064];
+      w = w - phi[4640];
+      const double kw = ws[36896] * w;
+      out[4064] = fma(kw, y[4640], out[4064]);
+      out[4640] = fma(kw, y[4064], out[4640]);
+      ws[173376] = fma(kw * y[4064], y[4640], ws[173376]);
+    }
+    {
+      double w = 0.2 * phi[4256];
+      w = fma(0.2, phi[4704], w);
+      w = fma(0.8, phi[4448], w);
+      w = w - phi[3840];
+      w = w - phi[4736];
+      const double kw = ws[36960] * w;
+      out[3840] = fma(kw, y[4736], out[3840]);
+      out[4736] = fma(kw, y[3840], out[4736]);
+      ws[173440] = fma(kw * y[3840], y[4736], ws[173440]);
+    }
+    {
+      double w = 1.0 * phi[4192];
+      w = fma(1.0, phi[4448], w);
+      w = w - phi[3840];
+      w = w - phi[4640];
+      const double kw = ws[37024] * w;
+      out[3840] = fma(kw, y[4640], out[3840]);
+      out[4640] = fma(kw, y[3840], out[4640]);
+      ws[173504] = fma(kw * y[3840], y[4640], ws[173504]);
+    }
+    {
+      double w = 1.8 * phi[4480];
+      w = fma(0.2, phi[4352], w);
+      w = fma(0.2, phi[4672], w);
+      w = fma(1.0, phi[4704], w);
+      w = w - phi[4256];
+      w = w - phi[4736];
+      const double kw = ws[37056] * w;
+      out[4256] = fma(kw, y[4736], out[4256]);
+      out[4736] = fma(kw, y[4256], out[4736]);
+      ws[173536] = fma(kw * y[4256], y[4736], ws[173536]);
+    }
+    {
+      double w = 1.0 * phi[4192];
+      w = fma(1.5, phi[4480], w);
+      w = fma(0.5, phi[4352], w);
+      w = fma(0.5, phi[4672], w);
+      w = fma(1.0, phi[4704], w);
+      w = w - phi[4256];
+      w = w - phi[4640];
+      const double kw = ws[37120] * w;
+      out[4256] = fma(kw, y[4640], out[4256]);
+      out[4640] = fma(kw, y[4256], out[4640]);
+      ws[173600] = fma(kw * y[4256], y[4640], ws[173600]);
+    }
+    {
+      double w = 1.0 * phi[4192];
+      w = fma(1.0, phi[4448], w);
+      w = fma(1.0, phi[4352], w);
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[4000];
+      w = w - phi[4640];
+      const double kw = ws[37184] * w;
+      out[4000] = fma(kw, y[4640], out[4000]);
+      out[4640] = fma(kw, y[4000], out[4640]);
+      ws[173664] = fma(kw * y[4000], y[4640], ws[173664]);
+    }
+    {
+      double w = 1.0 * phi[4448];
+      w = fma(1.0, phi[4480], w);
+      w = w - phi[4000];
+      w = w - phi[4736];
+      const double kw = ws[37216] * w;
+      out[4000] = fma(kw, y[4736], out[4000]);
+      out[4736] = fma(kw, y[4000], out[4736]);
+      ws[173696] = fma(kw * y[4000], y[4736], ws[173696]);
+    }
+    {
+      double w = 1.0 * phi[4704];
+      w = w - phi[4736];
+      const double kw = ws[37248] * w;
+      out[4736] = out[4736] + kw;
+      ws[173728] = fma(kw, y[4736], ws[173728]);
+    }
+    {
+      double w = 1.0 * phi[4704];
+      w = w - phi[4480];
+      w = w - phi[4736];
+      const double kw = ws[37280] * w;
+      out[4480] = fma(kw, y[4736], out[4480]);
+      out[4736] = fma(kw, y[4480], out[4736]);
+      ws[173760] = fma(kw * y[4480], y[4736], ws[173760]);
+    }
+    {
+      double w = 1.0 * phi[4416];
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[4736];
+      const double kw = ws[37312] * w;
+      out[4736] = out[4736] + kw;
+      ws[173792] = fma(kw, y[4736], ws[173792]);
+    }
+    {
+      double w = 0.991 * phi[4128];
+      w = fma(0.991, phi[4576], w);
+      w = fma(0.009, phi[4288], w);
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[832];
+      w = w - phi[4736];
+      const double kw = ws[37344] * w;
+      out[832] = fma(kw, y[4736], out[832]);
+      out[4736] = fma(kw, y[832], out[4736]);
+      ws[173824] = fma(kw * y[832], y[4736], ws[173824]);
+    }
+}
+__device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int phioff, int outoff)
+{
+    const double* __restrict__ y = ws + yoff * 32;
+    const double* __restrict__ phi = ws + phioff * 32;
+    double* __restrict__ out = ws + outoff * 32;
+    {
+      double w = 1.0 * phi[4512];
+      w = fma(1.0, phi[4704], w);
+      w = w - phi[2720];
+      w = w - phi[4736];
+      const double kw = ws[37376] * w;
+      out[2720] = fma(kw, y[4736], out[2720]);
+      out[4736] = fma(kw, y[2720], out[4736]);
+      ws[173856] = fma(kw * y[2720], y[4736], ws[173856]);
+    }
+    {
+      double w = 0.95 * phi[4128];
+      w = fma(0.9, phi[4704], w);
+      w = fma(0.1, phi[4576], w);
+      w = fma(0.1, phi[4672], w);
+      w = fma(0.078, phi[4512], w);
+      w = fma(0.011, phi[3840], w);
+      w = w - phi[864];
+      w = w - phi[4736];
+      const double kw = ws[37408] * w;
+      out[864] = fma(kw, y[4736], out[864]);
+      out[4736] = fma(kw, y[864], out[4736]);
+      ws[173888] = fma(kw * y[864], y[4736], ws[173888]);
+    }
+    {
+      double w = 1.0 * phi[4512];
+      w = fma(1.0, phi[4448], w);
+      w = fma(1.0, phi[4352], w);
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[3392];
+      w = w - phi[4736];
+      const double kw = ws[37504] * w;
+      out[3392] = fma(kw, y[4736], out[3392]);
+      out[4736] = fma(kw, y[3392], out[4736]);
+      ws[173984] = fma(kw * y[3392], y[4736], ws[173984]);
+    }
+    {
+      double w = 1.0 * phi[928];
+      w = w - phi[896];
+      w = w - phi[4736];
+      const double kw = ws[37536] * w;
+      out[896] = fma(kw, y[4736], out[896]);
+      out[4736] = fma(kw, y[896], out[4736]);
+      ws[174016] = fma(kw * y[896], y[4736], ws[174016]);
+    }
+    {
+      double w = 1.0 * phi[1984];
+      w = w - phi[4224];
+      w = w - phi[4736];
+      const double kw = ws[37568] * w;
+      out[4224] = fma(kw, y[4736], out[4224]);
+      out[4736] = fma(kw, y[4224], out[4736]);
+      ws[174048] = fma(kw * y[4224], y[4736], ws[174048]);
+    }
+    {
+      double w = 0.2 * phi[320];
+      w = fma(0.42, phi[3392], w);
+      w = fma(0.74, phi[4128], w);
+      w = fma(0.37, phi[4064], w);
+      w = fma(0.04, phi[4288], w);
+      w = fma(0.94, phi[4576], w);
+      w = fma(0.98, phi[4672], w);
+      w = fma(0.02, phi[960], w);
+      w = fma(-2.7, phi[4224], w);
+      w = w - phi[960];
+      const double kw = ws[37600] * w;
+      out[960] = out[960] + kw;
+      ws[174080] = fma(kw, y[960], ws[174080]);
+    }
+    {
+      double w = 1.0 * phi[320];
+      w = fma(1.0, phi[4704], w);
+      w = w - phi[960];
+      const double kw = ws[37632] * w;
+      out[960] = out[960] + kw;
+      ws[174112] = fma(kw, y[960], ws[174112]);
+    }
+    {
+      double w = 1.0 * phi[3648];
+      w = w - phi[960];
+      w = w - phi[4608];
+      const double kw = ws[37664] * w;
+      out[960] = fma(kw, y[4608], out[960]);
+      out[4608] = fma(kw, y[960], out[4608]);
+      ws[174144] = fma(kw * y[960], y[4608], ws[174144]);
+    }
+    {
+      double w = 0.7 * phi[4256];
+      w = fma(0.7, phi[4736], w);
+      w = fma(0.3, phi[3776], w);
+      w = fma(0.3, phi[4480], w);
+      w = fma(0.3, phi[4704], w);
+      w = w - phi[352];
+      w = w - phi[4736];
+      const double kw = ws[37696] * w;
+      out[352] = fma(kw, y[4736], out[352]);
+      out[4736] = fma(kw, y[352], out[4736]);
+      ws[174176] = fma(kw * y[352], y[4736], ws[174176]);
+    }
+    {
+      double w = 1.0 * phi[4512];
+      w = fma(1.0, phi[4704], w);
+      w = fma(1.0, phi[4480], w);
+      w = fma(0.7, phi[4576], w);
+      w = fma(0.7, phi[4672], w);
+      w = fma(0.3, phi[4736], w);
+      w = w - phi[2656];
+      w = w - phi[4160];
+      const double kw = ws[37728] * w;
+      out[2656] = fma(kw, y[4160], out[2656]);
+      out[4160] = fma(kw, y[2656], out[4160]);
+      ws[174208] = fma(kw * y[2656], y[4160], ws[174208]);
+    }
+    {
+      double w = 1.0 * phi[4576];
+      w = fma(1.0, phi[4672], w);
+      w = fma(1.56, phi[4512], w);
+      w = fma(0.22, phi[3840], w);
+      w = w - phi[2656];
+      w = w - phi[4736];
+      const double kw = ws[37760] * w;
+      out[2656] = fma(kw, y[4736], out[2656]);
+      out[4736] = fma(kw, y[2656], out[4736]);
+      ws[174240] = fma(kw * y[2656], y[4736], ws[174240]);
+    }
+    {
+      double w = 1.0 * phi[4512];
+      w = fma(0.35, phi[4480], w);
+      w = fma(0.27, phi[4704], w);
+      w = fma(0.17, phi[4736], w);
+      w = fma(0.42, phi[3776], w);
+      w = w - phi[2656];
+      w = w - phi[4320];
+      const double kw = ws[37792] * w;
+      out[2656] = fma(kw, y[4320], out[2656]);
+      out[4320] = fma(kw, y[2656], out[4320]);
+      ws[174272] = fma(kw * y[2656], y[4320], ws[174272]);
+    }
+    {
+      double w = 0.5 * phi[4608];
+      w = fma(0.5, phi[3648], w);
+      w = fma(0.5, phi[4576], w);
+      w = fma(0.5, phi[4352], w);
+      w = fma(1.0, phi[4672], w);
+      w = fma(1.125, phi[4512], w);
+      w = w - phi[2656];
+      w = w - phi[4640];
+      const double kw = ws[37824] * w;
+      out[2656] = fma(kw, y[4640], out[2656]);
+      out[4640] = fma(kw, y[2656], out[4640]);
+      ws[174304] = fma(kw * y[2656], y[4640], ws[174304]);
+    }
+    {
+      double w = 0.2 * phi[4128];
+      w = fma(0.3, phi[4064], w);
+      w = fma(0.1, phi[4704], w);
+      w = fma(0.2, phi[4576], w);
+      w = fma(0.2, phi[4480], w);
+      w = fma(0.2, phi[4512], w);
+      w = fma(0.01, phi[4288], w);
+      w = fma(0.21, phi[4672], w);
+      w = fma(0.2, phi[4224], w);
+      w = fma(0.1, phi[4736], w);
+      w = w - phi[3552];
+      w = w - phi[4160];
+      const double kw = ws[37856] * w;
+      out[3552] = fma(kw, y[4160], out[3552]);
+      out[4160] = fma(kw, y[3552], out[4160]);
+      ws[174336] = fma(kw * y[3552], y[4160], ws[174336]);
+    }
+    {
+      double w = 0.781 * phi[4512];
+      w = fma(0.488, phi[4128], w);
+      w = fma(0.488, phi[4064], w);
+      w = fma(0.976, phi[4576], w);
+      w = fma(0.195, phi[4352], w);
+      w = fma(0.024, phi[4288], w);
+      w = fma(1.195, phi[4672], w);
+      w = fma(-0.73, phi[4224], w);
+      w = w - phi[3552];
+      w = w - phi[4736];
+      const double kw = ws[37888] * w;
+      out[3552] = fma(kw, y[4736], out[3552]);
+      out[4736] = fma(kw, y[3552], out[4736]);
+      ws[174368] = fma(kw * y[3552], y[4736], ws[174368]);
+    }
+    {
+      double w = 0.295 * phi[4128];
+      w = fma(0.555, phi[4512], w);
+      w = fma(0.27, phi[4064], w);
+      w = fma(0.15, phi[4576], w);
+      w = fma(0.15, phi[4672], w);
+      w = fma(0.334, phi[4736], w);
+      w = fma(0.08, phi[4704], w);
+      w = fma(0.378, phi[4480], w);
+      w = fma(0.075, phi[4256], w);
+      w = fma(0.075, phi[4000], w);
+      w = fma(0.09, phi[3776], w);
+      w = fma(0.13, phi[3904], w);
+      w = fma(0.04, phi[3456], w);
+      w = fma(-0.79, phi[4224], w);
+      w = w - phi[3552];
+      w = w - phi[4320];
+      const double kw = ws[37920] * w;
+      out[3552] = fma(kw, y[4320], out[3552]);
+      out[4320] = fma(kw, y[3552], out[4320]);
+      ws[174400] = fma(kw * y[3552], y[4320], ws[174400]);
+    }
+    {
+      double w = 0.5 * phi[4608];
+      w = fma(0.5, phi[3648], w);
+      w = fma(0.48, phi[4352], w);
+      w = fma(0.48, phi[4576], w);
+      w = fma(0.04, phi[4288], w);
+      w = fma(1.0, phi[4672], w);
+      w = fma(0.5, phi[4512], w);
+      w = fma(0.25, phi[4128], w);
+      w = fma(0.375, phi[4064], w);
+      w = fma(-1.0, phi[4224], w);
+      w = w - phi[3552];
+      w = w - phi[4640];
+      const double kw = ws[37952] * w;
+      out[3552] = fma(kw, y[4640], out[3552]);
+      out[4640] = fma(kw, y[3552], out[4640]);
+      ws[174432] = fma(kw * y[3552], y[4640], ws[174432]);
+    }
+    {
+      double w = 1.24 * phi[4128];
+      w = fma(0.66, phi[4064], w);
+      w = fma(0.1, phi[4576], w);
+      w = fma(0.1, phi[4672], w);
+      w = fma(0.1, phi[4480], w);
+      w = fma(0.1, phi[4224], w);
+      w = w - phi[3136];
+      w = w - phi[4160];
+      const double kw = ws[37984] * w;
+      out[3136] = fma(kw, y[4160], out[3136]);
+      out[4160] = fma(kw, y[3136], out[4160]);
+      ws[174464] = fma(kw * y[3136], y[4160], ws[174464]);
+    }
+    {
+      double w = 1.3 * phi[4128];
+      w = fma(0.7, phi[4064], w);
+      w = fma(1.0, phi[4576], w);
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[3136];
+      w = w - phi[4736];
+      const double kw = ws[38016] * w;
+      out[3136] = fma(kw, y[4736], out[3136]);
+      out[4736] = fma(kw, y[3136], out[4736]);
+      ws[174496] = fma(kw * y[3136], y[4736], ws[174496]);
+    }
+    {
+      double w = 0.732 * phi[4128];
+      w = fma(0.442, phi[4064], w);
+      w = fma(0.128, phi[4512], w);
+      w = fma(0.245, phi[4480], w);
+      w = fma(0.5, phi[4736], w);
+      w = fma(0.3, phi[4576], w);
+      w = fma(0.3, phi[4672], w);
+      w = fma(0.24, phi[4256], w);
+      w = fma(0.06, phi[4000], w);
+      w = fma(0.29, phi[4224], w);
+      w = fma(0.08, phi[3904], w);
+      w = fma(0.08, phi[3456], w);
+      w = w - phi[3136];
+      w = w - phi[4320];
+      const double kw = ws[38048] * w;
+      out[3136] = fma(kw, y[4320], out[3136]);
+      out[4320] = fma(kw, y[3136], out[4320]);
+      ws[174528] = fma(kw * y[3136], y[4320], ws[174528]);
+    }
+    {
+      double w = 0.5 * phi[4608];
+      w = fma(0.5, phi[3648], w);
+      w = fma(0.48, phi[4352], w);
+      w = fma(0.48, phi[4576], w);
+      w = fma(0.04, phi[4288], w);
+      w = fma(1.0, phi[4672], w);
+      w = fma(0.5, phi[4128], w);
+      w = fma(0.625, phi[4064], w);
+      w = fma(1.0, phi[4224], w);
+      w = w - phi[3136];
+      w = w - phi[4640];
+      const double kw = ws[38080] * w;
+      out[3136] = fma(kw, y[4640], out[3136]);
+      out[4640] = fma(kw, y[3136], out[4640]);
+      ws[174560] = fma(kw * y[3136], y[4640], ws[174560]);
+    }
+    {
+      double w = 1.0 * phi[3424];
+      w = fma(1.0, phi[4672], w);
+      w = fma(1.0, phi[992], w);
+      w = w - phi[2528];
+      w = w - phi[4736];
+      const double kw = ws[38112] * w;
+      out[2528] = fma(kw, y[4736], out[2528]);
+      out[4736] = fma(kw, y[2528], out[4736]);
+      ws[174592] = fma(kw * y[2528], y[4736], ws[174592]);
+    }
+    {
+      double w = 0.75 * phi[3872];
+      w = fma(0.5, phi[4512], w);
+      w = fma(0.25, phi[4352], w);
+      w = fma(0.25, phi[4672], w);
+      w = fma(0.25, phi[4704], w);
+      w = fma(0.25, phi[4096], w);
+      w = fma(0.25, phi[4224], w);
+      w = w - phi[2528];
+      w = w - phi[4160];
+      const double kw = ws[38144] * w;
+      out[2528] = fma(kw, y[4160], out[2528]);
+      out[4160] = fma(kw, y[2528], out[4160]);
+      ws[174624] = fma(kw * y[2528], y[4160], ws[174624]);
+    }
+    {
+      double w = 0.1 * phi[1632];
+      w = fma(0.9, phi[4608], w);
+      w = fma(0.673, phi[4512], w);
+      w = fma(0.9, phi[3872], w);
+      w = fma(0.818, phi[4704], w);
+      w = fma(0.082, phi[4576], w);
+      w = fma(0.082, phi[4672], w);
+      w = w - phi[3424];
+      w = w - phi[4384];
+      const double kw = ws[38176] * w;
+      out[3424] = fma(kw, y[4384], out[3424]);
+      out[4384] = fma(kw, y[3424], out[4384]);
+      ws[174656] = fma(kw * y[3424], y[4384], ws[174656]);
+    }
+    {
+      double w = 0.88 * phi[1664];
+      w = fma(0.12, phi[4736], w);
+      w = fma(0.12, phi[4704], w);
+      w = fma(0.12, phi[4512], w);
+      w = fma(0.12, phi[3872], w);
+      w = w - phi[3424];
+      w = w - phi[4704];
+      const double kw = ws[38208] * w;
+      out[3424] = fma(kw, y[4704], out[3424]);
+      out[4704] = fma(kw, y[3424], out[4704]);
+      ws[174688] = fma(kw * y[3424], y[4704], ws[174688]);
+    }
+    {
+      double w = 0.598 * phi[4512];
+      w = fma(1.0, phi[3872], w);
+      w = fma(0.728, phi[4704], w);
+      w = fma(0.072, phi[4576], w);
+      w = fma(0.8, phi[4416], w);
+      w = fma(0.2, phi[3904], w);
+      w = fma(0.872, phi[4672], w);
+      w = w - phi[3424];
+      w = w - phi[4448];
+      const double kw = ws[38240] * w;
+      out[3424] = fma(kw, y[4448], out[3424]);
+      out[4448] = fma(kw, y[3424], out[4448]);
+      ws[174720] = fma(kw * y[3424], y[4448], ws[174720]);
+    }
+    {
+      double w = 0.598 * phi[4512];
+      w = fma(1.0, phi[3872], w);
+      w = fma(0.728, phi[4704], w);
+      w = fma(0.072, phi[4576], w);
+      w = fma(1.072, phi[4672], w);
+      w = w - phi[3424];
+      w = w - phi[4672];
+      const double kw = ws[38272] * w;
+      out[3424] = fma(kw, y[4672], out[3424]);
+      out[4672] = fma(kw, y[3424], out[4672]);
+      ws[174752] = fma(kw * y[3424], y[4672], ws[174752]);
+    }
+    {
+      double w = 1.0 * phi[4704];
+      w = fma(1.0, phi[1024], w);
+      w = w - phi[3424];
+      const double kw = ws[38304] * w;
+      out[3424] = out[3424] + kw;
+      ws[174784] = fma(kw, y[3424], ws[174784]);
+    }
+    {
+      double w = 0.6 * phi[4512];
+      w = fma(0.65, phi[3872], w);
+      w = fma(0.15, phi[4064], w);
+      w = fma(0.2, phi[4096], w);
+      w = fma(0.35, phi[4224], w);
+      w = fma(0.266, phi[4736], w);
+      w = fma(0.2, phi[4352], w);
+      w = fma(0.2, phi[4672], w);
+      w = fma(0.066, phi[4704], w);
+      w = fma(0.066, phi[4480], w);
+      w = w - phi[2528];
+      w = w - phi[4320];
+      const double kw = ws[38336] * w;
+      out[2528] = fma(kw, y[4320], out[2528]);
+      out[4320] = fma(kw, y[2528], out[4320]);
+      ws[174816] = fma(kw * y[2528], y[4320], ws[174816]);
+    }
+    {
+      double w = 0.35 * phi[4608];
+      w = fma(0.65, phi[4032], w);
+      w = fma(0.64, phi[4576], w);
+      w = fma(0.33, phi[4352], w);
+      w = fma(0.03, phi[4288], w);
+      w = fma(1.0, phi[4672], w);
+      w = fma(0.35, phi[4512], w);
+      w = fma(0.35, phi[3872], w);
+      w = fma(1.0, phi[992], w);
+      w = w - phi[2528];
+      w = w - phi[4640];
+      const double kw = ws[38368] * w;
+      out[2528] = fma(kw, y[4640], out[2528]);
+      out[4640] = fma(kw, y[2528], out[4640]);
+      ws[174848] = fma(kw * y[2528], y[4640], ws[174848]);
+    }
+    {
+      double w = 0.022 * phi[4288];
+      w = fma(0.521, phi[4352], w);
+      w = fma(0.115, phi[4000], w);
+      w = fma(0.115, phi[4416], w);
+      w = fma(0.269, phi[3840], w);
+      w = fma(0.269, phi[4448], w);
+      w = fma(0.457, phi[3744], w);
+      w = fma(0.117, phi[4224], w);
+      w = fma(0.137, phi[3392], w);
+      w = fma(0.137, phi[4480], w);
+      w = fma(0.137, phi[4704], w);
+      w = fma(0.658, phi[4672], w);
+      w = w - phi[3872];
+      w = w - phi[4736];
+      const double kw = ws[38400] * w;
+      out[3872] = fma(kw, y[4736], out[3872]);
+      out[4736] = fma(kw, y[3872], out[4736]);
+      ws[174880] = fma(kw * y[3872], y[4736], ws[174880]);
+    }
+    {
+      double w = 0.04 * phi[4128];
+      w = fma(0.231, phi[4512], w);
+      w = fma(0.531, phi[4000], w);
+      w = fma(0.17, phi[4256], w);
+      w = fma(0.17, phi[3392], w);
+      w = fma(0.543, phi[4480], w);
+      w = fma(0.461, phi[4736], w);
+      w = fma(0.15, phi[3776], w);
+      w = fma(0.398, phi[4704], w);
+      w = fma(0.143, phi[4448], w);
+      w = w - phi[3872];
+      w = w - phi[4320];
+      const double kw = ws[38432] * w;
+      out[3872] = fma(kw, y[4320], out[3872]);
+      out[4320] = fma(kw, y[3872], out[4320]);
+      ws[174912] = fma(kw * y[3872], y[4320], ws[174912]);
+    }
+    {
+      double w = 0.717 * phi[4192];
+      w = fma(0.142, phi[4032], w);
+      w = fma(0.142, phi[4608], w);
+      w = fma(0.142, phi[4352], w);
+      w = fma(0.142, phi[4576], w);
+      w = fma(0.113, phi[3840], w);
+      w = fma(0.113, phi[4000], w);
+      w = fma(0.717, phi[4224], w);
+      w = fma(0.717, phi[4096], w);
+      w = fma(0.284, phi[4672], w);
+      w = w - phi[3872];
+      w = w - phi[4640];
+      const double kw = ws[38464] * w;
+      out[3872] = fma(kw, y[4640], out[3872]);
+      out[4640] = fma(kw, y[3872], out[4640]);
+      ws[174944] = fma(kw * y[3872], y[4640], ws[174944]);
+    }
+    {
+      double w = 0.904 * phi[1056];
+      w = fma(0.933, phi[4736], w);
+      w = fma(0.067, phi[3424], w);
+      w = fma(0.067, phi[4672], w);
+      w = fma(0.029, phi[3136], w);
+      w = fma(0.029, phi[4064], w);
+      w = w - phi[1664];
+      w = w - phi[4736];
+      const double kw = ws[38528] * w;
+      out[1664] = fma(kw, y[4736], out[1664]);
+      out[4736] = fma(kw, y[1664], out[4736]);
+      ws[175008] = fma(kw * y[1664], y[4736], ws[175008]);
+    }
+    {
+      double w = 1.0 * phi[4192];
+      w = fma(1.0, phi[3872], w);
+      w = w - phi[1024];
+      w = w - phi[4640];
+      const double kw = ws[38592] * w;
+      out[1024] = fma(kw, y[4640], out[1024]);
+      out[4640] = fma(kw, y[1024], out[4640]);
+      ws[175072] = fma(kw * y[1024], y[4640], ws[175072]);
+    }
+}
+__device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int phioff, int outoff)
+{
+    const double* __restrict__ y = ws + yoff * 32;
+    const double* __restrict__ phi = ws + phioff * 32;
+    double* __restrict__ out = ws + outoff * 32;
+    {
+      double w = 1.0 * phi[3296];
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[1056];
+      w = w - phi[4736];
+      const double kw = ws[38624] * w;
+      out[1056] = fma(kw, y[4736], out[1056]);
+      out[4736] = fma(kw, y[1056], out[4736]);
+      ws[175104] = fma(kw * y[1056], y[4736], ws[175104]);
+    }
+    {
+      double w = 0.275 * phi[3840];
+      w = fma(0.275, phi[4256], w);
+      w = fma(0.275, phi[4000], w);
+      w = fma(1.125, phi[4736], w);
+      w = fma(0.825, phi[4704], w);
+      w = fma(0.375, phi[4512], w);
+      w = fma(0.074, phi[3776], w);
+      w = fma(0.251, phi[4480], w);
+      w = fma(2.175, phi[4224], w);
+      w = w - phi[3296];
+      w = w - phi[4704];
+      const double kw = ws[38656] * w;
+      out[3296] = fma(kw, y[4704], out[3296]);
+      out[4704] = fma(kw, y[3296], out[4704]);
+      ws[175136] = fma(kw * y[3296], y[4704], ws[175136]);
+    }
+    {
+      double w = 0.275 * phi[3840];
+      w = fma(0.275, phi[4256], w);
+      w = fma(0.275, phi[4000], w);
+      w = fma(0.125, phi[4736], w);
+      w = fma(0.825, phi[4704], w);
+      w = fma(0.375, phi[4512], w);
+      w = fma(1.0, phi[4608], w);
+      w = fma(0.251, phi[4480], w);
+      w = fma(2.175, phi[4224], w);
+      w = w - phi[3296];
+      w = w - phi[4384];
+      const double kw = ws[38688] * w;
+      out[3296] = fma(kw, y[4384], out[3296]);
+      out[4384] = fma(kw, y[3296], out[4384]);
+      ws[175168] = fma(kw * y[3296], y[4384], ws[175168]);
+    }
+    {
+      double w = 0.22 * phi[3840];
+      w = fma(0.22, phi[4256], w);
+      w = fma(0.22, phi[4000], w);
+      w = fma(0.1, phi[4736], w);
+      w = fma(0.66, phi[4704], w);
+      w = fma(0.3, phi[4512], w);
+      w = fma(0.2, phi[4480], w);
+      w = fma(1.74, phi[4224], w);
+      w = fma(0.8, phi[4416], w);
+      w = fma(0.2, phi[3904], w);
+      w = fma(0.8, phi[4672], w);
+      w = w - phi[3296];
+      w = w - phi[4448];
+      const double kw = ws[38720] * w;
+      out[3296] = fma(kw, y[4448], out[3296]);
+      out[4448] = fma(kw, y[3296], out[4448]);
+      ws[175200] = fma(kw * y[3296], y[4448], ws[175200]);
+    }
+    {
+      double w = 0.275 * phi[3840];
+      w = fma(0.275, phi[4256], w);
+      w = fma(0.275, phi[4000], w);
+      w = fma(0.125, phi[4736], w);
+      w = fma(0.825, phi[4704], w);
+      w = fma(0.375, phi[4512], w);
+      w = fma(0.251, phi[4480], w);
+      w = fma(2.175, phi[4224], w);
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[3296];
+      w = w - phi[4672];
+      const double kw = ws[38752] * w;
+      out[3296] = fma(kw, y[4672], out[3296]);
+      out[4672] = fma(kw, y[3296], out[4672]);
+      ws[175232] = fma(kw * y[3296], y[4672], ws[175232]);
+    }
+    {
+      double w = 0.63 * phi[4352];
+      w = fma(0.37, phi[4576], w);
+      w = fma(1.0, phi[4672], w);
+      w = fma(0.444, phi[4608], w);
+      w = fma(0.185, phi[4640], w);
+      w = fma(0.104, phi[1632], w);
+      w = fma(0.592, phi[4512], w);
+      w = fma(0.331, phi[3840], w);
+      w = fma(0.185, phi[3776], w);
+      w = fma(2.7, phi[4224], w);
+      w = fma(0.098, phi[3552], w);
+      w = fma(0.078, phi[4064], w);
+      w = fma(0.266, phi[4032], w);
+      w = w - phi[1632];
+      w = w - phi[4736];
+      const double kw = ws[38784] * w;
+      out[1632] = fma(kw, y[4736], out[1632]);
+      out[4736] = fma(kw, y[1632], out[4736]);
+      ws[175264] = fma(kw * y[1632], y[4736], ws[175264]);
+    }
+    {
+      double w = 0.15 * phi[4064];
+      w = fma(5.12, phi[4224], w);
+      w = fma(1.0, phi[2080], w);
+      w = w - phi[2048];
+      w = w - phi[4160];
+      const double kw = ws[38816] * w;
+      out[2048] = fma(kw, y[4160], out[2048]);
+      out[4160] = fma(kw, y[2048], out[4160]);
+      ws[175296] = fma(kw * y[2048], y[4160], ws[175296]);
+    }
+    {
+      double w = 0.75 * phi[4576];
+      w = fma(0.5, phi[4352], w);
+      w = fma(0.25, phi[4288], w);
+      w = fma(1.5, phi[4672], w);
+      w = fma(0.28, phi[4512], w);
+      w = fma(1.66, phi[4224], w);
+      w = fma(0.47, phi[4064], w);
+      w = fma(1.0, phi[2080], w);
+      w = w - phi[2048];
+      w = w - phi[4736];
+      const double kw = ws[38848] * w;
+      out[2048] = fma(kw, y[4736], out[2048]);
+      out[4736] = fma(kw, y[2048], out[4736]);
+      ws[175328] = fma(kw * y[2048], y[4736], ws[175328]);
+    }
+    {
+      double w = 0.57 * phi[4736];
+      w = fma(0.07, phi[4576], w);
+      w = fma(0.69, phi[4352], w);
+      w = fma(0.18, phi[4288], w);
+      w = fma(0.94, phi[4672], w);
+      w = fma(0.24, phi[4512], w);
+      w = fma(0.001, phi[4480], w);
+      w = fma(7.0, phi[4224], w);
+      w = fma(0.21, phi[4064], w);
+      w = fma(0.39, phi[4096], w);
+      w = fma(1.0, phi[2080], w);
+      w = w - phi[2048];
+      w = w - phi[4320];
+      const double kw = ws[38880] * w;
+      out[2048] = fma(kw, y[4320], out[2048]);
+      out[4320] = fma(kw, y[2048], out[4320]);
+      ws[175360] = fma(kw * y[2048], y[4320], ws[175360]);
+    }
+    {
+      double w = 0.47 * phi[4608];
+      w = fma(0.28, phi[4576], w);
+      w = fma(0.75, phi[4352], w);
+      w = fma(0.25, phi[4288], w);
+      w = fma(1.28, phi[4672], w);
+      w = fma(0.47, phi[4064], w);
+      w = fma(0.53, phi[4032], w);
+      w = fma(1.0, phi[2848], w);
+      w = w - phi[2048];
+      w = w - phi[4640];
+      const double kw = ws[38912] * w;
+      out[2048] = fma(kw, y[4640], out[2048]);
+      out[4640] = fma(kw, y[2048], out[4640]);
+      ws[175392] = fma(kw * y[2048], y[4640], ws[175392]);
+    }
+    {
+      double w = 0.15 * phi[4064];
+      w = fma(5.12, phi[4224], w);
+      w = fma(1.0, phi[2080], w);
+      w = w - phi[2112];
+      w = w - phi[4160];
+      const double kw = ws[38944] * w;
+      out[2112] = fma(kw, y[4160], out[2112]);
+      out[4160] = fma(kw, y[2112], out[4160]);
+      ws[175424] = fma(kw * y[2112], y[4160], ws[175424]);
+    }
+    {
+      double w = 0.75 * phi[4576];
+      w = fma(0.5, phi[4352], w);
+      w = fma(0.25, phi[4288], w);
+      w = fma(1.5, phi[4672], w);
+      w = fma(0.28, phi[4512], w);
+      w = fma(1.66, phi[4224], w);
+      w = fma(0.47, phi[4064], w);
+      w = fma(1.0, phi[2080], w);
+      w = w - phi[2112];
+      w = w - phi[4736];
+      const double kw = ws[38976] * w;
+      out[2112] = fma(kw, y[4736], out[2112]);
+      out[4736] = fma(kw, y[2112], out[4736]);
+      ws[175456] = fma(kw * y[2112], y[4736], ws[175456]);
+    }
+    {
+      double w = 0.57 * phi[4736];
+      w = fma(0.07, phi[4576], w);
+      w = fma(0.69, phi[4352], w);
+      w = fma(0.18, phi[4288], w);
+      w = fma(0.94, phi[4672], w);
+      w = fma(0.24, phi[4512], w);
+      w = fma(0.001, phi[4480], w);
+      w = fma(7.0, phi[4224], w);
+      w = fma(0.21, phi[4064], w);
+      w = fma(0.39, phi[4096], w);
+      w = fma(1.0, phi[2080], w);
+      w = w - phi[2112];
+      w = w - phi[4320];
+      const double kw = ws[39008] * w;
+      out[2112] = fma(kw, y[4320], out[2112]);
+      out[4320] = fma(kw, y[2112], out[4320]);
+      ws[175488] = fma(kw * y[2112], y[4320], ws[175488]);
+    }
+    {
+      double w = 0.47 * phi[4608];
+      w = fma(0.28, phi[4576], w);
+      w = fma(0.75, phi[4352], w);
+      w = fma(0.25, phi[4288], w);
+      w = fma(1.28, phi[4672], w);
+      w = fma(0.47, phi[4064], w);
+      w = fma(0.53, phi[4032], w);
+      w = w - phi[2112];
+      w = w - phi[4640];
+      const double kw = ws[39040] * w;
+      out[2112] = fma(kw, y[4640], out[2112]);
+      out[4640] = fma(kw, y[2112], out[4640]);
+      ws[175520] = fma(kw * y[2112], y[4640], ws[175520]);
+    }
+    {
+      double w = 0.53 * phi[3616];
+      w = fma(0.352, phi[3104], w);
+      w = fma(0.352, phi[4672], w);
+      w = fma(0.118, phi[3936], w);
+      w = fma(0.118, phi[4736], w);
+      w = fma(0.53, phi[4704], w);
+      w = fma(1.0, phi[2144], w);
+      w = w - phi[384];
+      w = w - phi[4736];
+      const double kw = ws[39072] * w;
+      out[384] = fma(kw, y[4736], out[384]);
+      out[4736] = fma(kw, y[384], out[4736]);
+      ws[175552] = fma(kw * y[384], y[4736], ws[175552]);
+    }
+    {
+      double w = 0.918 * phi[4608];
+      w = fma(0.082, phi[4032], w);
+      w = fma(0.918, phi[4256], w);
+      w = fma(0.918, phi[3936], w);
+      w = fma(0.918, phi[4704], w);
+      w = w - phi[3104];
+      w = w - phi[4384];
+      const double kw = ws[39104] * w;
+      out[3104] = fma(kw, y[4384], out[3104]);
+      out[4384] = fma(kw, y[3104], out[4384]);
+      ws[175584] = fma(kw * y[3104], y[4384], ws[175584]);
+    }
+    {
+      double w = 1.0 * phi[4256];
+      w = fma(1.0, phi[3936], w);
+      w = fma(1.0, phi[4704], w);
+      w = fma(1.0, phi[4416], w);
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[3104];
+      w = w - phi[4448];
+      const double kw = ws[39136] * w;
+      out[3104] = fma(kw, y[4448], out[3104]);
+      out[4448] = fma(kw, y[3104], out[4448]);
+      ws[175616] = fma(kw * y[3104], y[4448], ws[175616]);
+    }
+    {
+      double w = -phi[3104];
+      w = w - phi[4704];
+      const double kw = ws[39168] * w;
+      out[3104] = fma(kw, y[4704], out[3104]);
+      out[4704] = fma(kw, y[3104], out[4704]);
+      ws[175648] = fma(kw * y[3104], y[4704], ws[175648]);
+    }
+    {
+      double w = 1.0 * phi[4256];
+      w = fma(1.0, phi[3936], w);
+      w = fma(1.0, phi[4704], w);
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[3104];
+      w = w - phi[4672];
+      const double kw = ws[39200] * w;
+      out[3104] = fma(kw, y[4672], out[3104]);
+      out[4672] = fma(kw, y[3104], out[4672]);
+      ws[175680] = fma(kw * y[3104], y[4672], ws[175680]);
+    }
+    {
+      double w = 0.18 * phi[3616];
+      w = fma(0.65, phi[3488], w);
+      w = fma(0.72, phi[4672], w);
+      w = fma(0.1, phi[3936], w);
+      w = fma(0.1, phi[4736], w);
+      w = fma(0.07, phi[4576], w);
+      w = fma(0.18, phi[4704], w);
+      w = fma(1.0, phi[2944], w);
+      w = w - phi[1088];
+      w = w - phi[4736];
+      const double kw = ws[39232] * w;
+      out[1088] = fma(kw, y[4736], out[1088]);
+      out[4736] = fma(kw, y[1088], out[4736]);
+      ws[175712] = fma(kw * y[1088], y[4736], ws[175712]);
+    }
+    {
+      double w = 0.86 * phi[4608];
+      w = fma(0.14, phi[4032], w);
+      w = fma(0.417, phi[4256], w);
+      w = fma(0.443, phi[4000], w);
+      w = fma(0.66, phi[3936], w);
+      w = fma(0.2, phi[3808], w);
+      w = fma(0.86, phi[4704], w);
+      w = w - phi[3488];
+      w = w - phi[4384];
+      const double kw = ws[39264] * w;
+      out[3488] = fma(kw, y[4384], out[3488]);
+      out[4384] = fma(kw, y[3488], out[4384]);
+      ws[175744] = fma(kw * y[3488], y[4384], ws[175744]);
+    }
+    {
+      double w = 0.48 * phi[4256];
+      w = fma(0.52, phi[4000], w);
+      w = fma(0.77, phi[3936], w);
+      w = fma(0.23, phi[3808], w);
+      w = fma(1.0, phi[4704], w);
+      w = fma(1.0, phi[4416], w);
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[3488];
+      w = w - phi[4448];
+      const double kw = ws[39296] * w;
+      out[3488] = fma(kw, y[4448], out[3488]);
+      out[4448] = fma(kw, y[3488], out[4448]);
+      ws[175776] = fma(kw * y[3488], y[4448], ws[175776]);
+    }
+    {
+      double w = -phi[3488];
+      w = w - phi[4704];
+      const double kw = ws[39328] * w;
+      out[3488] = fma(kw, y[4704], out[3488]);
+      out[4704] = fma(kw, y[3488], out[4704]);
+      ws[175808] = fma(kw * y[3488], y[4704], ws[175808]);
+    }
+    {
+      double w = 0.48 * phi[4256];
+      w = fma(0.52, phi[4000], w);
+      w = fma(0.77, phi[3936], w);
+      w = fma(0.23, phi[3808], w);
+      w = fma(1.0, phi[4704], w);
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[3488];
+      w = w - phi[4672];
+      const double kw = ws[39360] * w;
+      out[3488] = fma(kw, y[4672], out[3488]);
+      out[4672] = fma(kw, y[3488], out[4672]);
+      ws[175840] = fma(kw * y[3488], y[4672], ws[175840]);
+    }
+    {
+      double w = 0.155 * phi[3616];
+      w = fma(0.544, phi[3584], w);
+      w = fma(0.602, phi[4672], w);
+      w = fma(0.244, phi[3808], w);
+      w = fma(0.244, phi[4736], w);
+      w = fma(0.058, phi[4576], w);
+      w = fma(0.155, phi[4704], w);
+      w = fma(1.0, phi[2496], w);
+      w = w - phi[1120];
+      w = w - phi[4736];
+      const double kw = ws[39392] * w;
+      out[1120] = fma(kw, y[4736], out[1120]);
+      out[4736] = fma(kw, y[1120], out[4736]);
+      ws[175872] = fma(kw * y[1120], y[4736], ws[175872]);
+    }
+    {
+      double w = 0.155 * phi[3616];
+      w = fma(0.544, phi[3584], w);
+      w = fma(0.602, phi[4672], w);
+      w = fma(0.244, phi[3808], w);
+      w = fma(0.244, phi[4736], w);
+      w = fma(0.058, phi[4576], w);
+      w = fma(0.155, phi[4704], w);
+      w = fma(1.0, phi[2560], w);
+      w = w - phi[1152];
+      w = w - phi[4736];
+      const double kw = ws[39424] * w;
+      out[1152] = fma(kw, y[4736], out[1152]);
+      out[4736] = fma(kw, y[1152], out[4736]);
+      ws[175904] = fma(kw * y[1152], y[4736], ws[175904]);
+    }
+    {
+      double w = 0.86 * phi[4608];
+      w = fma(0.14, phi[4032], w);
+      w = fma(0.221, phi[4256], w);
+      w = fma(0.675, phi[4000], w);
+      w = fma(0.3, phi[3936], w);
+      w = fma(0.56, phi[3808], w);
+      w = fma(0.86, phi[4704], w);
+      w = w - phi[3584];
+      w = w - phi[4384];
+      const double kw = ws[39456] * w;
+      out[3584] = fma(kw, y[4384], out[3584]);
+      out[4384] = fma(kw, y[3584], out[4384]);
+      ws[175936] = fma(kw * y[3584], y[4384], ws[175936]);
+    }
+    {
+      double w = -phi[3584];
+      w = w - phi[4704];
+      const double kw = ws[39488] * w;
+      out[3584] = fma(kw, y[4704], out[3584]);
+      out[4704] = fma(kw, y[3584], out[4704]);
+      ws[175968] = fma(kw * y[3584], y[4704], ws[175968]);
+    }
+    {
+      double w = 0.26 * phi[4256];
+      w = fma(0.77, phi[4000], w);
+      w = fma(0.35, phi[3936], w);
+      w = fma(0.65, phi[3808], w);
+      w = fma(1.0, phi[4704], w);
+      w = fma(1.0, phi[4416], w);
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[3584];
+      w = w - phi[4448];
+      const double kw = ws[39520] * w;
+      out[3584] = fma(kw, y[4448], out[3584]);
+      out[4448] = fma(kw, y[3584], out[4448]);
+      ws[176000] = fma(kw * y[3584], y[4448], ws[176000]);
+    }
+    {
+      double w = 0.26 * phi[4256];
+      w = fma(0.77, phi[4000], w);
+      w = fma(0.35, phi[3936], w);
+      w = fma(0.65, phi[3808], w);
+      w = fma(1.0, phi[4704], w);
+      w = fma(1.0, phi[4672], w);
+      w = w - phi[3584];
+      w = w - phi[4672];
+      const double kw = ws[39552] * w;
+      out[3584] = fma(kw, y[4672], out[3584]);
+      out[4672] = fma(kw, y[3584], out[4672]);
+      ws[176032] = fma(kw * y[3584], y[4672], ws[176032]);
+    }
+    {
+      double w = 0.025 * phi[4256];
+      w = fma(0.025, phi[3936], w);
+      w = fma(1.0, phi[4704], w);
+      w = fma(0.2, phi[3328], w);
+      w = fma(0.732, phi[1760], w);
+      w = fma(0.02, phi[4288], w);
+      w = fma(0.02, phi[4672], w);
+      w = w - phi[3616];
+      w = w - phi[4736];
+      const double kw = ws[39584] * w;
+      out[3616] = fma(kw, y[4736], out[3616]);
+      out[4736] = fma(kw, y[3616], out[4736]);
+      ws[176064] = fma(kw * y[3616], y[4736], ws[176064]);
+    }
+    {
+      double w = 0.3 * phi[3328];
+      w = fma(1.0, phi[4192], w);
+      w = fma(0.48, phi[4352], w);
+      w = fma(0.12, phi[4576], w);
+      w = fma(0.24, phi[4256], w);
+      w = fma(0.24, phi[4000], w);
+      w = fma(0.48, phi[3744], w);
+      w = fma(0.1, phi[4288], w);
+      w = fma(0.7, phi[4672], w);
+      w = w - phi[3616];
+      w = w - phi[4640];
+      const double kw = ws[39616] * w;
+      out[3616] = fma(kw, y[4640], out[3616]);
+      out[4640] = fma(kw, y[3616], out[4640]);
+      ws[176096] = fma(kw * y[3616], y[4640], ws[176096]);
+    }
+    {
+      double w = 1.0 * phi[2176];
+      w = w - phi[3328];
+      w = w - phi[4608];
+      const double kw = ws[39648] * w;
+      out[3328] = fma(kw, y[4608], out[3328]);
+      out[4608] = fma(kw, y[3328], out[4608]);
+      ws[176128] = fma(kw * y[3328], y[4608], ws[176128]);
+    }
+    {
+      double w = 1.0 * phi[3616];
+      w = w - phi[3328];
+      w = w - phi[4704];
+      const double kw = ws[39680] * w;
+      out[3328] = fma(kw, y[4704], out[3328]);
+      out[4704] = fma(kw, y[3328], out[4704]);
+      ws[176160] = fma(kw * y[3328], y[4704], ws[176160]);
+    }
+    {
+      double w = 1.0 * phi[4032];
+      w = fma(0.5, phi[3328], w);
+      w = w - phi[2176];
+      w = w - phi[4736];
+      const double kw = ws[39712] * w;
+      out[2176] = fma(kw, y[4736], out[2176]);
+      out[4736] = fma(kw, y[2176], out[4736]);
+      ws[176192] = fma(kw * y[2176], y[4736], ws[176192]);
+    }
+}
+}  // namespace mech_cb6r5_ae7_aq

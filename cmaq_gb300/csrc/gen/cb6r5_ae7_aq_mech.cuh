@@ -36,6 +36,16 @@ constexpr int EBI_OFF_YCP = 2575;
 constexpr int EBI_OFF_PROD = 2724;
 constexpr int EBI_OFF_LOSS = 2873;
 constexpr int EBI_OFF_PNEG = 3022;
+constexpr int ADJ_WS_ELEMS = 5657;
+constexpr int ADJ_LAM = 4116;
+constexpr int ADJ_MU1 = 4265;
+constexpr int ADJ_MU2 = 4414;
+constexpr int ADJ_MU3 = 4563;
+constexpr int ADJ_PHI = 4712;
+constexpr int ADJ_TMP = 4861;
+constexpr int ADJ_EMIS = 5010;
+constexpr int ADJ_GE = 5159;
+constexpr int ADJ_GK = 5308;
 constexpr double FLOPS_STEP_DAY = 36947.0;
 constexpr double FLOPS_STEP_NIGHT = 34766.0;
 extern __constant__ int c_inew2old[149];
@@ -81,6 +91,63 @@ __device__ void jacdecomp_1_11(double* __restrict__ ws, double gdtinv);
 __device__ void solve_1_0(double* __restrict__ ws, int rhs);
 __device__ void solve_1_1(double* __restrict__ ws, int rhs);
 __device__ void solve_1_2(double* __restrict__ ws, int rhs);
+__device__ void solve_t_0_0(double* __restrict__ ws, int rhs);
+__device__ void solve_t_0_1(double* __restrict__ ws, int rhs);
+__device__ void solve_t_0_2(double* __restrict__ ws, int rhs);
+__device__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_hess3_0_0(double* __restrict__ ws);
+__device__ void adj_hess3_0_1(double* __restrict__ ws);
+__device__ void adj_hess3_0_2(double* __restrict__ ws);
+__device__ void adj_hess3_0_3(double* __restrict__ ws);
+__device__ void adj_hess3_0_4(double* __restrict__ ws);
+__device__ void adj_hess3_0_5(double* __restrict__ ws);
+__device__ void adj_hess3_0_6(double* __restrict__ ws);
+__device__ void adj_hess3_0_7(double* __restrict__ ws);
+__device__ void adj_hess3_0_8(double* __restrict__ ws);
+__device__ void adj_hess3_0_9(double* __restrict__ ws);
+__device__ void adj_hess3_0_10(double* __restrict__ ws);
+__device__ void adj_hess3_0_11(double* __restrict__ ws);
+__device__ void adj_hess3_0_12(double* __restrict__ ws);
+__device__ void adj_hess3_0_13(double* __restrict__ ws);
+__device__ void adj_hess3_0_14(double* __restrict__ ws);
+__device__ void adj_hess3_0_15(double* __restrict__ ws);
+__device__ void adj_hess3_0_16(double* __restrict__ ws);
+__device__ void adj_hess3_0_17(double* __restrict__ ws);
+__device__ void adj_hess3_0_18(double* __restrict__ ws);
+__device__ void solve_t_1_0(double* __restrict__ ws, int rhs);
+__device__ void solve_t_1_1(double* __restrict__ ws, int rhs);
+__device__ void solve_t_1_2(double* __restrict__ ws, int rhs);
+__device__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_hess3_1_0(double* __restrict__ ws);
+__device__ void adj_hess3_1_1(double* __restrict__ ws);
+__device__ void adj_hess3_1_2(double* __restrict__ ws);
+__device__ void adj_hess3_1_3(double* __restrict__ ws);
+__device__ void adj_hess3_1_4(double* __restrict__ ws);
+__device__ void adj_hess3_1_5(double* __restrict__ ws);
+__device__ void adj_hess3_1_6(double* __restrict__ ws);
+__device__ void adj_hess3_1_7(double* __restrict__ ws);
+__device__ void adj_hess3_1_8(double* __restrict__ ws);
+__device__ void adj_hess3_1_9(double* __restrict__ ws);
+__device__ void adj_hess3_1_10(double* __restrict__ ws);
+__device__ void adj_hess3_1_11(double* __restrict__ ws);
+__device__ void adj_hess3_1_12(double* __restrict__ ws);
+__device__ void adj_hess3_1_13(double* __restrict__ ws);
+__device__ void adj_hess3_1_14(double* __restrict__ ws);
+__device__ void adj_hess3_1_15(double* __restrict__ ws);
+__device__ void adj_hess3_1_16(double* __restrict__ ws);
 constexpr int EBI_N_EBISP = 136;
 constexpr double EBI_DELTAT = 2.5;
 constexpr int EBI_NEBITER = 1000;
@@ -110,11 +177,49 @@ __device__ __forceinline__ void jacdecomp_0(double* __restrict__ ws, double gdti
     jacdecomp_0_11(ws, gdtinv);
     jacdecomp_0_12(ws, gdtinv);
 }
+__device__ __forceinline__ void jacdecomp_0_sync(double* __restrict__ ws, double gdtinv, bool go)
+{
+    if (go) jacdecomp_0_0(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_1(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_2(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_3(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_4(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_5(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_6(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_7(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_8(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_9(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_10(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_11(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_12(ws, gdtinv);
+    __syncthreads();
+}
 __device__ __forceinline__ void solve_0(double* __restrict__ ws, int rhs)
 {
     solve_0_0(ws, rhs);
     solve_0_1(ws, rhs);
     solve_0_2(ws, rhs);
+}
+__device__ __forceinline__ void solve_0_sync(double* __restrict__ ws, int rhs, bool go)
+{
+    if (go) solve_0_0(ws, rhs);
+    __syncthreads();
+    if (go) solve_0_1(ws, rhs);
+    __syncthreads();
+    if (go) solve_0_2(ws, rhs);
+    __syncthreads();
 }
 __device__ __forceinline__ void jacdecomp_1(double* __restrict__ ws, double gdtinv)
 {
@@ -131,11 +236,122 @@ __device__ __forceinline__ void jacdecomp_1(double* __restrict__ ws, double gdti
     jacdecomp_1_10(ws, gdtinv);
     jacdecomp_1_11(ws, gdtinv);
 }
+__device__ __forceinline__ void jacdecomp_1_sync(double* __restrict__ ws, double gdtinv, bool go)
+{
+    if (go) jacdecomp_1_0(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_1(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_2(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_3(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_4(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_5(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_6(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_7(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_8(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_9(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_10(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_11(ws, gdtinv);
+    __syncthreads();
+}
 __device__ __forceinline__ void solve_1(double* __restrict__ ws, int rhs)
 {
     solve_1_0(ws, rhs);
     solve_1_1(ws, rhs);
     solve_1_2(ws, rhs);
+}
+__device__ __forceinline__ void solve_1_sync(double* __restrict__ ws, int rhs, bool go)
+{
+    if (go) solve_1_0(ws, rhs);
+    __syncthreads();
+    if (go) solve_1_1(ws, rhs);
+    __syncthreads();
+    if (go) solve_1_2(ws, rhs);
+    __syncthreads();
+}
+__device__ __forceinline__ void solve_t_0(double* __restrict__ ws, int rhs)
+{
+    solve_t_0_0(ws, rhs);
+    solve_t_0_1(ws, rhs);
+    solve_t_0_2(ws, rhs);
+}
+__device__ __forceinline__ void adj_jtv_0(double* __restrict__ ws, int yoff, int phioff, int outoff)
+{
+    adj_jtv_0_0(ws, yoff, phioff, outoff);
+    adj_jtv_0_1(ws, yoff, phioff, outoff);
+    adj_jtv_0_2(ws, yoff, phioff, outoff);
+    adj_jtv_0_3(ws, yoff, phioff, outoff);
+    adj_jtv_0_4(ws, yoff, phioff, outoff);
+    adj_jtv_0_5(ws, yoff, phioff, outoff);
+    adj_jtv_0_6(ws, yoff, phioff, outoff);
+    adj_jtv_0_7(ws, yoff, phioff, outoff);
+}
+__device__ __forceinline__ void adj_hess3_0(double* __restrict__ ws)
+{
+    adj_hess3_0_0(ws);
+    adj_hess3_0_1(ws);
+    adj_hess3_0_2(ws);
+    adj_hess3_0_3(ws);
+    adj_hess3_0_4(ws);
+    adj_hess3_0_5(ws);
+    adj_hess3_0_6(ws);
+    adj_hess3_0_7(ws);
+    adj_hess3_0_8(ws);
+    adj_hess3_0_9(ws);
+    adj_hess3_0_10(ws);
+    adj_hess3_0_11(ws);
+    adj_hess3_0_12(ws);
+    adj_hess3_0_13(ws);
+    adj_hess3_0_14(ws);
+    adj_hess3_0_15(ws);
+    adj_hess3_0_16(ws);
+    adj_hess3_0_17(ws);
+    adj_hess3_0_18(ws);
+}
+__device__ __forceinline__ void solve_t_1(double* __restrict__ ws, int rhs)
+{
+    solve_t_1_0(ws, rhs);
+    solve_t_1_1(ws, rhs);
+    solve_t_1_2(ws, rhs);
+}
+__device__ __forceinline__ void adj_jtv_1(double* __restrict__ ws, int yoff, int phioff, int outoff)
+{
+    adj_jtv_1_0(ws, yoff, phioff, outoff);
+    adj_jtv_1_1(ws, yoff, phioff, outoff);
+    adj_jtv_1_2(ws, yoff, phioff, outoff);
+    adj_jtv_1_3(ws, yoff, phioff, outoff);
+    adj_jtv_1_4(ws, yoff, phioff, outoff);
+    adj_jtv_1_5(ws, yoff, phioff, outoff);
+    adj_jtv_1_6(ws, yoff, phioff, outoff);
+}
+__device__ __forceinline__ void adj_hess3_1(double* __restrict__ ws)
+{
+    adj_hess3_1_0(ws);
+    adj_hess3_1_1(ws);
+    adj_hess3_1_2(ws);
+    adj_hess3_1_3(ws);
+    adj_hess3_1_4(ws);
+    adj_hess3_1_5(ws);
+    adj_hess3_1_6(ws);
+    adj_hess3_1_7(ws);
+    adj_hess3_1_8(ws);
+    adj_hess3_1_9(ws);
+    adj_hess3_1_10(ws);
+    adj_hess3_1_11(ws);
+    adj_hess3_1_12(ws);
+    adj_hess3_1_13(ws);
+    adj_hess3_1_14(ws);
+    adj_hess3_1_15(ws);
+    adj_hess3_1_16(ws);
 }
 struct Traits {
     static constexpr int NSPEC = mech_cb6r5_ae7_aq::NSPEC;
@@ -163,6 +379,16 @@ struct Traits {
     static constexpr int EBI_OFF_PROD = mech_cb6r5_ae7_aq::EBI_OFF_PROD;
     static constexpr int EBI_OFF_LOSS = mech_cb6r5_ae7_aq::EBI_OFF_LOSS;
     static constexpr int EBI_OFF_PNEG = mech_cb6r5_ae7_aq::EBI_OFF_PNEG;
+    static constexpr int ADJ_WS_ELEMS = mech_cb6r5_ae7_aq::ADJ_WS_ELEMS;
+    static constexpr int ADJ_LAM = mech_cb6r5_ae7_aq::ADJ_LAM;
+    static constexpr int ADJ_MU1 = mech_cb6r5_ae7_aq::ADJ_MU1;
+    static constexpr int ADJ_MU2 = mech_cb6r5_ae7_aq::ADJ_MU2;
+    static constexpr int ADJ_MU3 = mech_cb6r5_ae7_aq::ADJ_MU3;
+    static constexpr int ADJ_PHI = mech_cb6r5_ae7_aq::ADJ_PHI;
+    static constexpr int ADJ_TMP = mech_cb6r5_ae7_aq::ADJ_TMP;
+    static constexpr int ADJ_EMIS = mech_cb6r5_ae7_aq::ADJ_EMIS;
+    static constexpr int ADJ_GE = mech_cb6r5_ae7_aq::ADJ_GE;
+    static constexpr int ADJ_GK = mech_cb6r5_ae7_aq::ADJ_GK;
     static constexpr const char* name() { return mech_cb6r5_ae7_aq::NAME; }
     static __device__ __forceinline__ int iold2new(int s) { return mech_cb6r5_ae7_aq::c_iold2new[s]; }
     static __device__ __forceinline__ int inew2old(int i) { return mech_cb6r5_ae7_aq::c_inew2old[i]; }
@@ -170,10 +396,33 @@ struct Traits {
     static __device__ __forceinline__ void explic_0(double* ws) { mech_cb6r5_ae7_aq::explic_0(ws); }
     static __device__ __forceinline__ void jacdecomp_0(double* ws, double g) { mech_cb6r5_ae7_aq::jacdecomp_0(ws, g); }
     static __device__ __forceinline__ void solve_0(double* ws, int r) { mech_cb6r5_ae7_aq::solve_0(ws, r); }
+    static __device__ __forceinline__ void jacdecomp_0_sync(double* ws, double g, bool go) { mech_cb6r5_ae7_aq::jacdecomp_0_sync(ws, g, go); }
+    static __device__ __forceinline__ void solve_0_sync(double* ws, int r, bool go) { mech_cb6r5_ae7_aq::solve_0_sync(ws, r, go); }
+    static __device__ __forceinline__ void solve_t_0(double* ws, int r) { mech_cb6r5_ae7_aq::solve_t_0(ws, r); }
+    static __device__ __forceinline__ void adj_jtv_0(double* ws, int y, int phi, int out) { mech_cb6r5_ae7_aq::adj_jtv_0(ws, y, phi, out); }
+    static __device__ __forceinline__ void adj_hess3_0(double* ws) { mech_cb6r5_ae7_aq::adj_hess3_0(ws); }
     static __device__ __forceinline__ void feval_1(double* ws, int s, int t) { mech_cb6r5_ae7_aq::feval_1(ws, s, t); }
     static __device__ __forceinline__ void explic_1(double* ws) { mech_cb6r5_ae7_aq::explic_1(ws); }
     static __device__ __forceinline__ void jacdecomp_1(double* ws, double g) { mech_cb6r5_ae7_aq::jacdecomp_1(ws, g); }
     static __device__ __forceinline__ void solve_1(double* ws, int r) { mech_cb6r5_ae7_aq::solve_1(ws, r); }
+    static __device__ __forceinline__ void jacdecomp_1_sync(double* ws, double g, bool go) { mech_cb6r5_ae7_aq::jacdecomp_1_sync(ws, g, go); }
+    static __device__ __forceinline__ void solve_1_sync(double* ws, int r, bool go) { mech_cb6r5_ae7_aq::solve_1_sync(ws, r, go); }
+    static __device__ __forceinline__ void solve_t_1(double* ws, int r) { mech_cb6r5_ae7_aq::solve_t_1(ws, r); }
+    static __device__ __forceinline__ void adj_jtv_1(double* ws, int y, int phi, int out) { mech_cb6r5_ae7_aq::adj_jtv_1(ws, y, phi, out); }
+    static __device__ __forceinline__ void adj_hess3_1(double* ws) { mech_cb6r5_ae7_aq::adj_hess3_1(ws); }
+    static constexpr int EBI_N_EBISP = mech_cb6r5_ae7_aq::EBI_N_EBISP;
+    static constexpr int EBI_NEBITER = mech_cb6r5_ae7_aq::EBI_NEBITER;
+    static constexpr int EBI_NPNEG = mech_cb6r5_ae7_aq::EBI_NPNEG;
+    static constexpr double EBI_DELTAT = mech_cb6r5_ae7_aq::EBI_DELTAT;
+    static __device__ __forceinline__ int ebi_ebisp(int e) { return mech_cb6r5_ae7_aq::c_ebi_ebisp[e]; }
+    static __device__ __forceinline__ double ebi_rtol(int i) { return mech_cb6r5_ae7_aq::c_ebi_rtol[i]; }
+    static __device__ __forceinline__ int ebi_pneg(int k) { return mech_cb6r5_ae7_aq::c_ebi_pneg[k]; }
+    static __device__ __forceinline__ void ebi_hrrates(double* ws) { mech_cb6r5_ae7_aq::ebi_hrrates(ws); }
+    static __device__ __forceinline__ void ebi_hrprodloss(double* ws) { mech_cb6r5_ae7_aq::ebi_hrprodloss(ws); }
+    static __device__ __forceinline__ void ebi_hrg1(double* ws, double dtc) { mech_cb6r5_ae7_aq::ebi_hrg1(ws, dtc); }
+    static __device__ __forceinline__ void ebi_hrg2(double* ws, double dtc) { mech_cb6r5_ae7_aq::ebi_hrg2(ws, dtc); }
+    static __device__ __forceinline__ void ebi_hrg3(double* ws, double dtc) { mech_cb6r5_ae7_aq::ebi_hrg3(ws, dtc); }
+    static __device__ __forceinline__ void ebi_hrg4(double* ws, double dtc) { mech_cb6r5_ae7_aq::ebi_hrg4(ws, dtc); }
     static __device__ __forceinline__ void rconst(double* ws, double t, double p, double h, double sw, int sun,
                                                   const double* rj, const double* het) { mech_cb6r5_ae7_aq::rconst(ws, t, p, h, sw, sun, rj, het); }
 };

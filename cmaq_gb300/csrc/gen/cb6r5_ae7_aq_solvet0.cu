@@ -1,0 +1,2679 @@
+// Generated by cmaq_gb300.mechgen.generate from CCTM/src/MECHS/cb6r5_ae7_aq/RXNS_DATA_MODULE.F90
+// and RXNS_FUNC_MODULE.F90 (sha256/16 4242f44b2527a299).  Do not edit.
+#include "cb6r5_ae7_aq_mech.cuh"
+#include <math.h>
+namespace mech_cb6r5_ae7_aq {
+__device__ __noinline__ void solve_t_0_0(double* __restrict__ ws, int rhs)
+{
+    const double* __restrict__ lu = ws + 72864;
+    const double* __restrict__ vd = ws + 126944;
+    double* __restrict__ b = ws + rhs * 32;
+    (void)vd;
+    {
+      double x = b[0];
+      b[0] = x * CHEM_LDLU(vd + 0);
+    }
+    {
+      double x = b[32];
+      b[32] = x * CHEM_LDLU(vd + 32);
+    }
+    {
+      double x = b[64];
+      b[64] = x * CHEM_LDLU(vd + 64);
+    }
+    {
+      double x = b[96];
+      b[96] = x * CHEM_LDLU(vd + 96);
+    }
+    {
+      double x = b[128];
+      b[128] = x * CHEM_LDLU(vd + 128);
+    }
+    {
+      double x = b[160];
+      b[160] = x * CHEM_LDLU(vd + 160);
+    }
+    {
+      double x = b[192];
+      b[192] = x * CHEM_LDLU(vd + 192);
+    }
+    {
+      double x = b[224];
+      b[224] = x * CHEM_LDLU(vd + 224);
+    }
+    {
+      double x = b[256];
+      b[256] = x * CHEM_LDLU(vd + 256);
+    }
+    {
+      double x = b[288];
+      b[288] = x * CHEM_LDLU(vd + 288);
+    }
+    {
+      double x = b[320];
+      b[320] = x * CHEM_LDLU(vd + 320);
+    }
+    {
+      double x = b[352];
+      b[352] = x * CHEM_LDLU(vd + 352);
+    }
+    {
+      double x = b[384];
+      b[384] = x * CHEM_LDLU(vd + 384);
+    }
+    {
+      double x = b[416];
+      b[416] = x * CHEM_LDLU(vd + 416);
+    }
+    {
+      double x = b[448];
+      b[448] = x * CHEM_LDLU(vd + 448);
+    }
+    {
+      double x = b[480];
+      b[480] = x * CHEM_LDLU(vd + 480);
+    }
+    {
+      double x = b[512];
+      b[512] = x * CHEM_LDLU(vd + 512);
+    }
+    {
+      double x = b[544];
+      b[544] = x * CHEM_LDLU(vd + 544);
+    }
+    {
+      double x = b[576];
+      b[576] = x * CHEM_LDLU(vd + 576);
+    }
+    {
+      double x = b[608];
+      b[608] = x * CHEM_LDLU(vd + 608);
+    }
+    {
+      double x = b[640];
+      b[640] = x * CHEM_LDLU(vd + 640);
+    }
+    {
+      double x = b[672];
+      b[672] = x * CHEM_LDLU(vd + 672);
+    }
+    {
+      double x = b[704];
+      b[704] = x * CHEM_LDLU(vd + 704);
+    }
+    {
+      double x = b[736];
+      b[736] = x * CHEM_LDLU(vd + 736);
+    }
+    {
+      double x = b[768];
+      b[768] = x * CHEM_LDLU(vd + 768);
+    }
+    {
+      double x = b[800];
+      b[800] = x * CHEM_LDLU(vd + 800);
+    }
+    {
+      double x = b[832];
+      b[832] = x * CHEM_LDLU(vd + 832);
+    }
+    {
+      double x = b[864];
+      b[864] = x * CHEM_LDLU(vd + 864);
+    }
+    {
+      double x = b[896];
+      b[896] = x * CHEM_LDLU(vd + 896);
+    }
+    {
+      double x = b[928];
+      b[928] = x * CHEM_LDLU(vd + 928);
+    }
+    {
+      double x = b[960];
+      x = fma(-CHEM_LDLU(lu + 49152), b[320], x);
+      b[960] = x * CHEM_LDLU(vd + 960);
+    }
+    {
+      double x = b[992];
+      b[992] = x * CHEM_LDLU(vd + 992);
+    }
+    {
+      double x = b[1024];
+      b[1024] = x * CHEM_LDLU(vd + 1024);
+    }
+    {
+      double x = b[1056];
+      b[1056] = x * CHEM_LDLU(vd + 1056);
+    }
+    {
+      double x = b[1088];
+      b[1088] = x * CHEM_LDLU(vd + 1088);
+    }
+    {
+      double x = b[1120];
+      b[1120] = x * CHEM_LDLU(vd + 1120);
+    }
+    {
+      double x = b[1152];
+      b[1152] = x * CHEM_LDLU(vd + 1152);
+    }
+    {
+      double x = b[1184];
+      b[1184] = x * CHEM_LDLU(vd + 1184);
+    }
+    {
+      double x = b[1216];
+      b[1216] = x * CHEM_LDLU(vd + 1216);
+    }
+    {
+      double x = b[1248];
+      x = fma(-CHEM_LDLU(lu + 48928), b[544], x);
+      b[1248] = x * CHEM_LDLU(vd + 1248);
+    }
+    {
+      double x = b[1280];
+      x = fma(-CHEM_LDLU(lu + 47744), b[1248], x);
+      b[1280] = x * CHEM_LDLU(vd + 1280);
+    }
+    {
+      double x = b[1312];
+      x = fma(-CHEM_LDLU(lu + 48896), b[576], x);
+      x = fma(-CHEM_LDLU(lu + 48864), b[608], x);
+      b[1312] = x * CHEM_LDLU(vd + 1312);
+    }
+    {
+      double x = b[1344];
+      b[1344] = x * CHEM_LDLU(vd + 1344);
+    }
+    {
+      double x = b[1376];
+      b[1376] = x * CHEM_LDLU(vd + 1376);
+    }
+    {
+      double x = b[1408];
+      b[1408] = x * CHEM_LDLU(vd + 1408);
+    }
+    {
+      double x = b[1440];
+      b[1440] = x * CHEM_LDLU(vd + 1440);
+    }
+    {
+      double x = b[1472];
+      b[1472] = x * CHEM_LDLU(vd + 1472);
+    }
+    {
+      double x = b[1504];
+      b[1504] = x * CHEM_LDLU(vd + 1504);
+    }
+    {
+      double x = b[1536];
+      b[1536] = x * CHEM_LDLU(vd + 1536);
+    }
+    {
+      double x = b[1568];
+      b[1568] = x * CHEM_LDLU(vd + 1568);
+    }
+    {
+      double x = b[1600];
+      b[1600] = x * CHEM_LDLU(vd + 1600);
+    }
+    {
+      double x = b[1632];
+      b[1632] = x * CHEM_LDLU(vd + 1632);
+    }
+    {
+      double x = b[1664];
+      x = fma(-CHEM_LDLU(lu + 48096), b[1056], x);
+      x = fma(-CHEM_LDLU(lu + 47616), b[1312], x);
+      b[1664] = x * CHEM_LDLU(vd + 1664);
+    }
+    {
+      double x = b[1696];
+      b[1696] = x * CHEM_LDLU(vd + 1696);
+    }
+    {
+      double x = b[1728];
+      b[1728] = x * CHEM_LDLU(vd + 1728);
+    }
+    {
+      double x = b[1760];
+      b[1760] = x * CHEM_LDLU(vd + 1760);
+    }
+    {
+      double x = b[1792];
+      b[1792] = x * CHEM_LDLU(vd + 1792);
+    }
+    {
+      double x = b[1824];
+      b[1824] = x * CHEM_LDLU(vd + 1824);
+    }
+    {
+      double x = b[1856];
+      b[1856] = x * CHEM_LDLU(vd + 1856);
+    }
+    {
+      double x = b[1888];
+      b[1888] = x * CHEM_LDLU(vd + 1888);
+    }
+    {
+      double x = b[1920];
+      x = fma(-CHEM_LDLU(lu + 48992), b[480], x);
+      x = fma(-CHEM_LDLU(lu + 48960), b[512], x);
+      b[1920] = x * CHEM_LDLU(vd + 1920);
+    }
+    {
+      double x = b[1952];
+      b[1952] = x * CHEM_LDLU(vd + 1952);
+    }
+    {
+      double x = b[1984];
+      x = fma(-CHEM_LDLU(lu + 48320), b[960], x);
+      b[1984] = x * CHEM_LDLU(vd + 1984);
+    }
+    {
+      double x = b[2016];
+      x = fma(-CHEM_LDLU(lu + 47168), b[1600], x);
+      b[2016] = x * CHEM_LDLU(vd + 2016);
+    }
+    {
+      double x = b[2048];
+      b[2048] = x * CHEM_LDLU(vd + 2048);
+    }
+    {
+      double x = b[2080];
+      b[2080] = x * CHEM_LDLU(vd + 2080);
+    }
+    {
+      double x = b[2112];
+      x = fma(-CHEM_LDLU(lu + 45664), b[2080], x);
+      b[2112] = x * CHEM_LDLU(vd + 2112);
+    }
+    {
+      double x = b[2144];
+      b[2144] = x * CHEM_LDLU(vd + 2144);
+    }
+    {
+      double x = b[2176];
+      b[2176] = x * CHEM_LDLU(vd + 2176);
+    }
+    {
+      double x = b[2208];
+      x = fma(-CHEM_LDLU(lu + 49248), b[256], x);
+      x = fma(-CHEM_LDLU(lu + 49184), b[288], x);
+      b[2208] = x * CHEM_LDLU(vd + 2208);
+    }
+    {
+      double x = b[2240];
+      b[2240] = x * CHEM_LDLU(vd + 2240);
+    }
+    {
+      double x = b[2272];
+      b[2272] = x * CHEM_LDLU(vd + 2272);
+    }
+    {
+      double x = b[2304];
+      b[2304] = x * CHEM_LDLU(vd + 2304);
+    }
+    {
+      double x = b[2336];
+      b[2336] = x * CHEM_LDLU(vd + 2336);
+    }
+    {
+      double x = b[2368];
+      b[2368] = x * CHEM_LDLU(vd + 2368);
+    }
+    {
+      double x = b[2400];
+      b[2400] = x * CHEM_LDLU(vd + 2400);
+    }
+    {
+      double x = b[2432];
+      b[2432] = x * CHEM_LDLU(vd + 2432);
+    }
+    {
+      double x = b[2464];
+      b[2464] = x * CHEM_LDLU(vd + 2464);
+    }
+    {
+      double x = b[2496];
+      x = fma(-CHEM_LDLU(lu + 45024), b[2240], x);
+      b[2496] = x * CHEM_LDLU(vd + 2496);
+    }
+    {
+      double x = b[2528];
+      x = fma(-CHEM_LDLU(lu + 48224), b[992], x);
+      b[2528] = x * CHEM_LDLU(vd + 2528);
+    }
+    {
+      double x = b[2560];
+      x = fma(-CHEM_LDLU(lu + 45056), b[2240], x);
+      b[2560] = x * CHEM_LDLU(vd + 2560);
+    }
+    {
+      double x = b[2592];
+      b[2592] = x * CHEM_LDLU(vd + 2592);
+    }
+    {
+      double x = b[2624];
+      b[2624] = x * CHEM_LDLU(vd + 2624);
+    }
+    {
+      double x = b[2656];
+      b[2656] = x * CHEM_LDLU(vd + 2656);
+    }
+    {
+      double x = b[2688];
+      b[2688] = x * CHEM_LDLU(vd + 2688);
+    }
+    {
+      double x = b[2720];
+      b[2720] = x * CHEM_LDLU(vd + 2720);
+    }
+    {
+      double x = b[2752];
+      x = fma(-CHEM_LDLU(lu + 47424), b[1504], x);
+      x = fma(-CHEM_LDLU(lu + 44736), b[2304], x);
+      b[2752] = x * CHEM_LDLU(vd + 2752);
+    }
+    {
+      double x = b[2784];
+      x = fma(-CHEM_LDLU(lu + 44768), b[2304], x);
+      x = fma(-CHEM_LDLU(lu + 42848), b[2752], x);
+      b[2784] = x * CHEM_LDLU(vd + 2784);
+    }
+    {
+      double x = b[2816];
+      x = fma(-CHEM_LDLU(lu + 44800), b[2304], x);
+      x = fma(-CHEM_LDLU(lu + 42880), b[2752], x);
+      x = fma(-CHEM_LDLU(lu + 42784), b[2784], x);
+      b[2816] = x * CHEM_LDLU(vd + 2816);
+    }
+    {
+      double x = b[2848];
+      b[2848] = x * CHEM_LDLU(vd + 2848);
+    }
+    {
+      double x = b[2880];
+      b[2880] = x * CHEM_LDLU(vd + 2880);
+    }
+    {
+      double x = b[2912];
+      b[2912] = x * CHEM_LDLU(vd + 2912);
+    }
+    {
+      double x = b[2944];
+      x = fma(-CHEM_LDLU(lu + 45088), b[2240], x);
+      x = fma(-CHEM_LDLU(lu + 43424), b[2624], x);
+      b[2944] = x * CHEM_LDLU(vd + 2944);
+    }
+    {
+      double x = b[2976];
+      b[2976] = x * CHEM_LDLU(vd + 2976);
+    }
+    {
+      double x = b[3008];
+      x = fma(-CHEM_LDLU(lu + 47840), b[1184], x);
+      x = fma(-CHEM_LDLU(lu + 47264), b[1568], x);
+      b[3008] = x * CHEM_LDLU(vd + 3008);
+    }
+    {
+      double x = b[3040];
+      b[3040] = x * CHEM_LDLU(vd + 3040);
+    }
+    {
+      double x = b[3072];
+      b[3072] = x * CHEM_LDLU(vd + 3072);
+    }
+    {
+      double x = b[3104];
+      b[3104] = x * CHEM_LDLU(vd + 3104);
+    }
+    {
+      double x = b[3136];
+      b[3136] = x * CHEM_LDLU(vd + 3136);
+    }
+    {
+      double x = b[3168];
+      x = fma(-CHEM_LDLU(lu + 42208), b[2912], x);
+      b[3168] = x * CHEM_LDLU(vd + 3168);
+    }
+    {
+      double x = b[3200];
+      x = fma(-CHEM_LDLU(lu + 42240), b[2912], x);
+      x = fma(-CHEM_LDLU(lu + 40992), b[3168], x);
+      b[3200] = x * CHEM_LDLU(vd + 3200);
+    }
+    {
+      double x = b[3232];
+      b[3232] = x * CHEM_LDLU(vd + 3232);
+    }
+    {
+      double x = b[3264];
+      b[3264] = x * CHEM_LDLU(vd + 3264);
+    }
+    {
+      double x = b[3296];
+      b[3296] = x * CHEM_LDLU(vd + 3296);
+    }
+    {
+      double x = b[3328];
+      x = fma(-CHEM_LDLU(lu + 45312), b[2176], x);
+      x = fma(-CHEM_LDLU(lu + 44064), b[2464], x);
+      b[3328] = x * CHEM_LDLU(vd + 3328);
+    }
+    {
+      double x = b[3360];
+      b[3360] = x * CHEM_LDLU(vd + 3360);
+    }
+    {
+      double x = b[3392];
+      b[3392] = x * CHEM_LDLU(vd + 3392);
+    }
+    {
+      double x = b[3424];
+      x = fma(-CHEM_LDLU(lu + 48160), b[1024], x);
+      x = fma(-CHEM_LDLU(lu + 47072), b[1632], x);
+      x = fma(-CHEM_LDLU(lu + 46976), b[1664], x);
+      x = fma(-CHEM_LDLU(lu + 41120), b[3136], x);
+      x = fma(-CHEM_LDLU(lu + 40640), b[3232], x);
+      x = fma(-CHEM_LDLU(lu + 40320), b[3296], x);
+      b[3424] = x * CHEM_LDLU(vd + 3424);
+    }
+    {
+      double x = b[3456];
+      x = fma(-CHEM_LDLU(lu + 41792), b[3008], x);
+      x = fma(-CHEM_LDLU(lu + 41632), b[3040], x);
+      b[3456] = x * CHEM_LDLU(vd + 3456);
+    }
+    {
+      double x = b[3488];
+      b[3488] = x * CHEM_LDLU(vd + 3488);
+    }
+    {
+      double x = b[3520];
+      x = fma(-CHEM_LDLU(lu + 47872), b[1184], x);
+      x = fma(-CHEM_LDLU(lu + 47776), b[1216], x);
+      x = fma(-CHEM_LDLU(lu + 46496), b[1824], x);
+      x = fma(-CHEM_LDLU(lu + 41824), b[3008], x);
+      x = fma(-CHEM_LDLU(lu + 41664), b[3040], x);
+      x = fma(-CHEM_LDLU(lu + 39072), b[3456], x);
+      b[3520] = x * CHEM_LDLU(vd + 3520);
+    }
+    {
+      double x = b[3552];
+      x = fma(-CHEM_LDLU(lu + 40672), b[3232], x);
+      x = fma(-CHEM_LDLU(lu + 39104), b[3456], x);
+      b[3552] = x * CHEM_LDLU(vd + 3552);
+    }
+    {
+      double x = b[3584];
+      b[3584] = x * CHEM_LDLU(vd + 3584);
+    }
+    {
+      double x = b[3616];
+      x = fma(-CHEM_LDLU(lu + 46688), b[1760], x);
+      x = fma(-CHEM_LDLU(lu + 40160), b[3328], x);
+      b[3616] = x * CHEM_LDLU(vd + 3616);
+    }
+    {
+      double x = b[3648];
+      b[3648] = x * CHEM_LDLU(vd + 3648);
+    }
+    {
+      double x = b[3680];
+      x = fma(-CHEM_LDLU(lu + 42272), b[2912], x);
+      x = fma(-CHEM_LDLU(lu + 41024), b[3168], x);
+      x = fma(-CHEM_LDLU(lu + 40896), b[3200], x);
+      b[3680] = x * CHEM_LDLU(vd + 3680);
+    }
+    {
+      double x = b[3712];
+      x = fma(-CHEM_LDLU(lu + 42304), b[2912], x);
+      x = fma(-CHEM_LDLU(lu + 41056), b[3168], x);
+      x = fma(-CHEM_LDLU(lu + 40928), b[3200], x);
+      x = fma(-CHEM_LDLU(lu + 37472), b[3680], x);
+      b[3712] = x * CHEM_LDLU(vd + 3712);
+    }
+    {
+      double x = b[3744];
+      x = fma(-CHEM_LDLU(lu + 46592), b[1792], x);
+      x = fma(-CHEM_LDLU(lu + 43104), b[2688], x);
+      b[3744] = x * CHEM_LDLU(vd + 3744);
+    }
+    {
+      double x = b[3776];
+      b[3776] = x * CHEM_LDLU(vd + 3776);
+    }
+    {
+      double x = b[3808];
+      b[3808] = x * CHEM_LDLU(vd + 3808);
+    }
+    {
+      double x = b[3840];
+      x = fma(-CHEM_LDLU(lu + 42944), b[2720], x);
+      b[3840] = x * CHEM_LDLU(vd + 3840);
+    }
+    {
+      double x = b[3872];
+      x = fma(-CHEM_LDLU(lu + 39712), b[3392], x);
+      x = fma(-CHEM_LDLU(lu + 38304), b[3552], x);
+      x = fma(-CHEM_LDLU(lu + 37536), b[3648], x);
+      x = fma(-CHEM_LDLU(lu + 37120), b[3744], x);
+      x = fma(-CHEM_LDLU(lu + 36768), b[3776], x);
+      x = fma(-CHEM_LDLU(lu + 36192), b[3840], x);
+      b[3872] = x * CHEM_LDLU(vd + 3872);
+    }
+    {
+      double x = b[3904];
+      b[3904] = x * CHEM_LDLU(vd + 3904);
+    }
+    {
+      double x = b[3936];
+      x = fma(-CHEM_LDLU(lu + 37152), b[3744], x);
+      x = fma(-CHEM_LDLU(lu + 35392), b[3904], x);
+      b[3936] = x * CHEM_LDLU(vd + 3936);
+    }
+    {
+      double x = b[3968];
+      b[3968] = x * CHEM_LDLU(vd + 3968);
+    }
+    {
+      double x = b[4000];
+      x = fma(-CHEM_LDLU(lu + 48800), b[640], x);
+      b[4000] = x * CHEM_LDLU(vd + 4000);
+    }
+    {
+      double x = b[4032];
+      b[4032] = x * CHEM_LDLU(vd + 4032);
+    }
+    {
+      double x = b[4064];
+      x = fma(-CHEM_LDLU(lu + 34656), b[3968], x);
+      b[4064] = x * CHEM_LDLU(vd + 4064);
+    }
+    {
+      double x = b[4096];
+      x = fma(-CHEM_LDLU(lu + 46144), b[1952], x);
+      x = fma(-CHEM_LDLU(lu + 43136), b[2688], x);
+      x = fma(-CHEM_LDLU(lu + 35424), b[3904], x);
+      b[4096] = x * CHEM_LDLU(vd + 4096);
+    }
+    {
+      double x = b[4128];
+      x = fma(-CHEM_LDLU(lu + 34688), b[3968], x);
+      b[4128] = x * CHEM_LDLU(vd + 4128);
+    }
+    {
+      double x = b[4160];
+      x = fma(-CHEM_LDLU(lu + 45824), b[2048], x);
+      x = fma(-CHEM_LDLU(lu + 45696), b[2080], x);
+      x = fma(-CHEM_LDLU(lu + 45536), b[2112], x);
+      x = fma(-CHEM_LDLU(lu + 44608), b[2336], x);
+      x = fma(-CHEM_LDLU(lu + 44480), b[2368], x);
+      x = fma(-CHEM_LDLU(lu + 43776), b[2528], x);
+      x = fma(-CHEM_LDLU(lu + 43264), b[2656], x);
+      x = fma(-CHEM_LDLU(lu + 42528), b[2848], x);
+      x = fma(-CHEM_LDLU(lu + 41152), b[3136], x);
+      x = fma(-CHEM_LDLU(lu + 40704), b[3232], x);
+      x = fma(-CHEM_LDLU(lu + 39904), b[3360], x);
+      x = fma(-CHEM_LDLU(lu + 39424), b[3424], x);
+      x = fma(-CHEM_LDLU(lu + 39136), b[3456], x);
+      x = fma(-CHEM_LDLU(lu + 38336), b[3552], x);
+      x = fma(-CHEM_LDLU(lu + 37568), b[3648], x);
+      x = fma(-CHEM_LDLU(lu + 36800), b[3776], x);
+      x = fma(-CHEM_LDLU(lu + 36224), b[3840], x);
+      x = fma(-CHEM_LDLU(lu + 35904), b[3872], x);
+      x = fma(-CHEM_LDLU(lu + 35456), b[3904], x);
+      x = fma(-CHEM_LDLU(lu + 34720), b[3968], x);
+      x = fma(-CHEM_LDLU(lu + 34336), b[4000], x);
+      x = fma(-CHEM_LDLU(lu + 33952), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 33600), b[4064], x);
+      x = fma(-CHEM_LDLU(lu + 33248), b[4096], x);
+      x = fma(-CHEM_LDLU(lu + 32896), b[4128], x);
+      b[4160] = x * CHEM_LDLU(vd + 4160);
+    }
+    {
+      double x = b[4192];
+      b[4192] = x * CHEM_LDLU(vd + 4192);
+    }
+    {
+      double x = b[4224];
+      x = fma(-CHEM_LDLU(lu + 46048), b[1984], x);
+      x = fma(-CHEM_LDLU(lu + 39744), b[3392], x);
+      x = fma(-CHEM_LDLU(lu + 37600), b[3648], x);
+      x = fma(-CHEM_LDLU(lu + 34752), b[3968], x);
+      x = fma(-CHEM_LDLU(lu + 33984), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 33632), b[4064], x);
+      x = fma(-CHEM_LDLU(lu + 33280), b[4096], x);
+      x = fma(-CHEM_LDLU(lu + 32928), b[4128], x);
+      x = fma(-CHEM_LDLU(lu + 32512), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 32064), b[4192], x);
+      b[4224] = x * CHEM_LDLU(vd + 4224);
+    }
+    {
+      double x = b[4256];
+      x = fma(-CHEM_LDLU(lu + 48832), b[640], x);
+      x = fma(-CHEM_LDLU(lu + 32096), b[4192], x);
+      b[4256] = x * CHEM_LDLU(vd + 4256);
+    }
+    {
+      double x = b[4288];
+      x = fma(-CHEM_LDLU(lu + 42368), b[2880], x);
+      x = fma(-CHEM_LDLU(lu + 37632), b[3648], x);
+      x = fma(-CHEM_LDLU(lu + 35488), b[3904], x);
+      x = fma(-CHEM_LDLU(lu + 34016), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 32128), b[4192], x);
+      b[4288] = x * CHEM_LDLU(vd + 4288);
+    }
+    {
+      double x = b[4320];
+      x = fma(-CHEM_LDLU(lu + 48768), b[672], x);
+      x = fma(-CHEM_LDLU(lu + 47296), b[1568], x);
+      x = fma(-CHEM_LDLU(lu + 46400), b[1856], x);
+      x = fma(-CHEM_LDLU(lu + 46304), b[1888], x);
+      x = fma(-CHEM_LDLU(lu + 45856), b[2048], x);
+      x = fma(-CHEM_LDLU(lu + 45728), b[2080], x);
+      x = fma(-CHEM_LDLU(lu + 45568), b[2112], x);
+      x = fma(-CHEM_LDLU(lu + 44352), b[2400], x);
+      x = fma(-CHEM_LDLU(lu + 44224), b[2432], x);
+      x = fma(-CHEM_LDLU(lu + 43808), b[2528], x);
+      x = fma(-CHEM_LDLU(lu + 43296), b[2656], x);
+      x = fma(-CHEM_LDLU(lu + 42560), b[2848], x);
+      x = fma(-CHEM_LDLU(lu + 41952), b[2976], x);
+      x = fma(-CHEM_LDLU(lu + 41856), b[3008], x);
+      x = fma(-CHEM_LDLU(lu + 41696), b[3040], x);
+      x = fma(-CHEM_LDLU(lu + 41184), b[3136], x);
+      x = fma(-CHEM_LDLU(lu + 40736), b[3232], x);
+      x = fma(-CHEM_LDLU(lu + 39936), b[3360], x);
+      x = fma(-CHEM_LDLU(lu + 39776), b[3392], x);
+      x = fma(-CHEM_LDLU(lu + 39456), b[3424], x);
+      x = fma(-CHEM_LDLU(lu + 39168), b[3456], x);
+      x = fma(-CHEM_LDLU(lu + 38624), b[3520], x);
+      x = fma(-CHEM_LDLU(lu + 38368), b[3552], x);
+      x = fma(-CHEM_LDLU(lu + 37664), b[3648], x);
+      x = fma(-CHEM_LDLU(lu + 36832), b[3776], x);
+      x = fma(-CHEM_LDLU(lu + 36512), b[3808], x);
+      x = fma(-CHEM_LDLU(lu + 36256), b[3840], x);
+      x = fma(-CHEM_LDLU(lu + 35936), b[3872], x);
+      x = fma(-CHEM_LDLU(lu + 35520), b[3904], x);
+      x = fma(-CHEM_LDLU(lu + 35104), b[3936], x);
+      x = fma(-CHEM_LDLU(lu + 34784), b[3968], x);
+      x = fma(-CHEM_LDLU(lu + 34368), b[4000], x);
+      x = fma(-CHEM_LDLU(lu + 34048), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 33664), b[4064], x);
+      x = fma(-CHEM_LDLU(lu + 33312), b[4096], x);
+      x = fma(-CHEM_LDLU(lu + 32960), b[4128], x);
+      x = fma(-CHEM_LDLU(lu + 32544), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 32160), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 31712), b[4224], x);
+      x = fma(-CHEM_LDLU(lu + 31360), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 30944), b[4288], x);
+      b[4320] = x * CHEM_LDLU(vd + 4320);
+    }
+    {
+      double x = b[4352];
+      x = fma(-CHEM_LDLU(lu + 42400), b[2880], x);
+      x = fma(-CHEM_LDLU(lu + 35552), b[3904], x);
+      x = fma(-CHEM_LDLU(lu + 30976), b[4288], x);
+      b[4352] = x * CHEM_LDLU(vd + 4352);
+    }
+    {
+      double x = b[4384];
+      x = fma(-CHEM_LDLU(lu + 47104), b[1632], x);
+      x = fma(-CHEM_LDLU(lu + 46784), b[1728], x);
+      x = fma(-CHEM_LDLU(lu + 45440), b[2144], x);
+      x = fma(-CHEM_LDLU(lu + 45120), b[2240], x);
+      x = fma(-CHEM_LDLU(lu + 44864), b[2272], x);
+      x = fma(-CHEM_LDLU(lu + 44096), b[2464], x);
+      x = fma(-CHEM_LDLU(lu + 43936), b[2496], x);
+      x = fma(-CHEM_LDLU(lu + 43648), b[2560], x);
+      x = fma(-CHEM_LDLU(lu + 43456), b[2624], x);
+      x = fma(-CHEM_LDLU(lu + 42592), b[2848], x);
+      x = fma(-CHEM_LDLU(lu + 42080), b[2944], x);
+      x = fma(-CHEM_LDLU(lu + 41504), b[3072], x);
+      x = fma(-CHEM_LDLU(lu + 41344), b[3104], x);
+      x = fma(-CHEM_LDLU(lu + 40512), b[3264], x);
+      x = fma(-CHEM_LDLU(lu + 40352), b[3296], x);
+      x = fma(-CHEM_LDLU(lu + 39968), b[3360], x);
+      x = fma(-CHEM_LDLU(lu + 39488), b[3424], x);
+      x = fma(-CHEM_LDLU(lu + 39200), b[3456], x);
+      x = fma(-CHEM_LDLU(lu + 38880), b[3488], x);
+      x = fma(-CHEM_LDLU(lu + 38656), b[3520], x);
+      x = fma(-CHEM_LDLU(lu + 38400), b[3552], x);
+      x = fma(-CHEM_LDLU(lu + 38112), b[3584], x);
+      x = fma(-CHEM_LDLU(lu + 37696), b[3648], x);
+      x = fma(-CHEM_LDLU(lu + 37184), b[3744], x);
+      x = fma(-CHEM_LDLU(lu + 36864), b[3776], x);
+      x = fma(-CHEM_LDLU(lu + 36544), b[3808], x);
+      x = fma(-CHEM_LDLU(lu + 36288), b[3840], x);
+      x = fma(-CHEM_LDLU(lu + 35968), b[3872], x);
+      x = fma(-CHEM_LDLU(lu + 35584), b[3904], x);
+      x = fma(-CHEM_LDLU(lu + 35136), b[3936], x);
+      x = fma(-CHEM_LDLU(lu + 34816), b[3968], x);
+      x = fma(-CHEM_LDLU(lu + 34400), b[4000], x);
+      x = fma(-CHEM_LDLU(lu + 34080), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 33696), b[4064], x);
+      x = fma(-CHEM_LDLU(lu + 33344), b[4096], x);
+      x = fma(-CHEM_LDLU(lu + 32992), b[4128], x);
+      x = fma(-CHEM_LDLU(lu + 32576), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 32192), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 31744), b[4224], x);
+      x = fma(-CHEM_LDLU(lu + 31392), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 31008), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 30624), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 30304), b[4352], x);
+      b[4384] = x * CHEM_LDLU(vd + 4384);
+    }
+    {
+      double x = b[4416];
+      x = fma(-CHEM_LDLU(lu + 44896), b[2272], x);
+      x = fma(-CHEM_LDLU(lu + 42976), b[2720], x);
+      x = fma(-CHEM_LDLU(lu + 38688), b[3520], x);
+      x = fma(-CHEM_LDLU(lu + 35616), b[3904], x);
+      x = fma(-CHEM_LDLU(lu + 34848), b[3968], x);
+      x = fma(-CHEM_LDLU(lu + 32608), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 32224), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 31776), b[4224], x);
+      x = fma(-CHEM_LDLU(lu + 31424), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 31040), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 30656), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 30336), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 29984), b[4384], x);
+      b[4416] = x * CHEM_LDLU(vd + 4416);
+    }
+    {
+      double x = b[4448];
+      x = fma(-CHEM_LDLU(lu + 47552), b[1344], x);
+      x = fma(-CHEM_LDLU(lu + 43168), b[2688], x);
+      x = fma(-CHEM_LDLU(lu + 41376), b[3104], x);
+      x = fma(-CHEM_LDLU(lu + 40384), b[3296], x);
+      x = fma(-CHEM_LDLU(lu + 39520), b[3424], x);
+      x = fma(-CHEM_LDLU(lu + 39232), b[3456], x);
+      x = fma(-CHEM_LDLU(lu + 38912), b[3488], x);
+      x = fma(-CHEM_LDLU(lu + 38432), b[3552], x);
+      x = fma(-CHEM_LDLU(lu + 38144), b[3584], x);
+      x = fma(-CHEM_LDLU(lu + 37728), b[3648], x);
+      x = fma(-CHEM_LDLU(lu + 37216), b[3744], x);
+      x = fma(-CHEM_LDLU(lu + 36896), b[3776], x);
+      x = fma(-CHEM_LDLU(lu + 36576), b[3808], x);
+      x = fma(-CHEM_LDLU(lu + 36320), b[3840], x);
+      x = fma(-CHEM_LDLU(lu + 36000), b[3872], x);
+      x = fma(-CHEM_LDLU(lu + 35648), b[3904], x);
+      x = fma(-CHEM_LDLU(lu + 35168), b[3936], x);
+      x = fma(-CHEM_LDLU(lu + 34880), b[3968], x);
+      x = fma(-CHEM_LDLU(lu + 34432), b[4000], x);
+      x = fma(-CHEM_LDLU(lu + 34112), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 33728), b[4064], x);
+      x = fma(-CHEM_LDLU(lu + 33376), b[4096], x);
+      x = fma(-CHEM_LDLU(lu + 33024), b[4128], x);
+      x = fma(-CHEM_LDLU(lu + 32640), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 32256), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 31808), b[4224], x);
+      x = fma(-CHEM_LDLU(lu + 31456), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 31072), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 30688), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 30368), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 30016), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 29696), b[4416], x);
+      b[4448] = x * CHEM_LDLU(vd + 4448);
+    }
+    {
+      double x = b[4480];
+      b[4480] = x * CHEM_LDLU(vd + 4480);
+    }
+    {
+      double x = b[4512];
+      x = fma(-CHEM_LDLU(lu + 46816), b[1728], x);
+      x = fma(-CHEM_LDLU(lu + 44928), b[2272], x);
+      x = fma(-CHEM_LDLU(lu + 36928), b[3776], x);
+      x = fma(-CHEM_LDLU(lu + 34912), b[3968], x);
+      x = fma(-CHEM_LDLU(lu + 32672), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 32288), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 31840), b[4224], x);
+      x = fma(-CHEM_LDLU(lu + 31488), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 31104), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 30720), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 30400), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 30048), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 29728), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 29440), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 29184), b[4480], x);
+      b[4512] = x * CHEM_LDLU(vd + 4512);
+    }
+    {
+      double x = b[4544];
+      x = fma(-CHEM_LDLU(lu + 48576), b[832], x);
+      x = fma(-CHEM_LDLU(lu + 48512), b[864], x);
+      x = fma(-CHEM_LDLU(lu + 48448), b[896], x);
+      x = fma(-CHEM_LDLU(lu + 48384), b[928], x);
+      x = fma(-CHEM_LDLU(lu + 48032), b[1088], x);
+      x = fma(-CHEM_LDLU(lu + 47968), b[1120], x);
+      x = fma(-CHEM_LDLU(lu + 47904), b[1152], x);
+      x = fma(-CHEM_LDLU(lu + 47360), b[1536], x);
+      x = fma(-CHEM_LDLU(lu + 47200), b[1600], x);
+      x = fma(-CHEM_LDLU(lu + 46080), b[1984], x);
+      x = fma(-CHEM_LDLU(lu + 45952), b[2016], x);
+      x = fma(-CHEM_LDLU(lu + 45216), b[2208], x);
+      x = fma(-CHEM_LDLU(lu + 44640), b[2336], x);
+      x = fma(-CHEM_LDLU(lu + 44512), b[2368], x);
+      x = fma(-CHEM_LDLU(lu + 44384), b[2400], x);
+      x = fma(-CHEM_LDLU(lu + 44256), b[2432], x);
+      x = fma(-CHEM_LDLU(lu + 43968), b[2496], x);
+      x = fma(-CHEM_LDLU(lu + 43840), b[2528], x);
+      x = fma(-CHEM_LDLU(lu + 43680), b[2560], x);
+      x = fma(-CHEM_LDLU(lu + 43488), b[2624], x);
+      x = fma(-CHEM_LDLU(lu + 43328), b[2656], x);
+      x = fma(-CHEM_LDLU(lu + 43008), b[2720], x);
+      x = fma(-CHEM_LDLU(lu + 42112), b[2944], x);
+      x = fma(-CHEM_LDLU(lu + 41984), b[2976], x);
+      x = fma(-CHEM_LDLU(lu + 41888), b[3008], x);
+      x = fma(-CHEM_LDLU(lu + 41728), b[3040], x);
+      x = fma(-CHEM_LDLU(lu + 41536), b[3072], x);
+      x = fma(-CHEM_LDLU(lu + 41216), b[3136], x);
+      x = fma(-CHEM_LDLU(lu + 40768), b[3232], x);
+      x = fma(-CHEM_LDLU(lu + 40544), b[3264], x);
+      x = fma(-CHEM_LDLU(lu + 40000), b[3360], x);
+      x = fma(-CHEM_LDLU(lu + 39808), b[3392], x);
+      x = fma(-CHEM_LDLU(lu + 39552), b[3424], x);
+      x = fma(-CHEM_LDLU(lu + 39264), b[3456], x);
+      x = fma(-CHEM_LDLU(lu + 38944), b[3488], x);
+      x = fma(-CHEM_LDLU(lu + 38720), b[3520], x);
+      x = fma(-CHEM_LDLU(lu + 38464), b[3552], x);
+      x = fma(-CHEM_LDLU(lu + 38176), b[3584], x);
+      x = fma(-CHEM_LDLU(lu + 37952), b[3616], x);
+      x = fma(-CHEM_LDLU(lu + 37760), b[3648], x);
+      x = fma(-CHEM_LDLU(lu + 37248), b[3744], x);
+      x = fma(-CHEM_LDLU(lu + 36960), b[3776], x);
+      x = fma(-CHEM_LDLU(lu + 36608), b[3808], x);
+      x = fma(-CHEM_LDLU(lu + 36352), b[3840], x);
+      x = fma(-CHEM_LDLU(lu + 36032), b[3872], x);
+      x = fma(-CHEM_LDLU(lu + 35680), b[3904], x);
+      x = fma(-CHEM_LDLU(lu + 35200), b[3936], x);
+      x = fma(-CHEM_LDLU(lu + 34944), b[3968], x);
+      x = fma(-CHEM_LDLU(lu + 34464), b[4000], x);
+      x = fma(-CHEM_LDLU(lu + 34144), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 33760), b[4064], x);
+      x = fma(-CHEM_LDLU(lu + 33408), b[4096], x);
+      x = fma(-CHEM_LDLU(lu + 33056), b[4128], x);
+      x = fma(-CHEM_LDLU(lu + 32704), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 32320), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 31872), b[4224], x);
+      x = fma(-CHEM_LDLU(lu + 31520), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 31136), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 30752), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 30432), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 30080), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 29760), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 29472), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 29216), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 28960), b[4512], x);
+      b[4544] = x * CHEM_LDLU(vd + 4544);
+    }
+    {
+      double x = b[4576];
+      x = fma(-CHEM_LDLU(lu + 42432), b[2880], x);
+      x = fma(-CHEM_LDLU(lu + 35712), b[3904], x);
+      x = fma(-CHEM_LDLU(lu + 31168), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 30112), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 29792), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 29504), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 29248), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 28992), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 28768), b[4544], x);
+      b[4576] = x * CHEM_LDLU(vd + 4576);
+    }
+    {
+      double x = b[4608];
+      x = fma(-CHEM_LDLU(lu + 48352), b[960], x);
+      x = fma(-CHEM_LDLU(lu + 47808), b[1216], x);
+      x = fma(-CHEM_LDLU(lu + 47680), b[1280], x);
+      x = fma(-CHEM_LDLU(lu + 47584), b[1344], x);
+      x = fma(-CHEM_LDLU(lu + 46880), b[1696], x);
+      x = fma(-CHEM_LDLU(lu + 46624), b[1792], x);
+      x = fma(-CHEM_LDLU(lu + 46528), b[1824], x);
+      x = fma(-CHEM_LDLU(lu + 46240), b[1920], x);
+      x = fma(-CHEM_LDLU(lu + 46176), b[1952], x);
+      x = fma(-CHEM_LDLU(lu + 45344), b[2176], x);
+      x = fma(-CHEM_LDLU(lu + 44128), b[2464], x);
+      x = fma(-CHEM_LDLU(lu + 43584), b[2592], x);
+      x = fma(-CHEM_LDLU(lu + 40192), b[3328], x);
+      x = fma(-CHEM_LDLU(lu + 39840), b[3392], x);
+      x = fma(-CHEM_LDLU(lu + 38752), b[3520], x);
+      x = fma(-CHEM_LDLU(lu + 37984), b[3616], x);
+      x = fma(-CHEM_LDLU(lu + 37792), b[3648], x);
+      x = fma(-CHEM_LDLU(lu + 37280), b[3744], x);
+      x = fma(-CHEM_LDLU(lu + 35744), b[3904], x);
+      x = fma(-CHEM_LDLU(lu + 35232), b[3936], x);
+      x = fma(-CHEM_LDLU(lu + 34496), b[4000], x);
+      x = fma(-CHEM_LDLU(lu + 34176), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 33792), b[4064], x);
+      x = fma(-CHEM_LDLU(lu + 33440), b[4096], x);
+      x = fma(-CHEM_LDLU(lu + 33088), b[4128], x);
+      x = fma(-CHEM_LDLU(lu + 32736), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 32352), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 31904), b[4224], x);
+      x = fma(-CHEM_LDLU(lu + 31552), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 31200), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 30784), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 30464), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 30144), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 29824), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 29536), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 29280), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 29024), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 28800), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 28608), b[4576], x);
+      b[4608] = x * CHEM_LDLU(vd + 4608);
+    }
+    {
+      double x = b[4640];
+      x = fma(-CHEM_LDLU(lu + 48256), b[992], x);
+      x = fma(-CHEM_LDLU(lu + 48192), b[1024], x);
+      x = fma(-CHEM_LDLU(lu + 47712), b[1280], x);
+      x = fma(-CHEM_LDLU(lu + 46720), b[1760], x);
+      x = fma(-CHEM_LDLU(lu + 46432), b[1856], x);
+      x = fma(-CHEM_LDLU(lu + 46336), b[1888], x);
+      x = fma(-CHEM_LDLU(lu + 46272), b[1920], x);
+      x = fma(-CHEM_LDLU(lu + 45984), b[2016], x);
+      x = fma(-CHEM_LDLU(lu + 45888), b[2048], x);
+      x = fma(-CHEM_LDLU(lu + 45760), b[2080], x);
+      x = fma(-CHEM_LDLU(lu + 45600), b[2112], x);
+      x = fma(-CHEM_LDLU(lu + 45376), b[2176], x);
+      x = fma(-CHEM_LDLU(lu + 45248), b[2208], x);
+      x = fma(-CHEM_LDLU(lu + 44672), b[2336], x);
+      x = fma(-CHEM_LDLU(lu + 44544), b[2368], x);
+      x = fma(-CHEM_LDLU(lu + 44416), b[2400], x);
+      x = fma(-CHEM_LDLU(lu + 44288), b[2432], x);
+      x = fma(-CHEM_LDLU(lu + 44160), b[2464], x);
+      x = fma(-CHEM_LDLU(lu + 43872), b[2528], x);
+      x = fma(-CHEM_LDLU(lu + 43616), b[2592], x);
+      x = fma(-CHEM_LDLU(lu + 43360), b[2656], x);
+      x = fma(-CHEM_LDLU(lu + 42624), b[2848], x);
+      x = fma(-CHEM_LDLU(lu + 42016), b[2976], x);
+      x = fma(-CHEM_LDLU(lu + 41248), b[3136], x);
+      x = fma(-CHEM_LDLU(lu + 40800), b[3232], x);
+      x = fma(-CHEM_LDLU(lu + 40224), b[3328], x);
+      x = fma(-CHEM_LDLU(lu + 40032), b[3360], x);
+      x = fma(-CHEM_LDLU(lu + 39584), b[3424], x);
+      x = fma(-CHEM_LDLU(lu + 39296), b[3456], x);
+      x = fma(-CHEM_LDLU(lu + 38784), b[3520], x);
+      x = fma(-CHEM_LDLU(lu + 38496), b[3552], x);
+      x = fma(-CHEM_LDLU(lu + 38016), b[3616], x);
+      x = fma(-CHEM_LDLU(lu + 37824), b[3648], x);
+      x = fma(-CHEM_LDLU(lu + 37312), b[3744], x);
+      x = fma(-CHEM_LDLU(lu + 36992), b[3776], x);
+      x = fma(-CHEM_LDLU(lu + 36640), b[3808], x);
+      x = fma(-CHEM_LDLU(lu + 36384), b[3840], x);
+      x = fma(-CHEM_LDLU(lu + 36064), b[3872], x);
+      x = fma(-CHEM_LDLU(lu + 35776), b[3904], x);
+      x = fma(-CHEM_LDLU(lu + 35264), b[3936], x);
+      x = fma(-CHEM_LDLU(lu + 34976), b[3968], x);
+      x = fma(-CHEM_LDLU(lu + 34528), b[4000], x);
+      x = fma(-CHEM_LDLU(lu + 34208), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 33824), b[4064], x);
+      x = fma(-CHEM_LDLU(lu + 33472), b[4096], x);
+      x = fma(-CHEM_LDLU(lu + 33120), b[4128], x);
+      x = fma(-CHEM_LDLU(lu + 32768), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 32384), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 31936), b[4224], x);
+      x = fma(-CHEM_LDLU(lu + 31584), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 31232), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 30816), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 30496), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 30176), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 29856), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 29568), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 29312), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 29056), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 28832), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 28640), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 28480), b[4608], x);
+      b[4640] = x * CHEM_LDLU(vd + 4640);
+    }
+    {
+      double x = b[4672];
+      x = fma(-CHEM_LDLU(lu + 43040), b[2720], x);
+      x = fma(-CHEM_LDLU(lu + 42656), b[2848], x);
+      x = fma(-CHEM_LDLU(lu + 41408), b[3104], x);
+      x = fma(-CHEM_LDLU(lu + 40416), b[3296], x);
+      x = fma(-CHEM_LDLU(lu + 40064), b[3360], x);
+      x = fma(-CHEM_LDLU(lu + 39616), b[3424], x);
+      x = fma(-CHEM_LDLU(lu + 39328), b[3456], x);
+      x = fma(-CHEM_LDLU(lu + 38976), b[3488], x);
+      x = fma(-CHEM_LDLU(lu + 38528), b[3552], x);
+      x = fma(-CHEM_LDLU(lu + 38208), b[3584], x);
+      x = fma(-CHEM_LDLU(lu + 37856), b[3648], x);
+      x = fma(-CHEM_LDLU(lu + 37344), b[3744], x);
+      x = fma(-CHEM_LDLU(lu + 37024), b[3776], x);
+      x = fma(-CHEM_LDLU(lu + 36672), b[3808], x);
+      x = fma(-CHEM_LDLU(lu + 36416), b[3840], x);
+      x = fma(-CHEM_LDLU(lu + 36096), b[3872], x);
+      x = fma(-CHEM_LDLU(lu + 35808), b[3904], x);
+      x = fma(-CHEM_LDLU(lu + 35296), b[3936], x);
+      x = fma(-CHEM_LDLU(lu + 35008), b[3968], x);
+      x = fma(-CHEM_LDLU(lu + 34560), b[4000], x);
+      x = fma(-CHEM_LDLU(lu + 34240), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 33856), b[4064], x);
+      x = fma(-CHEM_LDLU(lu + 33504), b[4096], x);
+      x = fma(-CHEM_LDLU(lu + 33152), b[4128], x);
+      x = fma(-CHEM_LDLU(lu + 32800), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 32416), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 31968), b[4224], x);
+      x = fma(-CHEM_LDLU(lu + 31616), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 31264), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 30848), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 30528), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 30208), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 29888), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 29600), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 29344), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 29088), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 28864), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 28672), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 28512), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 28384), b[4640], x);
+      b[4672] = x * CHEM_LDLU(vd + 4672);
+    }
+    {
+      double x = b[4704];
+      x = fma(-CHEM_LDLU(lu + 47008), b[1664], x);
+      x = fma(-CHEM_LDLU(lu + 46912), b[1696], x);
+      x = fma(-CHEM_LDLU(lu + 46848), b[1728], x);
+      x = fma(-CHEM_LDLU(lu + 46560), b[1824], x);
+      x = fma(-CHEM_LDLU(lu + 45472), b[2144], x);
+      x = fma(-CHEM_LDLU(lu + 45152), b[2240], x);
+      x = fma(-CHEM_LDLU(lu + 44960), b[2272], x);
+      x = fma(-CHEM_LDLU(lu + 44000), b[2496], x);
+      x = fma(-CHEM_LDLU(lu + 43712), b[2560], x);
+      x = fma(-CHEM_LDLU(lu + 43520), b[2624], x);
+      x = fma(-CHEM_LDLU(lu + 43200), b[2688], x);
+      x = fma(-CHEM_LDLU(lu + 42688), b[2848], x);
+      x = fma(-CHEM_LDLU(lu + 42464), b[2880], x);
+      x = fma(-CHEM_LDLU(lu + 42144), b[2944], x);
+      x = fma(-CHEM_LDLU(lu + 41568), b[3072], x);
+      x = fma(-CHEM_LDLU(lu + 41440), b[3104], x);
+      x = fma(-CHEM_LDLU(lu + 41280), b[3136], x);
+      x = fma(-CHEM_LDLU(lu + 40832), b[3232], x);
+      x = fma(-CHEM_LDLU(lu + 40576), b[3264], x);
+      x = fma(-CHEM_LDLU(lu + 40448), b[3296], x);
+      x = fma(-CHEM_LDLU(lu + 40256), b[3328], x);
+      x = fma(-CHEM_LDLU(lu + 40096), b[3360], x);
+      x = fma(-CHEM_LDLU(lu + 39648), b[3424], x);
+      x = fma(-CHEM_LDLU(lu + 39360), b[3456], x);
+      x = fma(-CHEM_LDLU(lu + 39008), b[3488], x);
+      x = fma(-CHEM_LDLU(lu + 38816), b[3520], x);
+      x = fma(-CHEM_LDLU(lu + 38560), b[3552], x);
+      x = fma(-CHEM_LDLU(lu + 38240), b[3584], x);
+      x = fma(-CHEM_LDLU(lu + 38048), b[3616], x);
+      x = fma(-CHEM_LDLU(lu + 37888), b[3648], x);
+      x = fma(-CHEM_LDLU(lu + 37376), b[3744], x);
+      x = fma(-CHEM_LDLU(lu + 37056), b[3776], x);
+      x = fma(-CHEM_LDLU(lu + 36704), b[3808], x);
+      x = fma(-CHEM_LDLU(lu + 36448), b[3840], x);
+      x = fma(-CHEM_LDLU(lu + 36128), b[3872], x);
+      x = fma(-CHEM_LDLU(lu + 35840), b[3904], x);
+      x = fma(-CHEM_LDLU(lu + 35328), b[3936], x);
+      x = fma(-CHEM_LDLU(lu + 35040), b[3968], x);
+      x = fma(-CHEM_LDLU(lu + 34592), b[4000], x);
+      x = fma(-CHEM_LDLU(lu + 34272), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 33888), b[4064], x);
+      x = fma(-CHEM_LDLU(lu + 33536), b[4096], x);
+      x = fma(-CHEM_LDLU(lu + 33184), b[4128], x);
+      x = fma(-CHEM_LDLU(lu + 32832), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 32448), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 32000), b[4224], x);
+      x = fma(-CHEM_LDLU(lu + 31648), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 31296), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 30880), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 30560), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 30240), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 29920), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 29632), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 29376), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 29120), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 28896), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 28704), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 28544), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 28416), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 28320), b[4672], x);
+      b[4704] = x * CHEM_LDLU(vd + 4704);
+    }
+}
+__device__ __noinline__ void solve_t_0_1(double* __restrict__ ws, int rhs)
+{
+    const double* __restrict__ lu = ws + 72864;
+    const double* __restrict__ vd = ws + 126944;
+    double* __restrict__ b = ws + rhs * 32;
+    (void)vd;
+    {
+      double x = b[4736];
+      x = fma(-CHEM_LDLU(lu + 49280), b[256], x);
+      x = fma(-CHEM_LDLU(lu + 49216), b[288], x);
+      x = fma(-CHEM_LDLU(lu + 49120), b[352], x);
+      x = fma(-CHEM_LDLU(lu + 49088), b[384], x);
+      x = fma(-CHEM_LDLU(lu + 49056), b[416], x);
+      x = fma(-CHEM_LDLU(lu + 49024), b[448], x);
+      x = fma(-CHEM_LDLU(lu + 48736), b[704], x);
+      x = fma(-CHEM_LDLU(lu + 48704), b[736], x);
+      x = fma(-CHEM_LDLU(lu + 48672), b[768], x);
+      x = fma(-CHEM_LDLU(lu + 48640), b[800], x);
+      x = fma(-CHEM_LDLU(lu + 48608), b[832], x);
+      x = fma(-CHEM_LDLU(lu + 48544), b[864], x);
+      x = fma(-CHEM_LDLU(lu + 48480), b[896], x);
+      x = fma(-CHEM_LDLU(lu + 48416), b[928], x);
+      x = fma(-CHEM_LDLU(lu + 48288), b[992], x);
+      x = fma(-CHEM_LDLU(lu + 48128), b[1056], x);
+      x = fma(-CHEM_LDLU(lu + 48064), b[1088], x);
+      x = fma(-CHEM_LDLU(lu + 48000), b[1120], x);
+      x = fma(-CHEM_LDLU(lu + 47936), b[1152], x);
+      x = fma(-CHEM_LDLU(lu + 47648), b[1312], x);
+      x = fma(-CHEM_LDLU(lu + 47520), b[1440], x);
+      x = fma(-CHEM_LDLU(lu + 47488), b[1472], x);
+      x = fma(-CHEM_LDLU(lu + 47456), b[1504], x);
+      x = fma(-CHEM_LDLU(lu + 47392), b[1536], x);
+      x = fma(-CHEM_LDLU(lu + 47328), b[1568], x);
+      x = fma(-CHEM_LDLU(lu + 47232), b[1600], x);
+      x = fma(-CHEM_LDLU(lu + 47136), b[1632], x);
+      x = fma(-CHEM_LDLU(lu + 47040), b[1664], x);
+      x = fma(-CHEM_LDLU(lu + 46944), b[1696], x);
+      x = fma(-CHEM_LDLU(lu + 46752), b[1760], x);
+      x = fma(-CHEM_LDLU(lu + 46656), b[1792], x);
+      x = fma(-CHEM_LDLU(lu + 46464), b[1856], x);
+      x = fma(-CHEM_LDLU(lu + 46368), b[1888], x);
+      x = fma(-CHEM_LDLU(lu + 46208), b[1952], x);
+      x = fma(-CHEM_LDLU(lu + 46112), b[1984], x);
+      x = fma(-CHEM_LDLU(lu + 46016), b[2016], x);
+      x = fma(-CHEM_LDLU(lu + 45920), b[2048], x);
+      x = fma(-CHEM_LDLU(lu + 45792), b[2080], x);
+      x = fma(-CHEM_LDLU(lu + 45632), b[2112], x);
+      x = fma(-CHEM_LDLU(lu + 45504), b[2144], x);
+      x = fma(-CHEM_LDLU(lu + 45408), b[2176], x);
+      x = fma(-CHEM_LDLU(lu + 45280), b[2208], x);
+      x = fma(-CHEM_LDLU(lu + 45184), b[2240], x);
+      x = fma(-CHEM_LDLU(lu + 44992), b[2272], x);
+      x = fma(-CHEM_LDLU(lu + 44832), b[2304], x);
+      x = fma(-CHEM_LDLU(lu + 44704), b[2336], x);
+      x = fma(-CHEM_LDLU(lu + 44576), b[2368], x);
+      x = fma(-CHEM_LDLU(lu + 44448), b[2400], x);
+      x = fma(-CHEM_LDLU(lu + 44320), b[2432], x);
+      x = fma(-CHEM_LDLU(lu + 44192), b[2464], x);
+      x = fma(-CHEM_LDLU(lu + 44032), b[2496], x);
+      x = fma(-CHEM_LDLU(lu + 43904), b[2528], x);
+      x = fma(-CHEM_LDLU(lu + 43744), b[2560], x);
+      x = fma(-CHEM_LDLU(lu + 43552), b[2624], x);
+      x = fma(-CHEM_LDLU(lu + 43392), b[2656], x);
+      x = fma(-CHEM_LDLU(lu + 43232), b[2688], x);
+      x = fma(-CHEM_LDLU(lu + 43072), b[2720], x);
+      x = fma(-CHEM_LDLU(lu + 42912), b[2752], x);
+      x = fma(-CHEM_LDLU(lu + 42816), b[2784], x);
+      x = fma(-CHEM_LDLU(lu + 42752), b[2816], x);
+      x = fma(-CHEM_LDLU(lu + 42720), b[2848], x);
+      x = fma(-CHEM_LDLU(lu + 42496), b[2880], x);
+      x = fma(-CHEM_LDLU(lu + 42336), b[2912], x);
+      x = fma(-CHEM_LDLU(lu + 42176), b[2944], x);
+      x = fma(-CHEM_LDLU(lu + 42048), b[2976], x);
+      x = fma(-CHEM_LDLU(lu + 41920), b[3008], x);
+      x = fma(-CHEM_LDLU(lu + 41760), b[3040], x);
+      x = fma(-CHEM_LDLU(lu + 41600), b[3072], x);
+      x = fma(-CHEM_LDLU(lu + 41472), b[3104], x);
+      x = fma(-CHEM_LDLU(lu + 41312), b[3136], x);
+      x = fma(-CHEM_LDLU(lu + 41088), b[3168], x);
+      x = fma(-CHEM_LDLU(lu + 40960), b[3200], x);
+      x = fma(-CHEM_LDLU(lu + 40864), b[3232], x);
+      x = fma(-CHEM_LDLU(lu + 40608), b[3264], x);
+      x = fma(-CHEM_LDLU(lu + 40480), b[3296], x);
+      x = fma(-CHEM_LDLU(lu + 40288), b[3328], x);
+      x = fma(-CHEM_LDLU(lu + 40128), b[3360], x);
+      x = fma(-CHEM_LDLU(lu + 39872), b[3392], x);
+      x = fma(-CHEM_LDLU(lu + 39680), b[3424], x);
+      x = fma(-CHEM_LDLU(lu + 39392), b[3456], x);
+      x = fma(-CHEM_LDLU(lu + 39040), b[3488], x);
+      x = fma(-CHEM_LDLU(lu + 38848), b[3520], x);
+      x = fma(-CHEM_LDLU(lu + 38592), b[3552], x);
+      x = fma(-CHEM_LDLU(lu + 38272), b[3584], x);
+      x = fma(-CHEM_LDLU(lu + 38080), b[3616], x);
+      x = fma(-CHEM_LDLU(lu + 37920), b[3648], x);
+      x = fma(-CHEM_LDLU(lu + 37504), b[3680], x);
+      x = fma(-CHEM_LDLU(lu + 37440), b[3712], x);
+      x = fma(-CHEM_LDLU(lu + 37408), b[3744], x);
+      x = fma(-CHEM_LDLU(lu + 37088), b[3776], x);
+      x = fma(-CHEM_LDLU(lu + 36736), b[3808], x);
+      x = fma(-CHEM_LDLU(lu + 36480), b[3840], x);
+      x = fma(-CHEM_LDLU(lu + 36160), b[3872], x);
+      x = fma(-CHEM_LDLU(lu + 35872), b[3904], x);
+      x = fma(-CHEM_LDLU(lu + 35360), b[3936], x);
+      x = fma(-CHEM_LDLU(lu + 35072), b[3968], x);
+      x = fma(-CHEM_LDLU(lu + 34624), b[4000], x);
+      x = fma(-CHEM_LDLU(lu + 34304), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 33920), b[4064], x);
+      x = fma(-CHEM_LDLU(lu + 33568), b[4096], x);
+      x = fma(-CHEM_LDLU(lu + 33216), b[4128], x);
+      x = fma(-CHEM_LDLU(lu + 32864), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 32480), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 32032), b[4224], x);
+      x = fma(-CHEM_LDLU(lu + 31680), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 31328), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 30912), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 30592), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 30272), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 29952), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 29664), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 29408), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 29152), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 28928), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 28736), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 28576), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 28448), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 28352), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 28288), b[4704], x);
+      b[4736] = x * CHEM_LDLU(vd + 4736);
+    }
+    {
+      double x = b[4704];
+      x = fma(-CHEM_LDLU(lu + 28256), b[4736], x);
+      b[4704] = x;
+    }
+    {
+      double x = b[4672];
+      x = fma(-CHEM_LDLU(lu + 25120), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 28224), b[4736], x);
+      b[4672] = x;
+    }
+    {
+      double x = b[4640];
+      x = fma(-CHEM_LDLU(lu + 23200), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 25088), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 28192), b[4736], x);
+      b[4640] = x;
+    }
+    {
+      double x = b[4608];
+      x = fma(-CHEM_LDLU(lu + 21376), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 23168), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 25056), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 28160), b[4736], x);
+      b[4608] = x;
+    }
+    {
+      double x = b[4576];
+      x = fma(-CHEM_LDLU(lu + 19808), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 21344), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 23136), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 25024), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 28128), b[4736], x);
+      b[4576] = x;
+    }
+    {
+      double x = b[4544];
+      x = fma(-CHEM_LDLU(lu + 18368), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 19776), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 21312), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 23104), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 24992), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 28096), b[4736], x);
+      b[4544] = x;
+    }
+    {
+      double x = b[4512];
+      x = fma(-CHEM_LDLU(lu + 17152), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 18336), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 19744), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 21280), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 23072), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 24960), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 28064), b[4736], x);
+      b[4512] = x;
+    }
+    {
+      double x = b[4480];
+      x = fma(-CHEM_LDLU(lu + 24928), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 28032), b[4736], x);
+      b[4480] = x;
+    }
+    {
+      double x = b[4448];
+      x = fma(-CHEM_LDLU(lu + 14944), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 15872), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 17120), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 18304), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 19712), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 21248), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 23040), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 24896), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 28000), b[4736], x);
+      b[4448] = x;
+    }
+    {
+      double x = b[4416];
+      x = fma(-CHEM_LDLU(lu + 14080), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 14912), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 15840), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 17088), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 18272), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 19680), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 21216), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 23008), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 24864), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 27968), b[4736], x);
+      b[4416] = x;
+    }
+    {
+      double x = b[4384];
+      x = fma(-CHEM_LDLU(lu + 13248), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 14048), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 14880), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 15808), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 17056), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 18240), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 19648), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 21184), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 22976), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 24832), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 27936), b[4736], x);
+      b[4384] = x;
+    }
+    {
+      double x = b[4352];
+      x = fma(-CHEM_LDLU(lu + 12416), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 13216), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 14016), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 18208), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 19616), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 21152), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 22944), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 24800), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 27904), b[4736], x);
+      b[4352] = x;
+    }
+    {
+      double x = b[4320];
+      x = fma(-CHEM_LDLU(lu + 11648), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 12384), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 13184), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 13984), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 14848), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 15776), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 17024), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 18176), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 19584), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 21120), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 22912), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 24768), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 27872), b[4736], x);
+      b[4320] = x;
+    }
+    {
+      double x = b[4288];
+      x = fma(-CHEM_LDLU(lu + 12352), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 13152), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 13952), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 18144), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 19552), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 21088), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 22880), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 24736), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 27840), b[4736], x);
+      b[4288] = x;
+    }
+    {
+      double x = b[4256];
+      x = fma(-CHEM_LDLU(lu + 11616), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 14816), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 19520), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 21056), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 22848), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 24704), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 27808), b[4736], x);
+      b[4256] = x;
+    }
+    {
+      double x = b[4224];
+      x = fma(-CHEM_LDLU(lu + 9792), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 10336), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 11008), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 11584), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 12320), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 13120), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 13920), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 14784), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 15744), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 16992), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 18112), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 19488), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 21024), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 22816), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 24672), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 27776), b[4736], x);
+      b[4224] = x;
+    }
+    {
+      double x = b[4192];
+      x = fma(-CHEM_LDLU(lu + 19456), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 20992), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 27744), b[4736], x);
+      b[4192] = x;
+    }
+    {
+      double x = b[4160];
+      x = fma(-CHEM_LDLU(lu + 8800), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 9248), b[4224], x);
+      x = fma(-CHEM_LDLU(lu + 9760), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 10304), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 10976), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 11552), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 12288), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 13088), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 13888), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 14752), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 15712), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 16960), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 18080), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 19424), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 20960), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 22784), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 24640), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 27712), b[4736], x);
+      b[4160] = x;
+    }
+    {
+      double x = b[4128];
+      x = fma(-CHEM_LDLU(lu + 8160), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 8768), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 13056), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 13856), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 14720), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 16928), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 20928), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 22752), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 24608), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 27680), b[4736], x);
+      b[4128] = x;
+    }
+    {
+      double x = b[4096];
+      x = fma(-CHEM_LDLU(lu + 7680), b[4128], x);
+      x = fma(-CHEM_LDLU(lu + 10944), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 12256), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 13024), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 13824), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 18048), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 19392), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 20896), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 22720), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 24576), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 27648), b[4736], x);
+      b[4096] = x;
+    }
+    {
+      double x = b[4064];
+      x = fma(-CHEM_LDLU(lu + 7232), b[4096], x);
+      x = fma(-CHEM_LDLU(lu + 7648), b[4128], x);
+      x = fma(-CHEM_LDLU(lu + 8128), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 8736), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 14688), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 16896), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 18016), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 20864), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 22688), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 24544), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 27616), b[4736], x);
+      b[4064] = x;
+    }
+    {
+      double x = b[4032];
+      x = fma(-CHEM_LDLU(lu + 8704), b[4192], x);
+      b[4032] = x;
+    }
+    {
+      double x = b[4000];
+      x = fma(-CHEM_LDLU(lu + 8672), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 11520), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 13792), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 14656), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 20832), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 22656), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 24512), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 27584), b[4736], x);
+      b[4000] = x;
+    }
+    {
+      double x = b[3968];
+      x = fma(-CHEM_LDLU(lu + 16864), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 27552), b[4736], x);
+      b[3968] = x;
+    }
+    {
+      double x = b[3936];
+      x = fma(-CHEM_LDLU(lu + 5888), b[4000], x);
+      x = fma(-CHEM_LDLU(lu + 6432), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 6880), b[4064], x);
+      x = fma(-CHEM_LDLU(lu + 7200), b[4096], x);
+      x = fma(-CHEM_LDLU(lu + 7616), b[4128], x);
+      x = fma(-CHEM_LDLU(lu + 8640), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 9728), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 10912), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 11488), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 12224), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 12992), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 13760), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 14624), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 15680), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 17984), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 19360), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 20800), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 22624), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 24480), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 27520), b[4736], x);
+      b[3936] = x;
+    }
+    {
+      double x = b[3904];
+      x = fma(-CHEM_LDLU(lu + 12960), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 22592), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 27488), b[4736], x);
+      b[3904] = x;
+    }
+    {
+      double x = b[3872];
+      x = fma(-CHEM_LDLU(lu + 4896), b[3904], x);
+      x = fma(-CHEM_LDLU(lu + 5568), b[3968], x);
+      x = fma(-CHEM_LDLU(lu + 5856), b[4000], x);
+      x = fma(-CHEM_LDLU(lu + 6400), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 6848), b[4064], x);
+      x = fma(-CHEM_LDLU(lu + 7168), b[4096], x);
+      x = fma(-CHEM_LDLU(lu + 7584), b[4128], x);
+      x = fma(-CHEM_LDLU(lu + 8096), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 8608), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 9216), b[4224], x);
+      x = fma(-CHEM_LDLU(lu + 9696), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 10272), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 10880), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 11456), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 12192), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 12928), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 13728), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 14592), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 15648), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 16832), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 17952), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 19328), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 20768), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 22560), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 24448), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 27456), b[4736], x);
+      b[3872] = x;
+    }
+    {
+      double x = b[3840];
+      x = fma(-CHEM_LDLU(lu + 5536), b[3968], x);
+      x = fma(-CHEM_LDLU(lu + 8576), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 9664), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 13696), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 14560), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 15616), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 16800), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 17920), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 20736), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 22528), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 24416), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 27424), b[4736], x);
+      b[3840] = x;
+    }
+    {
+      double x = b[3808];
+      x = fma(-CHEM_LDLU(lu + 5184), b[3936], x);
+      x = fma(-CHEM_LDLU(lu + 5824), b[4000], x);
+      x = fma(-CHEM_LDLU(lu + 6368), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 7552), b[4128], x);
+      x = fma(-CHEM_LDLU(lu + 9632), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 10240), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 10848), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 11424), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 13664), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 14528), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 17888), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 19296), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 20704), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 22496), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 24384), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 27392), b[4736], x);
+      b[3808] = x;
+    }
+    {
+      double x = b[3776];
+      x = fma(-CHEM_LDLU(lu + 24352), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 27360), b[4736], x);
+      b[3776] = x;
+    }
+    {
+      double x = b[3744];
+      x = fma(-CHEM_LDLU(lu + 4864), b[3904], x);
+      x = fma(-CHEM_LDLU(lu + 6336), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 6816), b[4064], x);
+      x = fma(-CHEM_LDLU(lu + 7136), b[4096], x);
+      x = fma(-CHEM_LDLU(lu + 9600), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 10816), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 11392), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 12160), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 12896), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 13632), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 14496), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 17856), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 19264), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 22464), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 24320), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 27328), b[4736], x);
+      b[3744] = x;
+    }
+    {
+      double x = b[3712];
+      x = fma(-CHEM_LDLU(lu + 27296), b[4736], x);
+      b[3712] = x;
+    }
+    {
+      double x = b[3680];
+      x = fma(-CHEM_LDLU(lu + 4032), b[3712], x);
+      x = fma(-CHEM_LDLU(lu + 27264), b[4736], x);
+      b[3680] = x;
+    }
+    {
+      double x = b[3648];
+      x = fma(-CHEM_LDLU(lu + 6304), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 19232), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 27232), b[4736], x);
+      b[3648] = x;
+    }
+    {
+      double x = b[3616];
+      x = fma(-CHEM_LDLU(lu + 4096), b[3744], x);
+      x = fma(-CHEM_LDLU(lu + 5152), b[3936], x);
+      x = fma(-CHEM_LDLU(lu + 5792), b[4000], x);
+      x = fma(-CHEM_LDLU(lu + 6272), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 8544), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 9568), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 10208), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 11360), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 12128), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 15584), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 17824), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 19200), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 20672), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 22432), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 24288), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 27200), b[4736], x);
+      b[3616] = x;
+    }
+    {
+      double x = b[3584];
+      x = fma(-CHEM_LDLU(lu + 4448), b[3808], x);
+      x = fma(-CHEM_LDLU(lu + 5120), b[3936], x);
+      x = fma(-CHEM_LDLU(lu + 5760), b[4000], x);
+      x = fma(-CHEM_LDLU(lu + 6240), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 9536), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 12096), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 12864), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 13600), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 19168), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 22400), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 24256), b[4704], x);
+      b[3584] = x;
+    }
+    {
+      double x = b[3552];
+      x = fma(-CHEM_LDLU(lu + 3488), b[3648], x);
+      x = fma(-CHEM_LDLU(lu + 4320), b[3776], x);
+      x = fma(-CHEM_LDLU(lu + 4832), b[3904], x);
+      x = fma(-CHEM_LDLU(lu + 5728), b[4000], x);
+      x = fma(-CHEM_LDLU(lu + 6784), b[4064], x);
+      x = fma(-CHEM_LDLU(lu + 7520), b[4128], x);
+      x = fma(-CHEM_LDLU(lu + 8064), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 9184), b[4224], x);
+      x = fma(-CHEM_LDLU(lu + 9504), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 10176), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 10784), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 11328), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 14464), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 15552), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 16768), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 17792), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 19136), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 20640), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 22368), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 24224), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 27168), b[4736], x);
+      b[3552] = x;
+    }
+    {
+      double x = b[3520];
+      x = fma(-CHEM_LDLU(lu + 8032), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 8512), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 10752), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 12064), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 12832), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 15520), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 16736), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 19104), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 20608), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 24192), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 27136), b[4736], x);
+      b[3520] = x;
+    }
+    {
+      double x = b[3488];
+      x = fma(-CHEM_LDLU(lu + 4416), b[3808], x);
+      x = fma(-CHEM_LDLU(lu + 5088), b[3936], x);
+      x = fma(-CHEM_LDLU(lu + 5696), b[4000], x);
+      x = fma(-CHEM_LDLU(lu + 6208), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 9472), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 12032), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 12800), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 13568), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 19072), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 22336), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 24160), b[4704], x);
+      b[3488] = x;
+    }
+    {
+      double x = b[3456];
+      x = fma(-CHEM_LDLU(lu + 8000), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 10720), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 16704), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 24128), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 27104), b[4736], x);
+      b[3456] = x;
+    }
+    {
+      double x = b[3424];
+      x = fma(-CHEM_LDLU(lu + 2880), b[3456], x);
+      x = fma(-CHEM_LDLU(lu + 3072), b[3552], x);
+      x = fma(-CHEM_LDLU(lu + 3456), b[3648], x);
+      x = fma(-CHEM_LDLU(lu + 4288), b[3776], x);
+      x = fma(-CHEM_LDLU(lu + 4608), b[3840], x);
+      x = fma(-CHEM_LDLU(lu + 4704), b[3872], x);
+      x = fma(-CHEM_LDLU(lu + 4800), b[3904], x);
+      x = fma(-CHEM_LDLU(lu + 5504), b[3968], x);
+      x = fma(-CHEM_LDLU(lu + 5664), b[4000], x);
+      x = fma(-CHEM_LDLU(lu + 6176), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 6752), b[4064], x);
+      x = fma(-CHEM_LDLU(lu + 7488), b[4128], x);
+      x = fma(-CHEM_LDLU(lu + 7968), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 8480), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 9152), b[4224], x);
+      x = fma(-CHEM_LDLU(lu + 9440), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 10144), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 10688), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 11296), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 12000), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 12768), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 13536), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 14432), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 15488), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 16672), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 17760), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 19040), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 20576), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 22304), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 24096), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 27072), b[4736], x);
+      b[3424] = x;
+    }
+    {
+      double x = b[3392];
+      x = fma(-CHEM_LDLU(lu + 11264), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 12736), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 13504), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 14400), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 15456), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 22272), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 27040), b[4736], x);
+      b[3392] = x;
+    }
+    {
+      double x = b[3360];
+      x = fma(-CHEM_LDLU(lu + 16640), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 27008), b[4736], x);
+      b[3360] = x;
+    }
+    {
+      double x = b[3328];
+      x = fma(-CHEM_LDLU(lu + 3296), b[3616], x);
+      x = fma(-CHEM_LDLU(lu + 5056), b[3936], x);
+      x = fma(-CHEM_LDLU(lu + 6144), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 8448), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 11968), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 15424), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 19008), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 20544), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 24064), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 26976), b[4736], x);
+      b[3328] = x;
+    }
+    {
+      double x = b[3296];
+      x = fma(-CHEM_LDLU(lu + 4256), b[3776], x);
+      x = fma(-CHEM_LDLU(lu + 4576), b[3840], x);
+      x = fma(-CHEM_LDLU(lu + 4768), b[3904], x);
+      x = fma(-CHEM_LDLU(lu + 5632), b[4000], x);
+      x = fma(-CHEM_LDLU(lu + 9120), b[4224], x);
+      x = fma(-CHEM_LDLU(lu + 9408), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 11936), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 12704), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 13472), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 14368), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 15392), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 18976), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 22240), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 24032), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 26944), b[4736], x);
+      b[3296] = x;
+    }
+    {
+      double x = b[3232];
+      x = fma(-CHEM_LDLU(lu + 14336), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 16608), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 24000), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 26912), b[4736], x);
+      b[3232] = x;
+    }
+    {
+      double x = b[3200];
+      x = fma(-CHEM_LDLU(lu + 3744), b[3680], x);
+      x = fma(-CHEM_LDLU(lu + 4000), b[3712], x);
+      x = fma(-CHEM_LDLU(lu + 26880), b[4736], x);
+      b[3200] = x;
+    }
+    {
+      double x = b[3168];
+      x = fma(-CHEM_LDLU(lu + 2176), b[3200], x);
+      x = fma(-CHEM_LDLU(lu + 3712), b[3680], x);
+      x = fma(-CHEM_LDLU(lu + 3968), b[3712], x);
+      x = fma(-CHEM_LDLU(lu + 26848), b[4736], x);
+      b[3168] = x;
+    }
+    {
+      double x = b[3136];
+      x = fma(-CHEM_LDLU(lu + 2272), b[3232], x);
+      x = fma(-CHEM_LDLU(lu + 2848), b[3456], x);
+      x = fma(-CHEM_LDLU(lu + 3040), b[3552], x);
+      x = fma(-CHEM_LDLU(lu + 3424), b[3648], x);
+      x = fma(-CHEM_LDLU(lu + 4736), b[3904], x);
+      x = fma(-CHEM_LDLU(lu + 5472), b[3968], x);
+      x = fma(-CHEM_LDLU(lu + 5600), b[4000], x);
+      x = fma(-CHEM_LDLU(lu + 6720), b[4064], x);
+      x = fma(-CHEM_LDLU(lu + 7456), b[4128], x);
+      x = fma(-CHEM_LDLU(lu + 7936), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 9088), b[4224], x);
+      x = fma(-CHEM_LDLU(lu + 9376), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 10112), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 10656), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 11232), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 14304), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 15360), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 16576), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 17728), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 18944), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 20512), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 22208), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 23968), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 26816), b[4736], x);
+      b[3136] = x;
+    }
+    {
+      double x = b[3104];
+      x = fma(-CHEM_LDLU(lu + 5024), b[3936], x);
+      x = fma(-CHEM_LDLU(lu + 6112), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 9344), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 11904), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 12672), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 13440), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 18912), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 22176), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 23936), b[4704], x);
+      b[3104] = x;
+    }
+    {
+      double x = b[3008];
+      x = fma(-CHEM_LDLU(lu + 1664), b[3040], x);
+      x = fma(-CHEM_LDLU(lu + 2816), b[3456], x);
+      x = fma(-CHEM_LDLU(lu + 10624), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 16544), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 26784), b[4736], x);
+      b[3008] = x;
+    }
+    {
+      double x = b[2976];
+      x = fma(-CHEM_LDLU(lu + 10592), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 16512), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 20480), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 26752), b[4736], x);
+      b[2976] = x;
+    }
+    {
+      double x = b[2944];
+      x = fma(-CHEM_LDLU(lu + 1824), b[3072], x);
+      x = fma(-CHEM_LDLU(lu + 2432), b[3264], x);
+      x = fma(-CHEM_LDLU(lu + 11872), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 23904), b[4704], x);
+      b[2944] = x;
+    }
+    {
+      double x = b[2912];
+      x = fma(-CHEM_LDLU(lu + 2016), b[3168], x);
+      x = fma(-CHEM_LDLU(lu + 2144), b[3200], x);
+      x = fma(-CHEM_LDLU(lu + 3680), b[3680], x);
+      x = fma(-CHEM_LDLU(lu + 3936), b[3712], x);
+      x = fma(-CHEM_LDLU(lu + 26720), b[4736], x);
+      b[2912] = x;
+    }
+    {
+      double x = b[2880];
+      x = fma(-CHEM_LDLU(lu + 10080), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 17696), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 22144), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 23872), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 26688), b[4736], x);
+      b[2880] = x;
+    }
+    {
+      double x = b[2848];
+      x = fma(-CHEM_LDLU(lu + 2592), b[3360], x);
+      x = fma(-CHEM_LDLU(lu + 11840), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 20448), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 22112), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 23840), b[4704], x);
+      b[2848] = x;
+    }
+    {
+      double x = b[2816];
+      x = fma(-CHEM_LDLU(lu + 1984), b[3168], x);
+      x = fma(-CHEM_LDLU(lu + 2112), b[3200], x);
+      x = fma(-CHEM_LDLU(lu + 3648), b[3680], x);
+      x = fma(-CHEM_LDLU(lu + 3904), b[3712], x);
+      x = fma(-CHEM_LDLU(lu + 26656), b[4736], x);
+      b[2816] = x;
+    }
+    {
+      double x = b[2784];
+      x = fma(-CHEM_LDLU(lu + 1472), b[2816], x);
+      x = fma(-CHEM_LDLU(lu + 1952), b[3168], x);
+      x = fma(-CHEM_LDLU(lu + 2080), b[3200], x);
+      x = fma(-CHEM_LDLU(lu + 3616), b[3680], x);
+      x = fma(-CHEM_LDLU(lu + 3872), b[3712], x);
+      x = fma(-CHEM_LDLU(lu + 26624), b[4736], x);
+      b[2784] = x;
+    }
+    {
+      double x = b[2752];
+      x = fma(-CHEM_LDLU(lu + 1344), b[2784], x);
+      x = fma(-CHEM_LDLU(lu + 1440), b[2816], x);
+      x = fma(-CHEM_LDLU(lu + 1920), b[3168], x);
+      x = fma(-CHEM_LDLU(lu + 2048), b[3200], x);
+      x = fma(-CHEM_LDLU(lu + 3584), b[3680], x);
+      x = fma(-CHEM_LDLU(lu + 3840), b[3712], x);
+      x = fma(-CHEM_LDLU(lu + 26592), b[4736], x);
+      b[2752] = x;
+    }
+    {
+      double x = b[2720];
+      x = fma(-CHEM_LDLU(lu + 5440), b[3968], x);
+      x = fma(-CHEM_LDLU(lu + 15328), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 16480), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 23808), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 26560), b[4736], x);
+      b[2720] = x;
+    }
+    {
+      double x = b[2688];
+      x = fma(-CHEM_LDLU(lu + 13408), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 26528), b[4736], x);
+      b[2688] = x;
+    }
+    {
+      double x = b[2656];
+      x = fma(-CHEM_LDLU(lu + 2240), b[3232], x);
+      x = fma(-CHEM_LDLU(lu + 3392), b[3648], x);
+      x = fma(-CHEM_LDLU(lu + 4224), b[3776], x);
+      x = fma(-CHEM_LDLU(lu + 4544), b[3840], x);
+      x = fma(-CHEM_LDLU(lu + 7904), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 10560), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 11200), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 14272), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 15296), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 16448), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 17664), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 18880), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 20416), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 22080), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 23776), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 26496), b[4736], x);
+      b[2656] = x;
+    }
+    {
+      double x = b[2592];
+      x = fma(-CHEM_LDLU(lu + 16416), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 18848), b[4608], x);
+      b[2592] = x;
+    }
+    {
+      double x = b[2560];
+      x = fma(-CHEM_LDLU(lu + 1184), b[2624], x);
+      x = fma(-CHEM_LDLU(lu + 1792), b[3072], x);
+      x = fma(-CHEM_LDLU(lu + 2400), b[3264], x);
+      x = fma(-CHEM_LDLU(lu + 11808), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 23744), b[4704], x);
+      b[2560] = x;
+    }
+    {
+      double x = b[2528];
+      x = fma(-CHEM_LDLU(lu + 2208), b[3232], x);
+      x = fma(-CHEM_LDLU(lu + 2784), b[3424], x);
+      x = fma(-CHEM_LDLU(lu + 4672), b[3872], x);
+      x = fma(-CHEM_LDLU(lu + 6080), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 6688), b[4064], x);
+      x = fma(-CHEM_LDLU(lu + 7104), b[4096], x);
+      x = fma(-CHEM_LDLU(lu + 7872), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 9056), b[4224], x);
+      x = fma(-CHEM_LDLU(lu + 10048), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 10528), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 11168), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 14240), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 15264), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 16384), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 17632), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 18816), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 20384), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 22048), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 23712), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 26464), b[4736], x);
+      b[2528] = x;
+    }
+    {
+      double x = b[2496];
+      x = fma(-CHEM_LDLU(lu + 1152), b[2624], x);
+      x = fma(-CHEM_LDLU(lu + 1760), b[3072], x);
+      x = fma(-CHEM_LDLU(lu + 2368), b[3264], x);
+      x = fma(-CHEM_LDLU(lu + 11776), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 23680), b[4704], x);
+      b[2496] = x;
+    }
+    {
+      double x = b[2464];
+      x = fma(-CHEM_LDLU(lu + 11744), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 18784), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 26432), b[4736], x);
+      b[2464] = x;
+    }
+    {
+      double x = b[2432];
+      x = fma(-CHEM_LDLU(lu + 10496), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 16352), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 20352), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 26400), b[4736], x);
+      b[2432] = x;
+    }
+    {
+      double x = b[2400];
+      x = fma(-CHEM_LDLU(lu + 1568), b[2976], x);
+      x = fma(-CHEM_LDLU(lu + 10464), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 16320), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 20320), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 26368), b[4736], x);
+      b[2400] = x;
+    }
+    {
+      double x = b[2368];
+      x = fma(-CHEM_LDLU(lu + 7840), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 16288), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 20288), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 26336), b[4736], x);
+      b[2368] = x;
+    }
+    {
+      double x = b[2336];
+      x = fma(-CHEM_LDLU(lu + 7808), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 16256), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 20256), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 26304), b[4736], x);
+      b[2336] = x;
+    }
+    {
+      double x = b[2304];
+      x = fma(-CHEM_LDLU(lu + 1248), b[2752], x);
+      x = fma(-CHEM_LDLU(lu + 1312), b[2784], x);
+      x = fma(-CHEM_LDLU(lu + 1408), b[2816], x);
+      x = fma(-CHEM_LDLU(lu + 3552), b[3680], x);
+      x = fma(-CHEM_LDLU(lu + 3808), b[3712], x);
+      x = fma(-CHEM_LDLU(lu + 26272), b[4736], x);
+      b[2304] = x;
+    }
+    {
+      double x = b[2272];
+      x = fma(-CHEM_LDLU(lu + 12640), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 15232), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 22016), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 26240), b[4736], x);
+      b[2272] = x;
+    }
+    {
+      double x = b[2208];
+      x = fma(-CHEM_LDLU(lu + 23648), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 26208), b[4736], x);
+      b[2208] = x;
+    }
+    {
+      double x = b[2176];
+      x = fma(-CHEM_LDLU(lu + 832), b[2464], x);
+      x = fma(-CHEM_LDLU(lu + 2560), b[3328], x);
+      x = fma(-CHEM_LDLU(lu + 4992), b[3936], x);
+      x = fma(-CHEM_LDLU(lu + 6048), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 8416), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 15200), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 20224), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 23616), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 26176), b[4736], x);
+      b[2176] = x;
+    }
+}
+__device__ __noinline__ void solve_t_0_2(double* __restrict__ ws, int rhs)
+{
+    const double* __restrict__ lu = ws + 72864;
+    const double* __restrict__ vd = ws + 126944;
+    double* __restrict__ b = ws + rhs * 32;
+    (void)vd;
+    {
+      double x = b[2144];
+      x = fma(-CHEM_LDLU(lu + 768), b[2240], x);
+      x = fma(-CHEM_LDLU(lu + 1728), b[3072], x);
+      x = fma(-CHEM_LDLU(lu + 2336), b[3264], x);
+      x = fma(-CHEM_LDLU(lu + 11712), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 23584), b[4704], x);
+      b[2144] = x;
+    }
+    {
+      double x = b[2112];
+      x = fma(-CHEM_LDLU(lu + 6016), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 6656), b[4064], x);
+      x = fma(-CHEM_LDLU(lu + 7072), b[4096], x);
+      x = fma(-CHEM_LDLU(lu + 7776), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 9024), b[4224], x);
+      x = fma(-CHEM_LDLU(lu + 10016), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 10432), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 11136), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 14208), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 15168), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 17600), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 18752), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 20192), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 21984), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 26144), b[4736], x);
+      b[2112] = x;
+    }
+    {
+      double x = b[2048];
+      x = fma(-CHEM_LDLU(lu + 672), b[2080], x);
+      x = fma(-CHEM_LDLU(lu + 1504), b[2848], x);
+      x = fma(-CHEM_LDLU(lu + 5984), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 6624), b[4064], x);
+      x = fma(-CHEM_LDLU(lu + 7040), b[4096], x);
+      x = fma(-CHEM_LDLU(lu + 7744), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 8992), b[4224], x);
+      x = fma(-CHEM_LDLU(lu + 9984), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 10400), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 11104), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 14176), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 15136), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 17568), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 18720), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 20160), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 21952), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 26112), b[4736], x);
+      b[2048] = x;
+    }
+    {
+      double x = b[2016];
+      x = fma(-CHEM_LDLU(lu + 736), b[2208], x);
+      x = fma(-CHEM_LDLU(lu + 2976), b[3520], x);
+      x = fma(-CHEM_LDLU(lu + 5408), b[3968], x);
+      x = fma(-CHEM_LDLU(lu + 8384), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 12608), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 15104), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 16224), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 20128), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 26080), b[4736], x);
+      b[2016] = x;
+    }
+    {
+      double x = b[1984];
+      x = fma(-CHEM_LDLU(lu + 2720), b[3392], x);
+      x = fma(-CHEM_LDLU(lu + 3360), b[3648], x);
+      x = fma(-CHEM_LDLU(lu + 6592), b[4064], x);
+      x = fma(-CHEM_LDLU(lu + 7008), b[4096], x);
+      x = fma(-CHEM_LDLU(lu + 7424), b[4128], x);
+      x = fma(-CHEM_LDLU(lu + 8960), b[4224], x);
+      x = fma(-CHEM_LDLU(lu + 9952), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 11072), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 12576), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 13376), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 17536), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 18688), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 21920), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 23552), b[4704], x);
+      b[1984] = x;
+    }
+    {
+      double x = b[1952];
+      x = fma(-CHEM_LDLU(lu + 6976), b[4096], x);
+      x = fma(-CHEM_LDLU(lu + 7392), b[4128], x);
+      x = fma(-CHEM_LDLU(lu + 17504), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 18656), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 20096), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 21888), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 26048), b[4736], x);
+      b[1952] = x;
+    }
+    {
+      double x = b[1920];
+      x = fma(-CHEM_LDLU(lu + 1088), b[2592], x);
+      x = fma(-CHEM_LDLU(lu + 8352), b[4192], x);
+      b[1920] = x;
+    }
+    {
+      double x = b[1856];
+      x = fma(-CHEM_LDLU(lu + 544), b[1888], x);
+      x = fma(-CHEM_LDLU(lu + 10368), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 20064), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 26016), b[4736], x);
+      b[1856] = x;
+    }
+    {
+      double x = b[1824];
+      x = fma(-CHEM_LDLU(lu + 16192), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 25984), b[4736], x);
+      b[1824] = x;
+    }
+    {
+      double x = b[1792];
+      x = fma(-CHEM_LDLU(lu + 4064), b[3744], x);
+      x = fma(-CHEM_LDLU(lu + 5952), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 9312), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 14144), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 18624), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 25952), b[4736], x);
+      b[1792] = x;
+    }
+    {
+      double x = b[1760];
+      x = fma(-CHEM_LDLU(lu + 2528), b[3328], x);
+      x = fma(-CHEM_LDLU(lu + 8320), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 15072), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 20032), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 23520), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 25920), b[4736], x);
+      b[1760] = x;
+    }
+    {
+      double x = b[1728];
+      x = fma(-CHEM_LDLU(lu + 800), b[2272], x);
+      x = fma(-CHEM_LDLU(lu + 4192), b[3776], x);
+      x = fma(-CHEM_LDLU(lu + 11680), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 15040), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 18592), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 23488), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 25888), b[4736], x);
+      b[1728] = x;
+    }
+    {
+      double x = b[1696];
+      x = fma(-CHEM_LDLU(lu + 18560), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 20000), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 23456), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 25856), b[4736], x);
+      b[1696] = x;
+    }
+    {
+      double x = b[1664];
+      x = fma(-CHEM_LDLU(lu + 1888), b[3136], x);
+      x = fma(-CHEM_LDLU(lu + 2496), b[3296], x);
+      x = fma(-CHEM_LDLU(lu + 2752), b[3424], x);
+      x = fma(-CHEM_LDLU(lu + 6560), b[4064], x);
+      x = fma(-CHEM_LDLU(lu + 21856), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 25824), b[4736], x);
+      b[1664] = x;
+    }
+    {
+      double x = b[1632];
+      x = fma(-CHEM_LDLU(lu + 3008), b[3552], x);
+      x = fma(-CHEM_LDLU(lu + 4160), b[3776], x);
+      x = fma(-CHEM_LDLU(lu + 4512), b[3840], x);
+      x = fma(-CHEM_LDLU(lu + 5920), b[4032], x);
+      x = fma(-CHEM_LDLU(lu + 6528), b[4064], x);
+      x = fma(-CHEM_LDLU(lu + 8928), b[4224], x);
+      x = fma(-CHEM_LDLU(lu + 11040), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 15008), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 17472), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 18528), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 19968), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 21824), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 25792), b[4736], x);
+      b[1632] = x;
+    }
+    {
+      double x = b[1536];
+      x = fma(-CHEM_LDLU(lu + 16160), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 25760), b[4736], x);
+      b[1536] = x;
+    }
+    {
+      double x = b[1504];
+      x = fma(-CHEM_LDLU(lu + 1216), b[2752], x);
+      x = fma(-CHEM_LDLU(lu + 1280), b[2784], x);
+      x = fma(-CHEM_LDLU(lu + 1376), b[2816], x);
+      x = fma(-CHEM_LDLU(lu + 3520), b[3680], x);
+      x = fma(-CHEM_LDLU(lu + 3776), b[3712], x);
+      x = fma(-CHEM_LDLU(lu + 25728), b[4736], x);
+      b[1504] = x;
+    }
+    {
+      double x = b[1472];
+      x = fma(-CHEM_LDLU(lu + 25696), b[4736], x);
+      b[1472] = x;
+    }
+    {
+      double x = b[1440];
+      x = fma(-CHEM_LDLU(lu + 25664), b[4736], x);
+      b[1440] = x;
+    }
+    {
+      double x = b[1344];
+      x = fma(-CHEM_LDLU(lu + 12544), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 13344), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 18496), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 19936), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 21792), b[4672], x);
+      b[1344] = x;
+    }
+    {
+      double x = b[1280];
+      x = fma(-CHEM_LDLU(lu + 640), b[1920], x);
+      x = fma(-CHEM_LDLU(lu + 1056), b[2592], x);
+      x = fma(-CHEM_LDLU(lu + 8288), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 18464), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 19904), b[4640], x);
+      b[1280] = x;
+    }
+    {
+      double x = b[1248];
+      x = fma(-CHEM_LDLU(lu + 1024), b[2592], x);
+      x = fma(-CHEM_LDLU(lu + 8256), b[4192], x);
+      b[1248] = x;
+    }
+    {
+      double x = b[1216];
+      x = fma(-CHEM_LDLU(lu + 512), b[1824], x);
+      x = fma(-CHEM_LDLU(lu + 2944), b[3520], x);
+      x = fma(-CHEM_LDLU(lu + 8224), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 16128), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 18432), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 19872), b[4640], x);
+      b[1216] = x;
+    }
+    {
+      double x = b[1184];
+      x = fma(-CHEM_LDLU(lu + 1600), b[3008], x);
+      x = fma(-CHEM_LDLU(lu + 1632), b[3040], x);
+      x = fma(-CHEM_LDLU(lu + 16096), b[4544], x);
+      b[1184] = x;
+    }
+    {
+      double x = b[1152];
+      x = fma(-CHEM_LDLU(lu + 896), b[2560], x);
+      x = fma(-CHEM_LDLU(lu + 3136), b[3584], x);
+      x = fma(-CHEM_LDLU(lu + 3264), b[3616], x);
+      x = fma(-CHEM_LDLU(lu + 4384), b[3808], x);
+      x = fma(-CHEM_LDLU(lu + 5376), b[3968], x);
+      x = fma(-CHEM_LDLU(lu + 16064), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 17440), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 21760), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 23424), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 25632), b[4736], x);
+      b[1152] = x;
+    }
+    {
+      double x = b[1120];
+      x = fma(-CHEM_LDLU(lu + 864), b[2496], x);
+      x = fma(-CHEM_LDLU(lu + 3104), b[3584], x);
+      x = fma(-CHEM_LDLU(lu + 3232), b[3616], x);
+      x = fma(-CHEM_LDLU(lu + 4352), b[3808], x);
+      x = fma(-CHEM_LDLU(lu + 5344), b[3968], x);
+      x = fma(-CHEM_LDLU(lu + 16032), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 17408), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 21728), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 23392), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 25600), b[4736], x);
+      b[1120] = x;
+    }
+    {
+      double x = b[1088];
+      x = fma(-CHEM_LDLU(lu + 1536), b[2944], x);
+      x = fma(-CHEM_LDLU(lu + 2912), b[3488], x);
+      x = fma(-CHEM_LDLU(lu + 3200), b[3616], x);
+      x = fma(-CHEM_LDLU(lu + 4960), b[3936], x);
+      x = fma(-CHEM_LDLU(lu + 5312), b[3968], x);
+      x = fma(-CHEM_LDLU(lu + 16000), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 17376), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 21696), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 23360), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 25568), b[4736], x);
+      b[1088] = x;
+    }
+    {
+      double x = b[1056];
+      x = fma(-CHEM_LDLU(lu + 224), b[1312], x);
+      x = fma(-CHEM_LDLU(lu + 2464), b[3296], x);
+      x = fma(-CHEM_LDLU(lu + 21664), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 25536), b[4736], x);
+      b[1056] = x;
+    }
+    {
+      double x = b[1024];
+      x = fma(-CHEM_LDLU(lu + 4640), b[3872], x);
+      x = fma(-CHEM_LDLU(lu + 8192), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 19840), b[4640], x);
+      x = fma(-CHEM_LDLU(lu + 25504), b[4736], x);
+      b[1024] = x;
+    }
+    {
+      double x = b[960];
+      x = fma(-CHEM_LDLU(lu + 2688), b[3392], x);
+      x = fma(-CHEM_LDLU(lu + 3328), b[3648], x);
+      x = fma(-CHEM_LDLU(lu + 6496), b[4064], x);
+      x = fma(-CHEM_LDLU(lu + 6944), b[4096], x);
+      x = fma(-CHEM_LDLU(lu + 7360), b[4128], x);
+      x = fma(-CHEM_LDLU(lu + 8896), b[4224], x);
+      x = fma(-CHEM_LDLU(lu + 9920), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 12512), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 13312), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 17344), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 18400), b[4608], x);
+      x = fma(-CHEM_LDLU(lu + 21632), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 23328), b[4704], x);
+      b[960] = x;
+    }
+    {
+      double x = b[928];
+      x = fma(-CHEM_LDLU(lu + 2656), b[3392], x);
+      x = fma(-CHEM_LDLU(lu + 6464), b[4064], x);
+      x = fma(-CHEM_LDLU(lu + 8864), b[4224], x);
+      x = fma(-CHEM_LDLU(lu + 9888), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 17312), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 21600), b[4672], x);
+      b[928] = x;
+    }
+    {
+      double x = b[896];
+      x = fma(-CHEM_LDLU(lu + 128), b[928], x);
+      x = fma(-CHEM_LDLU(lu + 2624), b[3392], x);
+      x = fma(-CHEM_LDLU(lu + 5280), b[3968], x);
+      x = fma(-CHEM_LDLU(lu + 9856), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 15968), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 17280), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 21568), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 25472), b[4736], x);
+      b[896] = x;
+    }
+    {
+      double x = b[864];
+      x = fma(-CHEM_LDLU(lu + 4480), b[3840], x);
+      x = fma(-CHEM_LDLU(lu + 5248), b[3968], x);
+      x = fma(-CHEM_LDLU(lu + 7328), b[4128], x);
+      x = fma(-CHEM_LDLU(lu + 14976), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 15936), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 17248), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 21536), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 23296), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 25440), b[4736], x);
+      b[864] = x;
+    }
+    {
+      double x = b[832];
+      x = fma(-CHEM_LDLU(lu + 5216), b[3968], x);
+      x = fma(-CHEM_LDLU(lu + 7296), b[4128], x);
+      x = fma(-CHEM_LDLU(lu + 9824), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 15904), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 17216), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 21504), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 25408), b[4736], x);
+      b[832] = x;
+    }
+    {
+      double x = b[768];
+      x = fma(-CHEM_LDLU(lu + 96), b[800], x);
+      x = fma(-CHEM_LDLU(lu + 25376), b[4736], x);
+      b[768] = x;
+    }
+    {
+      double x = b[736];
+      x = fma(-CHEM_LDLU(lu + 480), b[1472], x);
+      x = fma(-CHEM_LDLU(lu + 25344), b[4736], x);
+      b[736] = x;
+    }
+    {
+      double x = b[704];
+      x = fma(-CHEM_LDLU(lu + 448), b[1440], x);
+      x = fma(-CHEM_LDLU(lu + 25312), b[4736], x);
+      b[704] = x;
+    }
+    {
+      double x = b[672];
+      x = fma(-CHEM_LDLU(lu + 7712), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 25280), b[4736], x);
+      b[672] = x;
+    }
+    {
+      double x = b[576];
+      x = fma(-CHEM_LDLU(lu + 64), b[608], x);
+      x = fma(-CHEM_LDLU(lu + 192), b[1312], x);
+      b[576] = x;
+    }
+    {
+      double x = b[544];
+      x = fma(-CHEM_LDLU(lu + 160), b[1248], x);
+      x = fma(-CHEM_LDLU(lu + 992), b[2592], x);
+      b[544] = x;
+    }
+    {
+      double x = b[512];
+      x = fma(-CHEM_LDLU(lu + 608), b[1920], x);
+      x = fma(-CHEM_LDLU(lu + 960), b[2592], x);
+      b[512] = x;
+    }
+    {
+      double x = b[480];
+      x = fma(-CHEM_LDLU(lu + 576), b[1920], x);
+      x = fma(-CHEM_LDLU(lu + 928), b[2592], x);
+      b[480] = x;
+    }
+    {
+      double x = b[448];
+      x = fma(-CHEM_LDLU(lu + 1120), b[2624], x);
+      x = fma(-CHEM_LDLU(lu + 1696), b[3072], x);
+      x = fma(-CHEM_LDLU(lu + 2304), b[3264], x);
+      x = fma(-CHEM_LDLU(lu + 25248), b[4736], x);
+      b[448] = x;
+    }
+    {
+      double x = b[416];
+      x = fma(-CHEM_LDLU(lu + 12480), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 21472), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 25216), b[4736], x);
+      b[416] = x;
+    }
+    {
+      double x = b[384];
+      x = fma(-CHEM_LDLU(lu + 704), b[2144], x);
+      x = fma(-CHEM_LDLU(lu + 1856), b[3104], x);
+      x = fma(-CHEM_LDLU(lu + 3168), b[3616], x);
+      x = fma(-CHEM_LDLU(lu + 4928), b[3936], x);
+      x = fma(-CHEM_LDLU(lu + 21440), b[4672], x);
+      x = fma(-CHEM_LDLU(lu + 23264), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 25184), b[4736], x);
+      b[384] = x;
+    }
+    {
+      double x = b[352];
+      x = fma(-CHEM_LDLU(lu + 4128), b[3776], x);
+      x = fma(-CHEM_LDLU(lu + 9280), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 14112), b[4480], x);
+      x = fma(-CHEM_LDLU(lu + 23232), b[4704], x);
+      x = fma(-CHEM_LDLU(lu + 25152), b[4736], x);
+      b[352] = x;
+    }
+    {
+      double x = b[320];
+      x = fma(-CHEM_LDLU(lu + 6912), b[4096], x);
+      x = fma(-CHEM_LDLU(lu + 7264), b[4128], x);
+      x = fma(-CHEM_LDLU(lu + 8832), b[4224], x);
+      x = fma(-CHEM_LDLU(lu + 12448), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 13280), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 17184), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 21408), b[4672], x);
+      b[320] = x;
+    }
+    {
+      double x = b[224];
+      x = fma(-CHEM_LDLU(lu + 416), b[1408], x);
+      b[224] = x;
+    }
+    {
+      double x = b[192];
+      x = fma(-CHEM_LDLU(lu + 384), b[1408], x);
+      b[192] = x;
+    }
+    {
+      double x = b[160];
+      x = fma(-CHEM_LDLU(lu + 352), b[1408], x);
+      b[160] = x;
+    }
+    {
+      double x = b[128];
+      x = fma(-CHEM_LDLU(lu + 320), b[1376], x);
+      b[128] = x;
+    }
+    {
+      double x = b[96];
+      x = fma(-CHEM_LDLU(lu + 288), b[1376], x);
+      b[96] = x;
+    }
+    {
+      double x = b[64];
+      x = fma(-CHEM_LDLU(lu + 256), b[1376], x);
+      b[64] = x;
+    }
+    {
+      double x = b[0];
+      x = fma(-CHEM_LDLU(lu + 32), b[32], x);
+      b[0] = x;
+    }
+}
+}  // namespace mech_cb6r5_ae7_aq

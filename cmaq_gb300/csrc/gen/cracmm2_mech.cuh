@@ -36,6 +36,16 @@ constexpr int EBI_OFF_YCP = 3673;
 constexpr int EBI_OFF_PROD = 3862;
 constexpr int EBI_OFF_LOSS = 4051;
 constexpr int EBI_OFF_PNEG = 4240;
+constexpr int ADJ_WS_ELEMS = 8812;
+constexpr int ADJ_LAM = 6769;
+constexpr int ADJ_MU1 = 6958;
+constexpr int ADJ_MU2 = 7147;
+constexpr int ADJ_MU3 = 7336;
+constexpr int ADJ_PHI = 7525;
+constexpr int ADJ_TMP = 7714;
+constexpr int ADJ_EMIS = 7903;
+constexpr int ADJ_GE = 8092;
+constexpr int ADJ_GK = 8281;
 constexpr double FLOPS_STEP_DAY = 79988.0;
 constexpr double FLOPS_STEP_NIGHT = 77148.0;
 extern __constant__ int c_inew2old[189];
@@ -114,6 +124,106 @@ __device__ void solve_1_1(double* __restrict__ ws, int rhs);
 __device__ void solve_1_2(double* __restrict__ ws, int rhs);
 __device__ void solve_1_3(double* __restrict__ ws, int rhs);
 __device__ void solve_1_4(double* __restrict__ ws, int rhs);
+__device__ void solve_t_0_0(double* __restrict__ ws, int rhs);
+__device__ void solve_t_0_1(double* __restrict__ ws, int rhs);
+__device__ void solve_t_0_2(double* __restrict__ ws, int rhs);
+__device__ void solve_t_0_3(double* __restrict__ ws, int rhs);
+__device__ void solve_t_0_4(double* __restrict__ ws, int rhs);
+__device__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_0_12(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_hess3_0_0(double* __restrict__ ws);
+__device__ void adj_hess3_0_1(double* __restrict__ ws);
+__device__ void adj_hess3_0_2(double* __restrict__ ws);
+__device__ void adj_hess3_0_3(double* __restrict__ ws);
+__device__ void adj_hess3_0_4(double* __restrict__ ws);
+__device__ void adj_hess3_0_5(double* __restrict__ ws);
+__device__ void adj_hess3_0_6(double* __restrict__ ws);
+__device__ void adj_hess3_0_7(double* __restrict__ ws);
+__device__ void adj_hess3_0_8(double* __restrict__ ws);
+__device__ void adj_hess3_0_9(double* __restrict__ ws);
+__device__ void adj_hess3_0_10(double* __restrict__ ws);
+__device__ void adj_hess3_0_11(double* __restrict__ ws);
+__device__ void adj_hess3_0_12(double* __restrict__ ws);
+__device__ void adj_hess3_0_13(double* __restrict__ ws);
+__device__ void adj_hess3_0_14(double* __restrict__ ws);
+__device__ void adj_hess3_0_15(double* __restrict__ ws);
+__device__ void adj_hess3_0_16(double* __restrict__ ws);
+__device__ void adj_hess3_0_17(double* __restrict__ ws);
+__device__ void adj_hess3_0_18(double* __restrict__ ws);
+__device__ void adj_hess3_0_19(double* __restrict__ ws);
+__device__ void adj_hess3_0_20(double* __restrict__ ws);
+__device__ void adj_hess3_0_21(double* __restrict__ ws);
+__device__ void adj_hess3_0_22(double* __restrict__ ws);
+__device__ void adj_hess3_0_23(double* __restrict__ ws);
+__device__ void adj_hess3_0_24(double* __restrict__ ws);
+__device__ void adj_hess3_0_25(double* __restrict__ ws);
+__device__ void adj_hess3_0_26(double* __restrict__ ws);
+__device__ void adj_hess3_0_27(double* __restrict__ ws);
+__device__ void adj_hess3_0_28(double* __restrict__ ws);
+__device__ void adj_hess3_0_29(double* __restrict__ ws);
+__device__ void adj_hess3_0_30(double* __restrict__ ws);
+__device__ void adj_hess3_0_31(double* __restrict__ ws);
+__device__ void adj_hess3_0_32(double* __restrict__ ws);
+__device__ void solve_t_1_0(double* __restrict__ ws, int rhs);
+__device__ void solve_t_1_1(double* __restrict__ ws, int rhs);
+__device__ void solve_t_1_2(double* __restrict__ ws, int rhs);
+__device__ void solve_t_1_3(double* __restrict__ ws, int rhs);
+__device__ void solve_t_1_4(double* __restrict__ ws, int rhs);
+__device__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_1_11(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_jtv_1_12(double* __restrict__ ws, int yoff, int phioff, int outoff);
+__device__ void adj_hess3_1_0(double* __restrict__ ws);
+__device__ void adj_hess3_1_1(double* __restrict__ ws);
+__device__ void adj_hess3_1_2(double* __restrict__ ws);
+__device__ void adj_hess3_1_3(double* __restrict__ ws);
+__device__ void adj_hess3_1_4(double* __restrict__ ws);
+__device__ void adj_hess3_1_5(double* __restrict__ ws);
+__device__ void adj_hess3_1_6(double* __restrict__ ws);
+__device__ void adj_hess3_1_7(double* __restrict__ ws);
+__device__ void adj_hess3_1_8(double* __restrict__ ws);
+__device__ void adj_hess3_1_9(double* __restrict__ ws);
+__device__ void adj_hess3_1_10(double* __restrict__ ws);
+__device__ void adj_hess3_1_11(double* __restrict__ ws);
+__device__ void adj_hess3_1_12(double* __restrict__ ws);
+__device__ void adj_hess3_1_13(double* __restrict__ ws);
+__device__ void adj_hess3_1_14(double* __restrict__ ws);
+__device__ void adj_hess3_1_15(double* __restrict__ ws);
+__device__ void adj_hess3_1_16(double* __restrict__ ws);
+__device__ void adj_hess3_1_17(double* __restrict__ ws);
+__device__ void adj_hess3_1_18(double* __restrict__ ws);
+__device__ void adj_hess3_1_19(double* __restrict__ ws);
+__device__ void adj_hess3_1_20(double* __restrict__ ws);
+__device__ void adj_hess3_1_21(double* __restrict__ ws);
+__device__ void adj_hess3_1_22(double* __restrict__ ws);
+__device__ void adj_hess3_1_23(double* __restrict__ ws);
+__device__ void adj_hess3_1_24(double* __restrict__ ws);
+__device__ void adj_hess3_1_25(double* __restrict__ ws);
+__device__ void adj_hess3_1_26(double* __restrict__ ws);
+__device__ void adj_hess3_1_27(double* __restrict__ ws);
+__device__ void adj_hess3_1_28(double* __restrict__ ws);
+__device__ void adj_hess3_1_29(double* __restrict__ ws);
+__device__ void adj_hess3_1_30(double* __restrict__ ws);
 constexpr int EBI_N_EBISP = 176;
 constexpr double EBI_DELTAT = 2.5;
 constexpr int EBI_NEBITER = 1000;
@@ -157,6 +267,63 @@ __device__ __forceinline__ void jacdecomp_0(double* __restrict__ ws, double gdti
     jacdecomp_0_25(ws, gdtinv);
     jacdecomp_0_26(ws, gdtinv);
 }
+__device__ __forceinline__ void jacdecomp_0_sync(double* __restrict__ ws, double gdtinv, bool go)
+{
+    if (go) jacdecomp_0_0(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_1(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_2(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_3(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_4(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_5(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_6(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_7(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_8(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_9(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_10(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_11(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_12(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_13(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_14(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_15(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_16(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_17(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_18(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_19(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_20(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_21(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_22(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_23(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_24(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_25(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_26(ws, gdtinv);
+    __syncthreads();
+}
 __device__ __forceinline__ void solve_0(double* __restrict__ ws, int rhs)
 {
     solve_0_0(ws, rhs);
@@ -164,6 +331,19 @@ __device__ __forceinline__ void solve_0(double* __restrict__ ws, int rhs)
     solve_0_2(ws, rhs);
     solve_0_3(ws, rhs);
     solve_0_4(ws, rhs);
+}
+__device__ __forceinline__ void solve_0_sync(double* __restrict__ ws, int rhs, bool go)
+{
+    if (go) solve_0_0(ws, rhs);
+    __syncthreads();
+    if (go) solve_0_1(ws, rhs);
+    __syncthreads();
+    if (go) solve_0_2(ws, rhs);
+    __syncthreads();
+    if (go) solve_0_3(ws, rhs);
+    __syncthreads();
+    if (go) solve_0_4(ws, rhs);
+    __syncthreads();
 }
 __device__ __forceinline__ void jacdecomp_1(double* __restrict__ ws, double gdtinv)
 {
@@ -195,6 +375,63 @@ __device__ __forceinline__ void jacdecomp_1(double* __restrict__ ws, double gdti
     jacdecomp_1_25(ws, gdtinv);
     jacdecomp_1_26(ws, gdtinv);
 }
+__device__ __forceinline__ void jacdecomp_1_sync(double* __restrict__ ws, double gdtinv, bool go)
+{
+    if (go) jacdecomp_1_0(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_1(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_2(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_3(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_4(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_5(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_6(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_7(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_8(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_9(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_10(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_11(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_12(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_13(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_14(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_15(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_16(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_17(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_18(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_19(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_20(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_21(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_22(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_23(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_24(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_25(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_26(ws, gdtinv);
+    __syncthreads();
+}
 __device__ __forceinline__ void solve_1(double* __restrict__ ws, int rhs)
 {
     solve_1_0(ws, rhs);
@@ -202,6 +439,137 @@ __device__ __forceinline__ void solve_1(double* __restrict__ ws, int rhs)
     solve_1_2(ws, rhs);
     solve_1_3(ws, rhs);
     solve_1_4(ws, rhs);
+}
+__device__ __forceinline__ void solve_1_sync(double* __restrict__ ws, int rhs, bool go)
+{
+    if (go) solve_1_0(ws, rhs);
+    __syncthreads();
+    if (go) solve_1_1(ws, rhs);
+    __syncthreads();
+    if (go) solve_1_2(ws, rhs);
+    __syncthreads();
+    if (go) solve_1_3(ws, rhs);
+    __syncthreads();
+    if (go) solve_1_4(ws, rhs);
+    __syncthreads();
+}
+__device__ __forceinline__ void solve_t_0(double* __restrict__ ws, int rhs)
+{
+    solve_t_0_0(ws, rhs);
+    solve_t_0_1(ws, rhs);
+    solve_t_0_2(ws, rhs);
+    solve_t_0_3(ws, rhs);
+    solve_t_0_4(ws, rhs);
+}
+__device__ __forceinline__ void adj_jtv_0(double* __restrict__ ws, int yoff, int phioff, int outoff)
+{
+    adj_jtv_0_0(ws, yoff, phioff, outoff);
+    adj_jtv_0_1(ws, yoff, phioff, outoff);
+    adj_jtv_0_2(ws, yoff, phioff, outoff);
+    adj_jtv_0_3(ws, yoff, phioff, outoff);
+    adj_jtv_0_4(ws, yoff, phioff, outoff);
+    adj_jtv_0_5(ws, yoff, phioff, outoff);
+    adj_jtv_0_6(ws, yoff, phioff, outoff);
+    adj_jtv_0_7(ws, yoff, phioff, outoff);
+    adj_jtv_0_8(ws, yoff, phioff, outoff);
+    adj_jtv_0_9(ws, yoff, phioff, outoff);
+    adj_jtv_0_10(ws, yoff, phioff, outoff);
+    adj_jtv_0_11(ws, yoff, phioff, outoff);
+    adj_jtv_0_12(ws, yoff, phioff, outoff);
+}
+__device__ __forceinline__ void adj_hess3_0(double* __restrict__ ws)
+{
+    adj_hess3_0_0(ws);
+    adj_hess3_0_1(ws);
+    adj_hess3_0_2(ws);
+    adj_hess3_0_3(ws);
+    adj_hess3_0_4(ws);
+    adj_hess3_0_5(ws);
+    adj_hess3_0_6(ws);
+    adj_hess3_0_7(ws);
+    adj_hess3_0_8(ws);
+    adj_hess3_0_9(ws);
+    adj_hess3_0_10(ws);
+    adj_hess3_0_11(ws);
+    adj_hess3_0_12(ws);
+    adj_hess3_0_13(ws);
+    adj_hess3_0_14(ws);
+    adj_hess3_0_15(ws);
+    adj_hess3_0_16(ws);
+    adj_hess3_0_17(ws);
+    adj_hess3_0_18(ws);
+    adj_hess3_0_19(ws);
+    adj_hess3_0_20(ws);
+    adj_hess3_0_21(ws);
+    adj_hess3_0_22(ws);
+    adj_hess3_0_23(ws);
+    adj_hess3_0_24(ws);
+    adj_hess3_0_25(ws);
+    adj_hess3_0_26(ws);
+    adj_hess3_0_27(ws);
+    adj_hess3_0_28(ws);
+    adj_hess3_0_29(ws);
+    adj_hess3_0_30(ws);
+    adj_hess3_0_31(ws);
+    adj_hess3_0_32(ws);
+}
+__device__ __forceinline__ void solve_t_1(double* __restrict__ ws, int rhs)
+{
+    solve_t_1_0(ws, rhs);
+    solve_t_1_1(ws, rhs);
+    solve_t_1_2(ws, rhs);
+    solve_t_1_3(ws, rhs);
+    solve_t_1_4(ws, rhs);
+}
+__device__ __forceinline__ void adj_jtv_1(double* __restrict__ ws, int yoff, int phioff, int outoff)
+{
+    adj_jtv_1_0(ws, yoff, phioff, outoff);
+    adj_jtv_1_1(ws, yoff, phioff, outoff);
+    adj_jtv_1_2(ws, yoff, phioff, outoff);
+    adj_jtv_1_3(ws, yoff, phioff, outoff);
+    adj_jtv_1_4(ws, yoff, phioff, outoff);
+    adj_jtv_1_5(ws, yoff, phioff, outoff);
+    adj_jtv_1_6(ws, yoff, phioff, outoff);
+    adj_jtv_1_7(ws, yoff, phioff, outoff);
+    adj_jtv_1_8(ws, yoff, phioff, outoff);
+    adj_jtv_1_9(ws, yoff, phioff, outoff);
+    adj_jtv_1_10(ws, yoff, phioff, outoff);
+    adj_jtv_1_11(ws, yoff, phioff, outoff);
+    adj_jtv_1_12(ws, yoff, phioff, outoff);
+}
+__device__ __forceinline__ void adj_hess3_1(double* __restrict__ ws)
+{
+    adj_hess3_1_0(ws);
+    adj_hess3_1_1(ws);
+    adj_hess3_1_2(ws);
+    adj_hess3_1_3(ws);
+    adj_hess3_1_4(ws);
+    adj_hess3_1_5(ws);
+    adj_hess3_1_6(ws);
+    adj_hess3_1_7(ws);
+    adj_hess3_1_8(ws);
+    adj_hess3_1_9(ws);
+    adj_hess3_1_10(ws);
+    adj_hess3_1_11(ws);
+    adj_hess3_1_12(ws);
+    adj_hess3_1_13(ws);
+    adj_hess3_1_14(ws);
+    adj_hess3_1_15(ws);
+    adj_hess3_1_16(ws);
+    adj_hess3_1_17(ws);
+    adj_hess3_1_18(ws);
+    adj_hess3_1_19(ws);
+    adj_hess3_1_20(ws);
+    adj_hess3_1_21(ws);
+    adj_hess3_1_22(ws);
+    adj_hess3_1_23(ws);
+    adj_hess3_1_24(ws);
+    adj_hess3_1_25(ws);
+    adj_hess3_1_26(ws);
+    adj_hess3_1_27(ws);
+    adj_hess3_1_28(ws);
+    adj_hess3_1_29(ws);
+    adj_hess3_1_30(ws);
 }
 struct Traits {
     static constexpr int NSPEC = mech_cracmm2::NSPEC;
@@ -229,6 +597,16 @@ struct Traits {
     static constexpr int EBI_OFF_PROD = mech_cracmm2::EBI_OFF_PROD;
     static constexpr int EBI_OFF_LOSS = mech_cracmm2::EBI_OFF_LOSS;
     static constexpr int EBI_OFF_PNEG = mech_cracmm2::EBI_OFF_PNEG;
+    static constexpr int ADJ_WS_ELEMS = mech_cracmm2::ADJ_WS_ELEMS;
+    static constexpr int ADJ_LAM = mech_cracmm2::ADJ_LAM;
+    static constexpr int ADJ_MU1 = mech_cracmm2::ADJ_MU1;
+    static constexpr int ADJ_MU2 = mech_cracmm2::ADJ_MU2;
+    static constexpr int ADJ_MU3 = mech_cracmm2::ADJ_MU3;
+    static constexpr int ADJ_PHI = mech_cracmm2::ADJ_PHI;
+    static constexpr int ADJ_TMP = mech_cracmm2::ADJ_TMP;
+    static constexpr int ADJ_EMIS = mech_cracmm2::ADJ_EMIS;
+    static constexpr int ADJ_GE = mech_cracmm2::ADJ_GE;
+    static constexpr int ADJ_GK = mech_cracmm2::ADJ_GK;
     static constexpr const char* name() { return mech_cracmm2::NAME; }
     static __device__ __forceinline__ int iold2new(int s) { return mech_cracmm2::c_iold2new[s]; }
     static __device__ __forceinline__ int inew2old(int i) { return mech_cracmm2::c_inew2old[i]; }
@@ -236,10 +614,33 @@ struct Traits {
     static __device__ __forceinline__ void explic_0(double* ws) { mech_cracmm2::explic_0(ws); }
     static __device__ __forceinline__ void jacdecomp_0(double* ws, double g) { mech_cracmm2::jacdecomp_0(ws, g); }
     static __device__ __forceinline__ void solve_0(double* ws, int r) { mech_cracmm2::solve_0(ws, r); }
+    static __device__ __forceinline__ void jacdecomp_0_sync(double* ws, double g, bool go) { mech_cracmm2::jacdecomp_0_sync(ws, g, go); }
+    static __device__ __forceinline__ void solve_0_sync(double* ws, int r, bool go) { mech_cracmm2::solve_0_sync(ws, r, go); }
+    static __device__ __forceinline__ void solve_t_0(double* ws, int r) { mech_cracmm2::solve_t_0(ws, r); }
+    static __device__ __forceinline__ void adj_jtv_0(double* ws, int y, int phi, int out) { mech_cracmm2::adj_jtv_0(ws, y, phi, out); }
+    static __device__ __forceinline__ void adj_hess3_0(double* ws) { mech_cracmm2::adj_hess3_0(ws); }
     static __device__ __forceinline__ void feval_1(double* ws, int s, int t) { mech_cracmm2::feval_1(ws, s, t); }
     static __device__ __forceinline__ void explic_1(double* ws) { mech_cracmm2::explic_1(ws); }
     static __device__ __forceinline__ void jacdecomp_1(double* ws, double g) { mech_cracmm2::jacdecomp_1(ws, g); }
     static __device__ __forceinline__ void solve_1(double* ws, int r) { mech_cracmm2::solve_1(ws, r); }
+    static __device__ __forceinline__ void jacdecomp_1_sync(double* ws, double g, bool go) { mech_cracmm2::jacdecomp_1_sync(ws, g, go); }
+    static __device__ __forceinline__ void solve_1_sync(double* ws, int r, bool go) { mech_cracmm2::solve_1_sync(ws, r, go); }
+    static __device__ __forceinline__ void solve_t_1(double* ws, int r) { mech_cracmm2::solve_t_1(ws, r); }
+    static __device__ __forceinline__ void adj_jtv_1(double* ws, int y, int phi, int out) { mech_cracmm2::adj_jtv_1(ws, y, phi, out); }
+    static __device__ __forceinline__ void adj_hess3_1(double* ws) { mech_cracmm2::adj_hess3_1(ws); }
+    static constexpr int EBI_N_EBISP = mech_cracmm2::EBI_N_EBISP;
+    static constexpr int EBI_NEBITER = mech_cracmm2::EBI_NEBITER;
+    static constexpr int EBI_NPNEG = mech_cracmm2::EBI_NPNEG;
+    static constexpr double EBI_DELTAT = mech_cracmm2::EBI_DELTAT;
+    static __device__ __forceinline__ int ebi_ebisp(int e) { return mech_cracmm2::c_ebi_ebisp[e]; }
+    static __device__ __forceinline__ double ebi_rtol(int i) { return mech_cracmm2::c_ebi_rtol[i]; }
+    static __device__ __forceinline__ int ebi_pneg(int k) { return mech_cracmm2::c_ebi_pneg[k]; }
+    static __device__ __forceinline__ void ebi_hrrates(double* ws) { mech_cracmm2::ebi_hrrates(ws); }
+    static __device__ __forceinline__ void ebi_hrprodloss(double* ws) { mech_cracmm2::ebi_hrprodloss(ws); }
+    static __device__ __forceinline__ void ebi_hrg1(double* ws, double dtc) { mech_cracmm2::ebi_hrg1(ws, dtc); }
+    static __device__ __forceinline__ void ebi_hrg2(double* ws, double dtc) { mech_cracmm2::ebi_hrg2(ws, dtc); }
+    static __device__ __forceinline__ void ebi_hrg3(double* ws, double dtc) { mech_cracmm2::ebi_hrg3(ws, dtc); }
+    static __device__ __forceinline__ void ebi_hrg4(double* ws, double dtc) { mech_cracmm2::ebi_hrg4(ws, dtc); }
     static __device__ __forceinline__ void rconst(double* ws, double t, double p, double h, double sw, int sun,
                                                   const double* rj, const double* het) { mech_cracmm2::rconst(ws, t, p, h, sw, sun, rj, het); }
 };

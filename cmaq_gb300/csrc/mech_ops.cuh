@@ -5,6 +5,8 @@
 #include <stdint.h>
 #include "chem_kernels.cuh"
 #include "queue_kernels.cuh"
+#include "ebi.cuh"
+#include "adjoint.cuh"
 
 struct MechOps {
     const char* name;
@@ -16,9 +18,20 @@ struct MechOps {
     const int* inew2old;      // [nspec]
     const int* iold2new;      // [nspec]
     cudaError_t (*chem_static)(const chem::GridArgs&, int nblocks, cudaStream_t);
-    cudaError_t (*chem_queue)(const chem::GridArgs&, const chem::QueueArgs&, bool lockstep, int nblocks,
+    // sync: 0 free-running warps, 1 barriers between attempt phases, 2 also between chunks;
+    // wpb: warps per block (2, 4 or 8)
+    cudaError_t (*chem_queue)(const chem::GridArgs&, const chem::QueueArgs&, int sync, int wpb, int nblocks,
                               cudaStream_t);
+    cudaError_t (*queue_occupancy)(int sync, int wpb, int* blocks_per_sm);
     cudaError_t (*solve)(const chem::SolveArgs&, int nblocks, cudaStream_t);
+    cudaError_t (*chem_ebi)(const chem::GridArgs&, const chem::QueueArgs&, const chem::EbiArgs&, int nblocks,
+                            cudaStream_t);
+    cudaError_t (*ebi_solve)(const chem::EbiSolveArgs&, int nblocks, cudaStream_t);
+    double ebi_deltat;
+    int adj_ws_elems;
+    cudaError_t (*adj_forward)(const adj::Args&, int nblocks, cudaStream_t);
+    cudaError_t (*adj_reverse)(const adj::Args&, int nblocks, cudaStream_t);
+    cudaError_t (*adj_occupancy)(int* forward_bps, int* reverse_bps);
     cudaError_t (*rconst)(const chem::GridArgs&, double* rki, uint8_t* sunlit, int nblocks, cudaStream_t);
     cudaError_t (*occupancy)(int* blocks_per_sm);
 };
@@ -31,19 +44,76 @@ struct MechOps {
         chem::k_chem_ros3<T_><<<nb, chem::THREADS_PER_BLOCK, 0, s>>>(a);                            \
         return cudaGetLastError();                                                                  \
     }                                                                                               \
-    cudaError_t chem_queue_(const chem::GridArgs& a, const chem::QueueArgs& q, bool lockstep, int nb,   \
+    template <int SY, int W>                                                                        \
+    cudaError_t launch_q_(const chem::GridArgs& a, const chem::QueueArgs& q, int nb, cudaStream_t s)  \
+    {                                                                                               \
+        chem::k_chem_ros3_queue<T_, SY, W><<<nb, W * 32, 0, s>>>(a, q);                             \
+        return cudaGetLastError();                                                                  \
+    }                                                                                               \
+    template <int SY, int W>                                                                        \
+    cudaError_t occ_q_(int* bps)                                                                    \
+    {                                                                                               \
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, chem::k_chem_ros3_queue<T_, SY, W>, \
+                                                             W * 32, 0);                            \
+    }                                                                                               \
+    cudaError_t chem_queue_(const chem::GridArgs& a, const chem::QueueArgs& q, int sync, int wpb, int nb, \
                             cudaStream_t s)                                                         \
     {                                                                                               \
-        if (lockstep)                                                                               \
-            chem::k_chem_ros3_queue<T_, true><<<nb, chem::THREADS_PER_BLOCK, 0, s>>>(a, q);         \
-        else                                                                                        \
-            chem::k_chem_ros3_queue<T_, false><<<nb, chem::THREADS_PER_BLOCK, 0, s>>>(a, q);        \
-        return cudaGetLastError();                                                                  \
+        switch (sync * 16 + wpb) {                                                                  \
+        case 0 * 16 + 8: return launch_q_<0, 8>(a, q, nb, s);                                       \
+        case 1 * 16 + 8: return launch_q_<1, 8>(a, q, nb, s);                                       \
+        case 2 * 16 + 8: return launch_q_<2, 8>(a, q, nb, s);                                       \
+        case 1 * 16 + 4: return launch_q_<1, 4>(a, q, nb, s);                                       \
+        case 2 * 16 + 4: return launch_q_<2, 4>(a, q, nb, s);                                       \
+        case 1 * 16 + 2: return launch_q_<1, 2>(a, q, nb, s);                                       \
+        case 2 * 16 + 2: return launch_q_<2, 2>(a, q, nb, s);                                       \
+        default: return cudaErrorInvalidValue;                                                      \
+        }                                                                                           \
+    }                                                                                               \
+    cudaError_t queue_occupancy_(int sync, int wpb, int* bps)                                       \
+    {                                                                                               \
+        switch (sync * 16 + wpb) {                                                                  \
+        case 0 * 16 + 8: return occ_q_<0, 8>(bps);                                                  \
+        case 1 * 16 + 8: return occ_q_<1, 8>(bps);                                                  \
+        case 2 * 16 + 8: return occ_q_<2, 8>(bps);                                                  \
+        case 1 * 16 + 4: return occ_q_<1, 4>(bps);                                                  \
+        case 2 * 16 + 4: return occ_q_<2, 4>(bps);                                                  \
+        case 1 * 16 + 2: return occ_q_<1, 2>(bps);                                                  \
+        case 2 * 16 + 2: return occ_q_<2, 2>(bps);                                                  \
+        default: return cudaErrorInvalidValue;                                                      \
+        }                                                                                           \
     }                                                                                               \
     cudaError_t solve_(const chem::SolveArgs& a, int nb, cudaStream_t s)                            \
     {                                                                                               \
         chem::k_ros3_solve<T_><<<nb, chem::THREADS_PER_BLOCK, 0, s>>>(a);                           \
         return cudaGetLastError();                                                                  \
+    }                                                                                               \
+    cudaError_t chem_ebi_(const chem::GridArgs& a, const chem::QueueArgs& q, const chem::EbiArgs& e, int nb, \
+                          cudaStream_t s)                                                           \
+    {                                                                                               \
+        chem::k_chem_ebi_queue<T_><<<nb, chem::THREADS_PER_BLOCK, 0, s>>>(a, q, e);                 \
+        return cudaGetLastError();                                                                  \
+    }                                                                                               \
+    cudaError_t ebi_solve_(const chem::EbiSolveArgs& a, int nb, cudaStream_t s)                     \
+    {                                                                                               \
+        chem::k_ebi_solve<T_><<<nb, chem::THREADS_PER_BLOCK, 0, s>>>(a);                            \
+        return cudaGetLastError();                                                                  \
+    }                                                                                               \
+    cudaError_t adj_forward_(const adj::Args& a, int nb, cudaStream_t s)                            \
+    {                                                                                               \
+        adj::k_adj_forward<T_><<<nb, adj::THREADS, 0, s>>>(a);                                      \
+        return cudaGetLastError();                                                                  \
+    }                                                                                               \
+    cudaError_t adj_reverse_(const adj::Args& a, int nb, cudaStream_t s)                            \
+    {                                                                                               \
+        adj::k_adj_reverse<T_><<<nb, adj::THREADS, 0, s>>>(a);                                      \
+        return cudaGetLastError();                                                                  \
+    }                                                                                               \
+    cudaError_t adj_occupancy_(int* f, int* r)                                                      \
+    {                                                                                               \
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(f, adj::k_adj_forward<T_>, adj::THREADS, 0); \
+        if (e != cudaSuccess) return e;                                                             \
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(r, adj::k_adj_reverse<T_>, adj::THREADS, 0); \
     }                                                                                               \
     cudaError_t rconst_(const chem::GridArgs& a, double* rki, uint8_t* sun, int nb, cudaStream_t s) \
     {                                                                                               \
@@ -56,8 +126,7 @@ struct MechOps {
         cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(                              \
             &a, chem::k_chem_ros3<T_>, chem::THREADS_PER_BLOCK, 0);                                 \
         if (e != cudaSuccess) return e;                                                             \
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(                                          \
-            &b, chem::k_chem_ros3_queue<T_, false>, chem::THREADS_PER_BLOCK, 0);                    \
+        e = occ_q_<1, 8>(&b);                                                                       \
         *bps = a < b ? a : b;                                                                       \
         return e;                                                                                   \
     }                                                                                               \
@@ -66,5 +135,6 @@ struct MechOps {
                                    T_::NHETERO, T_::WS_ELEMS, T_::IARRAY_DAY, T_::IARRAY_NIGHT,     \
                                    NS::FLOPS_STEP_DAY, NS::FLOPS_STEP_NIGHT,                        \
                                    NS::h_cgrid_index, NS::h_convert, NS::h_molwt, NS::h_inew2old,   \
-                                   NS::h_iold2new, chem_static_, chem_queue_, solve_, rconst_,      \
-                                   occupancy_};
+                                   NS::h_iold2new, chem_static_, chem_queue_, queue_occupancy_,     \
+                                   solve_, chem_ebi_, ebi_solve_, T_::EBI_DELTAT,            \
+                                   T_::ADJ_WS_ELEMS, adj_forward_, adj_reverse_, adj_occupancy_, rconst_, occupancy_};

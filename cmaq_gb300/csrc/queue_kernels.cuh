@@ -22,13 +22,16 @@ struct QueueArgs {
     unsigned long long* head;         // next queue position (zeroed before the launch)
 };
 
-// LOCKSTEP: the block's warps run each step attempt together, with barriers between its
-// phases (the block leaves the loop only when none of its warps holds a cell).
-template <class M, bool LOCKSTEP>
-__global__ void __launch_bounds__(THREADS_PER_BLOCK, 1) k_chem_ros3_queue(GridArgs a, QueueArgs q)
+// SYNC > 0 ("lock-step"): the block's warps run each step attempt together, with
+// barriers between its phases (SYNC = 1) or also between the generated chunks (SYNC = 2);
+// the block leaves the loop only when none of its warps holds a cell.  WPB = warps per
+// block.
+template <class M, int SYNC, int WPB>
+__global__ void __launch_bounds__(WPB * 32, 8 / WPB) k_chem_ros3_queue(GridArgs a, QueueArgs q)
 {
+    constexpr bool LOCKSTEP = SYNC > 0;
     const int lane = threadIdx.x & 31;
-    const long long warp = (long long)blockIdx.x * WARPS_PER_BLOCK + (threadIdx.x >> 5);
+    const long long warp = (long long)blockIdx.x * WPB + (threadIdx.x >> 5);
     double* ws = warp_ws<M>(a.ws, warp);
     ros3::CellState s;
     long long cell = -1;
@@ -64,7 +67,7 @@ __global__ void __launch_bounds__(THREADS_PER_BLOCK, 1) k_chem_ros3_queue(GridAr
             if (!__any_sync(0xffffffffu, busy)) break;
             night = __all_sync(0xffffffffu, !busy || !sun) && a.use_night;
         }
-        ros3::attempt_phased<M, LOCKSTEP>(ws, s, a.chemstep, a.tol, night, a.max_iter, busy);
+        ros3::attempt_phased<M, SYNC>(ws, s, a.chemstep, a.tol, night, a.max_iter, busy);
         if (busy) {
             if (ros3::finished(s, a.chemstep)) {
                 scatter_cell<M>(a, cell, ws);

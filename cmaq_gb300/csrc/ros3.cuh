@@ -74,15 +74,38 @@ __device__ __forceinline__ bool finished(const CellState& s, double chemstep)
     return !(s.tnow < chemstep) || s.st.status != ST_OK;
 }
 
+// f += E (emission tendency of the cell, ppm/min)
+template <class M>
+__device__ __forceinline__ void add_emis(double* __restrict__ ws, int off)
+{
+    for (int n = 0; n < M::ISCHAN; ++n) ws[(off + n) * 32] = ws[(off + n) * 32] + ws[(M::ADJ_EMIS + n) * 32];
+}
+
+// One linear solve of a stage; SYNC as in attempt_phased.
+template <class M, int SYNC>
+__device__ __forceinline__ void solve_phase(double* __restrict__ ws, int rhs, bool night, bool go)
+{
+    if (SYNC == 2) {
+        if (night) M::solve_1_sync(ws, rhs, go); else M::solve_0_sync(ws, rhs, go);
+    } else {
+        if (go) {
+            if (night) M::solve_1(ws, rhs); else M::solve_0(ws, rhs);
+        }
+        if (SYNC) __syncthreads();
+    }
+}
+
 // One pass of the DO WHILE body of rbsolver.F:344-589 for one cell: stages, error
 // estimate, accept or reject, new step size.  Requires Y and RKI in ws.  `night` must be
 // warp-uniform: it selects the night reaction list and LU pattern, which give the same
 // numbers as the day pattern for a dark cell (the dropped reactions have zero rates)
-// with fewer operations.  Every thread of the warp (of the block when SYNC) calls this;
-// lanes with active == false do no work.  With SYNC the block's warps pass a barrier
-// between phases, so they walk the (large) generated code together and share the
-// instruction cache.
-template <class M, bool SYNC>
+// with fewer operations.  Every thread of the warp (of the block when SYNC > 0) calls
+// this; lanes with active == false do no work.  SYNC = 1: the block's warps pass a
+// barrier between phases; SYNC = 2: also after every generated chunk of the LU and the
+// solves.  Walking the (large) generated code together lets the warps share the
+// instruction cache.  EMIS: f(y) + E with the emission tendency E at ws[ADJ_EMIS] (only
+// the adjoint kernels, whose workspaces hold the adjoint arrays, set it).
+template <class M, int SYNC, bool EMIS = false>
 __device__ void attempt_phased(double* __restrict__ ws, CellState& s, double chemstep, Tol tol, bool night,
                                int max_iter, bool active)
 {
@@ -94,6 +117,7 @@ __device__ void attempt_phased(double* __restrict__ ws, CellState& s, double che
         // f(Y) is unchanged after a rejected step; it is kept in F0
         if (!s.have_f0) {
             if (night) M::feval_1(ws, M::OFF_Y, M::OFF_F0); else M::feval_0(ws, M::OFF_Y, M::OFF_F0);
+            if (EMIS) add_emis<M>(ws, M::OFF_F0);
             s.have_f0 = true;
         }
         dt = s.dt;
@@ -104,28 +128,29 @@ __device__ void attempt_phased(double* __restrict__ ws, CellState& s, double che
         if (night) M::explic_1(ws); else M::explic_0(ws);
     }
     if (SYNC) __syncthreads();
-    if (go) {
-        if (night) M::jacdecomp_1(ws, gdtinv); else M::jacdecomp_0(ws, gdtinv);
+    if (SYNC == 2) {
+        if (night) M::jacdecomp_1_sync(ws, gdtinv, go); else M::jacdecomp_0_sync(ws, gdtinv, go);
+    } else {
+        if (go) {
+            if (night) M::jacdecomp_1(ws, gdtinv); else M::jacdecomp_0(ws, gdtinv);
+        }
+        if (SYNC) __syncthreads();
     }
-    if (SYNC) __syncthreads();
     if (go) {   // stage 1
         for (int n = 0; n < M::NSPEC; ++n) ws[(M::OFF_K1 + n) * 32] = -ws[(M::OFF_F0 + n) * 32];
-        if (night) M::solve_1(ws, M::OFF_K1); else M::solve_0(ws, M::OFF_K1);
     }
-    if (SYNC) __syncthreads();
+    solve_phase<M, SYNC>(ws, M::OFF_K1, night, go);
     if (go) {   // stage 2
         for (int n = 0; n < M::NSPEC; ++n)
             ws[(M::OFF_YP + n) * 32] = ws[(M::OFF_Y + n) * 32] + ws[(M::OFF_K1 + n) * 32];
         if (night) M::feval_1(ws, M::OFF_YP, M::OFF_YDOT); else M::feval_0(ws, M::OFF_YP, M::OFF_YDOT);
+        if (EMIS) add_emis<M>(ws, M::OFF_YDOT);
         const double x1 = C21 * dtinv;
         for (int n = 0; n < M::NSPEC; ++n)
             ws[(M::OFF_K2 + n) * 32] = fma(-x1, ws[(M::OFF_K1 + n) * 32], -ws[(M::OFF_YDOT + n) * 32]);
     }
     if (SYNC) __syncthreads();
-    if (go) {
-        if (night) M::solve_1(ws, M::OFF_K2); else M::solve_0(ws, M::OFF_K2);
-    }
-    if (SYNC) __syncthreads();
+    solve_phase<M, SYNC>(ws, M::OFF_K2, night, go);
     if (go) {   // stage 3
         const double x1 = C31 * dtinv;
         const double x2 = C32 * dtinv;
@@ -133,9 +158,8 @@ __device__ void attempt_phased(double* __restrict__ ws, CellState& s, double che
             const double t = fma(-x1, ws[(M::OFF_K1 + n) * 32], -ws[(M::OFF_YDOT + n) * 32]);
             ws[(M::OFF_K3 + n) * 32] = fma(-x2, ws[(M::OFF_K2 + n) * 32], t);
         }
-        if (night) M::solve_1(ws, M::OFF_K3); else M::solve_0(ws, M::OFF_K3);
     }
-    if (SYNC) __syncthreads();
+    solve_phase<M, SYNC>(ws, M::OFF_K3, night, go);
     if (!go) return;
     // solution and error estimate
     double err = 0.0;
@@ -181,7 +205,7 @@ template <class M>
 __device__ __forceinline__ void attempt(double* __restrict__ ws, CellState& s, double chemstep, Tol tol,
                                         bool night, int max_iter)
 {
-    attempt_phased<M, false>(ws, s, chemstep, tol, night, max_iter, true);
+    attempt_phased<M, 0>(ws, s, chemstep, tol, night, max_iter, true);
 }
 
 // Integrate the cell in ws over chemstep minutes (the whole DO WHILE loop).

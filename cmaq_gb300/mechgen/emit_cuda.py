@@ -55,6 +55,18 @@ class Layout:
         self.vdiag = off; off += sp.ischan
         off = max(off, self.ebi_yc + 6 * ns)
         self.total = off
+        # discrete-adjoint arrays behind the forward workspace; only the adjoint kernels,
+        # whose per-warp stride is ADJ_WS_ELEMS, use them
+        self.adj_lam = off; off += ns       # adjoint of Y
+        self.adj_mu1 = off; off += ns       # adjoints of the stages K1..K3, solved in place
+        self.adj_mu2 = off; off += ns
+        self.adj_mu3 = off; off += ns
+        self.adj_phi = off; off += ns       # adjoint of an f evaluation
+        self.adj_tmp = off; off += ns
+        self.adj_emis = off; off += ns      # emission tendency added to f
+        self.adj_ge = off; off += ns        # gradient wrt the emission tendency
+        self.adj_gk = off; off += nr        # gradient wrt log rate multipliers
+        self.adj_total = off
 
 
 def _w(k: int) -> str:
@@ -91,6 +103,11 @@ def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src
         wrappers.append("{")
         wrappers.extend(f"    jacdecomp_{d}_{ci}(ws, gdtinv);" for ci in range(len(chunks)))
         wrappers.append("}")
+        # block-synchronous form: every thread calls it, `go` lanes work, barrier after each chunk
+        wrappers.append(f"__device__ __forceinline__ void jacdecomp_{d}_sync(double* __restrict__ ws, double gdtinv, bool go)")
+        wrappers.append("{")
+        wrappers.extend(f"    if (go) jacdecomp_{d}_{ci}(ws, gdtinv);\n    __syncthreads();" for ci in range(len(chunks)))
+        wrappers.append("}")
         schunks = _solve_chunks(sp, lay, d)
         for ci, code in enumerate(schunks):
             unit = f"solve{d}"
@@ -100,6 +117,32 @@ def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src
         wrappers.append("{")
         wrappers.extend(f"    solve_{d}_{ci}(ws, rhs);" for ci in range(len(schunks)))
         wrappers.append("}")
+        wrappers.append(f"__device__ __forceinline__ void solve_{d}_sync(double* __restrict__ ws, int rhs, bool go)")
+        wrappers.append("{")
+        wrappers.extend(f"    if (go) solve_{d}_{ci}(ws, rhs);\n    __syncthreads();" for ci in range(len(schunks)))
+        wrappers.append("}")
+
+    for d in range(2):
+        tchunks = _solve_t_chunks(sp, lay, d)
+        for ci, code in enumerate(tchunks):
+            units.setdefault(f"solvet{d}", []).extend(code)
+            decls.append(f"__device__ void solve_t_{d}_{ci}(double* __restrict__ ws, int rhs);")
+        wrappers.append(f"__device__ __forceinline__ void solve_t_{d}(double* __restrict__ ws, int rhs)")
+        wrappers.append("{")
+        wrappers.extend(f"    solve_t_{d}_{ci}(ws, rhs);" for ci in range(len(tchunks)))
+        wrappers.append("}")
+        # reaction-wise adjoint routines in bounded chunks, spread over translation units
+        for kind, chunks, sig, call in (
+                ("jtv", _adj_jtv(m, sp, lay, d), "double* __restrict__ ws, int yoff, int phioff, int outoff",
+                 "ws, yoff, phioff, outoff"),
+                ("hess3", _adj_hess3(m, sp, lay, d), "double* __restrict__ ws", "ws")):
+            for ci, code in enumerate(chunks):
+                units.setdefault(f"adj{d}_{kind}{ci // 4}", []).extend(code)
+                decls.append(f"__device__ void adj_{kind}_{d}_{ci}({sig});")
+            wrappers.append(f"__device__ __forceinline__ void adj_{kind}_{d}({sig})")
+            wrappers.append("{")
+            wrappers.extend(f"    adj_{kind}_{d}_{ci}({call});" for ci in range(len(chunks)))
+            wrappers.append("}")
 
     h = banner + ["#pragma once", "#include <cuda_runtime.h>", "#ifndef CHEM_HD", "#define CHEM_HD __device__",
                   "#endif",
@@ -114,7 +157,11 @@ def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src
               # EBI cell state reuses the workspace: YC, YC0, YCP, PROD, LOSS, PNEG after RKI/RXRAT
               ("EBI_OFF_YC", lay.ebi_yc), ("EBI_OFF_YC0", lay.ebi_yc + ns), ("EBI_OFF_YCP", lay.ebi_yc + 2 * ns),
               ("EBI_OFF_PROD", lay.ebi_yc + 3 * ns), ("EBI_OFF_LOSS", lay.ebi_yc + 4 * ns),
-              ("EBI_OFF_PNEG", lay.ebi_yc + 5 * ns))
+              ("EBI_OFF_PNEG", lay.ebi_yc + 5 * ns),
+              ("ADJ_WS_ELEMS", lay.adj_total), ("ADJ_LAM", lay.adj_lam), ("ADJ_MU1", lay.adj_mu1),
+              ("ADJ_MU2", lay.adj_mu2), ("ADJ_MU3", lay.adj_mu3), ("ADJ_PHI", lay.adj_phi),
+              ("ADJ_TMP", lay.adj_tmp), ("ADJ_EMIS", lay.adj_emis), ("ADJ_GE", lay.adj_ge),
+              ("ADJ_GK", lay.adj_gk))
     for k, v in consts:
         h.append(f"constexpr int {k} = {v};")
     h.append(f"constexpr double FLOPS_STEP_DAY = {float(flop_counts(m, sp, 0)['step_total'])};")
@@ -141,6 +188,23 @@ def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src
         h.append(f"    static __device__ __forceinline__ void explic_{d}(double* ws) {{ {ns_name}::explic_{d}(ws); }}")
         h.append(f"    static __device__ __forceinline__ void jacdecomp_{d}(double* ws, double g) {{ {ns_name}::jacdecomp_{d}(ws, g); }}")
         h.append(f"    static __device__ __forceinline__ void solve_{d}(double* ws, int r) {{ {ns_name}::solve_{d}(ws, r); }}")
+        h.append(f"    static __device__ __forceinline__ void jacdecomp_{d}_sync(double* ws, double g, bool go) {{ {ns_name}::jacdecomp_{d}_sync(ws, g, go); }}")
+        h.append(f"    static __device__ __forceinline__ void solve_{d}_sync(double* ws, int r, bool go) {{ {ns_name}::solve_{d}_sync(ws, r, go); }}")
+        h.append(f"    static __device__ __forceinline__ void solve_t_{d}(double* ws, int r) {{ {ns_name}::solve_t_{d}(ws, r); }}")
+        h.append(f"    static __device__ __forceinline__ void adj_jtv_{d}(double* ws, int y, int phi, int out) {{ {ns_name}::adj_jtv_{d}(ws, y, phi, out); }}")
+        h.append(f"    static __device__ __forceinline__ void adj_hess3_{d}(double* ws) {{ {ns_name}::adj_hess3_{d}(ws); }}")
+    if ebi_decl:
+        h.append(f"    static constexpr int EBI_N_EBISP = {ns_name}::EBI_N_EBISP;")
+        h.append(f"    static constexpr int EBI_NEBITER = {ns_name}::EBI_NEBITER;")
+        h.append(f"    static constexpr int EBI_NPNEG = {ns_name}::EBI_NPNEG;")
+        h.append(f"    static constexpr double EBI_DELTAT = {ns_name}::EBI_DELTAT;")
+        h.append(f"    static __device__ __forceinline__ int ebi_ebisp(int e) {{ return {ns_name}::c_ebi_ebisp[e]; }}")
+        h.append(f"    static __device__ __forceinline__ double ebi_rtol(int i) {{ return {ns_name}::c_ebi_rtol[i]; }}")
+        h.append(f"    static __device__ __forceinline__ int ebi_pneg(int k) {{ return {ns_name}::c_ebi_pneg[k]; }}")
+        for nm in ("hrrates", "hrprodloss"):
+            h.append(f"    static __device__ __forceinline__ void ebi_{nm}(double* ws) {{ {ns_name}::ebi_{nm}(ws); }}")
+        for nm in ("hrg1", "hrg2", "hrg3", "hrg4"):
+            h.append(f"    static __device__ __forceinline__ void ebi_{nm}(double* ws, double dtc) {{ {ns_name}::ebi_{nm}(ws, dtc); }}")
     h.append("    static __device__ __forceinline__ void rconst(double* ws, double t, double p, double h, double sw, int sun,")
     h.append(f"                                                  const double* rj, const double* het) {{ {ns_name}::rconst(ws, t, p, h, sw, sun, rj, het); }}")
     h.append("};")
@@ -370,3 +434,184 @@ def _solve_chunks(sp: SparseMech, lay: Layout, d: int) -> list[list[str]]:
         f.append("}")
         out.append(f)
     return out
+
+
+def _solve_t_chunks(sp: SparseMech, lay: Layout, d: int) -> list[list[str]]:
+    """Transposed solve A^T x = b in place at ws[rhs] with the LU factors of A = L U that
+    jacdecomp_d leaves (unit L, U with 1/U(i,i) in VDIAG): U^T z = b by ascending rows,
+    then L^T x = z by descending rows.  Each row gathers the column of U (or L) below
+    (above) its diagonal in ascending column order; the discrete adjoint of the stage
+    solves needs these."""
+    n = sp.ischan
+    col_u = {i: [] for i in range(n)}
+    col_l = {i: [] for i in range(n)}
+    for k in range(n):
+        for (st, j) in sp.upper[d][k]:
+            col_u[j].append((st, k))
+        for (st, j) in sp.lower[d][k]:
+            col_l[j].append((st, k))
+    pieces = []
+    for i in range(n):
+        o = ["    {", f"      double x = b[{i * 32}];"]
+        for (st, k) in sorted(col_u[i], key=lambda t: t[1]):
+            o.append(f"      x = fma(-CHEM_LDLU(lu + {st * 32}), b[{k * 32}], x);")
+        o.append(f"      b[{i * 32}] = x * CHEM_LDLU(vd + {i * 32});")
+        o.append("    }")
+        pieces.append((len(col_u[i]) + 1, o))
+    for i in range(n - 1, -1, -1):
+        if not col_l[i]:
+            continue
+        o = ["    {", f"      double x = b[{i * 32}];"]
+        for (st, k) in sorted(col_l[i], key=lambda t: t[1]):
+            o.append(f"      x = fma(-CHEM_LDLU(lu + {st * 32}), b[{k * 32}], x);")
+        o.append(f"      b[{i * 32}] = x;")
+        o.append("    }")
+        pieces.append((len(col_l[i]) + 1, o))
+    chunks, cur, cost = [], [], 0
+    for c, code in pieces:
+        if cur and cost + c > SOLVE_CHUNK_TERMS:
+            chunks.append(cur); cur, cost = [], 0
+        cur.append(code); cost += c
+    if cur:
+        chunks.append(cur)
+    out = []
+    for ci, ch in enumerate(chunks):
+        f = [f"__device__ __noinline__ void solve_t_{d}_{ci}(double* __restrict__ ws, int rhs)", "{",
+             f"    const double* __restrict__ lu = ws + {lay.lu * 32};",
+             f"    const double* __restrict__ vd = ws + {lay.vdiag * 32};",
+             "    double* __restrict__ b = ws + rhs * 32;",
+             "    (void)vd;"]
+        for code in ch:
+            f.extend(code)
+        f.append("}")
+        out.append(f)
+    return out
+
+
+def _stoich_sum(m: Mechanism, sp: SparseMech, r: int, vec: str, name: str) -> list[str]:
+    """``name`` = sum over reaction r's net stoichiometry of vec[]: products (SC-weighted,
+    in product order), then minus each reactant."""
+    o, first = [], True
+    for p in range(m.nprdct[r]):
+        sp_idx = sp.irm2[r][3 + p]
+        term = f"{vec}[{sp_idx * 32}]"
+        if first:
+            o.append(f"double {name} = {c_double(m.sc[r][p])} * {term};")
+            first = False
+        else:
+            o.append(f"{name} = fma({c_double(m.sc[r][p])}, {term}, {name});")
+    for i in range(m.nreact[r]):
+        term = f"{vec}[{sp.irm2[r][i] * 32}]"
+        if first:
+            o.append(f"double {name} = -{term};")
+            first = False
+        else:
+            o.append(f"{name} = {name} - {term};")
+    if first:
+        o.append(f"double {name} = 0.0;")
+    return o
+
+
+ADJ_CHUNK_LINES = 500    # generated lines per reaction-wise adjoint function; bounds ptxas time
+
+
+def _chunk_reactions(head: list[str], blocks: list[list[str]], name: str) -> list[list[str]]:
+    """Wrap per-reaction code blocks into __noinline__ functions of bounded size."""
+    out, cur, n = [], [], 0
+    for b in blocks:
+        if cur and n + len(b) > ADJ_CHUNK_LINES:
+            out.append(cur); cur, n = [], 0
+        cur.append(b); n += len(b)
+    if cur or not out:
+        out.append(cur)
+    funcs = []
+    for ci, ch in enumerate(out):
+        f = [head[0].format(name=f"{name}_{ci}"), "{"] + head[1:]
+        for b in ch:
+            f.extend(b)
+        f.append("}")
+        funcs.append(f)
+    return funcs
+
+
+def _adj_jtv(m: Mechanism, sp: SparseMech, lay: Layout, d: int) -> list[list[str]]:
+    """out += J(y)^T phi over the active reactions, and ADJ_GK[r] += w_r * R_r(y), the
+    derivative of phi . f(y) with respect to log k_r; w_r is phi contracted with the
+    reaction's net stoichiometry and R_r its rate.  Returned as chunk functions
+    adj_jtv_d_c, called in order."""
+    head = ["__device__ __noinline__ void {name}(double* __restrict__ ws, int yoff, int phioff, int outoff)",
+            "    const double* __restrict__ y = ws + yoff * 32;",
+            "    const double* __restrict__ phi = ws + phioff * 32;",
+            "    double* __restrict__ out = ws + outoff * 32;"]
+    blocks = []
+    for r in sp.active[d]:
+        nre = m.nreact[r]
+        if nre == 0 and m.nprdct[r] == 0:
+            continue
+        gk = _w(lay.adj_gk + r)
+        o = ["    {"]
+        o.extend("      " + t for t in _stoich_sum(m, sp, r, "phi", "w"))
+        o.append(f"      const double kw = {_w(lay.rki + r)} * w;")
+        a = [sp.irm2[r][i] * 32 for i in range(nre)]
+        if nre == 0:
+            o.append(f"      {gk} = {gk} + kw;")
+        elif nre == 1:
+            o.append(f"      out[{a[0]}] = out[{a[0]}] + kw;")
+            o.append(f"      {gk} = fma(kw, y[{a[0]}], {gk});")
+        elif nre == 2:
+            o.append(f"      out[{a[0]}] = fma(kw, y[{a[1]}], out[{a[0]}]);")
+            o.append(f"      out[{a[1]}] = fma(kw, y[{a[0]}], out[{a[1]}]);")
+            o.append(f"      {gk} = fma(kw * y[{a[0]}], y[{a[1]}], {gk});")
+        else:
+            o.append(f"      out[{a[0]}] = fma(kw * y[{a[1]}], y[{a[2]}], out[{a[0]}]);")
+            o.append(f"      out[{a[1]}] = fma(kw * y[{a[0]}], y[{a[2]}], out[{a[1]}]);")
+            o.append(f"      out[{a[2]}] = fma(kw * y[{a[0]}], y[{a[1]}], out[{a[2]}]);")
+            o.append(f"      {gk} = fma((kw * y[{a[0]}]) * y[{a[1]}], y[{a[2]}], {gk});")
+        o.append("    }")
+        blocks.append(o)
+    return _chunk_reactions(head, blocks, f"adj_jtv_{d}")
+
+
+def _adj_hess3(m: Mechanism, sp: SparseMech, lay: Layout, d: int) -> list[list[str]]:
+    """Second-order terms of the stage solves' adjoint: with nu_i the solved stage
+    adjoints (ADJ_MU1..3) and K_i the stages, ADJ_LAM -= sum_i d/dy (nu_i . J(y) K_i)
+    and ADJ_GK[r] -= sum_i d/d log k_r (nu_i . J(y) K_i), y = Y.  Per reaction the
+    three contractions share WK_s = sum_i w_i K_i[s] over its reactant slots s.  Returned
+    as chunk functions adj_hess3_d_c, called in order."""
+    head = ["__device__ __noinline__ void {name}(double* __restrict__ ws)",
+            f"    const double* __restrict__ y = ws + {lay.y * 32};",
+            f"    double* __restrict__ lam = ws + {lay.adj_lam * 32};"]
+    vecs = [("n1", lay.adj_mu1, "k1", lay.k1), ("n2", lay.adj_mu2, "k2", lay.k2), ("n3", lay.adj_mu3, "k3", lay.k3)]
+    for nv, off_n, kv, off_k in vecs:
+        head.append(f"    const double* __restrict__ {nv} = ws + {off_n * 32};")
+        head.append(f"    const double* __restrict__ {kv} = ws + {off_k * 32};")
+    blocks = []
+    for r in sp.active[d]:
+        nre = m.nreact[r]
+        if nre == 0:
+            continue
+        gk = _w(lay.adj_gk + r)
+        a = [sp.irm2[r][i] * 32 for i in range(nre)]
+        o = ["    {"]
+        for i, (nv, _, _, _) in enumerate(vecs):
+            o.extend("      " + t for t in _stoich_sum(m, sp, r, nv, f"w{i + 1}"))
+        for j in range(nre):
+            o.append(f"      double wk{j} = w1 * k1[{a[j]}];")
+            o.append(f"      wk{j} = fma(w2, k2[{a[j]}], wk{j});")
+            o.append(f"      wk{j} = fma(w3, k3[{a[j]}], wk{j});")
+        o.append(f"      const double kk = {_w(lay.rki + r)};")
+        if nre == 1:
+            o.append(f"      {gk} = fma(-kk, wk0, {gk});")
+        elif nre == 2:
+            o.append(f"      {gk} = fma(-kk, fma(y[{a[1]}], wk0, y[{a[0]}] * wk1), {gk});")
+            o.append(f"      lam[{a[0]}] = fma(-kk, wk1, lam[{a[0]}]);")
+            o.append(f"      lam[{a[1]}] = fma(-kk, wk0, lam[{a[1]}]);")
+        else:
+            o.append(f"      {gk} = fma(-kk, fma(y[{a[1]}] * y[{a[2]}], wk0, "
+                     f"fma(y[{a[0]}] * y[{a[2]}], wk1, (y[{a[0]}] * y[{a[1]}]) * wk2)), {gk});")
+            o.append(f"      lam[{a[0]}] = fma(-kk, fma(y[{a[2]}], wk1, y[{a[1]}] * wk2), lam[{a[0]}]);")
+            o.append(f"      lam[{a[1]}] = fma(-kk, fma(y[{a[2]}], wk0, y[{a[0]}] * wk2), lam[{a[1]}]);")
+            o.append(f"      lam[{a[2]}] = fma(-kk, fma(y[{a[1]}], wk0, y[{a[0]}] * wk1), lam[{a[2]}]);")
+        o.append("    }")
+        blocks.append(o)
+    return _chunk_reactions(head, blocks, f"adj_hess3_{d}")

@@ -63,9 +63,11 @@ typedef struct {
     int nspcsd;                /* number of CGRID species (CGRID_SPCS) */
     const int* cgrid_index;    /* [nspec] CGRID slot (1-based, as CGRID_INDEX) or NULL for the mechanism's table */
     int device;                /* CUDA device ordinal */
-    int max_iter;              /* cap on ROS3 step attempts per cell and call (<= 0: 100000) */
+    int max_iter;              /* cap per cell and call on ROS3 step attempts or EBI iterations (<= 0: 100000) */
 } cmaqchem_cfg;
 
+/* With CMAQCHEM_SOLVER_EBI, accepted_steps counts Backward-Euler iterations and
+ * rejected_steps / sunlit_attempts stay 0. */
 typedef struct {
     long long accepted_steps;  /* summed over cells */
     long long rejected_steps;
@@ -112,6 +114,41 @@ int cmaqchem_cell_stats(cmaqchem_handle* h, int* status, int* attempts);
 int cmaqchem_ros3_solve_device(cmaqchem_handle* h, long long ncell, double* y, const double* rki,
                                const unsigned char* night, double chemstep_min, int* status,
                                int* nsteps, int* nfails, void* stream);
+
+/* Solver-level entry replacing HRSOLVER (CCTM/src/gas/ebi_<mech>/hrsolver.F:26) for cells
+ * with given rate constants, device arrays: yc[nspec][ncell] in the mechanism's species
+ * order (ppm), updated in place; rki[nrxns][ncell].  tstep_sec is the synchronisation
+ * step in seconds, split into EBI steps as hrdriver.F:296-308 does.  Per-cell status
+ * (CMAQCHEM_CELL_* bits) and Backward-Euler iteration counts may be NULL. */
+int cmaqchem_ebi_solve_device(cmaqchem_handle* h, long long ncell, double* yc, const double* rki,
+                              int tstep_sec, int* status, int* iterations, void* stream);
+
+/* Discrete adjoint of RBSOLVER (no reference counterpart; the reference's gradient
+ * tool is the forward DDM-3D of CCTM/src/ddm3d/DDM3D_CHEM.F).  Solver-level, device
+ * arrays, species in the solver's order as for cmaqchem_ros3_solve_device.
+ *
+ * cmaqchem_adj_forward integrates nsync synchronisation steps of chemstep_min minutes
+ * with rate constants rki[nrxns][ncell] (step k uses rki + k * rki_sync_stride; stride
+ * 0 for constant rates) times kmult[nrxns] (NULL: 1) and the emission tendency
+ * emis[ischan][ncell] ppm/min added to f (NULL: 0).  y[ischan][ncell] is advanced in
+ * place; the state at the start of step k goes to checkpoints[k][ischan][ncell] and its
+ * accepted steps per cell to nsteps[k][ncell].  Returns the number of failed cell-steps.
+ *
+ * cmaqchem_adj_backward takes lambda = dL/dy at the end of the window and returns in
+ * it dL/dy at the start; it adds dL/d log kmult to grad_logk[nrxns] and dL/demis to
+ * grad_emis[ischan][ncell] (may be NULL).  The other arguments must be those of the
+ * forward call, whose checkpoints and step counts it reads; the accepted step sizes
+ * are held fixed (the discrete adjoint of the steps the forward pass took).  Needs
+ * device memory for the steps of one synchronisation step: sum(nsteps[k]) * (ischan
+ * + 1) doubles. */
+int cmaqchem_adj_forward(cmaqchem_handle* h, long long ncell, double* y, const double* rki,
+                         long long rki_sync_stride, const unsigned char* night, const double* kmult,
+                         const double* emis, int nsync, double chemstep_min, double* checkpoints,
+                         int* nsteps, void* stream);
+int cmaqchem_adj_backward(cmaqchem_handle* h, long long ncell, double* lambda, const double* rki,
+                          long long rki_sync_stride, const unsigned char* night, const double* kmult,
+                          const double* emis, int nsync, double chemstep_min, const double* checkpoints,
+                          const int* nsteps, double* grad_logk, double* grad_emis, void* stream);
 
 /* Rate constants only (CALC_RCONST, RXNS_FUNC_MODULE.F90) for the handle's grid, device
  * arrays: rki[nrxns][ncell], sunlit[ncell]. */

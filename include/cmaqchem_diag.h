@@ -14,9 +14,10 @@ extern "C" {
 int cmaqchem_diag_fp64_peak(int device, double* tflops, double* ms);
 
 /* Scheduling knobs of a handle, for the autotuner: "night_pattern" (1: warps whose cells are
- * all dark use the smaller night LU pattern; 0: the day pattern always, same numbers) and
- * "lockstep" (1: the work-queue kernel runs each block's warps through a step attempt
- * together, with barriers between its phases). */
+ * all dark use the smaller night LU pattern; 0: the day pattern always, same numbers),
+ * "lockstep" (work-queue kernel: 0 free-running warps, 1 (default) the block's warps run
+ * each step attempt together with barriers between its phases, 2 also between the
+ * generated chunks) and "block_warps" (2, 4 or 8 warps per block; 8 by default). */
 struct cmaqchem_handle;
 int cmaqchem_diag_set_tuning(struct cmaqchem_handle* h, const char* key, int value);
 

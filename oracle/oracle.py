@@ -55,6 +55,12 @@ def load(mech: str = "cb6r5_ae7_aq") -> C.CDLL:
     lib.oracle_mech_name.restype = C.c_char_p
     lib.oracle_chem_ebi.argtypes = [C.POINTER(OracleChemArgs)]
     lib.oracle_ebi_solve_cells.argtypes = [C.c_long, C.c_int, dp, dp, ip, C.POINTER(C.c_long), C.c_int]
+    lib.oracle_adj_forward.argtypes = [C.c_long, dp, dp, C.c_long, u8p, dp, dp, C.c_int, C.c_double, C.c_double,
+                                       C.c_double, dp, ip, dp, C.c_int, C.c_int]
+    lib.oracle_adj_backward.argtypes = [C.c_long, dp, dp, C.c_long, u8p, dp, dp, C.c_int, C.c_double, C.c_double,
+                                        C.c_double, dp, ip, dp, dp, C.c_int]
+    lib.oracle_adj_replay.argtypes = [C.c_long, dp, dp, C.c_long, u8p, dp, dp, C.c_int, ip, dp, C.c_int, C.c_int]
+    lib.oracle_adj_replay.restype = None
     lib.oracle_set_dtmin.argtypes = [C.c_double]
     lib.oracle_get_dtmin.restype = C.c_double
     return lib
@@ -177,3 +183,66 @@ class Oracle:
         import json
         man = json.loads((HERE.parent / "cmaq_gb300" / "mechs" / mech / "manifest.json").read_text())
         return np.array([1 if s["convert"] else 0 for s in man["species"]], np.int32)
+
+
+def _opt(a, ct):
+    return None if a is None else _p(a, ct)
+
+
+class AdjointWindow:
+    """Discrete adjoint of per-cell ROS3 over ``nsync`` synchronisation steps (oracle side).
+
+    y0 [nspec, n] (solver order), rki [nrxns, n] or [nsync, nrxns, n], night [n],
+    kmult [nrxns] or None, emis [nspec, n] or None."""
+
+    def __init__(self, oracle: "Oracle", rki, night, nsync: int, chemstep: float, rtol: float, atol: float,
+                 kmult=None, emis=None, hcap: int = 4096, threads: int = 0):
+        self.o, self.nsync, self.chemstep, self.rtol, self.atol = oracle, nsync, chemstep, rtol, atol
+        self.rki = np.ascontiguousarray(rki, np.float64)
+        self.stride = 0 if self.rki.ndim == 2 else self.rki.shape[1] * self.rki.shape[2]
+        self.night = np.ascontiguousarray(night, np.uint8)
+        self.n = self.night.shape[0]
+        self.kmult = None if kmult is None else np.ascontiguousarray(kmult, np.float64)
+        self.emis = None if emis is None else np.ascontiguousarray(emis, np.float64)
+        self.hcap, self.threads = hcap, threads
+
+    def forward(self, y0):
+        o, n = self.o, self.n
+        y = np.array(y0, np.float64, order="C", copy=True)
+        self.ck = np.zeros((self.nsync, o.nspec, n))
+        self.nsteps = np.zeros((self.nsync, n), np.int32)
+        self.hs = np.zeros((self.nsync, n, self.hcap))
+        bad = o.lib.oracle_adj_forward(n, _p(y, C.c_double), _p(self.rki, C.c_double), self.stride,
+                                       _p(self.night, C.c_uint8), _opt(self.kmult, C.c_double),
+                                       _opt(self.emis, C.c_double), self.nsync, self.chemstep, self.rtol,
+                                       self.atol, _p(self.ck, C.c_double), _p(self.nsteps, C.c_int),
+                                       _p(self.hs, C.c_double), self.hcap, self.threads)
+        if bad:
+            raise RuntimeError(f"{bad} failed cell-steps in the oracle forward window")
+        return y
+
+    def backward(self, lam_end):
+        o, n = self.o, self.n
+        lam = np.array(lam_end, np.float64, order="C", copy=True)
+        gk = np.zeros(o.nrxns)
+        ge = np.zeros((o.nspec, n))
+        bad = o.lib.oracle_adj_backward(n, _p(lam, C.c_double), _p(self.rki, C.c_double), self.stride,
+                                        _p(self.night, C.c_uint8), _opt(self.kmult, C.c_double),
+                                        _opt(self.emis, C.c_double), self.nsync, self.chemstep, self.rtol,
+                                        self.atol, _p(self.ck, C.c_double), _p(self.nsteps, C.c_int),
+                                        _p(gk, C.c_double), _p(ge, C.c_double), self.threads)
+        if bad:
+            raise RuntimeError(f"{bad} cell-steps re-ran differently in the oracle backward window")
+        return lam, gk, ge
+
+    def replay(self, y0, kmult=None, emis=None):
+        """The fixed-step map of the recorded forward run at other inputs."""
+        o, n = self.o, self.n
+        y = np.array(y0, np.float64, order="C", copy=True)
+        km = None if kmult is None else np.ascontiguousarray(kmult, np.float64)
+        em = None if emis is None else np.ascontiguousarray(emis, np.float64)
+        o.lib.oracle_adj_replay(n, _p(y, C.c_double), _p(self.rki, C.c_double), self.stride,
+                                _p(self.night, C.c_uint8), _opt(km, C.c_double), _opt(em, C.c_double),
+                                self.nsync, _p(self.nsteps, C.c_int), _p(self.hs, C.c_double), self.hcap,
+                                self.threads)
+        return y

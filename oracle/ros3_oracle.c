@@ -67,6 +67,11 @@ typedef struct {
     double* cc2;         /* CC2(ld, 0:MXARR-1) */
     double* vdiag;       /* VDIAG(ld, ISCHAN) */
     double* ydot, *k1, *k2, *k3, *yp, *err, *rxrat, *explic;
+    /* discrete-adjoint extensions (ld = 1 blocks only; NULL otherwise) */
+    const double* emis;  /* emission tendency added to every f evaluation */
+    double* tape_y;      /* Y before each accepted step, [tape_cap][NSPEC] */
+    double* tape_h;      /* its step size */
+    int tape_cap, tape_n;
 } Block;
 
 static void block_alloc(Block* b, int ld)
@@ -134,6 +139,8 @@ static void oracle_rbfeval(const Block* b, int ncsp, const double* yin, double* 
             for (int c = 0; c < n; ++c) yd[c] = fma(sc, rr[c], yd[c]);
         }
     }
+    if (b->emis)
+        for (int isp = 0; isp < MECH_ISCHAN; ++isp) ydot[isp] = ydot[isp] + b->emis[isp];
 }
 
 /* rbjacob.F: Jacobian scattered into CC2 by the PD pointer lists */
@@ -313,6 +320,11 @@ static SolverStats oracle_rbsolver(Block* b, int ncsp, double chemstep, const So
             maxerr = fmax_keepnan(fmax(maxerr, UROUND), sqrt(b->err[c] * cfg->rnspec));
         double dtfac = 0.9 / pow(maxerr, GROW);
         if (maxerr <= 1.0) {
+            if (b->tape_y && b->tape_n < b->tape_cap) {
+                memcpy(b->tape_y + (size_t)b->tape_n * MECH_NSPEC, b->y, sizeof(double) * MECH_NSPEC);
+                b->tape_h[b->tape_n] = dt;
+            }
+            if (b->tape_y) b->tape_n++;
             st.nsteps++;
             for (size_t q = 0; q < nsl; ++q) b->y[q] = fmax(b->yp[q], CONMIN);
             if (!finite) st.status |= ST_NONFINITE;
@@ -632,3 +644,6 @@ int oracle_chem(OracleChemArgs* a)
     free(ccol); free(crow); free(clev); free(blkcno); free(blklen); free(nordcell); free(errmx2);
     return nfailed;
 }
+
+/* ------------------------------------------------------------------ discrete adjoint */
+#include "ros3_adjoint.c"
