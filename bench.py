@@ -13,11 +13,14 @@ L2 flush is needed between steps.
 
 Arms and extras
 * gb300 (default): the batched persistent kernel (work queue ordered by previous
-  step counts) on device-resident arrays -> ``value``; the plain per-cell kernel on
-  the same steps -> ``plain``; the host-pointer C ABI with copies inside the timed
-  region -> ``e2e``; the FP64 roofline of the solver kernel; a bounded CPU sample of
-  the reference algorithm (the C oracle, BLKSIZE 50 with the stiffness reordering)
-  on the host cores -> ``cpu_baseline``.
+  step counts, launch shape autotuned on a 4-layer slice of the grid, the K calls
+  replayed from one captured CUDA graph) on device-resident arrays -> ``value``; the
+  plain per-cell kernel on the same steps -> ``plain``; the host-pointer C ABI with
+  copies inside the timed region -> ``e2e``; the FP64 roofline of the solver kernel;
+  a bounded CPU sample of the reference algorithm (the C oracle, BLKSIZE 50 with the
+  stiffness reordering) on the host cores -> ``cpu_baseline``; the differentiable
+  1-hour window on 100x100x35 cells (forward and discrete-adjoint times) ->
+  ``adjoint``; EBI against ROS3 on a 100x100x10 grid -> ``ebi``.
 * --impl reference: the reference algorithm (C oracle; the Fortran cannot be
   compiled here) on all host cores, bounded sample per step.
 
@@ -127,22 +130,30 @@ def flops_of(st: dict, info) -> float:
     return sun * info.flops_step_day + (att - sun) * info.flops_step_night
 
 
-def run_device(g, schedule: str, steps: int, warmup: int, dist, device: int, sample_clocks: bool):
-    """K timed CHEM calls on device-resident arrays from the initial state."""
+def run_device(g, schedule: str, steps: int, warmup: int, dist, device: int, sample_clocks: bool,
+               tuned: dict | None = None, graph: bool = False, solver: str = "ros3"):
+    """K timed CHEM calls on device-resident arrays from the initial state.  graph: the K
+    calls are replayed from one captured CUDA graph (cmaqchem_steps_device)."""
     import torch
     from cmaq_gb300.chem import ChemSolver
     dev = {k: torch.from_numpy(np.ascontiguousarray(getattr(g, k))).to(f"cuda:{device}")
            for k in ("conc", "ta", "qv", "dens", "pres", "seaice", "ocean_szone", "rj", "khetero")}
     conc0 = dev["conc"].clone()
     s = ChemSolver(g.mech, ncols=g.ncols, nrows=g.nrows, nlays=g.nlays, nspcsd=g.nspcsd, cgrid_index=g.cgrid_index,
-                   rtol=RTOL, atol=ATOL, schedule=schedule, device=device)
+                   rtol=RTOL, atol=ATOL, schedule=schedule, device=device, solver=solver,
+                   variant=(tuned or {}).get("variant", "r255"))
+    if tuned:
+        s.set_tuning(block_warps=tuned["block_warps"], lockstep=tuned["lockstep"])
     stream = torch.cuda.current_stream(device)
     args = [dev[k] for k in ("conc", "ta", "qv", "dens", "pres", "seaice", "ocean_szone", "rj", "khetero")]
     # every warm-up step is the hour's first CHEM call from the initial state, so the queue
     # order the timed hour starts from comes from the same call
     for _ in range(warmup):
         dev["conc"].copy_(conc0)
-        s.step(*args, tstep=TSTEP, stream=stream)
+        if graph:
+            s.steps(1, *args, tstep=TSTEP, stream=stream)   # also captures the graph
+        else:
+            s.step(*args, tstep=TSTEP, stream=stream)
     dev["conc"].copy_(conc0)
     torch.cuda.synchronize(device)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -154,8 +165,11 @@ def run_device(g, schedule: str, steps: int, warmup: int, dist, device: int, sam
     torch.cuda.synchronize(device)
     t0 = time.perf_counter()
     ev0.record(stream)
-    for _ in range(steps):
-        stats.append(s.step(*args, tstep=TSTEP, stream=stream))
+    if graph:
+        stats.append(s.steps(steps, *args, tstep=TSTEP, stream=stream))
+    else:
+        for _ in range(steps):
+            stats.append(s.step(*args, tstep=TSTEP, stream=stream))
     ev1.record(stream)
     torch.cuda.synchronize(device)
     wall = time.perf_counter() - t0
@@ -201,6 +215,78 @@ def run_e2e(g, steps: int, warmup: int, dist, device: int):
     barrier(dist)
     s.close()
     return {"wall_s": wall, "h2d": h2d, "d2h": d2h}
+
+
+def run_autotune(workload: str, seed: int, device: int) -> dict:
+    """Launch-shape autotuning on a layer slice of the workload grid (same columns and
+    distributions, 4 layers), 2 timed CHEM calls per candidate."""
+    from cmaq_gb300.autotune import tune
+    from cmaq_gb300.synthetic import make_grid
+    dims = dict(WORKLOADS[workload])
+    dims["nlays"] = min(4, dims["nlays"])
+    g = make_grid(seed=seed, **dims)
+    t0 = time.perf_counter()
+    res = tune(g, nsteps=2)
+    res["tuning_s"] = time.perf_counter() - t0
+    res["sample"] = f"{g.ncols}x{g.nrows}x{g.nlays} ({g.ncell} cells)"
+    return res
+
+
+def run_adjoint(device: int, nsync: int = STEPS_PER_HOUR) -> dict:
+    """The differentiable 1-hour window on 100x100x35 cells: forward (checkpointed) and
+    backward (discrete adjoint) of L = sum of surface O3 wrt initial concentrations,
+    per-reaction log rate multipliers and emission tendencies."""
+    import torch
+    from cmaq_gb300.adjoint import Ros3Window
+    from cmaq_gb300.chem import ChemSolver
+    from cmaq_gb300.synthetic import make_grid, manifest, solver_inputs
+    g = make_grid(seed=2018, ncols=100, nrows=100, nlays=35)
+    gs = ChemSolver(g.mech, ncols=g.ncols, nrows=g.nrows, nlays=g.nlays, nspcsd=g.nspcsd,
+                    cgrid_index=g.cgrid_index, rtol=RTOL, atol=ATOL, device=device)
+    y0, rki, night = solver_inputs(g, gs)
+    gs.close()
+    n = g.ncell
+    s = ChemSolver(g.mech, ncols=n, nrows=1, nlays=1, nspcsd=g.nspcsd, rtol=RTOL, atol=ATOL, device=device)
+    names = [sp["name"] for sp in manifest(g.mech)["species"]]
+    io3 = s.iold2new[names.index("O3")]
+    nsurf = g.ncols * g.nrows
+    w = Ros3Window(s, rki, night, nsync, 5.0)
+    logk = torch.zeros(s.info.nrxns, dtype=torch.float64, device=y0.device, requires_grad=True)
+    emis = torch.zeros_like(y0).requires_grad_(True)
+    times = []
+    for rep in range(2):                                   # the first pass is the warm-up
+        a = y0.clone().requires_grad_(True)
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        torch.cuda.synchronize(device)
+        e0.record()
+        y = w(a, logk, emis)
+        e1.record()
+        y[io3, :nsurf].sum().backward()
+        e2.record()
+        torch.cuda.synchronize(device)
+        times.append((e0.elapsed_time(e1), e1.elapsed_time(e2)))
+        logk.grad = None
+        emis.grad = None
+    fwd, bwd = times[-1]
+    s.close()
+    return {"workload": f"cb6r5_ae7_aq 100x100x35 ({n} cells), {nsync} x 5-min steps, solver level "
+                        "(rates from CALC_RCONST of the grid, fixed over the hour)",
+            "loss": "sum of O3 over the surface layer at the end of the hour",
+            "gradients": "initial concentrations, 349 log rate multipliers, emission tendencies",
+            "forward_ms": fwd, "backward_ms": bwd, "backward_over_forward": bwd / fwd,
+            "total_over_forward": (fwd + bwd) / fwd}
+
+
+def run_ebi(device: int, steps: int) -> dict:
+    """EBI (HRSOLVER) against batched ROS3 on one 100x100x10 grid of the same distributions."""
+    from cmaq_gb300.synthetic import make_grid
+    g = make_grid(seed=2018, ncols=100, nrows=100, nlays=10)
+    out = {"workload": f"cb6r5_ae7_aq 100x100x10 ({g.ncell} cells), {steps} x 5-min CHEM calls"}
+    for solver in ("ebi", "ros3"):
+        r = run_device(g, "queue", steps, 1, None, device, sample_clocks=False, solver=solver)
+        out[f"{solver}_ms_per_step"] = r["ms_total"] / steps
+        out[f"{solver}_value"] = g.ncell / (STEPS_PER_HOUR * r["ms_total"] / steps / 1e3)
+    return out
 
 
 def barrier(dist):
@@ -265,6 +351,9 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-kernel comparison")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-ebi", action="store_true")
     a = ap.parse_args()
     world, rank, local = dist_env()
 
@@ -306,9 +395,11 @@ def main():
     info, _ = _lib.mech_info("cb6r5_ae7_aq")
     peak_tf, _ = _lib.fp64_peak(device)
 
+    tuned = None if a.no_autotune else run_autotune(a.workload, 2018 + rank, device)
     g = make_inputs(a.workload, seed=2018 + rank)
     ncell = g.ncell
-    batched = run_device(g, "queue", a.steps, a.warmup, dist, device, sample_clocks=(rank == 0))
+    batched = run_device(g, "queue", a.steps, a.warmup, dist, device, sample_clocks=(rank == 0), tuned=tuned,
+                         graph=True)
     ms_step = max_over_ranks(batched["ms_total"] / a.steps, dist)
     value = world * ncell / (STEPS_PER_HOUR * ms_step / 1e3)
     fl = sum(flops_of(s, info) for s in batched["stats"])
@@ -341,6 +432,9 @@ def main():
                "sample": f"{r['cells']} cells of the same distributions x {r['steps']} CHEM calls "
                          f"(reference algorithm, BLKSIZE 50 + reordering, C restatement, {r['wall_s']:.1f} s)"}
 
+    adjoint = None if (a.no_adjoint or rank != 0) else run_adjoint(device)
+    ebi = None if (a.no_ebi or rank != 0) else run_ebi(device, a.steps)
+
     traffic = None
     tfile = ROOT / "profiles" / "traffic_per_step.json"
     if tfile.exists():
@@ -349,14 +443,18 @@ def main():
         except Exception:
             traffic = None
     if rank == 0:
-        launches_per_step = 4 if a.warmup > 0 else 1   # queue ordering (hist, scan, scatter) + solve
+        launches_per_step = 4   # queue ordering (hist, scan, scatter) + solve, replayed from one graph
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded; cmaq_gb300/synthetic.py)",
             "config": {"workload": f"cb6r5_ae7_aq {g.ncols}x{g.nrows}x{g.nlays} ({ncell} cells per GPU), "
                                    f"{a.steps} x 5-min CHEM calls from the initial state, rtol 1e-3, atol 1e-9 ppmV",
-                       "schedule": "batched (persistent, work queue ordered by previous step counts)",
+                       "schedule": "batched (persistent, work queue ordered by previous step counts; "
+                                   "the calls replayed from one captured CUDA graph)",
+                       "tuned": None if tuned is None else {k: tuned[k] for k in
+                                                            ("variant", "lockstep", "block_warps", "sample",
+                                                             "tuning_s")},
                        "cells": ncell, "step_attempts_per_cell": attempts / ncell / a.steps,
                        "l2": "inputs larger than L2 (CGRID %.1f GB); no flush" % (g.conc.nbytes / 1e9),
                        "parallelism": f"replicas x{world} (own grid per GPU)"},
@@ -366,6 +464,9 @@ def main():
                                         "MEASURED_PEAKS.json)",
                          "flops": "algorithmic FLOPs of the reference's ROS3 step per attempt x attempts"},
             "plain": plain,
+            "batched_over_plain": None if plain is None else value / plain["value"],
+            "adjoint": adjoint,
+            "ebi": ebi,
             "e2e": e2e,
             "cpu_baseline": cpu,
             "clocks": batched["clocks"],

@@ -54,6 +54,8 @@ def lib(variant: str = "r255") -> C.CDLL:
     L.cmaqchem_step.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, C.c_int, C.c_int, ip, C.POINTER(Stats)]
     L.cmaqchem_step_device.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, C.c_int, C.c_int, ip, vp,
                                        C.POINTER(Stats)]
+    L.cmaqchem_steps_device.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, C.c_int, C.c_int, ip, C.c_int, vp,
+                                        C.POINTER(Stats)]
     L.cmaqchem_cell_stats.argtypes = [vp, vp, vp]
     L.cmaqchem_ros3_solve_device.argtypes = [vp, C.c_longlong, vp, vp, vp, C.c_double, vp, vp, vp, vp]
     L.cmaqchem_ebi_solve_device.argtypes = [vp, C.c_longlong, vp, vp, C.c_int, vp, vp, vp]

@@ -1,0 +1,127 @@
+"""Autotuner for the batched (work-queue) chemistry kernel.
+
+The reference tunes its CPU chemistry by hand: BLKSIZE, the cells per vectorised
+block (rbdriver.F:140-141; CCTM/src/gas/ros3/rbdata_mod.F).  On the GPU the
+launch shape matters instead, and the best one depends on the mechanism (code
+size, registers) and on the grid's stiffness mix.  The tuner times a few CHEM calls
+of a sample of the grid for each candidate:
+
+* cells per block: 64, 128 or 256 (``block_warps`` 2, 4, 8; one cell per thread);
+* register cap: library variants r255 (none), r168, r128 (``cmaq_gb300.build``);
+* queue granularity: whether the block's warps pass barriers between the phases of
+  each step attempt (``lockstep`` 1), also between the generated chunks of the LU
+  and the solves (2), or run free (0, 256-cell blocks only); a lane always refills
+  from the queue as soon as its cell finishes.
+
+Results are cached as JSON keyed by mechanism, GPU name and grid size, so later runs
+on the same machine reuse them.  Every candidate computes bit-identical results (the
+schedule changes no arithmetic), so the choice affects speed only.
+"""
+from __future__ import annotations
+
+import json
+import time
+from dataclasses import asdict, dataclass
+from pathlib import Path
+
+import numpy as np
+
+from .chem import ChemSolver
+
+KEYS = ("conc", "ta", "qv", "dens", "pres", "seaice", "ocean_szone", "rj", "khetero")
+
+
+@dataclass(frozen=True)
+class Candidate:
+    variant: str = "r255"
+    lockstep: int = 1
+    block_warps: int = 4
+
+    def knobs(self) -> dict:
+        # block size first: every (lockstep, block_warps) pair is reachable from the defaults
+        return {"block_warps": self.block_warps, "lockstep": self.lockstep}
+
+
+def candidates(variants=("r255", "r168", "r128")) -> list[Candidate]:
+    out = []
+    for v in variants:
+        out.append(Candidate(v, 0, 8))
+        for ls in (1, 2):
+            for bw in (2, 4, 8):
+                out.append(Candidate(v, ls, bw))
+    return out
+
+
+def available_variants(build_missing: bool = False) -> list[str]:
+    from . import build as cbuild
+    have = []
+    for v in cbuild.VARIANTS:
+        if v == "lucs":
+            continue
+        if cbuild.lib_path(v).exists():
+            have.append(v)
+        elif build_missing:
+            cbuild.build(variant=v)
+            have.append(v)
+    return have
+
+
+def cache_key(mechanism: str, ncell: int) -> str:
+    import torch
+    name = torch.cuda.get_device_name() if torch.cuda.is_available() else "cpu"
+    bucket = 1 << max(0, int(ncell).bit_length() - 1)     # power-of-two bucket of the grid size
+    return f"{mechanism}|{name}|{bucket}"
+
+
+def _time_candidate(g, cand: Candidate, nsteps: int, dev: dict, conc0) -> float:
+    s = ChemSolver(g.mech, ncols=g.ncols, nrows=g.nrows, nlays=g.nlays, nspcsd=g.nspcsd,
+                   cgrid_index=g.cgrid_index, rtol=1e-3, atol=1e-9, schedule="queue", variant=cand.variant)
+    try:
+        s.set_tuning(**cand.knobs())
+        args = [dev[k] for k in KEYS]
+        dev["conc"].copy_(conc0)
+        s.step(*args)                    # first call from the initial state; gives the queue order
+        dev["conc"].copy_(conc0)
+        ms = 0.0
+        for _ in range(nsteps):
+            ms += s.step(*args)["device_ms"]
+        return ms
+    finally:
+        s.close()
+
+
+def tune(g, nsteps: int = 2, variants=None, cache: str | Path | None = None, verbose: bool = False) -> dict:
+    """Time every candidate on grid ``g`` (GridInputs); returns the best as a dict
+    {variant, lockstep, block_warps, ms, table}.  With ``cache``, a stored result for
+    the same key is returned without timing, and a new one is stored."""
+    import torch
+    key = cache_key(g.mech, g.ncell)
+    path = Path(cache) if cache else None
+    db = {}
+    if path and path.exists():
+        db = json.loads(path.read_text())
+        if key in db:
+            return db[key]
+    dev = {k: torch.from_numpy(np.ascontiguousarray(getattr(g, k))).cuda() for k in KEYS}
+    conc0 = dev["conc"].clone()
+    table = []
+    for cand in candidates(tuple(variants or available_variants())):
+        t0 = time.perf_counter()
+        ms = _time_candidate(g, cand, nsteps, dev, conc0)
+        table.append({**asdict(cand), "ms": ms})
+        if verbose:
+            print(f"autotune {cand}: {ms:.1f} ms ({time.perf_counter() - t0:.1f} s)", flush=True)
+    best = min(table, key=lambda r: r["ms"])
+    res = {**best, "nsteps": nsteps, "cells": g.ncell, "table": table}
+    if path:
+        db[key] = res
+        path.write_text(json.dumps(db, indent=1))
+    return res
+
+
+def tuned_solver(g, result: dict, **kw) -> ChemSolver:
+    """A queue-scheduled ChemSolver for grid ``g`` with the tuned variant and knobs."""
+    s = ChemSolver(g.mech, ncols=g.ncols, nrows=g.nrows, nlays=g.nlays, nspcsd=g.nspcsd, cgrid_index=g.cgrid_index,
+                   schedule="queue", variant=result["variant"], **kw)
+    s.set_tuning(block_warps=result["block_warps"], lockstep=result["lockstep"])
+    return s

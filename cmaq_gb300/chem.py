@@ -74,6 +74,9 @@ class ChemSolver:
         self.variant = variant
         self._L = _lib.lib(variant)
         self.info, self.inew2old = _lib.mech_info(mechanism)
+        self.iold2new = [0] * len(self.inew2old)
+        for i, old in enumerate(self.inew2old):
+            self.iold2new[old] = i
         self.shape = (nlays, nrows, ncols)
         self.nspcsd = nspcsd
         self.rtol = reference_tolerance(rtol) if reference_tolerances else float(rtol)
@@ -137,6 +140,22 @@ class ChemSolver:
             rc = self._L.cmaqchem_step_device(self._h, *ptrs, jdate, jtime, ts, s, C.byref(st))
         else:
             rc = self._L.cmaqchem_step(self._h, *ptrs, jdate, jtime, ts, C.byref(st))
+        check(rc, self._L)
+        return st.as_dict()
+
+    def steps(self, nsteps: int, conc, ta, qv, dens, pres, seaice, ocean_szone, rj, khetero, jdate: int = 2018182,
+              jtime: int = 0, tstep=(10000, 500, 500), stream=None) -> dict:
+        """``nsteps`` consecutive CHEM calls on CUDA tensors, replayed from one captured
+        CUDA graph without host synchronisation in between; totals over the calls."""
+        args = [conc, ta, qv, dens, pres, seaice, ocean_szone, rj, khetero]
+        if not all(_is_torch(a) for a in args):
+            raise ChemError("steps() takes CUDA tensors")
+        self._check_shapes(*args)
+        st = _lib.Stats()
+        s = C.c_void_p(stream) if isinstance(stream, int) else (
+            C.c_void_p(stream.cuda_stream) if stream is not None else None)
+        rc = self._L.cmaqchem_steps_device(self._h, *[_ptr(a) for a in args], jdate, jtime, tstep_array(tstep),
+                                           int(nsteps), s, C.byref(st))
         check(rc, self._L)
         return st.as_dict()
 

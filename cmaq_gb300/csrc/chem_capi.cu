@@ -56,6 +56,12 @@ int hhmmss_to_sec(int t)
 // error-text setter for the library's other translation units, not exported
 __attribute__((visibility("hidden"))) void cmaqchem_set_error(const std::string& msg) { g_err = msg; }
 
+// what a captured CHEM call depends on besides the handle's own buffers
+struct GraphKey {
+    const void* ptr[9];
+    int itmstep;
+};
+
 struct cmaqchem_handle {
     const MechOps* ops = nullptr;
     cmaqchem_cfg cfg{};
@@ -107,6 +113,9 @@ struct cmaqchem_handle {
     int* d_adj_status = nullptr;
     size_t adj_cell_cap = 0, adj_status_cap = 0;
     unsigned long long* d_adj_counters = nullptr;
+    // captured CHEM call of cmaqchem_steps_device
+    cudaGraphExec_t graph_exec = nullptr;
+    GraphKey graph_key{};
 };
 
 namespace {
@@ -122,6 +131,7 @@ void free_handle(cmaqchem_handle* h)
                     h->d_adj_order, h->d_adj_status, h->d_adj_counters};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -311,6 +321,8 @@ extern "C" int cmaqchem_diag_set_tuning(cmaqchem_handle* h, const char* key, int
     CK(cudaSetDevice(h->device));
     if (strcmp(key, "night_pattern") == 0) {
         h->use_night = value != 0;
+        if (h->graph_exec) CK(cudaGraphExecDestroy(h->graph_exec));
+        h->graph_exec = nullptr;
         return 0;
     }
     if (strcmp(key, "lockstep") == 0) {
@@ -324,26 +336,19 @@ extern "C" int cmaqchem_diag_set_tuning(cmaqchem_handle* h, const char* key, int
     } else {
         return fail(std::string("unknown tuning key ") + key);
     }
+    if (h->graph_exec) CK(cudaGraphExecDestroy(h->graph_exec));   // launch shape changed
+    h->graph_exec = nullptr;
     return configure_queue(h);
 }
 
-static int step_device_impl(cmaqchem_handle* h, float* conc, const float* ta, const float* qv, const float* dens,
-                            const float* pres, const float* seaice, const float* osz, const float* rj,
-                            const double* khet, const int tstep[3], cudaStream_t s, cmaqchem_stats* stats)
+// Enqueue the launches of one CHEM call (no host synchronisation).  sort: order the work
+// queue by the previous call's step attempts.
+static int enqueue_step(cmaqchem_handle* h, const chem::GridArgs& a, int itmstep, cudaStream_t s, bool sort)
 {
-    const void* ptrs[] = {conc, ta, qv, dens, pres, seaice, osz, rj, tstep, khet};
-    if (check_ptrs(ptrs, h->ops->nhetero > 0 ? 10 : 9)) return -1;
-    const int itmstep = hhmmss_to_sec(tstep[1]);
-    if (itmstep <= 0) return fail("TSTEP(2) must be a positive HHMMSS interval");
-    const double chemstep = (double)itmstep / 60.0;   // rbdriver.F:384-385
-    CK(cudaSetDevice(h->device));
-    chem::GridArgs a = grid_args(h, conc, ta, qv, dens, pres, seaice, osz, rj, khet, chemstep);
-    CK(cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned long long) * 5, s));
-    CK(cudaEventRecord(h->ev0, s));
     const bool ebi_solver = h->cfg.solver == CMAQCHEM_SOLVER_EBI;
     if (h->cfg.schedule == CMAQCHEM_SCHED_QUEUE || ebi_solver) {
         chem::QueueArgs q{nullptr, h->d_head};
-        if (h->have_history && h->cfg.schedule == CMAQCHEM_SCHED_QUEUE) {
+        if (sort && h->cfg.schedule == CMAQCHEM_SCHED_QUEUE) {
             const int nb = 4 * h->nsm;
             CK(cudaMemsetAsync(h->d_hist, 0, sizeof(unsigned int) * chem::QUEUE_BINS, s));
             chem::k_queue_hist<<<nb, 256, 0, s>>>(h->d_steps, h->ncell, h->d_hist);
@@ -367,6 +372,11 @@ static int step_device_impl(cmaqchem_handle* h, float* conc, const float* ta, co
     } else {
         CK(h->ops->chem_static(a, h->nblocks, s));
     }
+    return 0;
+}
+
+static int finish_steps(cmaqchem_handle* h, cudaStream_t s, cmaqchem_stats* stats)
+{
     CK(cudaEventRecord(h->ev1, s));
     unsigned long long cnt[5];
     CK(cudaMemcpyAsync(cnt, h->d_counters, sizeof(cnt), cudaMemcpyDeviceToHost, s));
@@ -385,6 +395,23 @@ static int step_device_impl(cmaqchem_handle* h, float* conc, const float* ta, co
     return (int)cnt[2];
 }
 
+static int step_device_impl(cmaqchem_handle* h, float* conc, const float* ta, const float* qv, const float* dens,
+                            const float* pres, const float* seaice, const float* osz, const float* rj,
+                            const double* khet, const int tstep[3], cudaStream_t s, cmaqchem_stats* stats)
+{
+    const void* ptrs[] = {conc, ta, qv, dens, pres, seaice, osz, rj, tstep, khet};
+    if (check_ptrs(ptrs, h->ops->nhetero > 0 ? 10 : 9)) return -1;
+    const int itmstep = hhmmss_to_sec(tstep[1]);
+    if (itmstep <= 0) return fail("TSTEP(2) must be a positive HHMMSS interval");
+    const double chemstep = (double)itmstep / 60.0;   // rbdriver.F:384-385
+    CK(cudaSetDevice(h->device));
+    chem::GridArgs a = grid_args(h, conc, ta, qv, dens, pres, seaice, osz, rj, khet, chemstep);
+    CK(cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned long long) * 5, s));
+    CK(cudaEventRecord(h->ev0, s));
+    if (enqueue_step(h, a, itmstep, s, h->have_history)) return -1;
+    return finish_steps(h, s, stats);
+}
+
 extern "C" int cmaqchem_step_device(cmaqchem_handle* h, float* conc, const float* ta, const float* qv,
                                     const float* dens, const float* pres, const float* seaice,
                                     const float* ocean_szone, const float* rj, const double* khetero, int jdate,
@@ -395,6 +422,49 @@ extern "C" int cmaqchem_step_device(cmaqchem_handle* h, float* conc, const float
     if (!h) return fail("null handle");
     cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
     return step_device_impl(h, conc, ta, qv, dens, pres, seaice, ocean_szone, rj, khetero, tstep, s, stats);
+}
+
+extern "C" int cmaqchem_steps_device(cmaqchem_handle* h, float* conc, const float* ta, const float* qv,
+                                     const float* dens, const float* pres, const float* seaice,
+                                     const float* ocean_szone, const float* rj, const double* khetero, int jdate,
+                                     int jtime, const int tstep[3], int nsteps, void* stream, cmaqchem_stats* stats)
+{
+    (void)jdate;
+    (void)jtime;
+    if (!h) return fail("null handle");
+    if (nsteps <= 0) return fail("nsteps must be positive");
+    const void* ptrs[] = {conc, ta, qv, dens, pres, seaice, ocean_szone, rj, tstep, khetero};
+    if (check_ptrs(ptrs, h->ops->nhetero > 0 ? 10 : 9)) return -1;
+    const int itmstep = hhmmss_to_sec(tstep[1]);
+    if (itmstep <= 0) return fail("TSTEP(2) must be a positive HHMMSS interval");
+    CK(cudaSetDevice(h->device));
+    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    GraphKey key{{conc, ta, qv, dens, pres, seaice, ocean_szone, rj, khetero}, itmstep};
+    if (!h->graph_exec || memcmp(&key, &h->graph_key, sizeof(key)) != 0) {
+        if (h->graph_exec) CK(cudaGraphExecDestroy(h->graph_exec));
+        h->graph_exec = nullptr;
+        chem::GridArgs a = grid_args(h, conc, ta, qv, dens, pres, seaice, ocean_szone, rj, khetero,
+                                     (double)itmstep / 60.0);
+        // capture one call on the handle's own stream; the work queue is always ordered
+        // (by zero counts before the first call, which is a plain permutation)
+        CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = enqueue_step(h, a, itmstep, h->stream, true);
+        cudaGraph_t g = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(h->stream, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return -1;
+        }
+        CK(ce);
+        const cudaError_t ie = cudaGraphInstantiate(&h->graph_exec, g, 0);
+        cudaGraphDestroy(g);
+        CK(ie);
+        h->graph_key = key;
+    }
+    CK(cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned long long) * 5, s));
+    CK(cudaEventRecord(h->ev0, s));
+    for (int i = 0; i < nsteps; ++i) CK(cudaGraphLaunch(h->graph_exec, s));
+    return finish_steps(h, s, stats);
 }
 
 extern "C" int cmaqchem_step(cmaqchem_handle* h, float* conc, const float* ta, const float* qv, const float* dens,

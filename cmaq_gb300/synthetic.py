@@ -162,3 +162,27 @@ CONFIGS = {
     "adjoint350k": dict(ncols=100, nrows=100, nlays=35),
     "cracmm2_1m": dict(ncols=200, nrows=200, nlays=25, mech="cracmm2"),
 }
+
+
+def solver_inputs(g: GridInputs, solver):
+    """Solver-level inputs of a grid on the GPU, gathered as one CHEM call does
+    (rbdriver.F:460-519): y0 [ischan, n] FP64 in the solver's species order from the
+    REAL(4) conversions, rki [nrxns, n] from the device CALC_RCONST, night [n] uint8."""
+    import torch
+    man = manifest(g.mech)
+    n = g.ncell
+    dev = torch.device("cuda")
+    conc = torch.from_numpy(np.ascontiguousarray(g.conc.reshape(g.nspcsd, n))).to(dev)
+    svol = (1.0 / torch.from_numpy(g.dens.reshape(n)).to(dev)).to(torch.float32)
+    y0 = torch.empty((len(man["species"]), n), dtype=torch.float64, device=dev)
+    for s, sp in enumerate(man["species"]):
+        v = conc[g.cgrid_index[s] - 1]
+        if sp["convert"]:
+            fwd = np.float32(np.float32(1.0e-3) * np.float32(28.9628)) / np.float32(sp["molwt"])
+            v = (float(np.float32(fwd)) * svol).to(torch.float32) * v
+        y0[solver.iold2new[s]] = torch.clamp_min(v.to(torch.float32), 1.0e-30).to(torch.float64)
+    t = {k: torch.from_numpy(np.ascontiguousarray(getattr(g, k))).to(dev)
+         for k in ("conc", "ta", "qv", "dens", "pres", "seaice", "ocean_szone", "rj", "khetero")}
+    rki, sun = solver.rconst(t["conc"], t["ta"], t["qv"], t["dens"], t["pres"], t["seaice"], t["ocean_szone"],
+                             t["rj"], t["khetero"])
+    return y0, rki, (1 - sun).to(torch.uint8)

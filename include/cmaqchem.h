@@ -103,6 +103,19 @@ int cmaqchem_step_device(cmaqchem_handle* h, float* conc, const float* ta, const
                          int jdate, int jtime, const int tstep[3], void* stream,
                          cmaqchem_stats* stats);
 
+/* nsteps consecutive CHEM calls on device arrays (same arguments as
+ * cmaqchem_step_device), for hosts that run chemistry alone over several
+ * synchronisation steps: the launches of one call are captured once as a CUDA graph
+ * (re-captured when a pointer, TSTEP(2) or a tuning knob changes) and replayed nsteps
+ * times with no host synchronisation in between; stats are summed over the calls.
+ * The first call on a handle captures on the handle's own stream, so it must not be
+ * made while another stream of the process is being captured. */
+int cmaqchem_steps_device(cmaqchem_handle* h, float* conc, const float* ta, const float* qv,
+                          const float* dens, const float* pres, const float* seaice,
+                          const float* ocean_szone, const float* rj, const double* khetero,
+                          int jdate, int jtime, const int tstep[3], int nsteps, void* stream,
+                          cmaqchem_stats* stats);
+
 /* Per-cell status of the last step call (CMAQCHEM_CELL_* bits) and step attempts,
  * copied to host arrays of ncols*nrows*nlays ints (either may be NULL). */
 int cmaqchem_cell_stats(cmaqchem_handle* h, int* status, int* attempts);

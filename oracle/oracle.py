@@ -61,6 +61,8 @@ def load(mech: str = "cb6r5_ae7_aq") -> C.CDLL:
                                         C.c_double, dp, ip, dp, dp, C.c_int]
     lib.oracle_adj_replay.argtypes = [C.c_long, dp, dp, C.c_long, u8p, dp, dp, C.c_int, ip, dp, C.c_int, C.c_int]
     lib.oracle_adj_replay.restype = None
+    lib.oracle_ddm3d_window.argtypes = [C.c_long, dp, dp, C.c_long, u8p, dp, C.c_int, C.c_double, C.c_double,
+                                        C.c_double, C.c_int, ip, ip, dp, C.c_int]
     lib.oracle_set_dtmin.argtypes = [C.c_double]
     lib.oracle_get_dtmin.restype = C.c_double
     return lib
@@ -246,3 +248,25 @@ class AdjointWindow:
                                 self.nsync, _p(self.nsteps, C.c_int), _p(self.hs, C.c_double), self.hcap,
                                 self.threads)
         return y
+
+
+def ddm3d_window(o: "Oracle", y0, rki, night, nsync: int, chemstep: float, rtol: float, atol: float, params,
+                 kmult=None, threads: int = 0):
+    """First-order DDM-3D sensitivities (CMAQ's SOLVE_DDM3D_CHEM restated) over a window.
+    params: list of ("init", species index in solver order) or ("rate", reaction index).
+    Returns (y_end, s_end [nparam, nspec, n])."""
+    y = np.array(y0, np.float64, order="C", copy=True)
+    rki = np.ascontiguousarray(rki, np.float64)
+    stride = 0 if rki.ndim == 2 else rki.shape[1] * rki.shape[2]
+    night = np.ascontiguousarray(night, np.uint8)
+    n = y.shape[1]
+    kind = np.array([0 if k == "init" else 1 for k, _ in params], np.int32)
+    idx = np.array([i for _, i in params], np.int32)
+    s_end = np.zeros((len(params), o.nspec, n))
+    km = None if kmult is None else np.ascontiguousarray(kmult, np.float64)
+    bad = o.lib.oracle_ddm3d_window(n, _p(y, C.c_double), _p(rki, C.c_double), stride, _p(night, C.c_uint8),
+                                    _opt(km, C.c_double), nsync, chemstep, rtol, atol, len(params),
+                                    _p(kind, C.c_int), _p(idx, C.c_int), _p(s_end, C.c_double), threads)
+    if bad:
+        raise RuntimeError(f"{bad} failed cell-steps in the DDM-3D window")
+    return y, s_end

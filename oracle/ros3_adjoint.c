@@ -405,3 +405,143 @@ void oracle_adj_replay(long n, double* y, const double* rki, long rki_stride, co
         block_free(&b);
     }
 }
+
+/* ------------------------------------------------------------------ DDM-3D (reference gradient)
+ *
+ * First-order DDM-3D sensitivities of the chemistry as CMAQ computes them
+ * (CCTM/src/ddm3d/DDM3D_CHEM.F:155-410, SOLVE_DDM3D_CHEM; driver hook rbdriver.F:619-651):
+ * after each synchronisation step of length DT the sensitivity vector S of a parameter
+ * is advanced by the Crank-Nicolson-type update
+ *
+ *     (I - DT/2 J(YAVE)) S_new = (I + DT/2 J(YAVE)) S_old + DT dF/dp(YAVE)
+ *
+ * with YAVE the step's time-averaged concentrations (rbsolver.F:468-475, 592-595) and J
+ * the Jacobian of the mechanism (MECHANISM_FUNCTIONS.F:755, EVALUATE_F_JAC_MECH).  For a
+ * reaction-rate parameter (IPT = 5) dF/dp is the rate of the reaction times its net
+ * stoichiometry (DDM3D_CHEM.F:338-385); for an initial-condition parameter it is zero
+ * and S starts at the unit vector.  The reference stores J in REAL(4) and factors with
+ * LINPACK SGEFA/SGESL; here everything is REAL(8) with partial pivoting. */
+
+static void dense_jac(const double* rki, const double* y, int ncsp, double* jac /* [n][n] row-major */)
+{
+    const int n = MECH_ISCHAN;
+    memset(jac, 0, sizeof(double) * n * n);
+    const int nu = mech_nuserat[ncsp];
+    for (int q = 0; q < nu; ++q) {
+        const int r = mech_nkuserat[ncsp * MECH_NRXNS + q];
+        const int nre = mech_nreact[r];
+        const int* a = &mech_irm2[r * (3 + MECH_MXPRD)];
+        double ex[3] = {0, 0, 0};
+        if (nre == 1) ex[0] = rki[r];
+        else if (nre == 2) { ex[0] = rki[r] * y[a[1]]; ex[1] = rki[r] * y[a[0]]; }
+        else if (nre == 3) {
+            ex[0] = rki[r] * y[a[1]] * y[a[2]]; ex[1] = rki[r] * y[a[0]] * y[a[2]]; ex[2] = rki[r] * y[a[1]] * y[a[0]];
+        }
+        for (int j = 0; j < nre; ++j) {
+            for (int i = 0; i < nre; ++i) jac[a[i] * n + a[j]] -= ex[j];
+            for (int p = 0; p < mech_nprdct[r]; ++p) jac[a[3 + p] * n + a[j]] += mech_sc[r * MECH_MXPRD + p] * ex[j];
+        }
+    }
+}
+
+static void lu_factor(double* m, int* piv, int n)
+{
+    for (int k = 0; k < n; ++k) {
+        int p = k;
+        for (int i = k + 1; i < n; ++i) if (fabs(m[i * n + k]) > fabs(m[p * n + k])) p = i;
+        piv[k] = p;
+        if (p != k) for (int j = 0; j < n; ++j) { double t = m[k * n + j]; m[k * n + j] = m[p * n + j]; m[p * n + j] = t; }
+        const double d = m[k * n + k];
+        for (int i = k + 1; i < n; ++i) {
+            const double l = m[i * n + k] / d;
+            m[i * n + k] = l;
+            if (l != 0.0) for (int j = k + 1; j < n; ++j) m[i * n + j] -= l * m[k * n + j];
+        }
+    }
+}
+
+static void lu_solve(const double* m, const int* piv, int n, double* b)
+{
+    for (int k = 0; k < n; ++k) { const int p = piv[k]; if (p != k) { double t = b[k]; b[k] = b[p]; b[p] = t; } }
+    for (int i = 0; i < n; ++i) for (int j = 0; j < i; ++j) b[i] -= m[i * n + j] * b[j];
+    for (int i = n - 1; i >= 0; --i) {
+        for (int j = i + 1; j < n; ++j) b[i] -= m[i * n + j] * b[j];
+        b[i] /= m[i * n + i];
+    }
+}
+
+/* DDM-3D over a window.  Parameters: kind[p] = 0 initial condition of species idx[p]
+ * (solver order), 1 log rate multiplier of reaction idx[p].  Returns s_end[p][nspec][n]
+ * and the end state in y (the forward is the oracle's rbsolver). */
+int oracle_ddm3d_window(long n, double* y, const double* rki, long rki_stride, const uint8_t* night,
+                        const double* kmult, int nsync, double chemstep, double rtol, double atol, int nparam,
+                        const int* kind, const int* idx, double* s_end, int threads)
+{
+    int nbad = 0;
+    const int ns = MECH_ISCHAN;
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel reduction(+ : nbad)
+#endif
+    {
+        Block b;
+        block_alloc(&b, 1);
+        b.ncells = 1;
+        double* jac = malloc(sizeof(double) * ns * ns);
+        double* am = malloc(sizeof(double) * ns * ns);
+        int* piv = malloc(sizeof(int) * ns);
+        double* sv = malloc(sizeof(double) * ns * (nparam > 0 ? nparam : 1));
+        double yave[MECH_NSPEC], tmp[MECH_NSPEC], src[MECH_NSPEC];
+        SolverCfg cfg = {rtol, atol, (double)(1.0f / (float)MECH_NSPEC), 100000};
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 4)
+#endif
+        for (long c = 0; c < n; ++c) {
+            for (int s = 0; s < MECH_NSPEC; ++s) b.y[s] = y[(size_t)s * n + c];
+            for (int p = 0; p < nparam; ++p)
+                for (int s = 0; s < ns; ++s) sv[p * ns + s] = (kind[p] == 0 && idx[p] == s) ? 1.0 : 0.0;
+            const int ncsp = night[c] ? 1 : 0;
+            for (int k = 0; k < nsync; ++k) {
+                for (int r = 0; r < MECH_NRXNS; ++r) {
+                    const double kk = rki[(size_t)k * rki_stride + (size_t)r * n + c];
+                    b.rki[r] = kmult ? kk * kmult[r] : kk;
+                }
+                memset(yave, 0, sizeof(yave));
+                b.yave = yave;
+                SolverStats st = oracle_rbsolver(&b, ncsp, chemstep, &cfg, NULL);
+                b.yave = NULL;
+                nbad += st.status != 0;
+                for (int s = 0; s < ns; ++s) yave[s] /= chemstep;
+                dense_jac(b.rki, yave, ncsp, jac);
+                for (int i = 0; i < ns * ns; ++i) am[i] = -0.5 * chemstep * jac[i];
+                for (int i = 0; i < ns; ++i) am[i * ns + i] += 1.0;
+                lu_factor(am, piv, ns);
+                for (int p = 0; p < nparam; ++p) {
+                    double* sp = sv + p * ns;
+                    memset(src, 0, sizeof(src));
+                    if (kind[p] == 1) {   /* DT * stoichiometry * rate at YAVE */
+                        const int r = idx[p];
+                        const int* a = &mech_irm2[r * (3 + MECH_MXPRD)];
+                        double rate = b.rki[r];
+                        for (int i = 0; i < mech_nreact[r]; ++i) rate *= yave[a[i]];
+                        for (int i = 0; i < mech_nreact[r]; ++i) src[a[i]] -= chemstep * rate;
+                        for (int q = 0; q < mech_nprdct[r]; ++q) src[a[3 + q]] += chemstep * rate * mech_sc[r * MECH_MXPRD + q];
+                    }
+                    for (int i = 0; i < ns; ++i) {
+                        double t = sp[i];
+                        for (int j = 0; j < ns; ++j) t += 0.5 * chemstep * jac[i * ns + j] * sp[j];
+                        tmp[i] = t + src[i];
+                    }
+                    lu_solve(am, piv, ns, tmp);
+                    memcpy(sp, tmp, sizeof(double) * ns);
+                }
+            }
+            for (int s = 0; s < MECH_NSPEC; ++s) y[(size_t)s * n + c] = b.y[s];
+            for (int p = 0; p < nparam; ++p)
+                for (int s = 0; s < ns; ++s) s_end[((size_t)p * ns + s) * n + c] = sv[p * ns + s];
+        }
+        free(jac); free(am); free(piv); free(sv);
+        block_free(&b);
+    }
+    return nbad;
+}

@@ -72,6 +72,7 @@ typedef struct {
     double* tape_y;      /* Y before each accepted step, [tape_cap][NSPEC] */
     double* tape_h;      /* its step size */
     int tape_cap, tape_n;
+    double* yave;        /* DDM-3D: time integral of Y over the accepted steps (rbsolver.F:468-475) */
 } Block;
 
 static void block_alloc(Block* b, int ld)
@@ -325,6 +326,8 @@ static SolverStats oracle_rbsolver(Block* b, int ncsp, double chemstep, const So
                 b->tape_h[b->tape_n] = dt;
             }
             if (b->tape_y) b->tape_n++;
+            if (b->yave)
+                for (int q = 0; q < MECH_NSPEC; ++q) b->yave[q] += 0.5 * (b->y[q] + fmax(b->yp[q], CONMIN)) * dt;
             st.nsteps++;
             for (size_t q = 0; q < nsl; ++q) b->y[q] = fmax(b->yp[q], CONMIN);
             if (!finite) st.status |= ST_NONFINITE;

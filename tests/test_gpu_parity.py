@@ -123,3 +123,19 @@ def test_shape_errors_are_reported(grid):
     with pytest.raises(ChemError):
         s.step(t["conc"][:, :1], t["ta"], t["qv"], t["dens"], t["pres"], t["seaice"], t["ocean_szone"], t["rj"],
                t["khetero"])
+
+
+def test_graph_replayed_steps_match_single_calls(grid):
+    from helpers import to_cuda
+    a, sa, _ = gpu_chem(grid, schedule="queue", nsteps=3)
+    s = _solver(grid, schedule="queue")
+    t = to_cuda(grid)
+    args = [t[k] for k in ("conc", "ta", "qv", "dens", "pres", "seaice", "ocean_szone", "rj", "khetero")]
+    st = s.steps(3, *args)
+    assert np.array_equal(t["conc"].cpu().numpy(), a)
+    assert st["accepted_steps"] == sum(x["accepted_steps"] for x in sa)
+    # a second replay continues from the new state, like further single calls
+    st2 = s.steps(1, *args)
+    b, sb, _ = gpu_chem(grid, schedule="queue", nsteps=4)
+    assert np.array_equal(t["conc"].cpu().numpy(), b)
+    assert st2["accepted_steps"] == sb[3]["accepted_steps"]
