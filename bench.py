@@ -354,6 +354,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-ebi", action="store_true")
+    ap.add_argument("--solver", default="ros3", choices=["ros3", "ebi"],
+                    help="solver of the timed CHEM calls (the metric is quoted for ros3)")
     a = ap.parse_args()
     world, rank, local = dist_env()
 
@@ -399,7 +401,7 @@ def main():
     g = make_inputs(a.workload, seed=2018 + rank)
     ncell = g.ncell
     batched = run_device(g, "queue", a.steps, a.warmup, dist, device, sample_clocks=(rank == 0), tuned=tuned,
-                         graph=True)
+                         graph=True, solver=a.solver)
     ms_step = max_over_ranks(batched["ms_total"] / a.steps, dist)
     value = world * ncell / (STEPS_PER_HOUR * ms_step / 1e3)
     fl = sum(flops_of(s, info) for s in batched["stats"])
@@ -435,17 +437,21 @@ def main():
     adjoint = None if (a.no_adjoint or rank != 0) else run_adjoint(device)
     ebi = None if (a.no_ebi or rank != 0) else run_ebi(device, a.steps)
 
-    traffic = None
+    traffic = traffic_note = None
     tfile = ROOT / "profiles" / "traffic_per_step.json"
     if tfile.exists():
         try:
-            traffic = json.loads(tfile.read_text()).get(a.workload)
+            t = json.loads(tfile.read_text()).get(a.workload)
+            traffic = None if t is None else float(t["bytes_per_launch"])
+            traffic_note = None if t is None else t["source"]
         except Exception:
             traffic = None
     if rank == 0:
         launches_per_step = 4   # queue ordering (hist, scan, scatter) + solve, replayed from one graph
+        if a.solver == "ebi":   # EBI iterations have no ROS3 FLOP count
+            achieved_tf = None
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+            "metric": METRIC if a.solver == "ros3" else METRIC.replace("ROS3", "EBI"), "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded; cmaq_gb300/synthetic.py)",
             "config": {"workload": f"cb6r5_ae7_aq {g.ncols}x{g.nrows}x{g.nlays} ({ncell} cells per GPU), "
@@ -458,8 +464,10 @@ def main():
                        "cells": ncell, "step_attempts_per_cell": attempts / ncell / a.steps,
                        "l2": "inputs larger than L2 (CGRID %.1f GB); no flush" % (g.conc.nbytes / 1e9),
                        "parallelism": f"replicas x{world} (own grid per GPU)"},
-            "roofline": {"bound": "fp64", "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
-                         "frac": achieved_tf / peak_tf, "traffic": traffic,
+            "roofline": None if achieved_tf is None else {
+                         "bound": "fp64", "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
+                         "frac": achieved_tf / peak_tf, "traffic": traffic, "traffic_source": traffic_note,
+                         "dram_gbs_from_traffic": None if traffic is None else traffic / (ms_step * 1e-3) / 1e9,
                          "peak_source": "measured live: FP64 FMA-chain kernel (no FP64 figure in "
                                         "MEASURED_PEAKS.json)",
                          "flops": "algorithmic FLOPs of the reference's ROS3 step per attempt x attempts"},

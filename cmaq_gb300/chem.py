@@ -94,7 +94,7 @@ class ChemSolver:
 
     def set_tuning(self, **knobs) -> None:
         """Scheduling knobs (see include/cmaqchem_diag.h): night_pattern=0/1, lockstep=0/1/2,
-        block_warps=2/4/8."""
+        block_warps=2/4/8, blocks_per_sm=0 (as many as fit) or a cap."""
         for k, v in knobs.items():
             check(self._L.cmaqchem_diag_set_tuning(self._h, k.encode(), int(v)), self._L)
 

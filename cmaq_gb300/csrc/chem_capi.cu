@@ -91,6 +91,7 @@ struct cmaqchem_handle {
     int q_sync = 1;          // work-queue kernel: barriers between attempt phases
     int q_wpb = 4;           // work-queue kernel: warps per block
     int q_nblocks = 0;
+    int q_bps_cap = 0;       // blocks per SM of the queue kernel, 0: as many as fit
     size_t ws_warps = 0;     // workspace capacity in warps
     // device staging of the host-pointer entry point, allocated on first use
     float *s_conc = nullptr, *s_ta = nullptr, *s_qv = nullptr, *s_dens = nullptr, *s_pres = nullptr;
@@ -154,7 +155,9 @@ int configure_queue(cmaqchem_handle* h)
 {
     int bps = 0;
     CK(h->ops->queue_occupancy(h->q_sync, h->q_wpb, &bps));
-    h->q_nblocks = h->nsm * (bps > 0 ? bps : 1);
+    if (bps < 1) bps = 1;
+    if (h->q_bps_cap > 0 && bps > h->q_bps_cap) bps = h->q_bps_cap;
+    h->q_nblocks = h->nsm * bps;
     return ensure_ws(h, (size_t)h->q_nblocks * h->q_wpb);
 }
 
@@ -329,6 +332,9 @@ extern "C" int cmaqchem_diag_set_tuning(cmaqchem_handle* h, const char* key, int
         if (value < 0 || value > 2) return fail("lockstep must be 0, 1 or 2");
         if (value == 0 && h->q_wpb != 8) return fail("lockstep 0 needs block_warps 8");
         h->q_sync = value;
+    } else if (strcmp(key, "blocks_per_sm") == 0) {
+        if (value < 0 || value > 32) return fail("blocks_per_sm must be 0 (as many as fit) .. 32");
+        h->q_bps_cap = value;
     } else if (strcmp(key, "block_warps") == 0) {
         if (value != 2 && value != 4 && value != 8) return fail("block_warps must be 2, 4 or 8");
         if (h->q_sync == 0 && value != 8) return fail("block_warps 2 or 4 needs lockstep 1 or 2");
