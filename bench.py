@@ -20,7 +20,9 @@ Arms and extras
   a bounded CPU sample of the reference algorithm (the C oracle, BLKSIZE 50 with the
   stiffness reordering) on the host cores -> ``cpu_baseline``; the differentiable
   1-hour window on 100x100x35 cells (forward and discrete-adjoint times) ->
-  ``adjoint``; EBI against ROS3 on a 100x100x10 grid -> ``ebi``.
+  ``adjoint``; EBI against ROS3 on a 100x100x10 grid -> ``ebi``; the CONUS grid with
+  skewed stiffness (30 % plume columns), batched against plain -> ``skewed``; CRACMM2 on
+  200x200x25 cells, batched hour and adjoint window -> ``cracmm2``.
 * --impl reference: the reference algorithm (C oracle; the Fortran cannot be
   compiled here) on all host cores, bounded sample per step.
 
@@ -232,7 +234,7 @@ def run_autotune(workload: str, seed: int, device: int) -> dict:
     return res
 
 
-def run_adjoint(device: int, nsync: int = STEPS_PER_HOUR) -> dict:
+def run_adjoint(device: int, nsync: int = STEPS_PER_HOUR, dims=(100, 100, 35)) -> dict:
     """The differentiable 1-hour window on 100x100x35 cells: forward (checkpointed) and
     backward (discrete adjoint) of L = sum of surface O3 wrt initial concentrations,
     per-reaction log rate multipliers and emission tendencies."""
@@ -240,7 +242,7 @@ def run_adjoint(device: int, nsync: int = STEPS_PER_HOUR) -> dict:
     from cmaq_gb300.adjoint import Ros3Window
     from cmaq_gb300.chem import ChemSolver
     from cmaq_gb300.synthetic import make_grid, manifest, solver_inputs
-    g = make_grid(seed=2018, ncols=100, nrows=100, nlays=35)
+    g = make_grid(seed=2018, ncols=dims[0], nrows=dims[1], nlays=dims[2])
     gs = ChemSolver(g.mech, ncols=g.ncols, nrows=g.nrows, nlays=g.nlays, nspcsd=g.nspcsd,
                     cgrid_index=g.cgrid_index, rtol=RTOL, atol=ATOL, device=device)
     y0, rki, night = solver_inputs(g, gs)
@@ -269,12 +271,80 @@ def run_adjoint(device: int, nsync: int = STEPS_PER_HOUR) -> dict:
         emis.grad = None
     fwd, bwd = times[-1]
     s.close()
-    return {"workload": f"cb6r5_ae7_aq 100x100x35 ({n} cells), {nsync} x 5-min steps, solver level "
+    return {"workload": f"cb6r5_ae7_aq {dims[0]}x{dims[1]}x{dims[2]} ({n} cells), {nsync} x 5-min steps, solver level "
                         "(rates from CALC_RCONST of the grid, fixed over the hour)",
             "loss": "sum of O3 over the surface layer at the end of the hour",
             "gradients": "initial concentrations, 349 log rate multipliers, emission tendencies",
             "forward_ms": fwd, "backward_ms": bwd, "backward_over_forward": bwd / fwd,
             "total_over_forward": (fwd + bwd) / fwd}
+
+
+def run_skewed(device: int, steps: int, tuned) -> dict:
+    """Config with skewed stiffness: the CONUS grid with 10x NOx/VOC plumes in 30 % of the
+    columns; batched (tuned, graph-replayed) against the plain per-cell kernel."""
+    from cmaq_gb300.synthetic import make_grid
+    g = make_grid(seed=2018, **WORKLOADS["conus_skewed"])
+    b = run_device(g, "queue", steps, 1, None, device, sample_clocks=False, tuned=tuned, graph=True)
+    p = run_device(g, "static", steps, 1, None, device, sample_clocks=False)
+    bv = g.ncell / (STEPS_PER_HOUR * b["ms_total"] / steps / 1e3)
+    pv = g.ncell / (STEPS_PER_HOUR * p["ms_total"] / steps / 1e3)
+    att = sum(st["accepted_steps"] + st["rejected_steps"] for st in b["stats"]) / g.ncell / steps
+    return {"workload": f"cb6r5_ae7_aq {g.ncols}x{g.nrows}x{g.nlays} ({g.ncell} cells), 30 % of columns with "
+                        f"10x NOx/VOC, {steps} x 5-min CHEM calls from the initial state",
+            "batched_value": bv, "plain_value": pv, "batched_over_plain": bv / pv,
+            "step_attempts_per_cell": att}
+
+
+def run_cracmm2(device: int, steps: int) -> dict:
+    """The larger mechanism on 200x200x25 cells: batched CHEM hour, then the differentiable
+    window (forward with checkpoints, backward) on the same grid within a 180 GB budget."""
+    import torch
+    from cmaq_gb300.adjoint import Ros3Window
+    from cmaq_gb300.chem import ChemSolver
+    from cmaq_gb300.synthetic import make_grid, manifest, solver_inputs
+    g = make_grid(mech="cracmm2", seed=2018, ncols=200, nrows=200, nlays=25)
+    b = run_device(g, "queue", steps, 1, None, device, sample_clocks=False, graph=True)
+    out = {"workload": f"cracmm2 200x200x25 ({g.ncell} cells), {steps} x 5-min calls",
+           "batched_value": g.ncell / (STEPS_PER_HOUR * b["ms_total"] / steps / 1e3),
+           "batched_ms_per_step": b["ms_total"] / steps}
+    gs = ChemSolver(g.mech, ncols=g.ncols, nrows=g.nrows, nlays=g.nlays, nspcsd=g.nspcsd,
+                    cgrid_index=g.cgrid_index, rtol=RTOL, atol=ATOL, device=device)
+    y0, rki, night = solver_inputs(g, gs)
+    gs.close()
+    n = g.ncell
+    s = ChemSolver(g.mech, ncols=n, nrows=1, nlays=1, nspcsd=g.nspcsd, rtol=RTOL, atol=ATOL, device=device)
+    ckpt = steps * s.info.ischan * n * 8
+    budget = 180 << 30
+    tape_mb = max(1024, (budget - ckpt - (16 << 30)) >> 20)   # 16 GB for inputs, gradients, workspaces
+    s.set_tuning(adjoint_tape_mb=int(tape_mb))
+    names = [sp["name"] for sp in manifest(g.mech)["species"]]
+    io3 = s.iold2new[names.index("O3")]
+    nsurf = g.ncols * g.nrows
+    logk = torch.zeros(s.info.nrxns, dtype=torch.float64, device=y0.device, requires_grad=True)
+    emis = torch.zeros_like(y0).requires_grad_(True)
+    times = []
+    for nsync in (1, steps):      # one-step pass first: allocates the first (largest) step's tape
+        w = Ros3Window(s, rki, night, nsync, 5.0)
+        a = y0.clone().requires_grad_(True)
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        torch.cuda.synchronize(device)
+        e0.record()
+        y = w(a, logk, emis)
+        e1.record()
+        y[io3, :nsurf].sum().backward()
+        e2.record()
+        torch.cuda.synchronize(device)
+        times.append((e0.elapsed_time(e1), e1.elapsed_time(e2)))
+        logk.grad = None
+        emis.grad = None
+    fwd, bwd = times[-1]
+    peak = torch.cuda.max_memory_allocated(device)
+    s.close()
+    out.update({"adjoint_forward_ms": fwd, "adjoint_backward_ms": bwd, "adjoint_backward_over_forward": bwd / fwd,
+                "adjoint_total_over_forward": (fwd + bwd) / fwd,
+                "adjoint_memory": f"checkpoints {ckpt / 2**30:.1f} GiB, tape budget {tape_mb / 1024:.1f} GiB "
+                                  f"(180 GB total budget), torch peak {peak / 2**30:.1f} GiB"})
+    return out
 
 
 def run_ebi(device: int, steps: int) -> dict:
@@ -305,30 +375,37 @@ def max_over_ranks(x: float, dist) -> float:
     return float(t.item())
 
 
-def cpu_reference(workload_cells: int, steps: int, warmup: int, threads: int, target_s: float = 20.0):
-    """The reference algorithm (C oracle: BLKSIZE 50, stiffness reordering) on host cores, on a
-    sample grid drawn from the same distributions; K calls from the initial state after W calls."""
+def cpu_reference(workload_cells: int, steps: int, warmup: int, threads: int, target_s: float = 20.0,
+                  solver: str = "ros3"):
+    """The reference algorithm (C oracle: ROS3 with BLKSIZE 50 and the stiffness reordering,
+    or EBI) on host cores, on a sample grid drawn from the same distributions; K calls from
+    the initial state after W calls."""
     sys.path.insert(0, str(ROOT / "oracle"))
     from oracle import Oracle
     from cmaq_gb300.synthetic import make_grid
     o = Oracle("cb6r5_ae7_aq")
     rt, at = float(np.float32(RTOL)), float(np.float32(ATOL))
+
+    def call(g, conc=None):
+        if solver == "ebi":
+            return o.chem_ebi(g, threads=threads, conc=conc)
+        return o.chem(g, blksize=50, rtol=rt, atol=at, threads=threads, conc=conc)
     # size the sample so that the timed calls take about target_s
     ncols = 20
     g = make_grid(ncols=ncols, nrows=10, nlays=10, seed=2018)
     t0 = time.perf_counter()
-    c, _ = o.chem(g, blksize=50, rtol=rt, atol=at, threads=threads)
+    c, _ = call(g)
     first = time.perf_counter() - t0
     est_hour = first * 3.0            # later calls are cheaper than the first
     scale = max(1, min(64, int(target_s / max(est_hour, 1e-3))))
     g = make_grid(ncols=ncols * scale, nrows=10, nlays=10, seed=2018)
     conc = g.conc.copy()
     for _ in range(warmup):
-        conc, _ = o.chem(g, blksize=50, rtol=rt, atol=at, threads=threads, conc=conc)
+        conc, _ = call(g, conc)
     conc = g.conc.copy()
     t0 = time.perf_counter()
     for _ in range(steps):
-        conc, _ = o.chem(g, blksize=50, rtol=rt, atol=at, threads=threads, conc=conc)
+        conc, _ = call(g, conc)
     wall = time.perf_counter() - t0
     value = g.ncell / (STEPS_PER_HOUR * wall / steps)
     return {"value": value, "cells": g.ncell, "wall_s": wall, "steps": steps}
@@ -354,6 +431,11 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-ebi", action="store_true")
+    ap.add_argument("--no-skewed", action="store_true")
+    ap.add_argument("--no-cracmm2", action="store_true")
+    ap.add_argument("--adjoint-dims", default="100x100x35", help="grid of the adjoint window, NCOLSxNROWSxNLAYS")
+    ap.add_argument("--only-adjoint", action="store_true",
+                    help="time only the adjoint window and print its own line (for profiling)")
     ap.add_argument("--solver", default="ros3", choices=["ros3", "ebi"],
                     help="solver of the timed CHEM calls (the metric is quoted for ros3)")
     a = ap.parse_args()
@@ -395,6 +477,15 @@ def main():
         cbuild.build()
         _lib.lib.cache_clear()
     info, _ = _lib.mech_info("cb6r5_ae7_aq")
+    adims = tuple(int(x) for x in a.adjoint_dims.split("x"))
+    if a.only_adjoint:
+        r = run_adjoint(device, a.steps, adims)
+        if rank == 0:
+            print(json.dumps({"metric": "ROS3 CB6r5 adjoint/forward time", "value": r["backward_over_forward"],
+                              "unit": "backward time / forward time", "n_gpus": 1, "steps": a.steps,
+                              "warmup": 1, "ms_per_step": (r["forward_ms"] + r["backward_ms"]) / a.steps,
+                              "higher_is_better": False, "dtype": "f64", "data": "synthetic", "adjoint": r}))
+        return 0
     peak_tf, _ = _lib.fp64_peak(device)
 
     tuned = None if a.no_autotune else run_autotune(a.workload, 2018 + rank, device)
@@ -430,12 +521,20 @@ def main():
     if rank == 0 and not a.no_cpu:
         thr = host_threads()
         r = cpu_reference(ncell, STEPS_PER_HOUR, 0, thr, target_s=15.0)
+        r1 = cpu_reference(ncell, STEPS_PER_HOUR, 0, 1, target_s=8.0)
+        re = cpu_reference(ncell, STEPS_PER_HOUR, 0, thr, target_s=8.0, solver="ebi")
         cpu = {"value": r["value"], "unit": UNIT, "cores": thr, "kind": "port",
                "sample": f"{r['cells']} cells of the same distributions x {r['steps']} CHEM calls "
-                         f"(reference algorithm, BLKSIZE 50 + reordering, C restatement, {r['wall_s']:.1f} s)"}
+                         f"(reference algorithm, BLKSIZE 50 + reordering, C restatement, {r['wall_s']:.1f} s)",
+               "single_core_value": r1["value"],
+               "single_core_sample": f"{r1['cells']} cells x {r1['steps']} calls, 1 thread",
+               "ebi_value": re["value"],
+               "ebi_sample": f"{re['cells']} cells x {re['steps']} EBI CHEM calls, {thr} threads"}
 
-    adjoint = None if (a.no_adjoint or rank != 0) else run_adjoint(device)
+    adjoint = None if (a.no_adjoint or rank != 0) else run_adjoint(device, STEPS_PER_HOUR, adims)
     ebi = None if (a.no_ebi or rank != 0) else run_ebi(device, a.steps)
+    skewed = None if (a.no_skewed or rank != 0) else run_skewed(device, a.steps, tuned)
+    cracmm2 = None if (a.no_cracmm2 or rank != 0) else run_cracmm2(device, a.steps)
 
     traffic = traffic_note = None
     tfile = ROOT / "profiles" / "traffic_per_step.json"
@@ -475,6 +574,8 @@ def main():
             "batched_over_plain": None if plain is None else value / plain["value"],
             "adjoint": adjoint,
             "ebi": ebi,
+            "skewed": skewed,
+            "cracmm2": cracmm2,
             "e2e": e2e,
             "cpu_baseline": cpu,
             "clocks": batched["clocks"],

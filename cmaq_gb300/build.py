@@ -23,7 +23,8 @@ BUILD = PKG / "_build"
 LIB = BUILD / "libcmaqchem.so"
 # build variants the autotuner can choose from: name -> extra nvcc flags
 VARIANTS = {"r255": [], "r168": ["-maxrregcount=168"], "r128": ["-maxrregcount=128"],
-            "lucs": ["-DCHEM_LDLU(p)=__ldcs(p)"]}
+            "lucs": ["-DCHEM_LDLU(p)=__ldcs(p)"], "pf": ["-DCHEM_USE_PREFETCH"],
+            "pf168": ["-DCHEM_USE_PREFETCH", "-maxrregcount=168"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-rdc=true", "-fmad=false", "-lineinfo", "-Xcompiler", "-fPIC",
               "-Xptxas", "-O3"]

@@ -49,8 +49,11 @@ struct Args {
     const double* kmult;           // [nrxns] rate multipliers, or nullptr (1)
     const double* emis;            // [ischan][ncell] emission tendencies (ppm/min), or nullptr (0)
     const uint8_t* night;          // [ncell] 1: night reaction list
-    const int* order;              // queue order, or nullptr for 0..ncell-1
+    const int* order;              // queue order, or nullptr for cell0, cell0 + 1, ...
     unsigned long long* head;      // queue head, zero before the launch
+    long long queue_len;           // cells in the queue (0: ncell)
+    long long cell0;               // first cell when order is nullptr
+    long long tape_base;           // tape entry of tape_off == tape_base (a batch's first entry)
     // forward
     const double* y_in;            // [ischan][ncell] state at the start of the step
     double* y_out;                 // [ischan][ncell] state at its end, or nullptr
@@ -92,6 +95,7 @@ __device__ __forceinline__ bool refill(const Args& a, long long& cell, bool& got
 {
     const int lane = threadIdx.x & 31;
     got = false;
+    const unsigned long long qlen = (unsigned long long)(a.queue_len > 0 ? a.queue_len : a.ncell);
     const unsigned need = __ballot_sync(0xffffffffu, cell < 0);
     if (!need) return false;
     const int leader = __ffs(need) - 1;
@@ -100,12 +104,12 @@ __device__ __forceinline__ bool refill(const Args& a, long long& cell, bool& got
     base = __shfl_sync(0xffffffffu, base, leader);
     if (cell < 0) {
         const unsigned long long pos = base + __popc(need & ((1u << lane) - 1u));
-        if (pos < (unsigned long long)a.ncell) {
-            cell = a.order ? a.order[pos] : (long long)pos;
+        if (pos < qlen) {
+            cell = a.order ? a.order[pos] : a.cell0 + (long long)pos;
             got = true;
         }
     }
-    return __any_sync(0xffffffffu, base + __popc(need) >= (unsigned long long)a.ncell);
+    return __any_sync(0xffffffffu, base + __popc(need) >= qlen);
 }
 
 // One synchronisation step of every cell.  Without tape_off: records the accepted steps
@@ -131,7 +135,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_adj_forward(Args a)
                 cnight = a.night[cell] != 0;
                 ros3::start(s);
                 if (taping) {
-                    base = a.tape_off[cell];
+                    base = a.tape_off[cell] - a.tape_base;
                     cap = a.nsteps[cell];
                     written = -1;
                 }
@@ -260,7 +264,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_adj_reverse(Args a)
                     ws[(M::ADJ_GE + i) * 32] = 0.0;
                 }
                 cnight = a.night[cell] != 0;
-                base = a.tape_off[cell];
+                base = a.tape_off[cell] - a.tape_base;
                 left = a.nsteps[cell];
             }
         }

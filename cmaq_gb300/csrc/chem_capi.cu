@@ -8,6 +8,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -114,6 +115,7 @@ struct cmaqchem_handle {
     int* d_adj_status = nullptr;
     size_t adj_cell_cap = 0, adj_status_cap = 0;
     unsigned long long* d_adj_counters = nullptr;
+    size_t adj_tape_budget = 0;        // bytes; 0: as large as the largest step needs and fits
     // captured CHEM call of cmaqchem_steps_device
     cudaGraphExec_t graph_exec = nullptr;
     GraphKey graph_key{};
@@ -332,6 +334,10 @@ extern "C" int cmaqchem_diag_set_tuning(cmaqchem_handle* h, const char* key, int
         if (value < 0 || value > 2) return fail("lockstep must be 0, 1 or 2");
         if (value == 0 && h->q_wpb != 8) return fail("lockstep 0 needs block_warps 8");
         h->q_sync = value;
+    } else if (strcmp(key, "adjoint_tape_mb") == 0) {
+        if (value < 0) return fail("adjoint_tape_mb must be >= 0");
+        h->adj_tape_budget = (size_t)value << 20;
+        return 0;
     } else if (strcmp(key, "blocks_per_sm") == 0) {
         if (value < 0 || value > 32) return fail("blocks_per_sm must be 0 (as many as fit) .. 32");
         h->q_bps_cap = value;
@@ -737,40 +743,88 @@ extern "C" int cmaqchem_adj_backward(cmaqchem_handle* h, long long ncell, double
         if (t < 0) return fail("negative step count");
         tmax = t > tmax ? t : tmax;
     }
-    if ((size_t)tmax > h->tape_cap) {
+    // tape capacity: the largest step's tape, or the budget (then steps run in cell batches)
+    const size_t entry_bytes = (size_t)(h->ops->ischan + 1) * sizeof(double);
+    size_t want = (size_t)tmax;
+    if (h->adj_tape_budget > 0) want = std::min(want, std::max<size_t>(1, h->adj_tape_budget / entry_bytes));
+    if (want > h->tape_cap || (h->adj_tape_budget > 0 && h->tape_cap * entry_bytes > h->adj_tape_budget)) {
         if (h->d_tape_y) CK(cudaFree(h->d_tape_y));
         if (h->d_tape_h) CK(cudaFree(h->d_tape_h));
         h->d_tape_y = nullptr;
         h->d_tape_h = nullptr;
         h->tape_cap = 0;
-        const size_t bytes = (size_t)tmax * h->ops->ischan * sizeof(double);
-        cudaError_t e = cudaMalloc(&h->d_tape_y, bytes);
-        if (e != cudaSuccess)
-            return fail("adjoint tape of " + std::to_string(bytes >> 20) + " MiB does not fit: " +
-                        cudaGetErrorString(e));
-        CK(cudaMalloc(&h->d_tape_h, (size_t)tmax * sizeof(double)));
-        h->tape_cap = (size_t)tmax;
+        for (;;) {   // without a budget, halve the request until it fits in free memory
+            cudaError_t e = cudaMalloc(&h->d_tape_y, want * h->ops->ischan * sizeof(double));
+            if (e == cudaSuccess) e = cudaMalloc(&h->d_tape_h, want * sizeof(double));
+            if (e == cudaSuccess) break;
+            cudaGetLastError();
+            if (h->d_tape_y) cudaFree(h->d_tape_y);
+            h->d_tape_y = nullptr;
+            if (h->adj_tape_budget > 0 || want < 1024)
+                return fail("adjoint tape of " + std::to_string((want * entry_bytes) >> 20) +
+                            " MiB does not fit: " + cudaGetErrorString(e));
+            want /= 2;
+        }
+        h->tape_cap = want;
     }
     CK(cudaMemsetAsync(h->d_adj_counters, 0, 3 * sizeof(unsigned long long), s));
     const size_t plane = (size_t)h->ops->ischan * ncell;
+    std::vector<long long> off;
+    std::vector<int> nst;
     for (int k = nsync - 1; k >= 0; --k) {
         adj::Args a = adj_args(h, ncell, rki + (size_t)k * rki_sync_stride, night, kmult, emis, chemstep_min);
         a.nsteps = const_cast<int*>(nsteps) + (size_t)k * ncell;
         a.tape_off = h->d_tape_off + (size_t)k * ncell;
         a.tape_y = h->d_tape_y;
         a.tape_h = h->d_tape_h;
-        if (adj_order(h, a.nsteps, ncell, s)) return -1;
-        a.order = h->d_adj_order;
-        // re-run the step from its checkpoint, recording the tape
         a.y_in = checkpoints + (size_t)k * plane;
-        CK(cudaMemsetAsync(h->d_head, 0, sizeof(unsigned long long), s));
-        CK(h->ops->adj_forward(a, h->adj_nblocks, s));
-        // reverse sweep
-        a.lam = lambda;
-        a.grad_logk = grad_logk;
-        a.grad_emis = grad_emis;
-        CK(cudaMemsetAsync(h->d_head, 0, sizeof(unsigned long long), s));
-        CK(h->ops->adj_reverse(a, h->adj_nblocks, s));
+        a.lam = nullptr;
+        // batches of consecutive cells whose tapes fit the capacity (one batch if the step fits)
+        std::vector<std::pair<long long, long long>> batches;
+        if ((size_t)tot[k] <= h->tape_cap) {
+            batches.push_back({0, ncell});
+        } else {
+            off.resize(ncell);
+            nst.resize(ncell);
+            CK(cudaMemcpyAsync(off.data(), a.tape_off, sizeof(long long) * ncell, cudaMemcpyDeviceToHost, s));
+            CK(cudaMemcpyAsync(nst.data(), a.nsteps, sizeof(int) * ncell, cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            long long c0 = 0;
+            while (c0 < ncell) {
+                if ((size_t)nst[c0] > h->tape_cap) return fail("one cell's tape exceeds the adjoint tape budget");
+                long long c1 = c0 + 1;
+                while (c1 < ncell && (size_t)(off[c1] + nst[c1] - off[c0]) <= h->tape_cap) ++c1;
+                batches.push_back({c0, c1});
+                c0 = c1;
+            }
+        }
+        for (const auto& bt : batches) {
+            const bool whole = bt.first == 0 && bt.second == ncell;
+            if (whole) {
+                if (adj_order(h, a.nsteps, ncell, s)) return -1;
+                a.order = h->d_adj_order;
+                a.queue_len = 0;
+                a.cell0 = 0;
+                a.tape_base = 0;
+            } else {
+                a.order = nullptr;
+                a.queue_len = bt.second - bt.first;
+                a.cell0 = bt.first;
+                a.tape_base = off[bt.first];
+            }
+            // re-run the step from its checkpoint, recording the tape
+            a.lam = nullptr;
+            a.grad_logk = nullptr;
+            a.grad_emis = nullptr;
+            CK(cudaMemsetAsync(h->d_head, 0, sizeof(unsigned long long), s));
+            CK(h->ops->adj_forward(a, h->adj_nblocks, s));
+            // reverse sweep
+            a.lam = lambda;
+            a.grad_logk = grad_logk;
+            a.grad_emis = grad_emis;
+            CK(cudaMemsetAsync(h->d_head, 0, sizeof(unsigned long long), s));
+            CK(h->ops->adj_reverse(a, h->adj_nblocks, s));
+        }
     }
     unsigned long long cnt[3];
     CK(cudaMemcpyAsync(cnt, h->d_adj_counters, sizeof(cnt), cudaMemcpyDeviceToHost, s));

@@ -9,6 +9,16 @@
 #ifndef CHEM_LDLU
 #define CHEM_LDLU(p) (*(p))
 #endif
+// L2 prefetch of workspace entries a few rows ahead (build variant 'pf'); off by default
+#ifdef CHEM_USE_PREFETCH
+__device__ __forceinline__ void chem_prefetch_l2(const double* p)
+{
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(p)));
+}
+#define CHEM_PREFETCH(p) chem_prefetch_l2(p)
+#else
+#define CHEM_PREFETCH(p) ((void)0)
+#endif
 namespace mech_cb6r5_ae7_aq {
 constexpr const char* NAME = "cb6r5_ae7_aq";
 constexpr int NSPEC = 149;

@@ -148,6 +148,16 @@ def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src
                   "#endif",
                   "// load of an LU factor or 1/U(i,i); a build may define it as a streaming load (__ldcs)",
                   "#ifndef CHEM_LDLU", "#define CHEM_LDLU(p) (*(p))", "#endif",
+                  "// L2 prefetch of workspace entries a few rows ahead (build variant 'pf'); off by default",
+                  "#ifdef CHEM_USE_PREFETCH",
+                  "__device__ __forceinline__ void chem_prefetch_l2(const double* p)",
+                  "{",
+                  '    asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(p)));',
+                  "}",
+                  "#define CHEM_PREFETCH(p) chem_prefetch_l2(p)",
+                  "#else",
+                  "#define CHEM_PREFETCH(p) ((void)0)",
+                  "#endif",
                   f"namespace {ns_name} {{", f'constexpr const char* NAME = "{mech}";']
     consts = (("NSPEC", ns), ("NRXNS", nr), ("ISCHAN", n), ("NPHOTAB", m.nphotab),
               ("NHETERO", m.nhetero), ("WS_ELEMS", lay.total), ("OFF_Y", lay.y), ("OFF_YP", lay.yp),
@@ -330,12 +340,26 @@ def _jacdecomp_chunks(m: Mechanism, sp: SparseMech, lay: Layout, d: int) -> list
     n = sp.ischan
     jpt = sp.jarraypt[d]
     terms = _jac_terms(m, sp, d)
+    # workspace elements each row reads (Jacobian terms, earlier rows' U, 1/U(k,k))
+    reads = []
+    for i in range(n):
+        r_set = []
+        cols = [j for (_, j) in sp.lower[d][i]] + [i] + [j for (_, j) in sp.upper[d][i]]
+        for j in cols:
+            for (r, ial, _, _) in terms.get(jpt[(i, j)], []):
+                r_set.append(lay.rki + r if m.nreact[r] == 1 else lay.ex[(r, ial)])
+        for (_, k) in sp.lower[d][i]:
+            r_set.append(lay.vdiag + k)
+            r_set.extend(lay.lu + st for (st, _) in sp.upper[d][k])
+        reads.append(list(dict.fromkeys(r_set)))
     rows_code = []
     for i in range(n):
         lower = sp.lower[d][i]
         upper = sp.upper[d][i]
         cols = [j for (_, j) in lower] + [i] + [j for (_, j) in upper]
         o = [f"    {{ // row {i}"]
+        if i + PREFETCH_AHEAD < n:
+            o.extend(f"      CHEM_PREFETCH(ws + {e * 32});" for e in reads[i + PREFETCH_AHEAD])
         nops = 0
         for j in cols:
             st = jpt[(i, j)]
@@ -394,22 +418,32 @@ def _jacdecomp_chunks(m: Mechanism, sp: SparseMech, lay: Layout, d: int) -> list
 
 
 SOLVE_CHUNK_TERMS = 800
+PREFETCH_AHEAD = 2      # rows ahead whose workspace reads a row prefetches (variant 'pf')
 
 
 def _solve_chunks(sp: SparseMech, lay: Layout, d: int) -> list[list[str]]:
     """Forward then backward substitution in place at ws[rhs] (rbsolve.F); each row
     sums its terms in the reference's column order."""
     n = sp.ischan
+    # rows in sweep order with the LU elements each reads
+    sweep = [("L", i, [lay.lu + st for (st, _) in sp.lower[d][i]]) for i in range(n)]
+    sweep += [("U", i, [lay.lu + st for (st, _) in sp.upper[d][i]] + [lay.vdiag + i]) for i in range(n - 1, -1, -1)]
+    ahead = {}
+    for q in range(len(sweep) - PREFETCH_AHEAD):
+        ahead[(sweep[q][0], sweep[q][1])] = sweep[q + PREFETCH_AHEAD][2]
+
+    def pf(kind, i):
+        return [f"      CHEM_PREFETCH(ws + {e * 32});" for e in ahead.get((kind, i), [])]
     pieces = []
     for i in range(n):
-        o = ["    {", f"      double x = b[{i * 32}];"]
+        o = ["    {"] + pf("L", i) + [f"      double x = b[{i * 32}];"]
         for (st, j) in sp.lower[d][i]:
             o.append(f"      x = fma(-CHEM_LDLU(lu + {st * 32}), b[{j * 32}], x);")
         o.append(f"      b[{i * 32}] = x;")
         o.append("    }")
         pieces.append((len(sp.lower[d][i]) + 1, o))
     for i in range(n - 1, -1, -1):
-        o = ["    {", f"      double x = b[{i * 32}];"]
+        o = ["    {"] + pf("U", i) + [f"      double x = b[{i * 32}];"]
         for (st, j) in sp.upper[d][i]:
             o.append(f"      x = fma(-CHEM_LDLU(lu + {st * 32}), b[{j * 32}], x);")
         o.append(f"      b[{i * 32}] = x * CHEM_LDLU(vd + {i * 32});")

@@ -61,7 +61,7 @@ def load(mech: str = "cb6r5_ae7_aq") -> C.CDLL:
                                         C.c_double, dp, ip, dp, dp, C.c_int]
     lib.oracle_adj_replay.argtypes = [C.c_long, dp, dp, C.c_long, u8p, dp, dp, C.c_int, ip, dp, C.c_int, C.c_int]
     lib.oracle_adj_replay.restype = None
-    lib.oracle_ddm3d_window.argtypes = [C.c_long, dp, dp, C.c_long, u8p, dp, C.c_int, C.c_double, C.c_double,
+    lib.oracle_ddm3d_window.argtypes = [C.c_long, dp, dp, C.c_long, u8p, dp, dp, C.c_int, C.c_double, C.c_double,
                                         C.c_double, C.c_int, ip, ip, dp, C.c_int]
     lib.oracle_set_dtmin.argtypes = [C.c_double]
     lib.oracle_get_dtmin.restype = C.c_double
@@ -251,21 +251,24 @@ class AdjointWindow:
 
 
 def ddm3d_window(o: "Oracle", y0, rki, night, nsync: int, chemstep: float, rtol: float, atol: float, params,
-                 kmult=None, threads: int = 0):
+                 kmult=None, emis=None, threads: int = 0):
     """First-order DDM-3D sensitivities (CMAQ's SOLVE_DDM3D_CHEM restated) over a window.
-    params: list of ("init", species index in solver order) or ("rate", reaction index).
+    params: list of ("init", species index in solver order), ("rate", reaction index) or
+    ("emis", species index: the emission tendency of that species in every cell).
     Returns (y_end, s_end [nparam, nspec, n])."""
     y = np.array(y0, np.float64, order="C", copy=True)
     rki = np.ascontiguousarray(rki, np.float64)
     stride = 0 if rki.ndim == 2 else rki.shape[1] * rki.shape[2]
     night = np.ascontiguousarray(night, np.uint8)
     n = y.shape[1]
-    kind = np.array([0 if k == "init" else 1 for k, _ in params], np.int32)
+    kind = np.array([{"init": 0, "rate": 1, "emis": 2}[k] for k, _ in params], np.int32)
     idx = np.array([i for _, i in params], np.int32)
     s_end = np.zeros((len(params), o.nspec, n))
     km = None if kmult is None else np.ascontiguousarray(kmult, np.float64)
+    em = None if emis is None else np.ascontiguousarray(emis, np.float64)
     bad = o.lib.oracle_ddm3d_window(n, _p(y, C.c_double), _p(rki, C.c_double), stride, _p(night, C.c_uint8),
-                                    _opt(km, C.c_double), nsync, chemstep, rtol, atol, len(params),
+                                    _opt(km, C.c_double), _opt(em, C.c_double), nsync, chemstep, rtol, atol,
+                                    len(params),
                                     _p(kind, C.c_int), _p(idx, C.c_int), _p(s_end, C.c_double), threads)
     if bad:
         raise RuntimeError(f"{bad} failed cell-steps in the DDM-3D window")

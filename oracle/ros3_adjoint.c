@@ -471,11 +471,14 @@ static void lu_solve(const double* m, const int* piv, int n, double* b)
 }
 
 /* DDM-3D over a window.  Parameters: kind[p] = 0 initial condition of species idx[p]
- * (solver order), 1 log rate multiplier of reaction idx[p].  Returns s_end[p][nspec][n]
- * and the end state in y (the forward is the oracle's rbsolver). */
+ * (solver order), 1 log rate multiplier of reaction idx[p], 2 emission tendency of
+ * species idx[p] (dF/dp = unit vector, the source DDM-3D adds for an emission
+ * parameter; here the emission enters f, so DT times it is the step's source).  emis
+ * [nspec][n] (or NULL) is the emission tendency of the forward.  Returns
+ * s_end[p][nspec][n] and the end state in y (the forward is the oracle's rbsolver). */
 int oracle_ddm3d_window(long n, double* y, const double* rki, long rki_stride, const uint8_t* night,
-                        const double* kmult, int nsync, double chemstep, double rtol, double atol, int nparam,
-                        const int* kind, const int* idx, double* s_end, int threads)
+                        const double* kmult, const double* emis, int nsync, double chemstep, double rtol,
+                        double atol, int nparam, const int* kind, const int* idx, double* s_end, int threads)
 {
     int nbad = 0;
     const int ns = MECH_ISCHAN;
@@ -491,7 +494,7 @@ int oracle_ddm3d_window(long n, double* y, const double* rki, long rki_stride, c
         double* am = malloc(sizeof(double) * ns * ns);
         int* piv = malloc(sizeof(int) * ns);
         double* sv = malloc(sizeof(double) * ns * (nparam > 0 ? nparam : 1));
-        double yave[MECH_NSPEC], tmp[MECH_NSPEC], src[MECH_NSPEC];
+        double yave[MECH_NSPEC], tmp[MECH_NSPEC], src[MECH_NSPEC], ebuf[MECH_NSPEC];
         SolverCfg cfg = {rtol, atol, (double)(1.0f / (float)MECH_NSPEC), 100000};
 #ifdef _OPENMP
 #pragma omp for schedule(dynamic, 4)
@@ -502,10 +505,7 @@ int oracle_ddm3d_window(long n, double* y, const double* rki, long rki_stride, c
                 for (int s = 0; s < ns; ++s) sv[p * ns + s] = (kind[p] == 0 && idx[p] == s) ? 1.0 : 0.0;
             const int ncsp = night[c] ? 1 : 0;
             for (int k = 0; k < nsync; ++k) {
-                for (int r = 0; r < MECH_NRXNS; ++r) {
-                    const double kk = rki[(size_t)k * rki_stride + (size_t)r * n + c];
-                    b.rki[r] = kmult ? kk * kmult[r] : kk;
-                }
+                load_cell(&b, n, c, rki + (size_t)k * rki_stride, kmult, emis, ebuf);
                 memset(yave, 0, sizeof(yave));
                 b.yave = yave;
                 SolverStats st = oracle_rbsolver(&b, ncsp, chemstep, &cfg, NULL);
@@ -526,6 +526,8 @@ int oracle_ddm3d_window(long n, double* y, const double* rki, long rki_stride, c
                         for (int i = 0; i < mech_nreact[r]; ++i) rate *= yave[a[i]];
                         for (int i = 0; i < mech_nreact[r]; ++i) src[a[i]] -= chemstep * rate;
                         for (int q = 0; q < mech_nprdct[r]; ++q) src[a[3 + q]] += chemstep * rate * mech_sc[r * MECH_MXPRD + q];
+                    } else if (kind[p] == 2) {
+                        src[idx[p]] = chemstep;
                     }
                     for (int i = 0; i < ns; ++i) {
                         double t = sp[i];

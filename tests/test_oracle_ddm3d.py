@@ -6,7 +6,8 @@ a 1-hour window (12 x 5-min synchronisation steps) that starts from a spun-up st
 DDM-3D advances sensitivities once per synchronisation step with a Crank-Nicolson-type
 update on time-averaged concentrations, an approximation of its own, so agreement is
 bounded by its accuracy: measured 3e-5 to 1.1e-2 relative here (initial-condition and
-rate-constant parameters); tolerance 2e-2.  From the unspun seeded state DDM-3D's
+rate-constant parameters; tolerance 2e-2) and 4e-5 to 1.4e-3 for NOx and VOC
+emission-tendency parameters (tolerance 1e-2).  From the unspun seeded state DDM-3D's
 update is far coarser in the first step (NOx initial-condition sensitivities off by
 up to 90% in CRACMM2) while the adjoint still matches finite differences, which is
 why the window starts after the spin-up.
@@ -43,3 +44,29 @@ def test_adjoint_agrees_with_ddm3d(mech):
         ddm = float((wt * s[p]).sum())
         adj = float(lam[i].sum()) if kind == "init" else float(gk[i])
         assert abs(adj - ddm) <= 2e-2 * abs(adj), (kind, i, adj, ddm)
+
+
+@pytest.mark.parametrize("mech", ["cb6r5_ae7_aq", "cracmm2"])
+def test_emission_gradients_agree_with_ddm3d(mech):
+    """NOx and VOC emission-tendency sensitivities (measured agreement 4e-5 to 1.4e-3)."""
+    from oracle import AdjointWindow, Oracle, ddm3d_window
+    o = Oracle(mech)
+    names = [sp["name"] for sp in manifest(mech)["species"]]
+    g = make_grid(mech=mech, ncols=4, nrows=3, nlays=1, seed=51, het=True)
+    y0, rki, night = gather_cells(g, o)
+    y1 = AdjointWindow(o, rki, night, 12, 5.0, RTOL, ATOL, threads=2).forward(y0)
+    emis = np.zeros_like(y1)
+    emis[o.iold2new[names.index("NO")]] = 1e-6
+    w = AdjointWindow(o, rki, night, 12, 5.0, RTOL, ATOL, emis=emis, threads=2)
+    yend = w.forward(y1)
+    wt = np.zeros_like(y1)
+    wt[o.iold2new[names.index("O3")]] = 1.0
+    _, _, ge = w.backward(wt)
+    voc = [s for s in ("FORM", "ALD2", "ISOP", "HCHO") if s in names][:2]
+    params = [("emis", int(o.iold2new[names.index(s)])) for s in ["NO", "NO2"] + voc]
+    yd, s = ddm3d_window(o, y1, rki, night, 12, 5.0, RTOL, ATOL, params, emis=emis, threads=2)
+    assert np.array_equal(yd, yend)
+    for p, (_, i) in enumerate(params):
+        ddm = float((wt * s[p]).sum())
+        adj = float(ge[i].sum())
+        assert abs(adj - ddm) <= 1e-2 * abs(adj), (i, adj, ddm)
