@@ -20,9 +20,10 @@ Arms and extras
   a bounded CPU sample of the reference algorithm (the C oracle, BLKSIZE 50 with the
   stiffness reordering) on the host cores -> ``cpu_baseline``; the differentiable
   1-hour window on 100x100x35 cells (forward and discrete-adjoint times) ->
-  ``adjoint``; EBI against ROS3 on a 100x100x10 grid -> ``ebi``; the CONUS grid with
-  skewed stiffness (30 % plume columns), batched against plain -> ``skewed``; CRACMM2 on
-  200x200x25 cells, batched hour and adjoint window -> ``cracmm2``.
+  ``adjoint``; EBI against ROS3 on a 100x100x10 grid -> ``ebi``; with --all-configs also
+  the CONUS grid with skewed stiffness (30 % plume columns), batched against plain ->
+  ``skewed``, and CRACMM2 on 200x200x25 cells, batched hour and adjoint window ->
+  ``cracmm2``.
 * --impl reference: the reference algorithm (C oracle; the Fortran cannot be
   compiled here) on all host cores, bounded sample per step.
 
@@ -207,8 +208,11 @@ def run_e2e(g, steps: int, warmup: int, dist, device: int):
         h["conc"][...] = conc0
         s.step(*args, tstep=TSTEP)
     h["conc"][...] = conc0
-    h2d = sum(a.nbytes for a in args)
-    d2h = h["conc"].nbytes
+    # the call copies the mechanism's CGRID planes (not all NSPCSD) and the other inputs
+    plane = h["conc"].nbytes // g.nspcsd
+    nplanes = len(set(int(c) for c in g.cgrid_index))
+    h2d = nplanes * plane + sum(a.nbytes for a in args[1:])
+    d2h = nplanes * plane
     barrier(dist)
     t0 = time.perf_counter()
     for _ in range(steps):
@@ -431,8 +435,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-ebi", action="store_true")
-    ap.add_argument("--no-skewed", action="store_true")
-    ap.add_argument("--no-cracmm2", action="store_true")
+    ap.add_argument("--all-configs", action="store_true",
+                    help="also time the skewed-stiffness CONUS grid and CRACMM2 on 1M cells (about 5 more minutes)")
     ap.add_argument("--adjoint-dims", default="100x100x35", help="grid of the adjoint window, NCOLSxNROWSxNLAYS")
     ap.add_argument("--only-adjoint", action="store_true",
                     help="time only the adjoint window and print its own line (for profiling)")
@@ -533,8 +537,8 @@ def main():
 
     adjoint = None if (a.no_adjoint or rank != 0) else run_adjoint(device, STEPS_PER_HOUR, adims)
     ebi = None if (a.no_ebi or rank != 0) else run_ebi(device, a.steps)
-    skewed = None if (a.no_skewed or rank != 0) else run_skewed(device, a.steps, tuned)
-    cracmm2 = None if (a.no_cracmm2 or rank != 0) else run_cracmm2(device, a.steps)
+    skewed = run_skewed(device, a.steps, tuned) if (a.all_configs and rank == 0) else None
+    cracmm2 = run_cracmm2(device, a.steps) if (a.all_configs and rank == 0) else None
 
     traffic = traffic_note = None
     tfile = ROOT / "profiles" / "traffic_per_step.json"

@@ -56,6 +56,8 @@ def lib(variant: str = "r255") -> C.CDLL:
                                        C.POINTER(Stats)]
     L.cmaqchem_steps_device.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, C.c_int, C.c_int, ip, C.c_int, vp,
                                         C.POINTER(Stats)]
+    L.cmaqchem_step_ddm_device.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, C.c_int, C.c_int, ip, vp, C.c_int,
+                                           vp, vp, vp, C.POINTER(Stats)]
     L.cmaqchem_cell_stats.argtypes = [vp, vp, vp]
     L.cmaqchem_ros3_solve_device.argtypes = [vp, C.c_longlong, vp, vp, vp, C.c_double, vp, vp, vp, vp]
     L.cmaqchem_ebi_solve_device.argtypes = [vp, C.c_longlong, vp, vp, C.c_int, vp, vp, vp]

@@ -7,7 +7,10 @@ size, registers) and on the grid's stiffness mix.  The tuner times a few CHEM ca
 of a sample of the grid for each candidate:
 
 * cells per block: 64, 128 or 256 (``block_warps`` 2, 4, 8; one cell per thread);
-* register cap: library variants r255 (none), r168, r128 (``cmaq_gb300.build``);
+* register cap and prefetch: library variants of ``cmaq_gb300.build`` (the default
+  library caps the generated functions at 168 registers and prefetches workspace rows;
+  ``nopf`` without the prefetch, ``full255`` neither (8 warps per SM), ``r168`` caps
+  every function);
 * queue granularity: whether the block's warps pass barriers between the phases of
   each step attempt (``lockstep`` 1), also between the generated chunks of the LU
   and the solves (2), or run free (0, 256-cell blocks only); a lane always refills
@@ -42,7 +45,7 @@ class Candidate:
         return {"block_warps": self.block_warps, "lockstep": self.lockstep}
 
 
-def candidates(variants=("r255", "r168", "r128")) -> list[Candidate]:
+def candidates(variants=("r255", "nopf", "full255", "r168")) -> list[Candidate]:
     out = []
     for v in variants:
         out.append(Candidate(v, 0, 8))
@@ -53,10 +56,11 @@ def candidates(variants=("r255", "r168", "r128")) -> list[Candidate]:
 
 
 def available_variants(build_missing: bool = False) -> list[str]:
+    """Built library variants (the default library always; others if built)."""
     from . import build as cbuild
     have = []
     for v in cbuild.VARIANTS:
-        if v == "lucs":
+        if v in ("lucs", "pf255", "r128"):
             continue
         if cbuild.lib_path(v).exists():
             have.append(v)

@@ -21,10 +21,25 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = BUILD / "libcmaqchem.so"
-# build variants the autotuner can choose from: name -> extra nvcc flags
-VARIANTS = {"r255": [], "r168": ["-maxrregcount=168"], "r128": ["-maxrregcount=128"],
-            "lucs": ["-DCHEM_LDLU(p)=__ldcs(p)"], "pf": ["-DCHEM_USE_PREFETCH"],
-            "pf168": ["-DCHEM_USE_PREFETCH", "-maxrregcount=168"]}
+# Build variants the autotuner can choose from: name -> (extra nvcc flags of the generated
+# mechanism code, extra flags of every translation unit).  The default ("r255" is the name
+# of the default library) caps the generated LU / solve / rate functions at 168 registers
+# and turns on their L2 prefetch a few rows ahead; together with the work-queue kernel's
+# launch bounds (12 resident warps per SM) this measured fastest.  The EBI routines and the
+# kernels themselves are not capped.
+GEN_DEFAULT = ["-maxrregcount=168", "-DCHEM_USE_PREFETCH"]
+Q8 = "-DCHEM_QUEUE_WARPS_PER_SM=8"
+VARIANTS = {"r255": (GEN_DEFAULT, []),
+            "nopf": (["-maxrregcount=168"], []),
+            "full255": ([], [Q8]), "pf255": (["-DCHEM_USE_PREFETCH"], [Q8]),
+            "r168": ([], ["-maxrregcount=168"]),
+            "r128": ([], ["-maxrregcount=128", "-DCHEM_QUEUE_WARPS_PER_SM=16"]),
+            "lucs": ([], ["-DCHEM_LDLU(p)=__ldcs(p)", Q8])}
+
+
+def _is_generated_math(src: Path) -> bool:
+    """Generated mechanism functions (rates, LU, solves, adjoint), not the EBI routines."""
+    return src.parent.name == "gen" and not src.name.endswith("_ebi.cu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-rdc=true", "-fmad=false", "-lineinfo", "-Xcompiler", "-fPIC",
               "-Xptxas", "-O3"]
@@ -57,7 +72,7 @@ def build(jobs: int | None = None, verbose: bool = False, variant: str = "r255")
     out_dir = BUILD if variant == "r255" else BUILD / variant
     out_dir.mkdir(parents=True, exist_ok=True)
     lib = lib_path(variant)
-    extra = list(VARIANTS[variant])
+    gen_extra, all_extra = (list(x) for x in VARIANTS[variant])
     nvcc = _nvcc()
     hdr_mtime = max(p.stat().st_mtime for p in _headers())
     todo, objs = [], []
@@ -71,6 +86,7 @@ def build(jobs: int | None = None, verbose: bool = False, variant: str = "r255")
 
     def compile_one(item):
         src, obj = item
+        extra = all_extra + (gen_extra if _is_generated_math(src) else [])
         cmd = [nvcc, *ARCH, *NVCC_FLAGS, *extra, "-I", str(CSRC), "-c", str(src), "-o", str(obj) + ".tmp"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

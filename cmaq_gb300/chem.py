@@ -143,6 +143,28 @@ class ChemSolver:
         check(rc, self._L)
         return st.as_dict()
 
+    def step_ddm(self, sengrid, conc, ta, qv, dens, pres, seaice, ocean_szone, rj, khetero, rate_mask=None,
+                 region=None, jdate: int = 2018182, jtime: int = 0, tstep=(10000, 500, 500), stream=None) -> dict:
+        """One CHEM call on CUDA tensors that also advances DDM-3D sensitivities: sengrid
+        [nspcsd, nparam, nlays, nrows, ncols] float32 (SENGRID(C,R,L,NP,SPC)); rate_mask
+        [nparam, nrxns] uint8 marks reaction-rate parameters' reactions; region [nparam, ...cells]
+        float32 weights (IREGION)."""
+        args = [conc, ta, qv, dens, pres, seaice, ocean_szone, rj, khetero]
+        if not all(_is_torch(a) for a in args) or not _is_torch(sengrid):
+            raise ChemError("step_ddm() takes CUDA tensors")
+        self._check_shapes(*args)
+        nparam = int(sengrid.shape[1])
+        if tuple(sengrid.shape) != (self.nspcsd, nparam) + self.shape or "float32" not in str(sengrid.dtype):
+            raise ChemError(f"sengrid must be float32 [{self.nspcsd}, nparam, {self.shape}]")
+        if rate_mask is not None and tuple(rate_mask.shape) != (nparam, self.info.nrxns):
+            raise ChemError("rate_mask must be [nparam, nrxns] uint8")
+        st = _lib.Stats()
+        s = C.c_void_p(stream.cuda_stream) if stream is not None else None
+        rc = self._L.cmaqchem_step_ddm_device(self._h, *[_ptr(a) for a in args], jdate, jtime, tstep_array(tstep),
+                                              _ptr(sengrid), nparam, _ptr(rate_mask), _ptr(region), s, C.byref(st))
+        check(rc, self._L)
+        return st.as_dict()
+
     def steps(self, nsteps: int, conc, ta, qv, dens, pres, seaice, ocean_szone, rj, khetero, jdate: int = 2018182,
               jtime: int = 0, tstep=(10000, 500, 500), stream=None) -> dict:
         """``nsteps`` consecutive CHEM calls on CUDA tensors, replayed from one captured

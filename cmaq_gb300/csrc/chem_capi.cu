@@ -67,6 +67,7 @@ struct cmaqchem_handle {
     const MechOps* ops = nullptr;
     cmaqchem_cfg cfg{};
     std::vector<int> cgrid_index;   // 0-based
+    std::vector<int> conc_planes;   // distinct CGRID planes of the mechanism's species, ascending
     int device = 0, nsm = 0, bps = 1, nblocks = 0;
     long long ncell = 0;
     int ncolrow = 0;
@@ -116,6 +117,7 @@ struct cmaqchem_handle {
     size_t adj_cell_cap = 0, adj_status_cap = 0;
     unsigned long long* d_adj_counters = nullptr;
     size_t adj_tape_budget = 0;        // bytes; 0: as large as the largest step needs and fits
+    double* d_yave = nullptr;          // DDM-3D: time-averaged concentrations of the call
     // captured CHEM call of cmaqchem_steps_device
     cudaGraphExec_t graph_exec = nullptr;
     GraphKey graph_key{};
@@ -131,7 +133,7 @@ void free_handle(cmaqchem_handle* h)
                     h->d_counters, h->d_order, h->d_hist, h->d_cursor, h->d_head, h->s_conc, h->s_ta,
                     h->s_qv, h->s_dens, h->s_pres, h->s_seaice, h->s_osz, h->s_rj, h->s_khet,
                     h->d_adj_ws, h->d_tape_y, h->d_tape_h, h->d_tape_off, h->d_tiles, h->d_tape_tot,
-                    h->d_adj_order, h->d_adj_status, h->d_adj_counters};
+                    h->d_adj_order, h->d_adj_status, h->d_adj_counters, h->d_yave};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
@@ -261,6 +263,9 @@ extern "C" int cmaqchem_init(const cmaqchem_cfg* cfg, cmaqchem_handle** out)
         }
         h->cgrid_index[s] = ci;
     }
+    h->conc_planes = h->cgrid_index;
+    std::sort(h->conc_planes.begin(), h->conc_planes.end());
+    h->conc_planes.erase(std::unique(h->conc_planes.begin(), h->conc_planes.end()), h->conc_planes.end());
     std::vector<float> fwd(m->nspec);
     std::vector<double> rev(m->nspec);
     for (int s = 0; s < m->nspec; ++s) {   // rbinit.F:252-253, REAL(4)
@@ -436,6 +441,39 @@ extern "C" int cmaqchem_step_device(cmaqchem_handle* h, float* conc, const float
     return step_device_impl(h, conc, ta, qv, dens, pres, seaice, ocean_szone, rj, khetero, tstep, s, stats);
 }
 
+extern "C" int cmaqchem_step_ddm_device(cmaqchem_handle* h, float* conc, const float* ta, const float* qv,
+                                        const float* dens, const float* pres, const float* seaice,
+                                        const float* ocean_szone, const float* rj, const double* khetero,
+                                        int jdate, int jtime, const int tstep[3], float* sengrid, int nparam,
+                                        const unsigned char* rate_mask, const float* region, void* stream,
+                                        cmaqchem_stats* stats)
+{
+    (void)jdate;
+    (void)jtime;
+    if (!h) return fail("null handle");
+    if (h->cfg.solver != CMAQCHEM_SOLVER_ROS3) return fail("DDM-3D is available with the ROS3 solver");
+    if (nparam <= 0 || !sengrid) return fail("DDM-3D needs sengrid and nparam > 0");
+    const void* ptrs[] = {conc, ta, qv, dens, pres, seaice, ocean_szone, rj, tstep, khetero};
+    if (check_ptrs(ptrs, h->ops->nhetero > 0 ? 10 : 9)) return -1;
+    const int itmstep = hhmmss_to_sec(tstep[1]);
+    if (itmstep <= 0) return fail("TSTEP(2) must be a positive HHMMSS interval");
+    CK(cudaSetDevice(h->device));
+    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    if (!h->d_yave) CK(cudaMalloc(&h->d_yave, sizeof(double) * h->ops->ischan * h->ncell));
+    chem::GridArgs a = grid_args(h, conc, ta, qv, dens, pres, seaice, ocean_szone, rj, khetero,
+                                 (double)itmstep / 60.0);
+    a.yave = h->d_yave;
+    CK(cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned long long) * 5, s));
+    CK(cudaEventRecord(h->ev0, s));
+    if (enqueue_step(h, a, itmstep, s, h->have_history)) return -1;
+    chem::DdmArgs d{sengrid, nparam, rate_mask, region, h->d_yave};
+    a.counters = nullptr;
+    a.cell_status = nullptr;
+    a.cell_steps = nullptr;
+    CK(h->ops->ddm_update(a, d, h->nblocks, s));
+    return finish_steps(h, s, stats);
+}
+
 extern "C" int cmaqchem_steps_device(cmaqchem_handle* h, float* conc, const float* ta, const float* qv,
                                      const float* dens, const float* pres, const float* seaice,
                                      const float* ocean_szone, const float* rj, const double* khetero, int jdate,
@@ -504,7 +542,10 @@ extern "C" int cmaqchem_step(cmaqchem_handle* h, float* conc, const float* ta, c
         CK(cudaMalloc(&h->s_khet, sizeof(double) * nc * (h->ops->nhetero > 0 ? h->ops->nhetero : 1)));
     }
     cudaStream_t s = h->stream;
-    CK(cudaMemcpyAsync(h->s_conc, conc, sizeof(float) * nconc, cudaMemcpyHostToDevice, s));
+    // only the mechanism's CGRID planes are read and written by CHEM
+    for (int p : h->conc_planes)
+        CK(cudaMemcpyAsync(h->s_conc + (size_t)p * nc, conc + (size_t)p * nc, sizeof(float) * nc,
+                           cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(h->s_ta, ta, sizeof(float) * nc, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(h->s_qv, qv, sizeof(float) * nc, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(h->s_dens, dens, sizeof(float) * nc, cudaMemcpyHostToDevice, s));
@@ -517,7 +558,9 @@ extern "C" int cmaqchem_step(cmaqchem_handle* h, float* conc, const float* ta, c
     const int rc = step_device_impl(h, h->s_conc, h->s_ta, h->s_qv, h->s_dens, h->s_pres, h->s_seaice, h->s_osz,
                                     h->s_rj, h->s_khet, tstep, s, stats);
     if (rc < 0) return rc;
-    CK(cudaMemcpyAsync(conc, h->s_conc, sizeof(float) * nconc, cudaMemcpyDeviceToHost, s));
+    for (int p : h->conc_planes)
+        CK(cudaMemcpyAsync(conc + (size_t)p * nc, h->s_conc + (size_t)p * nc, sizeof(float) * nc,
+                           cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     return rc;
 }

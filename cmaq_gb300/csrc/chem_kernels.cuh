@@ -58,7 +58,15 @@ struct GridArgs {
     unsigned long long* counters;  // [5]: accepted steps, rejected steps, failed cells, sunlit cells,
                                    //      step attempts of sunlit cells
     int use_night;                 // 1: all-dark warps use the night pattern; 0: day pattern always
+    double* yave;                  // [ischan][ncell] time-averaged Y of the call (DDM-3D), or nullptr
 };
+
+// DDM-3D: the cell's time-averaged concentrations (rbsolver.F:592-595) to a.yave
+template <class M>
+__device__ __forceinline__ void store_yave(const GridArgs& a, long long c, const double* __restrict__ ws)
+{
+    for (int i = 0; i < M::ISCHAN; ++i) a.yave[(size_t)i * a.ncell + c] = ws[(M::OFF_YAVE + i) * 32] / a.chemstep;
+}
 
 template <class M>
 __device__ __forceinline__ double* warp_ws(double* ws_all, long long warp_global)
@@ -129,8 +137,9 @@ __global__ void __launch_bounds__(THREADS_PER_BLOCK, 1) k_chem_ros3(GridArgs a)
         if (active) sun = gather_cell<M>(a, c, ws);
         const bool night = a.use_night && __all_sync(0xffffffffu, !sun);
         if (active) {
-            ros3::CellStats st = ros3::integrate<M>(ws, a.chemstep, a.tol, night, a.max_iter);
+            ros3::CellStats st = ros3::integrate<M>(ws, a.chemstep, a.tol, night, a.max_iter, a.yave != nullptr);
             scatter_cell<M>(a, c, ws);
+            if (a.yave) store_yave<M>(a, c, ws);
             acc_steps += st.nsteps;
             rej_steps += st.nfails;
             failed += st.status != ros3::ST_OK;

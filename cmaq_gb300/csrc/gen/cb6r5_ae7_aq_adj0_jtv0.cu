@@ -14,14 +14,14 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[4608];
       const double kw = ws[33376] * w;
       out[4608] = out[4608] + kw;
-      ws[169856] = fma(kw, y[4608], ws[169856]);
+      ws[174624] = fma(kw, y[4608], ws[174624]);
     }
     {
       double w = 1.0 * phi[4320];
       w = w - phi[4160];
       const double kw = ws[33408] * w;
       out[4160] = out[4160] + kw;
-      ws[169888] = fma(kw, y[4160], ws[169888]);
+      ws[174656] = fma(kw, y[4160], ws[174656]);
     }
     {
       double w = 1.0 * phi[4608];
@@ -30,7 +30,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[33440] * w;
       out[4320] = fma(kw, y[4384], out[4320]);
       out[4384] = fma(kw, y[4320], out[4384]);
-      ws[169920] = fma(kw * y[4320], y[4384], ws[169920]);
+      ws[174688] = fma(kw * y[4320], y[4384], ws[174688]);
     }
     {
       double w = 1.0 * phi[4608];
@@ -39,7 +39,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[33472] * w;
       out[4160] = fma(kw, y[4384], out[4160]);
       out[4384] = fma(kw, y[4160], out[4384]);
-      ws[169952] = fma(kw * y[4160], y[4384], ws[169952]);
+      ws[174720] = fma(kw * y[4160], y[4384], ws[174720]);
     }
     {
       double w = 1.0 * phi[4384];
@@ -48,7 +48,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[33504] * w;
       out[4160] = fma(kw, y[4608], out[4160]);
       out[4608] = fma(kw, y[4160], out[4608]);
-      ws[169984] = fma(kw * y[4160], y[4608], ws[169984]);
+      ws[174752] = fma(kw * y[4160], y[4608], ws[174752]);
     }
     {
       double w = 1.0 * phi[4640];
@@ -57,7 +57,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[33536] * w;
       out[4160] = fma(kw, y[4608], out[4160]);
       out[4608] = fma(kw, y[4160], out[4608]);
-      ws[170016] = fma(kw * y[4160], y[4608], ws[170016]);
+      ws[174784] = fma(kw * y[4160], y[4608], ws[174784]);
     }
     {
       double w = -phi[4160];
@@ -65,35 +65,35 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[33568] * w;
       out[4160] = fma(kw, y[4320], out[4160]);
       out[4320] = fma(kw, y[4160], out[4320]);
-      ws[170048] = fma(kw * y[4160], y[4320], ws[170048]);
+      ws[174816] = fma(kw * y[4160], y[4320], ws[174816]);
     }
     {
       double w = 1.0 * phi[4160];
       w = w - phi[4320];
       const double kw = ws[33600] * w;
       out[4320] = out[4320] + kw;
-      ws[170080] = fma(kw, y[4320], ws[170080]);
+      ws[174848] = fma(kw, y[4320], ws[174848]);
     }
     {
       double w = 1.0 * phi[672];
       w = w - phi[4320];
       const double kw = ws[33632] * w;
       out[4320] = out[4320] + kw;
-      ws[170112] = fma(kw, y[4320], ws[170112]);
+      ws[174880] = fma(kw, y[4320], ws[174880]);
     }
     {
       double w = 1.0 * phi[4160];
       w = w - phi[672];
       const double kw = ws[33664] * w;
       out[672] = out[672] + kw;
-      ws[170144] = fma(kw, y[672], ws[170144]);
+      ws[174912] = fma(kw, y[672], ws[174912]);
     }
     {
       double w = 2.0 * phi[4736];
       w = w - phi[672];
       const double kw = ws[33696] * w;
       out[672] = out[672] + kw;
-      ws[170176] = fma(kw, y[672], ws[170176]);
+      ws[174944] = fma(kw, y[672], ws[174944]);
     }
     {
       double w = 1.0 * phi[4704];
@@ -102,7 +102,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[33728] * w;
       out[4320] = fma(kw, y[4736], out[4320]);
       out[4736] = fma(kw, y[4320], out[4736]);
-      ws[170208] = fma(kw * y[4320], y[4736], ws[170208]);
+      ws[174976] = fma(kw * y[4320], y[4736], ws[174976]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -111,7 +111,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[33760] * w;
       out[4320] = fma(kw, y[4704], out[4320]);
       out[4704] = fma(kw, y[4320], out[4704]);
-      ws[170240] = fma(kw * y[4320], y[4704], ws[170240]);
+      ws[175008] = fma(kw * y[4320], y[4704], ws[175008]);
     }
     {
       double w = 1.0 * phi[4704];
@@ -120,7 +120,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[33792] * w;
       out[4736] = fma(kw, y[4160], out[4736]);
       out[4160] = fma(kw, y[4736], out[4160]);
-      ws[170272] = fma(kw * y[4736], y[4160], ws[170272]);
+      ws[175040] = fma(kw * y[4736], y[4160], ws[175040]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -129,7 +129,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[33824] * w;
       out[4704] = fma(kw, y[4160], out[4704]);
       out[4160] = fma(kw, y[4704], out[4160]);
-      ws[170304] = fma(kw * y[4704], y[4160], ws[170304]);
+      ws[175072] = fma(kw * y[4704], y[4160], ws[175072]);
     }
     {
       double w = 1.0 * phi[4160];
@@ -138,7 +138,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[33856] * w;
       out[4736] = fma(kw, y[4736], out[4736]);
       out[4736] = fma(kw, y[4736], out[4736]);
-      ws[170336] = fma(kw * y[4736], y[4736], ws[170336]);
+      ws[175104] = fma(kw * y[4736], y[4736], ws[175104]);
     }
     {
       double w = 1.0 * phi[3456];
@@ -147,7 +147,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[33888] * w;
       out[4736] = fma(kw, y[4736], out[4736]);
       out[4736] = fma(kw, y[4736], out[4736]);
-      ws[170368] = fma(kw * y[4736], y[4736], ws[170368]);
+      ws[175136] = fma(kw * y[4736], y[4736], ws[175136]);
     }
     {
       double w = -phi[4736];
@@ -155,7 +155,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[33920] * w;
       out[4736] = fma(kw, y[4704], out[4736]);
       out[4704] = fma(kw, y[4736], out[4704]);
-      ws[170400] = fma(kw * y[4736], y[4704], ws[170400]);
+      ws[175168] = fma(kw * y[4736], y[4704], ws[175168]);
     }
     {
       double w = 1.0 * phi[3456];
@@ -164,7 +164,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[33952] * w;
       out[4704] = fma(kw, y[4704], out[4704]);
       out[4704] = fma(kw, y[4704], out[4704]);
-      ws[170432] = fma(kw * y[4704], y[4704], ws[170432]);
+      ws[175200] = fma(kw * y[4704], y[4704], ws[175200]);
     }
     {
       double w = 1.0 * phi[3456];
@@ -173,14 +173,14 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[33984] * w;
       out[4704] = fma(kw, y[4704], out[4704]);
       out[4704] = fma(kw, y[4704], out[4704]);
-      ws[170464] = fma(kw * y[4704], y[4704], ws[170464]);
+      ws[175232] = fma(kw * y[4704], y[4704], ws[175232]);
     }
     {
       double w = 2.0 * phi[4736];
       w = w - phi[3456];
       const double kw = ws[34016] * w;
       out[3456] = out[3456] + kw;
-      ws[170496] = fma(kw, y[3456], ws[170496]);
+      ws[175264] = fma(kw, y[3456], ws[175264]);
     }
     {
       double w = 1.0 * phi[4704];
@@ -189,7 +189,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[34048] * w;
       out[3456] = fma(kw, y[4736], out[3456]);
       out[4736] = fma(kw, y[3456], out[4736]);
-      ws[170528] = fma(kw * y[3456], y[4736], ws[170528]);
+      ws[175296] = fma(kw * y[3456], y[4736], ws[175296]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -199,7 +199,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[34080] * w;
       out[3456] = fma(kw, y[4160], out[3456]);
       out[4160] = fma(kw, y[3456], out[4160]);
-      ws[170560] = fma(kw * y[3456], y[4160], ws[170560]);
+      ws[175328] = fma(kw * y[3456], y[4160], ws[175328]);
     }
     {
       double w = 2.0 * phi[4608];
@@ -208,7 +208,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[34112] * w;
       out[4384] = fma(kw, y[4384], out[4384]);
       out[4384] = fma(kw, y[4384], out[4384]);
-      ws[170592] = fma(kw * y[4384], y[4384], ws[170592]);
+      ws[175360] = fma(kw * y[4384], y[4384], ws[175360]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -218,7 +218,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[34144] * w;
       out[4704] = fma(kw, y[4384], out[4704]);
       out[4384] = fma(kw, y[4704], out[4384]);
-      ws[170624] = fma(kw * y[4704], y[4384], ws[170624]);
+      ws[175392] = fma(kw * y[4704], y[4384], ws[175392]);
     }
     {
       double w = 1.0 * phi[4640];
@@ -227,7 +227,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[34176] * w;
       out[4608] = fma(kw, y[4320], out[4608]);
       out[4320] = fma(kw, y[4608], out[4320]);
-      ws[170656] = fma(kw * y[4608], y[4320], ws[170656]);
+      ws[175424] = fma(kw * y[4608], y[4320], ws[175424]);
     }
     {
       double w = 1.0 * phi[4608];
@@ -235,14 +235,14 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[4640];
       const double kw = ws[34208] * w;
       out[4640] = out[4640] + kw;
-      ws[170688] = fma(kw, y[4640], ws[170688]);
+      ws[175456] = fma(kw, y[4640], ws[175456]);
     }
     {
       double w = 1.0 * phi[4384];
       w = w - phi[4640];
       const double kw = ws[34240] * w;
       out[4640] = out[4640] + kw;
-      ws[170720] = fma(kw, y[4640], ws[170720]);
+      ws[175488] = fma(kw, y[4640], ws[175488]);
     }
     {
       double w = 2.0 * phi[4608];
@@ -251,7 +251,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[34272] * w;
       out[4640] = fma(kw, y[4384], out[4640]);
       out[4384] = fma(kw, y[4640], out[4384]);
-      ws[170752] = fma(kw * y[4640], y[4384], ws[170752]);
+      ws[175520] = fma(kw * y[4640], y[4384], ws[175520]);
     }
     {
       double w = 1.0 * phi[4384];
@@ -261,7 +261,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[34304] * w;
       out[4640] = fma(kw, y[4608], out[4640]);
       out[4608] = fma(kw, y[4640], out[4608]);
-      ws[170784] = fma(kw * y[4640], y[4608], ws[170784]);
+      ws[175552] = fma(kw * y[4640], y[4608], ws[175552]);
     }
     {
       double w = 1.0 * phi[4608];
@@ -270,7 +270,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[34336] * w;
       out[4640] = fma(kw, y[4160], out[4640]);
       out[4160] = fma(kw, y[4640], out[4160]);
-      ws[170816] = fma(kw * y[4640], y[4160], ws[170816]);
+      ws[175584] = fma(kw * y[4640], y[4160], ws[175584]);
     }
     {
       double w = 1.0 * phi[4704];
@@ -280,7 +280,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[34368] * w;
       out[4640] = fma(kw, y[4736], out[4640]);
       out[4736] = fma(kw, y[4640], out[4736]);
-      ws[170848] = fma(kw * y[4640], y[4736], ws[170848]);
+      ws[175616] = fma(kw * y[4640], y[4736], ws[175616]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -290,7 +290,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[34400] * w;
       out[4640] = fma(kw, y[4704], out[4640]);
       out[4704] = fma(kw, y[4640], out[4704]);
-      ws[170880] = fma(kw * y[4640], y[4704], ws[170880]);
+      ws[175648] = fma(kw * y[4640], y[4704], ws[175648]);
     }
     {
       double w = 1.0 * phi[4608];
@@ -299,7 +299,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[34432] * w;
       out[4640] = fma(kw, y[4320], out[4640]);
       out[4320] = fma(kw, y[4640], out[4320]);
-      ws[170912] = fma(kw * y[4640], y[4320], ws[170912]);
+      ws[175680] = fma(kw * y[4640], y[4320], ws[175680]);
     }
     {
       double w = 2.0 * phi[4608];
@@ -308,7 +308,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[34464] * w;
       out[4640] = fma(kw, y[4640], out[4640]);
       out[4640] = fma(kw, y[4640], out[4640]);
-      ws[170944] = fma(kw * y[4640], y[4640], ws[170944]);
+      ws[175712] = fma(kw * y[4640], y[4640], ws[175712]);
     }
     {
       double w = 1.0 * phi[1280];
@@ -317,7 +317,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[34496] * w;
       out[4640] = fma(kw, y[4608], out[4640]);
       out[4608] = fma(kw, y[4640], out[4608]);
-      ws[170976] = fma(kw * y[4640], y[4608], ws[170976]);
+      ws[175744] = fma(kw * y[4640], y[4608], ws[175744]);
     }
     {
       double w = 1.0 * phi[4640];
@@ -325,7 +325,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[1280];
       const double kw = ws[34528] * w;
       out[1280] = out[1280] + kw;
-      ws[171008] = fma(kw, y[1280], ws[171008]);
+      ws[175776] = fma(kw, y[1280], ws[175776]);
     }
     {
       double w = 1.0 * phi[4608];
@@ -333,14 +333,14 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[1280];
       const double kw = ws[34560] * w;
       out[1280] = out[1280] + kw;
-      ws[171040] = fma(kw, y[1280], ws[171040]);
+      ws[175808] = fma(kw, y[1280], ws[175808]);
     }
     {
       double w = 2.0 * phi[4192];
       w = w - phi[1280];
       const double kw = ws[34592] * w;
       out[1280] = out[1280] + kw;
-      ws[171072] = fma(kw, y[1280], ws[171072]);
+      ws[175840] = fma(kw, y[1280], ws[175840]);
     }
     {
       double w = 1.0 * phi[2464];
@@ -349,7 +349,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[34624] * w;
       out[4384] = fma(kw, y[4736], out[4384]);
       out[4736] = fma(kw, y[4384], out[4736]);
-      ws[171104] = fma(kw * y[4384], y[4736], ws[171104]);
+      ws[175872] = fma(kw * y[4384], y[4736], ws[175872]);
     }
     {
       double w = 2.0 * phi[2464];
@@ -358,7 +358,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[34656] * w;
       out[4384] = fma(kw, y[4608], out[4384]);
       out[4608] = fma(kw, y[4384], out[4608]);
-      ws[171136] = fma(kw * y[4384], y[4608], ws[171136]);
+      ws[175904] = fma(kw * y[4384], y[4608], ws[175904]);
     }
     {
       double w = 1.0 * phi[4384];
@@ -368,7 +368,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[34688] * w;
       out[2464] = fma(kw, y[2464], out[2464]);
       out[2464] = fma(kw, y[2464], out[2464]);
-      ws[171168] = fma(kw * y[2464], y[2464], ws[171168]);
+      ws[175936] = fma(kw * y[2464], y[2464], ws[175936]);
     }
     {
       double w = 1.0 * phi[4384];
@@ -376,7 +376,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[2464];
       const double kw = ws[34720] * w;
       out[2464] = out[2464] + kw;
-      ws[171200] = fma(kw, y[2464], ws[171200]);
+      ws[175968] = fma(kw, y[2464], ws[175968]);
     }
     {
       double w = 1.0 * phi[4608];
@@ -385,7 +385,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[34752] * w;
       out[2464] = fma(kw, y[4736], out[2464]);
       out[4736] = fma(kw, y[2464], out[4736]);
-      ws[171232] = fma(kw * y[2464], y[4736], ws[171232]);
+      ws[176000] = fma(kw * y[2464], y[4736], ws[176000]);
     }
     {
       double w = 1.0 * phi[4192];
@@ -394,7 +394,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[34784] * w;
       out[4608] = fma(kw, y[4736], out[4608]);
       out[4736] = fma(kw, y[4608], out[4736]);
-      ws[171264] = fma(kw * y[4608], y[4736], ws[171264]);
+      ws[176032] = fma(kw * y[4608], y[4736], ws[176032]);
     }
     {
       double w = 1.0 * phi[4640];
@@ -403,7 +403,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[34816] * w;
       out[4192] = fma(kw, y[4736], out[4192]);
       out[4736] = fma(kw, y[4192], out[4736]);
-      ws[171296] = fma(kw * y[4192], y[4736], ws[171296]);
+      ws[176064] = fma(kw * y[4192], y[4736], ws[176064]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -411,7 +411,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[4192];
       const double kw = ws[34848] * w;
       out[4192] = out[4192] + kw;
-      ws[171328] = fma(kw, y[4192], ws[171328]);
+      ws[176096] = fma(kw, y[4192], ws[176096]);
     }
     {
       double w = 1.0 * phi[1696];
@@ -420,7 +420,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[34880] * w;
       out[4704] = fma(kw, y[4608], out[4704]);
       out[4608] = fma(kw, y[4704], out[4608]);
-      ws[171360] = fma(kw * y[4704], y[4608], ws[171360]);
+      ws[176128] = fma(kw * y[4704], y[4608], ws[176128]);
     }
     {
       double w = 1.0 * phi[4704];
@@ -428,7 +428,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[1696];
       const double kw = ws[34912] * w;
       out[1696] = out[1696] + kw;
-      ws[171392] = fma(kw, y[1696], ws[171392]);
+      ws[176160] = fma(kw, y[1696], ws[176160]);
     }
     {
       double w = 0.59 * phi[4704];
@@ -438,7 +438,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[1696];
       const double kw = ws[34944] * w;
       out[1696] = out[1696] + kw;
-      ws[171424] = fma(kw, y[1696], ws[171424]);
+      ws[176192] = fma(kw, y[1696], ws[176192]);
     }
     {
       double w = 1.0 * phi[4608];
@@ -447,7 +447,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[34976] * w;
       out[1696] = fma(kw, y[4736], out[1696]);
       out[4736] = fma(kw, y[1696], out[4736]);
-      ws[171456] = fma(kw * y[1696], y[4736], ws[171456]);
+      ws[176224] = fma(kw * y[1696], y[4736], ws[176224]);
     }
     {
       double w = 1.0 * phi[256];
@@ -458,7 +458,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[35008] * w;
       out[2208] = fma(kw, y[4736], out[2208]);
       out[4736] = fma(kw, y[2208], out[4736]);
-      ws[171488] = fma(kw * y[2208], y[4736], ws[171488]);
+      ws[176256] = fma(kw * y[2208], y[4736], ws[176256]);
     }
     {
       double w = 1.0 * phi[4608];
@@ -469,7 +469,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[35040] * w;
       out[4448] = fma(kw, y[4384], out[4448]);
       out[4384] = fma(kw, y[4448], out[4384]);
-      ws[171520] = fma(kw * y[4448], y[4384], ws[171520]);
+      ws[176288] = fma(kw * y[4448], y[4384], ws[176288]);
     }
     {
       double w = 1.0 * phi[1344];
@@ -478,7 +478,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[35072] * w;
       out[4448] = fma(kw, y[4608], out[4448]);
       out[4608] = fma(kw, y[4448], out[4608]);
-      ws[171552] = fma(kw * y[4448], y[4608], ws[171552]);
+      ws[176320] = fma(kw * y[4448], y[4608], ws[176320]);
     }
     {
       double w = 1.0 * phi[4608];
@@ -486,7 +486,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[1344];
       const double kw = ws[35104] * w;
       out[1344] = out[1344] + kw;
-      ws[171584] = fma(kw, y[1344], ws[171584]);
+      ws[176352] = fma(kw, y[1344], ws[176352]);
     }
     {
       double w = 0.6 * phi[4608];
@@ -497,7 +497,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[1344];
       const double kw = ws[35136] * w;
       out[1344] = out[1344] + kw;
-      ws[171616] = fma(kw, y[1344], ws[171616]);
+      ws[176384] = fma(kw, y[1344], ws[176384]);
     }
 }
 __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int phioff, int outoff)
@@ -517,7 +517,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[35168] * w;
       out[4448] = fma(kw, y[4704], out[4448]);
       out[4704] = fma(kw, y[4448], out[4704]);
-      ws[171648] = fma(kw * y[4448], y[4704], ws[171648]);
+      ws[176416] = fma(kw * y[4448], y[4704], ws[176416]);
     }
     {
       double w = 1.0 * phi[4416];
@@ -526,7 +526,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[35200] * w;
       out[4448] = fma(kw, y[4672], out[4448]);
       out[4672] = fma(kw, y[4448], out[4672]);
-      ws[171680] = fma(kw * y[4448], y[4672], ws[171680]);
+      ws[176448] = fma(kw * y[4448], y[4672], ws[176448]);
     }
     {
       double w = 2.0 * phi[4416];
@@ -536,7 +536,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[35232] * w;
       out[4448] = fma(kw, y[4448], out[4448]);
       out[4448] = fma(kw, y[4448], out[4448]);
-      ws[171712] = fma(kw * y[4448], y[4448], ws[171712]);
+      ws[176480] = fma(kw * y[4448], y[4448], ws[176480]);
     }
     {
       double w = 1.0 * phi[4416];
@@ -548,7 +548,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[35264] * w;
       out[4448] = fma(kw, y[4096], out[4448]);
       out[4096] = fma(kw, y[4448], out[4096]);
-      ws[171744] = fma(kw * y[4448], y[4096], ws[171744]);
+      ws[176512] = fma(kw * y[4448], y[4096], ws[176512]);
     }
     {
       double w = 1.0 * phi[4608];
@@ -560,7 +560,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[35296] * w;
       out[4096] = fma(kw, y[4384], out[4096]);
       out[4384] = fma(kw, y[4096], out[4384]);
-      ws[171776] = fma(kw * y[4096], y[4384], ws[171776]);
+      ws[176544] = fma(kw * y[4096], y[4384], ws[176544]);
     }
     {
       double w = 1.0 * phi[1952];
@@ -569,7 +569,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[35328] * w;
       out[4096] = fma(kw, y[4608], out[4096]);
       out[4608] = fma(kw, y[4096], out[4608]);
-      ws[171808] = fma(kw * y[4096], y[4608], ws[171808]);
+      ws[176576] = fma(kw * y[4096], y[4608], ws[176576]);
     }
     {
       double w = 1.0 * phi[4608];
@@ -577,7 +577,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       w = w - phi[1952];
       const double kw = ws[35360] * w;
       out[1952] = out[1952] + kw;
-      ws[171840] = fma(kw, y[1952], ws[171840]);
+      ws[176608] = fma(kw, y[1952], ws[176608]);
     }
     {
       double w = 0.6 * phi[4608];
@@ -589,7 +589,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       w = w - phi[1952];
       const double kw = ws[35392] * w;
       out[1952] = out[1952] + kw;
-      ws[171872] = fma(kw, y[1952], ws[171872]);
+      ws[176640] = fma(kw, y[1952], ws[176640]);
     }
     {
       double w = 0.37 * phi[2688];
@@ -603,7 +603,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[35424] * w;
       out[4096] = fma(kw, y[4704], out[4096]);
       out[4704] = fma(kw, y[4096], out[4704]);
-      ws[171904] = fma(kw * y[4096], y[4704], ws[171904]);
+      ws[176672] = fma(kw * y[4096], y[4704], ws[176672]);
     }
     {
       double w = 1.0 * phi[4416];
@@ -612,7 +612,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[35456] * w;
       out[4096] = fma(kw, y[4672], out[4096]);
       out[4672] = fma(kw, y[4096], out[4672]);
-      ws[171936] = fma(kw * y[4096], y[4672], ws[171936]);
+      ws[176704] = fma(kw * y[4096], y[4672], ws[176704]);
     }
     {
       double w = 2.0 * phi[4416];
@@ -622,7 +622,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[35488] * w;
       out[4096] = fma(kw, y[4096], out[4096]);
       out[4096] = fma(kw, y[4096], out[4096]);
-      ws[171968] = fma(kw * y[4096], y[4096], ws[171968]);
+      ws[176736] = fma(kw * y[4096], y[4096], ws[176736]);
     }
     {
       double w = 1.0 * phi[4384];
@@ -631,7 +631,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[35520] * w;
       out[4672] = fma(kw, y[4384], out[4672]);
       out[4384] = fma(kw, y[4672], out[4384]);
-      ws[172000] = fma(kw * y[4672], y[4384], ws[172000]);
+      ws[176768] = fma(kw * y[4672], y[4384], ws[176768]);
     }
     {
       double w = 1.0 * phi[4704];
@@ -640,7 +640,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[35552] * w;
       out[4672] = fma(kw, y[4704], out[4672]);
       out[4704] = fma(kw, y[4672], out[4704]);
-      ws[172032] = fma(kw * y[4672], y[4704], ws[172032]);
+      ws[176800] = fma(kw * y[4672], y[4704], ws[176800]);
     }
     {
       double w = -phi[4672];
@@ -648,7 +648,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[35584] * w;
       out[4672] = fma(kw, y[4672], out[4672]);
       out[4672] = fma(kw, y[4672], out[4672]);
-      ws[172064] = fma(kw * y[4672], y[4672], ws[172064]);
+      ws[176832] = fma(kw * y[4672], y[4672], ws[176832]);
     }
     {
       double w = 1.0 * phi[4512];
@@ -659,7 +659,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[35616] * w;
       out[4416] = fma(kw, y[4384], out[4416]);
       out[4384] = fma(kw, y[4416], out[4384]);
-      ws[172096] = fma(kw * y[4416], y[4384], ws[172096]);
+      ws[176864] = fma(kw * y[4416], y[4384], ws[176864]);
     }
     {
       double w = 0.9 * phi[2272];
@@ -669,7 +669,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[35648] * w;
       out[4416] = fma(kw, y[4704], out[4416]);
       out[4704] = fma(kw, y[4416], out[4704]);
-      ws[172128] = fma(kw * y[4416], y[4704], ws[172128]);
+      ws[176896] = fma(kw * y[4416], y[4704], ws[176896]);
     }
     {
       double w = 1.0 * phi[4512];
@@ -682,7 +682,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[35680] * w;
       out[4416] = fma(kw, y[4448], out[4416]);
       out[4448] = fma(kw, y[4416], out[4448]);
-      ws[172160] = fma(kw * y[4416], y[4448], ws[172160]);
+      ws[176928] = fma(kw * y[4416], y[4448], ws[176928]);
     }
     {
       double w = 0.685 * phi[4512];
@@ -694,7 +694,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[35712] * w;
       out[4416] = fma(kw, y[4672], out[4416]);
       out[4672] = fma(kw, y[4416], out[4672]);
-      ws[172192] = fma(kw * y[4416], y[4672], ws[172192]);
+      ws[176960] = fma(kw * y[4416], y[4672], ws[176960]);
     }
     {
       double w = 1.0 * phi[4608];
@@ -704,7 +704,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[35744] * w;
       out[4576] = fma(kw, y[4384], out[4576]);
       out[4384] = fma(kw, y[4576], out[4384]);
-      ws[172224] = fma(kw * y[4576], y[4384], ws[172224]);
+      ws[176992] = fma(kw * y[4576], y[4384], ws[176992]);
     }
     {
       double w = 1.0 * phi[2880];
@@ -713,7 +713,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[35776] * w;
       out[4576] = fma(kw, y[4704], out[4576]);
       out[4704] = fma(kw, y[4576], out[4704]);
-      ws[172256] = fma(kw * y[4576], y[4704], ws[172256]);
+      ws[177024] = fma(kw * y[4576], y[4704], ws[177024]);
     }
     {
       double w = 0.8 * phi[4704];
@@ -725,7 +725,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[35808] * w;
       out[4576] = fma(kw, y[4448], out[4576]);
       out[4448] = fma(kw, y[4576], out[4448]);
-      ws[172288] = fma(kw * y[4576], y[4448], ws[172288]);
+      ws[177056] = fma(kw * y[4576], y[4448], ws[177056]);
     }
     {
       double w = 0.6 * phi[4704];
@@ -735,7 +735,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[35840] * w;
       out[4576] = fma(kw, y[4672], out[4576]);
       out[4672] = fma(kw, y[4576], out[4672]);
-      ws[172320] = fma(kw * y[4576], y[4672], ws[172320]);
+      ws[177088] = fma(kw * y[4576], y[4672], ws[177088]);
     }
     {
       double w = 1.0 * phi[4608];
@@ -744,7 +744,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[35872] * w;
       out[4352] = fma(kw, y[4384], out[4352]);
       out[4384] = fma(kw, y[4352], out[4384]);
-      ws[172352] = fma(kw * y[4352], y[4384], ws[172352]);
+      ws[177120] = fma(kw * y[4352], y[4384], ws[177120]);
     }
     {
       double w = 1.0 * phi[2880];
@@ -753,7 +753,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[35904] * w;
       out[4352] = fma(kw, y[4704], out[4352]);
       out[4704] = fma(kw, y[4352], out[4704]);
-      ws[172384] = fma(kw * y[4352], y[4704], ws[172384]);
+      ws[177152] = fma(kw * y[4352], y[4704], ws[177152]);
     }
     {
       double w = 0.8 * phi[4416];
@@ -764,7 +764,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[35936] * w;
       out[4352] = fma(kw, y[4448], out[4352]);
       out[4448] = fma(kw, y[4352], out[4448]);
-      ws[172416] = fma(kw * y[4352], y[4448], ws[172416]);
+      ws[177184] = fma(kw * y[4352], y[4448], ws[177184]);
     }
     {
       double w = 1.0 * phi[4672];
@@ -773,7 +773,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[35968] * w;
       out[4352] = fma(kw, y[4672], out[4352]);
       out[4672] = fma(kw, y[4352], out[4672]);
-      ws[172448] = fma(kw * y[4352], y[4672], ws[172448]);
+      ws[177216] = fma(kw * y[4352], y[4672], ws[177216]);
     }
     {
       double w = 0.5 * phi[3648];
@@ -783,7 +783,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[36000] * w;
       out[4288] = fma(kw, y[4384], out[4288]);
       out[4384] = fma(kw, y[4288], out[4384]);
-      ws[172480] = fma(kw * y[4288], y[4384], ws[172480]);
+      ws[177248] = fma(kw * y[4288], y[4384], ws[177248]);
     }
     {
       double w = 1.0 * phi[2880];
@@ -792,7 +792,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[36032] * w;
       out[4288] = fma(kw, y[4704], out[4288]);
       out[4704] = fma(kw, y[4288], out[4704]);
-      ws[172512] = fma(kw * y[4288], y[4704], ws[172512]);
+      ws[177280] = fma(kw * y[4288], y[4704], ws[177280]);
     }
     {
       double w = 0.8 * phi[4704];
@@ -804,7 +804,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[36064] * w;
       out[4288] = fma(kw, y[4448], out[4288]);
       out[4448] = fma(kw, y[4288], out[4448]);
-      ws[172544] = fma(kw * y[4288], y[4448], ws[172544]);
+      ws[177312] = fma(kw * y[4288], y[4448], ws[177312]);
     }
     {
       double w = 1.0 * phi[4672];
@@ -813,7 +813,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[36096] * w;
       out[4288] = fma(kw, y[4672], out[4288]);
       out[4672] = fma(kw, y[4288], out[4672]);
-      ws[172576] = fma(kw * y[4288], y[4672], ws[172576]);
+      ws[177344] = fma(kw * y[4288], y[4672], ws[177344]);
     }
     {
       double w = 0.6 * phi[4416];
@@ -825,7 +825,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[36128] * w;
       out[2272] = fma(kw, y[4736], out[2272]);
       out[4736] = fma(kw, y[2272], out[4736]);
-      ws[172608] = fma(kw * y[2272], y[4736], ws[172608]);
+      ws[177376] = fma(kw * y[2272], y[4736], ws[177376]);
     }
     {
       double w = 1.0 * phi[4416];
@@ -834,7 +834,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       w = w - phi[2272];
       const double kw = ws[36160] * w;
       out[2272] = out[2272] + kw;
-      ws[172640] = fma(kw, y[2272], ws[172640]);
+      ws[177408] = fma(kw, y[2272], ws[177408]);
     }
     {
       double w = 0.54 * phi[4576];
@@ -846,7 +846,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[36192] * w;
       out[2880] = fma(kw, y[4736], out[2880]);
       out[4736] = fma(kw, y[2880], out[4736]);
-      ws[172672] = fma(kw * y[2880], y[4736], ws[172672]);
+      ws[177440] = fma(kw * y[2880], y[4736], ws[177440]);
     }
     {
       double w = 1.0 * phi[4704];
@@ -854,7 +854,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       w = w - phi[2880];
       const double kw = ws[36224] * w;
       out[2880] = out[2880] + kw;
-      ws[172704] = fma(kw, y[2880], ws[172704]);
+      ws[177472] = fma(kw, y[2880], ws[177472]);
     }
     {
       double w = 1.0 * phi[4032];
@@ -863,14 +863,14 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[36256] * w;
       out[3648] = fma(kw, y[4736], out[3648]);
       out[4736] = fma(kw, y[3648], out[4736]);
-      ws[172736] = fma(kw * y[3648], y[4736], ws[172736]);
+      ws[177504] = fma(kw * y[3648], y[4736], ws[177504]);
     }
     {
       double w = 1.0 * phi[4608];
       w = w - phi[3648];
       const double kw = ws[36288] * w;
       out[3648] = out[3648] + kw;
-      ws[172768] = fma(kw, y[3648], ws[172768]);
+      ws[177536] = fma(kw, y[3648], ws[177536]);
     }
     {
       double w = 1.0 * phi[4704];
@@ -879,7 +879,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[36320] * w;
       out[3776] = fma(kw, y[4736], out[3776]);
       out[4736] = fma(kw, y[3776], out[4736]);
-      ws[172800] = fma(kw * y[3776], y[4736], ws[172800]);
+      ws[177568] = fma(kw * y[3776], y[4736], ws[177568]);
     }
     {
       double w = 1.0 * phi[4416];
@@ -889,7 +889,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[36352] * w;
       out[3904] = fma(kw, y[4736], out[3904]);
       out[4736] = fma(kw, y[3904], out[4736]);
-      ws[172832] = fma(kw * y[3904], y[4736], ws[172832]);
+      ws[177600] = fma(kw * y[3904], y[4736], ws[177600]);
     }
     {
       double w = 1.0 * phi[4448];
@@ -898,7 +898,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[36384] * w;
       out[2688] = fma(kw, y[4736], out[2688]);
       out[4736] = fma(kw, y[2688], out[4736]);
-      ws[172864] = fma(kw * y[2688], y[4736], ws[172864]);
+      ws[177632] = fma(kw * y[2688], y[4736], ws[177632]);
     }
     {
       double w = 1.0 * phi[4704];
@@ -908,7 +908,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[36416] * w;
       out[4512] = fma(kw, y[4736], out[4512]);
       out[4736] = fma(kw, y[4512], out[4736]);
-      ws[172896] = fma(kw * y[4512], y[4736], ws[172896]);
+      ws[177664] = fma(kw * y[4512], y[4736], ws[177664]);
     }
     {
       double w = 2.0 * phi[4704];
@@ -916,14 +916,14 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       w = w - phi[4512];
       const double kw = ws[36448] * w;
       out[4512] = out[4512] + kw;
-      ws[172928] = fma(kw, y[4512], ws[172928]);
+      ws[177696] = fma(kw, y[4512], ws[177696]);
     }
     {
       double w = 1.0 * phi[4480];
       w = w - phi[4512];
       const double kw = ws[36480] * w;
       out[4512] = out[4512] + kw;
-      ws[172960] = fma(kw, y[4512], ws[172960]);
+      ws[177728] = fma(kw, y[4512], ws[177728]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -934,7 +934,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[36512] * w;
       out[4512] = fma(kw, y[4160], out[4512]);
       out[4160] = fma(kw, y[4512], out[4160]);
-      ws[172992] = fma(kw * y[4512], y[4160], ws[172992]);
+      ws[177760] = fma(kw * y[4512], y[4160], ws[177760]);
     }
     {
       double w = 1.0 * phi[4192];
@@ -945,7 +945,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[36544] * w;
       out[4512] = fma(kw, y[4640], out[4512]);
       out[4640] = fma(kw, y[4512], out[4640]);
-      ws[173024] = fma(kw * y[4512], y[4640], ws[173024]);
+      ws[177792] = fma(kw * y[4512], y[4640], ws[177792]);
     }
     {
       double w = 1.0 * phi[1728];
@@ -954,7 +954,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[36576] * w;
       out[4512] = fma(kw, y[4704], out[4512]);
       out[4704] = fma(kw, y[4512], out[4704]);
-      ws[173056] = fma(kw * y[4512], y[4704], ws[173056]);
+      ws[177824] = fma(kw * y[4512], y[4704], ws[177824]);
     }
     {
       double w = 1.0 * phi[4512];
@@ -962,7 +962,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       w = w - phi[1728];
       const double kw = ws[36608] * w;
       out[1728] = out[1728] + kw;
-      ws[173088] = fma(kw, y[1728], ws[173088]);
+      ws[177856] = fma(kw, y[1728], ws[177856]);
     }
     {
       double w = 1.0 * phi[3776];
@@ -973,7 +973,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[36640] * w;
       out[1728] = fma(kw, y[4384], out[1728]);
       out[4384] = fma(kw, y[1728], out[4384]);
-      ws[173120] = fma(kw * y[1728], y[4384], ws[173120]);
+      ws[177888] = fma(kw * y[1728], y[4384], ws[177888]);
     }
     {
       double w = 0.5 * phi[2272];
@@ -985,7 +985,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[36672] * w;
       out[1728] = fma(kw, y[4704], out[1728]);
       out[4704] = fma(kw, y[1728], out[4704]);
-      ws[173152] = fma(kw * y[1728], y[4704], ws[173152]);
+      ws[177920] = fma(kw * y[1728], y[4704], ws[177920]);
     }
     {
       double w = 1.0 * phi[4448];
@@ -995,7 +995,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[36704] * w;
       out[4128] = fma(kw, y[4160], out[4128]);
       out[4160] = fma(kw, y[4128], out[4160]);
-      ws[173184] = fma(kw * y[4128], y[4160], ws[173184]);
+      ws[177952] = fma(kw * y[4128], y[4160], ws[177952]);
     }
 }
 __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int phioff, int outoff)
@@ -1010,7 +1010,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[36736] * w;
       out[4128] = fma(kw, y[4736], out[4128]);
       out[4736] = fma(kw, y[4128], out[4736]);
-      ws[173216] = fma(kw * y[4128], y[4736], ws[173216]);
+      ws[177984] = fma(kw * y[4128], y[4736], ws[177984]);
     }
     {
       double w = 1.0 * phi[4448];
@@ -1020,7 +1020,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[36768] * w;
       out[4128] = fma(kw, y[4640], out[4128]);
       out[4640] = fma(kw, y[4128], out[4640]);
-      ws[173248] = fma(kw * y[4128], y[4640], ws[173248]);
+      ws[178016] = fma(kw * y[4128], y[4640], ws[178016]);
     }
     {
       double w = 1.0 * phi[4416];
@@ -1030,7 +1030,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       w = w - phi[4128];
       const double kw = ws[36800] * w;
       out[4128] = out[4128] + kw;
-      ws[173280] = fma(kw, y[4128], ws[173280]);
+      ws[178048] = fma(kw, y[4128], ws[178048]);
     }
     {
       double w = 1.0 * phi[4096];
@@ -1040,7 +1040,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[36832] * w;
       out[4064] = fma(kw, y[4160], out[4064]);
       out[4160] = fma(kw, y[4064], out[4160]);
-      ws[173312] = fma(kw * y[4064], y[4160], ws[173312]);
+      ws[178080] = fma(kw * y[4064], y[4160], ws[178080]);
     }
     {
       double w = 1.0 * phi[4096];
@@ -1049,7 +1049,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[36864] * w;
       out[4064] = fma(kw, y[4736], out[4064]);
       out[4736] = fma(kw, y[4064], out[4736]);
-      ws[173344] = fma(kw * y[4064], y[4736], ws[173344]);
+      ws[178112] = fma(kw * y[4064], y[4736], ws[178112]);
     }
     {
       double w = 1.0 * phi[4096];
@@ -1059,7 +1059,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[36896] * w;
       out[4064] = fma(kw, y[4640], out[4064]);
       out[4640] = fma(kw, y[4064], out[4640]);
-      ws[173376] = fma(kw * y[4064], y[4640], ws[173376]);
+      ws[178144] = fma(kw * y[4064], y[4640], ws[178144]);
     }
     {
       double w = 1.0 * phi[4128];
@@ -1070,7 +1070,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       w = w - phi[4064];
       const double kw = ws[36928] * w;
       out[4064] = out[4064] + kw;
-      ws[173408] = fma(kw, y[4064], ws[173408]);
+      ws[178176] = fma(kw, y[4064], ws[178176]);
     }
     {
       double w = 0.2 * phi[4256];
@@ -1081,7 +1081,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[36960] * w;
       out[3840] = fma(kw, y[4736], out[3840]);
       out[4736] = fma(kw, y[3840], out[4736]);
-      ws[173440] = fma(kw * y[3840], y[4736], ws[173440]);
+      ws[178208] = fma(kw * y[3840], y[4736], ws[178208]);
     }
     {
       double w = 0.74 * phi[4512];
@@ -1095,7 +1095,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       w = w - phi[3840];
       const double kw = ws[36992] * w;
       out[3840] = out[3840] + kw;
-      ws[173472] = fma(kw, y[3840], ws[173472]);
+      ws[178240] = fma(kw, y[3840], ws[178240]);
     }
     {
       double w = 1.0 * phi[4192];
@@ -1105,7 +1105,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[37024] * w;
       out[3840] = fma(kw, y[4640], out[3840]);
       out[4640] = fma(kw, y[3840], out[4640]);
-      ws[173504] = fma(kw * y[3840], y[4640], ws[173504]);
+      ws[178272] = fma(kw * y[3840], y[4640], ws[178272]);
     }
     {
       double w = 1.8 * phi[4480];
@@ -1117,7 +1117,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[37056] * w;
       out[4256] = fma(kw, y[4736], out[4256]);
       out[4736] = fma(kw, y[4256], out[4736]);
-      ws[173536] = fma(kw * y[4256], y[4736], ws[173536]);
+      ws[178304] = fma(kw * y[4256], y[4736], ws[178304]);
     }
     {
       double w = 2.0 * phi[4704];
@@ -1125,7 +1125,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       w = w - phi[4256];
       const double kw = ws[37088] * w;
       out[4256] = out[4256] + kw;
-      ws[173568] = fma(kw, y[4256], ws[173568]);
+      ws[178336] = fma(kw, y[4256], ws[178336]);
     }
     {
       double w = 1.0 * phi[4192];
@@ -1138,7 +1138,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[37120] * w;
       out[4256] = fma(kw, y[4640], out[4256]);
       out[4640] = fma(kw, y[4256], out[4640]);
-      ws[173600] = fma(kw * y[4256], y[4640], ws[173600]);
+      ws[178368] = fma(kw * y[4256], y[4640], ws[178368]);
     }
     {
       double w = 1.0 * phi[4448];
@@ -1147,7 +1147,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       w = w - phi[4000];
       const double kw = ws[37152] * w;
       out[4000] = out[4000] + kw;
-      ws[173632] = fma(kw, y[4000], ws[173632]);
+      ws[178400] = fma(kw, y[4000], ws[178400]);
     }
     {
       double w = 1.0 * phi[4192];
@@ -1159,7 +1159,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[37184] * w;
       out[4000] = fma(kw, y[4640], out[4000]);
       out[4640] = fma(kw, y[4000], out[4640]);
-      ws[173664] = fma(kw * y[4000], y[4640], ws[173664]);
+      ws[178432] = fma(kw * y[4000], y[4640], ws[178432]);
     }
     {
       double w = 1.0 * phi[4448];
@@ -1169,14 +1169,14 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[37216] * w;
       out[4000] = fma(kw, y[4736], out[4000]);
       out[4736] = fma(kw, y[4000], out[4736]);
-      ws[173696] = fma(kw * y[4000], y[4736], ws[173696]);
+      ws[178464] = fma(kw * y[4000], y[4736], ws[178464]);
     }
     {
       double w = 1.0 * phi[4704];
       w = w - phi[4736];
       const double kw = ws[37248] * w;
       out[4736] = out[4736] + kw;
-      ws[173728] = fma(kw, y[4736], ws[173728]);
+      ws[178496] = fma(kw, y[4736], ws[178496]);
     }
     {
       double w = 1.0 * phi[4704];
@@ -1185,7 +1185,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[37280] * w;
       out[4480] = fma(kw, y[4736], out[4480]);
       out[4736] = fma(kw, y[4480], out[4736]);
-      ws[173760] = fma(kw * y[4480], y[4736], ws[173760]);
+      ws[178528] = fma(kw * y[4480], y[4736], ws[178528]);
     }
     {
       double w = 1.0 * phi[4416];
@@ -1193,7 +1193,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       w = w - phi[4736];
       const double kw = ws[37312] * w;
       out[4736] = out[4736] + kw;
-      ws[173792] = fma(kw, y[4736], ws[173792]);
+      ws[178560] = fma(kw, y[4736], ws[178560]);
     }
     {
       double w = 0.991 * phi[4128];
@@ -1205,7 +1205,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[37344] * w;
       out[832] = fma(kw, y[4736], out[832]);
       out[4736] = fma(kw, y[832], out[4736]);
-      ws[173824] = fma(kw * y[832], y[4736], ws[173824]);
+      ws[178592] = fma(kw * y[832], y[4736], ws[178592]);
     }
     {
       double w = 1.0 * phi[4512];
@@ -1215,7 +1215,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[37376] * w;
       out[2720] = fma(kw, y[4736], out[2720]);
       out[4736] = fma(kw, y[2720], out[4736]);
-      ws[173856] = fma(kw * y[2720], y[4736], ws[173856]);
+      ws[178624] = fma(kw * y[2720], y[4736], ws[178624]);
     }
     {
       double w = 0.95 * phi[4128];
@@ -1229,7 +1229,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[37408] * w;
       out[864] = fma(kw, y[4736], out[864]);
       out[4736] = fma(kw, y[864], out[4736]);
-      ws[173888] = fma(kw * y[864], y[4736], ws[173888]);
+      ws[178656] = fma(kw * y[864], y[4736], ws[178656]);
     }
     {
       double w = 0.5 * phi[4128];
@@ -1242,7 +1242,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       w = w - phi[320];
       const double kw = ws[37440] * w;
       out[320] = out[320] + kw;
-      ws[173920] = fma(kw, y[320], ws[173920]);
+      ws[178688] = fma(kw, y[320], ws[178688]);
     }
     {
       double w = 0.38 * phi[4480];
@@ -1252,7 +1252,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       w = w - phi[3392];
       const double kw = ws[37472] * w;
       out[3392] = out[3392] + kw;
-      ws[173952] = fma(kw, y[3392], ws[173952]);
+      ws[178720] = fma(kw, y[3392], ws[178720]);
     }
     {
       double w = 1.0 * phi[4512];
@@ -1264,7 +1264,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[37504] * w;
       out[3392] = fma(kw, y[4736], out[3392]);
       out[4736] = fma(kw, y[3392], out[4736]);
-      ws[173984] = fma(kw * y[3392], y[4736], ws[173984]);
+      ws[178752] = fma(kw * y[3392], y[4736], ws[178752]);
     }
     {
       double w = 1.0 * phi[928];
@@ -1273,7 +1273,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[37536] * w;
       out[896] = fma(kw, y[4736], out[896]);
       out[4736] = fma(kw, y[896], out[4736]);
-      ws[174016] = fma(kw * y[896], y[4736], ws[174016]);
+      ws[178784] = fma(kw * y[896], y[4736], ws[178784]);
     }
     {
       double w = 1.0 * phi[1984];
@@ -1282,7 +1282,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[37568] * w;
       out[4224] = fma(kw, y[4736], out[4224]);
       out[4736] = fma(kw, y[4224], out[4736]);
-      ws[174048] = fma(kw * y[4224], y[4736], ws[174048]);
+      ws[178816] = fma(kw * y[4224], y[4736], ws[178816]);
     }
     {
       double w = 0.2 * phi[320];
@@ -1297,7 +1297,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       w = w - phi[960];
       const double kw = ws[37600] * w;
       out[960] = out[960] + kw;
-      ws[174080] = fma(kw, y[960], ws[174080]);
+      ws[178848] = fma(kw, y[960], ws[178848]);
     }
     {
       double w = 1.0 * phi[320];
@@ -1305,7 +1305,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       w = w - phi[960];
       const double kw = ws[37632] * w;
       out[960] = out[960] + kw;
-      ws[174112] = fma(kw, y[960], ws[174112]);
+      ws[178880] = fma(kw, y[960], ws[178880]);
     }
     {
       double w = 1.0 * phi[3648];
@@ -1314,7 +1314,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[37664] * w;
       out[960] = fma(kw, y[4608], out[960]);
       out[4608] = fma(kw, y[960], out[4608]);
-      ws[174144] = fma(kw * y[960], y[4608], ws[174144]);
+      ws[178912] = fma(kw * y[960], y[4608], ws[178912]);
     }
     {
       double w = 0.7 * phi[4256];
@@ -1327,7 +1327,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[37696] * w;
       out[352] = fma(kw, y[4736], out[352]);
       out[4736] = fma(kw, y[352], out[4736]);
-      ws[174176] = fma(kw * y[352], y[4736], ws[174176]);
+      ws[178944] = fma(kw * y[352], y[4736], ws[178944]);
     }
     {
       double w = 1.0 * phi[4512];
@@ -1341,7 +1341,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[37728] * w;
       out[2656] = fma(kw, y[4160], out[2656]);
       out[4160] = fma(kw, y[2656], out[4160]);
-      ws[174208] = fma(kw * y[2656], y[4160], ws[174208]);
+      ws[178976] = fma(kw * y[2656], y[4160], ws[178976]);
     }
     {
       double w = 1.0 * phi[4576];
@@ -1353,7 +1353,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[37760] * w;
       out[2656] = fma(kw, y[4736], out[2656]);
       out[4736] = fma(kw, y[2656], out[4736]);
-      ws[174240] = fma(kw * y[2656], y[4736], ws[174240]);
+      ws[179008] = fma(kw * y[2656], y[4736], ws[179008]);
     }
     {
       double w = 1.0 * phi[4512];
@@ -1366,7 +1366,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[37792] * w;
       out[2656] = fma(kw, y[4320], out[2656]);
       out[4320] = fma(kw, y[2656], out[4320]);
-      ws[174272] = fma(kw * y[2656], y[4320], ws[174272]);
+      ws[179040] = fma(kw * y[2656], y[4320], ws[179040]);
     }
     {
       double w = 0.5 * phi[4608];
@@ -1380,7 +1380,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[37824] * w;
       out[2656] = fma(kw, y[4640], out[2656]);
       out[4640] = fma(kw, y[2656], out[4640]);
-      ws[174304] = fma(kw * y[2656], y[4640], ws[174304]);
+      ws[179072] = fma(kw * y[2656], y[4640], ws[179072]);
     }
     {
       double w = 0.2 * phi[4128];
@@ -1398,7 +1398,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[37856] * w;
       out[3552] = fma(kw, y[4160], out[3552]);
       out[4160] = fma(kw, y[3552], out[4160]);
-      ws[174336] = fma(kw * y[3552], y[4160], ws[174336]);
+      ws[179104] = fma(kw * y[3552], y[4160], ws[179104]);
     }
     {
       double w = 0.781 * phi[4512];
@@ -1414,7 +1414,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[37888] * w;
       out[3552] = fma(kw, y[4736], out[3552]);
       out[4736] = fma(kw, y[3552], out[4736]);
-      ws[174368] = fma(kw * y[3552], y[4736], ws[174368]);
+      ws[179136] = fma(kw * y[3552], y[4736], ws[179136]);
     }
     {
       double w = 0.295 * phi[4128];
@@ -1436,7 +1436,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[37920] * w;
       out[3552] = fma(kw, y[4320], out[3552]);
       out[4320] = fma(kw, y[3552], out[4320]);
-      ws[174400] = fma(kw * y[3552], y[4320], ws[174400]);
+      ws[179168] = fma(kw * y[3552], y[4320], ws[179168]);
     }
     {
       double w = 0.5 * phi[4608];
@@ -1454,7 +1454,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[37952] * w;
       out[3552] = fma(kw, y[4640], out[3552]);
       out[4640] = fma(kw, y[3552], out[4640]);
-      ws[174432] = fma(kw * y[3552], y[4640], ws[174432]);
+      ws[179200] = fma(kw * y[3552], y[4640], ws[179200]);
     }
     {
       double w = 1.24 * phi[4128];
@@ -1468,7 +1468,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[37984] * w;
       out[3136] = fma(kw, y[4160], out[3136]);
       out[4160] = fma(kw, y[3136], out[4160]);
-      ws[174464] = fma(kw * y[3136], y[4160], ws[174464]);
+      ws[179232] = fma(kw * y[3136], y[4160], ws[179232]);
     }
     {
       double w = 1.3 * phi[4128];
@@ -1480,7 +1480,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38016] * w;
       out[3136] = fma(kw, y[4736], out[3136]);
       out[4736] = fma(kw, y[3136], out[4736]);
-      ws[174496] = fma(kw * y[3136], y[4736], ws[174496]);
+      ws[179264] = fma(kw * y[3136], y[4736], ws[179264]);
     }
     {
       double w = 0.732 * phi[4128];
@@ -1500,7 +1500,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38048] * w;
       out[3136] = fma(kw, y[4320], out[3136]);
       out[4320] = fma(kw, y[3136], out[4320]);
-      ws[174528] = fma(kw * y[3136], y[4320], ws[174528]);
+      ws[179296] = fma(kw * y[3136], y[4320], ws[179296]);
     }
 }
 __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int phioff, int outoff)
@@ -1523,7 +1523,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38080] * w;
       out[3136] = fma(kw, y[4640], out[3136]);
       out[4640] = fma(kw, y[3136], out[4640]);
-      ws[174560] = fma(kw * y[3136], y[4640], ws[174560]);
+      ws[179328] = fma(kw * y[3136], y[4640], ws[179328]);
     }
     {
       double w = 1.0 * phi[3424];
@@ -1534,7 +1534,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38112] * w;
       out[2528] = fma(kw, y[4736], out[2528]);
       out[4736] = fma(kw, y[2528], out[4736]);
-      ws[174592] = fma(kw * y[2528], y[4736], ws[174592]);
+      ws[179360] = fma(kw * y[2528], y[4736], ws[179360]);
     }
     {
       double w = 0.75 * phi[3872];
@@ -1549,7 +1549,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38144] * w;
       out[2528] = fma(kw, y[4160], out[2528]);
       out[4160] = fma(kw, y[2528], out[4160]);
-      ws[174624] = fma(kw * y[2528], y[4160], ws[174624]);
+      ws[179392] = fma(kw * y[2528], y[4160], ws[179392]);
     }
     {
       double w = 0.1 * phi[1632];
@@ -1564,7 +1564,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38176] * w;
       out[3424] = fma(kw, y[4384], out[3424]);
       out[4384] = fma(kw, y[3424], out[4384]);
-      ws[174656] = fma(kw * y[3424], y[4384], ws[174656]);
+      ws[179424] = fma(kw * y[3424], y[4384], ws[179424]);
     }
     {
       double w = 0.88 * phi[1664];
@@ -1577,7 +1577,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38208] * w;
       out[3424] = fma(kw, y[4704], out[3424]);
       out[4704] = fma(kw, y[3424], out[4704]);
-      ws[174688] = fma(kw * y[3424], y[4704], ws[174688]);
+      ws[179456] = fma(kw * y[3424], y[4704], ws[179456]);
     }
     {
       double w = 0.598 * phi[4512];
@@ -1592,7 +1592,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38240] * w;
       out[3424] = fma(kw, y[4448], out[3424]);
       out[4448] = fma(kw, y[3424], out[4448]);
-      ws[174720] = fma(kw * y[3424], y[4448], ws[174720]);
+      ws[179488] = fma(kw * y[3424], y[4448], ws[179488]);
     }
     {
       double w = 0.598 * phi[4512];
@@ -1605,7 +1605,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38272] * w;
       out[3424] = fma(kw, y[4672], out[3424]);
       out[4672] = fma(kw, y[3424], out[4672]);
-      ws[174752] = fma(kw * y[3424], y[4672], ws[174752]);
+      ws[179520] = fma(kw * y[3424], y[4672], ws[179520]);
     }
     {
       double w = 1.0 * phi[4704];
@@ -1613,7 +1613,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       w = w - phi[3424];
       const double kw = ws[38304] * w;
       out[3424] = out[3424] + kw;
-      ws[174784] = fma(kw, y[3424], ws[174784]);
+      ws[179552] = fma(kw, y[3424], ws[179552]);
     }
     {
       double w = 0.6 * phi[4512];
@@ -1631,7 +1631,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38336] * w;
       out[2528] = fma(kw, y[4320], out[2528]);
       out[4320] = fma(kw, y[2528], out[4320]);
-      ws[174816] = fma(kw * y[2528], y[4320], ws[174816]);
+      ws[179584] = fma(kw * y[2528], y[4320], ws[179584]);
     }
     {
       double w = 0.35 * phi[4608];
@@ -1648,7 +1648,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38368] * w;
       out[2528] = fma(kw, y[4640], out[2528]);
       out[4640] = fma(kw, y[2528], out[4640]);
-      ws[174848] = fma(kw * y[2528], y[4640], ws[174848]);
+      ws[179616] = fma(kw * y[2528], y[4640], ws[179616]);
     }
     {
       double w = 0.022 * phi[4288];
@@ -1668,7 +1668,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38400] * w;
       out[3872] = fma(kw, y[4736], out[3872]);
       out[4736] = fma(kw, y[3872], out[4736]);
-      ws[174880] = fma(kw * y[3872], y[4736], ws[174880]);
+      ws[179648] = fma(kw * y[3872], y[4736], ws[179648]);
     }
     {
       double w = 0.04 * phi[4128];
@@ -1686,7 +1686,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38432] * w;
       out[3872] = fma(kw, y[4320], out[3872]);
       out[4320] = fma(kw, y[3872], out[4320]);
-      ws[174912] = fma(kw * y[3872], y[4320], ws[174912]);
+      ws[179680] = fma(kw * y[3872], y[4320], ws[179680]);
     }
     {
       double w = 0.717 * phi[4192];
@@ -1704,7 +1704,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38464] * w;
       out[3872] = fma(kw, y[4640], out[3872]);
       out[4640] = fma(kw, y[3872], out[4640]);
-      ws[174944] = fma(kw * y[3872], y[4640], ws[174944]);
+      ws[179712] = fma(kw * y[3872], y[4640], ws[179712]);
     }
     {
       double w = 0.76 * phi[4704];
@@ -1721,7 +1721,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       w = w - phi[3872];
       const double kw = ws[38496] * w;
       out[3872] = out[3872] + kw;
-      ws[174976] = fma(kw, y[3872], ws[174976]);
+      ws[179744] = fma(kw, y[3872], ws[179744]);
     }
     {
       double w = 0.904 * phi[1056];
@@ -1735,7 +1735,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38528] * w;
       out[1664] = fma(kw, y[4736], out[1664]);
       out[4736] = fma(kw, y[1664], out[4736]);
-      ws[175008] = fma(kw * y[1664], y[4736], ws[175008]);
+      ws[179776] = fma(kw * y[1664], y[4736], ws[179776]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1743,7 +1743,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       w = w - phi[1024];
       const double kw = ws[38560] * w;
       out[1024] = out[1024] + kw;
-      ws[175040] = fma(kw, y[1024], ws[175040]);
+      ws[179808] = fma(kw, y[1024], ws[179808]);
     }
     {
       double w = 1.0 * phi[4192];
@@ -1753,7 +1753,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38592] * w;
       out[1024] = fma(kw, y[4640], out[1024]);
       out[4640] = fma(kw, y[1024], out[4640]);
-      ws[175072] = fma(kw * y[1024], y[4640], ws[175072]);
+      ws[179840] = fma(kw * y[1024], y[4640], ws[179840]);
     }
     {
       double w = 1.0 * phi[3296];
@@ -1763,7 +1763,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38624] * w;
       out[1056] = fma(kw, y[4736], out[1056]);
       out[4736] = fma(kw, y[1056], out[4736]);
-      ws[175104] = fma(kw * y[1056], y[4736], ws[175104]);
+      ws[179872] = fma(kw * y[1056], y[4736], ws[179872]);
     }
     {
       double w = 0.275 * phi[3840];
@@ -1780,7 +1780,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38656] * w;
       out[3296] = fma(kw, y[4704], out[3296]);
       out[4704] = fma(kw, y[3296], out[4704]);
-      ws[175136] = fma(kw * y[3296], y[4704], ws[175136]);
+      ws[179904] = fma(kw * y[3296], y[4704], ws[179904]);
     }
     {
       double w = 0.275 * phi[3840];
@@ -1797,7 +1797,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38688] * w;
       out[3296] = fma(kw, y[4384], out[3296]);
       out[4384] = fma(kw, y[3296], out[4384]);
-      ws[175168] = fma(kw * y[3296], y[4384], ws[175168]);
+      ws[179936] = fma(kw * y[3296], y[4384], ws[179936]);
     }
     {
       double w = 0.22 * phi[3840];
@@ -1816,7 +1816,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38720] * w;
       out[3296] = fma(kw, y[4448], out[3296]);
       out[4448] = fma(kw, y[3296], out[4448]);
-      ws[175200] = fma(kw * y[3296], y[4448], ws[175200]);
+      ws[179968] = fma(kw * y[3296], y[4448], ws[179968]);
     }
     {
       double w = 0.275 * phi[3840];
@@ -1833,7 +1833,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38752] * w;
       out[3296] = fma(kw, y[4672], out[3296]);
       out[4672] = fma(kw, y[3296], out[4672]);
-      ws[175232] = fma(kw * y[3296], y[4672], ws[175232]);
+      ws[180000] = fma(kw * y[3296], y[4672], ws[180000]);
     }
     {
       double w = 0.63 * phi[4352];
@@ -1854,7 +1854,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38784] * w;
       out[1632] = fma(kw, y[4736], out[1632]);
       out[4736] = fma(kw, y[1632], out[4736]);
-      ws[175264] = fma(kw * y[1632], y[4736], ws[175264]);
+      ws[180032] = fma(kw * y[1632], y[4736], ws[180032]);
     }
     {
       double w = 0.15 * phi[4064];
@@ -1865,7 +1865,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38816] * w;
       out[2048] = fma(kw, y[4160], out[2048]);
       out[4160] = fma(kw, y[2048], out[4160]);
-      ws[175296] = fma(kw * y[2048], y[4160], ws[175296]);
+      ws[180064] = fma(kw * y[2048], y[4160], ws[180064]);
     }
     {
       double w = 0.75 * phi[4576];
@@ -1881,7 +1881,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38848] * w;
       out[2048] = fma(kw, y[4736], out[2048]);
       out[4736] = fma(kw, y[2048], out[4736]);
-      ws[175328] = fma(kw * y[2048], y[4736], ws[175328]);
+      ws[180096] = fma(kw * y[2048], y[4736], ws[180096]);
     }
     {
       double w = 0.57 * phi[4736];
@@ -1900,7 +1900,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38880] * w;
       out[2048] = fma(kw, y[4320], out[2048]);
       out[4320] = fma(kw, y[2048], out[4320]);
-      ws[175360] = fma(kw * y[2048], y[4320], ws[175360]);
+      ws[180128] = fma(kw * y[2048], y[4320], ws[180128]);
     }
     {
       double w = 0.47 * phi[4608];
@@ -1916,7 +1916,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38912] * w;
       out[2048] = fma(kw, y[4640], out[2048]);
       out[4640] = fma(kw, y[2048], out[4640]);
-      ws[175392] = fma(kw * y[2048], y[4640], ws[175392]);
+      ws[180160] = fma(kw * y[2048], y[4640], ws[180160]);
     }
     {
       double w = 0.15 * phi[4064];
@@ -1927,7 +1927,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38944] * w;
       out[2112] = fma(kw, y[4160], out[2112]);
       out[4160] = fma(kw, y[2112], out[4160]);
-      ws[175424] = fma(kw * y[2112], y[4160], ws[175424]);
+      ws[180192] = fma(kw * y[2112], y[4160], ws[180192]);
     }
     {
       double w = 0.75 * phi[4576];
@@ -1943,7 +1943,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[38976] * w;
       out[2112] = fma(kw, y[4736], out[2112]);
       out[4736] = fma(kw, y[2112], out[4736]);
-      ws[175456] = fma(kw * y[2112], y[4736], ws[175456]);
+      ws[180224] = fma(kw * y[2112], y[4736], ws[180224]);
     }
     {
       double w = 0.57 * phi[4736];
@@ -1962,7 +1962,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39008] * w;
       out[2112] = fma(kw, y[4320], out[2112]);
       out[4320] = fma(kw, y[2112], out[4320]);
-      ws[175488] = fma(kw * y[2112], y[4320], ws[175488]);
+      ws[180256] = fma(kw * y[2112], y[4320], ws[180256]);
     }
     {
       double w = 0.47 * phi[4608];
@@ -1977,7 +1977,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39040] * w;
       out[2112] = fma(kw, y[4640], out[2112]);
       out[4640] = fma(kw, y[2112], out[4640]);
-      ws[175520] = fma(kw * y[2112], y[4640], ws[175520]);
+      ws[180288] = fma(kw * y[2112], y[4640], ws[180288]);
     }
     {
       double w = 0.53 * phi[3616];
@@ -1992,7 +1992,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39072] * w;
       out[384] = fma(kw, y[4736], out[384]);
       out[4736] = fma(kw, y[384], out[4736]);
-      ws[175552] = fma(kw * y[384], y[4736], ws[175552]);
+      ws[180320] = fma(kw * y[384], y[4736], ws[180320]);
     }
     {
       double w = 0.918 * phi[4608];
@@ -2005,7 +2005,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39104] * w;
       out[3104] = fma(kw, y[4384], out[3104]);
       out[4384] = fma(kw, y[3104], out[4384]);
-      ws[175584] = fma(kw * y[3104], y[4384], ws[175584]);
+      ws[180352] = fma(kw * y[3104], y[4384], ws[180352]);
     }
 }
 }  // namespace mech_cb6r5_ae7_aq

@@ -19,7 +19,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39136] * w;
       out[3104] = fma(kw, y[4448], out[3104]);
       out[4448] = fma(kw, y[3104], out[4448]);
-      ws[175616] = fma(kw * y[3104], y[4448], ws[175616]);
+      ws[180384] = fma(kw * y[3104], y[4448], ws[180384]);
     }
     {
       double w = -phi[3104];
@@ -27,7 +27,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39168] * w;
       out[3104] = fma(kw, y[4704], out[3104]);
       out[4704] = fma(kw, y[3104], out[4704]);
-      ws[175648] = fma(kw * y[3104], y[4704], ws[175648]);
+      ws[180416] = fma(kw * y[3104], y[4704], ws[180416]);
     }
     {
       double w = 1.0 * phi[4256];
@@ -39,7 +39,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39200] * w;
       out[3104] = fma(kw, y[4672], out[3104]);
       out[4672] = fma(kw, y[3104], out[4672]);
-      ws[175680] = fma(kw * y[3104], y[4672], ws[175680]);
+      ws[180448] = fma(kw * y[3104], y[4672], ws[180448]);
     }
     {
       double w = 0.18 * phi[3616];
@@ -55,7 +55,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39232] * w;
       out[1088] = fma(kw, y[4736], out[1088]);
       out[4736] = fma(kw, y[1088], out[4736]);
-      ws[175712] = fma(kw * y[1088], y[4736], ws[175712]);
+      ws[180480] = fma(kw * y[1088], y[4736], ws[180480]);
     }
     {
       double w = 0.86 * phi[4608];
@@ -70,7 +70,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39264] * w;
       out[3488] = fma(kw, y[4384], out[3488]);
       out[4384] = fma(kw, y[3488], out[4384]);
-      ws[175744] = fma(kw * y[3488], y[4384], ws[175744]);
+      ws[180512] = fma(kw * y[3488], y[4384], ws[180512]);
     }
     {
       double w = 0.48 * phi[4256];
@@ -85,7 +85,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39296] * w;
       out[3488] = fma(kw, y[4448], out[3488]);
       out[4448] = fma(kw, y[3488], out[4448]);
-      ws[175776] = fma(kw * y[3488], y[4448], ws[175776]);
+      ws[180544] = fma(kw * y[3488], y[4448], ws[180544]);
     }
     {
       double w = -phi[3488];
@@ -93,7 +93,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39328] * w;
       out[3488] = fma(kw, y[4704], out[3488]);
       out[4704] = fma(kw, y[3488], out[4704]);
-      ws[175808] = fma(kw * y[3488], y[4704], ws[175808]);
+      ws[180576] = fma(kw * y[3488], y[4704], ws[180576]);
     }
     {
       double w = 0.48 * phi[4256];
@@ -107,7 +107,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39360] * w;
       out[3488] = fma(kw, y[4672], out[3488]);
       out[4672] = fma(kw, y[3488], out[4672]);
-      ws[175840] = fma(kw * y[3488], y[4672], ws[175840]);
+      ws[180608] = fma(kw * y[3488], y[4672], ws[180608]);
     }
     {
       double w = 0.155 * phi[3616];
@@ -123,7 +123,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39392] * w;
       out[1120] = fma(kw, y[4736], out[1120]);
       out[4736] = fma(kw, y[1120], out[4736]);
-      ws[175872] = fma(kw * y[1120], y[4736], ws[175872]);
+      ws[180640] = fma(kw * y[1120], y[4736], ws[180640]);
     }
     {
       double w = 0.155 * phi[3616];
@@ -139,7 +139,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39424] * w;
       out[1152] = fma(kw, y[4736], out[1152]);
       out[4736] = fma(kw, y[1152], out[4736]);
-      ws[175904] = fma(kw * y[1152], y[4736], ws[175904]);
+      ws[180672] = fma(kw * y[1152], y[4736], ws[180672]);
     }
     {
       double w = 0.86 * phi[4608];
@@ -154,7 +154,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39456] * w;
       out[3584] = fma(kw, y[4384], out[3584]);
       out[4384] = fma(kw, y[3584], out[4384]);
-      ws[175936] = fma(kw * y[3584], y[4384], ws[175936]);
+      ws[180704] = fma(kw * y[3584], y[4384], ws[180704]);
     }
     {
       double w = -phi[3584];
@@ -162,7 +162,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39488] * w;
       out[3584] = fma(kw, y[4704], out[3584]);
       out[4704] = fma(kw, y[3584], out[4704]);
-      ws[175968] = fma(kw * y[3584], y[4704], ws[175968]);
+      ws[180736] = fma(kw * y[3584], y[4704], ws[180736]);
     }
     {
       double w = 0.26 * phi[4256];
@@ -177,7 +177,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39520] * w;
       out[3584] = fma(kw, y[4448], out[3584]);
       out[4448] = fma(kw, y[3584], out[4448]);
-      ws[176000] = fma(kw * y[3584], y[4448], ws[176000]);
+      ws[180768] = fma(kw * y[3584], y[4448], ws[180768]);
     }
     {
       double w = 0.26 * phi[4256];
@@ -191,7 +191,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39552] * w;
       out[3584] = fma(kw, y[4672], out[3584]);
       out[4672] = fma(kw, y[3584], out[4672]);
-      ws[176032] = fma(kw * y[3584], y[4672], ws[176032]);
+      ws[180800] = fma(kw * y[3584], y[4672], ws[180800]);
     }
     {
       double w = 0.025 * phi[4256];
@@ -206,7 +206,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39584] * w;
       out[3616] = fma(kw, y[4736], out[3616]);
       out[4736] = fma(kw, y[3616], out[4736]);
-      ws[176064] = fma(kw * y[3616], y[4736], ws[176064]);
+      ws[180832] = fma(kw * y[3616], y[4736], ws[180832]);
     }
     {
       double w = 0.3 * phi[3328];
@@ -223,7 +223,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39616] * w;
       out[3616] = fma(kw, y[4640], out[3616]);
       out[4640] = fma(kw, y[3616], out[4640]);
-      ws[176096] = fma(kw * y[3616], y[4640], ws[176096]);
+      ws[180864] = fma(kw * y[3616], y[4640], ws[180864]);
     }
     {
       double w = 1.0 * phi[2176];
@@ -232,7 +232,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39648] * w;
       out[3328] = fma(kw, y[4608], out[3328]);
       out[4608] = fma(kw, y[3328], out[4608]);
-      ws[176128] = fma(kw * y[3328], y[4608], ws[176128]);
+      ws[180896] = fma(kw * y[3328], y[4608], ws[180896]);
     }
     {
       double w = 1.0 * phi[3616];
@@ -241,7 +241,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39680] * w;
       out[3328] = fma(kw, y[4704], out[3328]);
       out[4704] = fma(kw, y[3328], out[4704]);
-      ws[176160] = fma(kw * y[3328], y[4704], ws[176160]);
+      ws[180928] = fma(kw * y[3328], y[4704], ws[180928]);
     }
     {
       double w = 1.0 * phi[4032];
@@ -251,7 +251,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39712] * w;
       out[2176] = fma(kw, y[4736], out[2176]);
       out[4736] = fma(kw, y[2176], out[4736]);
-      ws[176192] = fma(kw * y[2176], y[4736], ws[176192]);
+      ws[180960] = fma(kw * y[2176], y[4736], ws[180960]);
     }
     {
       double w = 1.0 * phi[4032];
@@ -262,7 +262,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39744] * w;
       out[2176] = fma(kw, y[4640], out[2176]);
       out[4640] = fma(kw, y[2176], out[4640]);
-      ws[176224] = fma(kw * y[2176], y[4640], ws[176224]);
+      ws[180992] = fma(kw * y[2176], y[4640], ws[180992]);
     }
     {
       double w = 1.0 * phi[2464];
@@ -272,7 +272,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       w = w - phi[2176];
       const double kw = ws[39776] * w;
       out[2176] = out[2176] + kw;
-      ws[176256] = fma(kw, y[2176], ws[176256]);
+      ws[181024] = fma(kw, y[2176], ws[181024]);
     }
     {
       double w = 0.4 * phi[4256];
@@ -283,7 +283,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       w = w - phi[3808];
       const double kw = ws[39808] * w;
       out[3808] = out[3808] + kw;
-      ws[176288] = fma(kw, y[3808], ws[176288]);
+      ws[181056] = fma(kw, y[3808], ws[181056]);
     }
     {
       double w = 1.0 * phi[4000];
@@ -295,7 +295,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39840] * w;
       out[3808] = fma(kw, y[4736], out[3808]);
       out[4736] = fma(kw, y[3808], out[4736]);
-      ws[176320] = fma(kw * y[3808], y[4736], ws[176320]);
+      ws[181088] = fma(kw * y[3808], y[4736], ws[181088]);
     }
     {
       double w = 1.2 * phi[4000];
@@ -310,7 +310,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39872] * w;
       out[3808] = fma(kw, y[4320], out[3808]);
       out[4320] = fma(kw, y[3808], out[4320]);
-      ws[176352] = fma(kw * y[3808], y[4320], ws[176352]);
+      ws[181120] = fma(kw * y[3808], y[4320], ws[181120]);
     }
     {
       double w = 0.5 * phi[4608];
@@ -326,7 +326,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39904] * w;
       out[3808] = fma(kw, y[4640], out[3808]);
       out[4640] = fma(kw, y[3808], out[4640]);
-      ws[176384] = fma(kw * y[3808], y[4640], ws[176384]);
+      ws[181152] = fma(kw * y[3808], y[4640], ws[181152]);
     }
     {
       double w = 1.0 * phi[3744];
@@ -335,7 +335,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       w = w - phi[3936];
       const double kw = ws[39936] * w;
       out[3936] = out[3936] + kw;
-      ws[176416] = fma(kw, y[3936], ws[176416]);
+      ws[181184] = fma(kw, y[3936], ws[181184]);
     }
     {
       double w = 0.6 * phi[3744];
@@ -347,7 +347,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39968] * w;
       out[3936] = fma(kw, y[4736], out[3936]);
       out[4736] = fma(kw, y[3936], out[4736]);
-      ws[176448] = fma(kw * y[3936], y[4736], ws[176448]);
+      ws[181216] = fma(kw * y[3936], y[4736], ws[181216]);
     }
     {
       double w = 1.4 * phi[4256];
@@ -363,7 +363,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40000] * w;
       out[3936] = fma(kw, y[4320], out[3936]);
       out[4320] = fma(kw, y[3936], out[4320]);
-      ws[176480] = fma(kw * y[3936], y[4320], ws[176480]);
+      ws[181248] = fma(kw * y[3936], y[4320], ws[181248]);
     }
     {
       double w = 1.0 * phi[3744];
@@ -373,7 +373,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40032] * w;
       out[3936] = fma(kw, y[4640], out[3936]);
       out[4640] = fma(kw, y[3936], out[4640]);
-      ws[176512] = fma(kw * y[3936], y[4640], ws[176512]);
+      ws[181280] = fma(kw * y[3936], y[4640], ws[181280]);
     }
     {
       double w = 0.14 * phi[4512];
@@ -384,7 +384,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40064] * w;
       out[1760] = fma(kw, y[4736], out[1760]);
       out[4736] = fma(kw, y[1760], out[4736]);
-      ws[176544] = fma(kw * y[1760], y[4736], ws[176544]);
+      ws[181312] = fma(kw * y[1760], y[4736], ws[181312]);
     }
     {
       double w = 1.0 * phi[3328];
@@ -394,7 +394,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40096] * w;
       out[1760] = fma(kw, y[4640], out[1760]);
       out[4640] = fma(kw, y[1760], out[4640]);
-      ws[176576] = fma(kw * y[1760], y[4640], ws[176576]);
+      ws[181344] = fma(kw * y[1760], y[4640], ws[181344]);
     }
     {
       double w = 1.0 * phi[4608];
@@ -407,7 +407,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40128] * w;
       out[3744] = fma(kw, y[4384], out[3744]);
       out[4384] = fma(kw, y[3744], out[4384]);
-      ws[176608] = fma(kw * y[3744], y[4384], ws[176608]);
+      ws[181376] = fma(kw * y[3744], y[4384], ws[181376]);
     }
     {
       double w = 1.0 * phi[1792];
@@ -416,7 +416,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40160] * w;
       out[3744] = fma(kw, y[4608], out[3744]);
       out[4608] = fma(kw, y[3744], out[4608]);
-      ws[176640] = fma(kw * y[3744], y[4608], ws[176640]);
+      ws[181408] = fma(kw * y[3744], y[4608], ws[181408]);
     }
     {
       double w = 1.0 * phi[3744];
@@ -424,7 +424,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       w = w - phi[1792];
       const double kw = ws[40192] * w;
       out[1792] = out[1792] + kw;
-      ws[176672] = fma(kw, y[1792], ws[176672]);
+      ws[181440] = fma(kw, y[1792], ws[181440]);
     }
     {
       double w = 0.37 * phi[2688];
@@ -438,7 +438,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40224] * w;
       out[3744] = fma(kw, y[4704], out[3744]);
       out[4704] = fma(kw, y[3744], out[4704]);
-      ws[176704] = fma(kw * y[3744], y[4704], ws[176704]);
+      ws[181472] = fma(kw * y[3744], y[4704], ws[181472]);
     }
     {
       double w = 1.0 * phi[4416];
@@ -450,7 +450,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40256] * w;
       out[3744] = fma(kw, y[4448], out[3744]);
       out[4448] = fma(kw, y[3744], out[4448]);
-      ws[176736] = fma(kw * y[3744], y[4448], ws[176736]);
+      ws[181504] = fma(kw * y[3744], y[4448], ws[181504]);
     }
     {
       double w = 0.8 * phi[4576];
@@ -462,7 +462,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40288] * w;
       out[3744] = fma(kw, y[4672], out[3744]);
       out[4672] = fma(kw, y[3744], out[4672]);
-      ws[176768] = fma(kw * y[3744], y[4672], ws[176768]);
+      ws[181536] = fma(kw * y[3744], y[4672], ws[181536]);
     }
     {
       double w = 0.5 * phi[4608];
@@ -474,7 +474,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40320] * w;
       out[1792] = fma(kw, y[4736], out[1792]);
       out[4736] = fma(kw, y[1792], out[4736]);
-      ws[176800] = fma(kw * y[1792], y[4736], ws[176800]);
+      ws[181568] = fma(kw * y[1792], y[4736], ws[181568]);
     }
     {
       double w = 1.0 * phi[4128];
@@ -484,7 +484,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40352] * w;
       out[1952] = fma(kw, y[4736], out[1952]);
       out[4736] = fma(kw, y[1952], out[4736]);
-      ws[176832] = fma(kw * y[1952], y[4736], ws[176832]);
+      ws[181600] = fma(kw * y[1952], y[4736], ws[181600]);
     }
     {
       double w = 1.0 * phi[4416];
@@ -494,7 +494,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40384] * w;
       out[416] = fma(kw, y[4736], out[416]);
       out[4736] = fma(kw, y[416], out[4736]);
-      ws[176864] = fma(kw * y[416], y[4736], ws[176864]);
+      ws[181632] = fma(kw * y[416], y[4736], ws[181632]);
     }
     {
       double w = 1.0 * phi[4288];
@@ -502,7 +502,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       w = w - phi[928];
       const double kw = ws[40416] * w;
       out[928] = out[928] + kw;
-      ws[176896] = fma(kw, y[928], ws[176896]);
+      ws[181664] = fma(kw, y[928], ws[181664]);
     }
 }
 __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int phioff, int outoff)
@@ -519,7 +519,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       w = w - phi[928];
       const double kw = ws[40448] * w;
       out[928] = out[928] + kw;
-      ws[176928] = fma(kw, y[928], ws[176928]);
+      ws[181696] = fma(kw, y[928], ws[181696]);
     }
     {
       double w = 1.0 * phi[4288];
@@ -527,7 +527,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       w = w - phi[1984];
       const double kw = ws[40480] * w;
       out[1984] = out[1984] + kw;
-      ws[176960] = fma(kw, y[1984], ws[176960]);
+      ws[181728] = fma(kw, y[1984], ws[181728]);
     }
     {
       double w = 0.126 * phi[4064];
@@ -539,7 +539,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       w = w - phi[1984];
       const double kw = ws[40512] * w;
       out[1984] = out[1984] + kw;
-      ws[176992] = fma(kw, y[1984], ws[176992]);
+      ws[181760] = fma(kw, y[1984], ws[181760]);
     }
     {
       double w = 1.0 * phi[4192];
@@ -548,14 +548,14 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40544] * w;
       out[4608] = fma(kw, y[4736], out[4608]);
       out[4736] = fma(kw, y[4608], out[4736]);
-      ws[177024] = fma(kw * y[4608], y[4736], ws[177024]);
+      ws[181792] = fma(kw * y[4608], y[4736], ws[181792]);
     }
     {
       double w = 2.0 * phi[4544];
       w = w - phi[1184];
       const double kw = ws[40576] * w;
       out[1184] = out[1184] + kw;
-      ws[177056] = fma(kw, y[1184], ws[177056]);
+      ws[181824] = fma(kw, y[1184], ws[181824]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -563,7 +563,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       w = w - phi[1824];
       const double kw = ws[40608] * w;
       out[1824] = out[1824] + kw;
-      ws[177088] = fma(kw, y[1824], ws[177088]);
+      ws[181856] = fma(kw, y[1824], ws[181856]);
     }
     {
       double w = 1.0 * phi[3520];
@@ -572,7 +572,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40640] * w;
       out[4544] = fma(kw, y[4320], out[4544]);
       out[4320] = fma(kw, y[4544], out[4320]);
-      ws[177120] = fma(kw * y[4544], y[4320], ws[177120]);
+      ws[181888] = fma(kw * y[4544], y[4320], ws[181888]);
     }
     {
       double w = 0.3 * phi[1184];
@@ -582,7 +582,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40672] * w;
       out[3520] = fma(kw, y[3520], out[3520]);
       out[3520] = fma(kw, y[3520], out[3520]);
-      ws[177152] = fma(kw * y[3520], y[3520], ws[177152]);
+      ws[181920] = fma(kw * y[3520], y[3520], ws[181920]);
     }
     {
       double w = 1.0 * phi[4544];
@@ -592,7 +592,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40704] * w;
       out[3520] = fma(kw, y[4384], out[3520]);
       out[4384] = fma(kw, y[3520], out[4384]);
-      ws[177184] = fma(kw * y[3520], y[4384], ws[177184]);
+      ws[181952] = fma(kw * y[3520], y[4384], ws[181952]);
     }
     {
       double w = 1.0 * phi[1824];
@@ -601,7 +601,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40736] * w;
       out[3520] = fma(kw, y[4704], out[3520]);
       out[4704] = fma(kw, y[3520], out[4704]);
-      ws[177216] = fma(kw * y[3520], y[4704], ws[177216]);
+      ws[181984] = fma(kw * y[3520], y[4704], ws[181984]);
     }
     {
       double w = 1.0 * phi[4544];
@@ -612,7 +612,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40768] * w;
       out[3520] = fma(kw, y[4416], out[3520]);
       out[4416] = fma(kw, y[3520], out[4416]);
-      ws[177248] = fma(kw * y[3520], y[4416], ws[177248]);
+      ws[182016] = fma(kw * y[3520], y[4416], ws[182016]);
     }
     {
       double w = 1.0 * phi[4544];
@@ -622,7 +622,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40800] * w;
       out[4736] = fma(kw, y[3232], out[4736]);
       out[3232] = fma(kw, y[4736], out[3232]);
-      ws[177280] = fma(kw * y[4736], y[3232], ws[177280]);
+      ws[182048] = fma(kw * y[4736], y[3232], ws[182048]);
     }
     {
       double w = 1.0 * phi[4544];
@@ -631,7 +631,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       w = w - phi[3232];
       const double kw = ws[40832] * w;
       out[3232] = out[3232] + kw;
-      ws[177312] = fma(kw, y[3232], ws[177312]);
+      ws[182080] = fma(kw, y[3232], ws[182080]);
     }
     {
       double w = 1.0 * phi[3968];
@@ -640,7 +640,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       w = w - phi[4544];
       const double kw = ws[40864] * w;
       out[4544] = out[4544] + kw;
-      ws[177344] = fma(kw, y[4544], ws[177344]);
+      ws[182112] = fma(kw, y[4544], ws[182112]);
     }
     {
       double w = 1.0 * phi[3968];
@@ -650,7 +650,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40896] * w;
       out[4544] = fma(kw, y[4224], out[4544]);
       out[4224] = fma(kw, y[4544], out[4224]);
-      ws[177376] = fma(kw * y[4544], y[4224], ws[177376]);
+      ws[182144] = fma(kw * y[4544], y[4224], ws[182144]);
     }
     {
       double w = 1.0 * phi[3968];
@@ -663,7 +663,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40928] * w;
       out[4544] = fma(kw, y[896], out[4544]);
       out[896] = fma(kw, y[4544], out[896]);
-      ws[177408] = fma(kw * y[4544], y[896], ws[177408]);
+      ws[182176] = fma(kw * y[4544], y[896], ws[182176]);
     }
     {
       double w = 1.0 * phi[3968];
@@ -676,7 +676,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40960] * w;
       out[4544] = fma(kw, y[832], out[4544]);
       out[832] = fma(kw, y[4544], out[832]);
-      ws[177440] = fma(kw * y[4544], y[832], ws[177440]);
+      ws[182208] = fma(kw * y[4544], y[832], ws[182208]);
     }
     {
       double w = 1.0 * phi[3232];
@@ -688,7 +688,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40992] * w;
       out[4544] = fma(kw, y[2656], out[4544]);
       out[2656] = fma(kw, y[4544], out[2656]);
-      ws[177472] = fma(kw * y[4544], y[2656], ws[177472]);
+      ws[182240] = fma(kw * y[4544], y[2656], ws[182240]);
     }
     {
       double w = 1.0 * phi[3232];
@@ -702,7 +702,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41024] * w;
       out[4544] = fma(kw, y[3552], out[4544]);
       out[3552] = fma(kw, y[4544], out[3552]);
-      ws[177504] = fma(kw * y[4544], y[3552], ws[177504]);
+      ws[182272] = fma(kw * y[4544], y[3552], ws[182272]);
     }
     {
       double w = 0.3 * phi[3968];
@@ -718,7 +718,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41056] * w;
       out[4544] = fma(kw, y[3136], out[4544]);
       out[3136] = fma(kw, y[4544], out[3136]);
-      ws[177536] = fma(kw * y[4544], y[3136], ws[177536]);
+      ws[182304] = fma(kw * y[4544], y[3136], ws[182304]);
     }
     {
       double w = 1.0 * phi[3232];
@@ -731,7 +731,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41088] * w;
       out[4544] = fma(kw, y[2528], out[4544]);
       out[2528] = fma(kw, y[4544], out[2528]);
-      ws[177568] = fma(kw * y[4544], y[2528], ws[177568]);
+      ws[182336] = fma(kw * y[4544], y[2528], ws[182336]);
     }
     {
       double w = 1.0 * phi[3968];
@@ -742,7 +742,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41120] * w;
       out[4544] = fma(kw, y[4512], out[4544]);
       out[4512] = fma(kw, y[4544], out[4512]);
-      ws[177600] = fma(kw * y[4544], y[4512], ws[177600]);
+      ws[182368] = fma(kw * y[4544], y[4512], ws[182368]);
     }
     {
       double w = 1.0 * phi[3968];
@@ -752,7 +752,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41152] * w;
       out[4544] = fma(kw, y[4128], out[4544]);
       out[4128] = fma(kw, y[4544], out[4128]);
-      ws[177632] = fma(kw * y[4544], y[4128], ws[177632]);
+      ws[182400] = fma(kw * y[4544], y[4128], ws[182400]);
     }
     {
       double w = 1.0 * phi[3968];
@@ -762,7 +762,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41184] * w;
       out[4544] = fma(kw, y[4064], out[4544]);
       out[4064] = fma(kw, y[4544], out[4064]);
-      ws[177664] = fma(kw * y[4544], y[4064], ws[177664]);
+      ws[182432] = fma(kw * y[4544], y[4064], ws[182432]);
     }
     {
       double w = 1.0 * phi[3968];
@@ -773,7 +773,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41216] * w;
       out[4544] = fma(kw, y[2720], out[4544]);
       out[2720] = fma(kw, y[4544], out[2720]);
-      ws[177696] = fma(kw * y[4544], y[2720], ws[177696]);
+      ws[182464] = fma(kw * y[4544], y[2720], ws[182464]);
     }
     {
       double w = 1.0 * phi[3968];
@@ -784,7 +784,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41248] * w;
       out[4544] = fma(kw, y[864], out[4544]);
       out[864] = fma(kw, y[4544], out[864]);
-      ws[177728] = fma(kw * y[4544], y[864], ws[177728]);
+      ws[182496] = fma(kw * y[4544], y[864], ws[182496]);
     }
     {
       double w = 1.0 * phi[4544];
@@ -793,7 +793,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41280] * w;
       out[3968] = fma(kw, y[4736], out[3968]);
       out[4736] = fma(kw, y[3968], out[4736]);
-      ws[177760] = fma(kw * y[3968], y[4736], ws[177760]);
+      ws[182528] = fma(kw * y[3968], y[4736], ws[182528]);
     }
     {
       double w = 1.0 * phi[3968];
@@ -810,7 +810,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41312] * w;
       out[4544] = fma(kw, y[1088], out[4544]);
       out[1088] = fma(kw, y[4544], out[1088]);
-      ws[177792] = fma(kw * y[4544], y[1088], ws[177792]);
+      ws[182560] = fma(kw * y[4544], y[1088], ws[182560]);
     }
     {
       double w = 1.0 * phi[3968];
@@ -827,7 +827,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41344] * w;
       out[4544] = fma(kw, y[1120], out[4544]);
       out[1120] = fma(kw, y[4544], out[1120]);
-      ws[177824] = fma(kw * y[4544], y[1120], ws[177824]);
+      ws[182592] = fma(kw * y[4544], y[1120], ws[182592]);
     }
     {
       double w = 1.0 * phi[3968];
@@ -844,7 +844,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41376] * w;
       out[4544] = fma(kw, y[1152], out[4544]);
       out[1152] = fma(kw, y[4544], out[1152]);
-      ws[177856] = fma(kw * y[4544], y[1152], ws[177856]);
+      ws[182624] = fma(kw * y[4544], y[1152], ws[182624]);
     }
     {
       double w = 1.0 * phi[4544];
@@ -852,7 +852,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       w = w - phi[2592];
       const double kw = ws[41408] * w;
       out[2592] = out[2592] + kw;
-      ws[177888] = fma(kw, y[2592], ws[177888]);
+      ws[182656] = fma(kw, y[2592], ws[182656]);
     }
     {
       double w = 1.0 * phi[1216];
@@ -861,7 +861,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41440] * w;
       out[3520] = fma(kw, y[4608], out[3520]);
       out[4608] = fma(kw, y[3520], out[4608]);
-      ws[177920] = fma(kw * y[3520], y[4608], ws[177920]);
+      ws[182688] = fma(kw * y[3520], y[4608], ws[182688]);
     }
     {
       double w = 1.0 * phi[3520];
@@ -869,7 +869,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       w = w - phi[1216];
       const double kw = ws[41472] * w;
       out[1216] = out[1216] + kw;
-      ws[177952] = fma(kw, y[1216], ws[177952]);
+      ws[182720] = fma(kw, y[1216], ws[182720]);
     }
     {
       double w = 1.0 * phi[4544];
@@ -877,7 +877,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       w = w - phi[1216];
       const double kw = ws[41504] * w;
       out[1216] = out[1216] + kw;
-      ws[177984] = fma(kw, y[1216], ws[177984]);
+      ws[182752] = fma(kw, y[1216], ws[182752]);
     }
     {
       double w = 1.0 * phi[1824];
@@ -885,7 +885,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       w = w - phi[1216];
       const double kw = ws[41536] * w;
       out[1216] = out[1216] + kw;
-      ws[178016] = fma(kw, y[1216], ws[178016]);
+      ws[182784] = fma(kw, y[1216], ws[182784]);
     }
     {
       double w = 1.0 * phi[1824];
@@ -893,7 +893,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       w = w - phi[1216];
       const double kw = ws[41568] * w;
       out[1216] = out[1216] + kw;
-      ws[178048] = fma(kw, y[1216], ws[178048]);
+      ws[182816] = fma(kw, y[1216], ws[182816]);
     }
     {
       double w = 1.0 * phi[4384];
@@ -905,7 +905,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41600] * w;
       out[2944] = fma(kw, y[4384], out[2944]);
       out[4384] = fma(kw, y[2944], out[4384]);
-      ws[178080] = fma(kw * y[2944], y[4384], ws[178080]);
+      ws[182848] = fma(kw * y[2944], y[4384], ws[182848]);
     }
     {
       double w = 1.0 * phi[4704];
@@ -915,7 +915,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41632] * w;
       out[2944] = fma(kw, y[4704], out[2944]);
       out[4704] = fma(kw, y[2944], out[4704]);
-      ws[178112] = fma(kw * y[2944], y[4704], ws[178112]);
+      ws[182880] = fma(kw * y[2944], y[4704], ws[182880]);
     }
     {
       double w = 1.0 * phi[4384];
@@ -927,7 +927,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41664] * w;
       out[2496] = fma(kw, y[4384], out[2496]);
       out[4384] = fma(kw, y[2496], out[4384]);
-      ws[178144] = fma(kw * y[2496], y[4384], ws[178144]);
+      ws[182912] = fma(kw * y[2496], y[4384], ws[182912]);
     }
     {
       double w = 1.0 * phi[4704];
@@ -937,7 +937,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41696] * w;
       out[2496] = fma(kw, y[4704], out[2496]);
       out[4704] = fma(kw, y[2496], out[4704]);
-      ws[178176] = fma(kw * y[2496], y[4704], ws[178176]);
+      ws[182944] = fma(kw * y[2496], y[4704], ws[182944]);
     }
     {
       double w = 1.0 * phi[4384];
@@ -948,7 +948,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41728] * w;
       out[2144] = fma(kw, y[4384], out[2144]);
       out[4384] = fma(kw, y[2144], out[4384]);
-      ws[178208] = fma(kw * y[2144], y[4384], ws[178208]);
+      ws[182976] = fma(kw * y[2144], y[4384], ws[182976]);
     }
     {
       double w = 1.0 * phi[4704];
@@ -958,7 +958,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41760] * w;
       out[2144] = fma(kw, y[4704], out[2144]);
       out[4704] = fma(kw, y[2144], out[4704]);
-      ws[178240] = fma(kw * y[2144], y[4704], ws[178240]);
+      ws[183008] = fma(kw * y[2144], y[4704], ws[183008]);
     }
     {
       double w = 1.0 * phi[4320];
@@ -968,7 +968,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41792] * w;
       out[1856] = fma(kw, y[4320], out[1856]);
       out[4320] = fma(kw, y[1856], out[4320]);
-      ws[178272] = fma(kw * y[1856], y[4320], ws[178272]);
+      ws[183040] = fma(kw * y[1856], y[4320], ws[183040]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -978,7 +978,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41824] * w;
       out[1856] = fma(kw, y[4736], out[1856]);
       out[4736] = fma(kw, y[1856], out[4736]);
-      ws[178304] = fma(kw * y[1856], y[4736], ws[178304]);
+      ws[183072] = fma(kw * y[1856], y[4736], ws[183072]);
     }
     {
       double w = 1.0 * phi[4640];
@@ -988,7 +988,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41856] * w;
       out[1856] = fma(kw, y[4640], out[1856]);
       out[4640] = fma(kw, y[1856], out[4640]);
-      ws[178336] = fma(kw * y[1856], y[4640], ws[178336]);
+      ws[183104] = fma(kw * y[1856], y[4640], ws[183104]);
     }
     {
       double w = 1.0 * phi[4384];
@@ -1000,7 +1000,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41888] * w;
       out[2560] = fma(kw, y[4384], out[2560]);
       out[4384] = fma(kw, y[2560], out[4384]);
-      ws[178368] = fma(kw * y[2560], y[4384], ws[178368]);
+      ws[183136] = fma(kw * y[2560], y[4384], ws[183136]);
     }
 }
 __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int phioff, int outoff)
@@ -1016,7 +1016,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41920] * w;
       out[2560] = fma(kw, y[4704], out[2560]);
       out[4704] = fma(kw, y[2560], out[4704]);
-      ws[178400] = fma(kw * y[2560], y[4704], ws[178400]);
+      ws[183168] = fma(kw * y[2560], y[4704], ws[183168]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1028,14 +1028,14 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41952] * w;
       out[448] = fma(kw, y[4736], out[448]);
       out[4736] = fma(kw, y[448], out[4736]);
-      ws[178432] = fma(kw * y[448], y[4736], ws[178432]);
+      ws[183200] = fma(kw * y[448], y[4736], ws[183200]);
     }
     {
       double w = 1.0 * phi[4192];
       w = w - phi[4032];
       const double kw = ws[41984] * w;
       out[4032] = out[4032] + kw;
-      ws[178464] = fma(kw, y[4032], ws[178464]);
+      ws[183232] = fma(kw, y[4032], ws[183232]);
     }
     {
       double w = 1.0 * phi[4192];
@@ -1043,7 +1043,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       w = w - phi[1280];
       const double kw = ws[42016] * w;
       out[1280] = out[1280] + kw;
-      ws[178496] = fma(kw, y[1280], ws[178496]);
+      ws[183264] = fma(kw, y[1280], ws[183264]);
     }
     {
       double w = 1.0 * phi[4192];
@@ -1051,21 +1051,21 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       w = w - phi[1280];
       const double kw = ws[42048] * w;
       out[1280] = out[1280] + kw;
-      ws[178528] = fma(kw, y[1280], ws[178528]);
+      ws[183296] = fma(kw, y[1280], ws[183296]);
     }
     {
       double w = 1.0 * phi[4192];
       w = w - phi[1920];
       const double kw = ws[42080] * w;
       out[1920] = out[1920] + kw;
-      ws[178560] = fma(kw, y[1920], ws[178560]);
+      ws[183328] = fma(kw, y[1920], ws[183328]);
     }
     {
       double w = 1.0 * phi[4192];
       w = w - phi[1248];
       const double kw = ws[42112] * w;
       out[1248] = out[1248] + kw;
-      ws[178592] = fma(kw, y[1248], ws[178592]);
+      ws[183360] = fma(kw, y[1248], ws[183360]);
     }
     {
       double w = 1.0 * phi[2592];
@@ -1074,7 +1074,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[42144] * w;
       out[1920] = fma(kw, y[480], out[1920]);
       out[480] = fma(kw, y[1920], out[480]);
-      ws[178624] = fma(kw * y[1920], y[480], ws[178624]);
+      ws[183392] = fma(kw * y[1920], y[480], ws[183392]);
     }
     {
       double w = 1.0 * phi[2592];
@@ -1083,7 +1083,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[42176] * w;
       out[1920] = fma(kw, y[512], out[1920]);
       out[512] = fma(kw, y[1920], out[512]);
-      ws[178656] = fma(kw * y[1920], y[512], ws[178656]);
+      ws[183424] = fma(kw * y[1920], y[512], ws[183424]);
     }
     {
       double w = 1.0 * phi[2592];
@@ -1092,7 +1092,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[42208] * w;
       out[1248] = fma(kw, y[544], out[1248]);
       out[544] = fma(kw, y[1248], out[544]);
-      ws[178688] = fma(kw * y[1248], y[544], ws[178688]);
+      ws[183456] = fma(kw * y[1248], y[544], ws[183456]);
     }
     {
       double w = 0.5 * phi[2464];
@@ -1100,20 +1100,20 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       w = w - phi[4608];
       const double kw = ws[42240] * w;
       out[4608] = out[4608] + kw;
-      ws[178720] = fma(kw, y[4608], ws[178720]);
+      ws[183488] = fma(kw, y[4608], ws[183488]);
     }
     {
       double w = -phi[4320];
       const double kw = ws[42272] * w;
       out[4320] = out[4320] + kw;
-      ws[178752] = fma(kw, y[4320], ws[178752]);
+      ws[183520] = fma(kw, y[4320], ws[183520]);
     }
     {
       double w = 1.0 * phi[1312];
       w = w - phi[1056];
       const double kw = ws[42304] * w;
       out[1056] = out[1056] + kw;
-      ws[178784] = fma(kw, y[1056], ws[178784]);
+      ws[183552] = fma(kw, y[1056], ws[183552]);
     }
     {
       double w = 1.0 * phi[608];
@@ -1122,28 +1122,28 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[42336] * w;
       out[1312] = fma(kw, y[576], out[1312]);
       out[576] = fma(kw, y[1312], out[576]);
-      ws[178816] = fma(kw * y[1312], y[576], ws[178816]);
+      ws[183584] = fma(kw * y[1312], y[576], ws[183584]);
     }
     {
       double w = 1.0 * phi[608];
       w = w - phi[1312];
       const double kw = ws[42368] * w;
       out[1312] = out[1312] + kw;
-      ws[178848] = fma(kw, y[1312], ws[178848]);
+      ws[183616] = fma(kw, y[1312], ws[183616]);
     }
     {
       double w = 1.0 * phi[640];
       w = w - phi[4256];
       const double kw = ws[42400] * w;
       out[4256] = out[4256] + kw;
-      ws[178880] = fma(kw, y[4256], ws[178880]);
+      ws[183648] = fma(kw, y[4256], ws[183648]);
     }
     {
       double w = 1.0 * phi[640];
       w = w - phi[4000];
       const double kw = ws[42432] * w;
       out[4000] = out[4000] + kw;
-      ws[178912] = fma(kw, y[4000], ws[178912]);
+      ws[183680] = fma(kw, y[4000], ws[183680]);
     }
     {
       double w = 1.0 * phi[4384];
@@ -1153,7 +1153,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[42464] * w;
       out[2848] = fma(kw, y[4384], out[2848]);
       out[4384] = fma(kw, y[2848], out[4384]);
-      ws[178944] = fma(kw * y[2848], y[4384], ws[178944]);
+      ws[183712] = fma(kw * y[2848], y[4384], ws[183712]);
     }
     {
       double w = 1.0 * phi[4704];
@@ -1163,7 +1163,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[42496] * w;
       out[2848] = fma(kw, y[4704], out[2848]);
       out[4704] = fma(kw, y[2848], out[4704]);
-      ws[178976] = fma(kw * y[2848], y[4704], ws[178976]);
+      ws[183744] = fma(kw * y[2848], y[4704], ws[183744]);
     }
     {
       double w = 1.0 * phi[4640];
@@ -1173,7 +1173,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[42528] * w;
       out[2848] = fma(kw, y[4640], out[2848]);
       out[4640] = fma(kw, y[2848], out[4640]);
-      ws[179008] = fma(kw * y[2848], y[4640], ws[179008]);
+      ws[183776] = fma(kw * y[2848], y[4640], ws[183776]);
     }
     {
       double w = 1.0 * phi[4672];
@@ -1183,7 +1183,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[42560] * w;
       out[2848] = fma(kw, y[4672], out[2848]);
       out[4672] = fma(kw, y[2848], out[4672]);
-      ws[179040] = fma(kw * y[2848], y[4672], ws[179040]);
+      ws[183808] = fma(kw * y[2848], y[4672], ws[183808]);
     }
     {
       double w = 1.0 * phi[4544];
@@ -1193,7 +1193,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[42592] * w;
       out[3360] = fma(kw, y[4544], out[3360]);
       out[4544] = fma(kw, y[3360], out[4544]);
-      ws[179072] = fma(kw * y[3360], y[4544], ws[179072]);
+      ws[183840] = fma(kw * y[3360], y[4544], ws[183840]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1203,62 +1203,62 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[42624] * w;
       out[3360] = fma(kw, y[4736], out[3360]);
       out[4736] = fma(kw, y[3360], out[4736]);
-      ws[179104] = fma(kw * y[3360], y[4736], ws[179104]);
+      ws[183872] = fma(kw * y[3360], y[4736], ws[183872]);
     }
     {
       double w = -phi[3360];
       const double kw = ws[42656] * w;
       out[3360] = out[3360] + kw;
-      ws[179136] = fma(kw, y[3360], ws[179136]);
+      ws[183904] = fma(kw, y[3360], ws[183904]);
     }
     {
       double w = 1.0 * phi[32];
       w = w - phi[0];
       const double kw = ws[42688] * w;
       out[0] = out[0] + kw;
-      ws[179168] = fma(kw, y[0], ws[179168]);
+      ws[183936] = fma(kw, y[0], ws[183936]);
     }
     {
       double w = 0.907 * phi[1376];
       w = w - phi[64];
       const double kw = ws[42720] * w;
       out[64] = out[64] + kw;
-      ws[179200] = fma(kw, y[64], ws[179200]);
+      ws[183968] = fma(kw, y[64], ws[183968]);
     }
     {
       double w = 0.925 * phi[1376];
       w = w - phi[96];
       const double kw = ws[42752] * w;
       out[96] = out[96] + kw;
-      ws[179232] = fma(kw, y[96], ws[179232]);
+      ws[184000] = fma(kw, y[96], ws[184000]);
     }
     {
       double w = 0.943 * phi[1376];
       w = w - phi[128];
       const double kw = ws[42784] * w;
       out[128] = out[128] + kw;
-      ws[179264] = fma(kw, y[128], ws[179264]);
+      ws[184032] = fma(kw, y[128], ws[184032]);
     }
     {
       double w = 0.5 * phi[1408];
       w = w - phi[160];
       const double kw = ws[42816] * w;
       out[160] = out[160] + kw;
-      ws[179296] = fma(kw, y[160], ws[179296]);
+      ws[184064] = fma(kw, y[160], ws[184064]);
     }
     {
       double w = 0.5 * phi[1408];
       w = w - phi[192];
       const double kw = ws[42848] * w;
       out[192] = out[192] + kw;
-      ws[179328] = fma(kw, y[192], ws[179328]);
+      ws[184096] = fma(kw, y[192], ws[184096]);
     }
     {
       double w = 1.5 * phi[1408];
       w = w - phi[224];
       const double kw = ws[42880] * w;
       out[224] = out[224] + kw;
-      ws[179360] = fma(kw, y[224], ws[179360]);
+      ws[184128] = fma(kw, y[224], ws[184128]);
     }
     {
       double w = 1.25 * phi[1440];
@@ -1269,7 +1269,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[42912] * w;
       out[704] = fma(kw, y[4736], out[704]);
       out[4736] = fma(kw, y[704], out[4736]);
-      ws[179392] = fma(kw * y[704], y[4736], ws[179392]);
+      ws[184160] = fma(kw * y[704], y[4736], ws[184160]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1278,7 +1278,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[42944] * w;
       out[1440] = fma(kw, y[4736], out[1440]);
       out[4736] = fma(kw, y[1440], out[4736]);
-      ws[179424] = fma(kw * y[1440], y[4736], ws[179424]);
+      ws[184192] = fma(kw * y[1440], y[4736], ws[184192]);
     }
     {
       double w = 1.25 * phi[1472];
@@ -1289,7 +1289,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[42976] * w;
       out[736] = fma(kw, y[4736], out[736]);
       out[4736] = fma(kw, y[736], out[4736]);
-      ws[179456] = fma(kw * y[736], y[4736], ws[179456]);
+      ws[184224] = fma(kw * y[736], y[4736], ws[184224]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1298,7 +1298,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43008] * w;
       out[1472] = fma(kw, y[4736], out[1472]);
       out[4736] = fma(kw, y[1472], out[4736]);
-      ws[179488] = fma(kw * y[1472], y[4736], ws[179488]);
+      ws[184256] = fma(kw * y[1472], y[4736], ws[184256]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1308,7 +1308,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43040] * w;
       out[768] = fma(kw, y[4736], out[768]);
       out[4736] = fma(kw, y[768], out[4736]);
-      ws[179520] = fma(kw * y[768], y[4736], ws[179520]);
+      ws[184288] = fma(kw * y[768], y[4736], ws[184288]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1326,7 +1326,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43072] * w;
       out[2752] = fma(kw, y[4736], out[2752]);
       out[4736] = fma(kw, y[2752], out[4736]);
-      ws[179552] = fma(kw * y[2752], y[4736], ws[179552]);
+      ws[184320] = fma(kw * y[2752], y[4736], ws[184320]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1341,7 +1341,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43104] * w;
       out[2784] = fma(kw, y[4736], out[2784]);
       out[4736] = fma(kw, y[2784], out[4736]);
-      ws[179584] = fma(kw * y[2784], y[4736], ws[179584]);
+      ws[184352] = fma(kw * y[2784], y[4736], ws[184352]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1356,7 +1356,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43136] * w;
       out[2816] = fma(kw, y[4736], out[2816]);
       out[4736] = fma(kw, y[2816], out[4736]);
-      ws[179616] = fma(kw * y[2816], y[4736], ws[179616]);
+      ws[184384] = fma(kw * y[2816], y[4736], ws[184384]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1371,7 +1371,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43168] * w;
       out[2304] = fma(kw, y[4736], out[2304]);
       out[4736] = fma(kw, y[2304], out[4736]);
-      ws[179648] = fma(kw * y[2304], y[4736], ws[179648]);
+      ws[184416] = fma(kw * y[2304], y[4736], ws[184416]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1385,7 +1385,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43200] * w;
       out[1504] = fma(kw, y[4736], out[1504]);
       out[4736] = fma(kw, y[1504], out[4736]);
-      ws[179680] = fma(kw * y[1504], y[4736], ws[179680]);
+      ws[184448] = fma(kw * y[1504], y[4736], ws[184448]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1399,7 +1399,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43232] * w;
       out[3680] = fma(kw, y[4736], out[3680]);
       out[4736] = fma(kw, y[3680], out[4736]);
-      ws[179712] = fma(kw * y[3680], y[4736], ws[179712]);
+      ws[184480] = fma(kw * y[3680], y[4736], ws[184480]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1413,7 +1413,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43264] * w;
       out[3712] = fma(kw, y[4736], out[3712]);
       out[4736] = fma(kw, y[3712], out[4736]);
-      ws[179744] = fma(kw * y[3712], y[4736], ws[179744]);
+      ws[184512] = fma(kw * y[3712], y[4736], ws[184512]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1427,7 +1427,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43296] * w;
       out[2912] = fma(kw, y[4736], out[2912]);
       out[4736] = fma(kw, y[2912], out[4736]);
-      ws[179776] = fma(kw * y[2912], y[4736], ws[179776]);
+      ws[184544] = fma(kw * y[2912], y[4736], ws[184544]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1441,7 +1441,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43328] * w;
       out[3168] = fma(kw, y[4736], out[3168]);
       out[4736] = fma(kw, y[3168], out[4736]);
-      ws[179808] = fma(kw * y[3168], y[4736], ws[179808]);
+      ws[184576] = fma(kw * y[3168], y[4736], ws[184576]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1455,7 +1455,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43360] * w;
       out[3200] = fma(kw, y[4736], out[3200]);
       out[4736] = fma(kw, y[3200], out[4736]);
-      ws[179840] = fma(kw * y[3200], y[4736], ws[179840]);
+      ws[184608] = fma(kw * y[3200], y[4736], ws[184608]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1464,7 +1464,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43392] * w;
       out[2336] = fma(kw, y[4736], out[2336]);
       out[4736] = fma(kw, y[2336], out[4736]);
-      ws[179872] = fma(kw * y[2336], y[4736], ws[179872]);
+      ws[184640] = fma(kw * y[2336], y[4736], ws[184640]);
     }
     {
       double w = 1.0 * phi[4640];
@@ -1473,7 +1473,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43424] * w;
       out[2336] = fma(kw, y[4640], out[2336]);
       out[4640] = fma(kw, y[2336], out[4640]);
-      ws[179904] = fma(kw * y[2336], y[4640], ws[179904]);
+      ws[184672] = fma(kw * y[2336], y[4640], ws[184672]);
     }
     {
       double w = 1.0 * phi[4160];
@@ -1482,19 +1482,19 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43456] * w;
       out[2336] = fma(kw, y[4160], out[2336]);
       out[4160] = fma(kw, y[2336], out[4160]);
-      ws[179936] = fma(kw * y[2336], y[4160], ws[179936]);
+      ws[184704] = fma(kw * y[2336], y[4160], ws[184704]);
     }
     {
       double w = -phi[2336];
       const double kw = ws[43488] * w;
       out[2336] = out[2336] + kw;
-      ws[179968] = fma(kw, y[2336], ws[179968]);
+      ws[184736] = fma(kw, y[2336], ws[184736]);
     }
     {
       double w = -phi[2336];
       const double kw = ws[43520] * w;
       out[2336] = out[2336] + kw;
-      ws[180000] = fma(kw, y[2336], ws[180000]);
+      ws[184768] = fma(kw, y[2336], ws[184768]);
     }
     {
       double w = 1.0 * phi[4544];
@@ -1503,7 +1503,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43552] * w;
       out[2336] = fma(kw, y[4544], out[2336]);
       out[4544] = fma(kw, y[2336], out[4544]);
-      ws[180032] = fma(kw * y[2336], y[4544], ws[180032]);
+      ws[184800] = fma(kw * y[2336], y[4544], ws[184800]);
     }
 }
 __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int phioff, int outoff)
@@ -1518,7 +1518,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43584] * w;
       out[2368] = fma(kw, y[4736], out[2368]);
       out[4736] = fma(kw, y[2368], out[4736]);
-      ws[180064] = fma(kw * y[2368], y[4736], ws[180064]);
+      ws[184832] = fma(kw * y[2368], y[4736], ws[184832]);
     }
     {
       double w = 1.0 * phi[4640];
@@ -1527,7 +1527,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43616] * w;
       out[2368] = fma(kw, y[4640], out[2368]);
       out[4640] = fma(kw, y[2368], out[4640]);
-      ws[180096] = fma(kw * y[2368], y[4640], ws[180096]);
+      ws[184864] = fma(kw * y[2368], y[4640], ws[184864]);
     }
     {
       double w = 1.0 * phi[4160];
@@ -1536,13 +1536,13 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43648] * w;
       out[2368] = fma(kw, y[4160], out[2368]);
       out[4160] = fma(kw, y[2368], out[4160]);
-      ws[180128] = fma(kw * y[2368], y[4160], ws[180128]);
+      ws[184896] = fma(kw * y[2368], y[4160], ws[184896]);
     }
     {
       double w = -phi[2368];
       const double kw = ws[43680] * w;
       out[2368] = out[2368] + kw;
-      ws[180160] = fma(kw, y[2368], ws[180160]);
+      ws[184928] = fma(kw, y[2368], ws[184928]);
     }
     {
       double w = 1.0 * phi[4544];
@@ -1551,7 +1551,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43712] * w;
       out[2368] = fma(kw, y[4544], out[2368]);
       out[4544] = fma(kw, y[2368], out[4544]);
-      ws[180192] = fma(kw * y[2368], y[4544], ws[180192]);
+      ws[184960] = fma(kw * y[2368], y[4544], ws[184960]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1561,7 +1561,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43744] * w;
       out[2400] = fma(kw, y[4736], out[2400]);
       out[4736] = fma(kw, y[2400], out[4736]);
-      ws[180224] = fma(kw * y[2400], y[4736], ws[180224]);
+      ws[184992] = fma(kw * y[2400], y[4736], ws[184992]);
     }
     {
       double w = 1.0 * phi[4320];
@@ -1571,7 +1571,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43776] * w;
       out[2400] = fma(kw, y[4320], out[2400]);
       out[4320] = fma(kw, y[2400], out[4320]);
-      ws[180256] = fma(kw * y[2400], y[4320], ws[180256]);
+      ws[185024] = fma(kw * y[2400], y[4320], ws[185024]);
     }
     {
       double w = 1.0 * phi[4640];
@@ -1581,7 +1581,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43808] * w;
       out[2400] = fma(kw, y[4640], out[2400]);
       out[4640] = fma(kw, y[2400], out[4640]);
-      ws[180288] = fma(kw * y[2400], y[4640], ws[180288]);
+      ws[185056] = fma(kw * y[2400], y[4640], ws[185056]);
     }
     {
       double w = 1.0 * phi[4544];
@@ -1591,7 +1591,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43840] * w;
       out[2400] = fma(kw, y[4544], out[2400]);
       out[4544] = fma(kw, y[2400], out[4544]);
-      ws[180320] = fma(kw * y[2400], y[4544], ws[180320]);
+      ws[185088] = fma(kw * y[2400], y[4544], ws[185088]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1600,7 +1600,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43872] * w;
       out[2432] = fma(kw, y[4736], out[2432]);
       out[4736] = fma(kw, y[2432], out[4736]);
-      ws[180352] = fma(kw * y[2432], y[4736], ws[180352]);
+      ws[185120] = fma(kw * y[2432], y[4736], ws[185120]);
     }
     {
       double w = 1.0 * phi[4320];
@@ -1609,7 +1609,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43904] * w;
       out[2432] = fma(kw, y[4320], out[2432]);
       out[4320] = fma(kw, y[2432], out[4320]);
-      ws[180384] = fma(kw * y[2432], y[4320], ws[180384]);
+      ws[185152] = fma(kw * y[2432], y[4320], ws[185152]);
     }
     {
       double w = 1.0 * phi[4640];
@@ -1618,13 +1618,13 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43936] * w;
       out[2432] = fma(kw, y[4640], out[2432]);
       out[4640] = fma(kw, y[2432], out[4640]);
-      ws[180416] = fma(kw * y[2432], y[4640], ws[180416]);
+      ws[185184] = fma(kw * y[2432], y[4640], ws[185184]);
     }
     {
       double w = -phi[2432];
       const double kw = ws[43968] * w;
       out[2432] = out[2432] + kw;
-      ws[180448] = fma(kw, y[2432], ws[180448]);
+      ws[185216] = fma(kw, y[2432], ws[185216]);
     }
     {
       double w = 1.0 * phi[4544];
@@ -1633,7 +1633,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44000] * w;
       out[2432] = fma(kw, y[4544], out[2432]);
       out[4544] = fma(kw, y[2432], out[4544]);
-      ws[180480] = fma(kw * y[2432], y[4544], ws[180480]);
+      ws[185248] = fma(kw * y[2432], y[4544], ws[185248]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1642,7 +1642,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44032] * w;
       out[2976] = fma(kw, y[4736], out[2976]);
       out[4736] = fma(kw, y[2976], out[4736]);
-      ws[180512] = fma(kw * y[2976], y[4736], ws[180512]);
+      ws[185280] = fma(kw * y[2976], y[4736], ws[185280]);
     }
     {
       double w = 1.0 * phi[4320];
@@ -1651,7 +1651,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44064] * w;
       out[2976] = fma(kw, y[4320], out[2976]);
       out[4320] = fma(kw, y[2976], out[4320]);
-      ws[180544] = fma(kw * y[2976], y[4320], ws[180544]);
+      ws[185312] = fma(kw * y[2976], y[4320], ws[185312]);
     }
     {
       double w = 1.0 * phi[4640];
@@ -1660,13 +1660,13 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44096] * w;
       out[2976] = fma(kw, y[4640], out[2976]);
       out[4640] = fma(kw, y[2976], out[4640]);
-      ws[180576] = fma(kw * y[2976], y[4640], ws[180576]);
+      ws[185344] = fma(kw * y[2976], y[4640], ws[185344]);
     }
     {
       double w = -phi[2976];
       const double kw = ws[44128] * w;
       out[2976] = out[2976] + kw;
-      ws[180608] = fma(kw, y[2976], ws[180608]);
+      ws[185376] = fma(kw, y[2976], ws[185376]);
     }
     {
       double w = 1.0 * phi[4544];
@@ -1675,7 +1675,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44160] * w;
       out[2976] = fma(kw, y[4544], out[2976]);
       out[4544] = fma(kw, y[2976], out[4544]);
-      ws[180640] = fma(kw * y[2976], y[4544], ws[180640]);
+      ws[185408] = fma(kw * y[2976], y[4544], ws[185408]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1684,7 +1684,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44192] * w;
       out[1536] = fma(kw, y[4736], out[1536]);
       out[4736] = fma(kw, y[1536], out[4736]);
-      ws[180672] = fma(kw * y[1536], y[4736], ws[180672]);
+      ws[185440] = fma(kw * y[1536], y[4736], ws[185440]);
     }
     {
       double w = 1.0 * phi[4544];
@@ -1693,7 +1693,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44224] * w;
       out[1536] = fma(kw, y[4544], out[1536]);
       out[4544] = fma(kw, y[1536], out[4544]);
-      ws[180704] = fma(kw * y[1536], y[4544], ws[180704]);
+      ws[185472] = fma(kw * y[1536], y[4544], ws[185472]);
     }
     {
       double w = 0.5 * phi[1568];
@@ -1704,7 +1704,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44256] * w;
       out[3008] = fma(kw, y[4320], out[3008]);
       out[4320] = fma(kw, y[3008], out[4320]);
-      ws[180736] = fma(kw * y[3008], y[4320], ws[180736]);
+      ws[185504] = fma(kw * y[3008], y[4320], ws[185504]);
     }
     {
       double w = 1.0 * phi[3040];
@@ -1714,7 +1714,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44288] * w;
       out[3008] = fma(kw, y[1184], out[3008]);
       out[1184] = fma(kw, y[3008], out[1184]);
-      ws[180768] = fma(kw * y[3008], y[1184], ws[180768]);
+      ws[185536] = fma(kw * y[3008], y[1184], ws[185536]);
     }
     {
       double w = 1.0 * phi[3040];
@@ -1724,7 +1724,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44320] * w;
       out[3008] = fma(kw, y[3456], out[3008]);
       out[3456] = fma(kw, y[3008], out[3456]);
-      ws[180800] = fma(kw * y[3008], y[3456], ws[180800]);
+      ws[185568] = fma(kw * y[3008], y[3456], ws[185568]);
     }
     {
       double w = 0.5 * phi[1568];
@@ -1735,7 +1735,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44352] * w;
       out[3008] = fma(kw, y[4736], out[3008]);
       out[4736] = fma(kw, y[3008], out[4736]);
-      ws[180832] = fma(kw * y[3008], y[4736], ws[180832]);
+      ws[185600] = fma(kw * y[3008], y[4736], ws[185600]);
     }
     {
       double w = 0.5 * phi[3008];
@@ -1746,7 +1746,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44384] * w;
       out[3008] = fma(kw, y[4544], out[3008]);
       out[4544] = fma(kw, y[3008], out[4544]);
-      ws[180864] = fma(kw * y[3008], y[4544], ws[180864]);
+      ws[185632] = fma(kw * y[3008], y[4544], ws[185632]);
     }
     {
       double w = 1.0 * phi[2208];
@@ -1757,7 +1757,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44416] * w;
       out[2016] = fma(kw, y[4736], out[2016]);
       out[4736] = fma(kw, y[2016], out[4736]);
-      ws[180896] = fma(kw * y[2016], y[4736], ws[180896]);
+      ws[185664] = fma(kw * y[2016], y[4736], ws[185664]);
     }
     {
       double w = 0.75 * phi[2208];
@@ -1768,7 +1768,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44448] * w;
       out[2016] = fma(kw, y[4736], out[2016]);
       out[4736] = fma(kw, y[2016], out[4736]);
-      ws[180928] = fma(kw * y[2016], y[4736], ws[180928]);
+      ws[185696] = fma(kw * y[2016], y[4736], ws[185696]);
     }
     {
       double w = 1.0 * phi[2208];
@@ -1780,7 +1780,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44480] * w;
       out[2016] = fma(kw, y[4640], out[2016]);
       out[4640] = fma(kw, y[2016], out[4640]);
-      ws[180960] = fma(kw * y[2016], y[4640], ws[180960]);
+      ws[185728] = fma(kw * y[2016], y[4640], ws[185728]);
     }
     {
       double w = 0.86 * phi[2208];
@@ -1794,7 +1794,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44512] * w;
       out[2016] = fma(kw, y[4544], out[2016]);
       out[4544] = fma(kw, y[2016], out[4544]);
-      ws[180992] = fma(kw * y[2016], y[4544], ws[180992]);
+      ws[185760] = fma(kw * y[2016], y[4544], ws[185760]);
     }
 }
 }  // namespace mech_cb6r5_ae7_aq

@@ -6,12 +6,12 @@ namespace mech_cb6r5_ae7_aq {
 __device__ __noinline__ void adj_hess3_1_16(double* __restrict__ ws)
 {
     const double* __restrict__ y = ws + 0;
-    double* __restrict__ lam = ws + 131712;
-    const double* __restrict__ n1 = ws + 136480;
+    double* __restrict__ lam = ws + 136480;
+    const double* __restrict__ n1 = ws + 141248;
     const double* __restrict__ k1 = ws + 19072;
-    const double* __restrict__ n2 = ws + 141248;
+    const double* __restrict__ n2 = ws + 146016;
     const double* __restrict__ k2 = ws + 23840;
-    const double* __restrict__ n3 = ws + 146016;
+    const double* __restrict__ n3 = ws + 150784;
     const double* __restrict__ k3 = ws + 28608;
     {
       double w1 = 1.0 * n1[4736];
@@ -30,7 +30,7 @@ __device__ __noinline__ void adj_hess3_1_16(double* __restrict__ ws)
       wk1 = fma(w2, k2[4736], wk1);
       wk1 = fma(w3, k3[4736], wk1);
       const double kk = ws[43872];
-      ws[180352] = fma(-kk, fma(y[4736], wk0, y[2432] * wk1), ws[180352]);
+      ws[185120] = fma(-kk, fma(y[4736], wk0, y[2432] * wk1), ws[185120]);
       lam[2432] = fma(-kk, wk1, lam[2432]);
       lam[4736] = fma(-kk, wk0, lam[4736]);
     }
@@ -51,7 +51,7 @@ __device__ __noinline__ void adj_hess3_1_16(double* __restrict__ ws)
       wk1 = fma(w2, k2[4320], wk1);
       wk1 = fma(w3, k3[4320], wk1);
       const double kk = ws[43904];
-      ws[180384] = fma(-kk, fma(y[4320], wk0, y[2432] * wk1), ws[180384]);
+      ws[185152] = fma(-kk, fma(y[4320], wk0, y[2432] * wk1), ws[185152]);
       lam[2432] = fma(-kk, wk1, lam[2432]);
       lam[4320] = fma(-kk, wk0, lam[4320]);
     }
@@ -72,7 +72,7 @@ __device__ __noinline__ void adj_hess3_1_16(double* __restrict__ ws)
       wk1 = fma(w2, k2[4640], wk1);
       wk1 = fma(w3, k3[4640], wk1);
       const double kk = ws[43936];
-      ws[180416] = fma(-kk, fma(y[4640], wk0, y[2432] * wk1), ws[180416]);
+      ws[185184] = fma(-kk, fma(y[4640], wk0, y[2432] * wk1), ws[185184]);
       lam[2432] = fma(-kk, wk1, lam[2432]);
       lam[4640] = fma(-kk, wk0, lam[4640]);
     }
@@ -93,7 +93,7 @@ __device__ __noinline__ void adj_hess3_1_16(double* __restrict__ ws)
       wk1 = fma(w2, k2[4544], wk1);
       wk1 = fma(w3, k3[4544], wk1);
       const double kk = ws[44000];
-      ws[180480] = fma(-kk, fma(y[4544], wk0, y[2432] * wk1), ws[180480]);
+      ws[185248] = fma(-kk, fma(y[4544], wk0, y[2432] * wk1), ws[185248]);
       lam[2432] = fma(-kk, wk1, lam[2432]);
       lam[4544] = fma(-kk, wk0, lam[4544]);
     }
@@ -114,7 +114,7 @@ __device__ __noinline__ void adj_hess3_1_16(double* __restrict__ ws)
       wk1 = fma(w2, k2[4736], wk1);
       wk1 = fma(w3, k3[4736], wk1);
       const double kk = ws[44032];
-      ws[180512] = fma(-kk, fma(y[4736], wk0, y[2976] * wk1), ws[180512]);
+      ws[185280] = fma(-kk, fma(y[4736], wk0, y[2976] * wk1), ws[185280]);
       lam[2976] = fma(-kk, wk1, lam[2976]);
       lam[4736] = fma(-kk, wk0, lam[4736]);
     }
@@ -135,7 +135,7 @@ __device__ __noinline__ void adj_hess3_1_16(double* __restrict__ ws)
       wk1 = fma(w2, k2[4320], wk1);
       wk1 = fma(w3, k3[4320], wk1);
       const double kk = ws[44064];
-      ws[180544] = fma(-kk, fma(y[4320], wk0, y[2976] * wk1), ws[180544]);
+      ws[185312] = fma(-kk, fma(y[4320], wk0, y[2976] * wk1), ws[185312]);
       lam[2976] = fma(-kk, wk1, lam[2976]);
       lam[4320] = fma(-kk, wk0, lam[4320]);
     }
@@ -156,7 +156,7 @@ __device__ __noinline__ void adj_hess3_1_16(double* __restrict__ ws)
       wk1 = fma(w2, k2[4640], wk1);
       wk1 = fma(w3, k3[4640], wk1);
       const double kk = ws[44096];
-      ws[180576] = fma(-kk, fma(y[4640], wk0, y[2976] * wk1), ws[180576]);
+      ws[185344] = fma(-kk, fma(y[4640], wk0, y[2976] * wk1), ws[185344]);
       lam[2976] = fma(-kk, wk1, lam[2976]);
       lam[4640] = fma(-kk, wk0, lam[4640]);
     }
@@ -177,7 +177,7 @@ __device__ __noinline__ void adj_hess3_1_16(double* __restrict__ ws)
       wk1 = fma(w2, k2[4544], wk1);
       wk1 = fma(w3, k3[4544], wk1);
       const double kk = ws[44160];
-      ws[180640] = fma(-kk, fma(y[4544], wk0, y[2976] * wk1), ws[180640]);
+      ws[185408] = fma(-kk, fma(y[4544], wk0, y[2976] * wk1), ws[185408]);
       lam[2976] = fma(-kk, wk1, lam[2976]);
       lam[4544] = fma(-kk, wk0, lam[4544]);
     }
@@ -198,7 +198,7 @@ __device__ __noinline__ void adj_hess3_1_16(double* __restrict__ ws)
       wk1 = fma(w2, k2[4736], wk1);
       wk1 = fma(w3, k3[4736], wk1);
       const double kk = ws[44192];
-      ws[180672] = fma(-kk, fma(y[4736], wk0, y[1536] * wk1), ws[180672]);
+      ws[185440] = fma(-kk, fma(y[4736], wk0, y[1536] * wk1), ws[185440]);
       lam[1536] = fma(-kk, wk1, lam[1536]);
       lam[4736] = fma(-kk, wk0, lam[4736]);
     }
@@ -219,7 +219,7 @@ __device__ __noinline__ void adj_hess3_1_16(double* __restrict__ ws)
       wk1 = fma(w2, k2[4544], wk1);
       wk1 = fma(w3, k3[4544], wk1);
       const double kk = ws[44224];
-      ws[180704] = fma(-kk, fma(y[4544], wk0, y[1536] * wk1), ws[180704]);
+      ws[185472] = fma(-kk, fma(y[4544], wk0, y[1536] * wk1), ws[185472]);
       lam[1536] = fma(-kk, wk1, lam[1536]);
       lam[4544] = fma(-kk, wk0, lam[4544]);
     }
@@ -246,7 +246,7 @@ __device__ __noinline__ void adj_hess3_1_16(double* __restrict__ ws)
       wk1 = fma(w2, k2[4320], wk1);
       wk1 = fma(w3, k3[4320], wk1);
       const double kk = ws[44256];
-      ws[180736] = fma(-kk, fma(y[4320], wk0, y[3008] * wk1), ws[180736]);
+      ws[185504] = fma(-kk, fma(y[4320], wk0, y[3008] * wk1), ws[185504]);
       lam[3008] = fma(-kk, wk1, lam[3008]);
       lam[4320] = fma(-kk, wk0, lam[4320]);
     }
@@ -270,7 +270,7 @@ __device__ __noinline__ void adj_hess3_1_16(double* __restrict__ ws)
       wk1 = fma(w2, k2[1184], wk1);
       wk1 = fma(w3, k3[1184], wk1);
       const double kk = ws[44288];
-      ws[180768] = fma(-kk, fma(y[1184], wk0, y[3008] * wk1), ws[180768]);
+      ws[185536] = fma(-kk, fma(y[1184], wk0, y[3008] * wk1), ws[185536]);
       lam[3008] = fma(-kk, wk1, lam[3008]);
       lam[1184] = fma(-kk, wk0, lam[1184]);
     }
@@ -294,7 +294,7 @@ __device__ __noinline__ void adj_hess3_1_16(double* __restrict__ ws)
       wk1 = fma(w2, k2[3456], wk1);
       wk1 = fma(w3, k3[3456], wk1);
       const double kk = ws[44320];
-      ws[180800] = fma(-kk, fma(y[3456], wk0, y[3008] * wk1), ws[180800]);
+      ws[185568] = fma(-kk, fma(y[3456], wk0, y[3008] * wk1), ws[185568]);
       lam[3008] = fma(-kk, wk1, lam[3008]);
       lam[3456] = fma(-kk, wk0, lam[3456]);
     }
@@ -321,7 +321,7 @@ __device__ __noinline__ void adj_hess3_1_16(double* __restrict__ ws)
       wk1 = fma(w2, k2[4736], wk1);
       wk1 = fma(w3, k3[4736], wk1);
       const double kk = ws[44352];
-      ws[180832] = fma(-kk, fma(y[4736], wk0, y[3008] * wk1), ws[180832]);
+      ws[185600] = fma(-kk, fma(y[4736], wk0, y[3008] * wk1), ws[185600]);
       lam[3008] = fma(-kk, wk1, lam[3008]);
       lam[4736] = fma(-kk, wk0, lam[4736]);
     }
@@ -348,7 +348,7 @@ __device__ __noinline__ void adj_hess3_1_16(double* __restrict__ ws)
       wk1 = fma(w2, k2[4544], wk1);
       wk1 = fma(w3, k3[4544], wk1);
       const double kk = ws[44384];
-      ws[180864] = fma(-kk, fma(y[4544], wk0, y[3008] * wk1), ws[180864]);
+      ws[185632] = fma(-kk, fma(y[4544], wk0, y[3008] * wk1), ws[185632]);
       lam[3008] = fma(-kk, wk1, lam[3008]);
       lam[4544] = fma(-kk, wk0, lam[4544]);
     }
@@ -375,7 +375,7 @@ __device__ __noinline__ void adj_hess3_1_16(double* __restrict__ ws)
       wk1 = fma(w2, k2[4736], wk1);
       wk1 = fma(w3, k3[4736], wk1);
       const double kk = ws[44416];
-      ws[180896] = fma(-kk, fma(y[4736], wk0, y[2016] * wk1), ws[180896]);
+      ws[185664] = fma(-kk, fma(y[4736], wk0, y[2016] * wk1), ws[185664]);
       lam[2016] = fma(-kk, wk1, lam[2016]);
       lam[4736] = fma(-kk, wk0, lam[4736]);
     }
@@ -402,7 +402,7 @@ __device__ __noinline__ void adj_hess3_1_16(double* __restrict__ ws)
       wk1 = fma(w2, k2[4736], wk1);
       wk1 = fma(w3, k3[4736], wk1);
       const double kk = ws[44448];
-      ws[180928] = fma(-kk, fma(y[4736], wk0, y[2016] * wk1), ws[180928]);
+      ws[185696] = fma(-kk, fma(y[4736], wk0, y[2016] * wk1), ws[185696]);
       lam[2016] = fma(-kk, wk1, lam[2016]);
       lam[4736] = fma(-kk, wk0, lam[4736]);
     }
@@ -432,7 +432,7 @@ __device__ __noinline__ void adj_hess3_1_16(double* __restrict__ ws)
       wk1 = fma(w2, k2[4640], wk1);
       wk1 = fma(w3, k3[4640], wk1);
       const double kk = ws[44480];
-      ws[180960] = fma(-kk, fma(y[4640], wk0, y[2016] * wk1), ws[180960]);
+      ws[185728] = fma(-kk, fma(y[4640], wk0, y[2016] * wk1), ws[185728]);
       lam[2016] = fma(-kk, wk1, lam[2016]);
       lam[4640] = fma(-kk, wk0, lam[4640]);
     }
@@ -468,7 +468,7 @@ __device__ __noinline__ void adj_hess3_1_16(double* __restrict__ ws)
       wk1 = fma(w2, k2[4544], wk1);
       wk1 = fma(w3, k3[4544], wk1);
       const double kk = ws[44512];
-      ws[180992] = fma(-kk, fma(y[4544], wk0, y[2016] * wk1), ws[180992]);
+      ws[185760] = fma(-kk, fma(y[4544], wk0, y[2016] * wk1), ws[185760]);
       lam[2016] = fma(-kk, wk1, lam[2016]);
       lam[4544] = fma(-kk, wk0, lam[4544]);
     }

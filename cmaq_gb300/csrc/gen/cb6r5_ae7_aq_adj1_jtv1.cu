@@ -17,7 +17,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39744] * w;
       out[2176] = fma(kw, y[4640], out[2176]);
       out[4640] = fma(kw, y[2176], out[4640]);
-      ws[176224] = fma(kw * y[2176], y[4640], ws[176224]);
+      ws[180992] = fma(kw * y[2176], y[4640], ws[180992]);
     }
     {
       double w = 1.0 * phi[4000];
@@ -29,7 +29,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39840] * w;
       out[3808] = fma(kw, y[4736], out[3808]);
       out[4736] = fma(kw, y[3808], out[4736]);
-      ws[176320] = fma(kw * y[3808], y[4736], ws[176320]);
+      ws[181088] = fma(kw * y[3808], y[4736], ws[181088]);
     }
     {
       double w = 1.2 * phi[4000];
@@ -44,7 +44,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39872] * w;
       out[3808] = fma(kw, y[4320], out[3808]);
       out[4320] = fma(kw, y[3808], out[4320]);
-      ws[176352] = fma(kw * y[3808], y[4320], ws[176352]);
+      ws[181120] = fma(kw * y[3808], y[4320], ws[181120]);
     }
     {
       double w = 0.5 * phi[4608];
@@ -60,7 +60,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39904] * w;
       out[3808] = fma(kw, y[4640], out[3808]);
       out[4640] = fma(kw, y[3808], out[4640]);
-      ws[176384] = fma(kw * y[3808], y[4640], ws[176384]);
+      ws[181152] = fma(kw * y[3808], y[4640], ws[181152]);
     }
     {
       double w = 0.6 * phi[3744];
@@ -72,7 +72,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[39968] * w;
       out[3936] = fma(kw, y[4736], out[3936]);
       out[4736] = fma(kw, y[3936], out[4736]);
-      ws[176448] = fma(kw * y[3936], y[4736], ws[176448]);
+      ws[181216] = fma(kw * y[3936], y[4736], ws[181216]);
     }
     {
       double w = 1.4 * phi[4256];
@@ -88,7 +88,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40000] * w;
       out[3936] = fma(kw, y[4320], out[3936]);
       out[4320] = fma(kw, y[3936], out[4320]);
-      ws[176480] = fma(kw * y[3936], y[4320], ws[176480]);
+      ws[181248] = fma(kw * y[3936], y[4320], ws[181248]);
     }
     {
       double w = 1.0 * phi[3744];
@@ -98,7 +98,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40032] * w;
       out[3936] = fma(kw, y[4640], out[3936]);
       out[4640] = fma(kw, y[3936], out[4640]);
-      ws[176512] = fma(kw * y[3936], y[4640], ws[176512]);
+      ws[181280] = fma(kw * y[3936], y[4640], ws[181280]);
     }
     {
       double w = 0.14 * phi[4512];
@@ -109,7 +109,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40064] * w;
       out[1760] = fma(kw, y[4736], out[1760]);
       out[4736] = fma(kw, y[1760], out[4736]);
-      ws[176544] = fma(kw * y[1760], y[4736], ws[176544]);
+      ws[181312] = fma(kw * y[1760], y[4736], ws[181312]);
     }
     {
       double w = 1.0 * phi[3328];
@@ -119,7 +119,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40096] * w;
       out[1760] = fma(kw, y[4640], out[1760]);
       out[4640] = fma(kw, y[1760], out[4640]);
-      ws[176576] = fma(kw * y[1760], y[4640], ws[176576]);
+      ws[181344] = fma(kw * y[1760], y[4640], ws[181344]);
     }
     {
       double w = 1.0 * phi[4608];
@@ -132,7 +132,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40128] * w;
       out[3744] = fma(kw, y[4384], out[3744]);
       out[4384] = fma(kw, y[3744], out[4384]);
-      ws[176608] = fma(kw * y[3744], y[4384], ws[176608]);
+      ws[181376] = fma(kw * y[3744], y[4384], ws[181376]);
     }
     {
       double w = 1.0 * phi[1792];
@@ -141,7 +141,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40160] * w;
       out[3744] = fma(kw, y[4608], out[3744]);
       out[4608] = fma(kw, y[3744], out[4608]);
-      ws[176640] = fma(kw * y[3744], y[4608], ws[176640]);
+      ws[181408] = fma(kw * y[3744], y[4608], ws[181408]);
     }
     {
       double w = 1.0 * phi[3744];
@@ -149,7 +149,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       w = w - phi[1792];
       const double kw = ws[40192] * w;
       out[1792] = out[1792] + kw;
-      ws[176672] = fma(kw, y[1792], ws[176672]);
+      ws[181440] = fma(kw, y[1792], ws[181440]);
     }
     {
       double w = 0.37 * phi[2688];
@@ -163,7 +163,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40224] * w;
       out[3744] = fma(kw, y[4704], out[3744]);
       out[4704] = fma(kw, y[3744], out[4704]);
-      ws[176704] = fma(kw * y[3744], y[4704], ws[176704]);
+      ws[181472] = fma(kw * y[3744], y[4704], ws[181472]);
     }
     {
       double w = 1.0 * phi[4416];
@@ -175,7 +175,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40256] * w;
       out[3744] = fma(kw, y[4448], out[3744]);
       out[4448] = fma(kw, y[3744], out[4448]);
-      ws[176736] = fma(kw * y[3744], y[4448], ws[176736]);
+      ws[181504] = fma(kw * y[3744], y[4448], ws[181504]);
     }
     {
       double w = 0.8 * phi[4576];
@@ -187,7 +187,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40288] * w;
       out[3744] = fma(kw, y[4672], out[3744]);
       out[4672] = fma(kw, y[3744], out[4672]);
-      ws[176768] = fma(kw * y[3744], y[4672], ws[176768]);
+      ws[181536] = fma(kw * y[3744], y[4672], ws[181536]);
     }
     {
       double w = 0.5 * phi[4608];
@@ -199,7 +199,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40320] * w;
       out[1792] = fma(kw, y[4736], out[1792]);
       out[4736] = fma(kw, y[1792], out[4736]);
-      ws[176800] = fma(kw * y[1792], y[4736], ws[176800]);
+      ws[181568] = fma(kw * y[1792], y[4736], ws[181568]);
     }
     {
       double w = 1.0 * phi[4128];
@@ -209,7 +209,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40352] * w;
       out[1952] = fma(kw, y[4736], out[1952]);
       out[4736] = fma(kw, y[1952], out[4736]);
-      ws[176832] = fma(kw * y[1952], y[4736], ws[176832]);
+      ws[181600] = fma(kw * y[1952], y[4736], ws[181600]);
     }
     {
       double w = 1.0 * phi[4416];
@@ -219,7 +219,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40384] * w;
       out[416] = fma(kw, y[4736], out[416]);
       out[4736] = fma(kw, y[416], out[4736]);
-      ws[176864] = fma(kw * y[416], y[4736], ws[176864]);
+      ws[181632] = fma(kw * y[416], y[4736], ws[181632]);
     }
     {
       double w = 1.0 * phi[4288];
@@ -227,7 +227,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       w = w - phi[928];
       const double kw = ws[40416] * w;
       out[928] = out[928] + kw;
-      ws[176896] = fma(kw, y[928], ws[176896]);
+      ws[181664] = fma(kw, y[928], ws[181664]);
     }
     {
       double w = 0.732 * phi[3392];
@@ -238,7 +238,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       w = w - phi[928];
       const double kw = ws[40448] * w;
       out[928] = out[928] + kw;
-      ws[176928] = fma(kw, y[928], ws[176928]);
+      ws[181696] = fma(kw, y[928], ws[181696]);
     }
     {
       double w = 1.0 * phi[4288];
@@ -246,7 +246,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       w = w - phi[1984];
       const double kw = ws[40480] * w;
       out[1984] = out[1984] + kw;
-      ws[176960] = fma(kw, y[1984], ws[176960]);
+      ws[181728] = fma(kw, y[1984], ws[181728]);
     }
     {
       double w = 0.126 * phi[4064];
@@ -258,7 +258,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       w = w - phi[1984];
       const double kw = ws[40512] * w;
       out[1984] = out[1984] + kw;
-      ws[176992] = fma(kw, y[1984], ws[176992]);
+      ws[181760] = fma(kw, y[1984], ws[181760]);
     }
     {
       double w = 1.0 * phi[4192];
@@ -267,7 +267,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40544] * w;
       out[4608] = fma(kw, y[4736], out[4608]);
       out[4736] = fma(kw, y[4608], out[4736]);
-      ws[177024] = fma(kw * y[4608], y[4736], ws[177024]);
+      ws[181792] = fma(kw * y[4608], y[4736], ws[181792]);
     }
     {
       double w = 1.0 * phi[3520];
@@ -276,7 +276,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40640] * w;
       out[4544] = fma(kw, y[4320], out[4544]);
       out[4320] = fma(kw, y[4544], out[4320]);
-      ws[177120] = fma(kw * y[4544], y[4320], ws[177120]);
+      ws[181888] = fma(kw * y[4544], y[4320], ws[181888]);
     }
     {
       double w = 0.3 * phi[1184];
@@ -286,7 +286,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40672] * w;
       out[3520] = fma(kw, y[3520], out[3520]);
       out[3520] = fma(kw, y[3520], out[3520]);
-      ws[177152] = fma(kw * y[3520], y[3520], ws[177152]);
+      ws[181920] = fma(kw * y[3520], y[3520], ws[181920]);
     }
     {
       double w = 1.0 * phi[4544];
@@ -296,7 +296,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40704] * w;
       out[3520] = fma(kw, y[4384], out[3520]);
       out[4384] = fma(kw, y[3520], out[4384]);
-      ws[177184] = fma(kw * y[3520], y[4384], ws[177184]);
+      ws[181952] = fma(kw * y[3520], y[4384], ws[181952]);
     }
     {
       double w = 1.0 * phi[1824];
@@ -305,7 +305,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40736] * w;
       out[3520] = fma(kw, y[4704], out[3520]);
       out[4704] = fma(kw, y[3520], out[4704]);
-      ws[177216] = fma(kw * y[3520], y[4704], ws[177216]);
+      ws[181984] = fma(kw * y[3520], y[4704], ws[181984]);
     }
     {
       double w = 1.0 * phi[4544];
@@ -316,7 +316,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40768] * w;
       out[3520] = fma(kw, y[4416], out[3520]);
       out[4416] = fma(kw, y[3520], out[4416]);
-      ws[177248] = fma(kw * y[3520], y[4416], ws[177248]);
+      ws[182016] = fma(kw * y[3520], y[4416], ws[182016]);
     }
     {
       double w = 1.0 * phi[4544];
@@ -326,7 +326,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40800] * w;
       out[4736] = fma(kw, y[3232], out[4736]);
       out[3232] = fma(kw, y[4736], out[3232]);
-      ws[177280] = fma(kw * y[4736], y[3232], ws[177280]);
+      ws[182048] = fma(kw * y[4736], y[3232], ws[182048]);
     }
     {
       double w = 1.0 * phi[3968];
@@ -335,7 +335,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       w = w - phi[4544];
       const double kw = ws[40864] * w;
       out[4544] = out[4544] + kw;
-      ws[177344] = fma(kw, y[4544], ws[177344]);
+      ws[182112] = fma(kw, y[4544], ws[182112]);
     }
     {
       double w = 1.0 * phi[3968];
@@ -345,7 +345,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40896] * w;
       out[4544] = fma(kw, y[4224], out[4544]);
       out[4224] = fma(kw, y[4544], out[4224]);
-      ws[177376] = fma(kw * y[4544], y[4224], ws[177376]);
+      ws[182144] = fma(kw * y[4544], y[4224], ws[182144]);
     }
     {
       double w = 1.0 * phi[3968];
@@ -358,7 +358,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40928] * w;
       out[4544] = fma(kw, y[896], out[4544]);
       out[896] = fma(kw, y[4544], out[896]);
-      ws[177408] = fma(kw * y[4544], y[896], ws[177408]);
+      ws[182176] = fma(kw * y[4544], y[896], ws[182176]);
     }
     {
       double w = 1.0 * phi[3968];
@@ -371,7 +371,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40960] * w;
       out[4544] = fma(kw, y[832], out[4544]);
       out[832] = fma(kw, y[4544], out[832]);
-      ws[177440] = fma(kw * y[4544], y[832], ws[177440]);
+      ws[182208] = fma(kw * y[4544], y[832], ws[182208]);
     }
     {
       double w = 1.0 * phi[3232];
@@ -383,7 +383,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[40992] * w;
       out[4544] = fma(kw, y[2656], out[4544]);
       out[2656] = fma(kw, y[4544], out[2656]);
-      ws[177472] = fma(kw * y[4544], y[2656], ws[177472]);
+      ws[182240] = fma(kw * y[4544], y[2656], ws[182240]);
     }
     {
       double w = 1.0 * phi[3232];
@@ -397,7 +397,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41024] * w;
       out[4544] = fma(kw, y[3552], out[4544]);
       out[3552] = fma(kw, y[4544], out[3552]);
-      ws[177504] = fma(kw * y[4544], y[3552], ws[177504]);
+      ws[182272] = fma(kw * y[4544], y[3552], ws[182272]);
     }
     {
       double w = 0.3 * phi[3968];
@@ -413,7 +413,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41056] * w;
       out[4544] = fma(kw, y[3136], out[4544]);
       out[3136] = fma(kw, y[4544], out[3136]);
-      ws[177536] = fma(kw * y[4544], y[3136], ws[177536]);
+      ws[182304] = fma(kw * y[4544], y[3136], ws[182304]);
     }
     {
       double w = 1.0 * phi[3232];
@@ -426,7 +426,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41088] * w;
       out[4544] = fma(kw, y[2528], out[4544]);
       out[2528] = fma(kw, y[4544], out[2528]);
-      ws[177568] = fma(kw * y[4544], y[2528], ws[177568]);
+      ws[182336] = fma(kw * y[4544], y[2528], ws[182336]);
     }
     {
       double w = 1.0 * phi[3968];
@@ -437,7 +437,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41120] * w;
       out[4544] = fma(kw, y[4512], out[4544]);
       out[4512] = fma(kw, y[4544], out[4512]);
-      ws[177600] = fma(kw * y[4544], y[4512], ws[177600]);
+      ws[182368] = fma(kw * y[4544], y[4512], ws[182368]);
     }
     {
       double w = 1.0 * phi[3968];
@@ -447,7 +447,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41152] * w;
       out[4544] = fma(kw, y[4128], out[4544]);
       out[4128] = fma(kw, y[4544], out[4128]);
-      ws[177632] = fma(kw * y[4544], y[4128], ws[177632]);
+      ws[182400] = fma(kw * y[4544], y[4128], ws[182400]);
     }
     {
       double w = 1.0 * phi[3968];
@@ -457,7 +457,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41184] * w;
       out[4544] = fma(kw, y[4064], out[4544]);
       out[4064] = fma(kw, y[4544], out[4064]);
-      ws[177664] = fma(kw * y[4544], y[4064], ws[177664]);
+      ws[182432] = fma(kw * y[4544], y[4064], ws[182432]);
     }
     {
       double w = 1.0 * phi[3968];
@@ -468,7 +468,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41216] * w;
       out[4544] = fma(kw, y[2720], out[4544]);
       out[2720] = fma(kw, y[4544], out[2720]);
-      ws[177696] = fma(kw * y[4544], y[2720], ws[177696]);
+      ws[182464] = fma(kw * y[4544], y[2720], ws[182464]);
     }
     {
       double w = 1.0 * phi[3968];
@@ -479,7 +479,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41248] * w;
       out[4544] = fma(kw, y[864], out[4544]);
       out[864] = fma(kw, y[4544], out[864]);
-      ws[177728] = fma(kw * y[4544], y[864], ws[177728]);
+      ws[182496] = fma(kw * y[4544], y[864], ws[182496]);
     }
     {
       double w = 1.0 * phi[4544];
@@ -488,7 +488,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41280] * w;
       out[3968] = fma(kw, y[4736], out[3968]);
       out[4736] = fma(kw, y[3968], out[4736]);
-      ws[177760] = fma(kw * y[3968], y[4736], ws[177760]);
+      ws[182528] = fma(kw * y[3968], y[4736], ws[182528]);
     }
     {
       double w = 1.0 * phi[3968];
@@ -505,7 +505,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41312] * w;
       out[4544] = fma(kw, y[1088], out[4544]);
       out[1088] = fma(kw, y[4544], out[1088]);
-      ws[177792] = fma(kw * y[4544], y[1088], ws[177792]);
+      ws[182560] = fma(kw * y[4544], y[1088], ws[182560]);
     }
 }
 __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int phioff, int outoff)
@@ -528,7 +528,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41344] * w;
       out[4544] = fma(kw, y[1120], out[4544]);
       out[1120] = fma(kw, y[4544], out[1120]);
-      ws[177824] = fma(kw * y[4544], y[1120], ws[177824]);
+      ws[182592] = fma(kw * y[4544], y[1120], ws[182592]);
     }
     {
       double w = 1.0 * phi[3968];
@@ -545,7 +545,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41376] * w;
       out[4544] = fma(kw, y[1152], out[4544]);
       out[1152] = fma(kw, y[4544], out[1152]);
-      ws[177856] = fma(kw * y[4544], y[1152], ws[177856]);
+      ws[182624] = fma(kw * y[4544], y[1152], ws[182624]);
     }
     {
       double w = 1.0 * phi[1216];
@@ -554,7 +554,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41440] * w;
       out[3520] = fma(kw, y[4608], out[3520]);
       out[4608] = fma(kw, y[3520], out[4608]);
-      ws[177920] = fma(kw * y[3520], y[4608], ws[177920]);
+      ws[182688] = fma(kw * y[3520], y[4608], ws[182688]);
     }
     {
       double w = 1.0 * phi[1824];
@@ -562,7 +562,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       w = w - phi[1216];
       const double kw = ws[41536] * w;
       out[1216] = out[1216] + kw;
-      ws[178016] = fma(kw, y[1216], ws[178016]);
+      ws[182784] = fma(kw, y[1216], ws[182784]);
     }
     {
       double w = 1.0 * phi[1824];
@@ -570,7 +570,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       w = w - phi[1216];
       const double kw = ws[41568] * w;
       out[1216] = out[1216] + kw;
-      ws[178048] = fma(kw, y[1216], ws[178048]);
+      ws[182816] = fma(kw, y[1216], ws[182816]);
     }
     {
       double w = 1.0 * phi[4384];
@@ -582,7 +582,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41600] * w;
       out[2944] = fma(kw, y[4384], out[2944]);
       out[4384] = fma(kw, y[2944], out[4384]);
-      ws[178080] = fma(kw * y[2944], y[4384], ws[178080]);
+      ws[182848] = fma(kw * y[2944], y[4384], ws[182848]);
     }
     {
       double w = 1.0 * phi[4704];
@@ -592,7 +592,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41632] * w;
       out[2944] = fma(kw, y[4704], out[2944]);
       out[4704] = fma(kw, y[2944], out[4704]);
-      ws[178112] = fma(kw * y[2944], y[4704], ws[178112]);
+      ws[182880] = fma(kw * y[2944], y[4704], ws[182880]);
     }
     {
       double w = 1.0 * phi[4384];
@@ -604,7 +604,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41664] * w;
       out[2496] = fma(kw, y[4384], out[2496]);
       out[4384] = fma(kw, y[2496], out[4384]);
-      ws[178144] = fma(kw * y[2496], y[4384], ws[178144]);
+      ws[182912] = fma(kw * y[2496], y[4384], ws[182912]);
     }
     {
       double w = 1.0 * phi[4704];
@@ -614,7 +614,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41696] * w;
       out[2496] = fma(kw, y[4704], out[2496]);
       out[4704] = fma(kw, y[2496], out[4704]);
-      ws[178176] = fma(kw * y[2496], y[4704], ws[178176]);
+      ws[182944] = fma(kw * y[2496], y[4704], ws[182944]);
     }
     {
       double w = 1.0 * phi[4384];
@@ -625,7 +625,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41728] * w;
       out[2144] = fma(kw, y[4384], out[2144]);
       out[4384] = fma(kw, y[2144], out[4384]);
-      ws[178208] = fma(kw * y[2144], y[4384], ws[178208]);
+      ws[182976] = fma(kw * y[2144], y[4384], ws[182976]);
     }
     {
       double w = 1.0 * phi[4704];
@@ -635,7 +635,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41760] * w;
       out[2144] = fma(kw, y[4704], out[2144]);
       out[4704] = fma(kw, y[2144], out[4704]);
-      ws[178240] = fma(kw * y[2144], y[4704], ws[178240]);
+      ws[183008] = fma(kw * y[2144], y[4704], ws[183008]);
     }
     {
       double w = 1.0 * phi[4320];
@@ -645,7 +645,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41792] * w;
       out[1856] = fma(kw, y[4320], out[1856]);
       out[4320] = fma(kw, y[1856], out[4320]);
-      ws[178272] = fma(kw * y[1856], y[4320], ws[178272]);
+      ws[183040] = fma(kw * y[1856], y[4320], ws[183040]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -655,7 +655,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41824] * w;
       out[1856] = fma(kw, y[4736], out[1856]);
       out[4736] = fma(kw, y[1856], out[4736]);
-      ws[178304] = fma(kw * y[1856], y[4736], ws[178304]);
+      ws[183072] = fma(kw * y[1856], y[4736], ws[183072]);
     }
     {
       double w = 1.0 * phi[4640];
@@ -665,7 +665,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41856] * w;
       out[1856] = fma(kw, y[4640], out[1856]);
       out[4640] = fma(kw, y[1856], out[4640]);
-      ws[178336] = fma(kw * y[1856], y[4640], ws[178336]);
+      ws[183104] = fma(kw * y[1856], y[4640], ws[183104]);
     }
     {
       double w = 1.0 * phi[4384];
@@ -677,7 +677,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41888] * w;
       out[2560] = fma(kw, y[4384], out[2560]);
       out[4384] = fma(kw, y[2560], out[4384]);
-      ws[178368] = fma(kw * y[2560], y[4384], ws[178368]);
+      ws[183136] = fma(kw * y[2560], y[4384], ws[183136]);
     }
     {
       double w = 1.0 * phi[4704];
@@ -687,7 +687,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41920] * w;
       out[2560] = fma(kw, y[4704], out[2560]);
       out[4704] = fma(kw, y[2560], out[4704]);
-      ws[178400] = fma(kw * y[2560], y[4704], ws[178400]);
+      ws[183168] = fma(kw * y[2560], y[4704], ws[183168]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -699,14 +699,14 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[41952] * w;
       out[448] = fma(kw, y[4736], out[448]);
       out[4736] = fma(kw, y[448], out[4736]);
-      ws[178432] = fma(kw * y[448], y[4736], ws[178432]);
+      ws[183200] = fma(kw * y[448], y[4736], ws[183200]);
     }
     {
       double w = 1.0 * phi[4192];
       w = w - phi[4032];
       const double kw = ws[41984] * w;
       out[4032] = out[4032] + kw;
-      ws[178464] = fma(kw, y[4032], ws[178464]);
+      ws[183232] = fma(kw, y[4032], ws[183232]);
     }
     {
       double w = 1.0 * phi[4192];
@@ -714,7 +714,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       w = w - phi[1280];
       const double kw = ws[42016] * w;
       out[1280] = out[1280] + kw;
-      ws[178496] = fma(kw, y[1280], ws[178496]);
+      ws[183264] = fma(kw, y[1280], ws[183264]);
     }
     {
       double w = 1.0 * phi[4192];
@@ -722,21 +722,21 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       w = w - phi[1280];
       const double kw = ws[42048] * w;
       out[1280] = out[1280] + kw;
-      ws[178528] = fma(kw, y[1280], ws[178528]);
+      ws[183296] = fma(kw, y[1280], ws[183296]);
     }
     {
       double w = 1.0 * phi[4192];
       w = w - phi[1920];
       const double kw = ws[42080] * w;
       out[1920] = out[1920] + kw;
-      ws[178560] = fma(kw, y[1920], ws[178560]);
+      ws[183328] = fma(kw, y[1920], ws[183328]);
     }
     {
       double w = 1.0 * phi[4192];
       w = w - phi[1248];
       const double kw = ws[42112] * w;
       out[1248] = out[1248] + kw;
-      ws[178592] = fma(kw, y[1248], ws[178592]);
+      ws[183360] = fma(kw, y[1248], ws[183360]);
     }
     {
       double w = 1.0 * phi[2592];
@@ -745,7 +745,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[42144] * w;
       out[1920] = fma(kw, y[480], out[1920]);
       out[480] = fma(kw, y[1920], out[480]);
-      ws[178624] = fma(kw * y[1920], y[480], ws[178624]);
+      ws[183392] = fma(kw * y[1920], y[480], ws[183392]);
     }
     {
       double w = 1.0 * phi[2592];
@@ -754,7 +754,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[42176] * w;
       out[1920] = fma(kw, y[512], out[1920]);
       out[512] = fma(kw, y[1920], out[512]);
-      ws[178656] = fma(kw * y[1920], y[512], ws[178656]);
+      ws[183424] = fma(kw * y[1920], y[512], ws[183424]);
     }
     {
       double w = 1.0 * phi[2592];
@@ -763,7 +763,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[42208] * w;
       out[1248] = fma(kw, y[544], out[1248]);
       out[544] = fma(kw, y[1248], out[544]);
-      ws[178688] = fma(kw * y[1248], y[544], ws[178688]);
+      ws[183456] = fma(kw * y[1248], y[544], ws[183456]);
     }
     {
       double w = 0.5 * phi[2464];
@@ -771,14 +771,14 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       w = w - phi[4608];
       const double kw = ws[42240] * w;
       out[4608] = out[4608] + kw;
-      ws[178720] = fma(kw, y[4608], ws[178720]);
+      ws[183488] = fma(kw, y[4608], ws[183488]);
     }
     {
       double w = 1.0 * phi[1312];
       w = w - phi[1056];
       const double kw = ws[42304] * w;
       out[1056] = out[1056] + kw;
-      ws[178784] = fma(kw, y[1056], ws[178784]);
+      ws[183552] = fma(kw, y[1056], ws[183552]);
     }
     {
       double w = 1.0 * phi[608];
@@ -787,28 +787,28 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[42336] * w;
       out[1312] = fma(kw, y[576], out[1312]);
       out[576] = fma(kw, y[1312], out[576]);
-      ws[178816] = fma(kw * y[1312], y[576], ws[178816]);
+      ws[183584] = fma(kw * y[1312], y[576], ws[183584]);
     }
     {
       double w = 1.0 * phi[608];
       w = w - phi[1312];
       const double kw = ws[42368] * w;
       out[1312] = out[1312] + kw;
-      ws[178848] = fma(kw, y[1312], ws[178848]);
+      ws[183616] = fma(kw, y[1312], ws[183616]);
     }
     {
       double w = 1.0 * phi[640];
       w = w - phi[4256];
       const double kw = ws[42400] * w;
       out[4256] = out[4256] + kw;
-      ws[178880] = fma(kw, y[4256], ws[178880]);
+      ws[183648] = fma(kw, y[4256], ws[183648]);
     }
     {
       double w = 1.0 * phi[640];
       w = w - phi[4000];
       const double kw = ws[42432] * w;
       out[4000] = out[4000] + kw;
-      ws[178912] = fma(kw, y[4000], ws[178912]);
+      ws[183680] = fma(kw, y[4000], ws[183680]);
     }
     {
       double w = 1.0 * phi[4384];
@@ -818,7 +818,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[42464] * w;
       out[2848] = fma(kw, y[4384], out[2848]);
       out[4384] = fma(kw, y[2848], out[4384]);
-      ws[178944] = fma(kw * y[2848], y[4384], ws[178944]);
+      ws[183712] = fma(kw * y[2848], y[4384], ws[183712]);
     }
     {
       double w = 1.0 * phi[4704];
@@ -828,7 +828,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[42496] * w;
       out[2848] = fma(kw, y[4704], out[2848]);
       out[4704] = fma(kw, y[2848], out[4704]);
-      ws[178976] = fma(kw * y[2848], y[4704], ws[178976]);
+      ws[183744] = fma(kw * y[2848], y[4704], ws[183744]);
     }
     {
       double w = 1.0 * phi[4640];
@@ -838,7 +838,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[42528] * w;
       out[2848] = fma(kw, y[4640], out[2848]);
       out[4640] = fma(kw, y[2848], out[4640]);
-      ws[179008] = fma(kw * y[2848], y[4640], ws[179008]);
+      ws[183776] = fma(kw * y[2848], y[4640], ws[183776]);
     }
     {
       double w = 1.0 * phi[4672];
@@ -848,7 +848,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[42560] * w;
       out[2848] = fma(kw, y[4672], out[2848]);
       out[4672] = fma(kw, y[2848], out[4672]);
-      ws[179040] = fma(kw * y[2848], y[4672], ws[179040]);
+      ws[183808] = fma(kw * y[2848], y[4672], ws[183808]);
     }
     {
       double w = 1.0 * phi[4544];
@@ -858,7 +858,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[42592] * w;
       out[3360] = fma(kw, y[4544], out[3360]);
       out[4544] = fma(kw, y[3360], out[4544]);
-      ws[179072] = fma(kw * y[3360], y[4544], ws[179072]);
+      ws[183840] = fma(kw * y[3360], y[4544], ws[183840]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -868,56 +868,56 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[42624] * w;
       out[3360] = fma(kw, y[4736], out[3360]);
       out[4736] = fma(kw, y[3360], out[4736]);
-      ws[179104] = fma(kw * y[3360], y[4736], ws[179104]);
+      ws[183872] = fma(kw * y[3360], y[4736], ws[183872]);
     }
     {
       double w = 1.0 * phi[32];
       w = w - phi[0];
       const double kw = ws[42688] * w;
       out[0] = out[0] + kw;
-      ws[179168] = fma(kw, y[0], ws[179168]);
+      ws[183936] = fma(kw, y[0], ws[183936]);
     }
     {
       double w = 0.907 * phi[1376];
       w = w - phi[64];
       const double kw = ws[42720] * w;
       out[64] = out[64] + kw;
-      ws[179200] = fma(kw, y[64], ws[179200]);
+      ws[183968] = fma(kw, y[64], ws[183968]);
     }
     {
       double w = 0.925 * phi[1376];
       w = w - phi[96];
       const double kw = ws[42752] * w;
       out[96] = out[96] + kw;
-      ws[179232] = fma(kw, y[96], ws[179232]);
+      ws[184000] = fma(kw, y[96], ws[184000]);
     }
     {
       double w = 0.943 * phi[1376];
       w = w - phi[128];
       const double kw = ws[42784] * w;
       out[128] = out[128] + kw;
-      ws[179264] = fma(kw, y[128], ws[179264]);
+      ws[184032] = fma(kw, y[128], ws[184032]);
     }
     {
       double w = 0.5 * phi[1408];
       w = w - phi[160];
       const double kw = ws[42816] * w;
       out[160] = out[160] + kw;
-      ws[179296] = fma(kw, y[160], ws[179296]);
+      ws[184064] = fma(kw, y[160], ws[184064]);
     }
     {
       double w = 0.5 * phi[1408];
       w = w - phi[192];
       const double kw = ws[42848] * w;
       out[192] = out[192] + kw;
-      ws[179328] = fma(kw, y[192], ws[179328]);
+      ws[184096] = fma(kw, y[192], ws[184096]);
     }
     {
       double w = 1.5 * phi[1408];
       w = w - phi[224];
       const double kw = ws[42880] * w;
       out[224] = out[224] + kw;
-      ws[179360] = fma(kw, y[224], ws[179360]);
+      ws[184128] = fma(kw, y[224], ws[184128]);
     }
     {
       double w = 1.25 * phi[1440];
@@ -928,7 +928,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[42912] * w;
       out[704] = fma(kw, y[4736], out[704]);
       out[4736] = fma(kw, y[704], out[4736]);
-      ws[179392] = fma(kw * y[704], y[4736], ws[179392]);
+      ws[184160] = fma(kw * y[704], y[4736], ws[184160]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -937,7 +937,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[42944] * w;
       out[1440] = fma(kw, y[4736], out[1440]);
       out[4736] = fma(kw, y[1440], out[4736]);
-      ws[179424] = fma(kw * y[1440], y[4736], ws[179424]);
+      ws[184192] = fma(kw * y[1440], y[4736], ws[184192]);
     }
     {
       double w = 1.25 * phi[1472];
@@ -948,7 +948,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[42976] * w;
       out[736] = fma(kw, y[4736], out[736]);
       out[4736] = fma(kw, y[736], out[4736]);
-      ws[179456] = fma(kw * y[736], y[4736], ws[179456]);
+      ws[184224] = fma(kw * y[736], y[4736], ws[184224]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -957,7 +957,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43008] * w;
       out[1472] = fma(kw, y[4736], out[1472]);
       out[4736] = fma(kw, y[1472], out[4736]);
-      ws[179488] = fma(kw * y[1472], y[4736], ws[179488]);
+      ws[184256] = fma(kw * y[1472], y[4736], ws[184256]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -967,7 +967,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43040] * w;
       out[768] = fma(kw, y[4736], out[768]);
       out[4736] = fma(kw, y[768], out[4736]);
-      ws[179520] = fma(kw * y[768], y[4736], ws[179520]);
+      ws[184288] = fma(kw * y[768], y[4736], ws[184288]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -985,7 +985,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43072] * w;
       out[2752] = fma(kw, y[4736], out[2752]);
       out[4736] = fma(kw, y[2752], out[4736]);
-      ws[179552] = fma(kw * y[2752], y[4736], ws[179552]);
+      ws[184320] = fma(kw * y[2752], y[4736], ws[184320]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1000,7 +1000,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43104] * w;
       out[2784] = fma(kw, y[4736], out[2784]);
       out[4736] = fma(kw, y[2784], out[4736]);
-      ws[179584] = fma(kw * y[2784], y[4736], ws[179584]);
+      ws[184352] = fma(kw * y[2784], y[4736], ws[184352]);
     }
 }
 __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int phioff, int outoff)
@@ -1021,7 +1021,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43136] * w;
       out[2816] = fma(kw, y[4736], out[2816]);
       out[4736] = fma(kw, y[2816], out[4736]);
-      ws[179616] = fma(kw * y[2816], y[4736], ws[179616]);
+      ws[184384] = fma(kw * y[2816], y[4736], ws[184384]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1036,7 +1036,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43168] * w;
       out[2304] = fma(kw, y[4736], out[2304]);
       out[4736] = fma(kw, y[2304], out[4736]);
-      ws[179648] = fma(kw * y[2304], y[4736], ws[179648]);
+      ws[184416] = fma(kw * y[2304], y[4736], ws[184416]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1050,7 +1050,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43200] * w;
       out[1504] = fma(kw, y[4736], out[1504]);
       out[4736] = fma(kw, y[1504], out[4736]);
-      ws[179680] = fma(kw * y[1504], y[4736], ws[179680]);
+      ws[184448] = fma(kw * y[1504], y[4736], ws[184448]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1064,7 +1064,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43232] * w;
       out[3680] = fma(kw, y[4736], out[3680]);
       out[4736] = fma(kw, y[3680], out[4736]);
-      ws[179712] = fma(kw * y[3680], y[4736], ws[179712]);
+      ws[184480] = fma(kw * y[3680], y[4736], ws[184480]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1078,7 +1078,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43264] * w;
       out[3712] = fma(kw, y[4736], out[3712]);
       out[4736] = fma(kw, y[3712], out[4736]);
-      ws[179744] = fma(kw * y[3712], y[4736], ws[179744]);
+      ws[184512] = fma(kw * y[3712], y[4736], ws[184512]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1092,7 +1092,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43296] * w;
       out[2912] = fma(kw, y[4736], out[2912]);
       out[4736] = fma(kw, y[2912], out[4736]);
-      ws[179776] = fma(kw * y[2912], y[4736], ws[179776]);
+      ws[184544] = fma(kw * y[2912], y[4736], ws[184544]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1106,7 +1106,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43328] * w;
       out[3168] = fma(kw, y[4736], out[3168]);
       out[4736] = fma(kw, y[3168], out[4736]);
-      ws[179808] = fma(kw * y[3168], y[4736], ws[179808]);
+      ws[184576] = fma(kw * y[3168], y[4736], ws[184576]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1120,7 +1120,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43360] * w;
       out[3200] = fma(kw, y[4736], out[3200]);
       out[4736] = fma(kw, y[3200], out[4736]);
-      ws[179840] = fma(kw * y[3200], y[4736], ws[179840]);
+      ws[184608] = fma(kw * y[3200], y[4736], ws[184608]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1129,7 +1129,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43392] * w;
       out[2336] = fma(kw, y[4736], out[2336]);
       out[4736] = fma(kw, y[2336], out[4736]);
-      ws[179872] = fma(kw * y[2336], y[4736], ws[179872]);
+      ws[184640] = fma(kw * y[2336], y[4736], ws[184640]);
     }
     {
       double w = 1.0 * phi[4640];
@@ -1138,7 +1138,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43424] * w;
       out[2336] = fma(kw, y[4640], out[2336]);
       out[4640] = fma(kw, y[2336], out[4640]);
-      ws[179904] = fma(kw * y[2336], y[4640], ws[179904]);
+      ws[184672] = fma(kw * y[2336], y[4640], ws[184672]);
     }
     {
       double w = 1.0 * phi[4160];
@@ -1147,7 +1147,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43456] * w;
       out[2336] = fma(kw, y[4160], out[2336]);
       out[4160] = fma(kw, y[2336], out[4160]);
-      ws[179936] = fma(kw * y[2336], y[4160], ws[179936]);
+      ws[184704] = fma(kw * y[2336], y[4160], ws[184704]);
     }
     {
       double w = 1.0 * phi[4544];
@@ -1156,7 +1156,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43552] * w;
       out[2336] = fma(kw, y[4544], out[2336]);
       out[4544] = fma(kw, y[2336], out[4544]);
-      ws[180032] = fma(kw * y[2336], y[4544], ws[180032]);
+      ws[184800] = fma(kw * y[2336], y[4544], ws[184800]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1165,7 +1165,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43584] * w;
       out[2368] = fma(kw, y[4736], out[2368]);
       out[4736] = fma(kw, y[2368], out[4736]);
-      ws[180064] = fma(kw * y[2368], y[4736], ws[180064]);
+      ws[184832] = fma(kw * y[2368], y[4736], ws[184832]);
     }
     {
       double w = 1.0 * phi[4640];
@@ -1174,7 +1174,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43616] * w;
       out[2368] = fma(kw, y[4640], out[2368]);
       out[4640] = fma(kw, y[2368], out[4640]);
-      ws[180096] = fma(kw * y[2368], y[4640], ws[180096]);
+      ws[184864] = fma(kw * y[2368], y[4640], ws[184864]);
     }
     {
       double w = 1.0 * phi[4160];
@@ -1183,7 +1183,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43648] * w;
       out[2368] = fma(kw, y[4160], out[2368]);
       out[4160] = fma(kw, y[2368], out[4160]);
-      ws[180128] = fma(kw * y[2368], y[4160], ws[180128]);
+      ws[184896] = fma(kw * y[2368], y[4160], ws[184896]);
     }
     {
       double w = 1.0 * phi[4544];
@@ -1192,7 +1192,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43712] * w;
       out[2368] = fma(kw, y[4544], out[2368]);
       out[4544] = fma(kw, y[2368], out[4544]);
-      ws[180192] = fma(kw * y[2368], y[4544], ws[180192]);
+      ws[184960] = fma(kw * y[2368], y[4544], ws[184960]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1202,7 +1202,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43744] * w;
       out[2400] = fma(kw, y[4736], out[2400]);
       out[4736] = fma(kw, y[2400], out[4736]);
-      ws[180224] = fma(kw * y[2400], y[4736], ws[180224]);
+      ws[184992] = fma(kw * y[2400], y[4736], ws[184992]);
     }
     {
       double w = 1.0 * phi[4320];
@@ -1212,7 +1212,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43776] * w;
       out[2400] = fma(kw, y[4320], out[2400]);
       out[4320] = fma(kw, y[2400], out[4320]);
-      ws[180256] = fma(kw * y[2400], y[4320], ws[180256]);
+      ws[185024] = fma(kw * y[2400], y[4320], ws[185024]);
     }
     {
       double w = 1.0 * phi[4640];
@@ -1222,7 +1222,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43808] * w;
       out[2400] = fma(kw, y[4640], out[2400]);
       out[4640] = fma(kw, y[2400], out[4640]);
-      ws[180288] = fma(kw * y[2400], y[4640], ws[180288]);
+      ws[185056] = fma(kw * y[2400], y[4640], ws[185056]);
     }
     {
       double w = 1.0 * phi[4544];
@@ -1232,7 +1232,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43840] * w;
       out[2400] = fma(kw, y[4544], out[2400]);
       out[4544] = fma(kw, y[2400], out[4544]);
-      ws[180320] = fma(kw * y[2400], y[4544], ws[180320]);
+      ws[185088] = fma(kw * y[2400], y[4544], ws[185088]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1241,7 +1241,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43872] * w;
       out[2432] = fma(kw, y[4736], out[2432]);
       out[4736] = fma(kw, y[2432], out[4736]);
-      ws[180352] = fma(kw * y[2432], y[4736], ws[180352]);
+      ws[185120] = fma(kw * y[2432], y[4736], ws[185120]);
     }
     {
       double w = 1.0 * phi[4320];
@@ -1250,7 +1250,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43904] * w;
       out[2432] = fma(kw, y[4320], out[2432]);
       out[4320] = fma(kw, y[2432], out[4320]);
-      ws[180384] = fma(kw * y[2432], y[4320], ws[180384]);
+      ws[185152] = fma(kw * y[2432], y[4320], ws[185152]);
     }
     {
       double w = 1.0 * phi[4640];
@@ -1259,7 +1259,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43936] * w;
       out[2432] = fma(kw, y[4640], out[2432]);
       out[4640] = fma(kw, y[2432], out[4640]);
-      ws[180416] = fma(kw * y[2432], y[4640], ws[180416]);
+      ws[185184] = fma(kw * y[2432], y[4640], ws[185184]);
     }
     {
       double w = 1.0 * phi[4544];
@@ -1268,7 +1268,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44000] * w;
       out[2432] = fma(kw, y[4544], out[2432]);
       out[4544] = fma(kw, y[2432], out[4544]);
-      ws[180480] = fma(kw * y[2432], y[4544], ws[180480]);
+      ws[185248] = fma(kw * y[2432], y[4544], ws[185248]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1277,7 +1277,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44032] * w;
       out[2976] = fma(kw, y[4736], out[2976]);
       out[4736] = fma(kw, y[2976], out[4736]);
-      ws[180512] = fma(kw * y[2976], y[4736], ws[180512]);
+      ws[185280] = fma(kw * y[2976], y[4736], ws[185280]);
     }
     {
       double w = 1.0 * phi[4320];
@@ -1286,7 +1286,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44064] * w;
       out[2976] = fma(kw, y[4320], out[2976]);
       out[4320] = fma(kw, y[2976], out[4320]);
-      ws[180544] = fma(kw * y[2976], y[4320], ws[180544]);
+      ws[185312] = fma(kw * y[2976], y[4320], ws[185312]);
     }
     {
       double w = 1.0 * phi[4640];
@@ -1295,7 +1295,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44096] * w;
       out[2976] = fma(kw, y[4640], out[2976]);
       out[4640] = fma(kw, y[2976], out[4640]);
-      ws[180576] = fma(kw * y[2976], y[4640], ws[180576]);
+      ws[185344] = fma(kw * y[2976], y[4640], ws[185344]);
     }
     {
       double w = 1.0 * phi[4544];
@@ -1304,7 +1304,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44160] * w;
       out[2976] = fma(kw, y[4544], out[2976]);
       out[4544] = fma(kw, y[2976], out[4544]);
-      ws[180640] = fma(kw * y[2976], y[4544], ws[180640]);
+      ws[185408] = fma(kw * y[2976], y[4544], ws[185408]);
     }
     {
       double w = 1.0 * phi[4736];
@@ -1313,7 +1313,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44192] * w;
       out[1536] = fma(kw, y[4736], out[1536]);
       out[4736] = fma(kw, y[1536], out[4736]);
-      ws[180672] = fma(kw * y[1536], y[4736], ws[180672]);
+      ws[185440] = fma(kw * y[1536], y[4736], ws[185440]);
     }
     {
       double w = 1.0 * phi[4544];
@@ -1322,7 +1322,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44224] * w;
       out[1536] = fma(kw, y[4544], out[1536]);
       out[4544] = fma(kw, y[1536], out[4544]);
-      ws[180704] = fma(kw * y[1536], y[4544], ws[180704]);
+      ws[185472] = fma(kw * y[1536], y[4544], ws[185472]);
     }
     {
       double w = 0.5 * phi[1568];
@@ -1333,7 +1333,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44256] * w;
       out[3008] = fma(kw, y[4320], out[3008]);
       out[4320] = fma(kw, y[3008], out[4320]);
-      ws[180736] = fma(kw * y[3008], y[4320], ws[180736]);
+      ws[185504] = fma(kw * y[3008], y[4320], ws[185504]);
     }
     {
       double w = 1.0 * phi[3040];
@@ -1343,7 +1343,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44288] * w;
       out[3008] = fma(kw, y[1184], out[3008]);
       out[1184] = fma(kw, y[3008], out[1184]);
-      ws[180768] = fma(kw * y[3008], y[1184], ws[180768]);
+      ws[185536] = fma(kw * y[3008], y[1184], ws[185536]);
     }
     {
       double w = 1.0 * phi[3040];
@@ -1353,7 +1353,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44320] * w;
       out[3008] = fma(kw, y[3456], out[3008]);
       out[3456] = fma(kw, y[3008], out[3456]);
-      ws[180800] = fma(kw * y[3008], y[3456], ws[180800]);
+      ws[185568] = fma(kw * y[3008], y[3456], ws[185568]);
     }
     {
       double w = 0.5 * phi[1568];
@@ -1364,7 +1364,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44352] * w;
       out[3008] = fma(kw, y[4736], out[3008]);
       out[4736] = fma(kw, y[3008], out[4736]);
-      ws[180832] = fma(kw * y[3008], y[4736], ws[180832]);
+      ws[185600] = fma(kw * y[3008], y[4736], ws[185600]);
     }
     {
       double w = 0.5 * phi[3008];
@@ -1375,7 +1375,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44384] * w;
       out[3008] = fma(kw, y[4544], out[3008]);
       out[4544] = fma(kw, y[3008], out[4544]);
-      ws[180864] = fma(kw * y[3008], y[4544], ws[180864]);
+      ws[185632] = fma(kw * y[3008], y[4544], ws[185632]);
     }
     {
       double w = 1.0 * phi[2208];
@@ -1386,7 +1386,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44416] * w;
       out[2016] = fma(kw, y[4736], out[2016]);
       out[4736] = fma(kw, y[2016], out[4736]);
-      ws[180896] = fma(kw * y[2016], y[4736], ws[180896]);
+      ws[185664] = fma(kw * y[2016], y[4736], ws[185664]);
     }
     {
       double w = 0.75 * phi[2208];
@@ -1397,7 +1397,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44448] * w;
       out[2016] = fma(kw, y[4736], out[2016]);
       out[4736] = fma(kw, y[2016], out[4736]);
-      ws[180928] = fma(kw * y[2016], y[4736], ws[180928]);
+      ws[185696] = fma(kw * y[2016], y[4736], ws[185696]);
     }
     {
       double w = 1.0 * phi[2208];
@@ -1409,7 +1409,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44480] * w;
       out[2016] = fma(kw, y[4640], out[2016]);
       out[4640] = fma(kw, y[2016], out[4640]);
-      ws[180960] = fma(kw * y[2016], y[4640], ws[180960]);
+      ws[185728] = fma(kw * y[2016], y[4640], ws[185728]);
     }
     {
       double w = 0.86 * phi[2208];
@@ -1423,7 +1423,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44512] * w;
       out[2016] = fma(kw, y[4544], out[2016]);
       out[4544] = fma(kw, y[2016], out[4544]);
-      ws[180992] = fma(kw * y[2016], y[4544], ws[180992]);
+      ws[185760] = fma(kw * y[2016], y[4544], ws[185760]);
     }
 }
 }  // namespace mech_cb6r5_ae7_aq

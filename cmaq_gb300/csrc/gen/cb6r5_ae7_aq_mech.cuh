@@ -26,7 +26,7 @@ constexpr int NRXNS = 349;
 constexpr int ISCHAN = 149;
 constexpr int NPHOTAB = 32;
 constexpr int NHETERO = 17;
-constexpr int WS_ELEMS = 4116;
+constexpr int WS_ELEMS = 4265;
 constexpr int OFF_Y = 0;
 constexpr int OFF_YP = 149;
 constexpr int OFF_YDOT = 298;
@@ -36,26 +36,27 @@ constexpr int OFF_K2 = 745;
 constexpr int OFF_K3 = 894;
 constexpr int OFF_RKI = 1043;
 constexpr int OFF_RXRAT = 1392;
-constexpr int OFF_LU = 2277;
-constexpr int OFF_VDIAG = 3967;
+constexpr int OFF_LU = 2426;
+constexpr int OFF_VDIAG = 4116;
 constexpr int IARRAY_DAY = 1689;
 constexpr int IARRAY_NIGHT = 1615;
-constexpr int EBI_OFF_YC = 2277;
-constexpr int EBI_OFF_YC0 = 2426;
-constexpr int EBI_OFF_YCP = 2575;
-constexpr int EBI_OFF_PROD = 2724;
-constexpr int EBI_OFF_LOSS = 2873;
-constexpr int EBI_OFF_PNEG = 3022;
-constexpr int ADJ_WS_ELEMS = 5657;
-constexpr int ADJ_LAM = 4116;
-constexpr int ADJ_MU1 = 4265;
-constexpr int ADJ_MU2 = 4414;
-constexpr int ADJ_MU3 = 4563;
-constexpr int ADJ_PHI = 4712;
-constexpr int ADJ_TMP = 4861;
-constexpr int ADJ_EMIS = 5010;
-constexpr int ADJ_GE = 5159;
-constexpr int ADJ_GK = 5308;
+constexpr int EBI_OFF_YC = 2426;
+constexpr int EBI_OFF_YC0 = 2575;
+constexpr int EBI_OFF_YCP = 2724;
+constexpr int EBI_OFF_PROD = 2873;
+constexpr int EBI_OFF_LOSS = 3022;
+constexpr int EBI_OFF_PNEG = 3171;
+constexpr int ADJ_WS_ELEMS = 5806;
+constexpr int ADJ_LAM = 4265;
+constexpr int ADJ_MU1 = 4414;
+constexpr int ADJ_MU2 = 4563;
+constexpr int ADJ_MU3 = 4712;
+constexpr int ADJ_PHI = 4861;
+constexpr int ADJ_TMP = 5010;
+constexpr int ADJ_EMIS = 5159;
+constexpr int ADJ_GE = 5308;
+constexpr int ADJ_GK = 5457;
+constexpr int OFF_YAVE = 2277;
 constexpr double FLOPS_STEP_DAY = 36947.0;
 constexpr double FLOPS_STEP_NIGHT = 34766.0;
 extern __constant__ int c_inew2old[149];
@@ -83,6 +84,23 @@ __device__ void jacdecomp_0_9(double* __restrict__ ws, double gdtinv);
 __device__ void jacdecomp_0_10(double* __restrict__ ws, double gdtinv);
 __device__ void jacdecomp_0_11(double* __restrict__ ws, double gdtinv);
 __device__ void jacdecomp_0_12(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_13(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_14(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_15(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_16(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_17(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_18(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_19(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_20(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_21(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_22(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_23(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_24(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_25(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_26(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_27(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_28(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_29(double* __restrict__ ws, double gdtinv);
 __device__ void solve_0_0(double* __restrict__ ws, int rhs);
 __device__ void solve_0_1(double* __restrict__ ws, int rhs);
 __device__ void solve_0_2(double* __restrict__ ws, int rhs);
@@ -98,6 +116,24 @@ __device__ void jacdecomp_1_8(double* __restrict__ ws, double gdtinv);
 __device__ void jacdecomp_1_9(double* __restrict__ ws, double gdtinv);
 __device__ void jacdecomp_1_10(double* __restrict__ ws, double gdtinv);
 __device__ void jacdecomp_1_11(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_12(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_13(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_14(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_15(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_16(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_17(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_18(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_19(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_20(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_21(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_22(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_23(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_24(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_25(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_26(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_27(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_28(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_29(double* __restrict__ ws, double gdtinv);
 __device__ void solve_1_0(double* __restrict__ ws, int rhs);
 __device__ void solve_1_1(double* __restrict__ ws, int rhs);
 __device__ void solve_1_2(double* __restrict__ ws, int rhs);
@@ -158,6 +194,30 @@ __device__ void adj_hess3_1_13(double* __restrict__ ws);
 __device__ void adj_hess3_1_14(double* __restrict__ ws);
 __device__ void adj_hess3_1_15(double* __restrict__ ws);
 __device__ void adj_hess3_1_16(double* __restrict__ ws);
+__device__ void ddm_jv_0_0(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_0_1(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_0_2(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_0_3(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_0_4(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_0_5(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_src_0_0(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_0_1(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_0_2(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_0_3(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_0_4(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_0_5(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_jv_1_0(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_1_1(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_1_2(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_1_3(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_1_4(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_1_5(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_src_1_0(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_1_1(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_1_2(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_1_3(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_1_4(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_1_5(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
 constexpr int EBI_N_EBISP = 136;
 constexpr double EBI_DELTAT = 2.5;
 constexpr int EBI_NEBITER = 1000;
@@ -186,6 +246,23 @@ __device__ __forceinline__ void jacdecomp_0(double* __restrict__ ws, double gdti
     jacdecomp_0_10(ws, gdtinv);
     jacdecomp_0_11(ws, gdtinv);
     jacdecomp_0_12(ws, gdtinv);
+    jacdecomp_0_13(ws, gdtinv);
+    jacdecomp_0_14(ws, gdtinv);
+    jacdecomp_0_15(ws, gdtinv);
+    jacdecomp_0_16(ws, gdtinv);
+    jacdecomp_0_17(ws, gdtinv);
+    jacdecomp_0_18(ws, gdtinv);
+    jacdecomp_0_19(ws, gdtinv);
+    jacdecomp_0_20(ws, gdtinv);
+    jacdecomp_0_21(ws, gdtinv);
+    jacdecomp_0_22(ws, gdtinv);
+    jacdecomp_0_23(ws, gdtinv);
+    jacdecomp_0_24(ws, gdtinv);
+    jacdecomp_0_25(ws, gdtinv);
+    jacdecomp_0_26(ws, gdtinv);
+    jacdecomp_0_27(ws, gdtinv);
+    jacdecomp_0_28(ws, gdtinv);
+    jacdecomp_0_29(ws, gdtinv);
 }
 __device__ __forceinline__ void jacdecomp_0_sync(double* __restrict__ ws, double gdtinv, bool go)
 {
@@ -214,6 +291,40 @@ __device__ __forceinline__ void jacdecomp_0_sync(double* __restrict__ ws, double
     if (go) jacdecomp_0_11(ws, gdtinv);
     __syncthreads();
     if (go) jacdecomp_0_12(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_13(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_14(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_15(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_16(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_17(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_18(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_19(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_20(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_21(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_22(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_23(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_24(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_25(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_26(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_27(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_28(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_29(ws, gdtinv);
     __syncthreads();
 }
 __device__ __forceinline__ void solve_0(double* __restrict__ ws, int rhs)
@@ -245,6 +356,24 @@ __device__ __forceinline__ void jacdecomp_1(double* __restrict__ ws, double gdti
     jacdecomp_1_9(ws, gdtinv);
     jacdecomp_1_10(ws, gdtinv);
     jacdecomp_1_11(ws, gdtinv);
+    jacdecomp_1_12(ws, gdtinv);
+    jacdecomp_1_13(ws, gdtinv);
+    jacdecomp_1_14(ws, gdtinv);
+    jacdecomp_1_15(ws, gdtinv);
+    jacdecomp_1_16(ws, gdtinv);
+    jacdecomp_1_17(ws, gdtinv);
+    jacdecomp_1_18(ws, gdtinv);
+    jacdecomp_1_19(ws, gdtinv);
+    jacdecomp_1_20(ws, gdtinv);
+    jacdecomp_1_21(ws, gdtinv);
+    jacdecomp_1_22(ws, gdtinv);
+    jacdecomp_1_23(ws, gdtinv);
+    jacdecomp_1_24(ws, gdtinv);
+    jacdecomp_1_25(ws, gdtinv);
+    jacdecomp_1_26(ws, gdtinv);
+    jacdecomp_1_27(ws, gdtinv);
+    jacdecomp_1_28(ws, gdtinv);
+    jacdecomp_1_29(ws, gdtinv);
 }
 __device__ __forceinline__ void jacdecomp_1_sync(double* __restrict__ ws, double gdtinv, bool go)
 {
@@ -271,6 +400,42 @@ __device__ __forceinline__ void jacdecomp_1_sync(double* __restrict__ ws, double
     if (go) jacdecomp_1_10(ws, gdtinv);
     __syncthreads();
     if (go) jacdecomp_1_11(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_12(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_13(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_14(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_15(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_16(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_17(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_18(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_19(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_20(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_21(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_22(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_23(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_24(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_25(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_26(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_27(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_28(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_29(ws, gdtinv);
     __syncthreads();
 }
 __device__ __forceinline__ void solve_1(double* __restrict__ ws, int rhs)
@@ -363,6 +528,42 @@ __device__ __forceinline__ void adj_hess3_1(double* __restrict__ ws)
     adj_hess3_1_15(ws);
     adj_hess3_1_16(ws);
 }
+__device__ __forceinline__ void ddm_jv_0(double* __restrict__ ws, int yoff, int voff, int outoff)
+{
+    ddm_jv_0_0(ws, yoff, voff, outoff);
+    ddm_jv_0_1(ws, yoff, voff, outoff);
+    ddm_jv_0_2(ws, yoff, voff, outoff);
+    ddm_jv_0_3(ws, yoff, voff, outoff);
+    ddm_jv_0_4(ws, yoff, voff, outoff);
+    ddm_jv_0_5(ws, yoff, voff, outoff);
+}
+__device__ __forceinline__ void ddm_src_0(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff)
+{
+    ddm_src_0_0(ws, mask, scale, outoff);
+    ddm_src_0_1(ws, mask, scale, outoff);
+    ddm_src_0_2(ws, mask, scale, outoff);
+    ddm_src_0_3(ws, mask, scale, outoff);
+    ddm_src_0_4(ws, mask, scale, outoff);
+    ddm_src_0_5(ws, mask, scale, outoff);
+}
+__device__ __forceinline__ void ddm_jv_1(double* __restrict__ ws, int yoff, int voff, int outoff)
+{
+    ddm_jv_1_0(ws, yoff, voff, outoff);
+    ddm_jv_1_1(ws, yoff, voff, outoff);
+    ddm_jv_1_2(ws, yoff, voff, outoff);
+    ddm_jv_1_3(ws, yoff, voff, outoff);
+    ddm_jv_1_4(ws, yoff, voff, outoff);
+    ddm_jv_1_5(ws, yoff, voff, outoff);
+}
+__device__ __forceinline__ void ddm_src_1(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff)
+{
+    ddm_src_1_0(ws, mask, scale, outoff);
+    ddm_src_1_1(ws, mask, scale, outoff);
+    ddm_src_1_2(ws, mask, scale, outoff);
+    ddm_src_1_3(ws, mask, scale, outoff);
+    ddm_src_1_4(ws, mask, scale, outoff);
+    ddm_src_1_5(ws, mask, scale, outoff);
+}
 struct Traits {
     static constexpr int NSPEC = mech_cb6r5_ae7_aq::NSPEC;
     static constexpr int NRXNS = mech_cb6r5_ae7_aq::NRXNS;
@@ -399,6 +600,7 @@ struct Traits {
     static constexpr int ADJ_EMIS = mech_cb6r5_ae7_aq::ADJ_EMIS;
     static constexpr int ADJ_GE = mech_cb6r5_ae7_aq::ADJ_GE;
     static constexpr int ADJ_GK = mech_cb6r5_ae7_aq::ADJ_GK;
+    static constexpr int OFF_YAVE = mech_cb6r5_ae7_aq::OFF_YAVE;
     static constexpr const char* name() { return mech_cb6r5_ae7_aq::NAME; }
     static __device__ __forceinline__ int iold2new(int s) { return mech_cb6r5_ae7_aq::c_iold2new[s]; }
     static __device__ __forceinline__ int inew2old(int i) { return mech_cb6r5_ae7_aq::c_inew2old[i]; }
@@ -411,6 +613,8 @@ struct Traits {
     static __device__ __forceinline__ void solve_t_0(double* ws, int r) { mech_cb6r5_ae7_aq::solve_t_0(ws, r); }
     static __device__ __forceinline__ void adj_jtv_0(double* ws, int y, int phi, int out) { mech_cb6r5_ae7_aq::adj_jtv_0(ws, y, phi, out); }
     static __device__ __forceinline__ void adj_hess3_0(double* ws) { mech_cb6r5_ae7_aq::adj_hess3_0(ws); }
+    static __device__ __forceinline__ void ddm_jv_0(double* ws, int y, int v, int out) { mech_cb6r5_ae7_aq::ddm_jv_0(ws, y, v, out); }
+    static __device__ __forceinline__ void ddm_src_0(double* ws, const unsigned char* mk, double sc, int out) { mech_cb6r5_ae7_aq::ddm_src_0(ws, mk, sc, out); }
     static __device__ __forceinline__ void feval_1(double* ws, int s, int t) { mech_cb6r5_ae7_aq::feval_1(ws, s, t); }
     static __device__ __forceinline__ void explic_1(double* ws) { mech_cb6r5_ae7_aq::explic_1(ws); }
     static __device__ __forceinline__ void jacdecomp_1(double* ws, double g) { mech_cb6r5_ae7_aq::jacdecomp_1(ws, g); }
@@ -420,6 +624,8 @@ struct Traits {
     static __device__ __forceinline__ void solve_t_1(double* ws, int r) { mech_cb6r5_ae7_aq::solve_t_1(ws, r); }
     static __device__ __forceinline__ void adj_jtv_1(double* ws, int y, int phi, int out) { mech_cb6r5_ae7_aq::adj_jtv_1(ws, y, phi, out); }
     static __device__ __forceinline__ void adj_hess3_1(double* ws) { mech_cb6r5_ae7_aq::adj_hess3_1(ws); }
+    static __device__ __forceinline__ void ddm_jv_1(double* ws, int y, int v, int out) { mech_cb6r5_ae7_aq::ddm_jv_1(ws, y, v, out); }
+    static __device__ __forceinline__ void ddm_src_1(double* ws, const unsigned char* mk, double sc, int out) { mech_cb6r5_ae7_aq::ddm_src_1(ws, mk, sc, out); }
     static constexpr int EBI_N_EBISP = mech_cb6r5_ae7_aq::EBI_N_EBISP;
     static constexpr int EBI_NEBITER = mech_cb6r5_ae7_aq::EBI_NEBITER;
     static constexpr int EBI_NPNEG = mech_cb6r5_ae7_aq::EBI_NPNEG;

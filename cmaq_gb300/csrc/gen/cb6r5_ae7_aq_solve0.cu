@@ -5,8 +5,8 @@
 namespace mech_cb6r5_ae7_aq {
 __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
 {
-    const double* __restrict__ lu = ws + 72864;
-    const double* __restrict__ vd = ws + 126944;
+    const double* __restrict__ lu = ws + 77632;
+    const double* __restrict__ vd = ws + 131712;
     double* __restrict__ b = ws + rhs * 32;
     (void)vd;
     {
@@ -79,7 +79,7 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[512] = x;
     }
     {
-      CHEM_PREFETCH(ws + 72928);
+      CHEM_PREFETCH(ws + 77696);
       double x = b[544];
       b[544] = x;
     }
@@ -105,7 +105,7 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[704] = x;
     }
     {
-      CHEM_PREFETCH(ws + 72960);
+      CHEM_PREFETCH(ws + 77728);
       double x = b[736];
       b[736] = x;
     }
@@ -123,7 +123,7 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[832] = x;
     }
     {
-      CHEM_PREFETCH(ws + 72992);
+      CHEM_PREFETCH(ws + 77760);
       double x = b[864];
       b[864] = x;
     }
@@ -165,7 +165,7 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[1152] = x;
     }
     {
-      CHEM_PREFETCH(ws + 73024);
+      CHEM_PREFETCH(ws + 77792);
       double x = b[1184];
       b[1184] = x;
     }
@@ -174,8 +174,8 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[1216] = x;
     }
     {
-      CHEM_PREFETCH(ws + 73056);
-      CHEM_PREFETCH(ws + 73088);
+      CHEM_PREFETCH(ws + 77824);
+      CHEM_PREFETCH(ws + 77856);
       double x = b[1248];
       x = fma(-CHEM_LDLU(lu + 160), b[544], x);
       b[1248] = x;
@@ -185,23 +185,23 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[1280] = x;
     }
     {
-      CHEM_PREFETCH(ws + 73120);
-      CHEM_PREFETCH(ws + 73152);
-      CHEM_PREFETCH(ws + 73184);
+      CHEM_PREFETCH(ws + 77888);
+      CHEM_PREFETCH(ws + 77920);
+      CHEM_PREFETCH(ws + 77952);
       double x = b[1312];
       x = fma(-CHEM_LDLU(lu + 192), b[576], x);
       x = fma(-CHEM_LDLU(lu + 224), b[1056], x);
       b[1312] = x;
     }
     {
-      CHEM_PREFETCH(ws + 73216);
-      CHEM_PREFETCH(ws + 73248);
-      CHEM_PREFETCH(ws + 73280);
+      CHEM_PREFETCH(ws + 77984);
+      CHEM_PREFETCH(ws + 78016);
+      CHEM_PREFETCH(ws + 78048);
       double x = b[1344];
       b[1344] = x;
     }
     {
-      CHEM_PREFETCH(ws + 73312);
+      CHEM_PREFETCH(ws + 78080);
       double x = b[1376];
       x = fma(-CHEM_LDLU(lu + 256), b[64], x);
       x = fma(-CHEM_LDLU(lu + 288), b[96], x);
@@ -209,7 +209,7 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[1376] = x;
     }
     {
-      CHEM_PREFETCH(ws + 73344);
+      CHEM_PREFETCH(ws + 78112);
       double x = b[1408];
       x = fma(-CHEM_LDLU(lu + 352), b[160], x);
       x = fma(-CHEM_LDLU(lu + 384), b[192], x);
@@ -259,7 +259,7 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[1728] = x;
     }
     {
-      CHEM_PREFETCH(ws + 73376);
+      CHEM_PREFETCH(ws + 78144);
       double x = b[1760];
       b[1760] = x;
     }
@@ -268,15 +268,15 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[1792] = x;
     }
     {
-      CHEM_PREFETCH(ws + 73408);
+      CHEM_PREFETCH(ws + 78176);
       double x = b[1824];
       x = fma(-CHEM_LDLU(lu + 512), b[1216], x);
       b[1824] = x;
     }
     {
-      CHEM_PREFETCH(ws + 73440);
-      CHEM_PREFETCH(ws + 73472);
-      CHEM_PREFETCH(ws + 73504);
+      CHEM_PREFETCH(ws + 78208);
+      CHEM_PREFETCH(ws + 78240);
+      CHEM_PREFETCH(ws + 78272);
       double x = b[1856];
       b[1856] = x;
     }
@@ -301,7 +301,7 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[1984] = x;
     }
     {
-      CHEM_PREFETCH(ws + 73536);
+      CHEM_PREFETCH(ws + 78304);
       double x = b[2016];
       b[2016] = x;
     }
@@ -310,7 +310,7 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[2048] = x;
     }
     {
-      CHEM_PREFETCH(ws + 73568);
+      CHEM_PREFETCH(ws + 78336);
       double x = b[2080];
       x = fma(-CHEM_LDLU(lu + 672), b[2048], x);
       b[2080] = x;
@@ -320,18 +320,18 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[2112] = x;
     }
     {
-      CHEM_PREFETCH(ws + 73600);
+      CHEM_PREFETCH(ws + 78368);
       double x = b[2144];
       x = fma(-CHEM_LDLU(lu + 704), b[384], x);
       b[2144] = x;
     }
     {
-      CHEM_PREFETCH(ws + 73632);
+      CHEM_PREFETCH(ws + 78400);
       double x = b[2176];
       b[2176] = x;
     }
     {
-      CHEM_PREFETCH(ws + 73664);
+      CHEM_PREFETCH(ws + 78432);
       double x = b[2208];
       x = fma(-CHEM_LDLU(lu + 736), b[2016], x);
       b[2208] = x;
@@ -359,12 +359,12 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[2368] = x;
     }
     {
-      CHEM_PREFETCH(ws + 73696);
+      CHEM_PREFETCH(ws + 78464);
       double x = b[2400];
       b[2400] = x;
     }
     {
-      CHEM_PREFETCH(ws + 73728);
+      CHEM_PREFETCH(ws + 78496);
       double x = b[2432];
       b[2432] = x;
     }
@@ -374,25 +374,25 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[2464] = x;
     }
     {
-      CHEM_PREFETCH(ws + 73760);
+      CHEM_PREFETCH(ws + 78528);
       double x = b[2496];
       x = fma(-CHEM_LDLU(lu + 864), b[1120], x);
       b[2496] = x;
     }
     {
-      CHEM_PREFETCH(ws + 73792);
-      CHEM_PREFETCH(ws + 73824);
-      CHEM_PREFETCH(ws + 73856);
-      CHEM_PREFETCH(ws + 73888);
-      CHEM_PREFETCH(ws + 73920);
-      CHEM_PREFETCH(ws + 73952);
+      CHEM_PREFETCH(ws + 78560);
+      CHEM_PREFETCH(ws + 78592);
+      CHEM_PREFETCH(ws + 78624);
+      CHEM_PREFETCH(ws + 78656);
+      CHEM_PREFETCH(ws + 78688);
+      CHEM_PREFETCH(ws + 78720);
       double x = b[2528];
       b[2528] = x;
     }
     {
-      CHEM_PREFETCH(ws + 73984);
-      CHEM_PREFETCH(ws + 74016);
-      CHEM_PREFETCH(ws + 74048);
+      CHEM_PREFETCH(ws + 78752);
+      CHEM_PREFETCH(ws + 78784);
+      CHEM_PREFETCH(ws + 78816);
       double x = b[2560];
       x = fma(-CHEM_LDLU(lu + 896), b[1152], x);
       b[2560] = x;
@@ -419,30 +419,30 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[2656] = x;
     }
     {
-      CHEM_PREFETCH(ws + 74080);
-      CHEM_PREFETCH(ws + 74112);
+      CHEM_PREFETCH(ws + 78848);
+      CHEM_PREFETCH(ws + 78880);
       double x = b[2688];
       b[2688] = x;
     }
     {
-      CHEM_PREFETCH(ws + 74144);
-      CHEM_PREFETCH(ws + 74176);
-      CHEM_PREFETCH(ws + 74208);
+      CHEM_PREFETCH(ws + 78912);
+      CHEM_PREFETCH(ws + 78944);
+      CHEM_PREFETCH(ws + 78976);
       double x = b[2720];
       b[2720] = x;
     }
     {
-      CHEM_PREFETCH(ws + 74240);
-      CHEM_PREFETCH(ws + 74272);
-      CHEM_PREFETCH(ws + 74304);
-      CHEM_PREFETCH(ws + 74336);
+      CHEM_PREFETCH(ws + 79008);
+      CHEM_PREFETCH(ws + 79040);
+      CHEM_PREFETCH(ws + 79072);
+      CHEM_PREFETCH(ws + 79104);
       double x = b[2752];
       x = fma(-CHEM_LDLU(lu + 1216), b[1504], x);
       x = fma(-CHEM_LDLU(lu + 1248), b[2304], x);
       b[2752] = x;
     }
     {
-      CHEM_PREFETCH(ws + 74368);
+      CHEM_PREFETCH(ws + 79136);
       double x = b[2784];
       x = fma(-CHEM_LDLU(lu + 1280), b[1504], x);
       x = fma(-CHEM_LDLU(lu + 1312), b[2304], x);
@@ -463,47 +463,47 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[2848] = x;
     }
     {
-      CHEM_PREFETCH(ws + 74400);
+      CHEM_PREFETCH(ws + 79168);
       double x = b[2880];
       b[2880] = x;
     }
     {
-      CHEM_PREFETCH(ws + 74432);
+      CHEM_PREFETCH(ws + 79200);
       double x = b[2912];
       b[2912] = x;
     }
     {
-      CHEM_PREFETCH(ws + 74464);
+      CHEM_PREFETCH(ws + 79232);
       double x = b[2944];
       x = fma(-CHEM_LDLU(lu + 1536), b[1088], x);
       b[2944] = x;
     }
     {
-      CHEM_PREFETCH(ws + 74496);
-      CHEM_PREFETCH(ws + 74528);
+      CHEM_PREFETCH(ws + 79264);
+      CHEM_PREFETCH(ws + 79296);
       double x = b[2976];
       x = fma(-CHEM_LDLU(lu + 1568), b[2400], x);
       b[2976] = x;
     }
     {
-      CHEM_PREFETCH(ws + 74560);
-      CHEM_PREFETCH(ws + 74592);
-      CHEM_PREFETCH(ws + 74624);
-      CHEM_PREFETCH(ws + 74656);
-      CHEM_PREFETCH(ws + 74688);
+      CHEM_PREFETCH(ws + 79328);
+      CHEM_PREFETCH(ws + 79360);
+      CHEM_PREFETCH(ws + 79392);
+      CHEM_PREFETCH(ws + 79424);
+      CHEM_PREFETCH(ws + 79456);
       double x = b[3008];
       x = fma(-CHEM_LDLU(lu + 1600), b[1184], x);
       b[3008] = x;
     }
     {
-      CHEM_PREFETCH(ws + 74720);
+      CHEM_PREFETCH(ws + 79488);
       double x = b[3040];
       x = fma(-CHEM_LDLU(lu + 1632), b[1184], x);
       x = fma(-CHEM_LDLU(lu + 1664), b[3008], x);
       b[3040] = x;
     }
     {
-      CHEM_PREFETCH(ws + 74752);
+      CHEM_PREFETCH(ws + 79520);
       double x = b[3072];
       x = fma(-CHEM_LDLU(lu + 1696), b[448], x);
       x = fma(-CHEM_LDLU(lu + 1728), b[2144], x);
@@ -513,28 +513,28 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[3072] = x;
     }
     {
-      CHEM_PREFETCH(ws + 74784);
-      CHEM_PREFETCH(ws + 74816);
-      CHEM_PREFETCH(ws + 74848);
-      CHEM_PREFETCH(ws + 74880);
+      CHEM_PREFETCH(ws + 79552);
+      CHEM_PREFETCH(ws + 79584);
+      CHEM_PREFETCH(ws + 79616);
+      CHEM_PREFETCH(ws + 79648);
       double x = b[3104];
       x = fma(-CHEM_LDLU(lu + 1856), b[384], x);
       b[3104] = x;
     }
     {
-      CHEM_PREFETCH(ws + 74912);
-      CHEM_PREFETCH(ws + 74944);
-      CHEM_PREFETCH(ws + 74976);
-      CHEM_PREFETCH(ws + 75008);
-      CHEM_PREFETCH(ws + 75040);
+      CHEM_PREFETCH(ws + 79680);
+      CHEM_PREFETCH(ws + 79712);
+      CHEM_PREFETCH(ws + 79744);
+      CHEM_PREFETCH(ws + 79776);
+      CHEM_PREFETCH(ws + 79808);
       double x = b[3136];
       x = fma(-CHEM_LDLU(lu + 1888), b[1664], x);
       b[3136] = x;
     }
     {
-      CHEM_PREFETCH(ws + 75072);
-      CHEM_PREFETCH(ws + 75104);
-      CHEM_PREFETCH(ws + 75136);
+      CHEM_PREFETCH(ws + 79840);
+      CHEM_PREFETCH(ws + 79872);
+      CHEM_PREFETCH(ws + 79904);
       double x = b[3168];
       x = fma(-CHEM_LDLU(lu + 1920), b[2752], x);
       x = fma(-CHEM_LDLU(lu + 1952), b[2784], x);
@@ -543,11 +543,11 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[3168] = x;
     }
     {
-      CHEM_PREFETCH(ws + 75168);
-      CHEM_PREFETCH(ws + 75200);
-      CHEM_PREFETCH(ws + 75232);
-      CHEM_PREFETCH(ws + 75264);
-      CHEM_PREFETCH(ws + 75296);
+      CHEM_PREFETCH(ws + 79936);
+      CHEM_PREFETCH(ws + 79968);
+      CHEM_PREFETCH(ws + 80000);
+      CHEM_PREFETCH(ws + 80032);
+      CHEM_PREFETCH(ws + 80064);
       double x = b[3200];
       x = fma(-CHEM_LDLU(lu + 2048), b[2752], x);
       x = fma(-CHEM_LDLU(lu + 2080), b[2784], x);
@@ -557,8 +557,8 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[3200] = x;
     }
     {
-      CHEM_PREFETCH(ws + 75328);
-      CHEM_PREFETCH(ws + 75360);
+      CHEM_PREFETCH(ws + 80096);
+      CHEM_PREFETCH(ws + 80128);
       double x = b[3232];
       x = fma(-CHEM_LDLU(lu + 2208), b[2528], x);
       x = fma(-CHEM_LDLU(lu + 2240), b[2656], x);
@@ -566,8 +566,8 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[3232] = x;
     }
     {
-      CHEM_PREFETCH(ws + 75392);
-      CHEM_PREFETCH(ws + 75424);
+      CHEM_PREFETCH(ws + 80160);
+      CHEM_PREFETCH(ws + 80192);
       double x = b[3264];
       x = fma(-CHEM_LDLU(lu + 2304), b[448], x);
       x = fma(-CHEM_LDLU(lu + 2336), b[2144], x);
@@ -577,33 +577,33 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[3264] = x;
     }
     {
-      CHEM_PREFETCH(ws + 75456);
+      CHEM_PREFETCH(ws + 80224);
       double x = b[3296];
       x = fma(-CHEM_LDLU(lu + 2464), b[1056], x);
       x = fma(-CHEM_LDLU(lu + 2496), b[1664], x);
       b[3296] = x;
     }
     {
-      CHEM_PREFETCH(ws + 75488);
-      CHEM_PREFETCH(ws + 75520);
-      CHEM_PREFETCH(ws + 75552);
-      CHEM_PREFETCH(ws + 75584);
+      CHEM_PREFETCH(ws + 80256);
+      CHEM_PREFETCH(ws + 80288);
+      CHEM_PREFETCH(ws + 80320);
+      CHEM_PREFETCH(ws + 80352);
       double x = b[3328];
       x = fma(-CHEM_LDLU(lu + 2528), b[1760], x);
       x = fma(-CHEM_LDLU(lu + 2560), b[2176], x);
       b[3328] = x;
     }
     {
-      CHEM_PREFETCH(ws + 75616);
-      CHEM_PREFETCH(ws + 75648);
+      CHEM_PREFETCH(ws + 80384);
+      CHEM_PREFETCH(ws + 80416);
       double x = b[3360];
       x = fma(-CHEM_LDLU(lu + 2592), b[2848], x);
       b[3360] = x;
     }
     {
-      CHEM_PREFETCH(ws + 75680);
-      CHEM_PREFETCH(ws + 75712);
-      CHEM_PREFETCH(ws + 75744);
+      CHEM_PREFETCH(ws + 80448);
+      CHEM_PREFETCH(ws + 80480);
+      CHEM_PREFETCH(ws + 80512);
       double x = b[3392];
       x = fma(-CHEM_LDLU(lu + 2624), b[896], x);
       x = fma(-CHEM_LDLU(lu + 2656), b[928], x);
@@ -612,15 +612,15 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[3392] = x;
     }
     {
-      CHEM_PREFETCH(ws + 75776);
+      CHEM_PREFETCH(ws + 80544);
       double x = b[3424];
       x = fma(-CHEM_LDLU(lu + 2752), b[1664], x);
       x = fma(-CHEM_LDLU(lu + 2784), b[2528], x);
       b[3424] = x;
     }
     {
-      CHEM_PREFETCH(ws + 75808);
-      CHEM_PREFETCH(ws + 75840);
+      CHEM_PREFETCH(ws + 80576);
+      CHEM_PREFETCH(ws + 80608);
       double x = b[3456];
       x = fma(-CHEM_LDLU(lu + 2816), b[3008], x);
       x = fma(-CHEM_LDLU(lu + 2848), b[3136], x);
@@ -628,27 +628,27 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[3456] = x;
     }
     {
-      CHEM_PREFETCH(ws + 75872);
-      CHEM_PREFETCH(ws + 75904);
-      CHEM_PREFETCH(ws + 75936);
+      CHEM_PREFETCH(ws + 80640);
+      CHEM_PREFETCH(ws + 80672);
+      CHEM_PREFETCH(ws + 80704);
       double x = b[3488];
       x = fma(-CHEM_LDLU(lu + 2912), b[1088], x);
       b[3488] = x;
     }
     {
-      CHEM_PREFETCH(ws + 75968);
-      CHEM_PREFETCH(ws + 76000);
+      CHEM_PREFETCH(ws + 80736);
+      CHEM_PREFETCH(ws + 80768);
       double x = b[3520];
       x = fma(-CHEM_LDLU(lu + 2944), b[1216], x);
       x = fma(-CHEM_LDLU(lu + 2976), b[2016], x);
       b[3520] = x;
     }
     {
-      CHEM_PREFETCH(ws + 76032);
-      CHEM_PREFETCH(ws + 76064);
-      CHEM_PREFETCH(ws + 76096);
-      CHEM_PREFETCH(ws + 76128);
-      CHEM_PREFETCH(ws + 76160);
+      CHEM_PREFETCH(ws + 80800);
+      CHEM_PREFETCH(ws + 80832);
+      CHEM_PREFETCH(ws + 80864);
+      CHEM_PREFETCH(ws + 80896);
+      CHEM_PREFETCH(ws + 80928);
       double x = b[3552];
       x = fma(-CHEM_LDLU(lu + 3008), b[1632], x);
       x = fma(-CHEM_LDLU(lu + 3040), b[3136], x);
@@ -656,26 +656,26 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[3552] = x;
     }
     {
-      CHEM_PREFETCH(ws + 76192);
-      CHEM_PREFETCH(ws + 76224);
-      CHEM_PREFETCH(ws + 76256);
-      CHEM_PREFETCH(ws + 76288);
-      CHEM_PREFETCH(ws + 76320);
-      CHEM_PREFETCH(ws + 76352);
+      CHEM_PREFETCH(ws + 80960);
+      CHEM_PREFETCH(ws + 80992);
+      CHEM_PREFETCH(ws + 81024);
+      CHEM_PREFETCH(ws + 81056);
+      CHEM_PREFETCH(ws + 81088);
+      CHEM_PREFETCH(ws + 81120);
       double x = b[3584];
       x = fma(-CHEM_LDLU(lu + 3104), b[1120], x);
       x = fma(-CHEM_LDLU(lu + 3136), b[1152], x);
       b[3584] = x;
     }
     {
-      CHEM_PREFETCH(ws + 76384);
-      CHEM_PREFETCH(ws + 76416);
-      CHEM_PREFETCH(ws + 76448);
-      CHEM_PREFETCH(ws + 76480);
-      CHEM_PREFETCH(ws + 76512);
-      CHEM_PREFETCH(ws + 76544);
-      CHEM_PREFETCH(ws + 76576);
-      CHEM_PREFETCH(ws + 76608);
+      CHEM_PREFETCH(ws + 81152);
+      CHEM_PREFETCH(ws + 81184);
+      CHEM_PREFETCH(ws + 81216);
+      CHEM_PREFETCH(ws + 81248);
+      CHEM_PREFETCH(ws + 81280);
+      CHEM_PREFETCH(ws + 81312);
+      CHEM_PREFETCH(ws + 81344);
+      CHEM_PREFETCH(ws + 81376);
       double x = b[3616];
       x = fma(-CHEM_LDLU(lu + 3168), b[384], x);
       x = fma(-CHEM_LDLU(lu + 3200), b[1088], x);
@@ -685,15 +685,15 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[3616] = x;
     }
     {
-      CHEM_PREFETCH(ws + 76640);
-      CHEM_PREFETCH(ws + 76672);
-      CHEM_PREFETCH(ws + 76704);
-      CHEM_PREFETCH(ws + 76736);
-      CHEM_PREFETCH(ws + 76768);
-      CHEM_PREFETCH(ws + 76800);
-      CHEM_PREFETCH(ws + 76832);
-      CHEM_PREFETCH(ws + 76864);
-      CHEM_PREFETCH(ws + 76896);
+      CHEM_PREFETCH(ws + 81408);
+      CHEM_PREFETCH(ws + 81440);
+      CHEM_PREFETCH(ws + 81472);
+      CHEM_PREFETCH(ws + 81504);
+      CHEM_PREFETCH(ws + 81536);
+      CHEM_PREFETCH(ws + 81568);
+      CHEM_PREFETCH(ws + 81600);
+      CHEM_PREFETCH(ws + 81632);
+      CHEM_PREFETCH(ws + 81664);
       double x = b[3648];
       x = fma(-CHEM_LDLU(lu + 3328), b[960], x);
       x = fma(-CHEM_LDLU(lu + 3360), b[1984], x);
@@ -704,8 +704,8 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[3648] = x;
     }
     {
-      CHEM_PREFETCH(ws + 76928);
-      CHEM_PREFETCH(ws + 76960);
+      CHEM_PREFETCH(ws + 81696);
+      CHEM_PREFETCH(ws + 81728);
       double x = b[3680];
       x = fma(-CHEM_LDLU(lu + 3520), b[1504], x);
       x = fma(-CHEM_LDLU(lu + 3552), b[2304], x);
@@ -718,13 +718,13 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[3680] = x;
     }
     {
-      CHEM_PREFETCH(ws + 76992);
-      CHEM_PREFETCH(ws + 77024);
-      CHEM_PREFETCH(ws + 77056);
-      CHEM_PREFETCH(ws + 77088);
-      CHEM_PREFETCH(ws + 77120);
-      CHEM_PREFETCH(ws + 77152);
-      CHEM_PREFETCH(ws + 77184);
+      CHEM_PREFETCH(ws + 81760);
+      CHEM_PREFETCH(ws + 81792);
+      CHEM_PREFETCH(ws + 81824);
+      CHEM_PREFETCH(ws + 81856);
+      CHEM_PREFETCH(ws + 81888);
+      CHEM_PREFETCH(ws + 81920);
+      CHEM_PREFETCH(ws + 81952);
       double x = b[3712];
       x = fma(-CHEM_LDLU(lu + 3776), b[1504], x);
       x = fma(-CHEM_LDLU(lu + 3808), b[2304], x);
@@ -738,21 +738,21 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[3712] = x;
     }
     {
-      CHEM_PREFETCH(ws + 77216);
-      CHEM_PREFETCH(ws + 77248);
-      CHEM_PREFETCH(ws + 77280);
-      CHEM_PREFETCH(ws + 77312);
+      CHEM_PREFETCH(ws + 81984);
+      CHEM_PREFETCH(ws + 82016);
+      CHEM_PREFETCH(ws + 82048);
+      CHEM_PREFETCH(ws + 82080);
       double x = b[3744];
       x = fma(-CHEM_LDLU(lu + 4064), b[1792], x);
       x = fma(-CHEM_LDLU(lu + 4096), b[3616], x);
       b[3744] = x;
     }
     {
-      CHEM_PREFETCH(ws + 77344);
-      CHEM_PREFETCH(ws + 77376);
-      CHEM_PREFETCH(ws + 77408);
-      CHEM_PREFETCH(ws + 77440);
-      CHEM_PREFETCH(ws + 77472);
+      CHEM_PREFETCH(ws + 82112);
+      CHEM_PREFETCH(ws + 82144);
+      CHEM_PREFETCH(ws + 82176);
+      CHEM_PREFETCH(ws + 82208);
+      CHEM_PREFETCH(ws + 82240);
       double x = b[3776];
       x = fma(-CHEM_LDLU(lu + 4128), b[352], x);
       x = fma(-CHEM_LDLU(lu + 4160), b[1632], x);
@@ -764,9 +764,9 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[3776] = x;
     }
     {
-      CHEM_PREFETCH(ws + 77504);
-      CHEM_PREFETCH(ws + 77536);
-      CHEM_PREFETCH(ws + 77568);
+      CHEM_PREFETCH(ws + 82272);
+      CHEM_PREFETCH(ws + 82304);
+      CHEM_PREFETCH(ws + 82336);
       double x = b[3808];
       x = fma(-CHEM_LDLU(lu + 4352), b[1120], x);
       x = fma(-CHEM_LDLU(lu + 4384), b[1152], x);
@@ -775,12 +775,12 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[3808] = x;
     }
     {
-      CHEM_PREFETCH(ws + 77600);
-      CHEM_PREFETCH(ws + 77632);
-      CHEM_PREFETCH(ws + 77664);
-      CHEM_PREFETCH(ws + 77696);
-      CHEM_PREFETCH(ws + 77728);
-      CHEM_PREFETCH(ws + 77760);
+      CHEM_PREFETCH(ws + 82368);
+      CHEM_PREFETCH(ws + 82400);
+      CHEM_PREFETCH(ws + 82432);
+      CHEM_PREFETCH(ws + 82464);
+      CHEM_PREFETCH(ws + 82496);
+      CHEM_PREFETCH(ws + 82528);
       double x = b[3840];
       x = fma(-CHEM_LDLU(lu + 4480), b[864], x);
       x = fma(-CHEM_LDLU(lu + 4512), b[1632], x);
@@ -790,15 +790,15 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[3840] = x;
     }
     {
-      CHEM_PREFETCH(ws + 77792);
-      CHEM_PREFETCH(ws + 77824);
-      CHEM_PREFETCH(ws + 77856);
-      CHEM_PREFETCH(ws + 77888);
-      CHEM_PREFETCH(ws + 77920);
-      CHEM_PREFETCH(ws + 77952);
-      CHEM_PREFETCH(ws + 77984);
-      CHEM_PREFETCH(ws + 78016);
-      CHEM_PREFETCH(ws + 78048);
+      CHEM_PREFETCH(ws + 82560);
+      CHEM_PREFETCH(ws + 82592);
+      CHEM_PREFETCH(ws + 82624);
+      CHEM_PREFETCH(ws + 82656);
+      CHEM_PREFETCH(ws + 82688);
+      CHEM_PREFETCH(ws + 82720);
+      CHEM_PREFETCH(ws + 82752);
+      CHEM_PREFETCH(ws + 82784);
+      CHEM_PREFETCH(ws + 82816);
       double x = b[3872];
       x = fma(-CHEM_LDLU(lu + 4640), b[1024], x);
       x = fma(-CHEM_LDLU(lu + 4672), b[2528], x);
@@ -806,18 +806,18 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[3872] = x;
     }
     {
-      CHEM_PREFETCH(ws + 78080);
-      CHEM_PREFETCH(ws + 78112);
-      CHEM_PREFETCH(ws + 78144);
-      CHEM_PREFETCH(ws + 78176);
-      CHEM_PREFETCH(ws + 78208);
-      CHEM_PREFETCH(ws + 78240);
-      CHEM_PREFETCH(ws + 78272);
-      CHEM_PREFETCH(ws + 78304);
-      CHEM_PREFETCH(ws + 78336);
-      CHEM_PREFETCH(ws + 78368);
-      CHEM_PREFETCH(ws + 78400);
-      CHEM_PREFETCH(ws + 78432);
+      CHEM_PREFETCH(ws + 82848);
+      CHEM_PREFETCH(ws + 82880);
+      CHEM_PREFETCH(ws + 82912);
+      CHEM_PREFETCH(ws + 82944);
+      CHEM_PREFETCH(ws + 82976);
+      CHEM_PREFETCH(ws + 83008);
+      CHEM_PREFETCH(ws + 83040);
+      CHEM_PREFETCH(ws + 83072);
+      CHEM_PREFETCH(ws + 83104);
+      CHEM_PREFETCH(ws + 83136);
+      CHEM_PREFETCH(ws + 83168);
+      CHEM_PREFETCH(ws + 83200);
       double x = b[3904];
       x = fma(-CHEM_LDLU(lu + 4736), b[3136], x);
       x = fma(-CHEM_LDLU(lu + 4768), b[3296], x);
@@ -828,16 +828,16 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[3904] = x;
     }
     {
-      CHEM_PREFETCH(ws + 78464);
-      CHEM_PREFETCH(ws + 78496);
-      CHEM_PREFETCH(ws + 78528);
-      CHEM_PREFETCH(ws + 78560);
-      CHEM_PREFETCH(ws + 78592);
-      CHEM_PREFETCH(ws + 78624);
-      CHEM_PREFETCH(ws + 78656);
-      CHEM_PREFETCH(ws + 78688);
-      CHEM_PREFETCH(ws + 78720);
-      CHEM_PREFETCH(ws + 78752);
+      CHEM_PREFETCH(ws + 83232);
+      CHEM_PREFETCH(ws + 83264);
+      CHEM_PREFETCH(ws + 83296);
+      CHEM_PREFETCH(ws + 83328);
+      CHEM_PREFETCH(ws + 83360);
+      CHEM_PREFETCH(ws + 83392);
+      CHEM_PREFETCH(ws + 83424);
+      CHEM_PREFETCH(ws + 83456);
+      CHEM_PREFETCH(ws + 83488);
+      CHEM_PREFETCH(ws + 83520);
       double x = b[3936];
       x = fma(-CHEM_LDLU(lu + 4928), b[384], x);
       x = fma(-CHEM_LDLU(lu + 4960), b[1088], x);
@@ -851,23 +851,23 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[3936] = x;
     }
     {
-      CHEM_PREFETCH(ws + 78784);
-      CHEM_PREFETCH(ws + 78816);
-      CHEM_PREFETCH(ws + 78848);
-      CHEM_PREFETCH(ws + 78880);
-      CHEM_PREFETCH(ws + 78912);
-      CHEM_PREFETCH(ws + 78944);
-      CHEM_PREFETCH(ws + 78976);
-      CHEM_PREFETCH(ws + 79008);
-      CHEM_PREFETCH(ws + 79040);
-      CHEM_PREFETCH(ws + 79072);
-      CHEM_PREFETCH(ws + 79104);
-      CHEM_PREFETCH(ws + 79136);
-      CHEM_PREFETCH(ws + 79168);
-      CHEM_PREFETCH(ws + 79200);
-      CHEM_PREFETCH(ws + 79232);
-      CHEM_PREFETCH(ws + 79264);
-      CHEM_PREFETCH(ws + 79296);
+      CHEM_PREFETCH(ws + 83552);
+      CHEM_PREFETCH(ws + 83584);
+      CHEM_PREFETCH(ws + 83616);
+      CHEM_PREFETCH(ws + 83648);
+      CHEM_PREFETCH(ws + 83680);
+      CHEM_PREFETCH(ws + 83712);
+      CHEM_PREFETCH(ws + 83744);
+      CHEM_PREFETCH(ws + 83776);
+      CHEM_PREFETCH(ws + 83808);
+      CHEM_PREFETCH(ws + 83840);
+      CHEM_PREFETCH(ws + 83872);
+      CHEM_PREFETCH(ws + 83904);
+      CHEM_PREFETCH(ws + 83936);
+      CHEM_PREFETCH(ws + 83968);
+      CHEM_PREFETCH(ws + 84000);
+      CHEM_PREFETCH(ws + 84032);
+      CHEM_PREFETCH(ws + 84064);
       double x = b[3968];
       x = fma(-CHEM_LDLU(lu + 5216), b[832], x);
       x = fma(-CHEM_LDLU(lu + 5248), b[864], x);
@@ -884,20 +884,20 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[3968] = x;
     }
     {
-      CHEM_PREFETCH(ws + 79328);
-      CHEM_PREFETCH(ws + 79360);
-      CHEM_PREFETCH(ws + 79392);
-      CHEM_PREFETCH(ws + 79424);
-      CHEM_PREFETCH(ws + 79456);
-      CHEM_PREFETCH(ws + 79488);
-      CHEM_PREFETCH(ws + 79520);
-      CHEM_PREFETCH(ws + 79552);
-      CHEM_PREFETCH(ws + 79584);
-      CHEM_PREFETCH(ws + 79616);
-      CHEM_PREFETCH(ws + 79648);
-      CHEM_PREFETCH(ws + 79680);
-      CHEM_PREFETCH(ws + 79712);
-      CHEM_PREFETCH(ws + 79744);
+      CHEM_PREFETCH(ws + 84096);
+      CHEM_PREFETCH(ws + 84128);
+      CHEM_PREFETCH(ws + 84160);
+      CHEM_PREFETCH(ws + 84192);
+      CHEM_PREFETCH(ws + 84224);
+      CHEM_PREFETCH(ws + 84256);
+      CHEM_PREFETCH(ws + 84288);
+      CHEM_PREFETCH(ws + 84320);
+      CHEM_PREFETCH(ws + 84352);
+      CHEM_PREFETCH(ws + 84384);
+      CHEM_PREFETCH(ws + 84416);
+      CHEM_PREFETCH(ws + 84448);
+      CHEM_PREFETCH(ws + 84480);
+      CHEM_PREFETCH(ws + 84512);
       double x = b[4000];
       x = fma(-CHEM_LDLU(lu + 5600), b[3136], x);
       x = fma(-CHEM_LDLU(lu + 5632), b[3296], x);
@@ -912,17 +912,17 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[4000] = x;
     }
     {
-      CHEM_PREFETCH(ws + 79776);
-      CHEM_PREFETCH(ws + 79808);
-      CHEM_PREFETCH(ws + 79840);
-      CHEM_PREFETCH(ws + 79872);
-      CHEM_PREFETCH(ws + 79904);
-      CHEM_PREFETCH(ws + 79936);
-      CHEM_PREFETCH(ws + 79968);
-      CHEM_PREFETCH(ws + 80000);
-      CHEM_PREFETCH(ws + 80032);
-      CHEM_PREFETCH(ws + 80064);
-      CHEM_PREFETCH(ws + 80096);
+      CHEM_PREFETCH(ws + 84544);
+      CHEM_PREFETCH(ws + 84576);
+      CHEM_PREFETCH(ws + 84608);
+      CHEM_PREFETCH(ws + 84640);
+      CHEM_PREFETCH(ws + 84672);
+      CHEM_PREFETCH(ws + 84704);
+      CHEM_PREFETCH(ws + 84736);
+      CHEM_PREFETCH(ws + 84768);
+      CHEM_PREFETCH(ws + 84800);
+      CHEM_PREFETCH(ws + 84832);
+      CHEM_PREFETCH(ws + 84864);
       double x = b[4032];
       x = fma(-CHEM_LDLU(lu + 5920), b[1632], x);
       x = fma(-CHEM_LDLU(lu + 5952), b[1792], x);
@@ -944,20 +944,20 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[4032] = x;
     }
     {
-      CHEM_PREFETCH(ws + 80128);
-      CHEM_PREFETCH(ws + 80160);
-      CHEM_PREFETCH(ws + 80192);
-      CHEM_PREFETCH(ws + 80224);
-      CHEM_PREFETCH(ws + 80256);
-      CHEM_PREFETCH(ws + 80288);
-      CHEM_PREFETCH(ws + 80320);
-      CHEM_PREFETCH(ws + 80352);
-      CHEM_PREFETCH(ws + 80384);
-      CHEM_PREFETCH(ws + 80416);
-      CHEM_PREFETCH(ws + 80448);
-      CHEM_PREFETCH(ws + 80480);
-      CHEM_PREFETCH(ws + 80512);
-      CHEM_PREFETCH(ws + 80544);
+      CHEM_PREFETCH(ws + 84896);
+      CHEM_PREFETCH(ws + 84928);
+      CHEM_PREFETCH(ws + 84960);
+      CHEM_PREFETCH(ws + 84992);
+      CHEM_PREFETCH(ws + 85024);
+      CHEM_PREFETCH(ws + 85056);
+      CHEM_PREFETCH(ws + 85088);
+      CHEM_PREFETCH(ws + 85120);
+      CHEM_PREFETCH(ws + 85152);
+      CHEM_PREFETCH(ws + 85184);
+      CHEM_PREFETCH(ws + 85216);
+      CHEM_PREFETCH(ws + 85248);
+      CHEM_PREFETCH(ws + 85280);
+      CHEM_PREFETCH(ws + 85312);
       double x = b[4064];
       x = fma(-CHEM_LDLU(lu + 6464), b[928], x);
       x = fma(-CHEM_LDLU(lu + 6496), b[960], x);
@@ -976,21 +976,21 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[4064] = x;
     }
     {
-      CHEM_PREFETCH(ws + 80576);
-      CHEM_PREFETCH(ws + 80608);
-      CHEM_PREFETCH(ws + 80640);
-      CHEM_PREFETCH(ws + 80672);
-      CHEM_PREFETCH(ws + 80704);
-      CHEM_PREFETCH(ws + 80736);
-      CHEM_PREFETCH(ws + 80768);
-      CHEM_PREFETCH(ws + 80800);
-      CHEM_PREFETCH(ws + 80832);
-      CHEM_PREFETCH(ws + 80864);
-      CHEM_PREFETCH(ws + 80896);
-      CHEM_PREFETCH(ws + 80928);
-      CHEM_PREFETCH(ws + 80960);
-      CHEM_PREFETCH(ws + 80992);
-      CHEM_PREFETCH(ws + 81024);
+      CHEM_PREFETCH(ws + 85344);
+      CHEM_PREFETCH(ws + 85376);
+      CHEM_PREFETCH(ws + 85408);
+      CHEM_PREFETCH(ws + 85440);
+      CHEM_PREFETCH(ws + 85472);
+      CHEM_PREFETCH(ws + 85504);
+      CHEM_PREFETCH(ws + 85536);
+      CHEM_PREFETCH(ws + 85568);
+      CHEM_PREFETCH(ws + 85600);
+      CHEM_PREFETCH(ws + 85632);
+      CHEM_PREFETCH(ws + 85664);
+      CHEM_PREFETCH(ws + 85696);
+      CHEM_PREFETCH(ws + 85728);
+      CHEM_PREFETCH(ws + 85760);
+      CHEM_PREFETCH(ws + 85792);
       double x = b[4096];
       x = fma(-CHEM_LDLU(lu + 6912), b[320], x);
       x = fma(-CHEM_LDLU(lu + 6944), b[960], x);
@@ -1006,26 +1006,26 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[4096] = x;
     }
     {
-      CHEM_PREFETCH(ws + 81056);
-      CHEM_PREFETCH(ws + 81088);
-      CHEM_PREFETCH(ws + 81120);
-      CHEM_PREFETCH(ws + 81152);
-      CHEM_PREFETCH(ws + 81184);
-      CHEM_PREFETCH(ws + 81216);
-      CHEM_PREFETCH(ws + 81248);
-      CHEM_PREFETCH(ws + 81280);
-      CHEM_PREFETCH(ws + 81312);
-      CHEM_PREFETCH(ws + 81344);
-      CHEM_PREFETCH(ws + 81376);
-      CHEM_PREFETCH(ws + 81408);
-      CHEM_PREFETCH(ws + 81440);
-      CHEM_PREFETCH(ws + 81472);
-      CHEM_PREFETCH(ws + 81504);
-      CHEM_PREFETCH(ws + 81536);
-      CHEM_PREFETCH(ws + 81568);
-      CHEM_PREFETCH(ws + 81600);
-      CHEM_PREFETCH(ws + 81632);
-      CHEM_PREFETCH(ws + 81664);
+      CHEM_PREFETCH(ws + 85824);
+      CHEM_PREFETCH(ws + 85856);
+      CHEM_PREFETCH(ws + 85888);
+      CHEM_PREFETCH(ws + 85920);
+      CHEM_PREFETCH(ws + 85952);
+      CHEM_PREFETCH(ws + 85984);
+      CHEM_PREFETCH(ws + 86016);
+      CHEM_PREFETCH(ws + 86048);
+      CHEM_PREFETCH(ws + 86080);
+      CHEM_PREFETCH(ws + 86112);
+      CHEM_PREFETCH(ws + 86144);
+      CHEM_PREFETCH(ws + 86176);
+      CHEM_PREFETCH(ws + 86208);
+      CHEM_PREFETCH(ws + 86240);
+      CHEM_PREFETCH(ws + 86272);
+      CHEM_PREFETCH(ws + 86304);
+      CHEM_PREFETCH(ws + 86336);
+      CHEM_PREFETCH(ws + 86368);
+      CHEM_PREFETCH(ws + 86400);
+      CHEM_PREFETCH(ws + 86432);
       double x = b[4128];
       x = fma(-CHEM_LDLU(lu + 7264), b[320], x);
       x = fma(-CHEM_LDLU(lu + 7296), b[832], x);
@@ -1044,20 +1044,20 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[4128] = x;
     }
     {
-      CHEM_PREFETCH(ws + 81696);
-      CHEM_PREFETCH(ws + 81728);
-      CHEM_PREFETCH(ws + 81760);
-      CHEM_PREFETCH(ws + 81792);
-      CHEM_PREFETCH(ws + 81824);
-      CHEM_PREFETCH(ws + 81856);
-      CHEM_PREFETCH(ws + 81888);
-      CHEM_PREFETCH(ws + 81920);
-      CHEM_PREFETCH(ws + 81952);
-      CHEM_PREFETCH(ws + 81984);
-      CHEM_PREFETCH(ws + 82016);
-      CHEM_PREFETCH(ws + 82048);
-      CHEM_PREFETCH(ws + 82080);
-      CHEM_PREFETCH(ws + 82112);
+      CHEM_PREFETCH(ws + 86464);
+      CHEM_PREFETCH(ws + 86496);
+      CHEM_PREFETCH(ws + 86528);
+      CHEM_PREFETCH(ws + 86560);
+      CHEM_PREFETCH(ws + 86592);
+      CHEM_PREFETCH(ws + 86624);
+      CHEM_PREFETCH(ws + 86656);
+      CHEM_PREFETCH(ws + 86688);
+      CHEM_PREFETCH(ws + 86720);
+      CHEM_PREFETCH(ws + 86752);
+      CHEM_PREFETCH(ws + 86784);
+      CHEM_PREFETCH(ws + 86816);
+      CHEM_PREFETCH(ws + 86848);
+      CHEM_PREFETCH(ws + 86880);
       double x = b[4160];
       x = fma(-CHEM_LDLU(lu + 7712), b[672], x);
       x = fma(-CHEM_LDLU(lu + 7744), b[2048], x);
@@ -1077,23 +1077,23 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[4160] = x;
     }
     {
-      CHEM_PREFETCH(ws + 82144);
-      CHEM_PREFETCH(ws + 82176);
-      CHEM_PREFETCH(ws + 82208);
-      CHEM_PREFETCH(ws + 82240);
-      CHEM_PREFETCH(ws + 82272);
-      CHEM_PREFETCH(ws + 82304);
-      CHEM_PREFETCH(ws + 82336);
-      CHEM_PREFETCH(ws + 82368);
-      CHEM_PREFETCH(ws + 82400);
-      CHEM_PREFETCH(ws + 82432);
-      CHEM_PREFETCH(ws + 82464);
-      CHEM_PREFETCH(ws + 82496);
-      CHEM_PREFETCH(ws + 82528);
-      CHEM_PREFETCH(ws + 82560);
-      CHEM_PREFETCH(ws + 82592);
-      CHEM_PREFETCH(ws + 82624);
-      CHEM_PREFETCH(ws + 82656);
+      CHEM_PREFETCH(ws + 86912);
+      CHEM_PREFETCH(ws + 86944);
+      CHEM_PREFETCH(ws + 86976);
+      CHEM_PREFETCH(ws + 87008);
+      CHEM_PREFETCH(ws + 87040);
+      CHEM_PREFETCH(ws + 87072);
+      CHEM_PREFETCH(ws + 87104);
+      CHEM_PREFETCH(ws + 87136);
+      CHEM_PREFETCH(ws + 87168);
+      CHEM_PREFETCH(ws + 87200);
+      CHEM_PREFETCH(ws + 87232);
+      CHEM_PREFETCH(ws + 87264);
+      CHEM_PREFETCH(ws + 87296);
+      CHEM_PREFETCH(ws + 87328);
+      CHEM_PREFETCH(ws + 87360);
+      CHEM_PREFETCH(ws + 87392);
+      CHEM_PREFETCH(ws + 87424);
       double x = b[4192];
       x = fma(-CHEM_LDLU(lu + 8192), b[1024], x);
       x = fma(-CHEM_LDLU(lu + 8224), b[1216], x);
@@ -1118,23 +1118,23 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[4192] = x;
     }
     {
-      CHEM_PREFETCH(ws + 82688);
-      CHEM_PREFETCH(ws + 82720);
-      CHEM_PREFETCH(ws + 82752);
-      CHEM_PREFETCH(ws + 82784);
-      CHEM_PREFETCH(ws + 82816);
-      CHEM_PREFETCH(ws + 82848);
-      CHEM_PREFETCH(ws + 82880);
-      CHEM_PREFETCH(ws + 82912);
-      CHEM_PREFETCH(ws + 82944);
-      CHEM_PREFETCH(ws + 82976);
-      CHEM_PREFETCH(ws + 83008);
-      CHEM_PREFETCH(ws + 83040);
-      CHEM_PREFETCH(ws + 83072);
-      CHEM_PREFETCH(ws + 83104);
-      CHEM_PREFETCH(ws + 83136);
-      CHEM_PREFETCH(ws + 83168);
-      CHEM_PREFETCH(ws + 83200);
+      CHEM_PREFETCH(ws + 87456);
+      CHEM_PREFETCH(ws + 87488);
+      CHEM_PREFETCH(ws + 87520);
+      CHEM_PREFETCH(ws + 87552);
+      CHEM_PREFETCH(ws + 87584);
+      CHEM_PREFETCH(ws + 87616);
+      CHEM_PREFETCH(ws + 87648);
+      CHEM_PREFETCH(ws + 87680);
+      CHEM_PREFETCH(ws + 87712);
+      CHEM_PREFETCH(ws + 87744);
+      CHEM_PREFETCH(ws + 87776);
+      CHEM_PREFETCH(ws + 87808);
+      CHEM_PREFETCH(ws + 87840);
+      CHEM_PREFETCH(ws + 87872);
+      CHEM_PREFETCH(ws + 87904);
+      CHEM_PREFETCH(ws + 87936);
+      CHEM_PREFETCH(ws + 87968);
       double x = b[4224];
       x = fma(-CHEM_LDLU(lu + 8832), b[320], x);
       x = fma(-CHEM_LDLU(lu + 8864), b[928], x);
@@ -1153,27 +1153,27 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[4224] = x;
     }
     {
-      CHEM_PREFETCH(ws + 83232);
-      CHEM_PREFETCH(ws + 83264);
-      CHEM_PREFETCH(ws + 83296);
-      CHEM_PREFETCH(ws + 83328);
-      CHEM_PREFETCH(ws + 83360);
-      CHEM_PREFETCH(ws + 83392);
-      CHEM_PREFETCH(ws + 83424);
-      CHEM_PREFETCH(ws + 83456);
-      CHEM_PREFETCH(ws + 83488);
-      CHEM_PREFETCH(ws + 83520);
-      CHEM_PREFETCH(ws + 83552);
-      CHEM_PREFETCH(ws + 83584);
-      CHEM_PREFETCH(ws + 83616);
-      CHEM_PREFETCH(ws + 83648);
-      CHEM_PREFETCH(ws + 83680);
-      CHEM_PREFETCH(ws + 83712);
-      CHEM_PREFETCH(ws + 83744);
-      CHEM_PREFETCH(ws + 83776);
-      CHEM_PREFETCH(ws + 83808);
-      CHEM_PREFETCH(ws + 83840);
-      CHEM_PREFETCH(ws + 83872);
+      CHEM_PREFETCH(ws + 88000);
+      CHEM_PREFETCH(ws + 88032);
+      CHEM_PREFETCH(ws + 88064);
+      CHEM_PREFETCH(ws + 88096);
+      CHEM_PREFETCH(ws + 88128);
+      CHEM_PREFETCH(ws + 88160);
+      CHEM_PREFETCH(ws + 88192);
+      CHEM_PREFETCH(ws + 88224);
+      CHEM_PREFETCH(ws + 88256);
+      CHEM_PREFETCH(ws + 88288);
+      CHEM_PREFETCH(ws + 88320);
+      CHEM_PREFETCH(ws + 88352);
+      CHEM_PREFETCH(ws + 88384);
+      CHEM_PREFETCH(ws + 88416);
+      CHEM_PREFETCH(ws + 88448);
+      CHEM_PREFETCH(ws + 88480);
+      CHEM_PREFETCH(ws + 88512);
+      CHEM_PREFETCH(ws + 88544);
+      CHEM_PREFETCH(ws + 88576);
+      CHEM_PREFETCH(ws + 88608);
+      CHEM_PREFETCH(ws + 88640);
       double x = b[4256];
       x = fma(-CHEM_LDLU(lu + 9280), b[352], x);
       x = fma(-CHEM_LDLU(lu + 9312), b[1792], x);
@@ -1195,26 +1195,26 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[4256] = x;
     }
     {
-      CHEM_PREFETCH(ws + 83904);
-      CHEM_PREFETCH(ws + 83936);
-      CHEM_PREFETCH(ws + 83968);
-      CHEM_PREFETCH(ws + 84000);
-      CHEM_PREFETCH(ws + 84032);
-      CHEM_PREFETCH(ws + 84064);
-      CHEM_PREFETCH(ws + 84096);
-      CHEM_PREFETCH(ws + 84128);
-      CHEM_PREFETCH(ws + 84160);
-      CHEM_PREFETCH(ws + 84192);
-      CHEM_PREFETCH(ws + 84224);
-      CHEM_PREFETCH(ws + 84256);
-      CHEM_PREFETCH(ws + 84288);
-      CHEM_PREFETCH(ws + 84320);
-      CHEM_PREFETCH(ws + 84352);
-      CHEM_PREFETCH(ws + 84384);
-      CHEM_PREFETCH(ws + 84416);
-      CHEM_PREFETCH(ws + 84448);
-      CHEM_PREFETCH(ws + 84480);
-      CHEM_PREFETCH(ws + 84512);
+      CHEM_PREFETCH(ws + 88672);
+      CHEM_PREFETCH(ws + 88704);
+      CHEM_PREFETCH(ws + 88736);
+      CHEM_PREFETCH(ws + 88768);
+      CHEM_PREFETCH(ws + 88800);
+      CHEM_PREFETCH(ws + 88832);
+      CHEM_PREFETCH(ws + 88864);
+      CHEM_PREFETCH(ws + 88896);
+      CHEM_PREFETCH(ws + 88928);
+      CHEM_PREFETCH(ws + 88960);
+      CHEM_PREFETCH(ws + 88992);
+      CHEM_PREFETCH(ws + 89024);
+      CHEM_PREFETCH(ws + 89056);
+      CHEM_PREFETCH(ws + 89088);
+      CHEM_PREFETCH(ws + 89120);
+      CHEM_PREFETCH(ws + 89152);
+      CHEM_PREFETCH(ws + 89184);
+      CHEM_PREFETCH(ws + 89216);
+      CHEM_PREFETCH(ws + 89248);
+      CHEM_PREFETCH(ws + 89280);
       double x = b[4288];
       x = fma(-CHEM_LDLU(lu + 9824), b[832], x);
       x = fma(-CHEM_LDLU(lu + 9856), b[896], x);
@@ -1236,30 +1236,30 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[4288] = x;
     }
     {
-      CHEM_PREFETCH(ws + 84544);
-      CHEM_PREFETCH(ws + 84576);
-      CHEM_PREFETCH(ws + 84608);
-      CHEM_PREFETCH(ws + 84640);
-      CHEM_PREFETCH(ws + 84672);
-      CHEM_PREFETCH(ws + 84704);
-      CHEM_PREFETCH(ws + 84736);
-      CHEM_PREFETCH(ws + 84768);
-      CHEM_PREFETCH(ws + 84800);
-      CHEM_PREFETCH(ws + 84832);
-      CHEM_PREFETCH(ws + 84864);
-      CHEM_PREFETCH(ws + 84896);
-      CHEM_PREFETCH(ws + 84928);
-      CHEM_PREFETCH(ws + 84960);
-      CHEM_PREFETCH(ws + 84992);
-      CHEM_PREFETCH(ws + 85024);
-      CHEM_PREFETCH(ws + 85056);
-      CHEM_PREFETCH(ws + 85088);
-      CHEM_PREFETCH(ws + 85120);
-      CHEM_PREFETCH(ws + 85152);
-      CHEM_PREFETCH(ws + 85184);
-      CHEM_PREFETCH(ws + 85216);
-      CHEM_PREFETCH(ws + 85248);
-      CHEM_PREFETCH(ws + 85280);
+      CHEM_PREFETCH(ws + 89312);
+      CHEM_PREFETCH(ws + 89344);
+      CHEM_PREFETCH(ws + 89376);
+      CHEM_PREFETCH(ws + 89408);
+      CHEM_PREFETCH(ws + 89440);
+      CHEM_PREFETCH(ws + 89472);
+      CHEM_PREFETCH(ws + 89504);
+      CHEM_PREFETCH(ws + 89536);
+      CHEM_PREFETCH(ws + 89568);
+      CHEM_PREFETCH(ws + 89600);
+      CHEM_PREFETCH(ws + 89632);
+      CHEM_PREFETCH(ws + 89664);
+      CHEM_PREFETCH(ws + 89696);
+      CHEM_PREFETCH(ws + 89728);
+      CHEM_PREFETCH(ws + 89760);
+      CHEM_PREFETCH(ws + 89792);
+      CHEM_PREFETCH(ws + 89824);
+      CHEM_PREFETCH(ws + 89856);
+      CHEM_PREFETCH(ws + 89888);
+      CHEM_PREFETCH(ws + 89920);
+      CHEM_PREFETCH(ws + 89952);
+      CHEM_PREFETCH(ws + 89984);
+      CHEM_PREFETCH(ws + 90016);
+      CHEM_PREFETCH(ws + 90048);
       double x = b[4320];
       x = fma(-CHEM_LDLU(lu + 10368), b[1856], x);
       x = fma(-CHEM_LDLU(lu + 10400), b[2048], x);
@@ -1285,32 +1285,32 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[4320] = x;
     }
     {
-      CHEM_PREFETCH(ws + 85312);
-      CHEM_PREFETCH(ws + 85344);
-      CHEM_PREFETCH(ws + 85376);
-      CHEM_PREFETCH(ws + 85408);
-      CHEM_PREFETCH(ws + 85440);
-      CHEM_PREFETCH(ws + 85472);
-      CHEM_PREFETCH(ws + 85504);
-      CHEM_PREFETCH(ws + 85536);
-      CHEM_PREFETCH(ws + 85568);
-      CHEM_PREFETCH(ws + 85600);
-      CHEM_PREFETCH(ws + 85632);
-      CHEM_PREFETCH(ws + 85664);
-      CHEM_PREFETCH(ws + 85696);
-      CHEM_PREFETCH(ws + 85728);
-      CHEM_PREFETCH(ws + 85760);
-      CHEM_PREFETCH(ws + 85792);
-      CHEM_PREFETCH(ws + 85824);
-      CHEM_PREFETCH(ws + 85856);
-      CHEM_PREFETCH(ws + 85888);
-      CHEM_PREFETCH(ws + 85920);
-      CHEM_PREFETCH(ws + 85952);
-      CHEM_PREFETCH(ws + 85984);
-      CHEM_PREFETCH(ws + 86016);
-      CHEM_PREFETCH(ws + 86048);
-      CHEM_PREFETCH(ws + 86080);
-      CHEM_PREFETCH(ws + 86112);
+      CHEM_PREFETCH(ws + 90080);
+      CHEM_PREFETCH(ws + 90112);
+      CHEM_PREFETCH(ws + 90144);
+      CHEM_PREFETCH(ws + 90176);
+      CHEM_PREFETCH(ws + 90208);
+      CHEM_PREFETCH(ws + 90240);
+      CHEM_PREFETCH(ws + 90272);
+      CHEM_PREFETCH(ws + 90304);
+      CHEM_PREFETCH(ws + 90336);
+      CHEM_PREFETCH(ws + 90368);
+      CHEM_PREFETCH(ws + 90400);
+      CHEM_PREFETCH(ws + 90432);
+      CHEM_PREFETCH(ws + 90464);
+      CHEM_PREFETCH(ws + 90496);
+      CHEM_PREFETCH(ws + 90528);
+      CHEM_PREFETCH(ws + 90560);
+      CHEM_PREFETCH(ws + 90592);
+      CHEM_PREFETCH(ws + 90624);
+      CHEM_PREFETCH(ws + 90656);
+      CHEM_PREFETCH(ws + 90688);
+      CHEM_PREFETCH(ws + 90720);
+      CHEM_PREFETCH(ws + 90752);
+      CHEM_PREFETCH(ws + 90784);
+      CHEM_PREFETCH(ws + 90816);
+      CHEM_PREFETCH(ws + 90848);
+      CHEM_PREFETCH(ws + 90880);
       double x = b[4352];
       x = fma(-CHEM_LDLU(lu + 11040), b[1632], x);
       x = fma(-CHEM_LDLU(lu + 11072), b[1984], x);
@@ -1335,32 +1335,32 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[4352] = x;
     }
     {
-      CHEM_PREFETCH(ws + 86144);
-      CHEM_PREFETCH(ws + 86176);
-      CHEM_PREFETCH(ws + 86208);
-      CHEM_PREFETCH(ws + 86240);
-      CHEM_PREFETCH(ws + 86272);
-      CHEM_PREFETCH(ws + 86304);
-      CHEM_PREFETCH(ws + 86336);
-      CHEM_PREFETCH(ws + 86368);
-      CHEM_PREFETCH(ws + 86400);
-      CHEM_PREFETCH(ws + 86432);
-      CHEM_PREFETCH(ws + 86464);
-      CHEM_PREFETCH(ws + 86496);
-      CHEM_PREFETCH(ws + 86528);
-      CHEM_PREFETCH(ws + 86560);
-      CHEM_PREFETCH(ws + 86592);
-      CHEM_PREFETCH(ws + 86624);
-      CHEM_PREFETCH(ws + 86656);
-      CHEM_PREFETCH(ws + 86688);
-      CHEM_PREFETCH(ws + 86720);
-      CHEM_PREFETCH(ws + 86752);
-      CHEM_PREFETCH(ws + 86784);
-      CHEM_PREFETCH(ws + 86816);
-      CHEM_PREFETCH(ws + 86848);
-      CHEM_PREFETCH(ws + 86880);
-      CHEM_PREFETCH(ws + 86912);
-      CHEM_PREFETCH(ws + 86944);
+      CHEM_PREFETCH(ws + 90912);
+      CHEM_PREFETCH(ws + 90944);
+      CHEM_PREFETCH(ws + 90976);
+      CHEM_PREFETCH(ws + 91008);
+      CHEM_PREFETCH(ws + 91040);
+      CHEM_PREFETCH(ws + 91072);
+      CHEM_PREFETCH(ws + 91104);
+      CHEM_PREFETCH(ws + 91136);
+      CHEM_PREFETCH(ws + 91168);
+      CHEM_PREFETCH(ws + 91200);
+      CHEM_PREFETCH(ws + 91232);
+      CHEM_PREFETCH(ws + 91264);
+      CHEM_PREFETCH(ws + 91296);
+      CHEM_PREFETCH(ws + 91328);
+      CHEM_PREFETCH(ws + 91360);
+      CHEM_PREFETCH(ws + 91392);
+      CHEM_PREFETCH(ws + 91424);
+      CHEM_PREFETCH(ws + 91456);
+      CHEM_PREFETCH(ws + 91488);
+      CHEM_PREFETCH(ws + 91520);
+      CHEM_PREFETCH(ws + 91552);
+      CHEM_PREFETCH(ws + 91584);
+      CHEM_PREFETCH(ws + 91616);
+      CHEM_PREFETCH(ws + 91648);
+      CHEM_PREFETCH(ws + 91680);
+      CHEM_PREFETCH(ws + 91712);
       double x = b[4384];
       x = fma(-CHEM_LDLU(lu + 11680), b[1728], x);
       x = fma(-CHEM_LDLU(lu + 11712), b[2144], x);
@@ -1389,33 +1389,33 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[4384] = x;
     }
     {
-      CHEM_PREFETCH(ws + 86976);
-      CHEM_PREFETCH(ws + 87008);
-      CHEM_PREFETCH(ws + 87040);
-      CHEM_PREFETCH(ws + 87072);
-      CHEM_PREFETCH(ws + 87104);
-      CHEM_PREFETCH(ws + 87136);
-      CHEM_PREFETCH(ws + 87168);
-      CHEM_PREFETCH(ws + 87200);
-      CHEM_PREFETCH(ws + 87232);
-      CHEM_PREFETCH(ws + 87264);
-      CHEM_PREFETCH(ws + 87296);
-      CHEM_PREFETCH(ws + 87328);
-      CHEM_PREFETCH(ws + 87360);
-      CHEM_PREFETCH(ws + 87392);
-      CHEM_PREFETCH(ws + 87424);
-      CHEM_PREFETCH(ws + 87456);
-      CHEM_PREFETCH(ws + 87488);
-      CHEM_PREFETCH(ws + 87520);
-      CHEM_PREFETCH(ws + 87552);
-      CHEM_PREFETCH(ws + 87584);
-      CHEM_PREFETCH(ws + 87616);
-      CHEM_PREFETCH(ws + 87648);
-      CHEM_PREFETCH(ws + 87680);
-      CHEM_PREFETCH(ws + 87712);
-      CHEM_PREFETCH(ws + 87744);
-      CHEM_PREFETCH(ws + 87776);
-      CHEM_PREFETCH(ws + 87808);
+      CHEM_PREFETCH(ws + 91744);
+      CHEM_PREFETCH(ws + 91776);
+      CHEM_PREFETCH(ws + 91808);
+      CHEM_PREFETCH(ws + 91840);
+      CHEM_PREFETCH(ws + 91872);
+      CHEM_PREFETCH(ws + 91904);
+      CHEM_PREFETCH(ws + 91936);
+      CHEM_PREFETCH(ws + 91968);
+      CHEM_PREFETCH(ws + 92000);
+      CHEM_PREFETCH(ws + 92032);
+      CHEM_PREFETCH(ws + 92064);
+      CHEM_PREFETCH(ws + 92096);
+      CHEM_PREFETCH(ws + 92128);
+      CHEM_PREFETCH(ws + 92160);
+      CHEM_PREFETCH(ws + 92192);
+      CHEM_PREFETCH(ws + 92224);
+      CHEM_PREFETCH(ws + 92256);
+      CHEM_PREFETCH(ws + 92288);
+      CHEM_PREFETCH(ws + 92320);
+      CHEM_PREFETCH(ws + 92352);
+      CHEM_PREFETCH(ws + 92384);
+      CHEM_PREFETCH(ws + 92416);
+      CHEM_PREFETCH(ws + 92448);
+      CHEM_PREFETCH(ws + 92480);
+      CHEM_PREFETCH(ws + 92512);
+      CHEM_PREFETCH(ws + 92544);
+      CHEM_PREFETCH(ws + 92576);
       double x = b[4416];
       x = fma(-CHEM_LDLU(lu + 12448), b[320], x);
       x = fma(-CHEM_LDLU(lu + 12480), b[416], x);
@@ -1446,35 +1446,35 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[4416] = x;
     }
     {
-      CHEM_PREFETCH(ws + 87840);
-      CHEM_PREFETCH(ws + 87872);
-      CHEM_PREFETCH(ws + 87904);
-      CHEM_PREFETCH(ws + 87936);
-      CHEM_PREFETCH(ws + 87968);
-      CHEM_PREFETCH(ws + 88000);
-      CHEM_PREFETCH(ws + 88032);
-      CHEM_PREFETCH(ws + 88064);
-      CHEM_PREFETCH(ws + 88096);
-      CHEM_PREFETCH(ws + 88128);
-      CHEM_PREFETCH(ws + 88160);
-      CHEM_PREFETCH(ws + 88192);
-      CHEM_PREFETCH(ws + 88224);
-      CHEM_PREFETCH(ws + 88256);
-      CHEM_PREFETCH(ws + 88288);
-      CHEM_PREFETCH(ws + 88320);
-      CHEM_PREFETCH(ws + 88352);
-      CHEM_PREFETCH(ws + 88384);
-      CHEM_PREFETCH(ws + 88416);
-      CHEM_PREFETCH(ws + 88448);
-      CHEM_PREFETCH(ws + 88480);
-      CHEM_PREFETCH(ws + 88512);
-      CHEM_PREFETCH(ws + 88544);
-      CHEM_PREFETCH(ws + 88576);
-      CHEM_PREFETCH(ws + 88608);
-      CHEM_PREFETCH(ws + 88640);
-      CHEM_PREFETCH(ws + 88672);
-      CHEM_PREFETCH(ws + 88704);
-      CHEM_PREFETCH(ws + 88736);
+      CHEM_PREFETCH(ws + 92608);
+      CHEM_PREFETCH(ws + 92640);
+      CHEM_PREFETCH(ws + 92672);
+      CHEM_PREFETCH(ws + 92704);
+      CHEM_PREFETCH(ws + 92736);
+      CHEM_PREFETCH(ws + 92768);
+      CHEM_PREFETCH(ws + 92800);
+      CHEM_PREFETCH(ws + 92832);
+      CHEM_PREFETCH(ws + 92864);
+      CHEM_PREFETCH(ws + 92896);
+      CHEM_PREFETCH(ws + 92928);
+      CHEM_PREFETCH(ws + 92960);
+      CHEM_PREFETCH(ws + 92992);
+      CHEM_PREFETCH(ws + 93024);
+      CHEM_PREFETCH(ws + 93056);
+      CHEM_PREFETCH(ws + 93088);
+      CHEM_PREFETCH(ws + 93120);
+      CHEM_PREFETCH(ws + 93152);
+      CHEM_PREFETCH(ws + 93184);
+      CHEM_PREFETCH(ws + 93216);
+      CHEM_PREFETCH(ws + 93248);
+      CHEM_PREFETCH(ws + 93280);
+      CHEM_PREFETCH(ws + 93312);
+      CHEM_PREFETCH(ws + 93344);
+      CHEM_PREFETCH(ws + 93376);
+      CHEM_PREFETCH(ws + 93408);
+      CHEM_PREFETCH(ws + 93440);
+      CHEM_PREFETCH(ws + 93472);
+      CHEM_PREFETCH(ws + 93504);
       double x = b[4448];
       x = fma(-CHEM_LDLU(lu + 13280), b[320], x);
       x = fma(-CHEM_LDLU(lu + 13312), b[960], x);
@@ -1505,46 +1505,46 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[4448] = x;
     }
     {
-      CHEM_PREFETCH(ws + 88768);
-      CHEM_PREFETCH(ws + 88800);
-      CHEM_PREFETCH(ws + 88832);
-      CHEM_PREFETCH(ws + 88864);
-      CHEM_PREFETCH(ws + 88896);
-      CHEM_PREFETCH(ws + 88928);
-      CHEM_PREFETCH(ws + 88960);
-      CHEM_PREFETCH(ws + 88992);
-      CHEM_PREFETCH(ws + 89024);
-      CHEM_PREFETCH(ws + 89056);
-      CHEM_PREFETCH(ws + 89088);
-      CHEM_PREFETCH(ws + 89120);
-      CHEM_PREFETCH(ws + 89152);
-      CHEM_PREFETCH(ws + 89184);
-      CHEM_PREFETCH(ws + 89216);
-      CHEM_PREFETCH(ws + 89248);
-      CHEM_PREFETCH(ws + 89280);
-      CHEM_PREFETCH(ws + 89312);
-      CHEM_PREFETCH(ws + 89344);
-      CHEM_PREFETCH(ws + 89376);
-      CHEM_PREFETCH(ws + 89408);
-      CHEM_PREFETCH(ws + 89440);
-      CHEM_PREFETCH(ws + 89472);
-      CHEM_PREFETCH(ws + 89504);
-      CHEM_PREFETCH(ws + 89536);
-      CHEM_PREFETCH(ws + 89568);
-      CHEM_PREFETCH(ws + 89600);
-      CHEM_PREFETCH(ws + 89632);
-      CHEM_PREFETCH(ws + 89664);
-      CHEM_PREFETCH(ws + 89696);
-      CHEM_PREFETCH(ws + 89728);
-      CHEM_PREFETCH(ws + 89760);
-      CHEM_PREFETCH(ws + 89792);
-      CHEM_PREFETCH(ws + 89824);
-      CHEM_PREFETCH(ws + 89856);
-      CHEM_PREFETCH(ws + 89888);
-      CHEM_PREFETCH(ws + 89920);
-      CHEM_PREFETCH(ws + 89952);
-      CHEM_PREFETCH(ws + 89984);
-      CHEM_PREFETCH(ws + 90016);
+      CHEM_PREFETCH(ws + 93536);
+      CHEM_PREFETCH(ws + 93568);
+      CHEM_PREFETCH(ws + 93600);
+      CHEM_PREFETCH(ws + 93632);
+      CHEM_PREFETCH(ws + 93664);
+      CHEM_PREFETCH(ws + 93696);
+      CHEM_PREFETCH(ws + 93728);
+      CHEM_PREFETCH(ws + 93760);
+      CHEM_PREFETCH(ws + 93792);
+      CHEM_PREFETCH(ws + 93824);
+      CHEM_PREFETCH(ws + 93856);
+      CHEM_PREFETCH(ws + 93888);
+      CHEM_PREFETCH(ws + 93920);
+      CHEM_PREFETCH(ws + 93952);
+      CHEM_PREFETCH(ws + 93984);
+      CHEM_PREFETCH(ws + 94016);
+      CHEM_PREFETCH(ws + 94048);
+      CHEM_PREFETCH(ws + 94080);
+      CHEM_PREFETCH(ws + 94112);
+      CHEM_PREFETCH(ws + 94144);
+      CHEM_PREFETCH(ws + 94176);
+      CHEM_PREFETCH(ws + 94208);
+      CHEM_PREFETCH(ws + 94240);
+      CHEM_PREFETCH(ws + 94272);
+      CHEM_PREFETCH(ws + 94304);
+      CHEM_PREFETCH(ws + 94336);
+      CHEM_PREFETCH(ws + 94368);
+      CHEM_PREFETCH(ws + 94400);
+      CHEM_PREFETCH(ws + 94432);
+      CHEM_PREFETCH(ws + 94464);
+      CHEM_PREFETCH(ws + 94496);
+      CHEM_PREFETCH(ws + 94528);
+      CHEM_PREFETCH(ws + 94560);
+      CHEM_PREFETCH(ws + 94592);
+      CHEM_PREFETCH(ws + 94624);
+      CHEM_PREFETCH(ws + 94656);
+      CHEM_PREFETCH(ws + 94688);
+      CHEM_PREFETCH(ws + 94720);
+      CHEM_PREFETCH(ws + 94752);
+      CHEM_PREFETCH(ws + 94784);
       double x = b[4480];
       x = fma(-CHEM_LDLU(lu + 14112), b[352], x);
       x = fma(-CHEM_LDLU(lu + 14144), b[1792], x);
@@ -1576,44 +1576,44 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[4480] = x;
     }
     {
-      CHEM_PREFETCH(ws + 90048);
-      CHEM_PREFETCH(ws + 90080);
-      CHEM_PREFETCH(ws + 90112);
-      CHEM_PREFETCH(ws + 90144);
-      CHEM_PREFETCH(ws + 90176);
-      CHEM_PREFETCH(ws + 90208);
-      CHEM_PREFETCH(ws + 90240);
-      CHEM_PREFETCH(ws + 90272);
-      CHEM_PREFETCH(ws + 90304);
-      CHEM_PREFETCH(ws + 90336);
-      CHEM_PREFETCH(ws + 90368);
-      CHEM_PREFETCH(ws + 90400);
-      CHEM_PREFETCH(ws + 90432);
-      CHEM_PREFETCH(ws + 90464);
-      CHEM_PREFETCH(ws + 90496);
-      CHEM_PREFETCH(ws + 90528);
-      CHEM_PREFETCH(ws + 90560);
-      CHEM_PREFETCH(ws + 90592);
-      CHEM_PREFETCH(ws + 90624);
-      CHEM_PREFETCH(ws + 90656);
-      CHEM_PREFETCH(ws + 90688);
-      CHEM_PREFETCH(ws + 90720);
-      CHEM_PREFETCH(ws + 90752);
-      CHEM_PREFETCH(ws + 90784);
-      CHEM_PREFETCH(ws + 90816);
-      CHEM_PREFETCH(ws + 90848);
-      CHEM_PREFETCH(ws + 90880);
-      CHEM_PREFETCH(ws + 90912);
-      CHEM_PREFETCH(ws + 90944);
-      CHEM_PREFETCH(ws + 90976);
-      CHEM_PREFETCH(ws + 91008);
-      CHEM_PREFETCH(ws + 91040);
-      CHEM_PREFETCH(ws + 91072);
-      CHEM_PREFETCH(ws + 91104);
-      CHEM_PREFETCH(ws + 91136);
-      CHEM_PREFETCH(ws + 91168);
-      CHEM_PREFETCH(ws + 91200);
-      CHEM_PREFETCH(ws + 91232);
+      CHEM_PREFETCH(ws + 94816);
+      CHEM_PREFETCH(ws + 94848);
+      CHEM_PREFETCH(ws + 94880);
+      CHEM_PREFETCH(ws + 94912);
+      CHEM_PREFETCH(ws + 94944);
+      CHEM_PREFETCH(ws + 94976);
+      CHEM_PREFETCH(ws + 95008);
+      CHEM_PREFETCH(ws + 95040);
+      CHEM_PREFETCH(ws + 95072);
+      CHEM_PREFETCH(ws + 95104);
+      CHEM_PREFETCH(ws + 95136);
+      CHEM_PREFETCH(ws + 95168);
+      CHEM_PREFETCH(ws + 95200);
+      CHEM_PREFETCH(ws + 95232);
+      CHEM_PREFETCH(ws + 95264);
+      CHEM_PREFETCH(ws + 95296);
+      CHEM_PREFETCH(ws + 95328);
+      CHEM_PREFETCH(ws + 95360);
+      CHEM_PREFETCH(ws + 95392);
+      CHEM_PREFETCH(ws + 95424);
+      CHEM_PREFETCH(ws + 95456);
+      CHEM_PREFETCH(ws + 95488);
+      CHEM_PREFETCH(ws + 95520);
+      CHEM_PREFETCH(ws + 95552);
+      CHEM_PREFETCH(ws + 95584);
+      CHEM_PREFETCH(ws + 95616);
+      CHEM_PREFETCH(ws + 95648);
+      CHEM_PREFETCH(ws + 95680);
+      CHEM_PREFETCH(ws + 95712);
+      CHEM_PREFETCH(ws + 95744);
+      CHEM_PREFETCH(ws + 95776);
+      CHEM_PREFETCH(ws + 95808);
+      CHEM_PREFETCH(ws + 95840);
+      CHEM_PREFETCH(ws + 95872);
+      CHEM_PREFETCH(ws + 95904);
+      CHEM_PREFETCH(ws + 95936);
+      CHEM_PREFETCH(ws + 95968);
+      CHEM_PREFETCH(ws + 96000);
       double x = b[4512];
       x = fma(-CHEM_LDLU(lu + 14976), b[864], x);
       x = fma(-CHEM_LDLU(lu + 15008), b[1632], x);
@@ -1647,51 +1647,51 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[4512] = x;
     }
     {
-      CHEM_PREFETCH(ws + 91264);
-      CHEM_PREFETCH(ws + 91296);
-      CHEM_PREFETCH(ws + 91328);
-      CHEM_PREFETCH(ws + 91360);
-      CHEM_PREFETCH(ws + 91392);
-      CHEM_PREFETCH(ws + 91424);
-      CHEM_PREFETCH(ws + 91456);
-      CHEM_PREFETCH(ws + 91488);
-      CHEM_PREFETCH(ws + 91520);
-      CHEM_PREFETCH(ws + 91552);
-      CHEM_PREFETCH(ws + 91584);
-      CHEM_PREFETCH(ws + 91616);
-      CHEM_PREFETCH(ws + 91648);
-      CHEM_PREFETCH(ws + 91680);
-      CHEM_PREFETCH(ws + 91712);
-      CHEM_PREFETCH(ws + 91744);
-      CHEM_PREFETCH(ws + 91776);
-      CHEM_PREFETCH(ws + 91808);
-      CHEM_PREFETCH(ws + 91840);
-      CHEM_PREFETCH(ws + 91872);
-      CHEM_PREFETCH(ws + 91904);
-      CHEM_PREFETCH(ws + 91936);
-      CHEM_PREFETCH(ws + 91968);
-      CHEM_PREFETCH(ws + 92000);
-      CHEM_PREFETCH(ws + 92032);
-      CHEM_PREFETCH(ws + 92064);
-      CHEM_PREFETCH(ws + 92096);
-      CHEM_PREFETCH(ws + 92128);
-      CHEM_PREFETCH(ws + 92160);
-      CHEM_PREFETCH(ws + 92192);
-      CHEM_PREFETCH(ws + 92224);
-      CHEM_PREFETCH(ws + 92256);
-      CHEM_PREFETCH(ws + 92288);
-      CHEM_PREFETCH(ws + 92320);
-      CHEM_PREFETCH(ws + 92352);
-      CHEM_PREFETCH(ws + 92384);
-      CHEM_PREFETCH(ws + 92416);
-      CHEM_PREFETCH(ws + 92448);
-      CHEM_PREFETCH(ws + 92480);
-      CHEM_PREFETCH(ws + 92512);
-      CHEM_PREFETCH(ws + 92544);
-      CHEM_PREFETCH(ws + 92576);
-      CHEM_PREFETCH(ws + 92608);
-      CHEM_PREFETCH(ws + 92640);
-      CHEM_PREFETCH(ws + 92672);
+      CHEM_PREFETCH(ws + 96032);
+      CHEM_PREFETCH(ws + 96064);
+      CHEM_PREFETCH(ws + 96096);
+      CHEM_PREFETCH(ws + 96128);
+      CHEM_PREFETCH(ws + 96160);
+      CHEM_PREFETCH(ws + 96192);
+      CHEM_PREFETCH(ws + 96224);
+      CHEM_PREFETCH(ws + 96256);
+      CHEM_PREFETCH(ws + 96288);
+      CHEM_PREFETCH(ws + 96320);
+      CHEM_PREFETCH(ws + 96352);
+      CHEM_PREFETCH(ws + 96384);
+      CHEM_PREFETCH(ws + 96416);
+      CHEM_PREFETCH(ws + 96448);
+      CHEM_PREFETCH(ws + 96480);
+      CHEM_PREFETCH(ws + 96512);
+      CHEM_PREFETCH(ws + 96544);
+      CHEM_PREFETCH(ws + 96576);
+      CHEM_PREFETCH(ws + 96608);
+      CHEM_PREFETCH(ws + 96640);
+      CHEM_PREFETCH(ws + 96672);
+      CHEM_PREFETCH(ws + 96704);
+      CHEM_PREFETCH(ws + 96736);
+      CHEM_PREFETCH(ws + 96768);
+      CHEM_PREFETCH(ws + 96800);
+      CHEM_PREFETCH(ws + 96832);
+      CHEM_PREFETCH(ws + 96864);
+      CHEM_PREFETCH(ws + 96896);
+      CHEM_PREFETCH(ws + 96928);
+      CHEM_PREFETCH(ws + 96960);
+      CHEM_PREFETCH(ws + 96992);
+      CHEM_PREFETCH(ws + 97024);
+      CHEM_PREFETCH(ws + 97056);
+      CHEM_PREFETCH(ws + 97088);
+      CHEM_PREFETCH(ws + 97120);
+      CHEM_PREFETCH(ws + 97152);
+      CHEM_PREFETCH(ws + 97184);
+      CHEM_PREFETCH(ws + 97216);
+      CHEM_PREFETCH(ws + 97248);
+      CHEM_PREFETCH(ws + 97280);
+      CHEM_PREFETCH(ws + 97312);
+      CHEM_PREFETCH(ws + 97344);
+      CHEM_PREFETCH(ws + 97376);
+      CHEM_PREFETCH(ws + 97408);
+      CHEM_PREFETCH(ws + 97440);
       double x = b[4544];
       x = fma(-CHEM_LDLU(lu + 15904), b[832], x);
       x = fma(-CHEM_LDLU(lu + 15936), b[864], x);
@@ -1736,55 +1736,55 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[4544] = x;
     }
     {
-      CHEM_PREFETCH(ws + 92704);
-      CHEM_PREFETCH(ws + 92736);
-      CHEM_PREFETCH(ws + 92768);
-      CHEM_PREFETCH(ws + 92800);
-      CHEM_PREFETCH(ws + 92832);
-      CHEM_PREFETCH(ws + 92864);
-      CHEM_PREFETCH(ws + 92896);
-      CHEM_PREFETCH(ws + 92928);
-      CHEM_PREFETCH(ws + 92960);
-      CHEM_PREFETCH(ws + 92992);
-      CHEM_PREFETCH(ws + 93024);
-      CHEM_PREFETCH(ws + 93056);
-      CHEM_PREFETCH(ws + 93088);
-      CHEM_PREFETCH(ws + 93120);
-      CHEM_PREFETCH(ws + 93152);
-      CHEM_PREFETCH(ws + 93184);
-      CHEM_PREFETCH(ws + 93216);
-      CHEM_PREFETCH(ws + 93248);
-      CHEM_PREFETCH(ws + 93280);
-      CHEM_PREFETCH(ws + 93312);
-      CHEM_PREFETCH(ws + 93344);
-      CHEM_PREFETCH(ws + 93376);
-      CHEM_PREFETCH(ws + 93408);
-      CHEM_PREFETCH(ws + 93440);
-      CHEM_PREFETCH(ws + 93472);
-      CHEM_PREFETCH(ws + 93504);
-      CHEM_PREFETCH(ws + 93536);
-      CHEM_PREFETCH(ws + 93568);
-      CHEM_PREFETCH(ws + 93600);
-      CHEM_PREFETCH(ws + 93632);
-      CHEM_PREFETCH(ws + 93664);
-      CHEM_PREFETCH(ws + 93696);
-      CHEM_PREFETCH(ws + 93728);
-      CHEM_PREFETCH(ws + 93760);
-      CHEM_PREFETCH(ws + 93792);
-      CHEM_PREFETCH(ws + 93824);
-      CHEM_PREFETCH(ws + 93856);
-      CHEM_PREFETCH(ws + 93888);
-      CHEM_PREFETCH(ws + 93920);
-      CHEM_PREFETCH(ws + 93952);
-      CHEM_PREFETCH(ws + 93984);
-      CHEM_PREFETCH(ws + 94016);
-      CHEM_PREFETCH(ws + 94048);
-      CHEM_PREFETCH(ws + 94080);
-      CHEM_PREFETCH(ws + 94112);
-      CHEM_PREFETCH(ws + 94144);
-      CHEM_PREFETCH(ws + 94176);
-      CHEM_PREFETCH(ws + 94208);
-      CHEM_PREFETCH(ws + 94240);
+      CHEM_PREFETCH(ws + 97472);
+      CHEM_PREFETCH(ws + 97504);
+      CHEM_PREFETCH(ws + 97536);
+      CHEM_PREFETCH(ws + 97568);
+      CHEM_PREFETCH(ws + 97600);
+      CHEM_PREFETCH(ws + 97632);
+      CHEM_PREFETCH(ws + 97664);
+      CHEM_PREFETCH(ws + 97696);
+      CHEM_PREFETCH(ws + 97728);
+      CHEM_PREFETCH(ws + 97760);
+      CHEM_PREFETCH(ws + 97792);
+      CHEM_PREFETCH(ws + 97824);
+      CHEM_PREFETCH(ws + 97856);
+      CHEM_PREFETCH(ws + 97888);
+      CHEM_PREFETCH(ws + 97920);
+      CHEM_PREFETCH(ws + 97952);
+      CHEM_PREFETCH(ws + 97984);
+      CHEM_PREFETCH(ws + 98016);
+      CHEM_PREFETCH(ws + 98048);
+      CHEM_PREFETCH(ws + 98080);
+      CHEM_PREFETCH(ws + 98112);
+      CHEM_PREFETCH(ws + 98144);
+      CHEM_PREFETCH(ws + 98176);
+      CHEM_PREFETCH(ws + 98208);
+      CHEM_PREFETCH(ws + 98240);
+      CHEM_PREFETCH(ws + 98272);
+      CHEM_PREFETCH(ws + 98304);
+      CHEM_PREFETCH(ws + 98336);
+      CHEM_PREFETCH(ws + 98368);
+      CHEM_PREFETCH(ws + 98400);
+      CHEM_PREFETCH(ws + 98432);
+      CHEM_PREFETCH(ws + 98464);
+      CHEM_PREFETCH(ws + 98496);
+      CHEM_PREFETCH(ws + 98528);
+      CHEM_PREFETCH(ws + 98560);
+      CHEM_PREFETCH(ws + 98592);
+      CHEM_PREFETCH(ws + 98624);
+      CHEM_PREFETCH(ws + 98656);
+      CHEM_PREFETCH(ws + 98688);
+      CHEM_PREFETCH(ws + 98720);
+      CHEM_PREFETCH(ws + 98752);
+      CHEM_PREFETCH(ws + 98784);
+      CHEM_PREFETCH(ws + 98816);
+      CHEM_PREFETCH(ws + 98848);
+      CHEM_PREFETCH(ws + 98880);
+      CHEM_PREFETCH(ws + 98912);
+      CHEM_PREFETCH(ws + 98944);
+      CHEM_PREFETCH(ws + 98976);
+      CHEM_PREFETCH(ws + 99008);
       double x = b[4576];
       x = fma(-CHEM_LDLU(lu + 17184), b[320], x);
       x = fma(-CHEM_LDLU(lu + 17216), b[832], x);
@@ -1827,264 +1827,6 @@ __device__ __noinline__ void solve_0_0(double* __restrict__ ws, int rhs)
       b[4576] = x;
     }
     {
-      CHEM_PREFETCH(ws + 94272);
-      CHEM_PREFETCH(ws + 94304);
-      CHEM_PREFETCH(ws + 94336);
-      CHEM_PREFETCH(ws + 94368);
-      CHEM_PREFETCH(ws + 94400);
-      CHEM_PREFETCH(ws + 94432);
-      CHEM_PREFETCH(ws + 94464);
-      CHEM_PREFETCH(ws + 94496);
-      CHEM_PREFETCH(ws + 94528);
-      CHEM_PREFETCH(ws + 94560);
-      CHEM_PREFETCH(ws + 94592);
-      CHEM_PREFETCH(ws + 94624);
-      CHEM_PREFETCH(ws + 94656);
-      CHEM_PREFETCH(ws + 94688);
-      CHEM_PREFETCH(ws + 94720);
-      CHEM_PREFETCH(ws + 94752);
-      CHEM_PREFETCH(ws + 94784);
-      CHEM_PREFETCH(ws + 94816);
-      CHEM_PREFETCH(ws + 94848);
-      CHEM_PREFETCH(ws + 94880);
-      CHEM_PREFETCH(ws + 94912);
-      CHEM_PREFETCH(ws + 94944);
-      CHEM_PREFETCH(ws + 94976);
-      CHEM_PREFETCH(ws + 95008);
-      CHEM_PREFETCH(ws + 95040);
-      CHEM_PREFETCH(ws + 95072);
-      CHEM_PREFETCH(ws + 95104);
-      CHEM_PREFETCH(ws + 95136);
-      CHEM_PREFETCH(ws + 95168);
-      CHEM_PREFETCH(ws + 95200);
-      CHEM_PREFETCH(ws + 95232);
-      CHEM_PREFETCH(ws + 95264);
-      CHEM_PREFETCH(ws + 95296);
-      CHEM_PREFETCH(ws + 95328);
-      CHEM_PREFETCH(ws + 95360);
-      CHEM_PREFETCH(ws + 95392);
-      CHEM_PREFETCH(ws + 95424);
-      CHEM_PREFETCH(ws + 95456);
-      CHEM_PREFETCH(ws + 95488);
-      CHEM_PREFETCH(ws + 95520);
-      CHEM_PREFETCH(ws + 95552);
-      CHEM_PREFETCH(ws + 95584);
-      CHEM_PREFETCH(ws + 95616);
-      CHEM_PREFETCH(ws + 95648);
-      CHEM_PREFETCH(ws + 95680);
-      CHEM_PREFETCH(ws + 95712);
-      CHEM_PREFETCH(ws + 95744);
-      CHEM_PREFETCH(ws + 95776);
-      CHEM_PREFETCH(ws + 95808);
-      CHEM_PREFETCH(ws + 95840);
-      CHEM_PREFETCH(ws + 95872);
-      CHEM_PREFETCH(ws + 95904);
-      CHEM_PREFETCH(ws + 95936);
-      CHEM_PREFETCH(ws + 95968);
-      CHEM_PREFETCH(ws + 96000);
-      CHEM_PREFETCH(ws + 96032);
-      CHEM_PREFETCH(ws + 96064);
-      double x = b[4608];
-      x = fma(-CHEM_LDLU(lu + 18400), b[960], x);
-      x = fma(-CHEM_LDLU(lu + 18432), b[1216], x);
-      x = fma(-CHEM_LDLU(lu + 18464), b[1280], x);
-      x = fma(-CHEM_LDLU(lu + 18496), b[1344], x);
-      x = fma(-CHEM_LDLU(lu + 18528), b[1632], x);
-      x = fma(-CHEM_LDLU(lu + 18560), b[1696], x);
-      x = fma(-CHEM_LDLU(lu + 18592), b[1728], x);
-      x = fma(-CHEM_LDLU(lu + 18624), b[1792], x);
-      x = fma(-CHEM_LDLU(lu + 18656), b[1952], x);
-      x = fma(-CHEM_LDLU(lu + 18688), b[1984], x);
-      x = fma(-CHEM_LDLU(lu + 18720), b[2048], x);
-      x = fma(-CHEM_LDLU(lu + 18752), b[2112], x);
-      x = fma(-CHEM_LDLU(lu + 18784), b[2464], x);
-      x = fma(-CHEM_LDLU(lu + 18816), b[2528], x);
-      x = fma(-CHEM_LDLU(lu + 18848), b[2592], x);
-      x = fma(-CHEM_LDLU(lu + 18880), b[2656], x);
-      x = fma(-CHEM_LDLU(lu + 18912), b[3104], x);
-      x = fma(-CHEM_LDLU(lu + 18944), b[3136], x);
-      x = fma(-CHEM_LDLU(lu + 18976), b[3296], x);
-      x = fma(-CHEM_LDLU(lu + 19008), b[3328], x);
-      x = fma(-CHEM_LDLU(lu + 19040), b[3424], x);
-      x = fma(-CHEM_LDLU(lu + 19072), b[3488], x);
-      x = fma(-CHEM_LDLU(lu + 19104), b[3520], x);
-      x = fma(-CHEM_LDLU(lu + 19136), b[3552], x);
-      x = fma(-CHEM_LDLU(lu + 19168), b[3584], x);
-      x = fma(-CHEM_LDLU(lu + 19200), b[3616], x);
-      x = fma(-CHEM_LDLU(lu + 19232), b[3648], x);
-      x = fma(-CHEM_LDLU(lu + 19264), b[3744], x);
-      x = fma(-CHEM_LDLU(lu + 19296), b[3808], x);
-      x = fma(-CHEM_LDLU(lu + 19328), b[3872], x);
-      x = fma(-CHEM_LDLU(lu + 19360), b[3936], x);
-      x = fma(-CHEM_LDLU(lu + 19392), b[4096], x);
-      x = fma(-CHEM_LDLU(lu + 19424), b[4160], x);
-      x = fma(-CHEM_LDLU(lu + 19456), b[4192], x);
-      x = fma(-CHEM_LDLU(lu + 19488), b[4224], x);
-      x = fma(-CHEM_LDLU(lu + 19520), b[4256], x);
-      x = fma(-CHEM_LDLU(lu + 19552), b[4288], x);
-      x = fma(-CHEM_LDLU(lu + 19584), b[4320], x);
-      x = fma(-CHEM_LDLU(lu + 19616), b[4352], x);
-      x = fma(-CHEM_LDLU(lu + 19648), b[4384], x);
-      x = fma(-CHEM_LDLU(lu + 19680), b[4416], x);
-      x = fma(-CHEM_LDLU(lu + 19712), b[4448], x);
-      x = fma(-CHEM_LDLU(lu + 19744), b[4512], x);
-      x = fma(-CHEM_LDLU(lu + 19776), b[4544], x);
-      x = fma(-CHEM_LDLU(lu + 19808), b[4576], x);
-      b[4608] = x;
-    }
-}
-__device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
-{
-    const double* __restrict__ lu = ws + 72864;
-    const double* __restrict__ vd = ws + 126944;
-    double* __restrict__ b = ws + rhs * 32;
-    (void)vd;
-    {
-      CHEM_PREFETCH(ws + 96096);
-      CHEM_PREFETCH(ws + 96128);
-      CHEM_PREFETCH(ws + 96160);
-      CHEM_PREFETCH(ws + 96192);
-      CHEM_PREFETCH(ws + 96224);
-      CHEM_PREFETCH(ws + 96256);
-      CHEM_PREFETCH(ws + 96288);
-      CHEM_PREFETCH(ws + 96320);
-      CHEM_PREFETCH(ws + 96352);
-      CHEM_PREFETCH(ws + 96384);
-      CHEM_PREFETCH(ws + 96416);
-      CHEM_PREFETCH(ws + 96448);
-      CHEM_PREFETCH(ws + 96480);
-      CHEM_PREFETCH(ws + 96512);
-      CHEM_PREFETCH(ws + 96544);
-      CHEM_PREFETCH(ws + 96576);
-      CHEM_PREFETCH(ws + 96608);
-      CHEM_PREFETCH(ws + 96640);
-      CHEM_PREFETCH(ws + 96672);
-      CHEM_PREFETCH(ws + 96704);
-      CHEM_PREFETCH(ws + 96736);
-      CHEM_PREFETCH(ws + 96768);
-      CHEM_PREFETCH(ws + 96800);
-      CHEM_PREFETCH(ws + 96832);
-      CHEM_PREFETCH(ws + 96864);
-      CHEM_PREFETCH(ws + 96896);
-      CHEM_PREFETCH(ws + 96928);
-      CHEM_PREFETCH(ws + 96960);
-      CHEM_PREFETCH(ws + 96992);
-      CHEM_PREFETCH(ws + 97024);
-      CHEM_PREFETCH(ws + 97056);
-      CHEM_PREFETCH(ws + 97088);
-      CHEM_PREFETCH(ws + 97120);
-      CHEM_PREFETCH(ws + 97152);
-      CHEM_PREFETCH(ws + 97184);
-      CHEM_PREFETCH(ws + 97216);
-      CHEM_PREFETCH(ws + 97248);
-      CHEM_PREFETCH(ws + 97280);
-      CHEM_PREFETCH(ws + 97312);
-      CHEM_PREFETCH(ws + 97344);
-      CHEM_PREFETCH(ws + 97376);
-      CHEM_PREFETCH(ws + 97408);
-      CHEM_PREFETCH(ws + 97440);
-      CHEM_PREFETCH(ws + 97472);
-      CHEM_PREFETCH(ws + 97504);
-      CHEM_PREFETCH(ws + 97536);
-      CHEM_PREFETCH(ws + 97568);
-      CHEM_PREFETCH(ws + 97600);
-      CHEM_PREFETCH(ws + 97632);
-      CHEM_PREFETCH(ws + 97664);
-      CHEM_PREFETCH(ws + 97696);
-      CHEM_PREFETCH(ws + 97728);
-      CHEM_PREFETCH(ws + 97760);
-      CHEM_PREFETCH(ws + 97792);
-      CHEM_PREFETCH(ws + 97824);
-      CHEM_PREFETCH(ws + 97856);
-      CHEM_PREFETCH(ws + 97888);
-      CHEM_PREFETCH(ws + 97920);
-      CHEM_PREFETCH(ws + 97952);
-      CHEM_PREFETCH(ws + 97984);
-      double x = b[4640];
-      x = fma(-CHEM_LDLU(lu + 19840), b[1024], x);
-      x = fma(-CHEM_LDLU(lu + 19872), b[1216], x);
-      x = fma(-CHEM_LDLU(lu + 19904), b[1280], x);
-      x = fma(-CHEM_LDLU(lu + 19936), b[1344], x);
-      x = fma(-CHEM_LDLU(lu + 19968), b[1632], x);
-      x = fma(-CHEM_LDLU(lu + 20000), b[1696], x);
-      x = fma(-CHEM_LDLU(lu + 20032), b[1760], x);
-      x = fma(-CHEM_LDLU(lu + 20064), b[1856], x);
-      x = fma(-CHEM_LDLU(lu + 20096), b[1952], x);
-      x = fma(-CHEM_LDLU(lu + 20128), b[2016], x);
-      x = fma(-CHEM_LDLU(lu + 20160), b[2048], x);
-      x = fma(-CHEM_LDLU(lu + 20192), b[2112], x);
-      x = fma(-CHEM_LDLU(lu + 20224), b[2176], x);
-      x = fma(-CHEM_LDLU(lu + 20256), b[2336], x);
-      x = fma(-CHEM_LDLU(lu + 20288), b[2368], x);
-      x = fma(-CHEM_LDLU(lu + 20320), b[2400], x);
-      x = fma(-CHEM_LDLU(lu + 20352), b[2432], x);
-      x = fma(-CHEM_LDLU(lu + 20384), b[2528], x);
-      x = fma(-CHEM_LDLU(lu + 20416), b[2656], x);
-      x = fma(-CHEM_LDLU(lu + 20448), b[2848], x);
-      x = fma(-CHEM_LDLU(lu + 20480), b[2976], x);
-      x = fma(-CHEM_LDLU(lu + 20512), b[3136], x);
-      x = fma(-CHEM_LDLU(lu + 20544), b[3328], x);
-      x = fma(-CHEM_LDLU(lu + 20576), b[3424], x);
-      x = fma(-CHEM_LDLU(lu + 20608), b[3520], x);
-      x = fma(-CHEM_LDLU(lu + 20640), b[3552], x);
-      x = fma(-CHEM_LDLU(lu + 20672), b[3616], x);
-      x = fma(-CHEM_LDLU(lu + 20704), b[3808], x);
-      x = fma(-CHEM_LDLU(lu + 20736), b[3840], x);
-      x = fma(-CHEM_LDLU(lu + 20768), b[3872], x);
-      x = fma(-CHEM_LDLU(lu + 20800), b[3936], x);
-      x = fma(-CHEM_LDLU(lu + 20832), b[4000], x);
-      x = fma(-CHEM_LDLU(lu + 20864), b[4064], x);
-      x = fma(-CHEM_LDLU(lu + 20896), b[4096], x);
-      x = fma(-CHEM_LDLU(lu + 20928), b[4128], x);
-      x = fma(-CHEM_LDLU(lu + 20960), b[4160], x);
-      x = fma(-CHEM_LDLU(lu + 20992), b[4192], x);
-      x = fma(-CHEM_LDLU(lu + 21024), b[4224], x);
-      x = fma(-CHEM_LDLU(lu + 21056), b[4256], x);
-      x = fma(-CHEM_LDLU(lu + 21088), b[4288], x);
-      x = fma(-CHEM_LDLU(lu + 21120), b[4320], x);
-      x = fma(-CHEM_LDLU(lu + 21152), b[4352], x);
-      x = fma(-CHEM_LDLU(lu + 21184), b[4384], x);
-      x = fma(-CHEM_LDLU(lu + 21216), b[4416], x);
-      x = fma(-CHEM_LDLU(lu + 21248), b[4448], x);
-      x = fma(-CHEM_LDLU(lu + 21280), b[4512], x);
-      x = fma(-CHEM_LDLU(lu + 21312), b[4544], x);
-      x = fma(-CHEM_LDLU(lu + 21344), b[4576], x);
-      x = fma(-CHEM_LDLU(lu + 21376), b[4608], x);
-      b[4640] = x;
-    }
-    {
-      CHEM_PREFETCH(ws + 98016);
-      CHEM_PREFETCH(ws + 98048);
-      CHEM_PREFETCH(ws + 98080);
-      CHEM_PREFETCH(ws + 98112);
-      CHEM_PREFETCH(ws + 98144);
-      CHEM_PREFETCH(ws + 98176);
-      CHEM_PREFETCH(ws + 98208);
-      CHEM_PREFETCH(ws + 98240);
-      CHEM_PREFETCH(ws + 98272);
-      CHEM_PREFETCH(ws + 98304);
-      CHEM_PREFETCH(ws + 98336);
-      CHEM_PREFETCH(ws + 98368);
-      CHEM_PREFETCH(ws + 98400);
-      CHEM_PREFETCH(ws + 98432);
-      CHEM_PREFETCH(ws + 98464);
-      CHEM_PREFETCH(ws + 98496);
-      CHEM_PREFETCH(ws + 98528);
-      CHEM_PREFETCH(ws + 98560);
-      CHEM_PREFETCH(ws + 98592);
-      CHEM_PREFETCH(ws + 98624);
-      CHEM_PREFETCH(ws + 98656);
-      CHEM_PREFETCH(ws + 98688);
-      CHEM_PREFETCH(ws + 98720);
-      CHEM_PREFETCH(ws + 98752);
-      CHEM_PREFETCH(ws + 98784);
-      CHEM_PREFETCH(ws + 98816);
-      CHEM_PREFETCH(ws + 98848);
-      CHEM_PREFETCH(ws + 98880);
-      CHEM_PREFETCH(ws + 98912);
-      CHEM_PREFETCH(ws + 98944);
-      CHEM_PREFETCH(ws + 98976);
-      CHEM_PREFETCH(ws + 99008);
       CHEM_PREFETCH(ws + 99040);
       CHEM_PREFETCH(ws + 99072);
       CHEM_PREFETCH(ws + 99104);
@@ -2142,6 +1884,62 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 100768);
       CHEM_PREFETCH(ws + 100800);
       CHEM_PREFETCH(ws + 100832);
+      double x = b[4608];
+      x = fma(-CHEM_LDLU(lu + 18400), b[960], x);
+      x = fma(-CHEM_LDLU(lu + 18432), b[1216], x);
+      x = fma(-CHEM_LDLU(lu + 18464), b[1280], x);
+      x = fma(-CHEM_LDLU(lu + 18496), b[1344], x);
+      x = fma(-CHEM_LDLU(lu + 18528), b[1632], x);
+      x = fma(-CHEM_LDLU(lu + 18560), b[1696], x);
+      x = fma(-CHEM_LDLU(lu + 18592), b[1728], x);
+      x = fma(-CHEM_LDLU(lu + 18624), b[1792], x);
+      x = fma(-CHEM_LDLU(lu + 18656), b[1952], x);
+      x = fma(-CHEM_LDLU(lu + 18688), b[1984], x);
+      x = fma(-CHEM_LDLU(lu + 18720), b[2048], x);
+      x = fma(-CHEM_LDLU(lu + 18752), b[2112], x);
+      x = fma(-CHEM_LDLU(lu + 18784), b[2464], x);
+      x = fma(-CHEM_LDLU(lu + 18816), b[2528], x);
+      x = fma(-CHEM_LDLU(lu + 18848), b[2592], x);
+      x = fma(-CHEM_LDLU(lu + 18880), b[2656], x);
+      x = fma(-CHEM_LDLU(lu + 18912), b[3104], x);
+      x = fma(-CHEM_LDLU(lu + 18944), b[3136], x);
+      x = fma(-CHEM_LDLU(lu + 18976), b[3296], x);
+      x = fma(-CHEM_LDLU(lu + 19008), b[3328], x);
+      x = fma(-CHEM_LDLU(lu + 19040), b[3424], x);
+      x = fma(-CHEM_LDLU(lu + 19072), b[3488], x);
+      x = fma(-CHEM_LDLU(lu + 19104), b[3520], x);
+      x = fma(-CHEM_LDLU(lu + 19136), b[3552], x);
+      x = fma(-CHEM_LDLU(lu + 19168), b[3584], x);
+      x = fma(-CHEM_LDLU(lu + 19200), b[3616], x);
+      x = fma(-CHEM_LDLU(lu + 19232), b[3648], x);
+      x = fma(-CHEM_LDLU(lu + 19264), b[3744], x);
+      x = fma(-CHEM_LDLU(lu + 19296), b[3808], x);
+      x = fma(-CHEM_LDLU(lu + 19328), b[3872], x);
+      x = fma(-CHEM_LDLU(lu + 19360), b[3936], x);
+      x = fma(-CHEM_LDLU(lu + 19392), b[4096], x);
+      x = fma(-CHEM_LDLU(lu + 19424), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 19456), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 19488), b[4224], x);
+      x = fma(-CHEM_LDLU(lu + 19520), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 19552), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 19584), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 19616), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 19648), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 19680), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 19712), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 19744), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 19776), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 19808), b[4576], x);
+      b[4608] = x;
+    }
+}
+__device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
+{
+    const double* __restrict__ lu = ws + 77632;
+    const double* __restrict__ vd = ws + 131712;
+    double* __restrict__ b = ws + rhs * 32;
+    (void)vd;
+    {
       CHEM_PREFETCH(ws + 100864);
       CHEM_PREFETCH(ws + 100896);
       CHEM_PREFETCH(ws + 100928);
@@ -2151,6 +1949,208 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 101056);
       CHEM_PREFETCH(ws + 101088);
       CHEM_PREFETCH(ws + 101120);
+      CHEM_PREFETCH(ws + 101152);
+      CHEM_PREFETCH(ws + 101184);
+      CHEM_PREFETCH(ws + 101216);
+      CHEM_PREFETCH(ws + 101248);
+      CHEM_PREFETCH(ws + 101280);
+      CHEM_PREFETCH(ws + 101312);
+      CHEM_PREFETCH(ws + 101344);
+      CHEM_PREFETCH(ws + 101376);
+      CHEM_PREFETCH(ws + 101408);
+      CHEM_PREFETCH(ws + 101440);
+      CHEM_PREFETCH(ws + 101472);
+      CHEM_PREFETCH(ws + 101504);
+      CHEM_PREFETCH(ws + 101536);
+      CHEM_PREFETCH(ws + 101568);
+      CHEM_PREFETCH(ws + 101600);
+      CHEM_PREFETCH(ws + 101632);
+      CHEM_PREFETCH(ws + 101664);
+      CHEM_PREFETCH(ws + 101696);
+      CHEM_PREFETCH(ws + 101728);
+      CHEM_PREFETCH(ws + 101760);
+      CHEM_PREFETCH(ws + 101792);
+      CHEM_PREFETCH(ws + 101824);
+      CHEM_PREFETCH(ws + 101856);
+      CHEM_PREFETCH(ws + 101888);
+      CHEM_PREFETCH(ws + 101920);
+      CHEM_PREFETCH(ws + 101952);
+      CHEM_PREFETCH(ws + 101984);
+      CHEM_PREFETCH(ws + 102016);
+      CHEM_PREFETCH(ws + 102048);
+      CHEM_PREFETCH(ws + 102080);
+      CHEM_PREFETCH(ws + 102112);
+      CHEM_PREFETCH(ws + 102144);
+      CHEM_PREFETCH(ws + 102176);
+      CHEM_PREFETCH(ws + 102208);
+      CHEM_PREFETCH(ws + 102240);
+      CHEM_PREFETCH(ws + 102272);
+      CHEM_PREFETCH(ws + 102304);
+      CHEM_PREFETCH(ws + 102336);
+      CHEM_PREFETCH(ws + 102368);
+      CHEM_PREFETCH(ws + 102400);
+      CHEM_PREFETCH(ws + 102432);
+      CHEM_PREFETCH(ws + 102464);
+      CHEM_PREFETCH(ws + 102496);
+      CHEM_PREFETCH(ws + 102528);
+      CHEM_PREFETCH(ws + 102560);
+      CHEM_PREFETCH(ws + 102592);
+      CHEM_PREFETCH(ws + 102624);
+      CHEM_PREFETCH(ws + 102656);
+      CHEM_PREFETCH(ws + 102688);
+      CHEM_PREFETCH(ws + 102720);
+      CHEM_PREFETCH(ws + 102752);
+      double x = b[4640];
+      x = fma(-CHEM_LDLU(lu + 19840), b[1024], x);
+      x = fma(-CHEM_LDLU(lu + 19872), b[1216], x);
+      x = fma(-CHEM_LDLU(lu + 19904), b[1280], x);
+      x = fma(-CHEM_LDLU(lu + 19936), b[1344], x);
+      x = fma(-CHEM_LDLU(lu + 19968), b[1632], x);
+      x = fma(-CHEM_LDLU(lu + 20000), b[1696], x);
+      x = fma(-CHEM_LDLU(lu + 20032), b[1760], x);
+      x = fma(-CHEM_LDLU(lu + 20064), b[1856], x);
+      x = fma(-CHEM_LDLU(lu + 20096), b[1952], x);
+      x = fma(-CHEM_LDLU(lu + 20128), b[2016], x);
+      x = fma(-CHEM_LDLU(lu + 20160), b[2048], x);
+      x = fma(-CHEM_LDLU(lu + 20192), b[2112], x);
+      x = fma(-CHEM_LDLU(lu + 20224), b[2176], x);
+      x = fma(-CHEM_LDLU(lu + 20256), b[2336], x);
+      x = fma(-CHEM_LDLU(lu + 20288), b[2368], x);
+      x = fma(-CHEM_LDLU(lu + 20320), b[2400], x);
+      x = fma(-CHEM_LDLU(lu + 20352), b[2432], x);
+      x = fma(-CHEM_LDLU(lu + 20384), b[2528], x);
+      x = fma(-CHEM_LDLU(lu + 20416), b[2656], x);
+      x = fma(-CHEM_LDLU(lu + 20448), b[2848], x);
+      x = fma(-CHEM_LDLU(lu + 20480), b[2976], x);
+      x = fma(-CHEM_LDLU(lu + 20512), b[3136], x);
+      x = fma(-CHEM_LDLU(lu + 20544), b[3328], x);
+      x = fma(-CHEM_LDLU(lu + 20576), b[3424], x);
+      x = fma(-CHEM_LDLU(lu + 20608), b[3520], x);
+      x = fma(-CHEM_LDLU(lu + 20640), b[3552], x);
+      x = fma(-CHEM_LDLU(lu + 20672), b[3616], x);
+      x = fma(-CHEM_LDLU(lu + 20704), b[3808], x);
+      x = fma(-CHEM_LDLU(lu + 20736), b[3840], x);
+      x = fma(-CHEM_LDLU(lu + 20768), b[3872], x);
+      x = fma(-CHEM_LDLU(lu + 20800), b[3936], x);
+      x = fma(-CHEM_LDLU(lu + 20832), b[4000], x);
+      x = fma(-CHEM_LDLU(lu + 20864), b[4064], x);
+      x = fma(-CHEM_LDLU(lu + 20896), b[4096], x);
+      x = fma(-CHEM_LDLU(lu + 20928), b[4128], x);
+      x = fma(-CHEM_LDLU(lu + 20960), b[4160], x);
+      x = fma(-CHEM_LDLU(lu + 20992), b[4192], x);
+      x = fma(-CHEM_LDLU(lu + 21024), b[4224], x);
+      x = fma(-CHEM_LDLU(lu + 21056), b[4256], x);
+      x = fma(-CHEM_LDLU(lu + 21088), b[4288], x);
+      x = fma(-CHEM_LDLU(lu + 21120), b[4320], x);
+      x = fma(-CHEM_LDLU(lu + 21152), b[4352], x);
+      x = fma(-CHEM_LDLU(lu + 21184), b[4384], x);
+      x = fma(-CHEM_LDLU(lu + 21216), b[4416], x);
+      x = fma(-CHEM_LDLU(lu + 21248), b[4448], x);
+      x = fma(-CHEM_LDLU(lu + 21280), b[4512], x);
+      x = fma(-CHEM_LDLU(lu + 21312), b[4544], x);
+      x = fma(-CHEM_LDLU(lu + 21344), b[4576], x);
+      x = fma(-CHEM_LDLU(lu + 21376), b[4608], x);
+      b[4640] = x;
+    }
+    {
+      CHEM_PREFETCH(ws + 102784);
+      CHEM_PREFETCH(ws + 102816);
+      CHEM_PREFETCH(ws + 102848);
+      CHEM_PREFETCH(ws + 102880);
+      CHEM_PREFETCH(ws + 102912);
+      CHEM_PREFETCH(ws + 102944);
+      CHEM_PREFETCH(ws + 102976);
+      CHEM_PREFETCH(ws + 103008);
+      CHEM_PREFETCH(ws + 103040);
+      CHEM_PREFETCH(ws + 103072);
+      CHEM_PREFETCH(ws + 103104);
+      CHEM_PREFETCH(ws + 103136);
+      CHEM_PREFETCH(ws + 103168);
+      CHEM_PREFETCH(ws + 103200);
+      CHEM_PREFETCH(ws + 103232);
+      CHEM_PREFETCH(ws + 103264);
+      CHEM_PREFETCH(ws + 103296);
+      CHEM_PREFETCH(ws + 103328);
+      CHEM_PREFETCH(ws + 103360);
+      CHEM_PREFETCH(ws + 103392);
+      CHEM_PREFETCH(ws + 103424);
+      CHEM_PREFETCH(ws + 103456);
+      CHEM_PREFETCH(ws + 103488);
+      CHEM_PREFETCH(ws + 103520);
+      CHEM_PREFETCH(ws + 103552);
+      CHEM_PREFETCH(ws + 103584);
+      CHEM_PREFETCH(ws + 103616);
+      CHEM_PREFETCH(ws + 103648);
+      CHEM_PREFETCH(ws + 103680);
+      CHEM_PREFETCH(ws + 103712);
+      CHEM_PREFETCH(ws + 103744);
+      CHEM_PREFETCH(ws + 103776);
+      CHEM_PREFETCH(ws + 103808);
+      CHEM_PREFETCH(ws + 103840);
+      CHEM_PREFETCH(ws + 103872);
+      CHEM_PREFETCH(ws + 103904);
+      CHEM_PREFETCH(ws + 103936);
+      CHEM_PREFETCH(ws + 103968);
+      CHEM_PREFETCH(ws + 104000);
+      CHEM_PREFETCH(ws + 104032);
+      CHEM_PREFETCH(ws + 104064);
+      CHEM_PREFETCH(ws + 104096);
+      CHEM_PREFETCH(ws + 104128);
+      CHEM_PREFETCH(ws + 104160);
+      CHEM_PREFETCH(ws + 104192);
+      CHEM_PREFETCH(ws + 104224);
+      CHEM_PREFETCH(ws + 104256);
+      CHEM_PREFETCH(ws + 104288);
+      CHEM_PREFETCH(ws + 104320);
+      CHEM_PREFETCH(ws + 104352);
+      CHEM_PREFETCH(ws + 104384);
+      CHEM_PREFETCH(ws + 104416);
+      CHEM_PREFETCH(ws + 104448);
+      CHEM_PREFETCH(ws + 104480);
+      CHEM_PREFETCH(ws + 104512);
+      CHEM_PREFETCH(ws + 104544);
+      CHEM_PREFETCH(ws + 104576);
+      CHEM_PREFETCH(ws + 104608);
+      CHEM_PREFETCH(ws + 104640);
+      CHEM_PREFETCH(ws + 104672);
+      CHEM_PREFETCH(ws + 104704);
+      CHEM_PREFETCH(ws + 104736);
+      CHEM_PREFETCH(ws + 104768);
+      CHEM_PREFETCH(ws + 104800);
+      CHEM_PREFETCH(ws + 104832);
+      CHEM_PREFETCH(ws + 104864);
+      CHEM_PREFETCH(ws + 104896);
+      CHEM_PREFETCH(ws + 104928);
+      CHEM_PREFETCH(ws + 104960);
+      CHEM_PREFETCH(ws + 104992);
+      CHEM_PREFETCH(ws + 105024);
+      CHEM_PREFETCH(ws + 105056);
+      CHEM_PREFETCH(ws + 105088);
+      CHEM_PREFETCH(ws + 105120);
+      CHEM_PREFETCH(ws + 105152);
+      CHEM_PREFETCH(ws + 105184);
+      CHEM_PREFETCH(ws + 105216);
+      CHEM_PREFETCH(ws + 105248);
+      CHEM_PREFETCH(ws + 105280);
+      CHEM_PREFETCH(ws + 105312);
+      CHEM_PREFETCH(ws + 105344);
+      CHEM_PREFETCH(ws + 105376);
+      CHEM_PREFETCH(ws + 105408);
+      CHEM_PREFETCH(ws + 105440);
+      CHEM_PREFETCH(ws + 105472);
+      CHEM_PREFETCH(ws + 105504);
+      CHEM_PREFETCH(ws + 105536);
+      CHEM_PREFETCH(ws + 105568);
+      CHEM_PREFETCH(ws + 105600);
+      CHEM_PREFETCH(ws + 105632);
+      CHEM_PREFETCH(ws + 105664);
+      CHEM_PREFETCH(ws + 105696);
+      CHEM_PREFETCH(ws + 105728);
+      CHEM_PREFETCH(ws + 105760);
+      CHEM_PREFETCH(ws + 105792);
+      CHEM_PREFETCH(ws + 105824);
+      CHEM_PREFETCH(ws + 105856);
+      CHEM_PREFETCH(ws + 105888);
       double x = b[4672];
       x = fma(-CHEM_LDLU(lu + 21408), b[320], x);
       x = fma(-CHEM_LDLU(lu + 21440), b[384], x);
@@ -2212,7 +2212,7 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[4672] = x;
     }
     {
-      CHEM_PREFETCH(ws + 131680);
+      CHEM_PREFETCH(ws + 136448);
       double x = b[4704];
       x = fma(-CHEM_LDLU(lu + 23232), b[352], x);
       x = fma(-CHEM_LDLU(lu + 23264), b[384], x);
@@ -2277,8 +2277,8 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[4704] = x;
     }
     {
-      CHEM_PREFETCH(ws + 101152);
-      CHEM_PREFETCH(ws + 131648);
+      CHEM_PREFETCH(ws + 105920);
+      CHEM_PREFETCH(ws + 136416);
       double x = b[4736];
       x = fma(-CHEM_LDLU(lu + 25152), b[352], x);
       x = fma(-CHEM_LDLU(lu + 25184), b[384], x);
@@ -2381,39 +2381,39 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[4736] = x;
     }
     {
-      CHEM_PREFETCH(ws + 101184);
-      CHEM_PREFETCH(ws + 101216);
-      CHEM_PREFETCH(ws + 131616);
+      CHEM_PREFETCH(ws + 105952);
+      CHEM_PREFETCH(ws + 105984);
+      CHEM_PREFETCH(ws + 136384);
       double x = b[4736];
       b[4736] = x * CHEM_LDLU(vd + 4736);
     }
     {
-      CHEM_PREFETCH(ws + 101248);
-      CHEM_PREFETCH(ws + 101280);
-      CHEM_PREFETCH(ws + 101312);
-      CHEM_PREFETCH(ws + 131584);
+      CHEM_PREFETCH(ws + 106016);
+      CHEM_PREFETCH(ws + 106048);
+      CHEM_PREFETCH(ws + 106080);
+      CHEM_PREFETCH(ws + 136352);
       double x = b[4704];
       x = fma(-CHEM_LDLU(lu + 28288), b[4736], x);
       b[4704] = x * CHEM_LDLU(vd + 4704);
     }
     {
-      CHEM_PREFETCH(ws + 101344);
-      CHEM_PREFETCH(ws + 101376);
-      CHEM_PREFETCH(ws + 101408);
-      CHEM_PREFETCH(ws + 101440);
-      CHEM_PREFETCH(ws + 131552);
+      CHEM_PREFETCH(ws + 106112);
+      CHEM_PREFETCH(ws + 106144);
+      CHEM_PREFETCH(ws + 106176);
+      CHEM_PREFETCH(ws + 106208);
+      CHEM_PREFETCH(ws + 136320);
       double x = b[4672];
       x = fma(-CHEM_LDLU(lu + 28320), b[4704], x);
       x = fma(-CHEM_LDLU(lu + 28352), b[4736], x);
       b[4672] = x * CHEM_LDLU(vd + 4672);
     }
     {
-      CHEM_PREFETCH(ws + 101472);
-      CHEM_PREFETCH(ws + 101504);
-      CHEM_PREFETCH(ws + 101536);
-      CHEM_PREFETCH(ws + 101568);
-      CHEM_PREFETCH(ws + 101600);
-      CHEM_PREFETCH(ws + 131520);
+      CHEM_PREFETCH(ws + 106240);
+      CHEM_PREFETCH(ws + 106272);
+      CHEM_PREFETCH(ws + 106304);
+      CHEM_PREFETCH(ws + 106336);
+      CHEM_PREFETCH(ws + 106368);
+      CHEM_PREFETCH(ws + 136288);
       double x = b[4640];
       x = fma(-CHEM_LDLU(lu + 28384), b[4672], x);
       x = fma(-CHEM_LDLU(lu + 28416), b[4704], x);
@@ -2421,13 +2421,13 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[4640] = x * CHEM_LDLU(vd + 4640);
     }
     {
-      CHEM_PREFETCH(ws + 101632);
-      CHEM_PREFETCH(ws + 101664);
-      CHEM_PREFETCH(ws + 101696);
-      CHEM_PREFETCH(ws + 101728);
-      CHEM_PREFETCH(ws + 101760);
-      CHEM_PREFETCH(ws + 101792);
-      CHEM_PREFETCH(ws + 131488);
+      CHEM_PREFETCH(ws + 106400);
+      CHEM_PREFETCH(ws + 106432);
+      CHEM_PREFETCH(ws + 106464);
+      CHEM_PREFETCH(ws + 106496);
+      CHEM_PREFETCH(ws + 106528);
+      CHEM_PREFETCH(ws + 106560);
+      CHEM_PREFETCH(ws + 136256);
       double x = b[4608];
       x = fma(-CHEM_LDLU(lu + 28480), b[4640], x);
       x = fma(-CHEM_LDLU(lu + 28512), b[4672], x);
@@ -2436,14 +2436,14 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[4608] = x * CHEM_LDLU(vd + 4608);
     }
     {
-      CHEM_PREFETCH(ws + 101824);
-      CHEM_PREFETCH(ws + 101856);
-      CHEM_PREFETCH(ws + 101888);
-      CHEM_PREFETCH(ws + 101920);
-      CHEM_PREFETCH(ws + 101952);
-      CHEM_PREFETCH(ws + 101984);
-      CHEM_PREFETCH(ws + 102016);
-      CHEM_PREFETCH(ws + 131456);
+      CHEM_PREFETCH(ws + 106592);
+      CHEM_PREFETCH(ws + 106624);
+      CHEM_PREFETCH(ws + 106656);
+      CHEM_PREFETCH(ws + 106688);
+      CHEM_PREFETCH(ws + 106720);
+      CHEM_PREFETCH(ws + 106752);
+      CHEM_PREFETCH(ws + 106784);
+      CHEM_PREFETCH(ws + 136224);
       double x = b[4576];
       x = fma(-CHEM_LDLU(lu + 28608), b[4608], x);
       x = fma(-CHEM_LDLU(lu + 28640), b[4640], x);
@@ -2453,15 +2453,15 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[4576] = x * CHEM_LDLU(vd + 4576);
     }
     {
-      CHEM_PREFETCH(ws + 102048);
-      CHEM_PREFETCH(ws + 102080);
-      CHEM_PREFETCH(ws + 102112);
-      CHEM_PREFETCH(ws + 102144);
-      CHEM_PREFETCH(ws + 102176);
-      CHEM_PREFETCH(ws + 102208);
-      CHEM_PREFETCH(ws + 102240);
-      CHEM_PREFETCH(ws + 102272);
-      CHEM_PREFETCH(ws + 131424);
+      CHEM_PREFETCH(ws + 106816);
+      CHEM_PREFETCH(ws + 106848);
+      CHEM_PREFETCH(ws + 106880);
+      CHEM_PREFETCH(ws + 106912);
+      CHEM_PREFETCH(ws + 106944);
+      CHEM_PREFETCH(ws + 106976);
+      CHEM_PREFETCH(ws + 107008);
+      CHEM_PREFETCH(ws + 107040);
+      CHEM_PREFETCH(ws + 136192);
       double x = b[4544];
       x = fma(-CHEM_LDLU(lu + 28768), b[4576], x);
       x = fma(-CHEM_LDLU(lu + 28800), b[4608], x);
@@ -2472,15 +2472,15 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[4544] = x * CHEM_LDLU(vd + 4544);
     }
     {
-      CHEM_PREFETCH(ws + 102304);
-      CHEM_PREFETCH(ws + 102336);
-      CHEM_PREFETCH(ws + 102368);
-      CHEM_PREFETCH(ws + 102400);
-      CHEM_PREFETCH(ws + 102432);
-      CHEM_PREFETCH(ws + 102464);
-      CHEM_PREFETCH(ws + 102496);
-      CHEM_PREFETCH(ws + 102528);
-      CHEM_PREFETCH(ws + 131392);
+      CHEM_PREFETCH(ws + 107072);
+      CHEM_PREFETCH(ws + 107104);
+      CHEM_PREFETCH(ws + 107136);
+      CHEM_PREFETCH(ws + 107168);
+      CHEM_PREFETCH(ws + 107200);
+      CHEM_PREFETCH(ws + 107232);
+      CHEM_PREFETCH(ws + 107264);
+      CHEM_PREFETCH(ws + 107296);
+      CHEM_PREFETCH(ws + 136160);
       double x = b[4512];
       x = fma(-CHEM_LDLU(lu + 28960), b[4544], x);
       x = fma(-CHEM_LDLU(lu + 28992), b[4576], x);
@@ -2492,16 +2492,16 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[4512] = x * CHEM_LDLU(vd + 4512);
     }
     {
-      CHEM_PREFETCH(ws + 102560);
-      CHEM_PREFETCH(ws + 102592);
-      CHEM_PREFETCH(ws + 102624);
-      CHEM_PREFETCH(ws + 102656);
-      CHEM_PREFETCH(ws + 102688);
-      CHEM_PREFETCH(ws + 102720);
-      CHEM_PREFETCH(ws + 102752);
-      CHEM_PREFETCH(ws + 102784);
-      CHEM_PREFETCH(ws + 102816);
-      CHEM_PREFETCH(ws + 131360);
+      CHEM_PREFETCH(ws + 107328);
+      CHEM_PREFETCH(ws + 107360);
+      CHEM_PREFETCH(ws + 107392);
+      CHEM_PREFETCH(ws + 107424);
+      CHEM_PREFETCH(ws + 107456);
+      CHEM_PREFETCH(ws + 107488);
+      CHEM_PREFETCH(ws + 107520);
+      CHEM_PREFETCH(ws + 107552);
+      CHEM_PREFETCH(ws + 107584);
+      CHEM_PREFETCH(ws + 136128);
       double x = b[4480];
       x = fma(-CHEM_LDLU(lu + 29184), b[4512], x);
       x = fma(-CHEM_LDLU(lu + 29216), b[4544], x);
@@ -2514,17 +2514,17 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[4480] = x * CHEM_LDLU(vd + 4480);
     }
     {
-      CHEM_PREFETCH(ws + 102848);
-      CHEM_PREFETCH(ws + 102880);
-      CHEM_PREFETCH(ws + 102912);
-      CHEM_PREFETCH(ws + 102944);
-      CHEM_PREFETCH(ws + 102976);
-      CHEM_PREFETCH(ws + 103008);
-      CHEM_PREFETCH(ws + 103040);
-      CHEM_PREFETCH(ws + 103072);
-      CHEM_PREFETCH(ws + 103104);
-      CHEM_PREFETCH(ws + 103136);
-      CHEM_PREFETCH(ws + 131328);
+      CHEM_PREFETCH(ws + 107616);
+      CHEM_PREFETCH(ws + 107648);
+      CHEM_PREFETCH(ws + 107680);
+      CHEM_PREFETCH(ws + 107712);
+      CHEM_PREFETCH(ws + 107744);
+      CHEM_PREFETCH(ws + 107776);
+      CHEM_PREFETCH(ws + 107808);
+      CHEM_PREFETCH(ws + 107840);
+      CHEM_PREFETCH(ws + 107872);
+      CHEM_PREFETCH(ws + 107904);
+      CHEM_PREFETCH(ws + 136096);
       double x = b[4448];
       x = fma(-CHEM_LDLU(lu + 29440), b[4512], x);
       x = fma(-CHEM_LDLU(lu + 29472), b[4544], x);
@@ -2537,17 +2537,17 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[4448] = x * CHEM_LDLU(vd + 4448);
     }
     {
-      CHEM_PREFETCH(ws + 103168);
-      CHEM_PREFETCH(ws + 103200);
-      CHEM_PREFETCH(ws + 103232);
-      CHEM_PREFETCH(ws + 103264);
-      CHEM_PREFETCH(ws + 103296);
-      CHEM_PREFETCH(ws + 103328);
-      CHEM_PREFETCH(ws + 103360);
-      CHEM_PREFETCH(ws + 103392);
-      CHEM_PREFETCH(ws + 103424);
-      CHEM_PREFETCH(ws + 103456);
-      CHEM_PREFETCH(ws + 131296);
+      CHEM_PREFETCH(ws + 107936);
+      CHEM_PREFETCH(ws + 107968);
+      CHEM_PREFETCH(ws + 108000);
+      CHEM_PREFETCH(ws + 108032);
+      CHEM_PREFETCH(ws + 108064);
+      CHEM_PREFETCH(ws + 108096);
+      CHEM_PREFETCH(ws + 108128);
+      CHEM_PREFETCH(ws + 108160);
+      CHEM_PREFETCH(ws + 108192);
+      CHEM_PREFETCH(ws + 108224);
+      CHEM_PREFETCH(ws + 136064);
       double x = b[4416];
       x = fma(-CHEM_LDLU(lu + 29696), b[4448], x);
       x = fma(-CHEM_LDLU(lu + 29728), b[4512], x);
@@ -2561,17 +2561,17 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[4416] = x * CHEM_LDLU(vd + 4416);
     }
     {
-      CHEM_PREFETCH(ws + 103488);
-      CHEM_PREFETCH(ws + 103520);
-      CHEM_PREFETCH(ws + 103552);
-      CHEM_PREFETCH(ws + 103584);
-      CHEM_PREFETCH(ws + 103616);
-      CHEM_PREFETCH(ws + 103648);
-      CHEM_PREFETCH(ws + 103680);
-      CHEM_PREFETCH(ws + 103712);
-      CHEM_PREFETCH(ws + 103744);
-      CHEM_PREFETCH(ws + 103776);
-      CHEM_PREFETCH(ws + 131264);
+      CHEM_PREFETCH(ws + 108256);
+      CHEM_PREFETCH(ws + 108288);
+      CHEM_PREFETCH(ws + 108320);
+      CHEM_PREFETCH(ws + 108352);
+      CHEM_PREFETCH(ws + 108384);
+      CHEM_PREFETCH(ws + 108416);
+      CHEM_PREFETCH(ws + 108448);
+      CHEM_PREFETCH(ws + 108480);
+      CHEM_PREFETCH(ws + 108512);
+      CHEM_PREFETCH(ws + 108544);
+      CHEM_PREFETCH(ws + 136032);
       double x = b[4384];
       x = fma(-CHEM_LDLU(lu + 29984), b[4416], x);
       x = fma(-CHEM_LDLU(lu + 30016), b[4448], x);
@@ -2586,20 +2586,20 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[4384] = x * CHEM_LDLU(vd + 4384);
     }
     {
-      CHEM_PREFETCH(ws + 103808);
-      CHEM_PREFETCH(ws + 103840);
-      CHEM_PREFETCH(ws + 103872);
-      CHEM_PREFETCH(ws + 103904);
-      CHEM_PREFETCH(ws + 103936);
-      CHEM_PREFETCH(ws + 103968);
-      CHEM_PREFETCH(ws + 104000);
-      CHEM_PREFETCH(ws + 104032);
-      CHEM_PREFETCH(ws + 104064);
-      CHEM_PREFETCH(ws + 104096);
-      CHEM_PREFETCH(ws + 104128);
-      CHEM_PREFETCH(ws + 104160);
-      CHEM_PREFETCH(ws + 104192);
-      CHEM_PREFETCH(ws + 131232);
+      CHEM_PREFETCH(ws + 108576);
+      CHEM_PREFETCH(ws + 108608);
+      CHEM_PREFETCH(ws + 108640);
+      CHEM_PREFETCH(ws + 108672);
+      CHEM_PREFETCH(ws + 108704);
+      CHEM_PREFETCH(ws + 108736);
+      CHEM_PREFETCH(ws + 108768);
+      CHEM_PREFETCH(ws + 108800);
+      CHEM_PREFETCH(ws + 108832);
+      CHEM_PREFETCH(ws + 108864);
+      CHEM_PREFETCH(ws + 108896);
+      CHEM_PREFETCH(ws + 108928);
+      CHEM_PREFETCH(ws + 108960);
+      CHEM_PREFETCH(ws + 136000);
       double x = b[4352];
       x = fma(-CHEM_LDLU(lu + 30304), b[4384], x);
       x = fma(-CHEM_LDLU(lu + 30336), b[4416], x);
@@ -2614,18 +2614,18 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[4352] = x * CHEM_LDLU(vd + 4352);
     }
     {
-      CHEM_PREFETCH(ws + 104224);
-      CHEM_PREFETCH(ws + 104256);
-      CHEM_PREFETCH(ws + 104288);
-      CHEM_PREFETCH(ws + 104320);
-      CHEM_PREFETCH(ws + 104352);
-      CHEM_PREFETCH(ws + 104384);
-      CHEM_PREFETCH(ws + 104416);
-      CHEM_PREFETCH(ws + 104448);
-      CHEM_PREFETCH(ws + 104480);
-      CHEM_PREFETCH(ws + 104512);
-      CHEM_PREFETCH(ws + 104544);
-      CHEM_PREFETCH(ws + 131200);
+      CHEM_PREFETCH(ws + 108992);
+      CHEM_PREFETCH(ws + 109024);
+      CHEM_PREFETCH(ws + 109056);
+      CHEM_PREFETCH(ws + 109088);
+      CHEM_PREFETCH(ws + 109120);
+      CHEM_PREFETCH(ws + 109152);
+      CHEM_PREFETCH(ws + 109184);
+      CHEM_PREFETCH(ws + 109216);
+      CHEM_PREFETCH(ws + 109248);
+      CHEM_PREFETCH(ws + 109280);
+      CHEM_PREFETCH(ws + 109312);
+      CHEM_PREFETCH(ws + 135968);
       double x = b[4320];
       x = fma(-CHEM_LDLU(lu + 30624), b[4384], x);
       x = fma(-CHEM_LDLU(lu + 30656), b[4416], x);
@@ -2640,18 +2640,18 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[4320] = x * CHEM_LDLU(vd + 4320);
     }
     {
-      CHEM_PREFETCH(ws + 104576);
-      CHEM_PREFETCH(ws + 104608);
-      CHEM_PREFETCH(ws + 104640);
-      CHEM_PREFETCH(ws + 104672);
-      CHEM_PREFETCH(ws + 104704);
-      CHEM_PREFETCH(ws + 104736);
-      CHEM_PREFETCH(ws + 104768);
-      CHEM_PREFETCH(ws + 104800);
-      CHEM_PREFETCH(ws + 104832);
-      CHEM_PREFETCH(ws + 104864);
-      CHEM_PREFETCH(ws + 104896);
-      CHEM_PREFETCH(ws + 131168);
+      CHEM_PREFETCH(ws + 109344);
+      CHEM_PREFETCH(ws + 109376);
+      CHEM_PREFETCH(ws + 109408);
+      CHEM_PREFETCH(ws + 109440);
+      CHEM_PREFETCH(ws + 109472);
+      CHEM_PREFETCH(ws + 109504);
+      CHEM_PREFETCH(ws + 109536);
+      CHEM_PREFETCH(ws + 109568);
+      CHEM_PREFETCH(ws + 109600);
+      CHEM_PREFETCH(ws + 109632);
+      CHEM_PREFETCH(ws + 109664);
+      CHEM_PREFETCH(ws + 135936);
       double x = b[4288];
       x = fma(-CHEM_LDLU(lu + 30944), b[4320], x);
       x = fma(-CHEM_LDLU(lu + 30976), b[4352], x);
@@ -2669,21 +2669,21 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[4288] = x * CHEM_LDLU(vd + 4288);
     }
     {
-      CHEM_PREFETCH(ws + 104928);
-      CHEM_PREFETCH(ws + 104960);
-      CHEM_PREFETCH(ws + 104992);
-      CHEM_PREFETCH(ws + 105024);
-      CHEM_PREFETCH(ws + 105056);
-      CHEM_PREFETCH(ws + 105088);
-      CHEM_PREFETCH(ws + 105120);
-      CHEM_PREFETCH(ws + 105152);
-      CHEM_PREFETCH(ws + 105184);
-      CHEM_PREFETCH(ws + 105216);
-      CHEM_PREFETCH(ws + 105248);
-      CHEM_PREFETCH(ws + 105280);
-      CHEM_PREFETCH(ws + 105312);
-      CHEM_PREFETCH(ws + 105344);
-      CHEM_PREFETCH(ws + 131136);
+      CHEM_PREFETCH(ws + 109696);
+      CHEM_PREFETCH(ws + 109728);
+      CHEM_PREFETCH(ws + 109760);
+      CHEM_PREFETCH(ws + 109792);
+      CHEM_PREFETCH(ws + 109824);
+      CHEM_PREFETCH(ws + 109856);
+      CHEM_PREFETCH(ws + 109888);
+      CHEM_PREFETCH(ws + 109920);
+      CHEM_PREFETCH(ws + 109952);
+      CHEM_PREFETCH(ws + 109984);
+      CHEM_PREFETCH(ws + 110016);
+      CHEM_PREFETCH(ws + 110048);
+      CHEM_PREFETCH(ws + 110080);
+      CHEM_PREFETCH(ws + 110112);
+      CHEM_PREFETCH(ws + 135904);
       double x = b[4256];
       x = fma(-CHEM_LDLU(lu + 31360), b[4320], x);
       x = fma(-CHEM_LDLU(lu + 31392), b[4384], x);
@@ -2699,19 +2699,19 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[4256] = x * CHEM_LDLU(vd + 4256);
     }
     {
-      CHEM_PREFETCH(ws + 105376);
-      CHEM_PREFETCH(ws + 105408);
-      CHEM_PREFETCH(ws + 105440);
-      CHEM_PREFETCH(ws + 105472);
-      CHEM_PREFETCH(ws + 105504);
-      CHEM_PREFETCH(ws + 105536);
-      CHEM_PREFETCH(ws + 105568);
-      CHEM_PREFETCH(ws + 105600);
-      CHEM_PREFETCH(ws + 105632);
-      CHEM_PREFETCH(ws + 105664);
-      CHEM_PREFETCH(ws + 105696);
-      CHEM_PREFETCH(ws + 105728);
-      CHEM_PREFETCH(ws + 131104);
+      CHEM_PREFETCH(ws + 110144);
+      CHEM_PREFETCH(ws + 110176);
+      CHEM_PREFETCH(ws + 110208);
+      CHEM_PREFETCH(ws + 110240);
+      CHEM_PREFETCH(ws + 110272);
+      CHEM_PREFETCH(ws + 110304);
+      CHEM_PREFETCH(ws + 110336);
+      CHEM_PREFETCH(ws + 110368);
+      CHEM_PREFETCH(ws + 110400);
+      CHEM_PREFETCH(ws + 110432);
+      CHEM_PREFETCH(ws + 110464);
+      CHEM_PREFETCH(ws + 110496);
+      CHEM_PREFETCH(ws + 135872);
       double x = b[4224];
       x = fma(-CHEM_LDLU(lu + 31712), b[4320], x);
       x = fma(-CHEM_LDLU(lu + 31744), b[4384], x);
@@ -2727,18 +2727,18 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[4224] = x * CHEM_LDLU(vd + 4224);
     }
     {
-      CHEM_PREFETCH(ws + 105760);
-      CHEM_PREFETCH(ws + 105792);
-      CHEM_PREFETCH(ws + 105824);
-      CHEM_PREFETCH(ws + 105856);
-      CHEM_PREFETCH(ws + 105888);
-      CHEM_PREFETCH(ws + 105920);
-      CHEM_PREFETCH(ws + 105952);
-      CHEM_PREFETCH(ws + 105984);
-      CHEM_PREFETCH(ws + 106016);
-      CHEM_PREFETCH(ws + 106048);
-      CHEM_PREFETCH(ws + 106080);
-      CHEM_PREFETCH(ws + 131072);
+      CHEM_PREFETCH(ws + 110528);
+      CHEM_PREFETCH(ws + 110560);
+      CHEM_PREFETCH(ws + 110592);
+      CHEM_PREFETCH(ws + 110624);
+      CHEM_PREFETCH(ws + 110656);
+      CHEM_PREFETCH(ws + 110688);
+      CHEM_PREFETCH(ws + 110720);
+      CHEM_PREFETCH(ws + 110752);
+      CHEM_PREFETCH(ws + 110784);
+      CHEM_PREFETCH(ws + 110816);
+      CHEM_PREFETCH(ws + 110848);
+      CHEM_PREFETCH(ws + 135840);
       double x = b[4192];
       x = fma(-CHEM_LDLU(lu + 32064), b[4224], x);
       x = fma(-CHEM_LDLU(lu + 32096), b[4256], x);
@@ -2757,18 +2757,18 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[4192] = x * CHEM_LDLU(vd + 4192);
     }
     {
-      CHEM_PREFETCH(ws + 106112);
-      CHEM_PREFETCH(ws + 106144);
-      CHEM_PREFETCH(ws + 106176);
-      CHEM_PREFETCH(ws + 106208);
-      CHEM_PREFETCH(ws + 106240);
-      CHEM_PREFETCH(ws + 106272);
-      CHEM_PREFETCH(ws + 106304);
-      CHEM_PREFETCH(ws + 106336);
-      CHEM_PREFETCH(ws + 106368);
-      CHEM_PREFETCH(ws + 106400);
-      CHEM_PREFETCH(ws + 106432);
-      CHEM_PREFETCH(ws + 131040);
+      CHEM_PREFETCH(ws + 110880);
+      CHEM_PREFETCH(ws + 110912);
+      CHEM_PREFETCH(ws + 110944);
+      CHEM_PREFETCH(ws + 110976);
+      CHEM_PREFETCH(ws + 111008);
+      CHEM_PREFETCH(ws + 111040);
+      CHEM_PREFETCH(ws + 111072);
+      CHEM_PREFETCH(ws + 111104);
+      CHEM_PREFETCH(ws + 111136);
+      CHEM_PREFETCH(ws + 111168);
+      CHEM_PREFETCH(ws + 111200);
+      CHEM_PREFETCH(ws + 135808);
       double x = b[4160];
       x = fma(-CHEM_LDLU(lu + 32512), b[4224], x);
       x = fma(-CHEM_LDLU(lu + 32544), b[4320], x);
@@ -2785,18 +2785,18 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[4160] = x * CHEM_LDLU(vd + 4160);
     }
     {
-      CHEM_PREFETCH(ws + 106464);
-      CHEM_PREFETCH(ws + 106496);
-      CHEM_PREFETCH(ws + 106528);
-      CHEM_PREFETCH(ws + 106560);
-      CHEM_PREFETCH(ws + 106592);
-      CHEM_PREFETCH(ws + 106624);
-      CHEM_PREFETCH(ws + 106656);
-      CHEM_PREFETCH(ws + 106688);
-      CHEM_PREFETCH(ws + 106720);
-      CHEM_PREFETCH(ws + 106752);
-      CHEM_PREFETCH(ws + 106784);
-      CHEM_PREFETCH(ws + 131008);
+      CHEM_PREFETCH(ws + 111232);
+      CHEM_PREFETCH(ws + 111264);
+      CHEM_PREFETCH(ws + 111296);
+      CHEM_PREFETCH(ws + 111328);
+      CHEM_PREFETCH(ws + 111360);
+      CHEM_PREFETCH(ws + 111392);
+      CHEM_PREFETCH(ws + 111424);
+      CHEM_PREFETCH(ws + 111456);
+      CHEM_PREFETCH(ws + 111488);
+      CHEM_PREFETCH(ws + 111520);
+      CHEM_PREFETCH(ws + 111552);
+      CHEM_PREFETCH(ws + 135776);
       double x = b[4128];
       x = fma(-CHEM_LDLU(lu + 32896), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 32928), b[4224], x);
@@ -2812,19 +2812,19 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[4128] = x * CHEM_LDLU(vd + 4128);
     }
     {
-      CHEM_PREFETCH(ws + 106816);
-      CHEM_PREFETCH(ws + 106848);
-      CHEM_PREFETCH(ws + 106880);
-      CHEM_PREFETCH(ws + 106912);
-      CHEM_PREFETCH(ws + 106944);
-      CHEM_PREFETCH(ws + 106976);
-      CHEM_PREFETCH(ws + 107008);
-      CHEM_PREFETCH(ws + 107040);
-      CHEM_PREFETCH(ws + 107072);
-      CHEM_PREFETCH(ws + 107104);
-      CHEM_PREFETCH(ws + 107136);
-      CHEM_PREFETCH(ws + 107168);
-      CHEM_PREFETCH(ws + 130976);
+      CHEM_PREFETCH(ws + 111584);
+      CHEM_PREFETCH(ws + 111616);
+      CHEM_PREFETCH(ws + 111648);
+      CHEM_PREFETCH(ws + 111680);
+      CHEM_PREFETCH(ws + 111712);
+      CHEM_PREFETCH(ws + 111744);
+      CHEM_PREFETCH(ws + 111776);
+      CHEM_PREFETCH(ws + 111808);
+      CHEM_PREFETCH(ws + 111840);
+      CHEM_PREFETCH(ws + 111872);
+      CHEM_PREFETCH(ws + 111904);
+      CHEM_PREFETCH(ws + 111936);
+      CHEM_PREFETCH(ws + 135744);
       double x = b[4096];
       x = fma(-CHEM_LDLU(lu + 33248), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 33280), b[4224], x);
@@ -2840,17 +2840,17 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[4096] = x * CHEM_LDLU(vd + 4096);
     }
     {
-      CHEM_PREFETCH(ws + 107200);
-      CHEM_PREFETCH(ws + 107232);
-      CHEM_PREFETCH(ws + 107264);
-      CHEM_PREFETCH(ws + 107296);
-      CHEM_PREFETCH(ws + 107328);
-      CHEM_PREFETCH(ws + 107360);
-      CHEM_PREFETCH(ws + 107392);
-      CHEM_PREFETCH(ws + 107424);
-      CHEM_PREFETCH(ws + 107456);
-      CHEM_PREFETCH(ws + 107488);
-      CHEM_PREFETCH(ws + 130944);
+      CHEM_PREFETCH(ws + 111968);
+      CHEM_PREFETCH(ws + 112000);
+      CHEM_PREFETCH(ws + 112032);
+      CHEM_PREFETCH(ws + 112064);
+      CHEM_PREFETCH(ws + 112096);
+      CHEM_PREFETCH(ws + 112128);
+      CHEM_PREFETCH(ws + 112160);
+      CHEM_PREFETCH(ws + 112192);
+      CHEM_PREFETCH(ws + 112224);
+      CHEM_PREFETCH(ws + 112256);
+      CHEM_PREFETCH(ws + 135712);
       double x = b[4064];
       x = fma(-CHEM_LDLU(lu + 33600), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 33632), b[4224], x);
@@ -2866,21 +2866,21 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[4064] = x * CHEM_LDLU(vd + 4064);
     }
     {
-      CHEM_PREFETCH(ws + 107520);
-      CHEM_PREFETCH(ws + 107552);
-      CHEM_PREFETCH(ws + 107584);
-      CHEM_PREFETCH(ws + 107616);
-      CHEM_PREFETCH(ws + 107648);
-      CHEM_PREFETCH(ws + 107680);
-      CHEM_PREFETCH(ws + 107712);
-      CHEM_PREFETCH(ws + 107744);
-      CHEM_PREFETCH(ws + 107776);
-      CHEM_PREFETCH(ws + 107808);
-      CHEM_PREFETCH(ws + 107840);
-      CHEM_PREFETCH(ws + 107872);
-      CHEM_PREFETCH(ws + 107904);
-      CHEM_PREFETCH(ws + 107936);
-      CHEM_PREFETCH(ws + 130912);
+      CHEM_PREFETCH(ws + 112288);
+      CHEM_PREFETCH(ws + 112320);
+      CHEM_PREFETCH(ws + 112352);
+      CHEM_PREFETCH(ws + 112384);
+      CHEM_PREFETCH(ws + 112416);
+      CHEM_PREFETCH(ws + 112448);
+      CHEM_PREFETCH(ws + 112480);
+      CHEM_PREFETCH(ws + 112512);
+      CHEM_PREFETCH(ws + 112544);
+      CHEM_PREFETCH(ws + 112576);
+      CHEM_PREFETCH(ws + 112608);
+      CHEM_PREFETCH(ws + 112640);
+      CHEM_PREFETCH(ws + 112672);
+      CHEM_PREFETCH(ws + 112704);
+      CHEM_PREFETCH(ws + 135680);
       double x = b[4032];
       x = fma(-CHEM_LDLU(lu + 33952), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 33984), b[4224], x);
@@ -2897,16 +2897,16 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[4032] = x * CHEM_LDLU(vd + 4032);
     }
     {
-      CHEM_PREFETCH(ws + 107968);
-      CHEM_PREFETCH(ws + 108000);
-      CHEM_PREFETCH(ws + 108032);
-      CHEM_PREFETCH(ws + 108064);
-      CHEM_PREFETCH(ws + 108096);
-      CHEM_PREFETCH(ws + 108128);
-      CHEM_PREFETCH(ws + 108160);
-      CHEM_PREFETCH(ws + 108192);
-      CHEM_PREFETCH(ws + 108224);
-      CHEM_PREFETCH(ws + 130880);
+      CHEM_PREFETCH(ws + 112736);
+      CHEM_PREFETCH(ws + 112768);
+      CHEM_PREFETCH(ws + 112800);
+      CHEM_PREFETCH(ws + 112832);
+      CHEM_PREFETCH(ws + 112864);
+      CHEM_PREFETCH(ws + 112896);
+      CHEM_PREFETCH(ws + 112928);
+      CHEM_PREFETCH(ws + 112960);
+      CHEM_PREFETCH(ws + 112992);
+      CHEM_PREFETCH(ws + 135648);
       double x = b[4000];
       x = fma(-CHEM_LDLU(lu + 34336), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 34368), b[4320], x);
@@ -2921,23 +2921,23 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[4000] = x * CHEM_LDLU(vd + 4000);
     }
     {
-      CHEM_PREFETCH(ws + 108256);
-      CHEM_PREFETCH(ws + 108288);
-      CHEM_PREFETCH(ws + 108320);
-      CHEM_PREFETCH(ws + 108352);
-      CHEM_PREFETCH(ws + 108384);
-      CHEM_PREFETCH(ws + 108416);
-      CHEM_PREFETCH(ws + 108448);
-      CHEM_PREFETCH(ws + 108480);
-      CHEM_PREFETCH(ws + 108512);
-      CHEM_PREFETCH(ws + 108544);
-      CHEM_PREFETCH(ws + 108576);
-      CHEM_PREFETCH(ws + 108608);
-      CHEM_PREFETCH(ws + 108640);
-      CHEM_PREFETCH(ws + 108672);
-      CHEM_PREFETCH(ws + 108704);
-      CHEM_PREFETCH(ws + 108736);
-      CHEM_PREFETCH(ws + 130848);
+      CHEM_PREFETCH(ws + 113024);
+      CHEM_PREFETCH(ws + 113056);
+      CHEM_PREFETCH(ws + 113088);
+      CHEM_PREFETCH(ws + 113120);
+      CHEM_PREFETCH(ws + 113152);
+      CHEM_PREFETCH(ws + 113184);
+      CHEM_PREFETCH(ws + 113216);
+      CHEM_PREFETCH(ws + 113248);
+      CHEM_PREFETCH(ws + 113280);
+      CHEM_PREFETCH(ws + 113312);
+      CHEM_PREFETCH(ws + 113344);
+      CHEM_PREFETCH(ws + 113376);
+      CHEM_PREFETCH(ws + 113408);
+      CHEM_PREFETCH(ws + 113440);
+      CHEM_PREFETCH(ws + 113472);
+      CHEM_PREFETCH(ws + 113504);
+      CHEM_PREFETCH(ws + 135616);
       double x = b[3968];
       x = fma(-CHEM_LDLU(lu + 34656), b[4064], x);
       x = fma(-CHEM_LDLU(lu + 34688), b[4128], x);
@@ -2956,16 +2956,16 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3968] = x * CHEM_LDLU(vd + 3968);
     }
     {
-      CHEM_PREFETCH(ws + 108768);
-      CHEM_PREFETCH(ws + 108800);
-      CHEM_PREFETCH(ws + 108832);
-      CHEM_PREFETCH(ws + 108864);
-      CHEM_PREFETCH(ws + 108896);
-      CHEM_PREFETCH(ws + 108928);
-      CHEM_PREFETCH(ws + 108960);
-      CHEM_PREFETCH(ws + 108992);
-      CHEM_PREFETCH(ws + 109024);
-      CHEM_PREFETCH(ws + 130816);
+      CHEM_PREFETCH(ws + 113536);
+      CHEM_PREFETCH(ws + 113568);
+      CHEM_PREFETCH(ws + 113600);
+      CHEM_PREFETCH(ws + 113632);
+      CHEM_PREFETCH(ws + 113664);
+      CHEM_PREFETCH(ws + 113696);
+      CHEM_PREFETCH(ws + 113728);
+      CHEM_PREFETCH(ws + 113760);
+      CHEM_PREFETCH(ws + 113792);
+      CHEM_PREFETCH(ws + 135584);
       double x = b[3936];
       x = fma(-CHEM_LDLU(lu + 35104), b[4320], x);
       x = fma(-CHEM_LDLU(lu + 35136), b[4384], x);
@@ -2979,17 +2979,17 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3936] = x * CHEM_LDLU(vd + 3936);
     }
     {
-      CHEM_PREFETCH(ws + 109056);
-      CHEM_PREFETCH(ws + 109088);
-      CHEM_PREFETCH(ws + 109120);
-      CHEM_PREFETCH(ws + 109152);
-      CHEM_PREFETCH(ws + 109184);
-      CHEM_PREFETCH(ws + 109216);
-      CHEM_PREFETCH(ws + 109248);
-      CHEM_PREFETCH(ws + 109280);
-      CHEM_PREFETCH(ws + 109312);
-      CHEM_PREFETCH(ws + 109344);
-      CHEM_PREFETCH(ws + 130784);
+      CHEM_PREFETCH(ws + 113824);
+      CHEM_PREFETCH(ws + 113856);
+      CHEM_PREFETCH(ws + 113888);
+      CHEM_PREFETCH(ws + 113920);
+      CHEM_PREFETCH(ws + 113952);
+      CHEM_PREFETCH(ws + 113984);
+      CHEM_PREFETCH(ws + 114016);
+      CHEM_PREFETCH(ws + 114048);
+      CHEM_PREFETCH(ws + 114080);
+      CHEM_PREFETCH(ws + 114112);
+      CHEM_PREFETCH(ws + 135552);
       double x = b[3904];
       x = fma(-CHEM_LDLU(lu + 35392), b[3936], x);
       x = fma(-CHEM_LDLU(lu + 35424), b[4096], x);
@@ -3010,15 +3010,15 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3904] = x * CHEM_LDLU(vd + 3904);
     }
     {
-      CHEM_PREFETCH(ws + 109376);
-      CHEM_PREFETCH(ws + 109408);
-      CHEM_PREFETCH(ws + 109440);
-      CHEM_PREFETCH(ws + 109472);
-      CHEM_PREFETCH(ws + 109504);
-      CHEM_PREFETCH(ws + 109536);
-      CHEM_PREFETCH(ws + 109568);
-      CHEM_PREFETCH(ws + 109600);
-      CHEM_PREFETCH(ws + 130752);
+      CHEM_PREFETCH(ws + 114144);
+      CHEM_PREFETCH(ws + 114176);
+      CHEM_PREFETCH(ws + 114208);
+      CHEM_PREFETCH(ws + 114240);
+      CHEM_PREFETCH(ws + 114272);
+      CHEM_PREFETCH(ws + 114304);
+      CHEM_PREFETCH(ws + 114336);
+      CHEM_PREFETCH(ws + 114368);
+      CHEM_PREFETCH(ws + 135520);
       double x = b[3872];
       x = fma(-CHEM_LDLU(lu + 35904), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 35936), b[4320], x);
@@ -3032,18 +3032,18 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3872] = x * CHEM_LDLU(vd + 3872);
     }
     {
-      CHEM_PREFETCH(ws + 109632);
-      CHEM_PREFETCH(ws + 109664);
-      CHEM_PREFETCH(ws + 109696);
-      CHEM_PREFETCH(ws + 109728);
-      CHEM_PREFETCH(ws + 109760);
-      CHEM_PREFETCH(ws + 109792);
-      CHEM_PREFETCH(ws + 109824);
-      CHEM_PREFETCH(ws + 109856);
-      CHEM_PREFETCH(ws + 109888);
-      CHEM_PREFETCH(ws + 109920);
-      CHEM_PREFETCH(ws + 109952);
-      CHEM_PREFETCH(ws + 130720);
+      CHEM_PREFETCH(ws + 114400);
+      CHEM_PREFETCH(ws + 114432);
+      CHEM_PREFETCH(ws + 114464);
+      CHEM_PREFETCH(ws + 114496);
+      CHEM_PREFETCH(ws + 114528);
+      CHEM_PREFETCH(ws + 114560);
+      CHEM_PREFETCH(ws + 114592);
+      CHEM_PREFETCH(ws + 114624);
+      CHEM_PREFETCH(ws + 114656);
+      CHEM_PREFETCH(ws + 114688);
+      CHEM_PREFETCH(ws + 114720);
+      CHEM_PREFETCH(ws + 135488);
       double x = b[3840];
       x = fma(-CHEM_LDLU(lu + 36192), b[3872], x);
       x = fma(-CHEM_LDLU(lu + 36224), b[4160], x);
@@ -3058,17 +3058,17 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3840] = x * CHEM_LDLU(vd + 3840);
     }
     {
-      CHEM_PREFETCH(ws + 109984);
-      CHEM_PREFETCH(ws + 110016);
-      CHEM_PREFETCH(ws + 110048);
-      CHEM_PREFETCH(ws + 110080);
-      CHEM_PREFETCH(ws + 110112);
-      CHEM_PREFETCH(ws + 110144);
-      CHEM_PREFETCH(ws + 110176);
-      CHEM_PREFETCH(ws + 110208);
-      CHEM_PREFETCH(ws + 110240);
-      CHEM_PREFETCH(ws + 110272);
-      CHEM_PREFETCH(ws + 130688);
+      CHEM_PREFETCH(ws + 114752);
+      CHEM_PREFETCH(ws + 114784);
+      CHEM_PREFETCH(ws + 114816);
+      CHEM_PREFETCH(ws + 114848);
+      CHEM_PREFETCH(ws + 114880);
+      CHEM_PREFETCH(ws + 114912);
+      CHEM_PREFETCH(ws + 114944);
+      CHEM_PREFETCH(ws + 114976);
+      CHEM_PREFETCH(ws + 115008);
+      CHEM_PREFETCH(ws + 115040);
+      CHEM_PREFETCH(ws + 135456);
       double x = b[3808];
       x = fma(-CHEM_LDLU(lu + 36512), b[4320], x);
       x = fma(-CHEM_LDLU(lu + 36544), b[4384], x);
@@ -3081,8 +3081,8 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3808] = x * CHEM_LDLU(vd + 3808);
     }
     {
-      CHEM_PREFETCH(ws + 110304);
-      CHEM_PREFETCH(ws + 130656);
+      CHEM_PREFETCH(ws + 115072);
+      CHEM_PREFETCH(ws + 135424);
       double x = b[3776];
       x = fma(-CHEM_LDLU(lu + 36768), b[3872], x);
       x = fma(-CHEM_LDLU(lu + 36800), b[4160], x);
@@ -3098,9 +3098,9 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3776] = x * CHEM_LDLU(vd + 3776);
     }
     {
-      CHEM_PREFETCH(ws + 110336);
-      CHEM_PREFETCH(ws + 110368);
-      CHEM_PREFETCH(ws + 130624);
+      CHEM_PREFETCH(ws + 115104);
+      CHEM_PREFETCH(ws + 115136);
+      CHEM_PREFETCH(ws + 135392);
       double x = b[3744];
       x = fma(-CHEM_LDLU(lu + 37120), b[3872], x);
       x = fma(-CHEM_LDLU(lu + 37152), b[3936], x);
@@ -3115,44 +3115,44 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3744] = x * CHEM_LDLU(vd + 3744);
     }
     {
-      CHEM_PREFETCH(ws + 110400);
-      CHEM_PREFETCH(ws + 110432);
-      CHEM_PREFETCH(ws + 110464);
-      CHEM_PREFETCH(ws + 110496);
-      CHEM_PREFETCH(ws + 110528);
-      CHEM_PREFETCH(ws + 110560);
-      CHEM_PREFETCH(ws + 110592);
-      CHEM_PREFETCH(ws + 110624);
-      CHEM_PREFETCH(ws + 110656);
-      CHEM_PREFETCH(ws + 110688);
-      CHEM_PREFETCH(ws + 110720);
-      CHEM_PREFETCH(ws + 110752);
-      CHEM_PREFETCH(ws + 110784);
-      CHEM_PREFETCH(ws + 130592);
+      CHEM_PREFETCH(ws + 115168);
+      CHEM_PREFETCH(ws + 115200);
+      CHEM_PREFETCH(ws + 115232);
+      CHEM_PREFETCH(ws + 115264);
+      CHEM_PREFETCH(ws + 115296);
+      CHEM_PREFETCH(ws + 115328);
+      CHEM_PREFETCH(ws + 115360);
+      CHEM_PREFETCH(ws + 115392);
+      CHEM_PREFETCH(ws + 115424);
+      CHEM_PREFETCH(ws + 115456);
+      CHEM_PREFETCH(ws + 115488);
+      CHEM_PREFETCH(ws + 115520);
+      CHEM_PREFETCH(ws + 115552);
+      CHEM_PREFETCH(ws + 135360);
       double x = b[3712];
       x = fma(-CHEM_LDLU(lu + 37440), b[4736], x);
       b[3712] = x * CHEM_LDLU(vd + 3712);
     }
     {
-      CHEM_PREFETCH(ws + 110816);
-      CHEM_PREFETCH(ws + 110848);
-      CHEM_PREFETCH(ws + 110880);
-      CHEM_PREFETCH(ws + 110912);
-      CHEM_PREFETCH(ws + 110944);
-      CHEM_PREFETCH(ws + 130560);
+      CHEM_PREFETCH(ws + 115584);
+      CHEM_PREFETCH(ws + 115616);
+      CHEM_PREFETCH(ws + 115648);
+      CHEM_PREFETCH(ws + 115680);
+      CHEM_PREFETCH(ws + 115712);
+      CHEM_PREFETCH(ws + 135328);
       double x = b[3680];
       x = fma(-CHEM_LDLU(lu + 37472), b[3712], x);
       x = fma(-CHEM_LDLU(lu + 37504), b[4736], x);
       b[3680] = x * CHEM_LDLU(vd + 3680);
     }
     {
-      CHEM_PREFETCH(ws + 110976);
-      CHEM_PREFETCH(ws + 111008);
-      CHEM_PREFETCH(ws + 111040);
-      CHEM_PREFETCH(ws + 111072);
-      CHEM_PREFETCH(ws + 111104);
-      CHEM_PREFETCH(ws + 111136);
-      CHEM_PREFETCH(ws + 130528);
+      CHEM_PREFETCH(ws + 115744);
+      CHEM_PREFETCH(ws + 115776);
+      CHEM_PREFETCH(ws + 115808);
+      CHEM_PREFETCH(ws + 115840);
+      CHEM_PREFETCH(ws + 115872);
+      CHEM_PREFETCH(ws + 115904);
+      CHEM_PREFETCH(ws + 135296);
       double x = b[3648];
       x = fma(-CHEM_LDLU(lu + 37536), b[3872], x);
       x = fma(-CHEM_LDLU(lu + 37568), b[4160], x);
@@ -3170,17 +3170,17 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3648] = x * CHEM_LDLU(vd + 3648);
     }
     {
-      CHEM_PREFETCH(ws + 111168);
-      CHEM_PREFETCH(ws + 111200);
-      CHEM_PREFETCH(ws + 111232);
-      CHEM_PREFETCH(ws + 111264);
-      CHEM_PREFETCH(ws + 111296);
-      CHEM_PREFETCH(ws + 111328);
-      CHEM_PREFETCH(ws + 111360);
-      CHEM_PREFETCH(ws + 111392);
-      CHEM_PREFETCH(ws + 111424);
-      CHEM_PREFETCH(ws + 111456);
-      CHEM_PREFETCH(ws + 130496);
+      CHEM_PREFETCH(ws + 115936);
+      CHEM_PREFETCH(ws + 115968);
+      CHEM_PREFETCH(ws + 116000);
+      CHEM_PREFETCH(ws + 116032);
+      CHEM_PREFETCH(ws + 116064);
+      CHEM_PREFETCH(ws + 116096);
+      CHEM_PREFETCH(ws + 116128);
+      CHEM_PREFETCH(ws + 116160);
+      CHEM_PREFETCH(ws + 116192);
+      CHEM_PREFETCH(ws + 116224);
+      CHEM_PREFETCH(ws + 135264);
       double x = b[3616];
       x = fma(-CHEM_LDLU(lu + 37952), b[4544], x);
       x = fma(-CHEM_LDLU(lu + 37984), b[4608], x);
@@ -3190,15 +3190,15 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3616] = x * CHEM_LDLU(vd + 3616);
     }
     {
-      CHEM_PREFETCH(ws + 111488);
-      CHEM_PREFETCH(ws + 111520);
-      CHEM_PREFETCH(ws + 111552);
-      CHEM_PREFETCH(ws + 111584);
-      CHEM_PREFETCH(ws + 111616);
-      CHEM_PREFETCH(ws + 111648);
-      CHEM_PREFETCH(ws + 111680);
-      CHEM_PREFETCH(ws + 111712);
-      CHEM_PREFETCH(ws + 130464);
+      CHEM_PREFETCH(ws + 116256);
+      CHEM_PREFETCH(ws + 116288);
+      CHEM_PREFETCH(ws + 116320);
+      CHEM_PREFETCH(ws + 116352);
+      CHEM_PREFETCH(ws + 116384);
+      CHEM_PREFETCH(ws + 116416);
+      CHEM_PREFETCH(ws + 116448);
+      CHEM_PREFETCH(ws + 116480);
+      CHEM_PREFETCH(ws + 135232);
       double x = b[3584];
       x = fma(-CHEM_LDLU(lu + 38112), b[4384], x);
       x = fma(-CHEM_LDLU(lu + 38144), b[4448], x);
@@ -3209,13 +3209,13 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3584] = x * CHEM_LDLU(vd + 3584);
     }
     {
-      CHEM_PREFETCH(ws + 111744);
-      CHEM_PREFETCH(ws + 111776);
-      CHEM_PREFETCH(ws + 111808);
-      CHEM_PREFETCH(ws + 111840);
-      CHEM_PREFETCH(ws + 111872);
-      CHEM_PREFETCH(ws + 111904);
-      CHEM_PREFETCH(ws + 130432);
+      CHEM_PREFETCH(ws + 116512);
+      CHEM_PREFETCH(ws + 116544);
+      CHEM_PREFETCH(ws + 116576);
+      CHEM_PREFETCH(ws + 116608);
+      CHEM_PREFETCH(ws + 116640);
+      CHEM_PREFETCH(ws + 116672);
+      CHEM_PREFETCH(ws + 135200);
       double x = b[3552];
       x = fma(-CHEM_LDLU(lu + 38304), b[3872], x);
       x = fma(-CHEM_LDLU(lu + 38336), b[4160], x);
@@ -3230,18 +3230,18 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3552] = x * CHEM_LDLU(vd + 3552);
     }
     {
-      CHEM_PREFETCH(ws + 111936);
-      CHEM_PREFETCH(ws + 111968);
-      CHEM_PREFETCH(ws + 112000);
-      CHEM_PREFETCH(ws + 112032);
-      CHEM_PREFETCH(ws + 112064);
-      CHEM_PREFETCH(ws + 112096);
-      CHEM_PREFETCH(ws + 112128);
-      CHEM_PREFETCH(ws + 112160);
-      CHEM_PREFETCH(ws + 112192);
-      CHEM_PREFETCH(ws + 112224);
-      CHEM_PREFETCH(ws + 112256);
-      CHEM_PREFETCH(ws + 130400);
+      CHEM_PREFETCH(ws + 116704);
+      CHEM_PREFETCH(ws + 116736);
+      CHEM_PREFETCH(ws + 116768);
+      CHEM_PREFETCH(ws + 116800);
+      CHEM_PREFETCH(ws + 116832);
+      CHEM_PREFETCH(ws + 116864);
+      CHEM_PREFETCH(ws + 116896);
+      CHEM_PREFETCH(ws + 116928);
+      CHEM_PREFETCH(ws + 116960);
+      CHEM_PREFETCH(ws + 116992);
+      CHEM_PREFETCH(ws + 117024);
+      CHEM_PREFETCH(ws + 135168);
       double x = b[3520];
       x = fma(-CHEM_LDLU(lu + 38624), b[4320], x);
       x = fma(-CHEM_LDLU(lu + 38656), b[4384], x);
@@ -3254,16 +3254,16 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3520] = x * CHEM_LDLU(vd + 3520);
     }
     {
-      CHEM_PREFETCH(ws + 112288);
-      CHEM_PREFETCH(ws + 112320);
-      CHEM_PREFETCH(ws + 112352);
-      CHEM_PREFETCH(ws + 112384);
-      CHEM_PREFETCH(ws + 112416);
-      CHEM_PREFETCH(ws + 112448);
-      CHEM_PREFETCH(ws + 112480);
-      CHEM_PREFETCH(ws + 112512);
-      CHEM_PREFETCH(ws + 112544);
-      CHEM_PREFETCH(ws + 130368);
+      CHEM_PREFETCH(ws + 117056);
+      CHEM_PREFETCH(ws + 117088);
+      CHEM_PREFETCH(ws + 117120);
+      CHEM_PREFETCH(ws + 117152);
+      CHEM_PREFETCH(ws + 117184);
+      CHEM_PREFETCH(ws + 117216);
+      CHEM_PREFETCH(ws + 117248);
+      CHEM_PREFETCH(ws + 117280);
+      CHEM_PREFETCH(ws + 117312);
+      CHEM_PREFETCH(ws + 135136);
       double x = b[3488];
       x = fma(-CHEM_LDLU(lu + 38880), b[4384], x);
       x = fma(-CHEM_LDLU(lu + 38912), b[4448], x);
@@ -3274,13 +3274,13 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3488] = x * CHEM_LDLU(vd + 3488);
     }
     {
-      CHEM_PREFETCH(ws + 112576);
-      CHEM_PREFETCH(ws + 112608);
-      CHEM_PREFETCH(ws + 112640);
-      CHEM_PREFETCH(ws + 112672);
-      CHEM_PREFETCH(ws + 112704);
-      CHEM_PREFETCH(ws + 112736);
-      CHEM_PREFETCH(ws + 130336);
+      CHEM_PREFETCH(ws + 117344);
+      CHEM_PREFETCH(ws + 117376);
+      CHEM_PREFETCH(ws + 117408);
+      CHEM_PREFETCH(ws + 117440);
+      CHEM_PREFETCH(ws + 117472);
+      CHEM_PREFETCH(ws + 117504);
+      CHEM_PREFETCH(ws + 135104);
       double x = b[3456];
       x = fma(-CHEM_LDLU(lu + 39072), b[3520], x);
       x = fma(-CHEM_LDLU(lu + 39104), b[3552], x);
@@ -3296,15 +3296,15 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3456] = x * CHEM_LDLU(vd + 3456);
     }
     {
-      CHEM_PREFETCH(ws + 112768);
-      CHEM_PREFETCH(ws + 112800);
-      CHEM_PREFETCH(ws + 112832);
-      CHEM_PREFETCH(ws + 112864);
-      CHEM_PREFETCH(ws + 112896);
-      CHEM_PREFETCH(ws + 112928);
-      CHEM_PREFETCH(ws + 112960);
-      CHEM_PREFETCH(ws + 112992);
-      CHEM_PREFETCH(ws + 130304);
+      CHEM_PREFETCH(ws + 117536);
+      CHEM_PREFETCH(ws + 117568);
+      CHEM_PREFETCH(ws + 117600);
+      CHEM_PREFETCH(ws + 117632);
+      CHEM_PREFETCH(ws + 117664);
+      CHEM_PREFETCH(ws + 117696);
+      CHEM_PREFETCH(ws + 117728);
+      CHEM_PREFETCH(ws + 117760);
+      CHEM_PREFETCH(ws + 135072);
       double x = b[3424];
       x = fma(-CHEM_LDLU(lu + 39424), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 39456), b[4320], x);
@@ -3318,12 +3318,12 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3424] = x * CHEM_LDLU(vd + 3424);
     }
     {
-      CHEM_PREFETCH(ws + 113024);
-      CHEM_PREFETCH(ws + 113056);
-      CHEM_PREFETCH(ws + 113088);
-      CHEM_PREFETCH(ws + 113120);
-      CHEM_PREFETCH(ws + 113152);
-      CHEM_PREFETCH(ws + 130272);
+      CHEM_PREFETCH(ws + 117792);
+      CHEM_PREFETCH(ws + 117824);
+      CHEM_PREFETCH(ws + 117856);
+      CHEM_PREFETCH(ws + 117888);
+      CHEM_PREFETCH(ws + 117920);
+      CHEM_PREFETCH(ws + 135040);
       double x = b[3392];
       x = fma(-CHEM_LDLU(lu + 39712), b[3872], x);
       x = fma(-CHEM_LDLU(lu + 39744), b[4224], x);
@@ -3334,13 +3334,13 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3392] = x * CHEM_LDLU(vd + 3392);
     }
     {
-      CHEM_PREFETCH(ws + 113184);
-      CHEM_PREFETCH(ws + 113216);
-      CHEM_PREFETCH(ws + 113248);
-      CHEM_PREFETCH(ws + 113280);
-      CHEM_PREFETCH(ws + 113312);
-      CHEM_PREFETCH(ws + 113344);
-      CHEM_PREFETCH(ws + 130240);
+      CHEM_PREFETCH(ws + 117952);
+      CHEM_PREFETCH(ws + 117984);
+      CHEM_PREFETCH(ws + 118016);
+      CHEM_PREFETCH(ws + 118048);
+      CHEM_PREFETCH(ws + 118080);
+      CHEM_PREFETCH(ws + 118112);
+      CHEM_PREFETCH(ws + 135008);
       double x = b[3360];
       x = fma(-CHEM_LDLU(lu + 39904), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 39936), b[4320], x);
@@ -3353,11 +3353,11 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3360] = x * CHEM_LDLU(vd + 3360);
     }
     {
-      CHEM_PREFETCH(ws + 113376);
-      CHEM_PREFETCH(ws + 113408);
-      CHEM_PREFETCH(ws + 113440);
-      CHEM_PREFETCH(ws + 113472);
-      CHEM_PREFETCH(ws + 130208);
+      CHEM_PREFETCH(ws + 118144);
+      CHEM_PREFETCH(ws + 118176);
+      CHEM_PREFETCH(ws + 118208);
+      CHEM_PREFETCH(ws + 118240);
+      CHEM_PREFETCH(ws + 134976);
       double x = b[3328];
       x = fma(-CHEM_LDLU(lu + 40160), b[3616], x);
       x = fma(-CHEM_LDLU(lu + 40192), b[4608], x);
@@ -3367,15 +3367,15 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3328] = x * CHEM_LDLU(vd + 3328);
     }
     {
-      CHEM_PREFETCH(ws + 113504);
-      CHEM_PREFETCH(ws + 113536);
-      CHEM_PREFETCH(ws + 113568);
-      CHEM_PREFETCH(ws + 113600);
-      CHEM_PREFETCH(ws + 113632);
-      CHEM_PREFETCH(ws + 113664);
-      CHEM_PREFETCH(ws + 113696);
-      CHEM_PREFETCH(ws + 113728);
-      CHEM_PREFETCH(ws + 130176);
+      CHEM_PREFETCH(ws + 118272);
+      CHEM_PREFETCH(ws + 118304);
+      CHEM_PREFETCH(ws + 118336);
+      CHEM_PREFETCH(ws + 118368);
+      CHEM_PREFETCH(ws + 118400);
+      CHEM_PREFETCH(ws + 118432);
+      CHEM_PREFETCH(ws + 118464);
+      CHEM_PREFETCH(ws + 118496);
+      CHEM_PREFETCH(ws + 134944);
       double x = b[3296];
       x = fma(-CHEM_LDLU(lu + 40320), b[3424], x);
       x = fma(-CHEM_LDLU(lu + 40352), b[4384], x);
@@ -3386,10 +3386,10 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3296] = x * CHEM_LDLU(vd + 3296);
     }
     {
-      CHEM_PREFETCH(ws + 113760);
-      CHEM_PREFETCH(ws + 113792);
-      CHEM_PREFETCH(ws + 113824);
-      CHEM_PREFETCH(ws + 130144);
+      CHEM_PREFETCH(ws + 118528);
+      CHEM_PREFETCH(ws + 118560);
+      CHEM_PREFETCH(ws + 118592);
+      CHEM_PREFETCH(ws + 134912);
       double x = b[3264];
       x = fma(-CHEM_LDLU(lu + 40512), b[4384], x);
       x = fma(-CHEM_LDLU(lu + 40544), b[4544], x);
@@ -3398,11 +3398,11 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3264] = x * CHEM_LDLU(vd + 3264);
     }
     {
-      CHEM_PREFETCH(ws + 113856);
-      CHEM_PREFETCH(ws + 113888);
-      CHEM_PREFETCH(ws + 113920);
-      CHEM_PREFETCH(ws + 113952);
-      CHEM_PREFETCH(ws + 130112);
+      CHEM_PREFETCH(ws + 118624);
+      CHEM_PREFETCH(ws + 118656);
+      CHEM_PREFETCH(ws + 118688);
+      CHEM_PREFETCH(ws + 118720);
+      CHEM_PREFETCH(ws + 134880);
       double x = b[3232];
       x = fma(-CHEM_LDLU(lu + 40640), b[3424], x);
       x = fma(-CHEM_LDLU(lu + 40672), b[3552], x);
@@ -3415,14 +3415,14 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3232] = x * CHEM_LDLU(vd + 3232);
     }
     {
-      CHEM_PREFETCH(ws + 113984);
-      CHEM_PREFETCH(ws + 114016);
-      CHEM_PREFETCH(ws + 114048);
-      CHEM_PREFETCH(ws + 114080);
-      CHEM_PREFETCH(ws + 114112);
-      CHEM_PREFETCH(ws + 114144);
-      CHEM_PREFETCH(ws + 114176);
-      CHEM_PREFETCH(ws + 130080);
+      CHEM_PREFETCH(ws + 118752);
+      CHEM_PREFETCH(ws + 118784);
+      CHEM_PREFETCH(ws + 118816);
+      CHEM_PREFETCH(ws + 118848);
+      CHEM_PREFETCH(ws + 118880);
+      CHEM_PREFETCH(ws + 118912);
+      CHEM_PREFETCH(ws + 118944);
+      CHEM_PREFETCH(ws + 134848);
       double x = b[3200];
       x = fma(-CHEM_LDLU(lu + 40896), b[3680], x);
       x = fma(-CHEM_LDLU(lu + 40928), b[3712], x);
@@ -3430,12 +3430,12 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3200] = x * CHEM_LDLU(vd + 3200);
     }
     {
-      CHEM_PREFETCH(ws + 114208);
-      CHEM_PREFETCH(ws + 114240);
-      CHEM_PREFETCH(ws + 114272);
-      CHEM_PREFETCH(ws + 114304);
-      CHEM_PREFETCH(ws + 114336);
-      CHEM_PREFETCH(ws + 130048);
+      CHEM_PREFETCH(ws + 118976);
+      CHEM_PREFETCH(ws + 119008);
+      CHEM_PREFETCH(ws + 119040);
+      CHEM_PREFETCH(ws + 119072);
+      CHEM_PREFETCH(ws + 119104);
+      CHEM_PREFETCH(ws + 134816);
       double x = b[3168];
       x = fma(-CHEM_LDLU(lu + 40992), b[3200], x);
       x = fma(-CHEM_LDLU(lu + 41024), b[3680], x);
@@ -3444,11 +3444,11 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3168] = x * CHEM_LDLU(vd + 3168);
     }
     {
-      CHEM_PREFETCH(ws + 114368);
-      CHEM_PREFETCH(ws + 114400);
-      CHEM_PREFETCH(ws + 114432);
-      CHEM_PREFETCH(ws + 114464);
-      CHEM_PREFETCH(ws + 130016);
+      CHEM_PREFETCH(ws + 119136);
+      CHEM_PREFETCH(ws + 119168);
+      CHEM_PREFETCH(ws + 119200);
+      CHEM_PREFETCH(ws + 119232);
+      CHEM_PREFETCH(ws + 134784);
       double x = b[3136];
       x = fma(-CHEM_LDLU(lu + 41120), b[3424], x);
       x = fma(-CHEM_LDLU(lu + 41152), b[4160], x);
@@ -3460,12 +3460,12 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3136] = x * CHEM_LDLU(vd + 3136);
     }
     {
-      CHEM_PREFETCH(ws + 114496);
-      CHEM_PREFETCH(ws + 114528);
-      CHEM_PREFETCH(ws + 114560);
-      CHEM_PREFETCH(ws + 114592);
-      CHEM_PREFETCH(ws + 114624);
-      CHEM_PREFETCH(ws + 129984);
+      CHEM_PREFETCH(ws + 119264);
+      CHEM_PREFETCH(ws + 119296);
+      CHEM_PREFETCH(ws + 119328);
+      CHEM_PREFETCH(ws + 119360);
+      CHEM_PREFETCH(ws + 119392);
+      CHEM_PREFETCH(ws + 134752);
       double x = b[3104];
       x = fma(-CHEM_LDLU(lu + 41344), b[4384], x);
       x = fma(-CHEM_LDLU(lu + 41376), b[4448], x);
@@ -3475,12 +3475,12 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3104] = x * CHEM_LDLU(vd + 3104);
     }
     {
-      CHEM_PREFETCH(ws + 114656);
-      CHEM_PREFETCH(ws + 114688);
-      CHEM_PREFETCH(ws + 114720);
-      CHEM_PREFETCH(ws + 114752);
-      CHEM_PREFETCH(ws + 114784);
-      CHEM_PREFETCH(ws + 129952);
+      CHEM_PREFETCH(ws + 119424);
+      CHEM_PREFETCH(ws + 119456);
+      CHEM_PREFETCH(ws + 119488);
+      CHEM_PREFETCH(ws + 119520);
+      CHEM_PREFETCH(ws + 119552);
+      CHEM_PREFETCH(ws + 134720);
       double x = b[3072];
       x = fma(-CHEM_LDLU(lu + 41504), b[4384], x);
       x = fma(-CHEM_LDLU(lu + 41536), b[4544], x);
@@ -3489,11 +3489,11 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3072] = x * CHEM_LDLU(vd + 3072);
     }
     {
-      CHEM_PREFETCH(ws + 114816);
-      CHEM_PREFETCH(ws + 114848);
-      CHEM_PREFETCH(ws + 114880);
-      CHEM_PREFETCH(ws + 114912);
-      CHEM_PREFETCH(ws + 129920);
+      CHEM_PREFETCH(ws + 119584);
+      CHEM_PREFETCH(ws + 119616);
+      CHEM_PREFETCH(ws + 119648);
+      CHEM_PREFETCH(ws + 119680);
+      CHEM_PREFETCH(ws + 134688);
       double x = b[3040];
       x = fma(-CHEM_LDLU(lu + 41632), b[3456], x);
       x = fma(-CHEM_LDLU(lu + 41664), b[3520], x);
@@ -3503,11 +3503,11 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3040] = x * CHEM_LDLU(vd + 3040);
     }
     {
-      CHEM_PREFETCH(ws + 114944);
-      CHEM_PREFETCH(ws + 114976);
-      CHEM_PREFETCH(ws + 115008);
-      CHEM_PREFETCH(ws + 115040);
-      CHEM_PREFETCH(ws + 129888);
+      CHEM_PREFETCH(ws + 119712);
+      CHEM_PREFETCH(ws + 119744);
+      CHEM_PREFETCH(ws + 119776);
+      CHEM_PREFETCH(ws + 119808);
+      CHEM_PREFETCH(ws + 134656);
       double x = b[3008];
       x = fma(-CHEM_LDLU(lu + 41792), b[3456], x);
       x = fma(-CHEM_LDLU(lu + 41824), b[3520], x);
@@ -3517,12 +3517,12 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[3008] = x * CHEM_LDLU(vd + 3008);
     }
     {
-      CHEM_PREFETCH(ws + 115072);
-      CHEM_PREFETCH(ws + 115104);
-      CHEM_PREFETCH(ws + 115136);
-      CHEM_PREFETCH(ws + 115168);
-      CHEM_PREFETCH(ws + 115200);
-      CHEM_PREFETCH(ws + 129856);
+      CHEM_PREFETCH(ws + 119840);
+      CHEM_PREFETCH(ws + 119872);
+      CHEM_PREFETCH(ws + 119904);
+      CHEM_PREFETCH(ws + 119936);
+      CHEM_PREFETCH(ws + 119968);
+      CHEM_PREFETCH(ws + 134624);
       double x = b[2976];
       x = fma(-CHEM_LDLU(lu + 41952), b[4320], x);
       x = fma(-CHEM_LDLU(lu + 41984), b[4544], x);
@@ -3531,12 +3531,12 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[2976] = x * CHEM_LDLU(vd + 2976);
     }
     {
-      CHEM_PREFETCH(ws + 115232);
-      CHEM_PREFETCH(ws + 115264);
-      CHEM_PREFETCH(ws + 115296);
-      CHEM_PREFETCH(ws + 115328);
-      CHEM_PREFETCH(ws + 115360);
-      CHEM_PREFETCH(ws + 129824);
+      CHEM_PREFETCH(ws + 120000);
+      CHEM_PREFETCH(ws + 120032);
+      CHEM_PREFETCH(ws + 120064);
+      CHEM_PREFETCH(ws + 120096);
+      CHEM_PREFETCH(ws + 120128);
+      CHEM_PREFETCH(ws + 134592);
       double x = b[2944];
       x = fma(-CHEM_LDLU(lu + 42080), b[4384], x);
       x = fma(-CHEM_LDLU(lu + 42112), b[4544], x);
@@ -3545,14 +3545,14 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[2944] = x * CHEM_LDLU(vd + 2944);
     }
     {
-      CHEM_PREFETCH(ws + 115392);
-      CHEM_PREFETCH(ws + 115424);
-      CHEM_PREFETCH(ws + 115456);
-      CHEM_PREFETCH(ws + 115488);
-      CHEM_PREFETCH(ws + 115520);
-      CHEM_PREFETCH(ws + 115552);
-      CHEM_PREFETCH(ws + 115584);
-      CHEM_PREFETCH(ws + 129792);
+      CHEM_PREFETCH(ws + 120160);
+      CHEM_PREFETCH(ws + 120192);
+      CHEM_PREFETCH(ws + 120224);
+      CHEM_PREFETCH(ws + 120256);
+      CHEM_PREFETCH(ws + 120288);
+      CHEM_PREFETCH(ws + 120320);
+      CHEM_PREFETCH(ws + 120352);
+      CHEM_PREFETCH(ws + 134560);
       double x = b[2912];
       x = fma(-CHEM_LDLU(lu + 42208), b[3168], x);
       x = fma(-CHEM_LDLU(lu + 42240), b[3200], x);
@@ -3562,8 +3562,8 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[2912] = x * CHEM_LDLU(vd + 2912);
     }
     {
-      CHEM_PREFETCH(ws + 115616);
-      CHEM_PREFETCH(ws + 129760);
+      CHEM_PREFETCH(ws + 120384);
+      CHEM_PREFETCH(ws + 134528);
       double x = b[2880];
       x = fma(-CHEM_LDLU(lu + 42368), b[4288], x);
       x = fma(-CHEM_LDLU(lu + 42400), b[4352], x);
@@ -3573,9 +3573,9 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[2880] = x * CHEM_LDLU(vd + 2880);
     }
     {
-      CHEM_PREFETCH(ws + 115648);
-      CHEM_PREFETCH(ws + 115680);
-      CHEM_PREFETCH(ws + 129728);
+      CHEM_PREFETCH(ws + 120416);
+      CHEM_PREFETCH(ws + 120448);
+      CHEM_PREFETCH(ws + 134496);
       double x = b[2848];
       x = fma(-CHEM_LDLU(lu + 42528), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 42560), b[4320], x);
@@ -3587,33 +3587,33 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[2848] = x * CHEM_LDLU(vd + 2848);
     }
     {
-      CHEM_PREFETCH(ws + 115712);
-      CHEM_PREFETCH(ws + 115744);
-      CHEM_PREFETCH(ws + 115776);
-      CHEM_PREFETCH(ws + 129696);
+      CHEM_PREFETCH(ws + 120480);
+      CHEM_PREFETCH(ws + 120512);
+      CHEM_PREFETCH(ws + 120544);
+      CHEM_PREFETCH(ws + 134464);
       double x = b[2816];
       x = fma(-CHEM_LDLU(lu + 42752), b[4736], x);
       b[2816] = x * CHEM_LDLU(vd + 2816);
     }
     {
-      CHEM_PREFETCH(ws + 115808);
-      CHEM_PREFETCH(ws + 115840);
-      CHEM_PREFETCH(ws + 115872);
-      CHEM_PREFETCH(ws + 115904);
-      CHEM_PREFETCH(ws + 115936);
-      CHEM_PREFETCH(ws + 129664);
+      CHEM_PREFETCH(ws + 120576);
+      CHEM_PREFETCH(ws + 120608);
+      CHEM_PREFETCH(ws + 120640);
+      CHEM_PREFETCH(ws + 120672);
+      CHEM_PREFETCH(ws + 120704);
+      CHEM_PREFETCH(ws + 134432);
       double x = b[2784];
       x = fma(-CHEM_LDLU(lu + 42784), b[2816], x);
       x = fma(-CHEM_LDLU(lu + 42816), b[4736], x);
       b[2784] = x * CHEM_LDLU(vd + 2784);
     }
     {
-      CHEM_PREFETCH(ws + 115968);
-      CHEM_PREFETCH(ws + 116000);
-      CHEM_PREFETCH(ws + 116032);
-      CHEM_PREFETCH(ws + 116064);
-      CHEM_PREFETCH(ws + 116096);
-      CHEM_PREFETCH(ws + 129632);
+      CHEM_PREFETCH(ws + 120736);
+      CHEM_PREFETCH(ws + 120768);
+      CHEM_PREFETCH(ws + 120800);
+      CHEM_PREFETCH(ws + 120832);
+      CHEM_PREFETCH(ws + 120864);
+      CHEM_PREFETCH(ws + 134400);
       double x = b[2752];
       x = fma(-CHEM_LDLU(lu + 42848), b[2784], x);
       x = fma(-CHEM_LDLU(lu + 42880), b[2816], x);
@@ -3621,12 +3621,12 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
       b[2752] = x * CHEM_LDLU(vd + 2752);
     }
     {
-      CHEM_PREFETCH(ws + 116128);
-      CHEM_PREFETCH(ws + 116160);
-      CHEM_PREFETCH(ws + 116192);
-      CHEM_PREFETCH(ws + 116224);
-      CHEM_PREFETCH(ws + 116256);
-      CHEM_PREFETCH(ws + 129600);
+      CHEM_PREFETCH(ws + 120896);
+      CHEM_PREFETCH(ws + 120928);
+      CHEM_PREFETCH(ws + 120960);
+      CHEM_PREFETCH(ws + 120992);
+      CHEM_PREFETCH(ws + 121024);
+      CHEM_PREFETCH(ws + 134368);
       double x = b[2720];
       x = fma(-CHEM_LDLU(lu + 42944), b[3840], x);
       x = fma(-CHEM_LDLU(lu + 42976), b[4416], x);
@@ -3638,17 +3638,17 @@ __device__ __noinline__ void solve_0_1(double* __restrict__ ws, int rhs)
 }
 __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
 {
-    const double* __restrict__ lu = ws + 72864;
-    const double* __restrict__ vd = ws + 126944;
+    const double* __restrict__ lu = ws + 77632;
+    const double* __restrict__ vd = ws + 131712;
     double* __restrict__ b = ws + rhs * 32;
     (void)vd;
     {
-      CHEM_PREFETCH(ws + 116288);
-      CHEM_PREFETCH(ws + 116320);
-      CHEM_PREFETCH(ws + 116352);
-      CHEM_PREFETCH(ws + 116384);
-      CHEM_PREFETCH(ws + 116416);
-      CHEM_PREFETCH(ws + 129568);
+      CHEM_PREFETCH(ws + 121056);
+      CHEM_PREFETCH(ws + 121088);
+      CHEM_PREFETCH(ws + 121120);
+      CHEM_PREFETCH(ws + 121152);
+      CHEM_PREFETCH(ws + 121184);
+      CHEM_PREFETCH(ws + 134336);
       double x = b[2688];
       x = fma(-CHEM_LDLU(lu + 43104), b[3744], x);
       x = fma(-CHEM_LDLU(lu + 43136), b[4096], x);
@@ -3658,9 +3658,9 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[2688] = x * CHEM_LDLU(vd + 2688);
     }
     {
-      CHEM_PREFETCH(ws + 116448);
-      CHEM_PREFETCH(ws + 116480);
-      CHEM_PREFETCH(ws + 129536);
+      CHEM_PREFETCH(ws + 121216);
+      CHEM_PREFETCH(ws + 121248);
+      CHEM_PREFETCH(ws + 134304);
       double x = b[2656];
       x = fma(-CHEM_LDLU(lu + 43264), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 43296), b[4320], x);
@@ -3670,11 +3670,11 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[2656] = x * CHEM_LDLU(vd + 2656);
     }
     {
-      CHEM_PREFETCH(ws + 116512);
-      CHEM_PREFETCH(ws + 116544);
-      CHEM_PREFETCH(ws + 116576);
-      CHEM_PREFETCH(ws + 116608);
-      CHEM_PREFETCH(ws + 129504);
+      CHEM_PREFETCH(ws + 121280);
+      CHEM_PREFETCH(ws + 121312);
+      CHEM_PREFETCH(ws + 121344);
+      CHEM_PREFETCH(ws + 121376);
+      CHEM_PREFETCH(ws + 134272);
       double x = b[2624];
       x = fma(-CHEM_LDLU(lu + 43424), b[2944], x);
       x = fma(-CHEM_LDLU(lu + 43456), b[4384], x);
@@ -3684,23 +3684,23 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[2624] = x * CHEM_LDLU(vd + 2624);
     }
     {
-      CHEM_PREFETCH(ws + 116640);
-      CHEM_PREFETCH(ws + 116672);
-      CHEM_PREFETCH(ws + 116704);
-      CHEM_PREFETCH(ws + 116736);
-      CHEM_PREFETCH(ws + 116768);
-      CHEM_PREFETCH(ws + 129472);
+      CHEM_PREFETCH(ws + 121408);
+      CHEM_PREFETCH(ws + 121440);
+      CHEM_PREFETCH(ws + 121472);
+      CHEM_PREFETCH(ws + 121504);
+      CHEM_PREFETCH(ws + 121536);
+      CHEM_PREFETCH(ws + 134240);
       double x = b[2592];
       x = fma(-CHEM_LDLU(lu + 43584), b[4608], x);
       x = fma(-CHEM_LDLU(lu + 43616), b[4640], x);
       b[2592] = x * CHEM_LDLU(vd + 2592);
     }
     {
-      CHEM_PREFETCH(ws + 116800);
-      CHEM_PREFETCH(ws + 116832);
-      CHEM_PREFETCH(ws + 116864);
-      CHEM_PREFETCH(ws + 116896);
-      CHEM_PREFETCH(ws + 129440);
+      CHEM_PREFETCH(ws + 121568);
+      CHEM_PREFETCH(ws + 121600);
+      CHEM_PREFETCH(ws + 121632);
+      CHEM_PREFETCH(ws + 121664);
+      CHEM_PREFETCH(ws + 134208);
       double x = b[2560];
       x = fma(-CHEM_LDLU(lu + 43648), b[4384], x);
       x = fma(-CHEM_LDLU(lu + 43680), b[4544], x);
@@ -3709,12 +3709,12 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[2560] = x * CHEM_LDLU(vd + 2560);
     }
     {
-      CHEM_PREFETCH(ws + 116928);
-      CHEM_PREFETCH(ws + 116960);
-      CHEM_PREFETCH(ws + 116992);
-      CHEM_PREFETCH(ws + 117024);
-      CHEM_PREFETCH(ws + 117056);
-      CHEM_PREFETCH(ws + 129408);
+      CHEM_PREFETCH(ws + 121696);
+      CHEM_PREFETCH(ws + 121728);
+      CHEM_PREFETCH(ws + 121760);
+      CHEM_PREFETCH(ws + 121792);
+      CHEM_PREFETCH(ws + 121824);
+      CHEM_PREFETCH(ws + 134176);
       double x = b[2528];
       x = fma(-CHEM_LDLU(lu + 43776), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 43808), b[4320], x);
@@ -3724,11 +3724,11 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[2528] = x * CHEM_LDLU(vd + 2528);
     }
     {
-      CHEM_PREFETCH(ws + 117088);
-      CHEM_PREFETCH(ws + 117120);
-      CHEM_PREFETCH(ws + 117152);
-      CHEM_PREFETCH(ws + 117184);
-      CHEM_PREFETCH(ws + 129376);
+      CHEM_PREFETCH(ws + 121856);
+      CHEM_PREFETCH(ws + 121888);
+      CHEM_PREFETCH(ws + 121920);
+      CHEM_PREFETCH(ws + 121952);
+      CHEM_PREFETCH(ws + 134144);
       double x = b[2496];
       x = fma(-CHEM_LDLU(lu + 43936), b[4384], x);
       x = fma(-CHEM_LDLU(lu + 43968), b[4544], x);
@@ -3737,11 +3737,11 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[2496] = x * CHEM_LDLU(vd + 2496);
     }
     {
-      CHEM_PREFETCH(ws + 117216);
-      CHEM_PREFETCH(ws + 117248);
-      CHEM_PREFETCH(ws + 117280);
-      CHEM_PREFETCH(ws + 117312);
-      CHEM_PREFETCH(ws + 129344);
+      CHEM_PREFETCH(ws + 121984);
+      CHEM_PREFETCH(ws + 122016);
+      CHEM_PREFETCH(ws + 122048);
+      CHEM_PREFETCH(ws + 122080);
+      CHEM_PREFETCH(ws + 134112);
       double x = b[2464];
       x = fma(-CHEM_LDLU(lu + 44064), b[3328], x);
       x = fma(-CHEM_LDLU(lu + 44096), b[4384], x);
@@ -3751,11 +3751,11 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[2464] = x * CHEM_LDLU(vd + 2464);
     }
     {
-      CHEM_PREFETCH(ws + 117344);
-      CHEM_PREFETCH(ws + 117376);
-      CHEM_PREFETCH(ws + 117408);
-      CHEM_PREFETCH(ws + 117440);
-      CHEM_PREFETCH(ws + 129312);
+      CHEM_PREFETCH(ws + 122112);
+      CHEM_PREFETCH(ws + 122144);
+      CHEM_PREFETCH(ws + 122176);
+      CHEM_PREFETCH(ws + 122208);
+      CHEM_PREFETCH(ws + 134080);
       double x = b[2432];
       x = fma(-CHEM_LDLU(lu + 44224), b[4320], x);
       x = fma(-CHEM_LDLU(lu + 44256), b[4544], x);
@@ -3764,11 +3764,11 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[2432] = x * CHEM_LDLU(vd + 2432);
     }
     {
-      CHEM_PREFETCH(ws + 117472);
-      CHEM_PREFETCH(ws + 117504);
-      CHEM_PREFETCH(ws + 117536);
-      CHEM_PREFETCH(ws + 117568);
-      CHEM_PREFETCH(ws + 129280);
+      CHEM_PREFETCH(ws + 122240);
+      CHEM_PREFETCH(ws + 122272);
+      CHEM_PREFETCH(ws + 122304);
+      CHEM_PREFETCH(ws + 122336);
+      CHEM_PREFETCH(ws + 134048);
       double x = b[2400];
       x = fma(-CHEM_LDLU(lu + 44352), b[4320], x);
       x = fma(-CHEM_LDLU(lu + 44384), b[4544], x);
@@ -3777,11 +3777,11 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[2400] = x * CHEM_LDLU(vd + 2400);
     }
     {
-      CHEM_PREFETCH(ws + 117600);
-      CHEM_PREFETCH(ws + 117632);
-      CHEM_PREFETCH(ws + 117664);
-      CHEM_PREFETCH(ws + 117696);
-      CHEM_PREFETCH(ws + 129248);
+      CHEM_PREFETCH(ws + 122368);
+      CHEM_PREFETCH(ws + 122400);
+      CHEM_PREFETCH(ws + 122432);
+      CHEM_PREFETCH(ws + 122464);
+      CHEM_PREFETCH(ws + 134016);
       double x = b[2368];
       x = fma(-CHEM_LDLU(lu + 44480), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 44512), b[4544], x);
@@ -3790,12 +3790,12 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[2368] = x * CHEM_LDLU(vd + 2368);
     }
     {
-      CHEM_PREFETCH(ws + 117728);
-      CHEM_PREFETCH(ws + 117760);
-      CHEM_PREFETCH(ws + 117792);
-      CHEM_PREFETCH(ws + 117824);
-      CHEM_PREFETCH(ws + 117856);
-      CHEM_PREFETCH(ws + 129216);
+      CHEM_PREFETCH(ws + 122496);
+      CHEM_PREFETCH(ws + 122528);
+      CHEM_PREFETCH(ws + 122560);
+      CHEM_PREFETCH(ws + 122592);
+      CHEM_PREFETCH(ws + 122624);
+      CHEM_PREFETCH(ws + 133984);
       double x = b[2336];
       x = fma(-CHEM_LDLU(lu + 44608), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 44640), b[4544], x);
@@ -3804,13 +3804,13 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[2336] = x * CHEM_LDLU(vd + 2336);
     }
     {
-      CHEM_PREFETCH(ws + 117888);
-      CHEM_PREFETCH(ws + 117920);
-      CHEM_PREFETCH(ws + 117952);
-      CHEM_PREFETCH(ws + 117984);
-      CHEM_PREFETCH(ws + 118016);
-      CHEM_PREFETCH(ws + 118048);
-      CHEM_PREFETCH(ws + 129184);
+      CHEM_PREFETCH(ws + 122656);
+      CHEM_PREFETCH(ws + 122688);
+      CHEM_PREFETCH(ws + 122720);
+      CHEM_PREFETCH(ws + 122752);
+      CHEM_PREFETCH(ws + 122784);
+      CHEM_PREFETCH(ws + 122816);
+      CHEM_PREFETCH(ws + 133952);
       double x = b[2304];
       x = fma(-CHEM_LDLU(lu + 44736), b[2752], x);
       x = fma(-CHEM_LDLU(lu + 44768), b[2784], x);
@@ -3819,10 +3819,10 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[2304] = x * CHEM_LDLU(vd + 2304);
     }
     {
-      CHEM_PREFETCH(ws + 118080);
-      CHEM_PREFETCH(ws + 118112);
-      CHEM_PREFETCH(ws + 118144);
-      CHEM_PREFETCH(ws + 129152);
+      CHEM_PREFETCH(ws + 122848);
+      CHEM_PREFETCH(ws + 122880);
+      CHEM_PREFETCH(ws + 122912);
+      CHEM_PREFETCH(ws + 133920);
       double x = b[2272];
       x = fma(-CHEM_LDLU(lu + 44864), b[4384], x);
       x = fma(-CHEM_LDLU(lu + 44896), b[4416], x);
@@ -3832,11 +3832,11 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[2272] = x * CHEM_LDLU(vd + 2272);
     }
     {
-      CHEM_PREFETCH(ws + 118176);
-      CHEM_PREFETCH(ws + 118208);
-      CHEM_PREFETCH(ws + 118240);
-      CHEM_PREFETCH(ws + 118272);
-      CHEM_PREFETCH(ws + 129120);
+      CHEM_PREFETCH(ws + 122944);
+      CHEM_PREFETCH(ws + 122976);
+      CHEM_PREFETCH(ws + 123008);
+      CHEM_PREFETCH(ws + 123040);
+      CHEM_PREFETCH(ws + 133888);
       double x = b[2240];
       x = fma(-CHEM_LDLU(lu + 45024), b[2496], x);
       x = fma(-CHEM_LDLU(lu + 45056), b[2560], x);
@@ -3847,10 +3847,10 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[2240] = x * CHEM_LDLU(vd + 2240);
     }
     {
-      CHEM_PREFETCH(ws + 118304);
-      CHEM_PREFETCH(ws + 118336);
-      CHEM_PREFETCH(ws + 118368);
-      CHEM_PREFETCH(ws + 129088);
+      CHEM_PREFETCH(ws + 123072);
+      CHEM_PREFETCH(ws + 123104);
+      CHEM_PREFETCH(ws + 123136);
+      CHEM_PREFETCH(ws + 133856);
       double x = b[2208];
       x = fma(-CHEM_LDLU(lu + 45216), b[4544], x);
       x = fma(-CHEM_LDLU(lu + 45248), b[4640], x);
@@ -3858,11 +3858,11 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[2208] = x * CHEM_LDLU(vd + 2208);
     }
     {
-      CHEM_PREFETCH(ws + 118400);
-      CHEM_PREFETCH(ws + 118432);
-      CHEM_PREFETCH(ws + 118464);
-      CHEM_PREFETCH(ws + 118496);
-      CHEM_PREFETCH(ws + 129056);
+      CHEM_PREFETCH(ws + 123168);
+      CHEM_PREFETCH(ws + 123200);
+      CHEM_PREFETCH(ws + 123232);
+      CHEM_PREFETCH(ws + 123264);
+      CHEM_PREFETCH(ws + 133824);
       double x = b[2176];
       x = fma(-CHEM_LDLU(lu + 45312), b[3328], x);
       x = fma(-CHEM_LDLU(lu + 45344), b[4608], x);
@@ -3871,12 +3871,12 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[2176] = x * CHEM_LDLU(vd + 2176);
     }
     {
-      CHEM_PREFETCH(ws + 118528);
-      CHEM_PREFETCH(ws + 118560);
-      CHEM_PREFETCH(ws + 118592);
-      CHEM_PREFETCH(ws + 118624);
-      CHEM_PREFETCH(ws + 118656);
-      CHEM_PREFETCH(ws + 129024);
+      CHEM_PREFETCH(ws + 123296);
+      CHEM_PREFETCH(ws + 123328);
+      CHEM_PREFETCH(ws + 123360);
+      CHEM_PREFETCH(ws + 123392);
+      CHEM_PREFETCH(ws + 123424);
+      CHEM_PREFETCH(ws + 133792);
       double x = b[2144];
       x = fma(-CHEM_LDLU(lu + 45440), b[4384], x);
       x = fma(-CHEM_LDLU(lu + 45472), b[4704], x);
@@ -3884,11 +3884,11 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[2144] = x * CHEM_LDLU(vd + 2144);
     }
     {
-      CHEM_PREFETCH(ws + 118688);
-      CHEM_PREFETCH(ws + 118720);
-      CHEM_PREFETCH(ws + 118752);
-      CHEM_PREFETCH(ws + 118784);
-      CHEM_PREFETCH(ws + 128992);
+      CHEM_PREFETCH(ws + 123456);
+      CHEM_PREFETCH(ws + 123488);
+      CHEM_PREFETCH(ws + 123520);
+      CHEM_PREFETCH(ws + 123552);
+      CHEM_PREFETCH(ws + 133760);
       double x = b[2112];
       x = fma(-CHEM_LDLU(lu + 45536), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 45568), b[4320], x);
@@ -3897,10 +3897,10 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[2112] = x * CHEM_LDLU(vd + 2112);
     }
     {
-      CHEM_PREFETCH(ws + 118816);
-      CHEM_PREFETCH(ws + 118848);
-      CHEM_PREFETCH(ws + 118880);
-      CHEM_PREFETCH(ws + 128960);
+      CHEM_PREFETCH(ws + 123584);
+      CHEM_PREFETCH(ws + 123616);
+      CHEM_PREFETCH(ws + 123648);
+      CHEM_PREFETCH(ws + 133728);
       double x = b[2080];
       x = fma(-CHEM_LDLU(lu + 45664), b[2112], x);
       x = fma(-CHEM_LDLU(lu + 45696), b[4160], x);
@@ -3910,10 +3910,10 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[2080] = x * CHEM_LDLU(vd + 2080);
     }
     {
-      CHEM_PREFETCH(ws + 118912);
-      CHEM_PREFETCH(ws + 118944);
-      CHEM_PREFETCH(ws + 118976);
-      CHEM_PREFETCH(ws + 128928);
+      CHEM_PREFETCH(ws + 123680);
+      CHEM_PREFETCH(ws + 123712);
+      CHEM_PREFETCH(ws + 123744);
+      CHEM_PREFETCH(ws + 133696);
       double x = b[2048];
       x = fma(-CHEM_LDLU(lu + 45824), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 45856), b[4320], x);
@@ -3922,10 +3922,10 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[2048] = x * CHEM_LDLU(vd + 2048);
     }
     {
-      CHEM_PREFETCH(ws + 119008);
-      CHEM_PREFETCH(ws + 119040);
-      CHEM_PREFETCH(ws + 119072);
-      CHEM_PREFETCH(ws + 128896);
+      CHEM_PREFETCH(ws + 123776);
+      CHEM_PREFETCH(ws + 123808);
+      CHEM_PREFETCH(ws + 123840);
+      CHEM_PREFETCH(ws + 133664);
       double x = b[2016];
       x = fma(-CHEM_LDLU(lu + 45952), b[4544], x);
       x = fma(-CHEM_LDLU(lu + 45984), b[4640], x);
@@ -3933,9 +3933,9 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[2016] = x * CHEM_LDLU(vd + 2016);
     }
     {
-      CHEM_PREFETCH(ws + 119104);
-      CHEM_PREFETCH(ws + 119136);
-      CHEM_PREFETCH(ws + 128864);
+      CHEM_PREFETCH(ws + 123872);
+      CHEM_PREFETCH(ws + 123904);
+      CHEM_PREFETCH(ws + 133632);
       double x = b[1984];
       x = fma(-CHEM_LDLU(lu + 46048), b[4224], x);
       x = fma(-CHEM_LDLU(lu + 46080), b[4544], x);
@@ -3943,10 +3943,10 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[1984] = x * CHEM_LDLU(vd + 1984);
     }
     {
-      CHEM_PREFETCH(ws + 119168);
-      CHEM_PREFETCH(ws + 119200);
-      CHEM_PREFETCH(ws + 119232);
-      CHEM_PREFETCH(ws + 128832);
+      CHEM_PREFETCH(ws + 123936);
+      CHEM_PREFETCH(ws + 123968);
+      CHEM_PREFETCH(ws + 124000);
+      CHEM_PREFETCH(ws + 133600);
       double x = b[1952];
       x = fma(-CHEM_LDLU(lu + 46144), b[4096], x);
       x = fma(-CHEM_LDLU(lu + 46176), b[4608], x);
@@ -3954,20 +3954,20 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[1952] = x * CHEM_LDLU(vd + 1952);
     }
     {
-      CHEM_PREFETCH(ws + 119264);
-      CHEM_PREFETCH(ws + 119296);
-      CHEM_PREFETCH(ws + 119328);
-      CHEM_PREFETCH(ws + 128800);
+      CHEM_PREFETCH(ws + 124032);
+      CHEM_PREFETCH(ws + 124064);
+      CHEM_PREFETCH(ws + 124096);
+      CHEM_PREFETCH(ws + 133568);
       double x = b[1920];
       x = fma(-CHEM_LDLU(lu + 46240), b[4608], x);
       x = fma(-CHEM_LDLU(lu + 46272), b[4640], x);
       b[1920] = x * CHEM_LDLU(vd + 1920);
     }
     {
-      CHEM_PREFETCH(ws + 119360);
-      CHEM_PREFETCH(ws + 119392);
-      CHEM_PREFETCH(ws + 119424);
-      CHEM_PREFETCH(ws + 128768);
+      CHEM_PREFETCH(ws + 124128);
+      CHEM_PREFETCH(ws + 124160);
+      CHEM_PREFETCH(ws + 124192);
+      CHEM_PREFETCH(ws + 133536);
       double x = b[1888];
       x = fma(-CHEM_LDLU(lu + 46304), b[4320], x);
       x = fma(-CHEM_LDLU(lu + 46336), b[4640], x);
@@ -3975,10 +3975,10 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[1888] = x * CHEM_LDLU(vd + 1888);
     }
     {
-      CHEM_PREFETCH(ws + 119456);
-      CHEM_PREFETCH(ws + 119488);
-      CHEM_PREFETCH(ws + 119520);
-      CHEM_PREFETCH(ws + 128736);
+      CHEM_PREFETCH(ws + 124224);
+      CHEM_PREFETCH(ws + 124256);
+      CHEM_PREFETCH(ws + 124288);
+      CHEM_PREFETCH(ws + 133504);
       double x = b[1856];
       x = fma(-CHEM_LDLU(lu + 46400), b[4320], x);
       x = fma(-CHEM_LDLU(lu + 46432), b[4640], x);
@@ -3986,10 +3986,10 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[1856] = x * CHEM_LDLU(vd + 1856);
     }
     {
-      CHEM_PREFETCH(ws + 119552);
-      CHEM_PREFETCH(ws + 119584);
-      CHEM_PREFETCH(ws + 119616);
-      CHEM_PREFETCH(ws + 128704);
+      CHEM_PREFETCH(ws + 124320);
+      CHEM_PREFETCH(ws + 124352);
+      CHEM_PREFETCH(ws + 124384);
+      CHEM_PREFETCH(ws + 133472);
       double x = b[1824];
       x = fma(-CHEM_LDLU(lu + 46496), b[3520], x);
       x = fma(-CHEM_LDLU(lu + 46528), b[4608], x);
@@ -3997,10 +3997,10 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[1824] = x * CHEM_LDLU(vd + 1824);
     }
     {
-      CHEM_PREFETCH(ws + 119648);
-      CHEM_PREFETCH(ws + 119680);
-      CHEM_PREFETCH(ws + 119712);
-      CHEM_PREFETCH(ws + 128672);
+      CHEM_PREFETCH(ws + 124416);
+      CHEM_PREFETCH(ws + 124448);
+      CHEM_PREFETCH(ws + 124480);
+      CHEM_PREFETCH(ws + 133440);
       double x = b[1792];
       x = fma(-CHEM_LDLU(lu + 46592), b[3744], x);
       x = fma(-CHEM_LDLU(lu + 46624), b[4608], x);
@@ -4008,10 +4008,10 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[1792] = x * CHEM_LDLU(vd + 1792);
     }
     {
-      CHEM_PREFETCH(ws + 119744);
-      CHEM_PREFETCH(ws + 119776);
-      CHEM_PREFETCH(ws + 119808);
-      CHEM_PREFETCH(ws + 128640);
+      CHEM_PREFETCH(ws + 124512);
+      CHEM_PREFETCH(ws + 124544);
+      CHEM_PREFETCH(ws + 124576);
+      CHEM_PREFETCH(ws + 133408);
       double x = b[1760];
       x = fma(-CHEM_LDLU(lu + 46688), b[3616], x);
       x = fma(-CHEM_LDLU(lu + 46720), b[4640], x);
@@ -4019,10 +4019,10 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[1760] = x * CHEM_LDLU(vd + 1760);
     }
     {
-      CHEM_PREFETCH(ws + 119840);
-      CHEM_PREFETCH(ws + 119872);
-      CHEM_PREFETCH(ws + 119904);
-      CHEM_PREFETCH(ws + 128608);
+      CHEM_PREFETCH(ws + 124608);
+      CHEM_PREFETCH(ws + 124640);
+      CHEM_PREFETCH(ws + 124672);
+      CHEM_PREFETCH(ws + 133376);
       double x = b[1728];
       x = fma(-CHEM_LDLU(lu + 46784), b[4384], x);
       x = fma(-CHEM_LDLU(lu + 46816), b[4512], x);
@@ -4030,10 +4030,10 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[1728] = x * CHEM_LDLU(vd + 1728);
     }
     {
-      CHEM_PREFETCH(ws + 119936);
-      CHEM_PREFETCH(ws + 119968);
-      CHEM_PREFETCH(ws + 120000);
-      CHEM_PREFETCH(ws + 128576);
+      CHEM_PREFETCH(ws + 124704);
+      CHEM_PREFETCH(ws + 124736);
+      CHEM_PREFETCH(ws + 124768);
+      CHEM_PREFETCH(ws + 133344);
       double x = b[1696];
       x = fma(-CHEM_LDLU(lu + 46880), b[4608], x);
       x = fma(-CHEM_LDLU(lu + 46912), b[4704], x);
@@ -4041,10 +4041,10 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[1696] = x * CHEM_LDLU(vd + 1696);
     }
     {
-      CHEM_PREFETCH(ws + 120032);
-      CHEM_PREFETCH(ws + 120064);
-      CHEM_PREFETCH(ws + 120096);
-      CHEM_PREFETCH(ws + 128544);
+      CHEM_PREFETCH(ws + 124800);
+      CHEM_PREFETCH(ws + 124832);
+      CHEM_PREFETCH(ws + 124864);
+      CHEM_PREFETCH(ws + 133312);
       double x = b[1664];
       x = fma(-CHEM_LDLU(lu + 46976), b[3424], x);
       x = fma(-CHEM_LDLU(lu + 47008), b[4704], x);
@@ -4052,10 +4052,10 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[1664] = x * CHEM_LDLU(vd + 1664);
     }
     {
-      CHEM_PREFETCH(ws + 120128);
-      CHEM_PREFETCH(ws + 120160);
-      CHEM_PREFETCH(ws + 120192);
-      CHEM_PREFETCH(ws + 128512);
+      CHEM_PREFETCH(ws + 124896);
+      CHEM_PREFETCH(ws + 124928);
+      CHEM_PREFETCH(ws + 124960);
+      CHEM_PREFETCH(ws + 133280);
       double x = b[1632];
       x = fma(-CHEM_LDLU(lu + 47072), b[3424], x);
       x = fma(-CHEM_LDLU(lu + 47104), b[4384], x);
@@ -4063,9 +4063,9 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[1632] = x * CHEM_LDLU(vd + 1632);
     }
     {
-      CHEM_PREFETCH(ws + 120224);
-      CHEM_PREFETCH(ws + 120256);
-      CHEM_PREFETCH(ws + 128480);
+      CHEM_PREFETCH(ws + 124992);
+      CHEM_PREFETCH(ws + 125024);
+      CHEM_PREFETCH(ws + 133248);
       double x = b[1600];
       x = fma(-CHEM_LDLU(lu + 47168), b[2016], x);
       x = fma(-CHEM_LDLU(lu + 47200), b[4544], x);
@@ -4073,9 +4073,9 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[1600] = x * CHEM_LDLU(vd + 1600);
     }
     {
-      CHEM_PREFETCH(ws + 120288);
-      CHEM_PREFETCH(ws + 120320);
-      CHEM_PREFETCH(ws + 128448);
+      CHEM_PREFETCH(ws + 125056);
+      CHEM_PREFETCH(ws + 125088);
+      CHEM_PREFETCH(ws + 133216);
       double x = b[1568];
       x = fma(-CHEM_LDLU(lu + 47264), b[3008], x);
       x = fma(-CHEM_LDLU(lu + 47296), b[4320], x);
@@ -4083,149 +4083,149 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[1568] = x * CHEM_LDLU(vd + 1568);
     }
     {
-      CHEM_PREFETCH(ws + 120352);
-      CHEM_PREFETCH(ws + 128416);
+      CHEM_PREFETCH(ws + 125120);
+      CHEM_PREFETCH(ws + 133184);
       double x = b[1536];
       x = fma(-CHEM_LDLU(lu + 47360), b[4544], x);
       x = fma(-CHEM_LDLU(lu + 47392), b[4736], x);
       b[1536] = x * CHEM_LDLU(vd + 1536);
     }
     {
-      CHEM_PREFETCH(ws + 120384);
-      CHEM_PREFETCH(ws + 128384);
+      CHEM_PREFETCH(ws + 125152);
+      CHEM_PREFETCH(ws + 133152);
       double x = b[1504];
       x = fma(-CHEM_LDLU(lu + 47424), b[2752], x);
       x = fma(-CHEM_LDLU(lu + 47456), b[4736], x);
       b[1504] = x * CHEM_LDLU(vd + 1504);
     }
     {
-      CHEM_PREFETCH(ws + 128352);
+      CHEM_PREFETCH(ws + 133120);
       double x = b[1472];
       x = fma(-CHEM_LDLU(lu + 47488), b[4736], x);
       b[1472] = x * CHEM_LDLU(vd + 1472);
     }
     {
-      CHEM_PREFETCH(ws + 128320);
+      CHEM_PREFETCH(ws + 133088);
       double x = b[1440];
       x = fma(-CHEM_LDLU(lu + 47520), b[4736], x);
       b[1440] = x * CHEM_LDLU(vd + 1440);
     }
     {
-      CHEM_PREFETCH(ws + 120416);
-      CHEM_PREFETCH(ws + 120448);
-      CHEM_PREFETCH(ws + 128288);
+      CHEM_PREFETCH(ws + 125184);
+      CHEM_PREFETCH(ws + 125216);
+      CHEM_PREFETCH(ws + 133056);
       double x = b[1408];
       b[1408] = x * CHEM_LDLU(vd + 1408);
     }
     {
-      CHEM_PREFETCH(ws + 120480);
-      CHEM_PREFETCH(ws + 120512);
-      CHEM_PREFETCH(ws + 128256);
+      CHEM_PREFETCH(ws + 125248);
+      CHEM_PREFETCH(ws + 125280);
+      CHEM_PREFETCH(ws + 133024);
       double x = b[1376];
       b[1376] = x * CHEM_LDLU(vd + 1376);
     }
     {
-      CHEM_PREFETCH(ws + 120544);
-      CHEM_PREFETCH(ws + 120576);
-      CHEM_PREFETCH(ws + 128224);
+      CHEM_PREFETCH(ws + 125312);
+      CHEM_PREFETCH(ws + 125344);
+      CHEM_PREFETCH(ws + 132992);
       double x = b[1344];
       x = fma(-CHEM_LDLU(lu + 47552), b[4448], x);
       x = fma(-CHEM_LDLU(lu + 47584), b[4608], x);
       b[1344] = x * CHEM_LDLU(vd + 1344);
     }
     {
-      CHEM_PREFETCH(ws + 120608);
-      CHEM_PREFETCH(ws + 128192);
+      CHEM_PREFETCH(ws + 125376);
+      CHEM_PREFETCH(ws + 132960);
       double x = b[1312];
       x = fma(-CHEM_LDLU(lu + 47616), b[1664], x);
       x = fma(-CHEM_LDLU(lu + 47648), b[4736], x);
       b[1312] = x * CHEM_LDLU(vd + 1312);
     }
     {
-      CHEM_PREFETCH(ws + 120640);
-      CHEM_PREFETCH(ws + 120672);
-      CHEM_PREFETCH(ws + 128160);
+      CHEM_PREFETCH(ws + 125408);
+      CHEM_PREFETCH(ws + 125440);
+      CHEM_PREFETCH(ws + 132928);
       double x = b[1280];
       x = fma(-CHEM_LDLU(lu + 47680), b[4608], x);
       x = fma(-CHEM_LDLU(lu + 47712), b[4640], x);
       b[1280] = x * CHEM_LDLU(vd + 1280);
     }
     {
-      CHEM_PREFETCH(ws + 120704);
-      CHEM_PREFETCH(ws + 120736);
-      CHEM_PREFETCH(ws + 128128);
+      CHEM_PREFETCH(ws + 125472);
+      CHEM_PREFETCH(ws + 125504);
+      CHEM_PREFETCH(ws + 132896);
       double x = b[1248];
       x = fma(-CHEM_LDLU(lu + 47744), b[1280], x);
       b[1248] = x * CHEM_LDLU(vd + 1248);
     }
     {
-      CHEM_PREFETCH(ws + 120768);
-      CHEM_PREFETCH(ws + 120800);
-      CHEM_PREFETCH(ws + 128096);
+      CHEM_PREFETCH(ws + 125536);
+      CHEM_PREFETCH(ws + 125568);
+      CHEM_PREFETCH(ws + 132864);
       double x = b[1216];
       x = fma(-CHEM_LDLU(lu + 47776), b[3520], x);
       x = fma(-CHEM_LDLU(lu + 47808), b[4608], x);
       b[1216] = x * CHEM_LDLU(vd + 1216);
     }
     {
-      CHEM_PREFETCH(ws + 120832);
-      CHEM_PREFETCH(ws + 120864);
-      CHEM_PREFETCH(ws + 128064);
+      CHEM_PREFETCH(ws + 125600);
+      CHEM_PREFETCH(ws + 125632);
+      CHEM_PREFETCH(ws + 132832);
       double x = b[1184];
       x = fma(-CHEM_LDLU(lu + 47840), b[3008], x);
       x = fma(-CHEM_LDLU(lu + 47872), b[3520], x);
       b[1184] = x * CHEM_LDLU(vd + 1184);
     }
     {
-      CHEM_PREFETCH(ws + 120896);
-      CHEM_PREFETCH(ws + 120928);
-      CHEM_PREFETCH(ws + 128032);
+      CHEM_PREFETCH(ws + 125664);
+      CHEM_PREFETCH(ws + 125696);
+      CHEM_PREFETCH(ws + 132800);
       double x = b[1152];
       x = fma(-CHEM_LDLU(lu + 47904), b[4544], x);
       x = fma(-CHEM_LDLU(lu + 47936), b[4736], x);
       b[1152] = x * CHEM_LDLU(vd + 1152);
     }
     {
-      CHEM_PREFETCH(ws + 120960);
-      CHEM_PREFETCH(ws + 120992);
-      CHEM_PREFETCH(ws + 128000);
+      CHEM_PREFETCH(ws + 125728);
+      CHEM_PREFETCH(ws + 125760);
+      CHEM_PREFETCH(ws + 132768);
       double x = b[1120];
       x = fma(-CHEM_LDLU(lu + 47968), b[4544], x);
       x = fma(-CHEM_LDLU(lu + 48000), b[4736], x);
       b[1120] = x * CHEM_LDLU(vd + 1120);
     }
     {
-      CHEM_PREFETCH(ws + 121024);
-      CHEM_PREFETCH(ws + 121056);
-      CHEM_PREFETCH(ws + 127968);
+      CHEM_PREFETCH(ws + 125792);
+      CHEM_PREFETCH(ws + 125824);
+      CHEM_PREFETCH(ws + 132736);
       double x = b[1088];
       x = fma(-CHEM_LDLU(lu + 48032), b[4544], x);
       x = fma(-CHEM_LDLU(lu + 48064), b[4736], x);
       b[1088] = x * CHEM_LDLU(vd + 1088);
     }
     {
-      CHEM_PREFETCH(ws + 121088);
-      CHEM_PREFETCH(ws + 121120);
-      CHEM_PREFETCH(ws + 121152);
-      CHEM_PREFETCH(ws + 127936);
+      CHEM_PREFETCH(ws + 125856);
+      CHEM_PREFETCH(ws + 125888);
+      CHEM_PREFETCH(ws + 125920);
+      CHEM_PREFETCH(ws + 132704);
       double x = b[1056];
       x = fma(-CHEM_LDLU(lu + 48096), b[1664], x);
       x = fma(-CHEM_LDLU(lu + 48128), b[4736], x);
       b[1056] = x * CHEM_LDLU(vd + 1056);
     }
     {
-      CHEM_PREFETCH(ws + 121184);
-      CHEM_PREFETCH(ws + 121216);
-      CHEM_PREFETCH(ws + 127904);
+      CHEM_PREFETCH(ws + 125952);
+      CHEM_PREFETCH(ws + 125984);
+      CHEM_PREFETCH(ws + 132672);
       double x = b[1024];
       x = fma(-CHEM_LDLU(lu + 48160), b[3424], x);
       x = fma(-CHEM_LDLU(lu + 48192), b[4640], x);
       b[1024] = x * CHEM_LDLU(vd + 1024);
     }
     {
-      CHEM_PREFETCH(ws + 121248);
-      CHEM_PREFETCH(ws + 121280);
-      CHEM_PREFETCH(ws + 127872);
+      CHEM_PREFETCH(ws + 126016);
+      CHEM_PREFETCH(ws + 126048);
+      CHEM_PREFETCH(ws + 132640);
       double x = b[992];
       x = fma(-CHEM_LDLU(lu + 48224), b[2528], x);
       x = fma(-CHEM_LDLU(lu + 48256), b[4640], x);
@@ -4233,205 +4233,205 @@ __device__ __noinline__ void solve_0_2(double* __restrict__ ws, int rhs)
       b[992] = x * CHEM_LDLU(vd + 992);
     }
     {
-      CHEM_PREFETCH(ws + 121312);
-      CHEM_PREFETCH(ws + 121344);
-      CHEM_PREFETCH(ws + 127840);
+      CHEM_PREFETCH(ws + 126080);
+      CHEM_PREFETCH(ws + 126112);
+      CHEM_PREFETCH(ws + 132608);
       double x = b[960];
       x = fma(-CHEM_LDLU(lu + 48320), b[1984], x);
       x = fma(-CHEM_LDLU(lu + 48352), b[4608], x);
       b[960] = x * CHEM_LDLU(vd + 960);
     }
     {
-      CHEM_PREFETCH(ws + 121376);
-      CHEM_PREFETCH(ws + 121408);
-      CHEM_PREFETCH(ws + 127808);
+      CHEM_PREFETCH(ws + 126144);
+      CHEM_PREFETCH(ws + 126176);
+      CHEM_PREFETCH(ws + 132576);
       double x = b[928];
       x = fma(-CHEM_LDLU(lu + 48384), b[4544], x);
       x = fma(-CHEM_LDLU(lu + 48416), b[4736], x);
       b[928] = x * CHEM_LDLU(vd + 928);
     }
     {
-      CHEM_PREFETCH(ws + 121440);
-      CHEM_PREFETCH(ws + 121472);
-      CHEM_PREFETCH(ws + 127776);
+      CHEM_PREFETCH(ws + 126208);
+      CHEM_PREFETCH(ws + 126240);
+      CHEM_PREFETCH(ws + 132544);
       double x = b[896];
       x = fma(-CHEM_LDLU(lu + 48448), b[4544], x);
       x = fma(-CHEM_LDLU(lu + 48480), b[4736], x);
       b[896] = x * CHEM_LDLU(vd + 896);
     }
     {
-      CHEM_PREFETCH(ws + 121504);
-      CHEM_PREFETCH(ws + 127744);
+      CHEM_PREFETCH(ws + 126272);
+      CHEM_PREFETCH(ws + 132512);
       double x = b[864];
       x = fma(-CHEM_LDLU(lu + 48512), b[4544], x);
       x = fma(-CHEM_LDLU(lu + 48544), b[4736], x);
       b[864] = x * CHEM_LDLU(vd + 864);
     }
     {
-      CHEM_PREFETCH(ws + 121536);
-      CHEM_PREFETCH(ws + 127712);
+      CHEM_PREFETCH(ws + 126304);
+      CHEM_PREFETCH(ws + 132480);
       double x = b[832];
       x = fma(-CHEM_LDLU(lu + 48576), b[4544], x);
       x = fma(-CHEM_LDLU(lu + 48608), b[4736], x);
       b[832] = x * CHEM_LDLU(vd + 832);
     }
     {
-      CHEM_PREFETCH(ws + 121568);
-      CHEM_PREFETCH(ws + 127680);
+      CHEM_PREFETCH(ws + 126336);
+      CHEM_PREFETCH(ws + 132448);
       double x = b[800];
       x = fma(-CHEM_LDLU(lu + 48640), b[4736], x);
       b[800] = x * CHEM_LDLU(vd + 800);
     }
     {
-      CHEM_PREFETCH(ws + 121600);
-      CHEM_PREFETCH(ws + 127648);
+      CHEM_PREFETCH(ws + 126368);
+      CHEM_PREFETCH(ws + 132416);
       double x = b[768];
       x = fma(-CHEM_LDLU(lu + 48672), b[4736], x);
       b[768] = x * CHEM_LDLU(vd + 768);
     }
     {
-      CHEM_PREFETCH(ws + 121632);
-      CHEM_PREFETCH(ws + 127616);
+      CHEM_PREFETCH(ws + 126400);
+      CHEM_PREFETCH(ws + 132384);
       double x = b[736];
       x = fma(-CHEM_LDLU(lu + 48704), b[4736], x);
       b[736] = x * CHEM_LDLU(vd + 736);
     }
     {
-      CHEM_PREFETCH(ws + 121664);
-      CHEM_PREFETCH(ws + 121696);
-      CHEM_PREFETCH(ws + 127584);
+      CHEM_PREFETCH(ws + 126432);
+      CHEM_PREFETCH(ws + 126464);
+      CHEM_PREFETCH(ws + 132352);
       double x = b[704];
       x = fma(-CHEM_LDLU(lu + 48736), b[4736], x);
       b[704] = x * CHEM_LDLU(vd + 704);
     }
     {
-      CHEM_PREFETCH(ws + 121728);
-      CHEM_PREFETCH(ws + 127552);
+      CHEM_PREFETCH(ws + 126496);
+      CHEM_PREFETCH(ws + 132320);
       double x = b[672];
       x = fma(-CHEM_LDLU(lu + 48768), b[4320], x);
       b[672] = x * CHEM_LDLU(vd + 672);
     }
     {
-      CHEM_PREFETCH(ws + 121760);
-      CHEM_PREFETCH(ws + 127520);
+      CHEM_PREFETCH(ws + 126528);
+      CHEM_PREFETCH(ws + 132288);
       double x = b[640];
       x = fma(-CHEM_LDLU(lu + 48800), b[4000], x);
       x = fma(-CHEM_LDLU(lu + 48832), b[4256], x);
       b[640] = x * CHEM_LDLU(vd + 640);
     }
     {
-      CHEM_PREFETCH(ws + 121792);
-      CHEM_PREFETCH(ws + 127488);
+      CHEM_PREFETCH(ws + 126560);
+      CHEM_PREFETCH(ws + 132256);
       double x = b[608];
       x = fma(-CHEM_LDLU(lu + 48864), b[1312], x);
       b[608] = x * CHEM_LDLU(vd + 608);
     }
     {
-      CHEM_PREFETCH(ws + 121824);
-      CHEM_PREFETCH(ws + 127456);
+      CHEM_PREFETCH(ws + 126592);
+      CHEM_PREFETCH(ws + 132224);
       double x = b[576];
       x = fma(-CHEM_LDLU(lu + 48896), b[1312], x);
       b[576] = x * CHEM_LDLU(vd + 576);
     }
     {
-      CHEM_PREFETCH(ws + 121856);
-      CHEM_PREFETCH(ws + 127424);
+      CHEM_PREFETCH(ws + 126624);
+      CHEM_PREFETCH(ws + 132192);
       double x = b[544];
       x = fma(-CHEM_LDLU(lu + 48928), b[1248], x);
       b[544] = x * CHEM_LDLU(vd + 544);
     }
     {
-      CHEM_PREFETCH(ws + 121888);
-      CHEM_PREFETCH(ws + 127392);
+      CHEM_PREFETCH(ws + 126656);
+      CHEM_PREFETCH(ws + 132160);
       double x = b[512];
       x = fma(-CHEM_LDLU(lu + 48960), b[1920], x);
       b[512] = x * CHEM_LDLU(vd + 512);
     }
     {
-      CHEM_PREFETCH(ws + 121920);
-      CHEM_PREFETCH(ws + 127360);
+      CHEM_PREFETCH(ws + 126688);
+      CHEM_PREFETCH(ws + 132128);
       double x = b[480];
       x = fma(-CHEM_LDLU(lu + 48992), b[1920], x);
       b[480] = x * CHEM_LDLU(vd + 480);
     }
     {
-      CHEM_PREFETCH(ws + 121952);
-      CHEM_PREFETCH(ws + 127328);
+      CHEM_PREFETCH(ws + 126720);
+      CHEM_PREFETCH(ws + 132096);
       double x = b[448];
       x = fma(-CHEM_LDLU(lu + 49024), b[4736], x);
       b[448] = x * CHEM_LDLU(vd + 448);
     }
     {
-      CHEM_PREFETCH(ws + 121984);
-      CHEM_PREFETCH(ws + 127296);
+      CHEM_PREFETCH(ws + 126752);
+      CHEM_PREFETCH(ws + 132064);
       double x = b[416];
       x = fma(-CHEM_LDLU(lu + 49056), b[4736], x);
       b[416] = x * CHEM_LDLU(vd + 416);
     }
     {
-      CHEM_PREFETCH(ws + 122016);
-      CHEM_PREFETCH(ws + 127264);
+      CHEM_PREFETCH(ws + 126784);
+      CHEM_PREFETCH(ws + 132032);
       double x = b[384];
       x = fma(-CHEM_LDLU(lu + 49088), b[4736], x);
       b[384] = x * CHEM_LDLU(vd + 384);
     }
     {
-      CHEM_PREFETCH(ws + 122048);
-      CHEM_PREFETCH(ws + 122080);
-      CHEM_PREFETCH(ws + 127232);
+      CHEM_PREFETCH(ws + 126816);
+      CHEM_PREFETCH(ws + 126848);
+      CHEM_PREFETCH(ws + 132000);
       double x = b[352];
       x = fma(-CHEM_LDLU(lu + 49120), b[4736], x);
       b[352] = x * CHEM_LDLU(vd + 352);
     }
     {
-      CHEM_PREFETCH(ws + 122112);
-      CHEM_PREFETCH(ws + 122144);
-      CHEM_PREFETCH(ws + 127200);
+      CHEM_PREFETCH(ws + 126880);
+      CHEM_PREFETCH(ws + 126912);
+      CHEM_PREFETCH(ws + 131968);
       double x = b[320];
       x = fma(-CHEM_LDLU(lu + 49152), b[960], x);
       b[320] = x * CHEM_LDLU(vd + 320);
     }
     {
-      CHEM_PREFETCH(ws + 127168);
+      CHEM_PREFETCH(ws + 131936);
       double x = b[288];
       x = fma(-CHEM_LDLU(lu + 49184), b[2208], x);
       x = fma(-CHEM_LDLU(lu + 49216), b[4736], x);
       b[288] = x * CHEM_LDLU(vd + 288);
     }
     {
-      CHEM_PREFETCH(ws + 127136);
+      CHEM_PREFETCH(ws + 131904);
       double x = b[256];
       x = fma(-CHEM_LDLU(lu + 49248), b[2208], x);
       x = fma(-CHEM_LDLU(lu + 49280), b[4736], x);
       b[256] = x * CHEM_LDLU(vd + 256);
     }
     {
-      CHEM_PREFETCH(ws + 127104);
+      CHEM_PREFETCH(ws + 131872);
       double x = b[224];
       b[224] = x * CHEM_LDLU(vd + 224);
     }
     {
-      CHEM_PREFETCH(ws + 127072);
+      CHEM_PREFETCH(ws + 131840);
       double x = b[192];
       b[192] = x * CHEM_LDLU(vd + 192);
     }
     {
-      CHEM_PREFETCH(ws + 127040);
+      CHEM_PREFETCH(ws + 131808);
       double x = b[160];
       b[160] = x * CHEM_LDLU(vd + 160);
     }
     {
-      CHEM_PREFETCH(ws + 127008);
+      CHEM_PREFETCH(ws + 131776);
       double x = b[128];
       b[128] = x * CHEM_LDLU(vd + 128);
     }
     {
-      CHEM_PREFETCH(ws + 126976);
+      CHEM_PREFETCH(ws + 131744);
       double x = b[96];
       b[96] = x * CHEM_LDLU(vd + 96);
     }
     {
-      CHEM_PREFETCH(ws + 126944);
+      CHEM_PREFETCH(ws + 131712);
       double x = b[64];
       b[64] = x * CHEM_LDLU(vd + 64);
     }

@@ -5,8 +5,8 @@
 namespace mech_cb6r5_ae7_aq {
 __device__ __noinline__ void solve_t_1_0(double* __restrict__ ws, int rhs)
 {
-    const double* __restrict__ lu = ws + 72864;
-    const double* __restrict__ vd = ws + 126944;
+    const double* __restrict__ lu = ws + 77632;
+    const double* __restrict__ vd = ws + 131712;
     double* __restrict__ b = ws + rhs * 32;
     (void)vd;
     {
@@ -1259,8 +1259,8 @@ __device__ __noinline__ void solve_t_1_0(double* __restrict__ ws, int rhs)
 }
 __device__ __noinline__ void solve_t_1_1(double* __restrict__ ws, int rhs)
 {
-    const double* __restrict__ lu = ws + 72864;
-    const double* __restrict__ vd = ws + 126944;
+    const double* __restrict__ lu = ws + 77632;
+    const double* __restrict__ vd = ws + 131712;
     double* __restrict__ b = ws + rhs * 32;
     (void)vd;
     {
@@ -2350,8 +2350,8 @@ __device__ __noinline__ void solve_t_1_1(double* __restrict__ ws, int rhs)
 }
 __device__ __noinline__ void solve_t_1_2(double* __restrict__ ws, int rhs)
 {
-    const double* __restrict__ lu = ws + 72864;
-    const double* __restrict__ vd = ws + 126944;
+    const double* __restrict__ lu = ws + 77632;
+    const double* __restrict__ vd = ws + 131712;
     double* __restrict__ b = ws + rhs * 32;
     (void)vd;
     {

@@ -6,12 +6,12 @@ namespace mech_cracmm2 {
 __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
 {
     const double* __restrict__ y = ws + 0;
-    double* __restrict__ lam = ws + 216608;
-    const double* __restrict__ n1 = ws + 222656;
+    double* __restrict__ lam = ws + 222656;
+    const double* __restrict__ n1 = ws + 228704;
     const double* __restrict__ k1 = ws + 24192;
-    const double* __restrict__ n2 = ws + 228704;
+    const double* __restrict__ n2 = ws + 234752;
     const double* __restrict__ k2 = ws + 30240;
-    const double* __restrict__ n3 = ws + 234752;
+    const double* __restrict__ n3 = ws + 240800;
     const double* __restrict__ k3 = ws + 36288;
     {
       double w1 = 1.0 * n1[2336];
@@ -24,7 +24,7 @@ __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
       wk0 = fma(w2, k2[5184], wk0);
       wk0 = fma(w3, k3[5184], wk0);
       const double kk = ws[42336];
-      ws[264992] = fma(-kk, wk0, ws[264992]);
+      ws[271040] = fma(-kk, wk0, ws[271040]);
     }
     {
       double w1 = 1.0 * n1[576];
@@ -37,7 +37,7 @@ __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
       wk0 = fma(w2, k2[5184], wk0);
       wk0 = fma(w3, k3[5184], wk0);
       const double kk = ws[42368];
-      ws[265024] = fma(-kk, wk0, ws[265024]);
+      ws[271072] = fma(-kk, wk0, ws[271072]);
     }
     {
       double w1 = 2.0 * n1[6016];
@@ -50,7 +50,7 @@ __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
       wk0 = fma(w2, k2[4000], wk0);
       wk0 = fma(w3, k3[4000], wk0);
       const double kk = ws[42400];
-      ws[265056] = fma(-kk, wk0, ws[265056]);
+      ws[271104] = fma(-kk, wk0, ws[271104]);
     }
     {
       double w1 = 1.0 * n1[2336];
@@ -66,7 +66,7 @@ __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
       wk0 = fma(w2, k2[5920], wk0);
       wk0 = fma(w3, k3[5920], wk0);
       const double kk = ws[42432];
-      ws[265088] = fma(-kk, wk0, ws[265088]);
+      ws[271136] = fma(-kk, wk0, ws[271136]);
     }
     {
       double w1 = 1.0 * n1[5824];
@@ -79,7 +79,7 @@ __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
       wk0 = fma(w2, k2[5952], wk0);
       wk0 = fma(w3, k3[5952], wk0);
       const double kk = ws[42464];
-      ws[265120] = fma(-kk, wk0, ws[265120]);
+      ws[271168] = fma(-kk, wk0, ws[271168]);
     }
     {
       double w1 = 1.0 * n1[2336];
@@ -95,7 +95,7 @@ __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
       wk0 = fma(w2, k2[5952], wk0);
       wk0 = fma(w3, k3[5952], wk0);
       const double kk = ws[42496];
-      ws[265152] = fma(-kk, wk0, ws[265152]);
+      ws[271200] = fma(-kk, wk0, ws[271200]);
     }
     {
       double w1 = 1.0 * n1[6016];
@@ -111,7 +111,7 @@ __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
       wk0 = fma(w2, k2[1184], wk0);
       wk0 = fma(w3, k3[1184], wk0);
       const double kk = ws[42528];
-      ws[265184] = fma(-kk, wk0, ws[265184]);
+      ws[271232] = fma(-kk, wk0, ws[271232]);
     }
     {
       double w1 = 1.0 * n1[6016];
@@ -127,7 +127,7 @@ __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
       wk0 = fma(w2, k2[5024], wk0);
       wk0 = fma(w3, k3[5024], wk0);
       const double kk = ws[42560];
-      ws[265216] = fma(-kk, wk0, ws[265216]);
+      ws[271264] = fma(-kk, wk0, ws[271264]);
     }
     {
       double w1 = 0.2 * n1[6016];
@@ -149,7 +149,7 @@ __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
       wk0 = fma(w2, k2[1280], wk0);
       wk0 = fma(w3, k3[1280], wk0);
       const double kk = ws[42592];
-      ws[265248] = fma(-kk, wk0, ws[265248]);
+      ws[271296] = fma(-kk, wk0, ws[271296]);
     }
     {
       double w1 = 1.0 * n1[5664];
@@ -162,7 +162,7 @@ __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
       wk0 = fma(w2, k2[5856], wk0);
       wk0 = fma(w3, k3[5856], wk0);
       const double kk = ws[42624];
-      ws[265280] = fma(-kk, wk0, ws[265280]);
+      ws[271328] = fma(-kk, wk0, ws[271328]);
     }
     {
       double w1 = 2.0 * n1[5984];
@@ -178,7 +178,7 @@ __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
       wk0 = fma(w2, k2[5856], wk0);
       wk0 = fma(w3, k3[5856], wk0);
       const double kk = ws[42656];
-      ws[265312] = fma(-kk, wk0, ws[265312]);
+      ws[271360] = fma(-kk, wk0, ws[271360]);
     }
     {
       double w1 = 1.0 * n1[5984];
@@ -197,7 +197,7 @@ __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
       wk0 = fma(w2, k2[5568], wk0);
       wk0 = fma(w3, k3[5568], wk0);
       const double kk = ws[42688];
-      ws[265344] = fma(-kk, wk0, ws[265344]);
+      ws[271392] = fma(-kk, wk0, ws[271392]);
     }
     {
       double w1 = 1.0 * n1[5984];
@@ -216,7 +216,7 @@ __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
       wk0 = fma(w2, k2[5760], wk0);
       wk0 = fma(w3, k3[5760], wk0);
       const double kk = ws[42720];
-      ws[265376] = fma(-kk, wk0, ws[265376]);
+      ws[271424] = fma(-kk, wk0, ws[271424]);
     }
     {
       double w1 = 1.0 * n1[5888];
@@ -232,7 +232,7 @@ __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
       wk0 = fma(w2, k2[4480], wk0);
       wk0 = fma(w3, k3[4480], wk0);
       const double kk = ws[42752];
-      ws[265408] = fma(-kk, wk0, ws[265408]);
+      ws[271456] = fma(-kk, wk0, ws[271456]);
     }
     {
       double w1 = 2.0 * n1[5888];
@@ -248,7 +248,7 @@ __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
       wk0 = fma(w2, k2[4480], wk0);
       wk0 = fma(w3, k3[4480], wk0);
       const double kk = ws[42784];
-      ws[265440] = fma(-kk, wk0, ws[265440]);
+      ws[271488] = fma(-kk, wk0, ws[271488]);
     }
     {
       double w1 = 1.22 * n1[5984];
@@ -276,7 +276,7 @@ __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
       wk0 = fma(w2, k2[3872], wk0);
       wk0 = fma(w3, k3[3872], wk0);
       const double kk = ws[42816];
-      ws[265472] = fma(-kk, wk0, ws[265472]);
+      ws[271520] = fma(-kk, wk0, ws[271520]);
     }
     {
       double w1 = 1.0 * n1[5984];
@@ -295,7 +295,7 @@ __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
       wk0 = fma(w2, k2[4544], wk0);
       wk0 = fma(w3, k3[4544], wk0);
       const double kk = ws[42848];
-      ws[265504] = fma(-kk, wk0, ws[265504]);
+      ws[271552] = fma(-kk, wk0, ws[271552]);
     }
     {
       double w1 = 1.0 * n1[5984];
@@ -314,7 +314,7 @@ __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
       wk0 = fma(w2, k2[4576], wk0);
       wk0 = fma(w3, k3[4576], wk0);
       const double kk = ws[42880];
-      ws[265536] = fma(-kk, wk0, ws[265536]);
+      ws[271584] = fma(-kk, wk0, ws[271584]);
     }
     {
       double w1 = 0.1 * n1[5888];
@@ -336,7 +336,7 @@ __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
       wk0 = fma(w2, k2[5280], wk0);
       wk0 = fma(w3, k3[5280], wk0);
       const double kk = ws[42912];
-      ws[265568] = fma(-kk, wk0, ws[265568]);
+      ws[271616] = fma(-kk, wk0, ws[271616]);
     }
     {
       double w1 = 1.5 * n1[5632];
@@ -355,7 +355,7 @@ __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
       wk0 = fma(w2, k2[5504], wk0);
       wk0 = fma(w3, k3[5504], wk0);
       const double kk = ws[42944];
-      ws[265600] = fma(-kk, wk0, ws[265600]);
+      ws[271648] = fma(-kk, wk0, ws[271648]);
     }
     {
       double w1 = 1.0 * n1[5984];
@@ -374,7 +374,7 @@ __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
       wk0 = fma(w2, k2[5344], wk0);
       wk0 = fma(w3, k3[5344], wk0);
       const double kk = ws[42976];
-      ws[265632] = fma(-kk, wk0, ws[265632]);
+      ws[271680] = fma(-kk, wk0, ws[271680]);
     }
     {
       double w1 = 0.34 * n1[6016];
@@ -405,7 +405,7 @@ __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
       wk0 = fma(w2, k2[4128], wk0);
       wk0 = fma(w3, k3[4128], wk0);
       const double kk = ws[43008];
-      ws[265664] = fma(-kk, wk0, ws[265664]);
+      ws[271712] = fma(-kk, wk0, ws[271712]);
     }
     {
       double w1 = 0.3 * n1[5888];
@@ -427,7 +427,7 @@ __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
       wk0 = fma(w2, k2[4736], wk0);
       wk0 = fma(w3, k3[4736], wk0);
       const double kk = ws[43040];
-      ws[265696] = fma(-kk, wk0, ws[265696]);
+      ws[271744] = fma(-kk, wk0, ws[271744]);
     }
     {
       double w1 = 2.0 * n1[5664];
@@ -440,7 +440,7 @@ __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
       wk0 = fma(w2, k2[5376], wk0);
       wk0 = fma(w3, k3[5376], wk0);
       const double kk = ws[43072];
-      ws[265728] = fma(-kk, wk0, ws[265728]);
+      ws[271776] = fma(-kk, wk0, ws[271776]);
     }
     {
       double w1 = 1.0 * n1[5856];
@@ -456,7 +456,7 @@ __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
       wk0 = fma(w2, k2[5376], wk0);
       wk0 = fma(w3, k3[5376], wk0);
       const double kk = ws[43104];
-      ws[265760] = fma(-kk, wk0, ws[265760]);
+      ws[271808] = fma(-kk, wk0, ws[271808]);
     }
     {
       double w1 = 2.0 * n1[5984];
@@ -472,7 +472,7 @@ __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
       wk0 = fma(w2, k2[5376], wk0);
       wk0 = fma(w3, k3[5376], wk0);
       const double kk = ws[43136];
-      ws[265792] = fma(-kk, wk0, ws[265792]);
+      ws[271840] = fma(-kk, wk0, ws[271840]);
     }
     {
       double w1 = 1.0 * n1[5984];
@@ -491,18 +491,18 @@ __device__ __noinline__ void adj_hess3_0_0(double* __restrict__ ws)
       wk0 = fma(w2, k2[5248], wk0);
       wk0 = fma(w3, k3[5248], wk0);
       const double kk = ws[43168];
-      ws[265824] = fma(-kk, wk0, ws[265824]);
+      ws[271872] = fma(-kk, wk0, ws[271872]);
     }
 }
 __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
 {
     const double* __restrict__ y = ws + 0;
-    double* __restrict__ lam = ws + 216608;
-    const double* __restrict__ n1 = ws + 222656;
+    double* __restrict__ lam = ws + 222656;
+    const double* __restrict__ n1 = ws + 228704;
     const double* __restrict__ k1 = ws + 24192;
-    const double* __restrict__ n2 = ws + 228704;
+    const double* __restrict__ n2 = ws + 234752;
     const double* __restrict__ k2 = ws + 30240;
-    const double* __restrict__ n3 = ws + 234752;
+    const double* __restrict__ n3 = ws + 240800;
     const double* __restrict__ k3 = ws + 36288;
     {
       double w1 = 1.5 * n1[5984];
@@ -530,7 +530,7 @@ __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
       wk0 = fma(w2, k2[5472], wk0);
       wk0 = fma(w3, k3[5472], wk0);
       const double kk = ws[43200];
-      ws[265856] = fma(-kk, wk0, ws[265856]);
+      ws[271904] = fma(-kk, wk0, ws[271904]);
     }
     {
       double w1 = 1.5 * n1[5984];
@@ -558,7 +558,7 @@ __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
       wk0 = fma(w2, k2[4320], wk0);
       wk0 = fma(w3, k3[4320], wk0);
       const double kk = ws[43232];
-      ws[265888] = fma(-kk, wk0, ws[265888]);
+      ws[271936] = fma(-kk, wk0, ws[271936]);
     }
     {
       double w1 = 1.0 * n1[3232];
@@ -577,7 +577,7 @@ __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
       wk0 = fma(w2, k2[4448], wk0);
       wk0 = fma(w3, k3[4448], wk0);
       const double kk = ws[43264];
-      ws[265920] = fma(-kk, wk0, ws[265920]);
+      ws[271968] = fma(-kk, wk0, ws[271968]);
     }
     {
       double w1 = 1.0 * n1[6016];
@@ -596,7 +596,7 @@ __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
       wk0 = fma(w2, k2[2816], wk0);
       wk0 = fma(w3, k3[2816], wk0);
       const double kk = ws[43296];
-      ws[265952] = fma(-kk, wk0, ws[265952]);
+      ws[272000] = fma(-kk, wk0, ws[272000]);
     }
     {
       double w1 = 1.0 * n1[6016];
@@ -615,7 +615,7 @@ __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
       wk0 = fma(w2, k2[5728], wk0);
       wk0 = fma(w3, k3[5728], wk0);
       const double kk = ws[43328];
-      ws[265984] = fma(-kk, wk0, ws[265984]);
+      ws[272032] = fma(-kk, wk0, ws[272032]);
     }
     {
       double w1 = 1.0 * n1[6016];
@@ -634,7 +634,7 @@ __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
       wk0 = fma(w2, k2[4096], wk0);
       wk0 = fma(w3, k3[4096], wk0);
       const double kk = ws[43360];
-      ws[266016] = fma(-kk, wk0, ws[266016]);
+      ws[272064] = fma(-kk, wk0, ws[272064]);
     }
     {
       double w1 = 1.0 * n1[6016];
@@ -653,7 +653,7 @@ __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
       wk0 = fma(w2, k2[4608], wk0);
       wk0 = fma(w3, k3[4608], wk0);
       const double kk = ws[43392];
-      ws[266048] = fma(-kk, wk0, ws[266048]);
+      ws[272096] = fma(-kk, wk0, ws[272096]);
     }
     {
       double w1 = 1.0 * n1[6016];
@@ -669,7 +669,7 @@ __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
       wk0 = fma(w2, k2[3680], wk0);
       wk0 = fma(w3, k3[3680], wk0);
       const double kk = ws[43424];
-      ws[266080] = fma(-kk, wk0, ws[266080]);
+      ws[272128] = fma(-kk, wk0, ws[272128]);
     }
     {
       double w1 = 1.0 * n1[5984];
@@ -691,7 +691,7 @@ __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
       wk0 = fma(w2, k2[5440], wk0);
       wk0 = fma(w3, k3[5440], wk0);
       const double kk = ws[43456];
-      ws[266112] = fma(-kk, wk0, ws[266112]);
+      ws[272160] = fma(-kk, wk0, ws[272160]);
     }
     {
       double w1 = 1.0 * n1[5792];
@@ -707,7 +707,7 @@ __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
       wk0 = fma(w2, k2[1088], wk0);
       wk0 = fma(w3, k3[1088], wk0);
       const double kk = ws[43488];
-      ws[266144] = fma(-kk, wk0, ws[266144]);
+      ws[272192] = fma(-kk, wk0, ws[272192]);
     }
     {
       double w1 = 1.0 * n1[5888];
@@ -723,7 +723,7 @@ __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
       wk0 = fma(w2, k2[1088], wk0);
       wk0 = fma(w3, k3[1088], wk0);
       const double kk = ws[43520];
-      ws[266176] = fma(-kk, wk0, ws[266176]);
+      ws[272224] = fma(-kk, wk0, ws[272224]);
     }
     {
       double w1 = 1.0 * n1[5920];
@@ -742,7 +742,7 @@ __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
       wk0 = fma(w2, k2[4384], wk0);
       wk0 = fma(w3, k3[4384], wk0);
       const double kk = ws[43552];
-      ws[266208] = fma(-kk, wk0, ws[266208]);
+      ws[272256] = fma(-kk, wk0, ws[272256]);
     }
     {
       double w1 = 1.0 * n1[5344];
@@ -758,7 +758,7 @@ __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
       wk0 = fma(w2, k2[1696], wk0);
       wk0 = fma(w3, k3[1696], wk0);
       const double kk = ws[43584];
-      ws[266240] = fma(-kk, wk0, ws[266240]);
+      ws[272288] = fma(-kk, wk0, ws[272288]);
     }
     {
       double w1 = 1.0 * n1[5984];
@@ -777,7 +777,7 @@ __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
       wk1 = fma(w2, k2[6016], wk1);
       wk1 = fma(w3, k3[6016], wk1);
       const double kk = ws[43616];
-      ws[266272] = fma(-kk, fma(y[6016], wk0, y[5184] * wk1), ws[266272]);
+      ws[272320] = fma(-kk, fma(y[6016], wk0, y[5184] * wk1), ws[272320]);
       lam[5184] = fma(-kk, wk1, lam[5184]);
       lam[6016] = fma(-kk, wk0, lam[6016]);
     }
@@ -798,7 +798,7 @@ __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
       wk1 = fma(w2, k2[5984], wk1);
       wk1 = fma(w3, k3[5984], wk1);
       const double kk = ws[43648];
-      ws[266304] = fma(-kk, fma(y[5984], wk0, y[5184] * wk1), ws[266304]);
+      ws[272352] = fma(-kk, fma(y[5984], wk0, y[5184] * wk1), ws[272352]);
       lam[5184] = fma(-kk, wk1, lam[5184]);
       lam[5984] = fma(-kk, wk0, lam[5984]);
     }
@@ -819,7 +819,7 @@ __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
       wk1 = fma(w2, k2[5824], wk1);
       wk1 = fma(w3, k3[5824], wk1);
       const double kk = ws[43680];
-      ws[266336] = fma(-kk, fma(y[5824], wk0, y[5184] * wk1), ws[266336]);
+      ws[272384] = fma(-kk, fma(y[5824], wk0, y[5184] * wk1), ws[272384]);
       lam[5184] = fma(-kk, wk1, lam[5184]);
       lam[5824] = fma(-kk, wk0, lam[5824]);
     }
@@ -840,7 +840,7 @@ __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
       wk1 = fma(w2, k2[5920], wk1);
       wk1 = fma(w3, k3[5920], wk1);
       const double kk = ws[43712];
-      ws[266368] = fma(-kk, fma(y[5920], wk0, y[5184] * wk1), ws[266368]);
+      ws[272416] = fma(-kk, fma(y[5920], wk0, y[5184] * wk1), ws[272416]);
       lam[5184] = fma(-kk, wk1, lam[5184]);
       lam[5920] = fma(-kk, wk0, lam[5920]);
     }
@@ -855,7 +855,7 @@ __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
       wk0 = fma(w2, k2[2336], wk0);
       wk0 = fma(w3, k3[2336], wk0);
       const double kk = ws[43744];
-      ws[266400] = fma(-kk, wk0, ws[266400]);
+      ws[272448] = fma(-kk, wk0, ws[272448]);
     }
     {
       double w1 = -n1[2336];
@@ -871,7 +871,7 @@ __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
       wk1 = fma(w2, k2[5184], wk1);
       wk1 = fma(w3, k3[5184], wk1);
       const double kk = ws[43776];
-      ws[266432] = fma(-kk, fma(y[5184], wk0, y[2336] * wk1), ws[266432]);
+      ws[272480] = fma(-kk, fma(y[5184], wk0, y[2336] * wk1), ws[272480]);
       lam[2336] = fma(-kk, wk1, lam[2336]);
       lam[5184] = fma(-kk, wk0, lam[5184]);
     }
@@ -886,7 +886,7 @@ __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
       wk0 = fma(w2, k2[576], wk0);
       wk0 = fma(w3, k3[576], wk0);
       const double kk = ws[43808];
-      ws[266464] = fma(-kk, wk0, ws[266464]);
+      ws[272512] = fma(-kk, wk0, ws[272512]);
     }
     {
       double w1 = 1.0 * n1[2336];
@@ -899,7 +899,7 @@ __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
       wk0 = fma(w2, k2[576], wk0);
       wk0 = fma(w3, k3[576], wk0);
       const double kk = ws[43840];
-      ws[266496] = fma(-kk, wk0, ws[266496]);
+      ws[272544] = fma(-kk, wk0, ws[272544]);
     }
     {
       double w1 = 2.0 * n1[6016];
@@ -912,7 +912,7 @@ __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
       wk0 = fma(w2, k2[576], wk0);
       wk0 = fma(w3, k3[576], wk0);
       const double kk = ws[43872];
-      ws[266528] = fma(-kk, wk0, ws[266528]);
+      ws[272576] = fma(-kk, wk0, ws[272576]);
     }
     {
       double w1 = 1.0 * n1[5984];
@@ -925,7 +925,7 @@ __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
       wk0 = fma(w2, k2[6016], wk0);
       wk0 = fma(w3, k3[6016], wk0);
       const double kk = ws[43904];
-      ws[266560] = fma(-kk, wk0, ws[266560]);
+      ws[272608] = fma(-kk, wk0, ws[272608]);
     }
     {
       double w1 = -n1[6016];
@@ -941,7 +941,7 @@ __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
       wk1 = fma(w2, k2[5984], wk1);
       wk1 = fma(w3, k3[5984], wk1);
       const double kk = ws[43936];
-      ws[266592] = fma(-kk, fma(y[5984], wk0, y[6016] * wk1), ws[266592]);
+      ws[272640] = fma(-kk, fma(y[5984], wk0, y[6016] * wk1), ws[272640]);
       lam[6016] = fma(-kk, wk1, lam[6016]);
       lam[5984] = fma(-kk, wk0, lam[5984]);
     }
@@ -962,7 +962,7 @@ __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
       wk1 = fma(w2, k2[5984], wk1);
       wk1 = fma(w3, k3[5984], wk1);
       const double kk = ws[43968];
-      ws[266624] = fma(-kk, fma(y[5984], wk0, y[5984] * wk1), ws[266624]);
+      ws[272672] = fma(-kk, fma(y[5984], wk0, y[5984] * wk1), ws[272672]);
       lam[5984] = fma(-kk, wk1, lam[5984]);
       lam[5984] = fma(-kk, wk0, lam[5984]);
     }
@@ -983,7 +983,7 @@ __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
       wk1 = fma(w2, k2[5984], wk1);
       wk1 = fma(w3, k3[5984], wk1);
       const double kk = ws[44000];
-      ws[266656] = fma(-kk, fma(y[5984], wk0, y[5984] * wk1), ws[266656]);
+      ws[272704] = fma(-kk, fma(y[5984], wk0, y[5984] * wk1), ws[272704]);
       lam[5984] = fma(-kk, wk1, lam[5984]);
       lam[5984] = fma(-kk, wk0, lam[5984]);
     }
@@ -991,12 +991,12 @@ __device__ __noinline__ void adj_hess3_0_1(double* __restrict__ ws)
 __device__ __noinline__ void adj_hess3_0_2(double* __restrict__ ws)
 {
     const double* __restrict__ y = ws + 0;
-    double* __restrict__ lam = ws + 216608;
-    const double* __restrict__ n1 = ws + 222656;
+    double* __restrict__ lam = ws + 222656;
+    const double* __restrict__ n1 = ws + 228704;
     const double* __restrict__ k1 = ws + 24192;
-    const double* __restrict__ n2 = ws + 228704;
+    const double* __restrict__ n2 = ws + 234752;
     const double* __restrict__ k2 = ws + 30240;
-    const double* __restrict__ n3 = ws + 234752;
+    const double* __restrict__ n3 = ws + 240800;
     const double* __restrict__ k3 = ws + 36288;
     {
       double w1 = 1.0 * n1[5984];
@@ -1015,7 +1015,7 @@ __device__ __noinline__ void adj_hess3_0_2(double* __restrict__ ws)
       wk1 = fma(w2, k2[6016], wk1);
       wk1 = fma(w3, k3[6016], wk1);
       const double kk = ws[44032];
-      ws[266688] = fma(-kk, fma(y[6016], wk0, y[4000] * wk1), ws[266688]);
+      ws[272736] = fma(-kk, fma(y[6016], wk0, y[4000] * wk1), ws[272736]);
       lam[4000] = fma(-kk, wk1, lam[4000]);
       lam[6016] = fma(-kk, wk0, lam[6016]);
     }
@@ -1036,7 +1036,7 @@ __device__ __noinline__ void adj_hess3_0_2(double* __restrict__ ws)
       wk1 = fma(w2, k2[2336], wk1);
       wk1 = fma(w3, k3[2336], wk1);
       const double kk = ws[44064];
-      ws[266720] = fma(-kk, fma(y[2336], wk0, y[5824] * wk1), ws[266720]);
+      ws[272768] = fma(-kk, fma(y[2336], wk0, y[5824] * wk1), ws[272768]);
       lam[5824] = fma(-kk, wk1, lam[5824]);
       lam[2336] = fma(-kk, wk0, lam[2336]);
     }
@@ -1057,7 +1057,7 @@ __device__ __noinline__ void adj_hess3_0_2(double* __restrict__ ws)
       wk1 = fma(w2, k2[6016], wk1);
       wk1 = fma(w3, k3[6016], wk1);
       const double kk = ws[44096];
-      ws[266752] = fma(-kk, fma(y[6016], wk0, y[5824] * wk1), ws[266752]);
+      ws[272800] = fma(-kk, fma(y[6016], wk0, y[5824] * wk1), ws[272800]);
       lam[5824] = fma(-kk, wk1, lam[5824]);
       lam[6016] = fma(-kk, wk0, lam[6016]);
     }
@@ -1081,7 +1081,7 @@ __device__ __noinline__ void adj_hess3_0_2(double* __restrict__ ws)
       wk1 = fma(w2, k2[5984], wk1);
       wk1 = fma(w3, k3[5984], wk1);
       const double kk = ws[44128];
-      ws[266784] = fma(-kk, fma(y[5984], wk0, y[5824] * wk1), ws[266784]);
+      ws[272832] = fma(-kk, fma(y[5984], wk0, y[5824] * wk1), ws[272832]);
       lam[5824] = fma(-kk, wk1, lam[5824]);
       lam[5984] = fma(-kk, wk0, lam[5984]);
     }
@@ -1102,7 +1102,7 @@ __device__ __noinline__ void adj_hess3_0_2(double* __restrict__ ws)
       wk1 = fma(w2, k2[5984], wk1);
       wk1 = fma(w3, k3[5984], wk1);
       const double kk = ws[44160];
-      ws[266816] = fma(-kk, fma(y[5984], wk0, y[5824] * wk1), ws[266816]);
+      ws[272864] = fma(-kk, fma(y[5984], wk0, y[5824] * wk1), ws[272864]);
       lam[5824] = fma(-kk, wk1, lam[5824]);
       lam[5984] = fma(-kk, wk0, lam[5984]);
     }
@@ -1123,7 +1123,7 @@ __device__ __noinline__ void adj_hess3_0_2(double* __restrict__ ws)
       wk1 = fma(w2, k2[5824], wk1);
       wk1 = fma(w3, k3[5824], wk1);
       const double kk = ws[44192];
-      ws[266848] = fma(-kk, fma(y[5824], wk0, y[5824] * wk1), ws[266848]);
+      ws[272896] = fma(-kk, fma(y[5824], wk0, y[5824] * wk1), ws[272896]);
       lam[5824] = fma(-kk, wk1, lam[5824]);
       lam[5824] = fma(-kk, wk0, lam[5824]);
     }
@@ -1144,7 +1144,7 @@ __device__ __noinline__ void adj_hess3_0_2(double* __restrict__ ws)
       wk1 = fma(w2, k2[6016], wk1);
       wk1 = fma(w3, k3[6016], wk1);
       const double kk = ws[44224];
-      ws[266880] = fma(-kk, fma(y[6016], wk0, y[1184] * wk1), ws[266880]);
+      ws[272928] = fma(-kk, fma(y[6016], wk0, y[1184] * wk1), ws[272928]);
       lam[1184] = fma(-kk, wk1, lam[1184]);
       lam[6016] = fma(-kk, wk0, lam[6016]);
     }
@@ -1165,7 +1165,7 @@ __device__ __noinline__ void adj_hess3_0_2(double* __restrict__ ws)
       wk1 = fma(w2, k2[2336], wk1);
       wk1 = fma(w3, k3[2336], wk1);
       const double kk = ws[44256];
-      ws[266912] = fma(-kk, fma(y[2336], wk0, y[5920] * wk1), ws[266912]);
+      ws[272960] = fma(-kk, fma(y[2336], wk0, y[5920] * wk1), ws[272960]);
       lam[5920] = fma(-kk, wk1, lam[5920]);
       lam[2336] = fma(-kk, wk0, lam[2336]);
     }
@@ -1186,7 +1186,7 @@ __device__ __noinline__ void adj_hess3_0_2(double* __restrict__ ws)
       wk1 = fma(w2, k2[2336], wk1);
       wk1 = fma(w3, k3[2336], wk1);
       const double kk = ws[44288];
-      ws[266944] = fma(-kk, fma(y[2336], wk0, y[5920] * wk1), ws[266944]);
+      ws[272992] = fma(-kk, fma(y[2336], wk0, y[5920] * wk1), ws[272992]);
       lam[5920] = fma(-kk, wk1, lam[5920]);
       lam[2336] = fma(-kk, wk0, lam[2336]);
     }
@@ -1207,7 +1207,7 @@ __device__ __noinline__ void adj_hess3_0_2(double* __restrict__ ws)
       wk1 = fma(w2, k2[6016], wk1);
       wk1 = fma(w3, k3[6016], wk1);
       const double kk = ws[44320];
-      ws[266976] = fma(-kk, fma(y[6016], wk0, y[5920] * wk1), ws[266976]);
+      ws[273024] = fma(-kk, fma(y[6016], wk0, y[5920] * wk1), ws[273024]);
       lam[5920] = fma(-kk, wk1, lam[5920]);
       lam[6016] = fma(-kk, wk0, lam[6016]);
     }
@@ -1228,7 +1228,7 @@ __device__ __noinline__ void adj_hess3_0_2(double* __restrict__ ws)
       wk1 = fma(w2, k2[6016], wk1);
       wk1 = fma(w3, k3[6016], wk1);
       const double kk = ws[44352];
-      ws[267008] = fma(-kk, fma(y[6016], wk0, y[5024] * wk1), ws[267008]);
+      ws[273056] = fma(-kk, fma(y[6016], wk0, y[5024] * wk1), ws[273056]);
       lam[5024] = fma(-kk, wk1, lam[5024]);
       lam[6016] = fma(-kk, wk0, lam[6016]);
     }
@@ -1252,7 +1252,7 @@ __device__ __noinline__ void adj_hess3_0_2(double* __restrict__ ws)
       wk1 = fma(w2, k2[6016], wk1);
       wk1 = fma(w3, k3[6016], wk1);
       const double kk = ws[44384];
-      ws[267040] = fma(-kk, fma(y[6016], wk0, y[5952] * wk1), ws[267040]);
+      ws[273088] = fma(-kk, fma(y[6016], wk0, y[5952] * wk1), ws[273088]);
       lam[5952] = fma(-kk, wk1, lam[5952]);
       lam[6016] = fma(-kk, wk0, lam[6016]);
     }
@@ -1279,7 +1279,7 @@ __device__ __noinline__ void adj_hess3_0_2(double* __restrict__ ws)
       wk1 = fma(w2, k2[5984], wk1);
       wk1 = fma(w3, k3[5984], wk1);
       const double kk = ws[44416];
-      ws[267072] = fma(-kk, fma(y[5984], wk0, y[5952] * wk1), ws[267072]);
+      ws[273120] = fma(-kk, fma(y[5984], wk0, y[5952] * wk1), ws[273120]);
       lam[5952] = fma(-kk, wk1, lam[5952]);
       lam[5984] = fma(-kk, wk0, lam[5984]);
     }
@@ -1300,7 +1300,7 @@ __device__ __noinline__ void adj_hess3_0_2(double* __restrict__ ws)
       wk1 = fma(w2, k2[5824], wk1);
       wk1 = fma(w3, k3[5824], wk1);
       const double kk = ws[44448];
-      ws[267104] = fma(-kk, fma(y[5824], wk0, y[5952] * wk1), ws[267104]);
+      ws[273152] = fma(-kk, fma(y[5824], wk0, y[5952] * wk1), ws[273152]);
       lam[5952] = fma(-kk, wk1, lam[5952]);
       lam[5824] = fma(-kk, wk0, lam[5824]);
     }
@@ -1324,7 +1324,7 @@ __device__ __noinline__ void adj_hess3_0_2(double* __restrict__ ws)
       wk1 = fma(w2, k2[5920], wk1);
       wk1 = fma(w3, k3[5920], wk1);
       const double kk = ws[44480];
-      ws[267136] = fma(-kk, fma(y[5920], wk0, y[5952] * wk1), ws[267136]);
+      ws[273184] = fma(-kk, fma(y[5920], wk0, y[5952] * wk1), ws[273184]);
       lam[5952] = fma(-kk, wk1, lam[5952]);
       lam[5920] = fma(-kk, wk0, lam[5920]);
     }
@@ -1345,7 +1345,7 @@ __device__ __noinline__ void adj_hess3_0_2(double* __restrict__ ws)
       wk1 = fma(w2, k2[5952], wk1);
       wk1 = fma(w3, k3[5952], wk1);
       const double kk = ws[44512];
-      ws[267168] = fma(-kk, fma(y[5952], wk0, y[5952] * wk1), ws[267168]);
+      ws[273216] = fma(-kk, fma(y[5952], wk0, y[5952] * wk1), ws[273216]);
       lam[5952] = fma(-kk, wk1, lam[5952]);
       lam[5952] = fma(-kk, wk0, lam[5952]);
     }
@@ -1366,7 +1366,7 @@ __device__ __noinline__ void adj_hess3_0_2(double* __restrict__ ws)
       wk1 = fma(w2, k2[5920], wk1);
       wk1 = fma(w3, k3[5920], wk1);
       const double kk = ws[44544];
-      ws[267200] = fma(-kk, fma(y[5920], wk0, y[5952] * wk1), ws[267200]);
+      ws[273248] = fma(-kk, fma(y[5920], wk0, y[5952] * wk1), ws[273248]);
       lam[5952] = fma(-kk, wk1, lam[5952]);
       lam[5920] = fma(-kk, wk0, lam[5920]);
     }
@@ -1384,7 +1384,7 @@ __device__ __noinline__ void adj_hess3_0_2(double* __restrict__ ws)
       wk0 = fma(w2, k2[1024], wk0);
       wk0 = fma(w3, k3[1024], wk0);
       const double kk = ws[44576];
-      ws[267232] = fma(-kk, wk0, ws[267232]);
+      ws[273280] = fma(-kk, wk0, ws[273280]);
     }
     {
       double w1 = 2.0 * n1[5024];
@@ -1397,7 +1397,7 @@ __device__ __noinline__ void adj_hess3_0_2(double* __restrict__ ws)
       wk0 = fma(w2, k2[1024], wk0);
       wk0 = fma(w3, k3[1024], wk0);
       const double kk = ws[44608];
-      ws[267264] = fma(-kk, wk0, ws[267264]);
+      ws[273312] = fma(-kk, wk0, ws[273312]);
     }
     {
       double w1 = 1.0 * n1[1280];
@@ -1416,7 +1416,7 @@ __device__ __noinline__ void adj_hess3_0_2(double* __restrict__ ws)
       wk1 = fma(w2, k2[5984], wk1);
       wk1 = fma(w3, k3[5984], wk1);
       const double kk = ws[44640];
-      ws[267296] = fma(-kk, fma(y[5984], wk0, y[5920] * wk1), ws[267296]);
+      ws[273344] = fma(-kk, fma(y[5984], wk0, y[5920] * wk1), ws[273344]);
       lam[5920] = fma(-kk, wk1, lam[5920]);
       lam[5984] = fma(-kk, wk0, lam[5984]);
     }
@@ -1434,7 +1434,7 @@ __device__ __noinline__ void adj_hess3_0_2(double* __restrict__ ws)
       wk0 = fma(w2, k2[1280], wk0);
       wk0 = fma(w3, k3[1280], wk0);
       const double kk = ws[44672];
-      ws[267328] = fma(-kk, wk0, ws[267328]);
+      ws[273376] = fma(-kk, wk0, ws[273376]);
     }
     {
       double w1 = 1.0 * n1[5920];
@@ -1453,7 +1453,7 @@ __device__ __noinline__ void adj_hess3_0_2(double* __restrict__ ws)
       wk1 = fma(w2, k2[6016], wk1);
       wk1 = fma(w3, k3[6016], wk1);
       const double kk = ws[44704];
-      ws[267360] = fma(-kk, fma(y[6016], wk0, y[1280] * wk1), ws[267360]);
+      ws[273408] = fma(-kk, fma(y[6016], wk0, y[1280] * wk1), ws[273408]);
       lam[1280] = fma(-kk, wk1, lam[1280]);
       lam[6016] = fma(-kk, wk0, lam[6016]);
     }
@@ -1480,7 +1480,7 @@ __device__ __noinline__ void adj_hess3_0_2(double* __restrict__ ws)
       wk1 = fma(w2, k2[6016], wk1);
       wk1 = fma(w3, k3[6016], wk1);
       const double kk = ws[44736];
-      ws[267392] = fma(-kk, fma(y[6016], wk0, y[160] * wk1), ws[267392]);
+      ws[273440] = fma(-kk, fma(y[6016], wk0, y[160] * wk1), ws[273440]);
       lam[160] = fma(-kk, wk1, lam[160]);
       lam[6016] = fma(-kk, wk0, lam[6016]);
     }
@@ -1488,12 +1488,12 @@ __device__ __noinline__ void adj_hess3_0_2(double* __restrict__ ws)
 __device__ __noinline__ void adj_hess3_0_3(double* __restrict__ ws)
 {
     const double* __restrict__ y = ws + 0;
-    double* __restrict__ lam = ws + 216608;
-    const double* __restrict__ n1 = ws + 222656;
+    double* __restrict__ lam = ws + 222656;
+    const double* __restrict__ n1 = ws + 228704;
     const double* __restrict__ k1 = ws + 24192;
-    const double* __restrict__ n2 = ws + 228704;
+    const double* __restrict__ n2 = ws + 234752;
     const double* __restrict__ k2 = ws + 30240;
-    const double* __restrict__ n3 = ws + 234752;
+    const double* __restrict__ n3 = ws + 240800;
     const double* __restrict__ k3 = ws + 36288;
     {
       double w1 = 1.0 * n1[5984];
@@ -1512,7 +1512,7 @@ __device__ __noinline__ void adj_hess3_0_3(double* __restrict__ ws)
       wk1 = fma(w2, k2[6016], wk1);
       wk1 = fma(w3, k3[6016], wk1);
       const double kk = ws[44768];
-      ws[267424] = fma(-kk, fma(y[6016], wk0, y[5664] * wk1), ws[267424]);
+      ws[273472] = fma(-kk, fma(y[6016], wk0, y[5664] * wk1), ws[273472]);
       lam[5664] = fma(-kk, wk1, lam[5664]);
       lam[6016] = fma(-kk, wk0, lam[6016]);
     }
@@ -1527,7 +1527,7 @@ __device__ __noinline__ void adj_hess3_0_3(double* __restrict__ ws)
       wk0 = fma(w2, k2[6016], wk0);
       wk0 = fma(w3, k3[6016], wk0);
       const double kk = ws[44800];
-      ws[267456] = fma(-kk, wk0, ws[267456]);
+      ws[273504] = fma(-kk, wk0, ws[273504]);
     }
     {
       double w1 = 1.0 * n1[5632];
@@ -1546,7 +1546,7 @@ __device__ __noinline__ void adj_hess3_0_3(double* __restrict__ ws)
       wk1 = fma(w2, k2[6016], wk1);
       wk1 = fma(w3, k3[6016], wk1);
       const double kk = ws[44832];
-      ws[267488] = fma(-kk, fma(y[6016], wk0, y[1888] * wk1), ws[267488]);
+      ws[273536] = fma(-kk, fma(y[6016], wk0, y[1888] * wk1), ws[273536]);
       lam[1888] = fma(-kk, wk1, lam[1888]);
       lam[6016] = fma(-kk, wk0, lam[6016]);
     }
@@ -1570,7 +1570,7 @@ __device__ __noinline__ void adj_hess3_0_3(double* __restrict__ ws)
       wk1 = fma(w2, k2[6016], wk1);
       wk1 = fma(w3, k3[6016], wk1);
       const double kk = ws[44864];
-      ws[267520] = fma(-kk, fma(y[6016], wk0, y[2176] * wk1), ws[267520]);
+      ws[273568] = fma(-kk, fma(y[6016], wk0, y[2176] * wk1), ws[273568]);
       lam[2176] = fma(-kk, wk1, lam[2176]);
       lam[6016] = fma(-kk, wk0, lam[6016]);
     }
@@ -1594,7 +1594,7 @@ __device__ __noinline__ void adj_hess3_0_3(double* __restrict__ ws)
       wk1 = fma(w2, k2[6016], wk1);
       wk1 = fma(w3, k3[6016], wk1);
       const double kk = ws[44896];
-      ws[267552] = fma(-kk, fma(y[6016], wk0, y[1120] * wk1), ws[267552]);
+      ws[273600] = fma(-kk, fma(y[6016], wk0, y[1120] * wk1), ws[273600]);
       lam[1120] = fma(-kk, wk1, lam[1120]);
       lam[6016] = fma(-kk, wk0, lam[6016]);
     }
@@ -1615,7 +1615,7 @@ __device__ __noinline__ void adj_hess3_0_3(double* __restrict__ ws)
       wk1 = fma(w2, k2[6016], wk1);
       wk1 = fma(w3, k3[6016], wk1);
       const double kk = ws[44928];
-      ws[267584] = fma(-kk, fma(y[6016], wk0, y[2240] * wk1), ws[267584]);
+      ws[273632] = fma(-kk, fma(y[6016], wk0, y[2240] * wk1), ws[273632]);
       lam[2240] = fma(-kk, wk1, lam[2240]);
       lam[6016] = fma(-kk, wk0, lam[6016]);
     }
@@ -1636,7 +1636,7 @@ __device__ __noinline__ void adj_hess3_0_3(double* __restrict__ ws)
       wk1 = fma(w2, k2[6016], wk1);
       wk1 = fma(w3, k3[6016], wk1);
       const double kk = ws[44960];
-      ws[267616] = fma(-kk, fma(y[6016], wk0, y[2752] * wk1), ws[267616]);
+      ws[273664] = fma(-kk, fma(y[6016], wk0, y[2752] * wk1), ws[273664]);
       lam[2752] = fma(-kk, wk1, lam[2752]);
       lam[6016] = fma(-kk, wk0, lam[6016]);
     }
@@ -1657,7 +1657,7 @@ __device__ __noinline__ void adj_hess3_0_3(double* __restrict__ ws)
       wk1 = fma(w2, k2[6016], wk1);
       wk1 = fma(w3, k3[6016], wk1);
       const double kk = ws[44992];
-      ws[267648] = fma(-kk, fma(y[6016], wk0, y[1152] * wk1), ws[267648]);
+      ws[273696] = fma(-kk, fma(y[6016], wk0, y[1152] * wk1), ws[273696]);
       lam[1152] = fma(-kk, wk1, lam[1152]);
       lam[6016] = fma(-kk, wk0, lam[6016]);
     }
@@ -1690,7 +1690,7 @@ __device__ __noinline__ void adj_hess3_0_3(double* __restrict__ ws)
       wk1 = fma(w2, k2[6016], wk1);
       wk1 = fma(w3, k3[6016], wk1);
       const double kk = ws[45024];
-      ws[267680] = fma(-kk, fma(y[6016], wk0, y[256] * wk1), ws[267680]);
+      ws[273728] = fma(-kk, fma(y[6016], wk0, y[256] * wk1), ws[273728]);
       lam[256] = fma(-kk, wk1, lam[256]);
       lam[6016] = fma(-kk, wk0, lam[6016]);
     }
@@ -1717,7 +1717,7 @@ __device__ __noinline__ void adj_hess3_0_3(double* __restrict__ ws)
       wk1 = fma(w2, k2[6016], wk1);
       wk1 = fma(w3, k3[6016], wk1);
       const double kk = ws[45056];
-      ws[267712] = fma(-kk, fma(y[6016], wk0, y[1216] * wk1), ws[267712]);
+      ws[273760] = fma(-kk, fma(y[6016], wk0, y[1216] * wk1), ws[273760]);
       lam[1216] = fma(-kk, wk1, lam[1216]);
       lam[6016] = fma(-kk, wk0, lam[6016]);
     }
@@ -1744,7 +1744,7 @@ __device__ __noinline__ void adj_hess3_0_3(double* __restrict__ ws)
       wk1 = fma(w2, k2[6016], wk1);
       wk1 = fma(w3, k3[6016], wk1);
       const double kk = ws[45088];
-      ws[267744] = fma(-kk, fma(y[6016], wk0, y[288] * wk1), ws[267744]);
+      ws[273792] = fma(-kk, fma(y[6016], wk0, y[288] * wk1), ws[273792]);
       lam[288] = fma(-kk, wk1, lam[288]);
       lam[6016] = fma(-kk, wk0, lam[6016]);
     }
@@ -1771,7 +1771,7 @@ __device__ __noinline__ void adj_hess3_0_3(double* __restrict__ ws)
       wk1 = fma(w2, k2[6016], wk1);
       wk1 = fma(w3, k3[6016], wk1);
       const double kk = ws[45120];
-      ws[267776] = fma(-kk, fma(y[6016], wk0, y[320] * wk1), ws[267776]);
+      ws[273824] = fma(-kk, fma(y[6016], wk0, y[320] * wk1), ws[273824]);
       lam[320] = fma(-kk, wk1, lam[320]);
       lam[6016] = fma(-kk, wk0, lam[6016]);
     }
@@ -1798,7 +1798,7 @@ __device__ __noinline__ void adj_hess3_0_3(double* __restrict__ ws)
       wk1 = fma(w2, k2[6016], wk1);
       wk1 = fma(w3, k3[6016], wk1);
       const double kk = ws[45152];
-      ws[267808] = fma(-kk, fma(y[6016], wk0, y[352] * wk1), ws[267808]);
+      ws[273856] = fma(-kk, fma(y[6016], wk0, y[352] * wk1), ws[273856]);
       lam[352] = fma(-kk, wk1, lam[352]);
       lam[6016] = fma(-kk, wk0, lam[6016]);
     }
@@ -1852,7 +1852,7 @@ __device__ __noinline__ void adj_hess3_0_3(double* __restrict__ ws)
       wk1 = fma(w2, k2[5184], wk1);
       wk1 = fma(w3, k3[5184], wk1);
       const double kk = ws[45184];
-      ws[267840] = fma(-kk, fma(y[5184], wk0, y[1312] * wk1), ws[267840]);
+      ws[273888] = fma(-kk, fma(y[5184], wk0, y[1312] * wk1), ws[273888]);
       lam[1312] = fma(-kk, wk1, lam[1312]);
       lam[5184] = fma(-kk, wk0, lam[5184]);
     }
@@ -1888,7 +1888,7 @@ __device__ __noinline__ void adj_hess3_0_3(double* __restrict__ ws)
       wk1 = fma(w2, k2[5952], wk1);
       wk1 = fma(w3, k3[5952], wk1);
       const double kk = ws[45216];
-      ws[267872] = fma(-kk, fma(y[5952], wk0, y[1312] * wk1), ws[267872]);
+      ws[273920] = fma(-kk, fma(y[5952], wk0, y[1312] * wk1), ws[273920]);
       lam[1312] = fma(-kk, wk1, lam[1312]);
       lam[5952] = fma(-kk, wk0, lam[5952]);
     }
@@ -1918,7 +1918,7 @@ __device__ __noinline__ void adj_hess3_0_3(double* __restrict__ ws)
       wk1 = fma(w2, k2[6016], wk1);
       wk1 = fma(w3, k3[6016], wk1);
       const double kk = ws[45248];
-      ws[267904] = fma(-kk, fma(y[6016], wk0, y[1312] * wk1), ws[267904]);
+      ws[273952] = fma(-kk, fma(y[6016], wk0, y[1312] * wk1), ws[273952]);
       lam[1312] = fma(-kk, wk1, lam[1312]);
       lam[6016] = fma(-kk, wk0, lam[6016]);
     }
@@ -1945,7 +1945,7 @@ __device__ __noinline__ void adj_hess3_0_3(double* __restrict__ ws)
       wk1 = fma(w2, k2[5984], wk1);
       wk1 = fma(w3, k3[5984], wk1);
       const double kk = ws[45280];
-      ws[267936] = fma(-kk, fma(y[5984], wk0, y[4288] * wk1), ws[267936]);
+      ws[273984] = fma(-kk, fma(y[5984], wk0, y[4288] * wk1), ws[273984]);
       lam[4288] = fma(-kk, wk1, lam[4288]);
       lam[5984] = fma(-kk, wk0, lam[5984]);
     }
@@ -1981,7 +1981,7 @@ __device__ __noinline__ void adj_hess3_0_3(double* __restrict__ ws)
       wk1 = fma(w2, k2[5824], wk1);
       wk1 = fma(w3, k3[5824], wk1);
       const double kk = ws[45312];
-      ws[267968] = fma(-kk, fma(y[5824], wk0, y[4288] * wk1), ws[267968]);
+      ws[274016] = fma(-kk, fma(y[5824], wk0, y[4288] * wk1), ws[274016]);
       lam[4288] = fma(-kk, wk1, lam[4288]);
       lam[5824] = fma(-kk, wk0, lam[5824]);
     }

@@ -6,12 +6,12 @@ namespace mech_cracmm2 {
 __device__ __noinline__ void adj_hess3_0_32(double* __restrict__ ws)
 {
     const double* __restrict__ y = ws + 0;
-    double* __restrict__ lam = ws + 216608;
-    const double* __restrict__ n1 = ws + 222656;
+    double* __restrict__ lam = ws + 222656;
+    const double* __restrict__ n1 = ws + 228704;
     const double* __restrict__ k1 = ws + 24192;
-    const double* __restrict__ n2 = ws + 228704;
+    const double* __restrict__ n2 = ws + 234752;
     const double* __restrict__ k2 = ws + 30240;
-    const double* __restrict__ n3 = ws + 234752;
+    const double* __restrict__ n3 = ws + 240800;
     const double* __restrict__ k3 = ws + 36288;
     {
       double w1 = 1.0 * n1[6016];
@@ -66,7 +66,7 @@ __device__ __noinline__ void adj_hess3_0_32(double* __restrict__ ws)
       wk1 = fma(w2, k2[6016], wk1);
       wk1 = fma(w3, k3[6016], wk1);
       const double kk = ws[59008];
-      ws[281664] = fma(-kk, fma(y[6016], wk0, y[4608] * wk1), ws[281664]);
+      ws[287712] = fma(-kk, fma(y[6016], wk0, y[4608] * wk1), ws[287712]);
       lam[4608] = fma(-kk, wk1, lam[4608]);
       lam[6016] = fma(-kk, wk0, lam[6016]);
     }
@@ -87,7 +87,7 @@ __device__ __noinline__ void adj_hess3_0_32(double* __restrict__ ws)
       wk1 = fma(w2, k2[6016], wk1);
       wk1 = fma(w3, k3[6016], wk1);
       const double kk = ws[59040];
-      ws[281696] = fma(-kk, fma(y[6016], wk0, y[928] * wk1), ws[281696]);
+      ws[287744] = fma(-kk, fma(y[6016], wk0, y[928] * wk1), ws[287744]);
       lam[928] = fma(-kk, wk1, lam[928]);
       lam[6016] = fma(-kk, wk0, lam[6016]);
     }
@@ -105,7 +105,7 @@ __device__ __noinline__ void adj_hess3_0_32(double* __restrict__ ws)
       wk0 = fma(w2, k2[96], wk0);
       wk0 = fma(w3, k3[96], wk0);
       const double kk = ws[59072];
-      ws[281728] = fma(-kk, wk0, ws[281728]);
+      ws[287776] = fma(-kk, wk0, ws[287776]);
     }
     {
       double w1 = 1.0 * n1[960];
@@ -121,7 +121,7 @@ __device__ __noinline__ void adj_hess3_0_32(double* __restrict__ ws)
       wk0 = fma(w2, k2[128], wk0);
       wk0 = fma(w3, k3[128], wk0);
       const double kk = ws[59104];
-      ws[281760] = fma(-kk, wk0, ws[281760]);
+      ws[287808] = fma(-kk, wk0, ws[287808]);
     }
     {
       double w1 = 1.0 * n1[3488];
@@ -140,7 +140,7 @@ __device__ __noinline__ void adj_hess3_0_32(double* __restrict__ ws)
       wk1 = fma(w2, k2[6016], wk1);
       wk1 = fma(w3, k3[6016], wk1);
       const double kk = ws[59136];
-      ws[281792] = fma(-kk, fma(y[6016], wk0, y[992] * wk1), ws[281792]);
+      ws[287840] = fma(-kk, fma(y[6016], wk0, y[992] * wk1), ws[287840]);
       lam[992] = fma(-kk, wk1, lam[992]);
       lam[6016] = fma(-kk, wk0, lam[6016]);
     }
@@ -161,7 +161,7 @@ __device__ __noinline__ void adj_hess3_0_32(double* __restrict__ ws)
       wk1 = fma(w2, k2[5984], wk1);
       wk1 = fma(w3, k3[5984], wk1);
       const double kk = ws[59168];
-      ws[281824] = fma(-kk, fma(y[5984], wk0, y[3488] * wk1), ws[281824]);
+      ws[287872] = fma(-kk, fma(y[5984], wk0, y[3488] * wk1), ws[287872]);
       lam[3488] = fma(-kk, wk1, lam[3488]);
       lam[5984] = fma(-kk, wk0, lam[5984]);
     }
@@ -191,7 +191,7 @@ __device__ __noinline__ void adj_hess3_0_32(double* __restrict__ ws)
       wk1 = fma(w2, k2[5824], wk1);
       wk1 = fma(w3, k3[5824], wk1);
       const double kk = ws[59200];
-      ws[281856] = fma(-kk, fma(y[5824], wk0, y[3488] * wk1), ws[281856]);
+      ws[287904] = fma(-kk, fma(y[5824], wk0, y[3488] * wk1), ws[287904]);
       lam[3488] = fma(-kk, wk1, lam[3488]);
       lam[5824] = fma(-kk, wk0, lam[5824]);
     }
@@ -221,7 +221,7 @@ __device__ __noinline__ void adj_hess3_0_32(double* __restrict__ ws)
       wk1 = fma(w2, k2[5952], wk1);
       wk1 = fma(w3, k3[5952], wk1);
       const double kk = ws[59232];
-      ws[281888] = fma(-kk, fma(y[5952], wk0, y[3488] * wk1), ws[281888]);
+      ws[287936] = fma(-kk, fma(y[5952], wk0, y[3488] * wk1), ws[287936]);
       lam[3488] = fma(-kk, wk1, lam[3488]);
       lam[5952] = fma(-kk, wk0, lam[5952]);
     }
@@ -251,7 +251,7 @@ __device__ __noinline__ void adj_hess3_0_32(double* __restrict__ ws)
       wk1 = fma(w2, k2[5888], wk1);
       wk1 = fma(w3, k3[5888], wk1);
       const double kk = ws[59264];
-      ws[281920] = fma(-kk, fma(y[5888], wk0, y[3488] * wk1), ws[281920]);
+      ws[287968] = fma(-kk, fma(y[5888], wk0, y[3488] * wk1), ws[287968]);
       lam[3488] = fma(-kk, wk1, lam[3488]);
       lam[5888] = fma(-kk, wk0, lam[5888]);
     }
@@ -284,7 +284,7 @@ __device__ __noinline__ void adj_hess3_0_32(double* __restrict__ ws)
       wk1 = fma(w2, k2[5792], wk1);
       wk1 = fma(w3, k3[5792], wk1);
       const double kk = ws[59296];
-      ws[281952] = fma(-kk, fma(y[5792], wk0, y[3488] * wk1), ws[281952]);
+      ws[288000] = fma(-kk, fma(y[5792], wk0, y[3488] * wk1), ws[288000]);
       lam[3488] = fma(-kk, wk1, lam[3488]);
       lam[5792] = fma(-kk, wk0, lam[5792]);
     }

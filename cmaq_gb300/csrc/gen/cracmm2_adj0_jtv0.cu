@@ -13,21 +13,21 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[5184];
       const double kw = ws[42336] * w;
       out[5184] = out[5184] + kw;
-      ws[264992] = fma(kw, y[5184], ws[264992]);
+      ws[271040] = fma(kw, y[5184], ws[271040]);
     }
     {
       double w = 1.0 * phi[576];
       w = w - phi[5184];
       const double kw = ws[42368] * w;
       out[5184] = out[5184] + kw;
-      ws[265024] = fma(kw, y[5184], ws[265024]);
+      ws[271072] = fma(kw, y[5184], ws[271072]);
     }
     {
       double w = 2.0 * phi[6016];
       w = w - phi[4000];
       const double kw = ws[42400] * w;
       out[4000] = out[4000] + kw;
-      ws[265056] = fma(kw, y[4000], ws[265056]);
+      ws[271104] = fma(kw, y[4000], ws[271104]);
     }
     {
       double w = 1.0 * phi[2336];
@@ -35,14 +35,14 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[5920];
       const double kw = ws[42432] * w;
       out[5920] = out[5920] + kw;
-      ws[265088] = fma(kw, y[5920], ws[265088]);
+      ws[271136] = fma(kw, y[5920], ws[271136]);
     }
     {
       double w = 1.0 * phi[5824];
       w = w - phi[5952];
       const double kw = ws[42464] * w;
       out[5952] = out[5952] + kw;
-      ws[265120] = fma(kw, y[5952], ws[265120]);
+      ws[271168] = fma(kw, y[5952], ws[271168]);
     }
     {
       double w = 1.0 * phi[2336];
@@ -50,7 +50,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[5952];
       const double kw = ws[42496] * w;
       out[5952] = out[5952] + kw;
-      ws[265152] = fma(kw, y[5952], ws[265152]);
+      ws[271200] = fma(kw, y[5952], ws[271200]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -58,7 +58,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[1184];
       const double kw = ws[42528] * w;
       out[1184] = out[1184] + kw;
-      ws[265184] = fma(kw, y[1184], ws[265184]);
+      ws[271232] = fma(kw, y[1184], ws[271232]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -66,7 +66,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[5024];
       const double kw = ws[42560] * w;
       out[5024] = out[5024] + kw;
-      ws[265216] = fma(kw, y[5024], ws[265216]);
+      ws[271264] = fma(kw, y[5024], ws[271264]);
     }
     {
       double w = 0.2 * phi[6016];
@@ -76,14 +76,14 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[1280];
       const double kw = ws[42592] * w;
       out[1280] = out[1280] + kw;
-      ws[265248] = fma(kw, y[1280], ws[265248]);
+      ws[271296] = fma(kw, y[1280], ws[271296]);
     }
     {
       double w = 1.0 * phi[5664];
       w = w - phi[5856];
       const double kw = ws[42624] * w;
       out[5856] = out[5856] + kw;
-      ws[265280] = fma(kw, y[5856], ws[265280]);
+      ws[271328] = fma(kw, y[5856], ws[271328]);
     }
     {
       double w = 2.0 * phi[5984];
@@ -91,7 +91,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[5856];
       const double kw = ws[42656] * w;
       out[5856] = out[5856] + kw;
-      ws[265312] = fma(kw, y[5856], ws[265312]);
+      ws[271360] = fma(kw, y[5856], ws[271360]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -100,7 +100,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[5568];
       const double kw = ws[42688] * w;
       out[5568] = out[5568] + kw;
-      ws[265344] = fma(kw, y[5568], ws[265344]);
+      ws[271392] = fma(kw, y[5568], ws[271392]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -109,7 +109,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[5760];
       const double kw = ws[42720] * w;
       out[5760] = out[5760] + kw;
-      ws[265376] = fma(kw, y[5760], ws[265376]);
+      ws[271424] = fma(kw, y[5760], ws[271424]);
     }
     {
       double w = 1.0 * phi[5888];
@@ -117,7 +117,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[4480];
       const double kw = ws[42752] * w;
       out[4480] = out[4480] + kw;
-      ws[265408] = fma(kw, y[4480], ws[265408]);
+      ws[271456] = fma(kw, y[4480], ws[271456]);
     }
     {
       double w = 2.0 * phi[5888];
@@ -125,7 +125,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[4480];
       const double kw = ws[42784] * w;
       out[4480] = out[4480] + kw;
-      ws[265440] = fma(kw, y[4480], ws[265440]);
+      ws[271488] = fma(kw, y[4480], ws[271488]);
     }
     {
       double w = 1.22 * phi[5984];
@@ -137,7 +137,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[3872];
       const double kw = ws[42816] * w;
       out[3872] = out[3872] + kw;
-      ws[265472] = fma(kw, y[3872], ws[265472]);
+      ws[271520] = fma(kw, y[3872], ws[271520]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -146,7 +146,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[4544];
       const double kw = ws[42848] * w;
       out[4544] = out[4544] + kw;
-      ws[265504] = fma(kw, y[4544], ws[265504]);
+      ws[271552] = fma(kw, y[4544], ws[271552]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -155,7 +155,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[4576];
       const double kw = ws[42880] * w;
       out[4576] = out[4576] + kw;
-      ws[265536] = fma(kw, y[4576], ws[265536]);
+      ws[271584] = fma(kw, y[4576], ws[271584]);
     }
     {
       double w = 0.1 * phi[5888];
@@ -165,7 +165,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[5280];
       const double kw = ws[42912] * w;
       out[5280] = out[5280] + kw;
-      ws[265568] = fma(kw, y[5280], ws[265568]);
+      ws[271616] = fma(kw, y[5280], ws[271616]);
     }
     {
       double w = 1.5 * phi[5632];
@@ -174,7 +174,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[5504];
       const double kw = ws[42944] * w;
       out[5504] = out[5504] + kw;
-      ws[265600] = fma(kw, y[5504], ws[265600]);
+      ws[271648] = fma(kw, y[5504], ws[271648]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -183,7 +183,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[5344];
       const double kw = ws[42976] * w;
       out[5344] = out[5344] + kw;
-      ws[265632] = fma(kw, y[5344], ws[265632]);
+      ws[271680] = fma(kw, y[5344], ws[271680]);
     }
     {
       double w = 0.34 * phi[6016];
@@ -196,7 +196,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[4128];
       const double kw = ws[43008] * w;
       out[4128] = out[4128] + kw;
-      ws[265664] = fma(kw, y[4128], ws[265664]);
+      ws[271712] = fma(kw, y[4128], ws[271712]);
     }
     {
       double w = 0.3 * phi[5888];
@@ -206,14 +206,14 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[4736];
       const double kw = ws[43040] * w;
       out[4736] = out[4736] + kw;
-      ws[265696] = fma(kw, y[4736], ws[265696]);
+      ws[271744] = fma(kw, y[4736], ws[271744]);
     }
     {
       double w = 2.0 * phi[5664];
       w = w - phi[5376];
       const double kw = ws[43072] * w;
       out[5376] = out[5376] + kw;
-      ws[265728] = fma(kw, y[5376], ws[265728]);
+      ws[271776] = fma(kw, y[5376], ws[271776]);
     }
     {
       double w = 1.0 * phi[5856];
@@ -221,7 +221,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[5376];
       const double kw = ws[43104] * w;
       out[5376] = out[5376] + kw;
-      ws[265760] = fma(kw, y[5376], ws[265760]);
+      ws[271808] = fma(kw, y[5376], ws[271808]);
     }
     {
       double w = 2.0 * phi[5984];
@@ -229,7 +229,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[5376];
       const double kw = ws[43136] * w;
       out[5376] = out[5376] + kw;
-      ws[265792] = fma(kw, y[5376], ws[265792]);
+      ws[271840] = fma(kw, y[5376], ws[271840]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -238,7 +238,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[5248];
       const double kw = ws[43168] * w;
       out[5248] = out[5248] + kw;
-      ws[265824] = fma(kw, y[5248], ws[265824]);
+      ws[271872] = fma(kw, y[5248], ws[271872]);
     }
     {
       double w = 1.5 * phi[5984];
@@ -250,7 +250,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[5472];
       const double kw = ws[43200] * w;
       out[5472] = out[5472] + kw;
-      ws[265856] = fma(kw, y[5472], ws[265856]);
+      ws[271904] = fma(kw, y[5472], ws[271904]);
     }
     {
       double w = 1.5 * phi[5984];
@@ -262,7 +262,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[4320];
       const double kw = ws[43232] * w;
       out[4320] = out[4320] + kw;
-      ws[265888] = fma(kw, y[4320], ws[265888]);
+      ws[271936] = fma(kw, y[4320], ws[271936]);
     }
     {
       double w = 1.0 * phi[3232];
@@ -271,7 +271,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[4448];
       const double kw = ws[43264] * w;
       out[4448] = out[4448] + kw;
-      ws[265920] = fma(kw, y[4448], ws[265920]);
+      ws[271968] = fma(kw, y[4448], ws[271968]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -280,7 +280,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[2816];
       const double kw = ws[43296] * w;
       out[2816] = out[2816] + kw;
-      ws[265952] = fma(kw, y[2816], ws[265952]);
+      ws[272000] = fma(kw, y[2816], ws[272000]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -289,7 +289,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[5728];
       const double kw = ws[43328] * w;
       out[5728] = out[5728] + kw;
-      ws[265984] = fma(kw, y[5728], ws[265984]);
+      ws[272032] = fma(kw, y[5728], ws[272032]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -298,7 +298,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[4096];
       const double kw = ws[43360] * w;
       out[4096] = out[4096] + kw;
-      ws[266016] = fma(kw, y[4096], ws[266016]);
+      ws[272064] = fma(kw, y[4096], ws[272064]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -307,7 +307,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[4608];
       const double kw = ws[43392] * w;
       out[4608] = out[4608] + kw;
-      ws[266048] = fma(kw, y[4608], ws[266048]);
+      ws[272096] = fma(kw, y[4608], ws[272096]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -315,7 +315,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[3680];
       const double kw = ws[43424] * w;
       out[3680] = out[3680] + kw;
-      ws[266080] = fma(kw, y[3680], ws[266080]);
+      ws[272128] = fma(kw, y[3680], ws[272128]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -325,7 +325,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[5440];
       const double kw = ws[43456] * w;
       out[5440] = out[5440] + kw;
-      ws[266112] = fma(kw, y[5440], ws[266112]);
+      ws[272160] = fma(kw, y[5440], ws[272160]);
     }
     {
       double w = 1.0 * phi[5792];
@@ -333,7 +333,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[1088];
       const double kw = ws[43488] * w;
       out[1088] = out[1088] + kw;
-      ws[266144] = fma(kw, y[1088], ws[266144]);
+      ws[272192] = fma(kw, y[1088], ws[272192]);
     }
     {
       double w = 1.0 * phi[5888];
@@ -341,7 +341,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[1088];
       const double kw = ws[43520] * w;
       out[1088] = out[1088] + kw;
-      ws[266176] = fma(kw, y[1088], ws[266176]);
+      ws[272224] = fma(kw, y[1088], ws[272224]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -350,7 +350,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[4384];
       const double kw = ws[43552] * w;
       out[4384] = out[4384] + kw;
-      ws[266208] = fma(kw, y[4384], ws[266208]);
+      ws[272256] = fma(kw, y[4384], ws[272256]);
     }
     {
       double w = 1.0 * phi[5344];
@@ -358,7 +358,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[1696];
       const double kw = ws[43584] * w;
       out[1696] = out[1696] + kw;
-      ws[266240] = fma(kw, y[1696], ws[266240]);
+      ws[272288] = fma(kw, y[1696], ws[272288]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -367,7 +367,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43616] * w;
       out[5184] = fma(kw, y[6016], out[5184]);
       out[6016] = fma(kw, y[5184], out[6016]);
-      ws[266272] = fma(kw * y[5184], y[6016], ws[266272]);
+      ws[272320] = fma(kw * y[5184], y[6016], ws[272320]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -376,7 +376,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43648] * w;
       out[5184] = fma(kw, y[5984], out[5184]);
       out[5984] = fma(kw, y[5184], out[5984]);
-      ws[266304] = fma(kw * y[5184], y[5984], ws[266304]);
+      ws[272352] = fma(kw * y[5184], y[5984], ws[272352]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -385,7 +385,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43680] * w;
       out[5184] = fma(kw, y[5824], out[5184]);
       out[5824] = fma(kw, y[5184], out[5824]);
-      ws[266336] = fma(kw * y[5184], y[5824], ws[266336]);
+      ws[272384] = fma(kw * y[5184], y[5824], ws[272384]);
     }
     {
       double w = 1.0 * phi[5952];
@@ -394,14 +394,14 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43712] * w;
       out[5184] = fma(kw, y[5920], out[5184]);
       out[5920] = fma(kw, y[5184], out[5920]);
-      ws[266368] = fma(kw * y[5184], y[5920], ws[266368]);
+      ws[272416] = fma(kw * y[5184], y[5920], ws[272416]);
     }
     {
       double w = 1.0 * phi[5184];
       w = w - phi[2336];
       const double kw = ws[43744] * w;
       out[2336] = out[2336] + kw;
-      ws[266400] = fma(kw, y[2336], ws[266400]);
+      ws[272448] = fma(kw, y[2336], ws[272448]);
     }
     {
       double w = -phi[2336];
@@ -409,35 +409,35 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43776] * w;
       out[2336] = fma(kw, y[5184], out[2336]);
       out[5184] = fma(kw, y[2336], out[5184]);
-      ws[266432] = fma(kw * y[2336], y[5184], ws[266432]);
+      ws[272480] = fma(kw * y[2336], y[5184], ws[272480]);
     }
     {
       double w = 1.0 * phi[2336];
       w = w - phi[576];
       const double kw = ws[43808] * w;
       out[576] = out[576] + kw;
-      ws[266464] = fma(kw, y[576], ws[266464]);
+      ws[272512] = fma(kw, y[576], ws[272512]);
     }
     {
       double w = 1.0 * phi[2336];
       w = w - phi[576];
       const double kw = ws[43840] * w;
       out[576] = out[576] + kw;
-      ws[266496] = fma(kw, y[576], ws[266496]);
+      ws[272544] = fma(kw, y[576], ws[272544]);
     }
     {
       double w = 2.0 * phi[6016];
       w = w - phi[576];
       const double kw = ws[43872] * w;
       out[576] = out[576] + kw;
-      ws[266528] = fma(kw, y[576], ws[266528]);
+      ws[272576] = fma(kw, y[576], ws[272576]);
     }
     {
       double w = 1.0 * phi[5984];
       w = w - phi[6016];
       const double kw = ws[43904] * w;
       out[6016] = out[6016] + kw;
-      ws[266560] = fma(kw, y[6016], ws[266560]);
+      ws[272608] = fma(kw, y[6016], ws[272608]);
     }
     {
       double w = -phi[6016];
@@ -445,7 +445,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43936] * w;
       out[6016] = fma(kw, y[5984], out[6016]);
       out[5984] = fma(kw, y[6016], out[5984]);
-      ws[266592] = fma(kw * y[6016], y[5984], ws[266592]);
+      ws[272640] = fma(kw * y[6016], y[5984], ws[272640]);
     }
     {
       double w = 1.0 * phi[4000];
@@ -454,7 +454,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43968] * w;
       out[5984] = fma(kw, y[5984], out[5984]);
       out[5984] = fma(kw, y[5984], out[5984]);
-      ws[266624] = fma(kw * y[5984], y[5984], ws[266624]);
+      ws[272672] = fma(kw * y[5984], y[5984], ws[272672]);
     }
     {
       double w = 1.0 * phi[4000];
@@ -463,7 +463,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44000] * w;
       out[5984] = fma(kw, y[5984], out[5984]);
       out[5984] = fma(kw, y[5984], out[5984]);
-      ws[266656] = fma(kw * y[5984], y[5984], ws[266656]);
+      ws[272704] = fma(kw * y[5984], y[5984], ws[272704]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -472,7 +472,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44032] * w;
       out[4000] = fma(kw, y[6016], out[4000]);
       out[6016] = fma(kw, y[4000], out[6016]);
-      ws[266688] = fma(kw * y[4000], y[6016], ws[266688]);
+      ws[272736] = fma(kw * y[4000], y[6016], ws[272736]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -481,7 +481,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44064] * w;
       out[5824] = fma(kw, y[2336], out[5824]);
       out[2336] = fma(kw, y[5824], out[2336]);
-      ws[266720] = fma(kw * y[5824], y[2336], ws[266720]);
+      ws[272768] = fma(kw * y[5824], y[2336], ws[272768]);
     }
     {
       double w = 1.0 * phi[1184];
@@ -490,7 +490,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44096] * w;
       out[5824] = fma(kw, y[6016], out[5824]);
       out[6016] = fma(kw, y[5824], out[6016]);
-      ws[266752] = fma(kw * y[5824], y[6016], ws[266752]);
+      ws[272800] = fma(kw * y[5824], y[6016], ws[272800]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -500,7 +500,7 @@ __device__ __noinline__ void adj_jtv_0_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44128] * w;
       out[5824] = fma(kw, y[5984], out[5824]);
       out[5984] = fma(kw, y[5824], out[5984]);
-      ws[266784] = fma(kw * y[5824], y[5984], ws[266784]);
+      ws[272832] = fma(kw * y[5824], y[5984], ws[272832]);
     }
 }
 __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int phioff, int outoff)
@@ -515,7 +515,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44160] * w;
       out[5824] = fma(kw, y[5984], out[5824]);
       out[5984] = fma(kw, y[5824], out[5984]);
-      ws[266816] = fma(kw * y[5824], y[5984], ws[266816]);
+      ws[272864] = fma(kw * y[5824], y[5984], ws[272864]);
     }
     {
       double w = 2.0 * phi[5920];
@@ -524,7 +524,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44192] * w;
       out[5824] = fma(kw, y[5824], out[5824]);
       out[5824] = fma(kw, y[5824], out[5824]);
-      ws[266848] = fma(kw * y[5824], y[5824], ws[266848]);
+      ws[272896] = fma(kw * y[5824], y[5824], ws[272896]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -533,7 +533,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44224] * w;
       out[1184] = fma(kw, y[6016], out[1184]);
       out[6016] = fma(kw, y[1184], out[6016]);
-      ws[266880] = fma(kw * y[1184], y[6016], ws[266880]);
+      ws[272928] = fma(kw * y[1184], y[6016], ws[272928]);
     }
     {
       double w = 1.0 * phi[5824];
@@ -542,7 +542,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44256] * w;
       out[5920] = fma(kw, y[2336], out[5920]);
       out[2336] = fma(kw, y[5920], out[2336]);
-      ws[266912] = fma(kw * y[5920], y[2336], ws[266912]);
+      ws[272960] = fma(kw * y[5920], y[2336], ws[272960]);
     }
     {
       double w = 1.0 * phi[5952];
@@ -551,7 +551,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44288] * w;
       out[5920] = fma(kw, y[2336], out[5920]);
       out[2336] = fma(kw, y[5920], out[2336]);
-      ws[266944] = fma(kw * y[5920], y[2336], ws[266944]);
+      ws[272992] = fma(kw * y[5920], y[2336], ws[272992]);
     }
     {
       double w = 1.0 * phi[5024];
@@ -560,7 +560,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44320] * w;
       out[5920] = fma(kw, y[6016], out[5920]);
       out[6016] = fma(kw, y[5920], out[6016]);
-      ws[266976] = fma(kw * y[5920], y[6016], ws[266976]);
+      ws[273024] = fma(kw * y[5920], y[6016], ws[273024]);
     }
     {
       double w = 1.0 * phi[5952];
@@ -569,7 +569,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44352] * w;
       out[5024] = fma(kw, y[6016], out[5024]);
       out[6016] = fma(kw, y[5024], out[6016]);
-      ws[267008] = fma(kw * y[5024], y[6016], ws[267008]);
+      ws[273056] = fma(kw * y[5024], y[6016], ws[273056]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -579,7 +579,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44384] * w;
       out[5952] = fma(kw, y[6016], out[5952]);
       out[6016] = fma(kw, y[5952], out[6016]);
-      ws[267040] = fma(kw * y[5952], y[6016], ws[267040]);
+      ws[273088] = fma(kw * y[5952], y[6016], ws[273088]);
     }
     {
       double w = 0.7 * phi[6016];
@@ -590,7 +590,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44416] * w;
       out[5952] = fma(kw, y[5984], out[5952]);
       out[5984] = fma(kw, y[5952], out[5984]);
-      ws[267072] = fma(kw * y[5952], y[5984], ws[267072]);
+      ws[273120] = fma(kw * y[5952], y[5984], ws[273120]);
     }
     {
       double w = 2.0 * phi[5920];
@@ -599,7 +599,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44448] * w;
       out[5952] = fma(kw, y[5824], out[5952]);
       out[5824] = fma(kw, y[5952], out[5824]);
-      ws[267104] = fma(kw * y[5952], y[5824], ws[267104]);
+      ws[273152] = fma(kw * y[5952], y[5824], ws[273152]);
     }
     {
       double w = 1.0 * phi[5824];
@@ -609,7 +609,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44480] * w;
       out[5952] = fma(kw, y[5920], out[5952]);
       out[5920] = fma(kw, y[5952], out[5920]);
-      ws[267136] = fma(kw * y[5952], y[5920], ws[267136]);
+      ws[273184] = fma(kw * y[5952], y[5920], ws[273184]);
     }
     {
       double w = 2.0 * phi[5920];
@@ -618,7 +618,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44512] * w;
       out[5952] = fma(kw, y[5952], out[5952]);
       out[5952] = fma(kw, y[5952], out[5952]);
-      ws[267168] = fma(kw * y[5952], y[5952], ws[267168]);
+      ws[273216] = fma(kw * y[5952], y[5952], ws[273216]);
     }
     {
       double w = 1.0 * phi[1024];
@@ -627,7 +627,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44544] * w;
       out[5952] = fma(kw, y[5920], out[5952]);
       out[5920] = fma(kw, y[5952], out[5920]);
-      ws[267200] = fma(kw * y[5952], y[5920], ws[267200]);
+      ws[273248] = fma(kw * y[5952], y[5920], ws[273248]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -635,14 +635,14 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       w = w - phi[1024];
       const double kw = ws[44576] * w;
       out[1024] = out[1024] + kw;
-      ws[267232] = fma(kw, y[1024], ws[267232]);
+      ws[273280] = fma(kw, y[1024], ws[273280]);
     }
     {
       double w = 2.0 * phi[5024];
       w = w - phi[1024];
       const double kw = ws[44608] * w;
       out[1024] = out[1024] + kw;
-      ws[267264] = fma(kw, y[1024], ws[267264]);
+      ws[273312] = fma(kw, y[1024], ws[273312]);
     }
     {
       double w = 1.0 * phi[1280];
@@ -651,7 +651,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44640] * w;
       out[5920] = fma(kw, y[5984], out[5920]);
       out[5984] = fma(kw, y[5920], out[5984]);
-      ws[267296] = fma(kw * y[5920], y[5984], ws[267296]);
+      ws[273344] = fma(kw * y[5920], y[5984], ws[273344]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -659,7 +659,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       w = w - phi[1280];
       const double kw = ws[44672] * w;
       out[1280] = out[1280] + kw;
-      ws[267328] = fma(kw, y[1280], ws[267328]);
+      ws[273376] = fma(kw, y[1280], ws[273376]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -668,7 +668,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44704] * w;
       out[1280] = fma(kw, y[6016], out[1280]);
       out[6016] = fma(kw, y[1280], out[6016]);
-      ws[267360] = fma(kw * y[1280], y[6016], ws[267360]);
+      ws[273408] = fma(kw * y[1280], y[6016], ws[273408]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -679,7 +679,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44736] * w;
       out[160] = fma(kw, y[6016], out[160]);
       out[6016] = fma(kw, y[160], out[6016]);
-      ws[267392] = fma(kw * y[160], y[6016], ws[267392]);
+      ws[273440] = fma(kw * y[160], y[6016], ws[273440]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -688,14 +688,14 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44768] * w;
       out[5664] = fma(kw, y[6016], out[5664]);
       out[6016] = fma(kw, y[5664], out[6016]);
-      ws[267424] = fma(kw * y[5664], y[6016], ws[267424]);
+      ws[273472] = fma(kw * y[5664], y[6016], ws[273472]);
     }
     {
       double w = 1.0 * phi[5888];
       w = w - phi[6016];
       const double kw = ws[44800] * w;
       out[6016] = out[6016] + kw;
-      ws[267456] = fma(kw, y[6016], ws[267456]);
+      ws[273504] = fma(kw, y[6016], ws[273504]);
     }
     {
       double w = 1.0 * phi[5632];
@@ -704,7 +704,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44832] * w;
       out[1888] = fma(kw, y[6016], out[1888]);
       out[6016] = fma(kw, y[1888], out[6016]);
-      ws[267488] = fma(kw * y[1888], y[6016], ws[267488]);
+      ws[273536] = fma(kw * y[1888], y[6016], ws[273536]);
     }
     {
       double w = 1.0 * phi[5408];
@@ -714,7 +714,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44864] * w;
       out[2176] = fma(kw, y[6016], out[2176]);
       out[6016] = fma(kw, y[2176], out[6016]);
-      ws[267520] = fma(kw * y[2176], y[6016], ws[267520]);
+      ws[273568] = fma(kw * y[2176], y[6016], ws[273568]);
     }
     {
       double w = 1.0 * phi[5120];
@@ -724,7 +724,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44896] * w;
       out[1120] = fma(kw, y[6016], out[1120]);
       out[6016] = fma(kw, y[1120], out[6016]);
-      ws[267552] = fma(kw * y[1120], y[6016], ws[267552]);
+      ws[273600] = fma(kw * y[1120], y[6016], ws[273600]);
     }
     {
       double w = 1.0 * phi[3008];
@@ -733,7 +733,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44928] * w;
       out[2240] = fma(kw, y[6016], out[2240]);
       out[6016] = fma(kw, y[2240], out[6016]);
-      ws[267584] = fma(kw * y[2240], y[6016], ws[267584]);
+      ws[273632] = fma(kw * y[2240], y[6016], ws[273632]);
     }
     {
       double w = 1.0 * phi[3200];
@@ -742,7 +742,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44960] * w;
       out[2752] = fma(kw, y[6016], out[2752]);
       out[6016] = fma(kw, y[2752], out[6016]);
-      ws[267616] = fma(kw * y[2752], y[6016], ws[267616]);
+      ws[273664] = fma(kw * y[2752], y[6016], ws[273664]);
     }
     {
       double w = 1.0 * phi[3328];
@@ -751,7 +751,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44992] * w;
       out[1152] = fma(kw, y[6016], out[1152]);
       out[6016] = fma(kw, y[1152], out[6016]);
-      ws[267648] = fma(kw * y[1152], y[6016], ws[267648]);
+      ws[273696] = fma(kw * y[1152], y[6016], ws[273696]);
     }
     {
       double w = 0.65 * phi[6016];
@@ -764,7 +764,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45024] * w;
       out[256] = fma(kw, y[6016], out[256]);
       out[6016] = fma(kw, y[256], out[6016]);
-      ws[267680] = fma(kw * y[256], y[6016], ws[267680]);
+      ws[273728] = fma(kw * y[256], y[6016], ws[273728]);
     }
     {
       double w = 0.47 * phi[3360];
@@ -775,7 +775,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45056] * w;
       out[1216] = fma(kw, y[6016], out[1216]);
       out[6016] = fma(kw, y[1216], out[6016]);
-      ws[267712] = fma(kw * y[1216], y[6016], ws[267712]);
+      ws[273760] = fma(kw * y[1216], y[6016], ws[273760]);
     }
     {
       double w = 0.82 * phi[3296];
@@ -786,7 +786,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45088] * w;
       out[288] = fma(kw, y[6016], out[288]);
       out[6016] = fma(kw, y[288], out[6016]);
-      ws[267744] = fma(kw * y[288], y[6016], ws[267744]);
+      ws[273792] = fma(kw * y[288], y[6016], ws[273792]);
     }
     {
       double w = 0.83 * phi[3104];
@@ -797,7 +797,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45120] * w;
       out[320] = fma(kw, y[6016], out[320]);
       out[6016] = fma(kw, y[320], out[6016]);
-      ws[267776] = fma(kw * y[320], y[6016], ws[267776]);
+      ws[273824] = fma(kw * y[320], y[6016], ws[273824]);
     }
     {
       double w = 0.82 * phi[3264];
@@ -808,7 +808,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45152] * w;
       out[352] = fma(kw, y[6016], out[352]);
       out[6016] = fma(kw, y[352], out[6016]);
-      ws[267808] = fma(kw * y[352], y[6016], ws[267808]);
+      ws[273856] = fma(kw * y[352], y[6016], ws[273856]);
     }
     {
       double w = 0.25 * phi[6016];
@@ -828,7 +828,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45184] * w;
       out[1312] = fma(kw, y[5184], out[1312]);
       out[5184] = fma(kw, y[1312], out[5184]);
-      ws[267840] = fma(kw * y[1312], y[5184], ws[267840]);
+      ws[273888] = fma(kw * y[1312], y[5184], ws[273888]);
     }
     {
       double w = 0.4 * phi[5920];
@@ -842,7 +842,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45216] * w;
       out[1312] = fma(kw, y[5952], out[1312]);
       out[5952] = fma(kw, y[1312], out[5952]);
-      ws[267872] = fma(kw * y[1312], y[5952], ws[267872]);
+      ws[273920] = fma(kw * y[1312], y[5952], ws[273920]);
     }
     {
       double w = 1.0 * phi[4288];
@@ -854,7 +854,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45248] * w;
       out[1312] = fma(kw, y[6016], out[1312]);
       out[6016] = fma(kw, y[1312], out[6016]);
-      ws[267904] = fma(kw * y[1312], y[6016], ws[267904]);
+      ws[273952] = fma(kw * y[1312], y[6016], ws[273952]);
     }
     {
       double w = 1.0 * phi[1344];
@@ -865,7 +865,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45280] * w;
       out[4288] = fma(kw, y[5984], out[4288]);
       out[5984] = fma(kw, y[4288], out[5984]);
-      ws[267936] = fma(kw * y[4288], y[5984], ws[267936]);
+      ws[273984] = fma(kw * y[4288], y[5984], ws[273984]);
     }
     {
       double w = 0.13 * phi[2784];
@@ -879,7 +879,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45312] * w;
       out[4288] = fma(kw, y[5824], out[4288]);
       out[5824] = fma(kw, y[4288], out[5824]);
-      ws[267968] = fma(kw * y[4288], y[5824], ws[267968]);
+      ws[274016] = fma(kw * y[4288], y[5824], ws[274016]);
     }
     {
       double w = 1.0 * phi[4288];
@@ -888,7 +888,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45344] * w;
       out[1344] = fma(kw, y[6016], out[1344]);
       out[6016] = fma(kw, y[1344], out[6016]);
-      ws[268000] = fma(kw * y[1344], y[6016], ws[268000]);
+      ws[274048] = fma(kw * y[1344], y[6016], ws[274048]);
     }
     {
       double w = 0.04 * phi[5248];
@@ -906,7 +906,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45376] * w;
       out[1344] = fma(kw, y[6016], out[1344]);
       out[6016] = fma(kw, y[1344], out[6016]);
-      ws[268032] = fma(kw * y[1344], y[6016], ws[268032]);
+      ws[274080] = fma(kw * y[1344], y[6016], ws[274080]);
     }
     {
       double w = 0.45 * phi[6016];
@@ -917,7 +917,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45408] * w;
       out[1632] = fma(kw, y[5984], out[1632]);
       out[5984] = fma(kw, y[1632], out[5984]);
-      ws[268064] = fma(kw * y[1632], y[5984], ws[268064]);
+      ws[274112] = fma(kw * y[1632], y[5984], ws[274112]);
     }
     {
       double w = 0.15 * phi[4736];
@@ -930,7 +930,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45440] * w;
       out[1632] = fma(kw, y[5824], out[1632]);
       out[5824] = fma(kw, y[1632], out[5824]);
-      ws[268096] = fma(kw * y[1632], y[5824], ws[268096]);
+      ws[274144] = fma(kw * y[1632], y[5824], ws[274144]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -942,7 +942,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45472] * w;
       out[2784] = fma(kw, y[6016], out[2784]);
       out[6016] = fma(kw, y[2784], out[6016]);
-      ws[268128] = fma(kw * y[2784], y[6016], ws[268128]);
+      ws[274176] = fma(kw * y[2784], y[6016], ws[274176]);
     }
     {
       double w = 1.0 * phi[5664];
@@ -954,7 +954,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45504] * w;
       out[6016] = fma(kw, y[2208], out[6016]);
       out[2208] = fma(kw, y[6016], out[2208]);
-      ws[268160] = fma(kw * y[6016], y[2208], ws[268160]);
+      ws[274208] = fma(kw * y[6016], y[2208], ws[274208]);
     }
     {
       double w = 1.0 * phi[5024];
@@ -962,7 +962,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       w = w - phi[2784];
       const double kw = ws[45536] * w;
       out[2784] = out[2784] + kw;
-      ws[268192] = fma(kw, y[2784], ws[268192]);
+      ws[274240] = fma(kw, y[2784], ws[274240]);
     }
     {
       double w = 0.57 * phi[4128];
@@ -972,7 +972,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45568] * w;
       out[1664] = fma(kw, y[6016], out[1664]);
       out[6016] = fma(kw, y[1664], out[6016]);
-      ws[268224] = fma(kw * y[1664], y[6016], ws[268224]);
+      ws[274272] = fma(kw * y[1664], y[6016], ws[274272]);
     }
     {
       double w = 0.975 * phi[4160];
@@ -982,7 +982,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45600] * w;
       out[1408] = fma(kw, y[6016], out[1408]);
       out[6016] = fma(kw, y[1408], out[6016]);
-      ws[268256] = fma(kw * y[1408], y[6016], ws[268256]);
+      ws[274304] = fma(kw * y[1408], y[6016], ws[274304]);
     }
     {
       double w = 0.945 * phi[4192];
@@ -992,7 +992,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45632] * w;
       out[1440] = fma(kw, y[6016], out[1440]);
       out[6016] = fma(kw, y[1440], out[6016]);
-      ws[268288] = fma(kw * y[1440], y[6016], ws[268288]);
+      ws[274336] = fma(kw * y[1440], y[6016], ws[274336]);
     }
     {
       double w = 0.23 * phi[2560];
@@ -1002,7 +1002,7 @@ __device__ __noinline__ void adj_jtv_0_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45664] * w;
       out[4544] = fma(kw, y[6016], out[4544]);
       out[6016] = fma(kw, y[4544], out[6016]);
-      ws[268320] = fma(kw * y[4544], y[6016], ws[268320]);
+      ws[274368] = fma(kw * y[4544], y[6016], ws[274368]);
     }
 }
 __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int phioff, int outoff)
@@ -1018,7 +1018,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45696] * w;
       out[4576] = fma(kw, y[6016], out[4576]);
       out[6016] = fma(kw, y[4576], out[6016]);
-      ws[268352] = fma(kw * y[4576], y[6016], ws[268352]);
+      ws[274400] = fma(kw * y[4576], y[6016], ws[274400]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1028,7 +1028,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45728] * w;
       out[5856] = fma(kw, y[6016], out[5856]);
       out[6016] = fma(kw, y[5856], out[6016]);
-      ws[268384] = fma(kw * y[5856], y[6016], ws[268384]);
+      ws[274432] = fma(kw * y[5856], y[6016], ws[274432]);
     }
     {
       double w = 1.0 * phi[5792];
@@ -1037,7 +1037,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45760] * w;
       out[5568] = fma(kw, y[6016], out[5568]);
       out[6016] = fma(kw, y[5568], out[6016]);
-      ws[268416] = fma(kw * y[5568], y[6016], ws[268416]);
+      ws[274464] = fma(kw * y[5568], y[6016], ws[274464]);
     }
     {
       double w = 1.0 * phi[4800];
@@ -1046,7 +1046,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45792] * w;
       out[5760] = fma(kw, y[6016], out[5760]);
       out[6016] = fma(kw, y[5760], out[6016]);
-      ws[268448] = fma(kw * y[5760], y[6016], ws[268448]);
+      ws[274496] = fma(kw * y[5760], y[6016], ws[274496]);
     }
     {
       double w = 1.0 * phi[2848];
@@ -1055,7 +1055,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45824] * w;
       out[4480] = fma(kw, y[6016], out[4480]);
       out[6016] = fma(kw, y[4480], out[6016]);
-      ws[268480] = fma(kw * y[4480], y[6016], ws[268480]);
+      ws[274528] = fma(kw * y[4480], y[6016], ws[274528]);
     }
     {
       double w = 1.0 * phi[5152];
@@ -1064,7 +1064,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45856] * w;
       out[5280] = fma(kw, y[6016], out[5280]);
       out[6016] = fma(kw, y[5280], out[6016]);
-      ws[268512] = fma(kw * y[5280], y[6016], ws[268512]);
+      ws[274560] = fma(kw * y[5280], y[6016], ws[274560]);
     }
     {
       double w = 1.0 * phi[3776];
@@ -1073,7 +1073,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45888] * w;
       out[5504] = fma(kw, y[6016], out[5504]);
       out[6016] = fma(kw, y[5504], out[6016]);
-      ws[268544] = fma(kw * y[5504], y[6016], ws[268544]);
+      ws[274592] = fma(kw * y[5504], y[6016], ws[274592]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1083,7 +1083,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45920] * w;
       out[5344] = fma(kw, y[6016], out[5344]);
       out[6016] = fma(kw, y[5344], out[6016]);
-      ws[268576] = fma(kw * y[5344], y[6016], ws[268576]);
+      ws[274624] = fma(kw * y[5344], y[6016], ws[274624]);
     }
     {
       double w = 0.57 * phi[4672];
@@ -1093,7 +1093,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45952] * w;
       out[4128] = fma(kw, y[6016], out[4128]);
       out[6016] = fma(kw, y[4128], out[6016]);
-      ws[268608] = fma(kw * y[4128], y[6016], ws[268608]);
+      ws[274656] = fma(kw * y[4128], y[6016], ws[274656]);
     }
     {
       double w = 1.0 * phi[2880];
@@ -1102,7 +1102,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45984] * w;
       out[4736] = fma(kw, y[6016], out[4736]);
       out[6016] = fma(kw, y[4736], out[6016]);
-      ws[268640] = fma(kw * y[4736], y[6016], ws[268640]);
+      ws[274688] = fma(kw * y[4736], y[6016], ws[274688]);
     }
     {
       double w = 0.313 * phi[5792];
@@ -1112,7 +1112,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46016] * w;
       out[3872] = fma(kw, y[6016], out[3872]);
       out[6016] = fma(kw, y[3872], out[6016]);
-      ws[268672] = fma(kw * y[3872], y[6016], ws[268672]);
+      ws[274720] = fma(kw * y[3872], y[6016], ws[274720]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1122,7 +1122,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46048] * w;
       out[5376] = fma(kw, y[6016], out[5376]);
       out[6016] = fma(kw, y[5376], out[6016]);
-      ws[268704] = fma(kw * y[5376], y[6016], ws[268704]);
+      ws[274752] = fma(kw * y[5376], y[6016], ws[274752]);
     }
     {
       double w = 1.0 * phi[5792];
@@ -1132,7 +1132,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46080] * w;
       out[5248] = fma(kw, y[6016], out[5248]);
       out[6016] = fma(kw, y[5248], out[6016]);
-      ws[268736] = fma(kw * y[5248], y[6016], ws[268736]);
+      ws[274784] = fma(kw * y[5248], y[6016], ws[274784]);
     }
     {
       double w = 0.52 * phi[5984];
@@ -1146,7 +1146,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46112] * w;
       out[5472] = fma(kw, y[6016], out[5472]);
       out[6016] = fma(kw, y[5472], out[6016]);
-      ws[268768] = fma(kw * y[5472], y[6016], ws[268768]);
+      ws[274816] = fma(kw * y[5472], y[6016], ws[274816]);
     }
     {
       double w = 0.52 * phi[5984];
@@ -1160,7 +1160,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46144] * w;
       out[4320] = fma(kw, y[6016], out[4320]);
       out[6016] = fma(kw, y[4320], out[6016]);
-      ws[268800] = fma(kw * y[4320], y[6016], ws[268800]);
+      ws[274848] = fma(kw * y[4320], y[6016], ws[274848]);
     }
     {
       double w = 0.56 * phi[5984];
@@ -1174,7 +1174,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46176] * w;
       out[3584] = fma(kw, y[6016], out[3584]);
       out[6016] = fma(kw, y[3584], out[6016]);
-      ws[268832] = fma(kw * y[3584], y[6016], ws[268832]);
+      ws[274880] = fma(kw * y[3584], y[6016], ws[274880]);
     }
     {
       double w = 1.0 * phi[2592];
@@ -1183,7 +1183,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46208] * w;
       out[4448] = fma(kw, y[6016], out[4448]);
       out[6016] = fma(kw, y[4448], out[6016]);
-      ws[268864] = fma(kw * y[4448], y[6016], ws[268864]);
+      ws[274912] = fma(kw * y[4448], y[6016], ws[274912]);
     }
     {
       double w = 0.152 * phi[3616];
@@ -1196,7 +1196,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46240] * w;
       out[1248] = fma(kw, y[6016], out[1248]);
       out[6016] = fma(kw, y[1248], out[6016]);
-      ws[268896] = fma(kw * y[1248], y[6016], ws[268896]);
+      ws[274944] = fma(kw * y[1248], y[6016], ws[274944]);
     }
     {
       double w = 0.2 * phi[3616];
@@ -1209,7 +1209,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46272] * w;
       out[2944] = fma(kw, y[6016], out[2944]);
       out[6016] = fma(kw, y[2944], out[6016]);
-      ws[268928] = fma(kw * y[2944], y[6016], ws[268928]);
+      ws[274976] = fma(kw * y[2944], y[6016], ws[274976]);
     }
     {
       double w = 1.0 * phi[3808];
@@ -1218,7 +1218,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46304] * w;
       out[1760] = fma(kw, y[6016], out[1760]);
       out[6016] = fma(kw, y[1760], out[6016]);
-      ws[268960] = fma(kw * y[1760], y[6016], ws[268960]);
+      ws[275008] = fma(kw * y[1760], y[6016], ws[275008]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1228,7 +1228,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46336] * w;
       out[5600] = fma(kw, y[6016], out[5600]);
       out[6016] = fma(kw, y[5600], out[6016]);
-      ws[268992] = fma(kw * y[5600], y[6016], ws[268992]);
+      ws[275040] = fma(kw * y[5600], y[6016], ws[275040]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1238,7 +1238,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46368] * w;
       out[1472] = fma(kw, y[6016], out[1472]);
       out[6016] = fma(kw, y[1472], out[6016]);
-      ws[269024] = fma(kw * y[1472], y[6016], ws[269024]);
+      ws[275072] = fma(kw * y[1472], y[6016], ws[275072]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1249,7 +1249,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46400] * w;
       out[5056] = fma(kw, y[6016], out[5056]);
       out[6016] = fma(kw, y[5056], out[6016]);
-      ws[269056] = fma(kw * y[5056], y[6016], ws[269056]);
+      ws[275104] = fma(kw * y[5056], y[6016], ws[275104]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1259,7 +1259,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46432] * w;
       out[1504] = fma(kw, y[6016], out[1504]);
       out[6016] = fma(kw, y[1504], out[6016]);
-      ws[269088] = fma(kw * y[1504], y[6016], ws[269088]);
+      ws[275136] = fma(kw * y[1504], y[6016], ws[275136]);
     }
     {
       double w = 0.35 * phi[6016];
@@ -1270,7 +1270,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46464] * w;
       out[2816] = fma(kw, y[6016], out[2816]);
       out[6016] = fma(kw, y[2816], out[6016]);
-      ws[269120] = fma(kw * y[2816], y[6016], ws[269120]);
+      ws[275168] = fma(kw * y[2816], y[6016], ws[275168]);
     }
     {
       double w = 0.01 * phi[6016];
@@ -1283,7 +1283,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46496] * w;
       out[5728] = fma(kw, y[6016], out[5728]);
       out[6016] = fma(kw, y[5728], out[6016]);
-      ws[269152] = fma(kw * y[5728], y[6016], ws[269152]);
+      ws[275200] = fma(kw * y[5728], y[6016], ws[275200]);
     }
     {
       double w = 0.01 * phi[6016];
@@ -1296,7 +1296,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46528] * w;
       out[4096] = fma(kw, y[6016], out[4096]);
       out[6016] = fma(kw, y[4096], out[6016]);
-      ws[269184] = fma(kw * y[4096], y[6016], ws[269184]);
+      ws[275232] = fma(kw * y[4096], y[6016], ws[275232]);
     }
     {
       double w = 0.01 * phi[6016];
@@ -1309,7 +1309,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46560] * w;
       out[4608] = fma(kw, y[6016], out[4608]);
       out[6016] = fma(kw, y[4608], out[6016]);
-      ws[269216] = fma(kw * y[4608], y[6016], ws[269216]);
+      ws[275264] = fma(kw * y[4608], y[6016], ws[275264]);
     }
     {
       double w = 1.0 * phi[4672];
@@ -1318,7 +1318,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46592] * w;
       out[1792] = fma(kw, y[6016], out[1792]);
       out[6016] = fma(kw, y[1792], out[6016]);
-      ws[269248] = fma(kw * y[1792], y[6016], ws[269248]);
+      ws[275296] = fma(kw * y[1792], y[6016], ws[275296]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1327,7 +1327,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46624] * w;
       out[4352] = fma(kw, y[6016], out[4352]);
       out[6016] = fma(kw, y[4352], out[6016]);
-      ws[269280] = fma(kw * y[4352], y[6016], ws[269280]);
+      ws[275328] = fma(kw * y[4352], y[6016], ws[275328]);
     }
     {
       double w = 0.64 * phi[5888];
@@ -1337,7 +1337,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46656] * w;
       out[5696] = fma(kw, y[6016], out[5696]);
       out[6016] = fma(kw, y[5696], out[6016]);
-      ws[269312] = fma(kw * y[5696], y[6016], ws[269312]);
+      ws[275360] = fma(kw * y[5696], y[6016], ws[275360]);
     }
     {
       double w = 0.35 * phi[6016];
@@ -1349,7 +1349,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46688] * w;
       out[3680] = fma(kw, y[6016], out[3680]);
       out[6016] = fma(kw, y[3680], out[6016]);
-      ws[269344] = fma(kw * y[3680], y[6016], ws[269344]);
+      ws[275392] = fma(kw * y[3680], y[6016], ws[275392]);
     }
     {
       double w = 1.0 * phi[5216];
@@ -1360,7 +1360,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46720] * w;
       out[1088] = fma(kw, y[6016], out[1088]);
       out[6016] = fma(kw, y[1088], out[6016]);
-      ws[269376] = fma(kw * y[1088], y[6016], ws[269376]);
+      ws[275424] = fma(kw * y[1088], y[6016], ws[275424]);
     }
     {
       double w = 1.0 * phi[5216];
@@ -1371,7 +1371,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46752] * w;
       out[1536] = fma(kw, y[6016], out[1536]);
       out[6016] = fma(kw, y[1536], out[6016]);
-      ws[269408] = fma(kw * y[1536], y[6016], ws[269408]);
+      ws[275456] = fma(kw * y[1536], y[6016], ws[275456]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1381,7 +1381,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46784] * w;
       out[1824] = fma(kw, y[6016], out[1824]);
       out[6016] = fma(kw, y[1824], out[6016]);
-      ws[269440] = fma(kw * y[1824], y[6016], ws[269440]);
+      ws[275488] = fma(kw * y[1824], y[6016], ws[275488]);
     }
     {
       double w = 1.0 * phi[5408];
@@ -1391,7 +1391,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46816] * w;
       out[5440] = fma(kw, y[6016], out[5440]);
       out[6016] = fma(kw, y[5440], out[6016]);
-      ws[269472] = fma(kw * y[5440], y[6016], ws[269472]);
+      ws[275520] = fma(kw * y[5440], y[6016], ws[275520]);
     }
     {
       double w = 0.33 * phi[1696];
@@ -1405,7 +1405,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46848] * w;
       out[4384] = fma(kw, y[6016], out[4384]);
       out[6016] = fma(kw, y[4384], out[6016]);
-      ws[269504] = fma(kw * y[4384], y[6016], ws[269504]);
+      ws[275552] = fma(kw * y[4384], y[6016], ws[275552]);
     }
     {
       double w = 1.0 * phi[5344];
@@ -1415,7 +1415,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46880] * w;
       out[1696] = fma(kw, y[6016], out[1696]);
       out[6016] = fma(kw, y[1696], out[6016]);
-      ws[269536] = fma(kw * y[1696], y[6016], ws[269536]);
+      ws[275584] = fma(kw * y[1696], y[6016], ws[275584]);
     }
     {
       double w = 0.08 * phi[6016];
@@ -1428,7 +1428,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46912] * w;
       out[2240] = fma(kw, y[5184], out[2240]);
       out[5184] = fma(kw, y[2240], out[5184]);
-      ws[269568] = fma(kw * y[2240], y[5184], ws[269568]);
+      ws[275616] = fma(kw * y[2240], y[5184], ws[275616]);
     }
     {
       double w = 0.22 * phi[6016];
@@ -1457,7 +1457,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46944] * w;
       out[2752] = fma(kw, y[5184], out[2752]);
       out[5184] = fma(kw, y[2752], out[5184]);
-      ws[269600] = fma(kw * y[2752], y[5184], ws[269600]);
+      ws[275648] = fma(kw * y[2752], y[5184], ws[275648]);
     }
     {
       double w = 0.46 * phi[6016];
@@ -1482,7 +1482,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46976] * w;
       out[1152] = fma(kw, y[5184], out[1152]);
       out[5184] = fma(kw, y[1152], out[5184]);
-      ws[269632] = fma(kw * y[1152], y[5184], ws[269632]);
+      ws[275680] = fma(kw * y[1152], y[5184], ws[275680]);
     }
     {
       double w = 0.6055 * phi[6016];
@@ -1503,7 +1503,7 @@ __device__ __noinline__ void adj_jtv_0_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47008] * w;
       out[1408] = fma(kw, y[5184], out[1408]);
       out[5184] = fma(kw, y[1408], out[5184]);
-      ws[269664] = fma(kw * y[1408], y[5184], ws[269664]);
+      ws[275712] = fma(kw * y[1408], y[5184], ws[275712]);
     }
 }
 __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int phioff, int outoff)
@@ -1524,7 +1524,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47040] * w;
       out[1440] = fma(kw, y[5184], out[1440]);
       out[5184] = fma(kw, y[1440], out[5184]);
-      ws[269696] = fma(kw * y[1440], y[5184], ws[269696]);
+      ws[275744] = fma(kw * y[1440], y[5184], ws[275744]);
     }
     {
       double w = 0.09 * phi[6016];
@@ -1538,7 +1538,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47072] * w;
       out[4576] = fma(kw, y[5184], out[4576]);
       out[5184] = fma(kw, y[4576], out[5184]);
-      ws[269728] = fma(kw * y[4576], y[5184], ws[269728]);
+      ws[275776] = fma(kw * y[4576], y[5184], ws[275776]);
     }
     {
       double w = 0.33 * phi[1696];
@@ -1552,7 +1552,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47104] * w;
       out[4384] = fma(kw, y[5184], out[4384]);
       out[5184] = fma(kw, y[4384], out[5184]);
-      ws[269760] = fma(kw * y[4384], y[5184], ws[269760]);
+      ws[275808] = fma(kw * y[4384], y[5184], ws[275808]);
     }
     {
       double w = 0.19 * phi[6016];
@@ -1566,7 +1566,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47136] * w;
       out[4128] = fma(kw, y[5184], out[4128]);
       out[5184] = fma(kw, y[4128], out[5184]);
-      ws[269792] = fma(kw * y[4128], y[5184], ws[269792]);
+      ws[275840] = fma(kw * y[4128], y[5184], ws[275840]);
     }
     {
       double w = 0.16 * phi[6016];
@@ -1584,7 +1584,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47168] * w;
       out[4736] = fma(kw, y[5184], out[4736]);
       out[5184] = fma(kw, y[4736], out[5184]);
-      ws[269824] = fma(kw * y[4736], y[5184], ws[269824]);
+      ws[275872] = fma(kw * y[4736], y[5184], ws[275872]);
     }
     {
       double w = 0.1 * phi[6016];
@@ -1604,7 +1604,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47200] * w;
       out[3872] = fma(kw, y[5184], out[3872]);
       out[5184] = fma(kw, y[3872], out[5184]);
-      ws[269856] = fma(kw * y[3872], y[5184], ws[269856]);
+      ws[275904] = fma(kw * y[3872], y[5184], ws[275904]);
     }
     {
       double w = 0.05 * phi[6016];
@@ -1621,7 +1621,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47232] * w;
       out[5472] = fma(kw, y[5184], out[5472]);
       out[5184] = fma(kw, y[5472], out[5184]);
-      ws[269888] = fma(kw * y[5472], y[5184], ws[269888]);
+      ws[275936] = fma(kw * y[5472], y[5184], ws[275936]);
     }
     {
       double w = 0.05 * phi[6016];
@@ -1639,7 +1639,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47264] * w;
       out[4320] = fma(kw, y[5184], out[4320]);
       out[5184] = fma(kw, y[4320], out[5184]);
-      ws[269920] = fma(kw * y[4320], y[5184], ws[269920]);
+      ws[275968] = fma(kw * y[4320], y[5184], ws[275968]);
     }
     {
       double w = 0.05 * phi[6016];
@@ -1655,7 +1655,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47296] * w;
       out[3584] = fma(kw, y[5184], out[3584]);
       out[5184] = fma(kw, y[3584], out[5184]);
-      ws[269952] = fma(kw * y[3584], y[5184], ws[269952]);
+      ws[276000] = fma(kw * y[3584], y[5184], ws[276000]);
     }
     {
       double w = 1.0 * phi[3040];
@@ -1664,7 +1664,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47328] * w;
       out[3808] = fma(kw, y[5184], out[3808]);
       out[5184] = fma(kw, y[3808], out[5184]);
-      ws[269984] = fma(kw * y[3808], y[5184], ws[269984]);
+      ws[276032] = fma(kw * y[3808], y[5184], ws[276032]);
     }
     {
       double w = 0.8 * phi[4032];
@@ -1674,7 +1674,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47360] * w;
       out[2240] = fma(kw, y[5952], out[2240]);
       out[5952] = fma(kw, y[2240], out[5952]);
-      ws[270016] = fma(kw * y[2240], y[5952], ws[270016]);
+      ws[276064] = fma(kw * y[2240], y[5952], ws[276064]);
     }
     {
       double w = 0.43 * phi[4032];
@@ -1684,7 +1684,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47392] * w;
       out[2752] = fma(kw, y[5952], out[2752]);
       out[5952] = fma(kw, y[2752], out[5952]);
-      ws[270048] = fma(kw * y[2752], y[5952], ws[270048]);
+      ws[276096] = fma(kw * y[2752], y[5952], ws[276096]);
     }
     {
       double w = 0.11 * phi[4032];
@@ -1694,7 +1694,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47424] * w;
       out[1152] = fma(kw, y[5952], out[1152]);
       out[5952] = fma(kw, y[1152], out[5952]);
-      ws[270080] = fma(kw * y[1152], y[5952], ws[270080]);
+      ws[276128] = fma(kw * y[1152], y[5952], ws[276128]);
     }
     {
       double w = 0.975 * phi[2624];
@@ -1704,7 +1704,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47456] * w;
       out[1408] = fma(kw, y[5952], out[1408]);
       out[5952] = fma(kw, y[1408], out[5952]);
-      ws[270112] = fma(kw * y[1408], y[5952], ws[270112]);
+      ws[276160] = fma(kw * y[1408], y[5952], ws[276160]);
     }
     {
       double w = 0.945 * phi[2656];
@@ -1714,7 +1714,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47488] * w;
       out[1440] = fma(kw, y[5952], out[1440]);
       out[5952] = fma(kw, y[1440], out[5952]);
-      ws[270144] = fma(kw * y[1440], y[5952], ws[270144]);
+      ws[276192] = fma(kw * y[1440], y[5952], ws[276192]);
     }
     {
       double w = 0.33 * phi[1696];
@@ -1728,7 +1728,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47520] * w;
       out[4384] = fma(kw, y[5952], out[4384]);
       out[5952] = fma(kw, y[4384], out[5952]);
-      ws[270176] = fma(kw * y[4384], y[5952], ws[270176]);
+      ws[276224] = fma(kw * y[4384], y[5952], ws[276224]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1739,7 +1739,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47552] * w;
       out[5856] = fma(kw, y[5952], out[5856]);
       out[5952] = fma(kw, y[5856], out[5952]);
-      ws[270208] = fma(kw * y[5856], y[5952], ws[270208]);
+      ws[276256] = fma(kw * y[5856], y[5952], ws[276256]);
     }
     {
       double w = 1.0 * phi[5792];
@@ -1749,7 +1749,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47584] * w;
       out[5568] = fma(kw, y[5952], out[5568]);
       out[5952] = fma(kw, y[5568], out[5952]);
-      ws[270240] = fma(kw * y[5568], y[5952], ws[270240]);
+      ws[276288] = fma(kw * y[5568], y[5952], ws[276288]);
     }
     {
       double w = 1.0 * phi[4800];
@@ -1759,7 +1759,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47616] * w;
       out[5760] = fma(kw, y[5952], out[5760]);
       out[5952] = fma(kw, y[5760], out[5952]);
-      ws[270272] = fma(kw * y[5760], y[5952], ws[270272]);
+      ws[276320] = fma(kw * y[5760], y[5952], ws[276320]);
     }
     {
       double w = 0.68 * phi[5856];
@@ -1773,7 +1773,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47648] * w;
       out[4128] = fma(kw, y[5952], out[4128]);
       out[5952] = fma(kw, y[4128], out[5952]);
-      ws[270304] = fma(kw * y[4128], y[5952], ws[270304]);
+      ws[276352] = fma(kw * y[4128], y[5952], ws[276352]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1787,7 +1787,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47680] * w;
       out[3872] = fma(kw, y[5952], out[3872]);
       out[5952] = fma(kw, y[3872], out[5952]);
-      ws[270336] = fma(kw * y[3872], y[5952], ws[270336]);
+      ws[276384] = fma(kw * y[3872], y[5952], ws[276384]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1798,7 +1798,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47712] * w;
       out[5376] = fma(kw, y[5952], out[5376]);
       out[5952] = fma(kw, y[5376], out[5952]);
-      ws[270368] = fma(kw * y[5376], y[5952], ws[270368]);
+      ws[276416] = fma(kw * y[5376], y[5952], ws[276416]);
     }
     {
       double w = 1.0 * phi[5792];
@@ -1809,7 +1809,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47744] * w;
       out[5248] = fma(kw, y[5952], out[5248]);
       out[5952] = fma(kw, y[5248], out[5952]);
-      ws[270400] = fma(kw * y[5248], y[5952], ws[270400]);
+      ws[276448] = fma(kw * y[5248], y[5952], ws[276448]);
     }
     {
       double w = 0.152 * phi[3616];
@@ -1822,7 +1822,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47776] * w;
       out[1248] = fma(kw, y[5952], out[1248]);
       out[5952] = fma(kw, y[1248], out[5952]);
-      ws[270432] = fma(kw * y[1248], y[5952], ws[270432]);
+      ws[276480] = fma(kw * y[1248], y[5952], ws[276480]);
     }
     {
       double w = 0.2 * phi[3616];
@@ -1835,7 +1835,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47808] * w;
       out[2944] = fma(kw, y[5952], out[2944]);
       out[5952] = fma(kw, y[2944], out[5952]);
-      ws[270464] = fma(kw * y[2944], y[5952], ws[270464]);
+      ws[276512] = fma(kw * y[2944], y[5952], ws[276512]);
     }
     {
       double w = 1.0 * phi[3808];
@@ -1845,7 +1845,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47840] * w;
       out[1760] = fma(kw, y[5952], out[1760]);
       out[5952] = fma(kw, y[1760], out[5952]);
-      ws[270496] = fma(kw * y[1760], y[5952], ws[270496]);
+      ws[276544] = fma(kw * y[1760], y[5952], ws[276544]);
     }
     {
       double w = 1.0 * phi[4672];
@@ -1855,21 +1855,21 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47872] * w;
       out[1824] = fma(kw, y[5952], out[1824]);
       out[5952] = fma(kw, y[1824], out[5952]);
-      ws[270528] = fma(kw * y[1824], y[5952], ws[270528]);
+      ws[276576] = fma(kw * y[1824], y[5952], ws[276576]);
     }
     {
       double w = 1.0 * phi[4256];
       w = w - phi[2560];
       const double kw = ws[47904] * w;
       out[2560] = out[2560] + kw;
-      ws[270560] = fma(kw, y[2560], ws[270560]);
+      ws[276608] = fma(kw, y[2560], ws[276608]);
     }
     {
       double w = 1.0 * phi[4256];
       w = w - phi[1728];
       const double kw = ws[47936] * w;
       out[1728] = out[1728] + kw;
-      ws[270592] = fma(kw, y[1728], ws[270592]);
+      ws[276640] = fma(kw, y[1728], ws[276640]);
     }
     {
       double w = 1.0 * phi[1088];
@@ -1878,7 +1878,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47968] * w;
       out[5792] = fma(kw, y[5920], out[5792]);
       out[5920] = fma(kw, y[5792], out[5920]);
-      ws[270624] = fma(kw * y[5792], y[5920], ws[270624]);
+      ws[276672] = fma(kw * y[5792], y[5920], ws[276672]);
     }
     {
       double w = 1.0 * phi[5792];
@@ -1886,7 +1886,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       w = w - phi[1088];
       const double kw = ws[48000] * w;
       out[1088] = out[1088] + kw;
-      ws[270656] = fma(kw, y[1088], ws[270656]);
+      ws[276704] = fma(kw, y[1088], ws[276704]);
     }
     {
       double w = 1.0 * phi[1536];
@@ -1895,7 +1895,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48032] * w;
       out[4800] = fma(kw, y[5920], out[4800]);
       out[5920] = fma(kw, y[4800], out[5920]);
-      ws[270688] = fma(kw * y[4800], y[5920], ws[270688]);
+      ws[276736] = fma(kw * y[4800], y[5920], ws[276736]);
     }
     {
       double w = 1.0 * phi[4800];
@@ -1903,7 +1903,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       w = w - phi[1536];
       const double kw = ws[48064] * w;
       out[1536] = out[1536] + kw;
-      ws[270720] = fma(kw, y[1536], ws[270720]);
+      ws[276768] = fma(kw, y[1536], ws[276768]);
     }
     {
       double w = 1.0 * phi[1824];
@@ -1912,7 +1912,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48096] * w;
       out[4672] = fma(kw, y[5920], out[4672]);
       out[5920] = fma(kw, y[4672], out[5920]);
-      ws[270752] = fma(kw * y[4672], y[5920], ws[270752]);
+      ws[276800] = fma(kw * y[4672], y[5920], ws[276800]);
     }
     {
       double w = 1.0 * phi[4672];
@@ -1920,7 +1920,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       w = w - phi[1824];
       const double kw = ws[48128] * w;
       out[1824] = out[1824] + kw;
-      ws[270784] = fma(kw, y[1824], ws[270784]);
+      ws[276832] = fma(kw, y[1824], ws[276832]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1931,7 +1931,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48160] * w;
       out[5888] = fma(kw, y[5824], out[5888]);
       out[5824] = fma(kw, y[5888], out[5824]);
-      ws[270816] = fma(kw * y[5888], y[5824], ws[270816]);
+      ws[276864] = fma(kw * y[5888], y[5824], ws[276864]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1942,7 +1942,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48192] * w;
       out[5632] = fma(kw, y[5824], out[5632]);
       out[5824] = fma(kw, y[5632], out[5824]);
-      ws[270848] = fma(kw * y[5632], y[5824], ws[270848]);
+      ws[276896] = fma(kw * y[5632], y[5824], ws[276896]);
     }
     {
       double w = 0.66 * phi[5984];
@@ -1960,7 +1960,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48224] * w;
       out[5408] = fma(kw, y[5824], out[5408]);
       out[5824] = fma(kw, y[5408], out[5824]);
-      ws[270880] = fma(kw * y[5408], y[5824], ws[270880]);
+      ws[276928] = fma(kw * y[5408], y[5824], ws[276928]);
     }
     {
       double w = 0.2 * phi[5984];
@@ -1981,7 +1981,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48256] * w;
       out[5120] = fma(kw, y[5824], out[5120]);
       out[5824] = fma(kw, y[5120], out[5824]);
-      ws[270912] = fma(kw * y[5120], y[5824], ws[270912]);
+      ws[276960] = fma(kw * y[5120], y[5824], ws[276960]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1993,7 +1993,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48288] * w;
       out[3008] = fma(kw, y[5824], out[3008]);
       out[5824] = fma(kw, y[3008], out[5824]);
-      ws[270944] = fma(kw * y[3008], y[5824], ws[270944]);
+      ws[276992] = fma(kw * y[3008], y[5824], ws[276992]);
     }
     {
       double w = 0.78 * phi[5984];
@@ -2009,7 +2009,7 @@ __device__ __noinline__ void adj_jtv_0_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48320] * w;
       out[3200] = fma(kw, y[5824], out[3200]);
       out[5824] = fma(kw, y[3200], out[5824]);
-      ws[270976] = fma(kw * y[3200], y[5824], ws[270976]);
+      ws[277024] = fma(kw * y[3200], y[5824], ws[277024]);
     }
 }
 }  // namespace mech_cracmm2

@@ -22,7 +22,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48352] * w;
       out[3328] = fma(kw, y[5824], out[3328]);
       out[5824] = fma(kw, y[3328], out[5824]);
-      ws[271008] = fma(kw * y[3328], y[5824], ws[271008]);
+      ws[277056] = fma(kw * y[3328], y[5824], ws[277056]);
     }
     {
       double w = 0.0 * phi[5440];
@@ -40,7 +40,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48384] * w;
       out[3360] = fma(kw, y[5824], out[3360]);
       out[5824] = fma(kw, y[3360], out[5824]);
-      ws[271040] = fma(kw * y[3360], y[5824], ws[271040]);
+      ws[277088] = fma(kw * y[3360], y[5824], ws[277088]);
     }
     {
       double w = 0.0002 * phi[5440];
@@ -58,7 +58,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48416] * w;
       out[3296] = fma(kw, y[5824], out[3296]);
       out[5824] = fma(kw, y[3296], out[5824]);
-      ws[271072] = fma(kw * y[3296], y[5824], ws[271072]);
+      ws[277120] = fma(kw * y[3296], y[5824], ws[277120]);
     }
     {
       double w = 0.0001 * phi[5440];
@@ -76,7 +76,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48448] * w;
       out[3104] = fma(kw, y[5824], out[3104]);
       out[5824] = fma(kw, y[3104], out[5824]);
-      ws[271104] = fma(kw * y[3104], y[5824], ws[271104]);
+      ws[277152] = fma(kw * y[3104], y[5824], ws[277152]);
     }
     {
       double w = 0.0002 * phi[5440];
@@ -94,7 +94,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48480] * w;
       out[3264] = fma(kw, y[5824], out[3264]);
       out[5824] = fma(kw, y[3264], out[5824]);
-      ws[271136] = fma(kw * y[3264], y[5824], ws[271136]);
+      ws[277184] = fma(kw * y[3264], y[5824], ws[277184]);
     }
     {
       double w = 0.237 * phi[4384];
@@ -112,7 +112,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48512] * w;
       out[4160] = fma(kw, y[5824], out[4160]);
       out[5824] = fma(kw, y[4160], out[5824]);
-      ws[271168] = fma(kw * y[4160], y[5824], ws[271168]);
+      ws[277216] = fma(kw * y[4160], y[5824], ws[277216]);
     }
     {
       double w = 0.82 * phi[6016];
@@ -123,7 +123,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48544] * w;
       out[3744] = fma(kw, y[5824], out[3744]);
       out[5824] = fma(kw, y[3744], out[5824]);
-      ws[271200] = fma(kw * y[3744], y[5824], ws[271200]);
+      ws[277248] = fma(kw * y[3744], y[5824], ws[277248]);
     }
     {
       double w = 1.6955 * phi[5920];
@@ -139,7 +139,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48576] * w;
       out[2624] = fma(kw, y[5824], out[2624]);
       out[5824] = fma(kw, y[2624], out[5824]);
-      ws[271232] = fma(kw * y[2624], y[5824], ws[271232]);
+      ws[277280] = fma(kw * y[2624], y[5824], ws[277280]);
     }
     {
       double w = 0.82 * phi[5920];
@@ -150,7 +150,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48608] * w;
       out[3840] = fma(kw, y[5824], out[3840]);
       out[5824] = fma(kw, y[3840], out[5824]);
-      ws[271264] = fma(kw * y[3840], y[5824], ws[271264]);
+      ws[277312] = fma(kw * y[3840], y[5824], ws[277312]);
     }
     {
       double w = 0.23 * phi[4384];
@@ -163,7 +163,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48640] * w;
       out[4192] = fma(kw, y[5824], out[4192]);
       out[5824] = fma(kw, y[4192], out[5824]);
-      ws[271296] = fma(kw * y[4192], y[5824], ws[271296]);
+      ws[277344] = fma(kw * y[4192], y[5824], ws[277344]);
     }
     {
       double w = 0.77 * phi[6016];
@@ -174,7 +174,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48672] * w;
       out[3936] = fma(kw, y[5824], out[3936]);
       out[5824] = fma(kw, y[3936], out[5824]);
-      ws[271328] = fma(kw * y[3936], y[5824], ws[271328]);
+      ws[277376] = fma(kw * y[3936], y[5824], ws[277376]);
     }
     {
       double w = 0.57 * phi[4384];
@@ -187,7 +187,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48704] * w;
       out[2656] = fma(kw, y[5824], out[2656]);
       out[5824] = fma(kw, y[2656], out[5824]);
-      ws[271360] = fma(kw * y[2656], y[5824], ws[271360]);
+      ws[277408] = fma(kw * y[2656], y[5824], ws[277408]);
     }
     {
       double w = 0.77 * phi[5920];
@@ -198,7 +198,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48736] * w;
       out[3712] = fma(kw, y[5824], out[3712]);
       out[5824] = fma(kw, y[3712], out[5824]);
-      ws[271392] = fma(kw * y[3712], y[5824], ws[271392]);
+      ws[277440] = fma(kw * y[3712], y[5824], ws[277440]);
     }
     {
       double w = 0.36 * phi[4384];
@@ -209,7 +209,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48768] * w;
       out[2560] = fma(kw, y[5824], out[2560]);
       out[5824] = fma(kw, y[2560], out[5824]);
-      ws[271424] = fma(kw * y[2560], y[5824], ws[271424]);
+      ws[277472] = fma(kw * y[2560], y[5824], ws[277472]);
     }
     {
       double w = 0.64 * phi[4384];
@@ -222,7 +222,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48800] * w;
       out[1728] = fma(kw, y[5824], out[1728]);
       out[5824] = fma(kw, y[1728], out[5824]);
-      ws[271456] = fma(kw * y[1728], y[5824], ws[271456]);
+      ws[277504] = fma(kw * y[1728], y[5824], ws[277504]);
     }
     {
       double w = 1.0 * phi[5888];
@@ -232,7 +232,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48832] * w;
       out[5792] = fma(kw, y[5824], out[5792]);
       out[5824] = fma(kw, y[5792], out[5824]);
-      ws[271488] = fma(kw * y[5792], y[5824], ws[271488]);
+      ws[277536] = fma(kw * y[5792], y[5824], ws[277536]);
     }
     {
       double w = 1.0 * phi[5632];
@@ -242,7 +242,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48864] * w;
       out[4800] = fma(kw, y[5824], out[4800]);
       out[5824] = fma(kw, y[4800], out[5824]);
-      ws[271520] = fma(kw * y[4800], y[5824], ws[271520]);
+      ws[277568] = fma(kw * y[4800], y[5824], ws[277568]);
     }
     {
       double w = 1.0 * phi[5792];
@@ -253,7 +253,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48896] * w;
       out[2848] = fma(kw, y[5824], out[2848]);
       out[5824] = fma(kw, y[2848], out[5824]);
-      ws[271552] = fma(kw * y[2848], y[5824], ws[271552]);
+      ws[277600] = fma(kw * y[2848], y[5824], ws[277600]);
     }
     {
       double w = 0.67 * phi[5984];
@@ -265,7 +265,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48928] * w;
       out[5152] = fma(kw, y[5824], out[5152]);
       out[5824] = fma(kw, y[5152], out[5824]);
-      ws[271584] = fma(kw * y[5152], y[5824], ws[271584]);
+      ws[277632] = fma(kw * y[5152], y[5824], ws[277632]);
     }
     {
       double w = 0.77 * phi[5984];
@@ -279,7 +279,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48960] * w;
       out[3776] = fma(kw, y[5824], out[3776]);
       out[5824] = fma(kw, y[3776], out[5824]);
-      ws[271616] = fma(kw * y[3776], y[5824], ws[271616]);
+      ws[277664] = fma(kw * y[3776], y[5824], ws[277664]);
     }
     {
       double w = 0.65 * phi[5888];
@@ -292,7 +292,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48992] * w;
       out[4672] = fma(kw, y[5824], out[4672]);
       out[5824] = fma(kw, y[4672], out[5824]);
-      ws[271648] = fma(kw * y[4672], y[5824], ws[271648]);
+      ws[277696] = fma(kw * y[4672], y[5824], ws[277696]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -304,7 +304,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49024] * w;
       out[3520] = fma(kw, y[5824], out[3520]);
       out[5824] = fma(kw, y[3520], out[5824]);
-      ws[271680] = fma(kw * y[3520], y[5824], ws[271680]);
+      ws[277728] = fma(kw * y[3520], y[5824], ws[277728]);
     }
     {
       double w = 0.3 * phi[5984];
@@ -319,7 +319,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49056] * w;
       out[2880] = fma(kw, y[5824], out[2880]);
       out[5824] = fma(kw, y[2880], out[5824]);
-      ws[271712] = fma(kw * y[2880], y[5824], ws[271712]);
+      ws[277760] = fma(kw * y[2880], y[5824], ws[277760]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -335,7 +335,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49088] * w;
       out[2912] = fma(kw, y[5824], out[2912]);
       out[5824] = fma(kw, y[2912], out[5824]);
-      ws[271744] = fma(kw * y[2912], y[5824], ws[271744]);
+      ws[277792] = fma(kw * y[2912], y[5824], ws[277792]);
     }
     {
       double w = 1.0 * phi[2272];
@@ -345,7 +345,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49120] * w;
       out[2592] = fma(kw, y[5824], out[2592]);
       out[5824] = fma(kw, y[2592], out[5824]);
-      ws[271776] = fma(kw * y[2592], y[5824], ws[271776]);
+      ws[277824] = fma(kw * y[2592], y[5824], ws[277824]);
     }
     {
       double w = 1.0 * phi[2688];
@@ -355,7 +355,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49152] * w;
       out[2272] = fma(kw, y[5824], out[2272]);
       out[5824] = fma(kw, y[2272], out[5824]);
-      ws[271808] = fma(kw * y[2272], y[5824], ws[271808]);
+      ws[277856] = fma(kw * y[2272], y[5824], ws[277856]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -368,7 +368,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49184] * w;
       out[3648] = fma(kw, y[5824], out[3648]);
       out[5824] = fma(kw, y[3648], out[5824]);
-      ws[271840] = fma(kw * y[3648], y[5824], ws[271840]);
+      ws[277888] = fma(kw * y[3648], y[5824], ws[277888]);
     }
     {
       double w = 1.0 * phi[3808];
@@ -378,7 +378,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49216] * w;
       out[3040] = fma(kw, y[5824], out[3040]);
       out[5824] = fma(kw, y[3040], out[5824]);
-      ws[271872] = fma(kw * y[3040], y[5824], ws[271872]);
+      ws[277920] = fma(kw * y[3040], y[5824], ws[277920]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -389,7 +389,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49248] * w;
       out[2976] = fma(kw, y[5824], out[2976]);
       out[5824] = fma(kw, y[2976], out[5824]);
-      ws[271904] = fma(kw * y[2976], y[5824], ws[271904]);
+      ws[277952] = fma(kw * y[2976], y[5824], ws[277952]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -400,7 +400,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49280] * w;
       out[4032] = fma(kw, y[5824], out[4032]);
       out[5824] = fma(kw, y[4032], out[5824]);
-      ws[271936] = fma(kw * y[4032], y[5824], ws[271936]);
+      ws[277984] = fma(kw * y[4032], y[5824], ws[277984]);
     }
     {
       double w = 2.0 * phi[5920];
@@ -412,7 +412,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49312] * w;
       out[4064] = fma(kw, y[5824], out[4064]);
       out[5824] = fma(kw, y[4064], out[5824]);
-      ws[271968] = fma(kw * y[4064], y[5824], ws[271968]);
+      ws[278016] = fma(kw * y[4064], y[5824], ws[278016]);
     }
     {
       double w = 2.0 * phi[5920];
@@ -423,7 +423,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49344] * w;
       out[3072] = fma(kw, y[5824], out[3072]);
       out[5824] = fma(kw, y[3072], out[5824]);
-      ws[272000] = fma(kw * y[3072], y[5824], ws[272000]);
+      ws[278048] = fma(kw * y[3072], y[5824], ws[278048]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -432,7 +432,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49376] * w;
       out[5216] = fma(kw, y[5824], out[5216]);
       out[5824] = fma(kw, y[5216], out[5824]);
-      ws[272032] = fma(kw * y[5216], y[5824], ws[272032]);
+      ws[278080] = fma(kw * y[5216], y[5824], ws[278080]);
     }
     {
       double w = 1.0 * phi[5440];
@@ -441,7 +441,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49408] * w;
       out[2688] = fma(kw, y[5920], out[2688]);
       out[5920] = fma(kw, y[2688], out[5920]);
-      ws[272064] = fma(kw * y[2688], y[5920], ws[272064]);
+      ws[278112] = fma(kw * y[2688], y[5920], ws[278112]);
     }
     {
       double w = 1.0 * phi[5440];
@@ -450,7 +450,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49440] * w;
       out[3232] = fma(kw, y[5920], out[3232]);
       out[5920] = fma(kw, y[3232], out[5920]);
-      ws[272096] = fma(kw * y[3232], y[5920], ws[272096]);
+      ws[278144] = fma(kw * y[3232], y[5920], ws[278144]);
     }
     {
       double w = 1.0 * phi[5440];
@@ -459,7 +459,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49472] * w;
       out[3808] = fma(kw, y[5920], out[3808]);
       out[5920] = fma(kw, y[3808], out[5920]);
-      ws[272128] = fma(kw * y[3808], y[5920], ws[272128]);
+      ws[278176] = fma(kw * y[3808], y[5920], ws[278176]);
     }
     {
       double w = 1.0 * phi[2816];
@@ -468,7 +468,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49504] * w;
       out[5888] = fma(kw, y[5984], out[5888]);
       out[5984] = fma(kw, y[5888], out[5984]);
-      ws[272160] = fma(kw * y[5888], y[5984], ws[272160]);
+      ws[278208] = fma(kw * y[5888], y[5984], ws[278208]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -477,7 +477,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49536] * w;
       out[5632] = fma(kw, y[5984], out[5632]);
       out[5984] = fma(kw, y[5632], out[5984]);
-      ws[272192] = fma(kw * y[5632], y[5984], ws[272192]);
+      ws[278240] = fma(kw * y[5632], y[5984], ws[278240]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -486,7 +486,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49568] * w;
       out[5408] = fma(kw, y[5984], out[5408]);
       out[5984] = fma(kw, y[5408], out[5984]);
-      ws[272224] = fma(kw * y[5408], y[5984], ws[272224]);
+      ws[278272] = fma(kw * y[5408], y[5984], ws[278272]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -495,7 +495,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49600] * w;
       out[5120] = fma(kw, y[5984], out[5120]);
       out[5984] = fma(kw, y[5120], out[5984]);
-      ws[272256] = fma(kw * y[5120], y[5984], ws[272256]);
+      ws[278304] = fma(kw * y[5120], y[5984], ws[278304]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -504,7 +504,7 @@ __device__ __noinline__ void adj_jtv_0_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49632] * w;
       out[3008] = fma(kw, y[5984], out[3008]);
       out[5984] = fma(kw, y[3008], out[5984]);
-      ws[272288] = fma(kw * y[3008], y[5984], ws[272288]);
+      ws[278336] = fma(kw * y[3008], y[5984], ws[278336]);
     }
 }
 __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int phioff, int outoff)
@@ -519,7 +519,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49664] * w;
       out[3200] = fma(kw, y[5984], out[3200]);
       out[5984] = fma(kw, y[3200], out[5984]);
-      ws[272320] = fma(kw * y[3200], y[5984], ws[272320]);
+      ws[278368] = fma(kw * y[3200], y[5984], ws[278368]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -528,7 +528,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49696] * w;
       out[3328] = fma(kw, y[5984], out[3328]);
       out[5984] = fma(kw, y[3328], out[5984]);
-      ws[272352] = fma(kw * y[3328], y[5984], ws[272352]);
+      ws[278400] = fma(kw * y[3328], y[5984], ws[278400]);
     }
     {
       double w = 0.6021 * phi[5728];
@@ -538,7 +538,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49728] * w;
       out[3360] = fma(kw, y[5984], out[3360]);
       out[5984] = fma(kw, y[3360], out[5984]);
-      ws[272384] = fma(kw * y[3360], y[5984], ws[272384]);
+      ws[278432] = fma(kw * y[3360], y[5984], ws[278432]);
     }
     {
       double w = 0.7195 * phi[5728];
@@ -548,7 +548,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49760] * w;
       out[3296] = fma(kw, y[5984], out[3296]);
       out[5984] = fma(kw, y[3296], out[5984]);
-      ws[272416] = fma(kw * y[3296], y[5984], ws[272416]);
+      ws[278464] = fma(kw * y[3296], y[5984], ws[278464]);
     }
     {
       double w = 0.0482 * phi[5728];
@@ -559,7 +559,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49792] * w;
       out[3104] = fma(kw, y[5984], out[3104]);
       out[5984] = fma(kw, y[3104], out[5984]);
-      ws[272448] = fma(kw * y[3104], y[5984], ws[272448]);
+      ws[278496] = fma(kw * y[3104], y[5984], ws[278496]);
     }
     {
       double w = 0.0854 * phi[5728];
@@ -570,7 +570,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49824] * w;
       out[3264] = fma(kw, y[5984], out[3264]);
       out[5984] = fma(kw, y[3264], out[5984]);
-      ws[272480] = fma(kw * y[3264], y[5984], ws[272480]);
+      ws[278528] = fma(kw * y[3264], y[5984], ws[278528]);
     }
     {
       double w = 0.039 * phi[4480];
@@ -586,7 +586,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49856] * w;
       out[4160] = fma(kw, y[5984], out[4160]);
       out[5984] = fma(kw, y[4160], out[5984]);
-      ws[272512] = fma(kw * y[4160], y[5984], ws[272512]);
+      ws[278560] = fma(kw * y[4160], y[5984], ws[278560]);
     }
     {
       double w = 1.0 * phi[4256];
@@ -595,7 +595,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49888] * w;
       out[3744] = fma(kw, y[5984], out[3744]);
       out[5984] = fma(kw, y[3744], out[5984]);
-      ws[272544] = fma(kw * y[3744], y[5984], ws[272544]);
+      ws[278592] = fma(kw * y[3744], y[5984], ws[278592]);
     }
     {
       double w = 0.461 * phi[4384];
@@ -610,7 +610,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49920] * w;
       out[2624] = fma(kw, y[5984], out[2624]);
       out[5984] = fma(kw, y[2624], out[5984]);
-      ws[272576] = fma(kw * y[2624], y[5984], ws[272576]);
+      ws[278624] = fma(kw * y[2624], y[5984], ws[278624]);
     }
     {
       double w = 1.0 * phi[4256];
@@ -619,7 +619,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49952] * w;
       out[3840] = fma(kw, y[5984], out[3840]);
       out[5984] = fma(kw, y[3840], out[5984]);
-      ws[272608] = fma(kw * y[3840], y[5984], ws[272608]);
+      ws[278656] = fma(kw * y[3840], y[5984], ws[278656]);
     }
     {
       double w = 0.9 * phi[4096];
@@ -632,7 +632,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49984] * w;
       out[4192] = fma(kw, y[5984], out[4192]);
       out[5984] = fma(kw, y[4192], out[5984]);
-      ws[272640] = fma(kw * y[4192], y[5984], ws[272640]);
+      ws[278688] = fma(kw * y[4192], y[5984], ws[278688]);
     }
     {
       double w = 1.0 * phi[4256];
@@ -641,7 +641,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50016] * w;
       out[3936] = fma(kw, y[5984], out[3936]);
       out[5984] = fma(kw, y[3936], out[5984]);
-      ws[272672] = fma(kw * y[3936], y[5984], ws[272672]);
+      ws[278720] = fma(kw * y[3936], y[5984], ws[278720]);
     }
     {
       double w = 0.77 * phi[4384];
@@ -654,7 +654,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50048] * w;
       out[2656] = fma(kw, y[5984], out[2656]);
       out[5984] = fma(kw, y[2656], out[5984]);
-      ws[272704] = fma(kw * y[2656], y[5984], ws[272704]);
+      ws[278752] = fma(kw * y[2656], y[5984], ws[278752]);
     }
     {
       double w = 1.0 * phi[4256];
@@ -663,7 +663,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50080] * w;
       out[3712] = fma(kw, y[5984], out[3712]);
       out[5984] = fma(kw, y[3712], out[5984]);
-      ws[272736] = fma(kw * y[3712], y[5984], ws[272736]);
+      ws[278784] = fma(kw * y[3712], y[5984], ws[278784]);
     }
     {
       double w = 0.75 * phi[4096];
@@ -674,7 +674,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50112] * w;
       out[2560] = fma(kw, y[5984], out[2560]);
       out[5984] = fma(kw, y[2560], out[5984]);
-      ws[272768] = fma(kw * y[2560], y[5984], ws[272768]);
+      ws[278816] = fma(kw * y[2560], y[5984], ws[278816]);
     }
     {
       double w = 0.9 * phi[4096];
@@ -687,7 +687,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50144] * w;
       out[1728] = fma(kw, y[5984], out[1728]);
       out[5984] = fma(kw, y[1728], out[5984]);
-      ws[272800] = fma(kw * y[1728], y[5984], ws[272800]);
+      ws[278848] = fma(kw * y[1728], y[5984], ws[278848]);
     }
     {
       double w = 0.44 * phi[6016];
@@ -699,7 +699,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50176] * w;
       out[5792] = fma(kw, y[5984], out[5792]);
       out[5984] = fma(kw, y[5792], out[5984]);
-      ws[272832] = fma(kw * y[5792], y[5984], ws[272832]);
+      ws[278880] = fma(kw * y[5792], y[5984], ws[278880]);
     }
     {
       double w = 0.44 * phi[6016];
@@ -711,7 +711,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50208] * w;
       out[4800] = fma(kw, y[5984], out[4800]);
       out[5984] = fma(kw, y[4800], out[5984]);
-      ws[272864] = fma(kw * y[4800], y[5984], ws[272864]);
+      ws[278912] = fma(kw * y[4800], y[5984], ws[278912]);
     }
     {
       double w = 0.15 * phi[6016];
@@ -723,7 +723,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50240] * w;
       out[2848] = fma(kw, y[5984], out[2848]);
       out[5984] = fma(kw, y[2848], out[5984]);
-      ws[272896] = fma(kw * y[2848], y[5984], ws[272896]);
+      ws[278944] = fma(kw * y[2848], y[5984], ws[278944]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -732,7 +732,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50272] * w;
       out[5152] = fma(kw, y[5984], out[5152]);
       out[5984] = fma(kw, y[5152], out[5984]);
-      ws[272928] = fma(kw * y[5152], y[5984], ws[272928]);
+      ws[278976] = fma(kw * y[5152], y[5984], ws[278976]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -741,7 +741,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50304] * w;
       out[3776] = fma(kw, y[5984], out[3776]);
       out[5984] = fma(kw, y[3776], out[5984]);
-      ws[272960] = fma(kw * y[3776], y[5984], ws[272960]);
+      ws[279008] = fma(kw * y[3776], y[5984], ws[279008]);
     }
     {
       double w = 1.0 * phi[1792];
@@ -750,7 +750,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50336] * w;
       out[4672] = fma(kw, y[5984], out[4672]);
       out[5984] = fma(kw, y[4672], out[5984]);
-      ws[272992] = fma(kw * y[4672], y[5984], ws[272992]);
+      ws[279040] = fma(kw * y[4672], y[5984], ws[279040]);
     }
     {
       double w = 1.0 * phi[1792];
@@ -759,7 +759,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50368] * w;
       out[3520] = fma(kw, y[5984], out[3520]);
       out[5984] = fma(kw, y[3520], out[5984]);
-      ws[273024] = fma(kw * y[3520], y[5984], ws[273024]);
+      ws[279072] = fma(kw * y[3520], y[5984], ws[279072]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -768,7 +768,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50400] * w;
       out[2880] = fma(kw, y[5984], out[2880]);
       out[5984] = fma(kw, y[2880], out[5984]);
-      ws[273056] = fma(kw * y[2880], y[5984], ws[273056]);
+      ws[279104] = fma(kw * y[2880], y[5984], ws[279104]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -777,7 +777,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50432] * w;
       out[2912] = fma(kw, y[5984], out[2912]);
       out[5984] = fma(kw, y[2912], out[5984]);
-      ws[273088] = fma(kw * y[2912], y[5984], ws[273088]);
+      ws[279136] = fma(kw * y[2912], y[5984], ws[279136]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -786,7 +786,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50464] * w;
       out[3648] = fma(kw, y[5984], out[3648]);
       out[5984] = fma(kw, y[3648], out[5984]);
-      ws[273120] = fma(kw * y[3648], y[5984], ws[273120]);
+      ws[279168] = fma(kw * y[3648], y[5984], ws[279168]);
     }
     {
       double w = 1.0 * phi[2944];
@@ -795,7 +795,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50496] * w;
       out[3232] = fma(kw, y[5984], out[3232]);
       out[5984] = fma(kw, y[3232], out[5984]);
-      ws[273152] = fma(kw * y[3232], y[5984], ws[273152]);
+      ws[279200] = fma(kw * y[3232], y[5984], ws[279200]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -804,7 +804,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50528] * w;
       out[3040] = fma(kw, y[5984], out[3040]);
       out[5984] = fma(kw, y[3040], out[5984]);
-      ws[273184] = fma(kw * y[3040], y[5984], ws[273184]);
+      ws[279232] = fma(kw * y[3040], y[5984], ws[279232]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -813,7 +813,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50560] * w;
       out[2976] = fma(kw, y[5984], out[2976]);
       out[5984] = fma(kw, y[2976], out[5984]);
-      ws[273216] = fma(kw * y[2976], y[5984], ws[273216]);
+      ws[279264] = fma(kw * y[2976], y[5984], ws[279264]);
     }
     {
       double w = 1.0 * phi[5440];
@@ -822,7 +822,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50592] * w;
       out[4032] = fma(kw, y[5984], out[4032]);
       out[5984] = fma(kw, y[4032], out[5984]);
-      ws[273248] = fma(kw * y[4032], y[5984], ws[273248]);
+      ws[279296] = fma(kw * y[4032], y[5984], ws[279296]);
     }
     {
       double w = 1.0 * phi[5440];
@@ -831,7 +831,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50624] * w;
       out[4064] = fma(kw, y[5984], out[4064]);
       out[5984] = fma(kw, y[4064], out[5984]);
-      ws[273280] = fma(kw * y[4064], y[5984], ws[273280]);
+      ws[279328] = fma(kw * y[4064], y[5984], ws[279328]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -840,7 +840,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50656] * w;
       out[3072] = fma(kw, y[5984], out[3072]);
       out[5984] = fma(kw, y[3072], out[5984]);
-      ws[273312] = fma(kw * y[3072], y[5984], ws[273312]);
+      ws[279360] = fma(kw * y[3072], y[5984], ws[279360]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -849,7 +849,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50688] * w;
       out[5216] = fma(kw, y[5984], out[5216]);
       out[5984] = fma(kw, y[5216], out[5984]);
-      ws[273344] = fma(kw * y[5216], y[5984], ws[273344]);
+      ws[279392] = fma(kw * y[5216], y[5984], ws[279392]);
     }
     {
       double w = 0.74 * phi[5984];
@@ -860,7 +860,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50720] * w;
       out[5888] = fma(kw, y[5888], out[5888]);
       out[5888] = fma(kw, y[5888], out[5888]);
-      ws[273376] = fma(kw * y[5888], y[5888], ws[273376]);
+      ws[279424] = fma(kw * y[5888], y[5888], ws[279424]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -873,7 +873,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50752] * w;
       out[5632] = fma(kw, y[5888], out[5632]);
       out[5888] = fma(kw, y[5632], out[5888]);
-      ws[273408] = fma(kw * y[5632], y[5888], ws[273408]);
+      ws[279456] = fma(kw * y[5632], y[5888], ws[279456]);
     }
     {
       double w = 0.894 * phi[5984];
@@ -891,7 +891,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50784] * w;
       out[5408] = fma(kw, y[5888], out[5408]);
       out[5888] = fma(kw, y[5408], out[5888]);
-      ws[273440] = fma(kw * y[5408], y[5888], ws[273440]);
+      ws[279488] = fma(kw * y[5408], y[5888], ws[279488]);
     }
     {
       double w = 0.842 * phi[5984];
@@ -908,7 +908,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50816] * w;
       out[5120] = fma(kw, y[5888], out[5120]);
       out[5888] = fma(kw, y[5120], out[5888]);
-      ws[273472] = fma(kw * y[5120], y[5888], ws[273472]);
+      ws[279520] = fma(kw * y[5120], y[5888], ws[279520]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -921,7 +921,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50848] * w;
       out[3008] = fma(kw, y[5888], out[3008]);
       out[5888] = fma(kw, y[3008], out[5888]);
-      ws[273504] = fma(kw * y[3008], y[5888], ws[273504]);
+      ws[279552] = fma(kw * y[3008], y[5888], ws[279552]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -935,7 +935,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50880] * w;
       out[3200] = fma(kw, y[5888], out[3200]);
       out[5888] = fma(kw, y[3200], out[5888]);
-      ws[273536] = fma(kw * y[3200], y[5888], ws[273536]);
+      ws[279584] = fma(kw * y[3200], y[5888], ws[279584]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -949,7 +949,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50912] * w;
       out[3328] = fma(kw, y[5888], out[3328]);
       out[5888] = fma(kw, y[3328], out[5888]);
-      ws[273568] = fma(kw * y[3328], y[5888], ws[273568]);
+      ws[279616] = fma(kw * y[3328], y[5888], ws[279616]);
     }
     {
       double w = 0.68 * phi[5856];
@@ -965,7 +965,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50944] * w;
       out[3360] = fma(kw, y[5888], out[3360]);
       out[5888] = fma(kw, y[3360], out[5888]);
-      ws[273600] = fma(kw * y[3360], y[5888], ws[273600]);
+      ws[279648] = fma(kw * y[3360], y[5888], ws[279648]);
     }
     {
       double w = 0.68 * phi[5856];
@@ -981,7 +981,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50976] * w;
       out[3296] = fma(kw, y[5888], out[3296]);
       out[5888] = fma(kw, y[3296], out[5888]);
-      ws[273632] = fma(kw * y[3296], y[5888], ws[273632]);
+      ws[279680] = fma(kw * y[3296], y[5888], ws[279680]);
     }
     {
       double w = 0.68 * phi[5856];
@@ -997,7 +997,7 @@ __device__ __noinline__ void adj_jtv_0_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51008] * w;
       out[3104] = fma(kw, y[5888], out[3104]);
       out[5888] = fma(kw, y[3104], out[5888]);
-      ws[273664] = fma(kw * y[3104], y[5888], ws[273664]);
+      ws[279712] = fma(kw * y[3104], y[5888], ws[279712]);
     }
 }
 __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int phioff, int outoff)
@@ -1019,7 +1019,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51040] * w;
       out[3264] = fma(kw, y[5888], out[3264]);
       out[5888] = fma(kw, y[3264], out[5888]);
-      ws[273696] = fma(kw * y[3264], y[5888], ws[273696]);
+      ws[279744] = fma(kw * y[3264], y[5888], ws[279744]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1036,7 +1036,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51072] * w;
       out[4288] = fma(kw, y[5888], out[4288]);
       out[5888] = fma(kw, y[4288], out[5888]);
-      ws[273728] = fma(kw * y[4288], y[5888], ws[273728]);
+      ws[279776] = fma(kw * y[4288], y[5888], ws[279776]);
     }
     {
       double w = 1.0295 * phi[5856];
@@ -1053,7 +1053,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51104] * w;
       out[4160] = fma(kw, y[5888], out[4160]);
       out[5888] = fma(kw, y[4160], out[5888]);
-      ws[273760] = fma(kw * y[4160], y[5888], ws[273760]);
+      ws[279808] = fma(kw * y[4160], y[5888], ws[279808]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1065,7 +1065,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51136] * w;
       out[3744] = fma(kw, y[5888], out[3744]);
       out[5888] = fma(kw, y[3744], out[5888]);
-      ws[273792] = fma(kw * y[3744], y[5888], ws[273792]);
+      ws[279840] = fma(kw * y[3744], y[5888], ws[279840]);
     }
     {
       double w = 0.341 * phi[4384];
@@ -1081,7 +1081,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51168] * w;
       out[2624] = fma(kw, y[5888], out[2624]);
       out[5888] = fma(kw, y[2624], out[5888]);
-      ws[273824] = fma(kw * y[2624], y[5888], ws[273824]);
+      ws[279872] = fma(kw * y[2624], y[5888], ws[279872]);
     }
     {
       double w = 0.75 * phi[5984];
@@ -1094,7 +1094,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51200] * w;
       out[3840] = fma(kw, y[5888], out[3840]);
       out[5888] = fma(kw, y[3840], out[5888]);
-      ws[273856] = fma(kw * y[3840], y[5888], ws[273856]);
+      ws[279904] = fma(kw * y[3840], y[5888], ws[279904]);
     }
     {
       double w = 0.25 * phi[5600];
@@ -1106,7 +1106,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51232] * w;
       out[4192] = fma(kw, y[5888], out[4192]);
       out[5888] = fma(kw, y[4192], out[5888]);
-      ws[273888] = fma(kw * y[4192], y[5888], ws[273888]);
+      ws[279936] = fma(kw * y[4192], y[5888], ws[279936]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1118,7 +1118,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51264] * w;
       out[3936] = fma(kw, y[5888], out[3936]);
       out[5888] = fma(kw, y[3936], out[5888]);
-      ws[273920] = fma(kw * y[3936], y[5888], ws[273920]);
+      ws[279968] = fma(kw * y[3936], y[5888], ws[279968]);
     }
     {
       double w = 0.69 * phi[4384];
@@ -1132,7 +1132,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51296] * w;
       out[2656] = fma(kw, y[5888], out[2656]);
       out[5888] = fma(kw, y[2656], out[5888]);
-      ws[273952] = fma(kw * y[2656], y[5888], ws[273952]);
+      ws[280000] = fma(kw * y[2656], y[5888], ws[280000]);
     }
     {
       double w = 0.75 * phi[5984];
@@ -1145,7 +1145,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51328] * w;
       out[3712] = fma(kw, y[5888], out[3712]);
       out[5888] = fma(kw, y[3712], out[5888]);
-      ws[273984] = fma(kw * y[3712], y[5888], ws[273984]);
+      ws[280032] = fma(kw * y[3712], y[5888], ws[280032]);
     }
     {
       double w = 0.9 * phi[5984];
@@ -1157,7 +1157,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51360] * w;
       out[5792] = fma(kw, y[5888], out[5792]);
       out[5888] = fma(kw, y[5792], out[5888]);
-      ws[274016] = fma(kw * y[5792], y[5888], ws[274016]);
+      ws[280064] = fma(kw * y[5792], y[5888], ws[280064]);
     }
     {
       double w = 0.9 * phi[5984];
@@ -1169,7 +1169,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51392] * w;
       out[4800] = fma(kw, y[5888], out[4800]);
       out[5888] = fma(kw, y[4800], out[5888]);
-      ws[274048] = fma(kw * y[4800], y[5888], ws[274048]);
+      ws[280096] = fma(kw * y[4800], y[5888], ws[280096]);
     }
     {
       double w = 0.5 * phi[5984];
@@ -1183,7 +1183,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51424] * w;
       out[2848] = fma(kw, y[5888], out[2848]);
       out[5888] = fma(kw, y[2848], out[5888]);
-      ws[274080] = fma(kw * y[2848], y[5888], ws[274080]);
+      ws[280128] = fma(kw * y[2848], y[5888], ws[280128]);
     }
     {
       double w = 0.834 * phi[5984];
@@ -1196,7 +1196,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51456] * w;
       out[5152] = fma(kw, y[5888], out[5152]);
       out[5888] = fma(kw, y[5152], out[5888]);
-      ws[274112] = fma(kw * y[5152], y[5888], ws[274112]);
+      ws[280160] = fma(kw * y[5152], y[5888], ws[280160]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1209,7 +1209,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51488] * w;
       out[3776] = fma(kw, y[5888], out[3776]);
       out[5888] = fma(kw, y[3776], out[5888]);
-      ws[274144] = fma(kw * y[3776], y[5888], ws[274144]);
+      ws[280192] = fma(kw * y[3776], y[5888], ws[280192]);
     }
     {
       double w = 0.5 * phi[5984];
@@ -1225,7 +1225,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51520] * w;
       out[4672] = fma(kw, y[5888], out[4672]);
       out[5888] = fma(kw, y[4672], out[5888]);
-      ws[274176] = fma(kw * y[4672], y[5888], ws[274176]);
+      ws[280224] = fma(kw * y[4672], y[5888], ws[280224]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1239,7 +1239,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51552] * w;
       out[3520] = fma(kw, y[5888], out[3520]);
       out[5888] = fma(kw, y[3520], out[5888]);
-      ws[274208] = fma(kw * y[3520], y[5888], ws[274208]);
+      ws[280256] = fma(kw * y[3520], y[5888], ws[280256]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1256,7 +1256,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51584] * w;
       out[2880] = fma(kw, y[5888], out[2880]);
       out[5888] = fma(kw, y[2880], out[5888]);
-      ws[274240] = fma(kw * y[2880], y[5888], ws[274240]);
+      ws[280288] = fma(kw * y[2880], y[5888], ws[280288]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1273,7 +1273,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51616] * w;
       out[2912] = fma(kw, y[5888], out[2912]);
       out[5888] = fma(kw, y[2912], out[5888]);
-      ws[274272] = fma(kw * y[2912], y[5888], ws[274272]);
+      ws[280320] = fma(kw * y[2912], y[5888], ws[280320]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1284,7 +1284,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51648] * w;
       out[2592] = fma(kw, y[5888], out[2592]);
       out[5888] = fma(kw, y[2592], out[5888]);
-      ws[274304] = fma(kw * y[2592], y[5888], ws[274304]);
+      ws[280352] = fma(kw * y[2592], y[5888], ws[280352]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1295,7 +1295,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51680] * w;
       out[2272] = fma(kw, y[5888], out[2272]);
       out[5888] = fma(kw, y[2272], out[5888]);
-      ws[274336] = fma(kw * y[2272], y[5888], ws[274336]);
+      ws[280384] = fma(kw * y[2272], y[5888], ws[280384]);
     }
     {
       double w = 2.0 * phi[5984];
@@ -1308,7 +1308,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51712] * w;
       out[3648] = fma(kw, y[5888], out[3648]);
       out[5888] = fma(kw, y[3648], out[5888]);
-      ws[274368] = fma(kw * y[3648], y[5888], ws[274368]);
+      ws[280416] = fma(kw * y[3648], y[5888], ws[280416]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1319,7 +1319,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51744] * w;
       out[3040] = fma(kw, y[5888], out[3040]);
       out[5888] = fma(kw, y[3040], out[5888]);
-      ws[274400] = fma(kw * y[3040], y[5888], ws[274400]);
+      ws[280448] = fma(kw * y[3040], y[5888], ws[280448]);
     }
     {
       double w = 1.0 * phi[5856];
@@ -1330,7 +1330,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51776] * w;
       out[2976] = fma(kw, y[5888], out[2976]);
       out[5888] = fma(kw, y[2976], out[5888]);
-      ws[274432] = fma(kw * y[2976], y[5888], ws[274432]);
+      ws[280480] = fma(kw * y[2976], y[5888], ws[280480]);
     }
     {
       double w = 2.0 * phi[5984];
@@ -1341,7 +1341,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51808] * w;
       out[4032] = fma(kw, y[5888], out[4032]);
       out[5888] = fma(kw, y[4032], out[5888]);
-      ws[274464] = fma(kw * y[4032], y[5888], ws[274464]);
+      ws[280512] = fma(kw * y[4032], y[5888], ws[280512]);
     }
     {
       double w = 0.5 * phi[5984];
@@ -1357,7 +1357,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51840] * w;
       out[4064] = fma(kw, y[5888], out[4064]);
       out[5888] = fma(kw, y[4064], out[5888]);
-      ws[274496] = fma(kw * y[4064], y[5888], ws[274496]);
+      ws[280544] = fma(kw * y[4064], y[5888], ws[280544]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1371,7 +1371,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51872] * w;
       out[3072] = fma(kw, y[5888], out[3072]);
       out[5888] = fma(kw, y[3072], out[5888]);
-      ws[274528] = fma(kw * y[3072], y[5888], ws[274528]);
+      ws[280576] = fma(kw * y[3072], y[5888], ws[280576]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1381,7 +1381,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51904] * w;
       out[5216] = fma(kw, y[5888], out[5216]);
       out[5888] = fma(kw, y[5216], out[5888]);
-      ws[274560] = fma(kw * y[5216], y[5888], ws[274560]);
+      ws[280608] = fma(kw * y[5216], y[5888], ws[280608]);
     }
     {
       double w = 0.5 * phi[5984];
@@ -1393,7 +1393,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51936] * w;
       out[5632] = fma(kw, y[5792], out[5632]);
       out[5792] = fma(kw, y[5632], out[5792]);
-      ws[274592] = fma(kw * y[5632], y[5792], ws[274592]);
+      ws[280640] = fma(kw * y[5632], y[5792], ws[280640]);
     }
     {
       double w = 0.394 * phi[5984];
@@ -1410,7 +1410,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51968] * w;
       out[5408] = fma(kw, y[5792], out[5408]);
       out[5792] = fma(kw, y[5408], out[5792]);
-      ws[274624] = fma(kw * y[5408], y[5792], ws[274624]);
+      ws[280672] = fma(kw * y[5408], y[5792], ws[280672]);
     }
     {
       double w = 0.342 * phi[5984];
@@ -1426,7 +1426,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52000] * w;
       out[5120] = fma(kw, y[5792], out[5120]);
       out[5792] = fma(kw, y[5120], out[5792]);
-      ws[274656] = fma(kw * y[5120], y[5792], ws[274656]);
+      ws[280704] = fma(kw * y[5120], y[5792], ws[280704]);
     }
     {
       double w = 0.5 * phi[5984];
@@ -1439,7 +1439,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52032] * w;
       out[3008] = fma(kw, y[5792], out[3008]);
       out[5792] = fma(kw, y[3008], out[5792]);
-      ws[274688] = fma(kw * y[3008], y[5792], ws[274688]);
+      ws[280736] = fma(kw * y[3008], y[5792], ws[280736]);
     }
     {
       double w = 0.5 * phi[5984];
@@ -1453,7 +1453,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52064] * w;
       out[3200] = fma(kw, y[5792], out[3200]);
       out[5792] = fma(kw, y[3200], out[5792]);
-      ws[274720] = fma(kw * y[3200], y[5792], ws[274720]);
+      ws[280768] = fma(kw * y[3200], y[5792], ws[280768]);
     }
     {
       double w = 0.5 * phi[5984];
@@ -1466,7 +1466,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52096] * w;
       out[3328] = fma(kw, y[5792], out[3328]);
       out[5792] = fma(kw, y[3328], out[5792]);
-      ws[274752] = fma(kw * y[3328], y[5792], ws[274752]);
+      ws[280800] = fma(kw * y[3328], y[5792], ws[280800]);
     }
     {
       double w = 0.7 * phi[5888];
@@ -1482,7 +1482,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52128] * w;
       out[3360] = fma(kw, y[5792], out[3360]);
       out[5792] = fma(kw, y[3360], out[5792]);
-      ws[274784] = fma(kw * y[3360], y[5792], ws[274784]);
+      ws[280832] = fma(kw * y[3360], y[5792], ws[280832]);
     }
     {
       double w = 0.7 * phi[5888];
@@ -1498,7 +1498,7 @@ __device__ __noinline__ void adj_jtv_0_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52160] * w;
       out[3296] = fma(kw, y[5792], out[3296]);
       out[5792] = fma(kw, y[3296], out[5792]);
-      ws[274816] = fma(kw * y[3296], y[5792], ws[274816]);
+      ws[280864] = fma(kw * y[3296], y[5792], ws[280864]);
     }
 }
 __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int phioff, int outoff)
@@ -1520,7 +1520,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52192] * w;
       out[3104] = fma(kw, y[5792], out[3104]);
       out[5792] = fma(kw, y[3104], out[5792]);
-      ws[274848] = fma(kw * y[3104], y[5792], ws[274848]);
+      ws[280896] = fma(kw * y[3104], y[5792], ws[280896]);
     }
     {
       double w = 0.7 * phi[5888];
@@ -1536,7 +1536,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52224] * w;
       out[3264] = fma(kw, y[5792], out[3264]);
       out[5792] = fma(kw, y[3264], out[5792]);
-      ws[274880] = fma(kw * y[3264], y[5792], ws[274880]);
+      ws[280928] = fma(kw * y[3264], y[5792], ws[280928]);
     }
     {
       double w = 0.5 * phi[5984];
@@ -1550,7 +1550,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52256] * w;
       out[4288] = fma(kw, y[5792], out[4288]);
       out[5792] = fma(kw, y[4288], out[5792]);
-      ws[274912] = fma(kw * y[4288], y[5792], ws[274912]);
+      ws[280960] = fma(kw * y[4288], y[5792], ws[280960]);
     }
     {
       double w = 0.2535 * phi[4544];
@@ -1567,7 +1567,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52288] * w;
       out[4160] = fma(kw, y[5792], out[4160]);
       out[5792] = fma(kw, y[4160], out[5792]);
-      ws[274944] = fma(kw * y[4160], y[5792], ws[274944]);
+      ws[280992] = fma(kw * y[4160], y[5792], ws[280992]);
     }
     {
       double w = 0.5 * phi[6016];
@@ -1579,7 +1579,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52320] * w;
       out[3744] = fma(kw, y[5792], out[3744]);
       out[5792] = fma(kw, y[3744], out[5792]);
-      ws[274976] = fma(kw * y[3744], y[5792], ws[274976]);
+      ws[281024] = fma(kw * y[3744], y[5792], ws[281024]);
     }
     {
       double w = 0.825 * phi[5920];
@@ -1595,7 +1595,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52352] * w;
       out[2624] = fma(kw, y[5792], out[2624]);
       out[5792] = fma(kw, y[2624], out[5792]);
-      ws[275008] = fma(kw * y[2624], y[5792], ws[275008]);
+      ws[281056] = fma(kw * y[2624], y[5792], ws[281056]);
     }
     {
       double w = 0.5 * phi[5920];
@@ -1607,7 +1607,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52384] * w;
       out[3840] = fma(kw, y[5792], out[3840]);
       out[5792] = fma(kw, y[3840], out[5792]);
-      ws[275040] = fma(kw * y[3840], y[5792], ws[275040]);
+      ws[281088] = fma(kw * y[3840], y[5792], ws[281088]);
     }
     {
       double w = 1.0 * phi[4576];
@@ -1619,7 +1619,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52416] * w;
       out[4192] = fma(kw, y[5792], out[4192]);
       out[5792] = fma(kw, y[4192], out[5792]);
-      ws[275072] = fma(kw * y[4192], y[5792], ws[275072]);
+      ws[281120] = fma(kw * y[4192], y[5792], ws[281120]);
     }
     {
       double w = 0.5 * phi[6016];
@@ -1631,7 +1631,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52448] * w;
       out[3936] = fma(kw, y[5792], out[3936]);
       out[5792] = fma(kw, y[3936], out[5792]);
-      ws[275104] = fma(kw * y[3936], y[5792], ws[275104]);
+      ws[281152] = fma(kw * y[3936], y[5792], ws[281152]);
     }
     {
       double w = 1.0 * phi[5888];
@@ -1644,7 +1644,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52480] * w;
       out[2656] = fma(kw, y[5792], out[2656]);
       out[5792] = fma(kw, y[2656], out[5792]);
-      ws[275136] = fma(kw * y[2656], y[5792], ws[275136]);
+      ws[281184] = fma(kw * y[2656], y[5792], ws[281184]);
     }
     {
       double w = 0.5 * phi[5888];
@@ -1656,7 +1656,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52512] * w;
       out[3712] = fma(kw, y[5792], out[3712]);
       out[5792] = fma(kw, y[3712], out[5792]);
-      ws[275168] = fma(kw * y[3712], y[5792], ws[275168]);
+      ws[281216] = fma(kw * y[3712], y[5792], ws[281216]);
     }
     {
       double w = 2.0 * phi[5888];
@@ -1665,7 +1665,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52544] * w;
       out[5792] = fma(kw, y[5792], out[5792]);
       out[5792] = fma(kw, y[5792], out[5792]);
-      ws[275200] = fma(kw * y[5792], y[5792], ws[275200]);
+      ws[281248] = fma(kw * y[5792], y[5792], ws[281248]);
     }
     {
       double w = 1.0 * phi[5888];
@@ -1675,7 +1675,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52576] * w;
       out[4800] = fma(kw, y[5792], out[4800]);
       out[5792] = fma(kw, y[4800], out[5792]);
-      ws[275232] = fma(kw * y[4800], y[5792], ws[275232]);
+      ws[281280] = fma(kw * y[4800], y[5792], ws[281280]);
     }
     {
       double w = 0.5 * phi[5888];
@@ -1687,7 +1687,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52608] * w;
       out[2848] = fma(kw, y[5792], out[2848]);
       out[5792] = fma(kw, y[2848], out[5792]);
-      ws[275264] = fma(kw * y[2848], y[5792], ws[275264]);
+      ws[281312] = fma(kw * y[2848], y[5792], ws[281312]);
     }
     {
       double w = 0.33 * phi[5984];
@@ -1700,7 +1700,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52640] * w;
       out[5152] = fma(kw, y[5792], out[5152]);
       out[5792] = fma(kw, y[5152], out[5792]);
-      ws[275296] = fma(kw * y[5152], y[5792], ws[275296]);
+      ws[281344] = fma(kw * y[5152], y[5792], ws[281344]);
     }
     {
       double w = 0.5 * phi[5984];
@@ -1712,7 +1712,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52672] * w;
       out[3776] = fma(kw, y[5792], out[3776]);
       out[5792] = fma(kw, y[3776], out[5792]);
-      ws[275328] = fma(kw * y[3776], y[5792], ws[275328]);
+      ws[281376] = fma(kw * y[3776], y[5792], ws[281376]);
     }
     {
       double w = 0.635 * phi[5696];
@@ -1725,7 +1725,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52704] * w;
       out[4672] = fma(kw, y[5792], out[4672]);
       out[5792] = fma(kw, y[4672], out[5792]);
-      ws[275360] = fma(kw * y[4672], y[5792], ws[275360]);
+      ws[281408] = fma(kw * y[4672], y[5792], ws[281408]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1739,7 +1739,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52736] * w;
       out[3520] = fma(kw, y[5792], out[3520]);
       out[5792] = fma(kw, y[3520], out[5792]);
-      ws[275392] = fma(kw * y[3520], y[5792], ws[275392]);
+      ws[281440] = fma(kw * y[3520], y[5792], ws[281440]);
     }
     {
       double w = 0.5 * phi[5984];
@@ -1755,7 +1755,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52768] * w;
       out[2880] = fma(kw, y[5792], out[2880]);
       out[5792] = fma(kw, y[2880], out[5792]);
-      ws[275424] = fma(kw * y[2880], y[5792], ws[275424]);
+      ws[281472] = fma(kw * y[2880], y[5792], ws[281472]);
     }
     {
       double w = 0.5 * phi[5984];
@@ -1772,7 +1772,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52800] * w;
       out[2912] = fma(kw, y[5792], out[2912]);
       out[5792] = fma(kw, y[2912], out[5792]);
-      ws[275456] = fma(kw * y[2912], y[5792], ws[275456]);
+      ws[281504] = fma(kw * y[2912], y[5792], ws[281504]);
     }
     {
       double w = 1.0 * phi[5888];
@@ -1782,7 +1782,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52832] * w;
       out[2592] = fma(kw, y[5792], out[2592]);
       out[5792] = fma(kw, y[2592], out[5792]);
-      ws[275488] = fma(kw * y[2592], y[5792], ws[275488]);
+      ws[281536] = fma(kw * y[2592], y[5792], ws[281536]);
     }
     {
       double w = 1.0 * phi[5888];
@@ -1792,7 +1792,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52864] * w;
       out[2272] = fma(kw, y[5792], out[2272]);
       out[5792] = fma(kw, y[2272], out[5792]);
-      ws[275520] = fma(kw * y[2272], y[5792], ws[275520]);
+      ws[281568] = fma(kw * y[2272], y[5792], ws[281568]);
     }
     {
       double w = 2.0 * phi[5984];
@@ -1805,7 +1805,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52896] * w;
       out[3648] = fma(kw, y[5792], out[3648]);
       out[5792] = fma(kw, y[3648], out[5792]);
-      ws[275552] = fma(kw * y[3648], y[5792], ws[275552]);
+      ws[281600] = fma(kw * y[3648], y[5792], ws[281600]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1816,7 +1816,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52928] * w;
       out[3040] = fma(kw, y[5792], out[3040]);
       out[5792] = fma(kw, y[3040], out[5792]);
-      ws[275584] = fma(kw * y[3040], y[5792], ws[275584]);
+      ws[281632] = fma(kw * y[3040], y[5792], ws[281632]);
     }
     {
       double w = 1.0 * phi[5888];
@@ -1826,7 +1826,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52960] * w;
       out[2976] = fma(kw, y[5792], out[2976]);
       out[5792] = fma(kw, y[2976], out[5792]);
-      ws[275616] = fma(kw * y[2976], y[5792], ws[275616]);
+      ws[281664] = fma(kw * y[2976], y[5792], ws[281664]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1837,7 +1837,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52992] * w;
       out[4032] = fma(kw, y[5792], out[4032]);
       out[5792] = fma(kw, y[4032], out[5792]);
-      ws[275648] = fma(kw * y[4032], y[5792], ws[275648]);
+      ws[281696] = fma(kw * y[4032], y[5792], ws[281696]);
     }
     {
       double w = 0.5 * phi[5888];
@@ -1851,7 +1851,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53024] * w;
       out[4064] = fma(kw, y[5792], out[4064]);
       out[5792] = fma(kw, y[4064], out[5792]);
-      ws[275680] = fma(kw * y[4064], y[5792], ws[275680]);
+      ws[281728] = fma(kw * y[4064], y[5792], ws[281728]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1865,7 +1865,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53056] * w;
       out[3072] = fma(kw, y[5792], out[3072]);
       out[5792] = fma(kw, y[3072], out[5792]);
-      ws[275712] = fma(kw * y[3072], y[5792], ws[275712]);
+      ws[281760] = fma(kw * y[3072], y[5792], ws[281760]);
     }
     {
       double w = 1.0 * phi[5888];
@@ -1874,7 +1874,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53088] * w;
       out[5216] = fma(kw, y[5792], out[5216]);
       out[5792] = fma(kw, y[5216], out[5792]);
-      ws[275744] = fma(kw * y[5216], y[5792], ws[275744]);
+      ws[281792] = fma(kw * y[5216], y[5792], ws[281792]);
     }
     {
       double w = 2.0 * phi[5632];
@@ -1883,7 +1883,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53120] * w;
       out[4800] = fma(kw, y[4800], out[4800]);
       out[4800] = fma(kw, y[4800], out[4800]);
-      ws[275776] = fma(kw * y[4800], y[4800], ws[275776]);
+      ws[281824] = fma(kw * y[4800], y[4800], ws[281824]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1894,7 +1894,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53152] * w;
       out[5888] = fma(kw, y[5952], out[5888]);
       out[5952] = fma(kw, y[5888], out[5952]);
-      ws[275808] = fma(kw * y[5888], y[5952], ws[275808]);
+      ws[281856] = fma(kw * y[5888], y[5952], ws[281856]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1905,7 +1905,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53184] * w;
       out[5632] = fma(kw, y[5952], out[5632]);
       out[5952] = fma(kw, y[5632], out[5952]);
-      ws[275840] = fma(kw * y[5632], y[5952], ws[275840]);
+      ws[281888] = fma(kw * y[5632], y[5952], ws[281888]);
     }
     {
       double w = 0.254 * phi[5984];
@@ -1922,7 +1922,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53216] * w;
       out[5408] = fma(kw, y[5952], out[5408]);
       out[5952] = fma(kw, y[5408], out[5952]);
-      ws[275872] = fma(kw * y[5408], y[5952], ws[275872]);
+      ws[281920] = fma(kw * y[5408], y[5952], ws[281920]);
     }
     {
       double w = 0.488 * phi[5984];
@@ -1942,7 +1942,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53248] * w;
       out[5120] = fma(kw, y[5952], out[5120]);
       out[5952] = fma(kw, y[5120], out[5952]);
-      ws[275904] = fma(kw * y[5120], y[5952], ws[275904]);
+      ws[281952] = fma(kw * y[5120], y[5952], ws[281952]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1954,7 +1954,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53280] * w;
       out[3008] = fma(kw, y[5952], out[3008]);
       out[5952] = fma(kw, y[3008], out[5952]);
-      ws[275936] = fma(kw * y[3008], y[5952], ws[275936]);
+      ws[281984] = fma(kw * y[3008], y[5952], ws[281984]);
     }
     {
       double w = 0.47 * phi[5760];
@@ -1969,7 +1969,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53312] * w;
       out[3200] = fma(kw, y[5952], out[3200]);
       out[5952] = fma(kw, y[3200], out[5952]);
-      ws[275968] = fma(kw * y[3200], y[5952], ws[275968]);
+      ws[282016] = fma(kw * y[3200], y[5952], ws[282016]);
     }
     {
       double w = 0.86 * phi[5984];
@@ -1984,7 +1984,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53344] * w;
       out[3328] = fma(kw, y[5952], out[3328]);
       out[5952] = fma(kw, y[3328], out[5952]);
-      ws[276000] = fma(kw * y[3328], y[5952], ws[276000]);
+      ws[282048] = fma(kw * y[3328], y[5952], ws[282048]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1999,7 +1999,7 @@ __device__ __noinline__ void adj_jtv_0_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53376] * w;
       out[3360] = fma(kw, y[5952], out[3360]);
       out[5952] = fma(kw, y[3360], out[5952]);
-      ws[276032] = fma(kw * y[3360], y[5952], ws[276032]);
+      ws[282080] = fma(kw * y[3360], y[5952], ws[282080]);
     }
 }
 }  // namespace mech_cracmm2

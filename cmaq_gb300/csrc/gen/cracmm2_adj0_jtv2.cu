@@ -21,7 +21,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53408] * w;
       out[3296] = fma(kw, y[5952], out[3296]);
       out[5952] = fma(kw, y[3296], out[5952]);
-      ws[276064] = fma(kw * y[3296], y[5952], ws[276064]);
+      ws[282112] = fma(kw * y[3296], y[5952], ws[282112]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -36,7 +36,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53440] * w;
       out[3104] = fma(kw, y[5952], out[3104]);
       out[5952] = fma(kw, y[3104], out[5952]);
-      ws[276096] = fma(kw * y[3104], y[5952], ws[276096]);
+      ws[282144] = fma(kw * y[3104], y[5952], ws[282144]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -51,7 +51,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53472] * w;
       out[3264] = fma(kw, y[5952], out[3264]);
       out[5952] = fma(kw, y[3264], out[5952]);
-      ws[276128] = fma(kw * y[3264], y[5952], ws[276128]);
+      ws[282176] = fma(kw * y[3264], y[5952], ws[282176]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -67,7 +67,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53504] * w;
       out[4288] = fma(kw, y[5952], out[4288]);
       out[5952] = fma(kw, y[4288], out[5952]);
-      ws[276160] = fma(kw * y[4288], y[5952], ws[276160]);
+      ws[282208] = fma(kw * y[4288], y[5952], ws[282208]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -84,7 +84,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53536] * w;
       out[4160] = fma(kw, y[5952], out[4160]);
       out[5952] = fma(kw, y[4160], out[5952]);
-      ws[276192] = fma(kw * y[4160], y[5952], ws[276192]);
+      ws[282240] = fma(kw * y[4160], y[5952], ws[282240]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -96,7 +96,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53568] * w;
       out[4192] = fma(kw, y[5952], out[4192]);
       out[5952] = fma(kw, y[4192], out[5952]);
-      ws[276224] = fma(kw * y[4192], y[5952], ws[276224]);
+      ws[282272] = fma(kw * y[4192], y[5952], ws[282272]);
     }
     {
       double w = 1.825 * phi[5920];
@@ -111,7 +111,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53600] * w;
       out[2624] = fma(kw, y[5952], out[2624]);
       out[5952] = fma(kw, y[2624], out[5952]);
-      ws[276256] = fma(kw * y[2624], y[5952], ws[276256]);
+      ws[282304] = fma(kw * y[2624], y[5952], ws[282304]);
     }
     {
       double w = 1.46 * phi[5920];
@@ -123,7 +123,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53632] * w;
       out[2656] = fma(kw, y[5952], out[2656]);
       out[5952] = fma(kw, y[2656], out[5952]);
-      ws[276288] = fma(kw * y[2656], y[5952], ws[276288]);
+      ws[282336] = fma(kw * y[2656], y[5952], ws[282336]);
     }
     {
       double w = 1.0 * phi[5888];
@@ -133,7 +133,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53664] * w;
       out[5792] = fma(kw, y[5952], out[5792]);
       out[5952] = fma(kw, y[5792], out[5952]);
-      ws[276320] = fma(kw * y[5792], y[5952], ws[276320]);
+      ws[282368] = fma(kw * y[5792], y[5952], ws[282368]);
     }
     {
       double w = 1.0 * phi[5632];
@@ -143,7 +143,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53696] * w;
       out[4800] = fma(kw, y[5952], out[4800]);
       out[5952] = fma(kw, y[4800], out[5952]);
-      ws[276352] = fma(kw * y[4800], y[5952], ws[276352]);
+      ws[282400] = fma(kw * y[4800], y[5952], ws[282400]);
     }
     {
       double w = 1.0 * phi[5792];
@@ -154,7 +154,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53728] * w;
       out[2848] = fma(kw, y[5952], out[2848]);
       out[5952] = fma(kw, y[2848], out[5952]);
-      ws[276384] = fma(kw * y[2848], y[5952], ws[276384]);
+      ws[282432] = fma(kw * y[2848], y[5952], ws[282432]);
     }
     {
       double w = 0.67 * phi[5984];
@@ -166,7 +166,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53760] * w;
       out[5152] = fma(kw, y[5952], out[5152]);
       out[5952] = fma(kw, y[5152], out[5952]);
-      ws[276416] = fma(kw * y[5152], y[5952], ws[276416]);
+      ws[282464] = fma(kw * y[5152], y[5952], ws[282464]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -177,7 +177,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53792] * w;
       out[3776] = fma(kw, y[5952], out[3776]);
       out[5952] = fma(kw, y[3776], out[5952]);
-      ws[276448] = fma(kw * y[3776], y[5952], ws[276448]);
+      ws[282496] = fma(kw * y[3776], y[5952], ws[282496]);
     }
     {
       double w = 1.0 * phi[5856];
@@ -189,7 +189,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53824] * w;
       out[4672] = fma(kw, y[5952], out[4672]);
       out[5952] = fma(kw, y[4672], out[5952]);
-      ws[276480] = fma(kw * y[4672], y[5952], ws[276480]);
+      ws[282528] = fma(kw * y[4672], y[5952], ws[282528]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -201,7 +201,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53856] * w;
       out[3520] = fma(kw, y[5952], out[3520]);
       out[5952] = fma(kw, y[3520], out[5952]);
-      ws[276512] = fma(kw * y[3520], y[5952], ws[276512]);
+      ws[282560] = fma(kw * y[3520], y[5952], ws[282560]);
     }
     {
       double w = 0.3 * phi[5984];
@@ -216,7 +216,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53888] * w;
       out[2880] = fma(kw, y[5952], out[2880]);
       out[5952] = fma(kw, y[2880], out[5952]);
-      ws[276544] = fma(kw * y[2880], y[5952], ws[276544]);
+      ws[282592] = fma(kw * y[2880], y[5952], ws[282592]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -232,7 +232,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53920] * w;
       out[2912] = fma(kw, y[5952], out[2912]);
       out[5952] = fma(kw, y[2912], out[5952]);
-      ws[276576] = fma(kw * y[2912], y[5952], ws[276576]);
+      ws[282624] = fma(kw * y[2912], y[5952], ws[282624]);
     }
     {
       double w = 1.0 * phi[2272];
@@ -242,7 +242,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53952] * w;
       out[2592] = fma(kw, y[5952], out[2592]);
       out[5952] = fma(kw, y[2592], out[5952]);
-      ws[276608] = fma(kw * y[2592], y[5952], ws[276608]);
+      ws[282656] = fma(kw * y[2592], y[5952], ws[282656]);
     }
     {
       double w = 1.0 * phi[2688];
@@ -252,7 +252,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53984] * w;
       out[2272] = fma(kw, y[5952], out[2272]);
       out[5952] = fma(kw, y[2272], out[5952]);
-      ws[276640] = fma(kw * y[2272], y[5952], ws[276640]);
+      ws[282688] = fma(kw * y[2272], y[5952], ws[282688]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -265,7 +265,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54016] * w;
       out[3648] = fma(kw, y[5952], out[3648]);
       out[5952] = fma(kw, y[3648], out[5952]);
-      ws[276672] = fma(kw * y[3648], y[5952], ws[276672]);
+      ws[282720] = fma(kw * y[3648], y[5952], ws[282720]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -275,7 +275,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54048] * w;
       out[3040] = fma(kw, y[5952], out[3040]);
       out[5952] = fma(kw, y[3040], out[5952]);
-      ws[276704] = fma(kw * y[3040], y[5952], ws[276704]);
+      ws[282752] = fma(kw * y[3040], y[5952], ws[282752]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -286,7 +286,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54080] * w;
       out[2976] = fma(kw, y[5952], out[2976]);
       out[5952] = fma(kw, y[2976], out[5952]);
-      ws[276736] = fma(kw * y[2976], y[5952], ws[276736]);
+      ws[282784] = fma(kw * y[2976], y[5952], ws[282784]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -297,7 +297,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54112] * w;
       out[4032] = fma(kw, y[5952], out[4032]);
       out[5952] = fma(kw, y[4032], out[5952]);
-      ws[276768] = fma(kw * y[4032], y[5952], ws[276768]);
+      ws[282816] = fma(kw * y[4032], y[5952], ws[282816]);
     }
     {
       double w = 2.0 * phi[5920];
@@ -309,7 +309,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54144] * w;
       out[4064] = fma(kw, y[5952], out[4064]);
       out[5952] = fma(kw, y[4064], out[5952]);
-      ws[276800] = fma(kw * y[4064], y[5952], ws[276800]);
+      ws[282848] = fma(kw * y[4064], y[5952], ws[282848]);
     }
     {
       double w = 2.0 * phi[5920];
@@ -320,7 +320,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54176] * w;
       out[3072] = fma(kw, y[5952], out[3072]);
       out[5952] = fma(kw, y[3072], out[5952]);
-      ws[276832] = fma(kw * y[3072], y[5952], ws[276832]);
+      ws[282880] = fma(kw * y[3072], y[5952], ws[282880]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -330,7 +330,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54208] * w;
       out[4032] = fma(kw, y[4032], out[4032]);
       out[4032] = fma(kw, y[4032], out[4032]);
-      ws[276864] = fma(kw * y[4032], y[4032], ws[276864]);
+      ws[282912] = fma(kw * y[4032], y[4032], ws[282912]);
     }
     {
       double w = 0.5 * phi[5984];
@@ -344,7 +344,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54240] * w;
       out[4032] = fma(kw, y[4064], out[4032]);
       out[4064] = fma(kw, y[4032], out[4064]);
-      ws[276896] = fma(kw * y[4032], y[4064], ws[276896]);
+      ws[282944] = fma(kw * y[4032], y[4064], ws[282944]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -357,7 +357,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54272] * w;
       out[4064] = fma(kw, y[4064], out[4064]);
       out[4064] = fma(kw, y[4064], out[4064]);
-      ws[276928] = fma(kw * y[4064], y[4064], ws[276928]);
+      ws[282976] = fma(kw * y[4064], y[4064], ws[282976]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -366,7 +366,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54304] * w;
       out[5216] = fma(kw, y[5952], out[5216]);
       out[5952] = fma(kw, y[5216], out[5952]);
-      ws[276960] = fma(kw * y[5216], y[5952], ws[276960]);
+      ws[283008] = fma(kw * y[5216], y[5952], ws[283008]);
     }
     {
       double w = 1.0 * phi[5632];
@@ -375,7 +375,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54336] * w;
       out[5216] = fma(kw, y[4800], out[5216]);
       out[4800] = fma(kw, y[5216], out[4800]);
-      ws[276992] = fma(kw * y[5216], y[4800], ws[276992]);
+      ws[283040] = fma(kw * y[5216], y[4800], ws[283040]);
     }
     {
       double w = -phi[5216];
@@ -383,7 +383,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54368] * w;
       out[5216] = fma(kw, y[5216], out[5216]);
       out[5216] = fma(kw, y[5216], out[5216]);
-      ws[277024] = fma(kw * y[5216], y[5216], ws[277024]);
+      ws[283072] = fma(kw * y[5216], y[5216], ws[283072]);
     }
     {
       double w = 0.96 * phi[4256];
@@ -397,7 +397,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54400] * w;
       out[3744] = fma(kw, y[4160], out[3744]);
       out[4160] = fma(kw, y[3744], out[4160]);
-      ws[277056] = fma(kw * y[3744], y[4160], ws[277056]);
+      ws[283104] = fma(kw * y[3744], y[4160], ws[283104]);
     }
     {
       double w = 0.96 * phi[4256];
@@ -411,7 +411,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54432] * w;
       out[3744] = fma(kw, y[4192], out[3744]);
       out[4192] = fma(kw, y[3744], out[4192]);
-      ws[277088] = fma(kw * y[3744], y[4192], ws[277088]);
+      ws[283136] = fma(kw * y[3744], y[4192], ws[283136]);
     }
     {
       double w = 0.96 * phi[4256];
@@ -426,7 +426,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54464] * w;
       out[3744] = fma(kw, y[4288], out[3744]);
       out[4288] = fma(kw, y[3744], out[4288]);
-      ws[277120] = fma(kw * y[3744], y[4288], ws[277120]);
+      ws[283168] = fma(kw * y[3744], y[4288], ws[283168]);
     }
     {
       double w = 0.96 * phi[4256];
@@ -440,7 +440,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54496] * w;
       out[3936] = fma(kw, y[4160], out[3936]);
       out[4160] = fma(kw, y[3936], out[4160]);
-      ws[277152] = fma(kw * y[3936], y[4160], ws[277152]);
+      ws[283200] = fma(kw * y[3936], y[4160], ws[283200]);
     }
     {
       double w = 0.96 * phi[4256];
@@ -454,7 +454,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54528] * w;
       out[3936] = fma(kw, y[4192], out[3936]);
       out[4192] = fma(kw, y[3936], out[4192]);
-      ws[277184] = fma(kw * y[3936], y[4192], ws[277184]);
+      ws[283232] = fma(kw * y[3936], y[4192], ws[283232]);
     }
     {
       double w = 0.96 * phi[4256];
@@ -469,7 +469,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54560] * w;
       out[3936] = fma(kw, y[4288], out[3936]);
       out[4288] = fma(kw, y[3936], out[4288]);
-      ws[277216] = fma(kw * y[3936], y[4288], ws[277216]);
+      ws[283264] = fma(kw * y[3936], y[4288], ws[283264]);
     }
     {
       double w = 0.96 * phi[4256];
@@ -483,7 +483,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54592] * w;
       out[3840] = fma(kw, y[4160], out[3840]);
       out[4160] = fma(kw, y[3840], out[4160]);
-      ws[277248] = fma(kw * y[3840], y[4160], ws[277248]);
+      ws[283296] = fma(kw * y[3840], y[4160], ws[283296]);
     }
     {
       double w = 0.96 * phi[4256];
@@ -497,7 +497,7 @@ __device__ __noinline__ void adj_jtv_0_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54624] * w;
       out[3840] = fma(kw, y[4192], out[3840]);
       out[4192] = fma(kw, y[3840], out[4192]);
-      ws[277280] = fma(kw * y[3840], y[4192], ws[277280]);
+      ws[283328] = fma(kw * y[3840], y[4192], ws[283328]);
     }
 }
 __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int phioff, int outoff)
@@ -518,7 +518,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54656] * w;
       out[3840] = fma(kw, y[4288], out[3840]);
       out[4288] = fma(kw, y[3840], out[4288]);
-      ws[277312] = fma(kw * y[3840], y[4288], ws[277312]);
+      ws[283360] = fma(kw * y[3840], y[4288], ws[283360]);
     }
     {
       double w = 0.96 * phi[4256];
@@ -532,7 +532,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54688] * w;
       out[3712] = fma(kw, y[4160], out[3712]);
       out[4160] = fma(kw, y[3712], out[4160]);
-      ws[277344] = fma(kw * y[3712], y[4160], ws[277344]);
+      ws[283392] = fma(kw * y[3712], y[4160], ws[283392]);
     }
     {
       double w = 0.96 * phi[4256];
@@ -546,7 +546,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54720] * w;
       out[3712] = fma(kw, y[4192], out[3712]);
       out[4192] = fma(kw, y[3712], out[4192]);
-      ws[277376] = fma(kw * y[3712], y[4192], ws[277376]);
+      ws[283424] = fma(kw * y[3712], y[4192], ws[283424]);
     }
     {
       double w = 0.96 * phi[4256];
@@ -561,7 +561,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54752] * w;
       out[3712] = fma(kw, y[4288], out[3712]);
       out[4288] = fma(kw, y[3712], out[4288]);
-      ws[277408] = fma(kw * y[3712], y[4288], ws[277408]);
+      ws[283456] = fma(kw * y[3712], y[4288], ws[283456]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -570,7 +570,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54784] * w;
       out[1376] = fma(kw, y[6016], out[1376]);
       out[6016] = fma(kw, y[1376], out[6016]);
-      ws[277440] = fma(kw * y[1376], y[6016], ws[277440]);
+      ws[283488] = fma(kw * y[1376], y[6016], ws[283488]);
     }
     {
       double w = 0.852 * phi[5632];
@@ -580,7 +580,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54816] * w;
       out[384] = fma(kw, y[6016], out[384]);
       out[6016] = fma(kw, y[384], out[6016]);
-      ws[277472] = fma(kw * y[384], y[6016], ws[277472]);
+      ws[283520] = fma(kw * y[384], y[6016], ws[283520]);
     }
     {
       double w = 1.0 * phi[5632];
@@ -590,7 +590,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54848] * w;
       out[416] = fma(kw, y[6016], out[416]);
       out[6016] = fma(kw, y[416], out[6016]);
-      ws[277504] = fma(kw * y[416], y[6016], ws[277504]);
+      ws[283552] = fma(kw * y[416], y[6016], ws[283552]);
     }
     {
       double w = 0.57 * phi[4672];
@@ -600,7 +600,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54880] * w;
       out[3552] = fma(kw, y[6016], out[3552]);
       out[6016] = fma(kw, y[3552], out[6016]);
-      ws[277536] = fma(kw * y[3552], y[6016], ws[277536]);
+      ws[283584] = fma(kw * y[3552], y[6016], ws[283584]);
     }
     {
       double w = 0.84 * phi[5664];
@@ -613,7 +613,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54912] * w;
       out[3552] = fma(kw, y[5184], out[3552]);
       out[5184] = fma(kw, y[3552], out[5184]);
-      ws[277568] = fma(kw * y[3552], y[5184], ws[277568]);
+      ws[283616] = fma(kw * y[3552], y[5184], ws[283616]);
     }
     {
       double w = 0.68 * phi[5856];
@@ -627,7 +627,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54944] * w;
       out[3552] = fma(kw, y[5952], out[3552]);
       out[5952] = fma(kw, y[3552], out[5952]);
-      ws[277600] = fma(kw * y[3552], y[5952], ws[277600]);
+      ws[283648] = fma(kw * y[3552], y[5952], ws[283648]);
     }
     {
       double w = 1.0 * phi[5664];
@@ -640,7 +640,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       w = w - phi[3552];
       const double kw = ws[54976] * w;
       out[3552] = out[3552] + kw;
-      ws[277632] = fma(kw, y[3552], ws[277632]);
+      ws[283680] = fma(kw, y[3552], ws[283680]);
     }
     {
       double w = 0.667 * phi[3136];
@@ -651,7 +651,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55008] * w;
       out[1568] = fma(kw, y[6016], out[1568]);
       out[6016] = fma(kw, y[1568], out[6016]);
-      ws[277664] = fma(kw * y[1568], y[6016], ws[277664]);
+      ws[283712] = fma(kw * y[1568], y[6016], ws[283712]);
     }
     {
       double w = 0.968 * phi[5984];
@@ -665,7 +665,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55040] * w;
       out[3136] = fma(kw, y[5824], out[3136]);
       out[5824] = fma(kw, y[3136], out[5824]);
-      ws[277696] = fma(kw * y[3136], y[5824], ws[277696]);
+      ws[283744] = fma(kw * y[3136], y[5824], ws[283744]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -678,7 +678,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55072] * w;
       out[3136] = fma(kw, y[5952], out[3136]);
       out[5952] = fma(kw, y[3136], out[5952]);
-      ws[277728] = fma(kw * y[3136], y[5952], ws[277728]);
+      ws[283776] = fma(kw * y[3136], y[5952], ws[283776]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -687,7 +687,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55104] * w;
       out[3136] = fma(kw, y[5984], out[3136]);
       out[5984] = fma(kw, y[3136], out[5984]);
-      ws[277760] = fma(kw * y[3136], y[5984], ws[277760]);
+      ws[283808] = fma(kw * y[3136], y[5984], ws[283808]);
     }
     {
       double w = 0.32 * phi[5600];
@@ -703,7 +703,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55136] * w;
       out[3136] = fma(kw, y[5888], out[3136]);
       out[5888] = fma(kw, y[3136], out[5888]);
-      ws[277792] = fma(kw * y[3136], y[5888], ws[277792]);
+      ws[283840] = fma(kw * y[3136], y[5888], ws[283840]);
     }
     {
       double w = 0.7 * phi[5888];
@@ -719,7 +719,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55168] * w;
       out[3136] = fma(kw, y[5792], out[3136]);
       out[5792] = fma(kw, y[3136], out[5792]);
-      ws[277824] = fma(kw * y[3136], y[5792], ws[277824]);
+      ws[283872] = fma(kw * y[3136], y[5792], ws[283872]);
     }
     {
       double w = 0.62 * phi[3552];
@@ -733,7 +733,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55200] * w;
       out[1568] = fma(kw, y[5184], out[1568]);
       out[5184] = fma(kw, y[1568], out[5184]);
-      ws[277856] = fma(kw * y[1568], y[5184], ws[277856]);
+      ws[283904] = fma(kw * y[1568], y[5184], ws[283904]);
     }
     {
       double w = 0.9 * phi[4032];
@@ -744,7 +744,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55232] * w;
       out[1568] = fma(kw, y[5952], out[1568]);
       out[5952] = fma(kw, y[1568], out[5952]);
-      ws[277888] = fma(kw * y[1568], y[5952], ws[277888]);
+      ws[283936] = fma(kw * y[1568], y[5952], ws[283936]);
     }
     {
       double w = 0.49 * phi[5472];
@@ -755,7 +755,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55264] * w;
       out[3168] = fma(kw, y[6016], out[3168]);
       out[6016] = fma(kw, y[3168], out[6016]);
-      ws[277920] = fma(kw * y[3168], y[6016], ws[277920]);
+      ws[283968] = fma(kw * y[3168], y[6016], ws[283968]);
     }
     {
       double w = 0.08 * phi[5440];
@@ -768,7 +768,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55296] * w;
       out[1856] = fma(kw, y[5824], out[1856]);
       out[5824] = fma(kw, y[1856], out[5824]);
-      ws[277952] = fma(kw * y[1856], y[5824], ws[277952]);
+      ws[284000] = fma(kw * y[1856], y[5824], ws[284000]);
     }
     {
       double w = 0.6 * phi[5728];
@@ -781,7 +781,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55328] * w;
       out[1856] = fma(kw, y[5984], out[1856]);
       out[5984] = fma(kw, y[1856], out[5984]);
-      ws[277984] = fma(kw * y[1856], y[5984], ws[277984]);
+      ws[284032] = fma(kw * y[1856], y[5984], ws[284032]);
     }
     {
       double w = 0.65 * phi[5504];
@@ -795,7 +795,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55360] * w;
       out[4512] = fma(kw, y[6016], out[4512]);
       out[6016] = fma(kw, y[4512], out[6016]);
-      ws[278016] = fma(kw * y[4512], y[6016], ws[278016]);
+      ws[284064] = fma(kw * y[4512], y[6016], ws[284064]);
     }
     {
       double w = 0.02 * phi[6016];
@@ -805,7 +805,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55392] * w;
       out[3168] = fma(kw, y[5184], out[3168]);
       out[5184] = fma(kw, y[3168], out[5184]);
-      ws[278048] = fma(kw * y[3168], y[5184], ws[278048]);
+      ws[284096] = fma(kw * y[3168], y[5184], ws[284096]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -816,7 +816,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55424] * w;
       out[3168] = fma(kw, y[5952], out[3168]);
       out[5952] = fma(kw, y[3168], out[5952]);
-      ws[278080] = fma(kw * y[3168], y[5952], ws[278080]);
+      ws[284128] = fma(kw * y[3168], y[5952], ws[284128]);
     }
     {
       double w = 0.613 * phi[5344];
@@ -827,7 +827,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55456] * w;
       out[448] = fma(kw, y[6016], out[448]);
       out[6016] = fma(kw, y[448], out[6016]);
-      ws[278112] = fma(kw * y[448], y[6016], ws[278112]);
+      ws[284160] = fma(kw * y[448], y[6016], ws[284160]);
     }
     {
       double w = 1.0 * phi[1920];
@@ -836,7 +836,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55488] * w;
       out[1600] = fma(kw, y[5952], out[1600]);
       out[5952] = fma(kw, y[1600], out[5952]);
-      ws[278144] = fma(kw * y[1600], y[5952], ws[278144]);
+      ws[284192] = fma(kw * y[1600], y[5952], ws[284192]);
     }
     {
       double w = 1.0 * phi[4928];
@@ -845,7 +845,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55520] * w;
       out[1920] = fma(kw, y[5984], out[1920]);
       out[5984] = fma(kw, y[1920], out[5984]);
-      ws[278176] = fma(kw * y[1920], y[5984], ws[278176]);
+      ws[284224] = fma(kw * y[1920], y[5984], ws[284224]);
     }
     {
       double w = 1.0 * phi[5536];
@@ -855,7 +855,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55552] * w;
       out[1920] = fma(kw, y[5824], out[1920]);
       out[5824] = fma(kw, y[1920], out[5824]);
-      ws[278208] = fma(kw * y[1920], y[5824], ws[278208]);
+      ws[284256] = fma(kw * y[1920], y[5824], ws[284256]);
     }
     {
       double w = 1.0 * phi[5536];
@@ -865,7 +865,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55584] * w;
       out[1920] = fma(kw, y[5952], out[1920]);
       out[5952] = fma(kw, y[1920], out[5952]);
-      ws[278240] = fma(kw * y[1920], y[5952], ws[278240]);
+      ws[284288] = fma(kw * y[1920], y[5952], ws[284288]);
     }
     {
       double w = 0.982 * phi[5536];
@@ -875,7 +875,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55616] * w;
       out[1600] = fma(kw, y[5184], out[1600]);
       out[5184] = fma(kw, y[1600], out[5184]);
-      ws[278272] = fma(kw * y[1600], y[5184], ws[278272]);
+      ws[284320] = fma(kw * y[1600], y[5184], ws[284320]);
     }
     {
       double w = 1.0 * phi[2304];
@@ -884,7 +884,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55648] * w;
       out[1600] = fma(kw, y[6016], out[1600]);
       out[6016] = fma(kw, y[1600], out[6016]);
-      ws[278304] = fma(kw * y[1600], y[6016], ws[278304]);
+      ws[284352] = fma(kw * y[1600], y[6016], ws[284352]);
     }
     {
       double w = 1.0 * phi[4960];
@@ -893,7 +893,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55680] * w;
       out[2304] = fma(kw, y[5984], out[2304]);
       out[5984] = fma(kw, y[2304], out[5984]);
-      ws[278336] = fma(kw * y[2304], y[5984], ws[278336]);
+      ws[284384] = fma(kw * y[2304], y[5984], ws[284384]);
     }
     {
       double w = 1.0 * phi[5536];
@@ -902,7 +902,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55712] * w;
       out[2304] = fma(kw, y[5952], out[2304]);
       out[5952] = fma(kw, y[2304], out[5952]);
-      ws[278368] = fma(kw * y[2304], y[5952], ws[278368]);
+      ws[284416] = fma(kw * y[2304], y[5952], ws[284416]);
     }
     {
       double w = 0.247 * phi[4992];
@@ -913,28 +913,28 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55744] * w;
       out[2304] = fma(kw, y[5824], out[2304]);
       out[5824] = fma(kw, y[2304], out[5824]);
-      ws[278400] = fma(kw * y[2304], y[5824], ws[278400]);
+      ws[284448] = fma(kw * y[2304], y[5824], ws[284448]);
     }
     {
       double w = 1.0 * phi[480];
       w = w - phi[5376];
       const double kw = ws[55776] * w;
       out[5376] = out[5376] + kw;
-      ws[278432] = fma(kw, y[5376], ws[278432]);
+      ws[284480] = fma(kw, y[5376], ws[284480]);
     }
     {
       double w = 1.0 * phi[480];
       w = w - phi[5248];
       const double kw = ws[55808] * w;
       out[5248] = out[5248] + kw;
-      ws[278464] = fma(kw, y[5248], ws[278464]);
+      ws[284512] = fma(kw, y[5248], ws[284512]);
     }
     {
       double w = 2.0 * phi[5024];
       w = w - phi[1024];
       const double kw = ws[55840] * w;
       out[1024] = out[1024] + kw;
-      ws[278496] = fma(kw, y[1024], ws[278496]);
+      ws[284544] = fma(kw, y[1024], ws[284544]);
     }
     {
       double w = 0.5 * phi[1184];
@@ -942,40 +942,40 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       w = w - phi[5920];
       const double kw = ws[55872] * w;
       out[5920] = out[5920] + kw;
-      ws[278528] = fma(kw, y[5920], ws[278528]);
+      ws[284576] = fma(kw, y[5920], ws[284576]);
     }
     {
       double w = -phi[5984];
       const double kw = ws[55904] * w;
       out[5984] = out[5984] + kw;
-      ws[278560] = fma(kw, y[5984], ws[278560]);
+      ws[284608] = fma(kw, y[5984], ws[284608]);
     }
     {
       double w = 1.0 * phi[5024];
       w = w - phi[5952];
       const double kw = ws[55936] * w;
       out[5952] = out[5952] + kw;
-      ws[278592] = fma(kw, y[5952], ws[278592]);
+      ws[284640] = fma(kw, y[5952], ws[284640]);
     }
     {
       double w = -phi[5184];
       const double kw = ws[55968] * w;
       out[5184] = out[5184] + kw;
-      ws[278624] = fma(kw, y[5184], ws[278624]);
+      ws[284672] = fma(kw, y[5184], ws[284672]);
     }
     {
       double w = 1.0 * phi[1056];
       w = w - phi[1376];
       const double kw = ws[56000] * w;
       out[1376] = out[1376] + kw;
-      ws[278656] = fma(kw, y[1376], ws[278656]);
+      ws[284704] = fma(kw, y[1376], ws[284704]);
     }
     {
       double w = 1.0 * phi[0];
       w = w - phi[1056];
       const double kw = ws[56032] * w;
       out[1056] = out[1056] + kw;
-      ws[278688] = fma(kw, y[1056], ws[278688]);
+      ws[284736] = fma(kw, y[1056], ws[284736]);
     }
     {
       double w = 1.0 * phi[544];
@@ -984,14 +984,14 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56064] * w;
       out[1056] = fma(kw, y[512], out[1056]);
       out[512] = fma(kw, y[1056], out[512]);
-      ws[278720] = fma(kw * y[1056], y[512], ws[278720]);
+      ws[284768] = fma(kw * y[1056], y[512], ws[284768]);
     }
     {
       double w = 1.0 * phi[32];
       w = w - phi[1664];
       const double kw = ws[56096] * w;
       out[1664] = out[1664] + kw;
-      ws[278752] = fma(kw, y[1664], ws[278752]);
+      ws[284800] = fma(kw, y[1664], ws[284800]);
     }
     {
       double w = 1.0 * phi[64];
@@ -999,7 +999,7 @@ __device__ __noinline__ void adj_jtv_0_9(double* __restrict__ ws, int yoff, int 
       w = w - phi[2208];
       const double kw = ws[56128] * w;
       out[2208] = out[2208] + kw;
-      ws[278784] = fma(kw, y[2208], ws[278784]);
+      ws[284832] = fma(kw, y[2208], ws[284832]);
     }
 }
 __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int phioff, int outoff)
@@ -1014,7 +1014,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[56160] * w;
       out[608] = fma(kw, y[6016], out[608]);
       out[6016] = fma(kw, y[608], out[6016]);
-      ws[278816] = fma(kw * y[608], y[6016], ws[278816]);
+      ws[284864] = fma(kw * y[608], y[6016], ws[284864]);
     }
     {
       double w = 1.0 * phi[2400];
@@ -1023,7 +1023,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[56192] * w;
       out[640] = fma(kw, y[6016], out[640]);
       out[6016] = fma(kw, y[640], out[6016]);
-      ws[278848] = fma(kw * y[640], y[6016], ws[278848]);
+      ws[284896] = fma(kw * y[640], y[6016], ws[284896]);
     }
     {
       double w = 1.0 * phi[2432];
@@ -1032,7 +1032,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[56224] * w;
       out[672] = fma(kw, y[6016], out[672]);
       out[6016] = fma(kw, y[672], out[6016]);
-      ws[278880] = fma(kw * y[672], y[6016], ws[278880]);
+      ws[284928] = fma(kw * y[672], y[6016], ws[284928]);
     }
     {
       double w = 1.0 * phi[2464];
@@ -1041,7 +1041,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[56256] * w;
       out[704] = fma(kw, y[6016], out[704]);
       out[6016] = fma(kw, y[704], out[6016]);
-      ws[278912] = fma(kw * y[704], y[6016], ws[278912]);
+      ws[284960] = fma(kw * y[704], y[6016], ws[284960]);
     }
     {
       double w = 1.0 * phi[2496];
@@ -1050,7 +1050,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[56288] * w;
       out[736] = fma(kw, y[6016], out[736]);
       out[6016] = fma(kw, y[736], out[6016]);
-      ws[278944] = fma(kw * y[736], y[6016], ws[278944]);
+      ws[284992] = fma(kw * y[736], y[6016], ws[284992]);
     }
     {
       double w = 1.0 * phi[2528];
@@ -1059,7 +1059,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[56320] * w;
       out[768] = fma(kw, y[6016], out[768]);
       out[6016] = fma(kw, y[768], out[6016]);
-      ws[278976] = fma(kw * y[768], y[6016], ws[278976]);
+      ws[285024] = fma(kw * y[768], y[6016], ws[285024]);
     }
     {
       double w = 1.0 * phi[3904];
@@ -1068,7 +1068,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[56352] * w;
       out[800] = fma(kw, y[6016], out[800]);
       out[6016] = fma(kw, y[800], out[6016]);
-      ws[279008] = fma(kw * y[800], y[6016], ws[279008]);
+      ws[285056] = fma(kw * y[800], y[6016], ws[285056]);
     }
     {
       double w = 0.72 * phi[1952];
@@ -1079,7 +1079,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[56384] * w;
       out[2368] = fma(kw, y[5824], out[2368]);
       out[5824] = fma(kw, y[2368], out[5824]);
-      ws[279040] = fma(kw * y[2368], y[5824], ws[279040]);
+      ws[285088] = fma(kw * y[2368], y[5824], ws[285088]);
     }
     {
       double w = 0.72 * phi[1984];
@@ -1090,7 +1090,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[56416] * w;
       out[2400] = fma(kw, y[5824], out[2400]);
       out[5824] = fma(kw, y[2400], out[5824]);
-      ws[279072] = fma(kw * y[2400], y[5824], ws[279072]);
+      ws[285120] = fma(kw * y[2400], y[5824], ws[285120]);
     }
     {
       double w = 0.72 * phi[2016];
@@ -1101,7 +1101,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[56448] * w;
       out[2432] = fma(kw, y[5824], out[2432]);
       out[5824] = fma(kw, y[2432], out[5824]);
-      ws[279104] = fma(kw * y[2432], y[5824], ws[279104]);
+      ws[285152] = fma(kw * y[2432], y[5824], ws[285152]);
     }
     {
       double w = 0.72 * phi[2048];
@@ -1112,7 +1112,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[56480] * w;
       out[2464] = fma(kw, y[5824], out[2464]);
       out[5824] = fma(kw, y[2464], out[5824]);
-      ws[279136] = fma(kw * y[2464], y[5824], ws[279136]);
+      ws[285184] = fma(kw * y[2464], y[5824], ws[285184]);
     }
     {
       double w = 0.72 * phi[2080];
@@ -1123,7 +1123,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[56512] * w;
       out[2496] = fma(kw, y[5824], out[2496]);
       out[5824] = fma(kw, y[2496], out[5824]);
-      ws[279168] = fma(kw * y[2496], y[5824], ws[279168]);
+      ws[285216] = fma(kw * y[2496], y[5824], ws[285216]);
     }
     {
       double w = 0.72 * phi[2112];
@@ -1134,7 +1134,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[56544] * w;
       out[2528] = fma(kw, y[5824], out[2528]);
       out[5824] = fma(kw, y[2528], out[5824]);
-      ws[279200] = fma(kw * y[2528], y[5824], ws[279200]);
+      ws[285248] = fma(kw * y[2528], y[5824], ws[285248]);
     }
     {
       double w = 0.74 * phi[2144];
@@ -1145,7 +1145,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[56576] * w;
       out[3904] = fma(kw, y[5824], out[3904]);
       out[5824] = fma(kw, y[3904], out[5824]);
-      ws[279232] = fma(kw * y[3904], y[5824], ws[279232]);
+      ws[285280] = fma(kw * y[3904], y[5824], ws[285280]);
     }
     {
       double w = 1.0 * phi[1952];
@@ -1155,7 +1155,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[56608] * w;
       out[2368] = fma(kw, y[5952], out[2368]);
       out[5952] = fma(kw, y[2368], out[5952]);
-      ws[279264] = fma(kw * y[2368], y[5952], ws[279264]);
+      ws[285312] = fma(kw * y[2368], y[5952], ws[285312]);
     }
     {
       double w = 1.0 * phi[1984];
@@ -1165,7 +1165,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[56640] * w;
       out[2400] = fma(kw, y[5952], out[2400]);
       out[5952] = fma(kw, y[2400], out[5952]);
-      ws[279296] = fma(kw * y[2400], y[5952], ws[279296]);
+      ws[285344] = fma(kw * y[2400], y[5952], ws[285344]);
     }
     {
       double w = 1.0 * phi[2016];
@@ -1175,7 +1175,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[56672] * w;
       out[2432] = fma(kw, y[5952], out[2432]);
       out[5952] = fma(kw, y[2432], out[5952]);
-      ws[279328] = fma(kw * y[2432], y[5952], ws[279328]);
+      ws[285376] = fma(kw * y[2432], y[5952], ws[285376]);
     }
     {
       double w = 1.0 * phi[2048];
@@ -1185,7 +1185,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[56704] * w;
       out[2464] = fma(kw, y[5952], out[2464]);
       out[5952] = fma(kw, y[2464], out[5952]);
-      ws[279360] = fma(kw * y[2464], y[5952], ws[279360]);
+      ws[285408] = fma(kw * y[2464], y[5952], ws[285408]);
     }
     {
       double w = 1.0 * phi[2080];
@@ -1195,7 +1195,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[56736] * w;
       out[2496] = fma(kw, y[5952], out[2496]);
       out[5952] = fma(kw, y[2496], out[5952]);
-      ws[279392] = fma(kw * y[2496], y[5952], ws[279392]);
+      ws[285440] = fma(kw * y[2496], y[5952], ws[285440]);
     }
     {
       double w = 1.0 * phi[2112];
@@ -1205,7 +1205,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[56768] * w;
       out[2528] = fma(kw, y[5952], out[2528]);
       out[5952] = fma(kw, y[2528], out[5952]);
-      ws[279424] = fma(kw * y[2528], y[5952], ws[279424]);
+      ws[285472] = fma(kw * y[2528], y[5952], ws[285472]);
     }
     {
       double w = 1.0 * phi[2144];
@@ -1215,7 +1215,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[56800] * w;
       out[3904] = fma(kw, y[5952], out[3904]);
       out[5952] = fma(kw, y[3904], out[5952]);
-      ws[279456] = fma(kw * y[3904], y[5952], ws[279456]);
+      ws[285504] = fma(kw * y[3904], y[5952], ws[285504]);
     }
     {
       double w = 1.0 * phi[5536];
@@ -1224,7 +1224,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[56832] * w;
       out[2368] = fma(kw, y[5984], out[2368]);
       out[5984] = fma(kw, y[2368], out[5984]);
-      ws[279488] = fma(kw * y[2368], y[5984], ws[279488]);
+      ws[285536] = fma(kw * y[2368], y[5984], ws[285536]);
     }
     {
       double w = 1.0 * phi[5088];
@@ -1233,7 +1233,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[56864] * w;
       out[2400] = fma(kw, y[5984], out[2400]);
       out[5984] = fma(kw, y[2400], out[5984]);
-      ws[279520] = fma(kw * y[2400], y[5984], ws[279520]);
+      ws[285568] = fma(kw * y[2400], y[5984], ws[285568]);
     }
     {
       double w = 1.0 * phi[4704];
@@ -1242,7 +1242,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[56896] * w;
       out[2432] = fma(kw, y[5984], out[2432]);
       out[5984] = fma(kw, y[2432], out[5984]);
-      ws[279552] = fma(kw * y[2432], y[5984], ws[279552]);
+      ws[285600] = fma(kw * y[2432], y[5984], ws[285600]);
     }
     {
       double w = 1.0 * phi[4960];
@@ -1251,7 +1251,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[56928] * w;
       out[2464] = fma(kw, y[5984], out[2464]);
       out[5984] = fma(kw, y[2464], out[5984]);
-      ws[279584] = fma(kw * y[2464], y[5984], ws[279584]);
+      ws[285632] = fma(kw * y[2464], y[5984], ws[285632]);
     }
     {
       double w = 1.0 * phi[4416];
@@ -1260,7 +1260,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[56960] * w;
       out[2496] = fma(kw, y[5984], out[2496]);
       out[5984] = fma(kw, y[2496], out[5984]);
-      ws[279616] = fma(kw * y[2496], y[5984], ws[279616]);
+      ws[285664] = fma(kw * y[2496], y[5984], ws[285664]);
     }
     {
       double w = 1.0 * phi[4832];
@@ -1269,7 +1269,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[56992] * w;
       out[2528] = fma(kw, y[5984], out[2528]);
       out[5984] = fma(kw, y[2528], out[5984]);
-      ws[279648] = fma(kw * y[2528], y[5984], ws[279648]);
+      ws[285696] = fma(kw * y[2528], y[5984], ws[285696]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -1278,7 +1278,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57024] * w;
       out[3904] = fma(kw, y[5984], out[3904]);
       out[5984] = fma(kw, y[3904], out[5984]);
-      ws[279680] = fma(kw * y[3904], y[5984], ws[279680]);
+      ws[285728] = fma(kw * y[3904], y[5984], ws[285728]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1286,7 +1286,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       w = w - phi[1952];
       const double kw = ws[57056] * w;
       out[1952] = out[1952] + kw;
-      ws[279712] = fma(kw, y[1952], ws[279712]);
+      ws[285760] = fma(kw, y[1952], ws[285760]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1294,7 +1294,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       w = w - phi[1984];
       const double kw = ws[57088] * w;
       out[1984] = out[1984] + kw;
-      ws[279744] = fma(kw, y[1984], ws[279744]);
+      ws[285792] = fma(kw, y[1984], ws[285792]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1302,7 +1302,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       w = w - phi[2016];
       const double kw = ws[57120] * w;
       out[2016] = out[2016] + kw;
-      ws[279776] = fma(kw, y[2016], ws[279776]);
+      ws[285824] = fma(kw, y[2016], ws[285824]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1310,7 +1310,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       w = w - phi[2048];
       const double kw = ws[57152] * w;
       out[2048] = out[2048] + kw;
-      ws[279808] = fma(kw, y[2048], ws[279808]);
+      ws[285856] = fma(kw, y[2048], ws[285856]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1318,7 +1318,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       w = w - phi[2080];
       const double kw = ws[57184] * w;
       out[2080] = out[2080] + kw;
-      ws[279840] = fma(kw, y[2080], ws[279840]);
+      ws[285888] = fma(kw, y[2080], ws[285888]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1326,7 +1326,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       w = w - phi[2112];
       const double kw = ws[57216] * w;
       out[2112] = out[2112] + kw;
-      ws[279872] = fma(kw, y[2112], ws[279872]);
+      ws[285920] = fma(kw, y[2112], ws[285920]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1334,7 +1334,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       w = w - phi[2144];
       const double kw = ws[57248] * w;
       out[2144] = out[2144] + kw;
-      ws[279904] = fma(kw, y[2144], ws[279904]);
+      ws[285952] = fma(kw, y[2144], ws[285952]);
     }
     {
       double w = 0.14 * phi[5088];
@@ -1346,7 +1346,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57280] * w;
       out[1952] = fma(kw, y[5824], out[1952]);
       out[5824] = fma(kw, y[1952], out[5824]);
-      ws[279936] = fma(kw * y[1952], y[5824], ws[279936]);
+      ws[285984] = fma(kw * y[1952], y[5824], ws[285984]);
     }
     {
       double w = 0.14 * phi[4992];
@@ -1358,7 +1358,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57312] * w;
       out[1984] = fma(kw, y[5824], out[1984]);
       out[5824] = fma(kw, y[1984], out[5824]);
-      ws[279968] = fma(kw * y[1984], y[5824], ws[279968]);
+      ws[286016] = fma(kw * y[1984], y[5824], ws[286016]);
     }
     {
       double w = 0.14 * phi[4960];
@@ -1370,7 +1370,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57344] * w;
       out[2016] = fma(kw, y[5824], out[2016]);
       out[5824] = fma(kw, y[2016], out[5824]);
-      ws[280000] = fma(kw * y[2016], y[5824], ws[280000]);
+      ws[286048] = fma(kw * y[2016], y[5824], ws[286048]);
     }
     {
       double w = 0.14 * phi[4416];
@@ -1382,7 +1382,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57376] * w;
       out[2048] = fma(kw, y[5824], out[2048]);
       out[5824] = fma(kw, y[2048], out[5824]);
-      ws[280032] = fma(kw * y[2048], y[5824], ws[280032]);
+      ws[286080] = fma(kw * y[2048], y[5824], ws[286080]);
     }
     {
       double w = 0.14 * phi[4832];
@@ -1394,7 +1394,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57408] * w;
       out[2080] = fma(kw, y[5824], out[2080]);
       out[5824] = fma(kw, y[2080], out[5824]);
-      ws[280064] = fma(kw * y[2080], y[5824], ws[280064]);
+      ws[286112] = fma(kw * y[2080], y[5824], ws[286112]);
     }
     {
       double w = 1.0 * phi[4832];
@@ -1405,7 +1405,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57440] * w;
       out[2112] = fma(kw, y[5824], out[2112]);
       out[5824] = fma(kw, y[2112], out[5824]);
-      ws[280096] = fma(kw * y[2112], y[5824], ws[280096]);
+      ws[286144] = fma(kw * y[2112], y[5824], ws[286144]);
     }
     {
       double w = 0.12 * phi[5440];
@@ -1417,7 +1417,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57472] * w;
       out[2144] = fma(kw, y[5824], out[2144]);
       out[5824] = fma(kw, y[2144], out[5824]);
-      ws[280128] = fma(kw * y[2144], y[5824], ws[280128]);
+      ws[286176] = fma(kw * y[2144], y[5824], ws[286176]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1428,7 +1428,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57504] * w;
       out[1952] = fma(kw, y[5952], out[1952]);
       out[5952] = fma(kw, y[1952], out[5952]);
-      ws[280160] = fma(kw * y[1952], y[5952], ws[280160]);
+      ws[286208] = fma(kw * y[1952], y[5952], ws[286208]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1439,7 +1439,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57536] * w;
       out[1984] = fma(kw, y[5952], out[1984]);
       out[5952] = fma(kw, y[1984], out[5952]);
-      ws[280192] = fma(kw * y[1984], y[5952], ws[280192]);
+      ws[286240] = fma(kw * y[1984], y[5952], ws[286240]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1450,7 +1450,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57568] * w;
       out[2016] = fma(kw, y[5952], out[2016]);
       out[5952] = fma(kw, y[2016], out[5952]);
-      ws[280224] = fma(kw * y[2016], y[5952], ws[280224]);
+      ws[286272] = fma(kw * y[2016], y[5952], ws[286272]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1461,7 +1461,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57600] * w;
       out[2048] = fma(kw, y[5952], out[2048]);
       out[5952] = fma(kw, y[2048], out[5952]);
-      ws[280256] = fma(kw * y[2048], y[5952], ws[280256]);
+      ws[286304] = fma(kw * y[2048], y[5952], ws[286304]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1472,7 +1472,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57632] * w;
       out[2080] = fma(kw, y[5952], out[2080]);
       out[5952] = fma(kw, y[2080], out[5952]);
-      ws[280288] = fma(kw * y[2080], y[5952], ws[280288]);
+      ws[286336] = fma(kw * y[2080], y[5952], ws[286336]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1483,7 +1483,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57664] * w;
       out[2112] = fma(kw, y[5952], out[2112]);
       out[5952] = fma(kw, y[2112], out[5952]);
-      ws[280320] = fma(kw * y[2112], y[5952], ws[280320]);
+      ws[286368] = fma(kw * y[2112], y[5952], ws[286368]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1494,7 +1494,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57696] * w;
       out[2144] = fma(kw, y[5952], out[2144]);
       out[5952] = fma(kw, y[2144], out[5952]);
-      ws[280352] = fma(kw * y[2144], y[5952], ws[280352]);
+      ws[286400] = fma(kw * y[2144], y[5952], ws[286400]);
     }
     {
       double w = 1.0 * phi[4992];
@@ -1503,7 +1503,7 @@ __device__ __noinline__ void adj_jtv_0_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57728] * w;
       out[1952] = fma(kw, y[5984], out[1952]);
       out[5984] = fma(kw, y[1952], out[5984]);
-      ws[280384] = fma(kw * y[1952], y[5984], ws[280384]);
+      ws[286432] = fma(kw * y[1952], y[5984], ws[286432]);
     }
 }
 __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int phioff, int outoff)
@@ -1518,7 +1518,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[57760] * w;
       out[1984] = fma(kw, y[5984], out[1984]);
       out[5984] = fma(kw, y[1984], out[5984]);
-      ws[280416] = fma(kw * y[1984], y[5984], ws[280416]);
+      ws[286464] = fma(kw * y[1984], y[5984], ws[286464]);
     }
     {
       double w = 1.0 * phi[4416];
@@ -1527,7 +1527,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[57792] * w;
       out[2016] = fma(kw, y[5984], out[2016]);
       out[5984] = fma(kw, y[2016], out[5984]);
-      ws[280448] = fma(kw * y[2016], y[5984], ws[280448]);
+      ws[286496] = fma(kw * y[2016], y[5984], ws[286496]);
     }
     {
       double w = 1.0 * phi[4832];
@@ -1536,7 +1536,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[57824] * w;
       out[2048] = fma(kw, y[5984], out[2048]);
       out[5984] = fma(kw, y[2048], out[5984]);
-      ws[280480] = fma(kw * y[2048], y[5984], ws[280480]);
+      ws[286528] = fma(kw * y[2048], y[5984], ws[286528]);
     }
     {
       double w = 1.0 * phi[4832];
@@ -1545,7 +1545,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[57856] * w;
       out[2080] = fma(kw, y[5984], out[2080]);
       out[5984] = fma(kw, y[2080], out[5984]);
-      ws[280512] = fma(kw * y[2080], y[5984], ws[280512]);
+      ws[286560] = fma(kw * y[2080], y[5984], ws[286560]);
     }
     {
       double w = 1.0 * phi[4832];
@@ -1554,7 +1554,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[57888] * w;
       out[2112] = fma(kw, y[5984], out[2112]);
       out[5984] = fma(kw, y[2112], out[5984]);
-      ws[280544] = fma(kw * y[2112], y[5984], ws[280544]);
+      ws[286592] = fma(kw * y[2112], y[5984], ws[286592]);
     }
     {
       double w = 1.0 * phi[5088];
@@ -1563,7 +1563,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[57920] * w;
       out[2144] = fma(kw, y[5984], out[2144]);
       out[5984] = fma(kw, y[2144], out[5984]);
-      ws[280576] = fma(kw * y[2144], y[5984], ws[280576]);
+      ws[286624] = fma(kw * y[2144], y[5984], ws[286624]);
     }
     {
       double w = 0.84 * phi[3392];
@@ -1574,7 +1574,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[57952] * w;
       out[832] = fma(kw, y[6016], out[832]);
       out[6016] = fma(kw, y[832], out[6016]);
-      ws[280608] = fma(kw * y[832], y[6016], ws[280608]);
+      ws[286656] = fma(kw * y[832], y[6016], ws[286656]);
     }
     {
       double w = 0.0595 * phi[5312];
@@ -1585,7 +1585,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[57984] * w;
       out[3392] = fma(kw, y[5984], out[3392]);
       out[5984] = fma(kw, y[3392], out[5984]);
-      ws[280640] = fma(kw * y[3392], y[5984], ws[280640]);
+      ws[286688] = fma(kw * y[3392], y[5984], ws[286688]);
     }
     {
       double w = 0.0001 * phi[5312];
@@ -1603,7 +1603,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58016] * w;
       out[3392] = fma(kw, y[5824], out[3392]);
       out[5824] = fma(kw, y[3392], out[5824]);
-      ws[280672] = fma(kw * y[3392], y[5824], ws[280672]);
+      ws[286720] = fma(kw * y[3392], y[5824], ws[286720]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1618,7 +1618,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58048] * w;
       out[3392] = fma(kw, y[5952], out[3392]);
       out[5952] = fma(kw, y[3392], out[5952]);
-      ws[280704] = fma(kw * y[3392], y[5952], ws[280704]);
+      ws[286752] = fma(kw * y[3392], y[5952], ws[286752]);
     }
     {
       double w = 0.68 * phi[5856];
@@ -1634,7 +1634,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58080] * w;
       out[3392] = fma(kw, y[5888], out[3392]);
       out[5888] = fma(kw, y[3392], out[5888]);
-      ws[280736] = fma(kw * y[3392], y[5888], ws[280736]);
+      ws[286784] = fma(kw * y[3392], y[5888], ws[286784]);
     }
     {
       double w = 0.7 * phi[5888];
@@ -1650,7 +1650,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58112] * w;
       out[3392] = fma(kw, y[5792], out[3392]);
       out[5792] = fma(kw, y[3392], out[5792]);
-      ws[280768] = fma(kw * y[3392], y[5792], ws[280768]);
+      ws[286816] = fma(kw * y[3392], y[5792], ws[286816]);
     }
     {
       double w = 0.84 * phi[3424];
@@ -1661,7 +1661,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58144] * w;
       out[864] = fma(kw, y[6016], out[864]);
       out[6016] = fma(kw, y[864], out[6016]);
-      ws[280800] = fma(kw * y[864], y[6016], ws[280800]);
+      ws[286848] = fma(kw * y[864], y[6016], ws[286848]);
     }
     {
       double w = 0.0595 * phi[5536];
@@ -1672,7 +1672,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58176] * w;
       out[3424] = fma(kw, y[5984], out[3424]);
       out[5984] = fma(kw, y[3424], out[5984]);
-      ws[280832] = fma(kw * y[3424], y[5984], ws[280832]);
+      ws[286880] = fma(kw * y[3424], y[5984], ws[286880]);
     }
     {
       double w = 0.0001 * phi[5536];
@@ -1690,7 +1690,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58208] * w;
       out[3424] = fma(kw, y[5824], out[3424]);
       out[5824] = fma(kw, y[3424], out[5824]);
-      ws[280864] = fma(kw * y[3424], y[5824], ws[280864]);
+      ws[286912] = fma(kw * y[3424], y[5824], ws[286912]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1705,7 +1705,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58240] * w;
       out[3424] = fma(kw, y[5952], out[3424]);
       out[5952] = fma(kw, y[3424], out[5952]);
-      ws[280896] = fma(kw * y[3424], y[5952], ws[280896]);
+      ws[286944] = fma(kw * y[3424], y[5952], ws[286944]);
     }
     {
       double w = 0.68 * phi[5856];
@@ -1721,7 +1721,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58272] * w;
       out[3424] = fma(kw, y[5888], out[3424]);
       out[5888] = fma(kw, y[3424], out[5888]);
-      ws[280928] = fma(kw * y[3424], y[5888], ws[280928]);
+      ws[286976] = fma(kw * y[3424], y[5888], ws[286976]);
     }
     {
       double w = 0.7 * phi[5888];
@@ -1737,7 +1737,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58304] * w;
       out[3424] = fma(kw, y[5792], out[3424]);
       out[5792] = fma(kw, y[3424], out[5792]);
-      ws[280960] = fma(kw * y[3424], y[5792], ws[280960]);
+      ws[287008] = fma(kw * y[3424], y[5792], ws[287008]);
     }
     {
       double w = 0.84 * phi[3456];
@@ -1748,7 +1748,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58336] * w;
       out[896] = fma(kw, y[6016], out[896]);
       out[6016] = fma(kw, y[896], out[6016]);
-      ws[280992] = fma(kw * y[896], y[6016], ws[280992]);
+      ws[287040] = fma(kw * y[896], y[6016], ws[287040]);
     }
     {
       double w = 0.0595 * phi[5536];
@@ -1759,7 +1759,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58368] * w;
       out[3456] = fma(kw, y[5984], out[3456]);
       out[5984] = fma(kw, y[3456], out[5984]);
-      ws[281024] = fma(kw * y[3456], y[5984], ws[281024]);
+      ws[287072] = fma(kw * y[3456], y[5984], ws[287072]);
     }
     {
       double w = 0.0595 * phi[5312];
@@ -1776,7 +1776,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58400] * w;
       out[3456] = fma(kw, y[5824], out[3456]);
       out[5824] = fma(kw, y[3456], out[5824]);
-      ws[281056] = fma(kw * y[3456], y[5824], ws[281056]);
+      ws[287104] = fma(kw * y[3456], y[5824], ws[287104]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1791,7 +1791,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58432] * w;
       out[3456] = fma(kw, y[5952], out[3456]);
       out[5952] = fma(kw, y[3456], out[5952]);
-      ws[281088] = fma(kw * y[3456], y[5952], ws[281088]);
+      ws[287136] = fma(kw * y[3456], y[5952], ws[287136]);
     }
     {
       double w = 0.68 * phi[5856];
@@ -1807,7 +1807,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58464] * w;
       out[3456] = fma(kw, y[5888], out[3456]);
       out[5888] = fma(kw, y[3456], out[5888]);
-      ws[281120] = fma(kw * y[3456], y[5888], ws[281120]);
+      ws[287168] = fma(kw * y[3456], y[5888], ws[287168]);
     }
     {
       double w = 0.7 * phi[5888];
@@ -1823,7 +1823,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58496] * w;
       out[3456] = fma(kw, y[5792], out[3456]);
       out[5792] = fma(kw, y[3456], out[5792]);
-      ws[281152] = fma(kw * y[3456], y[5792], ws[281152]);
+      ws[287200] = fma(kw * y[3456], y[5792], ws[287200]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -1841,7 +1841,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58528] * w;
       out[4768] = fma(kw, y[6016], out[4768]);
       out[6016] = fma(kw, y[4768], out[6016]);
-      ws[281184] = fma(kw * y[4768], y[6016], ws[281184]);
+      ws[287232] = fma(kw * y[4768], y[6016], ws[287232]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -1872,7 +1872,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58560] * w;
       out[4864] = fma(kw, y[6016], out[4864]);
       out[6016] = fma(kw, y[4864], out[6016]);
-      ws[281216] = fma(kw * y[4864], y[6016], ws[281216]);
+      ws[287264] = fma(kw * y[4864], y[6016], ws[287264]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -1907,7 +1907,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58592] * w;
       out[4832] = fma(kw, y[6016], out[4832]);
       out[6016] = fma(kw, y[4832], out[6016]);
-      ws[281248] = fma(kw * y[4832], y[6016], ws[281248]);
+      ws[287296] = fma(kw * y[4832], y[6016], ws[287296]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -1928,7 +1928,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58624] * w;
       out[4896] = fma(kw, y[6016], out[4896]);
       out[6016] = fma(kw, y[4896], out[6016]);
-      ws[281280] = fma(kw * y[4896], y[6016], ws[281280]);
+      ws[287328] = fma(kw * y[4896], y[6016], ws[287328]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -1961,7 +1961,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58656] * w;
       out[4640] = fma(kw, y[6016], out[4640]);
       out[6016] = fma(kw, y[4640], out[6016]);
-      ws[281312] = fma(kw * y[4640], y[6016], ws[281312]);
+      ws[287360] = fma(kw * y[4640], y[6016], ws[287360]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -1997,7 +1997,7 @@ __device__ __noinline__ void adj_jtv_0_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58688] * w;
       out[4416] = fma(kw, y[6016], out[4416]);
       out[6016] = fma(kw, y[4416], out[6016]);
-      ws[281344] = fma(kw * y[4416], y[6016], ws[281344]);
+      ws[287392] = fma(kw * y[4416], y[6016], ws[287392]);
     }
 }
 }  // namespace mech_cracmm2

@@ -35,7 +35,7 @@ __device__ __noinline__ void adj_jtv_0_12(double* __restrict__ ws, int yoff, int
       const double kw = ws[58720] * w;
       out[4928] = fma(kw, y[6016], out[4928]);
       out[6016] = fma(kw, y[4928], out[6016]);
-      ws[281376] = fma(kw * y[4928], y[6016], ws[281376]);
+      ws[287424] = fma(kw * y[4928], y[6016], ws[287424]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -70,7 +70,7 @@ __device__ __noinline__ void adj_jtv_0_12(double* __restrict__ ws, int yoff, int
       const double kw = ws[58752] * w;
       out[4960] = fma(kw, y[6016], out[4960]);
       out[6016] = fma(kw, y[4960], out[6016]);
-      ws[281408] = fma(kw * y[4960], y[6016], ws[281408]);
+      ws[287456] = fma(kw * y[4960], y[6016], ws[287456]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -103,7 +103,7 @@ __device__ __noinline__ void adj_jtv_0_12(double* __restrict__ ws, int yoff, int
       const double kw = ws[58784] * w;
       out[4992] = fma(kw, y[6016], out[4992]);
       out[6016] = fma(kw, y[4992], out[6016]);
-      ws[281440] = fma(kw * y[4992], y[6016], ws[281440]);
+      ws[287488] = fma(kw * y[4992], y[6016], ws[287488]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -139,7 +139,7 @@ __device__ __noinline__ void adj_jtv_0_12(double* __restrict__ ws, int yoff, int
       const double kw = ws[58816] * w;
       out[4704] = fma(kw, y[6016], out[4704]);
       out[6016] = fma(kw, y[4704], out[6016]);
-      ws[281472] = fma(kw * y[4704], y[6016], ws[281472]);
+      ws[287520] = fma(kw * y[4704], y[6016], ws[287520]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -175,7 +175,7 @@ __device__ __noinline__ void adj_jtv_0_12(double* __restrict__ ws, int yoff, int
       const double kw = ws[58848] * w;
       out[5088] = fma(kw, y[6016], out[5088]);
       out[6016] = fma(kw, y[5088], out[6016]);
-      ws[281504] = fma(kw * y[5088], y[6016], ws[281504]);
+      ws[287552] = fma(kw * y[5088], y[6016], ws[287552]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -210,7 +210,7 @@ __device__ __noinline__ void adj_jtv_0_12(double* __restrict__ ws, int yoff, int
       const double kw = ws[58880] * w;
       out[5536] = fma(kw, y[6016], out[5536]);
       out[6016] = fma(kw, y[5536], out[6016]);
-      ws[281536] = fma(kw * y[5536], y[6016], ws[281536]);
+      ws[287584] = fma(kw * y[5536], y[6016], ws[287584]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -243,7 +243,7 @@ __device__ __noinline__ void adj_jtv_0_12(double* __restrict__ ws, int yoff, int
       const double kw = ws[58912] * w;
       out[5312] = fma(kw, y[6016], out[5312]);
       out[6016] = fma(kw, y[5312], out[6016]);
-      ws[281568] = fma(kw * y[5312], y[6016], ws[281568]);
+      ws[287616] = fma(kw * y[5312], y[6016], ws[287616]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -277,7 +277,7 @@ __device__ __noinline__ void adj_jtv_0_12(double* __restrict__ ws, int yoff, int
       const double kw = ws[58944] * w;
       out[4224] = fma(kw, y[6016], out[4224]);
       out[6016] = fma(kw, y[4224], out[6016]);
-      ws[281600] = fma(kw * y[4224], y[6016], ws[281600]);
+      ws[287648] = fma(kw * y[4224], y[6016], ws[287648]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -308,7 +308,7 @@ __device__ __noinline__ void adj_jtv_0_12(double* __restrict__ ws, int yoff, int
       const double kw = ws[58976] * w;
       out[3968] = fma(kw, y[6016], out[3968]);
       out[6016] = fma(kw, y[3968], out[6016]);
-      ws[281632] = fma(kw * y[3968], y[6016], ws[281632]);
+      ws[287680] = fma(kw * y[3968], y[6016], ws[287680]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -329,7 +329,7 @@ __device__ __noinline__ void adj_jtv_0_12(double* __restrict__ ws, int yoff, int
       const double kw = ws[59008] * w;
       out[4608] = fma(kw, y[6016], out[4608]);
       out[6016] = fma(kw, y[4608], out[6016]);
-      ws[281664] = fma(kw * y[4608], y[6016], ws[281664]);
+      ws[287712] = fma(kw * y[4608], y[6016], ws[287712]);
     }
     {
       double w = 1.0 * phi[5888];
@@ -338,7 +338,7 @@ __device__ __noinline__ void adj_jtv_0_12(double* __restrict__ ws, int yoff, int
       const double kw = ws[59040] * w;
       out[928] = fma(kw, y[6016], out[928]);
       out[6016] = fma(kw, y[928], out[6016]);
-      ws[281696] = fma(kw * y[928], y[6016], ws[281696]);
+      ws[287744] = fma(kw * y[928], y[6016], ws[287744]);
     }
     {
       double w = 1.0 * phi[960];
@@ -346,7 +346,7 @@ __device__ __noinline__ void adj_jtv_0_12(double* __restrict__ ws, int yoff, int
       w = w - phi[96];
       const double kw = ws[59072] * w;
       out[96] = out[96] + kw;
-      ws[281728] = fma(kw, y[96], ws[281728]);
+      ws[287776] = fma(kw, y[96], ws[287776]);
     }
     {
       double w = 1.0 * phi[960];
@@ -354,7 +354,7 @@ __device__ __noinline__ void adj_jtv_0_12(double* __restrict__ ws, int yoff, int
       w = w - phi[128];
       const double kw = ws[59104] * w;
       out[128] = out[128] + kw;
-      ws[281760] = fma(kw, y[128], ws[281760]);
+      ws[287808] = fma(kw, y[128], ws[287808]);
     }
     {
       double w = 1.0 * phi[3488];
@@ -363,7 +363,7 @@ __device__ __noinline__ void adj_jtv_0_12(double* __restrict__ ws, int yoff, int
       const double kw = ws[59136] * w;
       out[992] = fma(kw, y[6016], out[992]);
       out[6016] = fma(kw, y[992], out[6016]);
-      ws[281792] = fma(kw * y[992], y[6016], ws[281792]);
+      ws[287840] = fma(kw * y[992], y[6016], ws[287840]);
     }
     {
       double w = 1.0 * phi[5536];
@@ -372,7 +372,7 @@ __device__ __noinline__ void adj_jtv_0_12(double* __restrict__ ws, int yoff, int
       const double kw = ws[59168] * w;
       out[3488] = fma(kw, y[5984], out[3488]);
       out[5984] = fma(kw, y[3488], out[5984]);
-      ws[281824] = fma(kw * y[3488], y[5984], ws[281824]);
+      ws[287872] = fma(kw * y[3488], y[5984], ws[287872]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -384,7 +384,7 @@ __device__ __noinline__ void adj_jtv_0_12(double* __restrict__ ws, int yoff, int
       const double kw = ws[59200] * w;
       out[3488] = fma(kw, y[5824], out[3488]);
       out[5824] = fma(kw, y[3488], out[5824]);
-      ws[281856] = fma(kw * y[3488], y[5824], ws[281856]);
+      ws[287904] = fma(kw * y[3488], y[5824], ws[287904]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -396,7 +396,7 @@ __device__ __noinline__ void adj_jtv_0_12(double* __restrict__ ws, int yoff, int
       const double kw = ws[59232] * w;
       out[3488] = fma(kw, y[5952], out[3488]);
       out[5952] = fma(kw, y[3488], out[5952]);
-      ws[281888] = fma(kw * y[3488], y[5952], ws[281888]);
+      ws[287936] = fma(kw * y[3488], y[5952], ws[287936]);
     }
     {
       double w = 1.37 * phi[5984];
@@ -408,7 +408,7 @@ __device__ __noinline__ void adj_jtv_0_12(double* __restrict__ ws, int yoff, int
       const double kw = ws[59264] * w;
       out[3488] = fma(kw, y[5888], out[3488]);
       out[5888] = fma(kw, y[3488], out[5888]);
-      ws[281920] = fma(kw * y[3488], y[5888], ws[281920]);
+      ws[287968] = fma(kw * y[3488], y[5888], ws[287968]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -421,7 +421,7 @@ __device__ __noinline__ void adj_jtv_0_12(double* __restrict__ ws, int yoff, int
       const double kw = ws[59296] * w;
       out[3488] = fma(kw, y[5792], out[3488]);
       out[5792] = fma(kw, y[3488], out[5792]);
-      ws[281952] = fma(kw * y[3488], y[5792], ws[281952]);
+      ws[288000] = fma(kw * y[3488], y[5792], ws[288000]);
     }
 }
 }  // namespace mech_cracmm2

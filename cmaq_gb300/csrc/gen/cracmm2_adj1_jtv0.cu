@@ -15,7 +15,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43616] * w;
       out[5184] = fma(kw, y[6016], out[5184]);
       out[6016] = fma(kw, y[5184], out[6016]);
-      ws[266272] = fma(kw * y[5184], y[6016], ws[266272]);
+      ws[272320] = fma(kw * y[5184], y[6016], ws[272320]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -24,7 +24,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43648] * w;
       out[5184] = fma(kw, y[5984], out[5184]);
       out[5984] = fma(kw, y[5184], out[5984]);
-      ws[266304] = fma(kw * y[5184], y[5984], ws[266304]);
+      ws[272352] = fma(kw * y[5184], y[5984], ws[272352]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -33,7 +33,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43680] * w;
       out[5184] = fma(kw, y[5824], out[5184]);
       out[5824] = fma(kw, y[5184], out[5824]);
-      ws[266336] = fma(kw * y[5184], y[5824], ws[266336]);
+      ws[272384] = fma(kw * y[5184], y[5824], ws[272384]);
     }
     {
       double w = 1.0 * phi[5952];
@@ -42,14 +42,14 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43712] * w;
       out[5184] = fma(kw, y[5920], out[5184]);
       out[5920] = fma(kw, y[5184], out[5920]);
-      ws[266368] = fma(kw * y[5184], y[5920], ws[266368]);
+      ws[272416] = fma(kw * y[5184], y[5920], ws[272416]);
     }
     {
       double w = 1.0 * phi[5184];
       w = w - phi[2336];
       const double kw = ws[43744] * w;
       out[2336] = out[2336] + kw;
-      ws[266400] = fma(kw, y[2336], ws[266400]);
+      ws[272448] = fma(kw, y[2336], ws[272448]);
     }
     {
       double w = -phi[2336];
@@ -57,35 +57,35 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43776] * w;
       out[2336] = fma(kw, y[5184], out[2336]);
       out[5184] = fma(kw, y[2336], out[5184]);
-      ws[266432] = fma(kw * y[2336], y[5184], ws[266432]);
+      ws[272480] = fma(kw * y[2336], y[5184], ws[272480]);
     }
     {
       double w = 1.0 * phi[2336];
       w = w - phi[576];
       const double kw = ws[43808] * w;
       out[576] = out[576] + kw;
-      ws[266464] = fma(kw, y[576], ws[266464]);
+      ws[272512] = fma(kw, y[576], ws[272512]);
     }
     {
       double w = 1.0 * phi[2336];
       w = w - phi[576];
       const double kw = ws[43840] * w;
       out[576] = out[576] + kw;
-      ws[266496] = fma(kw, y[576], ws[266496]);
+      ws[272544] = fma(kw, y[576], ws[272544]);
     }
     {
       double w = 2.0 * phi[6016];
       w = w - phi[576];
       const double kw = ws[43872] * w;
       out[576] = out[576] + kw;
-      ws[266528] = fma(kw, y[576], ws[266528]);
+      ws[272576] = fma(kw, y[576], ws[272576]);
     }
     {
       double w = 1.0 * phi[5984];
       w = w - phi[6016];
       const double kw = ws[43904] * w;
       out[6016] = out[6016] + kw;
-      ws[266560] = fma(kw, y[6016], ws[266560]);
+      ws[272608] = fma(kw, y[6016], ws[272608]);
     }
     {
       double w = -phi[6016];
@@ -93,7 +93,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43936] * w;
       out[6016] = fma(kw, y[5984], out[6016]);
       out[5984] = fma(kw, y[6016], out[5984]);
-      ws[266592] = fma(kw * y[6016], y[5984], ws[266592]);
+      ws[272640] = fma(kw * y[6016], y[5984], ws[272640]);
     }
     {
       double w = 1.0 * phi[4000];
@@ -102,7 +102,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[43968] * w;
       out[5984] = fma(kw, y[5984], out[5984]);
       out[5984] = fma(kw, y[5984], out[5984]);
-      ws[266624] = fma(kw * y[5984], y[5984], ws[266624]);
+      ws[272672] = fma(kw * y[5984], y[5984], ws[272672]);
     }
     {
       double w = 1.0 * phi[4000];
@@ -111,7 +111,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44000] * w;
       out[5984] = fma(kw, y[5984], out[5984]);
       out[5984] = fma(kw, y[5984], out[5984]);
-      ws[266656] = fma(kw * y[5984], y[5984], ws[266656]);
+      ws[272704] = fma(kw * y[5984], y[5984], ws[272704]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -120,7 +120,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44032] * w;
       out[4000] = fma(kw, y[6016], out[4000]);
       out[6016] = fma(kw, y[4000], out[6016]);
-      ws[266688] = fma(kw * y[4000], y[6016], ws[266688]);
+      ws[272736] = fma(kw * y[4000], y[6016], ws[272736]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -129,7 +129,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44064] * w;
       out[5824] = fma(kw, y[2336], out[5824]);
       out[2336] = fma(kw, y[5824], out[2336]);
-      ws[266720] = fma(kw * y[5824], y[2336], ws[266720]);
+      ws[272768] = fma(kw * y[5824], y[2336], ws[272768]);
     }
     {
       double w = 1.0 * phi[1184];
@@ -138,7 +138,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44096] * w;
       out[5824] = fma(kw, y[6016], out[5824]);
       out[6016] = fma(kw, y[5824], out[6016]);
-      ws[266752] = fma(kw * y[5824], y[6016], ws[266752]);
+      ws[272800] = fma(kw * y[5824], y[6016], ws[272800]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -148,7 +148,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44128] * w;
       out[5824] = fma(kw, y[5984], out[5824]);
       out[5984] = fma(kw, y[5824], out[5984]);
-      ws[266784] = fma(kw * y[5824], y[5984], ws[266784]);
+      ws[272832] = fma(kw * y[5824], y[5984], ws[272832]);
     }
     {
       double w = 1.0 * phi[5024];
@@ -157,7 +157,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44160] * w;
       out[5824] = fma(kw, y[5984], out[5824]);
       out[5984] = fma(kw, y[5824], out[5984]);
-      ws[266816] = fma(kw * y[5824], y[5984], ws[266816]);
+      ws[272864] = fma(kw * y[5824], y[5984], ws[272864]);
     }
     {
       double w = 2.0 * phi[5920];
@@ -166,7 +166,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44192] * w;
       out[5824] = fma(kw, y[5824], out[5824]);
       out[5824] = fma(kw, y[5824], out[5824]);
-      ws[266848] = fma(kw * y[5824], y[5824], ws[266848]);
+      ws[272896] = fma(kw * y[5824], y[5824], ws[272896]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -175,7 +175,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44224] * w;
       out[1184] = fma(kw, y[6016], out[1184]);
       out[6016] = fma(kw, y[1184], out[6016]);
-      ws[266880] = fma(kw * y[1184], y[6016], ws[266880]);
+      ws[272928] = fma(kw * y[1184], y[6016], ws[272928]);
     }
     {
       double w = 1.0 * phi[5824];
@@ -184,7 +184,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44256] * w;
       out[5920] = fma(kw, y[2336], out[5920]);
       out[2336] = fma(kw, y[5920], out[2336]);
-      ws[266912] = fma(kw * y[5920], y[2336], ws[266912]);
+      ws[272960] = fma(kw * y[5920], y[2336], ws[272960]);
     }
     {
       double w = 1.0 * phi[5952];
@@ -193,7 +193,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44288] * w;
       out[5920] = fma(kw, y[2336], out[5920]);
       out[2336] = fma(kw, y[5920], out[2336]);
-      ws[266944] = fma(kw * y[5920], y[2336], ws[266944]);
+      ws[272992] = fma(kw * y[5920], y[2336], ws[272992]);
     }
     {
       double w = 1.0 * phi[5024];
@@ -202,7 +202,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44320] * w;
       out[5920] = fma(kw, y[6016], out[5920]);
       out[6016] = fma(kw, y[5920], out[6016]);
-      ws[266976] = fma(kw * y[5920], y[6016], ws[266976]);
+      ws[273024] = fma(kw * y[5920], y[6016], ws[273024]);
     }
     {
       double w = 1.0 * phi[5952];
@@ -211,7 +211,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44352] * w;
       out[5024] = fma(kw, y[6016], out[5024]);
       out[6016] = fma(kw, y[5024], out[6016]);
-      ws[267008] = fma(kw * y[5024], y[6016], ws[267008]);
+      ws[273056] = fma(kw * y[5024], y[6016], ws[273056]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -221,7 +221,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44384] * w;
       out[5952] = fma(kw, y[6016], out[5952]);
       out[6016] = fma(kw, y[5952], out[6016]);
-      ws[267040] = fma(kw * y[5952], y[6016], ws[267040]);
+      ws[273088] = fma(kw * y[5952], y[6016], ws[273088]);
     }
     {
       double w = 0.7 * phi[6016];
@@ -232,7 +232,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44416] * w;
       out[5952] = fma(kw, y[5984], out[5952]);
       out[5984] = fma(kw, y[5952], out[5984]);
-      ws[267072] = fma(kw * y[5952], y[5984], ws[267072]);
+      ws[273120] = fma(kw * y[5952], y[5984], ws[273120]);
     }
     {
       double w = 2.0 * phi[5920];
@@ -241,7 +241,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44448] * w;
       out[5952] = fma(kw, y[5824], out[5952]);
       out[5824] = fma(kw, y[5952], out[5824]);
-      ws[267104] = fma(kw * y[5952], y[5824], ws[267104]);
+      ws[273152] = fma(kw * y[5952], y[5824], ws[273152]);
     }
     {
       double w = 1.0 * phi[5824];
@@ -251,7 +251,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44480] * w;
       out[5952] = fma(kw, y[5920], out[5952]);
       out[5920] = fma(kw, y[5952], out[5920]);
-      ws[267136] = fma(kw * y[5952], y[5920], ws[267136]);
+      ws[273184] = fma(kw * y[5952], y[5920], ws[273184]);
     }
     {
       double w = 2.0 * phi[5920];
@@ -260,7 +260,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44512] * w;
       out[5952] = fma(kw, y[5952], out[5952]);
       out[5952] = fma(kw, y[5952], out[5952]);
-      ws[267168] = fma(kw * y[5952], y[5952], ws[267168]);
+      ws[273216] = fma(kw * y[5952], y[5952], ws[273216]);
     }
     {
       double w = 1.0 * phi[1024];
@@ -269,7 +269,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44544] * w;
       out[5952] = fma(kw, y[5920], out[5952]);
       out[5920] = fma(kw, y[5952], out[5920]);
-      ws[267200] = fma(kw * y[5952], y[5920], ws[267200]);
+      ws[273248] = fma(kw * y[5952], y[5920], ws[273248]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -277,14 +277,14 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[1024];
       const double kw = ws[44576] * w;
       out[1024] = out[1024] + kw;
-      ws[267232] = fma(kw, y[1024], ws[267232]);
+      ws[273280] = fma(kw, y[1024], ws[273280]);
     }
     {
       double w = 2.0 * phi[5024];
       w = w - phi[1024];
       const double kw = ws[44608] * w;
       out[1024] = out[1024] + kw;
-      ws[267264] = fma(kw, y[1024], ws[267264]);
+      ws[273312] = fma(kw, y[1024], ws[273312]);
     }
     {
       double w = 1.0 * phi[1280];
@@ -293,7 +293,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44640] * w;
       out[5920] = fma(kw, y[5984], out[5920]);
       out[5984] = fma(kw, y[5920], out[5984]);
-      ws[267296] = fma(kw * y[5920], y[5984], ws[267296]);
+      ws[273344] = fma(kw * y[5920], y[5984], ws[273344]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -301,7 +301,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       w = w - phi[1280];
       const double kw = ws[44672] * w;
       out[1280] = out[1280] + kw;
-      ws[267328] = fma(kw, y[1280], ws[267328]);
+      ws[273376] = fma(kw, y[1280], ws[273376]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -310,7 +310,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44704] * w;
       out[1280] = fma(kw, y[6016], out[1280]);
       out[6016] = fma(kw, y[1280], out[6016]);
-      ws[267360] = fma(kw * y[1280], y[6016], ws[267360]);
+      ws[273408] = fma(kw * y[1280], y[6016], ws[273408]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -321,7 +321,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44736] * w;
       out[160] = fma(kw, y[6016], out[160]);
       out[6016] = fma(kw, y[160], out[6016]);
-      ws[267392] = fma(kw * y[160], y[6016], ws[267392]);
+      ws[273440] = fma(kw * y[160], y[6016], ws[273440]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -330,14 +330,14 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44768] * w;
       out[5664] = fma(kw, y[6016], out[5664]);
       out[6016] = fma(kw, y[5664], out[6016]);
-      ws[267424] = fma(kw * y[5664], y[6016], ws[267424]);
+      ws[273472] = fma(kw * y[5664], y[6016], ws[273472]);
     }
     {
       double w = 1.0 * phi[5888];
       w = w - phi[6016];
       const double kw = ws[44800] * w;
       out[6016] = out[6016] + kw;
-      ws[267456] = fma(kw, y[6016], ws[267456]);
+      ws[273504] = fma(kw, y[6016], ws[273504]);
     }
     {
       double w = 1.0 * phi[5632];
@@ -346,7 +346,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44832] * w;
       out[1888] = fma(kw, y[6016], out[1888]);
       out[6016] = fma(kw, y[1888], out[6016]);
-      ws[267488] = fma(kw * y[1888], y[6016], ws[267488]);
+      ws[273536] = fma(kw * y[1888], y[6016], ws[273536]);
     }
     {
       double w = 1.0 * phi[5408];
@@ -356,7 +356,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44864] * w;
       out[2176] = fma(kw, y[6016], out[2176]);
       out[6016] = fma(kw, y[2176], out[6016]);
-      ws[267520] = fma(kw * y[2176], y[6016], ws[267520]);
+      ws[273568] = fma(kw * y[2176], y[6016], ws[273568]);
     }
     {
       double w = 1.0 * phi[5120];
@@ -366,7 +366,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44896] * w;
       out[1120] = fma(kw, y[6016], out[1120]);
       out[6016] = fma(kw, y[1120], out[6016]);
-      ws[267552] = fma(kw * y[1120], y[6016], ws[267552]);
+      ws[273600] = fma(kw * y[1120], y[6016], ws[273600]);
     }
     {
       double w = 1.0 * phi[3008];
@@ -375,7 +375,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44928] * w;
       out[2240] = fma(kw, y[6016], out[2240]);
       out[6016] = fma(kw, y[2240], out[6016]);
-      ws[267584] = fma(kw * y[2240], y[6016], ws[267584]);
+      ws[273632] = fma(kw * y[2240], y[6016], ws[273632]);
     }
     {
       double w = 1.0 * phi[3200];
@@ -384,7 +384,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44960] * w;
       out[2752] = fma(kw, y[6016], out[2752]);
       out[6016] = fma(kw, y[2752], out[6016]);
-      ws[267616] = fma(kw * y[2752], y[6016], ws[267616]);
+      ws[273664] = fma(kw * y[2752], y[6016], ws[273664]);
     }
     {
       double w = 1.0 * phi[3328];
@@ -393,7 +393,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[44992] * w;
       out[1152] = fma(kw, y[6016], out[1152]);
       out[6016] = fma(kw, y[1152], out[6016]);
-      ws[267648] = fma(kw * y[1152], y[6016], ws[267648]);
+      ws[273696] = fma(kw * y[1152], y[6016], ws[273696]);
     }
     {
       double w = 0.65 * phi[6016];
@@ -406,7 +406,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45024] * w;
       out[256] = fma(kw, y[6016], out[256]);
       out[6016] = fma(kw, y[256], out[6016]);
-      ws[267680] = fma(kw * y[256], y[6016], ws[267680]);
+      ws[273728] = fma(kw * y[256], y[6016], ws[273728]);
     }
     {
       double w = 0.47 * phi[3360];
@@ -417,7 +417,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45056] * w;
       out[1216] = fma(kw, y[6016], out[1216]);
       out[6016] = fma(kw, y[1216], out[6016]);
-      ws[267712] = fma(kw * y[1216], y[6016], ws[267712]);
+      ws[273760] = fma(kw * y[1216], y[6016], ws[273760]);
     }
     {
       double w = 0.82 * phi[3296];
@@ -428,7 +428,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45088] * w;
       out[288] = fma(kw, y[6016], out[288]);
       out[6016] = fma(kw, y[288], out[6016]);
-      ws[267744] = fma(kw * y[288], y[6016], ws[267744]);
+      ws[273792] = fma(kw * y[288], y[6016], ws[273792]);
     }
     {
       double w = 0.83 * phi[3104];
@@ -439,7 +439,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45120] * w;
       out[320] = fma(kw, y[6016], out[320]);
       out[6016] = fma(kw, y[320], out[6016]);
-      ws[267776] = fma(kw * y[320], y[6016], ws[267776]);
+      ws[273824] = fma(kw * y[320], y[6016], ws[273824]);
     }
     {
       double w = 0.82 * phi[3264];
@@ -450,7 +450,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45152] * w;
       out[352] = fma(kw, y[6016], out[352]);
       out[6016] = fma(kw, y[352], out[6016]);
-      ws[267808] = fma(kw * y[352], y[6016], ws[267808]);
+      ws[273856] = fma(kw * y[352], y[6016], ws[273856]);
     }
     {
       double w = 0.25 * phi[6016];
@@ -470,7 +470,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45184] * w;
       out[1312] = fma(kw, y[5184], out[1312]);
       out[5184] = fma(kw, y[1312], out[5184]);
-      ws[267840] = fma(kw * y[1312], y[5184], ws[267840]);
+      ws[273888] = fma(kw * y[1312], y[5184], ws[273888]);
     }
     {
       double w = 0.4 * phi[5920];
@@ -484,7 +484,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45216] * w;
       out[1312] = fma(kw, y[5952], out[1312]);
       out[5952] = fma(kw, y[1312], out[5952]);
-      ws[267872] = fma(kw * y[1312], y[5952], ws[267872]);
+      ws[273920] = fma(kw * y[1312], y[5952], ws[273920]);
     }
     {
       double w = 1.0 * phi[4288];
@@ -496,7 +496,7 @@ __device__ __noinline__ void adj_jtv_1_0(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45248] * w;
       out[1312] = fma(kw, y[6016], out[1312]);
       out[6016] = fma(kw, y[1312], out[6016]);
-      ws[267904] = fma(kw * y[1312], y[6016], ws[267904]);
+      ws[273952] = fma(kw * y[1312], y[6016], ws[273952]);
     }
 }
 __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int phioff, int outoff)
@@ -513,7 +513,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45280] * w;
       out[4288] = fma(kw, y[5984], out[4288]);
       out[5984] = fma(kw, y[4288], out[5984]);
-      ws[267936] = fma(kw * y[4288], y[5984], ws[267936]);
+      ws[273984] = fma(kw * y[4288], y[5984], ws[273984]);
     }
     {
       double w = 0.13 * phi[2784];
@@ -527,7 +527,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45312] * w;
       out[4288] = fma(kw, y[5824], out[4288]);
       out[5824] = fma(kw, y[4288], out[5824]);
-      ws[267968] = fma(kw * y[4288], y[5824], ws[267968]);
+      ws[274016] = fma(kw * y[4288], y[5824], ws[274016]);
     }
     {
       double w = 1.0 * phi[4288];
@@ -536,7 +536,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45344] * w;
       out[1344] = fma(kw, y[6016], out[1344]);
       out[6016] = fma(kw, y[1344], out[6016]);
-      ws[268000] = fma(kw * y[1344], y[6016], ws[268000]);
+      ws[274048] = fma(kw * y[1344], y[6016], ws[274048]);
     }
     {
       double w = 0.04 * phi[5248];
@@ -554,7 +554,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45376] * w;
       out[1344] = fma(kw, y[6016], out[1344]);
       out[6016] = fma(kw, y[1344], out[6016]);
-      ws[268032] = fma(kw * y[1344], y[6016], ws[268032]);
+      ws[274080] = fma(kw * y[1344], y[6016], ws[274080]);
     }
     {
       double w = 0.45 * phi[6016];
@@ -565,7 +565,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45408] * w;
       out[1632] = fma(kw, y[5984], out[1632]);
       out[5984] = fma(kw, y[1632], out[5984]);
-      ws[268064] = fma(kw * y[1632], y[5984], ws[268064]);
+      ws[274112] = fma(kw * y[1632], y[5984], ws[274112]);
     }
     {
       double w = 0.15 * phi[4736];
@@ -578,7 +578,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45440] * w;
       out[1632] = fma(kw, y[5824], out[1632]);
       out[5824] = fma(kw, y[1632], out[5824]);
-      ws[268096] = fma(kw * y[1632], y[5824], ws[268096]);
+      ws[274144] = fma(kw * y[1632], y[5824], ws[274144]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -590,7 +590,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45472] * w;
       out[2784] = fma(kw, y[6016], out[2784]);
       out[6016] = fma(kw, y[2784], out[6016]);
-      ws[268128] = fma(kw * y[2784], y[6016], ws[268128]);
+      ws[274176] = fma(kw * y[2784], y[6016], ws[274176]);
     }
     {
       double w = 1.0 * phi[5664];
@@ -602,7 +602,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45504] * w;
       out[6016] = fma(kw, y[2208], out[6016]);
       out[2208] = fma(kw, y[6016], out[2208]);
-      ws[268160] = fma(kw * y[6016], y[2208], ws[268160]);
+      ws[274208] = fma(kw * y[6016], y[2208], ws[274208]);
     }
     {
       double w = 1.0 * phi[5024];
@@ -610,7 +610,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       w = w - phi[2784];
       const double kw = ws[45536] * w;
       out[2784] = out[2784] + kw;
-      ws[268192] = fma(kw, y[2784], ws[268192]);
+      ws[274240] = fma(kw, y[2784], ws[274240]);
     }
     {
       double w = 0.57 * phi[4128];
@@ -620,7 +620,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45568] * w;
       out[1664] = fma(kw, y[6016], out[1664]);
       out[6016] = fma(kw, y[1664], out[6016]);
-      ws[268224] = fma(kw * y[1664], y[6016], ws[268224]);
+      ws[274272] = fma(kw * y[1664], y[6016], ws[274272]);
     }
     {
       double w = 0.975 * phi[4160];
@@ -630,7 +630,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45600] * w;
       out[1408] = fma(kw, y[6016], out[1408]);
       out[6016] = fma(kw, y[1408], out[6016]);
-      ws[268256] = fma(kw * y[1408], y[6016], ws[268256]);
+      ws[274304] = fma(kw * y[1408], y[6016], ws[274304]);
     }
     {
       double w = 0.945 * phi[4192];
@@ -640,7 +640,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45632] * w;
       out[1440] = fma(kw, y[6016], out[1440]);
       out[6016] = fma(kw, y[1440], out[6016]);
-      ws[268288] = fma(kw * y[1440], y[6016], ws[268288]);
+      ws[274336] = fma(kw * y[1440], y[6016], ws[274336]);
     }
     {
       double w = 0.23 * phi[2560];
@@ -650,7 +650,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45664] * w;
       out[4544] = fma(kw, y[6016], out[4544]);
       out[6016] = fma(kw, y[4544], out[6016]);
-      ws[268320] = fma(kw * y[4544], y[6016], ws[268320]);
+      ws[274368] = fma(kw * y[4544], y[6016], ws[274368]);
     }
     {
       double w = 0.83 * phi[1728];
@@ -660,7 +660,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45696] * w;
       out[4576] = fma(kw, y[6016], out[4576]);
       out[6016] = fma(kw, y[4576], out[6016]);
-      ws[268352] = fma(kw * y[4576], y[6016], ws[268352]);
+      ws[274400] = fma(kw * y[4576], y[6016], ws[274400]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -670,7 +670,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45728] * w;
       out[5856] = fma(kw, y[6016], out[5856]);
       out[6016] = fma(kw, y[5856], out[6016]);
-      ws[268384] = fma(kw * y[5856], y[6016], ws[268384]);
+      ws[274432] = fma(kw * y[5856], y[6016], ws[274432]);
     }
     {
       double w = 1.0 * phi[5792];
@@ -679,7 +679,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45760] * w;
       out[5568] = fma(kw, y[6016], out[5568]);
       out[6016] = fma(kw, y[5568], out[6016]);
-      ws[268416] = fma(kw * y[5568], y[6016], ws[268416]);
+      ws[274464] = fma(kw * y[5568], y[6016], ws[274464]);
     }
     {
       double w = 1.0 * phi[4800];
@@ -688,7 +688,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45792] * w;
       out[5760] = fma(kw, y[6016], out[5760]);
       out[6016] = fma(kw, y[5760], out[6016]);
-      ws[268448] = fma(kw * y[5760], y[6016], ws[268448]);
+      ws[274496] = fma(kw * y[5760], y[6016], ws[274496]);
     }
     {
       double w = 1.0 * phi[2848];
@@ -697,7 +697,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45824] * w;
       out[4480] = fma(kw, y[6016], out[4480]);
       out[6016] = fma(kw, y[4480], out[6016]);
-      ws[268480] = fma(kw * y[4480], y[6016], ws[268480]);
+      ws[274528] = fma(kw * y[4480], y[6016], ws[274528]);
     }
     {
       double w = 1.0 * phi[5152];
@@ -706,7 +706,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45856] * w;
       out[5280] = fma(kw, y[6016], out[5280]);
       out[6016] = fma(kw, y[5280], out[6016]);
-      ws[268512] = fma(kw * y[5280], y[6016], ws[268512]);
+      ws[274560] = fma(kw * y[5280], y[6016], ws[274560]);
     }
     {
       double w = 1.0 * phi[3776];
@@ -715,7 +715,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45888] * w;
       out[5504] = fma(kw, y[6016], out[5504]);
       out[6016] = fma(kw, y[5504], out[6016]);
-      ws[268544] = fma(kw * y[5504], y[6016], ws[268544]);
+      ws[274592] = fma(kw * y[5504], y[6016], ws[274592]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -725,7 +725,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45920] * w;
       out[5344] = fma(kw, y[6016], out[5344]);
       out[6016] = fma(kw, y[5344], out[6016]);
-      ws[268576] = fma(kw * y[5344], y[6016], ws[268576]);
+      ws[274624] = fma(kw * y[5344], y[6016], ws[274624]);
     }
     {
       double w = 0.57 * phi[4672];
@@ -735,7 +735,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45952] * w;
       out[4128] = fma(kw, y[6016], out[4128]);
       out[6016] = fma(kw, y[4128], out[6016]);
-      ws[268608] = fma(kw * y[4128], y[6016], ws[268608]);
+      ws[274656] = fma(kw * y[4128], y[6016], ws[274656]);
     }
     {
       double w = 1.0 * phi[2880];
@@ -744,7 +744,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[45984] * w;
       out[4736] = fma(kw, y[6016], out[4736]);
       out[6016] = fma(kw, y[4736], out[6016]);
-      ws[268640] = fma(kw * y[4736], y[6016], ws[268640]);
+      ws[274688] = fma(kw * y[4736], y[6016], ws[274688]);
     }
     {
       double w = 0.313 * phi[5792];
@@ -754,7 +754,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46016] * w;
       out[3872] = fma(kw, y[6016], out[3872]);
       out[6016] = fma(kw, y[3872], out[6016]);
-      ws[268672] = fma(kw * y[3872], y[6016], ws[268672]);
+      ws[274720] = fma(kw * y[3872], y[6016], ws[274720]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -764,7 +764,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46048] * w;
       out[5376] = fma(kw, y[6016], out[5376]);
       out[6016] = fma(kw, y[5376], out[6016]);
-      ws[268704] = fma(kw * y[5376], y[6016], ws[268704]);
+      ws[274752] = fma(kw * y[5376], y[6016], ws[274752]);
     }
     {
       double w = 1.0 * phi[5792];
@@ -774,7 +774,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46080] * w;
       out[5248] = fma(kw, y[6016], out[5248]);
       out[6016] = fma(kw, y[5248], out[6016]);
-      ws[268736] = fma(kw * y[5248], y[6016], ws[268736]);
+      ws[274784] = fma(kw * y[5248], y[6016], ws[274784]);
     }
     {
       double w = 0.52 * phi[5984];
@@ -788,7 +788,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46112] * w;
       out[5472] = fma(kw, y[6016], out[5472]);
       out[6016] = fma(kw, y[5472], out[6016]);
-      ws[268768] = fma(kw * y[5472], y[6016], ws[268768]);
+      ws[274816] = fma(kw * y[5472], y[6016], ws[274816]);
     }
     {
       double w = 0.52 * phi[5984];
@@ -802,7 +802,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46144] * w;
       out[4320] = fma(kw, y[6016], out[4320]);
       out[6016] = fma(kw, y[4320], out[6016]);
-      ws[268800] = fma(kw * y[4320], y[6016], ws[268800]);
+      ws[274848] = fma(kw * y[4320], y[6016], ws[274848]);
     }
     {
       double w = 0.56 * phi[5984];
@@ -816,7 +816,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46176] * w;
       out[3584] = fma(kw, y[6016], out[3584]);
       out[6016] = fma(kw, y[3584], out[6016]);
-      ws[268832] = fma(kw * y[3584], y[6016], ws[268832]);
+      ws[274880] = fma(kw * y[3584], y[6016], ws[274880]);
     }
     {
       double w = 1.0 * phi[2592];
@@ -825,7 +825,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46208] * w;
       out[4448] = fma(kw, y[6016], out[4448]);
       out[6016] = fma(kw, y[4448], out[6016]);
-      ws[268864] = fma(kw * y[4448], y[6016], ws[268864]);
+      ws[274912] = fma(kw * y[4448], y[6016], ws[274912]);
     }
     {
       double w = 0.152 * phi[3616];
@@ -838,7 +838,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46240] * w;
       out[1248] = fma(kw, y[6016], out[1248]);
       out[6016] = fma(kw, y[1248], out[6016]);
-      ws[268896] = fma(kw * y[1248], y[6016], ws[268896]);
+      ws[274944] = fma(kw * y[1248], y[6016], ws[274944]);
     }
     {
       double w = 0.2 * phi[3616];
@@ -851,7 +851,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46272] * w;
       out[2944] = fma(kw, y[6016], out[2944]);
       out[6016] = fma(kw, y[2944], out[6016]);
-      ws[268928] = fma(kw * y[2944], y[6016], ws[268928]);
+      ws[274976] = fma(kw * y[2944], y[6016], ws[274976]);
     }
     {
       double w = 1.0 * phi[3808];
@@ -860,7 +860,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46304] * w;
       out[1760] = fma(kw, y[6016], out[1760]);
       out[6016] = fma(kw, y[1760], out[6016]);
-      ws[268960] = fma(kw * y[1760], y[6016], ws[268960]);
+      ws[275008] = fma(kw * y[1760], y[6016], ws[275008]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -870,7 +870,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46336] * w;
       out[5600] = fma(kw, y[6016], out[5600]);
       out[6016] = fma(kw, y[5600], out[6016]);
-      ws[268992] = fma(kw * y[5600], y[6016], ws[268992]);
+      ws[275040] = fma(kw * y[5600], y[6016], ws[275040]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -880,7 +880,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46368] * w;
       out[1472] = fma(kw, y[6016], out[1472]);
       out[6016] = fma(kw, y[1472], out[6016]);
-      ws[269024] = fma(kw * y[1472], y[6016], ws[269024]);
+      ws[275072] = fma(kw * y[1472], y[6016], ws[275072]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -891,7 +891,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46400] * w;
       out[5056] = fma(kw, y[6016], out[5056]);
       out[6016] = fma(kw, y[5056], out[6016]);
-      ws[269056] = fma(kw * y[5056], y[6016], ws[269056]);
+      ws[275104] = fma(kw * y[5056], y[6016], ws[275104]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -901,7 +901,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46432] * w;
       out[1504] = fma(kw, y[6016], out[1504]);
       out[6016] = fma(kw, y[1504], out[6016]);
-      ws[269088] = fma(kw * y[1504], y[6016], ws[269088]);
+      ws[275136] = fma(kw * y[1504], y[6016], ws[275136]);
     }
     {
       double w = 0.35 * phi[6016];
@@ -912,7 +912,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46464] * w;
       out[2816] = fma(kw, y[6016], out[2816]);
       out[6016] = fma(kw, y[2816], out[6016]);
-      ws[269120] = fma(kw * y[2816], y[6016], ws[269120]);
+      ws[275168] = fma(kw * y[2816], y[6016], ws[275168]);
     }
     {
       double w = 0.01 * phi[6016];
@@ -925,7 +925,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46496] * w;
       out[5728] = fma(kw, y[6016], out[5728]);
       out[6016] = fma(kw, y[5728], out[6016]);
-      ws[269152] = fma(kw * y[5728], y[6016], ws[269152]);
+      ws[275200] = fma(kw * y[5728], y[6016], ws[275200]);
     }
     {
       double w = 0.01 * phi[6016];
@@ -938,7 +938,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46528] * w;
       out[4096] = fma(kw, y[6016], out[4096]);
       out[6016] = fma(kw, y[4096], out[6016]);
-      ws[269184] = fma(kw * y[4096], y[6016], ws[269184]);
+      ws[275232] = fma(kw * y[4096], y[6016], ws[275232]);
     }
     {
       double w = 0.01 * phi[6016];
@@ -951,7 +951,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46560] * w;
       out[4608] = fma(kw, y[6016], out[4608]);
       out[6016] = fma(kw, y[4608], out[6016]);
-      ws[269216] = fma(kw * y[4608], y[6016], ws[269216]);
+      ws[275264] = fma(kw * y[4608], y[6016], ws[275264]);
     }
     {
       double w = 1.0 * phi[4672];
@@ -960,7 +960,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46592] * w;
       out[1792] = fma(kw, y[6016], out[1792]);
       out[6016] = fma(kw, y[1792], out[6016]);
-      ws[269248] = fma(kw * y[1792], y[6016], ws[269248]);
+      ws[275296] = fma(kw * y[1792], y[6016], ws[275296]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -969,7 +969,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46624] * w;
       out[4352] = fma(kw, y[6016], out[4352]);
       out[6016] = fma(kw, y[4352], out[6016]);
-      ws[269280] = fma(kw * y[4352], y[6016], ws[269280]);
+      ws[275328] = fma(kw * y[4352], y[6016], ws[275328]);
     }
     {
       double w = 0.64 * phi[5888];
@@ -979,7 +979,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46656] * w;
       out[5696] = fma(kw, y[6016], out[5696]);
       out[6016] = fma(kw, y[5696], out[6016]);
-      ws[269312] = fma(kw * y[5696], y[6016], ws[269312]);
+      ws[275360] = fma(kw * y[5696], y[6016], ws[275360]);
     }
     {
       double w = 0.35 * phi[6016];
@@ -991,7 +991,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46688] * w;
       out[3680] = fma(kw, y[6016], out[3680]);
       out[6016] = fma(kw, y[3680], out[6016]);
-      ws[269344] = fma(kw * y[3680], y[6016], ws[269344]);
+      ws[275392] = fma(kw * y[3680], y[6016], ws[275392]);
     }
     {
       double w = 1.0 * phi[5216];
@@ -1002,7 +1002,7 @@ __device__ __noinline__ void adj_jtv_1_1(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46720] * w;
       out[1088] = fma(kw, y[6016], out[1088]);
       out[6016] = fma(kw, y[1088], out[6016]);
-      ws[269376] = fma(kw * y[1088], y[6016], ws[269376]);
+      ws[275424] = fma(kw * y[1088], y[6016], ws[275424]);
     }
 }
 __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int phioff, int outoff)
@@ -1019,7 +1019,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46752] * w;
       out[1536] = fma(kw, y[6016], out[1536]);
       out[6016] = fma(kw, y[1536], out[6016]);
-      ws[269408] = fma(kw * y[1536], y[6016], ws[269408]);
+      ws[275456] = fma(kw * y[1536], y[6016], ws[275456]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1029,7 +1029,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46784] * w;
       out[1824] = fma(kw, y[6016], out[1824]);
       out[6016] = fma(kw, y[1824], out[6016]);
-      ws[269440] = fma(kw * y[1824], y[6016], ws[269440]);
+      ws[275488] = fma(kw * y[1824], y[6016], ws[275488]);
     }
     {
       double w = 1.0 * phi[5408];
@@ -1039,7 +1039,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46816] * w;
       out[5440] = fma(kw, y[6016], out[5440]);
       out[6016] = fma(kw, y[5440], out[6016]);
-      ws[269472] = fma(kw * y[5440], y[6016], ws[269472]);
+      ws[275520] = fma(kw * y[5440], y[6016], ws[275520]);
     }
     {
       double w = 0.33 * phi[1696];
@@ -1053,7 +1053,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46848] * w;
       out[4384] = fma(kw, y[6016], out[4384]);
       out[6016] = fma(kw, y[4384], out[6016]);
-      ws[269504] = fma(kw * y[4384], y[6016], ws[269504]);
+      ws[275552] = fma(kw * y[4384], y[6016], ws[275552]);
     }
     {
       double w = 1.0 * phi[5344];
@@ -1063,7 +1063,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46880] * w;
       out[1696] = fma(kw, y[6016], out[1696]);
       out[6016] = fma(kw, y[1696], out[6016]);
-      ws[269536] = fma(kw * y[1696], y[6016], ws[269536]);
+      ws[275584] = fma(kw * y[1696], y[6016], ws[275584]);
     }
     {
       double w = 0.08 * phi[6016];
@@ -1076,7 +1076,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46912] * w;
       out[2240] = fma(kw, y[5184], out[2240]);
       out[5184] = fma(kw, y[2240], out[5184]);
-      ws[269568] = fma(kw * y[2240], y[5184], ws[269568]);
+      ws[275616] = fma(kw * y[2240], y[5184], ws[275616]);
     }
     {
       double w = 0.22 * phi[6016];
@@ -1105,7 +1105,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46944] * w;
       out[2752] = fma(kw, y[5184], out[2752]);
       out[5184] = fma(kw, y[2752], out[5184]);
-      ws[269600] = fma(kw * y[2752], y[5184], ws[269600]);
+      ws[275648] = fma(kw * y[2752], y[5184], ws[275648]);
     }
     {
       double w = 0.46 * phi[6016];
@@ -1130,7 +1130,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[46976] * w;
       out[1152] = fma(kw, y[5184], out[1152]);
       out[5184] = fma(kw, y[1152], out[5184]);
-      ws[269632] = fma(kw * y[1152], y[5184], ws[269632]);
+      ws[275680] = fma(kw * y[1152], y[5184], ws[275680]);
     }
     {
       double w = 0.6055 * phi[6016];
@@ -1151,7 +1151,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47008] * w;
       out[1408] = fma(kw, y[5184], out[1408]);
       out[5184] = fma(kw, y[1408], out[5184]);
-      ws[269664] = fma(kw * y[1408], y[5184], ws[269664]);
+      ws[275712] = fma(kw * y[1408], y[5184], ws[275712]);
     }
     {
       double w = 0.66 * phi[6016];
@@ -1166,7 +1166,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47040] * w;
       out[1440] = fma(kw, y[5184], out[1440]);
       out[5184] = fma(kw, y[1440], out[5184]);
-      ws[269696] = fma(kw * y[1440], y[5184], ws[269696]);
+      ws[275744] = fma(kw * y[1440], y[5184], ws[275744]);
     }
     {
       double w = 0.09 * phi[6016];
@@ -1180,7 +1180,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47072] * w;
       out[4576] = fma(kw, y[5184], out[4576]);
       out[5184] = fma(kw, y[4576], out[5184]);
-      ws[269728] = fma(kw * y[4576], y[5184], ws[269728]);
+      ws[275776] = fma(kw * y[4576], y[5184], ws[275776]);
     }
     {
       double w = 0.33 * phi[1696];
@@ -1194,7 +1194,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47104] * w;
       out[4384] = fma(kw, y[5184], out[4384]);
       out[5184] = fma(kw, y[4384], out[5184]);
-      ws[269760] = fma(kw * y[4384], y[5184], ws[269760]);
+      ws[275808] = fma(kw * y[4384], y[5184], ws[275808]);
     }
     {
       double w = 0.19 * phi[6016];
@@ -1208,7 +1208,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47136] * w;
       out[4128] = fma(kw, y[5184], out[4128]);
       out[5184] = fma(kw, y[4128], out[5184]);
-      ws[269792] = fma(kw * y[4128], y[5184], ws[269792]);
+      ws[275840] = fma(kw * y[4128], y[5184], ws[275840]);
     }
     {
       double w = 0.16 * phi[6016];
@@ -1226,7 +1226,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47168] * w;
       out[4736] = fma(kw, y[5184], out[4736]);
       out[5184] = fma(kw, y[4736], out[5184]);
-      ws[269824] = fma(kw * y[4736], y[5184], ws[269824]);
+      ws[275872] = fma(kw * y[4736], y[5184], ws[275872]);
     }
     {
       double w = 0.1 * phi[6016];
@@ -1246,7 +1246,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47200] * w;
       out[3872] = fma(kw, y[5184], out[3872]);
       out[5184] = fma(kw, y[3872], out[5184]);
-      ws[269856] = fma(kw * y[3872], y[5184], ws[269856]);
+      ws[275904] = fma(kw * y[3872], y[5184], ws[275904]);
     }
     {
       double w = 0.05 * phi[6016];
@@ -1263,7 +1263,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47232] * w;
       out[5472] = fma(kw, y[5184], out[5472]);
       out[5184] = fma(kw, y[5472], out[5184]);
-      ws[269888] = fma(kw * y[5472], y[5184], ws[269888]);
+      ws[275936] = fma(kw * y[5472], y[5184], ws[275936]);
     }
     {
       double w = 0.05 * phi[6016];
@@ -1281,7 +1281,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47264] * w;
       out[4320] = fma(kw, y[5184], out[4320]);
       out[5184] = fma(kw, y[4320], out[5184]);
-      ws[269920] = fma(kw * y[4320], y[5184], ws[269920]);
+      ws[275968] = fma(kw * y[4320], y[5184], ws[275968]);
     }
     {
       double w = 0.05 * phi[6016];
@@ -1297,7 +1297,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47296] * w;
       out[3584] = fma(kw, y[5184], out[3584]);
       out[5184] = fma(kw, y[3584], out[5184]);
-      ws[269952] = fma(kw * y[3584], y[5184], ws[269952]);
+      ws[276000] = fma(kw * y[3584], y[5184], ws[276000]);
     }
     {
       double w = 1.0 * phi[3040];
@@ -1306,7 +1306,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47328] * w;
       out[3808] = fma(kw, y[5184], out[3808]);
       out[5184] = fma(kw, y[3808], out[5184]);
-      ws[269984] = fma(kw * y[3808], y[5184], ws[269984]);
+      ws[276032] = fma(kw * y[3808], y[5184], ws[276032]);
     }
     {
       double w = 0.8 * phi[4032];
@@ -1316,7 +1316,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47360] * w;
       out[2240] = fma(kw, y[5952], out[2240]);
       out[5952] = fma(kw, y[2240], out[5952]);
-      ws[270016] = fma(kw * y[2240], y[5952], ws[270016]);
+      ws[276064] = fma(kw * y[2240], y[5952], ws[276064]);
     }
     {
       double w = 0.43 * phi[4032];
@@ -1326,7 +1326,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47392] * w;
       out[2752] = fma(kw, y[5952], out[2752]);
       out[5952] = fma(kw, y[2752], out[5952]);
-      ws[270048] = fma(kw * y[2752], y[5952], ws[270048]);
+      ws[276096] = fma(kw * y[2752], y[5952], ws[276096]);
     }
     {
       double w = 0.11 * phi[4032];
@@ -1336,7 +1336,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47424] * w;
       out[1152] = fma(kw, y[5952], out[1152]);
       out[5952] = fma(kw, y[1152], out[5952]);
-      ws[270080] = fma(kw * y[1152], y[5952], ws[270080]);
+      ws[276128] = fma(kw * y[1152], y[5952], ws[276128]);
     }
     {
       double w = 0.975 * phi[2624];
@@ -1346,7 +1346,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47456] * w;
       out[1408] = fma(kw, y[5952], out[1408]);
       out[5952] = fma(kw, y[1408], out[5952]);
-      ws[270112] = fma(kw * y[1408], y[5952], ws[270112]);
+      ws[276160] = fma(kw * y[1408], y[5952], ws[276160]);
     }
     {
       double w = 0.945 * phi[2656];
@@ -1356,7 +1356,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47488] * w;
       out[1440] = fma(kw, y[5952], out[1440]);
       out[5952] = fma(kw, y[1440], out[5952]);
-      ws[270144] = fma(kw * y[1440], y[5952], ws[270144]);
+      ws[276192] = fma(kw * y[1440], y[5952], ws[276192]);
     }
     {
       double w = 0.33 * phi[1696];
@@ -1370,7 +1370,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47520] * w;
       out[4384] = fma(kw, y[5952], out[4384]);
       out[5952] = fma(kw, y[4384], out[5952]);
-      ws[270176] = fma(kw * y[4384], y[5952], ws[270176]);
+      ws[276224] = fma(kw * y[4384], y[5952], ws[276224]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1381,7 +1381,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47552] * w;
       out[5856] = fma(kw, y[5952], out[5856]);
       out[5952] = fma(kw, y[5856], out[5952]);
-      ws[270208] = fma(kw * y[5856], y[5952], ws[270208]);
+      ws[276256] = fma(kw * y[5856], y[5952], ws[276256]);
     }
     {
       double w = 1.0 * phi[5792];
@@ -1391,7 +1391,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47584] * w;
       out[5568] = fma(kw, y[5952], out[5568]);
       out[5952] = fma(kw, y[5568], out[5952]);
-      ws[270240] = fma(kw * y[5568], y[5952], ws[270240]);
+      ws[276288] = fma(kw * y[5568], y[5952], ws[276288]);
     }
     {
       double w = 1.0 * phi[4800];
@@ -1401,7 +1401,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47616] * w;
       out[5760] = fma(kw, y[5952], out[5760]);
       out[5952] = fma(kw, y[5760], out[5952]);
-      ws[270272] = fma(kw * y[5760], y[5952], ws[270272]);
+      ws[276320] = fma(kw * y[5760], y[5952], ws[276320]);
     }
     {
       double w = 0.68 * phi[5856];
@@ -1415,7 +1415,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47648] * w;
       out[4128] = fma(kw, y[5952], out[4128]);
       out[5952] = fma(kw, y[4128], out[5952]);
-      ws[270304] = fma(kw * y[4128], y[5952], ws[270304]);
+      ws[276352] = fma(kw * y[4128], y[5952], ws[276352]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1429,7 +1429,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47680] * w;
       out[3872] = fma(kw, y[5952], out[3872]);
       out[5952] = fma(kw, y[3872], out[5952]);
-      ws[270336] = fma(kw * y[3872], y[5952], ws[270336]);
+      ws[276384] = fma(kw * y[3872], y[5952], ws[276384]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1440,7 +1440,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47712] * w;
       out[5376] = fma(kw, y[5952], out[5376]);
       out[5952] = fma(kw, y[5376], out[5952]);
-      ws[270368] = fma(kw * y[5376], y[5952], ws[270368]);
+      ws[276416] = fma(kw * y[5376], y[5952], ws[276416]);
     }
     {
       double w = 1.0 * phi[5792];
@@ -1451,7 +1451,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47744] * w;
       out[5248] = fma(kw, y[5952], out[5248]);
       out[5952] = fma(kw, y[5248], out[5952]);
-      ws[270400] = fma(kw * y[5248], y[5952], ws[270400]);
+      ws[276448] = fma(kw * y[5248], y[5952], ws[276448]);
     }
     {
       double w = 0.152 * phi[3616];
@@ -1464,7 +1464,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47776] * w;
       out[1248] = fma(kw, y[5952], out[1248]);
       out[5952] = fma(kw, y[1248], out[5952]);
-      ws[270432] = fma(kw * y[1248], y[5952], ws[270432]);
+      ws[276480] = fma(kw * y[1248], y[5952], ws[276480]);
     }
     {
       double w = 0.2 * phi[3616];
@@ -1477,7 +1477,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47808] * w;
       out[2944] = fma(kw, y[5952], out[2944]);
       out[5952] = fma(kw, y[2944], out[5952]);
-      ws[270464] = fma(kw * y[2944], y[5952], ws[270464]);
+      ws[276512] = fma(kw * y[2944], y[5952], ws[276512]);
     }
     {
       double w = 1.0 * phi[3808];
@@ -1487,7 +1487,7 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47840] * w;
       out[1760] = fma(kw, y[5952], out[1760]);
       out[5952] = fma(kw, y[1760], out[5952]);
-      ws[270496] = fma(kw * y[1760], y[5952], ws[270496]);
+      ws[276544] = fma(kw * y[1760], y[5952], ws[276544]);
     }
     {
       double w = 1.0 * phi[4672];
@@ -1497,14 +1497,14 @@ __device__ __noinline__ void adj_jtv_1_2(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47872] * w;
       out[1824] = fma(kw, y[5952], out[1824]);
       out[5952] = fma(kw, y[1824], out[5952]);
-      ws[270528] = fma(kw * y[1824], y[5952], ws[270528]);
+      ws[276576] = fma(kw * y[1824], y[5952], ws[276576]);
     }
     {
       double w = 1.0 * phi[4256];
       w = w - phi[2560];
       const double kw = ws[47904] * w;
       out[2560] = out[2560] + kw;
-      ws[270560] = fma(kw, y[2560], ws[270560]);
+      ws[276608] = fma(kw, y[2560], ws[276608]);
     }
 }
 __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int phioff, int outoff)
@@ -1517,7 +1517,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       w = w - phi[1728];
       const double kw = ws[47936] * w;
       out[1728] = out[1728] + kw;
-      ws[270592] = fma(kw, y[1728], ws[270592]);
+      ws[276640] = fma(kw, y[1728], ws[276640]);
     }
     {
       double w = 1.0 * phi[1088];
@@ -1526,7 +1526,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[47968] * w;
       out[5792] = fma(kw, y[5920], out[5792]);
       out[5920] = fma(kw, y[5792], out[5920]);
-      ws[270624] = fma(kw * y[5792], y[5920], ws[270624]);
+      ws[276672] = fma(kw * y[5792], y[5920], ws[276672]);
     }
     {
       double w = 1.0 * phi[5792];
@@ -1534,7 +1534,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       w = w - phi[1088];
       const double kw = ws[48000] * w;
       out[1088] = out[1088] + kw;
-      ws[270656] = fma(kw, y[1088], ws[270656]);
+      ws[276704] = fma(kw, y[1088], ws[276704]);
     }
     {
       double w = 1.0 * phi[1536];
@@ -1543,7 +1543,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48032] * w;
       out[4800] = fma(kw, y[5920], out[4800]);
       out[5920] = fma(kw, y[4800], out[5920]);
-      ws[270688] = fma(kw * y[4800], y[5920], ws[270688]);
+      ws[276736] = fma(kw * y[4800], y[5920], ws[276736]);
     }
     {
       double w = 1.0 * phi[4800];
@@ -1551,7 +1551,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       w = w - phi[1536];
       const double kw = ws[48064] * w;
       out[1536] = out[1536] + kw;
-      ws[270720] = fma(kw, y[1536], ws[270720]);
+      ws[276768] = fma(kw, y[1536], ws[276768]);
     }
     {
       double w = 1.0 * phi[1824];
@@ -1560,7 +1560,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48096] * w;
       out[4672] = fma(kw, y[5920], out[4672]);
       out[5920] = fma(kw, y[4672], out[5920]);
-      ws[270752] = fma(kw * y[4672], y[5920], ws[270752]);
+      ws[276800] = fma(kw * y[4672], y[5920], ws[276800]);
     }
     {
       double w = 1.0 * phi[4672];
@@ -1568,7 +1568,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       w = w - phi[1824];
       const double kw = ws[48128] * w;
       out[1824] = out[1824] + kw;
-      ws[270784] = fma(kw, y[1824], ws[270784]);
+      ws[276832] = fma(kw, y[1824], ws[276832]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1579,7 +1579,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48160] * w;
       out[5888] = fma(kw, y[5824], out[5888]);
       out[5824] = fma(kw, y[5888], out[5824]);
-      ws[270816] = fma(kw * y[5888], y[5824], ws[270816]);
+      ws[276864] = fma(kw * y[5888], y[5824], ws[276864]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1590,7 +1590,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48192] * w;
       out[5632] = fma(kw, y[5824], out[5632]);
       out[5824] = fma(kw, y[5632], out[5824]);
-      ws[270848] = fma(kw * y[5632], y[5824], ws[270848]);
+      ws[276896] = fma(kw * y[5632], y[5824], ws[276896]);
     }
     {
       double w = 0.66 * phi[5984];
@@ -1608,7 +1608,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48224] * w;
       out[5408] = fma(kw, y[5824], out[5408]);
       out[5824] = fma(kw, y[5408], out[5824]);
-      ws[270880] = fma(kw * y[5408], y[5824], ws[270880]);
+      ws[276928] = fma(kw * y[5408], y[5824], ws[276928]);
     }
     {
       double w = 0.2 * phi[5984];
@@ -1629,7 +1629,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48256] * w;
       out[5120] = fma(kw, y[5824], out[5120]);
       out[5824] = fma(kw, y[5120], out[5824]);
-      ws[270912] = fma(kw * y[5120], y[5824], ws[270912]);
+      ws[276960] = fma(kw * y[5120], y[5824], ws[276960]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1641,7 +1641,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48288] * w;
       out[3008] = fma(kw, y[5824], out[3008]);
       out[5824] = fma(kw, y[3008], out[5824]);
-      ws[270944] = fma(kw * y[3008], y[5824], ws[270944]);
+      ws[276992] = fma(kw * y[3008], y[5824], ws[276992]);
     }
     {
       double w = 0.78 * phi[5984];
@@ -1657,7 +1657,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48320] * w;
       out[3200] = fma(kw, y[5824], out[3200]);
       out[5824] = fma(kw, y[3200], out[5824]);
-      ws[270976] = fma(kw * y[3200], y[5824], ws[270976]);
+      ws[277024] = fma(kw * y[3200], y[5824], ws[277024]);
     }
     {
       double w = 0.83 * phi[5984];
@@ -1673,7 +1673,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48352] * w;
       out[3328] = fma(kw, y[5824], out[3328]);
       out[5824] = fma(kw, y[3328], out[5824]);
-      ws[271008] = fma(kw * y[3328], y[5824], ws[271008]);
+      ws[277056] = fma(kw * y[3328], y[5824], ws[277056]);
     }
     {
       double w = 0.0 * phi[5440];
@@ -1691,7 +1691,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48384] * w;
       out[3360] = fma(kw, y[5824], out[3360]);
       out[5824] = fma(kw, y[3360], out[5824]);
-      ws[271040] = fma(kw * y[3360], y[5824], ws[271040]);
+      ws[277088] = fma(kw * y[3360], y[5824], ws[277088]);
     }
     {
       double w = 0.0002 * phi[5440];
@@ -1709,7 +1709,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48416] * w;
       out[3296] = fma(kw, y[5824], out[3296]);
       out[5824] = fma(kw, y[3296], out[5824]);
-      ws[271072] = fma(kw * y[3296], y[5824], ws[271072]);
+      ws[277120] = fma(kw * y[3296], y[5824], ws[277120]);
     }
     {
       double w = 0.0001 * phi[5440];
@@ -1727,7 +1727,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48448] * w;
       out[3104] = fma(kw, y[5824], out[3104]);
       out[5824] = fma(kw, y[3104], out[5824]);
-      ws[271104] = fma(kw * y[3104], y[5824], ws[271104]);
+      ws[277152] = fma(kw * y[3104], y[5824], ws[277152]);
     }
     {
       double w = 0.0002 * phi[5440];
@@ -1745,7 +1745,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48480] * w;
       out[3264] = fma(kw, y[5824], out[3264]);
       out[5824] = fma(kw, y[3264], out[5824]);
-      ws[271136] = fma(kw * y[3264], y[5824], ws[271136]);
+      ws[277184] = fma(kw * y[3264], y[5824], ws[277184]);
     }
     {
       double w = 0.237 * phi[4384];
@@ -1763,7 +1763,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48512] * w;
       out[4160] = fma(kw, y[5824], out[4160]);
       out[5824] = fma(kw, y[4160], out[5824]);
-      ws[271168] = fma(kw * y[4160], y[5824], ws[271168]);
+      ws[277216] = fma(kw * y[4160], y[5824], ws[277216]);
     }
     {
       double w = 0.82 * phi[6016];
@@ -1774,7 +1774,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48544] * w;
       out[3744] = fma(kw, y[5824], out[3744]);
       out[5824] = fma(kw, y[3744], out[5824]);
-      ws[271200] = fma(kw * y[3744], y[5824], ws[271200]);
+      ws[277248] = fma(kw * y[3744], y[5824], ws[277248]);
     }
     {
       double w = 1.6955 * phi[5920];
@@ -1790,7 +1790,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48576] * w;
       out[2624] = fma(kw, y[5824], out[2624]);
       out[5824] = fma(kw, y[2624], out[5824]);
-      ws[271232] = fma(kw * y[2624], y[5824], ws[271232]);
+      ws[277280] = fma(kw * y[2624], y[5824], ws[277280]);
     }
     {
       double w = 0.82 * phi[5920];
@@ -1801,7 +1801,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48608] * w;
       out[3840] = fma(kw, y[5824], out[3840]);
       out[5824] = fma(kw, y[3840], out[5824]);
-      ws[271264] = fma(kw * y[3840], y[5824], ws[271264]);
+      ws[277312] = fma(kw * y[3840], y[5824], ws[277312]);
     }
     {
       double w = 0.23 * phi[4384];
@@ -1814,7 +1814,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48640] * w;
       out[4192] = fma(kw, y[5824], out[4192]);
       out[5824] = fma(kw, y[4192], out[5824]);
-      ws[271296] = fma(kw * y[4192], y[5824], ws[271296]);
+      ws[277344] = fma(kw * y[4192], y[5824], ws[277344]);
     }
     {
       double w = 0.77 * phi[6016];
@@ -1825,7 +1825,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48672] * w;
       out[3936] = fma(kw, y[5824], out[3936]);
       out[5824] = fma(kw, y[3936], out[5824]);
-      ws[271328] = fma(kw * y[3936], y[5824], ws[271328]);
+      ws[277376] = fma(kw * y[3936], y[5824], ws[277376]);
     }
     {
       double w = 0.57 * phi[4384];
@@ -1838,7 +1838,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48704] * w;
       out[2656] = fma(kw, y[5824], out[2656]);
       out[5824] = fma(kw, y[2656], out[5824]);
-      ws[271360] = fma(kw * y[2656], y[5824], ws[271360]);
+      ws[277408] = fma(kw * y[2656], y[5824], ws[277408]);
     }
     {
       double w = 0.77 * phi[5920];
@@ -1849,7 +1849,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48736] * w;
       out[3712] = fma(kw, y[5824], out[3712]);
       out[5824] = fma(kw, y[3712], out[5824]);
-      ws[271392] = fma(kw * y[3712], y[5824], ws[271392]);
+      ws[277440] = fma(kw * y[3712], y[5824], ws[277440]);
     }
     {
       double w = 0.36 * phi[4384];
@@ -1860,7 +1860,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48768] * w;
       out[2560] = fma(kw, y[5824], out[2560]);
       out[5824] = fma(kw, y[2560], out[5824]);
-      ws[271424] = fma(kw * y[2560], y[5824], ws[271424]);
+      ws[277472] = fma(kw * y[2560], y[5824], ws[277472]);
     }
     {
       double w = 0.64 * phi[4384];
@@ -1873,7 +1873,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48800] * w;
       out[1728] = fma(kw, y[5824], out[1728]);
       out[5824] = fma(kw, y[1728], out[5824]);
-      ws[271456] = fma(kw * y[1728], y[5824], ws[271456]);
+      ws[277504] = fma(kw * y[1728], y[5824], ws[277504]);
     }
     {
       double w = 1.0 * phi[5888];
@@ -1883,7 +1883,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48832] * w;
       out[5792] = fma(kw, y[5824], out[5792]);
       out[5824] = fma(kw, y[5792], out[5824]);
-      ws[271488] = fma(kw * y[5792], y[5824], ws[271488]);
+      ws[277536] = fma(kw * y[5792], y[5824], ws[277536]);
     }
     {
       double w = 1.0 * phi[5632];
@@ -1893,7 +1893,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48864] * w;
       out[4800] = fma(kw, y[5824], out[4800]);
       out[5824] = fma(kw, y[4800], out[5824]);
-      ws[271520] = fma(kw * y[4800], y[5824], ws[271520]);
+      ws[277568] = fma(kw * y[4800], y[5824], ws[277568]);
     }
     {
       double w = 1.0 * phi[5792];
@@ -1904,7 +1904,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48896] * w;
       out[2848] = fma(kw, y[5824], out[2848]);
       out[5824] = fma(kw, y[2848], out[5824]);
-      ws[271552] = fma(kw * y[2848], y[5824], ws[271552]);
+      ws[277600] = fma(kw * y[2848], y[5824], ws[277600]);
     }
     {
       double w = 0.67 * phi[5984];
@@ -1916,7 +1916,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48928] * w;
       out[5152] = fma(kw, y[5824], out[5152]);
       out[5824] = fma(kw, y[5152], out[5824]);
-      ws[271584] = fma(kw * y[5152], y[5824], ws[271584]);
+      ws[277632] = fma(kw * y[5152], y[5824], ws[277632]);
     }
     {
       double w = 0.77 * phi[5984];
@@ -1930,7 +1930,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48960] * w;
       out[3776] = fma(kw, y[5824], out[3776]);
       out[5824] = fma(kw, y[3776], out[5824]);
-      ws[271616] = fma(kw * y[3776], y[5824], ws[271616]);
+      ws[277664] = fma(kw * y[3776], y[5824], ws[277664]);
     }
     {
       double w = 0.65 * phi[5888];
@@ -1943,7 +1943,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[48992] * w;
       out[4672] = fma(kw, y[5824], out[4672]);
       out[5824] = fma(kw, y[4672], out[5824]);
-      ws[271648] = fma(kw * y[4672], y[5824], ws[271648]);
+      ws[277696] = fma(kw * y[4672], y[5824], ws[277696]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1955,7 +1955,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49024] * w;
       out[3520] = fma(kw, y[5824], out[3520]);
       out[5824] = fma(kw, y[3520], out[5824]);
-      ws[271680] = fma(kw * y[3520], y[5824], ws[271680]);
+      ws[277728] = fma(kw * y[3520], y[5824], ws[277728]);
     }
     {
       double w = 0.3 * phi[5984];
@@ -1970,7 +1970,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49056] * w;
       out[2880] = fma(kw, y[5824], out[2880]);
       out[5824] = fma(kw, y[2880], out[5824]);
-      ws[271712] = fma(kw * y[2880], y[5824], ws[271712]);
+      ws[277760] = fma(kw * y[2880], y[5824], ws[277760]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1986,7 +1986,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49088] * w;
       out[2912] = fma(kw, y[5824], out[2912]);
       out[5824] = fma(kw, y[2912], out[5824]);
-      ws[271744] = fma(kw * y[2912], y[5824], ws[271744]);
+      ws[277792] = fma(kw * y[2912], y[5824], ws[277792]);
     }
     {
       double w = 1.0 * phi[2272];
@@ -1996,7 +1996,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49120] * w;
       out[2592] = fma(kw, y[5824], out[2592]);
       out[5824] = fma(kw, y[2592], out[5824]);
-      ws[271776] = fma(kw * y[2592], y[5824], ws[271776]);
+      ws[277824] = fma(kw * y[2592], y[5824], ws[277824]);
     }
     {
       double w = 1.0 * phi[2688];
@@ -2006,7 +2006,7 @@ __device__ __noinline__ void adj_jtv_1_3(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49152] * w;
       out[2272] = fma(kw, y[5824], out[2272]);
       out[5824] = fma(kw, y[2272], out[5824]);
-      ws[271808] = fma(kw * y[2272], y[5824], ws[271808]);
+      ws[277856] = fma(kw * y[2272], y[5824], ws[277856]);
     }
 }
 }  // namespace mech_cracmm2

@@ -19,7 +19,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49184] * w;
       out[3648] = fma(kw, y[5824], out[3648]);
       out[5824] = fma(kw, y[3648], out[5824]);
-      ws[271840] = fma(kw * y[3648], y[5824], ws[271840]);
+      ws[277888] = fma(kw * y[3648], y[5824], ws[277888]);
     }
     {
       double w = 1.0 * phi[3808];
@@ -29,7 +29,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49216] * w;
       out[3040] = fma(kw, y[5824], out[3040]);
       out[5824] = fma(kw, y[3040], out[5824]);
-      ws[271872] = fma(kw * y[3040], y[5824], ws[271872]);
+      ws[277920] = fma(kw * y[3040], y[5824], ws[277920]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -40,7 +40,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49248] * w;
       out[2976] = fma(kw, y[5824], out[2976]);
       out[5824] = fma(kw, y[2976], out[5824]);
-      ws[271904] = fma(kw * y[2976], y[5824], ws[271904]);
+      ws[277952] = fma(kw * y[2976], y[5824], ws[277952]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -51,7 +51,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49280] * w;
       out[4032] = fma(kw, y[5824], out[4032]);
       out[5824] = fma(kw, y[4032], out[5824]);
-      ws[271936] = fma(kw * y[4032], y[5824], ws[271936]);
+      ws[277984] = fma(kw * y[4032], y[5824], ws[277984]);
     }
     {
       double w = 2.0 * phi[5920];
@@ -63,7 +63,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49312] * w;
       out[4064] = fma(kw, y[5824], out[4064]);
       out[5824] = fma(kw, y[4064], out[5824]);
-      ws[271968] = fma(kw * y[4064], y[5824], ws[271968]);
+      ws[278016] = fma(kw * y[4064], y[5824], ws[278016]);
     }
     {
       double w = 2.0 * phi[5920];
@@ -74,7 +74,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49344] * w;
       out[3072] = fma(kw, y[5824], out[3072]);
       out[5824] = fma(kw, y[3072], out[5824]);
-      ws[272000] = fma(kw * y[3072], y[5824], ws[272000]);
+      ws[278048] = fma(kw * y[3072], y[5824], ws[278048]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -83,7 +83,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49376] * w;
       out[5216] = fma(kw, y[5824], out[5216]);
       out[5824] = fma(kw, y[5216], out[5824]);
-      ws[272032] = fma(kw * y[5216], y[5824], ws[272032]);
+      ws[278080] = fma(kw * y[5216], y[5824], ws[278080]);
     }
     {
       double w = 1.0 * phi[5440];
@@ -92,7 +92,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49408] * w;
       out[2688] = fma(kw, y[5920], out[2688]);
       out[5920] = fma(kw, y[2688], out[5920]);
-      ws[272064] = fma(kw * y[2688], y[5920], ws[272064]);
+      ws[278112] = fma(kw * y[2688], y[5920], ws[278112]);
     }
     {
       double w = 1.0 * phi[5440];
@@ -101,7 +101,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49440] * w;
       out[3232] = fma(kw, y[5920], out[3232]);
       out[5920] = fma(kw, y[3232], out[5920]);
-      ws[272096] = fma(kw * y[3232], y[5920], ws[272096]);
+      ws[278144] = fma(kw * y[3232], y[5920], ws[278144]);
     }
     {
       double w = 1.0 * phi[5440];
@@ -110,7 +110,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49472] * w;
       out[3808] = fma(kw, y[5920], out[3808]);
       out[5920] = fma(kw, y[3808], out[5920]);
-      ws[272128] = fma(kw * y[3808], y[5920], ws[272128]);
+      ws[278176] = fma(kw * y[3808], y[5920], ws[278176]);
     }
     {
       double w = 1.0 * phi[2816];
@@ -119,7 +119,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49504] * w;
       out[5888] = fma(kw, y[5984], out[5888]);
       out[5984] = fma(kw, y[5888], out[5984]);
-      ws[272160] = fma(kw * y[5888], y[5984], ws[272160]);
+      ws[278208] = fma(kw * y[5888], y[5984], ws[278208]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -128,7 +128,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49536] * w;
       out[5632] = fma(kw, y[5984], out[5632]);
       out[5984] = fma(kw, y[5632], out[5984]);
-      ws[272192] = fma(kw * y[5632], y[5984], ws[272192]);
+      ws[278240] = fma(kw * y[5632], y[5984], ws[278240]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -137,7 +137,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49568] * w;
       out[5408] = fma(kw, y[5984], out[5408]);
       out[5984] = fma(kw, y[5408], out[5984]);
-      ws[272224] = fma(kw * y[5408], y[5984], ws[272224]);
+      ws[278272] = fma(kw * y[5408], y[5984], ws[278272]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -146,7 +146,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49600] * w;
       out[5120] = fma(kw, y[5984], out[5120]);
       out[5984] = fma(kw, y[5120], out[5984]);
-      ws[272256] = fma(kw * y[5120], y[5984], ws[272256]);
+      ws[278304] = fma(kw * y[5120], y[5984], ws[278304]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -155,7 +155,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49632] * w;
       out[3008] = fma(kw, y[5984], out[3008]);
       out[5984] = fma(kw, y[3008], out[5984]);
-      ws[272288] = fma(kw * y[3008], y[5984], ws[272288]);
+      ws[278336] = fma(kw * y[3008], y[5984], ws[278336]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -164,7 +164,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49664] * w;
       out[3200] = fma(kw, y[5984], out[3200]);
       out[5984] = fma(kw, y[3200], out[5984]);
-      ws[272320] = fma(kw * y[3200], y[5984], ws[272320]);
+      ws[278368] = fma(kw * y[3200], y[5984], ws[278368]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -173,7 +173,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49696] * w;
       out[3328] = fma(kw, y[5984], out[3328]);
       out[5984] = fma(kw, y[3328], out[5984]);
-      ws[272352] = fma(kw * y[3328], y[5984], ws[272352]);
+      ws[278400] = fma(kw * y[3328], y[5984], ws[278400]);
     }
     {
       double w = 0.6021 * phi[5728];
@@ -183,7 +183,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49728] * w;
       out[3360] = fma(kw, y[5984], out[3360]);
       out[5984] = fma(kw, y[3360], out[5984]);
-      ws[272384] = fma(kw * y[3360], y[5984], ws[272384]);
+      ws[278432] = fma(kw * y[3360], y[5984], ws[278432]);
     }
     {
       double w = 0.7195 * phi[5728];
@@ -193,7 +193,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49760] * w;
       out[3296] = fma(kw, y[5984], out[3296]);
       out[5984] = fma(kw, y[3296], out[5984]);
-      ws[272416] = fma(kw * y[3296], y[5984], ws[272416]);
+      ws[278464] = fma(kw * y[3296], y[5984], ws[278464]);
     }
     {
       double w = 0.0482 * phi[5728];
@@ -204,7 +204,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49792] * w;
       out[3104] = fma(kw, y[5984], out[3104]);
       out[5984] = fma(kw, y[3104], out[5984]);
-      ws[272448] = fma(kw * y[3104], y[5984], ws[272448]);
+      ws[278496] = fma(kw * y[3104], y[5984], ws[278496]);
     }
     {
       double w = 0.0854 * phi[5728];
@@ -215,7 +215,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49824] * w;
       out[3264] = fma(kw, y[5984], out[3264]);
       out[5984] = fma(kw, y[3264], out[5984]);
-      ws[272480] = fma(kw * y[3264], y[5984], ws[272480]);
+      ws[278528] = fma(kw * y[3264], y[5984], ws[278528]);
     }
     {
       double w = 0.039 * phi[4480];
@@ -231,7 +231,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49856] * w;
       out[4160] = fma(kw, y[5984], out[4160]);
       out[5984] = fma(kw, y[4160], out[5984]);
-      ws[272512] = fma(kw * y[4160], y[5984], ws[272512]);
+      ws[278560] = fma(kw * y[4160], y[5984], ws[278560]);
     }
     {
       double w = 1.0 * phi[4256];
@@ -240,7 +240,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49888] * w;
       out[3744] = fma(kw, y[5984], out[3744]);
       out[5984] = fma(kw, y[3744], out[5984]);
-      ws[272544] = fma(kw * y[3744], y[5984], ws[272544]);
+      ws[278592] = fma(kw * y[3744], y[5984], ws[278592]);
     }
     {
       double w = 0.461 * phi[4384];
@@ -255,7 +255,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49920] * w;
       out[2624] = fma(kw, y[5984], out[2624]);
       out[5984] = fma(kw, y[2624], out[5984]);
-      ws[272576] = fma(kw * y[2624], y[5984], ws[272576]);
+      ws[278624] = fma(kw * y[2624], y[5984], ws[278624]);
     }
     {
       double w = 1.0 * phi[4256];
@@ -264,7 +264,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49952] * w;
       out[3840] = fma(kw, y[5984], out[3840]);
       out[5984] = fma(kw, y[3840], out[5984]);
-      ws[272608] = fma(kw * y[3840], y[5984], ws[272608]);
+      ws[278656] = fma(kw * y[3840], y[5984], ws[278656]);
     }
     {
       double w = 0.9 * phi[4096];
@@ -277,7 +277,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[49984] * w;
       out[4192] = fma(kw, y[5984], out[4192]);
       out[5984] = fma(kw, y[4192], out[5984]);
-      ws[272640] = fma(kw * y[4192], y[5984], ws[272640]);
+      ws[278688] = fma(kw * y[4192], y[5984], ws[278688]);
     }
     {
       double w = 1.0 * phi[4256];
@@ -286,7 +286,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50016] * w;
       out[3936] = fma(kw, y[5984], out[3936]);
       out[5984] = fma(kw, y[3936], out[5984]);
-      ws[272672] = fma(kw * y[3936], y[5984], ws[272672]);
+      ws[278720] = fma(kw * y[3936], y[5984], ws[278720]);
     }
     {
       double w = 0.77 * phi[4384];
@@ -299,7 +299,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50048] * w;
       out[2656] = fma(kw, y[5984], out[2656]);
       out[5984] = fma(kw, y[2656], out[5984]);
-      ws[272704] = fma(kw * y[2656], y[5984], ws[272704]);
+      ws[278752] = fma(kw * y[2656], y[5984], ws[278752]);
     }
     {
       double w = 1.0 * phi[4256];
@@ -308,7 +308,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50080] * w;
       out[3712] = fma(kw, y[5984], out[3712]);
       out[5984] = fma(kw, y[3712], out[5984]);
-      ws[272736] = fma(kw * y[3712], y[5984], ws[272736]);
+      ws[278784] = fma(kw * y[3712], y[5984], ws[278784]);
     }
     {
       double w = 0.75 * phi[4096];
@@ -319,7 +319,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50112] * w;
       out[2560] = fma(kw, y[5984], out[2560]);
       out[5984] = fma(kw, y[2560], out[5984]);
-      ws[272768] = fma(kw * y[2560], y[5984], ws[272768]);
+      ws[278816] = fma(kw * y[2560], y[5984], ws[278816]);
     }
     {
       double w = 0.9 * phi[4096];
@@ -332,7 +332,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50144] * w;
       out[1728] = fma(kw, y[5984], out[1728]);
       out[5984] = fma(kw, y[1728], out[5984]);
-      ws[272800] = fma(kw * y[1728], y[5984], ws[272800]);
+      ws[278848] = fma(kw * y[1728], y[5984], ws[278848]);
     }
     {
       double w = 0.44 * phi[6016];
@@ -344,7 +344,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50176] * w;
       out[5792] = fma(kw, y[5984], out[5792]);
       out[5984] = fma(kw, y[5792], out[5984]);
-      ws[272832] = fma(kw * y[5792], y[5984], ws[272832]);
+      ws[278880] = fma(kw * y[5792], y[5984], ws[278880]);
     }
     {
       double w = 0.44 * phi[6016];
@@ -356,7 +356,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50208] * w;
       out[4800] = fma(kw, y[5984], out[4800]);
       out[5984] = fma(kw, y[4800], out[5984]);
-      ws[272864] = fma(kw * y[4800], y[5984], ws[272864]);
+      ws[278912] = fma(kw * y[4800], y[5984], ws[278912]);
     }
     {
       double w = 0.15 * phi[6016];
@@ -368,7 +368,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50240] * w;
       out[2848] = fma(kw, y[5984], out[2848]);
       out[5984] = fma(kw, y[2848], out[5984]);
-      ws[272896] = fma(kw * y[2848], y[5984], ws[272896]);
+      ws[278944] = fma(kw * y[2848], y[5984], ws[278944]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -377,7 +377,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50272] * w;
       out[5152] = fma(kw, y[5984], out[5152]);
       out[5984] = fma(kw, y[5152], out[5984]);
-      ws[272928] = fma(kw * y[5152], y[5984], ws[272928]);
+      ws[278976] = fma(kw * y[5152], y[5984], ws[278976]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -386,7 +386,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50304] * w;
       out[3776] = fma(kw, y[5984], out[3776]);
       out[5984] = fma(kw, y[3776], out[5984]);
-      ws[272960] = fma(kw * y[3776], y[5984], ws[272960]);
+      ws[279008] = fma(kw * y[3776], y[5984], ws[279008]);
     }
     {
       double w = 1.0 * phi[1792];
@@ -395,7 +395,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50336] * w;
       out[4672] = fma(kw, y[5984], out[4672]);
       out[5984] = fma(kw, y[4672], out[5984]);
-      ws[272992] = fma(kw * y[4672], y[5984], ws[272992]);
+      ws[279040] = fma(kw * y[4672], y[5984], ws[279040]);
     }
     {
       double w = 1.0 * phi[1792];
@@ -404,7 +404,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50368] * w;
       out[3520] = fma(kw, y[5984], out[3520]);
       out[5984] = fma(kw, y[3520], out[5984]);
-      ws[273024] = fma(kw * y[3520], y[5984], ws[273024]);
+      ws[279072] = fma(kw * y[3520], y[5984], ws[279072]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -413,7 +413,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50400] * w;
       out[2880] = fma(kw, y[5984], out[2880]);
       out[5984] = fma(kw, y[2880], out[5984]);
-      ws[273056] = fma(kw * y[2880], y[5984], ws[273056]);
+      ws[279104] = fma(kw * y[2880], y[5984], ws[279104]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -422,7 +422,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50432] * w;
       out[2912] = fma(kw, y[5984], out[2912]);
       out[5984] = fma(kw, y[2912], out[5984]);
-      ws[273088] = fma(kw * y[2912], y[5984], ws[273088]);
+      ws[279136] = fma(kw * y[2912], y[5984], ws[279136]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -431,7 +431,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50464] * w;
       out[3648] = fma(kw, y[5984], out[3648]);
       out[5984] = fma(kw, y[3648], out[5984]);
-      ws[273120] = fma(kw * y[3648], y[5984], ws[273120]);
+      ws[279168] = fma(kw * y[3648], y[5984], ws[279168]);
     }
     {
       double w = 1.0 * phi[2944];
@@ -440,7 +440,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50496] * w;
       out[3232] = fma(kw, y[5984], out[3232]);
       out[5984] = fma(kw, y[3232], out[5984]);
-      ws[273152] = fma(kw * y[3232], y[5984], ws[273152]);
+      ws[279200] = fma(kw * y[3232], y[5984], ws[279200]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -449,7 +449,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50528] * w;
       out[3040] = fma(kw, y[5984], out[3040]);
       out[5984] = fma(kw, y[3040], out[5984]);
-      ws[273184] = fma(kw * y[3040], y[5984], ws[273184]);
+      ws[279232] = fma(kw * y[3040], y[5984], ws[279232]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -458,7 +458,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50560] * w;
       out[2976] = fma(kw, y[5984], out[2976]);
       out[5984] = fma(kw, y[2976], out[5984]);
-      ws[273216] = fma(kw * y[2976], y[5984], ws[273216]);
+      ws[279264] = fma(kw * y[2976], y[5984], ws[279264]);
     }
     {
       double w = 1.0 * phi[5440];
@@ -467,7 +467,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50592] * w;
       out[4032] = fma(kw, y[5984], out[4032]);
       out[5984] = fma(kw, y[4032], out[5984]);
-      ws[273248] = fma(kw * y[4032], y[5984], ws[273248]);
+      ws[279296] = fma(kw * y[4032], y[5984], ws[279296]);
     }
     {
       double w = 1.0 * phi[5440];
@@ -476,7 +476,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50624] * w;
       out[4064] = fma(kw, y[5984], out[4064]);
       out[5984] = fma(kw, y[4064], out[5984]);
-      ws[273280] = fma(kw * y[4064], y[5984], ws[273280]);
+      ws[279328] = fma(kw * y[4064], y[5984], ws[279328]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -485,7 +485,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50656] * w;
       out[3072] = fma(kw, y[5984], out[3072]);
       out[5984] = fma(kw, y[3072], out[5984]);
-      ws[273312] = fma(kw * y[3072], y[5984], ws[273312]);
+      ws[279360] = fma(kw * y[3072], y[5984], ws[279360]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -494,7 +494,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50688] * w;
       out[5216] = fma(kw, y[5984], out[5216]);
       out[5984] = fma(kw, y[5216], out[5984]);
-      ws[273344] = fma(kw * y[5216], y[5984], ws[273344]);
+      ws[279392] = fma(kw * y[5216], y[5984], ws[279392]);
     }
     {
       double w = 0.74 * phi[5984];
@@ -505,7 +505,7 @@ __device__ __noinline__ void adj_jtv_1_4(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50720] * w;
       out[5888] = fma(kw, y[5888], out[5888]);
       out[5888] = fma(kw, y[5888], out[5888]);
-      ws[273376] = fma(kw * y[5888], y[5888], ws[273376]);
+      ws[279424] = fma(kw * y[5888], y[5888], ws[279424]);
     }
 }
 __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int phioff, int outoff)
@@ -524,7 +524,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50752] * w;
       out[5632] = fma(kw, y[5888], out[5632]);
       out[5888] = fma(kw, y[5632], out[5888]);
-      ws[273408] = fma(kw * y[5632], y[5888], ws[273408]);
+      ws[279456] = fma(kw * y[5632], y[5888], ws[279456]);
     }
     {
       double w = 0.894 * phi[5984];
@@ -542,7 +542,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50784] * w;
       out[5408] = fma(kw, y[5888], out[5408]);
       out[5888] = fma(kw, y[5408], out[5888]);
-      ws[273440] = fma(kw * y[5408], y[5888], ws[273440]);
+      ws[279488] = fma(kw * y[5408], y[5888], ws[279488]);
     }
     {
       double w = 0.842 * phi[5984];
@@ -559,7 +559,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50816] * w;
       out[5120] = fma(kw, y[5888], out[5120]);
       out[5888] = fma(kw, y[5120], out[5888]);
-      ws[273472] = fma(kw * y[5120], y[5888], ws[273472]);
+      ws[279520] = fma(kw * y[5120], y[5888], ws[279520]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -572,7 +572,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50848] * w;
       out[3008] = fma(kw, y[5888], out[3008]);
       out[5888] = fma(kw, y[3008], out[5888]);
-      ws[273504] = fma(kw * y[3008], y[5888], ws[273504]);
+      ws[279552] = fma(kw * y[3008], y[5888], ws[279552]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -586,7 +586,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50880] * w;
       out[3200] = fma(kw, y[5888], out[3200]);
       out[5888] = fma(kw, y[3200], out[5888]);
-      ws[273536] = fma(kw * y[3200], y[5888], ws[273536]);
+      ws[279584] = fma(kw * y[3200], y[5888], ws[279584]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -600,7 +600,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50912] * w;
       out[3328] = fma(kw, y[5888], out[3328]);
       out[5888] = fma(kw, y[3328], out[5888]);
-      ws[273568] = fma(kw * y[3328], y[5888], ws[273568]);
+      ws[279616] = fma(kw * y[3328], y[5888], ws[279616]);
     }
     {
       double w = 0.68 * phi[5856];
@@ -616,7 +616,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50944] * w;
       out[3360] = fma(kw, y[5888], out[3360]);
       out[5888] = fma(kw, y[3360], out[5888]);
-      ws[273600] = fma(kw * y[3360], y[5888], ws[273600]);
+      ws[279648] = fma(kw * y[3360], y[5888], ws[279648]);
     }
     {
       double w = 0.68 * phi[5856];
@@ -632,7 +632,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[50976] * w;
       out[3296] = fma(kw, y[5888], out[3296]);
       out[5888] = fma(kw, y[3296], out[5888]);
-      ws[273632] = fma(kw * y[3296], y[5888], ws[273632]);
+      ws[279680] = fma(kw * y[3296], y[5888], ws[279680]);
     }
     {
       double w = 0.68 * phi[5856];
@@ -648,7 +648,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51008] * w;
       out[3104] = fma(kw, y[5888], out[3104]);
       out[5888] = fma(kw, y[3104], out[5888]);
-      ws[273664] = fma(kw * y[3104], y[5888], ws[273664]);
+      ws[279712] = fma(kw * y[3104], y[5888], ws[279712]);
     }
     {
       double w = 0.68 * phi[5856];
@@ -664,7 +664,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51040] * w;
       out[3264] = fma(kw, y[5888], out[3264]);
       out[5888] = fma(kw, y[3264], out[5888]);
-      ws[273696] = fma(kw * y[3264], y[5888], ws[273696]);
+      ws[279744] = fma(kw * y[3264], y[5888], ws[279744]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -681,7 +681,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51072] * w;
       out[4288] = fma(kw, y[5888], out[4288]);
       out[5888] = fma(kw, y[4288], out[5888]);
-      ws[273728] = fma(kw * y[4288], y[5888], ws[273728]);
+      ws[279776] = fma(kw * y[4288], y[5888], ws[279776]);
     }
     {
       double w = 1.0295 * phi[5856];
@@ -698,7 +698,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51104] * w;
       out[4160] = fma(kw, y[5888], out[4160]);
       out[5888] = fma(kw, y[4160], out[5888]);
-      ws[273760] = fma(kw * y[4160], y[5888], ws[273760]);
+      ws[279808] = fma(kw * y[4160], y[5888], ws[279808]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -710,7 +710,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51136] * w;
       out[3744] = fma(kw, y[5888], out[3744]);
       out[5888] = fma(kw, y[3744], out[5888]);
-      ws[273792] = fma(kw * y[3744], y[5888], ws[273792]);
+      ws[279840] = fma(kw * y[3744], y[5888], ws[279840]);
     }
     {
       double w = 0.341 * phi[4384];
@@ -726,7 +726,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51168] * w;
       out[2624] = fma(kw, y[5888], out[2624]);
       out[5888] = fma(kw, y[2624], out[5888]);
-      ws[273824] = fma(kw * y[2624], y[5888], ws[273824]);
+      ws[279872] = fma(kw * y[2624], y[5888], ws[279872]);
     }
     {
       double w = 0.75 * phi[5984];
@@ -739,7 +739,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51200] * w;
       out[3840] = fma(kw, y[5888], out[3840]);
       out[5888] = fma(kw, y[3840], out[5888]);
-      ws[273856] = fma(kw * y[3840], y[5888], ws[273856]);
+      ws[279904] = fma(kw * y[3840], y[5888], ws[279904]);
     }
     {
       double w = 0.25 * phi[5600];
@@ -751,7 +751,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51232] * w;
       out[4192] = fma(kw, y[5888], out[4192]);
       out[5888] = fma(kw, y[4192], out[5888]);
-      ws[273888] = fma(kw * y[4192], y[5888], ws[273888]);
+      ws[279936] = fma(kw * y[4192], y[5888], ws[279936]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -763,7 +763,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51264] * w;
       out[3936] = fma(kw, y[5888], out[3936]);
       out[5888] = fma(kw, y[3936], out[5888]);
-      ws[273920] = fma(kw * y[3936], y[5888], ws[273920]);
+      ws[279968] = fma(kw * y[3936], y[5888], ws[279968]);
     }
     {
       double w = 0.69 * phi[4384];
@@ -777,7 +777,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51296] * w;
       out[2656] = fma(kw, y[5888], out[2656]);
       out[5888] = fma(kw, y[2656], out[5888]);
-      ws[273952] = fma(kw * y[2656], y[5888], ws[273952]);
+      ws[280000] = fma(kw * y[2656], y[5888], ws[280000]);
     }
     {
       double w = 0.75 * phi[5984];
@@ -790,7 +790,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51328] * w;
       out[3712] = fma(kw, y[5888], out[3712]);
       out[5888] = fma(kw, y[3712], out[5888]);
-      ws[273984] = fma(kw * y[3712], y[5888], ws[273984]);
+      ws[280032] = fma(kw * y[3712], y[5888], ws[280032]);
     }
     {
       double w = 0.9 * phi[5984];
@@ -802,7 +802,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51360] * w;
       out[5792] = fma(kw, y[5888], out[5792]);
       out[5888] = fma(kw, y[5792], out[5888]);
-      ws[274016] = fma(kw * y[5792], y[5888], ws[274016]);
+      ws[280064] = fma(kw * y[5792], y[5888], ws[280064]);
     }
     {
       double w = 0.9 * phi[5984];
@@ -814,7 +814,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51392] * w;
       out[4800] = fma(kw, y[5888], out[4800]);
       out[5888] = fma(kw, y[4800], out[5888]);
-      ws[274048] = fma(kw * y[4800], y[5888], ws[274048]);
+      ws[280096] = fma(kw * y[4800], y[5888], ws[280096]);
     }
     {
       double w = 0.5 * phi[5984];
@@ -828,7 +828,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51424] * w;
       out[2848] = fma(kw, y[5888], out[2848]);
       out[5888] = fma(kw, y[2848], out[5888]);
-      ws[274080] = fma(kw * y[2848], y[5888], ws[274080]);
+      ws[280128] = fma(kw * y[2848], y[5888], ws[280128]);
     }
     {
       double w = 0.834 * phi[5984];
@@ -841,7 +841,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51456] * w;
       out[5152] = fma(kw, y[5888], out[5152]);
       out[5888] = fma(kw, y[5152], out[5888]);
-      ws[274112] = fma(kw * y[5152], y[5888], ws[274112]);
+      ws[280160] = fma(kw * y[5152], y[5888], ws[280160]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -854,7 +854,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51488] * w;
       out[3776] = fma(kw, y[5888], out[3776]);
       out[5888] = fma(kw, y[3776], out[5888]);
-      ws[274144] = fma(kw * y[3776], y[5888], ws[274144]);
+      ws[280192] = fma(kw * y[3776], y[5888], ws[280192]);
     }
     {
       double w = 0.5 * phi[5984];
@@ -870,7 +870,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51520] * w;
       out[4672] = fma(kw, y[5888], out[4672]);
       out[5888] = fma(kw, y[4672], out[5888]);
-      ws[274176] = fma(kw * y[4672], y[5888], ws[274176]);
+      ws[280224] = fma(kw * y[4672], y[5888], ws[280224]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -884,7 +884,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51552] * w;
       out[3520] = fma(kw, y[5888], out[3520]);
       out[5888] = fma(kw, y[3520], out[5888]);
-      ws[274208] = fma(kw * y[3520], y[5888], ws[274208]);
+      ws[280256] = fma(kw * y[3520], y[5888], ws[280256]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -901,7 +901,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51584] * w;
       out[2880] = fma(kw, y[5888], out[2880]);
       out[5888] = fma(kw, y[2880], out[5888]);
-      ws[274240] = fma(kw * y[2880], y[5888], ws[274240]);
+      ws[280288] = fma(kw * y[2880], y[5888], ws[280288]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -918,7 +918,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51616] * w;
       out[2912] = fma(kw, y[5888], out[2912]);
       out[5888] = fma(kw, y[2912], out[5888]);
-      ws[274272] = fma(kw * y[2912], y[5888], ws[274272]);
+      ws[280320] = fma(kw * y[2912], y[5888], ws[280320]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -929,7 +929,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51648] * w;
       out[2592] = fma(kw, y[5888], out[2592]);
       out[5888] = fma(kw, y[2592], out[5888]);
-      ws[274304] = fma(kw * y[2592], y[5888], ws[274304]);
+      ws[280352] = fma(kw * y[2592], y[5888], ws[280352]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -940,7 +940,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51680] * w;
       out[2272] = fma(kw, y[5888], out[2272]);
       out[5888] = fma(kw, y[2272], out[5888]);
-      ws[274336] = fma(kw * y[2272], y[5888], ws[274336]);
+      ws[280384] = fma(kw * y[2272], y[5888], ws[280384]);
     }
     {
       double w = 2.0 * phi[5984];
@@ -953,7 +953,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51712] * w;
       out[3648] = fma(kw, y[5888], out[3648]);
       out[5888] = fma(kw, y[3648], out[5888]);
-      ws[274368] = fma(kw * y[3648], y[5888], ws[274368]);
+      ws[280416] = fma(kw * y[3648], y[5888], ws[280416]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -964,7 +964,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51744] * w;
       out[3040] = fma(kw, y[5888], out[3040]);
       out[5888] = fma(kw, y[3040], out[5888]);
-      ws[274400] = fma(kw * y[3040], y[5888], ws[274400]);
+      ws[280448] = fma(kw * y[3040], y[5888], ws[280448]);
     }
     {
       double w = 1.0 * phi[5856];
@@ -975,7 +975,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51776] * w;
       out[2976] = fma(kw, y[5888], out[2976]);
       out[5888] = fma(kw, y[2976], out[5888]);
-      ws[274432] = fma(kw * y[2976], y[5888], ws[274432]);
+      ws[280480] = fma(kw * y[2976], y[5888], ws[280480]);
     }
     {
       double w = 2.0 * phi[5984];
@@ -986,7 +986,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51808] * w;
       out[4032] = fma(kw, y[5888], out[4032]);
       out[5888] = fma(kw, y[4032], out[5888]);
-      ws[274464] = fma(kw * y[4032], y[5888], ws[274464]);
+      ws[280512] = fma(kw * y[4032], y[5888], ws[280512]);
     }
     {
       double w = 0.5 * phi[5984];
@@ -1002,7 +1002,7 @@ __device__ __noinline__ void adj_jtv_1_5(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51840] * w;
       out[4064] = fma(kw, y[5888], out[4064]);
       out[5888] = fma(kw, y[4064], out[5888]);
-      ws[274496] = fma(kw * y[4064], y[5888], ws[274496]);
+      ws[280544] = fma(kw * y[4064], y[5888], ws[280544]);
     }
 }
 __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int phioff, int outoff)
@@ -1022,7 +1022,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51872] * w;
       out[3072] = fma(kw, y[5888], out[3072]);
       out[5888] = fma(kw, y[3072], out[5888]);
-      ws[274528] = fma(kw * y[3072], y[5888], ws[274528]);
+      ws[280576] = fma(kw * y[3072], y[5888], ws[280576]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1032,7 +1032,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51904] * w;
       out[5216] = fma(kw, y[5888], out[5216]);
       out[5888] = fma(kw, y[5216], out[5888]);
-      ws[274560] = fma(kw * y[5216], y[5888], ws[274560]);
+      ws[280608] = fma(kw * y[5216], y[5888], ws[280608]);
     }
     {
       double w = 0.5 * phi[5984];
@@ -1044,7 +1044,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51936] * w;
       out[5632] = fma(kw, y[5792], out[5632]);
       out[5792] = fma(kw, y[5632], out[5792]);
-      ws[274592] = fma(kw * y[5632], y[5792], ws[274592]);
+      ws[280640] = fma(kw * y[5632], y[5792], ws[280640]);
     }
     {
       double w = 0.394 * phi[5984];
@@ -1061,7 +1061,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[51968] * w;
       out[5408] = fma(kw, y[5792], out[5408]);
       out[5792] = fma(kw, y[5408], out[5792]);
-      ws[274624] = fma(kw * y[5408], y[5792], ws[274624]);
+      ws[280672] = fma(kw * y[5408], y[5792], ws[280672]);
     }
     {
       double w = 0.342 * phi[5984];
@@ -1077,7 +1077,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52000] * w;
       out[5120] = fma(kw, y[5792], out[5120]);
       out[5792] = fma(kw, y[5120], out[5792]);
-      ws[274656] = fma(kw * y[5120], y[5792], ws[274656]);
+      ws[280704] = fma(kw * y[5120], y[5792], ws[280704]);
     }
     {
       double w = 0.5 * phi[5984];
@@ -1090,7 +1090,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52032] * w;
       out[3008] = fma(kw, y[5792], out[3008]);
       out[5792] = fma(kw, y[3008], out[5792]);
-      ws[274688] = fma(kw * y[3008], y[5792], ws[274688]);
+      ws[280736] = fma(kw * y[3008], y[5792], ws[280736]);
     }
     {
       double w = 0.5 * phi[5984];
@@ -1104,7 +1104,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52064] * w;
       out[3200] = fma(kw, y[5792], out[3200]);
       out[5792] = fma(kw, y[3200], out[5792]);
-      ws[274720] = fma(kw * y[3200], y[5792], ws[274720]);
+      ws[280768] = fma(kw * y[3200], y[5792], ws[280768]);
     }
     {
       double w = 0.5 * phi[5984];
@@ -1117,7 +1117,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52096] * w;
       out[3328] = fma(kw, y[5792], out[3328]);
       out[5792] = fma(kw, y[3328], out[5792]);
-      ws[274752] = fma(kw * y[3328], y[5792], ws[274752]);
+      ws[280800] = fma(kw * y[3328], y[5792], ws[280800]);
     }
     {
       double w = 0.7 * phi[5888];
@@ -1133,7 +1133,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52128] * w;
       out[3360] = fma(kw, y[5792], out[3360]);
       out[5792] = fma(kw, y[3360], out[5792]);
-      ws[274784] = fma(kw * y[3360], y[5792], ws[274784]);
+      ws[280832] = fma(kw * y[3360], y[5792], ws[280832]);
     }
     {
       double w = 0.7 * phi[5888];
@@ -1149,7 +1149,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52160] * w;
       out[3296] = fma(kw, y[5792], out[3296]);
       out[5792] = fma(kw, y[3296], out[5792]);
-      ws[274816] = fma(kw * y[3296], y[5792], ws[274816]);
+      ws[280864] = fma(kw * y[3296], y[5792], ws[280864]);
     }
     {
       double w = 0.7 * phi[5888];
@@ -1165,7 +1165,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52192] * w;
       out[3104] = fma(kw, y[5792], out[3104]);
       out[5792] = fma(kw, y[3104], out[5792]);
-      ws[274848] = fma(kw * y[3104], y[5792], ws[274848]);
+      ws[280896] = fma(kw * y[3104], y[5792], ws[280896]);
     }
     {
       double w = 0.7 * phi[5888];
@@ -1181,7 +1181,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52224] * w;
       out[3264] = fma(kw, y[5792], out[3264]);
       out[5792] = fma(kw, y[3264], out[5792]);
-      ws[274880] = fma(kw * y[3264], y[5792], ws[274880]);
+      ws[280928] = fma(kw * y[3264], y[5792], ws[280928]);
     }
     {
       double w = 0.5 * phi[5984];
@@ -1195,7 +1195,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52256] * w;
       out[4288] = fma(kw, y[5792], out[4288]);
       out[5792] = fma(kw, y[4288], out[5792]);
-      ws[274912] = fma(kw * y[4288], y[5792], ws[274912]);
+      ws[280960] = fma(kw * y[4288], y[5792], ws[280960]);
     }
     {
       double w = 0.2535 * phi[4544];
@@ -1212,7 +1212,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52288] * w;
       out[4160] = fma(kw, y[5792], out[4160]);
       out[5792] = fma(kw, y[4160], out[5792]);
-      ws[274944] = fma(kw * y[4160], y[5792], ws[274944]);
+      ws[280992] = fma(kw * y[4160], y[5792], ws[280992]);
     }
     {
       double w = 0.5 * phi[6016];
@@ -1224,7 +1224,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52320] * w;
       out[3744] = fma(kw, y[5792], out[3744]);
       out[5792] = fma(kw, y[3744], out[5792]);
-      ws[274976] = fma(kw * y[3744], y[5792], ws[274976]);
+      ws[281024] = fma(kw * y[3744], y[5792], ws[281024]);
     }
     {
       double w = 0.825 * phi[5920];
@@ -1240,7 +1240,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52352] * w;
       out[2624] = fma(kw, y[5792], out[2624]);
       out[5792] = fma(kw, y[2624], out[5792]);
-      ws[275008] = fma(kw * y[2624], y[5792], ws[275008]);
+      ws[281056] = fma(kw * y[2624], y[5792], ws[281056]);
     }
     {
       double w = 0.5 * phi[5920];
@@ -1252,7 +1252,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52384] * w;
       out[3840] = fma(kw, y[5792], out[3840]);
       out[5792] = fma(kw, y[3840], out[5792]);
-      ws[275040] = fma(kw * y[3840], y[5792], ws[275040]);
+      ws[281088] = fma(kw * y[3840], y[5792], ws[281088]);
     }
     {
       double w = 1.0 * phi[4576];
@@ -1264,7 +1264,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52416] * w;
       out[4192] = fma(kw, y[5792], out[4192]);
       out[5792] = fma(kw, y[4192], out[5792]);
-      ws[275072] = fma(kw * y[4192], y[5792], ws[275072]);
+      ws[281120] = fma(kw * y[4192], y[5792], ws[281120]);
     }
     {
       double w = 0.5 * phi[6016];
@@ -1276,7 +1276,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52448] * w;
       out[3936] = fma(kw, y[5792], out[3936]);
       out[5792] = fma(kw, y[3936], out[5792]);
-      ws[275104] = fma(kw * y[3936], y[5792], ws[275104]);
+      ws[281152] = fma(kw * y[3936], y[5792], ws[281152]);
     }
     {
       double w = 1.0 * phi[5888];
@@ -1289,7 +1289,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52480] * w;
       out[2656] = fma(kw, y[5792], out[2656]);
       out[5792] = fma(kw, y[2656], out[5792]);
-      ws[275136] = fma(kw * y[2656], y[5792], ws[275136]);
+      ws[281184] = fma(kw * y[2656], y[5792], ws[281184]);
     }
     {
       double w = 0.5 * phi[5888];
@@ -1301,7 +1301,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52512] * w;
       out[3712] = fma(kw, y[5792], out[3712]);
       out[5792] = fma(kw, y[3712], out[5792]);
-      ws[275168] = fma(kw * y[3712], y[5792], ws[275168]);
+      ws[281216] = fma(kw * y[3712], y[5792], ws[281216]);
     }
     {
       double w = 2.0 * phi[5888];
@@ -1310,7 +1310,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52544] * w;
       out[5792] = fma(kw, y[5792], out[5792]);
       out[5792] = fma(kw, y[5792], out[5792]);
-      ws[275200] = fma(kw * y[5792], y[5792], ws[275200]);
+      ws[281248] = fma(kw * y[5792], y[5792], ws[281248]);
     }
     {
       double w = 1.0 * phi[5888];
@@ -1320,7 +1320,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52576] * w;
       out[4800] = fma(kw, y[5792], out[4800]);
       out[5792] = fma(kw, y[4800], out[5792]);
-      ws[275232] = fma(kw * y[4800], y[5792], ws[275232]);
+      ws[281280] = fma(kw * y[4800], y[5792], ws[281280]);
     }
     {
       double w = 0.5 * phi[5888];
@@ -1332,7 +1332,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52608] * w;
       out[2848] = fma(kw, y[5792], out[2848]);
       out[5792] = fma(kw, y[2848], out[5792]);
-      ws[275264] = fma(kw * y[2848], y[5792], ws[275264]);
+      ws[281312] = fma(kw * y[2848], y[5792], ws[281312]);
     }
     {
       double w = 0.33 * phi[5984];
@@ -1345,7 +1345,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52640] * w;
       out[5152] = fma(kw, y[5792], out[5152]);
       out[5792] = fma(kw, y[5152], out[5792]);
-      ws[275296] = fma(kw * y[5152], y[5792], ws[275296]);
+      ws[281344] = fma(kw * y[5152], y[5792], ws[281344]);
     }
     {
       double w = 0.5 * phi[5984];
@@ -1357,7 +1357,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52672] * w;
       out[3776] = fma(kw, y[5792], out[3776]);
       out[5792] = fma(kw, y[3776], out[5792]);
-      ws[275328] = fma(kw * y[3776], y[5792], ws[275328]);
+      ws[281376] = fma(kw * y[3776], y[5792], ws[281376]);
     }
     {
       double w = 0.635 * phi[5696];
@@ -1370,7 +1370,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52704] * w;
       out[4672] = fma(kw, y[5792], out[4672]);
       out[5792] = fma(kw, y[4672], out[5792]);
-      ws[275360] = fma(kw * y[4672], y[5792], ws[275360]);
+      ws[281408] = fma(kw * y[4672], y[5792], ws[281408]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1384,7 +1384,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52736] * w;
       out[3520] = fma(kw, y[5792], out[3520]);
       out[5792] = fma(kw, y[3520], out[5792]);
-      ws[275392] = fma(kw * y[3520], y[5792], ws[275392]);
+      ws[281440] = fma(kw * y[3520], y[5792], ws[281440]);
     }
     {
       double w = 0.5 * phi[5984];
@@ -1400,7 +1400,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52768] * w;
       out[2880] = fma(kw, y[5792], out[2880]);
       out[5792] = fma(kw, y[2880], out[5792]);
-      ws[275424] = fma(kw * y[2880], y[5792], ws[275424]);
+      ws[281472] = fma(kw * y[2880], y[5792], ws[281472]);
     }
     {
       double w = 0.5 * phi[5984];
@@ -1417,7 +1417,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52800] * w;
       out[2912] = fma(kw, y[5792], out[2912]);
       out[5792] = fma(kw, y[2912], out[5792]);
-      ws[275456] = fma(kw * y[2912], y[5792], ws[275456]);
+      ws[281504] = fma(kw * y[2912], y[5792], ws[281504]);
     }
     {
       double w = 1.0 * phi[5888];
@@ -1427,7 +1427,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52832] * w;
       out[2592] = fma(kw, y[5792], out[2592]);
       out[5792] = fma(kw, y[2592], out[5792]);
-      ws[275488] = fma(kw * y[2592], y[5792], ws[275488]);
+      ws[281536] = fma(kw * y[2592], y[5792], ws[281536]);
     }
     {
       double w = 1.0 * phi[5888];
@@ -1437,7 +1437,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52864] * w;
       out[2272] = fma(kw, y[5792], out[2272]);
       out[5792] = fma(kw, y[2272], out[5792]);
-      ws[275520] = fma(kw * y[2272], y[5792], ws[275520]);
+      ws[281568] = fma(kw * y[2272], y[5792], ws[281568]);
     }
     {
       double w = 2.0 * phi[5984];
@@ -1450,7 +1450,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52896] * w;
       out[3648] = fma(kw, y[5792], out[3648]);
       out[5792] = fma(kw, y[3648], out[5792]);
-      ws[275552] = fma(kw * y[3648], y[5792], ws[275552]);
+      ws[281600] = fma(kw * y[3648], y[5792], ws[281600]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1461,7 +1461,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52928] * w;
       out[3040] = fma(kw, y[5792], out[3040]);
       out[5792] = fma(kw, y[3040], out[5792]);
-      ws[275584] = fma(kw * y[3040], y[5792], ws[275584]);
+      ws[281632] = fma(kw * y[3040], y[5792], ws[281632]);
     }
     {
       double w = 1.0 * phi[5888];
@@ -1471,7 +1471,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52960] * w;
       out[2976] = fma(kw, y[5792], out[2976]);
       out[5792] = fma(kw, y[2976], out[5792]);
-      ws[275616] = fma(kw * y[2976], y[5792], ws[275616]);
+      ws[281664] = fma(kw * y[2976], y[5792], ws[281664]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1482,7 +1482,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[52992] * w;
       out[4032] = fma(kw, y[5792], out[4032]);
       out[5792] = fma(kw, y[4032], out[5792]);
-      ws[275648] = fma(kw * y[4032], y[5792], ws[275648]);
+      ws[281696] = fma(kw * y[4032], y[5792], ws[281696]);
     }
     {
       double w = 0.5 * phi[5888];
@@ -1496,7 +1496,7 @@ __device__ __noinline__ void adj_jtv_1_6(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53024] * w;
       out[4064] = fma(kw, y[5792], out[4064]);
       out[5792] = fma(kw, y[4064], out[5792]);
-      ws[275680] = fma(kw * y[4064], y[5792], ws[275680]);
+      ws[281728] = fma(kw * y[4064], y[5792], ws[281728]);
     }
 }
 __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int phioff, int outoff)
@@ -1516,7 +1516,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53056] * w;
       out[3072] = fma(kw, y[5792], out[3072]);
       out[5792] = fma(kw, y[3072], out[5792]);
-      ws[275712] = fma(kw * y[3072], y[5792], ws[275712]);
+      ws[281760] = fma(kw * y[3072], y[5792], ws[281760]);
     }
     {
       double w = 1.0 * phi[5888];
@@ -1525,7 +1525,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53088] * w;
       out[5216] = fma(kw, y[5792], out[5216]);
       out[5792] = fma(kw, y[5216], out[5792]);
-      ws[275744] = fma(kw * y[5216], y[5792], ws[275744]);
+      ws[281792] = fma(kw * y[5216], y[5792], ws[281792]);
     }
     {
       double w = 2.0 * phi[5632];
@@ -1534,7 +1534,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53120] * w;
       out[4800] = fma(kw, y[4800], out[4800]);
       out[4800] = fma(kw, y[4800], out[4800]);
-      ws[275776] = fma(kw * y[4800], y[4800], ws[275776]);
+      ws[281824] = fma(kw * y[4800], y[4800], ws[281824]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1545,7 +1545,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53152] * w;
       out[5888] = fma(kw, y[5952], out[5888]);
       out[5952] = fma(kw, y[5888], out[5952]);
-      ws[275808] = fma(kw * y[5888], y[5952], ws[275808]);
+      ws[281856] = fma(kw * y[5888], y[5952], ws[281856]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1556,7 +1556,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53184] * w;
       out[5632] = fma(kw, y[5952], out[5632]);
       out[5952] = fma(kw, y[5632], out[5952]);
-      ws[275840] = fma(kw * y[5632], y[5952], ws[275840]);
+      ws[281888] = fma(kw * y[5632], y[5952], ws[281888]);
     }
     {
       double w = 0.254 * phi[5984];
@@ -1573,7 +1573,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53216] * w;
       out[5408] = fma(kw, y[5952], out[5408]);
       out[5952] = fma(kw, y[5408], out[5952]);
-      ws[275872] = fma(kw * y[5408], y[5952], ws[275872]);
+      ws[281920] = fma(kw * y[5408], y[5952], ws[281920]);
     }
     {
       double w = 0.488 * phi[5984];
@@ -1593,7 +1593,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53248] * w;
       out[5120] = fma(kw, y[5952], out[5120]);
       out[5952] = fma(kw, y[5120], out[5952]);
-      ws[275904] = fma(kw * y[5120], y[5952], ws[275904]);
+      ws[281952] = fma(kw * y[5120], y[5952], ws[281952]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1605,7 +1605,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53280] * w;
       out[3008] = fma(kw, y[5952], out[3008]);
       out[5952] = fma(kw, y[3008], out[5952]);
-      ws[275936] = fma(kw * y[3008], y[5952], ws[275936]);
+      ws[281984] = fma(kw * y[3008], y[5952], ws[281984]);
     }
     {
       double w = 0.47 * phi[5760];
@@ -1620,7 +1620,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53312] * w;
       out[3200] = fma(kw, y[5952], out[3200]);
       out[5952] = fma(kw, y[3200], out[5952]);
-      ws[275968] = fma(kw * y[3200], y[5952], ws[275968]);
+      ws[282016] = fma(kw * y[3200], y[5952], ws[282016]);
     }
     {
       double w = 0.86 * phi[5984];
@@ -1635,7 +1635,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53344] * w;
       out[3328] = fma(kw, y[5952], out[3328]);
       out[5952] = fma(kw, y[3328], out[5952]);
-      ws[276000] = fma(kw * y[3328], y[5952], ws[276000]);
+      ws[282048] = fma(kw * y[3328], y[5952], ws[282048]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1650,7 +1650,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53376] * w;
       out[3360] = fma(kw, y[5952], out[3360]);
       out[5952] = fma(kw, y[3360], out[5952]);
-      ws[276032] = fma(kw * y[3360], y[5952], ws[276032]);
+      ws[282080] = fma(kw * y[3360], y[5952], ws[282080]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1665,7 +1665,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53408] * w;
       out[3296] = fma(kw, y[5952], out[3296]);
       out[5952] = fma(kw, y[3296], out[5952]);
-      ws[276064] = fma(kw * y[3296], y[5952], ws[276064]);
+      ws[282112] = fma(kw * y[3296], y[5952], ws[282112]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1680,7 +1680,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53440] * w;
       out[3104] = fma(kw, y[5952], out[3104]);
       out[5952] = fma(kw, y[3104], out[5952]);
-      ws[276096] = fma(kw * y[3104], y[5952], ws[276096]);
+      ws[282144] = fma(kw * y[3104], y[5952], ws[282144]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1695,7 +1695,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53472] * w;
       out[3264] = fma(kw, y[5952], out[3264]);
       out[5952] = fma(kw, y[3264], out[5952]);
-      ws[276128] = fma(kw * y[3264], y[5952], ws[276128]);
+      ws[282176] = fma(kw * y[3264], y[5952], ws[282176]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1711,7 +1711,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53504] * w;
       out[4288] = fma(kw, y[5952], out[4288]);
       out[5952] = fma(kw, y[4288], out[5952]);
-      ws[276160] = fma(kw * y[4288], y[5952], ws[276160]);
+      ws[282208] = fma(kw * y[4288], y[5952], ws[282208]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1728,7 +1728,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53536] * w;
       out[4160] = fma(kw, y[5952], out[4160]);
       out[5952] = fma(kw, y[4160], out[5952]);
-      ws[276192] = fma(kw * y[4160], y[5952], ws[276192]);
+      ws[282240] = fma(kw * y[4160], y[5952], ws[282240]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1740,7 +1740,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53568] * w;
       out[4192] = fma(kw, y[5952], out[4192]);
       out[5952] = fma(kw, y[4192], out[5952]);
-      ws[276224] = fma(kw * y[4192], y[5952], ws[276224]);
+      ws[282272] = fma(kw * y[4192], y[5952], ws[282272]);
     }
     {
       double w = 1.825 * phi[5920];
@@ -1755,7 +1755,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53600] * w;
       out[2624] = fma(kw, y[5952], out[2624]);
       out[5952] = fma(kw, y[2624], out[5952]);
-      ws[276256] = fma(kw * y[2624], y[5952], ws[276256]);
+      ws[282304] = fma(kw * y[2624], y[5952], ws[282304]);
     }
     {
       double w = 1.46 * phi[5920];
@@ -1767,7 +1767,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53632] * w;
       out[2656] = fma(kw, y[5952], out[2656]);
       out[5952] = fma(kw, y[2656], out[5952]);
-      ws[276288] = fma(kw * y[2656], y[5952], ws[276288]);
+      ws[282336] = fma(kw * y[2656], y[5952], ws[282336]);
     }
     {
       double w = 1.0 * phi[5888];
@@ -1777,7 +1777,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53664] * w;
       out[5792] = fma(kw, y[5952], out[5792]);
       out[5952] = fma(kw, y[5792], out[5952]);
-      ws[276320] = fma(kw * y[5792], y[5952], ws[276320]);
+      ws[282368] = fma(kw * y[5792], y[5952], ws[282368]);
     }
     {
       double w = 1.0 * phi[5632];
@@ -1787,7 +1787,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53696] * w;
       out[4800] = fma(kw, y[5952], out[4800]);
       out[5952] = fma(kw, y[4800], out[5952]);
-      ws[276352] = fma(kw * y[4800], y[5952], ws[276352]);
+      ws[282400] = fma(kw * y[4800], y[5952], ws[282400]);
     }
     {
       double w = 1.0 * phi[5792];
@@ -1798,7 +1798,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53728] * w;
       out[2848] = fma(kw, y[5952], out[2848]);
       out[5952] = fma(kw, y[2848], out[5952]);
-      ws[276384] = fma(kw * y[2848], y[5952], ws[276384]);
+      ws[282432] = fma(kw * y[2848], y[5952], ws[282432]);
     }
     {
       double w = 0.67 * phi[5984];
@@ -1810,7 +1810,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53760] * w;
       out[5152] = fma(kw, y[5952], out[5152]);
       out[5952] = fma(kw, y[5152], out[5952]);
-      ws[276416] = fma(kw * y[5152], y[5952], ws[276416]);
+      ws[282464] = fma(kw * y[5152], y[5952], ws[282464]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1821,7 +1821,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53792] * w;
       out[3776] = fma(kw, y[5952], out[3776]);
       out[5952] = fma(kw, y[3776], out[5952]);
-      ws[276448] = fma(kw * y[3776], y[5952], ws[276448]);
+      ws[282496] = fma(kw * y[3776], y[5952], ws[282496]);
     }
     {
       double w = 1.0 * phi[5856];
@@ -1833,7 +1833,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53824] * w;
       out[4672] = fma(kw, y[5952], out[4672]);
       out[5952] = fma(kw, y[4672], out[5952]);
-      ws[276480] = fma(kw * y[4672], y[5952], ws[276480]);
+      ws[282528] = fma(kw * y[4672], y[5952], ws[282528]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1845,7 +1845,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53856] * w;
       out[3520] = fma(kw, y[5952], out[3520]);
       out[5952] = fma(kw, y[3520], out[5952]);
-      ws[276512] = fma(kw * y[3520], y[5952], ws[276512]);
+      ws[282560] = fma(kw * y[3520], y[5952], ws[282560]);
     }
     {
       double w = 0.3 * phi[5984];
@@ -1860,7 +1860,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53888] * w;
       out[2880] = fma(kw, y[5952], out[2880]);
       out[5952] = fma(kw, y[2880], out[5952]);
-      ws[276544] = fma(kw * y[2880], y[5952], ws[276544]);
+      ws[282592] = fma(kw * y[2880], y[5952], ws[282592]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1876,7 +1876,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53920] * w;
       out[2912] = fma(kw, y[5952], out[2912]);
       out[5952] = fma(kw, y[2912], out[5952]);
-      ws[276576] = fma(kw * y[2912], y[5952], ws[276576]);
+      ws[282624] = fma(kw * y[2912], y[5952], ws[282624]);
     }
     {
       double w = 1.0 * phi[2272];
@@ -1886,7 +1886,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53952] * w;
       out[2592] = fma(kw, y[5952], out[2592]);
       out[5952] = fma(kw, y[2592], out[5952]);
-      ws[276608] = fma(kw * y[2592], y[5952], ws[276608]);
+      ws[282656] = fma(kw * y[2592], y[5952], ws[282656]);
     }
     {
       double w = 1.0 * phi[2688];
@@ -1896,7 +1896,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[53984] * w;
       out[2272] = fma(kw, y[5952], out[2272]);
       out[5952] = fma(kw, y[2272], out[5952]);
-      ws[276640] = fma(kw * y[2272], y[5952], ws[276640]);
+      ws[282688] = fma(kw * y[2272], y[5952], ws[282688]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1909,7 +1909,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54016] * w;
       out[3648] = fma(kw, y[5952], out[3648]);
       out[5952] = fma(kw, y[3648], out[5952]);
-      ws[276672] = fma(kw * y[3648], y[5952], ws[276672]);
+      ws[282720] = fma(kw * y[3648], y[5952], ws[282720]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1919,7 +1919,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54048] * w;
       out[3040] = fma(kw, y[5952], out[3040]);
       out[5952] = fma(kw, y[3040], out[5952]);
-      ws[276704] = fma(kw * y[3040], y[5952], ws[276704]);
+      ws[282752] = fma(kw * y[3040], y[5952], ws[282752]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1930,7 +1930,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54080] * w;
       out[2976] = fma(kw, y[5952], out[2976]);
       out[5952] = fma(kw, y[2976], out[5952]);
-      ws[276736] = fma(kw * y[2976], y[5952], ws[276736]);
+      ws[282784] = fma(kw * y[2976], y[5952], ws[282784]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1941,7 +1941,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54112] * w;
       out[4032] = fma(kw, y[5952], out[4032]);
       out[5952] = fma(kw, y[4032], out[5952]);
-      ws[276768] = fma(kw * y[4032], y[5952], ws[276768]);
+      ws[282816] = fma(kw * y[4032], y[5952], ws[282816]);
     }
     {
       double w = 2.0 * phi[5920];
@@ -1953,7 +1953,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54144] * w;
       out[4064] = fma(kw, y[5952], out[4064]);
       out[5952] = fma(kw, y[4064], out[5952]);
-      ws[276800] = fma(kw * y[4064], y[5952], ws[276800]);
+      ws[282848] = fma(kw * y[4064], y[5952], ws[282848]);
     }
     {
       double w = 2.0 * phi[5920];
@@ -1964,7 +1964,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54176] * w;
       out[3072] = fma(kw, y[5952], out[3072]);
       out[5952] = fma(kw, y[3072], out[5952]);
-      ws[276832] = fma(kw * y[3072], y[5952], ws[276832]);
+      ws[282880] = fma(kw * y[3072], y[5952], ws[282880]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -1974,7 +1974,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54208] * w;
       out[4032] = fma(kw, y[4032], out[4032]);
       out[4032] = fma(kw, y[4032], out[4032]);
-      ws[276864] = fma(kw * y[4032], y[4032], ws[276864]);
+      ws[282912] = fma(kw * y[4032], y[4032], ws[282912]);
     }
     {
       double w = 0.5 * phi[5984];
@@ -1988,7 +1988,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54240] * w;
       out[4032] = fma(kw, y[4064], out[4032]);
       out[4064] = fma(kw, y[4032], out[4064]);
-      ws[276896] = fma(kw * y[4032], y[4064], ws[276896]);
+      ws[282944] = fma(kw * y[4032], y[4064], ws[282944]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -2001,7 +2001,7 @@ __device__ __noinline__ void adj_jtv_1_7(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54272] * w;
       out[4064] = fma(kw, y[4064], out[4064]);
       out[4064] = fma(kw, y[4064], out[4064]);
-      ws[276928] = fma(kw * y[4064], y[4064], ws[276928]);
+      ws[282976] = fma(kw * y[4064], y[4064], ws[282976]);
     }
 }
 }  // namespace mech_cracmm2

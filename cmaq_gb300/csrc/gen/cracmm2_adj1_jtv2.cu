@@ -15,7 +15,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54304] * w;
       out[5216] = fma(kw, y[5952], out[5216]);
       out[5952] = fma(kw, y[5216], out[5952]);
-      ws[276960] = fma(kw * y[5216], y[5952], ws[276960]);
+      ws[283008] = fma(kw * y[5216], y[5952], ws[283008]);
     }
     {
       double w = 1.0 * phi[5632];
@@ -24,7 +24,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54336] * w;
       out[5216] = fma(kw, y[4800], out[5216]);
       out[4800] = fma(kw, y[5216], out[4800]);
-      ws[276992] = fma(kw * y[5216], y[4800], ws[276992]);
+      ws[283040] = fma(kw * y[5216], y[4800], ws[283040]);
     }
     {
       double w = -phi[5216];
@@ -32,7 +32,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54368] * w;
       out[5216] = fma(kw, y[5216], out[5216]);
       out[5216] = fma(kw, y[5216], out[5216]);
-      ws[277024] = fma(kw * y[5216], y[5216], ws[277024]);
+      ws[283072] = fma(kw * y[5216], y[5216], ws[283072]);
     }
     {
       double w = 0.96 * phi[4256];
@@ -46,7 +46,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54400] * w;
       out[3744] = fma(kw, y[4160], out[3744]);
       out[4160] = fma(kw, y[3744], out[4160]);
-      ws[277056] = fma(kw * y[3744], y[4160], ws[277056]);
+      ws[283104] = fma(kw * y[3744], y[4160], ws[283104]);
     }
     {
       double w = 0.96 * phi[4256];
@@ -60,7 +60,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54432] * w;
       out[3744] = fma(kw, y[4192], out[3744]);
       out[4192] = fma(kw, y[3744], out[4192]);
-      ws[277088] = fma(kw * y[3744], y[4192], ws[277088]);
+      ws[283136] = fma(kw * y[3744], y[4192], ws[283136]);
     }
     {
       double w = 0.96 * phi[4256];
@@ -75,7 +75,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54464] * w;
       out[3744] = fma(kw, y[4288], out[3744]);
       out[4288] = fma(kw, y[3744], out[4288]);
-      ws[277120] = fma(kw * y[3744], y[4288], ws[277120]);
+      ws[283168] = fma(kw * y[3744], y[4288], ws[283168]);
     }
     {
       double w = 0.96 * phi[4256];
@@ -89,7 +89,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54496] * w;
       out[3936] = fma(kw, y[4160], out[3936]);
       out[4160] = fma(kw, y[3936], out[4160]);
-      ws[277152] = fma(kw * y[3936], y[4160], ws[277152]);
+      ws[283200] = fma(kw * y[3936], y[4160], ws[283200]);
     }
     {
       double w = 0.96 * phi[4256];
@@ -103,7 +103,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54528] * w;
       out[3936] = fma(kw, y[4192], out[3936]);
       out[4192] = fma(kw, y[3936], out[4192]);
-      ws[277184] = fma(kw * y[3936], y[4192], ws[277184]);
+      ws[283232] = fma(kw * y[3936], y[4192], ws[283232]);
     }
     {
       double w = 0.96 * phi[4256];
@@ -118,7 +118,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54560] * w;
       out[3936] = fma(kw, y[4288], out[3936]);
       out[4288] = fma(kw, y[3936], out[4288]);
-      ws[277216] = fma(kw * y[3936], y[4288], ws[277216]);
+      ws[283264] = fma(kw * y[3936], y[4288], ws[283264]);
     }
     {
       double w = 0.96 * phi[4256];
@@ -132,7 +132,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54592] * w;
       out[3840] = fma(kw, y[4160], out[3840]);
       out[4160] = fma(kw, y[3840], out[4160]);
-      ws[277248] = fma(kw * y[3840], y[4160], ws[277248]);
+      ws[283296] = fma(kw * y[3840], y[4160], ws[283296]);
     }
     {
       double w = 0.96 * phi[4256];
@@ -146,7 +146,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54624] * w;
       out[3840] = fma(kw, y[4192], out[3840]);
       out[4192] = fma(kw, y[3840], out[4192]);
-      ws[277280] = fma(kw * y[3840], y[4192], ws[277280]);
+      ws[283328] = fma(kw * y[3840], y[4192], ws[283328]);
     }
     {
       double w = 0.96 * phi[4256];
@@ -161,7 +161,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54656] * w;
       out[3840] = fma(kw, y[4288], out[3840]);
       out[4288] = fma(kw, y[3840], out[4288]);
-      ws[277312] = fma(kw * y[3840], y[4288], ws[277312]);
+      ws[283360] = fma(kw * y[3840], y[4288], ws[283360]);
     }
     {
       double w = 0.96 * phi[4256];
@@ -175,7 +175,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54688] * w;
       out[3712] = fma(kw, y[4160], out[3712]);
       out[4160] = fma(kw, y[3712], out[4160]);
-      ws[277344] = fma(kw * y[3712], y[4160], ws[277344]);
+      ws[283392] = fma(kw * y[3712], y[4160], ws[283392]);
     }
     {
       double w = 0.96 * phi[4256];
@@ -189,7 +189,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54720] * w;
       out[3712] = fma(kw, y[4192], out[3712]);
       out[4192] = fma(kw, y[3712], out[4192]);
-      ws[277376] = fma(kw * y[3712], y[4192], ws[277376]);
+      ws[283424] = fma(kw * y[3712], y[4192], ws[283424]);
     }
     {
       double w = 0.96 * phi[4256];
@@ -204,7 +204,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54752] * w;
       out[3712] = fma(kw, y[4288], out[3712]);
       out[4288] = fma(kw, y[3712], out[4288]);
-      ws[277408] = fma(kw * y[3712], y[4288], ws[277408]);
+      ws[283456] = fma(kw * y[3712], y[4288], ws[283456]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -213,7 +213,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54784] * w;
       out[1376] = fma(kw, y[6016], out[1376]);
       out[6016] = fma(kw, y[1376], out[6016]);
-      ws[277440] = fma(kw * y[1376], y[6016], ws[277440]);
+      ws[283488] = fma(kw * y[1376], y[6016], ws[283488]);
     }
     {
       double w = 0.852 * phi[5632];
@@ -223,7 +223,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54816] * w;
       out[384] = fma(kw, y[6016], out[384]);
       out[6016] = fma(kw, y[384], out[6016]);
-      ws[277472] = fma(kw * y[384], y[6016], ws[277472]);
+      ws[283520] = fma(kw * y[384], y[6016], ws[283520]);
     }
     {
       double w = 1.0 * phi[5632];
@@ -233,7 +233,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54848] * w;
       out[416] = fma(kw, y[6016], out[416]);
       out[6016] = fma(kw, y[416], out[6016]);
-      ws[277504] = fma(kw * y[416], y[6016], ws[277504]);
+      ws[283552] = fma(kw * y[416], y[6016], ws[283552]);
     }
     {
       double w = 0.57 * phi[4672];
@@ -243,7 +243,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54880] * w;
       out[3552] = fma(kw, y[6016], out[3552]);
       out[6016] = fma(kw, y[3552], out[6016]);
-      ws[277536] = fma(kw * y[3552], y[6016], ws[277536]);
+      ws[283584] = fma(kw * y[3552], y[6016], ws[283584]);
     }
     {
       double w = 0.84 * phi[5664];
@@ -256,7 +256,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54912] * w;
       out[3552] = fma(kw, y[5184], out[3552]);
       out[5184] = fma(kw, y[3552], out[5184]);
-      ws[277568] = fma(kw * y[3552], y[5184], ws[277568]);
+      ws[283616] = fma(kw * y[3552], y[5184], ws[283616]);
     }
     {
       double w = 0.68 * phi[5856];
@@ -270,7 +270,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[54944] * w;
       out[3552] = fma(kw, y[5952], out[3552]);
       out[5952] = fma(kw, y[3552], out[5952]);
-      ws[277600] = fma(kw * y[3552], y[5952], ws[277600]);
+      ws[283648] = fma(kw * y[3552], y[5952], ws[283648]);
     }
     {
       double w = 0.667 * phi[3136];
@@ -281,7 +281,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55008] * w;
       out[1568] = fma(kw, y[6016], out[1568]);
       out[6016] = fma(kw, y[1568], out[6016]);
-      ws[277664] = fma(kw * y[1568], y[6016], ws[277664]);
+      ws[283712] = fma(kw * y[1568], y[6016], ws[283712]);
     }
     {
       double w = 0.968 * phi[5984];
@@ -295,7 +295,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55040] * w;
       out[3136] = fma(kw, y[5824], out[3136]);
       out[5824] = fma(kw, y[3136], out[5824]);
-      ws[277696] = fma(kw * y[3136], y[5824], ws[277696]);
+      ws[283744] = fma(kw * y[3136], y[5824], ws[283744]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -308,7 +308,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55072] * w;
       out[3136] = fma(kw, y[5952], out[3136]);
       out[5952] = fma(kw, y[3136], out[5952]);
-      ws[277728] = fma(kw * y[3136], y[5952], ws[277728]);
+      ws[283776] = fma(kw * y[3136], y[5952], ws[283776]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -317,7 +317,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55104] * w;
       out[3136] = fma(kw, y[5984], out[3136]);
       out[5984] = fma(kw, y[3136], out[5984]);
-      ws[277760] = fma(kw * y[3136], y[5984], ws[277760]);
+      ws[283808] = fma(kw * y[3136], y[5984], ws[283808]);
     }
     {
       double w = 0.32 * phi[5600];
@@ -333,7 +333,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55136] * w;
       out[3136] = fma(kw, y[5888], out[3136]);
       out[5888] = fma(kw, y[3136], out[5888]);
-      ws[277792] = fma(kw * y[3136], y[5888], ws[277792]);
+      ws[283840] = fma(kw * y[3136], y[5888], ws[283840]);
     }
     {
       double w = 0.7 * phi[5888];
@@ -349,7 +349,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55168] * w;
       out[3136] = fma(kw, y[5792], out[3136]);
       out[5792] = fma(kw, y[3136], out[5792]);
-      ws[277824] = fma(kw * y[3136], y[5792], ws[277824]);
+      ws[283872] = fma(kw * y[3136], y[5792], ws[283872]);
     }
     {
       double w = 0.62 * phi[3552];
@@ -363,7 +363,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55200] * w;
       out[1568] = fma(kw, y[5184], out[1568]);
       out[5184] = fma(kw, y[1568], out[5184]);
-      ws[277856] = fma(kw * y[1568], y[5184], ws[277856]);
+      ws[283904] = fma(kw * y[1568], y[5184], ws[283904]);
     }
     {
       double w = 0.9 * phi[4032];
@@ -374,7 +374,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55232] * w;
       out[1568] = fma(kw, y[5952], out[1568]);
       out[5952] = fma(kw, y[1568], out[5952]);
-      ws[277888] = fma(kw * y[1568], y[5952], ws[277888]);
+      ws[283936] = fma(kw * y[1568], y[5952], ws[283936]);
     }
     {
       double w = 0.49 * phi[5472];
@@ -385,7 +385,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55264] * w;
       out[3168] = fma(kw, y[6016], out[3168]);
       out[6016] = fma(kw, y[3168], out[6016]);
-      ws[277920] = fma(kw * y[3168], y[6016], ws[277920]);
+      ws[283968] = fma(kw * y[3168], y[6016], ws[283968]);
     }
     {
       double w = 0.08 * phi[5440];
@@ -398,7 +398,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55296] * w;
       out[1856] = fma(kw, y[5824], out[1856]);
       out[5824] = fma(kw, y[1856], out[5824]);
-      ws[277952] = fma(kw * y[1856], y[5824], ws[277952]);
+      ws[284000] = fma(kw * y[1856], y[5824], ws[284000]);
     }
     {
       double w = 0.6 * phi[5728];
@@ -411,7 +411,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55328] * w;
       out[1856] = fma(kw, y[5984], out[1856]);
       out[5984] = fma(kw, y[1856], out[5984]);
-      ws[277984] = fma(kw * y[1856], y[5984], ws[277984]);
+      ws[284032] = fma(kw * y[1856], y[5984], ws[284032]);
     }
     {
       double w = 0.65 * phi[5504];
@@ -425,7 +425,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55360] * w;
       out[4512] = fma(kw, y[6016], out[4512]);
       out[6016] = fma(kw, y[4512], out[6016]);
-      ws[278016] = fma(kw * y[4512], y[6016], ws[278016]);
+      ws[284064] = fma(kw * y[4512], y[6016], ws[284064]);
     }
     {
       double w = 0.02 * phi[6016];
@@ -435,7 +435,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55392] * w;
       out[3168] = fma(kw, y[5184], out[3168]);
       out[5184] = fma(kw, y[3168], out[5184]);
-      ws[278048] = fma(kw * y[3168], y[5184], ws[278048]);
+      ws[284096] = fma(kw * y[3168], y[5184], ws[284096]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -446,7 +446,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55424] * w;
       out[3168] = fma(kw, y[5952], out[3168]);
       out[5952] = fma(kw, y[3168], out[5952]);
-      ws[278080] = fma(kw * y[3168], y[5952], ws[278080]);
+      ws[284128] = fma(kw * y[3168], y[5952], ws[284128]);
     }
     {
       double w = 0.613 * phi[5344];
@@ -457,7 +457,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55456] * w;
       out[448] = fma(kw, y[6016], out[448]);
       out[6016] = fma(kw, y[448], out[6016]);
-      ws[278112] = fma(kw * y[448], y[6016], ws[278112]);
+      ws[284160] = fma(kw * y[448], y[6016], ws[284160]);
     }
     {
       double w = 1.0 * phi[1920];
@@ -466,7 +466,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55488] * w;
       out[1600] = fma(kw, y[5952], out[1600]);
       out[5952] = fma(kw, y[1600], out[5952]);
-      ws[278144] = fma(kw * y[1600], y[5952], ws[278144]);
+      ws[284192] = fma(kw * y[1600], y[5952], ws[284192]);
     }
     {
       double w = 1.0 * phi[4928];
@@ -475,7 +475,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55520] * w;
       out[1920] = fma(kw, y[5984], out[1920]);
       out[5984] = fma(kw, y[1920], out[5984]);
-      ws[278176] = fma(kw * y[1920], y[5984], ws[278176]);
+      ws[284224] = fma(kw * y[1920], y[5984], ws[284224]);
     }
     {
       double w = 1.0 * phi[5536];
@@ -485,7 +485,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55552] * w;
       out[1920] = fma(kw, y[5824], out[1920]);
       out[5824] = fma(kw, y[1920], out[5824]);
-      ws[278208] = fma(kw * y[1920], y[5824], ws[278208]);
+      ws[284256] = fma(kw * y[1920], y[5824], ws[284256]);
     }
     {
       double w = 1.0 * phi[5536];
@@ -495,7 +495,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55584] * w;
       out[1920] = fma(kw, y[5952], out[1920]);
       out[5952] = fma(kw, y[1920], out[5952]);
-      ws[278240] = fma(kw * y[1920], y[5952], ws[278240]);
+      ws[284288] = fma(kw * y[1920], y[5952], ws[284288]);
     }
     {
       double w = 0.982 * phi[5536];
@@ -505,7 +505,7 @@ __device__ __noinline__ void adj_jtv_1_8(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55616] * w;
       out[1600] = fma(kw, y[5184], out[1600]);
       out[5184] = fma(kw, y[1600], out[5184]);
-      ws[278272] = fma(kw * y[1600], y[5184], ws[278272]);
+      ws[284320] = fma(kw * y[1600], y[5184], ws[284320]);
     }
 }
 __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int phioff, int outoff)
@@ -520,7 +520,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55648] * w;
       out[1600] = fma(kw, y[6016], out[1600]);
       out[6016] = fma(kw, y[1600], out[6016]);
-      ws[278304] = fma(kw * y[1600], y[6016], ws[278304]);
+      ws[284352] = fma(kw * y[1600], y[6016], ws[284352]);
     }
     {
       double w = 1.0 * phi[4960];
@@ -529,7 +529,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55680] * w;
       out[2304] = fma(kw, y[5984], out[2304]);
       out[5984] = fma(kw, y[2304], out[5984]);
-      ws[278336] = fma(kw * y[2304], y[5984], ws[278336]);
+      ws[284384] = fma(kw * y[2304], y[5984], ws[284384]);
     }
     {
       double w = 1.0 * phi[5536];
@@ -538,7 +538,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55712] * w;
       out[2304] = fma(kw, y[5952], out[2304]);
       out[5952] = fma(kw, y[2304], out[5952]);
-      ws[278368] = fma(kw * y[2304], y[5952], ws[278368]);
+      ws[284416] = fma(kw * y[2304], y[5952], ws[284416]);
     }
     {
       double w = 0.247 * phi[4992];
@@ -549,28 +549,28 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[55744] * w;
       out[2304] = fma(kw, y[5824], out[2304]);
       out[5824] = fma(kw, y[2304], out[5824]);
-      ws[278400] = fma(kw * y[2304], y[5824], ws[278400]);
+      ws[284448] = fma(kw * y[2304], y[5824], ws[284448]);
     }
     {
       double w = 1.0 * phi[480];
       w = w - phi[5376];
       const double kw = ws[55776] * w;
       out[5376] = out[5376] + kw;
-      ws[278432] = fma(kw, y[5376], ws[278432]);
+      ws[284480] = fma(kw, y[5376], ws[284480]);
     }
     {
       double w = 1.0 * phi[480];
       w = w - phi[5248];
       const double kw = ws[55808] * w;
       out[5248] = out[5248] + kw;
-      ws[278464] = fma(kw, y[5248], ws[278464]);
+      ws[284512] = fma(kw, y[5248], ws[284512]);
     }
     {
       double w = 2.0 * phi[5024];
       w = w - phi[1024];
       const double kw = ws[55840] * w;
       out[1024] = out[1024] + kw;
-      ws[278496] = fma(kw, y[1024], ws[278496]);
+      ws[284544] = fma(kw, y[1024], ws[284544]);
     }
     {
       double w = 0.5 * phi[1184];
@@ -578,34 +578,34 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       w = w - phi[5920];
       const double kw = ws[55872] * w;
       out[5920] = out[5920] + kw;
-      ws[278528] = fma(kw, y[5920], ws[278528]);
+      ws[284576] = fma(kw, y[5920], ws[284576]);
     }
     {
       double w = -phi[5984];
       const double kw = ws[55904] * w;
       out[5984] = out[5984] + kw;
-      ws[278560] = fma(kw, y[5984], ws[278560]);
+      ws[284608] = fma(kw, y[5984], ws[284608]);
     }
     {
       double w = 1.0 * phi[5024];
       w = w - phi[5952];
       const double kw = ws[55936] * w;
       out[5952] = out[5952] + kw;
-      ws[278592] = fma(kw, y[5952], ws[278592]);
+      ws[284640] = fma(kw, y[5952], ws[284640]);
     }
     {
       double w = 1.0 * phi[1056];
       w = w - phi[1376];
       const double kw = ws[56000] * w;
       out[1376] = out[1376] + kw;
-      ws[278656] = fma(kw, y[1376], ws[278656]);
+      ws[284704] = fma(kw, y[1376], ws[284704]);
     }
     {
       double w = 1.0 * phi[0];
       w = w - phi[1056];
       const double kw = ws[56032] * w;
       out[1056] = out[1056] + kw;
-      ws[278688] = fma(kw, y[1056], ws[278688]);
+      ws[284736] = fma(kw, y[1056], ws[284736]);
     }
     {
       double w = 1.0 * phi[544];
@@ -614,14 +614,14 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56064] * w;
       out[1056] = fma(kw, y[512], out[1056]);
       out[512] = fma(kw, y[1056], out[512]);
-      ws[278720] = fma(kw * y[1056], y[512], ws[278720]);
+      ws[284768] = fma(kw * y[1056], y[512], ws[284768]);
     }
     {
       double w = 1.0 * phi[32];
       w = w - phi[1664];
       const double kw = ws[56096] * w;
       out[1664] = out[1664] + kw;
-      ws[278752] = fma(kw, y[1664], ws[278752]);
+      ws[284800] = fma(kw, y[1664], ws[284800]);
     }
     {
       double w = 1.0 * phi[64];
@@ -629,7 +629,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       w = w - phi[2208];
       const double kw = ws[56128] * w;
       out[2208] = out[2208] + kw;
-      ws[278784] = fma(kw, y[2208], ws[278784]);
+      ws[284832] = fma(kw, y[2208], ws[284832]);
     }
     {
       double w = 1.0 * phi[2368];
@@ -638,7 +638,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56160] * w;
       out[608] = fma(kw, y[6016], out[608]);
       out[6016] = fma(kw, y[608], out[6016]);
-      ws[278816] = fma(kw * y[608], y[6016], ws[278816]);
+      ws[284864] = fma(kw * y[608], y[6016], ws[284864]);
     }
     {
       double w = 1.0 * phi[2400];
@@ -647,7 +647,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56192] * w;
       out[640] = fma(kw, y[6016], out[640]);
       out[6016] = fma(kw, y[640], out[6016]);
-      ws[278848] = fma(kw * y[640], y[6016], ws[278848]);
+      ws[284896] = fma(kw * y[640], y[6016], ws[284896]);
     }
     {
       double w = 1.0 * phi[2432];
@@ -656,7 +656,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56224] * w;
       out[672] = fma(kw, y[6016], out[672]);
       out[6016] = fma(kw, y[672], out[6016]);
-      ws[278880] = fma(kw * y[672], y[6016], ws[278880]);
+      ws[284928] = fma(kw * y[672], y[6016], ws[284928]);
     }
     {
       double w = 1.0 * phi[2464];
@@ -665,7 +665,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56256] * w;
       out[704] = fma(kw, y[6016], out[704]);
       out[6016] = fma(kw, y[704], out[6016]);
-      ws[278912] = fma(kw * y[704], y[6016], ws[278912]);
+      ws[284960] = fma(kw * y[704], y[6016], ws[284960]);
     }
     {
       double w = 1.0 * phi[2496];
@@ -674,7 +674,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56288] * w;
       out[736] = fma(kw, y[6016], out[736]);
       out[6016] = fma(kw, y[736], out[6016]);
-      ws[278944] = fma(kw * y[736], y[6016], ws[278944]);
+      ws[284992] = fma(kw * y[736], y[6016], ws[284992]);
     }
     {
       double w = 1.0 * phi[2528];
@@ -683,7 +683,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56320] * w;
       out[768] = fma(kw, y[6016], out[768]);
       out[6016] = fma(kw, y[768], out[6016]);
-      ws[278976] = fma(kw * y[768], y[6016], ws[278976]);
+      ws[285024] = fma(kw * y[768], y[6016], ws[285024]);
     }
     {
       double w = 1.0 * phi[3904];
@@ -692,7 +692,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56352] * w;
       out[800] = fma(kw, y[6016], out[800]);
       out[6016] = fma(kw, y[800], out[6016]);
-      ws[279008] = fma(kw * y[800], y[6016], ws[279008]);
+      ws[285056] = fma(kw * y[800], y[6016], ws[285056]);
     }
     {
       double w = 0.72 * phi[1952];
@@ -703,7 +703,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56384] * w;
       out[2368] = fma(kw, y[5824], out[2368]);
       out[5824] = fma(kw, y[2368], out[5824]);
-      ws[279040] = fma(kw * y[2368], y[5824], ws[279040]);
+      ws[285088] = fma(kw * y[2368], y[5824], ws[285088]);
     }
     {
       double w = 0.72 * phi[1984];
@@ -714,7 +714,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56416] * w;
       out[2400] = fma(kw, y[5824], out[2400]);
       out[5824] = fma(kw, y[2400], out[5824]);
-      ws[279072] = fma(kw * y[2400], y[5824], ws[279072]);
+      ws[285120] = fma(kw * y[2400], y[5824], ws[285120]);
     }
     {
       double w = 0.72 * phi[2016];
@@ -725,7 +725,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56448] * w;
       out[2432] = fma(kw, y[5824], out[2432]);
       out[5824] = fma(kw, y[2432], out[5824]);
-      ws[279104] = fma(kw * y[2432], y[5824], ws[279104]);
+      ws[285152] = fma(kw * y[2432], y[5824], ws[285152]);
     }
     {
       double w = 0.72 * phi[2048];
@@ -736,7 +736,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56480] * w;
       out[2464] = fma(kw, y[5824], out[2464]);
       out[5824] = fma(kw, y[2464], out[5824]);
-      ws[279136] = fma(kw * y[2464], y[5824], ws[279136]);
+      ws[285184] = fma(kw * y[2464], y[5824], ws[285184]);
     }
     {
       double w = 0.72 * phi[2080];
@@ -747,7 +747,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56512] * w;
       out[2496] = fma(kw, y[5824], out[2496]);
       out[5824] = fma(kw, y[2496], out[5824]);
-      ws[279168] = fma(kw * y[2496], y[5824], ws[279168]);
+      ws[285216] = fma(kw * y[2496], y[5824], ws[285216]);
     }
     {
       double w = 0.72 * phi[2112];
@@ -758,7 +758,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56544] * w;
       out[2528] = fma(kw, y[5824], out[2528]);
       out[5824] = fma(kw, y[2528], out[5824]);
-      ws[279200] = fma(kw * y[2528], y[5824], ws[279200]);
+      ws[285248] = fma(kw * y[2528], y[5824], ws[285248]);
     }
     {
       double w = 0.74 * phi[2144];
@@ -769,7 +769,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56576] * w;
       out[3904] = fma(kw, y[5824], out[3904]);
       out[5824] = fma(kw, y[3904], out[5824]);
-      ws[279232] = fma(kw * y[3904], y[5824], ws[279232]);
+      ws[285280] = fma(kw * y[3904], y[5824], ws[285280]);
     }
     {
       double w = 1.0 * phi[1952];
@@ -779,7 +779,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56608] * w;
       out[2368] = fma(kw, y[5952], out[2368]);
       out[5952] = fma(kw, y[2368], out[5952]);
-      ws[279264] = fma(kw * y[2368], y[5952], ws[279264]);
+      ws[285312] = fma(kw * y[2368], y[5952], ws[285312]);
     }
     {
       double w = 1.0 * phi[1984];
@@ -789,7 +789,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56640] * w;
       out[2400] = fma(kw, y[5952], out[2400]);
       out[5952] = fma(kw, y[2400], out[5952]);
-      ws[279296] = fma(kw * y[2400], y[5952], ws[279296]);
+      ws[285344] = fma(kw * y[2400], y[5952], ws[285344]);
     }
     {
       double w = 1.0 * phi[2016];
@@ -799,7 +799,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56672] * w;
       out[2432] = fma(kw, y[5952], out[2432]);
       out[5952] = fma(kw, y[2432], out[5952]);
-      ws[279328] = fma(kw * y[2432], y[5952], ws[279328]);
+      ws[285376] = fma(kw * y[2432], y[5952], ws[285376]);
     }
     {
       double w = 1.0 * phi[2048];
@@ -809,7 +809,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56704] * w;
       out[2464] = fma(kw, y[5952], out[2464]);
       out[5952] = fma(kw, y[2464], out[5952]);
-      ws[279360] = fma(kw * y[2464], y[5952], ws[279360]);
+      ws[285408] = fma(kw * y[2464], y[5952], ws[285408]);
     }
     {
       double w = 1.0 * phi[2080];
@@ -819,7 +819,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56736] * w;
       out[2496] = fma(kw, y[5952], out[2496]);
       out[5952] = fma(kw, y[2496], out[5952]);
-      ws[279392] = fma(kw * y[2496], y[5952], ws[279392]);
+      ws[285440] = fma(kw * y[2496], y[5952], ws[285440]);
     }
     {
       double w = 1.0 * phi[2112];
@@ -829,7 +829,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56768] * w;
       out[2528] = fma(kw, y[5952], out[2528]);
       out[5952] = fma(kw, y[2528], out[5952]);
-      ws[279424] = fma(kw * y[2528], y[5952], ws[279424]);
+      ws[285472] = fma(kw * y[2528], y[5952], ws[285472]);
     }
     {
       double w = 1.0 * phi[2144];
@@ -839,7 +839,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56800] * w;
       out[3904] = fma(kw, y[5952], out[3904]);
       out[5952] = fma(kw, y[3904], out[5952]);
-      ws[279456] = fma(kw * y[3904], y[5952], ws[279456]);
+      ws[285504] = fma(kw * y[3904], y[5952], ws[285504]);
     }
     {
       double w = 1.0 * phi[5536];
@@ -848,7 +848,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56832] * w;
       out[2368] = fma(kw, y[5984], out[2368]);
       out[5984] = fma(kw, y[2368], out[5984]);
-      ws[279488] = fma(kw * y[2368], y[5984], ws[279488]);
+      ws[285536] = fma(kw * y[2368], y[5984], ws[285536]);
     }
     {
       double w = 1.0 * phi[5088];
@@ -857,7 +857,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56864] * w;
       out[2400] = fma(kw, y[5984], out[2400]);
       out[5984] = fma(kw, y[2400], out[5984]);
-      ws[279520] = fma(kw * y[2400], y[5984], ws[279520]);
+      ws[285568] = fma(kw * y[2400], y[5984], ws[285568]);
     }
     {
       double w = 1.0 * phi[4704];
@@ -866,7 +866,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56896] * w;
       out[2432] = fma(kw, y[5984], out[2432]);
       out[5984] = fma(kw, y[2432], out[5984]);
-      ws[279552] = fma(kw * y[2432], y[5984], ws[279552]);
+      ws[285600] = fma(kw * y[2432], y[5984], ws[285600]);
     }
     {
       double w = 1.0 * phi[4960];
@@ -875,7 +875,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56928] * w;
       out[2464] = fma(kw, y[5984], out[2464]);
       out[5984] = fma(kw, y[2464], out[5984]);
-      ws[279584] = fma(kw * y[2464], y[5984], ws[279584]);
+      ws[285632] = fma(kw * y[2464], y[5984], ws[285632]);
     }
     {
       double w = 1.0 * phi[4416];
@@ -884,7 +884,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56960] * w;
       out[2496] = fma(kw, y[5984], out[2496]);
       out[5984] = fma(kw, y[2496], out[5984]);
-      ws[279616] = fma(kw * y[2496], y[5984], ws[279616]);
+      ws[285664] = fma(kw * y[2496], y[5984], ws[285664]);
     }
     {
       double w = 1.0 * phi[4832];
@@ -893,7 +893,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[56992] * w;
       out[2528] = fma(kw, y[5984], out[2528]);
       out[5984] = fma(kw, y[2528], out[5984]);
-      ws[279648] = fma(kw * y[2528], y[5984], ws[279648]);
+      ws[285696] = fma(kw * y[2528], y[5984], ws[285696]);
     }
     {
       double w = 1.0 * phi[5728];
@@ -902,7 +902,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[57024] * w;
       out[3904] = fma(kw, y[5984], out[3904]);
       out[5984] = fma(kw, y[3904], out[5984]);
-      ws[279680] = fma(kw * y[3904], y[5984], ws[279680]);
+      ws[285728] = fma(kw * y[3904], y[5984], ws[285728]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -910,7 +910,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       w = w - phi[1952];
       const double kw = ws[57056] * w;
       out[1952] = out[1952] + kw;
-      ws[279712] = fma(kw, y[1952], ws[279712]);
+      ws[285760] = fma(kw, y[1952], ws[285760]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -918,7 +918,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       w = w - phi[1984];
       const double kw = ws[57088] * w;
       out[1984] = out[1984] + kw;
-      ws[279744] = fma(kw, y[1984], ws[279744]);
+      ws[285792] = fma(kw, y[1984], ws[285792]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -926,7 +926,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       w = w - phi[2016];
       const double kw = ws[57120] * w;
       out[2016] = out[2016] + kw;
-      ws[279776] = fma(kw, y[2016], ws[279776]);
+      ws[285824] = fma(kw, y[2016], ws[285824]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -934,7 +934,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       w = w - phi[2048];
       const double kw = ws[57152] * w;
       out[2048] = out[2048] + kw;
-      ws[279808] = fma(kw, y[2048], ws[279808]);
+      ws[285856] = fma(kw, y[2048], ws[285856]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -942,7 +942,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       w = w - phi[2080];
       const double kw = ws[57184] * w;
       out[2080] = out[2080] + kw;
-      ws[279840] = fma(kw, y[2080], ws[279840]);
+      ws[285888] = fma(kw, y[2080], ws[285888]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -950,7 +950,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       w = w - phi[2112];
       const double kw = ws[57216] * w;
       out[2112] = out[2112] + kw;
-      ws[279872] = fma(kw, y[2112], ws[279872]);
+      ws[285920] = fma(kw, y[2112], ws[285920]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -958,7 +958,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       w = w - phi[2144];
       const double kw = ws[57248] * w;
       out[2144] = out[2144] + kw;
-      ws[279904] = fma(kw, y[2144], ws[279904]);
+      ws[285952] = fma(kw, y[2144], ws[285952]);
     }
     {
       double w = 0.14 * phi[5088];
@@ -970,7 +970,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[57280] * w;
       out[1952] = fma(kw, y[5824], out[1952]);
       out[5824] = fma(kw, y[1952], out[5824]);
-      ws[279936] = fma(kw * y[1952], y[5824], ws[279936]);
+      ws[285984] = fma(kw * y[1952], y[5824], ws[285984]);
     }
     {
       double w = 0.14 * phi[4992];
@@ -982,7 +982,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[57312] * w;
       out[1984] = fma(kw, y[5824], out[1984]);
       out[5824] = fma(kw, y[1984], out[5824]);
-      ws[279968] = fma(kw * y[1984], y[5824], ws[279968]);
+      ws[286016] = fma(kw * y[1984], y[5824], ws[286016]);
     }
     {
       double w = 0.14 * phi[4960];
@@ -994,7 +994,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[57344] * w;
       out[2016] = fma(kw, y[5824], out[2016]);
       out[5824] = fma(kw, y[2016], out[5824]);
-      ws[280000] = fma(kw * y[2016], y[5824], ws[280000]);
+      ws[286048] = fma(kw * y[2016], y[5824], ws[286048]);
     }
     {
       double w = 0.14 * phi[4416];
@@ -1006,7 +1006,7 @@ __device__ __noinline__ void adj_jtv_1_9(double* __restrict__ ws, int yoff, int 
       const double kw = ws[57376] * w;
       out[2048] = fma(kw, y[5824], out[2048]);
       out[5824] = fma(kw, y[2048], out[5824]);
-      ws[280032] = fma(kw * y[2048], y[5824], ws[280032]);
+      ws[286080] = fma(kw * y[2048], y[5824], ws[286080]);
     }
 }
 __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int phioff, int outoff)
@@ -1024,7 +1024,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57408] * w;
       out[2080] = fma(kw, y[5824], out[2080]);
       out[5824] = fma(kw, y[2080], out[5824]);
-      ws[280064] = fma(kw * y[2080], y[5824], ws[280064]);
+      ws[286112] = fma(kw * y[2080], y[5824], ws[286112]);
     }
     {
       double w = 1.0 * phi[4832];
@@ -1035,7 +1035,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57440] * w;
       out[2112] = fma(kw, y[5824], out[2112]);
       out[5824] = fma(kw, y[2112], out[5824]);
-      ws[280096] = fma(kw * y[2112], y[5824], ws[280096]);
+      ws[286144] = fma(kw * y[2112], y[5824], ws[286144]);
     }
     {
       double w = 0.12 * phi[5440];
@@ -1047,7 +1047,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57472] * w;
       out[2144] = fma(kw, y[5824], out[2144]);
       out[5824] = fma(kw, y[2144], out[5824]);
-      ws[280128] = fma(kw * y[2144], y[5824], ws[280128]);
+      ws[286176] = fma(kw * y[2144], y[5824], ws[286176]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1058,7 +1058,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57504] * w;
       out[1952] = fma(kw, y[5952], out[1952]);
       out[5952] = fma(kw, y[1952], out[5952]);
-      ws[280160] = fma(kw * y[1952], y[5952], ws[280160]);
+      ws[286208] = fma(kw * y[1952], y[5952], ws[286208]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1069,7 +1069,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57536] * w;
       out[1984] = fma(kw, y[5952], out[1984]);
       out[5952] = fma(kw, y[1984], out[5952]);
-      ws[280192] = fma(kw * y[1984], y[5952], ws[280192]);
+      ws[286240] = fma(kw * y[1984], y[5952], ws[286240]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1080,7 +1080,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57568] * w;
       out[2016] = fma(kw, y[5952], out[2016]);
       out[5952] = fma(kw, y[2016], out[5952]);
-      ws[280224] = fma(kw * y[2016], y[5952], ws[280224]);
+      ws[286272] = fma(kw * y[2016], y[5952], ws[286272]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1091,7 +1091,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57600] * w;
       out[2048] = fma(kw, y[5952], out[2048]);
       out[5952] = fma(kw, y[2048], out[5952]);
-      ws[280256] = fma(kw * y[2048], y[5952], ws[280256]);
+      ws[286304] = fma(kw * y[2048], y[5952], ws[286304]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1102,7 +1102,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57632] * w;
       out[2080] = fma(kw, y[5952], out[2080]);
       out[5952] = fma(kw, y[2080], out[5952]);
-      ws[280288] = fma(kw * y[2080], y[5952], ws[280288]);
+      ws[286336] = fma(kw * y[2080], y[5952], ws[286336]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1113,7 +1113,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57664] * w;
       out[2112] = fma(kw, y[5952], out[2112]);
       out[5952] = fma(kw, y[2112], out[5952]);
-      ws[280320] = fma(kw * y[2112], y[5952], ws[280320]);
+      ws[286368] = fma(kw * y[2112], y[5952], ws[286368]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1124,7 +1124,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57696] * w;
       out[2144] = fma(kw, y[5952], out[2144]);
       out[5952] = fma(kw, y[2144], out[5952]);
-      ws[280352] = fma(kw * y[2144], y[5952], ws[280352]);
+      ws[286400] = fma(kw * y[2144], y[5952], ws[286400]);
     }
     {
       double w = 1.0 * phi[4992];
@@ -1133,7 +1133,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57728] * w;
       out[1952] = fma(kw, y[5984], out[1952]);
       out[5984] = fma(kw, y[1952], out[5984]);
-      ws[280384] = fma(kw * y[1952], y[5984], ws[280384]);
+      ws[286432] = fma(kw * y[1952], y[5984], ws[286432]);
     }
     {
       double w = 1.0 * phi[4960];
@@ -1142,7 +1142,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57760] * w;
       out[1984] = fma(kw, y[5984], out[1984]);
       out[5984] = fma(kw, y[1984], out[5984]);
-      ws[280416] = fma(kw * y[1984], y[5984], ws[280416]);
+      ws[286464] = fma(kw * y[1984], y[5984], ws[286464]);
     }
     {
       double w = 1.0 * phi[4416];
@@ -1151,7 +1151,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57792] * w;
       out[2016] = fma(kw, y[5984], out[2016]);
       out[5984] = fma(kw, y[2016], out[5984]);
-      ws[280448] = fma(kw * y[2016], y[5984], ws[280448]);
+      ws[286496] = fma(kw * y[2016], y[5984], ws[286496]);
     }
     {
       double w = 1.0 * phi[4832];
@@ -1160,7 +1160,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57824] * w;
       out[2048] = fma(kw, y[5984], out[2048]);
       out[5984] = fma(kw, y[2048], out[5984]);
-      ws[280480] = fma(kw * y[2048], y[5984], ws[280480]);
+      ws[286528] = fma(kw * y[2048], y[5984], ws[286528]);
     }
     {
       double w = 1.0 * phi[4832];
@@ -1169,7 +1169,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57856] * w;
       out[2080] = fma(kw, y[5984], out[2080]);
       out[5984] = fma(kw, y[2080], out[5984]);
-      ws[280512] = fma(kw * y[2080], y[5984], ws[280512]);
+      ws[286560] = fma(kw * y[2080], y[5984], ws[286560]);
     }
     {
       double w = 1.0 * phi[4832];
@@ -1178,7 +1178,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57888] * w;
       out[2112] = fma(kw, y[5984], out[2112]);
       out[5984] = fma(kw, y[2112], out[5984]);
-      ws[280544] = fma(kw * y[2112], y[5984], ws[280544]);
+      ws[286592] = fma(kw * y[2112], y[5984], ws[286592]);
     }
     {
       double w = 1.0 * phi[5088];
@@ -1187,7 +1187,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57920] * w;
       out[2144] = fma(kw, y[5984], out[2144]);
       out[5984] = fma(kw, y[2144], out[5984]);
-      ws[280576] = fma(kw * y[2144], y[5984], ws[280576]);
+      ws[286624] = fma(kw * y[2144], y[5984], ws[286624]);
     }
     {
       double w = 0.84 * phi[3392];
@@ -1198,7 +1198,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57952] * w;
       out[832] = fma(kw, y[6016], out[832]);
       out[6016] = fma(kw, y[832], out[6016]);
-      ws[280608] = fma(kw * y[832], y[6016], ws[280608]);
+      ws[286656] = fma(kw * y[832], y[6016], ws[286656]);
     }
     {
       double w = 0.0595 * phi[5312];
@@ -1209,7 +1209,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[57984] * w;
       out[3392] = fma(kw, y[5984], out[3392]);
       out[5984] = fma(kw, y[3392], out[5984]);
-      ws[280640] = fma(kw * y[3392], y[5984], ws[280640]);
+      ws[286688] = fma(kw * y[3392], y[5984], ws[286688]);
     }
     {
       double w = 0.0001 * phi[5312];
@@ -1227,7 +1227,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[58016] * w;
       out[3392] = fma(kw, y[5824], out[3392]);
       out[5824] = fma(kw, y[3392], out[5824]);
-      ws[280672] = fma(kw * y[3392], y[5824], ws[280672]);
+      ws[286720] = fma(kw * y[3392], y[5824], ws[286720]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1242,7 +1242,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[58048] * w;
       out[3392] = fma(kw, y[5952], out[3392]);
       out[5952] = fma(kw, y[3392], out[5952]);
-      ws[280704] = fma(kw * y[3392], y[5952], ws[280704]);
+      ws[286752] = fma(kw * y[3392], y[5952], ws[286752]);
     }
     {
       double w = 0.68 * phi[5856];
@@ -1258,7 +1258,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[58080] * w;
       out[3392] = fma(kw, y[5888], out[3392]);
       out[5888] = fma(kw, y[3392], out[5888]);
-      ws[280736] = fma(kw * y[3392], y[5888], ws[280736]);
+      ws[286784] = fma(kw * y[3392], y[5888], ws[286784]);
     }
     {
       double w = 0.7 * phi[5888];
@@ -1274,7 +1274,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[58112] * w;
       out[3392] = fma(kw, y[5792], out[3392]);
       out[5792] = fma(kw, y[3392], out[5792]);
-      ws[280768] = fma(kw * y[3392], y[5792], ws[280768]);
+      ws[286816] = fma(kw * y[3392], y[5792], ws[286816]);
     }
     {
       double w = 0.84 * phi[3424];
@@ -1285,7 +1285,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[58144] * w;
       out[864] = fma(kw, y[6016], out[864]);
       out[6016] = fma(kw, y[864], out[6016]);
-      ws[280800] = fma(kw * y[864], y[6016], ws[280800]);
+      ws[286848] = fma(kw * y[864], y[6016], ws[286848]);
     }
     {
       double w = 0.0595 * phi[5536];
@@ -1296,7 +1296,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[58176] * w;
       out[3424] = fma(kw, y[5984], out[3424]);
       out[5984] = fma(kw, y[3424], out[5984]);
-      ws[280832] = fma(kw * y[3424], y[5984], ws[280832]);
+      ws[286880] = fma(kw * y[3424], y[5984], ws[286880]);
     }
     {
       double w = 0.0001 * phi[5536];
@@ -1314,7 +1314,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[58208] * w;
       out[3424] = fma(kw, y[5824], out[3424]);
       out[5824] = fma(kw, y[3424], out[5824]);
-      ws[280864] = fma(kw * y[3424], y[5824], ws[280864]);
+      ws[286912] = fma(kw * y[3424], y[5824], ws[286912]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1329,7 +1329,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[58240] * w;
       out[3424] = fma(kw, y[5952], out[3424]);
       out[5952] = fma(kw, y[3424], out[5952]);
-      ws[280896] = fma(kw * y[3424], y[5952], ws[280896]);
+      ws[286944] = fma(kw * y[3424], y[5952], ws[286944]);
     }
     {
       double w = 0.68 * phi[5856];
@@ -1345,7 +1345,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[58272] * w;
       out[3424] = fma(kw, y[5888], out[3424]);
       out[5888] = fma(kw, y[3424], out[5888]);
-      ws[280928] = fma(kw * y[3424], y[5888], ws[280928]);
+      ws[286976] = fma(kw * y[3424], y[5888], ws[286976]);
     }
     {
       double w = 0.7 * phi[5888];
@@ -1361,7 +1361,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[58304] * w;
       out[3424] = fma(kw, y[5792], out[3424]);
       out[5792] = fma(kw, y[3424], out[5792]);
-      ws[280960] = fma(kw * y[3424], y[5792], ws[280960]);
+      ws[287008] = fma(kw * y[3424], y[5792], ws[287008]);
     }
     {
       double w = 0.84 * phi[3456];
@@ -1372,7 +1372,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[58336] * w;
       out[896] = fma(kw, y[6016], out[896]);
       out[6016] = fma(kw, y[896], out[6016]);
-      ws[280992] = fma(kw * y[896], y[6016], ws[280992]);
+      ws[287040] = fma(kw * y[896], y[6016], ws[287040]);
     }
     {
       double w = 0.0595 * phi[5536];
@@ -1383,7 +1383,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[58368] * w;
       out[3456] = fma(kw, y[5984], out[3456]);
       out[5984] = fma(kw, y[3456], out[5984]);
-      ws[281024] = fma(kw * y[3456], y[5984], ws[281024]);
+      ws[287072] = fma(kw * y[3456], y[5984], ws[287072]);
     }
     {
       double w = 0.0595 * phi[5312];
@@ -1400,7 +1400,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[58400] * w;
       out[3456] = fma(kw, y[5824], out[3456]);
       out[5824] = fma(kw, y[3456], out[5824]);
-      ws[281056] = fma(kw * y[3456], y[5824], ws[281056]);
+      ws[287104] = fma(kw * y[3456], y[5824], ws[287104]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -1415,7 +1415,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[58432] * w;
       out[3456] = fma(kw, y[5952], out[3456]);
       out[5952] = fma(kw, y[3456], out[5952]);
-      ws[281088] = fma(kw * y[3456], y[5952], ws[281088]);
+      ws[287136] = fma(kw * y[3456], y[5952], ws[287136]);
     }
     {
       double w = 0.68 * phi[5856];
@@ -1431,7 +1431,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[58464] * w;
       out[3456] = fma(kw, y[5888], out[3456]);
       out[5888] = fma(kw, y[3456], out[5888]);
-      ws[281120] = fma(kw * y[3456], y[5888], ws[281120]);
+      ws[287168] = fma(kw * y[3456], y[5888], ws[287168]);
     }
     {
       double w = 0.7 * phi[5888];
@@ -1447,7 +1447,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[58496] * w;
       out[3456] = fma(kw, y[5792], out[3456]);
       out[5792] = fma(kw, y[3456], out[5792]);
-      ws[281152] = fma(kw * y[3456], y[5792], ws[281152]);
+      ws[287200] = fma(kw * y[3456], y[5792], ws[287200]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -1465,7 +1465,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[58528] * w;
       out[4768] = fma(kw, y[6016], out[4768]);
       out[6016] = fma(kw, y[4768], out[6016]);
-      ws[281184] = fma(kw * y[4768], y[6016], ws[281184]);
+      ws[287232] = fma(kw * y[4768], y[6016], ws[287232]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -1496,7 +1496,7 @@ __device__ __noinline__ void adj_jtv_1_10(double* __restrict__ ws, int yoff, int
       const double kw = ws[58560] * w;
       out[4864] = fma(kw, y[6016], out[4864]);
       out[6016] = fma(kw, y[4864], out[6016]);
-      ws[281216] = fma(kw * y[4864], y[6016], ws[281216]);
+      ws[287264] = fma(kw * y[4864], y[6016], ws[287264]);
     }
 }
 __device__ __noinline__ void adj_jtv_1_11(double* __restrict__ ws, int yoff, int phioff, int outoff)
@@ -1537,7 +1537,7 @@ __device__ __noinline__ void adj_jtv_1_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58592] * w;
       out[4832] = fma(kw, y[6016], out[4832]);
       out[6016] = fma(kw, y[4832], out[6016]);
-      ws[281248] = fma(kw * y[4832], y[6016], ws[281248]);
+      ws[287296] = fma(kw * y[4832], y[6016], ws[287296]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -1558,7 +1558,7 @@ __device__ __noinline__ void adj_jtv_1_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58624] * w;
       out[4896] = fma(kw, y[6016], out[4896]);
       out[6016] = fma(kw, y[4896], out[6016]);
-      ws[281280] = fma(kw * y[4896], y[6016], ws[281280]);
+      ws[287328] = fma(kw * y[4896], y[6016], ws[287328]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -1591,7 +1591,7 @@ __device__ __noinline__ void adj_jtv_1_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58656] * w;
       out[4640] = fma(kw, y[6016], out[4640]);
       out[6016] = fma(kw, y[4640], out[6016]);
-      ws[281312] = fma(kw * y[4640], y[6016], ws[281312]);
+      ws[287360] = fma(kw * y[4640], y[6016], ws[287360]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -1627,7 +1627,7 @@ __device__ __noinline__ void adj_jtv_1_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58688] * w;
       out[4416] = fma(kw, y[6016], out[4416]);
       out[6016] = fma(kw, y[4416], out[6016]);
-      ws[281344] = fma(kw * y[4416], y[6016], ws[281344]);
+      ws[287392] = fma(kw * y[4416], y[6016], ws[287392]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -1656,7 +1656,7 @@ __device__ __noinline__ void adj_jtv_1_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58720] * w;
       out[4928] = fma(kw, y[6016], out[4928]);
       out[6016] = fma(kw, y[4928], out[6016]);
-      ws[281376] = fma(kw * y[4928], y[6016], ws[281376]);
+      ws[287424] = fma(kw * y[4928], y[6016], ws[287424]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -1691,7 +1691,7 @@ __device__ __noinline__ void adj_jtv_1_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58752] * w;
       out[4960] = fma(kw, y[6016], out[4960]);
       out[6016] = fma(kw, y[4960], out[6016]);
-      ws[281408] = fma(kw * y[4960], y[6016], ws[281408]);
+      ws[287456] = fma(kw * y[4960], y[6016], ws[287456]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -1724,7 +1724,7 @@ __device__ __noinline__ void adj_jtv_1_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58784] * w;
       out[4992] = fma(kw, y[6016], out[4992]);
       out[6016] = fma(kw, y[4992], out[6016]);
-      ws[281440] = fma(kw * y[4992], y[6016], ws[281440]);
+      ws[287488] = fma(kw * y[4992], y[6016], ws[287488]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -1760,7 +1760,7 @@ __device__ __noinline__ void adj_jtv_1_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58816] * w;
       out[4704] = fma(kw, y[6016], out[4704]);
       out[6016] = fma(kw, y[4704], out[6016]);
-      ws[281472] = fma(kw * y[4704], y[6016], ws[281472]);
+      ws[287520] = fma(kw * y[4704], y[6016], ws[287520]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -1796,7 +1796,7 @@ __device__ __noinline__ void adj_jtv_1_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58848] * w;
       out[5088] = fma(kw, y[6016], out[5088]);
       out[6016] = fma(kw, y[5088], out[6016]);
-      ws[281504] = fma(kw * y[5088], y[6016], ws[281504]);
+      ws[287552] = fma(kw * y[5088], y[6016], ws[287552]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -1831,7 +1831,7 @@ __device__ __noinline__ void adj_jtv_1_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58880] * w;
       out[5536] = fma(kw, y[6016], out[5536]);
       out[6016] = fma(kw, y[5536], out[6016]);
-      ws[281536] = fma(kw * y[5536], y[6016], ws[281536]);
+      ws[287584] = fma(kw * y[5536], y[6016], ws[287584]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -1864,7 +1864,7 @@ __device__ __noinline__ void adj_jtv_1_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58912] * w;
       out[5312] = fma(kw, y[6016], out[5312]);
       out[6016] = fma(kw, y[5312], out[6016]);
-      ws[281568] = fma(kw * y[5312], y[6016], ws[281568]);
+      ws[287616] = fma(kw * y[5312], y[6016], ws[287616]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -1898,7 +1898,7 @@ __device__ __noinline__ void adj_jtv_1_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58944] * w;
       out[4224] = fma(kw, y[6016], out[4224]);
       out[6016] = fma(kw, y[4224], out[6016]);
-      ws[281600] = fma(kw * y[4224], y[6016], ws[281600]);
+      ws[287648] = fma(kw * y[4224], y[6016], ws[287648]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -1929,7 +1929,7 @@ __device__ __noinline__ void adj_jtv_1_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[58976] * w;
       out[3968] = fma(kw, y[6016], out[3968]);
       out[6016] = fma(kw, y[3968], out[6016]);
-      ws[281632] = fma(kw * y[3968], y[6016], ws[281632]);
+      ws[287680] = fma(kw * y[3968], y[6016], ws[287680]);
     }
     {
       double w = 1.0 * phi[6016];
@@ -1950,7 +1950,7 @@ __device__ __noinline__ void adj_jtv_1_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[59008] * w;
       out[4608] = fma(kw, y[6016], out[4608]);
       out[6016] = fma(kw, y[4608], out[6016]);
-      ws[281664] = fma(kw * y[4608], y[6016], ws[281664]);
+      ws[287712] = fma(kw * y[4608], y[6016], ws[287712]);
     }
     {
       double w = 1.0 * phi[5888];
@@ -1959,7 +1959,7 @@ __device__ __noinline__ void adj_jtv_1_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[59040] * w;
       out[928] = fma(kw, y[6016], out[928]);
       out[6016] = fma(kw, y[928], out[6016]);
-      ws[281696] = fma(kw * y[928], y[6016], ws[281696]);
+      ws[287744] = fma(kw * y[928], y[6016], ws[287744]);
     }
     {
       double w = 1.0 * phi[960];
@@ -1967,7 +1967,7 @@ __device__ __noinline__ void adj_jtv_1_11(double* __restrict__ ws, int yoff, int
       w = w - phi[96];
       const double kw = ws[59072] * w;
       out[96] = out[96] + kw;
-      ws[281728] = fma(kw, y[96], ws[281728]);
+      ws[287776] = fma(kw, y[96], ws[287776]);
     }
     {
       double w = 1.0 * phi[960];
@@ -1975,7 +1975,7 @@ __device__ __noinline__ void adj_jtv_1_11(double* __restrict__ ws, int yoff, int
       w = w - phi[128];
       const double kw = ws[59104] * w;
       out[128] = out[128] + kw;
-      ws[281760] = fma(kw, y[128], ws[281760]);
+      ws[287808] = fma(kw, y[128], ws[287808]);
     }
     {
       double w = 1.0 * phi[3488];
@@ -1984,7 +1984,7 @@ __device__ __noinline__ void adj_jtv_1_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[59136] * w;
       out[992] = fma(kw, y[6016], out[992]);
       out[6016] = fma(kw, y[992], out[6016]);
-      ws[281792] = fma(kw * y[992], y[6016], ws[281792]);
+      ws[287840] = fma(kw * y[992], y[6016], ws[287840]);
     }
     {
       double w = 1.0 * phi[5536];
@@ -1993,7 +1993,7 @@ __device__ __noinline__ void adj_jtv_1_11(double* __restrict__ ws, int yoff, int
       const double kw = ws[59168] * w;
       out[3488] = fma(kw, y[5984], out[3488]);
       out[5984] = fma(kw, y[3488], out[5984]);
-      ws[281824] = fma(kw * y[3488], y[5984], ws[281824]);
+      ws[287872] = fma(kw * y[3488], y[5984], ws[287872]);
     }
 }
 }  // namespace mech_cracmm2

@@ -18,7 +18,7 @@ __device__ __noinline__ void adj_jtv_1_12(double* __restrict__ ws, int yoff, int
       const double kw = ws[59200] * w;
       out[3488] = fma(kw, y[5824], out[3488]);
       out[5824] = fma(kw, y[3488], out[5824]);
-      ws[281856] = fma(kw * y[3488], y[5824], ws[281856]);
+      ws[287904] = fma(kw * y[3488], y[5824], ws[287904]);
     }
     {
       double w = 1.0 * phi[5920];
@@ -30,7 +30,7 @@ __device__ __noinline__ void adj_jtv_1_12(double* __restrict__ ws, int yoff, int
       const double kw = ws[59232] * w;
       out[3488] = fma(kw, y[5952], out[3488]);
       out[5952] = fma(kw, y[3488], out[5952]);
-      ws[281888] = fma(kw * y[3488], y[5952], ws[281888]);
+      ws[287936] = fma(kw * y[3488], y[5952], ws[287936]);
     }
     {
       double w = 1.37 * phi[5984];
@@ -42,7 +42,7 @@ __device__ __noinline__ void adj_jtv_1_12(double* __restrict__ ws, int yoff, int
       const double kw = ws[59264] * w;
       out[3488] = fma(kw, y[5888], out[3488]);
       out[5888] = fma(kw, y[3488], out[5888]);
-      ws[281920] = fma(kw * y[3488], y[5888], ws[281920]);
+      ws[287968] = fma(kw * y[3488], y[5888], ws[287968]);
     }
     {
       double w = 1.0 * phi[5984];
@@ -55,7 +55,7 @@ __device__ __noinline__ void adj_jtv_1_12(double* __restrict__ ws, int yoff, int
       const double kw = ws[59296] * w;
       out[3488] = fma(kw, y[5792], out[3488]);
       out[5792] = fma(kw, y[3488], out[5792]);
-      ws[281952] = fma(kw * y[3488], y[5792], ws[281952]);
+      ws[288000] = fma(kw * y[3488], y[5792], ws[288000]);
     }
 }
 }  // namespace mech_cracmm2

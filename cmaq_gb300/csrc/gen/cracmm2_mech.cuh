@@ -26,7 +26,7 @@ constexpr int NRXNS = 531;
 constexpr int ISCHAN = 189;
 constexpr int NPHOTAB = 32;
 constexpr int NHETERO = 9;
-constexpr int WS_ELEMS = 6769;
+constexpr int WS_ELEMS = 6958;
 constexpr int OFF_Y = 0;
 constexpr int OFF_YP = 189;
 constexpr int OFF_YDOT = 378;
@@ -36,26 +36,27 @@ constexpr int OFF_K2 = 945;
 constexpr int OFF_K3 = 1134;
 constexpr int OFF_RKI = 1323;
 constexpr int OFF_RXRAT = 1854;
-constexpr int OFF_LU = 3295;
-constexpr int OFF_VDIAG = 6580;
+constexpr int OFF_LU = 3484;
+constexpr int OFF_VDIAG = 6769;
 constexpr int IARRAY_DAY = 3284;
 constexpr int IARRAY_NIGHT = 3199;
-constexpr int EBI_OFF_YC = 3295;
-constexpr int EBI_OFF_YC0 = 3484;
-constexpr int EBI_OFF_YCP = 3673;
-constexpr int EBI_OFF_PROD = 3862;
-constexpr int EBI_OFF_LOSS = 4051;
-constexpr int EBI_OFF_PNEG = 4240;
-constexpr int ADJ_WS_ELEMS = 8812;
-constexpr int ADJ_LAM = 6769;
-constexpr int ADJ_MU1 = 6958;
-constexpr int ADJ_MU2 = 7147;
-constexpr int ADJ_MU3 = 7336;
-constexpr int ADJ_PHI = 7525;
-constexpr int ADJ_TMP = 7714;
-constexpr int ADJ_EMIS = 7903;
-constexpr int ADJ_GE = 8092;
-constexpr int ADJ_GK = 8281;
+constexpr int EBI_OFF_YC = 3484;
+constexpr int EBI_OFF_YC0 = 3673;
+constexpr int EBI_OFF_YCP = 3862;
+constexpr int EBI_OFF_PROD = 4051;
+constexpr int EBI_OFF_LOSS = 4240;
+constexpr int EBI_OFF_PNEG = 4429;
+constexpr int ADJ_WS_ELEMS = 9001;
+constexpr int ADJ_LAM = 6958;
+constexpr int ADJ_MU1 = 7147;
+constexpr int ADJ_MU2 = 7336;
+constexpr int ADJ_MU3 = 7525;
+constexpr int ADJ_PHI = 7714;
+constexpr int ADJ_TMP = 7903;
+constexpr int ADJ_EMIS = 8092;
+constexpr int ADJ_GE = 8281;
+constexpr int ADJ_GK = 8470;
+constexpr int OFF_YAVE = 3295;
 constexpr double FLOPS_STEP_DAY = 79988.0;
 constexpr double FLOPS_STEP_NIGHT = 77148.0;
 extern __constant__ int c_inew2old[189];
@@ -97,6 +98,32 @@ __device__ void jacdecomp_0_23(double* __restrict__ ws, double gdtinv);
 __device__ void jacdecomp_0_24(double* __restrict__ ws, double gdtinv);
 __device__ void jacdecomp_0_25(double* __restrict__ ws, double gdtinv);
 __device__ void jacdecomp_0_26(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_27(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_28(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_29(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_30(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_31(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_32(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_33(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_34(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_35(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_36(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_37(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_38(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_39(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_40(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_41(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_42(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_43(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_44(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_45(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_46(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_47(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_48(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_49(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_50(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_51(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_0_52(double* __restrict__ ws, double gdtinv);
 __device__ void solve_0_0(double* __restrict__ ws, int rhs);
 __device__ void solve_0_1(double* __restrict__ ws, int rhs);
 __device__ void solve_0_2(double* __restrict__ ws, int rhs);
@@ -129,6 +156,32 @@ __device__ void jacdecomp_1_23(double* __restrict__ ws, double gdtinv);
 __device__ void jacdecomp_1_24(double* __restrict__ ws, double gdtinv);
 __device__ void jacdecomp_1_25(double* __restrict__ ws, double gdtinv);
 __device__ void jacdecomp_1_26(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_27(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_28(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_29(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_30(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_31(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_32(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_33(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_34(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_35(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_36(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_37(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_38(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_39(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_40(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_41(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_42(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_43(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_44(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_45(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_46(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_47(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_48(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_49(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_50(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_51(double* __restrict__ ws, double gdtinv);
+__device__ void jacdecomp_1_52(double* __restrict__ ws, double gdtinv);
 __device__ void solve_1_0(double* __restrict__ ws, int rhs);
 __device__ void solve_1_1(double* __restrict__ ws, int rhs);
 __device__ void solve_1_2(double* __restrict__ ws, int rhs);
@@ -234,6 +287,46 @@ __device__ void adj_hess3_1_27(double* __restrict__ ws);
 __device__ void adj_hess3_1_28(double* __restrict__ ws);
 __device__ void adj_hess3_1_29(double* __restrict__ ws);
 __device__ void adj_hess3_1_30(double* __restrict__ ws);
+__device__ void ddm_jv_0_0(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_0_1(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_0_2(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_0_3(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_0_4(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_0_5(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_0_6(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_0_7(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_0_8(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_0_9(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_src_0_0(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_0_1(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_0_2(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_0_3(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_0_4(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_0_5(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_0_6(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_0_7(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_0_8(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_0_9(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_jv_1_0(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_1_1(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_1_2(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_1_3(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_1_4(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_1_5(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_1_6(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_1_7(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_1_8(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_jv_1_9(double* __restrict__ ws, int yoff, int voff, int outoff);
+__device__ void ddm_src_1_0(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_1_1(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_1_2(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_1_3(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_1_4(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_1_5(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_1_6(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_1_7(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_1_8(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+__device__ void ddm_src_1_9(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
 constexpr int EBI_N_EBISP = 176;
 constexpr double EBI_DELTAT = 2.5;
 constexpr int EBI_NEBITER = 1000;
@@ -276,6 +369,32 @@ __device__ __forceinline__ void jacdecomp_0(double* __restrict__ ws, double gdti
     jacdecomp_0_24(ws, gdtinv);
     jacdecomp_0_25(ws, gdtinv);
     jacdecomp_0_26(ws, gdtinv);
+    jacdecomp_0_27(ws, gdtinv);
+    jacdecomp_0_28(ws, gdtinv);
+    jacdecomp_0_29(ws, gdtinv);
+    jacdecomp_0_30(ws, gdtinv);
+    jacdecomp_0_31(ws, gdtinv);
+    jacdecomp_0_32(ws, gdtinv);
+    jacdecomp_0_33(ws, gdtinv);
+    jacdecomp_0_34(ws, gdtinv);
+    jacdecomp_0_35(ws, gdtinv);
+    jacdecomp_0_36(ws, gdtinv);
+    jacdecomp_0_37(ws, gdtinv);
+    jacdecomp_0_38(ws, gdtinv);
+    jacdecomp_0_39(ws, gdtinv);
+    jacdecomp_0_40(ws, gdtinv);
+    jacdecomp_0_41(ws, gdtinv);
+    jacdecomp_0_42(ws, gdtinv);
+    jacdecomp_0_43(ws, gdtinv);
+    jacdecomp_0_44(ws, gdtinv);
+    jacdecomp_0_45(ws, gdtinv);
+    jacdecomp_0_46(ws, gdtinv);
+    jacdecomp_0_47(ws, gdtinv);
+    jacdecomp_0_48(ws, gdtinv);
+    jacdecomp_0_49(ws, gdtinv);
+    jacdecomp_0_50(ws, gdtinv);
+    jacdecomp_0_51(ws, gdtinv);
+    jacdecomp_0_52(ws, gdtinv);
 }
 __device__ __forceinline__ void jacdecomp_0_sync(double* __restrict__ ws, double gdtinv, bool go)
 {
@@ -333,6 +452,58 @@ __device__ __forceinline__ void jacdecomp_0_sync(double* __restrict__ ws, double
     __syncthreads();
     if (go) jacdecomp_0_26(ws, gdtinv);
     __syncthreads();
+    if (go) jacdecomp_0_27(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_28(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_29(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_30(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_31(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_32(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_33(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_34(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_35(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_36(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_37(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_38(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_39(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_40(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_41(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_42(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_43(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_44(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_45(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_46(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_47(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_48(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_49(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_50(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_51(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_0_52(ws, gdtinv);
+    __syncthreads();
 }
 __device__ __forceinline__ void solve_0(double* __restrict__ ws, int rhs)
 {
@@ -384,6 +555,32 @@ __device__ __forceinline__ void jacdecomp_1(double* __restrict__ ws, double gdti
     jacdecomp_1_24(ws, gdtinv);
     jacdecomp_1_25(ws, gdtinv);
     jacdecomp_1_26(ws, gdtinv);
+    jacdecomp_1_27(ws, gdtinv);
+    jacdecomp_1_28(ws, gdtinv);
+    jacdecomp_1_29(ws, gdtinv);
+    jacdecomp_1_30(ws, gdtinv);
+    jacdecomp_1_31(ws, gdtinv);
+    jacdecomp_1_32(ws, gdtinv);
+    jacdecomp_1_33(ws, gdtinv);
+    jacdecomp_1_34(ws, gdtinv);
+    jacdecomp_1_35(ws, gdtinv);
+    jacdecomp_1_36(ws, gdtinv);
+    jacdecomp_1_37(ws, gdtinv);
+    jacdecomp_1_38(ws, gdtinv);
+    jacdecomp_1_39(ws, gdtinv);
+    jacdecomp_1_40(ws, gdtinv);
+    jacdecomp_1_41(ws, gdtinv);
+    jacdecomp_1_42(ws, gdtinv);
+    jacdecomp_1_43(ws, gdtinv);
+    jacdecomp_1_44(ws, gdtinv);
+    jacdecomp_1_45(ws, gdtinv);
+    jacdecomp_1_46(ws, gdtinv);
+    jacdecomp_1_47(ws, gdtinv);
+    jacdecomp_1_48(ws, gdtinv);
+    jacdecomp_1_49(ws, gdtinv);
+    jacdecomp_1_50(ws, gdtinv);
+    jacdecomp_1_51(ws, gdtinv);
+    jacdecomp_1_52(ws, gdtinv);
 }
 __device__ __forceinline__ void jacdecomp_1_sync(double* __restrict__ ws, double gdtinv, bool go)
 {
@@ -440,6 +637,58 @@ __device__ __forceinline__ void jacdecomp_1_sync(double* __restrict__ ws, double
     if (go) jacdecomp_1_25(ws, gdtinv);
     __syncthreads();
     if (go) jacdecomp_1_26(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_27(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_28(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_29(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_30(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_31(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_32(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_33(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_34(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_35(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_36(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_37(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_38(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_39(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_40(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_41(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_42(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_43(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_44(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_45(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_46(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_47(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_48(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_49(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_50(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_51(ws, gdtinv);
+    __syncthreads();
+    if (go) jacdecomp_1_52(ws, gdtinv);
     __syncthreads();
 }
 __device__ __forceinline__ void solve_1(double* __restrict__ ws, int rhs)
@@ -581,6 +830,58 @@ __device__ __forceinline__ void adj_hess3_1(double* __restrict__ ws)
     adj_hess3_1_29(ws);
     adj_hess3_1_30(ws);
 }
+__device__ __forceinline__ void ddm_jv_0(double* __restrict__ ws, int yoff, int voff, int outoff)
+{
+    ddm_jv_0_0(ws, yoff, voff, outoff);
+    ddm_jv_0_1(ws, yoff, voff, outoff);
+    ddm_jv_0_2(ws, yoff, voff, outoff);
+    ddm_jv_0_3(ws, yoff, voff, outoff);
+    ddm_jv_0_4(ws, yoff, voff, outoff);
+    ddm_jv_0_5(ws, yoff, voff, outoff);
+    ddm_jv_0_6(ws, yoff, voff, outoff);
+    ddm_jv_0_7(ws, yoff, voff, outoff);
+    ddm_jv_0_8(ws, yoff, voff, outoff);
+    ddm_jv_0_9(ws, yoff, voff, outoff);
+}
+__device__ __forceinline__ void ddm_src_0(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff)
+{
+    ddm_src_0_0(ws, mask, scale, outoff);
+    ddm_src_0_1(ws, mask, scale, outoff);
+    ddm_src_0_2(ws, mask, scale, outoff);
+    ddm_src_0_3(ws, mask, scale, outoff);
+    ddm_src_0_4(ws, mask, scale, outoff);
+    ddm_src_0_5(ws, mask, scale, outoff);
+    ddm_src_0_6(ws, mask, scale, outoff);
+    ddm_src_0_7(ws, mask, scale, outoff);
+    ddm_src_0_8(ws, mask, scale, outoff);
+    ddm_src_0_9(ws, mask, scale, outoff);
+}
+__device__ __forceinline__ void ddm_jv_1(double* __restrict__ ws, int yoff, int voff, int outoff)
+{
+    ddm_jv_1_0(ws, yoff, voff, outoff);
+    ddm_jv_1_1(ws, yoff, voff, outoff);
+    ddm_jv_1_2(ws, yoff, voff, outoff);
+    ddm_jv_1_3(ws, yoff, voff, outoff);
+    ddm_jv_1_4(ws, yoff, voff, outoff);
+    ddm_jv_1_5(ws, yoff, voff, outoff);
+    ddm_jv_1_6(ws, yoff, voff, outoff);
+    ddm_jv_1_7(ws, yoff, voff, outoff);
+    ddm_jv_1_8(ws, yoff, voff, outoff);
+    ddm_jv_1_9(ws, yoff, voff, outoff);
+}
+__device__ __forceinline__ void ddm_src_1(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff)
+{
+    ddm_src_1_0(ws, mask, scale, outoff);
+    ddm_src_1_1(ws, mask, scale, outoff);
+    ddm_src_1_2(ws, mask, scale, outoff);
+    ddm_src_1_3(ws, mask, scale, outoff);
+    ddm_src_1_4(ws, mask, scale, outoff);
+    ddm_src_1_5(ws, mask, scale, outoff);
+    ddm_src_1_6(ws, mask, scale, outoff);
+    ddm_src_1_7(ws, mask, scale, outoff);
+    ddm_src_1_8(ws, mask, scale, outoff);
+    ddm_src_1_9(ws, mask, scale, outoff);
+}
 struct Traits {
     static constexpr int NSPEC = mech_cracmm2::NSPEC;
     static constexpr int NRXNS = mech_cracmm2::NRXNS;
@@ -617,6 +918,7 @@ struct Traits {
     static constexpr int ADJ_EMIS = mech_cracmm2::ADJ_EMIS;
     static constexpr int ADJ_GE = mech_cracmm2::ADJ_GE;
     static constexpr int ADJ_GK = mech_cracmm2::ADJ_GK;
+    static constexpr int OFF_YAVE = mech_cracmm2::OFF_YAVE;
     static constexpr const char* name() { return mech_cracmm2::NAME; }
     static __device__ __forceinline__ int iold2new(int s) { return mech_cracmm2::c_iold2new[s]; }
     static __device__ __forceinline__ int inew2old(int i) { return mech_cracmm2::c_inew2old[i]; }
@@ -629,6 +931,8 @@ struct Traits {
     static __device__ __forceinline__ void solve_t_0(double* ws, int r) { mech_cracmm2::solve_t_0(ws, r); }
     static __device__ __forceinline__ void adj_jtv_0(double* ws, int y, int phi, int out) { mech_cracmm2::adj_jtv_0(ws, y, phi, out); }
     static __device__ __forceinline__ void adj_hess3_0(double* ws) { mech_cracmm2::adj_hess3_0(ws); }
+    static __device__ __forceinline__ void ddm_jv_0(double* ws, int y, int v, int out) { mech_cracmm2::ddm_jv_0(ws, y, v, out); }
+    static __device__ __forceinline__ void ddm_src_0(double* ws, const unsigned char* mk, double sc, int out) { mech_cracmm2::ddm_src_0(ws, mk, sc, out); }
     static __device__ __forceinline__ void feval_1(double* ws, int s, int t) { mech_cracmm2::feval_1(ws, s, t); }
     static __device__ __forceinline__ void explic_1(double* ws) { mech_cracmm2::explic_1(ws); }
     static __device__ __forceinline__ void jacdecomp_1(double* ws, double g) { mech_cracmm2::jacdecomp_1(ws, g); }
@@ -638,6 +942,8 @@ struct Traits {
     static __device__ __forceinline__ void solve_t_1(double* ws, int r) { mech_cracmm2::solve_t_1(ws, r); }
     static __device__ __forceinline__ void adj_jtv_1(double* ws, int y, int phi, int out) { mech_cracmm2::adj_jtv_1(ws, y, phi, out); }
     static __device__ __forceinline__ void adj_hess3_1(double* ws) { mech_cracmm2::adj_hess3_1(ws); }
+    static __device__ __forceinline__ void ddm_jv_1(double* ws, int y, int v, int out) { mech_cracmm2::ddm_jv_1(ws, y, v, out); }
+    static __device__ __forceinline__ void ddm_src_1(double* ws, const unsigned char* mk, double sc, int out) { mech_cracmm2::ddm_src_1(ws, mk, sc, out); }
     static constexpr int EBI_N_EBISP = mech_cracmm2::EBI_N_EBISP;
     static constexpr int EBI_NEBITER = mech_cracmm2::EBI_NEBITER;
     static constexpr int EBI_NPNEG = mech_cracmm2::EBI_NPNEG;

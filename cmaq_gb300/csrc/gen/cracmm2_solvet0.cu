@@ -5,8 +5,8 @@
 namespace mech_cracmm2 {
 __device__ __noinline__ void solve_t_0_0(double* __restrict__ ws, int rhs)
 {
-    const double* __restrict__ lu = ws + 105440;
-    const double* __restrict__ vd = ws + 210560;
+    const double* __restrict__ lu = ws + 111488;
+    const double* __restrict__ vd = ws + 216608;
     double* __restrict__ b = ws + rhs * 32;
     (void)vd;
     {
@@ -1310,8 +1310,8 @@ __device__ __noinline__ void solve_t_0_0(double* __restrict__ ws, int rhs)
 }
 __device__ __noinline__ void solve_t_0_1(double* __restrict__ ws, int rhs)
 {
-    const double* __restrict__ lu = ws + 105440;
-    const double* __restrict__ vd = ws + 210560;
+    const double* __restrict__ lu = ws + 111488;
+    const double* __restrict__ vd = ws + 216608;
     double* __restrict__ b = ws + rhs * 32;
     (void)vd;
     {
@@ -2183,8 +2183,8 @@ __device__ __noinline__ void solve_t_0_1(double* __restrict__ ws, int rhs)
 }
 __device__ __noinline__ void solve_t_0_2(double* __restrict__ ws, int rhs)
 {
-    const double* __restrict__ lu = ws + 105440;
-    const double* __restrict__ vd = ws + 210560;
+    const double* __restrict__ lu = ws + 111488;
+    const double* __restrict__ vd = ws + 216608;
     double* __restrict__ b = ws + rhs * 32;
     (void)vd;
     {
@@ -3100,8 +3100,8 @@ __device__ __noinline__ void solve_t_0_2(double* __restrict__ ws, int rhs)
 }
 __device__ __noinline__ void solve_t_0_3(double* __restrict__ ws, int rhs)
 {
-    const double* __restrict__ lu = ws + 105440;
-    const double* __restrict__ vd = ws + 210560;
+    const double* __restrict__ lu = ws + 111488;
+    const double* __restrict__ vd = ws + 216608;
     double* __restrict__ b = ws + rhs * 32;
     (void)vd;
     {
@@ -4077,8 +4077,8 @@ __device__ __noinline__ void solve_t_0_3(double* __restrict__ ws, int rhs)
 }
 __device__ __noinline__ void solve_t_0_4(double* __restrict__ ws, int rhs)
 {
-    const double* __restrict__ lu = ws + 105440;
-    const double* __restrict__ vd = ws + 210560;
+    const double* __restrict__ lu = ws + 111488;
+    const double* __restrict__ vd = ws + 216608;
     double* __restrict__ b = ws + rhs * 32;
     (void)vd;
     {

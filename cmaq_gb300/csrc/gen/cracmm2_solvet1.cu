@@ -5,8 +5,8 @@
 namespace mech_cracmm2 {
 __device__ __noinline__ void solve_t_1_0(double* __restrict__ ws, int rhs)
 {
-    const double* __restrict__ lu = ws + 105440;
-    const double* __restrict__ vd = ws + 210560;
+    const double* __restrict__ lu = ws + 111488;
+    const double* __restrict__ vd = ws + 216608;
     double* __restrict__ b = ws + rhs * 32;
     (void)vd;
     {
@@ -1296,8 +1296,8 @@ __device__ __noinline__ void solve_t_1_0(double* __restrict__ ws, int rhs)
 }
 __device__ __noinline__ void solve_t_1_1(double* __restrict__ ws, int rhs)
 {
-    const double* __restrict__ lu = ws + 105440;
-    const double* __restrict__ vd = ws + 210560;
+    const double* __restrict__ lu = ws + 111488;
+    const double* __restrict__ vd = ws + 216608;
     double* __restrict__ b = ws + rhs * 32;
     (void)vd;
     {
@@ -2184,8 +2184,8 @@ __device__ __noinline__ void solve_t_1_1(double* __restrict__ ws, int rhs)
 }
 __device__ __noinline__ void solve_t_1_2(double* __restrict__ ws, int rhs)
 {
-    const double* __restrict__ lu = ws + 105440;
-    const double* __restrict__ vd = ws + 210560;
+    const double* __restrict__ lu = ws + 111488;
+    const double* __restrict__ vd = ws + 216608;
     double* __restrict__ b = ws + rhs * 32;
     (void)vd;
     {
@@ -3112,8 +3112,8 @@ __device__ __noinline__ void solve_t_1_2(double* __restrict__ ws, int rhs)
 }
 __device__ __noinline__ void solve_t_1_3(double* __restrict__ ws, int rhs)
 {
-    const double* __restrict__ lu = ws + 105440;
-    const double* __restrict__ vd = ws + 210560;
+    const double* __restrict__ lu = ws + 111488;
+    const double* __restrict__ vd = ws + 216608;
     double* __restrict__ b = ws + rhs * 32;
     (void)vd;
     {
@@ -4120,8 +4120,8 @@ __device__ __noinline__ void solve_t_1_3(double* __restrict__ ws, int rhs)
 }
 __device__ __noinline__ void solve_t_1_4(double* __restrict__ ws, int rhs)
 {
-    const double* __restrict__ lu = ws + 105440;
-    const double* __restrict__ vd = ws + 210560;
+    const double* __restrict__ lu = ws + 111488;
+    const double* __restrict__ vd = ws + 216608;
     double* __restrict__ b = ws + rhs * 32;
     (void)vd;
     {

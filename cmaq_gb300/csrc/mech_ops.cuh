@@ -7,6 +7,7 @@
 #include "queue_kernels.cuh"
 #include "ebi.cuh"
 #include "adjoint.cuh"
+#include "ddm.cuh"
 
 struct MechOps {
     const char* name;
@@ -32,6 +33,7 @@ struct MechOps {
     cudaError_t (*adj_forward)(const adj::Args&, int nblocks, cudaStream_t);
     cudaError_t (*adj_reverse)(const adj::Args&, int nblocks, cudaStream_t);
     cudaError_t (*adj_occupancy)(int* forward_bps, int* reverse_bps);
+    cudaError_t (*ddm_update)(const chem::GridArgs&, const chem::DdmArgs&, int nblocks, cudaStream_t);
     cudaError_t (*rconst)(const chem::GridArgs&, double* rki, uint8_t* sunlit, int nblocks, cudaStream_t);
     cudaError_t (*occupancy)(int* blocks_per_sm);
 };
@@ -115,6 +117,11 @@ struct MechOps {
         if (e != cudaSuccess) return e;                                                             \
         return cudaOccupancyMaxActiveBlocksPerMultiprocessor(r, adj::k_adj_reverse<T_>, adj::THREADS, 0); \
     }                                                                                               \
+    cudaError_t ddm_update_(const chem::GridArgs& a, const chem::DdmArgs& d, int nb, cudaStream_t s) \
+    {                                                                                               \
+        chem::k_ddm_update<T_><<<nb, chem::THREADS_PER_BLOCK, 0, s>>>(a, d);                        \
+        return cudaGetLastError();                                                                  \
+    }                                                                                               \
     cudaError_t rconst_(const chem::GridArgs& a, double* rki, uint8_t* sun, int nb, cudaStream_t s) \
     {                                                                                               \
         chem::k_rconst<T_><<<nb, chem::THREADS_PER_BLOCK, 0, s>>>(a, rki, sun);                     \
@@ -137,4 +144,5 @@ struct MechOps {
                                    NS::h_cgrid_index, NS::h_convert, NS::h_molwt, NS::h_inew2old,   \
                                    NS::h_iold2new, chem_static_, chem_queue_, queue_occupancy_,     \
                                    solve_, chem_ebi_, ebi_solve_, T_::EBI_DELTAT,            \
-                                   T_::ADJ_WS_ELEMS, adj_forward_, adj_reverse_, adj_occupancy_, rconst_, occupancy_};
+                                   T_::ADJ_WS_ELEMS, adj_forward_, adj_reverse_, adj_occupancy_, ddm_update_,     \
+                                   rconst_, occupancy_};

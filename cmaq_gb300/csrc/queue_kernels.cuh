@@ -26,8 +26,14 @@ struct QueueArgs {
 // barriers between its phases (SYNC = 1) or also between the generated chunks (SYNC = 2);
 // the block leaves the loop only when none of its warps holds a cell.  WPB = warps per
 // block.
+// Launch bounds: CHEM_QUEUE_WARPS_PER_SM resident warps per SM (12 by default; the
+// generated functions the kernel calls must be built for that register budget).
+#ifndef CHEM_QUEUE_WARPS_PER_SM
+#define CHEM_QUEUE_WARPS_PER_SM 12
+#endif
 template <class M, int SYNC, int WPB>
-__global__ void __launch_bounds__(WPB * 32, 8 / WPB) k_chem_ros3_queue(GridArgs a, QueueArgs q)
+__global__ void __launch_bounds__(WPB * 32, CHEM_QUEUE_WARPS_PER_SM / WPB > 0 ? CHEM_QUEUE_WARPS_PER_SM / WPB : 1)
+    k_chem_ros3_queue(GridArgs a, QueueArgs q)
 {
     constexpr bool LOCKSTEP = SYNC > 0;
     const int lane = threadIdx.x & 31;
@@ -53,6 +59,10 @@ __global__ void __launch_bounds__(WPB * 32, 8 / WPB) k_chem_ros3_queue(GridArgs 
                         cell = q.order ? q.order[pos] : (long long)pos;
                         sun = gather_cell<M>(a, cell, ws);
                         ros3::start(s);
+                        if (a.yave) {
+                            s.yave = true;
+                            for (int i = 0; i < M::ISCHAN; ++i) ws[(M::OFF_YAVE + i) * 32] = 0.0;
+                        }
                     }
                 }
                 drained = __any_sync(0xffffffffu, base + __popc(need) >= (unsigned long long)a.ncell);
@@ -71,6 +81,7 @@ __global__ void __launch_bounds__(WPB * 32, 8 / WPB) k_chem_ros3_queue(GridArgs 
         if (busy) {
             if (ros3::finished(s, a.chemstep)) {
                 scatter_cell<M>(a, cell, ws);
+                if (a.yave) store_yave<M>(a, cell, ws);
                 acc_steps += s.st.nsteps;
                 rej_steps += s.st.nfails;
                 failed += s.st.status != ros3::ST_OK;

@@ -56,6 +56,7 @@ struct CellState {
     double tnow, dt;
     int iter;
     bool lpass, have_f0;
+    bool yave;          // accumulate the time integral of Y in ws[OFF_YAVE] (DDM-3D)
     CellStats st;
 };
 
@@ -66,6 +67,7 @@ __device__ __forceinline__ void start(CellState& s)
     s.iter = 0;
     s.lpass = false;
     s.have_f0 = false;
+    s.yave = false;
     s.st = CellStats{0, 0, 0, ST_OK};
 }
 
@@ -184,8 +186,16 @@ __device__ void attempt_phased(double* __restrict__ ws, CellState& s, double che
     double dtfac = 0.9 / pow(maxerr, GROW);
     if (maxerr <= 1.0) {
         s.st.nsteps++;
-        for (int n = 0; n < M::NSPEC; ++n)
-            ws[(M::OFF_Y + n) * 32] = fmax(ws[(M::OFF_YP + n) * 32], CONMIN);
+        if (s.yave) {   // YAVE += (Y + Y') / 2 * DT (rbsolver.F:468-475)
+            for (int n = 0; n < M::NSPEC; ++n) {
+                const double yn = fmax(ws[(M::OFF_YP + n) * 32], CONMIN);
+                ws[(M::OFF_YAVE + n) * 32] = ws[(M::OFF_YAVE + n) * 32] + 0.5 * (ws[(M::OFF_Y + n) * 32] + yn) * dt;
+                ws[(M::OFF_Y + n) * 32] = yn;
+            }
+        } else {
+            for (int n = 0; n < M::NSPEC; ++n)
+                ws[(M::OFF_Y + n) * 32] = fmax(ws[(M::OFF_YP + n) * 32], CONMIN);
+        }
         if (!finite) s.st.status |= ST_NONFINITE;
         s.have_f0 = false;
         s.tnow = tend;
@@ -210,10 +220,15 @@ __device__ __forceinline__ void attempt(double* __restrict__ ws, CellState& s, d
 
 // Integrate the cell in ws over chemstep minutes (the whole DO WHILE loop).
 template <class M>
-__device__ CellStats integrate(double* __restrict__ ws, double chemstep, Tol tol, bool night, int max_iter)
+__device__ CellStats integrate(double* __restrict__ ws, double chemstep, Tol tol, bool night, int max_iter,
+                               bool yave = false)
 {
     CellState s;
     start(s);
+    if (yave) {
+        s.yave = true;
+        for (int n = 0; n < M::NSPEC; ++n) ws[(M::OFF_YAVE + n) * 32] = 0.0;
+    }
     while (!finished(s, chemstep)) attempt<M>(ws, s, chemstep, tol, night, max_iter);
     return s.st;
 }

@@ -49,6 +49,7 @@ class Layout:
                 for ial in range(m.nreact[r]):
                     self.ex[(r, ial)] = off
                     off += 1
+        self.yave = off; off += ns      # DDM-3D: time integral of Y over the accepted steps
         self.lu = off; off += max(sp.iarray) + 1      # 1-based storage, slot 0 unused
         # EBI species arrays overlay the LU region (the two solvers never share a cell state)
         self.ebi_yc = self.lu
@@ -144,6 +145,21 @@ def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src
             wrappers.extend(f"    adj_{kind}_{d}_{ci}({call});" for ci in range(len(chunks)))
             wrappers.append("}")
 
+    for d in range(2):
+        for kind, chunks, sig, call in (
+                ("jv", _ddm_jv(m, sp, lay, d), "double* __restrict__ ws, int yoff, int voff, int outoff",
+                 "ws, yoff, voff, outoff"),
+                ("src", _ddm_src(m, sp, lay, d),
+                 "double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff",
+                 "ws, mask, scale, outoff")):
+            for ci, code in enumerate(chunks):
+                units.setdefault(f"ddm{d}_{kind}{ci // 4}", []).extend(code)
+                decls.append(f"__device__ void ddm_{kind}_{d}_{ci}({sig});")
+            wrappers.append(f"__device__ __forceinline__ void ddm_{kind}_{d}({sig})")
+            wrappers.append("{")
+            wrappers.extend(f"    ddm_{kind}_{d}_{ci}({call});" for ci in range(len(chunks)))
+            wrappers.append("}")
+
     h = banner + ["#pragma once", "#include <cuda_runtime.h>", "#ifndef CHEM_HD", "#define CHEM_HD __device__",
                   "#endif",
                   "// load of an LU factor or 1/U(i,i); a build may define it as a streaming load (__ldcs)",
@@ -171,7 +187,7 @@ def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src
               ("ADJ_WS_ELEMS", lay.adj_total), ("ADJ_LAM", lay.adj_lam), ("ADJ_MU1", lay.adj_mu1),
               ("ADJ_MU2", lay.adj_mu2), ("ADJ_MU3", lay.adj_mu3), ("ADJ_PHI", lay.adj_phi),
               ("ADJ_TMP", lay.adj_tmp), ("ADJ_EMIS", lay.adj_emis), ("ADJ_GE", lay.adj_ge),
-              ("ADJ_GK", lay.adj_gk))
+              ("ADJ_GK", lay.adj_gk), ("OFF_YAVE", lay.yave))
     for k, v in consts:
         h.append(f"constexpr int {k} = {v};")
     h.append(f"constexpr double FLOPS_STEP_DAY = {float(flop_counts(m, sp, 0)['step_total'])};")
@@ -203,6 +219,8 @@ def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src
         h.append(f"    static __device__ __forceinline__ void solve_t_{d}(double* ws, int r) {{ {ns_name}::solve_t_{d}(ws, r); }}")
         h.append(f"    static __device__ __forceinline__ void adj_jtv_{d}(double* ws, int y, int phi, int out) {{ {ns_name}::adj_jtv_{d}(ws, y, phi, out); }}")
         h.append(f"    static __device__ __forceinline__ void adj_hess3_{d}(double* ws) {{ {ns_name}::adj_hess3_{d}(ws); }}")
+        h.append(f"    static __device__ __forceinline__ void ddm_jv_{d}(double* ws, int y, int v, int out) {{ {ns_name}::ddm_jv_{d}(ws, y, v, out); }}")
+        h.append(f"    static __device__ __forceinline__ void ddm_src_{d}(double* ws, const unsigned char* mk, double sc, int out) {{ {ns_name}::ddm_src_{d}(ws, mk, sc, out); }}")
     if ebi_decl:
         h.append(f"    static constexpr int EBI_N_EBISP = {ns_name}::EBI_N_EBISP;")
         h.append(f"    static constexpr int EBI_NEBITER = {ns_name}::EBI_NEBITER;")
@@ -330,7 +348,7 @@ def _jac_terms(m: Mechanism, sp: SparseMech, d: int) -> dict[int, list[tuple]]:
     return terms
 
 
-JAC_CHUNK_OPS = 700     # elimination ops per generated function; bounds ptxas time
+JAC_CHUNK_OPS = 200     # elimination ops per generated function; bounds ptxas time and register spills
 
 
 def _jacdecomp_chunks(m: Mechanism, sp: SparseMech, lay: Layout, d: int) -> list[list[str]]:
@@ -649,3 +667,58 @@ def _adj_hess3(m: Mechanism, sp: SparseMech, lay: Layout, d: int) -> list[list[s
         o.append("    }")
         blocks.append(o)
     return _chunk_reactions(head, blocks, f"adj_hess3_{d}")
+
+
+def _ddm_jv(m: Mechanism, sp: SparseMech, lay: Layout, d: int) -> list[list[str]]:
+    """out += J(y) v over the active reactions (the Jacobian-vector product of the DDM-3D
+    update, DDM3D_CHEM.F:386-396): per reaction d = grad R . v, then every species of the
+    reaction's net stoichiometry gets its coefficient times d."""
+    head = ["__device__ __noinline__ void {name}(double* __restrict__ ws, int yoff, int voff, int outoff)",
+            "    const double* __restrict__ y = ws + yoff * 32;",
+            "    const double* __restrict__ v = ws + voff * 32;",
+            "    double* __restrict__ out = ws + outoff * 32;"]
+    blocks = []
+    for r in sp.active[d]:
+        nre = m.nreact[r]
+        if nre == 0:
+            continue
+        a = [sp.irm2[r][i] * 32 for i in range(nre)]
+        k = _w(lay.rki + r)
+        o = ["    {"]
+        if nre == 1:
+            o.append(f"      const double dr = {k} * v[{a[0]}];")
+        elif nre == 2:
+            o.append(f"      const double dr = {k} * fma(y[{a[1]}], v[{a[0]}], y[{a[0]}] * v[{a[1]}]);")
+        else:
+            o.append(f"      const double dr = {k} * fma(y[{a[1]}] * y[{a[2]}], v[{a[0]}], "
+                     f"fma(y[{a[0]}] * y[{a[2]}], v[{a[1]}], (y[{a[0]}] * y[{a[1]}]) * v[{a[2]}]));")
+        for i in range(nre):
+            o.append(f"      out[{a[i]}] = out[{a[i]}] - dr;")
+        for p in range(m.nprdct[r]):
+            t = sp.irm2[r][3 + p] * 32
+            o.append(f"      out[{t}] = fma({c_double(m.sc[r][p])}, dr, out[{t}]);")
+        o.append("    }")
+        blocks.append(o)
+    return _chunk_reactions(head, blocks, f"ddm_jv_{d}")
+
+
+def _ddm_src(m: Mechanism, sp: SparseMech, lay: Layout, d: int) -> list[list[str]]:
+    """out += scale * sum over the reactions with mask[r] != 0 of the net stoichiometry
+    times the rate RXRAT (as left by feval): the source of a reaction-rate parameter
+    (DDM3D_CHEM.F:338-385).  The mask is the same for every lane, so the branches are
+    uniform."""
+    head = ["__device__ __noinline__ void {name}(double* __restrict__ ws, const unsigned char* __restrict__ mask, "
+            "double scale, int outoff)",
+            "    double* __restrict__ out = ws + outoff * 32;"]
+    blocks = []
+    for r in sp.active[d]:
+        o = [f"    if (mask[{r}]) {{", f"      const double q = scale * {_w(lay.rxrat + r)};"]
+        for i in range(m.nreact[r]):
+            t = sp.irm2[r][i] * 32
+            o.append(f"      out[{t}] = out[{t}] - q;")
+        for p in range(m.nprdct[r]):
+            t = sp.irm2[r][3 + p] * 32
+            o.append(f"      out[{t}] = fma({c_double(m.sc[r][p])}, q, out[{t}]);")
+        o.append("    }")
+        blocks.append(o)
+    return _chunk_reactions(head, blocks, f"ddm_src_{d}")

@@ -116,6 +116,21 @@ int cmaqchem_steps_device(cmaqchem_handle* h, float* conc, const float* ta, cons
                           int jdate, int jtime, const int tstep[3], int nsteps, void* stream,
                           cmaqchem_stats* stats);
 
+/* One CHEM call with first-order DDM-3D sensitivities (CCTM/src/ddm3d/DDM3D_CHEM.F:155,
+ * SOLVE_DDM3D_CHEM, called per cell from rbdriver.F:619-651): after the concentrations,
+ * every parameter's sensitivities in sengrid, the reference's SENGRID(NCOLS, NROWS, NLAYS,
+ * NPMAX, NSPCSD) REAL(4) with nparam = NPMAX, advance over the step.  rate_mask
+ * [nparam][nrxns] (device, may be NULL) marks the reactions of reaction-rate parameters
+ * (IPT = 5: IRXN(NP, RXN) = 1); region [nparam][ncols*nrows*nlays] (device, may be NULL
+ * for 1) weights their source as IREGION does.  Parameters with no reaction in the mask
+ * (initial and boundary conditions, emissions) only propagate.  ROS3 solver only. */
+int cmaqchem_step_ddm_device(cmaqchem_handle* h, float* conc, const float* ta, const float* qv,
+                             const float* dens, const float* pres, const float* seaice,
+                             const float* ocean_szone, const float* rj, const double* khetero,
+                             int jdate, int jtime, const int tstep[3], float* sengrid, int nparam,
+                             const unsigned char* rate_mask, const float* region, void* stream,
+                             cmaqchem_stats* stats);
+
 /* Per-cell status of the last step call (CMAQCHEM_CELL_* bits) and step attempts,
  * copied to host arrays of ncols*nrows*nlays ints (either may be NULL). */
 int cmaqchem_cell_stats(cmaqchem_handle* h, int* status, int* attempts);
