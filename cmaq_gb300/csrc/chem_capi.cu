@@ -57,6 +57,8 @@ int hhmmss_to_sec(int t)
 // error-text setter for the library's other translation units, not exported
 __attribute__((visibility("hidden"))) void cmaqchem_set_error(const std::string& msg) { g_err = msg; }
 
+constexpr int MAX_E2E_CHUNKS = 16;
+
 // what a captured CHEM call depends on besides the handle's own buffers
 struct GraphKey {
     const void* ptr[9];
@@ -101,6 +103,11 @@ struct cmaqchem_handle {
     double* s_khet = nullptr;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // host-pointer path: copy stream and per-chunk events
+    int e2e_chunks = 4;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_in[MAX_E2E_CHUNKS] = {};
+    cudaEvent_t ev_done[MAX_E2E_CHUNKS] = {};
     // discrete adjoint (allocated on first use, grown as needed)
     int adj_nblocks = 0;
     double* d_adj_ws = nullptr;
@@ -137,6 +144,11 @@ void free_handle(cmaqchem_handle* h)
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+    for (int i = 0; i < MAX_E2E_CHUNKS; ++i) {
+        if (h->ev_in[i]) cudaEventDestroy(h->ev_in[i]);
+        if (h->ev_done[i]) cudaEventDestroy(h->ev_done[i]);
+    }
+    if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -339,6 +351,10 @@ extern "C" int cmaqchem_diag_set_tuning(cmaqchem_handle* h, const char* key, int
         if (value < 0 || value > 2) return fail("lockstep must be 0, 1 or 2");
         if (value == 0 && h->q_wpb != 8) return fail("lockstep 0 needs block_warps 8");
         h->q_sync = value;
+    } else if (strcmp(key, "host_chunks") == 0) {
+        if (value < 1 || value > MAX_E2E_CHUNKS) return fail("host_chunks must be 1 .. 16");
+        h->e2e_chunks = value;
+        return 0;
     } else if (strcmp(key, "adjoint_tape_mb") == 0) {
         if (value < 0) return fail("adjoint_tape_mb must be >= 0");
         h->adj_tape_budget = (size_t)value << 20;
@@ -360,21 +376,24 @@ extern "C" int cmaqchem_diag_set_tuning(cmaqchem_handle* h, const char* key, int
 
 // Enqueue the launches of one CHEM call (no host synchronisation).  sort: order the work
 // queue by the previous call's step attempts.
-static int enqueue_step(cmaqchem_handle* h, const chem::GridArgs& a, int itmstep, cudaStream_t s, bool sort)
+static int enqueue_step(cmaqchem_handle* h, const chem::GridArgs& a, int itmstep, cudaStream_t s, bool sort,
+                        long long c0 = 0, long long c1 = -1)
 {
     const bool ebi_solver = h->cfg.solver == CMAQCHEM_SOLVER_EBI;
+    if (c1 < 0) c1 = h->ncell;
+    const long long n = c1 - c0;
     if (h->cfg.schedule == CMAQCHEM_SCHED_QUEUE || ebi_solver) {
-        chem::QueueArgs q{nullptr, h->d_head};
+        chem::QueueArgs q{nullptr, h->d_head, n, c0};
         if (sort && h->cfg.schedule == CMAQCHEM_SCHED_QUEUE) {
             const int nb = 4 * h->nsm;
             CK(cudaMemsetAsync(h->d_hist, 0, sizeof(unsigned int) * chem::QUEUE_BINS, s));
-            chem::k_queue_hist<<<nb, 256, 0, s>>>(h->d_steps, h->ncell, h->d_hist);
+            chem::k_queue_hist<<<nb, 256, 0, s>>>(h->d_steps + c0, n, h->d_hist);
             CK(cudaGetLastError());
             chem::k_queue_scan<<<1, chem::QUEUE_BINS, 0, s>>>(h->d_hist, h->d_cursor);
             CK(cudaGetLastError());
-            chem::k_queue_scatter<<<nb, 256, 0, s>>>(h->d_steps, h->ncell, h->d_cursor, h->d_order);
+            chem::k_queue_scatter<<<nb, 256, 0, s>>>(h->d_steps + c0, n, h->d_cursor, h->d_order + c0);
             CK(cudaGetLastError());
-            q.order = h->d_order;
+            q.order = h->d_order + c0;
         }
         CK(cudaMemsetAsync(h->d_head, 0, sizeof(unsigned long long), s));
         if (ebi_solver) {
@@ -541,27 +560,57 @@ extern "C" int cmaqchem_step(cmaqchem_handle* h, float* conc, const float* ta, c
         CK(cudaMalloc(&h->s_rj, sizeof(float) * nc * h->ops->nphotab));
         CK(cudaMalloc(&h->s_khet, sizeof(double) * nc * (h->ops->nhetero > 0 ? h->ops->nhetero : 1)));
     }
+    const int itmstep = hhmmss_to_sec(tstep[1]);
+    if (itmstep <= 0) return fail("TSTEP(2) must be a positive HHMMSS interval");
     cudaStream_t s = h->stream;
-    // only the mechanism's CGRID planes are read and written by CHEM
-    for (int p : h->conc_planes)
-        CK(cudaMemcpyAsync(h->s_conc + (size_t)p * nc, conc + (size_t)p * nc, sizeof(float) * nc,
-                           cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(h->s_ta, ta, sizeof(float) * nc, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(h->s_qv, qv, sizeof(float) * nc, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(h->s_dens, dens, sizeof(float) * nc, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(h->s_pres, pres, sizeof(float) * nc, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(h->s_seaice, seaice, sizeof(float) * ncr, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(h->s_osz, ocean_szone, sizeof(float) * ncr, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(h->s_rj, rj, sizeof(float) * nc * h->ops->nphotab, cudaMemcpyHostToDevice, s));
-    if (h->ops->nhetero > 0)
-        CK(cudaMemcpyAsync(h->s_khet, khetero, sizeof(double) * nc * h->ops->nhetero, cudaMemcpyHostToDevice, s));
-    const int rc = step_device_impl(h, h->s_conc, h->s_ta, h->s_qv, h->s_dens, h->s_pres, h->s_seaice, h->s_osz,
-                                    h->s_rj, h->s_khet, tstep, s, stats);
-    if (rc < 0) return rc;
-    for (int p : h->conc_planes)
-        CK(cudaMemcpyAsync(conc + (size_t)p * nc, h->s_conc + (size_t)p * nc, sizeof(float) * nc,
-                           cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
+    cudaStream_t cs = h->copy_stream;
+    if (!cs) {
+        CK(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+        cs = h->copy_stream;
+        for (int i = 0; i < MAX_E2E_CHUNKS; ++i) {
+            CK(cudaEventCreateWithFlags(&h->ev_in[i], cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&h->ev_done[i], cudaEventDisableTiming));
+        }
+    }
+    // The grid is split into chunks of consecutive cells: the inputs of chunk i+1 travel
+    // and the results of chunk i-1 come back while chunk i is integrated.  Only the
+    // mechanism's CGRID planes are read and written by CHEM.
+    const bool chunked = h->cfg.schedule == CMAQCHEM_SCHED_QUEUE || h->cfg.solver == CMAQCHEM_SOLVER_EBI;
+    const int nch = chunked ? std::max(1, std::min<int>(h->e2e_chunks, (int)std::min<long long>(MAX_E2E_CHUNKS, nc))) : 1;
+    const int nhet = h->ops->nhetero;
+    CK(cudaMemcpyAsync(h->s_seaice, seaice, sizeof(float) * ncr, cudaMemcpyHostToDevice, cs));
+    CK(cudaMemcpyAsync(h->s_osz, ocean_szone, sizeof(float) * ncr, cudaMemcpyHostToDevice, cs));
+    chem::GridArgs a = grid_args(h, h->s_conc, h->s_ta, h->s_qv, h->s_dens, h->s_pres, h->s_seaice, h->s_osz,
+                                 h->s_rj, h->s_khet, (double)itmstep / 60.0);
+    CK(cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned long long) * 5, s));
+    CK(cudaEventRecord(h->ev0, s));
+    for (int i = 0; i < nch; ++i) {
+        const size_t c0 = nc * i / nch, c1 = nc * (i + 1) / nch, n = c1 - c0;
+        auto h2d = [&](void* dst, const void* src, size_t bytes) {
+            return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, cs);
+        };
+        for (int p : h->conc_planes) CK(h2d(h->s_conc + p * nc + c0, conc + p * nc + c0, sizeof(float) * n));
+        CK(h2d(h->s_ta + c0, ta + c0, sizeof(float) * n));
+        CK(h2d(h->s_qv + c0, qv + c0, sizeof(float) * n));
+        CK(h2d(h->s_dens + c0, dens + c0, sizeof(float) * n));
+        CK(h2d(h->s_pres + c0, pres + c0, sizeof(float) * n));
+        for (int k = 0; k < h->ops->nphotab; ++k) CK(h2d(h->s_rj + k * nc + c0, rj + k * nc + c0, sizeof(float) * n));
+        if (nhet > 0) CK(h2d(h->s_khet + c0 * nhet, khetero + c0 * nhet, sizeof(double) * n * nhet));
+        CK(cudaEventRecord(h->ev_in[i], cs));
+        CK(cudaStreamWaitEvent(s, h->ev_in[i], 0));
+        if (nch == 1) {
+            if (enqueue_step(h, a, itmstep, s, h->have_history)) return -1;
+        } else {
+            if (enqueue_step(h, a, itmstep, s, h->have_history, (long long)c0, (long long)c1)) return -1;
+        }
+        CK(cudaEventRecord(h->ev_done[i], s));
+        CK(cudaStreamWaitEvent(cs, h->ev_done[i], 0));
+        for (int p : h->conc_planes)
+            CK(cudaMemcpyAsync(conc + p * nc + c0, h->s_conc + p * nc + c0, sizeof(float) * n,
+                               cudaMemcpyDeviceToHost, cs));
+    }
+    const int rc = finish_steps(h, s, stats);
+    CK(cudaStreamSynchronize(cs));
     return rc;
 }
 

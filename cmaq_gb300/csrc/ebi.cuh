@@ -241,13 +241,13 @@ __global__ void __launch_bounds__(THREADS_PER_BLOCK, 1) k_chem_ebi_queue(GridArg
                 base = __shfl_sync(0xffffffffu, base, leader);
                 if (cell < 0) {
                     const unsigned long long pos = base + __popc(need & ((1u << lane) - 1u));
-                    if (pos < (unsigned long long)a.ncell) {
-                        cell = q.order ? q.order[pos] : (long long)pos;
+                    if (pos < queue_len(q, a.ncell)) {
+                        cell = q.cell0 + (q.order ? q.order[pos] : (long long)pos);
                         sun = gather_cell_ebi<M>(a, e, cell, ws);
                         ebi::start<M>(ws, s, e.n_ebi_steps, e.tmstep);
                     }
                 }
-                drained = __any_sync(0xffffffffu, base + __popc(need) >= (unsigned long long)a.ncell);
+                drained = __any_sync(0xffffffffu, base + __popc(need) >= queue_len(q, a.ncell));
             }
         }
         const bool busy = cell >= 0;

@@ -18,9 +18,16 @@ namespace chem {
 constexpr int QUEUE_BINS = 256;
 
 struct QueueArgs {
-    const int* order;                 // [ncell] cell indices in queue order, or nullptr for 0..ncell-1
+    const int* order;                 // queue order of cells relative to cell0, or nullptr for 0, 1, ...
     unsigned long long* head;         // next queue position (zeroed before the launch)
+    long long qlen;                   // cells in the queue (0: the whole grid)
+    long long cell0;                  // first cell of the range the queue covers
 };
+
+__device__ __forceinline__ unsigned long long queue_len(const QueueArgs& q, long long ncell)
+{
+    return (unsigned long long)(q.qlen > 0 ? q.qlen : ncell);
+}
 
 // SYNC > 0 ("lock-step"): the block's warps run each step attempt together, with
 // barriers between its phases (SYNC = 1) or also between the generated chunks (SYNC = 2);
@@ -55,8 +62,8 @@ __global__ void __launch_bounds__(WPB * 32, CHEM_QUEUE_WARPS_PER_SM / WPB > 0 ? 
                 base = __shfl_sync(0xffffffffu, base, leader);
                 if (cell < 0) {
                     const unsigned long long pos = base + __popc(need & ((1u << lane) - 1u));
-                    if (pos < (unsigned long long)a.ncell) {
-                        cell = q.order ? q.order[pos] : (long long)pos;
+                    if (pos < queue_len(q, a.ncell)) {
+                        cell = q.cell0 + (q.order ? q.order[pos] : (long long)pos);
                         sun = gather_cell<M>(a, cell, ws);
                         ros3::start(s);
                         if (a.yave) {
@@ -65,7 +72,7 @@ __global__ void __launch_bounds__(WPB * 32, CHEM_QUEUE_WARPS_PER_SM / WPB > 0 ? 
                         }
                     }
                 }
-                drained = __any_sync(0xffffffffu, base + __popc(need) >= (unsigned long long)a.ncell);
+                drained = __any_sync(0xffffffffu, base + __popc(need) >= queue_len(q, a.ncell));
             }
         }
         const bool busy = cell >= 0;

@@ -89,7 +89,10 @@ typedef struct {
 int cmaqchem_init(const cmaqchem_cfg* cfg, cmaqchem_handle** out);
 
 /* One CHEM call on host arrays (rbdriver.F:373-785): copies the inputs to the device,
- * integrates every cell over TSTEP(2) and copies CONC back.  tstep = TSTEP(3) HHMMSS. */
+ * integrates every cell over TSTEP(2) and copies CONC back.  tstep = TSTEP(3) HHMMSS.
+ * Only the mechanism's CONC planes travel; with the work-queue schedule the grid moves
+ * in chunks of consecutive cells whose copies overlap the integration of the previous
+ * chunk.  Pinned host memory makes the copies asynchronous. */
 int cmaqchem_step(cmaqchem_handle* h, float* conc, const float* ta, const float* qv,
                   const float* dens, const float* pres, const float* seaice,
                   const float* ocean_szone, const float* rj, const double* khetero,

@@ -21,7 +21,9 @@ int cmaqchem_diag_fp64_peak(int device, double* tflops, double* ms);
  * needs 8), "blocks_per_sm" (cap on resident blocks per SM of the work-queue kernel,
  * 0 (default): as many as fit) and "adjoint_tape_mb" (device memory for the adjoint's
  * step tape; a synchronisation step whose tape is larger is processed in batches of
- * consecutive cells; 0 (default): the largest step's tape, halved until it fits). */
+ * consecutive cells; 0 (default): the largest step's tape, halved until it fits) and
+ * "host_chunks" (1-16, default 4: cmaqchem_step moves the grid in that many chunks of
+ * consecutive cells so that copies overlap the integration of the previous chunk). */
 struct cmaqchem_handle;
 int cmaqchem_diag_set_tuning(struct cmaqchem_handle* h, const char* key, int value);
 
