@@ -96,6 +96,8 @@ struct cmaqchem_handle {
     int q_wpb = 4;           // work-queue kernel: warps per block
     int q_nblocks = 0;
     int q_bps_cap = 0;       // blocks per SM of the queue kernel, 0: as many as fit
+    int ebi_warp = 1;        // EBI: 1 one cell per warp (shared memory), 0 one cell per lane
+    int ebiw_nblocks = 0;
     size_t ws_warps = 0;     // workspace capacity in warps
     // device staging of the host-pointer entry point, allocated on first use
     float *s_conc = nullptr, *s_ta = nullptr, *s_qv = nullptr, *s_dens = nullptr, *s_pres = nullptr;
@@ -105,7 +107,7 @@ struct cmaqchem_handle {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // host-pointer path: copy stream and per-chunk events
     int e2e_chunks = 4;
-    cudaStream_t copy_stream = nullptr;
+    cudaStream_t copy_stream = nullptr, back_stream = nullptr;
     cudaEvent_t ev_in[MAX_E2E_CHUNKS] = {};
     cudaEvent_t ev_done[MAX_E2E_CHUNKS] = {};
     // discrete adjoint (allocated on first use, grown as needed)
@@ -149,6 +151,7 @@ void free_handle(cmaqchem_handle* h)
         if (h->ev_done[i]) cudaEventDestroy(h->ev_done[i]);
     }
     if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
+    if (h->back_stream) cudaStreamDestroy(h->back_stream);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -300,6 +303,12 @@ extern "C" int cmaqchem_init(const cmaqchem_cfg* cfg, cmaqchem_handle** out)
         h->nblocks = h->nsm * h->bps;
         if (ensure_ws(h, (size_t)h->nblocks * chem::WARPS_PER_BLOCK)) return -1;
         if (configure_queue(h)) return -1;
+        if (cfg->solver == CMAQCHEM_SOLVER_EBI) {
+            int bw = 0;
+            CK(m->ebi_warp_occupancy(&bw));
+            h->ebiw_nblocks = h->nsm * (bw > 0 ? bw : 1);
+            if (ensure_ws(h, (size_t)h->ebiw_nblocks * chem::EBIW_WPB)) return -1;
+        }
         CK(cudaMalloc(&h->d_cgrid_index, sizeof(int) * m->nspec));
         CK(cudaMalloc(&h->d_convert, sizeof(int) * m->nspec));
         CK(cudaMalloc(&h->d_fwd, sizeof(float) * m->nspec));
@@ -351,6 +360,11 @@ extern "C" int cmaqchem_diag_set_tuning(cmaqchem_handle* h, const char* key, int
         if (value < 0 || value > 2) return fail("lockstep must be 0, 1 or 2");
         if (value == 0 && h->q_wpb != 8) return fail("lockstep 0 needs block_warps 8");
         h->q_sync = value;
+    } else if (strcmp(key, "ebi_warp") == 0) {
+        h->ebi_warp = value != 0;
+        if (h->graph_exec) CK(cudaGraphExecDestroy(h->graph_exec));
+        h->graph_exec = nullptr;
+        return 0;
     } else if (strcmp(key, "host_chunks") == 0) {
         if (value < 1 || value > MAX_E2E_CHUNKS) return fail("host_chunks must be 1 .. 16");
         h->e2e_chunks = value;
@@ -401,7 +415,8 @@ static int enqueue_step(cmaqchem_handle* h, const chem::GridArgs& a, int itmstep
             ebi::steps_for(itmstep, h->ops->ebi_deltat, &e.n_ebi_steps, &e.tmstep);
             e.fwd = h->d_ebi_fwd;
             e.rev = h->d_ebi_rev;
-            CK(h->ops->chem_ebi(a, q, e, h->nblocks, s));
+            if (h->ebi_warp) CK(h->ops->chem_ebi_warp(a, q, e, h->ebiw_nblocks, s));
+            else CK(h->ops->chem_ebi(a, q, e, h->nblocks, s));
         } else {
             CK(h->ops->chem_queue(a, q, h->q_sync, h->q_wpb, h->q_nblocks, s));
         }
@@ -563,9 +578,10 @@ extern "C" int cmaqchem_step(cmaqchem_handle* h, float* conc, const float* ta, c
     const int itmstep = hhmmss_to_sec(tstep[1]);
     if (itmstep <= 0) return fail("TSTEP(2) must be a positive HHMMSS interval");
     cudaStream_t s = h->stream;
-    cudaStream_t cs = h->copy_stream;
+    cudaStream_t cs = h->copy_stream;       // host -> device
     if (!cs) {
         CK(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+        CK(cudaStreamCreateWithFlags(&h->back_stream, cudaStreamNonBlocking));
         cs = h->copy_stream;
         for (int i = 0; i < MAX_E2E_CHUNKS; ++i) {
             CK(cudaEventCreateWithFlags(&h->ev_in[i], cudaEventDisableTiming));
@@ -584,6 +600,8 @@ extern "C" int cmaqchem_step(cmaqchem_handle* h, float* conc, const float* ta, c
                                  h->s_rj, h->s_khet, (double)itmstep / 60.0);
     CK(cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned long long) * 5, s));
     CK(cudaEventRecord(h->ev0, s));
+    // uploads of every chunk in order on one stream, the integration of chunk i once its
+    // inputs are in, its write-back on a third stream once it is integrated
     for (int i = 0; i < nch; ++i) {
         const size_t c0 = nc * i / nch, c1 = nc * (i + 1) / nch, n = c1 - c0;
         auto h2d = [&](void* dst, const void* src, size_t bytes) {
@@ -597,6 +615,9 @@ extern "C" int cmaqchem_step(cmaqchem_handle* h, float* conc, const float* ta, c
         for (int k = 0; k < h->ops->nphotab; ++k) CK(h2d(h->s_rj + k * nc + c0, rj + k * nc + c0, sizeof(float) * n));
         if (nhet > 0) CK(h2d(h->s_khet + c0 * nhet, khetero + c0 * nhet, sizeof(double) * n * nhet));
         CK(cudaEventRecord(h->ev_in[i], cs));
+    }
+    for (int i = 0; i < nch; ++i) {
+        const size_t c0 = nc * i / nch, c1 = nc * (i + 1) / nch, n = c1 - c0;
         CK(cudaStreamWaitEvent(s, h->ev_in[i], 0));
         if (nch == 1) {
             if (enqueue_step(h, a, itmstep, s, h->have_history)) return -1;
@@ -604,13 +625,13 @@ extern "C" int cmaqchem_step(cmaqchem_handle* h, float* conc, const float* ta, c
             if (enqueue_step(h, a, itmstep, s, h->have_history, (long long)c0, (long long)c1)) return -1;
         }
         CK(cudaEventRecord(h->ev_done[i], s));
-        CK(cudaStreamWaitEvent(cs, h->ev_done[i], 0));
+        CK(cudaStreamWaitEvent(h->back_stream, h->ev_done[i], 0));
         for (int p : h->conc_planes)
             CK(cudaMemcpyAsync(conc + p * nc + c0, h->s_conc + p * nc + c0, sizeof(float) * n,
-                               cudaMemcpyDeviceToHost, cs));
+                               cudaMemcpyDeviceToHost, h->back_stream));
     }
     const int rc = finish_steps(h, s, stats);
-    CK(cudaStreamSynchronize(cs));
+    CK(cudaStreamSynchronize(h->back_stream));
     return rc;
 }
 

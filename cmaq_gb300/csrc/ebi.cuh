@@ -313,3 +313,255 @@ __global__ void __launch_bounds__(THREADS_PER_BLOCK, 1) k_ebi_solve(EbiSolveArgs
 }
 
 }  // namespace chem
+
+namespace chem {
+
+// Warp-cooperative EBI: one cell per warp, its EBI state (YC, YC0, YCP, PROD, LOSS, PNEG,
+// NOTMAX, RKI, RXRAT) in shared memory.  HRRATES and HRPRODLOSS run from tables, their
+// statements spread over the lanes; HRG1-HRG4 (short, sequential) run on lane 0; the
+// per-species loops of HRSOLVER are split over the lanes and their convergence flags
+// combined by warp votes.  Every value is computed with the same operations in the same
+// order as the per-lane kernel and the oracle, so results are bit-identical; what
+// changes is that a cell's iteration runs on 32 lanes from shared memory instead of on
+// one lane from the (DRAM-resident) workspace, which shortens the long cells that set
+// the call time.
+constexpr int EBIW_WPB = 4;
+
+template <class M>
+__device__ void ebiw_gather(const GridArgs& a, const EbiArgs& e, long long c, double* __restrict__ sm,
+                            double* __restrict__ ws0, int lane, bool& sun)
+{
+    const float inv_dens = __fdiv_rn(1.0f, a.dens[c]);
+    for (int s = lane; s < M::NSPEC; s += 32) {
+        const float cv = a.cgrid[(size_t)a.cgrid_index[s] * a.ncell + c];
+        const float v = a.convert[s] ? fmaxf(CONCMIN_F, __fmul_rn(__fmul_rn(inv_dens, e.fwd[s]), cv))
+                                     : fmaxf(cv, CONCMIN_F);
+        sm[M::EBIW_YC + s] = (double)v;
+    }
+    int lsun = 0;
+    if (lane == 0) {   // met, rate constants of the cell into lane 0's workspace column
+        const double temp = (double)a.ta[c];
+        const double atmpres = (double)(1.0f / 101325.0f) * (double)a.pres[c];
+        const float maomv = 1.0e6f * 28.9628f / 18.0153f;
+        const double h2o = (double)fmaxf(__fmul_rn(maomv, a.qv[c]), 0.0f);
+        const int col = (int)(c % a.ncolrow);
+        const double seawater = fmax(0.0, (double)__fsub_rn(a.ocean_szone[col], a.seaice[col]));
+        double rjv[M::NPHOTAB];
+        for (int k = 0; k < M::NPHOTAB; ++k) {
+            rjv[k] = (double)a.rj[(size_t)k * a.ncell + c];
+            lsun |= rjv[k] > 0.0;
+        }
+        double hetv[M::NHETERO];
+        for (int k = 0; k < M::NHETERO; ++k) hetv[k] = a.khet[(size_t)c * M::NHETERO + k];
+        M::rconst(ws0, temp, atmpres, h2o, seawater, lsun, rjv, hetv);
+    }
+    sun = __shfl_sync(0xffffffffu, lsun, 0) != 0;
+    __syncwarp();
+    for (int r = lane; r < M::NRXNS; r += 32) {
+        sm[M::EBIW_RKI + r] = ws0[(M::OFF_RKI + r) * 32];
+        sm[M::EBIW_RXRAT + r] = 0.0;
+    }
+    for (int s = lane; s < M::NSPEC; s += 32) {
+        sm[M::EBIW_PROD + s] = 0.0;
+        sm[M::EBIW_LOSS + s] = 0.0;
+        sm[M::EBIW_PNEG + s] = 0.0;
+        sm[M::EBIW_YCP + s] = 0.0;
+        sm[M::EBIW_YC0 + s] = 0.0;
+        sm[M::EBIW_NOTMAX + s] = sm[M::EBIW_YC + s] <= ebi::MAXPRED ? 1.0 : 0.0;
+    }
+    __syncwarp();
+}
+
+// One Backward-Euler iteration of the warp's cell plus HRSOLVER's bookkeeping (the same
+// control flow as ebi::iterate; the scalar state is kept identically by every lane).
+template <class M>
+__device__ void ebiw_iterate(double* __restrict__ sm, ebi::State& s, int max_iter, int lane)
+{
+    using namespace ebi;
+    if (s.total_iter >= max_iter) {
+        s.status |= ST_MAXITER;
+        s.done = true;
+        return;
+    }
+    if (s.substep_start) {
+        if (s.lebi_conv)
+            for (int i = lane; i < M::NSPEC; i += 32) sm[M::EBIW_YC0 + i] = sm[M::EBIW_YC + i];
+        s.substep_start = false;
+        s.iter = 0;
+    }
+    s.iter++;
+    s.total_iter++;
+    const double dtc = s.dtc;
+    __syncwarp();
+    {   // HRRATES
+        const int* rr = M::ebiw_rate_r();
+        const int* nf = M::ebiw_rate_nf();
+        const int* sp = M::ebiw_rate_sp();
+        for (int q = lane; q < M::EBIW_NRATE; q += 32) {
+            const int r = rr[q];
+            double acc = sm[M::EBIW_RKI + r];
+            for (int j = 0; j < nf[q]; ++j) acc = acc * sm[M::EBIW_YC + sp[3 * q + j]];
+            sm[M::EBIW_RXRAT + r] = acc;
+        }
+    }
+    __syncwarp();
+    if (lane == 0) {
+        M::ebiw_hrg1(sm, dtc);
+        M::ebiw_hrg2(sm, dtc);
+        M::ebiw_hrg3(sm, dtc);
+        M::ebiw_hrg4(sm, dtc);
+    }
+    __syncwarp();
+    {   // HRPRODLOSS
+        const int* ptr = M::ebiw_pl_ptr();
+        const int* kind = M::ebiw_pl_kind();
+        const int* spc = M::ebiw_pl_sp();
+        const int* t0 = M::ebiw_pl_t0();
+        const int* tr = M::ebiw_term_r();
+        const double* tc = M::ebiw_term_c();
+        for (int q = ptr[lane]; q < ptr[lane + 1]; ++q) {
+            double acc = 0.0;
+            const int a0 = t0[q], a1 = t0[q + 1];
+            if (a1 > a0) {
+                acc = tc[a0] * sm[M::EBIW_RXRAT + tr[a0]];
+                for (int t = a0 + 1; t < a1; ++t) acc = acc + tc[t] * sm[M::EBIW_RXRAT + tr[t]];
+            }
+            const int base = kind[q] == 0 ? M::EBIW_PROD : (kind[q] == 1 ? M::EBIW_LOSS : M::EBIW_PNEG);
+            sm[base + spc[q]] = acc;
+        }
+    }
+    __syncwarp();
+    for (int e = lane; e < M::EBI_N_EBISP; e += 32) {
+        const int sp = M::ebi_ebisp(e);
+        const double yc = sm[M::EBIW_YC + sp];
+        sm[M::EBIW_YCP + sp] = yc * ((sm[M::EBIW_YC0 + sp] + sm[M::EBIW_PROD + sp] * dtc) /
+                                     (yc + sm[M::EBIW_LOSS + sp] * dtc));
+    }
+    __syncwarp();
+    if (lane == 0) {
+        for (int k = 0; k < M::EBI_NPNEG; ++k) {
+            const int p = M::ebi_pneg(k);
+            const double pneg = sm[M::EBIW_PNEG + p];
+            if (pneg > 0.0) {
+                const double fxdloss = pneg * dtc;
+                const double yc0 = sm[M::EBIW_YC0 + p], prod = sm[M::EBIW_PROD + p];
+                if (fxdloss >= yc0 + prod * dtc) {
+                    sm[M::EBIW_YCP + p] = 0.0;
+                } else {
+                    const double varloss = fmax(sm[M::EBIW_LOSS + p] - pneg, ZERO);
+                    sm[M::EBIW_YCP + p] = (yc0 + prod * dtc - fxdloss) / (1.0 + varloss * dtc / sm[M::EBIW_YC + p]);
+                }
+            }
+        }
+    }
+    __syncwarp();
+    bool conv = true, mxfl = false;
+    for (int i = lane; i < M::NSPEC; i += 32) {
+        const double ycp = fmax(ZERO, sm[M::EBIW_YCP + i]);
+        const double yc = sm[M::EBIW_YC + i];
+        const double aerror = fmax(fabs(yc - ycp), EPSLON);
+        const double rerror = aerror / fmax(FLOOR, fabs(yc + ycp));
+        if (rerror > M::ebi_rtol(i) || aerror > 1.0e-5) conv = false;
+        if (ycp > MAXPRED && sm[M::EBIW_NOTMAX + i] != 0.0) {
+            mxfl = true;
+            conv = false;
+        }
+        sm[M::EBIW_YCP + i] = ycp;
+        sm[M::EBIW_YC + i] = ycp;
+    }
+    conv = __all_sync(0xffffffffu, conv);
+    mxfl = __any_sync(0xffffffffu, mxfl);
+    s.lebi_conv = conv;
+    if (conv) {
+        s.ninr++;
+        s.substep_start = true;
+        if (s.ninr <= s.n_inr_steps) return;
+        s.nebi++;
+        if (s.nebi > s.n_ebi_steps) {
+            s.done = true;
+            return;
+        }
+        if (s.nbkups != 0) {
+            s.nbkups = 0;
+            s.n_inr_steps = 1;
+            s.dtc = s.tmstep;
+        }
+        s.ninr = 1;
+        return;
+    }
+    if (mxfl || s.iter >= M::EBI_NEBITER) {
+        s.nbkups++;
+        if (s.dtc > DTMIN) {
+            __syncwarp();
+            for (int i = lane; i < M::NSPEC; i += 32) sm[M::EBIW_YC + i] = sm[M::EBIW_YC0 + i];
+            s.dtc = 0.5 * s.dtc;
+            s.n_inr_steps = 1 << (s.nbkups < 30 ? s.nbkups : 30);
+            s.ninr = 1;
+            s.substep_start = true;
+            return;
+        }
+        s.status |= ST_DT_UNDERFLOW;
+        s.done = true;
+    }
+}
+
+// One EBI CHEM call, a cell per warp from the work queue.  Dynamic shared memory:
+// EBIW_WPB * EBIW_ELEMS doubles.
+template <class M>
+__global__ void __launch_bounds__(EBIW_WPB * 32) k_chem_ebi_warp(GridArgs a, QueueArgs q, EbiArgs e)
+{
+    extern __shared__ double smem_all[];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    double* sm = smem_all + (size_t)wib * M::EBIW_ELEMS;
+    const long long warp = (long long)blockIdx.x * EBIW_WPB + wib;
+    double* ws0 = a.ws + (size_t)warp * ((size_t)M::WS_ELEMS * 32);   // lane 0's workspace column
+    const unsigned long long qlen = queue_len(q, a.ncell);
+    unsigned long long iters = 0, failed = 0, sunlit = 0;
+    for (;;) {
+        unsigned long long pos = 0;
+        if (lane == 0) pos = atomicAdd(q.head, 1ull);
+        pos = __shfl_sync(0xffffffffu, pos, 0);
+        if (pos >= qlen) break;
+        const long long cell = q.cell0 + (q.order ? q.order[pos] : (long long)pos);
+        bool sun = false;
+        ebiw_gather<M>(a, e, cell, sm, ws0, lane, sun);
+        ebi::State s;
+        s.tmstep = e.tmstep;
+        s.dtc = e.tmstep;
+        s.n_ebi_steps = e.n_ebi_steps;
+        s.nebi = 1;
+        s.ninr = 1;
+        s.n_inr_steps = 1;
+        s.nbkups = 0;
+        s.iter = 0;
+        s.total_iter = 0;
+        s.lebi_conv = true;
+        s.substep_start = true;
+        s.done = false;
+        s.status = ebi::ST_OK;
+        while (!s.done) ebiw_iterate<M>(sm, s, a.max_iter, lane);
+        __syncwarp();
+        const float dens = a.dens[cell];
+        for (int sp = lane; sp < M::NSPEC; sp += 32) {   // write-back (hrdriver.F:446-454)
+            const double y = fmax(sm[M::EBIW_YC + sp], 1.0e-30);
+            const float v = a.convert[sp] ? (float)((double)__fmul_rn(e.rev[sp], dens) * y) : (float)y;
+            a.cgrid[(size_t)a.cgrid_index[sp] * a.ncell + cell] = v;
+        }
+        if (lane == 0) {
+            iters += s.total_iter;
+            failed += s.status != ebi::ST_OK;
+            sunlit += sun;
+            if (a.cell_status) a.cell_status[cell] = s.status;
+            if (a.cell_steps) a.cell_steps[cell] = s.total_iter;
+        }
+        __syncwarp();
+    }
+    if (a.counters && lane == 0) {
+        atomicAdd(&a.counters[0], iters);
+        atomicAdd(&a.counters[2], failed);
+        atomicAdd(&a.counters[3], sunlit);
+    }
+}
+
+}  // namespace chem

@@ -57,6 +57,16 @@ constexpr int ADJ_EMIS = 8092;
 constexpr int ADJ_GE = 8281;
 constexpr int ADJ_GK = 8470;
 constexpr int OFF_YAVE = 3295;
+constexpr int EBIW_YC = 0;
+constexpr int EBIW_YC0 = 189;
+constexpr int EBIW_YCP = 378;
+constexpr int EBIW_PROD = 567;
+constexpr int EBIW_LOSS = 756;
+constexpr int EBIW_PNEG = 945;
+constexpr int EBIW_NOTMAX = 1134;
+constexpr int EBIW_RKI = 1323;
+constexpr int EBIW_RXRAT = 1854;
+constexpr int EBIW_ELEMS = 2385;
 constexpr double FLOPS_STEP_DAY = 79988.0;
 constexpr double FLOPS_STEP_NIGHT = 77148.0;
 extern __constant__ int c_inew2old[189];
@@ -340,6 +350,24 @@ __device__ void ebi_hrg1(double* __restrict__ ws, double dtc);
 __device__ void ebi_hrg2(double* __restrict__ ws, double dtc);
 __device__ void ebi_hrg3(double* __restrict__ ws, double dtc);
 __device__ void ebi_hrg4(double* __restrict__ ws, double dtc);
+constexpr int EBIW_NRATE = 510;
+constexpr int EBIW_NPL = 352;
+constexpr int EBIW_NTERM = 2196;
+extern __device__ const int c_ebiw_rate_r[EBIW_NRATE];
+extern __device__ const int c_ebiw_rate_nf[EBIW_NRATE];
+extern __device__ const int c_ebiw_rate_sp[EBIW_NRATE * 3];
+extern __device__ const int c_ebiw_pl_ptr[33];
+extern __device__ const int c_ebiw_pl_kind[EBIW_NPL];
+extern __device__ const int c_ebiw_pl_sp[EBIW_NPL];
+extern __device__ const int c_ebiw_pl_t0[EBIW_NPL + 1];
+extern __device__ const int c_ebiw_term_r[EBIW_NTERM > 0 ? EBIW_NTERM : 1];
+extern __device__ const double c_ebiw_term_c[EBIW_NTERM > 0 ? EBIW_NTERM : 1];
+namespace wsm {
+__device__ void ebi_hrg1(double* __restrict__ sm, double dtc);
+__device__ void ebi_hrg2(double* __restrict__ sm, double dtc);
+__device__ void ebi_hrg3(double* __restrict__ sm, double dtc);
+__device__ void ebi_hrg4(double* __restrict__ sm, double dtc);
+}  // namespace wsm
 __device__ __forceinline__ void jacdecomp_0(double* __restrict__ ws, double gdtinv)
 {
     jacdecomp_0_0(ws, gdtinv);
@@ -919,6 +947,16 @@ struct Traits {
     static constexpr int ADJ_GE = mech_cracmm2::ADJ_GE;
     static constexpr int ADJ_GK = mech_cracmm2::ADJ_GK;
     static constexpr int OFF_YAVE = mech_cracmm2::OFF_YAVE;
+    static constexpr int EBIW_YC = mech_cracmm2::EBIW_YC;
+    static constexpr int EBIW_YC0 = mech_cracmm2::EBIW_YC0;
+    static constexpr int EBIW_YCP = mech_cracmm2::EBIW_YCP;
+    static constexpr int EBIW_PROD = mech_cracmm2::EBIW_PROD;
+    static constexpr int EBIW_LOSS = mech_cracmm2::EBIW_LOSS;
+    static constexpr int EBIW_PNEG = mech_cracmm2::EBIW_PNEG;
+    static constexpr int EBIW_NOTMAX = mech_cracmm2::EBIW_NOTMAX;
+    static constexpr int EBIW_RKI = mech_cracmm2::EBIW_RKI;
+    static constexpr int EBIW_RXRAT = mech_cracmm2::EBIW_RXRAT;
+    static constexpr int EBIW_ELEMS = mech_cracmm2::EBIW_ELEMS;
     static constexpr const char* name() { return mech_cracmm2::NAME; }
     static __device__ __forceinline__ int iold2new(int s) { return mech_cracmm2::c_iold2new[s]; }
     static __device__ __forceinline__ int inew2old(int i) { return mech_cracmm2::c_inew2old[i]; }
@@ -954,9 +992,23 @@ struct Traits {
     static __device__ __forceinline__ void ebi_hrrates(double* ws) { mech_cracmm2::ebi_hrrates(ws); }
     static __device__ __forceinline__ void ebi_hrprodloss(double* ws) { mech_cracmm2::ebi_hrprodloss(ws); }
     static __device__ __forceinline__ void ebi_hrg1(double* ws, double dtc) { mech_cracmm2::ebi_hrg1(ws, dtc); }
+    static __device__ __forceinline__ void ebiw_hrg1(double* sm, double dtc) { mech_cracmm2::wsm::ebi_hrg1(sm, dtc); }
     static __device__ __forceinline__ void ebi_hrg2(double* ws, double dtc) { mech_cracmm2::ebi_hrg2(ws, dtc); }
+    static __device__ __forceinline__ void ebiw_hrg2(double* sm, double dtc) { mech_cracmm2::wsm::ebi_hrg2(sm, dtc); }
     static __device__ __forceinline__ void ebi_hrg3(double* ws, double dtc) { mech_cracmm2::ebi_hrg3(ws, dtc); }
+    static __device__ __forceinline__ void ebiw_hrg3(double* sm, double dtc) { mech_cracmm2::wsm::ebi_hrg3(sm, dtc); }
     static __device__ __forceinline__ void ebi_hrg4(double* ws, double dtc) { mech_cracmm2::ebi_hrg4(ws, dtc); }
+    static __device__ __forceinline__ void ebiw_hrg4(double* sm, double dtc) { mech_cracmm2::wsm::ebi_hrg4(sm, dtc); }
+    static constexpr int EBIW_NRATE = mech_cracmm2::EBIW_NRATE;
+    static __device__ __forceinline__ const int* ebiw_rate_r() { return mech_cracmm2::c_ebiw_rate_r; }
+    static __device__ __forceinline__ const int* ebiw_rate_nf() { return mech_cracmm2::c_ebiw_rate_nf; }
+    static __device__ __forceinline__ const int* ebiw_rate_sp() { return mech_cracmm2::c_ebiw_rate_sp; }
+    static __device__ __forceinline__ const int* ebiw_pl_ptr() { return mech_cracmm2::c_ebiw_pl_ptr; }
+    static __device__ __forceinline__ const int* ebiw_pl_kind() { return mech_cracmm2::c_ebiw_pl_kind; }
+    static __device__ __forceinline__ const int* ebiw_pl_sp() { return mech_cracmm2::c_ebiw_pl_sp; }
+    static __device__ __forceinline__ const int* ebiw_pl_t0() { return mech_cracmm2::c_ebiw_pl_t0; }
+    static __device__ __forceinline__ const int* ebiw_term_r() { return mech_cracmm2::c_ebiw_term_r; }
+    static __device__ __forceinline__ const double* ebiw_term_c() { return mech_cracmm2::c_ebiw_term_c; }
     static __device__ __forceinline__ void rconst(double* ws, double t, double p, double h, double sw, int sun,
                                                   const double* rj, const double* het) { mech_cracmm2::rconst(ws, t, p, h, sw, sun, rj, het); }
 };

@@ -28,6 +28,9 @@ struct MechOps {
     cudaError_t (*chem_ebi)(const chem::GridArgs&, const chem::QueueArgs&, const chem::EbiArgs&, int nblocks,
                             cudaStream_t);
     cudaError_t (*ebi_solve)(const chem::EbiSolveArgs&, int nblocks, cudaStream_t);
+    cudaError_t (*chem_ebi_warp)(const chem::GridArgs&, const chem::QueueArgs&, const chem::EbiArgs&, int nblocks,
+                                 cudaStream_t);
+    cudaError_t (*ebi_warp_occupancy)(int* blocks_per_sm);
     double ebi_deltat;
     int adj_ws_elems;
     cudaError_t (*adj_forward)(const adj::Args&, int nblocks, cudaStream_t);
@@ -96,6 +99,27 @@ struct MechOps {
         chem::k_chem_ebi_queue<T_><<<nb, chem::THREADS_PER_BLOCK, 0, s>>>(a, q, e);                 \
         return cudaGetLastError();                                                                  \
     }                                                                                               \
+    size_t ebiw_smem_() { return (size_t)chem::EBIW_WPB * T_::EBIW_ELEMS * sizeof(double); }        \
+    cudaError_t ebiw_attr_()                                                                        \
+    {                                                                                               \
+        return cudaFuncSetAttribute(chem::k_chem_ebi_warp<T_>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                    (int)ebiw_smem_());                                             \
+    }                                                                                               \
+    cudaError_t chem_ebi_warp_(const chem::GridArgs& a, const chem::QueueArgs& q, const chem::EbiArgs& e, \
+                               int nb, cudaStream_t s)                                              \
+    {                                                                                               \
+        cudaError_t r = ebiw_attr_();                                                               \
+        if (r != cudaSuccess) return r;                                                             \
+        chem::k_chem_ebi_warp<T_><<<nb, chem::EBIW_WPB * 32, ebiw_smem_(), s>>>(a, q, e);           \
+        return cudaGetLastError();                                                                  \
+    }                                                                                               \
+    cudaError_t ebi_warp_occupancy_(int* bps)                                                       \
+    {                                                                                               \
+        cudaError_t r = ebiw_attr_();                                                               \
+        if (r != cudaSuccess) return r;                                                             \
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, chem::k_chem_ebi_warp<T_>,        \
+                                                             chem::EBIW_WPB * 32, ebiw_smem_());    \
+    }                                                                                               \
     cudaError_t ebi_solve_(const chem::EbiSolveArgs& a, int nb, cudaStream_t s)                     \
     {                                                                                               \
         chem::k_ebi_solve<T_><<<nb, chem::THREADS_PER_BLOCK, 0, s>>>(a);                            \
@@ -143,6 +167,7 @@ struct MechOps {
                                    NS::FLOPS_STEP_DAY, NS::FLOPS_STEP_NIGHT,                        \
                                    NS::h_cgrid_index, NS::h_convert, NS::h_molwt, NS::h_inew2old,   \
                                    NS::h_iold2new, chem_static_, chem_queue_, queue_occupancy_,     \
-                                   solve_, chem_ebi_, ebi_solve_, T_::EBI_DELTAT,            \
+                                   solve_, chem_ebi_, ebi_solve_, chem_ebi_warp_, ebi_warp_occupancy_, \
+                                   T_::EBI_DELTAT,                                                  \
                                    T_::ADJ_WS_ELEMS, adj_forward_, adj_reverse_, adj_occupancy_, ddm_update_,     \
                                    rconst_, occupancy_};

@@ -187,7 +187,11 @@ def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src
               ("ADJ_WS_ELEMS", lay.adj_total), ("ADJ_LAM", lay.adj_lam), ("ADJ_MU1", lay.adj_mu1),
               ("ADJ_MU2", lay.adj_mu2), ("ADJ_MU3", lay.adj_mu3), ("ADJ_PHI", lay.adj_phi),
               ("ADJ_TMP", lay.adj_tmp), ("ADJ_EMIS", lay.adj_emis), ("ADJ_GE", lay.adj_ge),
-              ("ADJ_GK", lay.adj_gk), ("OFF_YAVE", lay.yave))
+              ("ADJ_GK", lay.adj_gk), ("OFF_YAVE", lay.yave),
+              # warp-cooperative EBI: one cell's state in shared memory (doubles)
+              ("EBIW_YC", 0), ("EBIW_YC0", ns), ("EBIW_YCP", 2 * ns), ("EBIW_PROD", 3 * ns),
+              ("EBIW_LOSS", 4 * ns), ("EBIW_PNEG", 5 * ns), ("EBIW_NOTMAX", 6 * ns), ("EBIW_RKI", 7 * ns),
+              ("EBIW_RXRAT", 7 * ns + nr), ("EBIW_ELEMS", 7 * ns + 2 * nr))
     for k, v in consts:
         h.append(f"constexpr int {k} = {v};")
     h.append(f"constexpr double FLOPS_STEP_DAY = {float(flop_counts(m, sp, 0)['step_total'])};")
@@ -233,6 +237,17 @@ def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src
             h.append(f"    static __device__ __forceinline__ void ebi_{nm}(double* ws) {{ {ns_name}::ebi_{nm}(ws); }}")
         for nm in ("hrg1", "hrg2", "hrg3", "hrg4"):
             h.append(f"    static __device__ __forceinline__ void ebi_{nm}(double* ws, double dtc) {{ {ns_name}::ebi_{nm}(ws, dtc); }}")
+            h.append(f"    static __device__ __forceinline__ void ebiw_{nm}(double* sm, double dtc) {{ {ns_name}::wsm::ebi_{nm}(sm, dtc); }}")
+        h.append(f"    static constexpr int EBIW_NRATE = {ns_name}::EBIW_NRATE;")
+        h.append(f"    static __device__ __forceinline__ const int* ebiw_rate_r() {{ return {ns_name}::c_ebiw_rate_r; }}")
+        h.append(f"    static __device__ __forceinline__ const int* ebiw_rate_nf() {{ return {ns_name}::c_ebiw_rate_nf; }}")
+        h.append(f"    static __device__ __forceinline__ const int* ebiw_rate_sp() {{ return {ns_name}::c_ebiw_rate_sp; }}")
+        h.append(f"    static __device__ __forceinline__ const int* ebiw_pl_ptr() {{ return {ns_name}::c_ebiw_pl_ptr; }}")
+        h.append(f"    static __device__ __forceinline__ const int* ebiw_pl_kind() {{ return {ns_name}::c_ebiw_pl_kind; }}")
+        h.append(f"    static __device__ __forceinline__ const int* ebiw_pl_sp() {{ return {ns_name}::c_ebiw_pl_sp; }}")
+        h.append(f"    static __device__ __forceinline__ const int* ebiw_pl_t0() {{ return {ns_name}::c_ebiw_pl_t0; }}")
+        h.append(f"    static __device__ __forceinline__ const int* ebiw_term_r() {{ return {ns_name}::c_ebiw_term_r; }}")
+        h.append(f"    static __device__ __forceinline__ const double* ebiw_term_c() {{ return {ns_name}::c_ebiw_term_c; }}")
     h.append("    static __device__ __forceinline__ void rconst(double* ws, double t, double p, double h, double sw, int sun,")
     h.append(f"                                                  const double* rj, const double* het) {{ {ns_name}::rconst(ws, t, p, h, sw, sun, rj, het); }}")
     h.append("};")

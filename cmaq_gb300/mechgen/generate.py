@@ -264,10 +264,74 @@ def ebi_oracle_source(ebi: dict, mech: str, nspec: int) -> str:
     return "\n".join(L)
 
 
+def ebi_warp_tables(ebi: dict) -> dict:
+    """Tables of HRRATES and HRPRODLOSS for the warp-cooperative EBI kernel.  Every
+    statement of both routines is a left-deep product RKI(r) * YC(a) * ... or a left-deep
+    sum of terms RXRAT(r) / c * RXRAT(r) (checked here), so a loop over a statement's
+    table entries performs the same operations in the same order as the straight-line
+    code.  HRPRODLOSS statements are spread over the 32 lanes longest first (each lane
+    gets the next statement while it has the least work)."""
+    rates = []
+    for lhs, rhs in ebi["routines"]["hrrates"][1]:
+        fac = []
+        node = rhs
+        while node[0] == "bin" and node[1] == "*":
+            if node[3][0] != "arr" or node[3][1] != "YC":
+                raise ValueError("unsupported HRRATES statement")
+            fac.append(node[3][2])
+            node = node[2]
+        if not (lhs[0] == "arr" and lhs[1] == "RXRAT" and node[0] == "arr" and node[1] == "RKI"
+                and node[2] == lhs[2] and len(fac) <= 3):
+            raise ValueError("unsupported HRRATES statement")
+        rates.append((lhs[2], list(reversed(fac))))
+
+    def terms(node):
+        if node[0] == "num" and node[1] == 0.0:
+            return []
+        if node[0] == "arr" and node[1] == "RXRAT":
+            return [(node[2], 1.0)]
+        if node[0] == "bin" and node[1] == "*" and node[2][0] == "num" and node[3][0] == "arr" \
+                and node[3][1] == "RXRAT":
+            return [(node[3][2], node[2][1])]
+        if node[0] == "bin" and node[1] == "+":
+            right = terms(node[3])
+            if len(right) != 1:
+                raise ValueError("unsupported HRPRODLOSS statement")
+            return terms(node[2]) + right
+        raise ValueError("unsupported HRPRODLOSS statement")
+    kinds = {"PROD": 0, "LOSS": 1, "PNEG": 2}
+    stmts = []
+    for lhs, rhs in ebi["routines"]["hrprodloss"][1]:
+        if lhs[0] != "arr" or lhs[1] not in kinds:
+            raise ValueError("unsupported HRPRODLOSS target")
+        stmts.append((kinds[lhs[1]], lhs[2], terms(rhs)))
+    load = [0] * 32
+    lanes = [[] for _ in range(32)]
+    for st in sorted(stmts, key=lambda t: -max(1, len(t[2]))):
+        k = min(range(32), key=lambda q: load[q])
+        lanes[k].append(st)
+        load[k] += max(1, len(st[2]))
+    ordered = [st for lane in lanes for st in lane]
+    ptr = [0]
+    for lane in lanes:
+        ptr.append(ptr[-1] + len(lane))
+    t0, tr, tc = [], [], []
+    for st in ordered:
+        t0.append(len(tr))
+        for (r, c) in st[2]:
+            tr.append(r)
+            tc.append(c)
+    t0.append(len(tr))
+    return {"rates": rates, "pl": ordered, "pl_ptr": ptr, "pl_t0": t0, "term_r": tr, "term_c": tc,
+            "max_lane_terms": max(load)}
+
+
 def ebi_cuda_source(ebi: dict, mech: str, nspec: int) -> tuple[str, str]:
     """(declarations for the mechanism header, translation unit of device routines)."""
     from .ebi_translate import c_routines
     ns_name = f"mech_{mech}"
+    wt = ebi_warp_tables(ebi)
+    nrate, npl, nterm = len(wt["rates"]), len(wt["pl"]), len(wt["term_r"])
     decl = [f"constexpr int EBI_N_EBISP = {len(ebi['ebisp'])};",
             f"constexpr double EBI_DELTAT = {c_double(ebi['deltat'])};",
             f"constexpr int EBI_NEBITER = {ebi['nebiter']};",
@@ -278,6 +342,22 @@ def ebi_cuda_source(ebi: dict, mech: str, nspec: int) -> tuple[str, str]:
     for name in ebi["routines"]:
         args = ", double dtc" if name.startswith("hrg") else ""
         decl.append(f"__device__ void ebi_{name}(double* __restrict__ ws{args});")
+    # warp-cooperative kernel: cell state in shared memory, tables of HRRATES / HRPRODLOSS
+    decl += [f"constexpr int EBIW_NRATE = {nrate};", f"constexpr int EBIW_NPL = {npl};",
+             f"constexpr int EBIW_NTERM = {nterm};",
+             "extern __device__ const int c_ebiw_rate_r[EBIW_NRATE];",
+             "extern __device__ const int c_ebiw_rate_nf[EBIW_NRATE];",
+             "extern __device__ const int c_ebiw_rate_sp[EBIW_NRATE * 3];",
+             "extern __device__ const int c_ebiw_pl_ptr[33];",
+             "extern __device__ const int c_ebiw_pl_kind[EBIW_NPL];",
+             "extern __device__ const int c_ebiw_pl_sp[EBIW_NPL];",
+             "extern __device__ const int c_ebiw_pl_t0[EBIW_NPL + 1];",
+             "extern __device__ const int c_ebiw_term_r[EBIW_NTERM > 0 ? EBIW_NTERM : 1];",
+             "extern __device__ const double c_ebiw_term_c[EBIW_NTERM > 0 ? EBIW_NTERM : 1];",
+             "namespace wsm {"]
+    for name in ("hrg1", "hrg2", "hrg3", "hrg4"):
+        decl.append(f"__device__ void ebi_{name}(double* __restrict__ sm, double dtc);")
+    decl.append("}  // namespace wsm")
     tu = [f"// Generated by cmaq_gb300.mechgen.generate from CCTM/src/gas/ebi_{mech}/hr*.F.  Do not edit.",
           "// Translated EBI routines HRRATES, HRPRODLOSS, HRG1-HRG4 on the per-cell workspace.",
           f'#include "{mech}_mech.cuh"', "#include <math.h>", f"namespace {ns_name} {{",
@@ -294,8 +374,38 @@ def ebi_cuda_source(ebi: dict, mech: str, nspec: int) -> tuple[str, str]:
           "#define EBI_PROD(i) ws[(EBI_OFF_PROD + (i)) * 32]",
           "#define EBI_LOSS(i) ws[(EBI_OFF_LOSS + (i)) * 32]",
           "#define EBI_PNEG(i) ws[(EBI_OFF_PNEG + (i)) * 32]",
-          c_routines(ebi, "__device__ __noinline__"),
-          f"}}  // namespace {ns_name}"]
+          c_routines(ebi, "__device__ __noinline__")]
+
+    def arr(ctype, name, vals, fmt=str):
+        vals = list(vals) or [0]
+        return f"__device__ const {ctype} {name}[{len(vals)}] = {{{', '.join(fmt(v) for v in vals)}}};"
+    tu += ["// tables of the warp-cooperative kernel (HRRATES / HRPRODLOSS as data, same operation order)",
+           arr("int", "c_ebiw_rate_r", [r for r, _ in wt["rates"]]),
+           arr("int", "c_ebiw_rate_nf", [len(f) for _, f in wt["rates"]]),
+           arr("int", "c_ebiw_rate_sp", [x for _, f in wt["rates"] for x in (f + [0, 0, 0])[:3]]),
+           arr("int", "c_ebiw_pl_ptr", wt["pl_ptr"]),
+           arr("int", "c_ebiw_pl_kind", [k for k, _, _ in wt["pl"]]),
+           arr("int", "c_ebiw_pl_sp", [sp for _, sp, _ in wt["pl"]]),
+           arr("int", "c_ebiw_pl_t0", wt["pl_t0"]),
+           arr("int", "c_ebiw_term_r", wt["term_r"]),
+           arr("double", "c_ebiw_term_c", wt["term_c"], c_double),
+           "// HRG1-HRG4 on the warp's shared-memory cell state (run by one lane)",
+           "namespace wsm {",
+           "#undef EBI_CELL_ARGS", "#undef EBI_YC", "#undef EBI_YC0", "#undef EBI_YCP", "#undef EBI_RKI",
+           "#undef EBI_RXRAT", "#undef EBI_PROD", "#undef EBI_LOSS", "#undef EBI_PNEG",
+           "#define EBI_CELL_ARGS double* __restrict__ sm",
+           "#define EBI_YC(i) sm[EBIW_YC + (i)]",
+           "#define EBI_YC0(i) sm[EBIW_YC0 + (i)]",
+           "#define EBI_YCP(i) sm[EBIW_YCP + (i)]",
+           "#define EBI_RKI(r) sm[EBIW_RKI + (r)]",
+           "#define EBI_RXRAT(r) sm[EBIW_RXRAT + (r)]",
+           "#define EBI_PROD(i) sm[EBIW_PROD + (i)]",
+           "#define EBI_LOSS(i) sm[EBIW_LOSS + (i)]",
+           "#define EBI_PNEG(i) sm[EBIW_PNEG + (i)]",
+           c_routines({**ebi, "routines": {k: v for k, v in ebi["routines"].items() if k.startswith("hrg")}},
+                      "__device__ __noinline__"),
+           "}  // namespace wsm",
+           f"}}  // namespace {ns_name}"]
     return "\n".join(decl), "\n".join(tu) + "\n"
 
 

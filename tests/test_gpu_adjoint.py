@@ -134,3 +134,28 @@ def test_tape_budget_batches_give_the_same_gradients(case):
     assert np.array_equal(res[0][0], res[1][0])
     assert np.array_equal(res[0][2], res[1][2])
     assert _rel_vec(res[1][1], res[0][1]) < 1e-12
+
+
+@pytest.mark.parametrize("ncell", [1, 33])
+def test_adjoint_on_ragged_cell_counts(ncell):
+    """One cell and one cell more than a warp: the queue and the tape offsets cover ragged
+    sizes; gradients match the oracle."""
+    import torch
+    from oracle import AdjointWindow, Oracle
+    from cmaq_gb300.adjoint import Ros3Window
+    from cmaq_gb300.chem import ChemSolver
+    o = Oracle("cb6r5_ae7_aq")
+    g = make_grid(ncols=ncell, nrows=1, nlays=1, seed=42)
+    y0, rki, night = gather_cells(g, o)
+    ow = AdjointWindow(o, rki, night, 2, 5.0, RTOL, ATOL, threads=2)
+    y_ref = ow.forward(y0)
+    lam_ref, gk_ref, _ = ow.backward(np.ones_like(y_ref))
+    s = ChemSolver("cb6r5_ae7_aq", ncols=ncell, nrows=1, nlays=1, nspcsd=g.nspcsd, rtol=1e-3, atol=1e-9)
+    w = Ros3Window(s, torch.from_numpy(rki).cuda(), torch.from_numpy(night).cuda(), 2, 5.0)
+    a = torch.from_numpy(y0).cuda().requires_grad_(True)
+    k = torch.zeros(o.nrxns, dtype=torch.float64, device="cuda", requires_grad=True)
+    y = w(a, k)
+    assert rel_err(y.detach().cpu().numpy(), y_ref) < 1e-9
+    y.sum().backward()
+    assert _rel_vec(a.grad.cpu().numpy(), lam_ref) < 1e-7
+    assert _rel_vec(k.grad.cpu().numpy(), gk_ref) < 1e-7
