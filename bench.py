@@ -144,7 +144,7 @@ def run_device(g, schedule: str, steps: int, warmup: int, dist, device: int, sam
     conc0 = dev["conc"].clone()
     s = ChemSolver(g.mech, ncols=g.ncols, nrows=g.nrows, nlays=g.nlays, nspcsd=g.nspcsd, cgrid_index=g.cgrid_index,
                    rtol=RTOL, atol=ATOL, schedule=schedule, device=device, solver=solver,
-                   variant=(tuned or {}).get("variant", "r255"))
+                   variant=(tuned or {}).get("variant", "default"))
     if tuned:
         s.set_tuning(block_warps=tuned["block_warps"], lockstep=tuned["lockstep"])
     stream = torch.cuda.current_stream(device)

@@ -43,9 +43,9 @@ class MechInfo(C.Structure):
 
 
 @lru_cache(maxsize=None)
-def lib(variant: str = "r255") -> C.CDLL:
+def lib(variant: str = "default") -> C.CDLL:
     """The library build of one register-cap variant (see cmaq_gb300/build.py)."""
-    path = LIB_PATH if variant == "r255" else LIB_PATH.parent / variant / "libcmaqchem.so"
+    path = LIB_PATH if variant == "default" else LIB_PATH.parent / variant / "libcmaqchem.so"
     if not path.exists():
         raise ChemError(f"{path} is not built; run `python -m cmaq_gb300.build {variant}` (needs nvcc)")
     L = C.CDLL(str(path))

@@ -8,9 +8,9 @@ of a sample of the grid for each candidate:
 
 * cells per block: 64, 128 or 256 (``block_warps`` 2, 4, 8; one cell per thread);
 * register cap and prefetch: library variants of ``cmaq_gb300.build`` (the default
-  library caps the generated functions at 168 registers and prefetches workspace rows;
-  ``nopf`` without the prefetch, ``full255`` neither (8 warps per SM), ``r168`` caps
-  every function);
+  library caps the generated functions at 128 registers for 16 warps per SM and
+  prefetches workspace rows; ``g168`` 168 registers and 12 warps; ``nopf`` 168 without
+  the prefetch; ``full255`` no cap (8 warps); ``r168`` caps every function);
 * queue granularity: whether the block's warps pass barriers between the phases of
   each step attempt (``lockstep`` 1), also between the generated chunks of the LU
   and the solves (2), or run free (0, 256-cell blocks only); a lane always refills
@@ -36,7 +36,7 @@ KEYS = ("conc", "ta", "qv", "dens", "pres", "seaice", "ocean_szone", "rj", "khet
 
 @dataclass(frozen=True)
 class Candidate:
-    variant: str = "r255"
+    variant: str = "default"
     lockstep: int = 1
     block_warps: int = 4
 
@@ -45,7 +45,7 @@ class Candidate:
         return {"block_warps": self.block_warps, "lockstep": self.lockstep}
 
 
-def candidates(variants=("r255", "nopf", "full255", "r168")) -> list[Candidate]:
+def candidates(variants=("default", "g168", "nopf", "full255", "r168")) -> list[Candidate]:
     out = []
     for v in variants:
         out.append(Candidate(v, 0, 8))

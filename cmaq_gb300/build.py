@@ -22,14 +22,15 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = BUILD / "libcmaqchem.so"
 # Build variants the autotuner can choose from: name -> (extra nvcc flags of the generated
-# mechanism code, extra flags of every translation unit).  The default ("r255" is the name
-# of the default library) caps the generated LU / solve / rate functions at 168 registers
-# and turns on their L2 prefetch a few rows ahead; together with the work-queue kernel's
-# launch bounds (12 resident warps per SM) this measured fastest.  The EBI routines and the
-# kernels themselves are not capped.
-GEN_DEFAULT = ["-maxrregcount=168", "-DCHEM_USE_PREFETCH"]
+# mechanism code, extra flags of every translation unit).  The default library caps the
+# generated LU / solve / rate / adjoint functions at 128 registers and turns on their L2
+# prefetch a few rows ahead, and the work-queue kernel carries launch bounds for 16
+# resident warps per SM; this measured fastest (see the launch-shape sweep in profiles/).
+# The EBI routines and the kernels' own code are not capped.
+GEN_DEFAULT = ["-maxrregcount=128", "-DCHEM_USE_PREFETCH"]
 Q8 = "-DCHEM_QUEUE_WARPS_PER_SM=8"
-VARIANTS = {"r255": (GEN_DEFAULT, []),
+VARIANTS = {"default": (GEN_DEFAULT, ["-DCHEM_QUEUE_WARPS_PER_SM=16"]),
+            "g168": (["-maxrregcount=168", "-DCHEM_USE_PREFETCH"], []),
             "nopf": (["-maxrregcount=168"], []),
             "full255": ([], [Q8]), "pf255": (["-DCHEM_USE_PREFETCH"], [Q8]),
             "r168": ([], ["-maxrregcount=168"]),
@@ -61,15 +62,15 @@ def _headers() -> list[Path]:
             + sorted((PKG.parent / "include").glob("*.h")))
 
 
-def lib_path(variant: str = "r255") -> Path:
-    return LIB if variant == "r255" else BUILD / variant / "libcmaqchem.so"
+def lib_path(variant: str = "default") -> Path:
+    return LIB if variant == "default" else BUILD / variant / "libcmaqchem.so"
 
 
-def build(jobs: int | None = None, verbose: bool = False, variant: str = "r255") -> Path:
+def build(jobs: int | None = None, verbose: bool = False, variant: str = "default") -> Path:
     """Build one register-cap variant (``r255`` is the default library)."""
     if variant not in VARIANTS:
         raise ValueError(f"unknown variant {variant}")
-    out_dir = BUILD if variant == "r255" else BUILD / variant
+    out_dir = BUILD if variant == "default" else BUILD / variant
     out_dir.mkdir(parents=True, exist_ok=True)
     lib = lib_path(variant)
     gen_extra, all_extra = (list(x) for x in VARIANTS[variant])
@@ -108,6 +109,6 @@ def build(jobs: int | None = None, verbose: bool = False, variant: str = "r255")
 
 
 if __name__ == "__main__":
-    for v in (sys.argv[1:] or ["r255"]):
+    for v in (sys.argv[1:] or ["default"]):
         print(build(verbose=True, variant=v))
     sys.exit(0)

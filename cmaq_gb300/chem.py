@@ -64,7 +64,7 @@ class ChemSolver:
 
     def __init__(self, mechanism: str = "cb6r5_ae7_aq", *, ncols: int, nrows: int, nlays: int, nspcsd: int,
                  cgrid_index=None, rtol: float = 1.0e-3, atol: float = 1.0e-7, schedule: str = "queue",
-                 device: int = 0, max_iter: int = 0, reference_tolerances: bool = True, variant: str = "r255",
+                 device: int = 0, max_iter: int = 0, reference_tolerances: bool = True, variant: str = "default",
                  solver: str = "ros3"):
         if solver not in SOLVERS:
             raise ChemError(f"unknown solver {solver!r}; use one of {sorted(SOLVERS)}")

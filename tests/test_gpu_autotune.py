@@ -13,11 +13,11 @@ def test_tune_returns_and_caches_a_candidate(tmp_path):
     from helpers import to_cuda
     g = make_grid(ncols=10, nrows=8, nlays=3, seed=61)
     cache = tmp_path / "tune.json"
-    res = tune(g, nsteps=1, variants=("r255",), cache=cache)
+    res = tune(g, nsteps=1, variants=("default",), cache=cache)
     assert {"variant", "lockstep", "block_warps", "ms"} <= set(res)
-    assert len(res["table"]) == len(candidates(("r255",)))
+    assert len(res["table"]) == len(candidates(("default",)))
     assert res["ms"] == min(r["ms"] for r in res["table"])
-    again = tune(g, nsteps=1, variants=("r255",), cache=cache)
+    again = tune(g, nsteps=1, variants=("default",), cache=cache)
     assert again == res
     # the tuned solver and the default one agree bit for bit
     outs = []
