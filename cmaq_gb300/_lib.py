@@ -62,9 +62,9 @@ def lib(variant: str = "default") -> C.CDLL:
     L.cmaqchem_ros3_solve_device.argtypes = [vp, C.c_longlong, vp, vp, vp, C.c_double, vp, vp, vp, vp]
     L.cmaqchem_ebi_solve_device.argtypes = [vp, C.c_longlong, vp, vp, C.c_int, vp, vp, vp]
     L.cmaqchem_adj_forward.argtypes = [vp, C.c_longlong, vp, vp, C.c_longlong, vp, vp, vp, C.c_int, C.c_double,
-                                       vp, vp, vp]
+                                       vp, vp, vp, C.c_size_t, vp]
     L.cmaqchem_adj_backward.argtypes = [vp, C.c_longlong, vp, vp, C.c_longlong, vp, vp, vp, C.c_int, C.c_double,
-                                        vp, vp, vp, vp, vp]
+                                        vp, vp, vp, C.c_size_t, vp, vp, vp]
     L.cmaqchem_rconst_device.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     L.cmaqchem_mech_info_get.argtypes = [C.c_char_p, C.POINTER(MechInfo), ip]
     L.cmaqchem_destroy.argtypes = [vp]

@@ -36,7 +36,10 @@ class Ros3Window:
     the solver handle, rate constants rki [nrxns, n] (or [nsync, nrxns, n], one plane per
     synchronisation step) and the night flags [n] (uint8, night reaction list)."""
 
-    def __init__(self, solver: ChemSolver, rki, night, nsync: int, chemstep: float = 5.0):
+    def __init__(self, solver: ChemSolver, rki, night, nsync: int, chemstep: float = 5.0, tape_bytes=None):
+        """tape_bytes: device memory for the tape the forward pass records (None: up to half
+        the free memory, sized for about 16 accepted steps per cell and step; 0: no tape,
+        the backward pass re-runs every step from its checkpoint)."""
         if rki.dtype != torch.float64 or night.dtype != torch.uint8:
             raise ChemError("rki must be float64 and night uint8")
         if rki.dim() not in (2, 3) or not rki.is_contiguous():
@@ -47,6 +50,11 @@ class Ros3Window:
         self.nsync, self.chemstep = int(nsync), float(chemstep)
         self.n = rki.shape[-1]
         self.stride = 0 if rki.dim() == 2 else rki.shape[1] * rki.shape[2]
+        if tape_bytes is None:
+            free, _ = torch.cuda.mem_get_info(rki.device)
+            want = self.n * self.nsync * (16 * (solver.info.ischan + 1) * 8 + 64)
+            tape_bytes = min(want, free // 2)
+        self.tape_bytes = int(tape_bytes)
 
     def __call__(self, y0, log_k=None, emis=None):
         return Ros3WindowFn.apply(y0, log_k, emis, self)
@@ -67,13 +75,16 @@ class Ros3WindowFn(torch.autograd.Function):
         e = None if emis is None else emis.detach().to(torch.float64).contiguous()
         ck = torch.empty((w.nsync, ischan, w.n), dtype=torch.float64, device=y.device)
         nsteps = torch.empty((w.nsync, w.n), dtype=torch.int32, device=y.device)
+        tape = torch.empty(w.tape_bytes, dtype=torch.uint8, device=y.device) if w.tape_bytes > 0 else None
         rc = s._L.cmaqchem_adj_forward(s._h, w.n, _ptr(y), _ptr(w.rki), w.stride, _ptr(w.night), _ptr(kmult),
-                                       _ptr(e), w.nsync, w.chemstep, _ptr(ck), _ptr(nsteps), _stream())
+                                       _ptr(e), w.nsync, w.chemstep, _ptr(ck), _ptr(nsteps), _ptr(tape),
+                                       w.tape_bytes, _stream())
         check(rc, s._L)
         if rc > 0:
             raise ChemError(f"{rc} cell-steps failed in the chemistry window")
         ctx.w = w
         ctx.has_k, ctx.has_e = log_k is not None, emis is not None
+        ctx.tape = tape
         ctx.save_for_backward(ck, nsteps, *(t for t in (kmult, e) if t is not None))
         return y
 
@@ -89,14 +100,16 @@ class Ros3WindowFn(torch.autograd.Function):
         gk = torch.zeros(s.info.nrxns, dtype=torch.float64, device=lam.device)
         ge = torch.zeros_like(e) if (e is not None and ctx.needs_input_grad[2]) else None
         rc = s._L.cmaqchem_adj_backward(s._h, w.n, _ptr(lam), _ptr(w.rki), w.stride, _ptr(w.night), _ptr(kmult),
-                                        _ptr(e), w.nsync, w.chemstep, _ptr(ck), _ptr(nsteps), _ptr(gk), _ptr(ge),
-                                        _stream())
+                                        _ptr(e), w.nsync, w.chemstep, _ptr(ck), _ptr(nsteps), _ptr(ctx.tape),
+                                        w.tape_bytes if ctx.tape is not None else 0, _ptr(gk), _ptr(ge), _stream())
         check(rc, s._L)
+        ctx.tape = None
         return (lam if ctx.needs_input_grad[0] else None,
                 gk if ctx.has_k and ctx.needs_input_grad[1] else None,
                 ge, None)
 
 
-def ros3_window(solver: ChemSolver, y0, rki, night, nsync: int, chemstep: float = 5.0, log_k=None, emis=None):
+def ros3_window(solver: ChemSolver, y0, rki, night, nsync: int, chemstep: float = 5.0, log_k=None, emis=None,
+                tape_bytes=None):
     """y at the end of ``nsync`` synchronisation steps; differentiable in y0, log_k, emis."""
-    return Ros3Window(solver, rki, night, nsync, chemstep)(y0, log_k, emis)
+    return Ros3Window(solver, rki, night, nsync, chemstep, tape_bytes)(y0, log_k, emis)

@@ -38,6 +38,7 @@ namespace adj {
 
 constexpr int WPB = 8;
 constexpr int THREADS = WPB * 32;
+constexpr int TAPE_BLOCK = 4;
 
 struct Args {
     long long ncell;
@@ -63,6 +64,16 @@ struct Args {
     const long long* tape_off;     // [ncell] first tape entry of each cell (tape forward, reverse)
     double* tape_y;                // [entries][ischan] Y before each accepted step
     double* tape_h;                // [entries] its step size
+    // tape recorded by the forward pass itself: linked blocks of TAPE_BLOCK accepted
+    // steps per cell and synchronisation step, taken from a pool with one atomic each
+    double* pool_y;                // [pool_blocks * TAPE_BLOCK][ischan]
+    double* pool_h;                // [pool_blocks * TAPE_BLOCK]
+    long long* pool_prev;          // [pool_blocks] previous block of the same cell and step, -1: none
+    long long pool_blocks;
+    unsigned long long* pool_head; // blocks taken so far
+    unsigned int* pool_ovf;        // cells of this step whose tape did not fit (the step is re-run)
+    long long* last_block;         // [ncell] last block of each cell in this step (-1: no accepted step)
+    int* last_fill;                // [ncell] entries used in that block
     // reverse
     double* lam;                   // [ischan][ncell] dL/dY at the end of the step in, at its start out
     double* grad_logk;             // [nrxns] += dL/dlog kmult
@@ -120,9 +131,11 @@ __global__ void __launch_bounds__(THREADS, 1) k_adj_forward(Args a)
 {
     double* ws = lane_ws<M>(a.ws);
     const bool taping = a.tape_off != nullptr;
+    const bool pooling = !taping && a.pool_y != nullptr;
     ros3::CellState s;
-    long long cell = -1, base = 0;
-    int cap = 0, written = -1;
+    long long cell = -1, base = 0, blk = -1;
+    int cap = 0, written = -1, fill = TAPE_BLOCK;
+    bool pool_ok = true;
     bool cnight = false, drained = false;
     unsigned long long overruns = 0, failed = 0;
     for (;;) {
@@ -138,6 +151,12 @@ __global__ void __launch_bounds__(THREADS, 1) k_adj_forward(Args a)
                     base = a.tape_off[cell] - a.tape_base;
                     cap = a.nsteps[cell];
                     written = -1;
+                }
+                if (pooling) {
+                    blk = -1;
+                    fill = TAPE_BLOCK;
+                    written = -1;
+                    pool_ok = true;
                 }
             }
         }
@@ -156,16 +175,49 @@ __global__ void __launch_bounds__(THREADS, 1) k_adj_forward(Args a)
                 written = nacc;
             }
         }
+        if (busy && pooling && pool_ok) {
+            h = s.dt;
+            if (s.tnow + h > a.chemstep) h = a.chemstep - s.tnow;
+            if (written != nacc) {   // a slot for this accepted-step candidate
+                if (fill == TAPE_BLOCK) {
+                    const unsigned long long nb = atomicAdd(a.pool_head, 1ull);
+                    if ((long long)nb < a.pool_blocks) {
+                        a.pool_prev[nb] = blk;
+                        blk = (long long)nb;
+                        fill = 0;
+                    } else {
+                        pool_ok = false;
+                    }
+                }
+                if (pool_ok) {
+                    double* t = a.pool_y + (size_t)(blk * TAPE_BLOCK + fill) * M::ISCHAN;
+                    for (int i = 0; i < M::ISCHAN; ++i) t[i] = ws[(M::OFF_Y + i) * 32];
+                    written = nacc;
+                }
+            }
+        }
         ros3::attempt_phased<M, 0, true>(ws, s, a.chemstep, a.tol, night, a.max_iter, busy);
         if (busy) {
             if (taping && s.st.nsteps != nacc) {
                 if (nacc < cap) a.tape_h[base + nacc] = h;
                 else overruns++;
             }
+            if (pooling && pool_ok && s.st.nsteps != nacc) {
+                a.pool_h[blk * TAPE_BLOCK + fill] = h;
+                fill++;
+            }
             if (ros3::finished(s, a.chemstep)) {
                 if (a.y_out)
                     for (int i = 0; i < M::ISCHAN; ++i) a.y_out[(size_t)i * a.ncell + cell] = ws[(M::OFF_Y + i) * 32];
                 if (!taping) a.nsteps[cell] = s.st.nsteps;
+                if (pooling) {
+                    if (pool_ok) {
+                        a.last_block[cell] = blk;
+                        a.last_fill[cell] = fill;
+                    } else {
+                        atomicAdd(a.pool_ovf, 1u);
+                    }
+                }
                 if (a.status) a.status[cell] = s.st.status;
                 failed += s.st.status != ros3::ST_OK;
                 cell = -1;
@@ -249,8 +301,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_adj_reverse(Args a)
 {
     double* ws = lane_ws<M>(a.ws);
     for (int r = 0; r < M::NRXNS; ++r) ws[(M::ADJ_GK + r) * 32] = 0.0;
-    long long cell = -1, base = 0;
-    int left = 0;
+    long long cell = -1, base = 0, blk = -1;
+    int left = 0, fill = 0;
+    const bool pooled = a.last_block != nullptr;
     bool cnight = false, drained = false;
     unsigned long long ncells = 0;
     for (;;) {
@@ -264,8 +317,13 @@ __global__ void __launch_bounds__(THREADS, 1) k_adj_reverse(Args a)
                     ws[(M::ADJ_GE + i) * 32] = 0.0;
                 }
                 cnight = a.night[cell] != 0;
-                base = a.tape_off[cell] - a.tape_base;
                 left = a.nsteps[cell];
+                if (pooled) {
+                    blk = a.last_block[cell];
+                    fill = a.last_fill[cell];
+                } else {
+                    base = a.tape_off[cell] - a.tape_base;
+                }
             }
         }
         const bool busy = cell >= 0;
@@ -274,9 +332,20 @@ __global__ void __launch_bounds__(THREADS, 1) k_adj_reverse(Args a)
         const bool night = __all_sync(0xffffffffu, !work || cnight);
         if (work) {
             --left;
-            const double* t = a.tape_y + (size_t)(base + left) * M::ISCHAN;
+            size_t e;
+            if (pooled) {
+                if (fill == 0) {
+                    blk = a.pool_prev[blk];
+                    fill = TAPE_BLOCK;
+                }
+                --fill;
+                e = (size_t)(blk * TAPE_BLOCK + fill);
+            } else {
+                e = (size_t)(base + left);
+            }
+            const double* t = (pooled ? a.pool_y : a.tape_y) + e * M::ISCHAN;
             for (int i = 0; i < M::ISCHAN; ++i) ws[(M::OFF_Y + i) * 32] = t[i];
-            reverse_step<M>(ws, a.tape_h[base + left], night);
+            reverse_step<M>(ws, (pooled ? a.pool_h : a.tape_h)[e], night);
         }
         if (busy && left == 0) {
             for (int i = 0; i < M::ISCHAN; ++i) a.lam[(size_t)i * a.ncell + cell] = ws[(M::ADJ_LAM + i) * 32];

@@ -93,7 +93,7 @@ struct cmaqchem_handle {
     // tuning knobs (cmaqchem_diag_set_tuning)
     int use_night = 1;
     int q_sync = 1;          // work-queue kernel: barriers between attempt phases
-    int q_wpb = 4;           // work-queue kernel: warps per block
+    int q_wpb = 8;           // work-queue kernel: warps per block
     int q_nblocks = 0;
     int q_bps_cap = 0;       // blocks per SM of the queue kernel, 0: as many as fit
     int ebi_warp = 1;        // EBI: 1 one cell per warp (shared memory), 0 one cell per lane
@@ -777,6 +777,46 @@ adj::Args adj_args(cmaqchem_handle* h, long long ncell, const double* rki, const
     return a;
 }
 
+// Carving of a caller's forward-tape buffer: head, per-step overflow counters, per-step
+// last block and fill of every cell, then the block pool (previous-block links, step
+// sizes, states).
+struct TapePool {
+    unsigned long long* head = nullptr;
+    unsigned int* ovf = nullptr;
+    long long* last_block = nullptr;
+    int* last_fill = nullptr;
+    long long* prev = nullptr;
+    double* h = nullptr;
+    double* y = nullptr;
+    long long blocks = 0;
+};
+
+TapePool carve_pool(void* buf, size_t bytes, long long ncell, int nsync, int ischan)
+{
+    TapePool t;
+    if (!buf) return t;
+    auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    size_t off = 0;
+    const size_t o_head = off; off = align(off + sizeof(unsigned long long));
+    const size_t o_ovf = off; off = align(off + sizeof(unsigned int) * nsync);
+    const size_t o_lb = off; off = align(off + sizeof(long long) * nsync * ncell);
+    const size_t o_lf = off; off = align(off + sizeof(int) * nsync * ncell);
+    if (bytes <= off) return t;
+    const size_t per_block = sizeof(long long) + adj::TAPE_BLOCK * sizeof(double) * (1 + (size_t)ischan);
+    const long long nb = (long long)((bytes - off - 3 * 256) / per_block);
+    if (nb < 1) return t;
+    char* b = (char*)buf;
+    t.head = (unsigned long long*)(b + o_head);
+    t.ovf = (unsigned int*)(b + o_ovf);
+    t.last_block = (long long*)(b + o_lb);
+    t.last_fill = (int*)(b + o_lf);
+    t.prev = (long long*)(b + off); off = align(off + sizeof(long long) * nb);
+    t.h = (double*)(b + off); off = align(off + sizeof(double) * nb * adj::TAPE_BLOCK);
+    t.y = (double*)(b + off);
+    t.blocks = nb;
+    return t;
+}
+
 int adj_check(cmaqchem_handle* h, long long ncell, const void* y, const double* rki, const unsigned char* night,
               int nsync, double chemstep, const void* ck, const int* nsteps)
 {
@@ -794,13 +834,18 @@ int adj_check(cmaqchem_handle* h, long long ncell, const void* y, const double* 
 extern "C" int cmaqchem_adj_forward(cmaqchem_handle* h, long long ncell, double* y, const double* rki,
                                     long long rki_sync_stride, const unsigned char* night, const double* kmult,
                                     const double* emis, int nsync, double chemstep_min, double* checkpoints,
-                                    int* nsteps, void* stream)
+                                    int* nsteps, void* tape, size_t tape_bytes, void* stream)
 {
     if (adj_check(h, ncell, y, rki, night, nsync, chemstep_min, checkpoints, nsteps)) return -1;
     CK(cudaSetDevice(h->device));
     cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
     if (adj_setup(h, ncell)) return -1;
     CK(cudaMemsetAsync(h->d_adj_counters, 0, 3 * sizeof(unsigned long long), s));
+    const TapePool pool = carve_pool(tape, tape_bytes, ncell, nsync, h->ops->ischan);
+    if (pool.blocks > 0) {
+        CK(cudaMemsetAsync(pool.head, 0, sizeof(unsigned long long), s));
+        CK(cudaMemsetAsync(pool.ovf, 0, sizeof(unsigned int) * nsync, s));
+    }
     const size_t plane = (size_t)h->ops->ischan * ncell;
     for (int k = 0; k < nsync; ++k) {
         double* ck = checkpoints + (size_t)k * plane;
@@ -810,6 +855,16 @@ extern "C" int cmaqchem_adj_forward(cmaqchem_handle* h, long long ncell, double*
         a.y_out = y;
         a.nsteps = nsteps + (size_t)k * ncell;
         a.status = h->d_adj_status;
+        if (pool.blocks > 0) {
+            a.pool_y = pool.y;
+            a.pool_h = pool.h;
+            a.pool_prev = pool.prev;
+            a.pool_blocks = pool.blocks;
+            a.pool_head = pool.head;
+            a.pool_ovf = pool.ovf + k;
+            a.last_block = pool.last_block + (size_t)k * ncell;
+            a.last_fill = pool.last_fill + (size_t)k * ncell;
+        }
         if (k > 0) {
             if (adj_order(h, nsteps + (size_t)(k - 1) * ncell, ncell, s)) return -1;
             a.order = h->d_adj_order;
@@ -826,13 +881,48 @@ extern "C" int cmaqchem_adj_forward(cmaqchem_handle* h, long long ncell, double*
 extern "C" int cmaqchem_adj_backward(cmaqchem_handle* h, long long ncell, double* lambda, const double* rki,
                                      long long rki_sync_stride, const unsigned char* night, const double* kmult,
                                      const double* emis, int nsync, double chemstep_min, const double* checkpoints,
-                                     const int* nsteps, double* grad_logk, double* grad_emis, void* stream)
+                                     const int* nsteps, const void* tape, size_t tape_bytes, double* grad_logk,
+                                     double* grad_emis, void* stream)
 {
     if (adj_check(h, ncell, lambda, rki, night, nsync, chemstep_min, checkpoints, nsteps)) return -1;
     if (!grad_logk) return fail("null array argument");
     CK(cudaSetDevice(h->device));
     cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
     if (adj_setup(h, ncell)) return -1;
+    // steps whose tape the forward pass recorded completely skip the re-run
+    const TapePool pool = carve_pool(const_cast<void*>(tape), tape_bytes, ncell, nsync, h->ops->ischan);
+    std::vector<unsigned int> ovf(nsync, 1u);
+    if (pool.blocks > 0) {
+        CK(cudaMemcpyAsync(ovf.data(), pool.ovf, sizeof(unsigned int) * nsync, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+    }
+    bool need_rerun = false;
+    for (unsigned int v : ovf) need_rerun = need_rerun || v != 0;
+    if (!need_rerun) {
+        CK(cudaMemsetAsync(h->d_adj_counters, 0, 3 * sizeof(unsigned long long), s));
+        for (int k = nsync - 1; k >= 0; --k) {
+            adj::Args a = adj_args(h, ncell, rki + (size_t)k * rki_sync_stride, night, kmult, emis, chemstep_min);
+            a.nsteps = const_cast<int*>(nsteps) + (size_t)k * ncell;
+            a.pool_y = pool.y;
+            a.pool_h = pool.h;
+            a.pool_prev = pool.prev;
+            a.pool_blocks = pool.blocks;
+            a.last_block = pool.last_block + (size_t)k * ncell;
+            a.last_fill = pool.last_fill + (size_t)k * ncell;
+            if (adj_order(h, a.nsteps, ncell, s)) return -1;
+            a.order = h->d_adj_order;
+            a.lam = lambda;
+            a.grad_logk = grad_logk;
+            a.grad_emis = grad_emis;
+            CK(cudaMemsetAsync(h->d_head, 0, sizeof(unsigned long long), s));
+            CK(h->ops->adj_reverse(a, h->adj_nblocks, s));
+        }
+        unsigned long long cnt[3];
+        CK(cudaMemcpyAsync(cnt, h->d_adj_counters, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        if (cnt[1] != (unsigned long long)ncell * nsync) return fail("reverse sweep did not visit every cell");
+        return 0;
+    }
     // tape offsets of every synchronisation step
     const int ntiles = (int)((ncell + adj::SCAN_TILE - 1) / adj::SCAN_TILE);
     if (grow(&h->d_tape_off, &h->tape_off_cap, (size_t)nsync * ncell)) return -1;
@@ -885,6 +975,24 @@ extern "C" int cmaqchem_adj_backward(cmaqchem_handle* h, long long ncell, double
     std::vector<long long> off;
     std::vector<int> nst;
     for (int k = nsync - 1; k >= 0; --k) {
+        if (pool.blocks > 0 && ovf[k] == 0) {   // this step's tape is complete in the pool
+            adj::Args a = adj_args(h, ncell, rki + (size_t)k * rki_sync_stride, night, kmult, emis, chemstep_min);
+            a.nsteps = const_cast<int*>(nsteps) + (size_t)k * ncell;
+            a.pool_y = pool.y;
+            a.pool_h = pool.h;
+            a.pool_prev = pool.prev;
+            a.pool_blocks = pool.blocks;
+            a.last_block = pool.last_block + (size_t)k * ncell;
+            a.last_fill = pool.last_fill + (size_t)k * ncell;
+            if (adj_order(h, a.nsteps, ncell, s)) return -1;
+            a.order = h->d_adj_order;
+            a.lam = lambda;
+            a.grad_logk = grad_logk;
+            a.grad_emis = grad_emis;
+            CK(cudaMemsetAsync(h->d_head, 0, sizeof(unsigned long long), s));
+            CK(h->ops->adj_reverse(a, h->adj_nblocks, s));
+            continue;
+        }
         adj::Args a = adj_args(h, ncell, rki + (size_t)k * rki_sync_stride, night, kmult, emis, chemstep_min);
         a.nsteps = const_cast<int*>(nsteps) + (size_t)k * ncell;
         a.tape_off = h->d_tape_off + (size_t)k * ncell;

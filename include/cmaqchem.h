@@ -165,21 +165,28 @@ int cmaqchem_ebi_solve_device(cmaqchem_handle* h, long long ncell, double* yc, c
  * place; the state at the start of step k goes to checkpoints[k][ischan][ncell] and its
  * accepted steps per cell to nsteps[k][ncell].  Returns the number of failed cell-steps.
  *
+ * tape (device, tape_bytes long, may be NULL) receives the state and step size of every
+ * accepted step as the forward pass takes it, in linked blocks of 4 steps per cell and
+ * synchronisation step: about (ischan + 1) * 8 bytes per accepted step plus 12 bytes
+ * per cell and step.  Steps that do not fit are recorded as incomplete.
+ *
  * cmaqchem_adj_backward takes lambda = dL/dy at the end of the window and returns in
  * it dL/dy at the start; it adds dL/d log kmult to grad_logk[nrxns] and dL/demis to
  * grad_emis[ischan][ncell] (may be NULL).  The other arguments must be those of the
- * forward call, whose checkpoints and step counts it reads; the accepted step sizes
- * are held fixed (the discrete adjoint of the steps the forward pass took).  Needs
- * device memory for the steps of one synchronisation step: sum(nsteps[k]) * (ischan
- * + 1) doubles. */
+ * forward call, whose checkpoints, step counts and tape it reads; the accepted step
+ * sizes are held fixed (the discrete adjoint of the steps the forward pass took).  A
+ * step whose tape is missing or incomplete is re-run from its checkpoint, which needs
+ * device memory for that step's accepted steps: sum(nsteps[k]) * (ischan + 1) doubles
+ * (bounded by the "adjoint_tape_mb" knob, cmaqchem_diag.h). */
 int cmaqchem_adj_forward(cmaqchem_handle* h, long long ncell, double* y, const double* rki,
                          long long rki_sync_stride, const unsigned char* night, const double* kmult,
                          const double* emis, int nsync, double chemstep_min, double* checkpoints,
-                         int* nsteps, void* stream);
+                         int* nsteps, void* tape, size_t tape_bytes, void* stream);
 int cmaqchem_adj_backward(cmaqchem_handle* h, long long ncell, double* lambda, const double* rki,
                           long long rki_sync_stride, const unsigned char* night, const double* kmult,
                           const double* emis, int nsync, double chemstep_min, const double* checkpoints,
-                          const int* nsteps, double* grad_logk, double* grad_emis, void* stream);
+                          const int* nsteps, const void* tape, size_t tape_bytes, double* grad_logk,
+                          double* grad_emis, void* stream);
 
 /* Rate constants only (CALC_RCONST, RXNS_FUNC_MODULE.F90) for the handle's grid, device
  * arrays: rki[nrxns][ncell], sunlit[ncell]. */

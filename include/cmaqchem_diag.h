@@ -17,7 +17,7 @@ int cmaqchem_diag_fp64_peak(int device, double* tflops, double* ms);
  * all dark use the smaller night LU pattern; 0: the day pattern always, same numbers),
  * "lockstep" (work-queue kernel: 0 free-running warps, 1 (default) the block's warps run
  * each step attempt together with barriers between its phases, 2 also between the
- * generated chunks), "block_warps" (2, 4 or 8 warps per block; 4 by default; 0 lockstep
+ * generated chunks), "block_warps" (2, 4 or 8 warps per block; 8 by default; 0 lockstep
  * needs 8), "blocks_per_sm" (cap on resident blocks per SM of the work-queue kernel,
  * 0 (default): as many as fit) and "adjoint_tape_mb" (device memory for the adjoint's
  * step tape; a synchronisation step whose tape is larger is processed in batches of

@@ -121,7 +121,7 @@ def test_tape_budget_batches_give_the_same_gradients(case):
     import torch
     from cmaq_gb300.adjoint import Ros3Window
     c = case
-    w = Ros3Window(c["s"], c["t"]["rki"], c["t"]["night"], 2, 5.0)
+    w = Ros3Window(c["s"], c["t"]["rki"], c["t"]["night"], 2, 5.0, tape_bytes=0)   # every step re-run
     res = []
     for mb in (0, 1):
         c["s"].set_tuning(adjoint_tape_mb=mb)
@@ -159,3 +159,28 @@ def test_adjoint_on_ragged_cell_counts(ncell):
     y.sum().backward()
     assert _rel_vec(a.grad.cpu().numpy(), lam_ref) < 1e-7
     assert _rel_vec(k.grad.cpu().numpy(), gk_ref) < 1e-7
+
+
+def test_forward_tape_full_partial_and_absent_agree(case):
+    """The tape recorded by the forward pass (complete, partial: later steps re-run, or
+    absent: every step re-run) changes nothing but the log-k summation order."""
+    import torch
+    from cmaq_gb300.adjoint import Ros3Window
+    c = case
+    res = []
+    n, ischan = c["y0"].shape[1], c["s"].info.ischan
+    one_step = n * 3 * 64 + 4 * n * (ischan + 1) * 8      # room for about one step's blocks
+    for tb in (None, one_step, 0):
+        w = Ros3Window(c["s"], c["t"]["rki"], c["t"]["night"], 3, 5.0, tape_bytes=tb)
+        y0 = c["t"]["y0"].clone().requires_grad_(True)
+        logk = torch.log(c["t"]["kmult"]).clone().requires_grad_(True)
+        emis = c["t"]["emis"].clone().requires_grad_(True)
+        y = w(y0, logk, emis)
+        (y * y.detach().clamp_min(1e-12).reciprocal()).sum().backward()
+        res.append((y.detach().cpu().numpy(), y0.grad.cpu().numpy(), logk.grad.cpu().numpy(),
+                    emis.grad.cpu().numpy()))
+    for r in res[1:]:
+        assert np.array_equal(r[0], res[0][0])
+        assert np.array_equal(r[1], res[0][1])
+        assert np.array_equal(r[3], res[0][3])
+        assert _rel_vec(r[2], res[0][2]) < 1e-12
