@@ -127,7 +127,7 @@ __device__ __forceinline__ bool refill(const Args& a, long long& cell, bool& got
 // of each cell in nsteps.  With tape_off: stores Y and h of each accepted step at the
 // cell's tape entries (at most nsteps[c] of them).
 template <class M>
-__global__ void __launch_bounds__(THREADS, 1) k_adj_forward(Args a)
+__global__ void __launch_bounds__(THREADS, 2) k_adj_forward(Args a)
 {
     double* ws = lane_ws<M>(a.ws);
     const bool taping = a.tape_off != nullptr;
@@ -161,8 +161,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_adj_forward(Args a)
             }
         }
         const bool busy = cell >= 0;
-        if (!__any_sync(0xffffffffu, busy)) break;
-        const bool night = __all_sync(0xffffffffu, !busy || cnight);
+        // the block's warps run each step attempt together (barriers between its phases)
+        if (!__syncthreads_or(busy)) break;
+        const bool night = __syncthreads_and(!busy || cnight);
         double h = 0.0;
         const int nacc = s.st.nsteps;
         if (busy && taping) {
@@ -196,7 +197,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_adj_forward(Args a)
                 }
             }
         }
-        ros3::attempt_phased<M, 0, true>(ws, s, a.chemstep, a.tol, night, a.max_iter, busy);
+        ros3::attempt_phased<M, 1, true>(ws, s, a.chemstep, a.tol, night, a.max_iter, busy);
         if (busy) {
             if (taping && s.st.nsteps != nacc) {
                 if (nacc < cap) a.tape_h[base + nacc] = h;
@@ -229,75 +230,96 @@ __global__ void __launch_bounds__(THREADS, 1) k_adj_forward(Args a)
 }
 
 // Adjoint of one accepted step at Y = ws[OFF_Y] with step size h; updates ADJ_LAM and
-// accumulates ADJ_GE and ADJ_GK.
+// accumulates ADJ_GE and ADJ_GK.  Every thread of the block calls it; lanes with go ==
+// false do no work; the block passes a barrier between the phases so that its warps
+// walk the (large) generated code together.
 template <class M>
-__device__ void reverse_step(double* __restrict__ ws, double h, bool night)
+__device__ void reverse_step(double* __restrict__ ws, double h, bool night, bool go)
 {
     using namespace ros3;
-    const double dtinv = 1.0 / h;
+    const double dtinv = go ? 1.0 / h : 0.0;
     const double gdtinv = dtinv * RGAM;
-    // recompute the stages exactly as the forward step did
-    if (night) M::feval_1(ws, M::OFF_Y, M::OFF_F0); else M::feval_0(ws, M::OFF_Y, M::OFF_F0);
-    add_emis<M>(ws, M::OFF_F0);
-    if (night) M::explic_1(ws); else M::explic_0(ws);
-    if (night) M::jacdecomp_1(ws, gdtinv); else M::jacdecomp_0(ws, gdtinv);
-    for (int n = 0; n < M::ISCHAN; ++n) ws[(M::OFF_K1 + n) * 32] = -ws[(M::OFF_F0 + n) * 32];
-    if (night) M::solve_1(ws, M::OFF_K1); else M::solve_0(ws, M::OFF_K1);
-    for (int n = 0; n < M::ISCHAN; ++n)
-        ws[(M::OFF_YP + n) * 32] = ws[(M::OFF_Y + n) * 32] + ws[(M::OFF_K1 + n) * 32];
-    if (night) M::feval_1(ws, M::OFF_YP, M::OFF_YDOT); else M::feval_0(ws, M::OFF_YP, M::OFF_YDOT);
-    add_emis<M>(ws, M::OFF_YDOT);
     const double x21 = C21 * dtinv, x31 = C31 * dtinv, x32 = C32 * dtinv;
-    for (int n = 0; n < M::ISCHAN; ++n)
-        ws[(M::OFF_K2 + n) * 32] = fma(-x21, ws[(M::OFF_K1 + n) * 32], -ws[(M::OFF_YDOT + n) * 32]);
-    if (night) M::solve_1(ws, M::OFF_K2); else M::solve_0(ws, M::OFF_K2);
-    for (int n = 0; n < M::ISCHAN; ++n) {
-        const double t = fma(-x31, ws[(M::OFF_K1 + n) * 32], -ws[(M::OFF_YDOT + n) * 32]);
-        ws[(M::OFF_K3 + n) * 32] = fma(-x32, ws[(M::OFF_K2 + n) * 32], t);
+    // recompute the stages exactly as the forward step did
+    if (go) {
+        if (night) M::feval_1(ws, M::OFF_Y, M::OFF_F0); else M::feval_0(ws, M::OFF_Y, M::OFF_F0);
+        add_emis<M>(ws, M::OFF_F0);
+        if (night) M::explic_1(ws); else M::explic_0(ws);
     }
-    if (night) M::solve_1(ws, M::OFF_K3); else M::solve_0(ws, M::OFF_K3);
-    // clipped components of Y' pass no gradient
-    for (int n = 0; n < M::ISCHAN; ++n) {
-        double yn = fma(B1, ws[(M::OFF_K1 + n) * 32], ws[(M::OFF_Y + n) * 32]);
-        yn = fma(B2, ws[(M::OFF_K2 + n) * 32], yn);
-        yn = fma(B3, ws[(M::OFF_K3 + n) * 32], yn);
-        if (!(yn > CONMIN)) ws[(M::ADJ_LAM + n) * 32] = 0.0;
-        ws[(M::ADJ_MU3 + n) * 32] = B3 * ws[(M::ADJ_LAM + n) * 32];
+    __syncthreads();
+    if (go) {
+        if (night) M::jacdecomp_1(ws, gdtinv); else M::jacdecomp_0(ws, gdtinv);
+        for (int n = 0; n < M::ISCHAN; ++n) ws[(M::OFF_K1 + n) * 32] = -ws[(M::OFF_F0 + n) * 32];
     }
-    if (night) M::solve_t_1(ws, M::ADJ_MU3); else M::solve_t_0(ws, M::ADJ_MU3);
-    for (int n = 0; n < M::ISCHAN; ++n)
-        ws[(M::ADJ_MU2 + n) * 32] = fma(-x32, ws[(M::ADJ_MU3 + n) * 32], B2 * ws[(M::ADJ_LAM + n) * 32]);
-    if (night) M::solve_t_1(ws, M::ADJ_MU2); else M::solve_t_0(ws, M::ADJ_MU2);
-    for (int n = 0; n < M::ISCHAN; ++n) {
-        const double phi = -ws[(M::ADJ_MU3 + n) * 32] - ws[(M::ADJ_MU2 + n) * 32];
-        ws[(M::ADJ_PHI + n) * 32] = phi;
-        ws[(M::ADJ_GE + n) * 32] = ws[(M::ADJ_GE + n) * 32] + phi;
-        ws[(M::ADJ_TMP + n) * 32] = 0.0;
+    __syncthreads();
+    solve_phase<M, 1>(ws, M::OFF_K1, night, go);
+    if (go) {
+        for (int n = 0; n < M::ISCHAN; ++n)
+            ws[(M::OFF_YP + n) * 32] = ws[(M::OFF_Y + n) * 32] + ws[(M::OFF_K1 + n) * 32];
+        if (night) M::feval_1(ws, M::OFF_YP, M::OFF_YDOT); else M::feval_0(ws, M::OFF_YP, M::OFF_YDOT);
+        add_emis<M>(ws, M::OFF_YDOT);
+        for (int n = 0; n < M::ISCHAN; ++n)
+            ws[(M::OFF_K2 + n) * 32] = fma(-x21, ws[(M::OFF_K1 + n) * 32], -ws[(M::OFF_YDOT + n) * 32]);
     }
-    if (night) M::adj_jtv_1(ws, M::OFF_YP, M::ADJ_PHI, M::ADJ_TMP);
-    else M::adj_jtv_0(ws, M::OFF_YP, M::ADJ_PHI, M::ADJ_TMP);
-    for (int n = 0; n < M::ISCHAN; ++n) {
-        const double lam = ws[(M::ADJ_LAM + n) * 32];
-        const double t = ws[(M::ADJ_TMP + n) * 32];
-        const double mu = fma(-x21, ws[(M::ADJ_MU2 + n) * 32], fma(-x31, ws[(M::ADJ_MU3 + n) * 32], B1 * lam));
-        ws[(M::ADJ_MU1 + n) * 32] = mu + t;
-        ws[(M::ADJ_LAM + n) * 32] = lam + t;
+    __syncthreads();
+    solve_phase<M, 1>(ws, M::OFF_K2, night, go);
+    if (go) {
+        for (int n = 0; n < M::ISCHAN; ++n) {
+            const double t = fma(-x31, ws[(M::OFF_K1 + n) * 32], -ws[(M::OFF_YDOT + n) * 32]);
+            ws[(M::OFF_K3 + n) * 32] = fma(-x32, ws[(M::OFF_K2 + n) * 32], t);
+        }
     }
-    if (night) M::solve_t_1(ws, M::ADJ_MU1); else M::solve_t_0(ws, M::ADJ_MU1);
-    for (int n = 0; n < M::ISCHAN; ++n) {
-        const double phi = -ws[(M::ADJ_MU1 + n) * 32];
-        ws[(M::ADJ_PHI + n) * 32] = phi;
-        ws[(M::ADJ_GE + n) * 32] = ws[(M::ADJ_GE + n) * 32] + phi;
+    solve_phase<M, 1>(ws, M::OFF_K3, night, go);
+    if (go) {   // clipped components of Y' pass no gradient
+        for (int n = 0; n < M::ISCHAN; ++n) {
+            double yn = fma(B1, ws[(M::OFF_K1 + n) * 32], ws[(M::OFF_Y + n) * 32]);
+            yn = fma(B2, ws[(M::OFF_K2 + n) * 32], yn);
+            yn = fma(B3, ws[(M::OFF_K3 + n) * 32], yn);
+            if (!(yn > CONMIN)) ws[(M::ADJ_LAM + n) * 32] = 0.0;
+            ws[(M::ADJ_MU3 + n) * 32] = B3 * ws[(M::ADJ_LAM + n) * 32];
+        }
+        if (night) M::solve_t_1(ws, M::ADJ_MU3); else M::solve_t_0(ws, M::ADJ_MU3);
+        for (int n = 0; n < M::ISCHAN; ++n)
+            ws[(M::ADJ_MU2 + n) * 32] = fma(-x32, ws[(M::ADJ_MU3 + n) * 32], B2 * ws[(M::ADJ_LAM + n) * 32]);
     }
-    if (night) M::adj_jtv_1(ws, M::OFF_Y, M::ADJ_PHI, M::ADJ_LAM);
-    else M::adj_jtv_0(ws, M::OFF_Y, M::ADJ_PHI, M::ADJ_LAM);
-    if (night) M::adj_hess3_1(ws); else M::adj_hess3_0(ws);
+    __syncthreads();
+    if (go) {
+        if (night) M::solve_t_1(ws, M::ADJ_MU2); else M::solve_t_0(ws, M::ADJ_MU2);
+        for (int n = 0; n < M::ISCHAN; ++n) {
+            const double phi = -ws[(M::ADJ_MU3 + n) * 32] - ws[(M::ADJ_MU2 + n) * 32];
+            ws[(M::ADJ_PHI + n) * 32] = phi;
+            ws[(M::ADJ_GE + n) * 32] = ws[(M::ADJ_GE + n) * 32] + phi;
+            ws[(M::ADJ_TMP + n) * 32] = 0.0;
+        }
+        if (night) M::adj_jtv_1(ws, M::OFF_YP, M::ADJ_PHI, M::ADJ_TMP);
+        else M::adj_jtv_0(ws, M::OFF_YP, M::ADJ_PHI, M::ADJ_TMP);
+        for (int n = 0; n < M::ISCHAN; ++n) {
+            const double lam = ws[(M::ADJ_LAM + n) * 32];
+            const double t = ws[(M::ADJ_TMP + n) * 32];
+            const double mu = fma(-x21, ws[(M::ADJ_MU2 + n) * 32], fma(-x31, ws[(M::ADJ_MU3 + n) * 32], B1 * lam));
+            ws[(M::ADJ_MU1 + n) * 32] = mu + t;
+            ws[(M::ADJ_LAM + n) * 32] = lam + t;
+        }
+    }
+    __syncthreads();
+    if (go) {
+        if (night) M::solve_t_1(ws, M::ADJ_MU1); else M::solve_t_0(ws, M::ADJ_MU1);
+        for (int n = 0; n < M::ISCHAN; ++n) {
+            const double phi = -ws[(M::ADJ_MU1 + n) * 32];
+            ws[(M::ADJ_PHI + n) * 32] = phi;
+            ws[(M::ADJ_GE + n) * 32] = ws[(M::ADJ_GE + n) * 32] + phi;
+        }
+        if (night) M::adj_jtv_1(ws, M::OFF_Y, M::ADJ_PHI, M::ADJ_LAM);
+        else M::adj_jtv_0(ws, M::OFF_Y, M::ADJ_PHI, M::ADJ_LAM);
+        if (night) M::adj_hess3_1(ws); else M::adj_hess3_0(ws);
+    }
+    __syncthreads();
 }
 
 // Reverse sweep of one synchronisation step: each cell walks its tape entries backwards.
 // Cells are pulled from the queue (ordered by accepted steps, most first).
 template <class M>
-__global__ void __launch_bounds__(THREADS, 1) k_adj_reverse(Args a)
+__global__ void __launch_bounds__(THREADS, 2) k_adj_reverse(Args a)
 {
     double* ws = lane_ws<M>(a.ws);
     for (int r = 0; r < M::NRXNS; ++r) ws[(M::ADJ_GK + r) * 32] = 0.0;
@@ -327,9 +349,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_adj_reverse(Args a)
             }
         }
         const bool busy = cell >= 0;
-        if (!__any_sync(0xffffffffu, busy)) break;
+        if (!__syncthreads_or(busy)) break;
         const bool work = busy && left > 0;
-        const bool night = __all_sync(0xffffffffu, !work || cnight);
+        const bool night = __syncthreads_and(!work || cnight);
+        double hstep = 0.0;
         if (work) {
             --left;
             size_t e;
@@ -345,8 +368,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_adj_reverse(Args a)
             }
             const double* t = (pooled ? a.pool_y : a.tape_y) + e * M::ISCHAN;
             for (int i = 0; i < M::ISCHAN; ++i) ws[(M::OFF_Y + i) * 32] = t[i];
-            reverse_step<M>(ws, (pooled ? a.pool_h : a.tape_h)[e], night);
+            hstep = (pooled ? a.pool_h : a.tape_h)[e];
         }
+        reverse_step<M>(ws, hstep, night, work);
         if (busy && left == 0) {
             for (int i = 0; i < M::ISCHAN; ++i) a.lam[(size_t)i * a.ncell + cell] = ws[(M::ADJ_LAM + i) * 32];
             if (a.grad_emis)
