@@ -122,9 +122,16 @@ __device__ void scatter_cell(const GridArgs& a, long long c, const double* __res
 }
 
 // One CHEM call, cells distributed statically: warp w takes cells [32w, 32w+32) then
-// strides by the grid's warp count.  Each lane integrates its own cell.
+// strides by the grid's warp count.  Each lane integrates its own cell.  Same occupancy
+// target as the work-queue kernel (CHEM_QUEUE_WARPS_PER_SM), so that the two schedules
+// differ only in how cells reach the lanes.
+#ifndef CHEM_QUEUE_WARPS_PER_SM
+#define CHEM_QUEUE_WARPS_PER_SM 12
+#endif
 template <class M>
-__global__ void __launch_bounds__(THREADS_PER_BLOCK, 1) k_chem_ros3(GridArgs a)
+__global__ void __launch_bounds__(THREADS_PER_BLOCK,
+                                  CHEM_QUEUE_WARPS_PER_SM / WARPS_PER_BLOCK > 0 ? CHEM_QUEUE_WARPS_PER_SM / WARPS_PER_BLOCK : 1)
+    k_chem_ros3(GridArgs a)
 {
     const long long nwarps = (long long)gridDim.x * WARPS_PER_BLOCK;
     const long long warp = (long long)blockIdx.x * WARPS_PER_BLOCK + (threadIdx.x >> 5);

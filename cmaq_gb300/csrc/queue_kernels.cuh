@@ -33,11 +33,8 @@ __device__ __forceinline__ unsigned long long queue_len(const QueueArgs& q, long
 // barriers between its phases (SYNC = 1) or also between the generated chunks (SYNC = 2);
 // the block leaves the loop only when none of its warps holds a cell.  WPB = warps per
 // block.
-// Launch bounds: CHEM_QUEUE_WARPS_PER_SM resident warps per SM (12 by default; the
+// Launch bounds: CHEM_QUEUE_WARPS_PER_SM resident warps per SM (chem_kernels.cuh; the
 // generated functions the kernel calls must be built for that register budget).
-#ifndef CHEM_QUEUE_WARPS_PER_SM
-#define CHEM_QUEUE_WARPS_PER_SM 12
-#endif
 template <class M, int SYNC, int WPB>
 __global__ void __launch_bounds__(WPB * 32, CHEM_QUEUE_WARPS_PER_SM / WPB > 0 ? CHEM_QUEUE_WARPS_PER_SM / WPB : 1)
     k_chem_ros3_queue(GridArgs a, QueueArgs q)
