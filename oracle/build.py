@@ -37,7 +37,7 @@ def build(mechs=MECHS, force: bool = False) -> list[Path]:
         out = lib_path(mech)
         outs.append(out)
         newest = max(p.stat().st_mtime for p in (src, src_ebi, gen, gen_ebi, HERE / "oracle.h",
-                                                 HERE / "ros3_adjoint.c"))
+                                                 HERE / "ros3_adjoint.c", HERE / "gear_oracle.c"))
         if not force and out.exists() and out.stat().st_mtime > newest:
             continue
         cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",

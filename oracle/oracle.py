@@ -1,7 +1,8 @@
 """ctypes binding of the CPU oracle (test infrastructure only).
 
 Loads ``oracle/_build/liboracle_<mech>.so`` (see ``oracle/build.py``), a C
-restatement of CMAQ's ROS3 chemistry (CCTM/src/gas/ros3/*.F).  Tests, the smoke
+restatement of CMAQ's ROS3, EBI and SMVGEAR chemistry (CCTM/src/gas/ros3/*.F,
+ebi_<mech>/*.F, smvgear/*.F).  Tests, the smoke
 check and the CPU-baseline leg of the benchmark use it as the checker; nothing
 in the product imports it.
 """
@@ -63,6 +64,11 @@ def load(mech: str = "cb6r5_ae7_aq") -> C.CDLL:
     lib.oracle_adj_replay.restype = None
     lib.oracle_ddm3d_window.argtypes = [C.c_long, dp, dp, C.c_long, u8p, dp, dp, C.c_int, C.c_double, C.c_double,
                                         C.c_double, C.c_int, ip, ip, dp, C.c_int]
+    lib.oracle_gear_cfg_size.restype = C.c_size_t
+    lib.oracle_gear_cfg.argtypes = [C.c_double, C.c_float, C.c_float, C.c_float, C.c_int, C.c_void_p]
+    lib.oracle_gear_cfg.restype = None
+    lib.oracle_gear_cells.argtypes = [C.c_long, C.c_double, C.c_void_p, dp, dp, u8p, ip, C.c_int]
+    lib.oracle_gear_chem.argtypes = [C.POINTER(OracleChemArgs), C.c_void_p]
     lib.oracle_set_dtmin.argtypes = [C.c_double]
     lib.oracle_get_dtmin.restype = C.c_double
     return lib
@@ -179,6 +185,49 @@ class Oracle:
         self.lib.oracle_ebi_solve_cells(n, tstep_sec, _p(yc, C.c_double), _p(rki, C.c_double), _p(st, C.c_int),
                                         it.ctypes.data_as(C.POINTER(C.c_long)), threads)
         return yc, st, it
+
+    # ---- SMVGEAR (CCTM/src/gas/smvgear)
+
+    GEAR_STATS = ("nsteps", "ncfail", "nefail", "npderiv", "nsubfun", "nnewt", "maxord", "status")
+
+    def gear_cfg(self, rtol: float = float(np.float32(1e-3)), max_atol: float = 1e-7, min_atol: float = 1e-9,
+                 conc_floor: float = 1e-12, max_iter: int = 100000):
+        """Tolerances and Gear coefficients: rtol = REAL(GEAR_RTOL, 8); the three others are the
+        REAL(4) run-time settings GEAR_MAX_ATOL, GEAR_MIN_ATOL, GEAR_CONC_FLOOR (ppmV)."""
+        buf = C.create_string_buffer(self.lib.oracle_gear_cfg_size())
+        self.lib.oracle_gear_cfg(rtol, max_atol, min_atol, conc_floor, max_iter, buf)
+        return buf
+
+    def gear_cells(self, y, rk, night, chemstep: float, cfg=None, threads: int = 0):
+        """Per-cell SMVGEAR (BLKSIZE = 1) over chemstep minutes; y (nspec, n) solver order.
+        Returns (y, stats[n, 8]) with the columns of GEAR_STATS."""
+        cfg = cfg if cfg is not None else self.gear_cfg()
+        y = np.array(y, dtype=np.float64, order="C", copy=True)
+        rk = np.ascontiguousarray(rk, np.float64)
+        night = np.ascontiguousarray(night, np.uint8)
+        n = y.shape[1]
+        stats = np.zeros((n, 8), np.int32)
+        self.lib.oracle_gear_cells(n, chemstep, cfg, _p(y, C.c_double), _p(rk, C.c_double), _p(night, C.c_uint8),
+                                   _p(stats, C.c_int), threads)
+        return y, stats
+
+    def chem_gear(self, g, tstep_sec: int = 300, blksize: int = 50, cfg=None, lreorder: bool = True,
+                  threads: int = 0, conc=None):
+        """One SMVGEAR CHEM call (grdriver.F) on a GridInputs-like object; returns (new conc, totals)."""
+        cfg = cfg if cfg is not None else self.gear_cfg()
+        conc = np.array(g.conc if conc is None else conc, dtype=np.float32, order="C", copy=True)
+        man_cgi = np.ascontiguousarray(g.cgrid_index - 1, np.int32)
+        convert = np.ascontiguousarray(self.convert_flags(g.mech), np.int32)
+        keep = [conc, man_cgi, convert]
+        a = OracleChemArgs(g.ncols, g.nrows, g.nlays, g.nspcsd, _p(conc, C.c_float), _p(man_cgi, C.c_int),
+                           _p(convert, C.c_int), _p(g.ta, C.c_float), _p(g.qv, C.c_float), _p(g.dens, C.c_float),
+                           _p(g.pres, C.c_float), _p(g.seaice, C.c_float), _p(g.ocean_szone, C.c_float),
+                           _p(g.rj, C.c_float), _p(g.khetero, C.c_double), tstep_sec, 0.0, 0.0, blksize,
+                           int(lreorder), 0, threads, 0, 0, 0)
+        rc = self.lib.oracle_gear_chem(C.byref(a), cfg)
+        del keep
+        return conc, {"rc": rc, "nsteps": a.nsteps_total, "nfails": a.nfails_total,
+                      "nfailed_blocks": a.nfailed_blocks}
 
     @staticmethod
     def convert_flags(mech: str) -> np.ndarray:

@@ -454,11 +454,13 @@ int oracle_rbsolver_cells(long ncell, double chemstep, double rtol, double atol,
 
 /* OracleChemArgs: oracle.h */
 
-/* Per-block gather (rbdriver.F:460-511), CALC_RCONST and day/night choice (:513-519). */
+/* Per-block gather (rbdriver.F:460-511), CALC_RCONST and day/night choice (:513-519).
+ * gear: the SMVGEAR driver's REAL(8) concentration floor (grdriver.F:419-422) instead of
+ * ROS3's REAL(4) one. */
 static int gather_block(const OracleChemArgs* a, const int* ccol, const int* crow, const int* clev,
                         const long* nordcell, long offset, int numcells, Block* b, double* blktemp,
                         double* blkpres, double* blkh2o, double* blkdens, float* blksvol,
-                        double* blksea, double* rjblk, double* blkhet, const float* fwd)
+                        double* blksea, double* rjblk, double* blkhet, const float* fwd, int gear)
 {
     const float PA2ATM = 1.0f / 101325.0f;
     const float MAOMV = 28.9628f / 18.0153f;
@@ -483,10 +485,8 @@ static int gather_block(const OracleChemArgs* a, const int* ccol, const int* cro
             const long cell = nordcell[offset + c];
             const long g = ccol[cell] + (long)a->ncols * (crow[cell] + (long)a->nrows * clev[cell]);
             const float cv = a->conc[(size_t)spc * ncell + g];
-            float v;
-            if (a->convert[isp]) v = fmaxf(fwd[isp] * blksvol[c] * cv, 1.0e-30f);
-            else v = fmaxf(cv, 1.0e-30f);
-            b->y[(size_t)ispnew * b->ld + c] = (double)v;
+            const float v = a->convert[isp] ? fwd[isp] * blksvol[c] * cv : cv;
+            b->y[(size_t)ispnew * b->ld + c] = gear ? fmax((double)v, 1.0e-30) : (double)fmaxf(v, 1.0e-30f);
         }
     }
     int lsun = 0;
@@ -503,6 +503,50 @@ static int gather_block(const OracleChemArgs* a, const int* ccol, const int* cro
     b->ncells = numcells;
     mech_calc_rconst(numcells, b->ld, blktemp, blkpres, blkh2o, rjblk, blkhet, lsun, blksea, b->rki);
     return lsun ? 0 : 1;   /* NCSP: 0 = day, 1 = night */
+}
+
+/* Heap sort of the cells by stiffness ERRMX2, ascending, carrying NORDCELL along
+ * (rbdriver.F:683-724; the same sort is grdriver.F:662-706). */
+static void heap_sort_cells(double* errmx2, long* nordcell, long noxyz)
+{
+    long lval = noxyz / 2 + 1, irval = noxyz;
+    double vallow;
+    long jreord;
+    /* 1-based indexing helpers */
+    double* E = errmx2 - 1;
+    long* N = nordcell - 1;
+    for (;;) {
+        if (lval > 1) {
+            lval = lval - 1;
+            vallow = E[lval];
+            jreord = N[lval];
+        } else {
+            vallow = E[irval];
+            jreord = N[irval];
+            E[irval] = E[1];
+            N[irval] = N[1];
+            irval = irval - 1;
+            if (irval == 1) {
+                E[irval] = vallow;
+                N[irval] = jreord;
+                return;
+            }
+        }
+        long ipar = lval, jpar = lval + lval;
+        while (jpar <= irval) {
+            if (jpar < irval && E[jpar] < E[jpar + 1]) jpar = jpar + 1;
+            if (vallow < E[jpar]) {
+                E[ipar] = E[jpar];
+                N[ipar] = N[jpar];
+                ipar = jpar;
+                jpar = jpar + jpar;
+            } else {
+                jpar = irval + 1;
+            }
+        }
+        E[ipar] = vallow;
+        N[ipar] = jreord;
+    }
 }
 
 /* One CHEM call (rbdriver.F) on the whole grid with the given BLKSIZE. */
@@ -573,7 +617,7 @@ int oracle_chem(OracleChemArgs* a)
                 const int numcells = blklen[blk];
                 const long offset = blkcno[blk];
                 const int ncsp = gather_block(a, ccol, crow, clev, nordcell, offset, numcells, &b, blktemp,
-                                              blkpres, blkh2o, blkdens, blksvol, blksea, rjblk, blkhet, fwd);
+                                              blkpres, blkh2o, blkdens, blksvol, blksea, rjblk, blkhet, fwd, 0);
                 if (ordering_pass) {
                     oracle_rbsolver(&b, ncsp, chemstep, &cfg, &errmx2[offset]);
                     continue;
@@ -599,47 +643,7 @@ int oracle_chem(OracleChemArgs* a)
             free(blktemp); free(blkpres); free(blkh2o); free(blkdens); free(blksvol); free(blksea);
             free(rjblk); free(blkhet);
         }
-        if (ordering_pass) {
-            /* heap sort of cells by ERRMX2, ascending (rbdriver.F:683-724) */
-            long lval = noxyz / 2 + 1, irval = noxyz;
-            double vallow;
-            long jreord;
-            /* 1-based indexing helpers */
-            double* E = errmx2 - 1;
-            long* N = nordcell - 1;
-            for (;;) {
-                if (lval > 1) {
-                    lval = lval - 1;
-                    vallow = E[lval];
-                    jreord = N[lval];
-                } else {
-                    vallow = E[irval];
-                    jreord = N[irval];
-                    E[irval] = E[1];
-                    N[irval] = N[1];
-                    irval = irval - 1;
-                    if (irval == 1) {
-                        E[irval] = vallow;
-                        N[irval] = jreord;
-                        break;
-                    }
-                }
-                long ipar = lval, jpar = lval + lval;
-                while (jpar <= irval) {
-                    if (jpar < irval && E[jpar] < E[jpar + 1]) jpar = jpar + 1;
-                    if (vallow < E[jpar]) {
-                        E[ipar] = E[jpar];
-                        N[ipar] = N[jpar];
-                        ipar = jpar;
-                        jpar = jpar + jpar;
-                    } else {
-                        jpar = irval + 1;
-                    }
-                }
-                E[ipar] = vallow;
-                N[ipar] = jreord;
-            }
-        }
+        if (ordering_pass) heap_sort_cells(errmx2, nordcell, noxyz);
     }
     a->nsteps_total = tot_steps;
     a->nfails_total = tot_fails;
@@ -650,3 +654,6 @@ int oracle_chem(OracleChemArgs* a)
 
 /* ------------------------------------------------------------------ discrete adjoint */
 #include "ros3_adjoint.c"
+
+/* ------------------------------------------------------------------ SMVGEAR */
+#include "gear_oracle.c"

@@ -8,8 +8,9 @@ from cmaq_gb300.synthetic import GridInputs, manifest
 F32 = np.float32
 
 
-def gather_cells(g: GridInputs, o):
+def gather_cells(g: GridInputs, o, gear: bool = False):
     """Per-cell inputs gathered like rbdriver.F:460-511 (REAL(4) arithmetic), cells in CGRID order.
+    gear: SMVGEAR's REAL(8) concentration floor (grdriver.F:419-422) instead of ROS3's REAL(4) one.
 
     Returns y [nspec, n] (solver species order), rki [nrxns, n], night [n] via the oracle's CALC_RCONST."""
     man = manifest(g.mech)
@@ -23,7 +24,10 @@ def gather_cells(g: GridInputs, o):
         if sp["convert"]:
             fwd = F32(F32(1.0e-3) * F32(28.9628)) / F32(sp["molwt"])
             v = (F32(fwd) * svol).astype(F32) * v
-        y[o.iold2new[s]] = np.maximum(v.astype(F32), F32(1.0e-30)).astype(np.float64)
+        if gear:
+            y[o.iold2new[s]] = np.maximum(v.astype(F32).astype(np.float64), 1.0e-30)
+        else:
+            y[o.iold2new[s]] = np.maximum(v.astype(F32), F32(1.0e-30)).astype(np.float64)
     temp = g.ta.reshape(n).astype(np.float64)
     pres = (F32(F32(1.0) / F32(101325.0)) * g.pres.reshape(n)).astype(F32).astype(np.float64)
     qv2ppm = F32(F32(1.0e6) * F32(F32(28.9628) / F32(18.0153)))
