@@ -363,6 +363,24 @@ def run_ebi(device: int, steps: int) -> dict:
     return out
 
 
+def run_gear(device: int, steps: int) -> dict:
+    """SMVGEAR against batched ROS3 on one 100x100x10 grid of the same distributions
+    (GEAR_RTOL 1e-3, OPTIMAL_ATOL_PPM between 1e-9 and 1e-7 ppmV).  A Gear call lasts as
+    long as its stiffest cell (tens of seconds here), so at most 3 calls are timed."""
+    from cmaq_gb300.synthetic import make_grid
+    steps = min(steps, 3)
+    g = make_grid(seed=2018, ncols=100, nrows=100, nlays=10)
+    out = {"workload": f"cb6r5_ae7_aq 100x100x10 ({g.ncell} cells), the hour's first {steps} x 5-min CHEM calls"}
+    for solver in ("gear", "ros3"):
+        r = run_device(g, "queue", steps, 1, None, device, sample_clocks=False, solver=solver)
+        out[f"{solver}_ms_per_step"] = r["ms_total"] / steps
+        out[f"{solver}_value"] = g.ncell / (STEPS_PER_HOUR * r["ms_total"] / steps / 1e3)
+        if solver == "gear":
+            out["gear_steps_per_cell"] = sum(st["accepted_steps"] for st in r["stats"]) / g.ncell / steps
+            out["gear_failures_per_cell"] = sum(st["rejected_steps"] for st in r["stats"]) / g.ncell / steps
+    return out
+
+
 def barrier(dist):
     if dist is not None:
         import torch.distributed as tdist
@@ -393,6 +411,8 @@ def cpu_reference(workload_cells: int, steps: int, warmup: int, threads: int, ta
     def call(g, conc=None):
         if solver == "ebi":
             return o.chem_ebi(g, threads=threads, conc=conc)
+        if solver == "gear":
+            return o.chem_gear(g, blksize=50, threads=threads, conc=conc)
         return o.chem(g, blksize=50, rtol=rt, atol=at, threads=threads, conc=conc)
     # size the sample so that the timed calls take about target_s
     ncols = 20
@@ -435,12 +455,13 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-ebi", action="store_true")
+    ap.add_argument("--no-gear", action="store_true")
     ap.add_argument("--all-configs", action="store_true",
                     help="also time the skewed-stiffness CONUS grid and CRACMM2 on 1M cells (about 5 more minutes)")
     ap.add_argument("--adjoint-dims", default="100x100x35", help="grid of the adjoint window, NCOLSxNROWSxNLAYS")
     ap.add_argument("--only-adjoint", action="store_true",
                     help="time only the adjoint window and print its own line (for profiling)")
-    ap.add_argument("--solver", default="ros3", choices=["ros3", "ebi"],
+    ap.add_argument("--solver", default="ros3", choices=["ros3", "ebi", "gear"],
                     help="solver of the timed CHEM calls (the metric is quoted for ros3)")
     a = ap.parse_args()
     world, rank, local = dist_env()
@@ -527,16 +548,21 @@ def main():
         r = cpu_reference(ncell, STEPS_PER_HOUR, 0, thr, target_s=15.0)
         r1 = cpu_reference(ncell, STEPS_PER_HOUR, 0, 1, target_s=8.0)
         re = cpu_reference(ncell, STEPS_PER_HOUR, 0, thr, target_s=8.0, solver="ebi")
+        rg = None if a.no_gear else cpu_reference(ncell, STEPS_PER_HOUR, 0, thr, target_s=8.0, solver="gear")
         cpu = {"value": r["value"], "unit": UNIT, "cores": thr, "kind": "port",
                "sample": f"{r['cells']} cells of the same distributions x {r['steps']} CHEM calls "
                          f"(reference algorithm, BLKSIZE 50 + reordering, C restatement, {r['wall_s']:.1f} s)",
                "single_core_value": r1["value"],
                "single_core_sample": f"{r1['cells']} cells x {r1['steps']} calls, 1 thread",
                "ebi_value": re["value"],
-               "ebi_sample": f"{re['cells']} cells x {re['steps']} EBI CHEM calls, {thr} threads"}
+               "ebi_sample": f"{re['cells']} cells x {re['steps']} EBI CHEM calls, {thr} threads",
+               "gear_value": None if rg is None else rg["value"],
+               "gear_sample": None if rg is None else
+               f"{rg['cells']} cells x {rg['steps']} SMVGEAR CHEM calls (BLKSIZE 50 + reordering), {thr} threads"}
 
     adjoint = None if (a.no_adjoint or rank != 0) else run_adjoint(device, STEPS_PER_HOUR, adims)
     ebi = None if (a.no_ebi or rank != 0) else run_ebi(device, a.steps)
+    gear = None if (a.no_gear or rank != 0) else run_gear(device, a.steps)
     skewed = run_skewed(device, a.steps, tuned) if (a.all_configs and rank == 0) else None
     cracmm2 = run_cracmm2(device, a.steps) if (a.all_configs and rank == 0) else None
 
@@ -551,10 +577,10 @@ def main():
             traffic = None
     if rank == 0:
         launches_per_step = 4   # queue ordering (hist, scan, scatter) + solve, replayed from one graph
-        if a.solver == "ebi":   # EBI iterations have no ROS3 FLOP count
+        if a.solver != "ros3":   # EBI iterations and Gear steps have no ROS3 FLOP count
             achieved_tf = None
         line = {
-            "metric": METRIC if a.solver == "ros3" else METRIC.replace("ROS3", "EBI"), "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+            "metric": METRIC if a.solver == "ros3" else METRIC.replace("ROS3", a.solver.upper()), "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded; cmaq_gb300/synthetic.py)",
             "config": {"workload": f"cb6r5_ae7_aq {g.ncols}x{g.nrows}x{g.nlays} ({ncell} cells per GPU), "
@@ -578,6 +604,7 @@ def main():
             "batched_over_plain": None if plain is None else value / plain["value"],
             "adjoint": adjoint,
             "ebi": ebi,
+            "gear": gear,
             "skewed": skewed,
             "cracmm2": cracmm2,
             "e2e": e2e,

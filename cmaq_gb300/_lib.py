@@ -11,7 +11,7 @@ from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "_build" / "libcmaqchem.so"
 
-SOLVER_ROS3, SOLVER_EBI = 0, 1
+SOLVER_ROS3, SOLVER_EBI, SOLVER_GEAR = 0, 1, 2
 SCHED_STATIC, SCHED_QUEUE = 0, 1
 CELL_DT_UNDERFLOW, CELL_MAXITER, CELL_NONFINITE = 1, 2, 4
 
@@ -61,6 +61,8 @@ def lib(variant: str = "default") -> C.CDLL:
     L.cmaqchem_cell_stats.argtypes = [vp, vp, vp]
     L.cmaqchem_ros3_solve_device.argtypes = [vp, C.c_longlong, vp, vp, vp, C.c_double, vp, vp, vp, vp]
     L.cmaqchem_ebi_solve_device.argtypes = [vp, C.c_longlong, vp, vp, C.c_int, vp, vp, vp]
+    L.cmaqchem_gear_solve_device.argtypes = [vp, C.c_longlong, vp, vp, vp, C.c_double, vp, vp]
+    L.cmaqchem_gear_tolerances.argtypes = [vp, C.c_float, C.c_float, C.c_float]
     L.cmaqchem_adj_forward.argtypes = [vp, C.c_longlong, vp, vp, C.c_longlong, vp, vp, vp, C.c_int, C.c_double,
                                        vp, vp, vp, C.c_size_t, vp]
     L.cmaqchem_adj_backward.argtypes = [vp, C.c_longlong, vp, vp, C.c_longlong, vp, vp, vp, C.c_int, C.c_double,

@@ -26,7 +26,7 @@ import numpy as np
 from . import _lib
 from ._lib import ChemError, check
 
-SOLVERS = {"ros3": _lib.SOLVER_ROS3, "ebi": _lib.SOLVER_EBI}
+SOLVERS = {"ros3": _lib.SOLVER_ROS3, "ebi": _lib.SOLVER_EBI, "gear": _lib.SOLVER_GEAR}
 SCHEDULES = {"static": _lib.SCHED_STATIC, "plain": _lib.SCHED_STATIC, "queue": _lib.SCHED_QUEUE,
              "batched": _lib.SCHED_QUEUE}
 
@@ -229,6 +229,24 @@ class ChemSolver:
         check(self._L.cmaqchem_ebi_solve_device(self._h, n, _ptr(yc), _ptr(rki), int(tstep_sec), _ptr(st),
                                                 _ptr(it), s), self._L)
         return (st, it) if with_stats else None
+
+    GEAR_STATS = ("nsteps", "ncfail", "nefail", "npderiv", "nsubfun", "nnewt", "maxord", "status")
+
+    def gear_solve(self, y, rk, night, chemstep_min: float, with_stats: bool = False, stream=None):
+        """SMVGEAR (grsmvgear.F, BLKSIZE = 1) on CUDA tensors: y [nspec, n] (solver species order,
+        ppm) in place, rk [nrxns, n], night [n] uint8.  Optional per-cell statistics [n, 8] with
+        the columns of GEAR_STATS.  Needs a handle made with solver="gear"."""
+        import torch
+        n = y.shape[1]
+        st = torch.zeros((n, 8), dtype=torch.int32, device=y.device) if with_stats else None
+        s = C.c_void_p(stream.cuda_stream) if stream is not None else None
+        check(self._L.cmaqchem_gear_solve_device(self._h, n, _ptr(y), _ptr(rk), _ptr(night), chemstep_min,
+                                                 _ptr(st), s), self._L)
+        return st
+
+    def gear_tolerances(self, max_atol: float = 1e-7, min_atol: float = 1e-9, conc_floor: float = 1e-12) -> None:
+        """GEAR_MAX_ATOL, GEAR_MIN_ATOL, GEAR_CONC_FLOOR (ppmV) of a solver="gear" handle."""
+        check(self._L.cmaqchem_gear_tolerances(self._h, max_atol, min_atol, conc_floor), self._L)
 
     def rconst(self, conc, ta, qv, dens, pres, seaice, ocean_szone, rj, khetero):
         """CALC_RCONST for every cell of the grid (CUDA tensors): returns rki [nrxns, ncell], sunlit [ncell]."""

@@ -4,6 +4,7 @@
 // (rbdriver.F:226-371): mechanism tables (here: device tables and the generated code),
 // the domain size and the solver's work arrays (here: per-warp device workspaces).
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdint.h>
 #include <stdio.h>
 #include <string.h>
@@ -99,6 +100,14 @@ struct cmaqchem_handle {
     int ebi_warp = 1;        // EBI: 1 one cell per warp (shared memory), 0 one cell per lane
     int ebiw_nblocks = 0;
     size_t ws_warps = 0;     // workspace capacity in warps
+    int ws_elems = 0;        // workspace elements per lane (the solver's layout)
+    // SMVGEAR
+    gear::Coef gear_coef{};
+    gear::Coef* d_gear_coef = nullptr;
+    int gear_nblocks = 0;
+    int gear_warp = 1;          // 1: one cell per warp in shared memory (k_gear_warp), 0: one per lane
+    int gearw_nblocks = 0;
+    float gear_max_atol = 1.0e-7f, gear_min_atol = 1.0e-9f, gear_floor = 1.0e-12f;
     // device staging of the host-pointer entry point, allocated on first use
     float *s_conc = nullptr, *s_ta = nullptr, *s_qv = nullptr, *s_dens = nullptr, *s_pres = nullptr;
     float *s_seaice = nullptr, *s_osz = nullptr, *s_rj = nullptr;
@@ -142,7 +151,7 @@ void free_handle(cmaqchem_handle* h)
                     h->d_counters, h->d_order, h->d_hist, h->d_cursor, h->d_head, h->s_conc, h->s_ta,
                     h->s_qv, h->s_dens, h->s_pres, h->s_seaice, h->s_osz, h->s_rj, h->s_khet,
                     h->d_adj_ws, h->d_tape_y, h->d_tape_h, h->d_tape_off, h->d_tiles, h->d_tape_tot,
-                    h->d_adj_order, h->d_adj_status, h->d_adj_counters, h->d_yave};
+                    h->d_adj_order, h->d_adj_status, h->d_adj_counters, h->d_yave, h->d_gear_coef};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
@@ -164,7 +173,7 @@ int ensure_ws(cmaqchem_handle* h, size_t warps)
     if (warps <= h->ws_warps) return 0;
     if (h->d_ws) CK(cudaFree(h->d_ws));
     h->d_ws = nullptr;
-    CK(cudaMalloc(&h->d_ws, warps * (size_t)h->ops->ws_elems * 32 * sizeof(double)));
+    CK(cudaMalloc(&h->d_ws, warps * (size_t)h->ws_elems * 32 * sizeof(double)));
     h->ws_warps = warps;
     return 0;
 }
@@ -178,6 +187,55 @@ int configure_queue(cmaqchem_handle* h)
     if (h->q_bps_cap > 0 && bps > h->q_bps_cap) bps = h->q_bps_cap;
     h->q_nblocks = h->nsm * bps;
     return ensure_ws(h, (size_t)h->q_nblocks * h->q_wpb);
+}
+
+// Gear coefficients and tolerances: GRINIT / JSPARSE constants (grinit.F:163-171,
+// grsprse.F:682-720) and the OPTIMAL_ATOL_PPM levels (GRVARS.F:640-668); the same numbers
+// as the oracle's (REAL(4) expressions in REAL(4)).
+void gear_coefficients(double rtol, float max_atol, float min_atol, float conc_floor, int max_iter, gear::Coef* g)
+{
+    static const double pertst[3][7] = {{2.0, 4.5, 7.333, 10.42, 13.7, 17.15, 1.0},
+                                        {3.0, 6.0, 9.167, 12.5, 15.98, 1.0, 1.0},
+                                        {1.0, 1.0, 0.5, 0.1667, 0.04133, 0.008267, 1.0}};
+    *g = gear::Coef{};
+    for (int q = 0; q < 7; ++q) {
+        const int nqq = q + 1;
+        g->enqq1[q] = (double)(0.5f / (float)nqq);
+        g->enqq2[q] = (double)(0.5f / (float)(nqq + 1));
+        g->enqq3[q] = (double)(0.5f / (float)(nqq + 2));
+        g->conpst[q] = 1.0 / (pertst[0][q] * g->enqq3[q]);
+        g->conp15[q] = 1.5 * g->conpst[q];
+        for (int k = 0; k < 3; ++k) g->pertst[q][k] = pertst[k][q] * pertst[k][q];
+    }
+    // Nordsieck coefficients of the BDF formulas of order 1-6 (grsprse.F:698-720)
+    const double rows[6][7] = {{1.0, 1.0},
+                               {2.0 / 3.0, 1.0, 1.0 / 3.0},
+                               {6.0 / 11.0, 1.0, 6.0 / 11.0, 1.0 / 11.0},
+                               {12.0 / 25.0, 1.0, 0.70, 0.20, 0.02},
+                               {60.0 / 137.0, 1.0, 225.0 / 274.0, 85.0 / 274.0, 15.0 / 274.0, 1.0 / 274.0},
+                               {180.0 / 441.0, 1.0, 406.0 / 441.0, 735.0 / 1764.0, 175.0 / 1764.0, 21.0 / 1764.0,
+                                1.0 / 1764.0}};
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 7; ++j) g->aset[i][j] = rows[i][j];
+    g->errmax = rtol;
+    g->ylow = (double)min_atol;
+    const double abhi = log10((double)max_atol), ablo = log10((double)min_atol);
+    g->atol_level[0] = pow(10.0, abhi);
+    g->atol_level[gear::NBINS] = pow(10.0, ablo);
+    for (int i = 2; i <= gear::NBINS; ++i) {
+        const double t = (abhi - ablo) * (double)(gear::NBINS - i + 1) / (double)gear::NBINS;
+        g->atol_level[i - 1] = pow(10.0, ablo + t);
+    }
+    g->atol_floor = (double)conc_floor;
+    g->max_iter = max_iter;
+}
+
+int upload_gear_coef(cmaqchem_handle* h)
+{
+    gear_coefficients(h->cfg.rtol, h->gear_max_atol, h->gear_min_atol, h->gear_floor, h->max_iter, &h->gear_coef);
+    if (!h->d_gear_coef) CK(cudaMalloc(&h->d_gear_coef, sizeof(gear::Coef)));
+    CK(cudaMemcpy(h->d_gear_coef, &h->gear_coef, sizeof(gear::Coef), cudaMemcpyHostToDevice));
+    return 0;
 }
 
 chem::GridArgs grid_args(cmaqchem_handle* h, float* conc, const float* ta, const float* qv, const float* dens,
@@ -255,7 +313,9 @@ extern "C" int cmaqchem_init(const cmaqchem_cfg* cfg, cmaqchem_handle** out)
     *out = nullptr;
     const MechOps* m = find_mech(cfg->mechanism);
     if (!m) return fail(std::string("unknown mechanism ") + (cfg->mechanism ? cfg->mechanism : "(null)"));
-    if (cfg->solver != CMAQCHEM_SOLVER_ROS3 && cfg->solver != CMAQCHEM_SOLVER_EBI) return fail("unknown solver");
+    if (cfg->solver != CMAQCHEM_SOLVER_ROS3 && cfg->solver != CMAQCHEM_SOLVER_EBI &&
+        cfg->solver != CMAQCHEM_SOLVER_GEAR)
+        return fail("unknown solver");
     if (cfg->schedule != CMAQCHEM_SCHED_STATIC && cfg->schedule != CMAQCHEM_SCHED_QUEUE)
         return fail("unknown schedule");
     if (cfg->ncols <= 0 || cfg->nrows <= 0 || cfg->nlays <= 0) return fail("domain dimensions must be positive");
@@ -268,6 +328,14 @@ extern "C" int cmaqchem_init(const cmaqchem_cfg* cfg, cmaqchem_handle** out)
     h->ncolrow = cfg->ncols * cfg->nrows;
     h->ncell = (long long)h->ncolrow * cfg->nlays;
     h->max_iter = cfg->max_iter > 0 ? cfg->max_iter : 100000;
+    h->ws_elems = cfg->solver == CMAQCHEM_SOLVER_GEAR ? m->gear_ws_elems : m->ws_elems;
+    if (cfg->solver == CMAQCHEM_SOLVER_GEAR) {
+        h->gear_min_atol = (float)cfg->atol;   // cfg.atol = REAL(GEAR_MIN_ATOL, 8)
+        if (!(h->gear_max_atol > h->gear_min_atol) || !(h->gear_min_atol > h->gear_floor)) {
+            delete h;
+            return fail("SMVGEAR needs GEAR_MAX_ATOL (1e-7) > atol > GEAR_CONC_FLOOR (1e-12)");
+        }
+    }
     h->rnspec = (double)(1.0f / (float)m->nspec);   // RNSPEC = 1.0 / FLOAT(N_SPEC), REAL(4)
     h->cgrid_index.resize(m->nspec);
     for (int s = 0; s < m->nspec; ++s) {
@@ -303,6 +371,17 @@ extern "C" int cmaqchem_init(const cmaqchem_cfg* cfg, cmaqchem_handle** out)
         h->nblocks = h->nsm * h->bps;
         if (ensure_ws(h, (size_t)h->nblocks * chem::WARPS_PER_BLOCK)) return -1;
         if (configure_queue(h)) return -1;
+        if (cfg->solver == CMAQCHEM_SOLVER_GEAR) {
+            int gb = 0;
+            CK(m->gear_occupancy(&gb));
+            h->gear_nblocks = h->nsm * (gb > 0 ? gb : 1);
+            if (ensure_ws(h, (size_t)h->gear_nblocks * chem::GEAR_WPB)) return -1;
+            int gw = 0;
+            CK(m->gear_warp_occupancy(&gw));
+            h->gearw_nblocks = h->nsm * (gw > 0 ? gw : 1);
+            if (ensure_ws(h, (size_t)h->gearw_nblocks)) return -1;
+            if (upload_gear_coef(h)) return -1;
+        }
         if (cfg->solver == CMAQCHEM_SOLVER_EBI) {
             int bw = 0;
             CK(m->ebi_warp_occupancy(&bw));
@@ -360,6 +439,11 @@ extern "C" int cmaqchem_diag_set_tuning(cmaqchem_handle* h, const char* key, int
         if (value < 0 || value > 2) return fail("lockstep must be 0, 1 or 2");
         if (value == 0 && h->q_wpb != 8) return fail("lockstep 0 needs block_warps 8");
         h->q_sync = value;
+    } else if (strcmp(key, "gear_warp") == 0) {
+        h->gear_warp = value != 0;
+        if (h->graph_exec) CK(cudaGraphExecDestroy(h->graph_exec));
+        h->graph_exec = nullptr;
+        return 0;
     } else if (strcmp(key, "ebi_warp") == 0) {
         h->ebi_warp = value != 0;
         if (h->graph_exec) CK(cudaGraphExecDestroy(h->graph_exec));
@@ -394,11 +478,12 @@ static int enqueue_step(cmaqchem_handle* h, const chem::GridArgs& a, int itmstep
                         long long c0 = 0, long long c1 = -1)
 {
     const bool ebi_solver = h->cfg.solver == CMAQCHEM_SOLVER_EBI;
+    const bool gear_solver = h->cfg.solver == CMAQCHEM_SOLVER_GEAR;
     if (c1 < 0) c1 = h->ncell;
     const long long n = c1 - c0;
-    if (h->cfg.schedule == CMAQCHEM_SCHED_QUEUE || ebi_solver) {
+    if (h->cfg.schedule == CMAQCHEM_SCHED_QUEUE || ebi_solver || gear_solver) {
         chem::QueueArgs q{nullptr, h->d_head, n, c0};
-        if (sort && h->cfg.schedule == CMAQCHEM_SCHED_QUEUE) {
+        if (sort && (h->cfg.schedule == CMAQCHEM_SCHED_QUEUE || gear_solver)) {
             const int nb = 4 * h->nsm;
             CK(cudaMemsetAsync(h->d_hist, 0, sizeof(unsigned int) * chem::QUEUE_BINS, s));
             chem::k_queue_hist<<<nb, 256, 0, s>>>(h->d_steps + c0, n, h->d_hist);
@@ -410,7 +495,12 @@ static int enqueue_step(cmaqchem_handle* h, const chem::GridArgs& a, int itmstep
             q.order = h->d_order + c0;
         }
         CK(cudaMemsetAsync(h->d_head, 0, sizeof(unsigned long long), s));
-        if (ebi_solver) {
+        if (gear_solver) {
+            chem::GearArgs g{};
+            g.coef = h->d_gear_coef;
+            if (h->gear_warp) CK(h->ops->gear_warp(a, q, g, true, h->gearw_nblocks, s));
+            else CK(h->ops->gear(a, q, g, true, h->gear_nblocks, s));
+        } else if (ebi_solver) {
             chem::EbiArgs e{};
             ebi::steps_for(itmstep, h->ops->ebi_deltat, &e.n_ebi_steps, &e.tmstep);
             e.fwd = h->d_ebi_fwd;
@@ -591,7 +681,7 @@ extern "C" int cmaqchem_step(cmaqchem_handle* h, float* conc, const float* ta, c
     // The grid is split into chunks of consecutive cells: the inputs of chunk i+1 travel
     // and the results of chunk i-1 come back while chunk i is integrated.  Only the
     // mechanism's CGRID planes are read and written by CHEM.
-    const bool chunked = h->cfg.schedule == CMAQCHEM_SCHED_QUEUE || h->cfg.solver == CMAQCHEM_SOLVER_EBI;
+    const bool chunked = h->cfg.schedule == CMAQCHEM_SCHED_QUEUE || h->cfg.solver != CMAQCHEM_SOLVER_ROS3;
     const int nch = chunked ? std::max(1, std::min<int>(h->e2e_chunks, (int)std::min<long long>(MAX_E2E_CHUNKS, nc))) : 1;
     const int nhet = h->ops->nhetero;
     CK(cudaMemcpyAsync(h->s_seaice, seaice, sizeof(float) * ncr, cudaMemcpyHostToDevice, cs));
@@ -694,6 +784,52 @@ extern "C" int cmaqchem_ebi_solve_device(cmaqchem_handle* h, long long ncell, do
     CK(h->ops->ebi_solve(a, h->nblocks, s));
     CK(cudaStreamSynchronize(s));
     return 0;
+}
+
+extern "C" int cmaqchem_gear_solve_device(cmaqchem_handle* h, long long ncell, double* y, const double* rk,
+                                          const unsigned char* night, double chemstep_min, int* cell_stats,
+                                          void* stream)
+{
+    if (!h) return fail("null handle");
+    if (h->cfg.solver != CMAQCHEM_SOLVER_GEAR) return fail("the handle was not made for CMAQCHEM_SOLVER_GEAR");
+    if (ncell < 0) return fail("ncell must be >= 0");
+    if (ncell == 0) return 0;
+    if (!y || !rk || !night) return fail("null array argument");
+    if (!(chemstep_min > 0.0)) return fail("chemstep must be positive");
+    CK(cudaSetDevice(h->device));
+    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    chem::GridArgs a{};
+    a.ncell = ncell;
+    a.chemstep = chemstep_min;
+    a.ws = h->d_ws;
+    a.max_iter = h->max_iter;
+    chem::QueueArgs q{nullptr, h->d_head, ncell, 0};
+    chem::GearArgs g{};
+    g.coef = h->d_gear_coef;
+    g.y = y;
+    g.rk = rk;
+    g.night = night;
+    g.cell_stats = cell_stats;
+    CK(cudaMemsetAsync(h->d_head, 0, sizeof(unsigned long long), s));
+    if (h->gear_warp) CK(h->ops->gear_warp(a, q, g, false, h->gearw_nblocks, s));
+    else CK(h->ops->gear(a, q, g, false, h->gear_nblocks, s));
+    CK(cudaStreamSynchronize(s));
+    return 0;
+}
+
+extern "C" int cmaqchem_gear_tolerances(cmaqchem_handle* h, float max_atol, float min_atol, float conc_floor)
+{
+    if (!h) return fail("null handle");
+    if (h->cfg.solver != CMAQCHEM_SOLVER_GEAR) return fail("the handle was not made for CMAQCHEM_SOLVER_GEAR");
+    if (!(max_atol > min_atol) || !(min_atol > conc_floor) || !(conc_floor > 0.0f))
+        return fail("need max_atol > min_atol > conc_floor > 0");
+    CK(cudaSetDevice(h->device));
+    h->gear_max_atol = max_atol;
+    h->gear_min_atol = min_atol;
+    h->gear_floor = conc_floor;
+    if (h->graph_exec) CK(cudaGraphExecDestroy(h->graph_exec));
+    h->graph_exec = nullptr;
+    return upload_gear_coef(h);
 }
 
 extern "C" int cmaqchem_rconst_device(cmaqchem_handle* h, const float* conc, const float* ta, const float* qv,

@@ -74,9 +74,11 @@ __device__ __forceinline__ double* warp_ws(double* ws_all, long long warp_global
     return ws_all + (size_t)warp_global * ((size_t)M::WS_ELEMS * 32) + (threadIdx.x & 31);
 }
 
-// Gather one cell into ws (Y, RKI); returns the cell's sunlight flag.
+// Gather one cell into ws (Y, RKI); returns the cell's sunlight flag.  floor64: the
+// SMVGEAR driver's REAL(8) concentration floor (grdriver.F:419-422) instead of ROS3's
+// REAL(4) one.
 template <class M>
-__device__ bool gather_cell(const GridArgs& a, long long c, double* __restrict__ ws)
+__device__ bool gather_cell(const GridArgs& a, long long c, double* __restrict__ ws, bool floor64 = false)
 {
     const float taf = a.ta[c];
     const float densf = a.dens[c];
@@ -88,10 +90,8 @@ __device__ bool gather_cell(const GridArgs& a, long long c, double* __restrict__
     const double seawater = (double)fmaxf(0.0f, __fsub_rn(a.ocean_szone[col], a.seaice[col]));
     for (int s = 0; s < M::ISCHAN; ++s) {
         const float conc = a.cgrid[(size_t)a.cgrid_index[s] * a.ncell + c];
-        float v;
-        if (a.convert[s]) v = fmaxf(__fmul_rn(__fmul_rn(a.fwd_conv[s], svol), conc), CONCMIN_F);
-        else v = fmaxf(conc, CONCMIN_F);
-        ws[(M::OFF_Y + M::iold2new(s)) * 32] = (double)v;
+        const float v = a.convert[s] ? __fmul_rn(__fmul_rn(a.fwd_conv[s], svol), conc) : conc;
+        ws[(M::OFF_Y + M::iold2new(s)) * 32] = floor64 ? fmax((double)v, 1.0e-30) : (double)fmaxf(v, CONCMIN_F);
     }
     double rjv[M::NPHOTAB];
     bool sun = false;

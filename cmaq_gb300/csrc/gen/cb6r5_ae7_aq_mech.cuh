@@ -57,6 +57,14 @@ constexpr int ADJ_EMIS = 5159;
 constexpr int ADJ_GE = 5308;
 constexpr int ADJ_GK = 5457;
 constexpr int OFF_YAVE = 2277;
+constexpr int GEAR_WS_ELEMS = 5159;
+constexpr int GEAR_CNEW = 0;
+constexpr int GEAR_GLOSS = 298;
+constexpr int GEAR_DTLOS = 596;
+constexpr int GEAR_CHOLD = 745;
+constexpr int GEAR_CEST = 894;
+constexpr int GEAR_BLKCONC = 447;
+constexpr int GEAR_CONC = 4265;
 constexpr int EBIW_YC = 0;
 constexpr int EBIW_YC0 = 149;
 constexpr int EBIW_YCP = 298;
@@ -81,6 +89,72 @@ __device__ void feval_0(double* __restrict__ ws, int src, int dst);
 __device__ void explic_0(double* __restrict__ ws);
 __device__ void feval_1(double* __restrict__ ws, int src, int dst);
 __device__ void explic_1(double* __restrict__ ws);
+__device__ void gear_explic_0(double* __restrict__ ws);
+__device__ void feval_s1_0(double* __restrict__ ws, int src, int dst);
+__device__ void gear_explic_s1_0(double* __restrict__ ws);
+__device__ void gear_pdecomp_0_0(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_0(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_1(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_1(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_2(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_2(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_3(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_3(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_4(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_4(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_5(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_5(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_6(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_6(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_7(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_7(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_8(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_8(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_9(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_9(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_10(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_10(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_11(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_11(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_12(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_12(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_13(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_13(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_14(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_14(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_15(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_15(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_16(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_16(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_17(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_17(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_18(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_18(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_19(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_19(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_20(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_20(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_21(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_21(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_22(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_22(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_23(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_23(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_24(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_24(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_25(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_25(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_26(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_26(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_27(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_27(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_28(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_28(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_29(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_29(double* __restrict__ ws, double r1delt);
+__device__ void solve_s1_0_0(double* __restrict__ ws, int rhs);
+__device__ void solve_s1_0_1(double* __restrict__ ws, int rhs);
+__device__ void solve_s1_0_2(double* __restrict__ ws, int rhs);
 __device__ void jacdecomp_0_0(double* __restrict__ ws, double gdtinv);
 __device__ void jacdecomp_0_1(double* __restrict__ ws, double gdtinv);
 __device__ void jacdecomp_0_2(double* __restrict__ ws, double gdtinv);
@@ -259,6 +333,78 @@ __device__ void ebi_hrg2(double* __restrict__ sm, double dtc);
 __device__ void ebi_hrg3(double* __restrict__ sm, double dtc);
 __device__ void ebi_hrg4(double* __restrict__ sm, double dtc);
 }  // namespace wsm
+__device__ __forceinline__ void gear_pdecomp_0(double* __restrict__ ws, double r1delt)
+{
+    gear_pdecomp_0_0(ws, r1delt);
+    gear_pdecomp_0_1(ws, r1delt);
+    gear_pdecomp_0_2(ws, r1delt);
+    gear_pdecomp_0_3(ws, r1delt);
+    gear_pdecomp_0_4(ws, r1delt);
+    gear_pdecomp_0_5(ws, r1delt);
+    gear_pdecomp_0_6(ws, r1delt);
+    gear_pdecomp_0_7(ws, r1delt);
+    gear_pdecomp_0_8(ws, r1delt);
+    gear_pdecomp_0_9(ws, r1delt);
+    gear_pdecomp_0_10(ws, r1delt);
+    gear_pdecomp_0_11(ws, r1delt);
+    gear_pdecomp_0_12(ws, r1delt);
+    gear_pdecomp_0_13(ws, r1delt);
+    gear_pdecomp_0_14(ws, r1delt);
+    gear_pdecomp_0_15(ws, r1delt);
+    gear_pdecomp_0_16(ws, r1delt);
+    gear_pdecomp_0_17(ws, r1delt);
+    gear_pdecomp_0_18(ws, r1delt);
+    gear_pdecomp_0_19(ws, r1delt);
+    gear_pdecomp_0_20(ws, r1delt);
+    gear_pdecomp_0_21(ws, r1delt);
+    gear_pdecomp_0_22(ws, r1delt);
+    gear_pdecomp_0_23(ws, r1delt);
+    gear_pdecomp_0_24(ws, r1delt);
+    gear_pdecomp_0_25(ws, r1delt);
+    gear_pdecomp_0_26(ws, r1delt);
+    gear_pdecomp_0_27(ws, r1delt);
+    gear_pdecomp_0_28(ws, r1delt);
+    gear_pdecomp_0_29(ws, r1delt);
+}
+__device__ __forceinline__ void gear_pdecomp_s1_0(double* __restrict__ ws, double r1delt)
+{
+    gear_pdecomp_s1_0_0(ws, r1delt);
+    gear_pdecomp_s1_0_1(ws, r1delt);
+    gear_pdecomp_s1_0_2(ws, r1delt);
+    gear_pdecomp_s1_0_3(ws, r1delt);
+    gear_pdecomp_s1_0_4(ws, r1delt);
+    gear_pdecomp_s1_0_5(ws, r1delt);
+    gear_pdecomp_s1_0_6(ws, r1delt);
+    gear_pdecomp_s1_0_7(ws, r1delt);
+    gear_pdecomp_s1_0_8(ws, r1delt);
+    gear_pdecomp_s1_0_9(ws, r1delt);
+    gear_pdecomp_s1_0_10(ws, r1delt);
+    gear_pdecomp_s1_0_11(ws, r1delt);
+    gear_pdecomp_s1_0_12(ws, r1delt);
+    gear_pdecomp_s1_0_13(ws, r1delt);
+    gear_pdecomp_s1_0_14(ws, r1delt);
+    gear_pdecomp_s1_0_15(ws, r1delt);
+    gear_pdecomp_s1_0_16(ws, r1delt);
+    gear_pdecomp_s1_0_17(ws, r1delt);
+    gear_pdecomp_s1_0_18(ws, r1delt);
+    gear_pdecomp_s1_0_19(ws, r1delt);
+    gear_pdecomp_s1_0_20(ws, r1delt);
+    gear_pdecomp_s1_0_21(ws, r1delt);
+    gear_pdecomp_s1_0_22(ws, r1delt);
+    gear_pdecomp_s1_0_23(ws, r1delt);
+    gear_pdecomp_s1_0_24(ws, r1delt);
+    gear_pdecomp_s1_0_25(ws, r1delt);
+    gear_pdecomp_s1_0_26(ws, r1delt);
+    gear_pdecomp_s1_0_27(ws, r1delt);
+    gear_pdecomp_s1_0_28(ws, r1delt);
+    gear_pdecomp_s1_0_29(ws, r1delt);
+}
+__device__ __forceinline__ void solve_s1_0(double* __restrict__ ws, int rhs)
+{
+    solve_s1_0_0(ws, rhs);
+    solve_s1_0_1(ws, rhs);
+    solve_s1_0_2(ws, rhs);
+}
 __device__ __forceinline__ void jacdecomp_0(double* __restrict__ ws, double gdtinv)
 {
     jacdecomp_0_0(ws, gdtinv);
@@ -629,6 +775,14 @@ struct Traits {
     static constexpr int ADJ_GE = mech_cb6r5_ae7_aq::ADJ_GE;
     static constexpr int ADJ_GK = mech_cb6r5_ae7_aq::ADJ_GK;
     static constexpr int OFF_YAVE = mech_cb6r5_ae7_aq::OFF_YAVE;
+    static constexpr int GEAR_WS_ELEMS = mech_cb6r5_ae7_aq::GEAR_WS_ELEMS;
+    static constexpr int GEAR_CNEW = mech_cb6r5_ae7_aq::GEAR_CNEW;
+    static constexpr int GEAR_GLOSS = mech_cb6r5_ae7_aq::GEAR_GLOSS;
+    static constexpr int GEAR_DTLOS = mech_cb6r5_ae7_aq::GEAR_DTLOS;
+    static constexpr int GEAR_CHOLD = mech_cb6r5_ae7_aq::GEAR_CHOLD;
+    static constexpr int GEAR_CEST = mech_cb6r5_ae7_aq::GEAR_CEST;
+    static constexpr int GEAR_BLKCONC = mech_cb6r5_ae7_aq::GEAR_BLKCONC;
+    static constexpr int GEAR_CONC = mech_cb6r5_ae7_aq::GEAR_CONC;
     static constexpr int EBIW_YC = mech_cb6r5_ae7_aq::EBIW_YC;
     static constexpr int EBIW_YC0 = mech_cb6r5_ae7_aq::EBIW_YC0;
     static constexpr int EBIW_YCP = mech_cb6r5_ae7_aq::EBIW_YCP;
@@ -644,6 +798,12 @@ struct Traits {
     static __device__ __forceinline__ int inew2old(int i) { return mech_cb6r5_ae7_aq::c_inew2old[i]; }
     static __device__ __forceinline__ void feval_0(double* ws, int s, int t) { mech_cb6r5_ae7_aq::feval_0(ws, s, t); }
     static __device__ __forceinline__ void explic_0(double* ws) { mech_cb6r5_ae7_aq::explic_0(ws); }
+    static __device__ __forceinline__ void gear_explic_0(double* ws) { mech_cb6r5_ae7_aq::gear_explic_0(ws); }
+    static __device__ __forceinline__ void gear_pdecomp_0(double* ws, double r) { mech_cb6r5_ae7_aq::gear_pdecomp_0(ws, r); }
+    static __device__ __forceinline__ void feval_s1_0(double* ws, int s, int t) { mech_cb6r5_ae7_aq::feval_s1_0(ws, s, t); }
+    static __device__ __forceinline__ void gear_explic_s1_0(double* ws) { mech_cb6r5_ae7_aq::gear_explic_s1_0(ws); }
+    static __device__ __forceinline__ void gear_pdecomp_s1_0(double* ws, double r) { mech_cb6r5_ae7_aq::gear_pdecomp_s1_0(ws, r); }
+    static __device__ __forceinline__ void solve_s1_0(double* ws, int r) { mech_cb6r5_ae7_aq::solve_s1_0(ws, r); }
     static __device__ __forceinline__ void jacdecomp_0(double* ws, double g) { mech_cb6r5_ae7_aq::jacdecomp_0(ws, g); }
     static __device__ __forceinline__ void solve_0(double* ws, int r) { mech_cb6r5_ae7_aq::solve_0(ws, r); }
     static __device__ __forceinline__ void jacdecomp_0_sync(double* ws, double g, bool go) { mech_cb6r5_ae7_aq::jacdecomp_0_sync(ws, g, go); }

@@ -6231,4 +6231,279 @@ __device__ __noinline__ void explic_1(double* __restrict__ ws)
     { const double kk = ws[44480]; ws[72736] = kk * y[4640]; ws[72768] = kk * y[2016]; }
     { const double kk = ws[44512]; ws[72800] = kk * y[4544]; ws[72832] = kk * y[2016]; }
 }
+// Partial-derivative products of 2- and 3-reactant reactions (grpderiv.F:163-189).
+__device__ __noinline__ void gear_explic_0(double* __restrict__ ws)
+{
+    const double* __restrict__ y = ws + 0;
+#define CEFF_(v) ((v) <= 1.0e-30 ? 0.0 : (v))
+    { const double kk = ws[33440]; ws[55712] = kk * CEFF_(y[4384]); ws[55744] = kk * CEFF_(y[4320]); }
+    { const double kk = ws[33472]; ws[55776] = kk * CEFF_(y[4384]); ws[55808] = kk * CEFF_(y[4160]); }
+    { const double kk = ws[33504]; ws[55840] = kk * CEFF_(y[4608]); ws[55872] = kk * CEFF_(y[4160]); }
+    { const double kk = ws[33536]; ws[55904] = kk * CEFF_(y[4608]); ws[55936] = kk * CEFF_(y[4160]); }
+    { const double kk = ws[33568]; ws[55968] = kk * CEFF_(y[4320]); ws[56000] = kk * CEFF_(y[4160]); }
+    { const double kk = ws[33728]; ws[56032] = kk * CEFF_(y[4736]); ws[56064] = kk * CEFF_(y[4320]); }
+    { const double kk = ws[33760]; ws[56096] = kk * CEFF_(y[4704]); ws[56128] = kk * CEFF_(y[4320]); }
+    { const double kk = ws[33792]; ws[56160] = kk * CEFF_(y[4160]); ws[56192] = kk * CEFF_(y[4736]); }
+    { const double kk = ws[33824]; ws[56224] = kk * CEFF_(y[4160]); ws[56256] = kk * CEFF_(y[4704]); }
+    { const double kk = ws[33856]; ws[56288] = kk * CEFF_(y[4736]); ws[56320] = kk * CEFF_(y[4736]); }
+    { const double kk = ws[33888]; ws[56352] = kk * CEFF_(y[4736]); ws[56384] = kk * CEFF_(y[4736]); }
+    { const double kk = ws[33920]; ws[56416] = kk * CEFF_(y[4704]); ws[56448] = kk * CEFF_(y[4736]); }
+    { const double kk = ws[33952]; ws[56480] = kk * CEFF_(y[4704]); ws[56512] = kk * CEFF_(y[4704]); }
+    { const double kk = ws[33984]; ws[56544] = kk * CEFF_(y[4704]); ws[56576] = kk * CEFF_(y[4704]); }
+    { const double kk = ws[34048]; ws[56608] = kk * CEFF_(y[4736]); ws[56640] = kk * CEFF_(y[3456]); }
+    { const double kk = ws[34080]; ws[56672] = kk * CEFF_(y[4160]); ws[56704] = kk * CEFF_(y[3456]); }
+    { const double kk = ws[34112]; ws[56736] = kk * CEFF_(y[4384]); ws[56768] = kk * CEFF_(y[4384]); }
+    { const double kk = ws[34144]; ws[56800] = kk * CEFF_(y[4384]); ws[56832] = kk * CEFF_(y[4704]); }
+    { const double kk = ws[34176]; ws[56864] = kk * CEFF_(y[4320]); ws[56896] = kk * CEFF_(y[4608]); }
+    { const double kk = ws[34272]; ws[56928] = kk * CEFF_(y[4384]); ws[56960] = kk * CEFF_(y[4640]); }
+    { const double kk = ws[34304]; ws[56992] = kk * CEFF_(y[4608]); ws[57024] = kk * CEFF_(y[4640]); }
+    { const double kk = ws[34336]; ws[57056] = kk * CEFF_(y[4160]); ws[57088] = kk * CEFF_(y[4640]); }
+    { const double kk = ws[34368]; ws[57120] = kk * CEFF_(y[4736]); ws[57152] = kk * CEFF_(y[4640]); }
+    { const double kk = ws[34400]; ws[57184] = kk * CEFF_(y[4704]); ws[57216] = kk * CEFF_(y[4640]); }
+    { const double kk = ws[34432]; ws[57248] = kk * CEFF_(y[4320]); ws[57280] = kk * CEFF_(y[4640]); }
+    { const double kk = ws[34464]; ws[57312] = kk * CEFF_(y[4640]); ws[57344] = kk * CEFF_(y[4640]); }
+    { const double kk = ws[34496]; ws[57376] = kk * CEFF_(y[4608]); ws[57408] = kk * CEFF_(y[4640]); }
+    { const double kk = ws[34624]; ws[57440] = kk * CEFF_(y[4736]); ws[57472] = kk * CEFF_(y[4384]); }
+    { const double kk = ws[34656]; ws[57504] = kk * CEFF_(y[4608]); ws[57536] = kk * CEFF_(y[4384]); }
+    { const double kk = ws[34688]; ws[57568] = kk * CEFF_(y[2464]); ws[57600] = kk * CEFF_(y[2464]); }
+    { const double kk = ws[34752]; ws[57632] = kk * CEFF_(y[4736]); ws[57664] = kk * CEFF_(y[2464]); }
+    { const double kk = ws[34784]; ws[57696] = kk * CEFF_(y[4736]); ws[57728] = kk * CEFF_(y[4608]); }
+    { const double kk = ws[34816]; ws[57760] = kk * CEFF_(y[4736]); ws[57792] = kk * CEFF_(y[4192]); }
+    { const double kk = ws[34880]; ws[57824] = kk * CEFF_(y[4608]); ws[57856] = kk * CEFF_(y[4704]); }
+    { const double kk = ws[34976]; ws[57888] = kk * CEFF_(y[4736]); ws[57920] = kk * CEFF_(y[1696]); }
+    { const double kk = ws[35008]; ws[57952] = kk * CEFF_(y[4736]); ws[57984] = kk * CEFF_(y[2208]); }
+    { const double kk = ws[35040]; ws[58016] = kk * CEFF_(y[4384]); ws[58048] = kk * CEFF_(y[4448]); }
+    { const double kk = ws[35072]; ws[58080] = kk * CEFF_(y[4608]); ws[58112] = kk * CEFF_(y[4448]); }
+    { const double kk = ws[35168]; ws[58144] = kk * CEFF_(y[4704]); ws[58176] = kk * CEFF_(y[4448]); }
+    { const double kk = ws[35200]; ws[58208] = kk * CEFF_(y[4672]); ws[58240] = kk * CEFF_(y[4448]); }
+    { const double kk = ws[35232]; ws[58272] = kk * CEFF_(y[4448]); ws[58304] = kk * CEFF_(y[4448]); }
+    { const double kk = ws[35264]; ws[58336] = kk * CEFF_(y[4096]); ws[58368] = kk * CEFF_(y[4448]); }
+    { const double kk = ws[35296]; ws[58400] = kk * CEFF_(y[4384]); ws[58432] = kk * CEFF_(y[4096]); }
+    { const double kk = ws[35328]; ws[58464] = kk * CEFF_(y[4608]); ws[58496] = kk * CEFF_(y[4096]); }
+    { const double kk = ws[35424]; ws[58528] = kk * CEFF_(y[4704]); ws[58560] = kk * CEFF_(y[4096]); }
+    { const double kk = ws[35456]; ws[58592] = kk * CEFF_(y[4672]); ws[58624] = kk * CEFF_(y[4096]); }
+    { const double kk = ws[35488]; ws[58656] = kk * CEFF_(y[4096]); ws[58688] = kk * CEFF_(y[4096]); }
+    { const double kk = ws[35520]; ws[58720] = kk * CEFF_(y[4384]); ws[58752] = kk * CEFF_(y[4672]); }
+    { const double kk = ws[35552]; ws[58784] = kk * CEFF_(y[4704]); ws[58816] = kk * CEFF_(y[4672]); }
+    { const double kk = ws[35584]; ws[58848] = kk * CEFF_(y[4672]); ws[58880] = kk * CEFF_(y[4672]); }
+    { const double kk = ws[35616]; ws[58912] = kk * CEFF_(y[4384]); ws[58944] = kk * CEFF_(y[4416]); }
+    { const double kk = ws[35648]; ws[58976] = kk * CEFF_(y[4704]); ws[59008] = kk * CEFF_(y[4416]); }
+    { const double kk = ws[35680]; ws[59040] = kk * CEFF_(y[4448]); ws[59072] = kk * CEFF_(y[4416]); }
+    { const double kk = ws[35712]; ws[59104] = kk * CEFF_(y[4672]); ws[59136] = kk * CEFF_(y[4416]); }
+    { const double kk = ws[35744]; ws[59168] = kk * CEFF_(y[4384]); ws[59200] = kk * CEFF_(y[4576]); }
+    { const double kk = ws[35776]; ws[59232] = kk * CEFF_(y[4704]); ws[59264] = kk * CEFF_(y[4576]); }
+    { const double kk = ws[35808]; ws[59296] = kk * CEFF_(y[4448]); ws[59328] = kk * CEFF_(y[4576]); }
+    { const double kk = ws[35840]; ws[59360] = kk * CEFF_(y[4672]); ws[59392] = kk * CEFF_(y[4576]); }
+    { const double kk = ws[35872]; ws[59424] = kk * CEFF_(y[4384]); ws[59456] = kk * CEFF_(y[4352]); }
+    { const double kk = ws[35904]; ws[59488] = kk * CEFF_(y[4704]); ws[59520] = kk * CEFF_(y[4352]); }
+    { const double kk = ws[35936]; ws[59552] = kk * CEFF_(y[4448]); ws[59584] = kk * CEFF_(y[4352]); }
+    { const double kk = ws[35968]; ws[59616] = kk * CEFF_(y[4672]); ws[59648] = kk * CEFF_(y[4352]); }
+    { const double kk = ws[36000]; ws[59680] = kk * CEFF_(y[4384]); ws[59712] = kk * CEFF_(y[4288]); }
+    { const double kk = ws[36032]; ws[59744] = kk * CEFF_(y[4704]); ws[59776] = kk * CEFF_(y[4288]); }
+    { const double kk = ws[36064]; ws[59808] = kk * CEFF_(y[4448]); ws[59840] = kk * CEFF_(y[4288]); }
+    { const double kk = ws[36096]; ws[59872] = kk * CEFF_(y[4672]); ws[59904] = kk * CEFF_(y[4288]); }
+    { const double kk = ws[36128]; ws[59936] = kk * CEFF_(y[4736]); ws[59968] = kk * CEFF_(y[2272]); }
+    { const double kk = ws[36192]; ws[60000] = kk * CEFF_(y[4736]); ws[60032] = kk * CEFF_(y[2880]); }
+    { const double kk = ws[36256]; ws[60064] = kk * CEFF_(y[4736]); ws[60096] = kk * CEFF_(y[3648]); }
+    { const double kk = ws[36320]; ws[60128] = kk * CEFF_(y[4736]); ws[60160] = kk * CEFF_(y[3776]); }
+    { const double kk = ws[36352]; ws[60192] = kk * CEFF_(y[4736]); ws[60224] = kk * CEFF_(y[3904]); }
+    { const double kk = ws[36384]; ws[60256] = kk * CEFF_(y[4736]); ws[60288] = kk * CEFF_(y[2688]); }
+    { const double kk = ws[36416]; ws[60320] = kk * CEFF_(y[4736]); ws[60352] = kk * CEFF_(y[4512]); }
+    { const double kk = ws[36512]; ws[60384] = kk * CEFF_(y[4160]); ws[60416] = kk * CEFF_(y[4512]); }
+    { const double kk = ws[36544]; ws[60448] = kk * CEFF_(y[4640]); ws[60480] = kk * CEFF_(y[4512]); }
+    { const double kk = ws[36576]; ws[60512] = kk * CEFF_(y[4704]); ws[60544] = kk * CEFF_(y[4512]); }
+    { const double kk = ws[36640]; ws[60576] = kk * CEFF_(y[4384]); ws[60608] = kk * CEFF_(y[1728]); }
+    { const double kk = ws[36672]; ws[60640] = kk * CEFF_(y[4704]); ws[60672] = kk * CEFF_(y[1728]); }
+    { const double kk = ws[36704]; ws[60704] = kk * CEFF_(y[4160]); ws[60736] = kk * CEFF_(y[4128]); }
+    { const double kk = ws[36736]; ws[60768] = kk * CEFF_(y[4736]); ws[60800] = kk * CEFF_(y[4128]); }
+    { const double kk = ws[36768]; ws[60832] = kk * CEFF_(y[4640]); ws[60864] = kk * CEFF_(y[4128]); }
+    { const double kk = ws[36832]; ws[60896] = kk * CEFF_(y[4160]); ws[60928] = kk * CEFF_(y[4064]); }
+    { const double kk = ws[36864]; ws[60960] = kk * CEFF_(y[4736]); ws[60992] = kk * CEFF_(y[4064]); }
+    { const double kk = ws[36896]; ws[61024] = kk * CEFF_(y[4640]); ws[61056] = kk * CEFF_(y[4064]); }
+    { const double kk = ws[36960]; ws[61088] = kk * CEFF_(y[4736]); ws[61120] = kk * CEFF_(y[3840]); }
+    { const double kk = ws[37024]; ws[61152] = kk * CEFF_(y[4640]); ws[61184] = kk * CEFF_(y[3840]); }
+    { const double kk = ws[37056]; ws[61216] = kk * CEFF_(y[4736]); ws[61248] = kk * CEFF_(y[4256]); }
+    { const double kk = ws[37120]; ws[61280] = kk * CEFF_(y[4640]); ws[61312] = kk * CEFF_(y[4256]); }
+    { const double kk = ws[37184]; ws[61344] = kk * CEFF_(y[4640]); ws[61376] = kk * CEFF_(y[4000]); }
+    { const double kk = ws[37216]; ws[61408] = kk * CEFF_(y[4736]); ws[61440] = kk * CEFF_(y[4000]); }
+    { const double kk = ws[37280]; ws[61472] = kk * CEFF_(y[4736]); ws[61504] = kk * CEFF_(y[4480]); }
+    { const double kk = ws[37344]; ws[61536] = kk * CEFF_(y[4736]); ws[61568] = kk * CEFF_(y[832]); }
+    { const double kk = ws[37376]; ws[61600] = kk * CEFF_(y[4736]); ws[61632] = kk * CEFF_(y[2720]); }
+    { const double kk = ws[37408]; ws[61664] = kk * CEFF_(y[4736]); ws[61696] = kk * CEFF_(y[864]); }
+    { const double kk = ws[37504]; ws[61728] = kk * CEFF_(y[4736]); ws[61760] = kk * CEFF_(y[3392]); }
+    { const double kk = ws[37536]; ws[61792] = kk * CEFF_(y[4736]); ws[61824] = kk * CEFF_(y[896]); }
+    { const double kk = ws[37568]; ws[61856] = kk * CEFF_(y[4736]); ws[61888] = kk * CEFF_(y[4224]); }
+    { const double kk = ws[37664]; ws[61920] = kk * CEFF_(y[4608]); ws[61952] = kk * CEFF_(y[960]); }
+    { const double kk = ws[37696]; ws[61984] = kk * CEFF_(y[4736]); ws[62016] = kk * CEFF_(y[352]); }
+    { const double kk = ws[37728]; ws[62048] = kk * CEFF_(y[4160]); ws[62080] = kk * CEFF_(y[2656]); }
+    { const double kk = ws[37760]; ws[62112] = kk * CEFF_(y[4736]); ws[62144] = kk * CEFF_(y[2656]); }
+    { const double kk = ws[37792]; ws[62176] = kk * CEFF_(y[4320]); ws[62208] = kk * CEFF_(y[2656]); }
+    { const double kk = ws[37824]; ws[62240] = kk * CEFF_(y[4640]); ws[62272] = kk * CEFF_(y[2656]); }
+    { const double kk = ws[37856]; ws[62304] = kk * CEFF_(y[4160]); ws[62336] = kk * CEFF_(y[3552]); }
+    { const double kk = ws[37888]; ws[62368] = kk * CEFF_(y[4736]); ws[62400] = kk * CEFF_(y[3552]); }
+    { const double kk = ws[37920]; ws[62432] = kk * CEFF_(y[4320]); ws[62464] = kk * CEFF_(y[3552]); }
+    { const double kk = ws[37952]; ws[62496] = kk * CEFF_(y[4640]); ws[62528] = kk * CEFF_(y[3552]); }
+    { const double kk = ws[37984]; ws[62560] = kk * CEFF_(y[4160]); ws[62592] = kk * CEFF_(y[3136]); }
+    { const double kk = ws[38016]; ws[62624] = kk * CEFF_(y[4736]); ws[62656] = kk * CEFF_(y[3136]); }
+    { const double kk = ws[38048]; ws[62688] = kk * CEFF_(y[4320]); ws[62720] = kk * CEFF_(y[3136]); }
+    { const double kk = ws[38080]; ws[62752] = kk * CEFF_(y[4640]); ws[62784] = kk * CEFF_(y[3136]); }
+    { const double kk = ws[38112]; ws[62816] = kk * CEFF_(y[4736]); ws[62848] = kk * CEFF_(y[2528]); }
+    { const double kk = ws[38144]; ws[62880] = kk * CEFF_(y[4160]); ws[62912] = kk * CEFF_(y[2528]); }
+    { const double kk = ws[38176]; ws[62944] = kk * CEFF_(y[4384]); ws[62976] = kk * CEFF_(y[3424]); }
+    { const double kk = ws[38208]; ws[63008] = kk * CEFF_(y[4704]); ws[63040] = kk * CEFF_(y[3424]); }
+    { const double kk = ws[38240]; ws[63072] = kk * CEFF_(y[4448]); ws[63104] = kk * CEFF_(y[3424]); }
+    { const double kk = ws[38272]; ws[63136] = kk * CEFF_(y[4672]); ws[63168] = kk * CEFF_(y[3424]); }
+    { const double kk = ws[38336]; ws[63200] = kk * CEFF_(y[4320]); ws[63232] = kk * CEFF_(y[2528]); }
+    { const double kk = ws[38368]; ws[63264] = kk * CEFF_(y[4640]); ws[63296] = kk * CEFF_(y[2528]); }
+    { const double kk = ws[38400]; ws[63328] = kk * CEFF_(y[4736]); ws[63360] = kk * CEFF_(y[3872]); }
+    { const double kk = ws[38432]; ws[63392] = kk * CEFF_(y[4320]); ws[63424] = kk * CEFF_(y[3872]); }
+    { const double kk = ws[38464]; ws[63456] = kk * CEFF_(y[4640]); ws[63488] = kk * CEFF_(y[3872]); }
+    { const double kk = ws[38528]; ws[63520] = kk * CEFF_(y[4736]); ws[63552] = kk * CEFF_(y[1664]); }
+    { const double kk = ws[38592]; ws[63584] = kk * CEFF_(y[4640]); ws[63616] = kk * CEFF_(y[1024]); }
+    { const double kk = ws[38624]; ws[63648] = kk * CEFF_(y[4736]); ws[63680] = kk * CEFF_(y[1056]); }
+    { const double kk = ws[38656]; ws[63712] = kk * CEFF_(y[4704]); ws[63744] = kk * CEFF_(y[3296]); }
+    { const double kk = ws[38688]; ws[63776] = kk * CEFF_(y[4384]); ws[63808] = kk * CEFF_(y[3296]); }
+    { const double kk = ws[38720]; ws[63840] = kk * CEFF_(y[4448]); ws[63872] = kk * CEFF_(y[3296]); }
+    { const double kk = ws[38752]; ws[63904] = kk * CEFF_(y[4672]); ws[63936] = kk * CEFF_(y[3296]); }
+    { const double kk = ws[38784]; ws[63968] = kk * CEFF_(y[4736]); ws[64000] = kk * CEFF_(y[1632]); }
+    { const double kk = ws[38816]; ws[64032] = kk * CEFF_(y[4160]); ws[64064] = kk * CEFF_(y[2048]); }
+    { const double kk = ws[38848]; ws[64096] = kk * CEFF_(y[4736]); ws[64128] = kk * CEFF_(y[2048]); }
+    { const double kk = ws[38880]; ws[64160] = kk * CEFF_(y[4320]); ws[64192] = kk * CEFF_(y[2048]); }
+    { const double kk = ws[38912]; ws[64224] = kk * CEFF_(y[4640]); ws[64256] = kk * CEFF_(y[2048]); }
+    { const double kk = ws[38944]; ws[64288] = kk * CEFF_(y[4160]); ws[64320] = kk * CEFF_(y[2112]); }
+    { const double kk = ws[38976]; ws[64352] = kk * CEFF_(y[4736]); ws[64384] = kk * CEFF_(y[2112]); }
+    { const double kk = ws[39008]; ws[64416] = kk * CEFF_(y[4320]); ws[64448] = kk * CEFF_(y[2112]); }
+    { const double kk = ws[39040]; ws[64480] = kk * CEFF_(y[4640]); ws[64512] = kk * CEFF_(y[2112]); }
+    { const double kk = ws[39072]; ws[64544] = kk * CEFF_(y[4736]); ws[64576] = kk * CEFF_(y[384]); }
+    { const double kk = ws[39104]; ws[64608] = kk * CEFF_(y[4384]); ws[64640] = kk * CEFF_(y[3104]); }
+    { const double kk = ws[39136]; ws[64672] = kk * CEFF_(y[4448]); ws[64704] = kk * CEFF_(y[3104]); }
+    { const double kk = ws[39168]; ws[64736] = kk * CEFF_(y[4704]); ws[64768] = kk * CEFF_(y[3104]); }
+    { const double kk = ws[39200]; ws[64800] = kk * CEFF_(y[4672]); ws[64832] = kk * CEFF_(y[3104]); }
+    { const double kk = ws[39232]; ws[64864] = kk * CEFF_(y[4736]); ws[64896] = kk * CEFF_(y[1088]); }
+    { const double kk = ws[39264]; ws[64928] = kk * CEFF_(y[4384]); ws[64960] = kk * CEFF_(y[3488]); }
+    { const double kk = ws[39296]; ws[64992] = kk * CEFF_(y[4448]); ws[65024] = kk * CEFF_(y[3488]); }
+    { const double kk = ws[39328]; ws[65056] = kk * CEFF_(y[4704]); ws[65088] = kk * CEFF_(y[3488]); }
+    { const double kk = ws[39360]; ws[65120] = kk * CEFF_(y[4672]); ws[65152] = kk * CEFF_(y[3488]); }
+    { const double kk = ws[39392]; ws[65184] = kk * CEFF_(y[4736]); ws[65216] = kk * CEFF_(y[1120]); }
+    { const double kk = ws[39424]; ws[65248] = kk * CEFF_(y[4736]); ws[65280] = kk * CEFF_(y[1152]); }
+    { const double kk = ws[39456]; ws[65312] = kk * CEFF_(y[4384]); ws[65344] = kk * CEFF_(y[3584]); }
+    { const double kk = ws[39488]; ws[65376] = kk * CEFF_(y[4704]); ws[65408] = kk * CEFF_(y[3584]); }
+    { const double kk = ws[39520]; ws[65440] = kk * CEFF_(y[4448]); ws[65472] = kk * CEFF_(y[3584]); }
+    { const double kk = ws[39552]; ws[65504] = kk * CEFF_(y[4672]); ws[65536] = kk * CEFF_(y[3584]); }
+    { const double kk = ws[39584]; ws[65568] = kk * CEFF_(y[4736]); ws[65600] = kk * CEFF_(y[3616]); }
+    { const double kk = ws[39616]; ws[65632] = kk * CEFF_(y[4640]); ws[65664] = kk * CEFF_(y[3616]); }
+    { const double kk = ws[39648]; ws[65696] = kk * CEFF_(y[4608]); ws[65728] = kk * CEFF_(y[3328]); }
+    { const double kk = ws[39680]; ws[65760] = kk * CEFF_(y[4704]); ws[65792] = kk * CEFF_(y[3328]); }
+    { const double kk = ws[39712]; ws[65824] = kk * CEFF_(y[4736]); ws[65856] = kk * CEFF_(y[2176]); }
+    { const double kk = ws[39744]; ws[65888] = kk * CEFF_(y[4640]); ws[65920] = kk * CEFF_(y[2176]); }
+    { const double kk = ws[39840]; ws[65952] = kk * CEFF_(y[4736]); ws[65984] = kk * CEFF_(y[3808]); }
+    { const double kk = ws[39872]; ws[66016] = kk * CEFF_(y[4320]); ws[66048] = kk * CEFF_(y[3808]); }
+    { const double kk = ws[39904]; ws[66080] = kk * CEFF_(y[4640]); ws[66112] = kk * CEFF_(y[3808]); }
+    { const double kk = ws[39968]; ws[66144] = kk * CEFF_(y[4736]); ws[66176] = kk * CEFF_(y[3936]); }
+    { const double kk = ws[40000]; ws[66208] = kk * CEFF_(y[4320]); ws[66240] = kk * CEFF_(y[3936]); }
+    { const double kk = ws[40032]; ws[66272] = kk * CEFF_(y[4640]); ws[66304] = kk * CEFF_(y[3936]); }
+    { const double kk = ws[40064]; ws[66336] = kk * CEFF_(y[4736]); ws[66368] = kk * CEFF_(y[1760]); }
+    { const double kk = ws[40096]; ws[66400] = kk * CEFF_(y[4640]); ws[66432] = kk * CEFF_(y[1760]); }
+    { const double kk = ws[40128]; ws[66464] = kk * CEFF_(y[4384]); ws[66496] = kk * CEFF_(y[3744]); }
+    { const double kk = ws[40160]; ws[66528] = kk * CEFF_(y[4608]); ws[66560] = kk * CEFF_(y[3744]); }
+    { const double kk = ws[40224]; ws[66592] = kk * CEFF_(y[4704]); ws[66624] = kk * CEFF_(y[3744]); }
+    { const double kk = ws[40256]; ws[66656] = kk * CEFF_(y[4448]); ws[66688] = kk * CEFF_(y[3744]); }
+    { const double kk = ws[40288]; ws[66720] = kk * CEFF_(y[4672]); ws[66752] = kk * CEFF_(y[3744]); }
+    { const double kk = ws[40320]; ws[66784] = kk * CEFF_(y[4736]); ws[66816] = kk * CEFF_(y[1792]); }
+    { const double kk = ws[40352]; ws[66848] = kk * CEFF_(y[4736]); ws[66880] = kk * CEFF_(y[1952]); }
+    { const double kk = ws[40384]; ws[66912] = kk * CEFF_(y[4736]); ws[66944] = kk * CEFF_(y[416]); }
+    { const double kk = ws[40544]; ws[66976] = kk * CEFF_(y[4736]); ws[67008] = kk * CEFF_(y[4608]); }
+    { const double kk = ws[40640]; ws[67040] = kk * CEFF_(y[4320]); ws[67072] = kk * CEFF_(y[4544]); }
+    { const double kk = ws[40672]; ws[67104] = kk * CEFF_(y[3520]); ws[67136] = kk * CEFF_(y[3520]); }
+    { const double kk = ws[40704]; ws[67168] = kk * CEFF_(y[4384]); ws[67200] = kk * CEFF_(y[3520]); }
+    { const double kk = ws[40736]; ws[67232] = kk * CEFF_(y[4704]); ws[67264] = kk * CEFF_(y[3520]); }
+    { const double kk = ws[40768]; ws[67296] = kk * CEFF_(y[4416]); ws[67328] = kk * CEFF_(y[3520]); }
+    { const double kk = ws[40800]; ws[67360] = kk * CEFF_(y[3232]); ws[67392] = kk * CEFF_(y[4736]); }
+    { const double kk = ws[40896]; ws[67424] = kk * CEFF_(y[4224]); ws[67456] = kk * CEFF_(y[4544]); }
+    { const double kk = ws[40928]; ws[67488] = kk * CEFF_(y[896]); ws[67520] = kk * CEFF_(y[4544]); }
+    { const double kk = ws[40960]; ws[67552] = kk * CEFF_(y[832]); ws[67584] = kk * CEFF_(y[4544]); }
+    { const double kk = ws[40992]; ws[67616] = kk * CEFF_(y[2656]); ws[67648] = kk * CEFF_(y[4544]); }
+    { const double kk = ws[41024]; ws[67680] = kk * CEFF_(y[3552]); ws[67712] = kk * CEFF_(y[4544]); }
+    { const double kk = ws[41056]; ws[67744] = kk * CEFF_(y[3136]); ws[67776] = kk * CEFF_(y[4544]); }
+    { const double kk = ws[41088]; ws[67808] = kk * CEFF_(y[2528]); ws[67840] = kk * CEFF_(y[4544]); }
+    { const double kk = ws[41120]; ws[67872] = kk * CEFF_(y[4512]); ws[67904] = kk * CEFF_(y[4544]); }
+    { const double kk = ws[41152]; ws[67936] = kk * CEFF_(y[4128]); ws[67968] = kk * CEFF_(y[4544]); }
+    { const double kk = ws[41184]; ws[68000] = kk * CEFF_(y[4064]); ws[68032] = kk * CEFF_(y[4544]); }
+    { const double kk = ws[41216]; ws[68064] = kk * CEFF_(y[2720]); ws[68096] = kk * CEFF_(y[4544]); }
+    { const double kk = ws[41248]; ws[68128] = kk * CEFF_(y[864]); ws[68160] = kk * CEFF_(y[4544]); }
+    { const double kk = ws[41280]; ws[68192] = kk * CEFF_(y[4736]); ws[68224] = kk * CEFF_(y[3968]); }
+    { const double kk = ws[41312]; ws[68256] = kk * CEFF_(y[1088]); ws[68288] = kk * CEFF_(y[4544]); }
+    { const double kk = ws[41344]; ws[68320] = kk * CEFF_(y[1120]); ws[68352] = kk * CEFF_(y[4544]); }
+    { const double kk = ws[41376]; ws[68384] = kk * CEFF_(y[1152]); ws[68416] = kk * CEFF_(y[4544]); }
+    { const double kk = ws[41440]; ws[68448] = kk * CEFF_(y[4608]); ws[68480] = kk * CEFF_(y[3520]); }
+    { const double kk = ws[41600]; ws[68512] = kk * CEFF_(y[4384]); ws[68544] = kk * CEFF_(y[2944]); }
+    { const double kk = ws[41632]; ws[68576] = kk * CEFF_(y[4704]); ws[68608] = kk * CEFF_(y[2944]); }
+    { const double kk = ws[41664]; ws[68640] = kk * CEFF_(y[4384]); ws[68672] = kk * CEFF_(y[2496]); }
+    { const double kk = ws[41696]; ws[68704] = kk * CEFF_(y[4704]); ws[68736] = kk * CEFF_(y[2496]); }
+    { const double kk = ws[41728]; ws[68768] = kk * CEFF_(y[4384]); ws[68800] = kk * CEFF_(y[2144]); }
+    { const double kk = ws[41760]; ws[68832] = kk * CEFF_(y[4704]); ws[68864] = kk * CEFF_(y[2144]); }
+    { const double kk = ws[41792]; ws[68896] = kk * CEFF_(y[4320]); ws[68928] = kk * CEFF_(y[1856]); }
+    { const double kk = ws[41824]; ws[68960] = kk * CEFF_(y[4736]); ws[68992] = kk * CEFF_(y[1856]); }
+    { const double kk = ws[41856]; ws[69024] = kk * CEFF_(y[4640]); ws[69056] = kk * CEFF_(y[1856]); }
+    { const double kk = ws[41888]; ws[69088] = kk * CEFF_(y[4384]); ws[69120] = kk * CEFF_(y[2560]); }
+    { const double kk = ws[41920]; ws[69152] = kk * CEFF_(y[4704]); ws[69184] = kk * CEFF_(y[2560]); }
+    { const double kk = ws[41952]; ws[69216] = kk * CEFF_(y[4736]); ws[69248] = kk * CEFF_(y[448]); }
+    { const double kk = ws[42144]; ws[69280] = kk * CEFF_(y[480]); ws[69312] = kk * CEFF_(y[1920]); }
+    { const double kk = ws[42176]; ws[69344] = kk * CEFF_(y[512]); ws[69376] = kk * CEFF_(y[1920]); }
+    { const double kk = ws[42208]; ws[69408] = kk * CEFF_(y[544]); ws[69440] = kk * CEFF_(y[1248]); }
+    { const double kk = ws[42336]; ws[69472] = kk * CEFF_(y[576]); ws[69504] = kk * CEFF_(y[1312]); }
+    { const double kk = ws[42464]; ws[69536] = kk * CEFF_(y[4384]); ws[69568] = kk * CEFF_(y[2848]); }
+    { const double kk = ws[42496]; ws[69600] = kk * CEFF_(y[4704]); ws[69632] = kk * CEFF_(y[2848]); }
+    { const double kk = ws[42528]; ws[69664] = kk * CEFF_(y[4640]); ws[69696] = kk * CEFF_(y[2848]); }
+    { const double kk = ws[42560]; ws[69728] = kk * CEFF_(y[4672]); ws[69760] = kk * CEFF_(y[2848]); }
+    { const double kk = ws[42592]; ws[69792] = kk * CEFF_(y[4544]); ws[69824] = kk * CEFF_(y[3360]); }
+    { const double kk = ws[42624]; ws[69856] = kk * CEFF_(y[4736]); ws[69888] = kk * CEFF_(y[3360]); }
+    { const double kk = ws[42912]; ws[69920] = kk * CEFF_(y[4736]); ws[69952] = kk * CEFF_(y[704]); }
+    { const double kk = ws[42944]; ws[69984] = kk * CEFF_(y[4736]); ws[70016] = kk * CEFF_(y[1440]); }
+    { const double kk = ws[42976]; ws[70048] = kk * CEFF_(y[4736]); ws[70080] = kk * CEFF_(y[736]); }
+    { const double kk = ws[43008]; ws[70112] = kk * CEFF_(y[4736]); ws[70144] = kk * CEFF_(y[1472]); }
+    { const double kk = ws[43040]; ws[70176] = kk * CEFF_(y[4736]); ws[70208] = kk * CEFF_(y[768]); }
+    { const double kk = ws[43072]; ws[70240] = kk * CEFF_(y[4736]); ws[70272] = kk * CEFF_(y[2752]); }
+    { const double kk = ws[43104]; ws[70304] = kk * CEFF_(y[4736]); ws[70336] = kk * CEFF_(y[2784]); }
+    { const double kk = ws[43136]; ws[70368] = kk * CEFF_(y[4736]); ws[70400] = kk * CEFF_(y[2816]); }
+    { const double kk = ws[43168]; ws[70432] = kk * CEFF_(y[4736]); ws[70464] = kk * CEFF_(y[2304]); }
+    { const double kk = ws[43200]; ws[70496] = kk * CEFF_(y[4736]); ws[70528] = kk * CEFF_(y[1504]); }
+    { const double kk = ws[43232]; ws[70560] = kk * CEFF_(y[4736]); ws[70592] = kk * CEFF_(y[3680]); }
+    { const double kk = ws[43264]; ws[70624] = kk * CEFF_(y[4736]); ws[70656] = kk * CEFF_(y[3712]); }
+    { const double kk = ws[43296]; ws[70688] = kk * CEFF_(y[4736]); ws[70720] = kk * CEFF_(y[2912]); }
+    { const double kk = ws[43328]; ws[70752] = kk * CEFF_(y[4736]); ws[70784] = kk * CEFF_(y[3168]); }
+    { const double kk = ws[43360]; ws[70816] = kk * CEFF_(y[4736]); ws[70848] = kk * CEFF_(y[3200]); }
+    { const double kk = ws[43392]; ws[70880] = kk * CEFF_(y[4736]); ws[70912] = kk * CEFF_(y[2336]); }
+    { const double kk = ws[43424]; ws[70944] = kk * CEFF_(y[4640]); ws[70976] = kk * CEFF_(y[2336]); }
+    { const double kk = ws[43456]; ws[71008] = kk * CEFF_(y[4160]); ws[71040] = kk * CEFF_(y[2336]); }
+    { const double kk = ws[43552]; ws[71072] = kk * CEFF_(y[4544]); ws[71104] = kk * CEFF_(y[2336]); }
+    { const double kk = ws[43584]; ws[71136] = kk * CEFF_(y[4736]); ws[71168] = kk * CEFF_(y[2368]); }
+    { const double kk = ws[43616]; ws[71200] = kk * CEFF_(y[4640]); ws[71232] = kk * CEFF_(y[2368]); }
+    { const double kk = ws[43648]; ws[71264] = kk * CEFF_(y[4160]); ws[71296] = kk * CEFF_(y[2368]); }
+    { const double kk = ws[43712]; ws[71328] = kk * CEFF_(y[4544]); ws[71360] = kk * CEFF_(y[2368]); }
+    { const double kk = ws[43744]; ws[71392] = kk * CEFF_(y[4736]); ws[71424] = kk * CEFF_(y[2400]); }
+    { const double kk = ws[43776]; ws[71456] = kk * CEFF_(y[4320]); ws[71488] = kk * CEFF_(y[2400]); }
+    { const double kk = ws[43808]; ws[71520] = kk * CEFF_(y[4640]); ws[71552] = kk * CEFF_(y[2400]); }
+    { const double kk = ws[43840]; ws[71584] = kk * CEFF_(y[4544]); ws[71616] = kk * CEFF_(y[2400]); }
+    { const double kk = ws[43872]; ws[71648] = kk * CEFF_(y[4736]); ws[71680] = kk * CEFF_(y[2432]); }
+    { const double kk = ws[43904]; ws[71712] = kk * CEFF_(y[4320]); ws[71744] = kk * CEFF_(y[2432]); }
+    { const double kk = ws[43936]; ws[71776] = kk * CEFF_(y[4640]); ws[71808] = kk * CEFF_(y[2432]); }
+    { const double kk = ws[44000]; ws[71840] = kk * CEFF_(y[4544]); ws[71872] = kk * CEFF_(y[2432]); }
+    { const double kk = ws[44032]; ws[71904] = kk * CEFF_(y[4736]); ws[71936] = kk * CEFF_(y[2976]); }
+    { const double kk = ws[44064]; ws[71968] = kk * CEFF_(y[4320]); ws[72000] = kk * CEFF_(y[2976]); }
+    { const double kk = ws[44096]; ws[72032] = kk * CEFF_(y[4640]); ws[72064] = kk * CEFF_(y[2976]); }
+    { const double kk = ws[44160]; ws[72096] = kk * CEFF_(y[4544]); ws[72128] = kk * CEFF_(y[2976]); }
+    { const double kk = ws[44192]; ws[72160] = kk * CEFF_(y[4736]); ws[72192] = kk * CEFF_(y[1536]); }
+    { const double kk = ws[44224]; ws[72224] = kk * CEFF_(y[4544]); ws[72256] = kk * CEFF_(y[1536]); }
+    { const double kk = ws[44256]; ws[72288] = kk * CEFF_(y[4320]); ws[72320] = kk * CEFF_(y[3008]); }
+    { const double kk = ws[44288]; ws[72352] = kk * CEFF_(y[1184]); ws[72384] = kk * CEFF_(y[3008]); }
+    { const double kk = ws[44320]; ws[72416] = kk * CEFF_(y[3456]); ws[72448] = kk * CEFF_(y[3008]); }
+    { const double kk = ws[44352]; ws[72480] = kk * CEFF_(y[4736]); ws[72512] = kk * CEFF_(y[3008]); }
+    { const double kk = ws[44384]; ws[72544] = kk * CEFF_(y[4544]); ws[72576] = kk * CEFF_(y[3008]); }
+    { const double kk = ws[44416]; ws[72608] = kk * CEFF_(y[4736]); ws[72640] = kk * CEFF_(y[2016]); }
+    { const double kk = ws[44448]; ws[72672] = kk * CEFF_(y[4736]); ws[72704] = kk * CEFF_(y[2016]); }
+    { const double kk = ws[44480]; ws[72736] = kk * CEFF_(y[4640]); ws[72768] = kk * CEFF_(y[2016]); }
+    { const double kk = ws[44512]; ws[72800] = kk * CEFF_(y[4544]); ws[72832] = kk * CEFF_(y[2016]); }
+#undef CEFF_
+}
 }  // namespace mech_cb6r5_ae7_aq

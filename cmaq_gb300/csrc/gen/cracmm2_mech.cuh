@@ -57,6 +57,14 @@ constexpr int ADJ_EMIS = 8092;
 constexpr int ADJ_GE = 8281;
 constexpr int ADJ_GK = 8470;
 constexpr int OFF_YAVE = 3295;
+constexpr int GEAR_WS_ELEMS = 8092;
+constexpr int GEAR_CNEW = 0;
+constexpr int GEAR_GLOSS = 378;
+constexpr int GEAR_DTLOS = 756;
+constexpr int GEAR_CHOLD = 945;
+constexpr int GEAR_CEST = 1134;
+constexpr int GEAR_BLKCONC = 567;
+constexpr int GEAR_CONC = 6958;
 constexpr int EBIW_YC = 0;
 constexpr int EBIW_YC0 = 189;
 constexpr int EBIW_YCP = 378;
@@ -81,6 +89,120 @@ __device__ void feval_0(double* __restrict__ ws, int src, int dst);
 __device__ void explic_0(double* __restrict__ ws);
 __device__ void feval_1(double* __restrict__ ws, int src, int dst);
 __device__ void explic_1(double* __restrict__ ws);
+__device__ void gear_explic_0(double* __restrict__ ws);
+__device__ void feval_s1_0(double* __restrict__ ws, int src, int dst);
+__device__ void gear_explic_s1_0(double* __restrict__ ws);
+__device__ void gear_pdecomp_0_0(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_0(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_1(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_1(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_2(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_2(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_3(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_3(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_4(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_4(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_5(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_5(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_6(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_6(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_7(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_7(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_8(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_8(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_9(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_9(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_10(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_10(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_11(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_11(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_12(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_12(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_13(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_13(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_14(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_14(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_15(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_15(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_16(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_16(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_17(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_17(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_18(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_18(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_19(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_19(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_20(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_20(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_21(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_21(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_22(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_22(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_23(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_23(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_24(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_24(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_25(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_25(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_26(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_26(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_27(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_27(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_28(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_28(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_29(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_29(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_30(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_30(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_31(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_31(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_32(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_32(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_33(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_33(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_34(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_34(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_35(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_35(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_36(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_36(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_37(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_37(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_38(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_38(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_39(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_39(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_40(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_40(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_41(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_41(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_42(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_42(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_43(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_43(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_44(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_44(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_45(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_45(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_46(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_46(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_47(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_47(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_48(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_48(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_49(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_49(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_50(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_50(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_51(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_51(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_0_52(double* __restrict__ ws, double r1delt);
+__device__ void gear_pdecomp_s1_0_52(double* __restrict__ ws, double r1delt);
+__device__ void solve_s1_0_0(double* __restrict__ ws, int rhs);
+__device__ void solve_s1_0_1(double* __restrict__ ws, int rhs);
+__device__ void solve_s1_0_2(double* __restrict__ ws, int rhs);
+__device__ void solve_s1_0_3(double* __restrict__ ws, int rhs);
+__device__ void solve_s1_0_4(double* __restrict__ ws, int rhs);
 __device__ void jacdecomp_0_0(double* __restrict__ ws, double gdtinv);
 __device__ void jacdecomp_0_1(double* __restrict__ ws, double gdtinv);
 __device__ void jacdecomp_0_2(double* __restrict__ ws, double gdtinv);
@@ -368,6 +490,126 @@ __device__ void ebi_hrg2(double* __restrict__ sm, double dtc);
 __device__ void ebi_hrg3(double* __restrict__ sm, double dtc);
 __device__ void ebi_hrg4(double* __restrict__ sm, double dtc);
 }  // namespace wsm
+__device__ __forceinline__ void gear_pdecomp_0(double* __restrict__ ws, double r1delt)
+{
+    gear_pdecomp_0_0(ws, r1delt);
+    gear_pdecomp_0_1(ws, r1delt);
+    gear_pdecomp_0_2(ws, r1delt);
+    gear_pdecomp_0_3(ws, r1delt);
+    gear_pdecomp_0_4(ws, r1delt);
+    gear_pdecomp_0_5(ws, r1delt);
+    gear_pdecomp_0_6(ws, r1delt);
+    gear_pdecomp_0_7(ws, r1delt);
+    gear_pdecomp_0_8(ws, r1delt);
+    gear_pdecomp_0_9(ws, r1delt);
+    gear_pdecomp_0_10(ws, r1delt);
+    gear_pdecomp_0_11(ws, r1delt);
+    gear_pdecomp_0_12(ws, r1delt);
+    gear_pdecomp_0_13(ws, r1delt);
+    gear_pdecomp_0_14(ws, r1delt);
+    gear_pdecomp_0_15(ws, r1delt);
+    gear_pdecomp_0_16(ws, r1delt);
+    gear_pdecomp_0_17(ws, r1delt);
+    gear_pdecomp_0_18(ws, r1delt);
+    gear_pdecomp_0_19(ws, r1delt);
+    gear_pdecomp_0_20(ws, r1delt);
+    gear_pdecomp_0_21(ws, r1delt);
+    gear_pdecomp_0_22(ws, r1delt);
+    gear_pdecomp_0_23(ws, r1delt);
+    gear_pdecomp_0_24(ws, r1delt);
+    gear_pdecomp_0_25(ws, r1delt);
+    gear_pdecomp_0_26(ws, r1delt);
+    gear_pdecomp_0_27(ws, r1delt);
+    gear_pdecomp_0_28(ws, r1delt);
+    gear_pdecomp_0_29(ws, r1delt);
+    gear_pdecomp_0_30(ws, r1delt);
+    gear_pdecomp_0_31(ws, r1delt);
+    gear_pdecomp_0_32(ws, r1delt);
+    gear_pdecomp_0_33(ws, r1delt);
+    gear_pdecomp_0_34(ws, r1delt);
+    gear_pdecomp_0_35(ws, r1delt);
+    gear_pdecomp_0_36(ws, r1delt);
+    gear_pdecomp_0_37(ws, r1delt);
+    gear_pdecomp_0_38(ws, r1delt);
+    gear_pdecomp_0_39(ws, r1delt);
+    gear_pdecomp_0_40(ws, r1delt);
+    gear_pdecomp_0_41(ws, r1delt);
+    gear_pdecomp_0_42(ws, r1delt);
+    gear_pdecomp_0_43(ws, r1delt);
+    gear_pdecomp_0_44(ws, r1delt);
+    gear_pdecomp_0_45(ws, r1delt);
+    gear_pdecomp_0_46(ws, r1delt);
+    gear_pdecomp_0_47(ws, r1delt);
+    gear_pdecomp_0_48(ws, r1delt);
+    gear_pdecomp_0_49(ws, r1delt);
+    gear_pdecomp_0_50(ws, r1delt);
+    gear_pdecomp_0_51(ws, r1delt);
+    gear_pdecomp_0_52(ws, r1delt);
+}
+__device__ __forceinline__ void gear_pdecomp_s1_0(double* __restrict__ ws, double r1delt)
+{
+    gear_pdecomp_s1_0_0(ws, r1delt);
+    gear_pdecomp_s1_0_1(ws, r1delt);
+    gear_pdecomp_s1_0_2(ws, r1delt);
+    gear_pdecomp_s1_0_3(ws, r1delt);
+    gear_pdecomp_s1_0_4(ws, r1delt);
+    gear_pdecomp_s1_0_5(ws, r1delt);
+    gear_pdecomp_s1_0_6(ws, r1delt);
+    gear_pdecomp_s1_0_7(ws, r1delt);
+    gear_pdecomp_s1_0_8(ws, r1delt);
+    gear_pdecomp_s1_0_9(ws, r1delt);
+    gear_pdecomp_s1_0_10(ws, r1delt);
+    gear_pdecomp_s1_0_11(ws, r1delt);
+    gear_pdecomp_s1_0_12(ws, r1delt);
+    gear_pdecomp_s1_0_13(ws, r1delt);
+    gear_pdecomp_s1_0_14(ws, r1delt);
+    gear_pdecomp_s1_0_15(ws, r1delt);
+    gear_pdecomp_s1_0_16(ws, r1delt);
+    gear_pdecomp_s1_0_17(ws, r1delt);
+    gear_pdecomp_s1_0_18(ws, r1delt);
+    gear_pdecomp_s1_0_19(ws, r1delt);
+    gear_pdecomp_s1_0_20(ws, r1delt);
+    gear_pdecomp_s1_0_21(ws, r1delt);
+    gear_pdecomp_s1_0_22(ws, r1delt);
+    gear_pdecomp_s1_0_23(ws, r1delt);
+    gear_pdecomp_s1_0_24(ws, r1delt);
+    gear_pdecomp_s1_0_25(ws, r1delt);
+    gear_pdecomp_s1_0_26(ws, r1delt);
+    gear_pdecomp_s1_0_27(ws, r1delt);
+    gear_pdecomp_s1_0_28(ws, r1delt);
+    gear_pdecomp_s1_0_29(ws, r1delt);
+    gear_pdecomp_s1_0_30(ws, r1delt);
+    gear_pdecomp_s1_0_31(ws, r1delt);
+    gear_pdecomp_s1_0_32(ws, r1delt);
+    gear_pdecomp_s1_0_33(ws, r1delt);
+    gear_pdecomp_s1_0_34(ws, r1delt);
+    gear_pdecomp_s1_0_35(ws, r1delt);
+    gear_pdecomp_s1_0_36(ws, r1delt);
+    gear_pdecomp_s1_0_37(ws, r1delt);
+    gear_pdecomp_s1_0_38(ws, r1delt);
+    gear_pdecomp_s1_0_39(ws, r1delt);
+    gear_pdecomp_s1_0_40(ws, r1delt);
+    gear_pdecomp_s1_0_41(ws, r1delt);
+    gear_pdecomp_s1_0_42(ws, r1delt);
+    gear_pdecomp_s1_0_43(ws, r1delt);
+    gear_pdecomp_s1_0_44(ws, r1delt);
+    gear_pdecomp_s1_0_45(ws, r1delt);
+    gear_pdecomp_s1_0_46(ws, r1delt);
+    gear_pdecomp_s1_0_47(ws, r1delt);
+    gear_pdecomp_s1_0_48(ws, r1delt);
+    gear_pdecomp_s1_0_49(ws, r1delt);
+    gear_pdecomp_s1_0_50(ws, r1delt);
+    gear_pdecomp_s1_0_51(ws, r1delt);
+    gear_pdecomp_s1_0_52(ws, r1delt);
+}
+__device__ __forceinline__ void solve_s1_0(double* __restrict__ ws, int rhs)
+{
+    solve_s1_0_0(ws, rhs);
+    solve_s1_0_1(ws, rhs);
+    solve_s1_0_2(ws, rhs);
+    solve_s1_0_3(ws, rhs);
+    solve_s1_0_4(ws, rhs);
+}
 __device__ __forceinline__ void jacdecomp_0(double* __restrict__ ws, double gdtinv)
 {
     jacdecomp_0_0(ws, gdtinv);
@@ -947,6 +1189,14 @@ struct Traits {
     static constexpr int ADJ_GE = mech_cracmm2::ADJ_GE;
     static constexpr int ADJ_GK = mech_cracmm2::ADJ_GK;
     static constexpr int OFF_YAVE = mech_cracmm2::OFF_YAVE;
+    static constexpr int GEAR_WS_ELEMS = mech_cracmm2::GEAR_WS_ELEMS;
+    static constexpr int GEAR_CNEW = mech_cracmm2::GEAR_CNEW;
+    static constexpr int GEAR_GLOSS = mech_cracmm2::GEAR_GLOSS;
+    static constexpr int GEAR_DTLOS = mech_cracmm2::GEAR_DTLOS;
+    static constexpr int GEAR_CHOLD = mech_cracmm2::GEAR_CHOLD;
+    static constexpr int GEAR_CEST = mech_cracmm2::GEAR_CEST;
+    static constexpr int GEAR_BLKCONC = mech_cracmm2::GEAR_BLKCONC;
+    static constexpr int GEAR_CONC = mech_cracmm2::GEAR_CONC;
     static constexpr int EBIW_YC = mech_cracmm2::EBIW_YC;
     static constexpr int EBIW_YC0 = mech_cracmm2::EBIW_YC0;
     static constexpr int EBIW_YCP = mech_cracmm2::EBIW_YCP;
@@ -962,6 +1212,12 @@ struct Traits {
     static __device__ __forceinline__ int inew2old(int i) { return mech_cracmm2::c_inew2old[i]; }
     static __device__ __forceinline__ void feval_0(double* ws, int s, int t) { mech_cracmm2::feval_0(ws, s, t); }
     static __device__ __forceinline__ void explic_0(double* ws) { mech_cracmm2::explic_0(ws); }
+    static __device__ __forceinline__ void gear_explic_0(double* ws) { mech_cracmm2::gear_explic_0(ws); }
+    static __device__ __forceinline__ void gear_pdecomp_0(double* ws, double r) { mech_cracmm2::gear_pdecomp_0(ws, r); }
+    static __device__ __forceinline__ void feval_s1_0(double* ws, int s, int t) { mech_cracmm2::feval_s1_0(ws, s, t); }
+    static __device__ __forceinline__ void gear_explic_s1_0(double* ws) { mech_cracmm2::gear_explic_s1_0(ws); }
+    static __device__ __forceinline__ void gear_pdecomp_s1_0(double* ws, double r) { mech_cracmm2::gear_pdecomp_s1_0(ws, r); }
+    static __device__ __forceinline__ void solve_s1_0(double* ws, int r) { mech_cracmm2::solve_s1_0(ws, r); }
     static __device__ __forceinline__ void jacdecomp_0(double* ws, double g) { mech_cracmm2::jacdecomp_0(ws, g); }
     static __device__ __forceinline__ void solve_0(double* ws, int r) { mech_cracmm2::solve_0(ws, r); }
     static __device__ __forceinline__ void jacdecomp_0_sync(double* ws, double g, bool go) { mech_cracmm2::jacdecomp_0_sync(ws, g, go); }

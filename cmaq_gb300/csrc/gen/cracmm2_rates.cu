@@ -10558,4 +10558,466 @@ __device__ __noinline__ void explic_1(double* __restrict__ ws)
     { const double kk = ws[59264]; ws[105312] = kk * y[5888]; ws[105344] = kk * y[3488]; }
     { const double kk = ws[59296]; ws[105376] = kk * y[5792]; ws[105408] = kk * y[3488]; }
 }
+// Partial-derivative products of 2- and 3-reactant reactions (grpderiv.F:163-189).
+__device__ __noinline__ void gear_explic_0(double* __restrict__ ws)
+{
+    const double* __restrict__ y = ws + 0;
+#define CEFF_(v) ((v) <= 1.0e-30 ? 0.0 : (v))
+    { const double kk = ws[43616]; ws[76320] = kk * CEFF_(y[6016]); ws[76352] = kk * CEFF_(y[5184]); }
+    { const double kk = ws[43648]; ws[76384] = kk * CEFF_(y[5984]); ws[76416] = kk * CEFF_(y[5184]); }
+    { const double kk = ws[43680]; ws[76448] = kk * CEFF_(y[5824]); ws[76480] = kk * CEFF_(y[5184]); }
+    { const double kk = ws[43712]; ws[76512] = kk * CEFF_(y[5920]); ws[76544] = kk * CEFF_(y[5184]); }
+    { const double kk = ws[43776]; ws[76576] = kk * CEFF_(y[5184]); ws[76608] = kk * CEFF_(y[2336]); }
+    { const double kk = ws[43936]; ws[76640] = kk * CEFF_(y[5984]); ws[76672] = kk * CEFF_(y[6016]); }
+    { const double kk = ws[43968]; ws[76704] = kk * CEFF_(y[5984]); ws[76736] = kk * CEFF_(y[5984]); }
+    { const double kk = ws[44000]; ws[76768] = kk * CEFF_(y[5984]); ws[76800] = kk * CEFF_(y[5984]); }
+    { const double kk = ws[44032]; ws[76832] = kk * CEFF_(y[6016]); ws[76864] = kk * CEFF_(y[4000]); }
+    { const double kk = ws[44064]; ws[76896] = kk * CEFF_(y[2336]); ws[76928] = kk * CEFF_(y[5824]); }
+    { const double kk = ws[44096]; ws[76960] = kk * CEFF_(y[6016]); ws[76992] = kk * CEFF_(y[5824]); }
+    { const double kk = ws[44128]; ws[77024] = kk * CEFF_(y[5984]); ws[77056] = kk * CEFF_(y[5824]); }
+    { const double kk = ws[44160]; ws[77088] = kk * CEFF_(y[5984]); ws[77120] = kk * CEFF_(y[5824]); }
+    { const double kk = ws[44192]; ws[77152] = kk * CEFF_(y[5824]); ws[77184] = kk * CEFF_(y[5824]); }
+    { const double kk = ws[44224]; ws[77216] = kk * CEFF_(y[6016]); ws[77248] = kk * CEFF_(y[1184]); }
+    { const double kk = ws[44256]; ws[77280] = kk * CEFF_(y[2336]); ws[77312] = kk * CEFF_(y[5920]); }
+    { const double kk = ws[44288]; ws[77344] = kk * CEFF_(y[2336]); ws[77376] = kk * CEFF_(y[5920]); }
+    { const double kk = ws[44320]; ws[77408] = kk * CEFF_(y[6016]); ws[77440] = kk * CEFF_(y[5920]); }
+    { const double kk = ws[44352]; ws[77472] = kk * CEFF_(y[6016]); ws[77504] = kk * CEFF_(y[5024]); }
+    { const double kk = ws[44384]; ws[77536] = kk * CEFF_(y[6016]); ws[77568] = kk * CEFF_(y[5952]); }
+    { const double kk = ws[44416]; ws[77600] = kk * CEFF_(y[5984]); ws[77632] = kk * CEFF_(y[5952]); }
+    { const double kk = ws[44448]; ws[77664] = kk * CEFF_(y[5824]); ws[77696] = kk * CEFF_(y[5952]); }
+    { const double kk = ws[44480]; ws[77728] = kk * CEFF_(y[5920]); ws[77760] = kk * CEFF_(y[5952]); }
+    { const double kk = ws[44512]; ws[77792] = kk * CEFF_(y[5952]); ws[77824] = kk * CEFF_(y[5952]); }
+    { const double kk = ws[44544]; ws[77856] = kk * CEFF_(y[5920]); ws[77888] = kk * CEFF_(y[5952]); }
+    { const double kk = ws[44640]; ws[77920] = kk * CEFF_(y[5984]); ws[77952] = kk * CEFF_(y[5920]); }
+    { const double kk = ws[44704]; ws[77984] = kk * CEFF_(y[6016]); ws[78016] = kk * CEFF_(y[1280]); }
+    { const double kk = ws[44736]; ws[78048] = kk * CEFF_(y[6016]); ws[78080] = kk * CEFF_(y[160]); }
+    { const double kk = ws[44768]; ws[78112] = kk * CEFF_(y[6016]); ws[78144] = kk * CEFF_(y[5664]); }
+    { const double kk = ws[44832]; ws[78176] = kk * CEFF_(y[6016]); ws[78208] = kk * CEFF_(y[1888]); }
+    { const double kk = ws[44864]; ws[78240] = kk * CEFF_(y[6016]); ws[78272] = kk * CEFF_(y[2176]); }
+    { const double kk = ws[44896]; ws[78304] = kk * CEFF_(y[6016]); ws[78336] = kk * CEFF_(y[1120]); }
+    { const double kk = ws[44928]; ws[78368] = kk * CEFF_(y[6016]); ws[78400] = kk * CEFF_(y[2240]); }
+    { const double kk = ws[44960]; ws[78432] = kk * CEFF_(y[6016]); ws[78464] = kk * CEFF_(y[2752]); }
+    { const double kk = ws[44992]; ws[78496] = kk * CEFF_(y[6016]); ws[78528] = kk * CEFF_(y[1152]); }
+    { const double kk = ws[45024]; ws[78560] = kk * CEFF_(y[6016]); ws[78592] = kk * CEFF_(y[256]); }
+    { const double kk = ws[45056]; ws[78624] = kk * CEFF_(y[6016]); ws[78656] = kk * CEFF_(y[1216]); }
+    { const double kk = ws[45088]; ws[78688] = kk * CEFF_(y[6016]); ws[78720] = kk * CEFF_(y[288]); }
+    { const double kk = ws[45120]; ws[78752] = kk * CEFF_(y[6016]); ws[78784] = kk * CEFF_(y[320]); }
+    { const double kk = ws[45152]; ws[78816] = kk * CEFF_(y[6016]); ws[78848] = kk * CEFF_(y[352]); }
+    { const double kk = ws[45184]; ws[78880] = kk * CEFF_(y[5184]); ws[78912] = kk * CEFF_(y[1312]); }
+    { const double kk = ws[45216]; ws[78944] = kk * CEFF_(y[5952]); ws[78976] = kk * CEFF_(y[1312]); }
+    { const double kk = ws[45248]; ws[79008] = kk * CEFF_(y[6016]); ws[79040] = kk * CEFF_(y[1312]); }
+    { const double kk = ws[45280]; ws[79072] = kk * CEFF_(y[5984]); ws[79104] = kk * CEFF_(y[4288]); }
+    { const double kk = ws[45312]; ws[79136] = kk * CEFF_(y[5824]); ws[79168] = kk * CEFF_(y[4288]); }
+    { const double kk = ws[45344]; ws[79200] = kk * CEFF_(y[6016]); ws[79232] = kk * CEFF_(y[1344]); }
+    { const double kk = ws[45376]; ws[79264] = kk * CEFF_(y[6016]); ws[79296] = kk * CEFF_(y[1344]); }
+    { const double kk = ws[45408]; ws[79328] = kk * CEFF_(y[5984]); ws[79360] = kk * CEFF_(y[1632]); }
+    { const double kk = ws[45440]; ws[79392] = kk * CEFF_(y[5824]); ws[79424] = kk * CEFF_(y[1632]); }
+    { const double kk = ws[45472]; ws[79456] = kk * CEFF_(y[6016]); ws[79488] = kk * CEFF_(y[2784]); }
+    { const double kk = ws[45504]; ws[79520] = kk * CEFF_(y[2208]); ws[79552] = kk * CEFF_(y[6016]); }
+    { const double kk = ws[45568]; ws[79584] = kk * CEFF_(y[6016]); ws[79616] = kk * CEFF_(y[1664]); }
+    { const double kk = ws[45600]; ws[79648] = kk * CEFF_(y[6016]); ws[79680] = kk * CEFF_(y[1408]); }
+    { const double kk = ws[45632]; ws[79712] = kk * CEFF_(y[6016]); ws[79744] = kk * CEFF_(y[1440]); }
+    { const double kk = ws[45664]; ws[79776] = kk * CEFF_(y[6016]); ws[79808] = kk * CEFF_(y[4544]); }
+    { const double kk = ws[45696]; ws[79840] = kk * CEFF_(y[6016]); ws[79872] = kk * CEFF_(y[4576]); }
+    { const double kk = ws[45728]; ws[79904] = kk * CEFF_(y[6016]); ws[79936] = kk * CEFF_(y[5856]); }
+    { const double kk = ws[45760]; ws[79968] = kk * CEFF_(y[6016]); ws[80000] = kk * CEFF_(y[5568]); }
+    { const double kk = ws[45792]; ws[80032] = kk * CEFF_(y[6016]); ws[80064] = kk * CEFF_(y[5760]); }
+    { const double kk = ws[45824]; ws[80096] = kk * CEFF_(y[6016]); ws[80128] = kk * CEFF_(y[4480]); }
+    { const double kk = ws[45856]; ws[80160] = kk * CEFF_(y[6016]); ws[80192] = kk * CEFF_(y[5280]); }
+    { const double kk = ws[45888]; ws[80224] = kk * CEFF_(y[6016]); ws[80256] = kk * CEFF_(y[5504]); }
+    { const double kk = ws[45920]; ws[80288] = kk * CEFF_(y[6016]); ws[80320] = kk * CEFF_(y[5344]); }
+    { const double kk = ws[45952]; ws[80352] = kk * CEFF_(y[6016]); ws[80384] = kk * CEFF_(y[4128]); }
+    { const double kk = ws[45984]; ws[80416] = kk * CEFF_(y[6016]); ws[80448] = kk * CEFF_(y[4736]); }
+    { const double kk = ws[46016]; ws[80480] = kk * CEFF_(y[6016]); ws[80512] = kk * CEFF_(y[3872]); }
+    { const double kk = ws[46048]; ws[80544] = kk * CEFF_(y[6016]); ws[80576] = kk * CEFF_(y[5376]); }
+    { const double kk = ws[46080]; ws[80608] = kk * CEFF_(y[6016]); ws[80640] = kk * CEFF_(y[5248]); }
+    { const double kk = ws[46112]; ws[80672] = kk * CEFF_(y[6016]); ws[80704] = kk * CEFF_(y[5472]); }
+    { const double kk = ws[46144]; ws[80736] = kk * CEFF_(y[6016]); ws[80768] = kk * CEFF_(y[4320]); }
+    { const double kk = ws[46176]; ws[80800] = kk * CEFF_(y[6016]); ws[80832] = kk * CEFF_(y[3584]); }
+    { const double kk = ws[46208]; ws[80864] = kk * CEFF_(y[6016]); ws[80896] = kk * CEFF_(y[4448]); }
+    { const double kk = ws[46240]; ws[80928] = kk * CEFF_(y[6016]); ws[80960] = kk * CEFF_(y[1248]); }
+    { const double kk = ws[46272]; ws[80992] = kk * CEFF_(y[6016]); ws[81024] = kk * CEFF_(y[2944]); }
+    { const double kk = ws[46304]; ws[81056] = kk * CEFF_(y[6016]); ws[81088] = kk * CEFF_(y[1760]); }
+    { const double kk = ws[46336]; ws[81120] = kk * CEFF_(y[6016]); ws[81152] = kk * CEFF_(y[5600]); }
+    { const double kk = ws[46368]; ws[81184] = kk * CEFF_(y[6016]); ws[81216] = kk * CEFF_(y[1472]); }
+    { const double kk = ws[46400]; ws[81248] = kk * CEFF_(y[6016]); ws[81280] = kk * CEFF_(y[5056]); }
+    { const double kk = ws[46432]; ws[81312] = kk * CEFF_(y[6016]); ws[81344] = kk * CEFF_(y[1504]); }
+    { const double kk = ws[46464]; ws[81376] = kk * CEFF_(y[6016]); ws[81408] = kk * CEFF_(y[2816]); }
+    { const double kk = ws[46496]; ws[81440] = kk * CEFF_(y[6016]); ws[81472] = kk * CEFF_(y[5728]); }
+    { const double kk = ws[46528]; ws[81504] = kk * CEFF_(y[6016]); ws[81536] = kk * CEFF_(y[4096]); }
+    { const double kk = ws[46560]; ws[81568] = kk * CEFF_(y[6016]); ws[81600] = kk * CEFF_(y[4608]); }
+    { const double kk = ws[46592]; ws[81632] = kk * CEFF_(y[6016]); ws[81664] = kk * CEFF_(y[1792]); }
+    { const double kk = ws[46624]; ws[81696] = kk * CEFF_(y[6016]); ws[81728] = kk * CEFF_(y[4352]); }
+    { const double kk = ws[46656]; ws[81760] = kk * CEFF_(y[6016]); ws[81792] = kk * CEFF_(y[5696]); }
+    { const double kk = ws[46688]; ws[81824] = kk * CEFF_(y[6016]); ws[81856] = kk * CEFF_(y[3680]); }
+    { const double kk = ws[46720]; ws[81888] = kk * CEFF_(y[6016]); ws[81920] = kk * CEFF_(y[1088]); }
+    { const double kk = ws[46752]; ws[81952] = kk * CEFF_(y[6016]); ws[81984] = kk * CEFF_(y[1536]); }
+    { const double kk = ws[46784]; ws[82016] = kk * CEFF_(y[6016]); ws[82048] = kk * CEFF_(y[1824]); }
+    { const double kk = ws[46816]; ws[82080] = kk * CEFF_(y[6016]); ws[82112] = kk * CEFF_(y[5440]); }
+    { const double kk = ws[46848]; ws[82144] = kk * CEFF_(y[6016]); ws[82176] = kk * CEFF_(y[4384]); }
+    { const double kk = ws[46880]; ws[82208] = kk * CEFF_(y[6016]); ws[82240] = kk * CEFF_(y[1696]); }
+    { const double kk = ws[46912]; ws[82272] = kk * CEFF_(y[5184]); ws[82304] = kk * CEFF_(y[2240]); }
+    { const double kk = ws[46944]; ws[82336] = kk * CEFF_(y[5184]); ws[82368] = kk * CEFF_(y[2752]); }
+    { const double kk = ws[46976]; ws[82400] = kk * CEFF_(y[5184]); ws[82432] = kk * CEFF_(y[1152]); }
+    { const double kk = ws[47008]; ws[82464] = kk * CEFF_(y[5184]); ws[82496] = kk * CEFF_(y[1408]); }
+    { const double kk = ws[47040]; ws[82528] = kk * CEFF_(y[5184]); ws[82560] = kk * CEFF_(y[1440]); }
+    { const double kk = ws[47072]; ws[82592] = kk * CEFF_(y[5184]); ws[82624] = kk * CEFF_(y[4576]); }
+    { const double kk = ws[47104]; ws[82656] = kk * CEFF_(y[5184]); ws[82688] = kk * CEFF_(y[4384]); }
+    { const double kk = ws[47136]; ws[82720] = kk * CEFF_(y[5184]); ws[82752] = kk * CEFF_(y[4128]); }
+    { const double kk = ws[47168]; ws[82784] = kk * CEFF_(y[5184]); ws[82816] = kk * CEFF_(y[4736]); }
+    { const double kk = ws[47200]; ws[82848] = kk * CEFF_(y[5184]); ws[82880] = kk * CEFF_(y[3872]); }
+    { const double kk = ws[47232]; ws[82912] = kk * CEFF_(y[5184]); ws[82944] = kk * CEFF_(y[5472]); }
+    { const double kk = ws[47264]; ws[82976] = kk * CEFF_(y[5184]); ws[83008] = kk * CEFF_(y[4320]); }
+    { const double kk = ws[47296]; ws[83040] = kk * CEFF_(y[5184]); ws[83072] = kk * CEFF_(y[3584]); }
+    { const double kk = ws[47328]; ws[83104] = kk * CEFF_(y[5184]); ws[83136] = kk * CEFF_(y[3808]); }
+    { const double kk = ws[47360]; ws[83168] = kk * CEFF_(y[5952]); ws[83200] = kk * CEFF_(y[2240]); }
+    { const double kk = ws[47392]; ws[83232] = kk * CEFF_(y[5952]); ws[83264] = kk * CEFF_(y[2752]); }
+    { const double kk = ws[47424]; ws[83296] = kk * CEFF_(y[5952]); ws[83328] = kk * CEFF_(y[1152]); }
+    { const double kk = ws[47456]; ws[83360] = kk * CEFF_(y[5952]); ws[83392] = kk * CEFF_(y[1408]); }
+    { const double kk = ws[47488]; ws[83424] = kk * CEFF_(y[5952]); ws[83456] = kk * CEFF_(y[1440]); }
+    { const double kk = ws[47520]; ws[83488] = kk * CEFF_(y[5952]); ws[83520] = kk * CEFF_(y[4384]); }
+    { const double kk = ws[47552]; ws[83552] = kk * CEFF_(y[5952]); ws[83584] = kk * CEFF_(y[5856]); }
+    { const double kk = ws[47584]; ws[83616] = kk * CEFF_(y[5952]); ws[83648] = kk * CEFF_(y[5568]); }
+    { const double kk = ws[47616]; ws[83680] = kk * CEFF_(y[5952]); ws[83712] = kk * CEFF_(y[5760]); }
+    { const double kk = ws[47648]; ws[83744] = kk * CEFF_(y[5952]); ws[83776] = kk * CEFF_(y[4128]); }
+    { const double kk = ws[47680]; ws[83808] = kk * CEFF_(y[5952]); ws[83840] = kk * CEFF_(y[3872]); }
+    { const double kk = ws[47712]; ws[83872] = kk * CEFF_(y[5952]); ws[83904] = kk * CEFF_(y[5376]); }
+    { const double kk = ws[47744]; ws[83936] = kk * CEFF_(y[5952]); ws[83968] = kk * CEFF_(y[5248]); }
+    { const double kk = ws[47776]; ws[84000] = kk * CEFF_(y[5952]); ws[84032] = kk * CEFF_(y[1248]); }
+    { const double kk = ws[47808]; ws[84064] = kk * CEFF_(y[5952]); ws[84096] = kk * CEFF_(y[2944]); }
+    { const double kk = ws[47840]; ws[84128] = kk * CEFF_(y[5952]); ws[84160] = kk * CEFF_(y[1760]); }
+    { const double kk = ws[47872]; ws[84192] = kk * CEFF_(y[5952]); ws[84224] = kk * CEFF_(y[1824]); }
+    { const double kk = ws[47968]; ws[84256] = kk * CEFF_(y[5920]); ws[84288] = kk * CEFF_(y[5792]); }
+    { const double kk = ws[48032]; ws[84320] = kk * CEFF_(y[5920]); ws[84352] = kk * CEFF_(y[4800]); }
+    { const double kk = ws[48096]; ws[84384] = kk * CEFF_(y[5920]); ws[84416] = kk * CEFF_(y[4672]); }
+    { const double kk = ws[48160]; ws[84448] = kk * CEFF_(y[5824]); ws[84480] = kk * CEFF_(y[5888]); }
+    { const double kk = ws[48192]; ws[84512] = kk * CEFF_(y[5824]); ws[84544] = kk * CEFF_(y[5632]); }
+    { const double kk = ws[48224]; ws[84576] = kk * CEFF_(y[5824]); ws[84608] = kk * CEFF_(y[5408]); }
+    { const double kk = ws[48256]; ws[84640] = kk * CEFF_(y[5824]); ws[84672] = kk * CEFF_(y[5120]); }
+    { const double kk = ws[48288]; ws[84704] = kk * CEFF_(y[5824]); ws[84736] = kk * CEFF_(y[3008]); }
+    { const double kk = ws[48320]; ws[84768] = kk * CEFF_(y[5824]); ws[84800] = kk * CEFF_(y[3200]); }
+    { const double kk = ws[48352]; ws[84832] = kk * CEFF_(y[5824]); ws[84864] = kk * CEFF_(y[3328]); }
+    { const double kk = ws[48384]; ws[84896] = kk * CEFF_(y[5824]); ws[84928] = kk * CEFF_(y[3360]); }
+    { const double kk = ws[48416]; ws[84960] = kk * CEFF_(y[5824]); ws[84992] = kk * CEFF_(y[3296]); }
+    { const double kk = ws[48448]; ws[85024] = kk * CEFF_(y[5824]); ws[85056] = kk * CEFF_(y[3104]); }
+    { const double kk = ws[48480]; ws[85088] = kk * CEFF_(y[5824]); ws[85120] = kk * CEFF_(y[3264]); }
+    { const double kk = ws[48512]; ws[85152] = kk * CEFF_(y[5824]); ws[85184] = kk * CEFF_(y[4160]); }
+    { const double kk = ws[48544]; ws[85216] = kk * CEFF_(y[5824]); ws[85248] = kk * CEFF_(y[3744]); }
+    { const double kk = ws[48576]; ws[85280] = kk * CEFF_(y[5824]); ws[85312] = kk * CEFF_(y[2624]); }
+    { const double kk = ws[48608]; ws[85344] = kk * CEFF_(y[5824]); ws[85376] = kk * CEFF_(y[3840]); }
+    { const double kk = ws[48640]; ws[85408] = kk * CEFF_(y[5824]); ws[85440] = kk * CEFF_(y[4192]); }
+    { const double kk = ws[48672]; ws[85472] = kk * CEFF_(y[5824]); ws[85504] = kk * CEFF_(y[3936]); }
+    { const double kk = ws[48704]; ws[85536] = kk * CEFF_(y[5824]); ws[85568] = kk * CEFF_(y[2656]); }
+    { const double kk = ws[48736]; ws[85600] = kk * CEFF_(y[5824]); ws[85632] = kk * CEFF_(y[3712]); }
+    { const double kk = ws[48768]; ws[85664] = kk * CEFF_(y[5824]); ws[85696] = kk * CEFF_(y[2560]); }
+    { const double kk = ws[48800]; ws[85728] = kk * CEFF_(y[5824]); ws[85760] = kk * CEFF_(y[1728]); }
+    { const double kk = ws[48832]; ws[85792] = kk * CEFF_(y[5824]); ws[85824] = kk * CEFF_(y[5792]); }
+    { const double kk = ws[48864]; ws[85856] = kk * CEFF_(y[5824]); ws[85888] = kk * CEFF_(y[4800]); }
+    { const double kk = ws[48896]; ws[85920] = kk * CEFF_(y[5824]); ws[85952] = kk * CEFF_(y[2848]); }
+    { const double kk = ws[48928]; ws[85984] = kk * CEFF_(y[5824]); ws[86016] = kk * CEFF_(y[5152]); }
+    { const double kk = ws[48960]; ws[86048] = kk * CEFF_(y[5824]); ws[86080] = kk * CEFF_(y[3776]); }
+    { const double kk = ws[48992]; ws[86112] = kk * CEFF_(y[5824]); ws[86144] = kk * CEFF_(y[4672]); }
+    { const double kk = ws[49024]; ws[86176] = kk * CEFF_(y[5824]); ws[86208] = kk * CEFF_(y[3520]); }
+    { const double kk = ws[49056]; ws[86240] = kk * CEFF_(y[5824]); ws[86272] = kk * CEFF_(y[2880]); }
+    { const double kk = ws[49088]; ws[86304] = kk * CEFF_(y[5824]); ws[86336] = kk * CEFF_(y[2912]); }
+    { const double kk = ws[49120]; ws[86368] = kk * CEFF_(y[5824]); ws[86400] = kk * CEFF_(y[2592]); }
+    { const double kk = ws[49152]; ws[86432] = kk * CEFF_(y[5824]); ws[86464] = kk * CEFF_(y[2272]); }
+    { const double kk = ws[49184]; ws[86496] = kk * CEFF_(y[5824]); ws[86528] = kk * CEFF_(y[3648]); }
+    { const double kk = ws[49216]; ws[86560] = kk * CEFF_(y[5824]); ws[86592] = kk * CEFF_(y[3040]); }
+    { const double kk = ws[49248]; ws[86624] = kk * CEFF_(y[5824]); ws[86656] = kk * CEFF_(y[2976]); }
+    { const double kk = ws[49280]; ws[86688] = kk * CEFF_(y[5824]); ws[86720] = kk * CEFF_(y[4032]); }
+    { const double kk = ws[49312]; ws[86752] = kk * CEFF_(y[5824]); ws[86784] = kk * CEFF_(y[4064]); }
+    { const double kk = ws[49344]; ws[86816] = kk * CEFF_(y[5824]); ws[86848] = kk * CEFF_(y[3072]); }
+    { const double kk = ws[49376]; ws[86880] = kk * CEFF_(y[5824]); ws[86912] = kk * CEFF_(y[5216]); }
+    { const double kk = ws[49408]; ws[86944] = kk * CEFF_(y[5920]); ws[86976] = kk * CEFF_(y[2688]); }
+    { const double kk = ws[49440]; ws[87008] = kk * CEFF_(y[5920]); ws[87040] = kk * CEFF_(y[3232]); }
+    { const double kk = ws[49472]; ws[87072] = kk * CEFF_(y[5920]); ws[87104] = kk * CEFF_(y[3808]); }
+    { const double kk = ws[49504]; ws[87136] = kk * CEFF_(y[5984]); ws[87168] = kk * CEFF_(y[5888]); }
+    { const double kk = ws[49536]; ws[87200] = kk * CEFF_(y[5984]); ws[87232] = kk * CEFF_(y[5632]); }
+    { const double kk = ws[49568]; ws[87264] = kk * CEFF_(y[5984]); ws[87296] = kk * CEFF_(y[5408]); }
+    { const double kk = ws[49600]; ws[87328] = kk * CEFF_(y[5984]); ws[87360] = kk * CEFF_(y[5120]); }
+    { const double kk = ws[49632]; ws[87392] = kk * CEFF_(y[5984]); ws[87424] = kk * CEFF_(y[3008]); }
+    { const double kk = ws[49664]; ws[87456] = kk * CEFF_(y[5984]); ws[87488] = kk * CEFF_(y[3200]); }
+    { const double kk = ws[49696]; ws[87520] = kk * CEFF_(y[5984]); ws[87552] = kk * CEFF_(y[3328]); }
+    { const double kk = ws[49728]; ws[87584] = kk * CEFF_(y[5984]); ws[87616] = kk * CEFF_(y[3360]); }
+    { const double kk = ws[49760]; ws[87648] = kk * CEFF_(y[5984]); ws[87680] = kk * CEFF_(y[3296]); }
+    { const double kk = ws[49792]; ws[87712] = kk * CEFF_(y[5984]); ws[87744] = kk * CEFF_(y[3104]); }
+    { const double kk = ws[49824]; ws[87776] = kk * CEFF_(y[5984]); ws[87808] = kk * CEFF_(y[3264]); }
+    { const double kk = ws[49856]; ws[87840] = kk * CEFF_(y[5984]); ws[87872] = kk * CEFF_(y[4160]); }
+    { const double kk = ws[49888]; ws[87904] = kk * CEFF_(y[5984]); ws[87936] = kk * CEFF_(y[3744]); }
+    { const double kk = ws[49920]; ws[87968] = kk * CEFF_(y[5984]); ws[88000] = kk * CEFF_(y[2624]); }
+    { const double kk = ws[49952]; ws[88032] = kk * CEFF_(y[5984]); ws[88064] = kk * CEFF_(y[3840]); }
+    { const double kk = ws[49984]; ws[88096] = kk * CEFF_(y[5984]); ws[88128] = kk * CEFF_(y[4192]); }
+    { const double kk = ws[50016]; ws[88160] = kk * CEFF_(y[5984]); ws[88192] = kk * CEFF_(y[3936]); }
+    { const double kk = ws[50048]; ws[88224] = kk * CEFF_(y[5984]); ws[88256] = kk * CEFF_(y[2656]); }
+    { const double kk = ws[50080]; ws[88288] = kk * CEFF_(y[5984]); ws[88320] = kk * CEFF_(y[3712]); }
+    { const double kk = ws[50112]; ws[88352] = kk * CEFF_(y[5984]); ws[88384] = kk * CEFF_(y[2560]); }
+    { const double kk = ws[50144]; ws[88416] = kk * CEFF_(y[5984]); ws[88448] = kk * CEFF_(y[1728]); }
+    { const double kk = ws[50176]; ws[88480] = kk * CEFF_(y[5984]); ws[88512] = kk * CEFF_(y[5792]); }
+    { const double kk = ws[50208]; ws[88544] = kk * CEFF_(y[5984]); ws[88576] = kk * CEFF_(y[4800]); }
+    { const double kk = ws[50240]; ws[88608] = kk * CEFF_(y[5984]); ws[88640] = kk * CEFF_(y[2848]); }
+    { const double kk = ws[50272]; ws[88672] = kk * CEFF_(y[5984]); ws[88704] = kk * CEFF_(y[5152]); }
+    { const double kk = ws[50304]; ws[88736] = kk * CEFF_(y[5984]); ws[88768] = kk * CEFF_(y[3776]); }
+    { const double kk = ws[50336]; ws[88800] = kk * CEFF_(y[5984]); ws[88832] = kk * CEFF_(y[4672]); }
+    { const double kk = ws[50368]; ws[88864] = kk * CEFF_(y[5984]); ws[88896] = kk * CEFF_(y[3520]); }
+    { const double kk = ws[50400]; ws[88928] = kk * CEFF_(y[5984]); ws[88960] = kk * CEFF_(y[2880]); }
+    { const double kk = ws[50432]; ws[88992] = kk * CEFF_(y[5984]); ws[89024] = kk * CEFF_(y[2912]); }
+    { const double kk = ws[50464]; ws[89056] = kk * CEFF_(y[5984]); ws[89088] = kk * CEFF_(y[3648]); }
+    { const double kk = ws[50496]; ws[89120] = kk * CEFF_(y[5984]); ws[89152] = kk * CEFF_(y[3232]); }
+    { const double kk = ws[50528]; ws[89184] = kk * CEFF_(y[5984]); ws[89216] = kk * CEFF_(y[3040]); }
+    { const double kk = ws[50560]; ws[89248] = kk * CEFF_(y[5984]); ws[89280] = kk * CEFF_(y[2976]); }
+    { const double kk = ws[50592]; ws[89312] = kk * CEFF_(y[5984]); ws[89344] = kk * CEFF_(y[4032]); }
+    { const double kk = ws[50624]; ws[89376] = kk * CEFF_(y[5984]); ws[89408] = kk * CEFF_(y[4064]); }
+    { const double kk = ws[50656]; ws[89440] = kk * CEFF_(y[5984]); ws[89472] = kk * CEFF_(y[3072]); }
+    { const double kk = ws[50688]; ws[89504] = kk * CEFF_(y[5984]); ws[89536] = kk * CEFF_(y[5216]); }
+    { const double kk = ws[50720]; ws[89568] = kk * CEFF_(y[5888]); ws[89600] = kk * CEFF_(y[5888]); }
+    { const double kk = ws[50752]; ws[89632] = kk * CEFF_(y[5888]); ws[89664] = kk * CEFF_(y[5632]); }
+    { const double kk = ws[50784]; ws[89696] = kk * CEFF_(y[5888]); ws[89728] = kk * CEFF_(y[5408]); }
+    { const double kk = ws[50816]; ws[89760] = kk * CEFF_(y[5888]); ws[89792] = kk * CEFF_(y[5120]); }
+    { const double kk = ws[50848]; ws[89824] = kk * CEFF_(y[5888]); ws[89856] = kk * CEFF_(y[3008]); }
+    { const double kk = ws[50880]; ws[89888] = kk * CEFF_(y[5888]); ws[89920] = kk * CEFF_(y[3200]); }
+    { const double kk = ws[50912]; ws[89952] = kk * CEFF_(y[5888]); ws[89984] = kk * CEFF_(y[3328]); }
+    { const double kk = ws[50944]; ws[90016] = kk * CEFF_(y[5888]); ws[90048] = kk * CEFF_(y[3360]); }
+    { const double kk = ws[50976]; ws[90080] = kk * CEFF_(y[5888]); ws[90112] = kk * CEFF_(y[3296]); }
+    { const double kk = ws[51008]; ws[90144] = kk * CEFF_(y[5888]); ws[90176] = kk * CEFF_(y[3104]); }
+    { const double kk = ws[51040]; ws[90208] = kk * CEFF_(y[5888]); ws[90240] = kk * CEFF_(y[3264]); }
+    { const double kk = ws[51072]; ws[90272] = kk * CEFF_(y[5888]); ws[90304] = kk * CEFF_(y[4288]); }
+    { const double kk = ws[51104]; ws[90336] = kk * CEFF_(y[5888]); ws[90368] = kk * CEFF_(y[4160]); }
+    { const double kk = ws[51136]; ws[90400] = kk * CEFF_(y[5888]); ws[90432] = kk * CEFF_(y[3744]); }
+    { const double kk = ws[51168]; ws[90464] = kk * CEFF_(y[5888]); ws[90496] = kk * CEFF_(y[2624]); }
+    { const double kk = ws[51200]; ws[90528] = kk * CEFF_(y[5888]); ws[90560] = kk * CEFF_(y[3840]); }
+    { const double kk = ws[51232]; ws[90592] = kk * CEFF_(y[5888]); ws[90624] = kk * CEFF_(y[4192]); }
+    { const double kk = ws[51264]; ws[90656] = kk * CEFF_(y[5888]); ws[90688] = kk * CEFF_(y[3936]); }
+    { const double kk = ws[51296]; ws[90720] = kk * CEFF_(y[5888]); ws[90752] = kk * CEFF_(y[2656]); }
+    { const double kk = ws[51328]; ws[90784] = kk * CEFF_(y[5888]); ws[90816] = kk * CEFF_(y[3712]); }
+    { const double kk = ws[51360]; ws[90848] = kk * CEFF_(y[5888]); ws[90880] = kk * CEFF_(y[5792]); }
+    { const double kk = ws[51392]; ws[90912] = kk * CEFF_(y[5888]); ws[90944] = kk * CEFF_(y[4800]); }
+    { const double kk = ws[51424]; ws[90976] = kk * CEFF_(y[5888]); ws[91008] = kk * CEFF_(y[2848]); }
+    { const double kk = ws[51456]; ws[91040] = kk * CEFF_(y[5888]); ws[91072] = kk * CEFF_(y[5152]); }
+    { const double kk = ws[51488]; ws[91104] = kk * CEFF_(y[5888]); ws[91136] = kk * CEFF_(y[3776]); }
+    { const double kk = ws[51520]; ws[91168] = kk * CEFF_(y[5888]); ws[91200] = kk * CEFF_(y[4672]); }
+    { const double kk = ws[51552]; ws[91232] = kk * CEFF_(y[5888]); ws[91264] = kk * CEFF_(y[3520]); }
+    { const double kk = ws[51584]; ws[91296] = kk * CEFF_(y[5888]); ws[91328] = kk * CEFF_(y[2880]); }
+    { const double kk = ws[51616]; ws[91360] = kk * CEFF_(y[5888]); ws[91392] = kk * CEFF_(y[2912]); }
+    { const double kk = ws[51648]; ws[91424] = kk * CEFF_(y[5888]); ws[91456] = kk * CEFF_(y[2592]); }
+    { const double kk = ws[51680]; ws[91488] = kk * CEFF_(y[5888]); ws[91520] = kk * CEFF_(y[2272]); }
+    { const double kk = ws[51712]; ws[91552] = kk * CEFF_(y[5888]); ws[91584] = kk * CEFF_(y[3648]); }
+    { const double kk = ws[51744]; ws[91616] = kk * CEFF_(y[5888]); ws[91648] = kk * CEFF_(y[3040]); }
+    { const double kk = ws[51776]; ws[91680] = kk * CEFF_(y[5888]); ws[91712] = kk * CEFF_(y[2976]); }
+    { const double kk = ws[51808]; ws[91744] = kk * CEFF_(y[5888]); ws[91776] = kk * CEFF_(y[4032]); }
+    { const double kk = ws[51840]; ws[91808] = kk * CEFF_(y[5888]); ws[91840] = kk * CEFF_(y[4064]); }
+    { const double kk = ws[51872]; ws[91872] = kk * CEFF_(y[5888]); ws[91904] = kk * CEFF_(y[3072]); }
+    { const double kk = ws[51904]; ws[91936] = kk * CEFF_(y[5888]); ws[91968] = kk * CEFF_(y[5216]); }
+    { const double kk = ws[51936]; ws[92000] = kk * CEFF_(y[5792]); ws[92032] = kk * CEFF_(y[5632]); }
+    { const double kk = ws[51968]; ws[92064] = kk * CEFF_(y[5792]); ws[92096] = kk * CEFF_(y[5408]); }
+    { const double kk = ws[52000]; ws[92128] = kk * CEFF_(y[5792]); ws[92160] = kk * CEFF_(y[5120]); }
+    { const double kk = ws[52032]; ws[92192] = kk * CEFF_(y[5792]); ws[92224] = kk * CEFF_(y[3008]); }
+    { const double kk = ws[52064]; ws[92256] = kk * CEFF_(y[5792]); ws[92288] = kk * CEFF_(y[3200]); }
+    { const double kk = ws[52096]; ws[92320] = kk * CEFF_(y[5792]); ws[92352] = kk * CEFF_(y[3328]); }
+    { const double kk = ws[52128]; ws[92384] = kk * CEFF_(y[5792]); ws[92416] = kk * CEFF_(y[3360]); }
+    { const double kk = ws[52160]; ws[92448] = kk * CEFF_(y[5792]); ws[92480] = kk * CEFF_(y[3296]); }
+    { const double kk = ws[52192]; ws[92512] = kk * CEFF_(y[5792]); ws[92544] = kk * CEFF_(y[3104]); }
+    { const double kk = ws[52224]; ws[92576] = kk * CEFF_(y[5792]); ws[92608] = kk * CEFF_(y[3264]); }
+    { const double kk = ws[52256]; ws[92640] = kk * CEFF_(y[5792]); ws[92672] = kk * CEFF_(y[4288]); }
+    { const double kk = ws[52288]; ws[92704] = kk * CEFF_(y[5792]); ws[92736] = kk * CEFF_(y[4160]); }
+    { const double kk = ws[52320]; ws[92768] = kk * CEFF_(y[5792]); ws[92800] = kk * CEFF_(y[3744]); }
+    { const double kk = ws[52352]; ws[92832] = kk * CEFF_(y[5792]); ws[92864] = kk * CEFF_(y[2624]); }
+    { const double kk = ws[52384]; ws[92896] = kk * CEFF_(y[5792]); ws[92928] = kk * CEFF_(y[3840]); }
+    { const double kk = ws[52416]; ws[92960] = kk * CEFF_(y[5792]); ws[92992] = kk * CEFF_(y[4192]); }
+    { const double kk = ws[52448]; ws[93024] = kk * CEFF_(y[5792]); ws[93056] = kk * CEFF_(y[3936]); }
+    { const double kk = ws[52480]; ws[93088] = kk * CEFF_(y[5792]); ws[93120] = kk * CEFF_(y[2656]); }
+    { const double kk = ws[52512]; ws[93152] = kk * CEFF_(y[5792]); ws[93184] = kk * CEFF_(y[3712]); }
+    { const double kk = ws[52544]; ws[93216] = kk * CEFF_(y[5792]); ws[93248] = kk * CEFF_(y[5792]); }
+    { const double kk = ws[52576]; ws[93280] = kk * CEFF_(y[5792]); ws[93312] = kk * CEFF_(y[4800]); }
+    { const double kk = ws[52608]; ws[93344] = kk * CEFF_(y[5792]); ws[93376] = kk * CEFF_(y[2848]); }
+    { const double kk = ws[52640]; ws[93408] = kk * CEFF_(y[5792]); ws[93440] = kk * CEFF_(y[5152]); }
+    { const double kk = ws[52672]; ws[93472] = kk * CEFF_(y[5792]); ws[93504] = kk * CEFF_(y[3776]); }
+    { const double kk = ws[52704]; ws[93536] = kk * CEFF_(y[5792]); ws[93568] = kk * CEFF_(y[4672]); }
+    { const double kk = ws[52736]; ws[93600] = kk * CEFF_(y[5792]); ws[93632] = kk * CEFF_(y[3520]); }
+    { const double kk = ws[52768]; ws[93664] = kk * CEFF_(y[5792]); ws[93696] = kk * CEFF_(y[2880]); }
+    { const double kk = ws[52800]; ws[93728] = kk * CEFF_(y[5792]); ws[93760] = kk * CEFF_(y[2912]); }
+    { const double kk = ws[52832]; ws[93792] = kk * CEFF_(y[5792]); ws[93824] = kk * CEFF_(y[2592]); }
+    { const double kk = ws[52864]; ws[93856] = kk * CEFF_(y[5792]); ws[93888] = kk * CEFF_(y[2272]); }
+    { const double kk = ws[52896]; ws[93920] = kk * CEFF_(y[5792]); ws[93952] = kk * CEFF_(y[3648]); }
+    { const double kk = ws[52928]; ws[93984] = kk * CEFF_(y[5792]); ws[94016] = kk * CEFF_(y[3040]); }
+    { const double kk = ws[52960]; ws[94048] = kk * CEFF_(y[5792]); ws[94080] = kk * CEFF_(y[2976]); }
+    { const double kk = ws[52992]; ws[94112] = kk * CEFF_(y[5792]); ws[94144] = kk * CEFF_(y[4032]); }
+    { const double kk = ws[53024]; ws[94176] = kk * CEFF_(y[5792]); ws[94208] = kk * CEFF_(y[4064]); }
+    { const double kk = ws[53056]; ws[94240] = kk * CEFF_(y[5792]); ws[94272] = kk * CEFF_(y[3072]); }
+    { const double kk = ws[53088]; ws[94304] = kk * CEFF_(y[5792]); ws[94336] = kk * CEFF_(y[5216]); }
+    { const double kk = ws[53120]; ws[94368] = kk * CEFF_(y[4800]); ws[94400] = kk * CEFF_(y[4800]); }
+    { const double kk = ws[53152]; ws[94432] = kk * CEFF_(y[5952]); ws[94464] = kk * CEFF_(y[5888]); }
+    { const double kk = ws[53184]; ws[94496] = kk * CEFF_(y[5952]); ws[94528] = kk * CEFF_(y[5632]); }
+    { const double kk = ws[53216]; ws[94560] = kk * CEFF_(y[5952]); ws[94592] = kk * CEFF_(y[5408]); }
+    { const double kk = ws[53248]; ws[94624] = kk * CEFF_(y[5952]); ws[94656] = kk * CEFF_(y[5120]); }
+    { const double kk = ws[53280]; ws[94688] = kk * CEFF_(y[5952]); ws[94720] = kk * CEFF_(y[3008]); }
+    { const double kk = ws[53312]; ws[94752] = kk * CEFF_(y[5952]); ws[94784] = kk * CEFF_(y[3200]); }
+    { const double kk = ws[53344]; ws[94816] = kk * CEFF_(y[5952]); ws[94848] = kk * CEFF_(y[3328]); }
+    { const double kk = ws[53376]; ws[94880] = kk * CEFF_(y[5952]); ws[94912] = kk * CEFF_(y[3360]); }
+    { const double kk = ws[53408]; ws[94944] = kk * CEFF_(y[5952]); ws[94976] = kk * CEFF_(y[3296]); }
+    { const double kk = ws[53440]; ws[95008] = kk * CEFF_(y[5952]); ws[95040] = kk * CEFF_(y[3104]); }
+    { const double kk = ws[53472]; ws[95072] = kk * CEFF_(y[5952]); ws[95104] = kk * CEFF_(y[3264]); }
+    { const double kk = ws[53504]; ws[95136] = kk * CEFF_(y[5952]); ws[95168] = kk * CEFF_(y[4288]); }
+    { const double kk = ws[53536]; ws[95200] = kk * CEFF_(y[5952]); ws[95232] = kk * CEFF_(y[4160]); }
+    { const double kk = ws[53568]; ws[95264] = kk * CEFF_(y[5952]); ws[95296] = kk * CEFF_(y[4192]); }
+    { const double kk = ws[53600]; ws[95328] = kk * CEFF_(y[5952]); ws[95360] = kk * CEFF_(y[2624]); }
+    { const double kk = ws[53632]; ws[95392] = kk * CEFF_(y[5952]); ws[95424] = kk * CEFF_(y[2656]); }
+    { const double kk = ws[53664]; ws[95456] = kk * CEFF_(y[5952]); ws[95488] = kk * CEFF_(y[5792]); }
+    { const double kk = ws[53696]; ws[95520] = kk * CEFF_(y[5952]); ws[95552] = kk * CEFF_(y[4800]); }
+    { const double kk = ws[53728]; ws[95584] = kk * CEFF_(y[5952]); ws[95616] = kk * CEFF_(y[2848]); }
+    { const double kk = ws[53760]; ws[95648] = kk * CEFF_(y[5952]); ws[95680] = kk * CEFF_(y[5152]); }
+    { const double kk = ws[53792]; ws[95712] = kk * CEFF_(y[5952]); ws[95744] = kk * CEFF_(y[3776]); }
+    { const double kk = ws[53824]; ws[95776] = kk * CEFF_(y[5952]); ws[95808] = kk * CEFF_(y[4672]); }
+    { const double kk = ws[53856]; ws[95840] = kk * CEFF_(y[5952]); ws[95872] = kk * CEFF_(y[3520]); }
+    { const double kk = ws[53888]; ws[95904] = kk * CEFF_(y[5952]); ws[95936] = kk * CEFF_(y[2880]); }
+    { const double kk = ws[53920]; ws[95968] = kk * CEFF_(y[5952]); ws[96000] = kk * CEFF_(y[2912]); }
+    { const double kk = ws[53952]; ws[96032] = kk * CEFF_(y[5952]); ws[96064] = kk * CEFF_(y[2592]); }
+    { const double kk = ws[53984]; ws[96096] = kk * CEFF_(y[5952]); ws[96128] = kk * CEFF_(y[2272]); }
+    { const double kk = ws[54016]; ws[96160] = kk * CEFF_(y[5952]); ws[96192] = kk * CEFF_(y[3648]); }
+    { const double kk = ws[54048]; ws[96224] = kk * CEFF_(y[5952]); ws[96256] = kk * CEFF_(y[3040]); }
+    { const double kk = ws[54080]; ws[96288] = kk * CEFF_(y[5952]); ws[96320] = kk * CEFF_(y[2976]); }
+    { const double kk = ws[54112]; ws[96352] = kk * CEFF_(y[5952]); ws[96384] = kk * CEFF_(y[4032]); }
+    { const double kk = ws[54144]; ws[96416] = kk * CEFF_(y[5952]); ws[96448] = kk * CEFF_(y[4064]); }
+    { const double kk = ws[54176]; ws[96480] = kk * CEFF_(y[5952]); ws[96512] = kk * CEFF_(y[3072]); }
+    { const double kk = ws[54208]; ws[96544] = kk * CEFF_(y[4032]); ws[96576] = kk * CEFF_(y[4032]); }
+    { const double kk = ws[54240]; ws[96608] = kk * CEFF_(y[4064]); ws[96640] = kk * CEFF_(y[4032]); }
+    { const double kk = ws[54272]; ws[96672] = kk * CEFF_(y[4064]); ws[96704] = kk * CEFF_(y[4064]); }
+    { const double kk = ws[54304]; ws[96736] = kk * CEFF_(y[5952]); ws[96768] = kk * CEFF_(y[5216]); }
+    { const double kk = ws[54336]; ws[96800] = kk * CEFF_(y[4800]); ws[96832] = kk * CEFF_(y[5216]); }
+    { const double kk = ws[54368]; ws[96864] = kk * CEFF_(y[5216]); ws[96896] = kk * CEFF_(y[5216]); }
+    { const double kk = ws[54400]; ws[96928] = kk * CEFF_(y[4160]); ws[96960] = kk * CEFF_(y[3744]); }
+    { const double kk = ws[54432]; ws[96992] = kk * CEFF_(y[4192]); ws[97024] = kk * CEFF_(y[3744]); }
+    { const double kk = ws[54464]; ws[97056] = kk * CEFF_(y[4288]); ws[97088] = kk * CEFF_(y[3744]); }
+    { const double kk = ws[54496]; ws[97120] = kk * CEFF_(y[4160]); ws[97152] = kk * CEFF_(y[3936]); }
+    { const double kk = ws[54528]; ws[97184] = kk * CEFF_(y[4192]); ws[97216] = kk * CEFF_(y[3936]); }
+    { const double kk = ws[54560]; ws[97248] = kk * CEFF_(y[4288]); ws[97280] = kk * CEFF_(y[3936]); }
+    { const double kk = ws[54592]; ws[97312] = kk * CEFF_(y[4160]); ws[97344] = kk * CEFF_(y[3840]); }
+    { const double kk = ws[54624]; ws[97376] = kk * CEFF_(y[4192]); ws[97408] = kk * CEFF_(y[3840]); }
+    { const double kk = ws[54656]; ws[97440] = kk * CEFF_(y[4288]); ws[97472] = kk * CEFF_(y[3840]); }
+    { const double kk = ws[54688]; ws[97504] = kk * CEFF_(y[4160]); ws[97536] = kk * CEFF_(y[3712]); }
+    { const double kk = ws[54720]; ws[97568] = kk * CEFF_(y[4192]); ws[97600] = kk * CEFF_(y[3712]); }
+    { const double kk = ws[54752]; ws[97632] = kk * CEFF_(y[4288]); ws[97664] = kk * CEFF_(y[3712]); }
+    { const double kk = ws[54784]; ws[97696] = kk * CEFF_(y[6016]); ws[97728] = kk * CEFF_(y[1376]); }
+    { const double kk = ws[54816]; ws[97760] = kk * CEFF_(y[6016]); ws[97792] = kk * CEFF_(y[384]); }
+    { const double kk = ws[54848]; ws[97824] = kk * CEFF_(y[6016]); ws[97856] = kk * CEFF_(y[416]); }
+    { const double kk = ws[54880]; ws[97888] = kk * CEFF_(y[6016]); ws[97920] = kk * CEFF_(y[3552]); }
+    { const double kk = ws[54912]; ws[97952] = kk * CEFF_(y[5184]); ws[97984] = kk * CEFF_(y[3552]); }
+    { const double kk = ws[54944]; ws[98016] = kk * CEFF_(y[5952]); ws[98048] = kk * CEFF_(y[3552]); }
+    { const double kk = ws[55008]; ws[98080] = kk * CEFF_(y[6016]); ws[98112] = kk * CEFF_(y[1568]); }
+    { const double kk = ws[55040]; ws[98144] = kk * CEFF_(y[5824]); ws[98176] = kk * CEFF_(y[3136]); }
+    { const double kk = ws[55072]; ws[98208] = kk * CEFF_(y[5952]); ws[98240] = kk * CEFF_(y[3136]); }
+    { const double kk = ws[55104]; ws[98272] = kk * CEFF_(y[5984]); ws[98304] = kk * CEFF_(y[3136]); }
+    { const double kk = ws[55136]; ws[98336] = kk * CEFF_(y[5888]); ws[98368] = kk * CEFF_(y[3136]); }
+    { const double kk = ws[55168]; ws[98400] = kk * CEFF_(y[5792]); ws[98432] = kk * CEFF_(y[3136]); }
+    { const double kk = ws[55200]; ws[98464] = kk * CEFF_(y[5184]); ws[98496] = kk * CEFF_(y[1568]); }
+    { const double kk = ws[55232]; ws[98528] = kk * CEFF_(y[5952]); ws[98560] = kk * CEFF_(y[1568]); }
+    { const double kk = ws[55264]; ws[98592] = kk * CEFF_(y[6016]); ws[98624] = kk * CEFF_(y[3168]); }
+    { const double kk = ws[55296]; ws[98656] = kk * CEFF_(y[5824]); ws[98688] = kk * CEFF_(y[1856]); }
+    { const double kk = ws[55328]; ws[98720] = kk * CEFF_(y[5984]); ws[98752] = kk * CEFF_(y[1856]); }
+    { const double kk = ws[55360]; ws[98784] = kk * CEFF_(y[6016]); ws[98816] = kk * CEFF_(y[4512]); }
+    { const double kk = ws[55392]; ws[98848] = kk * CEFF_(y[5184]); ws[98880] = kk * CEFF_(y[3168]); }
+    { const double kk = ws[55424]; ws[98912] = kk * CEFF_(y[5952]); ws[98944] = kk * CEFF_(y[3168]); }
+    { const double kk = ws[55456]; ws[98976] = kk * CEFF_(y[6016]); ws[99008] = kk * CEFF_(y[448]); }
+    { const double kk = ws[55488]; ws[99040] = kk * CEFF_(y[5952]); ws[99072] = kk * CEFF_(y[1600]); }
+    { const double kk = ws[55520]; ws[99104] = kk * CEFF_(y[5984]); ws[99136] = kk * CEFF_(y[1920]); }
+    { const double kk = ws[55552]; ws[99168] = kk * CEFF_(y[5824]); ws[99200] = kk * CEFF_(y[1920]); }
+    { const double kk = ws[55584]; ws[99232] = kk * CEFF_(y[5952]); ws[99264] = kk * CEFF_(y[1920]); }
+    { const double kk = ws[55616]; ws[99296] = kk * CEFF_(y[5184]); ws[99328] = kk * CEFF_(y[1600]); }
+    { const double kk = ws[55648]; ws[99360] = kk * CEFF_(y[6016]); ws[99392] = kk * CEFF_(y[1600]); }
+    { const double kk = ws[55680]; ws[99424] = kk * CEFF_(y[5984]); ws[99456] = kk * CEFF_(y[2304]); }
+    { const double kk = ws[55712]; ws[99488] = kk * CEFF_(y[5952]); ws[99520] = kk * CEFF_(y[2304]); }
+    { const double kk = ws[55744]; ws[99552] = kk * CEFF_(y[5824]); ws[99584] = kk * CEFF_(y[2304]); }
+    { const double kk = ws[56064]; ws[99616] = kk * CEFF_(y[512]); ws[99648] = kk * CEFF_(y[1056]); }
+    { const double kk = ws[56160]; ws[99680] = kk * CEFF_(y[6016]); ws[99712] = kk * CEFF_(y[608]); }
+    { const double kk = ws[56192]; ws[99744] = kk * CEFF_(y[6016]); ws[99776] = kk * CEFF_(y[640]); }
+    { const double kk = ws[56224]; ws[99808] = kk * CEFF_(y[6016]); ws[99840] = kk * CEFF_(y[672]); }
+    { const double kk = ws[56256]; ws[99872] = kk * CEFF_(y[6016]); ws[99904] = kk * CEFF_(y[704]); }
+    { const double kk = ws[56288]; ws[99936] = kk * CEFF_(y[6016]); ws[99968] = kk * CEFF_(y[736]); }
+    { const double kk = ws[56320]; ws[100000] = kk * CEFF_(y[6016]); ws[100032] = kk * CEFF_(y[768]); }
+    { const double kk = ws[56352]; ws[100064] = kk * CEFF_(y[6016]); ws[100096] = kk * CEFF_(y[800]); }
+    { const double kk = ws[56384]; ws[100128] = kk * CEFF_(y[5824]); ws[100160] = kk * CEFF_(y[2368]); }
+    { const double kk = ws[56416]; ws[100192] = kk * CEFF_(y[5824]); ws[100224] = kk * CEFF_(y[2400]); }
+    { const double kk = ws[56448]; ws[100256] = kk * CEFF_(y[5824]); ws[100288] = kk * CEFF_(y[2432]); }
+    { const double kk = ws[56480]; ws[100320] = kk * CEFF_(y[5824]); ws[100352] = kk * CEFF_(y[2464]); }
+    { const double kk = ws[56512]; ws[100384] = kk * CEFF_(y[5824]); ws[100416] = kk * CEFF_(y[2496]); }
+    { const double kk = ws[56544]; ws[100448] = kk * CEFF_(y[5824]); ws[100480] = kk * CEFF_(y[2528]); }
+    { const double kk = ws[56576]; ws[100512] = kk * CEFF_(y[5824]); ws[100544] = kk * CEFF_(y[3904]); }
+    { const double kk = ws[56608]; ws[100576] = kk * CEFF_(y[5952]); ws[100608] = kk * CEFF_(y[2368]); }
+    { const double kk = ws[56640]; ws[100640] = kk * CEFF_(y[5952]); ws[100672] = kk * CEFF_(y[2400]); }
+    { const double kk = ws[56672]; ws[100704] = kk * CEFF_(y[5952]); ws[100736] = kk * CEFF_(y[2432]); }
+    { const double kk = ws[56704]; ws[100768] = kk * CEFF_(y[5952]); ws[100800] = kk * CEFF_(y[2464]); }
+    { const double kk = ws[56736]; ws[100832] = kk * CEFF_(y[5952]); ws[100864] = kk * CEFF_(y[2496]); }
+    { const double kk = ws[56768]; ws[100896] = kk * CEFF_(y[5952]); ws[100928] = kk * CEFF_(y[2528]); }
+    { const double kk = ws[56800]; ws[100960] = kk * CEFF_(y[5952]); ws[100992] = kk * CEFF_(y[3904]); }
+    { const double kk = ws[56832]; ws[101024] = kk * CEFF_(y[5984]); ws[101056] = kk * CEFF_(y[2368]); }
+    { const double kk = ws[56864]; ws[101088] = kk * CEFF_(y[5984]); ws[101120] = kk * CEFF_(y[2400]); }
+    { const double kk = ws[56896]; ws[101152] = kk * CEFF_(y[5984]); ws[101184] = kk * CEFF_(y[2432]); }
+    { const double kk = ws[56928]; ws[101216] = kk * CEFF_(y[5984]); ws[101248] = kk * CEFF_(y[2464]); }
+    { const double kk = ws[56960]; ws[101280] = kk * CEFF_(y[5984]); ws[101312] = kk * CEFF_(y[2496]); }
+    { const double kk = ws[56992]; ws[101344] = kk * CEFF_(y[5984]); ws[101376] = kk * CEFF_(y[2528]); }
+    { const double kk = ws[57024]; ws[101408] = kk * CEFF_(y[5984]); ws[101440] = kk * CEFF_(y[3904]); }
+    { const double kk = ws[57280]; ws[101472] = kk * CEFF_(y[5824]); ws[101504] = kk * CEFF_(y[1952]); }
+    { const double kk = ws[57312]; ws[101536] = kk * CEFF_(y[5824]); ws[101568] = kk * CEFF_(y[1984]); }
+    { const double kk = ws[57344]; ws[101600] = kk * CEFF_(y[5824]); ws[101632] = kk * CEFF_(y[2016]); }
+    { const double kk = ws[57376]; ws[101664] = kk * CEFF_(y[5824]); ws[101696] = kk * CEFF_(y[2048]); }
+    { const double kk = ws[57408]; ws[101728] = kk * CEFF_(y[5824]); ws[101760] = kk * CEFF_(y[2080]); }
+    { const double kk = ws[57440]; ws[101792] = kk * CEFF_(y[5824]); ws[101824] = kk * CEFF_(y[2112]); }
+    { const double kk = ws[57472]; ws[101856] = kk * CEFF_(y[5824]); ws[101888] = kk * CEFF_(y[2144]); }
+    { const double kk = ws[57504]; ws[101920] = kk * CEFF_(y[5952]); ws[101952] = kk * CEFF_(y[1952]); }
+    { const double kk = ws[57536]; ws[101984] = kk * CEFF_(y[5952]); ws[102016] = kk * CEFF_(y[1984]); }
+    { const double kk = ws[57568]; ws[102048] = kk * CEFF_(y[5952]); ws[102080] = kk * CEFF_(y[2016]); }
+    { const double kk = ws[57600]; ws[102112] = kk * CEFF_(y[5952]); ws[102144] = kk * CEFF_(y[2048]); }
+    { const double kk = ws[57632]; ws[102176] = kk * CEFF_(y[5952]); ws[102208] = kk * CEFF_(y[2080]); }
+    { const double kk = ws[57664]; ws[102240] = kk * CEFF_(y[5952]); ws[102272] = kk * CEFF_(y[2112]); }
+    { const double kk = ws[57696]; ws[102304] = kk * CEFF_(y[5952]); ws[102336] = kk * CEFF_(y[2144]); }
+    { const double kk = ws[57728]; ws[102368] = kk * CEFF_(y[5984]); ws[102400] = kk * CEFF_(y[1952]); }
+    { const double kk = ws[57760]; ws[102432] = kk * CEFF_(y[5984]); ws[102464] = kk * CEFF_(y[1984]); }
+    { const double kk = ws[57792]; ws[102496] = kk * CEFF_(y[5984]); ws[102528] = kk * CEFF_(y[2016]); }
+    { const double kk = ws[57824]; ws[102560] = kk * CEFF_(y[5984]); ws[102592] = kk * CEFF_(y[2048]); }
+    { const double kk = ws[57856]; ws[102624] = kk * CEFF_(y[5984]); ws[102656] = kk * CEFF_(y[2080]); }
+    { const double kk = ws[57888]; ws[102688] = kk * CEFF_(y[5984]); ws[102720] = kk * CEFF_(y[2112]); }
+    { const double kk = ws[57920]; ws[102752] = kk * CEFF_(y[5984]); ws[102784] = kk * CEFF_(y[2144]); }
+    { const double kk = ws[57952]; ws[102816] = kk * CEFF_(y[6016]); ws[102848] = kk * CEFF_(y[832]); }
+    { const double kk = ws[57984]; ws[102880] = kk * CEFF_(y[5984]); ws[102912] = kk * CEFF_(y[3392]); }
+    { const double kk = ws[58016]; ws[102944] = kk * CEFF_(y[5824]); ws[102976] = kk * CEFF_(y[3392]); }
+    { const double kk = ws[58048]; ws[103008] = kk * CEFF_(y[5952]); ws[103040] = kk * CEFF_(y[3392]); }
+    { const double kk = ws[58080]; ws[103072] = kk * CEFF_(y[5888]); ws[103104] = kk * CEFF_(y[3392]); }
+    { const double kk = ws[58112]; ws[103136] = kk * CEFF_(y[5792]); ws[103168] = kk * CEFF_(y[3392]); }
+    { const double kk = ws[58144]; ws[103200] = kk * CEFF_(y[6016]); ws[103232] = kk * CEFF_(y[864]); }
+    { const double kk = ws[58176]; ws[103264] = kk * CEFF_(y[5984]); ws[103296] = kk * CEFF_(y[3424]); }
+    { const double kk = ws[58208]; ws[103328] = kk * CEFF_(y[5824]); ws[103360] = kk * CEFF_(y[3424]); }
+    { const double kk = ws[58240]; ws[103392] = kk * CEFF_(y[5952]); ws[103424] = kk * CEFF_(y[3424]); }
+    { const double kk = ws[58272]; ws[103456] = kk * CEFF_(y[5888]); ws[103488] = kk * CEFF_(y[3424]); }
+    { const double kk = ws[58304]; ws[103520] = kk * CEFF_(y[5792]); ws[103552] = kk * CEFF_(y[3424]); }
+    { const double kk = ws[58336]; ws[103584] = kk * CEFF_(y[6016]); ws[103616] = kk * CEFF_(y[896]); }
+    { const double kk = ws[58368]; ws[103648] = kk * CEFF_(y[5984]); ws[103680] = kk * CEFF_(y[3456]); }
+    { const double kk = ws[58400]; ws[103712] = kk * CEFF_(y[5824]); ws[103744] = kk * CEFF_(y[3456]); }
+    { const double kk = ws[58432]; ws[103776] = kk * CEFF_(y[5952]); ws[103808] = kk * CEFF_(y[3456]); }
+    { const double kk = ws[58464]; ws[103840] = kk * CEFF_(y[5888]); ws[103872] = kk * CEFF_(y[3456]); }
+    { const double kk = ws[58496]; ws[103904] = kk * CEFF_(y[5792]); ws[103936] = kk * CEFF_(y[3456]); }
+    { const double kk = ws[58528]; ws[103968] = kk * CEFF_(y[6016]); ws[104000] = kk * CEFF_(y[4768]); }
+    { const double kk = ws[58560]; ws[104032] = kk * CEFF_(y[6016]); ws[104064] = kk * CEFF_(y[4864]); }
+    { const double kk = ws[58592]; ws[104096] = kk * CEFF_(y[6016]); ws[104128] = kk * CEFF_(y[4832]); }
+    { const double kk = ws[58624]; ws[104160] = kk * CEFF_(y[6016]); ws[104192] = kk * CEFF_(y[4896]); }
+    { const double kk = ws[58656]; ws[104224] = kk * CEFF_(y[6016]); ws[104256] = kk * CEFF_(y[4640]); }
+    { const double kk = ws[58688]; ws[104288] = kk * CEFF_(y[6016]); ws[104320] = kk * CEFF_(y[4416]); }
+    { const double kk = ws[58720]; ws[104352] = kk * CEFF_(y[6016]); ws[104384] = kk * CEFF_(y[4928]); }
+    { const double kk = ws[58752]; ws[104416] = kk * CEFF_(y[6016]); ws[104448] = kk * CEFF_(y[4960]); }
+    { const double kk = ws[58784]; ws[104480] = kk * CEFF_(y[6016]); ws[104512] = kk * CEFF_(y[4992]); }
+    { const double kk = ws[58816]; ws[104544] = kk * CEFF_(y[6016]); ws[104576] = kk * CEFF_(y[4704]); }
+    { const double kk = ws[58848]; ws[104608] = kk * CEFF_(y[6016]); ws[104640] = kk * CEFF_(y[5088]); }
+    { const double kk = ws[58880]; ws[104672] = kk * CEFF_(y[6016]); ws[104704] = kk * CEFF_(y[5536]); }
+    { const double kk = ws[58912]; ws[104736] = kk * CEFF_(y[6016]); ws[104768] = kk * CEFF_(y[5312]); }
+    { const double kk = ws[58944]; ws[104800] = kk * CEFF_(y[6016]); ws[104832] = kk * CEFF_(y[4224]); }
+    { const double kk = ws[58976]; ws[104864] = kk * CEFF_(y[6016]); ws[104896] = kk * CEFF_(y[3968]); }
+    { const double kk = ws[59008]; ws[104928] = kk * CEFF_(y[6016]); ws[104960] = kk * CEFF_(y[4608]); }
+    { const double kk = ws[59040]; ws[104992] = kk * CEFF_(y[6016]); ws[105024] = kk * CEFF_(y[928]); }
+    { const double kk = ws[59136]; ws[105056] = kk * CEFF_(y[6016]); ws[105088] = kk * CEFF_(y[992]); }
+    { const double kk = ws[59168]; ws[105120] = kk * CEFF_(y[5984]); ws[105152] = kk * CEFF_(y[3488]); }
+    { const double kk = ws[59200]; ws[105184] = kk * CEFF_(y[5824]); ws[105216] = kk * CEFF_(y[3488]); }
+    { const double kk = ws[59232]; ws[105248] = kk * CEFF_(y[5952]); ws[105280] = kk * CEFF_(y[3488]); }
+    { const double kk = ws[59264]; ws[105312] = kk * CEFF_(y[5888]); ws[105344] = kk * CEFF_(y[3488]); }
+    { const double kk = ws[59296]; ws[105376] = kk * CEFF_(y[5792]); ws[105408] = kk * CEFF_(y[3488]); }
+#undef CEFF_
+}
 }  // namespace mech_cracmm2

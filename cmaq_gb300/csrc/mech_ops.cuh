@@ -8,6 +8,7 @@
 #include "ebi.cuh"
 #include "adjoint.cuh"
 #include "ddm.cuh"
+#include "gear.cuh"
 
 struct MechOps {
     const char* name;
@@ -39,6 +40,15 @@ struct MechOps {
     cudaError_t (*ddm_update)(const chem::GridArgs&, const chem::DdmArgs&, int nblocks, cudaStream_t);
     cudaError_t (*rconst)(const chem::GridArgs&, double* rki, uint8_t* sunlit, int nblocks, cudaStream_t);
     cudaError_t (*occupancy)(int* blocks_per_sm);
+    int gear_ws_elems;
+    // grid: one Gear CHEM call on GridArgs; otherwise the solver-level entry on GearArgs' arrays
+    cudaError_t (*gear)(const chem::GridArgs&, const chem::QueueArgs&, const chem::GearArgs&, bool grid, int nblocks,
+                        cudaStream_t);
+    cudaError_t (*gear_occupancy)(int* blocks_per_sm);
+    // one cell per warp with its workspace in shared memory (one-warp blocks)
+    cudaError_t (*gear_warp)(const chem::GridArgs&, const chem::QueueArgs&, const chem::GearArgs&, bool grid,
+                             int nblocks, cudaStream_t);
+    cudaError_t (*gear_warp_occupancy)(int* blocks_per_sm);
 };
 
 #define DEFINE_MECH_OPS(NS, SYMBOL)                                                                 \
@@ -102,8 +112,11 @@ struct MechOps {
     size_t ebiw_smem_() { return (size_t)chem::EBIW_WPB * T_::EBIW_ELEMS * sizeof(double); }        \
     cudaError_t ebiw_attr_()                                                                        \
     {                                                                                               \
-        return cudaFuncSetAttribute(chem::k_chem_ebi_warp<T_>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                                    (int)ebiw_smem_());                                             \
+        cudaError_t r = cudaFuncSetAttribute(chem::k_chem_ebi_warp<T_>,                             \
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ebiw_smem_()); \
+        if (r != cudaSuccess) return r;                                                             \
+        return cudaFuncSetAttribute(chem::k_chem_ebi_warp<T_>, cudaFuncAttributePreferredSharedMemoryCarveout, \
+                                    (int)cudaSharedmemCarveoutMaxShared);                           \
     }                                                                                               \
     cudaError_t chem_ebi_warp_(const chem::GridArgs& a, const chem::QueueArgs& q, const chem::EbiArgs& e, \
                                int nb, cudaStream_t s)                                              \
@@ -151,6 +164,54 @@ struct MechOps {
         chem::k_rconst<T_><<<nb, chem::THREADS_PER_BLOCK, 0, s>>>(a, rki, sun);                     \
         return cudaGetLastError();                                                                  \
     }                                                                                               \
+    cudaError_t gear_(const chem::GridArgs& a, const chem::QueueArgs& q, const chem::GearArgs& g, bool grid, \
+                      int nb, cudaStream_t s)                                                       \
+    {                                                                                               \
+        if (grid) chem::k_gear<T_, true><<<nb, chem::GEAR_WPB * 32, 0, s>>>(a, q, g);               \
+        else chem::k_gear<T_, false><<<nb, chem::GEAR_WPB * 32, 0, s>>>(a, q, g);                   \
+        return cudaGetLastError();                                                                  \
+    }                                                                                               \
+    cudaError_t gear_occupancy_(int* bps)                                                           \
+    {                                                                                               \
+        int a = 0, b = 0;                                                                           \
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, chem::k_gear<T_, true>,   \
+                                                                      chem::GEAR_WPB * 32, 0);      \
+        if (e != cudaSuccess) return e;                                                             \
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, chem::k_gear<T_, false>, chem::GEAR_WPB * 32, 0); \
+        *bps = a < b ? a : b;                                                                       \
+        return e;                                                                                   \
+    }                                                                                               \
+    size_t gearw_smem_() { return (size_t)T_::GEAR_WS_ELEMS * sizeof(double); }                     \
+    template <bool G>                                                                               \
+    cudaError_t gearw_attr_()                                                                       \
+    {                                                                                               \
+        cudaError_t r = cudaFuncSetAttribute(chem::k_gear_warp<T_, G>,                              \
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gearw_smem_()); \
+        if (r != cudaSuccess) return r;                                                             \
+        return cudaFuncSetAttribute(chem::k_gear_warp<T_, G>, cudaFuncAttributePreferredSharedMemoryCarveout, \
+                                    (int)cudaSharedmemCarveoutMaxShared);                           \
+    }                                                                                               \
+    cudaError_t gear_warp_(const chem::GridArgs& a, const chem::QueueArgs& q, const chem::GearArgs& g, bool grid, \
+                           int nb, cudaStream_t s)                                                  \
+    {                                                                                               \
+        cudaError_t r = grid ? gearw_attr_<true>() : gearw_attr_<false>();                          \
+        if (r != cudaSuccess) return r;                                                             \
+        if (grid) chem::k_gear_warp<T_, true><<<nb, 32, gearw_smem_(), s>>>(a, q, g);               \
+        else chem::k_gear_warp<T_, false><<<nb, 32, gearw_smem_(), s>>>(a, q, g);                   \
+        return cudaGetLastError();                                                                  \
+    }                                                                                               \
+    cudaError_t gear_warp_occupancy_(int* bps)                                                      \
+    {                                                                                               \
+        cudaError_t r = gearw_attr_<true>();                                                        \
+        if (r == cudaSuccess) r = gearw_attr_<false>();                                             \
+        if (r != cudaSuccess) return r;                                                             \
+        int a = 0, b = 0;                                                                           \
+        r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, chem::k_gear_warp<T_, true>, 32, gearw_smem_()); \
+        if (r != cudaSuccess) return r;                                                             \
+        r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, chem::k_gear_warp<T_, false>, 32, gearw_smem_()); \
+        *bps = a < b ? a : b;                                                                       \
+        return r;                                                                                   \
+    }                                                                                               \
     cudaError_t occupancy_(int* bps)                                                                \
     {                                                                                               \
         int a = 0, b = 0;                                                                           \
@@ -170,4 +231,5 @@ struct MechOps {
                                    solve_, chem_ebi_, ebi_solve_, chem_ebi_warp_, ebi_warp_occupancy_, \
                                    T_::EBI_DELTAT,                                                  \
                                    T_::ADJ_WS_ELEMS, adj_forward_, adj_reverse_, adj_occupancy_, ddm_update_,     \
-                                   rconst_, occupancy_};
+                                   rconst_, occupancy_, T_::GEAR_WS_ELEMS, gear_, gear_occupancy_,   \
+                                   gear_warp_, gear_warp_occupancy_};

@@ -21,6 +21,8 @@ same rule, so both compute the same sums with the same roundings.
 """
 from __future__ import annotations
 
+import re
+
 from .emit_common import RATE_HELPERS, c_double
 from .fortran_tables import Mechanism
 from .rate_expr import RateProgram
@@ -68,10 +70,41 @@ class Layout:
         self.adj_ge = off; off += ns        # gradient wrt the emission tendency
         self.adj_gk = off; off += nr        # gradient wrt log rate multipliers
         self.adj_total = off
+        # SMVGEAR: CNEW, GLOSS, DTLOS, CHOLD, CEST and the gathered concentrations reuse Y,
+        # YDOT, K1, K2, K3 and F0; the Nordsieck history CONC (6 x ISCHAN) lies behind the
+        # forward workspace (only the Gear kernels, per-warp stride GEAR_WS_ELEMS, use it)
+        self.gear_conc = self.total
+        self.gear_total = self.total + 6 * sp.ischan
 
 
 def _w(k: int) -> str:
     return f"ws[{k * 32}]"
+
+
+_IDX = re.compile(r"\b(ws|yin|yout|lu|b|vd|y)\[(\d+)\]")
+_PTR = re.compile(r"\b(ws|lu|vd) \+ (\d+)\b")
+
+
+def _stride1(lines: list[str], renames: list[tuple[str, str]]) -> list[str]:
+    """The same routine for a workspace of one cell with stride 1 (a warp's shared-memory
+    copy): every element index k*32 becomes k, L2 prefetches are dropped, names get the
+    _s1 infix.  The arithmetic and its order are unchanged."""
+    def div(mm):
+        v = int(mm.group(2))
+        assert v % 32 == 0, mm.group(0)
+        return mm.group(0)[: -len(mm.group(2)) - (1 if mm.group(0).endswith("]") else 0)] + \
+            str(v // 32) + ("]" if mm.group(0).endswith("]") else "")
+    out = []
+    for ln in lines:
+        if "CHEM_PREFETCH" in ln:
+            continue
+        ln = _IDX.sub(div, ln)
+        ln = _PTR.sub(div, ln)
+        ln = ln.replace("src * 32", "src").replace("dst * 32", "dst").replace("rhs * 32", "rhs")
+        for a, b in renames:
+            ln = ln.replace(a, b)
+        out.append(ln)
+    return out
 
 
 def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src_hash: str,
@@ -88,12 +121,41 @@ def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src
     units["rates"] = _rconst(m, prog, lay)
     for d in range(2):
         units["rates"] += _feval(m, sp, lay, d) + _explic(m, sp, lay, d)
+    # SMVGEAR uses the day pattern for every cell (see csrc/gear.cuh); the warp-per-cell
+    # kernel runs stride-1 copies of its routines on the cell's shared-memory workspace
+    units["rates"] += _explic(m, sp, lay, 0, gear=True)
+    units["s1_rates"] = _stride1(_feval(m, sp, lay, 0), [("feval_0(", "feval_s1_0(")]) + \
+        _stride1(_explic(m, sp, lay, 0, gear=True), [("gear_explic_0(", "gear_explic_s1_0(")])
     decls: list[str] = ["__device__ void rconst(double* __restrict__ ws, double temp_in, double press, double h2o, "
                         "double seawater, int lsunlight, const double* __restrict__ rjv, const double* __restrict__ hetv);"]
     for d in range(2):
         decls.append(f"__device__ void feval_{d}(double* __restrict__ ws, int src, int dst);")
         decls.append(f"__device__ void explic_{d}(double* __restrict__ ws);")
+    decls.append("__device__ void gear_explic_0(double* __restrict__ ws);")
+    decls.append("__device__ void feval_s1_0(double* __restrict__ ws, int src, int dst);")
+    decls.append("__device__ void gear_explic_s1_0(double* __restrict__ ws);")
     wrappers: list[str] = []
+    for d in range(1):
+        gchunks = _jacdecomp_chunks(m, sp, lay, d, gear=True)
+        for ci, code in enumerate(gchunks):
+            units.setdefault(f"glu{d}_{ci // 3}", []).extend(code)
+            units.setdefault(f"s1_glu{d}_{ci // 3}", []).extend(
+                _stride1(code, [(f"gear_pdecomp_{d}_{ci}(", f"gear_pdecomp_s1_{d}_{ci}(")]))
+            decls.append(f"__device__ void gear_pdecomp_{d}_{ci}(double* __restrict__ ws, double r1delt);")
+            decls.append(f"__device__ void gear_pdecomp_s1_{d}_{ci}(double* __restrict__ ws, double r1delt);")
+        for infix in ("", "s1_"):
+            wrappers.append(f"__device__ __forceinline__ void gear_pdecomp_{infix}{d}(double* __restrict__ ws, double r1delt)")
+            wrappers.append("{")
+            wrappers.extend(f"    gear_pdecomp_{infix}{d}_{ci}(ws, r1delt);" for ci in range(len(gchunks)))
+            wrappers.append("}")
+        schunks = _solve_chunks(sp, lay, d)
+        for ci, code in enumerate(schunks):
+            units.setdefault(f"s1_solve{d}", []).extend(_stride1(code, [(f"solve_{d}_{ci}(", f"solve_s1_{d}_{ci}(")]))
+            decls.append(f"__device__ void solve_s1_{d}_{ci}(double* __restrict__ ws, int rhs);")
+        wrappers.append(f"__device__ __forceinline__ void solve_s1_{d}(double* __restrict__ ws, int rhs)")
+        wrappers.append("{")
+        wrappers.extend(f"    solve_s1_{d}_{ci}(ws, rhs);" for ci in range(len(schunks)))
+        wrappers.append("}")
     for d in range(2):
         chunks = _jacdecomp_chunks(m, sp, lay, d)
         for ci, code in enumerate(chunks):
@@ -188,6 +250,9 @@ def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src
               ("ADJ_MU2", lay.adj_mu2), ("ADJ_MU3", lay.adj_mu3), ("ADJ_PHI", lay.adj_phi),
               ("ADJ_TMP", lay.adj_tmp), ("ADJ_EMIS", lay.adj_emis), ("ADJ_GE", lay.adj_ge),
               ("ADJ_GK", lay.adj_gk), ("OFF_YAVE", lay.yave),
+              ("GEAR_WS_ELEMS", lay.gear_total), ("GEAR_CNEW", lay.y), ("GEAR_GLOSS", lay.ydot),
+              ("GEAR_DTLOS", lay.k1), ("GEAR_CHOLD", lay.k2), ("GEAR_CEST", lay.k3), ("GEAR_BLKCONC", lay.f0),
+              ("GEAR_CONC", lay.gear_conc),
               # warp-cooperative EBI: one cell's state in shared memory (doubles)
               ("EBIW_YC", 0), ("EBIW_YC0", ns), ("EBIW_YCP", 2 * ns), ("EBIW_PROD", 3 * ns),
               ("EBIW_LOSS", 4 * ns), ("EBIW_PNEG", 5 * ns), ("EBIW_NOTMAX", 6 * ns), ("EBIW_RKI", 7 * ns),
@@ -216,6 +281,13 @@ def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src
     for d in range(2):
         h.append(f"    static __device__ __forceinline__ void feval_{d}(double* ws, int s, int t) {{ {ns_name}::feval_{d}(ws, s, t); }}")
         h.append(f"    static __device__ __forceinline__ void explic_{d}(double* ws) {{ {ns_name}::explic_{d}(ws); }}")
+        if d == 0:
+            h.append(f"    static __device__ __forceinline__ void gear_explic_0(double* ws) {{ {ns_name}::gear_explic_0(ws); }}")
+            h.append(f"    static __device__ __forceinline__ void gear_pdecomp_0(double* ws, double r) {{ {ns_name}::gear_pdecomp_0(ws, r); }}")
+            h.append(f"    static __device__ __forceinline__ void feval_s1_0(double* ws, int s, int t) {{ {ns_name}::feval_s1_0(ws, s, t); }}")
+            h.append(f"    static __device__ __forceinline__ void gear_explic_s1_0(double* ws) {{ {ns_name}::gear_explic_s1_0(ws); }}")
+            h.append(f"    static __device__ __forceinline__ void gear_pdecomp_s1_0(double* ws, double r) {{ {ns_name}::gear_pdecomp_s1_0(ws, r); }}")
+            h.append(f"    static __device__ __forceinline__ void solve_s1_0(double* ws, int r) {{ {ns_name}::solve_s1_0(ws, r); }}")
         h.append(f"    static __device__ __forceinline__ void jacdecomp_{d}(double* ws, double g) {{ {ns_name}::jacdecomp_{d}(ws, g); }}")
         h.append(f"    static __device__ __forceinline__ void solve_{d}(double* ws, int r) {{ {ns_name}::solve_{d}(ws, r); }}")
         h.append(f"    static __device__ __forceinline__ void jacdecomp_{d}_sync(double* ws, double g, bool go) {{ {ns_name}::jacdecomp_{d}_sync(ws, g, go); }}")
@@ -328,26 +400,36 @@ def _ex_ref(m: Mechanism, sp: SparseMech, lay: Layout, r: int, ial: int) -> str:
     return _w(lay.ex[(r, ial)])
 
 
-def _explic(m: Mechanism, sp: SparseMech, lay: Layout, d: int) -> list[str]:
-    o = [f"// Partial-derivative products of 2- and 3-reactant reactions (rbjacob.F:112-143).",
-         f"__device__ __noinline__ void explic_{d}(double* __restrict__ ws)",
+def _explic(m: Mechanism, sp: SparseMech, lay: Layout, d: int, gear: bool = False) -> list[str]:
+    """Partial-derivative products of 2- and 3-reactant reactions into the EX slots.  gear:
+    SMVGEAR's form, with concentrations at or below ZBOUND = 1e-30 taken as zero
+    (CEFF of grpderiv.F:147-155, products of :163-189)."""
+    name = f"gear_explic_{d}" if gear else f"explic_{d}"
+    src = "grpderiv.F:163-189" if gear else "rbjacob.F:112-143"
+    o = [f"// Partial-derivative products of 2- and 3-reactant reactions ({src}).",
+         f"__device__ __noinline__ void {name}(double* __restrict__ ws)",
          "{",
          f"    const double* __restrict__ y = ws + {lay.y * 32};"]
+    if gear:
+        o.append("#define CEFF_(v) ((v) <= 1.0e-30 ? 0.0 : (v))")
     for r in sp.active[d]:
         nre = m.nreact[r]
         k = _w(lay.rki + r)
+        wrap = (lambda e: f"CEFF_({e})") if gear else (lambda e: e)
         if nre == 2:
-            y1 = f"y[{sp.irm2[r][0] * 32}]"
-            y2 = f"y[{sp.irm2[r][1] * 32}]"
+            y1 = wrap(f"y[{sp.irm2[r][0] * 32}]")
+            y2 = wrap(f"y[{sp.irm2[r][1] * 32}]")
             o.append(f"    {{ const double kk = {k}; {_w(lay.ex[(r, 0)])} = kk * {y2}; {_w(lay.ex[(r, 1)])} = kk * {y1}; }}")
         elif nre == 3:
-            y1 = f"y[{sp.irm2[r][0] * 32}]"
-            y2 = f"y[{sp.irm2[r][1] * 32}]"
-            y3 = f"y[{sp.irm2[r][2] * 32}]"
+            y1 = wrap(f"y[{sp.irm2[r][0] * 32}]")
+            y2 = wrap(f"y[{sp.irm2[r][1] * 32}]")
+            y3 = wrap(f"y[{sp.irm2[r][2] * 32}]")
             o.append(f"    {{ const double kk = {k}; const double cr2 = kk * {y2};"
                      f" {_w(lay.ex[(r, 0)])} = cr2 * {y3};"
                      f" {_w(lay.ex[(r, 1)])} = (kk * {y1}) * {y3};"
                      f" {_w(lay.ex[(r, 2)])} = cr2 * {y1}; }}")
+    if gear:
+        o.append("#undef CEFF_")
     o.append("}")
     return o
 
@@ -366,10 +448,14 @@ def _jac_terms(m: Mechanism, sp: SparseMech, d: int) -> dict[int, list[tuple]]:
 JAC_CHUNK_OPS = 200     # elimination ops per generated function; bounds ptxas time and register spills
 
 
-def _jacdecomp_chunks(m: Mechanism, sp: SparseMech, lay: Layout, d: int) -> list[list[str]]:
+def _jacdecomp_chunks(m: Mechanism, sp: SparseMech, lay: Layout, d: int, gear: bool = False) -> list[list[str]]:
     """Jacobian - I/(gamma h) and its LU factors, row by row.  Each entry receives the same
     updates in the same order as the column-ordered elimination of rbdecomp.F; L is stored
-    scaled by 1/U(k,k) and VDIAG = 1/U(i,i).  Rows are grouped into functions of bounded size."""
+    scaled by 1/U(k,k) and VDIAG = 1/U(i,i).  Rows are grouped into functions of bounded size.
+    gear: SMVGEAR's predictor matrix P = I - ASN1*DELT*J instead (grpderiv.F:131-226: every
+    entry starts at 0, the diagonal at 1, and takes R1DELT = -ASN1*DELT times each
+    partial-derivative term in PDERIV's order), factored by the same elimination
+    (grdecomp.F is rbdecomp.F)."""
     n = sp.ischan
     jpt = sp.jarraypt[d]
     terms = _jac_terms(m, sp, d)
@@ -398,6 +484,17 @@ def _jacdecomp_chunks(m: Mechanism, sp: SparseMech, lay: Layout, d: int) -> list
             st = jpt[(i, j)]
             tl = terms.get(st, [])
             var = f"a{j}"
+            if gear:
+                o.append(f"      double {var} = {'1.0' if j == i else '0.0'};")
+                for (r, ial, coef, sign) in tl:
+                    ex = _ex_ref(m, sp, lay, r, ial)
+                    if sign < 0:
+                        o.append(f"      {var} = fma(-r1delt, {ex}, {var});")
+                    elif coef is None:
+                        o.append(f"      {var} = fma(r1delt, {ex}, {var});")
+                    else:
+                        o.append(f"      {var} = fma({c_double(coef)} * r1delt, {ex}, {var});")
+                continue
             if not tl:
                 o.append(f"      double {var} = 0.0;")
                 continue
@@ -418,7 +515,8 @@ def _jacdecomp_chunks(m: Mechanism, sp: SparseMech, lay: Layout, d: int) -> list
                     o.append(f"      {var} = {var} + {ex};")
                 else:
                     o.append(f"      {var} = fma({c_double(coef)}, {ex}, {var});")
-        o.append(f"      a{i} = a{i} - gdtinv;")
+        if not gear:
+            o.append(f"      a{i} = a{i} - gdtinv;")
         for (st_ik, k) in lower:
             o.append(f"      a{k} = a{k} * CHEM_LDLU(vd + {k * 32});")
             o.append(f"      lu[{st_ik * 32}] = a{k};")
@@ -440,7 +538,9 @@ def _jacdecomp_chunks(m: Mechanism, sp: SparseMech, lay: Layout, d: int) -> list
         chunks.append(cur)
     out = []
     for ci, ch in enumerate(chunks):
-        f = [f"__device__ __noinline__ void jacdecomp_{d}_{ci}(double* __restrict__ ws, double gdtinv)", "{",
+        sig = f"gear_pdecomp_{d}_{ci}(double* __restrict__ ws, double r1delt)" if gear else \
+            f"jacdecomp_{d}_{ci}(double* __restrict__ ws, double gdtinv)"
+        f = [f"__device__ __noinline__ void {sig}", "{",
              f"    double* __restrict__ lu = ws + {lay.lu * 32};",
              f"    double* __restrict__ vd = ws + {lay.vdiag * 32};"]
         for code in ch:

@@ -6,6 +6,7 @@
  *     SUBROUTINE CHEM( CONC, JDATE, JTIME, TSTEP )
  *         CCTM/src/gas/ros3/rbdriver.F:20-785          (ROS3 solver)
  *         CCTM/src/gas/ebi_cb6r5_ae7_aq/hrdriver.F:20  (EBI solver)
+ *         CCTM/src/gas/smvgear/grdriver.F:16           (SMVGEAR solver)
  *     called once per synchronisation step from CCTM/src/driver/sciproc.F:298
  *
  * The operator's implicit inputs, which the Fortran reads through modules, are
@@ -40,6 +41,7 @@ extern "C" {
 
 #define CMAQCHEM_SOLVER_ROS3 0
 #define CMAQCHEM_SOLVER_EBI 1
+#define CMAQCHEM_SOLVER_GEAR 2   /* SMVGEAR; cfg.rtol = REAL(GEAR_RTOL, 8), cfg.atol = REAL(GEAR_MIN_ATOL, 8) */
 
 /* How cells are scheduled on the GPU; every mode integrates each cell with its own
  * step size (the reference with BLKSIZE = 1). */
@@ -67,7 +69,8 @@ typedef struct {
 } cmaqchem_cfg;
 
 /* With CMAQCHEM_SOLVER_EBI, accepted_steps counts Backward-Euler iterations and
- * rejected_steps / sunlit_attempts stay 0. */
+ * rejected_steps / sunlit_attempts stay 0.  With CMAQCHEM_SOLVER_GEAR, rejected_steps
+ * counts corrector convergence failures plus error-test failures. */
 typedef struct {
     long long accepted_steps;  /* summed over cells */
     long long rejected_steps;
@@ -153,6 +156,23 @@ int cmaqchem_ros3_solve_device(cmaqchem_handle* h, long long ncell, double* y, c
  * (CMAQCHEM_CELL_* bits) and Backward-Euler iteration counts may be NULL. */
 int cmaqchem_ebi_solve_device(cmaqchem_handle* h, long long ncell, double* yc, const double* rki,
                               int tstep_sec, int* status, int* iterations, void* stream);
+
+/* Solver-level entry replacing SMVGEAR (CCTM/src/gas/smvgear/grsmvgear.F:26) for cells with
+ * given rate constants, one cell per block (BLKSIZE = 1), device arrays: y[nspec][ncell]
+ * in the solver's species order (ppm), updated in place; rk[nrxns][ncell];
+ * night[ncell] = 1 for cells without sunlight (night reaction list, HMAXNIT, H0FAC = 1).
+ * The handle must have been made with CMAQCHEM_SOLVER_GEAR.  cell_stats (may be NULL)
+ * receives per cell 8 ints: accepted steps, convergence failures, error-test failures,
+ * Jacobian evaluations, right-hand-side evaluations, Newton starts, highest order used
+ * and status (CMAQCHEM_CELL_* bits). */
+int cmaqchem_gear_solve_device(cmaqchem_handle* h, long long ncell, double* y, const double* rk,
+                               const unsigned char* night, double chemstep_min, int* cell_stats, void* stream);
+
+/* SMVGEAR tolerances of a CMAQCHEM_SOLVER_GEAR handle, as the run-time settings
+ * GEAR_MAX_ATOL, GEAR_MIN_ATOL and GEAR_CONC_FLOOR (ppmV, REAL(4); defaults 1e-7,
+ * cfg.atol and 1e-12) from which OPTIMAL_ATOL_PPM picks each cell's absolute tolerance
+ * (CCTM/src/gas/smvgear/GRVARS.F:597-708).  max_atol > min_atol > conc_floor. */
+int cmaqchem_gear_tolerances(cmaqchem_handle* h, float max_atol, float min_atol, float conc_floor);
 
 /* Discrete adjoint of RBSOLVER (no reference counterpart; the reference's gradient
  * tool is the forward DDM-3D of CCTM/src/ddm3d/DDM3D_CHEM.F).  Solver-level, device

@@ -69,6 +69,8 @@ def load(mech: str = "cb6r5_ae7_aq") -> C.CDLL:
     lib.oracle_gear_cfg.restype = None
     lib.oracle_gear_cells.argtypes = [C.c_long, C.c_double, C.c_void_p, dp, dp, u8p, ip, C.c_int]
     lib.oracle_gear_chem.argtypes = [C.POINTER(OracleChemArgs), C.c_void_p]
+    lib.oracle_gear_pow.argtypes = [C.c_double, C.c_double]
+    lib.oracle_gear_pow.restype = C.c_double
     lib.oracle_set_dtmin.argtypes = [C.c_double]
     lib.oracle_get_dtmin.restype = C.c_double
     return lib

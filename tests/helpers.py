@@ -74,3 +74,19 @@ def rel_err(a, b, floor=1e-10):
     if not m.any():
         return 0.0
     return float(np.max(np.abs(a[m] - b[m]) / np.maximum(np.abs(b[m]), floor)))
+
+
+def writeback(g: GridInputs, o, y):
+    """CONC after a CHEM call whose per-cell solver results are y [nspec, n] (solver order):
+    the REAL(4) write-back of rbdriver.F:577-595 / grdriver.F:577-596."""
+    man = manifest(g.mech)
+    n = g.ncell
+    out = g.conc.reshape(g.nspcsd, n).copy()
+    dens = g.dens.reshape(n).astype(np.float64)
+    for s, sp in enumerate(man["species"]):
+        v = y[o.iold2new[s]]
+        if sp["convert"]:
+            fwd = F32(F32(F32(1.0e-3) * F32(28.9628)) / F32(sp["molwt"]))
+            v = (np.float64(F32(1.0) / fwd) * dens) * v
+        out[g.cgrid_index[s] - 1] = v.astype(F32)
+    return out.reshape(g.conc.shape)

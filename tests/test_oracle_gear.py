@@ -15,7 +15,7 @@ be compiled here, so the restatement is pinned by properties:
 import numpy as np
 import pytest
 
-from helpers import gather_cells
+from helpers import gather_cells, writeback
 from cmaq_gb300.synthetic import make_grid
 
 F32 = np.float32
@@ -53,19 +53,7 @@ def test_chem_blksize1_equals_per_cell_solver(case):
     conc, tot = o.chem_gear(g, tstep_sec=300, blksize=1, threads=4)
     assert tot["rc"] == 0
     y, st = o.gear_cells(case["y0"], case["rk"], case["night"], 5.0, threads=4)
-    # write-back of the per-cell results as grdriver.F:577-596 does
-    from cmaq_gb300.synthetic import manifest
-    man = manifest(g.mech)
-    n = g.ncell
-    want = g.conc.reshape(g.nspcsd, n).copy()
-    dens = g.dens.reshape(n).astype(np.float64)
-    for s, sp in enumerate(man["species"]):
-        v = y[o.iold2new[s]]
-        if sp["convert"]:
-            fwd = F32(F32(F32(1.0e-3) * F32(28.9628)) / F32(sp["molwt"]))
-            v = (np.float64(F32(1.0) / fwd) * dens) * v
-        want[g.cgrid_index[s] - 1] = v.astype(F32)
-    assert np.array_equal(conc.reshape(g.nspcsd, n), want)
+    assert np.array_equal(conc, writeback(g, o, y))
     assert tot["nsteps"] == int(st[:, 0].sum())
 
 
@@ -89,3 +77,22 @@ def test_gear_coefficients():
     for q in range(7):
         assert enqq[0, q] == float(F32(0.5) / F32(q + 1))
         assert enqq[2, q] == float(F32(0.5) / F32(q + 3))
+
+
+def test_gear_pow_accuracy():
+    """The portable x**y shared by the oracle and the device (exp(y log x) from series)
+    against libm's pow over the step-size estimates' range: x = DER/E from 1e-30 to 1e12,
+    y = the REAL(4) ENQQ1-3 exponents."""
+    from oracle import Oracle
+    lib = Oracle("cb6r5_ae7_aq").lib
+    rng = np.random.default_rng(5)
+    xs = np.concatenate([10.0 ** rng.uniform(-30, 12, 4000), [1.0, 0.5, 2.0, 1e-300, 7.0]])
+    ys = [float(F32(0.5) / F32(q)) for q in range(1, 10)]
+    worst = 0.0
+    for y in ys:
+        for x in xs:
+            ref = float(np.power(x, y))
+            err = abs(lib.oracle_gear_pow(float(x), y) - ref) / ref
+            worst = max(worst, err / max(1.0, abs(y * np.log(x))))
+    assert worst < 4e-16
+    assert lib.oracle_gear_pow(0.0, 0.25) == 0.0
