@@ -130,17 +130,41 @@ static __device__ double gpow(double x, double y)
 }
 
 // The state machine below runs in two forms.  S = 32, COOP = false: one cell per lane on
-// the per-warp workspace ([element][lane]).  S = 1, COOP = true: one cell per warp on the
-// warp's shared-memory copy of the cell's workspace; element-wise species loops are spread
-// over the lanes (LOOP, then SYNC), while every lane runs the control flow, the reductions
-// (in the reference's order) and the generated routines itself, so all lanes hold the same
-// state and write the same values.  Both forms perform the same operations in the same
-// order on every element.
+// the per-warp workspace ([element][lane]), calling the generated routines.  S = 1,
+// COOP = true: one cell per warp on the warp's shared-memory copy of the cell's workspace;
+// element-wise species loops are spread over the lanes (LOOP, then SYNC) and the f
+// evaluation, P and its LU and the solves run in table-driven cooperative forms
+// (coop_feval, coop_pdecomp, coop_solve), while every lane runs the control flow and the
+// reductions (in the reference's order) itself, so all lanes hold the same state.  Both
+// forms perform the same operations in the same order on every element.
 #define GW(off) ws[(off) * S]
 #define LOOP(i, n) for (int i = (COOP ? (int)(threadIdx.x & 31) : 0); i < (n); i += (COOP ? 32 : 1))
 #define SYNC()                 \
     do {                       \
         if (COOP) __syncwarp(); \
+    } while (0)
+
+// Sum over species of e_j * e_j in species order (fma chain), e_j = EXPR(j).  Cooperative
+// form: the lanes form the e_j into the scratch array GEAR_E first, then every lane runs
+// the chain; the same products and the same order either way.
+#define REDUCE_SQ(result, EXPR)                                                              \
+    do {                                                                                     \
+        double dely_ = 0.0;                                                                  \
+        if (COOP) {                                                                          \
+            SYNC();                                                                          \
+            LOOP(j, isc) GW(M::GEAR_E + j) = (EXPR);                                         \
+            SYNC();                                                                          \
+            for (int j = 0; j < isc; ++j) {                                                  \
+                const double e_ = GW(M::GEAR_E + j);                                         \
+                dely_ = fma(e_, e_, dely_);                                                  \
+            }                                                                                \
+        } else {                                                                             \
+            for (int j = 0; j < isc; ++j) {                                                  \
+                const double e_ = (EXPR);                                                    \
+                dely_ = fma(e_, e_, dely_);                                                  \
+            }                                                                                \
+        }                                                                                    \
+        result = dely_;                                                                      \
     } while (0)
 
 // OPTIMAL_ATOL_PPM (GRVARS.F:670-706) for one cell
@@ -264,11 +288,8 @@ loop_initialize:
 init_post:
     {
         const double yloweps = s.ylowa / epslow;
-        double dely = 0.0;
-        for (int j = 0; j < isc; ++j) {
-            const double e = GL(j) / (CN(j) + yloweps);
-            dely = fma(e, e, dely);
-        }
+        double dely;
+        REDUCE_SQ(dely, GL(j) / (CN(j) + yloweps));
         const double rmstop = dely > 0.0 ? dely : 0.0;
         double delt = sqrt(epslow / (abst2 + rmstop / order)) * h0fac;
         delt = min2(delt, chemstep);
@@ -377,11 +398,8 @@ iter_post:
             CN(i) = fma(asn1, d, CO(i));
         }
         SYNC();
-        double dely = 0.0;
-        for (int i = 0; i < isc; ++i) {
-            const double e = GL(i) * CH(i);
-            dely = fma(e, e, dely);
-        }
+        double dely;
+        REDUCE_SQ(dely, GL(j) * CH(j));
         const double rmserrp = s.rmserr;
         s.der2max = dely > 0.0 ? dely : 0.0;
         s.rmserr = sqrt(s.der2max / order);
@@ -410,11 +428,8 @@ iter_post:
 converged:
     s.jeval = 0;
     if (s.l3 > 1) {
-        double dely = 0.0;
-        for (int j = 0; j < isc; ++j) {
-            const double e = DT(j) * CH(j);
-            dely = fma(e, e, dely);
-        }
+        double dely;
+        REDUCE_SQ(dely, DT(j) * CH(j));
         s.der2max = dely > 0.0 ? dely : 0.0;
     }
     if (s.der2max > s.enqq) {
@@ -481,11 +496,8 @@ converged:
     // step size and order of the next step (grsmvgear.F:893-995)
     if (s.higher_order) {
         if (s.nqq < MAXORD) {
-            double dely = 0.0;
-            for (int j = 0; j < isc; ++j) {
-                const double e = (DT(j) - CE(j)) * CH(j);
-                dely = fma(e, e, dely);
-            }
+            double dely;
+            REDUCE_SQ(dely, (DT(j) - CE(j)) * CH(j));
             const double der3max = dely > 0.0 ? dely : 0.0;
             const double pr3 = (double)1.4f * gpow(der3max / s.eup, K->enqq3[s.nqq - 1]);
             s.rdeltup = 1.0 / (pr3 + OPT4MIC);
@@ -499,12 +511,9 @@ converged:
         const double rdeltsm = 1.0 / (pr2 + OPT2MIC);
         double rdeltdn = 0.0;
         if (s.nqq > 1) {
-            double dely = 0.0;
+            double dely;
             const int col = (s.kstep - 1) * isc;
-            for (int j = 0; j < isc; ++j) {
-                const double e = CO(col + j) * CH(j);
-                dely = fma(e, e, dely);
-            }
+            REDUCE_SQ(dely, CO(col + j) * CH(j));
             const double der1max = dely > 0.0 ? dely : 0.0;
             const double pr1 = 1.3 * gpow(der1max / s.edwn, K->enqq1[s.nqq - 1]);
             rdeltdn = 1.0 / (pr1 + OPT3MIC);
@@ -537,6 +546,152 @@ converged:
 #undef ASET
 }
 
+// ---- warp-cooperative forms of the generated routines (one cell per warp, workspace in
+// shared memory with stride 1), driven by the generator's gw tables.  Each element gets
+// the same operations in the same order as in the generated sequential code.
+
+// GLOSS = f(CNEW): rates over the lanes, then each species' terms in RBFEVAL's order by
+// the lane the species is assigned to
+template <class M>
+__device__ void coop_feval(double* __restrict__ ws)
+{
+    const int lane = threadIdx.x & 31;
+    const int* ar = M::gw_act_r();
+    const int* asp = M::gw_act_sp();
+    for (int t = lane; t < M::GW_NACT; t += 32) {
+        double x = ws[M::OFF_RKI + ar[t]];
+        const int s0 = asp[3 * t], s1 = asp[3 * t + 1], s2 = asp[3 * t + 2];
+        if (s0 >= 0) x = x * ws[M::GEAR_CNEW + s0];
+        if (s1 >= 0) x = x * ws[M::GEAR_CNEW + s1];
+        if (s2 >= 0) x = x * ws[M::GEAR_CNEW + s2];
+        ws[M::OFF_RXRAT + ar[t]] = x;
+    }
+    __syncwarp();
+    const int* lp = M::gw_lane_ptr();
+    const int* ls = M::gw_lane_sp();
+    const int* sptr = M::gw_sum_ptr();
+    const int* sr = M::gw_sum_r();
+    const int* sk = M::gw_sum_k();
+    const double* sc = M::gw_sum_c();
+    for (int u = lp[lane]; u < lp[lane + 1]; ++u) {
+        const int sp = ls[u];
+        const int t0 = sptr[sp], t1 = sptr[sp + 1];
+        double a = 0.0;
+        if (t0 < t1) {
+            const double r0 = ws[M::OFF_RXRAT + sr[t0]];
+            a = sk[t0] ? sc[t0] * r0 : -r0;
+            for (int t = t0 + 1; t < t1; ++t) {
+                const double rr = ws[M::OFF_RXRAT + sr[t]];
+                a = sk[t] ? fma(sc[t], rr, a) : a - rr;
+            }
+        }
+        ws[M::GEAR_GLOSS + sp] = a;
+    }
+    __syncwarp();
+}
+
+// P = I - ASN1*DELT*J at CNEW and its LU factors: EXPLIC and the assembly over the lanes,
+// then the elimination pivot by pivot (L entries of the pivot's column scaled, then its
+// updates, each over the lanes)
+template <class M>
+__device__ void coop_pdecomp(double* __restrict__ ws, double r1delt)
+{
+    const int lane = threadIdx.x & 31;
+    const int* xr = M::gw_ex_r();
+    const int* xs = M::gw_ex_sp();
+    const int* xo = M::gw_ex_off();
+#define CEFF_(v) ((v) <= 1.0e-30 ? 0.0 : (v))
+    for (int t = lane; t < M::GW_NEX; t += 32) {
+        const double kk = ws[M::OFF_RKI + xr[t]];
+        const double y1 = CEFF_(ws[M::GEAR_CNEW + xs[3 * t]]);
+        const double y2 = CEFF_(ws[M::GEAR_CNEW + xs[3 * t + 1]]);
+        const int o = xo[t];
+        if (xs[3 * t + 2] < 0) {
+            ws[o] = kk * y2;
+            ws[o + 1] = kk * y1;
+        } else {
+            const double y3 = CEFF_(ws[M::GEAR_CNEW + xs[3 * t + 2]]);
+            const double cr2 = kk * y2;
+            ws[o] = cr2 * y3;
+            ws[o + 1] = (kk * y1) * y3;
+            ws[o + 2] = cr2 * y1;
+        }
+    }
+#undef CEFF_
+    __syncwarp();
+    double* __restrict__ lu = ws + M::OFF_LU;
+    double* __restrict__ vd = ws + M::OFF_VDIAG;
+    const int* ap = M::gw_asm_ptr();
+    const int* asrc = M::gw_asm_src();
+    const int* ak = M::gw_asm_kind();
+    const double* ac = M::gw_asm_c();
+    constexpr int NST = M::IARRAY_DAY;
+    for (int st = lane + 1; st <= NST; st += 32) {
+        double a = st > NST - M::ISCHAN ? 1.0 : 0.0;   // the diagonal is stored last
+        for (int t = ap[st]; t < ap[st + 1]; ++t) {
+            const double ex = ws[asrc[t]];
+            const int k = ak[t];
+            a = k < 0 ? fma(-r1delt, ex, a) : (k == 0 ? fma(r1delt, ex, a) : fma(ac[t] * r1delt, ex, a));
+        }
+        lu[st] = a;
+    }
+    __syncwarp();
+    const int* pd = M::gw_piv_diag();
+    const int* lsp = M::gw_lsc_ptr();
+    const int* lst = M::gw_lsc_st();
+    const int* upp = M::gw_up_ptr();
+    const int* uij = M::gw_up_ij();
+    const int* uik = M::gw_up_ik();
+    const int* ukj = M::gw_up_kj();
+    for (int k = 0; k < M::ISCHAN; ++k) {
+        const double v = 1.0 / lu[pd[k]];
+        vd[k] = v;
+        for (int t = lsp[k] + lane; t < lsp[k + 1]; t += 32) lu[lst[t]] = lu[lst[t]] * v;
+        __syncwarp();
+        for (int t = upp[k] + lane; t < upp[k + 1]; t += 32) lu[uij[t]] = fma(-lu[uik[t]], lu[ukj[t]], lu[uij[t]]);
+        __syncwarp();
+    }
+}
+
+// forward then backward substitution in place at ws[rhs], rows of a dependency level over
+// the lanes, each row's terms in RBSOLVE's order
+template <class M>
+__device__ void coop_solve(double* __restrict__ ws, int rhs)
+{
+    const int lane = threadIdx.x & 31;
+    const double* __restrict__ lu = ws + M::OFF_LU;
+    const double* __restrict__ vd = ws + M::OFF_VDIAG;
+    double* __restrict__ b = ws + rhs;
+    const int* flp = M::gw_fl_ptr();
+    const int* flr = M::gw_fl_row();
+    const int* frp = M::gw_fr_ptr();
+    const int* frs = M::gw_fr_st();
+    const int* frc = M::gw_fr_col();
+    for (int l = 0; l < M::GW_NFL; ++l) {
+        for (int u = flp[l] + lane; u < flp[l + 1]; u += 32) {
+            const int i = flr[u];
+            double x = b[i];
+            for (int t = frp[i]; t < frp[i + 1]; ++t) x = fma(-lu[frs[t]], b[frc[t]], x);
+            b[i] = x;
+        }
+        __syncwarp();
+    }
+    const int* blp = M::gw_bl_ptr();
+    const int* blr = M::gw_bl_row();
+    const int* brp = M::gw_br_ptr();
+    const int* brs = M::gw_br_st();
+    const int* brc = M::gw_br_col();
+    for (int l = 0; l < M::GW_NBL; ++l) {
+        for (int u = blp[l] + lane; u < blp[l + 1]; u += 32) {
+            const int i = blr[u];
+            double x = b[i];
+            for (int t = brp[i]; t < brp[i + 1]; ++t) x = fma(-lu[brs[t]], b[brc[t]], x);
+            b[i] = x * vd[i];
+        }
+        __syncwarp();
+    }
+}
+
 // The f evaluation a cell asked for, with its predictor matrix first and its corrector
 // solve after (day pattern, see the file comment).
 template <class M, int S, bool COOP>
@@ -544,15 +699,14 @@ __device__ __forceinline__ void evaluate(double* __restrict__ ws, const State& s
 {
     if (go && s.need_jac) {
         if (COOP) {
-            M::gear_explic_s1_0(ws);
-            M::gear_pdecomp_s1_0(ws, s.r1delt);
+            coop_pdecomp<M>(ws, s.r1delt);
         } else {
             M::gear_explic_0(ws);
             M::gear_pdecomp_0(ws, s.r1delt);
         }
     }
     if (go) {
-        if (COOP) M::feval_s1_0(ws, M::GEAR_CNEW, M::GEAR_GLOSS);
+        if (COOP) coop_feval<M>(ws);
         else M::feval_0(ws, M::GEAR_CNEW, M::GEAR_GLOSS);
         SYNC();
         LOOP(i, M::ISCHAN) {   // SUBFUN's floor (grsubfun.F:164-171)
@@ -568,11 +722,12 @@ __device__ __forceinline__ void evaluate(double* __restrict__ ws, const State& s
             g = fma(delt, g, -(GW(M::GEAR_CONC + M::ISCHAN + i) + GW(M::GEAR_DTLOS + i)));
         }
         SYNC();
-        if (COOP) M::solve_s1_0(ws, M::GEAR_GLOSS);
+        if (COOP) coop_solve<M>(ws, M::GEAR_GLOSS);
         else M::solve_0(ws, M::GEAR_GLOSS);
         SYNC();
     }
 }
+#undef REDUCE_SQ
 #undef LOOP
 #undef SYNC
 #undef GW
@@ -690,11 +845,11 @@ __global__ void __launch_bounds__(GEAR_WPB * 32, GEAR_WARPS_PER_SM / GEAR_WPB) k
 
 // One cell per warp, the cell's workspace in shared memory (GEAR_WS_ELEMS doubles,
 // stride 1; dynamic shared memory of that size per one-warp block): the lanes share the
-// element-wise work of the state machine and all run the generated routines (stride-1
-// copies), so a cell advances at shared-memory rather than L2 latency.  SMVGEAR's
-// stiffest cells need tens of thousands of Newton iterations in one call, and a call lasts
-// as long as its slowest cell.  Cells come from the work queue; results equal k_gear's
-// bit for bit.
+// cell's element-wise work, f evaluation, LU and solves.  SMVGEAR's stiffest cells need
+// tens of thousands of Newton iterations in one call, a call lasts as long as its slowest
+// cell, and on this GPU one FP64 warp instruction takes 64 cycles whatever its number of
+// active lanes, so a lone cell must spread its FP64 work over the lanes to advance.
+// Cells come from the work queue; results equal k_gear's bit for bit.
 template <class M, bool GRID>
 __global__ void __launch_bounds__(32) k_gear_warp(GridArgs a, QueueArgs q, GearArgs g)
 {

@@ -65,6 +65,7 @@ constexpr int GEAR_CHOLD = 745;
 constexpr int GEAR_CEST = 894;
 constexpr int GEAR_BLKCONC = 447;
 constexpr int GEAR_CONC = 4265;
+constexpr int GEAR_E = 149;
 constexpr int EBIW_YC = 0;
 constexpr int EBIW_YC0 = 149;
 constexpr int EBIW_YCP = 298;
@@ -90,71 +91,36 @@ __device__ void explic_0(double* __restrict__ ws);
 __device__ void feval_1(double* __restrict__ ws, int src, int dst);
 __device__ void explic_1(double* __restrict__ ws);
 __device__ void gear_explic_0(double* __restrict__ ws);
-__device__ void feval_s1_0(double* __restrict__ ws, int src, int dst);
-__device__ void gear_explic_s1_0(double* __restrict__ ws);
 __device__ void gear_pdecomp_0_0(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_0(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_1(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_1(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_2(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_2(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_3(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_3(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_4(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_4(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_5(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_5(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_6(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_6(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_7(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_7(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_8(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_8(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_9(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_9(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_10(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_10(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_11(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_11(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_12(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_12(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_13(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_13(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_14(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_14(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_15(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_15(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_16(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_16(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_17(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_17(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_18(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_18(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_19(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_19(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_20(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_20(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_21(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_21(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_22(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_22(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_23(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_23(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_24(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_24(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_25(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_25(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_26(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_26(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_27(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_27(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_28(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_28(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_29(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_29(double* __restrict__ ws, double r1delt);
-__device__ void solve_s1_0_0(double* __restrict__ ws, int rhs);
-__device__ void solve_s1_0_1(double* __restrict__ ws, int rhs);
-__device__ void solve_s1_0_2(double* __restrict__ ws, int rhs);
 __device__ void jacdecomp_0_0(double* __restrict__ ws, double gdtinv);
 __device__ void jacdecomp_0_1(double* __restrict__ ws, double gdtinv);
 __device__ void jacdecomp_0_2(double* __restrict__ ws, double gdtinv);
@@ -302,6 +268,38 @@ __device__ void ddm_src_1_2(double* __restrict__ ws, const unsigned char* __rest
 __device__ void ddm_src_1_3(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
 __device__ void ddm_src_1_4(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
 __device__ void ddm_src_1_5(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+extern __device__ const int c_gw_act_r[349];
+extern __device__ const int c_gw_act_sp[1047];
+extern __device__ const int c_gw_sum_ptr[150];
+extern __device__ const int c_gw_sum_r[1738];
+extern __device__ const int c_gw_sum_k[1738];
+extern __device__ const int c_gw_lane_ptr[33];
+extern __device__ const int c_gw_lane_sp[149];
+extern __device__ const int c_gw_ex_r[268];
+extern __device__ const int c_gw_ex_sp[804];
+extern __device__ const int c_gw_ex_off[268];
+extern __device__ const int c_gw_asm_ptr[1691];
+extern __device__ const int c_gw_asm_src[3213];
+extern __device__ const int c_gw_asm_kind[3213];
+extern __device__ const int c_gw_piv_diag[149];
+extern __device__ const int c_gw_lsc_ptr[150];
+extern __device__ const int c_gw_lsc_st[883];
+extern __device__ const int c_gw_up_ptr[150];
+extern __device__ const int c_gw_up_ij[5247];
+extern __device__ const int c_gw_up_ik[5247];
+extern __device__ const int c_gw_up_kj[5247];
+extern __device__ const int c_gw_fl_ptr[23];
+extern __device__ const int c_gw_fl_row[149];
+extern __device__ const int c_gw_bl_ptr[20];
+extern __device__ const int c_gw_bl_row[149];
+extern __device__ const int c_gw_fr_ptr[150];
+extern __device__ const int c_gw_fr_st[883];
+extern __device__ const int c_gw_fr_col[883];
+extern __device__ const int c_gw_br_ptr[150];
+extern __device__ const int c_gw_br_st[657];
+extern __device__ const int c_gw_br_col[657];
+extern __device__ const double c_gw_sum_c[1738];
+extern __device__ const double c_gw_asm_c[3213];
 constexpr int EBI_N_EBISP = 136;
 constexpr double EBI_DELTAT = 2.5;
 constexpr int EBI_NEBITER = 1000;
@@ -365,45 +363,6 @@ __device__ __forceinline__ void gear_pdecomp_0(double* __restrict__ ws, double r
     gear_pdecomp_0_27(ws, r1delt);
     gear_pdecomp_0_28(ws, r1delt);
     gear_pdecomp_0_29(ws, r1delt);
-}
-__device__ __forceinline__ void gear_pdecomp_s1_0(double* __restrict__ ws, double r1delt)
-{
-    gear_pdecomp_s1_0_0(ws, r1delt);
-    gear_pdecomp_s1_0_1(ws, r1delt);
-    gear_pdecomp_s1_0_2(ws, r1delt);
-    gear_pdecomp_s1_0_3(ws, r1delt);
-    gear_pdecomp_s1_0_4(ws, r1delt);
-    gear_pdecomp_s1_0_5(ws, r1delt);
-    gear_pdecomp_s1_0_6(ws, r1delt);
-    gear_pdecomp_s1_0_7(ws, r1delt);
-    gear_pdecomp_s1_0_8(ws, r1delt);
-    gear_pdecomp_s1_0_9(ws, r1delt);
-    gear_pdecomp_s1_0_10(ws, r1delt);
-    gear_pdecomp_s1_0_11(ws, r1delt);
-    gear_pdecomp_s1_0_12(ws, r1delt);
-    gear_pdecomp_s1_0_13(ws, r1delt);
-    gear_pdecomp_s1_0_14(ws, r1delt);
-    gear_pdecomp_s1_0_15(ws, r1delt);
-    gear_pdecomp_s1_0_16(ws, r1delt);
-    gear_pdecomp_s1_0_17(ws, r1delt);
-    gear_pdecomp_s1_0_18(ws, r1delt);
-    gear_pdecomp_s1_0_19(ws, r1delt);
-    gear_pdecomp_s1_0_20(ws, r1delt);
-    gear_pdecomp_s1_0_21(ws, r1delt);
-    gear_pdecomp_s1_0_22(ws, r1delt);
-    gear_pdecomp_s1_0_23(ws, r1delt);
-    gear_pdecomp_s1_0_24(ws, r1delt);
-    gear_pdecomp_s1_0_25(ws, r1delt);
-    gear_pdecomp_s1_0_26(ws, r1delt);
-    gear_pdecomp_s1_0_27(ws, r1delt);
-    gear_pdecomp_s1_0_28(ws, r1delt);
-    gear_pdecomp_s1_0_29(ws, r1delt);
-}
-__device__ __forceinline__ void solve_s1_0(double* __restrict__ ws, int rhs)
-{
-    solve_s1_0_0(ws, rhs);
-    solve_s1_0_1(ws, rhs);
-    solve_s1_0_2(ws, rhs);
 }
 __device__ __forceinline__ void jacdecomp_0(double* __restrict__ ws, double gdtinv)
 {
@@ -783,6 +742,7 @@ struct Traits {
     static constexpr int GEAR_CEST = mech_cb6r5_ae7_aq::GEAR_CEST;
     static constexpr int GEAR_BLKCONC = mech_cb6r5_ae7_aq::GEAR_BLKCONC;
     static constexpr int GEAR_CONC = mech_cb6r5_ae7_aq::GEAR_CONC;
+    static constexpr int GEAR_E = mech_cb6r5_ae7_aq::GEAR_E;
     static constexpr int EBIW_YC = mech_cb6r5_ae7_aq::EBIW_YC;
     static constexpr int EBIW_YC0 = mech_cb6r5_ae7_aq::EBIW_YC0;
     static constexpr int EBIW_YCP = mech_cb6r5_ae7_aq::EBIW_YCP;
@@ -800,10 +760,6 @@ struct Traits {
     static __device__ __forceinline__ void explic_0(double* ws) { mech_cb6r5_ae7_aq::explic_0(ws); }
     static __device__ __forceinline__ void gear_explic_0(double* ws) { mech_cb6r5_ae7_aq::gear_explic_0(ws); }
     static __device__ __forceinline__ void gear_pdecomp_0(double* ws, double r) { mech_cb6r5_ae7_aq::gear_pdecomp_0(ws, r); }
-    static __device__ __forceinline__ void feval_s1_0(double* ws, int s, int t) { mech_cb6r5_ae7_aq::feval_s1_0(ws, s, t); }
-    static __device__ __forceinline__ void gear_explic_s1_0(double* ws) { mech_cb6r5_ae7_aq::gear_explic_s1_0(ws); }
-    static __device__ __forceinline__ void gear_pdecomp_s1_0(double* ws, double r) { mech_cb6r5_ae7_aq::gear_pdecomp_s1_0(ws, r); }
-    static __device__ __forceinline__ void solve_s1_0(double* ws, int r) { mech_cb6r5_ae7_aq::solve_s1_0(ws, r); }
     static __device__ __forceinline__ void jacdecomp_0(double* ws, double g) { mech_cb6r5_ae7_aq::jacdecomp_0(ws, g); }
     static __device__ __forceinline__ void solve_0(double* ws, int r) { mech_cb6r5_ae7_aq::solve_0(ws, r); }
     static __device__ __forceinline__ void jacdecomp_0_sync(double* ws, double g, bool go) { mech_cb6r5_ae7_aq::jacdecomp_0_sync(ws, g, go); }
@@ -851,6 +807,42 @@ struct Traits {
     static __device__ __forceinline__ const int* ebiw_pl_t0() { return mech_cb6r5_ae7_aq::c_ebiw_pl_t0; }
     static __device__ __forceinline__ const int* ebiw_term_r() { return mech_cb6r5_ae7_aq::c_ebiw_term_r; }
     static __device__ __forceinline__ const double* ebiw_term_c() { return mech_cb6r5_ae7_aq::c_ebiw_term_c; }
+    static constexpr int GW_NACT = 349;
+    static constexpr int GW_NEX = 268;
+    static constexpr int GW_NFL = 22;
+    static constexpr int GW_NBL = 19;
+    static __device__ __forceinline__ const int* gw_act_r() { return mech_cb6r5_ae7_aq::c_gw_act_r; }
+    static __device__ __forceinline__ const int* gw_act_sp() { return mech_cb6r5_ae7_aq::c_gw_act_sp; }
+    static __device__ __forceinline__ const int* gw_sum_ptr() { return mech_cb6r5_ae7_aq::c_gw_sum_ptr; }
+    static __device__ __forceinline__ const int* gw_sum_r() { return mech_cb6r5_ae7_aq::c_gw_sum_r; }
+    static __device__ __forceinline__ const int* gw_sum_k() { return mech_cb6r5_ae7_aq::c_gw_sum_k; }
+    static __device__ __forceinline__ const int* gw_lane_ptr() { return mech_cb6r5_ae7_aq::c_gw_lane_ptr; }
+    static __device__ __forceinline__ const int* gw_lane_sp() { return mech_cb6r5_ae7_aq::c_gw_lane_sp; }
+    static __device__ __forceinline__ const int* gw_ex_r() { return mech_cb6r5_ae7_aq::c_gw_ex_r; }
+    static __device__ __forceinline__ const int* gw_ex_sp() { return mech_cb6r5_ae7_aq::c_gw_ex_sp; }
+    static __device__ __forceinline__ const int* gw_ex_off() { return mech_cb6r5_ae7_aq::c_gw_ex_off; }
+    static __device__ __forceinline__ const int* gw_asm_ptr() { return mech_cb6r5_ae7_aq::c_gw_asm_ptr; }
+    static __device__ __forceinline__ const int* gw_asm_src() { return mech_cb6r5_ae7_aq::c_gw_asm_src; }
+    static __device__ __forceinline__ const int* gw_asm_kind() { return mech_cb6r5_ae7_aq::c_gw_asm_kind; }
+    static __device__ __forceinline__ const int* gw_piv_diag() { return mech_cb6r5_ae7_aq::c_gw_piv_diag; }
+    static __device__ __forceinline__ const int* gw_lsc_ptr() { return mech_cb6r5_ae7_aq::c_gw_lsc_ptr; }
+    static __device__ __forceinline__ const int* gw_lsc_st() { return mech_cb6r5_ae7_aq::c_gw_lsc_st; }
+    static __device__ __forceinline__ const int* gw_up_ptr() { return mech_cb6r5_ae7_aq::c_gw_up_ptr; }
+    static __device__ __forceinline__ const int* gw_up_ij() { return mech_cb6r5_ae7_aq::c_gw_up_ij; }
+    static __device__ __forceinline__ const int* gw_up_ik() { return mech_cb6r5_ae7_aq::c_gw_up_ik; }
+    static __device__ __forceinline__ const int* gw_up_kj() { return mech_cb6r5_ae7_aq::c_gw_up_kj; }
+    static __device__ __forceinline__ const int* gw_fl_ptr() { return mech_cb6r5_ae7_aq::c_gw_fl_ptr; }
+    static __device__ __forceinline__ const int* gw_fl_row() { return mech_cb6r5_ae7_aq::c_gw_fl_row; }
+    static __device__ __forceinline__ const int* gw_bl_ptr() { return mech_cb6r5_ae7_aq::c_gw_bl_ptr; }
+    static __device__ __forceinline__ const int* gw_bl_row() { return mech_cb6r5_ae7_aq::c_gw_bl_row; }
+    static __device__ __forceinline__ const int* gw_fr_ptr() { return mech_cb6r5_ae7_aq::c_gw_fr_ptr; }
+    static __device__ __forceinline__ const int* gw_fr_st() { return mech_cb6r5_ae7_aq::c_gw_fr_st; }
+    static __device__ __forceinline__ const int* gw_fr_col() { return mech_cb6r5_ae7_aq::c_gw_fr_col; }
+    static __device__ __forceinline__ const int* gw_br_ptr() { return mech_cb6r5_ae7_aq::c_gw_br_ptr; }
+    static __device__ __forceinline__ const int* gw_br_st() { return mech_cb6r5_ae7_aq::c_gw_br_st; }
+    static __device__ __forceinline__ const int* gw_br_col() { return mech_cb6r5_ae7_aq::c_gw_br_col; }
+    static __device__ __forceinline__ const double* gw_sum_c() { return mech_cb6r5_ae7_aq::c_gw_sum_c; }
+    static __device__ __forceinline__ const double* gw_asm_c() { return mech_cb6r5_ae7_aq::c_gw_asm_c; }
     static __device__ __forceinline__ void rconst(double* ws, double t, double p, double h, double sw, int sun,
                                                   const double* rj, const double* het) { mech_cb6r5_ae7_aq::rconst(ws, t, p, h, sw, sun, rj, het); }
 };

@@ -65,6 +65,7 @@ constexpr int GEAR_CHOLD = 945;
 constexpr int GEAR_CEST = 1134;
 constexpr int GEAR_BLKCONC = 567;
 constexpr int GEAR_CONC = 6958;
+constexpr int GEAR_E = 189;
 constexpr int EBIW_YC = 0;
 constexpr int EBIW_YC0 = 189;
 constexpr int EBIW_YCP = 378;
@@ -90,119 +91,59 @@ __device__ void explic_0(double* __restrict__ ws);
 __device__ void feval_1(double* __restrict__ ws, int src, int dst);
 __device__ void explic_1(double* __restrict__ ws);
 __device__ void gear_explic_0(double* __restrict__ ws);
-__device__ void feval_s1_0(double* __restrict__ ws, int src, int dst);
-__device__ void gear_explic_s1_0(double* __restrict__ ws);
 __device__ void gear_pdecomp_0_0(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_0(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_1(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_1(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_2(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_2(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_3(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_3(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_4(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_4(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_5(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_5(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_6(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_6(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_7(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_7(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_8(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_8(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_9(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_9(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_10(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_10(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_11(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_11(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_12(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_12(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_13(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_13(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_14(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_14(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_15(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_15(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_16(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_16(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_17(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_17(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_18(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_18(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_19(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_19(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_20(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_20(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_21(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_21(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_22(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_22(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_23(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_23(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_24(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_24(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_25(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_25(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_26(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_26(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_27(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_27(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_28(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_28(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_29(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_29(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_30(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_30(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_31(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_31(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_32(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_32(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_33(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_33(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_34(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_34(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_35(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_35(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_36(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_36(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_37(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_37(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_38(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_38(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_39(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_39(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_40(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_40(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_41(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_41(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_42(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_42(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_43(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_43(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_44(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_44(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_45(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_45(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_46(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_46(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_47(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_47(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_48(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_48(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_49(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_49(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_50(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_50(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_51(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_51(double* __restrict__ ws, double r1delt);
 __device__ void gear_pdecomp_0_52(double* __restrict__ ws, double r1delt);
-__device__ void gear_pdecomp_s1_0_52(double* __restrict__ ws, double r1delt);
-__device__ void solve_s1_0_0(double* __restrict__ ws, int rhs);
-__device__ void solve_s1_0_1(double* __restrict__ ws, int rhs);
-__device__ void solve_s1_0_2(double* __restrict__ ws, int rhs);
-__device__ void solve_s1_0_3(double* __restrict__ ws, int rhs);
-__device__ void solve_s1_0_4(double* __restrict__ ws, int rhs);
 __device__ void jacdecomp_0_0(double* __restrict__ ws, double gdtinv);
 __device__ void jacdecomp_0_1(double* __restrict__ ws, double gdtinv);
 __device__ void jacdecomp_0_2(double* __restrict__ ws, double gdtinv);
@@ -459,6 +400,38 @@ __device__ void ddm_src_1_6(double* __restrict__ ws, const unsigned char* __rest
 __device__ void ddm_src_1_7(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
 __device__ void ddm_src_1_8(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
 __device__ void ddm_src_1_9(double* __restrict__ ws, const unsigned char* __restrict__ mask, double scale, int outoff);
+extern __device__ const int c_gw_act_r[531];
+extern __device__ const int c_gw_act_sp[1593];
+extern __device__ const int c_gw_sum_ptr[190];
+extern __device__ const int c_gw_sum_r[3238];
+extern __device__ const int c_gw_sum_k[3238];
+extern __device__ const int c_gw_lane_ptr[33];
+extern __device__ const int c_gw_lane_sp[189];
+extern __device__ const int c_gw_ex_r[455];
+extern __device__ const int c_gw_ex_sp[1365];
+extern __device__ const int c_gw_ex_off[455];
+extern __device__ const int c_gw_asm_ptr[3286];
+extern __device__ const int c_gw_asm_src[6231];
+extern __device__ const int c_gw_asm_kind[6231];
+extern __device__ const int c_gw_piv_diag[189];
+extern __device__ const int c_gw_lsc_ptr[190];
+extern __device__ const int c_gw_lsc_st[1968];
+extern __device__ const int c_gw_up_ptr[190];
+extern __device__ const int c_gw_up_ij[15259];
+extern __device__ const int c_gw_up_ik[15259];
+extern __device__ const int c_gw_up_kj[15259];
+extern __device__ const int c_gw_fl_ptr[30];
+extern __device__ const int c_gw_fl_row[189];
+extern __device__ const int c_gw_bl_ptr[26];
+extern __device__ const int c_gw_bl_row[189];
+extern __device__ const int c_gw_fr_ptr[190];
+extern __device__ const int c_gw_fr_st[1968];
+extern __device__ const int c_gw_fr_col[1968];
+extern __device__ const int c_gw_br_ptr[190];
+extern __device__ const int c_gw_br_st[1127];
+extern __device__ const int c_gw_br_col[1127];
+extern __device__ const double c_gw_sum_c[3238];
+extern __device__ const double c_gw_asm_c[6231];
 constexpr int EBI_N_EBISP = 176;
 constexpr double EBI_DELTAT = 2.5;
 constexpr int EBI_NEBITER = 1000;
@@ -545,70 +518,6 @@ __device__ __forceinline__ void gear_pdecomp_0(double* __restrict__ ws, double r
     gear_pdecomp_0_50(ws, r1delt);
     gear_pdecomp_0_51(ws, r1delt);
     gear_pdecomp_0_52(ws, r1delt);
-}
-__device__ __forceinline__ void gear_pdecomp_s1_0(double* __restrict__ ws, double r1delt)
-{
-    gear_pdecomp_s1_0_0(ws, r1delt);
-    gear_pdecomp_s1_0_1(ws, r1delt);
-    gear_pdecomp_s1_0_2(ws, r1delt);
-    gear_pdecomp_s1_0_3(ws, r1delt);
-    gear_pdecomp_s1_0_4(ws, r1delt);
-    gear_pdecomp_s1_0_5(ws, r1delt);
-    gear_pdecomp_s1_0_6(ws, r1delt);
-    gear_pdecomp_s1_0_7(ws, r1delt);
-    gear_pdecomp_s1_0_8(ws, r1delt);
-    gear_pdecomp_s1_0_9(ws, r1delt);
-    gear_pdecomp_s1_0_10(ws, r1delt);
-    gear_pdecomp_s1_0_11(ws, r1delt);
-    gear_pdecomp_s1_0_12(ws, r1delt);
-    gear_pdecomp_s1_0_13(ws, r1delt);
-    gear_pdecomp_s1_0_14(ws, r1delt);
-    gear_pdecomp_s1_0_15(ws, r1delt);
-    gear_pdecomp_s1_0_16(ws, r1delt);
-    gear_pdecomp_s1_0_17(ws, r1delt);
-    gear_pdecomp_s1_0_18(ws, r1delt);
-    gear_pdecomp_s1_0_19(ws, r1delt);
-    gear_pdecomp_s1_0_20(ws, r1delt);
-    gear_pdecomp_s1_0_21(ws, r1delt);
-    gear_pdecomp_s1_0_22(ws, r1delt);
-    gear_pdecomp_s1_0_23(ws, r1delt);
-    gear_pdecomp_s1_0_24(ws, r1delt);
-    gear_pdecomp_s1_0_25(ws, r1delt);
-    gear_pdecomp_s1_0_26(ws, r1delt);
-    gear_pdecomp_s1_0_27(ws, r1delt);
-    gear_pdecomp_s1_0_28(ws, r1delt);
-    gear_pdecomp_s1_0_29(ws, r1delt);
-    gear_pdecomp_s1_0_30(ws, r1delt);
-    gear_pdecomp_s1_0_31(ws, r1delt);
-    gear_pdecomp_s1_0_32(ws, r1delt);
-    gear_pdecomp_s1_0_33(ws, r1delt);
-    gear_pdecomp_s1_0_34(ws, r1delt);
-    gear_pdecomp_s1_0_35(ws, r1delt);
-    gear_pdecomp_s1_0_36(ws, r1delt);
-    gear_pdecomp_s1_0_37(ws, r1delt);
-    gear_pdecomp_s1_0_38(ws, r1delt);
-    gear_pdecomp_s1_0_39(ws, r1delt);
-    gear_pdecomp_s1_0_40(ws, r1delt);
-    gear_pdecomp_s1_0_41(ws, r1delt);
-    gear_pdecomp_s1_0_42(ws, r1delt);
-    gear_pdecomp_s1_0_43(ws, r1delt);
-    gear_pdecomp_s1_0_44(ws, r1delt);
-    gear_pdecomp_s1_0_45(ws, r1delt);
-    gear_pdecomp_s1_0_46(ws, r1delt);
-    gear_pdecomp_s1_0_47(ws, r1delt);
-    gear_pdecomp_s1_0_48(ws, r1delt);
-    gear_pdecomp_s1_0_49(ws, r1delt);
-    gear_pdecomp_s1_0_50(ws, r1delt);
-    gear_pdecomp_s1_0_51(ws, r1delt);
-    gear_pdecomp_s1_0_52(ws, r1delt);
-}
-__device__ __forceinline__ void solve_s1_0(double* __restrict__ ws, int rhs)
-{
-    solve_s1_0_0(ws, rhs);
-    solve_s1_0_1(ws, rhs);
-    solve_s1_0_2(ws, rhs);
-    solve_s1_0_3(ws, rhs);
-    solve_s1_0_4(ws, rhs);
 }
 __device__ __forceinline__ void jacdecomp_0(double* __restrict__ ws, double gdtinv)
 {
@@ -1197,6 +1106,7 @@ struct Traits {
     static constexpr int GEAR_CEST = mech_cracmm2::GEAR_CEST;
     static constexpr int GEAR_BLKCONC = mech_cracmm2::GEAR_BLKCONC;
     static constexpr int GEAR_CONC = mech_cracmm2::GEAR_CONC;
+    static constexpr int GEAR_E = mech_cracmm2::GEAR_E;
     static constexpr int EBIW_YC = mech_cracmm2::EBIW_YC;
     static constexpr int EBIW_YC0 = mech_cracmm2::EBIW_YC0;
     static constexpr int EBIW_YCP = mech_cracmm2::EBIW_YCP;
@@ -1214,10 +1124,6 @@ struct Traits {
     static __device__ __forceinline__ void explic_0(double* ws) { mech_cracmm2::explic_0(ws); }
     static __device__ __forceinline__ void gear_explic_0(double* ws) { mech_cracmm2::gear_explic_0(ws); }
     static __device__ __forceinline__ void gear_pdecomp_0(double* ws, double r) { mech_cracmm2::gear_pdecomp_0(ws, r); }
-    static __device__ __forceinline__ void feval_s1_0(double* ws, int s, int t) { mech_cracmm2::feval_s1_0(ws, s, t); }
-    static __device__ __forceinline__ void gear_explic_s1_0(double* ws) { mech_cracmm2::gear_explic_s1_0(ws); }
-    static __device__ __forceinline__ void gear_pdecomp_s1_0(double* ws, double r) { mech_cracmm2::gear_pdecomp_s1_0(ws, r); }
-    static __device__ __forceinline__ void solve_s1_0(double* ws, int r) { mech_cracmm2::solve_s1_0(ws, r); }
     static __device__ __forceinline__ void jacdecomp_0(double* ws, double g) { mech_cracmm2::jacdecomp_0(ws, g); }
     static __device__ __forceinline__ void solve_0(double* ws, int r) { mech_cracmm2::solve_0(ws, r); }
     static __device__ __forceinline__ void jacdecomp_0_sync(double* ws, double g, bool go) { mech_cracmm2::jacdecomp_0_sync(ws, g, go); }
@@ -1265,6 +1171,42 @@ struct Traits {
     static __device__ __forceinline__ const int* ebiw_pl_t0() { return mech_cracmm2::c_ebiw_pl_t0; }
     static __device__ __forceinline__ const int* ebiw_term_r() { return mech_cracmm2::c_ebiw_term_r; }
     static __device__ __forceinline__ const double* ebiw_term_c() { return mech_cracmm2::c_ebiw_term_c; }
+    static constexpr int GW_NACT = 531;
+    static constexpr int GW_NEX = 455;
+    static constexpr int GW_NFL = 29;
+    static constexpr int GW_NBL = 25;
+    static __device__ __forceinline__ const int* gw_act_r() { return mech_cracmm2::c_gw_act_r; }
+    static __device__ __forceinline__ const int* gw_act_sp() { return mech_cracmm2::c_gw_act_sp; }
+    static __device__ __forceinline__ const int* gw_sum_ptr() { return mech_cracmm2::c_gw_sum_ptr; }
+    static __device__ __forceinline__ const int* gw_sum_r() { return mech_cracmm2::c_gw_sum_r; }
+    static __device__ __forceinline__ const int* gw_sum_k() { return mech_cracmm2::c_gw_sum_k; }
+    static __device__ __forceinline__ const int* gw_lane_ptr() { return mech_cracmm2::c_gw_lane_ptr; }
+    static __device__ __forceinline__ const int* gw_lane_sp() { return mech_cracmm2::c_gw_lane_sp; }
+    static __device__ __forceinline__ const int* gw_ex_r() { return mech_cracmm2::c_gw_ex_r; }
+    static __device__ __forceinline__ const int* gw_ex_sp() { return mech_cracmm2::c_gw_ex_sp; }
+    static __device__ __forceinline__ const int* gw_ex_off() { return mech_cracmm2::c_gw_ex_off; }
+    static __device__ __forceinline__ const int* gw_asm_ptr() { return mech_cracmm2::c_gw_asm_ptr; }
+    static __device__ __forceinline__ const int* gw_asm_src() { return mech_cracmm2::c_gw_asm_src; }
+    static __device__ __forceinline__ const int* gw_asm_kind() { return mech_cracmm2::c_gw_asm_kind; }
+    static __device__ __forceinline__ const int* gw_piv_diag() { return mech_cracmm2::c_gw_piv_diag; }
+    static __device__ __forceinline__ const int* gw_lsc_ptr() { return mech_cracmm2::c_gw_lsc_ptr; }
+    static __device__ __forceinline__ const int* gw_lsc_st() { return mech_cracmm2::c_gw_lsc_st; }
+    static __device__ __forceinline__ const int* gw_up_ptr() { return mech_cracmm2::c_gw_up_ptr; }
+    static __device__ __forceinline__ const int* gw_up_ij() { return mech_cracmm2::c_gw_up_ij; }
+    static __device__ __forceinline__ const int* gw_up_ik() { return mech_cracmm2::c_gw_up_ik; }
+    static __device__ __forceinline__ const int* gw_up_kj() { return mech_cracmm2::c_gw_up_kj; }
+    static __device__ __forceinline__ const int* gw_fl_ptr() { return mech_cracmm2::c_gw_fl_ptr; }
+    static __device__ __forceinline__ const int* gw_fl_row() { return mech_cracmm2::c_gw_fl_row; }
+    static __device__ __forceinline__ const int* gw_bl_ptr() { return mech_cracmm2::c_gw_bl_ptr; }
+    static __device__ __forceinline__ const int* gw_bl_row() { return mech_cracmm2::c_gw_bl_row; }
+    static __device__ __forceinline__ const int* gw_fr_ptr() { return mech_cracmm2::c_gw_fr_ptr; }
+    static __device__ __forceinline__ const int* gw_fr_st() { return mech_cracmm2::c_gw_fr_st; }
+    static __device__ __forceinline__ const int* gw_fr_col() { return mech_cracmm2::c_gw_fr_col; }
+    static __device__ __forceinline__ const int* gw_br_ptr() { return mech_cracmm2::c_gw_br_ptr; }
+    static __device__ __forceinline__ const int* gw_br_st() { return mech_cracmm2::c_gw_br_st; }
+    static __device__ __forceinline__ const int* gw_br_col() { return mech_cracmm2::c_gw_br_col; }
+    static __device__ __forceinline__ const double* gw_sum_c() { return mech_cracmm2::c_gw_sum_c; }
+    static __device__ __forceinline__ const double* gw_asm_c() { return mech_cracmm2::c_gw_asm_c; }
     static __device__ __forceinline__ void rconst(double* ws, double t, double p, double h, double sw, int sun,
                                                   const double* rj, const double* het) { mech_cracmm2::rconst(ws, t, p, h, sw, sun, rj, het); }
 };

@@ -21,8 +21,6 @@ same rule, so both compute the same sums with the same roundings.
 """
 from __future__ import annotations
 
-import re
-
 from .emit_common import RATE_HELPERS, c_double
 from .fortran_tables import Mechanism
 from .rate_expr import RateProgram
@@ -81,32 +79,6 @@ def _w(k: int) -> str:
     return f"ws[{k * 32}]"
 
 
-_IDX = re.compile(r"\b(ws|yin|yout|lu|b|vd|y)\[(\d+)\]")
-_PTR = re.compile(r"\b(ws|lu|vd) \+ (\d+)\b")
-
-
-def _stride1(lines: list[str], renames: list[tuple[str, str]]) -> list[str]:
-    """The same routine for a workspace of one cell with stride 1 (a warp's shared-memory
-    copy): every element index k*32 becomes k, L2 prefetches are dropped, names get the
-    _s1 infix.  The arithmetic and its order are unchanged."""
-    def div(mm):
-        v = int(mm.group(2))
-        assert v % 32 == 0, mm.group(0)
-        return mm.group(0)[: -len(mm.group(2)) - (1 if mm.group(0).endswith("]") else 0)] + \
-            str(v // 32) + ("]" if mm.group(0).endswith("]") else "")
-    out = []
-    for ln in lines:
-        if "CHEM_PREFETCH" in ln:
-            continue
-        ln = _IDX.sub(div, ln)
-        ln = _PTR.sub(div, ln)
-        ln = ln.replace("src * 32", "src").replace("dst * 32", "dst").replace("rhs * 32", "rhs")
-        for a, b in renames:
-            ln = ln.replace(a, b)
-        out.append(ln)
-    return out
-
-
 def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src_hash: str,
                  ebi_decl: str = "") -> dict[str, str]:
     """Return {file name: text}: one header with declarations and the kernel traits,
@@ -122,39 +94,25 @@ def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src
     for d in range(2):
         units["rates"] += _feval(m, sp, lay, d) + _explic(m, sp, lay, d)
     # SMVGEAR uses the day pattern for every cell (see csrc/gear.cuh); the warp-per-cell
-    # kernel runs stride-1 copies of its routines on the cell's shared-memory workspace
+    # kernel runs table-driven cooperative forms of its routines
     units["rates"] += _explic(m, sp, lay, 0, gear=True)
-    units["s1_rates"] = _stride1(_feval(m, sp, lay, 0), [("feval_0(", "feval_s1_0(")]) + \
-        _stride1(_explic(m, sp, lay, 0, gear=True), [("gear_explic_0(", "gear_explic_s1_0(")])
+    gw_decl, gw_defs, gw_info = _gear_warp_tables(m, sp, lay)
+    units["gw_tables"] = gw_defs
     decls: list[str] = ["__device__ void rconst(double* __restrict__ ws, double temp_in, double press, double h2o, "
                         "double seawater, int lsunlight, const double* __restrict__ rjv, const double* __restrict__ hetv);"]
     for d in range(2):
         decls.append(f"__device__ void feval_{d}(double* __restrict__ ws, int src, int dst);")
         decls.append(f"__device__ void explic_{d}(double* __restrict__ ws);")
     decls.append("__device__ void gear_explic_0(double* __restrict__ ws);")
-    decls.append("__device__ void feval_s1_0(double* __restrict__ ws, int src, int dst);")
-    decls.append("__device__ void gear_explic_s1_0(double* __restrict__ ws);")
     wrappers: list[str] = []
     for d in range(1):
         gchunks = _jacdecomp_chunks(m, sp, lay, d, gear=True)
         for ci, code in enumerate(gchunks):
             units.setdefault(f"glu{d}_{ci // 3}", []).extend(code)
-            units.setdefault(f"s1_glu{d}_{ci // 3}", []).extend(
-                _stride1(code, [(f"gear_pdecomp_{d}_{ci}(", f"gear_pdecomp_s1_{d}_{ci}(")]))
             decls.append(f"__device__ void gear_pdecomp_{d}_{ci}(double* __restrict__ ws, double r1delt);")
-            decls.append(f"__device__ void gear_pdecomp_s1_{d}_{ci}(double* __restrict__ ws, double r1delt);")
-        for infix in ("", "s1_"):
-            wrappers.append(f"__device__ __forceinline__ void gear_pdecomp_{infix}{d}(double* __restrict__ ws, double r1delt)")
-            wrappers.append("{")
-            wrappers.extend(f"    gear_pdecomp_{infix}{d}_{ci}(ws, r1delt);" for ci in range(len(gchunks)))
-            wrappers.append("}")
-        schunks = _solve_chunks(sp, lay, d)
-        for ci, code in enumerate(schunks):
-            units.setdefault(f"s1_solve{d}", []).extend(_stride1(code, [(f"solve_{d}_{ci}(", f"solve_s1_{d}_{ci}(")]))
-            decls.append(f"__device__ void solve_s1_{d}_{ci}(double* __restrict__ ws, int rhs);")
-        wrappers.append(f"__device__ __forceinline__ void solve_s1_{d}(double* __restrict__ ws, int rhs)")
+        wrappers.append(f"__device__ __forceinline__ void gear_pdecomp_{d}(double* __restrict__ ws, double r1delt)")
         wrappers.append("{")
-        wrappers.extend(f"    solve_s1_{d}_{ci}(ws, rhs);" for ci in range(len(schunks)))
+        wrappers.extend(f"    gear_pdecomp_{d}_{ci}(ws, r1delt);" for ci in range(len(gchunks)))
         wrappers.append("}")
     for d in range(2):
         chunks = _jacdecomp_chunks(m, sp, lay, d)
@@ -252,7 +210,7 @@ def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src
               ("ADJ_GK", lay.adj_gk), ("OFF_YAVE", lay.yave),
               ("GEAR_WS_ELEMS", lay.gear_total), ("GEAR_CNEW", lay.y), ("GEAR_GLOSS", lay.ydot),
               ("GEAR_DTLOS", lay.k1), ("GEAR_CHOLD", lay.k2), ("GEAR_CEST", lay.k3), ("GEAR_BLKCONC", lay.f0),
-              ("GEAR_CONC", lay.gear_conc),
+              ("GEAR_CONC", lay.gear_conc), ("GEAR_E", lay.yp),
               # warp-cooperative EBI: one cell's state in shared memory (doubles)
               ("EBIW_YC", 0), ("EBIW_YC0", ns), ("EBIW_YCP", 2 * ns), ("EBIW_PROD", 3 * ns),
               ("EBIW_LOSS", 4 * ns), ("EBIW_PNEG", 5 * ns), ("EBIW_NOTMAX", 6 * ns), ("EBIW_RKI", 7 * ns),
@@ -269,6 +227,7 @@ def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src
     h.append(f"static const int h_convert[{ns}] = {{{', '.join('1' if c else '0' for c in m.convert_conc)}}};")
     h.append(f"static const double h_molwt[{ns}] = {{{', '.join(c_double(x) for x in m.molwt)}}};")
     h.extend(decls)
+    h.extend(gw_decl)
     if ebi_decl:
         h.append(ebi_decl)
     h.extend(wrappers)
@@ -284,10 +243,6 @@ def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src
         if d == 0:
             h.append(f"    static __device__ __forceinline__ void gear_explic_0(double* ws) {{ {ns_name}::gear_explic_0(ws); }}")
             h.append(f"    static __device__ __forceinline__ void gear_pdecomp_0(double* ws, double r) {{ {ns_name}::gear_pdecomp_0(ws, r); }}")
-            h.append(f"    static __device__ __forceinline__ void feval_s1_0(double* ws, int s, int t) {{ {ns_name}::feval_s1_0(ws, s, t); }}")
-            h.append(f"    static __device__ __forceinline__ void gear_explic_s1_0(double* ws) {{ {ns_name}::gear_explic_s1_0(ws); }}")
-            h.append(f"    static __device__ __forceinline__ void gear_pdecomp_s1_0(double* ws, double r) {{ {ns_name}::gear_pdecomp_s1_0(ws, r); }}")
-            h.append(f"    static __device__ __forceinline__ void solve_s1_0(double* ws, int r) {{ {ns_name}::solve_s1_0(ws, r); }}")
         h.append(f"    static __device__ __forceinline__ void jacdecomp_{d}(double* ws, double g) {{ {ns_name}::jacdecomp_{d}(ws, g); }}")
         h.append(f"    static __device__ __forceinline__ void solve_{d}(double* ws, int r) {{ {ns_name}::solve_{d}(ws, r); }}")
         h.append(f"    static __device__ __forceinline__ void jacdecomp_{d}_sync(double* ws, double g, bool go) {{ {ns_name}::jacdecomp_{d}_sync(ws, g, go); }}")
@@ -320,6 +275,11 @@ def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src
         h.append(f"    static __device__ __forceinline__ const int* ebiw_pl_t0() {{ return {ns_name}::c_ebiw_pl_t0; }}")
         h.append(f"    static __device__ __forceinline__ const int* ebiw_term_r() {{ return {ns_name}::c_ebiw_term_r; }}")
         h.append(f"    static __device__ __forceinline__ const double* ebiw_term_c() {{ return {ns_name}::c_ebiw_term_c; }}")
+    for k, v in gw_info["sizes"].items():
+        h.append(f"    static constexpr int {k} = {v};")
+    for k in gw_info["names"]:
+        ty = "double" if k in ("sum_c", "asm_c") else "int"
+        h.append(f"    static __device__ __forceinline__ const {ty}* gw_{k}() {{ return {ns_name}::c_gw_{k}; }}")
     h.append("    static __device__ __forceinline__ void rconst(double* ws, double t, double p, double h, double sw, int sun,")
     h.append(f"                                                  const double* rj, const double* het) {{ {ns_name}::rconst(ws, t, p, h, sw, sun, rj, het); }}")
     h.append("};")
@@ -335,6 +295,120 @@ def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src
         t.append(f"}}  // namespace {ns_name}")
         files[f"{mech}_{unit}.cu"] = "\n".join(t) + "\n"
     return files
+
+
+def _gear_warp_tables(m: Mechanism, sp: SparseMech, lay: Layout) -> tuple[list[str], list[str], dict]:
+    """Tables of the warp-cooperative SMVGEAR routines (day pattern), each listing the
+    operations of the generated sequential routines in an order that lanes can share
+    without changing any element's operation sequence:
+      rates (RXRAT of each active reaction) and, per species, its derivative terms in
+      RBFEVAL's order, species given to lanes longest-first;
+      the partial-derivative products (EXPLIC) of 2- and 3-reactant reactions;
+      per LU storage entry its P assembly terms in PDERIV's order;
+      the elimination by pivot (right-looking): the L entries a pivot scales and the
+      updates it makes, each entry still receiving its updates in ascending pivot order;
+      forward and backward substitution rows grouped in dependency levels.
+    Returns (header declarations, table definitions, sizes)."""
+    d = 0
+    n = sp.ischan
+    act = list(sp.active[d])
+    rate_sp = []
+    for r in act:
+        rate_sp += [sp.irm2[r][i] if i < m.nreact[r] else -1 for i in range(3)]
+    contrib: dict[int, list] = {}
+    for r in act:
+        for i in range(m.nreact[r]):
+            contrib.setdefault(sp.irm2[r][i], []).append((r, None))
+        for p in range(m.nprdct[r]):
+            contrib.setdefault(sp.irm2[r][3 + p], []).append((r, m.sc[r][p]))
+    sum_ptr, sum_r, sum_k, sum_c = [0], [], [], []
+    for s_ in range(n):
+        for (r, c) in contrib.get(s_, []):
+            sum_r.append(r)
+            sum_k.append(0 if c is None else 1)
+            sum_c.append(0.0 if c is None else c)
+        sum_ptr.append(len(sum_r))
+    loads = [0] * 32
+    lanes: list[list[int]] = [[] for _ in range(32)]
+    for s_ in sorted(range(n), key=lambda q: -(sum_ptr[q + 1] - sum_ptr[q])):
+        ln = min(range(32), key=lambda q: loads[q])
+        lanes[ln].append(s_)
+        loads[ln] += sum_ptr[s_ + 1] - sum_ptr[s_] + 1
+    lane_ptr, lane_sp = [0], []
+    for ln in range(32):
+        lane_sp += lanes[ln]
+        lane_ptr.append(len(lane_sp))
+    ex_r, ex_sp, ex_off = [], [], []
+    for r in act:
+        if m.nreact[r] >= 2:
+            ex_r.append(r)
+            ex_sp += [sp.irm2[r][i] if i < m.nreact[r] else -1 for i in range(3)]
+            ex_off.append(lay.ex[(r, 0)])
+    terms = _jac_terms(m, sp, d)
+    iarr = sp.iarray[d]
+    asm_ptr, asm_src, asm_kind, asm_c = [0, 0], [], [], []
+    for st in range(1, iarr + 1):
+        for (r, ial, coef, sign) in terms.get(st, []):
+            asm_src.append(lay.rki + r if m.nreact[r] == 1 else lay.ex[(r, ial)])
+            asm_kind.append(-1 if sign < 0 else (0 if coef is None else 1))
+            asm_c.append(0.0 if coef is None else coef)
+        asm_ptr.append(len(asm_src))
+    jpt = sp.jarraypt[d]
+    piv_diag = [jpt[(k, k)] for k in range(n)]
+    lsc_ptr, lsc_st, up_ptr, up_ij, up_ik, up_kj = [0], [], [0], [], [], []
+    rows_of = {k: [] for k in range(n)}
+    for i in range(n):
+        for (st_ik, k) in sp.lower[d][i]:
+            rows_of[k].append((i, st_ik))
+    for k in range(n):
+        for (i, st_ik) in rows_of[k]:
+            lsc_st.append(st_ik)
+            for (st_kj, j) in sp.upper[d][k]:
+                up_ij.append(jpt[(i, j)])
+                up_ik.append(st_ik)
+                up_kj.append(st_kj)
+        lsc_ptr.append(len(lsc_st))
+        up_ptr.append(len(up_ij))
+
+    def levels(deps, order):
+        lv = {}
+        for i in order:
+            lv[i] = 1 + max((lv[j] for j in deps(i)), default=0)
+        nl = max(lv.values())
+        ptr, rows = [0], []
+        for l in range(1, nl + 1):
+            rows += [i for i in order if lv[i] == l]
+            ptr.append(len(rows))
+        return ptr, rows
+    fl_ptr, fl_row = levels(lambda i: [j for (_, j) in sp.lower[d][i]], list(range(n)))
+    bl_ptr, bl_row = levels(lambda i: [j for (_, j) in sp.upper[d][i]], list(range(n - 1, -1, -1)))
+    fr_ptr, fr_st, fr_col, br_ptr, br_st, br_col = [0], [], [], [0], [], []
+    for i in range(n):
+        for (st, j) in sp.lower[d][i]:
+            fr_st.append(st); fr_col.append(j)
+        fr_ptr.append(len(fr_st))
+        for (st, j) in sp.upper[d][i]:
+            br_st.append(st); br_col.append(j)
+        br_ptr.append(len(br_st))
+    ints = {"act_r": act, "act_sp": rate_sp, "sum_ptr": sum_ptr, "sum_r": sum_r, "sum_k": sum_k,
+            "lane_ptr": lane_ptr, "lane_sp": lane_sp, "ex_r": ex_r, "ex_sp": ex_sp, "ex_off": ex_off,
+            "asm_ptr": asm_ptr, "asm_src": asm_src, "asm_kind": asm_kind, "piv_diag": piv_diag,
+            "lsc_ptr": lsc_ptr, "lsc_st": lsc_st, "up_ptr": up_ptr, "up_ij": up_ij, "up_ik": up_ik,
+            "up_kj": up_kj, "fl_ptr": fl_ptr, "fl_row": fl_row, "bl_ptr": bl_ptr, "bl_row": bl_row,
+            "fr_ptr": fr_ptr, "fr_st": fr_st, "fr_col": fr_col, "br_ptr": br_ptr, "br_st": br_st,
+            "br_col": br_col}
+    dbls = {"sum_c": sum_c, "asm_c": asm_c}
+    sizes = {"GW_NACT": len(act), "GW_NEX": len(ex_r), "GW_NFL": len(fl_ptr) - 1, "GW_NBL": len(bl_ptr) - 1}
+    decl, defs = [], []
+    for k, v in ints.items():
+        v = v or [0]
+        decl.append(f"extern __device__ const int c_gw_{k}[{len(v)}];")
+        defs.append(f"__device__ const int c_gw_{k}[{len(v)}] = {{{', '.join(map(str, v))}}};")
+    for k, v in dbls.items():
+        v = v or [0.0]
+        decl.append(f"extern __device__ const double c_gw_{k}[{len(v)}];")
+        defs.append(f"__device__ const double c_gw_{k}[{len(v)}] = {{{', '.join(c_double(x) for x in v)}}};")
+    return decl, defs, {"sizes": sizes, "names": list(ints) + list(dbls)}
 
 
 def _rconst(m: Mechanism, prog: RateProgram, lay: Layout) -> list[str]:
