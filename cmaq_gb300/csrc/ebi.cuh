@@ -175,6 +175,12 @@ struct EbiArgs {
     double tmstep;        // EBI_TMSTEP [min]
     const float* fwd;     // [nspec] FORWARD_CONV of the EBI driver (hrinit.F:90)
     const float* rev;     // [nspec] REVERSE_CONV (hrinit.F:91)
+    // one-cell-per-lane kernel: a cell still running after defer_after iterations (> 0) is
+    // dropped and its index appended to deferred[*ndeferred]; the one-cell-per-warp kernel
+    // then integrates it from its gathered inputs (the same result)
+    int defer_after;
+    int* deferred;
+    unsigned long long* ndeferred;
 };
 
 // Gather one cell as hrdriver.F:372-415 does (REAL(4) conc and met, REAL(8) pressure factor).
@@ -254,7 +260,10 @@ __global__ void __launch_bounds__(THREADS_PER_BLOCK, 1) k_chem_ebi_queue(GridArg
         if (!__any_sync(0xffffffffu, busy)) break;
         if (busy) {
             ebi::iterate<M>(ws, s, a.max_iter);
-            if (s.done) {
+            if (!s.done && e.defer_after > 0 && s.total_iter >= e.defer_after) {
+                e.deferred[atomicAdd(e.ndeferred, 1ull)] = (int)cell;
+                cell = -1;
+            } else if (s.done) {
                 scatter_cell_ebi<M>(a, e, cell, ws);
                 iters += s.total_iter;
                 failed += s.status != ebi::ST_OK;

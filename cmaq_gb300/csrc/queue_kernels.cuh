@@ -22,10 +22,12 @@ struct QueueArgs {
     unsigned long long* head;         // next queue position (zeroed before the launch)
     long long qlen;                   // cells in the queue (0: the whole grid)
     long long cell0;                  // first cell of the range the queue covers
+    const unsigned long long* qlen_dev;   // if set: the queue length, written by an earlier kernel
 };
 
 __device__ __forceinline__ unsigned long long queue_len(const QueueArgs& q, long long ncell)
 {
+    if (q.qlen_dev) return *q.qlen_dev;
     return (unsigned long long)(q.qlen > 0 ? q.qlen : ncell);
 }
 

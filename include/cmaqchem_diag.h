@@ -25,8 +25,12 @@ int cmaqchem_diag_fp64_peak(int device, double* tflops, double* ms);
  * "host_chunks" (1-16, default 4: cmaqchem_step moves the grid in that many chunks of
  * consecutive cells so that copies overlap the integration of the previous chunk) and
  * "ebi_warp" (EBI solver: 1 (default) one cell per warp with its state in shared memory,
- * 0 one cell per lane; same results) and "gear_warp" (SMVGEAR: 1 (default) one cell per
- * warp with its workspace in shared memory, 0 one cell per lane; same results). */
+ * 0 one cell per lane; same results), "ebi_defer" (EBI: n > 0 runs one cell per lane and
+ * hands the cells still iterating after n Backward-Euler iterations to the one-cell-per-warp
+ * kernel, which integrates them from their inputs; default 100; 0: ebi_warp alone decides;
+ * same results) and
+ * "gear_warp" (SMVGEAR: 1 (default) one cell per warp with its workspace in shared memory,
+ * 0 one cell per lane; same results). */
 struct cmaqchem_handle;
 int cmaqchem_diag_set_tuning(struct cmaqchem_handle* h, const char* key, int value);
 

@@ -93,16 +93,19 @@ def test_ebi_iteration_cap_is_reported():
 
 @pytest.mark.parametrize("mech_name", ["cb6r5_ae7_aq", "cracmm2"])
 def test_warp_and_lane_ebi_kernels_are_bit_identical(mech_name):
-    """One cell per warp (state in shared memory, routines spread over the lanes) and one
-    cell per lane compute every value with the same operations: identical output and
-    iteration counts over two calls."""
+    """One cell per warp (state in shared memory, routines spread over the lanes), one cell
+    per lane, and one cell per lane handing long-running cells to the warp kernel compute
+    every value with the same operations: identical output and iteration counts over two
+    calls."""
     g = make_grid(mech=mech_name, ncols=10, nrows=7, nlays=3, seed=27, het=True)
     res = []
-    for warp in (1, 0):
+    for warp, defer in ((1, 0), (0, 0), (1, 50)):
         s = _solver(g)
-        s.set_tuning(ebi_warp=warp)
+        s.set_tuning(ebi_warp=warp, ebi_defer=defer)   # (1, 50): lanes, then warps past 50 iterations
         conc, stats = _run(g, s, nsteps=2)
         res.append((conc, [x["accepted_steps"] for x in stats], s.cell_stats()[1]))
-    assert np.array_equal(res[0][0], res[1][0])
-    assert res[0][1] == res[1][1]
-    assert np.array_equal(res[0][2], res[1][2])
+    assert (res[2][2] > 50).any()                         # some cells were handed to the warp kernel
+    for r in res[1:]:
+        assert np.array_equal(res[0][0], r[0])
+        assert res[0][1] == r[1]
+        assert np.array_equal(res[0][2], r[2])
