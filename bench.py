@@ -512,6 +512,7 @@ def main():
                               "higher_is_better": False, "dtype": "f64", "data": "synthetic", "adjoint": r}))
         return 0
     peak_tf, _ = _lib.fp64_peak(device)
+    issue = {f"{k}_lanes": _lib.fp64_issue(device, k) for k in (1, 32)}
 
     tuned = None if a.no_autotune else run_autotune(a.workload, 2018 + rank, device)
     g = make_inputs(a.workload, seed=2018 + rank)
@@ -599,7 +600,8 @@ def main():
                          "dram_gbs_from_traffic": None if traffic is None else traffic / (ms_step * 1e-3) / 1e9,
                          "peak_source": "measured live: FP64 FMA-chain kernel (no FP64 figure in "
                                         "MEASURED_PEAKS.json)",
-                         "flops": "algorithmic FLOPs of the reference's ROS3 step per attempt x attempts"},
+                         "flops": "algorithmic FLOPs of the reference's ROS3 step per attempt x attempts",
+                         "fp64_chain_cycles_per_fma": issue},
             "plain": plain,
             "batched_over_plain": None if plain is None else value / plain["value"],
             "adjoint": adjoint,

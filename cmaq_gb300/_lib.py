@@ -73,6 +73,7 @@ def lib(variant: str = "default") -> C.CDLL:
     L.cmaqchem_destroy.restype = None
     L.cmaqchem_last_error.argtypes = [C.c_char_p, C.c_size_t]
     L.cmaqchem_diag_fp64_peak.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.cmaqchem_diag_fp64_issue.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double)]
     L.cmaqchem_diag_set_tuning.argtypes = [vp, C.c_char_p, C.c_int]
     return L
 
@@ -83,6 +84,14 @@ def fp64_peak(device: int = 0) -> tuple[float, float]:
     if lib().cmaqchem_diag_fp64_peak(device, C.byref(tf), C.byref(ms)) != 0:
         raise ChemError("FP64 peak measurement failed")
     return tf.value, ms.value
+
+
+def fp64_issue(device: int = 0, active_lanes: int = 1) -> float:
+    """Clock cycles per link of a dependent FP64 FMA chain of one warp with active_lanes lanes."""
+    c = C.c_double()
+    if lib().cmaqchem_diag_fp64_issue(device, int(active_lanes), C.byref(c)) != 0:
+        raise ChemError("FP64 issue measurement failed")
+    return c.value
 
 
 def last_error(L: C.CDLL | None = None) -> str:

@@ -26,7 +26,45 @@ __global__ void k_fp64_fma(int iters, double b, double c, double* sink)
     if (s == -1.2345e300) sink[threadIdx.x] = s;
 }
 
+// One warp; lanes below `active` run one dependent FMA chain of `iters` links; lane 0
+// reports the clock cycles the chain took.
+__global__ void k_fp64_issue(int active, int iters, double b, double c, double* sink, long long* cycles)
+{
+    const int lane = threadIdx.x & 31;
+    double a = (double)lane * 1.0e-3;
+    const long long t0 = clock64();
+    if (lane < active)
+        for (int i = 0; i < iters; ++i) a = fma(a, b, c);
+    __syncwarp();
+    const long long t1 = clock64();
+    if (a == -1.2345e300) sink[lane] = a;
+    if (lane == 0) *cycles = t1 - t0;
+}
+
 }  // namespace
+
+extern "C" int cmaqchem_diag_fp64_issue(int device, int active_lanes, double* cycles_per_instruction)
+{
+    if (active_lanes < 1 || active_lanes > 32 || !cycles_per_instruction) return -1;
+    if (cudaSetDevice(device) != cudaSuccess) return -1;
+    double* sink = nullptr;
+    long long* cyc = nullptr;
+    if (cudaMalloc(&sink, 32 * sizeof(double)) != cudaSuccess) return -1;
+    if (cudaMalloc(&cyc, sizeof(long long)) != cudaSuccess) {
+        cudaFree(sink);
+        return -1;
+    }
+    const int iters = 20000;
+    k_fp64_issue<<<1, 32>>>(active_lanes, 64, 0.999999, 1.0e-7, sink, cyc);   // warm-up
+    k_fp64_issue<<<1, 32>>>(active_lanes, iters, 0.999999, 1.0e-7, sink, cyc);
+    long long c = 0;
+    cudaError_t err = cudaMemcpy(&c, cyc, sizeof(long long), cudaMemcpyDeviceToHost);
+    cudaFree(sink);
+    cudaFree(cyc);
+    if (err != cudaSuccess) return -1;
+    *cycles_per_instruction = (double)c / iters;
+    return 0;
+}
 
 extern "C" int cmaqchem_diag_fp64_peak(int device, double* tflops, double* ms)
 {

@@ -13,6 +13,10 @@ extern "C" {
  * on every SM: TFLOP/s (an FMA counts 2) and the kernel time in ms. */
 int cmaqchem_diag_fp64_peak(int device, double* tflops, double* ms);
 
+/* Clock cycles per link of a dependent FP64 FMA chain run by one warp with active_lanes
+ * (1-32) lanes active: the latency a cell's sequential FP64 work pays per operation. */
+int cmaqchem_diag_fp64_issue(int device, int active_lanes, double* cycles_per_instruction);
+
 /* Scheduling knobs of a handle, for the autotuner: "night_pattern" (1: warps whose cells are
  * all dark use the smaller night LU pattern; 0: the day pattern always, same numbers),
  * "lockstep" (work-queue kernel: 0 free-running warps, 1 (default) the block's warps run
