@@ -476,7 +476,7 @@ def main():
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic (seeded; cmaq_gb300/synthetic.py)",
                 "config": {"workload": f"cb6r5_ae7_aq sample grid {r['cells']} cells (same distributions as "
-                                       "459x299x35), 12 x 5-min CHEM calls, rtol 1e-3 atol 1e-9",
+                                       f"459x299x35), {r['steps']} x 5-min CHEM calls, rtol 1e-3 atol 1e-9",
                            "algorithm": "reference ROS3 (BLKSIZE 50, stiffness reordering) restated in C; "
                                         "the Fortran reference cannot be compiled on this image"},
                 "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": thr, "kind": "port",
