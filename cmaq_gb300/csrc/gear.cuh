@@ -63,6 +63,7 @@ struct State {
     int label;
     bool need_jac;       // the next f evaluation is preceded by P and its LU factors
     bool lsun;
+    bool yave;           // DDM-3D: accumulate CAVEG (grsmvgear.F, sens blocks)
     int ifsuccess, idoub, nslp, jrestar, nqq, nqqold, kstep, jeval, l3, nqqisc, jfail, nylowred;
     bool higher_order;
     double xelaps, told, rdelmax, hratio, asn1, delt, rdelt, enqq, eup, edwn, drate, rmserr, der2max, rdeltup;
@@ -210,29 +211,36 @@ __device__ __forceinline__ void predict(double* __restrict__ ws, int nqq, int nq
 }
 
 template <class M, int S, bool COOP>
-__device__ void start(State& s, double* __restrict__ ws, bool lsun, const Coef* __restrict__ K)
+__device__ void start(State& s, double* __restrict__ ws, bool lsun, const Coef* __restrict__ K, bool yave = false)
 {
     s = State{};
     s.label = L_BEGIN;
     s.lsun = lsun;
+    s.yave = yave;
     s.rmserr = 0.0;
     s.drate = 0.7;
-    LOOP(i, M::NSPEC) GW(M::GEAR_BLKCONC + i) = GW(M::GEAR_CNEW + i);
+    LOOP(i, M::NSPEC) {
+        GW(M::GEAR_BLKCONC + i) = GW(M::GEAR_CNEW + i);
+        if (yave) GW(M::GEAR_CAVEG + i) = 0.0;   // CAVEG = 0 (grsmvgear.F:273-274)
+    }
     SYNC();
     s.ylowa = optimal_atol<M, S>(ws, K);
 }
 
-// grsmvgear.F:1002-1005, plus the status checks of this build
+// grsmvgear.F:1002-1005 (and CAVEG / CHEMSTEP floored at CONCMIN, :1007-1013), plus the
+// status checks of this build
 template <class M, int S, bool COOP>
-__device__ int finish(State& s, double* __restrict__ ws, bool failed)
+__device__ int finish(State& s, double* __restrict__ ws, bool failed, double chemstep)
 {
     constexpr int isc = M::ISCHAN;
+    const double rchem = 1.0 / chemstep;
     bool bad = false;
     LOOP(i, isc) {
         double& c = GW(M::GEAR_CNEW + i);
         if (failed) c = GW(M::GEAR_CONC + i);   // last accepted state
         if (c <= ZBOUND) c = CONCMIN;
         bad = bad || !isfinite(c);
+        if (s.yave) GW(M::GEAR_CAVEG + i) = max2(GW(M::GEAR_CAVEG + i) * rchem, CONCMIN);
     }
     SYNC();
     if (COOP) bad = __any_sync(0xffffffffu, bad);
@@ -300,6 +308,7 @@ init_post:
         LOOP(j, isc) {
             CO(j) = CN(j);
             CO(isc + j) = dl * GL(j);
+            if (s.yave) GW(M::GEAR_CFINI + j) = GW(M::GEAR_BLKCONC + j);   // CFINI = BLKCONC (grsmvgear.F:427-431)
         }
         SYNC();
         s.nqqold = 0;
@@ -311,7 +320,7 @@ loop_order:
     s.higher_order = true;
     {
         const double timremain = chemstep - s.xelaps;
-        if (timremain <= OMIC) return finish<M, S, COOP>(s, ws, false);
+        if (timremain <= OMIC) return finish<M, S, COOP>(s, ws, false, chemstep);
         if (s.nqq != s.nqqold) {
             s.nqqold = s.nqq;
             s.kstep = s.nqq + 1;
@@ -335,7 +344,7 @@ loop_order:
             goto loop_begin;
         }
         s.st.status |= ST_DT_UNDERFLOW;
-        return finish<M, S, COOP>(s, ws, true);
+        return finish<M, S, COOP>(s, ws, true, chemstep);
     }
     if (s.rdelt != 1.0) {
         double rdelta = 1.0;
@@ -382,7 +391,7 @@ newton_iter:
     if (K->max_iter > 0 && s.st.nsubfun >= K->max_iter) {
         predict<M, S, COOP>(ws, s.nqq, s.nqqisc, -1.0);
         s.st.status |= ST_MAXITER;
-        return finish<M, S, COOP>(s, ws, true);
+        return finish<M, S, COOP>(s, ws, true, chemstep);
     }
     s.st.nsubfun++;
     s.label = L_ITER_POST;
@@ -457,7 +466,7 @@ converged:
             SYNC();
             if (s.jrestar == 100) {
                 s.st.status |= ST_MAXITER;
-                return finish<M, S, COOP>(s, ws, true);
+                return finish<M, S, COOP>(s, ws, true, chemstep);
             }
             goto loop_initialize;
         }
@@ -479,6 +488,11 @@ converged:
                 CO(i) = ZBOUND;
                 CN(i) = ZBOUND;
                 for (int k = 1; k <= 5; ++k) CO(i + k * isc) = 0.0;
+            }
+            if (s.yave) {   // CAVEG += 0.5 (CFINI + CONC) DELT; CFINI = CONC (grsmvgear.F:841-849)
+                const double c = CO(i);
+                GW(M::GEAR_CAVEG + i) = fma(0.5 * (GW(M::GEAR_CFINI + i) + c), s.delt, GW(M::GEAR_CAVEG + i));
+                GW(M::GEAR_CFINI + i) = c;
             }
         }
         SYNC();
@@ -793,7 +807,7 @@ __global__ void __launch_bounds__(GEAR_WPB * 32, GEAR_WARPS_PER_SM / GEAR_WPB) k
                                 ws[(M::OFF_RKI + r) * 32] = g.rk[(size_t)r * a.ncell + cell];
                             sun = g.night[cell] == 0;
                         }
-                        gear::start<M, 32, false>(s, ws, sun, K);
+                        gear::start<M, 32, false>(s, ws, sun, K, a.yave != nullptr);
                     }
                 }
                 drained = __any_sync(0xffffffffu, base + __popc(need) >= queue_len(q, a.ncell));
@@ -804,6 +818,9 @@ __global__ void __launch_bounds__(GEAR_WPB * 32, GEAR_WARPS_PER_SM / GEAR_WPB) k
         if (busy && gear::advance<M, 32, false>(ws, s, K, a.chemstep) == gear::DONE) {
             if (GRID) {
                 scatter_cell<M>(a, cell, ws);
+                if (a.yave)
+                    for (int i = 0; i < M::ISCHAN; ++i)
+                        a.yave[(size_t)i * a.ncell + cell] = ws[(M::GEAR_CAVEG + i) * 32];
             } else {
                 for (int i = 0; i < M::NSPEC; ++i) g.y[(size_t)i * a.ncell + cell] = ws[(M::GEAR_CNEW + i) * 32];
                 if (g.cell_stats) {
@@ -881,7 +898,7 @@ __global__ void __launch_bounds__(32) k_gear_warp(GridArgs a, QueueArgs q, GearA
         }
         __syncwarp();
         gear::State s;
-        gear::start<M, 1, true>(s, sm, sun, K);
+        gear::start<M, 1, true>(s, sm, sun, K, GRID && a.yave != nullptr);
         while (gear::advance<M, 1, true>(sm, s, K, a.chemstep) == gear::NEED_F)
             gear::evaluate<M, 1, true>(sm, s, true);
         if (GRID) {   // write-back as scatter_cell
@@ -891,6 +908,7 @@ __global__ void __launch_bounds__(32) k_gear_warp(GridArgs a, QueueArgs q, GearA
                 const double y = sm[M::GEAR_CNEW + i];
                 const float v = a.convert[old] ? (float)((a.rev_conv[old] * densd) * y) : (float)y;
                 a.cgrid[(size_t)a.cgrid_index[old] * a.ncell + cell] = v;
+                if (a.yave) a.yave[(size_t)i * a.ncell + cell] = sm[M::GEAR_CAVEG + i];
             }
         } else {
             for (int i = lane; i < M::NSPEC; i += 32) g.y[(size_t)i * a.ncell + cell] = sm[M::GEAR_CNEW + i];

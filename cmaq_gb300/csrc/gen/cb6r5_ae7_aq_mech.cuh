@@ -57,7 +57,7 @@ constexpr int ADJ_EMIS = 5159;
 constexpr int ADJ_GE = 5308;
 constexpr int ADJ_GK = 5457;
 constexpr int OFF_YAVE = 2277;
-constexpr int GEAR_WS_ELEMS = 5159;
+constexpr int GEAR_WS_ELEMS = 5308;
 constexpr int GEAR_CNEW = 0;
 constexpr int GEAR_GLOSS = 298;
 constexpr int GEAR_DTLOS = 596;
@@ -66,6 +66,8 @@ constexpr int GEAR_CEST = 894;
 constexpr int GEAR_BLKCONC = 447;
 constexpr int GEAR_CONC = 4265;
 constexpr int GEAR_E = 149;
+constexpr int GEAR_CAVEG = 2277;
+constexpr int GEAR_CFINI = 5159;
 constexpr int EBIW_YC = 0;
 constexpr int EBIW_YC0 = 149;
 constexpr int EBIW_YCP = 298;
@@ -743,6 +745,8 @@ struct Traits {
     static constexpr int GEAR_BLKCONC = mech_cb6r5_ae7_aq::GEAR_BLKCONC;
     static constexpr int GEAR_CONC = mech_cb6r5_ae7_aq::GEAR_CONC;
     static constexpr int GEAR_E = mech_cb6r5_ae7_aq::GEAR_E;
+    static constexpr int GEAR_CAVEG = mech_cb6r5_ae7_aq::GEAR_CAVEG;
+    static constexpr int GEAR_CFINI = mech_cb6r5_ae7_aq::GEAR_CFINI;
     static constexpr int EBIW_YC = mech_cb6r5_ae7_aq::EBIW_YC;
     static constexpr int EBIW_YC0 = mech_cb6r5_ae7_aq::EBIW_YC0;
     static constexpr int EBIW_YCP = mech_cb6r5_ae7_aq::EBIW_YCP;

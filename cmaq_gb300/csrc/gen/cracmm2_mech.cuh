@@ -57,7 +57,7 @@ constexpr int ADJ_EMIS = 8092;
 constexpr int ADJ_GE = 8281;
 constexpr int ADJ_GK = 8470;
 constexpr int OFF_YAVE = 3295;
-constexpr int GEAR_WS_ELEMS = 8092;
+constexpr int GEAR_WS_ELEMS = 8281;
 constexpr int GEAR_CNEW = 0;
 constexpr int GEAR_GLOSS = 378;
 constexpr int GEAR_DTLOS = 756;
@@ -66,6 +66,8 @@ constexpr int GEAR_CEST = 1134;
 constexpr int GEAR_BLKCONC = 567;
 constexpr int GEAR_CONC = 6958;
 constexpr int GEAR_E = 189;
+constexpr int GEAR_CAVEG = 3295;
+constexpr int GEAR_CFINI = 8092;
 constexpr int EBIW_YC = 0;
 constexpr int EBIW_YC0 = 189;
 constexpr int EBIW_YCP = 378;
@@ -1107,6 +1109,8 @@ struct Traits {
     static constexpr int GEAR_BLKCONC = mech_cracmm2::GEAR_BLKCONC;
     static constexpr int GEAR_CONC = mech_cracmm2::GEAR_CONC;
     static constexpr int GEAR_E = mech_cracmm2::GEAR_E;
+    static constexpr int GEAR_CAVEG = mech_cracmm2::GEAR_CAVEG;
+    static constexpr int GEAR_CFINI = mech_cracmm2::GEAR_CFINI;
     static constexpr int EBIW_YC = mech_cracmm2::EBIW_YC;
     static constexpr int EBIW_YC0 = mech_cracmm2::EBIW_YC0;
     static constexpr int EBIW_YCP = mech_cracmm2::EBIW_YCP;

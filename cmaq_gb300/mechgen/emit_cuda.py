@@ -73,6 +73,10 @@ class Layout:
         # forward workspace (only the Gear kernels, per-warp stride GEAR_WS_ELEMS, use it)
         self.gear_conc = self.total
         self.gear_total = self.total + 6 * sp.ischan
+        # DDM-3D with SMVGEAR: CAVEG (time integral over the accepted steps) uses YAVE, CFINI
+        # (the state at the previous accepted step) follows the history
+        self.gear_cfini = self.gear_total
+        self.gear_total += ns
 
 
 def _w(k: int) -> str:
@@ -210,7 +214,8 @@ def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src
               ("ADJ_GK", lay.adj_gk), ("OFF_YAVE", lay.yave),
               ("GEAR_WS_ELEMS", lay.gear_total), ("GEAR_CNEW", lay.y), ("GEAR_GLOSS", lay.ydot),
               ("GEAR_DTLOS", lay.k1), ("GEAR_CHOLD", lay.k2), ("GEAR_CEST", lay.k3), ("GEAR_BLKCONC", lay.f0),
-              ("GEAR_CONC", lay.gear_conc), ("GEAR_E", lay.yp),
+              ("GEAR_CONC", lay.gear_conc), ("GEAR_E", lay.yp), ("GEAR_CAVEG", lay.yave),
+              ("GEAR_CFINI", lay.gear_cfini),
               # warp-cooperative EBI: one cell's state in shared memory (doubles)
               ("EBIW_YC", 0), ("EBIW_YC0", ns), ("EBIW_YCP", 2 * ns), ("EBIW_PROD", 3 * ns),
               ("EBIW_LOSS", 4 * ns), ("EBIW_PNEG", 5 * ns), ("EBIW_NOTMAX", 6 * ns), ("EBIW_RKI", 7 * ns),

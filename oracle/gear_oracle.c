@@ -127,6 +127,8 @@ typedef struct {
     double* gloss, *dtlos, *chold, *cest, *ceff;   /* (ld, ISCHAN) */
     double* blkconc;     /* initial CNEW, new order */
     double* dely, *ylowa, *yloweps, *yloweps1;     /* (ld) */
+    double* cfini;       /* DDM-3D: state at the previous accepted step (ld, ISCHAN) */
+    double* caveg;       /* DDM-3D: CAVEG (ld, ISCHAN) when not NULL (grsmvgear.F sens blocks) */
 } GearBlock;
 
 static void gear_alloc(GearBlock* g, int ld)
@@ -144,13 +146,15 @@ static void gear_alloc(GearBlock* g, int ld)
     g->ylowa = calloc((size_t)ld, sizeof(double));
     g->yloweps = calloc((size_t)ld, sizeof(double));
     g->yloweps1 = calloc((size_t)ld, sizeof(double));
+    g->cfini = calloc(ns, sizeof(double));
+    g->caveg = NULL;
 }
 
 static void gear_free(GearBlock* g)
 {
     block_free(&g->b);
     free(g->conc); free(g->gloss); free(g->dtlos); free(g->chold); free(g->cest); free(g->ceff);
-    free(g->blkconc); free(g->dely); free(g->ylowa); free(g->yloweps); free(g->yloweps1);
+    free(g->blkconc); free(g->dely); free(g->ylowa); free(g->yloweps); free(g->yloweps1); free(g->cfini);
 }
 
 /* SUBFUN: GLOSS = dc/dt at CNEW; a species at the floor does not lose mass further. */
@@ -309,6 +313,7 @@ static GearStats oracle_smvgear(GearBlock* g, int ncsp, int lsun, double chemste
 #define CO(col, c) conc[(size_t)(col) * ld + (c)]
 #define SP(arr, s, c) (arr)[(size_t)(s) * ld + (c)]
 #define ASET(i, j) cfg->aset[(i) - 1][(j) - 1]
+    if (g->caveg && !ordering) memset(g->caveg, 0, sizeof(double) * (size_t)isc * ld);   /* :273-274 */
     if (ordering) {
         for (int c = 0; c < n; ++c) g->ylowa[c] = cfg->ylow;
     } else {
@@ -368,6 +373,9 @@ loop_initialize:
     nqqold = 0;
     rdelt = 1.0;
     jeval = 1;
+    if (g->caveg)   /* CFINI = BLKCONC (grsmvgear.F:427-431) */
+        for (int j = 0; j < isc; ++j)
+            for (int c = 0; c < n; ++c) SP(g->cfini, j, c) = SP(g->blkconc, j, c);
 
 loop_order:
     higher_order = 1;
@@ -566,6 +574,13 @@ converged:
                     SP(cnew, i, c) = G_ZBOUND;
                     for (int k = 1; k <= 5; ++k) CO(i + k * isc, c) = 0.0;
                 }
+        if (g->caveg)   /* CAVEG += 0.5 (CFINI + CONC) DELT; CFINI = CONC (grsmvgear.F:841-849) */
+            for (int i = 0; i < isc; ++i)
+                for (int c = 0; c < n; ++c) {
+                    const double cv = CO(i, c);
+                    SP(g->caveg, i, c) = fma(0.5 * (SP(g->cfini, i, c) + cv), delt, SP(g->caveg, i, c));
+                    SP(g->cfini, i, c) = cv;
+                }
         if (idoub > 1) {
             idoub--;
             if (idoub == 1)
@@ -640,6 +655,11 @@ done:
             if (SP(cnew, i, c) <= G_ZBOUND) SP(cnew, i, c) = G_CONCMIN;
             if (!isfinite(SP(cnew, i, c))) st.status |= ST_NONFINITE;
         }
+    if (g->caveg) {   /* CAVEG / CHEMSTEP floored at CONCMIN (grsmvgear.F:1007-1013) */
+        const double rchem = 1.0 / chemstep;
+        for (int i = 0; i < isc; ++i)
+            for (int c = 0; c < n; ++c) SP(g->caveg, i, c) = g_max2(SP(g->caveg, i, c) * rchem, G_CONCMIN);
+    }
 #undef CO
 #undef SP
 #undef ASET

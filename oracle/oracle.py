@@ -63,7 +63,7 @@ def load(mech: str = "cb6r5_ae7_aq") -> C.CDLL:
     lib.oracle_adj_replay.argtypes = [C.c_long, dp, dp, C.c_long, u8p, dp, dp, C.c_int, ip, dp, C.c_int, C.c_int]
     lib.oracle_adj_replay.restype = None
     lib.oracle_ddm3d_window.argtypes = [C.c_long, dp, dp, C.c_long, u8p, dp, dp, C.c_int, C.c_double, C.c_double,
-                                        C.c_double, C.c_int, ip, ip, dp, C.c_int]
+                                        C.c_double, C.c_int, ip, ip, dp, C.c_int, C.c_void_p]
     lib.oracle_gear_cfg_size.restype = C.c_size_t
     lib.oracle_gear_cfg.argtypes = [C.c_double, C.c_float, C.c_float, C.c_float, C.c_int, C.c_void_p]
     lib.oracle_gear_cfg.restype = None
@@ -302,11 +302,14 @@ class AdjointWindow:
 
 
 def ddm3d_window(o: "Oracle", y0, rki, night, nsync: int, chemstep: float, rtol: float, atol: float, params,
-                 kmult=None, emis=None, threads: int = 0):
+                 kmult=None, emis=None, threads: int = 0, gear_cfg=None):
     """First-order DDM-3D sensitivities (CMAQ's SOLVE_DDM3D_CHEM restated) over a window.
     params: list of ("init", species index in solver order), ("rate", reaction index) or
     ("emis", species index: the emission tendency of that species in every cell).
-    Returns (y_end, s_end [nparam, nspec, n])."""
+    gear_cfg (Oracle.gear_cfg()): the steps are SMVGEAR's and the averages its CAVEG
+    (no emission tendency then).  Returns (y_end, s_end [nparam, nspec, n])."""
+    if gear_cfg is not None and emis is not None:
+        raise ValueError("the SMVGEAR path has no emission tendency")
     y = np.array(y0, np.float64, order="C", copy=True)
     rki = np.ascontiguousarray(rki, np.float64)
     stride = 0 if rki.ndim == 2 else rki.shape[1] * rki.shape[2]
@@ -320,7 +323,8 @@ def ddm3d_window(o: "Oracle", y0, rki, night, nsync: int, chemstep: float, rtol:
     bad = o.lib.oracle_ddm3d_window(n, _p(y, C.c_double), _p(rki, C.c_double), stride, _p(night, C.c_uint8),
                                     _opt(km, C.c_double), _opt(em, C.c_double), nsync, chemstep, rtol, atol,
                                     len(params),
-                                    _p(kind, C.c_int), _p(idx, C.c_int), _p(s_end, C.c_double), threads)
+                                    _p(kind, C.c_int), _p(idx, C.c_int), _p(s_end, C.c_double), threads,
+                                    gear_cfg)
     if bad:
         raise RuntimeError(f"{bad} failed cell-steps in the DDM-3D window")
     return y, s_end

@@ -478,8 +478,12 @@ static void lu_solve(const double* m, const int* piv, int n, double* b)
  * s_end[p][nspec][n] and the end state in y (the forward is the oracle's rbsolver). */
 int oracle_ddm3d_window(long n, double* y, const double* rki, long rki_stride, const uint8_t* night,
                         const double* kmult, const double* emis, int nsync, double chemstep, double rtol,
-                        double atol, int nparam, const int* kind, const int* idx, double* s_end, int threads)
+                        double atol, int nparam, const int* kind, const int* idx, double* s_end, int threads,
+                        const void* gear_cfg)
 {
+    /* gear_cfg != NULL: each step is SMVGEAR's (GearCfg of oracle_gear_cfg) and the averaged
+     * concentrations are its CAVEG (grdriver.F hands CAVEG to SOLVE_DDM3D_CHEM) */
+    const GearCfg* gcfg = (const GearCfg*)gear_cfg;
     int nbad = 0;
     const int ns = MECH_ISCHAN;
 #ifdef _OPENMP
@@ -496,6 +500,12 @@ int oracle_ddm3d_window(long n, double* y, const double* rki, long rki_stride, c
         double* sv = malloc(sizeof(double) * ns * (nparam > 0 ? nparam : 1));
         double yave[MECH_NSPEC], tmp[MECH_NSPEC], src[MECH_NSPEC], ebuf[MECH_NSPEC];
         SolverCfg cfg = {rtol, atol, (double)(1.0f / (float)MECH_NSPEC), 100000};
+        GearBlock gb;
+        if (gcfg) {
+            gear_alloc(&gb, 1);
+            gb.b.ncells = 1;
+            gb.caveg = yave;
+        }
 #ifdef _OPENMP
 #pragma omp for schedule(dynamic, 4)
 #endif
@@ -507,11 +517,20 @@ int oracle_ddm3d_window(long n, double* y, const double* rki, long rki_stride, c
             for (int k = 0; k < nsync; ++k) {
                 load_cell(&b, n, c, rki + (size_t)k * rki_stride, kmult, emis, ebuf);
                 memset(yave, 0, sizeof(yave));
-                b.yave = yave;
-                SolverStats st = oracle_rbsolver(&b, ncsp, chemstep, &cfg, NULL);
-                b.yave = NULL;
-                nbad += st.status != 0;
-                for (int s = 0; s < ns; ++s) yave[s] /= chemstep;
+                if (gcfg) {
+                    memcpy(gb.b.y, b.y, sizeof(double) * MECH_NSPEC);
+                    memcpy(gb.blkconc, b.y, sizeof(double) * MECH_NSPEC);
+                    memcpy(gb.b.rki, b.rki, sizeof(double) * MECH_NRXNS);
+                    GearStats gst = oracle_smvgear(&gb, ncsp, !night[c], chemstep, gcfg, NULL);
+                    memcpy(b.y, gb.b.y, sizeof(double) * MECH_NSPEC);
+                    nbad += gst.status != 0;
+                } else {
+                    b.yave = yave;
+                    SolverStats st = oracle_rbsolver(&b, ncsp, chemstep, &cfg, NULL);
+                    b.yave = NULL;
+                    nbad += st.status != 0;
+                    for (int s = 0; s < ns; ++s) yave[s] /= chemstep;
+                }
                 dense_jac(b.rki, yave, ncsp, jac);
                 for (int i = 0; i < ns * ns; ++i) am[i] = -0.5 * chemstep * jac[i];
                 for (int i = 0; i < ns; ++i) am[i * ns + i] += 1.0;
@@ -544,6 +563,7 @@ int oracle_ddm3d_window(long n, double* y, const double* rki, long rki_stride, c
         }
         free(jac); free(am); free(piv); free(sv);
         block_free(&b);
+        if (gcfg) gear_free(&gb);
     }
     return nbad;
 }

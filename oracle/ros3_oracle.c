@@ -652,8 +652,8 @@ int oracle_chem(OracleChemArgs* a)
     return nfailed;
 }
 
-/* ------------------------------------------------------------------ discrete adjoint */
-#include "ros3_adjoint.c"
-
 /* ------------------------------------------------------------------ SMVGEAR */
 #include "gear_oracle.c"
+
+/* ------------------------------------------------------------------ discrete adjoint, DDM-3D */
+#include "ros3_adjoint.c"

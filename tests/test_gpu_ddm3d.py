@@ -64,3 +64,42 @@ def test_ddm3d_leaves_concentrations_as_plain_chem():
                                      "khetero")])
     assert np.array_equal(t["conc"].cpu().numpy(), plain)
     assert float(sen.abs().max()) == 0.0
+
+
+@pytest.mark.parametrize("mech", ["cb6r5_ae7_aq", "cracmm2"])
+def test_ddm3d_with_smvgear_matches_oracle(mech):
+    """The DDM-3D step of a Gear CHEM call (CAVEG from the Gear kernel) against the oracle's
+    DDM-3D on SMVGEAR, both on the device's rate constants (SMVGEAR's discrete choices flip
+    on ulp differences of exp/pow); tolerance as above."""
+    import torch
+    from oracle import Oracle, ddm3d_window
+    from cmaq_gb300.chem import ChemSolver
+    o = Oracle(mech)
+    names = [sp["name"] for sp in manifest(mech)["species"]]
+    g = make_grid(mech=mech, ncols=8, nrows=6, nlays=3, seed=84, het=True)
+    s = ChemSolver(mech, ncols=g.ncols, nrows=g.nrows, nlays=g.nlays, nspcsd=g.nspcsd,
+                   cgrid_index=g.cgrid_index, rtol=1e-3, atol=1e-9, solver="gear")
+    t = to_cuda(g)
+    args = [t[k] for k in ("conc", "ta", "qv", "dens", "pres", "seaice", "ocean_szone", "rj", "khetero")]
+    rk_dev, _ = s.rconst(*args)
+    y0, _, night = gather_cells(g, o, gear=True)
+    i_o3, i_no2 = (int(o.iold2new[names.index(sp)]) for sp in ("O3", "NO2"))
+    r_a, r_b = 0, 2
+    params = [("init", i_o3), ("init", i_no2), ("rate", r_a), ("rate", r_b)]
+    _, s_ref = ddm3d_window(o, y0, rk_dev.cpu().numpy(), night, 1, 5.0, RTOL, ATOL, params, threads=4,
+                            gear_cfg=o.gear_cfg())
+    npar = len(params)
+    sen = torch.zeros((g.nspcsd, npar) + tuple(g.conc.shape[1:]), dtype=torch.float32, device="cuda")
+    sen[g.cgrid_index[names.index("O3")] - 1, 0] = 1.0
+    sen[g.cgrid_index[names.index("NO2")] - 1, 1] = 1.0
+    mask = torch.zeros((npar, o.nrxns), dtype=torch.uint8, device="cuda")
+    mask[2, r_a] = 1
+    mask[3, r_b] = 1
+    st = s.step_ddm(sen, *args, rate_mask=mask)
+    assert st["failed_cells"] == 0
+    got = sen.cpu().numpy().reshape(g.nspcsd, npar, -1)
+    for p in range(npar):
+        ref = s_ref[p]
+        gp = np.stack([got[g.cgrid_index[o.inew2old[i]] - 1, p] for i in range(o.nspec)])
+        scale = np.abs(ref).max()
+        assert np.abs(gp - ref).max() <= 1e-5 * scale, (p, np.abs(gp - ref).max() / scale)

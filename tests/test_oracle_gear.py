@@ -96,3 +96,23 @@ def test_gear_pow_accuracy():
             worst = max(worst, err / max(1.0, abs(y * np.log(x))))
     assert worst < 4e-16
     assert lib.oracle_gear_pow(0.0, 0.25) == 0.0
+
+
+def test_ddm3d_with_smvgear_agrees_with_ros3():
+    """DDM-3D driven by SMVGEAR's CAVEG (grsmvgear.F sens blocks) against DDM-3D driven by
+    ROS3's YAVE over one 5-min step: two solvers at rtol 1e-3 (measured 1e-4 to 3e-3 of
+    each parameter's largest sensitivity)."""
+    from oracle import Oracle, ddm3d_window
+    from cmaq_gb300.synthetic import manifest
+    for mech in ("cb6r5_ae7_aq", "cracmm2"):
+        o = Oracle(mech)
+        names = [sp["name"] for sp in manifest(mech)["species"]]
+        g = make_grid(mech=mech, ncols=6, nrows=4, nlays=2, seed=83, het=True)
+        y0, rk, night = gather_cells(g, o, gear=True)
+        params = [("init", int(o.iold2new[names.index("O3")])), ("init", int(o.iold2new[names.index("NO2")])),
+                  ("rate", 0), ("rate", 2)]
+        rt, at = float(F32(1e-3)), float(F32(1e-9))
+        _, s_r = ddm3d_window(o, y0, rk, night, 1, 5.0, rt, at, params, threads=4)
+        _, s_g = ddm3d_window(o, y0, rk, night, 1, 5.0, rt, at, params, threads=4, gear_cfg=o.gear_cfg())
+        for p in range(len(params)):
+            assert np.abs(s_g[p] - s_r[p]).max() <= 1e-2 * np.abs(s_r[p]).max()
