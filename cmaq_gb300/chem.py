@@ -5,9 +5,12 @@ CMAQ calls ``CHEM(CGRID, JDATE, JTIME, TSTEP)`` once per synchronisation step
 (rbdriver.F:226-371) and reads met, photolysis and heterogeneous rates through
 modules.  Here:
 
-* :class:`ChemSolver` owns a library handle (the first-call state) and exposes
-  ``step`` (one CHEM call), the solver-level ``solve`` (RBSOLVER with given rate
-  constants) and ``rconst`` (CALC_RCONST);
+* :class:`ChemSolver` owns a library handle (the first-call state) for one of the
+  reference's solvers (``solver="ros3"``, ``"ebi"`` or ``"gear"`` for SMVGEAR) and exposes
+  ``step`` (one CHEM call), ``steps`` (several, from one captured CUDA graph),
+  ``step_ddm`` (a CHEM call with DDM-3D sensitivities), the solver-level ``solve``
+  (RBSOLVER), ``ebi_solve`` (HRSOLVER) and ``gear_solve`` (SMVGEAR) with given rate
+  constants, and ``rconst`` (CALC_RCONST);
 * :func:`CHEM` keeps the reference's call signature; the implicit inputs are set
   with :func:`set_environment`, the analogue of the modules CHEM reads.
 
