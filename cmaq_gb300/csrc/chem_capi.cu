@@ -604,7 +604,6 @@ extern "C" int cmaqchem_step_ddm_device(cmaqchem_handle* h, float* conc, const f
     (void)jdate;
     (void)jtime;
     if (!h) return fail("null handle");
-    if (h->cfg.solver == CMAQCHEM_SOLVER_EBI) return fail("DDM-3D is available with the ROS3 and SMVGEAR solvers");
     if (nparam <= 0 || !sengrid) return fail("DDM-3D needs sengrid and nparam > 0");
     const void* ptrs[] = {conc, ta, qv, dens, pres, seaice, ocean_szone, rj, tstep, khetero};
     if (check_ptrs(ptrs, h->ops->nhetero > 0 ? 10 : 9)) return -1;

@@ -71,8 +71,12 @@ __device__ void start(double* __restrict__ ws, State& s, int n_ebi_steps, double
 }
 
 // One Backward-Euler iteration of the current sub-step and the bookkeeping that follows it.
+// yv (nullptr: off): the cell's YCDDM in the caller's YAVE array (solver species order,
+// stride ystride), YCDDM += (0.5 DTC) (YC + YC0) at every converged sub-step
+// (hrsolver.F:372-376)
 template <class M>
-__device__ void iterate(double* __restrict__ ws, State& s, int max_iter)
+__device__ void iterate(double* __restrict__ ws, State& s, int max_iter, double* yv = nullptr,
+                        long long ystride = 0)
 {
     if (s.total_iter >= max_iter) {
         s.status |= ST_MAXITER;
@@ -132,6 +136,13 @@ __device__ void iterate(double* __restrict__ ws, State& s, int max_iter)
     }
     s.lebi_conv = conv;
     if (conv) {                               // CYCLE SUBSTEP_EBI
+        if (yv) {
+            static_assert(M::ISCHAN == M::NSPEC, "YCDDM is stored in the solver's species order");
+            for (int i = 0; i < M::NSPEC; ++i) {
+                double& a = yv[(size_t)M::iold2new(i) * ystride];
+                a = fma(0.5 * dtc, ws[(M::EBI_OFF_YC + i) * 32] + ws[(M::EBI_OFF_YC0 + i) * 32], a);
+            }
+        }
         s.ninr++;
         s.substep_start = true;
         if (s.ninr <= s.n_inr_steps) return;
@@ -227,6 +238,23 @@ __device__ void scatter_cell_ebi(const GridArgs& a, const EbiArgs& e, long long 
 }
 
 // One EBI CHEM call; lanes pull cells from the work queue (ordered by previous iterations).
+// DDM-3D: YCDDM of a cell zeroed when the cell starts (hrsolver.F:169-171) and divided by
+// CHEMSTEP, values below 1e-25 set to zero, when it ends (:443-447); lanes first..., step
+template <class M>
+__device__ __forceinline__ void ycddm_zero(double* yv, long long stride, int first, int step)
+{
+    for (int i = first; i < M::NSPEC; i += step) yv[(size_t)i * stride] = 0.0;
+}
+template <class M>
+__device__ __forceinline__ void ycddm_finish(double* yv, long long stride, double chemstep, int first, int step)
+{
+    for (int i = first; i < M::NSPEC; i += step) {
+        double& a = yv[(size_t)i * stride];
+        a = a / chemstep;
+        if (a < 1.0e-25) a = 0.0;
+    }
+}
+
 template <class M>
 __global__ void __launch_bounds__(THREADS_PER_BLOCK, 1) k_chem_ebi_queue(GridArgs a, QueueArgs q, EbiArgs e)
 {
@@ -251,6 +279,7 @@ __global__ void __launch_bounds__(THREADS_PER_BLOCK, 1) k_chem_ebi_queue(GridArg
                         cell = q.cell0 + (q.order ? q.order[pos] : (long long)pos);
                         sun = gather_cell_ebi<M>(a, e, cell, ws);
                         ebi::start<M>(ws, s, e.n_ebi_steps, e.tmstep);
+                        if (a.yave) ycddm_zero<M>(a.yave + cell, a.ncell, 0, 1);
                     }
                 }
                 drained = __any_sync(0xffffffffu, base + __popc(need) >= queue_len(q, a.ncell));
@@ -259,12 +288,13 @@ __global__ void __launch_bounds__(THREADS_PER_BLOCK, 1) k_chem_ebi_queue(GridArg
         const bool busy = cell >= 0;
         if (!__any_sync(0xffffffffu, busy)) break;
         if (busy) {
-            ebi::iterate<M>(ws, s, a.max_iter);
+            ebi::iterate<M>(ws, s, a.max_iter, a.yave ? a.yave + cell : nullptr, a.ncell);
             if (!s.done && e.defer_after > 0 && s.total_iter >= e.defer_after) {
                 e.deferred[atomicAdd(e.ndeferred, 1ull)] = (int)cell;
                 cell = -1;
             } else if (s.done) {
                 scatter_cell_ebi<M>(a, e, cell, ws);
+                if (a.yave) ycddm_finish<M>(a.yave + cell, a.ncell, a.chemstep, 0, 1);
                 iters += s.total_iter;
                 failed += s.status != ebi::ST_OK;
                 sunlit += sun;
@@ -384,7 +414,8 @@ __device__ void ebiw_gather(const GridArgs& a, const EbiArgs& e, long long c, do
 // One Backward-Euler iteration of the warp's cell plus HRSOLVER's bookkeeping (the same
 // control flow as ebi::iterate; the scalar state is kept identically by every lane).
 template <class M>
-__device__ void ebiw_iterate(double* __restrict__ sm, ebi::State& s, int max_iter, int lane)
+__device__ void ebiw_iterate(double* __restrict__ sm, ebi::State& s, int max_iter, int lane, double* yv = nullptr,
+                             long long ystride = 0)
 {
     using namespace ebi;
     if (s.total_iter >= max_iter) {
@@ -482,6 +513,11 @@ __device__ void ebiw_iterate(double* __restrict__ sm, ebi::State& s, int max_ite
     mxfl = __any_sync(0xffffffffu, mxfl);
     s.lebi_conv = conv;
     if (conv) {
+        if (yv)   // each lane its own species, whose YC and YC0 it wrote itself
+            for (int i = lane; i < M::NSPEC; i += 32) {
+                double& a = yv[(size_t)M::iold2new(i) * ystride];
+                a = fma(0.5 * dtc, sm[M::EBIW_YC + i] + sm[M::EBIW_YC0 + i], a);
+            }
         s.ninr++;
         s.substep_start = true;
         if (s.ninr <= s.n_inr_steps) return;
@@ -549,8 +585,12 @@ __global__ void __launch_bounds__(EBIW_WPB * 32) k_chem_ebi_warp(GridArgs a, Que
         s.substep_start = true;
         s.done = false;
         s.status = ebi::ST_OK;
-        while (!s.done) ebiw_iterate<M>(sm, s, a.max_iter, lane);
+        double* yv = a.yave ? a.yave + cell : nullptr;
+        if (yv) ycddm_zero<M>(yv, a.ncell, lane, 32);
         __syncwarp();
+        while (!s.done) ebiw_iterate<M>(sm, s, a.max_iter, lane, yv, a.ncell);
+        __syncwarp();
+        if (yv) ycddm_finish<M>(yv, a.ncell, a.chemstep, lane, 32);
         const float dens = a.dens[cell];
         for (int sp = lane; sp < M::NSPEC; sp += 32) {   // write-back (hrdriver.F:446-454)
             const double y = fmax(sm[M::EBIW_YC + sp], 1.0e-30);

@@ -129,8 +129,9 @@ int cmaqchem_steps_device(cmaqchem_handle* h, float* conc, const float* ta, cons
  * [nparam][nrxns] (device, may be NULL) marks the reactions of reaction-rate parameters
  * (IPT = 5: IRXN(NP, RXN) = 1); region [nparam][ncols*nrows*nlays] (device, may be NULL
  * for 1) weights their source as IREGION does.  Parameters with no reaction in the mask
- * (initial and boundary conditions, emissions) only propagate.  ROS3 and SMVGEAR solvers
- * (with SMVGEAR the time-averaged concentrations are its CAVEG, grsmvgear.F sens blocks). */
+ * (initial and boundary conditions, emissions) only propagate.  Any solver: the
+ * time-averaged concentrations are ROS3's YAVE, SMVGEAR's CAVEG or EBI's YCDDM (the
+ * sens blocks of rbsolver.F, grsmvgear.F and hrsolver.F). */
 int cmaqchem_step_ddm_device(cmaqchem_handle* h, float* conc, const float* ta, const float* qv,
                              const float* dens, const float* pres, const float* seaice,
                              const float* ocean_szone, const float* rj, const double* khetero,

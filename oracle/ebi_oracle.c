@@ -46,8 +46,9 @@ static const double EBI_DTMIN = 1.0e-08, EBI_EPSLON = 1.0e-30, EBI_MAXPRED = 1.0
                     EBI_FLOOR = 1.0e-08;
 
 /* HRSOLVER for one cell; returns 0, or ST_DT_UNDERFLOW when the sub-step fell to DTMIN
- * (the reference stops the run there).  n_it counts Backward-Euler iterations. */
-static int ebi_hrsolver(EbiCell* c, double ebi_tmstep, int n_ebi_steps, long* n_it, int max_iter)
+ * (the reference stops the run there).  n_it counts Backward-Euler iterations.  ycddm
+ * (NULL: off): YCDDM += (0.5 DTC) (YC + YC0) at every converged sub-step (hrsolver.F:372-376). */
+static int ebi_hrsolver(EbiCell* c, double ebi_tmstep, int n_ebi_steps, long* n_it, int max_iter, double* ycddm)
 {
     int notmax[MECH_NSPEC];
     double dtc = ebi_tmstep;
@@ -101,6 +102,8 @@ static int ebi_hrsolver(EbiCell* c, double ebi_tmstep, int n_ebi_steps, long* n_
                 if (mxfl) break;
                 if (lebi_conv) {
                     converged = 1;
+                    if (ycddm)
+                        for (int s = 0; s < MECH_NSPEC; ++s) ycddm[s] = fma(0.5 * dtc, c->yc[s] + c->yc0[s], ycddm[s]);
                     break;
                 }
             }
@@ -162,13 +165,72 @@ int oracle_ebi_solve_cells(long n, int tstep_sec, double* yc, const double* rki,
         for (int s = 0; s < MECH_NSPEC; ++s) c.yc[s] = yc[(size_t)s * n + i];
         for (int r = 0; r < MECH_NRXNS; ++r) c.rki[r] = rki[(size_t)r * n + i];
         long it = 0;
-        const int st = ebi_hrsolver(&c, ebi_tmstep, n_ebi_steps, &it, 0);
+        const int st = ebi_hrsolver(&c, ebi_tmstep, n_ebi_steps, &it, 0, NULL);
         for (int s = 0; s < MECH_NSPEC; ++s) yc[(size_t)s * n + i] = c.yc[s];
         if (status) status[i] = st;
         if (iters) iters[i] = it;
         nbad += st != 0;
     }
     return nbad;
+}
+
+/* HRSOLVER for one cell (yc mechanism order, in place) with the DDM-3D average YCDDM of
+ * the call: zeroed first (hrsolver.F:169-171), divided by CHEMSTEP and values below 1e-25
+ * set to zero after (:443-447), also when the cell failed.  Returns the cell's status. */
+int oracle_ebi_cell(double* yc, const double* rki, int tstep_sec, double* ycddm)
+{
+    int n_ebi_steps;
+    double ebi_tmstep;
+    ebi_steps(tstep_sec, &n_ebi_steps, &ebi_tmstep);
+    EbiCell c;
+    memset(&c, 0, sizeof(c));
+    memcpy(c.yc, yc, sizeof(c.yc));
+    memcpy(c.rki, rki, sizeof(c.rki));
+    for (int s = 0; s < MECH_NSPEC; ++s) ycddm[s] = 0.0;
+    long it = 0;
+    const int st = ebi_hrsolver(&c, ebi_tmstep, n_ebi_steps, &it, 0, ycddm);
+    const double chemstep = (double)tstep_sec / 60.0;
+    for (int s = 0; s < MECH_NSPEC; ++s) {
+        ycddm[s] = ycddm[s] / chemstep;
+        if (ycddm[s] < 1.0e-25) ycddm[s] = 0.0;
+    }
+    memcpy(yc, c.yc, sizeof(c.yc));
+    return st;
+}
+
+/* The EBI driver's gather of every cell (hrdriver.F:372-415): yc[nspec][ncell] mechanism
+ * order, rki[nrxns][ncell] from CALC_RCONST, night[ncell] = no sunlight. */
+void oracle_ebi_gather(const OracleChemArgs* a, double* yc, double* rki, uint8_t* night)
+{
+    const long nxy = (long)a->ncols * a->nrows;
+    const long ncell = nxy * a->nlays;
+    float fwd[MECH_NSPEC];
+    for (int s = 0; s < MECH_NSPEC; ++s) fwd[s] = (float)((double)(1.0e-3f * 28.9628f) / mech_molwt[s]);
+    const double pa2atm = (double)(1.0f / 101325.0f);
+    const float maomv = 1.0e6f * 28.9628f / 18.0153f;
+    for (long g = 0; g < ncell; ++g) {
+        const long col2 = g % nxy;
+        const float inv_dens = 1.0f / a->dens[g];
+        for (int s = 0; s < MECH_NSPEC; ++s) {
+            const float cv = a->conc[(size_t)a->cgrid_index[s] * ncell + g];
+            yc[(size_t)s * ncell + g] =
+                a->convert[s] ? (double)fmaxf(1.0e-30f, inv_dens * fwd[s] * cv) : (double)fmaxf(cv, 1.0e-30f);
+        }
+        const double temp = (double)a->ta[g];
+        const double atmpres = pa2atm * (double)a->pres[g];
+        const double h2o = (double)fmaxf(maomv * a->qv[g], 0.0f);
+        const double seawater = fmax(0.0, (double)(a->ocean_szone[col2] - a->seaice[col2]));
+        double rjin[MECH_NPHOTAB], het[MECH_NHETERO > 0 ? MECH_NHETERO : 1], rk[MECH_NRXNS];
+        int lsun = 0;
+        for (int k = 0; k < MECH_NPHOTAB; ++k) {
+            rjin[k] = (double)a->rj[(size_t)k * ncell + g];
+            if (rjin[k] > 0.0) lsun = 1;
+        }
+        for (int k = 0; k < MECH_NHETERO; ++k) het[k] = a->khetero[(size_t)g * MECH_NHETERO + k];
+        mech_calc_rconst(1, 1, &temp, &atmpres, &h2o, rjin, het, lsun, &seawater, rk);
+        for (int r = 0; r < MECH_NRXNS; ++r) rki[(size_t)r * ncell + g] = rk[r];
+        night[g] = lsun ? 0 : 1;
+    }
 }
 
 /* One EBI CHEM call (hrdriver.F) on the whole grid. */
@@ -215,7 +277,7 @@ int oracle_chem_ebi(OracleChemArgs* a)
         for (int k = 0; k < MECH_NHETERO; ++k) het[k] = a->khetero[(size_t)g * MECH_NHETERO + k];
         mech_calc_rconst(1, 1, &temp, &atmpres, &h2o, rjin, het, lsun, &seawater, c.rki);
         long it = 0;
-        const int st = ebi_hrsolver(&c, ebi_tmstep, n_ebi_steps, &it, a->max_iter);
+        const int st = ebi_hrsolver(&c, ebi_tmstep, n_ebi_steps, &it, a->max_iter, NULL);
         tot_it += it;
         nbad += st != 0;
         const float dens = a->dens[g];

@@ -63,7 +63,9 @@ def load(mech: str = "cb6r5_ae7_aq") -> C.CDLL:
     lib.oracle_adj_replay.argtypes = [C.c_long, dp, dp, C.c_long, u8p, dp, dp, C.c_int, ip, dp, C.c_int, C.c_int]
     lib.oracle_adj_replay.restype = None
     lib.oracle_ddm3d_window.argtypes = [C.c_long, dp, dp, C.c_long, u8p, dp, dp, C.c_int, C.c_double, C.c_double,
-                                        C.c_double, C.c_int, ip, ip, dp, C.c_int, C.c_void_p]
+                                        C.c_double, C.c_int, ip, ip, dp, C.c_int, C.c_void_p, C.c_int]
+    lib.oracle_ebi_gather.argtypes = [C.POINTER(OracleChemArgs), dp, dp, u8p]
+    lib.oracle_ebi_gather.restype = None
     lib.oracle_gear_cfg_size.restype = C.c_size_t
     lib.oracle_gear_cfg.argtypes = [C.c_double, C.c_float, C.c_float, C.c_float, C.c_int, C.c_void_p]
     lib.oracle_gear_cfg.restype = None
@@ -231,6 +233,23 @@ class Oracle:
         return conc, {"rc": rc, "nsteps": a.nsteps_total, "nfails": a.nfails_total,
                       "nfailed_blocks": a.nfailed_blocks}
 
+    def ebi_gather(self, g):
+        """The EBI driver's gather of a GridInputs-like object: (yc [nspec, n] mechanism order,
+        rki [nrxns, n], night [n])."""
+        conc = np.ascontiguousarray(g.conc, np.float32)
+        man_cgi = np.ascontiguousarray(g.cgrid_index - 1, np.int32)
+        convert = np.ascontiguousarray(self.convert_flags(g.mech), np.int32)
+        a = OracleChemArgs(g.ncols, g.nrows, g.nlays, g.nspcsd, _p(conc, C.c_float), _p(man_cgi, C.c_int),
+                           _p(convert, C.c_int), _p(g.ta, C.c_float), _p(g.qv, C.c_float), _p(g.dens, C.c_float),
+                           _p(g.pres, C.c_float), _p(g.seaice, C.c_float), _p(g.ocean_szone, C.c_float),
+                           _p(g.rj, C.c_float), _p(g.khetero, C.c_double), 300, 0.0, 0.0, 1, 0, 0, 0, 0, 0, 0)
+        n = g.ncell
+        yc = np.zeros((self.nspec, n))
+        rki = np.zeros((self.nrxns, n))
+        night = np.zeros(n, np.uint8)
+        self.lib.oracle_ebi_gather(C.byref(a), _p(yc, C.c_double), _p(rki, C.c_double), _p(night, C.c_uint8))
+        return yc, rki, night
+
     @staticmethod
     def convert_flags(mech: str) -> np.ndarray:
         import json
@@ -302,14 +321,15 @@ class AdjointWindow:
 
 
 def ddm3d_window(o: "Oracle", y0, rki, night, nsync: int, chemstep: float, rtol: float, atol: float, params,
-                 kmult=None, emis=None, threads: int = 0, gear_cfg=None):
+                 kmult=None, emis=None, threads: int = 0, gear_cfg=None, ebi: bool = False):
     """First-order DDM-3D sensitivities (CMAQ's SOLVE_DDM3D_CHEM restated) over a window.
     params: list of ("init", species index in solver order), ("rate", reaction index) or
     ("emis", species index: the emission tendency of that species in every cell).
-    gear_cfg (Oracle.gear_cfg()): the steps are SMVGEAR's and the averages its CAVEG
-    (no emission tendency then).  Returns (y_end, s_end [nparam, nspec, n])."""
-    if gear_cfg is not None and emis is not None:
-        raise ValueError("the SMVGEAR path has no emission tendency")
+    gear_cfg (Oracle.gear_cfg()): the steps are SMVGEAR's and the averages its CAVEG;
+    ebi: the steps are HRSOLVER's and the averages its YCDDM (no emission tendency in
+    either).  Returns (y_end, s_end [nparam, nspec, n])."""
+    if (gear_cfg is not None or ebi) and emis is not None:
+        raise ValueError("the SMVGEAR and EBI paths have no emission tendency")
     y = np.array(y0, np.float64, order="C", copy=True)
     rki = np.ascontiguousarray(rki, np.float64)
     stride = 0 if rki.ndim == 2 else rki.shape[1] * rki.shape[2]
@@ -324,7 +344,7 @@ def ddm3d_window(o: "Oracle", y0, rki, night, nsync: int, chemstep: float, rtol:
                                     _opt(km, C.c_double), _opt(em, C.c_double), nsync, chemstep, rtol, atol,
                                     len(params),
                                     _p(kind, C.c_int), _p(idx, C.c_int), _p(s_end, C.c_double), threads,
-                                    gear_cfg)
+                                    gear_cfg, int(bool(ebi)))
     if bad:
         raise RuntimeError(f"{bad} failed cell-steps in the DDM-3D window")
     return y, s_end

@@ -476,13 +476,16 @@ static void lu_solve(const double* m, const int* piv, int n, double* b)
  * parameter; here the emission enters f, so DT times it is the step's source).  emis
  * [nspec][n] (or NULL) is the emission tendency of the forward.  Returns
  * s_end[p][nspec][n] and the end state in y (the forward is the oracle's rbsolver). */
+int oracle_ebi_cell(double* yc, const double* rki, int tstep_sec, double* ycddm);   /* ebi_oracle.c */
+
 int oracle_ddm3d_window(long n, double* y, const double* rki, long rki_stride, const uint8_t* night,
                         const double* kmult, const double* emis, int nsync, double chemstep, double rtol,
                         double atol, int nparam, const int* kind, const int* idx, double* s_end, int threads,
-                        const void* gear_cfg)
+                        const void* gear_cfg, int ebi)
 {
     /* gear_cfg != NULL: each step is SMVGEAR's (GearCfg of oracle_gear_cfg) and the averaged
-     * concentrations are its CAVEG (grdriver.F hands CAVEG to SOLVE_DDM3D_CHEM) */
+     * concentrations are its CAVEG (grdriver.F hands CAVEG to SOLVE_DDM3D_CHEM); ebi != 0:
+     * each step is HRSOLVER's and the averages its YCDDM (hrdriver.F:477-490) */
     const GearCfg* gcfg = (const GearCfg*)gear_cfg;
     int nbad = 0;
     const int ns = MECH_ISCHAN;
@@ -517,7 +520,15 @@ int oracle_ddm3d_window(long n, double* y, const double* rki, long rki_stride, c
             for (int k = 0; k < nsync; ++k) {
                 load_cell(&b, n, c, rki + (size_t)k * rki_stride, kmult, emis, ebuf);
                 memset(yave, 0, sizeof(yave));
-                if (gcfg) {
+                if (ebi) {
+                    double ycm[MECH_NSPEC], ydd[MECH_NSPEC];
+                    for (int s = 0; s < MECH_NSPEC; ++s) ycm[s] = b.y[mech_iold2new[s]];
+                    nbad += oracle_ebi_cell(ycm, b.rki, (int)lround(chemstep * 60.0), ydd) != 0;
+                    for (int s = 0; s < MECH_NSPEC; ++s) {
+                        b.y[mech_iold2new[s]] = ycm[s];
+                        yave[mech_iold2new[s]] = ydd[s];
+                    }
+                } else if (gcfg) {
                     memcpy(gb.b.y, b.y, sizeof(double) * MECH_NSPEC);
                     memcpy(gb.blkconc, b.y, sizeof(double) * MECH_NSPEC);
                     memcpy(gb.b.rki, b.rki, sizeof(double) * MECH_NRXNS);

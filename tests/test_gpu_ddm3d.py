@@ -103,3 +103,42 @@ def test_ddm3d_with_smvgear_matches_oracle(mech):
         gp = np.stack([got[g.cgrid_index[o.inew2old[i]] - 1, p] for i in range(o.nspec)])
         scale = np.abs(ref).max()
         assert np.abs(gp - ref).max() <= 1e-5 * scale, (p, np.abs(gp - ref).max() / scale)
+
+
+@pytest.mark.parametrize("mech", ["cb6r5_ae7_aq", "cracmm2"])
+def test_ddm3d_with_ebi_matches_oracle(mech):
+    """The DDM-3D step of an EBI CHEM call (YCDDM from the EBI kernels) against the oracle's
+    DDM-3D on HRSOLVER with the EBI driver's gather.  Device and host rate constants differ
+    by ulps (exp/pow), which can move EBI's convergence test in single cells: tolerance 1e-4
+    of each parameter's largest sensitivity."""
+    import torch
+    from oracle import Oracle, ddm3d_window
+    from cmaq_gb300.chem import ChemSolver
+    o = Oracle(mech)
+    names = [sp["name"] for sp in manifest(mech)["species"]]
+    g = make_grid(mech=mech, ncols=8, nrows=6, nlays=3, seed=86, het=True)
+    yc, rk, night = o.ebi_gather(g)
+    y0 = yc[o.inew2old]
+    i_o3, i_no2 = (int(o.iold2new[names.index(sp)]) for sp in ("O3", "NO2"))
+    r_a, r_b = 0, 2
+    params = [("init", i_o3), ("init", i_no2), ("rate", r_a), ("rate", r_b)]
+    _, s_ref = ddm3d_window(o, y0, rk, night, 1, 5.0, RTOL, ATOL, params, threads=4, ebi=True)
+    s = ChemSolver(mech, ncols=g.ncols, nrows=g.nrows, nlays=g.nlays, nspcsd=g.nspcsd,
+                   cgrid_index=g.cgrid_index, rtol=1e-3, atol=1e-9, solver="ebi")
+    t = to_cuda(g)
+    npar = len(params)
+    sen = torch.zeros((g.nspcsd, npar) + tuple(g.conc.shape[1:]), dtype=torch.float32, device="cuda")
+    sen[g.cgrid_index[names.index("O3")] - 1, 0] = 1.0
+    sen[g.cgrid_index[names.index("NO2")] - 1, 1] = 1.0
+    mask = torch.zeros((npar, o.nrxns), dtype=torch.uint8, device="cuda")
+    mask[2, r_a] = 1
+    mask[3, r_b] = 1
+    st = s.step_ddm(sen, *[t[k] for k in ("conc", "ta", "qv", "dens", "pres", "seaice", "ocean_szone", "rj",
+                                          "khetero")], rate_mask=mask)
+    assert st["failed_cells"] == 0
+    got = sen.cpu().numpy().reshape(g.nspcsd, npar, -1)
+    for p in range(npar):
+        ref = s_ref[p]
+        gp = np.stack([got[g.cgrid_index[o.inew2old[i]] - 1, p] for i in range(o.nspec)])
+        scale = np.abs(ref).max()
+        assert np.abs(gp - ref).max() <= 1e-4 * scale, (p, np.abs(gp - ref).max() / scale)
