@@ -42,3 +42,59 @@ def test_fortran_shim_binds_the_header_names():
         pytest.skip("INTEGRATION.md not written yet")
     for n in ("cmaqchem_init", "cmaqchem_step", "cmaqchem_last_error"):
         assert n in shim
+
+
+HOST_PROGRAM = r"""
+#include <stdio.h>
+#include <stdlib.h>
+#include "cmaqchem.h"
+
+int main(void) {
+    cmaqchem_mech_info info;
+    int* order;
+    int i, sum = 0;
+    char msg[256];
+    if (cmaqchem_mech_info_get("cb6r5_ae7_aq", &info, NULL) != 0) return 2;
+    order = (int*)malloc(sizeof(int) * (size_t)info.nspec);
+    if (cmaqchem_mech_info_get("cb6r5_ae7_aq", NULL, order) != 0) return 3;
+    for (i = 0; i < info.nspec; ++i) sum += order[i];
+    free(order);
+    if (cmaqchem_mech_info_get("not_a_mechanism", &info, NULL) == 0) return 4;
+    cmaqchem_last_error(msg, sizeof msg);
+    printf("%d %d %d %d %d\n%s\n", info.nspec, info.nrxns, info.iarray_day, info.iarray_night, sum, msg);
+    return 0;
+}
+"""
+
+
+def _gcc():
+    import shutil
+    return shutil.which("gcc")
+
+
+@pytest.mark.skipif(_gcc() is None, reason="no C compiler")
+@pytest.mark.parametrize("lang,std", [("c", "-std=c99"), ("c++", "-std=c++11")])
+def test_headers_compile_standalone(lang, std):
+    """Each public header compiles on its own, as C for a Fortran/C host and as C++."""
+    import subprocess
+    for h in sorted((ROOT / "include").glob("*.h")):
+        r = subprocess.run([_gcc(), std, "-Wall", "-Wextra", "-Werror", "-pedantic", "-fsyntax-only", "-x", lang,
+                            str(h)], capture_output=True, text=True)
+        assert r.returncode == 0, (h.name, r.stderr)
+
+
+@pytest.mark.skipif(_gcc() is None or not LIB.exists(), reason="no C compiler or libcmaqchem.so not built")
+def test_c_host_program_links_and_calls(tmp_path):
+    """A plain C program built against include/cmaqchem.h links libcmaqchem.so and calls
+    the host-only entry points, the way a non-Python host model binds the library."""
+    import subprocess
+    src = tmp_path / "host.c"
+    src.write_text(HOST_PROGRAM)
+    exe = tmp_path / "host"
+    subprocess.run([_gcc(), "-std=c99", "-Wall", "-Werror", "-I", str(ROOT / "include"), str(src), "-o", str(exe),
+                    "-L", str(LIB.parent), "-lcmaqchem", f"-Wl,-rpath,{LIB.parent}"], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr
+    first, msg = r.stdout.splitlines()[:2]
+    assert first.split() == ["149", "349", "1689", "1615", str(sum(range(149)))]
+    assert "unknown mechanism" in msg
