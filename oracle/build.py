@@ -3,7 +3,8 @@
     python oracle/build.py [mech ...]
 
 Compiles ``oracle/ros3_oracle.c`` once per mechanism into
-``oracle/_build/liboracle_<mech>.so`` with gcc.  ``-ffp-contract=off`` keeps the
+``oracle/_build/liboracle_<mech>.so`` with gcc, and ``oracle/kmt2_oracle.c`` (the
+KMT2 aqueous cloud chemistry, one mechanism) into ``oracle/_build/liboracle_kmt2.so``.  ``-ffp-contract=off`` keeps the
 compiler from fusing operations beyond the explicit ``fma`` calls; no
 ``-march`` flag, so the library builds the same on x86-64 and aarch64.
 
@@ -25,6 +26,15 @@ def lib_path(mech: str) -> Path:
     return HERE / "_build" / f"liboracle_{mech}.so"
 
 
+def kmt2_lib_path() -> Path:
+    return HERE / "_build" / "liboracle_kmt2.so"
+
+
+def _gcc(srcs, out: Path, defines=()):
+    return ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
+            *defines, "-Wno-unused-function", "-I", str(HERE), *[str(s) for s in srcs], "-o", str(out) + ".tmp", "-lm"]
+
+
 def build(mechs=MECHS, force: bool = False) -> list[Path]:
     out_dir = HERE / "_build"
     out_dir.mkdir(exist_ok=True)
@@ -37,13 +47,16 @@ def build(mechs=MECHS, force: bool = False) -> list[Path]:
         out = lib_path(mech)
         outs.append(out)
         newest = max(p.stat().st_mtime for p in (src, src_ebi, gen, gen_ebi, HERE / "oracle.h",
-                                                 HERE / "ros3_adjoint.c", HERE / "gear_oracle.c"))
+                                                 HERE / "ros3_adjoint.c", HERE / "gear_oracle.c",
+                                                 HERE / "portable_pow.h"))
         if not force and out.exists() and out.stat().st_mtime > newest:
             continue
-        cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
-               "-fno-fast-math", f'-DMECH_SOURCE="gen/{mech}_mech.c"', f'-DEBI_SOURCE="gen/{mech}_ebi.c"',
-               "-Wno-unused-function", "-I", str(HERE), str(src), str(src_ebi), "-o", str(out) + ".tmp", "-lm"]
+        cmd = _gcc([src, src_ebi], out, (f'-DMECH_SOURCE="gen/{mech}_mech.c"', f'-DEBI_SOURCE="gen/{mech}_ebi.c"'))
         procs.append((subprocess.Popen(cmd, cwd=HERE), out))
+    kout = kmt2_lib_path()
+    kdeps = (HERE / "kmt2_oracle.c", HERE / "gen" / "kmt2_aq.c", HERE / "portable_pow.h")
+    if force or not kout.exists() or kout.stat().st_mtime <= max(p.stat().st_mtime for p in kdeps):
+        procs.append((subprocess.Popen(_gcc([kdeps[0]], kout), cwd=HERE), kout))
     for p, out in procs:
         if p.wait() != 0:
             raise RuntimeError(f"oracle build failed for {out.name}")

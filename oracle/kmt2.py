@@ -1,0 +1,197 @@
+"""ctypes binding of the KMT2 aqueous-chemistry oracle (test infrastructure only).
+
+Loads ``oracle/_build/liboracle_kmt2.so`` (``oracle/kmt2_oracle.c`` with the tables of
+``oracle/gen/kmt2_aq.c``), a C restatement of the kinetic core of CMAQ's KMT2 cloud
+chemistry (CCTM/src/cloud/acm_ae7_kmt2: AQCHEM's set-up, the KPP rate laws, Fun,
+Jac_SP, KppDecomp / KppSolve and the Rodas3 Rosenbrock integrator).  Nothing in the
+product imports it.
+
+``synthetic_cells`` makes seeded cloudy-cell inputs: the AQCHEM arguments the kinetic
+core reads and the state vector as Initialize maps it from the gas and aerosol arrays
+(aqchem_Initialize.F90:308-421), in mixing ratios with ranges typical of polluted and
+clean continental clouds.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from functools import lru_cache
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+
+P_TEMP2, P_PRES_PA, P_TAUCLD, P_PRCRATE, P_WCAVG, P_WTAVG, P_AIRM, P_ALFA0, P_ALFA3, P_COSZEN, P_JH2O2, P_HO, \
+    P_ISPC8, P_MTPYRAC, P_PHOTO = range(15)
+STATS = ("nstp", "nacc", "nrej", "nfun", "njac", "ndec", "nsol", "nsng", "ierr", "nkron")
+
+
+@lru_cache(maxsize=None)
+def load() -> C.CDLL:
+    import sys
+    sys.path.insert(0, str(HERE))
+    try:
+        import build as _b  # oracle/build.py
+    finally:
+        sys.path.pop(0)
+    _b.build([])            # incremental: rebuilds the KMT2 library when its sources changed
+    path = _b.kmt2_lib_path()
+    lib = C.CDLL(str(path))
+    dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int)
+    lib.oracle_kq_sizes.argtypes = [ip]
+    lib.oracle_kq_name.argtypes = [C.c_int]
+    lib.oracle_kq_name.restype = C.c_char_p
+    lib.oracle_kq_lu_structure.argtypes = [ip, ip, ip]
+    lib.oracle_kq_setup.argtypes = [dp, dp, dp, dp, dp, dp, dp]
+    lib.oracle_kq_rconst_at.argtypes = [dp, dp, dp, dp]
+    lib.oracle_kq_fun.argtypes = [dp, dp, dp, dp]
+    lib.oracle_kq_fun.restype = None
+    lib.oracle_kq_jac.argtypes = [dp, dp, dp, dp]
+    lib.oracle_kq_jac.restype = None
+    lib.oracle_kq_decomp.argtypes = [dp]
+    lib.oracle_kq_solve.argtypes = [dp, dp]
+    lib.oracle_kq_solve.restype = None
+    lib.oracle_kq_set_rtol_scale.argtypes = [C.c_double]
+    lib.oracle_kq_set_rtol_scale.restype = None
+    lib.oracle_kq_cells.argtypes = [C.c_longlong, dp, dp, dp, dp, ip, C.c_int]
+    return lib
+
+
+def _p(a: np.ndarray, ct=C.c_double):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+class KMT2Oracle:
+    def __init__(self):
+        self.lib = load()
+        s = (C.c_int * 8)()
+        self.lib.oracle_kq_sizes(s)
+        self.nvar, self.nfix, self.nreact, self.lu_nonzero, self.nb, self.nhenry, self.nparam, self.nstat = list(s)
+        self.names = [self.lib.oracle_kq_name(i).decode() for i in range(self.nvar + self.nfix)]
+        self.index = {n: i for i, n in enumerate(self.names)}
+        icol = np.zeros(self.lu_nonzero, np.int32)
+        crow = np.zeros(self.nvar + 1, np.int32)
+        diag = np.zeros(self.nvar + 1, np.int32)
+        self.lib.oracle_kq_lu_structure(_p(icol, C.c_int), _p(crow, C.c_int), _p(diag, C.c_int))
+        self.lu_icol, self.lu_crow, self.lu_diag = icol, crow, diag
+        self.lu_irow = np.repeat(np.arange(self.nvar, dtype=np.int32), np.diff(crow))
+
+    # ------------------------------------------------------------------ pieces
+    def setup(self, params, var_mix):
+        params = np.ascontiguousarray(params, np.float64)
+        var_mix = np.ascontiguousarray(var_mix, np.float64)
+        var = np.zeros(self.nvar)
+        fix = np.zeros(self.nfix)
+        rconst = np.zeros(self.nreact)
+        henry = np.zeros(self.nhenry)
+        sc = np.zeros(8)
+        rc = self.lib.oracle_kq_setup(_p(params), _p(var_mix), _p(var), _p(fix), _p(rconst), _p(henry), _p(sc))
+        if rc != 0:
+            raise ValueError(f"AQCHEM set-up failed ({rc})")
+        keys = ("phi2", "cfactor", "stion", "gm1", "gm2", "wetfac", "delinvt", "tend")
+        return var, fix, rconst, henry, dict(zip(keys, sc))
+
+    def rconst_at(self, params, var_mix, var):
+        out = np.zeros(self.nreact)
+        rc = self.lib.oracle_kq_rconst_at(_p(np.ascontiguousarray(params, np.float64)),
+                                          _p(np.ascontiguousarray(var_mix, np.float64)),
+                                          _p(np.ascontiguousarray(var, np.float64)), _p(out))
+        if rc != 0:
+            raise ValueError(f"AQCHEM set-up failed ({rc})")
+        return out
+
+    def fun(self, var, fix, rconst):
+        out = np.zeros(self.nvar)
+        self.lib.oracle_kq_fun(_p(np.ascontiguousarray(var, np.float64)), _p(np.ascontiguousarray(fix, np.float64)),
+                               _p(np.ascontiguousarray(rconst, np.float64)), _p(out))
+        return out
+
+    def jac(self, var, fix, rconst):
+        out = np.zeros(self.lu_nonzero)
+        self.lib.oracle_kq_jac(_p(np.ascontiguousarray(var, np.float64)), _p(np.ascontiguousarray(fix, np.float64)),
+                               _p(np.ascontiguousarray(rconst, np.float64)), _p(out))
+        return out
+
+    def decomp(self, jvs):
+        a = np.array(jvs, np.float64)
+        ising = self.lib.oracle_kq_decomp(_p(a))
+        return a, ising
+
+    def solve(self, lu, b):
+        x = np.array(b, np.float64)
+        self.lib.oracle_kq_solve(_p(np.ascontiguousarray(lu, np.float64)), _p(x))
+        return x
+
+    def dense(self, jvs):
+        m = np.zeros((self.nvar, self.nvar))
+        m[self.lu_irow, self.lu_icol] = jvs
+        return m
+
+    # ------------------------------------------------------------------ integration
+    def cells(self, params, var_mix, threads: int = 0, rtol_scale: float = 1.0):
+        """Integrate cells over their cloud time; rtol_scale multiplies the reference's
+        RTOL (convergence tests only)."""
+        self.lib.oracle_kq_set_rtol_scale(rtol_scale)
+        params = np.ascontiguousarray(params, np.float64)
+        var_mix = np.ascontiguousarray(var_mix, np.float64)
+        n = params.shape[0]
+        var = np.zeros((n, self.nvar))
+        fix = np.zeros((n, self.nfix))
+        st = np.zeros((n, self.nstat), np.int32)
+        threads = threads or min(16, max(1, __import__("os").cpu_count() or 1))
+        try:
+            nfail = self.lib.oracle_kq_cells(n, _p(params), _p(var_mix), _p(var), _p(fix), _p(st, C.c_int), threads)
+        finally:
+            self.lib.oracle_kq_set_rtol_scale(1.0)
+        return var, fix, st, nfail
+
+    # ------------------------------------------------------------------ synthetic cells
+    def synthetic_cells(self, n: int, seed: int = 0, ispc8: int = 0, mtpyrac: int = 0):
+        """Seeded cloudy cells: temperature 268-298 K, 700-1000 hPa, liquid water
+        0.05-1 g/m3, cloud time 600-3600 s, half of them precipitating; gas and aerosol
+        species log-uniform within a decade or two of typical continental values."""
+        rng = np.random.default_rng(seed)
+        p = np.zeros((n, self.nparam))
+        f32 = lambda a: a.astype(np.float32).astype(np.float64)   # REAL(4) arguments
+        p[:, P_TEMP2] = f32(rng.uniform(268.0, 298.0, n))
+        p[:, P_PRES_PA] = f32(rng.uniform(70000.0, 100000.0, n))
+        p[:, P_TAUCLD] = f32(rng.choice([600.0, 1200.0, 1800.0, 3600.0], n))
+        p[:, P_PRCRATE] = f32(np.where(rng.random(n) < 0.5, rng.uniform(0.1, 5.0, n), 0.0))
+        wc = rng.uniform(5e-5, 1e-3, n)
+        p[:, P_WCAVG] = f32(wc)
+        p[:, P_WTAVG] = f32(wc * rng.uniform(1.0, 1.5, n))
+        p[:, P_AIRM] = f32(rng.uniform(5e3, 8e4, n))
+        p[:, P_ALFA0] = f32(10 ** rng.uniform(-5, -3, n))
+        p[:, P_ALFA3] = f32(10 ** rng.uniform(-5, -3, n))
+        p[:, P_COSZEN] = f32(rng.uniform(-0.5, 1.0, n))
+        p[:, P_JH2O2] = np.where(p[:, P_COSZEN] > 0, 10 ** rng.uniform(-6.5, -5, n), 0.0)
+        p[:, P_HO] = 10 ** rng.uniform(-14.5, -12.5, n)
+        p[:, P_ISPC8] = ispc8
+        p[:, P_MTPYRAC] = mtpyrac
+        v = np.zeros((n, self.nvar))
+        lu = lambda lo, hi: 10 ** rng.uniform(lo, hi, n)
+        ranges = {
+            "G_SO2": (-9.5, -8), "G_HNO3": (-10.5, -9), "G_CO2": (-3.45, -3.35), "G_NH3": (-10.5, -8.5),
+            "G_H2O2": (-10, -8.7), "G_O3": (-7.6, -7.2), "G_HCOOH": (-10.5, -9), "G_MHP": (-10.5, -9),
+            "G_PAA": (-11, -10), "G_HCL": (-11.5, -10), "G_GLY": (-11.5, -10), "G_MGLY": (-11.5, -10),
+            "G_IEPOX": (-11, -9.5), "G_NO2": (-10, -8), "G_HONO": (-11.5, -10), "G_HNO4": (-12, -10.5),
+            "G_NO3": (-13.5, -12), "G_CH3O2": (-12.5, -11), "G_GCOL": (-12, -10.5), "G_CCOOH": (-10.5, -9),
+            "G_HCHO": (-9.5, -8.5), "G_HO2": (-12, -10.7), "G_HCHOP": (-13, -11),
+            "A_NO3AKN": (-13, -11.5), "A_NH4AKN": (-12.5, -11), "A_CLAKN": (-14, -12.5), "A_NAAKN": (-14, -12.5),
+            "A_SO4AKN": (-12.5, -11), "A_PECAKN": (-13, -11.5), "A_POAAKN": (-12.5, -11), "A_PRIAKN": (-13, -11.5),
+            "L_SO4MIN2": (-10, -9), "L_NO3MIN": (-10.5, -9.3), "L_NH4PLUS": (-9.8, -8.8), "L_CLMIN": (-12, -10.5),
+            "L_PRIACC": (-11.5, -10), "L_NAPLUS": (-12, -10.5), "L_CAPLUS2": (-12.5, -11), "L_MGPLUS2": (-13, -11.5),
+            "L_KPLUS": (-13, -11.5), "L_PECACC": (-11.5, -10.5), "L_ORGC": (-12, -10.5), "L_OXLACMIN2": (-12, -10.5),
+            "L_POAACC": (-11, -9.8), "L_FEPLUS3": (-14.5, -13), "L_MNPLUS2": (-15.5, -14),
+        }
+        if ispc8:
+            ranges.update({"G_IMAE": (-12, -10.5), "G_IHMML": (-12, -10.5), "L_IETET": (-12, -10.5),
+                           "L_IEOS": (-12, -10.5), "L_DIMER": (-13, -11.5), "L_IMGA": (-13, -11.5),
+                           "L_IMOS": (-13, -11.5)})
+        else:
+            ranges["L_ISO3"] = (-12, -10.5)
+        if mtpyrac:
+            ranges["G_PYRAC"] = (-12, -10.5)
+        for name, (lo, hi) in ranges.items():
+            v[:, self.index[name]] = lu(lo, hi)
+        return p, v

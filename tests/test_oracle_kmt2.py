@@ -1,0 +1,332 @@
+"""KMT2 aqueous cloud chemistry oracle (CCTM/src/cloud/acm_ae7_kmt2), CPU only.
+
+What pins the restatement to the reference, without a Fortran compiler to run it:
+* the generator derives the Jacobian terms and the LU structure and checks them term
+  for term against the reference's aqchem_Jacobian.F90 and aqchem_JacobianSP.F90
+  (test_generator_matches_the_reference, skipped without the CMAQ sources);
+* rate laws, Henry's law constants, the set-up's unit conversions and the initial
+  charge balance against formulas restated here from the reference text, to the last
+  bit where the operation order is the same;
+* J against finite differences of f, the sparse LU against a dense solve;
+* Rodas3 with the reference's tolerances against the same integration with RTOL
+  scaled down (convergence), and the reference's step statistics' invariants.
+"""
+import os
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+sys.path.insert(0, str(ROOT / "oracle"))
+from kmt2 import (KMT2Oracle, P_AIRM, P_ALFA3, P_COSZEN, P_HO, P_ISPC8, P_JH2O2, P_MTPYRAC,  # noqa: E402
+                  P_PRCRATE, P_PRES_PA, P_TAUCLD, P_TEMP2, P_WCAVG, P_WTAVG, STATS)
+
+CMAQ = Path(os.environ.get("CMAQ_ROOT", "/root/reference"))
+KMT2_DIR = CMAQ / "CCTM" / "src" / "cloud" / "acm_ae7_kmt2"
+S = {n: i for i, n in enumerate(STATS)}
+
+
+@pytest.fixture(scope="module")
+def o():
+    return KMT2Oracle()
+
+
+@pytest.fixture(scope="module")
+def cells(o):
+    return o.synthetic_cells(24, seed=5)
+
+
+def test_sizes(o):
+    assert (o.nvar, o.nfix, o.nreact, o.lu_nonzero) == (161, 4, 269, 738)
+    assert o.names[o.index["L_HPLUS"]] == "L_HPLUS" and o.index["L_HPLUS"] == 155
+    assert o.names[o.nvar:] == ["L_H2O", "G_HO", "L_O2", "DUMMY"]
+    assert (np.diff(o.lu_crow) > 0).all() and (o.lu_icol[o.lu_diag[:-1]] == np.arange(o.nvar)).all()
+
+
+@pytest.mark.skipif(not KMT2_DIR.exists(), reason="CMAQ sources not available")
+def test_generator_matches_the_reference_and_the_committed_tables():
+    """kpp_aq.load raises unless the derived Jacobian terms and LU structure equal
+    aqchem_Jacobian.F90 / aqchem_JacobianSP.F90; the committed tables are its output."""
+    from cmaq_gb300.mechgen import kpp_aq
+    k = kpp_aq.load(str(CMAQ))
+    assert len(k.lu_irow) == 738 and len(k.blist) == 364
+    assert (ROOT / "oracle" / "gen" / "kmt2_aq.c").read_text() == kpp_aq.oracle_source(k)
+
+
+# ----------------------------------------------------------------------------- set-up
+def _f32(x):
+    return np.float32(x)
+
+
+def test_henry_constants(o, cells):
+    """HLCONST (hlconst.F:509-511) in REAL(4); GCOLH / CH3O2H in double; HCHOH = 2.5.
+    numpy's float32 exp and libm's expf may differ by one ulp."""
+    p, v = cells
+    for c in range(4):
+        _, _, _, henry, _ = o.setup(p[c], v[c])
+        t = _f32(p[c, P_TEMP2])
+        tfac = (_f32(298.0) - t) / (_f32(298.0) * t)
+        so2 = _f32(1.4) * np.exp(_f32(2900.0) * tfac, dtype=np.float32)
+        assert abs(henry[0] - float(so2)) <= float(np.spacing(so2))     # SO2H, the first one used
+        assert henry[0] == float(np.float32(henry[0]))                  # a REAL(4) value
+        td = float(t)
+        gcol = 4.1e4 * np.exp(4.6e3 * ((298.0 - td) / (298.0 * td)))
+        assert gcol in henry
+        assert 2.5 in henry
+
+
+def test_setup_units_and_charge_balance(o, cells):
+    """aqchem_Initialize.F90:252-288, 425-485 restated: CFACTOR, PHI2, fixed species,
+    and H+ / OH- from the charge balance of the initial ions."""
+    p, v = cells
+    ix = o.index
+    for c in range(6):
+        var, fix, _, _, sc = o.setup(p[c], v[c])
+        t, pres = float(_f32(p[c, P_TEMP2])), float(_f32(p[c, P_PRES_PA]))
+        cfactor = pres / (t * float(np.float32(8.314510))) * 6.0221413e17
+        assert sc["cfactor"] == cfactor
+        lwcfrac = float(_f32(p[c, P_WCAVG])) * 1.0e-3
+        phi2 = 1000.0 / 6.022e23 / lwcfrac
+        assert sc["phi2"] == phi2
+        delinvt = (298.0 - t) / (298.0 * t)
+        assert fix[ix["L_H2O"] - o.nvar] == 55.5 * (1.0 / phi2)
+        assert fix[ix["G_HO"] - o.nvar] == p[c, P_HO] * cfactor
+        o2 = float(np.float32(0.21)) * (pres / 101325.0) * 1.3e-3 * np.exp(1500.0 * delinvt) * (1.0 / phi2)
+        assert fix[ix["L_O2"] - o.nvar] == o2
+        kept = [i for i in range(o.nvar) if o.names[i] not in ("L_HPLUS", "L_OHMIN")]
+        assert np.array_equal(var[kept], cfactor * v[c, kept])
+        pos = 2.0 * (var[ix["L_CAPLUS2"]] + var[ix["L_MGPLUS2"]]) + var[ix["L_NAPLUS"]] + var[ix["L_KPLUS"]] \
+            + var[ix["L_NH4PLUS"]]
+        neg = 2.0 * (var[ix["L_SO4MIN2"]] + var[ix["L_OXLACMIN2"]]) + var[ix["L_NO3MIN"]] + var[ix["L_CLMIN"]]
+        h, oh = var[ix["L_HPLUS"]] * phi2, var[ix["L_OHMIN"]] * phi2
+        kw = 1.0e-14 * np.exp(-6.955e3 * delinvt)
+        assert abs((h + pos * phi2) - (oh + neg * phi2)) <= 1e-9 * (h + pos * phi2)
+        assert abs(h * oh / kw - 1.0) < 1e-12
+
+
+def test_wet_removal_and_cloud_thickness(o, cells):
+    """TWASH / WETFAC_KPP (aqchem_Initialize.F90:270-280) from the cloud thickness of
+    aqchem_kmt.F90:511, where AIRM * TEMP2 is a REAL(4) product."""
+    p, v = cells
+    for c in range(len(p)):
+        _, _, rc, _, sc = o.setup(p[c], v[c])
+        airm, t, pres = _f32(p[c, P_AIRM]), _f32(p[c, P_TEMP2]), float(_f32(p[c, P_PRES_PA]))
+        cthk1 = float(np.float32(airm * t)) * 0.08206 / (pres / 101325.0 * 1000.0)
+        prc = float(_f32(p[c, P_PRCRATE]))
+        twash = float(_f32(p[c, P_WTAVG])) * 1000.0 * cthk1 * 3600.0 / (1000.0 * max(1.0e-20, prc))
+        wet = 1.0 / twash if prc > 0 else 0.0
+        assert sc["wetfac"] == wet
+        assert rc[95] == wet and rc[268] == wet                  # RCONST(96), RCONST(269)
+        assert rc[32] == float(_f32(p[c, P_ALFA3]))              # RCONST(33) = ALFA3_KPP
+        assert sc["tend"] == float(_f32(p[c, P_TAUCLD]))
+
+
+def _kmt(t, accom, dg, mw):
+    rad = 1.6e-5 * 0.5
+    v = np.sqrt(8.0 * 8.3145 * t * 1000.0 / float(np.float32(3.1415926536)) / mw)
+    kmt = (rad * rad) / (3.0 * dg)
+    kmt = kmt + (4.0 * rad / (3.0 * v * accom))
+    return 1.0 / kmt
+
+
+def test_rate_laws_set_once(o, cells):
+    """KMTF / KMTB / HYDF / KPHOT / constants (aqchem_Initialize.F90:53-152, 491-636)."""
+    p, v = cells
+    for c in range(4):
+        _, _, rc, henry, sc = o.setup(p[c], v[c])
+        t = float(_f32(p[c, P_TEMP2]))
+        lwc = float(_f32(p[c, P_WCAVG]))
+        assert rc[0] == _kmt(t, 0.11, 1.28e-5, 64.064) * lwc / 1000.0           # RCONST(1)
+        assert rc[16] == _kmt(t, 0.11, 1.28e-5, 64.064) / (0.08206 * t * henry[0])  # RCONST(17), SO2H
+        assert rc[188] == 1.8e-1 * np.exp(4.03e3 * sc["delinvt"]) * sc["phi2"]    # RCONST(189) HYDF
+        assert rc[189] == 5.1e-3                                                 # RCONST(190)
+        assert rc[91] == 1.1                                                     # RCONST(92)
+        assert rc[192] == p[c, P_JH2O2]                                          # RCONST(193) KPHOT(J)
+        assert rc[231] == 0.0                                                    # RCONST(232), PHOTO = 0
+        assert rc[170] == 0.0 and rc[175] == 0.0                                 # MTPYRAC = 0
+
+
+def test_pyruvic_acid_switch(o):
+    p, v = o.synthetic_cells(2, seed=9, mtpyrac=1)
+    _, _, rc, _, _ = o.setup(p[0], v[0])
+    t = float(_f32(p[0, P_TEMP2]))
+    assert rc[170] == 1.0 * (_kmt(t, 0.0322, 1.24e-5, 88.06) * float(_f32(p[0, P_WCAVG])) / 1000.0)
+
+
+def test_rate_laws_refreshed_from_the_state(o, cells):
+    """Update_RCONST (aqchem_Rates.F90:415-581): ionic strength, activity coefficients,
+    DISF / DISB / KRXN / KIEPOX, restated here from the reference text."""
+    p, v = cells
+    ix = o.index
+    for c in range(4):
+        var, fix, rc, _, sc = o.setup(p[c], v[c])
+        phi2, d = sc["phi2"], sc["delinvt"]
+        x = lambda n: var[ix[n]]
+        s = (x("L_HPLUS") + x("L_NH4PLUS") + x("L_OHMIN") + x("L_HCO3MIN") + x("L_O2MIN") + x("L_NO2MIN")
+             + x("L_NO4MIN") + x("L_GLYACMIN") + x("L_OXLACMIN") + x("L_PYRACMIN") + x("L_GCOLACMIN")
+             + x("L_CCOOHMIN") + x("L_HSO3MIN") + x("L_HCOOMIN") + x("L_NO3MIN") + x("L_HSO4MIN") + x("L_HMSMIN")
+             + x("L_NAPLUS") + x("L_KPLUS") + x("L_CLMIN") + x("L_SO4MIN") + x("L_SO3MIN") + x("L_HMSMIN")
+             + x("L_SO5MIN") + x("L_HSO5MIN") + x("L_CO2MIN") + 3.0 * x("L_FEPLUS3") + 2.0 * x("L_MNPLUS2")
+             + 4.0 * (x("L_SO4MIN2") + x("L_CO3MIN2") + x("L_OXLACMIN2") + x("L_SO3MIN2") + x("L_MNPLUS2")
+                      + x("L_CAPLUS2") + x("L_MGPLUS2")) + 9.0 * x("L_FEPLUS3"))
+        stion = 0.5 * s * phi2
+        assert sc["stion"] == stion
+        gm1 = 10.0 ** (-0.509 * (np.sqrt(stion) / (1.0 + np.sqrt(stion)) - 0.2 * stion))
+        assert abs(sc["gm1"] / gm1 - 1) < 1e-15
+        gm1, gm2 = sc["gm1"], sc["gm2"]
+        assert rc[40] == 2.0e8 * (1.39e-2 * np.exp(1.87e3 * d))                 # DISF(.., 0)
+        assert rc[41] == 5.0e10 * (6.72e-8 * np.exp(3.55e2 * d)) * gm1          # DISF(.., 1)
+        assert rc[54] == 2.0e8 * gm1 * gm1 * phi2                               # DISB(2.0D8, 2)
+        assert rc[55] == 5.0e10 * gm1 * gm2 * phi2                              # DISB(5.0D10, 1)
+        k = 7.45e7 * np.exp(-4756.08 * d)                                       # KRXN(.., 1, 0, 0)
+        assert rc[68] == (k / (1.0 + 13.0 * x("L_HPLUS") * phi2)) * phi2 * phi2
+        k = 750.0 * np.exp(0.0 * d)                                             # KRXN(750, 0, 0, 0, 1)
+        svi = 1.0 + 75.0 * ((x("L_H2SO4") + x("L_HSO4MIN") + x("L_SO4MIN2")) * phi2) ** 0.67
+        assert abs(rc[72] / ((k / svi) * phi2) - 1) < 1e-15
+        assert rc[239] == 2.6e-2 * np.exp(0.0 * d) / phi2 * phi2                # KRXN(.., 4, 0, 0)
+        assert rc[146] == 0.0 and rc[153] == 0.0                                # KIEPOX TYPE >= 1 off
+        assert rc[150] > 0.0                                                    # KIEPOX TYPE 0 on (ISPC8 = 0)
+
+
+def test_rates_follow_the_state(o, cells):
+    """Rates refreshed from a changed state: more H+ -> larger ionic strength, smaller
+    activity coefficients, smaller DISF(.., 1)."""
+    p, v = cells
+    var, _, rc0, _, _ = o.setup(p[0], v[0])
+    var2 = var.copy()
+    var2[o.index["L_HPLUS"]] *= 1e3
+    var2[o.index["L_SO4MIN2"]] *= 1e3
+    rc1 = o.rconst_at(p[0], v[0], var2)
+    assert rc1[41] < rc0[41]
+    assert np.array_equal(rc1[:40], rc0[:40])                                   # set once: unchanged
+
+
+def test_isoprene_epoxide_switch(o):
+    """ISPC8 = 1 switches KIEPOX from TYPE 0 to TYPE >= 1 rates."""
+    p, v = o.synthetic_cells(2, seed=11, ispc8=1)
+    _, _, rc, _, _ = o.setup(p[0], v[0])
+    assert rc[146] > 0.0 and rc[153] > 0.0 and rc[150] == 0.0
+
+
+# ----------------------------------------------------------------------------- f, J, LU
+def test_jacobian_against_finite_differences(o, cells):
+    p, v = cells
+    rng = np.random.default_rng(3)
+    for c in range(3):
+        var, fix, rc, _, _ = o.setup(p[c], v[c])
+        y = var * rng.uniform(0.5, 1.5, o.nvar) + 1e3
+        jd = o.dense(o.jac(y, fix, rc))
+        f0 = o.fun(y, fix, rc)
+        for j in rng.choice(o.nvar, 40, replace=False):
+            h = 1e-6 * abs(y[j])
+            yp, ym = y.copy(), y.copy()
+            yp[j] += h
+            ym[j] -= h
+            fp, fm = o.fun(yp, fix, rc), o.fun(ym, fix, rc)
+            col = (fp - fm) / (2 * h)
+            # the difference quotient resolves nothing below the rounding of f itself
+            tol = 1e-6 * np.abs(jd[:, j]).max() + 64 * np.finfo(float).eps * np.maximum(abs(fp), abs(fm)) / (2 * h)
+            assert (np.abs(col - jd[:, j]) <= tol).all(), (c, j)
+        assert np.isfinite(f0).all()
+
+
+def test_jacobian_pattern_is_the_lu_pattern(o, cells):
+    """Every nonzero of J lies in the stored LU structure (the structure's fill-in entries
+    start at zero)."""
+    p, v = cells
+    var, fix, rc, _, _ = o.setup(p[0], v[0])
+    jvs = o.jac(var + 1.0, fix, rc)
+    assert np.count_nonzero(jvs) <= 670                    # NONZERO of aqchem_Parameters.F90
+    assert np.count_nonzero(jvs) > 500
+
+
+def test_sparse_lu_against_dense_solve(o, cells):
+    p, v = cells
+    rng = np.random.default_rng(4)
+    var, fix, rc, _, _ = o.setup(p[1], v[1])
+    for h in (1e-3, 1.0, 60.0):
+        jac = o.jac(var + 1.0, fix, rc)
+        g = -jac
+        g[o.lu_diag[:-1]] += 1.0 / (h * 0.5)               # ros_PrepareMatrix, gamma(1) = 0.5
+        lu, ising = o.decomp(g)
+        assert ising == 0
+        b = rng.standard_normal(o.nvar)
+        x = o.solve(lu, b)
+        xd = np.linalg.solve(o.dense(g), b)
+        assert np.abs(x - xd).max() <= 1e-9 * np.abs(xd).max()
+
+
+def test_singular_pivot_is_reported(o):
+    """KppDecomp returns the 1-based row whose diagonal is below TINY (checked on the
+    row before its elimination, as the reference does)."""
+    jvs = np.ones(o.lu_nonzero)
+    jvs[o.lu_diag[7]] = 0.0
+    _, ising = o.decomp(jvs)
+    assert ising == 8
+
+
+# ----------------------------------------------------------------------------- integration
+def test_integration_finishes_with_consistent_statistics(o, cells):
+    p, v = cells
+    var, fix, st, nfail = o.cells(p, v)
+    assert nfail == 0 and (st[:, S["ierr"]] == 1).all() and (st[:, S["nkron"]] == 1).all()
+    assert np.isfinite(var).all()
+    nacc, nstp = st[:, S["nacc"]], st[:, S["nstp"]]
+    assert (nacc >= 1).all() and (nstp >= nacc).all()
+    assert (st[:, S["njac"]] == nacc).all()                          # one Jacobian per accepted step
+    assert (st[:, S["ndec"]] == nstp + st[:, S["nsng"]]).all()
+    assert (st[:, S["nsol"]] == 4 * nstp).all()                     # four Rodas3 stages
+    assert (st[:, S["nfun"]] == nacc + 2 * nstp).all()              # stages 3 and 4 evaluate f
+    ph = -np.log10(var[:, o.index["L_HPLUS"]] * (1000.0 / 6.022e23 / (p[:, P_WCAVG].astype(np.float32) * 1e-3)))
+    assert ((ph > 1.5) & (ph < 8.0)).all()
+
+
+def test_threads_give_the_same_bits(o, cells):
+    p, v = cells
+    a = o.cells(p, v, threads=1)
+    b = o.cells(p, v, threads=8)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[2], b[2])
+
+
+def test_rodas3_converges_to_the_tight_solution(o):
+    """The reference's tolerances (RTOL 1e-2, 1e-3 for H2O2 / GLY / MGLY / IETET) against
+    the same integration with RTOL x 1e-4: the error shrinks with the tolerance."""
+    p, v = o.synthetic_cells(12, seed=21)
+    ref, _, _, nf = o.cells(p, v, rtol_scale=1e-4)
+    assert nf == 0
+    errs = []
+    for scale in (1.0, 1e-2):
+        y, _, st, nf = o.cells(p, v, rtol_scale=scale)
+        assert nf == 0
+        big = np.abs(ref) > 1e-6 * np.abs(ref).max(axis=1, keepdims=True)
+        errs.append(np.max(np.abs(y - ref)[big] / np.abs(ref)[big]))
+    assert errs[1] < errs[0]
+    assert errs[0] < 0.05 and errs[1] < 5e-3
+
+
+def test_sulfate_production_and_gas_uptake(o, cells):
+    """Chemistry sanity over the cloud time: SO2 is taken up and oxidised, sulfate grows,
+    dissolved species exist only through uptake."""
+    p, v = cells
+    var, _, _, _ = o.cells(p, v)
+    var0 = np.array([o.setup(p[c], v[c])[0] for c in range(len(p))])
+    so2 = o.index["G_SO2"]
+    assert (var[:, so2] < var0[:, so2]).all()
+    s6 = [o.index[n] for n in ("L_SO4MIN2", "L_HSO4MIN", "L_H2SO4", "WD_H2SO4")]   # incl. wet deposition
+    assert (var[:, s6].sum(axis=1) > var0[:, s6].sum(axis=1)).all()
+
+
+def test_met_data_error_is_reported(o, cells):
+    p, v = cells
+    bad = p[:2].copy()
+    bad[0, P_TEMP2] = 0.0
+    var, _, st, nfail = o.cells(bad, v[:2])
+    assert nfail == 1 and st[0, S["ierr"]] < 0 and st[1, S["ierr"]] == 1
+
+
+def test_sunlit_and_dark_cells(o, cells):
+    p, v = cells
+    assert (p[:, P_COSZEN] > 0).any() and (p[:, P_COSZEN] <= 0).any()
+    assert (p[:, P_PRCRATE] > 0).any() and (p[:, P_PRCRATE] == 0).any()
