@@ -429,11 +429,82 @@ def oracle_source(k: KppMech) -> str:
     return "\n".join(out)
 
 
+def _term(coef: float, x: str) -> str:
+    if coef == 1.0:
+        return f" + {x}"
+    if coef == -1.0:
+        return f" - {x}"
+    return f" + {c_dbl(coef)} * {x}"
+
+
+def _factor(f: int, nvar: int, acc) -> str:
+    return acc("v", f) if f < nvar else acc("f", f - nvar)
+
+
+def unrolled_routines(k: KppMech, qual: str = "static", acc=None) -> str:
+    """Straight-line f, J, LU factorisation and solve with the operations, operands
+    and order of the table-driven oracle (Fun, Jac_SP, KppDecomp, KppSolve): the form
+    the device kernel takes, checked bit for bit against the tables on the CPU.
+    ``acc(array, index)`` renders an element access (plain indexing by default)."""
+    acc = acc or (lambda name, i: f"{name}[{i}]")
+    n = k.nvar
+    out = []
+    # Fun
+    out.append(f"{qual} void kqu_fun(const double* v, const double* f, const double* r, double* vdot)\n{{")
+    for rx, facs in enumerate(k.factors):
+        out.append(f"    const double a{rx} = " + " * ".join([acc("r", rx)] + [_factor(x, n, acc) for x in facs]) + ";")
+    for i, terms in enumerate(k.vdot):
+        out.append(f"    {acc('vdot', i)} = 0.0" + "".join(_term(c, f"a{rx}") for c, rx in terms) + ";")
+    out.append("}\n")
+    # Jac_SP
+    out.append(f"{qual} void kqu_jac(const double* v, const double* f, const double* r, double* jvs)\n{{")
+    for b, (rx, mult, others) in enumerate(k.blist):
+        parts = [acc("r", rx)] + ([c_dbl(float(mult))] if mult > 1 else []) + [_factor(x, n, acc) for x in others]
+        out.append(f"    const double b{b} = " + " * ".join(parts) + ";")
+    for e, terms in enumerate(k.jvs):
+        out.append(f"    {acc('jvs', e)} = 0.0" + "".join(_term(c, f"b{b}") for c, b in terms) + ";")
+    out.append("}\n")
+    # KppDecomp: row k's work row is row k of the stored factors itself (its pattern holds
+    # every column the elimination touches)
+    pos = {(k.lu_irow[e], k.lu_icol[e]): e for e in range(len(k.lu_irow))}
+    out.append(f"{qual} int kqu_decomp(double* jvs)\n{{")
+    for row in range(n):
+        out.append(f"    if (fabs({acc('jvs', k.lu_diag[row])}) < DBL_MIN) return {row + 1};")
+        for kk in range(k.lu_crow[row], k.lu_diag[row]):
+            j = k.lu_icol[kk]
+            out.append(f"    {{ const double a = -{acc('jvs', kk)} / {acc('jvs', k.lu_diag[j])}; {acc('jvs', kk)} = -a;")
+            for jj in range(k.lu_diag[j] + 1, k.lu_crow[j + 1]):
+                q = pos[(row, k.lu_icol[jj])]
+                out.append(f"      {acc('jvs', q)} = {acc('jvs', q)} + a * {acc('jvs', jj)};")
+            out.append("    }")
+    out.append("    return 0;\n}\n")
+    # KppSolve
+    out.append(f"{qual} void kqu_solve(const double* jvs, double* x)\n{{")
+    for row in range(n):
+        terms = "".join(f" - {acc('jvs', kk)} * {acc('x', k.lu_icol[kk])}" for kk in range(k.lu_crow[row], k.lu_diag[row]))
+        if terms:
+            out.append(f"    {acc('x', row)} = {acc('x', row)}{terms};")
+    for row in range(n - 1, -1, -1):
+        terms = "".join(f" - {acc('jvs', kk)} * {acc('x', k.lu_icol[kk])}"
+                        for kk in range(k.lu_diag[row] + 1, k.lu_crow[row + 1]))
+        out.append(f"    {acc('x', row)} = ({acc('x', row)}{terms}) / {acc('jvs', k.lu_diag[row])};")
+    out.append("}\n")
+    return "\n".join(out)
+
+
+def unrolled_source(k: KppMech) -> str:
+    return ("/* Generated by cmaq_gb300/mechgen/kpp_aq.py from CCTM/src/cloud/acm_ae7_kmt2: straight-line\n"
+            " * f, J, LU factorisation and solve of the KMT2 aqueous mechanism, the same operations in\n"
+            " * the same order as the table-driven routines of oracle/kmt2_oracle.c.  Do not edit. */\n\n"
+            + unrolled_routines(k))
+
+
 def write_outputs(cmaq_root: str) -> KppMech:
     k = load(cmaq_root)
     odir = REPO / "oracle" / "gen"
     odir.mkdir(parents=True, exist_ok=True)
     (odir / "kmt2_aq.c").write_text(oracle_source(k))
+    (odir / "kmt2_aq_unrolled.c").write_text(unrolled_source(k))
     return k
 
 

@@ -54,7 +54,8 @@ def build(mechs=MECHS, force: bool = False) -> list[Path]:
         cmd = _gcc([src, src_ebi], out, (f'-DMECH_SOURCE="gen/{mech}_mech.c"', f'-DEBI_SOURCE="gen/{mech}_ebi.c"'))
         procs.append((subprocess.Popen(cmd, cwd=HERE), out))
     kout = kmt2_lib_path()
-    kdeps = (HERE / "kmt2_oracle.c", HERE / "gen" / "kmt2_aq.c", HERE / "portable_pow.h")
+    kdeps = (HERE / "kmt2_oracle.c", HERE / "gen" / "kmt2_aq.c", HERE / "gen" / "kmt2_aq_unrolled.c",
+             HERE / "portable_pow.h")
     if force or not kout.exists() or kout.stat().st_mtime <= max(p.stat().st_mtime for p in kdeps):
         procs.append((subprocess.Popen(_gcc([kdeps[0]], kout), cwd=HERE), kout))
     for p, out in procs:

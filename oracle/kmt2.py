@@ -51,6 +51,12 @@ def load() -> C.CDLL:
     lib.oracle_kq_decomp.argtypes = [dp]
     lib.oracle_kq_solve.argtypes = [dp, dp]
     lib.oracle_kq_solve.restype = None
+    for name in ("oracle_kq_fun_unrolled", "oracle_kq_jac_unrolled"):
+        getattr(lib, name).argtypes = [dp, dp, dp, dp]
+        getattr(lib, name).restype = None
+    lib.oracle_kq_decomp_unrolled.argtypes = [dp]
+    lib.oracle_kq_solve_unrolled.argtypes = [dp, dp]
+    lib.oracle_kq_solve_unrolled.restype = None
     lib.oracle_kq_set_rtol_scale.argtypes = [C.c_double]
     lib.oracle_kq_set_rtol_scale.restype = None
     lib.oracle_kq_cells.argtypes = [C.c_longlong, dp, dp, dp, dp, ip, C.c_int]
@@ -100,26 +106,26 @@ class KMT2Oracle:
             raise ValueError(f"AQCHEM set-up failed ({rc})")
         return out
 
-    def fun(self, var, fix, rconst):
+    def fun(self, var, fix, rconst, unrolled: bool = False):
         out = np.zeros(self.nvar)
-        self.lib.oracle_kq_fun(_p(np.ascontiguousarray(var, np.float64)), _p(np.ascontiguousarray(fix, np.float64)),
+        (self.lib.oracle_kq_fun_unrolled if unrolled else self.lib.oracle_kq_fun)(_p(np.ascontiguousarray(var, np.float64)), _p(np.ascontiguousarray(fix, np.float64)),
                                _p(np.ascontiguousarray(rconst, np.float64)), _p(out))
         return out
 
-    def jac(self, var, fix, rconst):
+    def jac(self, var, fix, rconst, unrolled: bool = False):
         out = np.zeros(self.lu_nonzero)
-        self.lib.oracle_kq_jac(_p(np.ascontiguousarray(var, np.float64)), _p(np.ascontiguousarray(fix, np.float64)),
+        (self.lib.oracle_kq_jac_unrolled if unrolled else self.lib.oracle_kq_jac)(_p(np.ascontiguousarray(var, np.float64)), _p(np.ascontiguousarray(fix, np.float64)),
                                _p(np.ascontiguousarray(rconst, np.float64)), _p(out))
         return out
 
-    def decomp(self, jvs):
+    def decomp(self, jvs, unrolled: bool = False):
         a = np.array(jvs, np.float64)
-        ising = self.lib.oracle_kq_decomp(_p(a))
+        ising = (self.lib.oracle_kq_decomp_unrolled if unrolled else self.lib.oracle_kq_decomp)(_p(a))
         return a, ising
 
-    def solve(self, lu, b):
+    def solve(self, lu, b, unrolled: bool = False):
         x = np.array(b, np.float64)
-        self.lib.oracle_kq_solve(_p(np.ascontiguousarray(lu, np.float64)), _p(x))
+        (self.lib.oracle_kq_solve_unrolled if unrolled else self.lib.oracle_kq_solve)(_p(np.ascontiguousarray(lu, np.float64)), _p(x))
         return x
 
     def dense(self, jvs):

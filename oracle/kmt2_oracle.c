@@ -11,7 +11,8 @@
  *                 start of every step)
  *   f, J          aqchem_Function.F90 (Fun), aqchem_Jacobian.F90 (Jac_SP): walked from the
  *                 generated tables of gen/kmt2_aq.c (reaction factors, tendencies,
- *                 derivative terms)
+ *                 derivative terms); gen/kmt2_aq_unrolled.c holds the same routines as
+ *                 straight-line code
  *   LU, solve     aqchem_LinearAlgebra.F90:57-94 (KppDecomp), :655-916 (KppSolve)
  *   integrator    aqchem_Integrator.F90:79-132 (INTEGRATE), :135-425 (Rosenbrock
  *                 parameters), :485-690 (ros_Integrator), :694-724 (ros_ErrorNorm),
@@ -35,6 +36,7 @@
 #include <string.h>
 
 #include "gen/kmt2_aq.c"
+#include "gen/kmt2_aq_unrolled.c"
 #include "portable_pow.h"
 
 /* per-cell parameters: the AQCHEM arguments the kinetic core reads */
@@ -648,6 +650,19 @@ void oracle_kq_jac(const double* var, const double* fix, const double* rconst, d
 int oracle_kq_decomp(double* jvs) { return kq_decomp(jvs); }
 
 void oracle_kq_set_rtol_scale(double scale) { kq_rtol_scale = scale; }
+
+/* The generated straight-line routines (gen/kmt2_aq_unrolled.c), the form of the device
+ * code, for the tests that hold them to the table-driven ones bit for bit. */
+void oracle_kq_fun_unrolled(const double* var, const double* fix, const double* rconst, double* vdot)
+{
+    kqu_fun(var, fix, rconst, vdot);
+}
+void oracle_kq_jac_unrolled(const double* var, const double* fix, const double* rconst, double* jvs)
+{
+    kqu_jac(var, fix, rconst, jvs);
+}
+int oracle_kq_decomp_unrolled(double* jvs) { return kqu_decomp(jvs); }
+void oracle_kq_solve_unrolled(const double* jvs, double* x) { kqu_solve(jvs, x); }
 
 void oracle_kq_solve(const double* jvs, double* x) { kq_solve(jvs, x); }
 

@@ -53,6 +53,7 @@ def test_generator_matches_the_reference_and_the_committed_tables():
     k = kpp_aq.load(str(CMAQ))
     assert len(k.lu_irow) == 738 and len(k.blist) == 364
     assert (ROOT / "oracle" / "gen" / "kmt2_aq.c").read_text() == kpp_aq.oracle_source(k)
+    assert (ROOT / "oracle" / "gen" / "kmt2_aq_unrolled.c").read_text() == kpp_aq.unrolled_source(k)
 
 
 # ----------------------------------------------------------------------------- set-up
@@ -256,6 +257,31 @@ def test_sparse_lu_against_dense_solve(o, cells):
         x = o.solve(lu, b)
         xd = np.linalg.solve(o.dense(g), b)
         assert np.abs(x - xd).max() <= 1e-9 * np.abs(xd).max()
+
+
+def test_straight_line_routines_equal_the_tables_bit_for_bit(o, cells):
+    """The generated straight-line f / J / LU / solve (the device code's form) against
+    the table-driven routines: identical bits on states across the cells, including
+    negative entries and zeros."""
+    p, v = cells
+    rng = np.random.default_rng(8)
+    for c in range(6):
+        var, fix, rc, _, _ = o.setup(p[c], v[c])
+        y = var * rng.uniform(0.3, 3.0, o.nvar)
+        y[rng.choice(o.nvar, 10, replace=False)] *= -1e-3
+        assert np.array_equal(o.fun(y, fix, rc), o.fun(y, fix, rc, unrolled=True))
+        jac = o.jac(y, fix, rc)
+        assert np.array_equal(jac, o.jac(y, fix, rc, unrolled=True))
+        g = -jac
+        g[o.lu_diag[:-1]] += 1.0 / (rng.uniform(1e-3, 100.0) * 0.5)
+        lu_t, s_t = o.decomp(g)
+        lu_u, s_u = o.decomp(g, unrolled=True)
+        assert s_t == s_u == 0 and np.array_equal(lu_t, lu_u)
+        b = rng.standard_normal(o.nvar) * np.abs(y + 1.0)
+        assert np.array_equal(o.solve(lu_t, b), o.solve(lu_u, b, unrolled=True))
+    jvs = np.ones(o.lu_nonzero)
+    jvs[o.lu_diag[40]] = 0.0
+    assert o.decomp(jvs)[1] == o.decomp(jvs, unrolled=True)[1] == 41
 
 
 def test_singular_pivot_is_reported(o):
