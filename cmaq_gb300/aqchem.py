@@ -1,0 +1,58 @@
+"""KMT2 aqueous cloud chemistry on the GPU: the kinetic core of CMAQ's AQCHEM
+(CCTM/src/cloud/acm_ae7_kmt2/aqchem_kmt.F90:371-543) for a batch of cloudy cells.
+
+    var_out, stats = aqchem_kinetics(params, var_mix)
+
+``params`` [15][n] and ``var_mix`` [161][n] are float64 CUDA tensors laid out as
+``include/cmaqchem.h`` (``cmaqchem_kmt2_solve_device``) describes: AQCHEM's arguments per
+cell, and the KPP state as the reference's Initialize maps the gas and aerosol arrays
+(mixing ratios).  ``var_out`` is the state after the cloud time TAUCLD in molec/cm3, as
+KPP's VAR; ``stats`` [10][n] int32 the integrator's counters per cell (see
+``STATS``).  The call runs in libcmaqchem.so; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+
+from . import _lib
+
+NVAR, NFIX, NPARAM = 161, 4, 15
+PARAMS = ("temp2", "pres_pa", "taucld", "prcrate", "wcavg", "wtavg", "airm", "alfa0", "alfa3", "coszen", "jh2o2",
+          "ho", "ispc8", "mtpyrac", "photo")
+STATS = ("nstp", "nacc", "nrej", "nfun", "njac", "ndec", "nsol", "nsng", "ierr", "npass")
+LANES_PER_SM = 256   # two 128-thread blocks of 255 registers each fit an SM
+
+
+def _ptr(t: torch.Tensor | None):
+    return C.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def aqchem_kinetics(params: torch.Tensor, var_mix: torch.Tensor, *, lanes: int | None = None, with_fix: bool = False,
+                    stream: torch.cuda.Stream | None = None):
+    """Integrate n cloudy cells over their TAUCLD; returns (var_out, stats) or, with
+    with_fix, (var_out, fix_out, stats).  ``lanes`` caps the cells integrated at once
+    (the workspace holds 25.6 KB per lane); by default 256 per SM."""
+    for name, t, rows in (("params", params, NPARAM), ("var_mix", var_mix, NVAR)):
+        if not (t.is_cuda and t.dtype == torch.float64 and t.dim() == 2 and t.shape[0] == rows and t.is_contiguous()):
+            raise ValueError(f"{name} must be a contiguous float64 CUDA tensor of shape ({rows}, n)")
+    n = params.shape[1]
+    if var_mix.shape[1] != n or var_mix.device != params.device:
+        raise ValueError("params and var_mix must describe the same cells on the same device")
+    dev = params.device
+    var_out = torch.empty((NVAR, n), dtype=torch.float64, device=dev)
+    fix_out = torch.empty((NFIX, n), dtype=torch.float64, device=dev) if with_fix else None
+    stats = torch.zeros((len(STATS), n), dtype=torch.int32, device=dev)
+    if n == 0:
+        return (var_out, fix_out, stats) if with_fix else (var_out, stats)
+    L = _lib.lib()
+    if lanes is None:
+        lanes = torch.cuda.get_device_properties(dev).multi_processor_count * LANES_PER_SM
+    lanes = max(1, min(int(lanes), n))
+    ws = torch.empty(L.cmaqchem_kmt2_workspace_doubles(lanes), dtype=torch.float64, device=dev)
+    s = stream or torch.cuda.current_stream(dev)
+    with torch.cuda.device(dev):
+        _lib.check(L.cmaqchem_kmt2_solve_device(n, _ptr(params), _ptr(var_mix), _ptr(var_out), _ptr(fix_out),
+                                                _ptr(stats), _ptr(ws), ws.numel(), C.c_void_p(s.cuda_stream)))
+    return (var_out, fix_out, stats) if with_fix else (var_out, stats)

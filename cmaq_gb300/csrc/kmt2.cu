@@ -1,0 +1,79 @@
+// C ABI of the KMT2 aqueous cloud chemistry kernel (include/cmaqchem.h:
+// cmaqchem_kmt2_*): the kinetic core of AQCHEM (CCTM/src/cloud/acm_ae7_kmt2/aqchem_kmt.F90:
+// 371-543) for a batch of cloudy cells, one cell per thread.
+//
+// Each thread is a lane with its own slice of the caller's workspace (element i at
+// ws[lane + i * nlanes], so a warp's 32 lanes read consecutive doubles) and integrates
+// cells lane, lane + nlanes, ...; inputs and outputs are [element][cell].  The loops of
+// the integrator are bounded (200,000 Rodas3 steps per pass, 5 step halvings per
+// singular factorisation, 16 passes), so every thread ends.
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "../../include/cmaqchem.h"
+#include "kmt2.cuh"
+
+__attribute__((visibility("hidden"))) void cmaqchem_set_error(const std::string& msg);
+
+static_assert(kmt2::NVAR == CMAQCHEM_KMT2_NVAR && kmt2::NFIX == CMAQCHEM_KMT2_NFIX, "KMT2 sizes");
+static_assert(kmt2::NPARAM == CMAQCHEM_KMT2_NPARAM && kmt2::NSTAT == CMAQCHEM_KMT2_NSTAT, "KMT2 layout");
+
+namespace {
+
+constexpr int KMT2_THREADS = 128;
+
+struct Kmt2Args {
+    const double* params;
+    const double* var_mix;
+    double* var_out;
+    double* fix_out;
+    int* stats;
+    double* ws;
+    long long ncell;
+    long long nlanes;
+};
+
+__global__ void __launch_bounds__(KMT2_THREADS) k_kmt2_cells(Kmt2Args a)
+{
+    const long long lane = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (lane >= a.nlanes) return;
+    double* ws = a.ws + lane;
+    for (long long c = lane; c < a.ncell; c += a.nlanes)
+        kmt2::kq_cell(a.params + c, a.var_mix + c, a.var_out + c, a.fix_out ? a.fix_out + c : nullptr, a.stats + c,
+                      a.ncell, ws, a.nlanes);
+}
+
+int fail(const std::string& msg)
+{
+    cmaqchem_set_error(msg);
+    return -1;
+}
+
+}  // namespace
+
+extern "C" long long cmaqchem_kmt2_workspace_doubles(long long nlanes)
+{
+    return nlanes > 0 ? nlanes * (long long)kmt2::WS_ELEMS : 0;
+}
+
+extern "C" int cmaqchem_kmt2_solve_device(long long ncell, const double* params, const double* var_mix,
+                                          double* var_out, double* fix_out, int* stats, double* workspace,
+                                          long long workspace_doubles, void* stream)
+{
+    if (ncell < 0) return fail("ncell must be >= 0");
+    if (ncell == 0) return 0;
+    if (!params || !var_mix || !var_out || !stats || !workspace) return fail("null array argument");
+    long long nlanes = workspace_doubles / kmt2::WS_ELEMS;
+    if (nlanes < 1) return fail("workspace smaller than one lane (cmaqchem_kmt2_workspace_doubles(1) doubles)");
+    if (nlanes > ncell) nlanes = ncell;
+    const long long blocks = (nlanes + KMT2_THREADS - 1) / KMT2_THREADS;
+    if (blocks > 0x7fffffffLL) return fail("too many lanes");
+    Kmt2Args a{params, var_mix, var_out, fix_out, stats, workspace, ncell, nlanes};
+    cudaStream_t s = (cudaStream_t)stream;
+    k_kmt2_cells<<<(unsigned)blocks, KMT2_THREADS, 0, s>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail(std::string("k_kmt2_cells: ") + cudaGetErrorString(e));
+    return 0;
+}

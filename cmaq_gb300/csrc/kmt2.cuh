@@ -1,0 +1,462 @@
+// KMT2 aqueous cloud chemistry: the kinetic core of AQCHEM (CCTM/src/cloud/acm_ae7_kmt2)
+// for one cloudy cell, as host/device code.
+//
+//   set-up      aqchem_kmt.F90:371-396, 511 (Henry's law constants, cloud thickness) and
+//               aqchem_Initialize.F90:252-288, 425-485, 491-636 (units, tolerances, fixed
+//               species, pH by charge balance, the rate constants set once)
+//   rates       aqchem_Rates.F90:146-362 (DISF, DISB, KRXN, KIEPOX), :415-581
+//               (Update_RCONST: ionic strength, activity coefficients), refreshed from the
+//               accepted state before every step, as the reference's Fun / Jac templates
+//               do (aqchem_Integrator.F90:1318-1388: Update_RCONST reads the module's VAR,
+//               which is the integrator's Y)
+//   f, J, LU    generated straight-line Fun, Jac_SP, KppDecomp, KppSolve (gen/kmt2_aq.cuh)
+//   integrator  KPP Rosenbrock with Rodas3, autonomous, vector tolerances and the
+//               reference's defaults (aqchem_Integrator.F90:79-132, 300-425, 485-831,
+//               1070-1134); AQCHEM's DO WHILE (T < TEND) loop (aqchem_kmt.F90:530-543)
+//               with at most 16 passes
+//
+// The same operations in the same order as the reference's Fortran (REAL(4) literals
+// and REAL(4) intermediates kept, no contraction of a*b+c: the library is compiled with
+// -fmad=false).  One cell's arrays live in a lane-interleaved FP64 workspace (element
+// i of a lane at ws[i * s]); inputs and outputs are [element][cell] with stride n.
+// The header compiles as plain C++ too, so the host can run exactly this code.
+#pragma once
+
+#include <float.h>
+#include <math.h>
+
+#ifdef __CUDACC__
+#define KQ_HD __host__ __device__
+#define KQ_NOINLINE __noinline__
+#else
+#define KQ_HD
+#define KQ_NOINLINE
+#endif
+
+namespace kmt2 {
+
+#include "gen/kmt2_aq_consts.cuh"
+
+// per-cell parameters, [KQ_NPARAM][ncell] (include/cmaqchem.h: CMAQCHEM_KMT2_*)
+enum { P_TEMP2 = 0, P_PRES_PA, P_TAUCLD, P_PRCRATE, P_WCAVG, P_WTAVG, P_AIRM, P_ALFA0, P_ALFA3, P_COSZEN,
+       P_JH2O2, P_HO, P_ISPC8, P_MTPYRAC, P_PHOTO, NPARAM };
+// per-cell statistics, [NSTAT][ncell]
+enum { S_NSTP = 0, S_NACC, S_NREJ, S_NFUN, S_NJAC, S_NDEC, S_NSOL, S_NSNG, S_IERR, S_NKRON, NSTAT };
+// workspace layout of one lane (elements)
+constexpr int W_Y = 0, W_YNEW = NVAR, W_FCN0 = 2 * NVAR, W_FCN = 3 * NVAR, W_K = 4 * NVAR, W_YERR = 8 * NVAR,
+              W_JAC0 = 9 * NVAR, W_GHIMJ = W_JAC0 + LU_NONZERO, W_R = W_GHIMJ + LU_NONZERO, W_F = W_R + NREACT,
+              WS_ELEMS = W_F + NFIX;
+
+struct Cell {   // aqchem_Global of one cell
+    double temp_kpp, press, lwc, lwcfrac, delinvt, phi2, invphi2, ddiam;
+    double czen, photo, jh2o2, alfa3, alfa0, wetfac, cfactor, tend, dt;
+    double stion, gm1, gm2;
+    int ispc8, mtpyrac;
+    double henry[NHENRY];
+};
+
+// ----------------------------------------------------------------------------- rate laws
+// HLCONST with EFFECTIVE = .FALSE. (hlconst.F:509-511), REAL(4) throughout
+KQ_HD inline float kq_hlconst(float a, float e, float temp)
+{
+    const float tfac = (298.0f - temp) / (298.0f * temp);
+    return a * expf(e * tfac);
+}
+
+// Schwartz (1986) mass-transfer coefficient of KMTF / KMTB (aqchem_Initialize.F90:53-104);
+// PI is a REAL(4) literal there
+KQ_HD inline double kq_kmt(const Cell& c, double accom, double dg, double mw)
+{
+    const double rad = c.ddiam * 0.5;
+    const double v = sqrt(8.0 * 8.3145 * c.temp_kpp * 1000.0 / (double)3.1415926536f / mw);
+    double kmt = (rad * rad) / (3.0 * dg);
+    kmt = kmt + (4.0 * rad / (3.0 * v * accom));
+    return 1.0 / kmt;
+}
+KQ_HD inline double kq_kmtf(const Cell& c, double accom, double dg, double mw)
+{
+    return kq_kmt(c, accom, dg, mw) * c.lwc / 1000.0;
+}
+KQ_HD inline double kq_kmtb(const Cell& c, double hl, double accom, double dg, double mw)
+{
+    return kq_kmt(c, accom, dg, mw) / (0.08206 * c.temp_kpp * hl);
+}
+// aqchem_Initialize.F90:106-117
+KQ_HD inline double kq_hydf(const Cell& c, double kf, double dh)
+{
+    const double k = kf * exp(dh * c.delinvt);
+    return k * c.phi2;
+}
+// aqchem_Initialize.F90:132-152 (a negative J: the COSZEN estimate scaled by PHOTO)
+KQ_HD inline double kq_kphot(const Cell& c, double maxc, double jval)
+{
+    if (!(jval < 0.0)) return jval;
+    return c.czen > 0.001 ? c.photo * 2.718281828 * maxc * exp(-1.0 / c.czen) : 0.0;
+}
+// aqchem_Rates.F90:146-158
+KQ_HD inline double kq_disf(const Cell& c, double keq, double dh, double kb, int g1)
+{
+    const double k = kb * (keq * exp(dh * c.delinvt));
+    return g1 == 1 ? k * c.gm1 : k;
+}
+// aqchem_Rates.F90:160-174
+KQ_HD inline double kq_disb(const Cell& c, double kb, int g1)
+{
+    double k = kb;
+    if (g1 == 1) k = k * c.gm1 * c.gm2;
+    else if (g1 == 2) k = k * c.gm1 * c.gm1;
+    return k * c.phi2;
+}
+// Q of the aqueous diffusion limitation for a first-order rate krate (aqchem_Rates.F90:
+// 225-242, 300-316, 338-354)
+KQ_HD inline double kq_diffusion_factor(const Cell& c, double krate)
+{
+    const double q1 = krate < 0.0 ? 0.0 : c.ddiam / 2.0 * sqrt(krate / 1.0e-9);
+    if (!(q1 > 1.0e-3)) return 1.0;
+    if (q1 > 100.0) return 3.0 / q1;
+    const double e2 = exp(2.0 * q1);
+    const double coth = (e2 + 1.0) / (e2 - 1.0);
+    const double q = 3.0 * ((coth / q1) - (1.0 / (q1 * q1)));
+    return q > 1.0 ? 1.0 : q;
+}
+// aqchem_Rates.F90:176-249
+KQ_HD inline double kq_krxn(const Cell& c, const double* v, long long s, double kr, double dh, int rtype, int qy,
+                            int metal)
+{
+    const double phi2 = c.phi2;
+    double k = kr * exp(dh * c.delinvt);
+    if (rtype == 1) k = (k / (1.0 + 13.0 * v[L_HPLUS * s] * phi2)) * phi2;
+    else if (rtype == 3) k = k * phi2;
+    else if (rtype == 4) k = k / phi2;
+    if (metal > 0) {
+        const double s6 = (v[L_H2SO4 * s] + v[L_HSO4MIN * s] + v[L_SO4MIN2 * s]) * phi2;
+        k = k / (1.0 + 75.0 * pow(s6, 0.67));
+    }
+    if (qy >= 1) {
+        const double k1 = 2.4e+4 * exp(0.0 * c.delinvt);
+        const double k2 = 3.7e+5 * exp(-5530.88 * c.delinvt);
+        const double k3 = 1.5e+9 * exp(-5280.56 * c.delinvt);
+        const double kt = (k1 * v[L_SO2 * s] + k2 * v[L_HSO3MIN * s] + k3 * v[L_SO3MIN2 * s]) * phi2;
+        k = k * kq_diffusion_factor(c, kt);
+    }
+    return k * phi2;
+}
+// aqchem_Rates.F90:251-362
+KQ_HD inline double kq_kiepox(const Cell& c, const double* v, const double* f, long long s, double kh, double khso4,
+                              int type)
+{
+    const double phi2 = c.phi2;
+    if (c.ispc8 <= 0 ? type > 0 : type < 1) return 0.0;
+    const double h = v[L_HPLUS * s], hso4 = v[L_HSO4MIN * s], so4 = v[L_SO4MIN2 * s];
+    double kiepox = kh * h * phi2 + khso4 * hso4 * phi2;
+    double kt = (9.0e-4 * h * phi2 + 1.31e-5 * hso4 * phi2) * f[L_H2O * s] * phi2;
+    if (type <= 1) {
+        kt = kt + (8.83e-3 * h * phi2 + 2.92e-6 * hso4 * phi2) * so4 * phi2;
+        const double kn = 2.0e-4 * h * phi2 + 2.92e-6 * hso4 * phi2;
+        if (c.ispc8 <= 0) {
+            kt = kt + kn * v[L_NO3MIN * s] * phi2;
+        } else {
+            kt = kt + kn * v[L_IETET * s] * phi2;
+            kt = kt + kn * v[L_IEOS * s] * phi2;
+        }
+    } else {
+        kt = kt + (2.0e-4 * h * phi2 + 2.92e-6 * hso4 * phi2) * so4 * phi2;
+    }
+    kiepox = kiepox * kq_diffusion_factor(c, kt);
+    return kiepox * phi2;
+}
+
+// ionic strength and activity coefficients (aqchem_Rates.F90:423-452), terms in the
+// reference's order (L_HMSMIN twice, as there)
+KQ_HD inline void kq_ionic(Cell& c, const double* v, long long s)
+{
+#define V(n) v[(n) * s]
+    const double sum = V(L_HPLUS) + V(L_NH4PLUS) + V(L_OHMIN) + V(L_HCO3MIN) + V(L_O2MIN) + V(L_NO2MIN)
+                     + V(L_NO4MIN) + V(L_GLYACMIN) + V(L_OXLACMIN) + V(L_PYRACMIN) + V(L_GCOLACMIN) + V(L_CCOOHMIN)
+                     + V(L_HSO3MIN) + V(L_HCOOMIN) + V(L_NO3MIN) + V(L_HSO4MIN) + V(L_HMSMIN) + V(L_NAPLUS)
+                     + V(L_KPLUS) + V(L_CLMIN) + V(L_SO4MIN) + V(L_SO3MIN) + V(L_HMSMIN) + V(L_SO5MIN)
+                     + V(L_HSO5MIN) + V(L_CO2MIN) + 3.0 * V(L_FEPLUS3) + 2.0 * V(L_MNPLUS2)
+                     + 4.0 * (V(L_SO4MIN2) + V(L_CO3MIN2) + V(L_OXLACMIN2) + V(L_SO3MIN2) + V(L_MNPLUS2)
+                              + V(L_CAPLUS2) + V(L_MGPLUS2))
+                     + 9.0 * V(L_FEPLUS3);
+#undef V
+    c.stion = 0.5 * sum * c.phi2;
+    const double lg1 = -0.509 * (sqrt(c.stion) / (1.0 + sqrt(c.stion)) - 0.2 * c.stion);
+    c.gm1 = pow(10.0, lg1);
+    const double gm2 = pow(10.0, lg1 * 4.0);
+    c.gm2 = gm2 > 1.0e-30 ? gm2 : 1.0e-30;
+}
+
+// x**y for x >= 0, y > 0 from series with IEEE +, -, *, /, fma, frexp/ldexp and rint only,
+// identical on host and device (the routine of the Gear kernels, gear.cuh: gpow; libm
+// and CUDA pow differ by ulps, which move step-size decisions): log by 2 atanh(s) to
+// s^23 after x = m 2^k, exp by Taylor to r^13 after a Cody-Waite reduction by ln 2.
+KQ_HD inline double kq_pow(double x, double y)
+{
+    if (!(x > 0.0)) return x == 0.0 ? 0.0 : x;
+    if (isinf(x)) return x;
+    int k;
+    double m = frexp(x, &k);
+    if (m < 0x1.6a09e667f3bcdp-1) {
+        m = m * 2.0;
+        k = k - 1;
+    }
+    const double u = (m - 1.0) / (m + 1.0);
+    const double z = u * u;
+    double p = 0x1.642c8590b2164p-5;
+    p = fma(p, z, 0x1.8618618618618p-5);
+    p = fma(p, z, 0x1.af286bca1af28p-5);
+    p = fma(p, z, 0x1.e1e1e1e1e1e1ep-5);
+    p = fma(p, z, 0x1.1111111111111p-4);
+    p = fma(p, z, 0x1.3b13b13b13b14p-4);
+    p = fma(p, z, 0x1.745d1745d1746p-4);
+    p = fma(p, z, 0x1.c71c71c71c71cp-4);
+    p = fma(p, z, 0x1.2492492492492p-3);
+    p = fma(p, z, 0x1.999999999999ap-3);
+    p = fma(p, z, 0x1.5555555555555p-2);
+    p = fma(p, z, 1.0);
+    const double ln2_hi = 0x1.62e42fee00000p-1, ln2_lo = 0x1.a39ef35793c76p-33;
+    const double lx = fma((double)k, ln2_hi, fma((double)k, ln2_lo, (2.0 * u) * p));
+    const double t = y * lx;
+    if (t > 709.0) return INFINITY;
+    if (t < -745.0) return 0.0;
+    const double n = rint(t * 0x1.71547652b82fep+0);
+    const double r = fma(-n, ln2_lo, fma(-n, ln2_hi, t));
+    double e = 0x1.6124613a86d09p-33;
+    e = fma(e, r, 0x1.1eed8eff8d898p-29);
+    e = fma(e, r, 0x1.ae64567f544e4p-26);
+    e = fma(e, r, 0x1.27e4fb7789f5cp-22);
+    e = fma(e, r, 0x1.71de3a556c734p-19);
+    e = fma(e, r, 0x1.a01a01a01a01ap-16);
+    e = fma(e, r, 0x1.a01a01a01a01ap-13);
+    e = fma(e, r, 0x1.6c16c16c16c17p-10);
+    e = fma(e, r, 0x1.1111111111111p-7);
+    e = fma(e, r, 0x1.5555555555555p-5);
+    e = fma(e, r, 0x1.5555555555555p-3);
+    e = fma(e, r, 0.5);
+    e = fma(e, r, 1.0);
+    e = fma(e, r, 1.0);
+    return ldexp(e, (int)n);
+}
+
+#include "gen/kmt2_aq.cuh"
+
+// ----------------------------------------------------------------------------- set-up
+// AQCHEM before the integration; y, f, r are the lane's workspace arrays.  Returns 0, or
+// -1 for the reference's MET DATA ERROR (aqchem_kmt.F90:427-431), -2 for its initial pH
+// error (aqchem_Initialize.F90:476-481).
+KQ_HD inline int kq_setup(Cell& c, const double* p, long long n, const double* vmix, double* y, double* f, double* r,
+                          long long s)
+{
+    const float temp2 = (float)p[P_TEMP2 * n], pres_pa = (float)p[P_PRES_PA * n];
+    const float taucld = (float)p[P_TAUCLD * n], prcrate = (float)p[P_PRCRATE * n];
+    const float wcavg = (float)p[P_WCAVG * n], wtavg = (float)p[P_WTAVG * n], airm = (float)p[P_AIRM * n];
+    if (temp2 <= 0.0f || airm <= 0.0f || pres_pa <= 0.0f) return -1;
+    kq_henry(c, temp2);
+    c.jh2o2 = p[P_JH2O2 * n];
+    c.ispc8 = (int)p[P_ISPC8 * n];
+    c.mtpyrac = (int)p[P_MTPYRAC * n];
+    c.photo = p[P_PHOTO * n];
+    const double cthk1 = (double)(airm * temp2) * 0.08206 / ((double)pres_pa / 101325.0 * 1000.0);
+    c.dt = (double)taucld;
+    c.tend = 0.0 + c.dt;
+    c.ddiam = 1.6e-5;
+    c.temp_kpp = (double)temp2;
+    c.press = (double)pres_pa / 101325.0;
+    c.lwc = (double)wcavg;
+    c.lwcfrac = c.lwc * 1.0e-3;
+    c.delinvt = (298.0 - c.temp_kpp) / (298.0 * c.temp_kpp);
+    const double prc = (double)prcrate > 1.0e-20 ? (double)prcrate : 1.0e-20;
+    const double twash = (double)wtavg * 1000.0 * cthk1 * 3600.0 / (1000.0 * prc);
+    c.wetfac = prcrate > 0.0f ? 1.0 / twash : 0.0;
+    c.alfa3 = (double)(float)p[P_ALFA3 * n];
+    c.alfa0 = (double)(float)p[P_ALFA0 * n];
+    c.phi2 = 1000.0 / 6.022e23 / c.lwcfrac;
+    c.invphi2 = 1.0 / c.phi2;
+    c.czen = (double)(float)p[P_COSZEN * n];
+    c.cfactor = (double)pres_pa / (c.temp_kpp * (double)8.314510f) * 6.0221413e17;
+    for (int i = 0; i < NVAR; ++i) y[i * s] = c.cfactor * vmix[i * n];
+    for (int i = 0; i < NFIX; ++i) f[i * s] = c.cfactor * 0.0;
+    f[L_H2O * s] = 55.5 * c.invphi2;
+    f[G_HO * s] = p[P_HO * n] * c.cfactor;
+    f[L_O2 * s] = (double)0.21f * c.press * 1.3e-3 * exp(1500.0 * c.delinvt) * c.invphi2;
+    const double kw = 1.00e-14 * exp(-6.955e+03 * c.delinvt);
+    double pos = 2.0 * (y[L_CAPLUS2 * s] + y[L_MGPLUS2 * s]) + y[L_NAPLUS * s] + y[L_KPLUS * s] + y[L_NH4PLUS * s];
+    double neg = 2.0 * (y[L_SO4MIN2 * s] + y[L_OXLACMIN2 * s]) + y[L_NO3MIN * s] + y[L_CLMIN * s];
+    pos = pos * c.phi2;
+    neg = neg * c.phi2;
+    const double chg = pos - neg;
+    const double oh = (chg + sqrt(chg * chg + 4.0 * kw)) * 0.5;
+    if (!(oh > 0.0)) return -2;
+    y[L_OHMIN * s] = oh * c.invphi2;
+    y[L_HPLUS * s] = (kw / oh) * c.invphi2;
+    kq_rates_once(c, y, f, r, s);
+    return 0;
+}
+
+KQ_HD inline void kq_axpy(double a, const double* x, double* y, long long s)   // WAXPY: y += a x, a = 0 skipped
+{
+    if (a == 0.0) return;
+    for (int i = 0; i < NVAR; ++i) y[i * s] = y[i * s] + a * x[i * s];
+}
+KQ_HD inline void kq_copy(const double* x, double* y, long long s)
+{
+    for (int i = 0; i < NVAR; ++i) y[i * s] = x[i * s];
+}
+
+// ros_ErrorNorm (aqchem_Integrator.F90:694-724)
+KQ_HD inline double kq_error_norm(const double* y, const double* ynew, const double* yerr, long long s)
+{
+    double err = 0.0;
+    for (int i = 0; i < NVAR; ++i) {
+        const double ymax = fmax(fabs(y[i * s]), fabs(ynew[i * s]));
+        const double q = yerr[i * s] / (kq_atol(i) + kq_rtol(i) * ymax);
+        err = err + q * q;
+    }
+    err = sqrt(err / (double)NVAR);
+    return err > 1.0e-10 ? err : 1.0e-10;
+}
+
+// One INTEGRATE call: ros_Integrator with Rodas3 (aqchem_Integrator.F90:485-690, 1070-1134),
+// its four stages written out with Rodas3's coefficients (A = 2, 0, 2, 0, 1; C = 4, 1, -1,
+// 1, -1, -8/3; M = 2, 0, 1, 1; E = 0, 0, 0, 1; gamma_1 = 1/2; new f at stages 3 and 4).
+// Returns IERR (1 = success); *texit is the time of the last accepted step (0 if none).
+KQ_HD inline int kq_integrate(Cell& c, double* ws, long long s, double tstart, double tend, double* texit,
+                              long long* st)
+{
+    double* y = ws + W_Y * s;
+    double* ynew = ws + W_YNEW * s;
+    double* fcn0 = ws + W_FCN0 * s;
+    double* fcn = ws + W_FCN * s;
+    double* k1 = ws + W_K * s;
+    double* k2 = k1 + NVAR * s;
+    double* k3 = k2 + NVAR * s;
+    double* k4 = k3 + NVAR * s;
+    double* yerr = ws + W_YERR * s;
+    double* jac0 = ws + W_JAC0 * s;
+    double* ghimj = ws + W_GHIMJ * s;
+    double* r = ws + W_R * s;
+    const double* f = ws + W_F * s;
+    const double roundoff = DBL_EPSILON, hmax = fabs(tend - tstart);
+    long long nstp = 0, nacc = 0;
+    double t = tstart, h = fmin(1.0e-5, hmax);
+    *texit = 0.0;
+    if (fabs(h) <= 10.0 * roundoff) h = 1.0e-5;
+    bool reject_last = false, reject_more = false;
+    while (fabs(t - tend) >= roundoff) {
+        if (nstp > 200000) return -6;
+        if ((t + 0.1 * h) == t || h <= roundoff) return -7;
+        h = fmin(h, fabs(tend - t));
+        kq_ionic(c, y, s);
+        kq_rates_update(c, y, f, r, s);
+        kqu_fun(y, f, r, fcn0, s);
+        st[S_NFUN]++;
+        kqu_jac(y, f, r, jac0, s);
+        st[S_NJAC]++;
+        for (;;) {
+            int nsing = 0;
+            for (;;) {                                           // ros_PrepareMatrix
+                for (int i = 0; i < LU_NONZERO; ++i) ghimj[i * s] = -jac0[i * s];
+                const double ghinv = 1.0 / (h * 0.5);
+                kq_add_diagonal(ghimj, ghinv, s);
+                const int ising = kqu_decomp(ghimj, s);
+                st[S_NDEC]++;
+                if (ising == 0) break;
+                st[S_NSNG]++;
+                if (++nsing > 5) return -8;
+                h = h * 0.5;
+            }
+            kq_copy(fcn0, k1, s);                                // stage 1
+            kqu_solve(ghimj, k1, s);
+            kq_copy(fcn0, k2, s);                                // stage 2 (no new f)
+            kq_axpy(4.0 / h, k1, k2, s);
+            kqu_solve(ghimj, k2, s);
+            kq_copy(y, ynew, s);                                 // stage 3
+            kq_axpy(2.0, k1, ynew, s);
+            kqu_fun(ynew, f, r, fcn, s);
+            st[S_NFUN]++;
+            kq_copy(fcn, k3, s);
+            kq_axpy(1.0 / h, k1, k3, s);
+            kq_axpy(-1.0 / h, k2, k3, s);
+            kqu_solve(ghimj, k3, s);
+            kq_copy(y, ynew, s);                                 // stage 4
+            kq_axpy(2.0, k1, ynew, s);
+            kq_axpy(1.0, k3, ynew, s);
+            kqu_fun(ynew, f, r, fcn, s);
+            st[S_NFUN]++;
+            kq_copy(fcn, k4, s);
+            kq_axpy(1.0 / h, k1, k4, s);
+            kq_axpy(-1.0 / h, k2, k4, s);
+            kq_axpy(-(8.0 / 3.0) / h, k3, k4, s);
+            kqu_solve(ghimj, k4, s);
+            st[S_NSOL] += 4;
+            kq_copy(y, ynew, s);                                 // new state and error
+            kq_axpy(2.0, k1, ynew, s);
+            kq_axpy(1.0, k3, ynew, s);
+            kq_axpy(1.0, k4, ynew, s);
+            for (int i = 0; i < NVAR; ++i) yerr[i * s] = 0.0;
+            kq_axpy(1.0, k4, yerr, s);
+            const double err = kq_error_norm(y, ynew, yerr, s);
+            double hnew = h * fmin(6.0, fmax(0.2, 0.9 / kq_pow(err, 1.0 / 3.0)));
+            nstp++;
+            st[S_NSTP]++;
+            if (err <= 1.0) {                                    // accept (Hmin = 0)
+                nacc++;
+                st[S_NACC]++;
+                kq_copy(ynew, y, s);
+                t = t + h;
+                hnew = fmax(0.0, fmin(hnew, hmax));
+                if (reject_last) hnew = fmin(hnew, h);
+                *texit = t;
+                reject_last = reject_more = false;
+                h = hnew;
+                break;
+            }
+            if (reject_more) hnew = h * 0.1;                     // reject
+            reject_more = reject_last;
+            reject_last = true;
+            h = hnew;
+            if (nacc >= 1) st[S_NREJ]++;
+        }
+    }
+    return 1;
+}
+
+// One cloudy cell: set-up, AQCHEM's integration loop, the state (molec/cm3) to vout and
+// the fixed species to fout (if given); statistics to st[S_* * n].  Returns 0 when the
+// integration finished.
+KQ_HD inline int kq_cell(const double* p, const double* vmix, double* vout, double* fout, int* st_out, long long n,
+                         double* ws, long long s)
+{
+    Cell c;
+    long long st[NSTAT];
+    for (int i = 0; i < NSTAT; ++i) st[i] = 0;
+    double* y = ws + W_Y * s;
+    double* f = ws + W_F * s;
+    int ierr = kq_setup(c, p, n, vmix, y, f, ws + W_R * s, s);
+    if (ierr != 0) {
+        ierr -= 100;
+    } else {
+        double t = 0.0;
+        ierr = 1;
+        while (t < c.tend) {
+            if (st[S_NKRON] >= 16) {
+                ierr = -100;
+                break;
+            }
+            st[S_NKRON]++;
+            double texit = 0.0;
+            ierr = kq_integrate(c, ws, s, t, t + c.dt, &texit, st);
+            t = texit;
+            if (ierr < 0 && texit <= 0.0) break;
+        }
+        for (int i = 0; i < NVAR; ++i) vout[i * n] = y[i * s];
+        if (fout)
+            for (int i = 0; i < NFIX; ++i) fout[i * n] = f[i * s];
+    }
+    st[S_IERR] = ierr;
+    for (int i = 0; i < NSTAT; ++i) st_out[i * n] = (int)st[i];
+    return ierr == 1 ? 0 : 1;
+}
+
+}  // namespace kmt2

@@ -19,6 +19,12 @@ evaluation code (``oracle/kmt2_oracle.c``) walks:
 * tolerances                     ``aqchem_Initialize.F90`` ``RTOL`` / ``ATOL``
 * Henry's law constants          ``aqchem_kmt.F90:371-396`` with the table of ``hlconst.F``
 
+and, for the device code, ``cmaq_gb300/csrc/gen/kmt2_aq_consts.cuh`` (sizes, species
+indices) and ``cmaq_gb300/csrc/gen/kmt2_aq.cuh`` (Henry's law constants, rate constants,
+tolerances, f, J, LU factorisation and solve as strided straight-line code; the rate-law
+functions they call are in ``csrc/kmt2.cuh``).  ``oracle/gen/kmt2_aq_unrolled.c`` holds
+the same straight-line f, J, LU and solve for the oracle's bit-for-bit check.
+
 The Jacobian terms (one partial derivative per reaction and variable reactant,
 combined per Jacobian entry with the species' net coefficients) and the sparse LU
 structure (the Jacobian pattern plus its symbolic fill-in in KPP's species order)
@@ -492,6 +498,93 @@ def unrolled_routines(k: KppMech, qual: str = "static", acc=None) -> str:
     return "\n".join(out)
 
 
+def device_consts(k: KppMech) -> str:
+    """Sizes and species indices for the device code (``namespace kmt2``)."""
+    out = ["// Generated by cmaq_gb300/mechgen/kpp_aq.py from CCTM/src/cloud/acm_ae7_kmt2 (KPP aqueous",
+           "// mechanism of the KMT2 cloud chemistry).  Included inside namespace kmt2.  Do not edit.",
+           "#pragma once", "",
+           f"constexpr int NVAR = {k.nvar};", f"constexpr int NFIX = {k.nfix};", f"constexpr int NREACT = {k.nreact};",
+           f"constexpr int LU_NONZERO = {len(k.lu_irow)};", f"constexpr int NHENRY = {len(k.henry)};", ""]
+    for name, i in sorted(k.index.items(), key=lambda t: t[1]):
+        out.append(f"constexpr int {name} = {i if i < k.nvar else i - k.nvar};")
+    return "\n".join(out) + "\n"
+
+
+def _rate_call(kind: str, a: list[float]) -> str:
+    d = c_dbl
+    if kind == "DISF":
+        return f"kq_disf(c, {d(a[0])}, {d(a[1])}, {d(a[2])}, {int(a[3])})"
+    if kind == "DISB":
+        return f"kq_disb(c, {d(a[0])}, {int(a[1])})"
+    if kind == "KRXN":
+        return f"kq_krxn(c, v, s, {d(a[0])}, {d(a[1])}, {int(a[2])}, {int(a[3])}, {int(a[4])})"
+    if kind == "KIEPOX":
+        return f"kq_kiepox(c, v, f, s, {d(a[0])}, {d(a[1])}, {int(a[2])})"
+    if kind == "KMTF":
+        return f"kq_kmtf(c, {d(a[0])}, {d(a[1])}, {d(a[2])})"
+    if kind == "KMTB":
+        return f"kq_kmtb(c, c.henry[{int(a[0])}], {d(a[1])}, {d(a[2])}, {d(a[3])})"
+    if kind == "HYDF":
+        return f"kq_hydf(c, {d(a[0])}, {d(a[1])})"
+    if kind == "KPHOT":
+        return f"kq_kphot(c, {d(a[0])}, {'c.jh2o2' if a[1] == -2.0 else d(a[1])})"
+    if kind == "ALFA3":
+        return "c.alfa3"
+    if kind == "WETFAC":
+        return "c.wetfac"
+    return d(a[0])
+
+
+def device_source(k: KppMech) -> str:
+    """Strided straight-line routines for the device code (``namespace kmt2``, after the
+    rate-law functions of csrc/kmt2.cuh): Henry's law constants, the rate constants set
+    once and refreshed, RTOL, f, J, LU factorisation and solve.  Arrays live in a
+    lane-interleaved workspace: element i of a lane at ``p[i * s]``."""
+    out = ["// Generated by cmaq_gb300/mechgen/kpp_aq.py from CCTM/src/cloud/acm_ae7_kmt2: Henry's law",
+           "// constants (aqchem_kmt.F90:371-396), rate constants (aqchem_Initialize.F90:491-636,",
+           "// aqchem_Rates.F90:456-579), tolerances, Fun, Jac_SP, KppDecomp, KppSolve as straight-line",
+           "// code.  Included inside namespace kmt2 by csrc/kmt2.cuh.  Do not edit.",
+           "#pragma once", ""]
+    out.append("KQ_HD inline void kq_henry(Cell& c, float t2)\n{")
+    for h, (name, kind, a, e) in enumerate(k.henry):
+        if kind == "hlconst":
+            out.append(f"    c.henry[{h}] = (double)kq_hlconst((float){c_dbl(a)}, (float){c_dbl(e)}, t2);   // {name}")
+        elif kind == "exp":
+            out.append(f"    c.henry[{h}] = {c_dbl(a)} * exp({c_dbl(e)} * ((298.0 - (double)t2) / (298.0 * (double)t2)));"
+                       f"   // {name}")
+        else:
+            out.append(f"    c.henry[{h}] = {c_dbl(a)};   // {name}")
+    out.append("}\n")
+    for fn, upd in (("kq_rates_once", False), ("kq_rates_update", True)):
+        out.append(f"KQ_HD KQ_NOINLINE void {fn}(const Cell& c, const double* v, const double* f, double* r, long long s)\n{{")
+        if not upd:
+            out.append("    (void)v;\n    (void)f;")
+        for rx, (kind, args, refreshed, mt) in enumerate(k.rates):
+            if refreshed != upd:
+                continue
+            call = _rate_call(kind, args)
+            if mt:
+                call = f"(double)c.mtpyrac * {call}"
+            out.append(f"    r[{rx} * s] = {call};")
+        out.append("}\n")
+    special = sorted({i for i in range(k.nvar) if k.rtol[i] != k.rtol[0]})
+    assert len(set(k.atol)) == 1 and len({k.rtol[i] for i in special}) <= 1
+    cond = " || ".join(f"i == {i}" for i in special) or "false"
+    alt = c_dbl(k.rtol[special[0]]) if special else c_dbl(k.rtol[0])
+    out.append(f"KQ_HD inline double kq_rtol(int i) {{ return ({cond}) ? {alt} : {c_dbl(k.rtol[0])}; }}")
+    out.append(f"KQ_HD inline double kq_atol(int) {{ return {c_dbl(k.atol[0])}; }}\n")
+    out.append("KQ_HD inline void kq_add_diagonal(double* g, double x, long long s)\n{")
+    out += [f"    g[{d} * s] = g[{d} * s] + x;" for d in k.lu_diag[:-1]]
+    out.append("}\n")
+    body = unrolled_routines(k, qual="KQ_HD KQ_NOINLINE", acc=lambda name, i: f"{name}[{i} * s]")
+    for fn in ("kqu_fun(const double* v, const double* f, const double* r, double* vdot)",
+               "kqu_jac(const double* v, const double* f, const double* r, double* jvs)",
+               "kqu_decomp(double* jvs)", "kqu_solve(const double* jvs, double* x)"):
+        body = body.replace(fn, fn[:-1] + ", long long s)")
+    out.append(body)
+    return "\n".join(out)
+
+
 def unrolled_source(k: KppMech) -> str:
     return ("/* Generated by cmaq_gb300/mechgen/kpp_aq.py from CCTM/src/cloud/acm_ae7_kmt2: straight-line\n"
             " * f, J, LU factorisation and solve of the KMT2 aqueous mechanism, the same operations in\n"
@@ -505,6 +598,10 @@ def write_outputs(cmaq_root: str) -> KppMech:
     odir.mkdir(parents=True, exist_ok=True)
     (odir / "kmt2_aq.c").write_text(oracle_source(k))
     (odir / "kmt2_aq_unrolled.c").write_text(unrolled_source(k))
+    cdir = REPO / "cmaq_gb300" / "csrc" / "gen"
+    cdir.mkdir(parents=True, exist_ok=True)
+    (cdir / "kmt2_aq_consts.cuh").write_text(device_consts(k))
+    (cdir / "kmt2_aq.cuh").write_text(device_source(k))
     return k
 
 

@@ -243,6 +243,34 @@ int cmaqchem_ros3_solve_noalloc(const char* mechanism, long long ncell, double* 
                                 const unsigned char* night, double chemstep_min, double rtol,
                                 double atol, int* status, void* stream);
 
+/* KMT2 aqueous cloud chemistry (CCTM/src/cloud/acm_ae7_kmt2): the kinetic core of AQCHEM
+ * (aqchem_kmt.F90:371-543: Henry's law constants, Initialize, Update_RCONST and the KPP
+ * Rodas3 integration over TAUCLD) for ncell cloudy cells on the current device, one cell
+ * per thread.  No handle; the caller supplies a device workspace of at least
+ * cmaqchem_kmt2_workspace_doubles(1) doubles, and workspace / cmaqchem_kmt2_workspace_doubles(1)
+ * cells are integrated at a time.  Device arrays, [element][cell]:
+ *   params  [CMAQCHEM_KMT2_NPARAM][ncell]: TEMP2 (K), PRES_PA (Pa), TAUCLD (s), PRCRATE (mm/h),
+ *           WCAVG, WTAVG (kg/m3), AIRM (mol/m2), ALFA0, ALFA3 (1/s), COSZEN, JH2O2 (1/s),
+ *           GAS(LHO) (mol/mol), ISPC8, MTPYRAC, PHOTO (0/1); AQCHEM's REAL arguments are read
+ *           as float, as the reference has them;
+ *   var_mix [CMAQCHEM_KMT2_NVAR][ncell]: the KPP state as Initialize maps GAS and AEROSOL
+ *           (aqchem_Initialize.F90:308-421, mol/molV; L_HPLUS and L_OHMIN are recomputed);
+ *   var_out [CMAQCHEM_KMT2_NVAR][ncell]: the state at TAUCLD (molec/cm3, KPP's units);
+ *   fix_out [CMAQCHEM_KMT2_NFIX][ncell] or NULL: the fixed species;
+ *   stats   [CMAQCHEM_KMT2_NSTAT][ncell] int: steps, accepted, rejected, f and J evaluations,
+ *           factorisations, solves, singular factorisations, IERR (1 = success; < 0: the
+ *           reference's ros_ErrorMsg codes, -101 / -102 for its MET DATA and initial pH
+ *           errors, -100 after 16 integration passes), integration passes.
+ * Synchronises the stream; returns 0, or -1 on bad arguments or a CUDA error. */
+#define CMAQCHEM_KMT2_NVAR 161
+#define CMAQCHEM_KMT2_NFIX 4
+#define CMAQCHEM_KMT2_NPARAM 15
+#define CMAQCHEM_KMT2_NSTAT 10
+long long cmaqchem_kmt2_workspace_doubles(long long nlanes);
+int cmaqchem_kmt2_solve_device(long long ncell, const double* params, const double* var_mix, double* var_out,
+                               double* fix_out, int* stats, double* workspace, long long workspace_doubles,
+                               void* stream);
+
 /* Text of the last error of the calling thread; returns its length. */
 int cmaqchem_last_error(char* buf, size_t len);
 

@@ -1,0 +1,94 @@
+"""GPU parity of the KMT2 aqueous cloud chemistry kernel (CCTM/src/cloud/acm_ae7_kmt2)
+against the CPU oracle, through the C ABI (cmaqchem_kmt2_solve_device).
+
+The device code equals the oracle bit for bit when built for the host
+(tests/test_kmt2_host.py); on the GPU only CUDA's exp / pow / expf differ from libm by
+ulps.  Those move the rate constants in their last bits, so a cell takes the oracle's
+step sequence unless an accept / reject decision falls within rounding of its threshold.
+Tolerances: at least 90 % of the cells with the oracle's step counts, relative 1e-8 on
+those cells' species above 1e-6 of the cell's largest; every cell finished and within
+5e-2 (the reference's RTOL is 1e-2) of the oracle.
+"""
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+sys.path.insert(0, str(ROOT / "oracle"))
+from kmt2 import KMT2Oracle, P_TEMP2, STATS  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+IERR, NSTP, NACC = STATS.index("ierr"), STATS.index("nstp"), STATS.index("nacc")
+
+
+@pytest.fixture(scope="module")
+def o():
+    return KMT2Oracle()
+
+
+def _gpu(p, v, **kw):
+    import torch
+    from cmaq_gb300.aqchem import aqchem_kinetics
+    pt = torch.from_numpy(np.ascontiguousarray(p.T)).cuda()
+    vt = torch.from_numpy(np.ascontiguousarray(v.T)).cuda()
+    var, fix, st = aqchem_kinetics(pt, vt, with_fix=True, **kw)
+    torch.cuda.synchronize()
+    return var.cpu().numpy().T, fix.cpu().numpy().T, st.cpu().numpy().T
+
+
+def _rel(a, b):
+    big = np.abs(b) > 1e-6 * np.abs(b).max(axis=1, keepdims=True)
+    return np.where(big, np.abs(a - b) / np.maximum(np.abs(b), 1e-300), 0.0).max(axis=1)
+
+
+@pytest.mark.parametrize("seed,ispc8,mtpyrac", [(31, 0, 0), (32, 1, 1)])
+def test_kmt2_kernel_parity(o, seed, ispc8, mtpyrac):
+    p, v = o.synthetic_cells(200, seed=seed, ispc8=ispc8, mtpyrac=mtpyrac)
+    var, fix, st = _gpu(p, v)
+    vr, fr, sr, nfail = o.cells(p, v)
+    assert nfail == 0 and (st[:, IERR] == 1).all()
+    same = (st[:, NSTP] == sr[:, NSTP]) & (st[:, NACC] == sr[:, NACC])
+    assert same.mean() >= 0.9
+    err = _rel(var, vr)
+    assert err[same].max() < 1e-8
+    assert err.max() < 5e-2
+    assert np.abs(fix - fr).max() <= 1e-14 * np.abs(fr).max()
+
+
+def test_kmt2_lanes_do_not_change_the_bits(o):
+    """Fewer lanes than cells (each lane integrates several cells in turn) gives the same
+    bits as one lane per cell."""
+    p, v = o.synthetic_cells(45, seed=33)
+    a = _gpu(p, v)
+    b = _gpu(p, v, lanes=7)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[2], b[2])
+
+
+def test_kmt2_failed_cell_and_empty_call(o):
+    import torch
+    from cmaq_gb300.aqchem import aqchem_kinetics
+    p, v = o.synthetic_cells(4, seed=34)
+    p[1, P_TEMP2] = 0.0
+    _, _, st = _gpu(p, v)
+    assert st[1, IERR] == -101 and (st[[0, 2, 3], IERR] == 1).all()
+    out, stats = aqchem_kinetics(torch.zeros((15, 0), dtype=torch.float64, device="cuda"),
+                                 torch.zeros((161, 0), dtype=torch.float64, device="cuda"))
+    assert out.shape == (161, 0) and stats.shape == (10, 0)
+
+
+def test_kmt2_rejects_bad_arguments():
+    import torch
+    from cmaq_gb300 import _lib
+    from cmaq_gb300.aqchem import aqchem_kinetics
+    with pytest.raises(ValueError):
+        aqchem_kinetics(torch.zeros((15, 3), dtype=torch.float32, device="cuda"),
+                        torch.zeros((161, 3), dtype=torch.float64, device="cuda"))
+    L = _lib.lib()
+    ws = torch.empty(10, dtype=torch.float64, device="cuda")
+    x = torch.zeros((161, 2), dtype=torch.float64, device="cuda")
+    import ctypes as C
+    rc = L.cmaqchem_kmt2_solve_device(2, C.c_void_p(x.data_ptr()), C.c_void_p(x.data_ptr()), C.c_void_p(x.data_ptr()),
+                                      None, C.c_void_p(ws.data_ptr()), C.c_void_p(ws.data_ptr()), ws.numel(), None)
+    assert rc == -1 and "workspace" in _lib.last_error()
