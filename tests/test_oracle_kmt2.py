@@ -48,12 +48,16 @@ def test_sizes(o):
 @pytest.mark.skipif(not KMT2_DIR.exists(), reason="CMAQ sources not available")
 def test_generator_matches_the_reference_and_the_committed_tables():
     """kpp_aq.load raises unless the derived Jacobian terms and LU structure equal
-    aqchem_Jacobian.F90 / aqchem_JacobianSP.F90; the committed tables are its output."""
+    aqchem_Jacobian.F90 / aqchem_JacobianSP.F90; the committed oracle tables and device
+    headers are its output."""
     from cmaq_gb300.mechgen import kpp_aq
     k = kpp_aq.load(str(CMAQ))
     assert len(k.lu_irow) == 738 and len(k.blist) == 364
     assert (ROOT / "oracle" / "gen" / "kmt2_aq.c").read_text() == kpp_aq.oracle_source(k)
     assert (ROOT / "oracle" / "gen" / "kmt2_aq_unrolled.c").read_text() == kpp_aq.unrolled_source(k)
+    gen = ROOT / "cmaq_gb300" / "csrc" / "gen"
+    assert (gen / "kmt2_aq_consts.cuh").read_text() == kpp_aq.device_consts(k)
+    assert (gen / "kmt2_aq.cuh").read_text() == kpp_aq.device_source(k)
 
 
 # ----------------------------------------------------------------------------- set-up
