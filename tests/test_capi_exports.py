@@ -98,3 +98,30 @@ def test_c_host_program_links_and_calls(tmp_path):
     first, msg = r.stdout.splitlines()[:2]
     assert first.split() == ["149", "349", "1689", "1615", str(sum(range(149)))]
     assert "unknown mechanism" in msg
+
+
+@pytest.mark.skipif(not LIB.exists(), reason="libcmaqchem.so not built")
+def test_kmt2_entry_checks_arguments_before_any_cuda_call():
+    """cmaqchem_kmt2_* reject bad arguments on the host (no GPU needed)."""
+    from cmaq_gb300 import _lib
+    L = _lib.lib()
+    per_lane = L.cmaqchem_kmt2_workspace_doubles(1)
+    assert per_lane == 9 * 161 + 2 * 738 + 269 + 4
+    assert L.cmaqchem_kmt2_workspace_doubles(1000) == 1000 * per_lane
+    assert L.cmaqchem_kmt2_workspace_doubles(0) == 0
+    assert L.cmaqchem_kmt2_solve_device(0, None, None, None, None, None, None, 0, None) == 0
+    assert L.cmaqchem_kmt2_solve_device(-1, None, None, None, None, None, None, 0, None) == -1
+    assert "ncell" in _lib.last_error()
+    assert L.cmaqchem_kmt2_solve_device(4, None, None, None, None, None, None, 0, None) == -1
+    assert "null" in _lib.last_error()
+    buf = (C.c_double * 8)()
+    p = C.cast(buf, C.c_void_p)
+    assert L.cmaqchem_kmt2_solve_device(4, p, p, p, None, p, p, 8, None) == -1
+    assert "workspace" in _lib.last_error()
+
+
+def test_aqchem_wrapper_rejects_host_tensors():
+    torch = pytest.importorskip("torch")
+    from cmaq_gb300.aqchem import aqchem_kinetics
+    with pytest.raises(ValueError, match="CUDA tensor"):
+        aqchem_kinetics(torch.zeros((15, 2), dtype=torch.float64), torch.zeros((161, 2), dtype=torch.float64))
