@@ -23,7 +23,9 @@ and, for the device code, ``cmaq_gb300/csrc/gen/kmt2_aq_consts.cuh`` (sizes, spe
 indices) and ``cmaq_gb300/csrc/gen/kmt2_aq.cuh`` (Henry's law constants, rate constants,
 tolerances, f, J, LU factorisation and solve as strided straight-line code; the rate-law
 functions they call are in ``csrc/kmt2.cuh``).  ``oracle/gen/kmt2_aq_unrolled.c`` holds
-the same straight-line f, J, LU and solve for the oracle's bit-for-bit check.
+the same straight-line f, J, LU and solve for the oracle's bit-for-bit check, and
+``cmaq_gb300/mechs/kmt2/manifest.json`` the species names and the FLOP counts of those
+routines (the benchmark's algorithmic work per step).
 
 The Jacobian terms (one partial derivative per reaction and variable reactant,
 combined per Jacobian entry with the species' net coefficients) and the sparse LU
@@ -38,6 +40,7 @@ Fortran literal kinds are kept: a literal without a ``D`` exponent or ``_dp`` ki
 from __future__ import annotations
 
 import argparse
+import json
 import os
 import re
 from dataclasses import dataclass, field
@@ -585,6 +588,28 @@ def device_source(k: KppMech) -> str:
     return "\n".join(out)
 
 
+def flop_counts(k: KppMech) -> dict:
+    """Floating-point operations of the straight-line routines as emitted (a multiply by
+    a coefficient of +-1 is not emitted; divide = 1), and of one Rodas3 attempt's vector
+    work (11 axpys, 2 scaled by 1, the error norm's 6 per species)."""
+    unit = lambda c: abs(c) == 1.0
+    fun = sum(len(f) for f in k.factors) + sum(len(t) + sum(not unit(c) for c, _ in t) for t in k.vdot)
+    jac = sum((b[1] > 1) + len(b[2]) for b in k.blist) + sum(len(t) + sum(not unit(c) for c, _ in t) for t in k.jvs)
+    lower = sum(k.lu_diag[r] - k.lu_crow[r] for r in range(k.nvar))
+    updates = sum(k.lu_crow[k.lu_icol[kk] + 1] - k.lu_diag[k.lu_icol[kk]] - 1
+                  for r in range(k.nvar) for kk in range(k.lu_crow[r], k.lu_diag[r]))
+    decomp = lower + 2 * updates + k.nvar                  # divisions, multiply-adds, diagonal shift
+    solve = 2 * (len(k.lu_irow) - k.nvar) + k.nvar
+    vector = 11 * 2 * k.nvar + 6 * k.nvar
+    return {"fun": fun, "jac": jac, "decomp": decomp, "solve": solve, "vector": vector,
+            "per_step": fun + jac, "per_attempt": decomp + 4 * solve + 2 * fun + vector}
+
+
+def manifest(k: KppMech) -> dict:
+    return {"mechanism": "kmt2 (CCTM/src/cloud/acm_ae7_kmt2)", "nvar": k.nvar, "nfix": k.nfix, "nreact": k.nreact,
+            "lu_nonzero": len(k.lu_irow), "species": k.names, "flops": flop_counts(k)}
+
+
 def unrolled_source(k: KppMech) -> str:
     return ("/* Generated by cmaq_gb300/mechgen/kpp_aq.py from CCTM/src/cloud/acm_ae7_kmt2: straight-line\n"
             " * f, J, LU factorisation and solve of the KMT2 aqueous mechanism, the same operations in\n"
@@ -602,6 +627,9 @@ def write_outputs(cmaq_root: str) -> KppMech:
     cdir.mkdir(parents=True, exist_ok=True)
     (cdir / "kmt2_aq_consts.cuh").write_text(device_consts(k))
     (cdir / "kmt2_aq.cuh").write_text(device_source(k))
+    mdir = REPO / "cmaq_gb300" / "mechs" / "kmt2"
+    mdir.mkdir(parents=True, exist_ok=True)
+    (mdir / "manifest.json").write_text(json.dumps(manifest(k), indent=1) + "\n")
     return k
 
 

@@ -186,3 +186,73 @@ def solver_inputs(g: GridInputs, solver):
     rki, sun = solver.rconst(t["conc"], t["ta"], t["qv"], t["dens"], t["pres"], t["seaice"], t["ocean_szone"],
                              t["rj"], t["khetero"])
     return y0, rki, (1 - sun).to(torch.uint8)
+
+
+# ----------------------------------------------------------------------------- cloudy cells
+KMT2_PARAMS = ("temp2", "pres_pa", "taucld", "prcrate", "wcavg", "wtavg", "airm", "alfa0", "alfa3", "coszen", "jh2o2",
+               "ho", "ispc8", "mtpyrac", "photo")
+
+# log10 ranges of the state as AQCHEM's Initialize maps it from GAS and AEROSOL (mol/molV)
+_CLOUD_RANGES = {
+    "G_SO2": (-9.5, -8), "G_HNO3": (-10.5, -9), "G_CO2": (-3.45, -3.35), "G_NH3": (-10.5, -8.5),
+    "G_H2O2": (-10, -8.7), "G_O3": (-7.6, -7.2), "G_HCOOH": (-10.5, -9), "G_MHP": (-10.5, -9),
+    "G_PAA": (-11, -10), "G_HCL": (-11.5, -10), "G_GLY": (-11.5, -10), "G_MGLY": (-11.5, -10),
+    "G_IEPOX": (-11, -9.5), "G_NO2": (-10, -8), "G_HONO": (-11.5, -10), "G_HNO4": (-12, -10.5),
+    "G_NO3": (-13.5, -12), "G_CH3O2": (-12.5, -11), "G_GCOL": (-12, -10.5), "G_CCOOH": (-10.5, -9),
+    "G_HCHO": (-9.5, -8.5), "G_HO2": (-12, -10.7), "G_HCHOP": (-13, -11),
+    "A_NO3AKN": (-13, -11.5), "A_NH4AKN": (-12.5, -11), "A_CLAKN": (-14, -12.5), "A_NAAKN": (-14, -12.5),
+    "A_SO4AKN": (-12.5, -11), "A_PECAKN": (-13, -11.5), "A_POAAKN": (-12.5, -11), "A_PRIAKN": (-13, -11.5),
+    "L_SO4MIN2": (-10, -9), "L_NO3MIN": (-10.5, -9.3), "L_NH4PLUS": (-9.8, -8.8), "L_CLMIN": (-12, -10.5),
+    "L_PRIACC": (-11.5, -10), "L_NAPLUS": (-12, -10.5), "L_CAPLUS2": (-12.5, -11), "L_MGPLUS2": (-13, -11.5),
+    "L_KPLUS": (-13, -11.5), "L_PECACC": (-11.5, -10.5), "L_ORGC": (-12, -10.5), "L_OXLACMIN2": (-12, -10.5),
+    "L_POAACC": (-11, -9.8), "L_FEPLUS3": (-14.5, -13), "L_MNPLUS2": (-15.5, -14),
+}
+_CLOUD_RANGES_ISPC8 = {"G_IMAE": (-12, -10.5), "G_IHMML": (-12, -10.5), "L_IETET": (-12, -10.5),
+                       "L_IEOS": (-12, -10.5), "L_DIMER": (-13, -11.5), "L_IMGA": (-13, -11.5),
+                       "L_IMOS": (-13, -11.5)}
+
+
+def kmt2_manifest() -> dict:
+    return json.loads((Path(__file__).resolve().parent / "mechs" / "kmt2" / "manifest.json").read_text())
+
+
+def make_cloud_cells(n: int, seed: int = 0, ispc8: int = 0, mtpyrac: int = 0):
+    """Seeded cloudy cells for the KMT2 aqueous chemistry: (params [n][15], var_mix
+    [n][161]) in the order of ``KMT2_PARAMS`` and of the KPP species.  Temperature
+    268-298 K, 700-1000 hPa, liquid water 0.05-1 g/m3, cloud time 600-3600 s, half of
+    the cells precipitating 0.1-5 mm/h, cloudy air mass 5e3-8e4 mol/m2, Aitken
+    scavenging 1e-5-1e-3 1/s, cos(zenith) -0.5-1 with J(H2O2) 3e-7-1e-5 1/s when sunlit;
+    gas and aerosol species log-uniform within the decades of ``_CLOUD_RANGES``.  REAL
+    arguments of AQCHEM are rounded to float32."""
+    names = kmt2_manifest()["species"]
+    index = {s: i for i, s in enumerate(names)}
+    rng = np.random.default_rng(seed)
+    p = np.zeros((n, len(KMT2_PARAMS)))
+    f32 = lambda a: a.astype(np.float32).astype(np.float64)
+    col = {k: i for i, k in enumerate(KMT2_PARAMS)}
+    p[:, col["temp2"]] = f32(rng.uniform(268.0, 298.0, n))
+    p[:, col["pres_pa"]] = f32(rng.uniform(70000.0, 100000.0, n))
+    p[:, col["taucld"]] = f32(rng.choice([600.0, 1200.0, 1800.0, 3600.0], n))
+    p[:, col["prcrate"]] = f32(np.where(rng.random(n) < 0.5, rng.uniform(0.1, 5.0, n), 0.0))
+    wc = rng.uniform(5e-5, 1e-3, n)
+    p[:, col["wcavg"]] = f32(wc)
+    p[:, col["wtavg"]] = f32(wc * rng.uniform(1.0, 1.5, n))
+    p[:, col["airm"]] = f32(rng.uniform(5e3, 8e4, n))
+    p[:, col["alfa0"]] = f32(10 ** rng.uniform(-5, -3, n))
+    p[:, col["alfa3"]] = f32(10 ** rng.uniform(-5, -3, n))
+    p[:, col["coszen"]] = f32(rng.uniform(-0.5, 1.0, n))
+    p[:, col["jh2o2"]] = np.where(p[:, col["coszen"]] > 0, 10 ** rng.uniform(-6.5, -5, n), 0.0)
+    p[:, col["ho"]] = 10 ** rng.uniform(-14.5, -12.5, n)
+    p[:, col["ispc8"]] = ispc8
+    p[:, col["mtpyrac"]] = mtpyrac
+    v = np.zeros((n, int(kmt2_manifest()["nvar"])))
+    ranges = dict(_CLOUD_RANGES)
+    if ispc8:
+        ranges.update(_CLOUD_RANGES_ISPC8)
+    else:
+        ranges["L_ISO3"] = (-12, -10.5)
+    if mtpyrac:
+        ranges["G_PYRAC"] = (-12, -10.5)
+    for name, (lo, hi) in ranges.items():
+        v[:, index[name]] = 10 ** rng.uniform(lo, hi, n)
+    return p, v

@@ -6,10 +6,10 @@ chemistry (CCTM/src/cloud/acm_ae7_kmt2: AQCHEM's set-up, the KPP rate laws, Fun,
 Jac_SP, KppDecomp / KppSolve and the Rodas3 Rosenbrock integrator).  Nothing in the
 product imports it.
 
-``synthetic_cells`` makes seeded cloudy-cell inputs: the AQCHEM arguments the kinetic
-core reads and the state vector as Initialize maps it from the gas and aerosol arrays
-(aqchem_Initialize.F90:308-421), in mixing ratios with ranges typical of polluted and
-clean continental clouds.
+``synthetic_cells`` gives the seeded cloudy-cell inputs of
+``cmaq_gb300.synthetic.make_cloud_cells``: the AQCHEM arguments the kinetic core reads
+and the state vector as Initialize maps it from the gas and aerosol arrays
+(aqchem_Initialize.F90:308-421), in mixing ratios.
 """
 from __future__ import annotations
 
@@ -153,51 +153,11 @@ class KMT2Oracle:
 
     # ------------------------------------------------------------------ synthetic cells
     def synthetic_cells(self, n: int, seed: int = 0, ispc8: int = 0, mtpyrac: int = 0):
-        """Seeded cloudy cells: temperature 268-298 K, 700-1000 hPa, liquid water
-        0.05-1 g/m3, cloud time 600-3600 s, half of them precipitating; gas and aerosol
-        species log-uniform within a decade or two of typical continental values."""
-        rng = np.random.default_rng(seed)
-        p = np.zeros((n, self.nparam))
-        f32 = lambda a: a.astype(np.float32).astype(np.float64)   # REAL(4) arguments
-        p[:, P_TEMP2] = f32(rng.uniform(268.0, 298.0, n))
-        p[:, P_PRES_PA] = f32(rng.uniform(70000.0, 100000.0, n))
-        p[:, P_TAUCLD] = f32(rng.choice([600.0, 1200.0, 1800.0, 3600.0], n))
-        p[:, P_PRCRATE] = f32(np.where(rng.random(n) < 0.5, rng.uniform(0.1, 5.0, n), 0.0))
-        wc = rng.uniform(5e-5, 1e-3, n)
-        p[:, P_WCAVG] = f32(wc)
-        p[:, P_WTAVG] = f32(wc * rng.uniform(1.0, 1.5, n))
-        p[:, P_AIRM] = f32(rng.uniform(5e3, 8e4, n))
-        p[:, P_ALFA0] = f32(10 ** rng.uniform(-5, -3, n))
-        p[:, P_ALFA3] = f32(10 ** rng.uniform(-5, -3, n))
-        p[:, P_COSZEN] = f32(rng.uniform(-0.5, 1.0, n))
-        p[:, P_JH2O2] = np.where(p[:, P_COSZEN] > 0, 10 ** rng.uniform(-6.5, -5, n), 0.0)
-        p[:, P_HO] = 10 ** rng.uniform(-14.5, -12.5, n)
-        p[:, P_ISPC8] = ispc8
-        p[:, P_MTPYRAC] = mtpyrac
-        v = np.zeros((n, self.nvar))
-        lu = lambda lo, hi: 10 ** rng.uniform(lo, hi, n)
-        ranges = {
-            "G_SO2": (-9.5, -8), "G_HNO3": (-10.5, -9), "G_CO2": (-3.45, -3.35), "G_NH3": (-10.5, -8.5),
-            "G_H2O2": (-10, -8.7), "G_O3": (-7.6, -7.2), "G_HCOOH": (-10.5, -9), "G_MHP": (-10.5, -9),
-            "G_PAA": (-11, -10), "G_HCL": (-11.5, -10), "G_GLY": (-11.5, -10), "G_MGLY": (-11.5, -10),
-            "G_IEPOX": (-11, -9.5), "G_NO2": (-10, -8), "G_HONO": (-11.5, -10), "G_HNO4": (-12, -10.5),
-            "G_NO3": (-13.5, -12), "G_CH3O2": (-12.5, -11), "G_GCOL": (-12, -10.5), "G_CCOOH": (-10.5, -9),
-            "G_HCHO": (-9.5, -8.5), "G_HO2": (-12, -10.7), "G_HCHOP": (-13, -11),
-            "A_NO3AKN": (-13, -11.5), "A_NH4AKN": (-12.5, -11), "A_CLAKN": (-14, -12.5), "A_NAAKN": (-14, -12.5),
-            "A_SO4AKN": (-12.5, -11), "A_PECAKN": (-13, -11.5), "A_POAAKN": (-12.5, -11), "A_PRIAKN": (-13, -11.5),
-            "L_SO4MIN2": (-10, -9), "L_NO3MIN": (-10.5, -9.3), "L_NH4PLUS": (-9.8, -8.8), "L_CLMIN": (-12, -10.5),
-            "L_PRIACC": (-11.5, -10), "L_NAPLUS": (-12, -10.5), "L_CAPLUS2": (-12.5, -11), "L_MGPLUS2": (-13, -11.5),
-            "L_KPLUS": (-13, -11.5), "L_PECACC": (-11.5, -10.5), "L_ORGC": (-12, -10.5), "L_OXLACMIN2": (-12, -10.5),
-            "L_POAACC": (-11, -9.8), "L_FEPLUS3": (-14.5, -13), "L_MNPLUS2": (-15.5, -14),
-        }
-        if ispc8:
-            ranges.update({"G_IMAE": (-12, -10.5), "G_IHMML": (-12, -10.5), "L_IETET": (-12, -10.5),
-                           "L_IEOS": (-12, -10.5), "L_DIMER": (-13, -11.5), "L_IMGA": (-13, -11.5),
-                           "L_IMOS": (-13, -11.5)})
-        else:
-            ranges["L_ISO3"] = (-12, -10.5)
-        if mtpyrac:
-            ranges["G_PYRAC"] = (-12, -10.5)
-        for name, (lo, hi) in ranges.items():
-            v[:, self.index[name]] = lu(lo, hi)
-        return p, v
+        """Seeded cloudy cells (cmaq_gb300.synthetic.make_cloud_cells: the benchmark's
+        inputs), params [n][15] and var_mix [n][161]."""
+        import sys
+        root = str(HERE.parent)
+        if root not in sys.path:
+            sys.path.insert(0, root)
+        from cmaq_gb300.synthetic import make_cloud_cells
+        return make_cloud_cells(n, seed=seed, ispc8=ispc8, mtpyrac=mtpyrac)
