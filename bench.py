@@ -26,6 +26,10 @@ Arms and extras
   ``cracmm2``.
 * --impl reference: the reference algorithm (C oracle; the Fortran cannot be
   compiled here) on all host cores, bounded sample per step.
+* --only-aqchem: the KMT2 aqueous kinetics kernel alone (cmaqchem_kmt2_solve_device) on
+  --aqchem-cells seeded cloudy cells per call, with its own line: cells/s, FP64
+  roofline, end to end through pinned host memory, the C oracle on a host sample and a
+  parity summary of that sample.
 
 Multi-GPU (torchrun): every rank integrates its own grid of the same size (CMAQ
 gives each process its own subdomain; chemistry exchanges nothing), timing is the
@@ -381,6 +385,72 @@ def run_gear(device: int, steps: int) -> dict:
     return out
 
 
+def run_aqchem(device: int, ncell: int, steps: int, warmup: int, threads: int) -> dict:
+    """KMT2 aqueous kinetics (cmaqchem_kmt2_solve_device): one call integrates ncell seeded
+    cloudy cells over their cloud time.  Device time by CUDA events around each call
+    (inputs resident); end to end with the inputs copied from pinned host memory and the
+    state copied back; FLOPs from the per-cell step counts and the generated routines'
+    operation counts (cmaq_gb300/mechs/kmt2/manifest.json); the oracle on a CPU sample
+    for the baseline and a parity summary of that sample."""
+    import torch
+    from cmaq_gb300.aqchem import aqchem_kinetics
+    from cmaq_gb300.synthetic import kmt2_manifest, make_cloud_cells
+    fl = kmt2_manifest()["flops"]
+    p, v = make_cloud_cells(ncell, seed=2018)
+    dev = torch.device(f"cuda:{device}")
+    hp = torch.from_numpy(np.ascontiguousarray(p.T)).pin_memory()
+    hv = torch.from_numpy(np.ascontiguousarray(v.T)).pin_memory()
+    hout = torch.empty((161, ncell), dtype=torch.float64).pin_memory()
+    pt, vt = hp.to(dev), hv.to(dev)
+    for _ in range(warmup):
+        out, st = aqchem_kinetics(pt, vt)
+    torch.cuda.synchronize(dev)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ms = []
+    for _ in range(steps):
+        ev[0].record()
+        out, st = aqchem_kinetics(pt, vt)
+        ev[1].record()
+        torch.cuda.synchronize(dev)
+        ms.append(ev[0].elapsed_time(ev[1]))
+    sd = st.cpu().numpy().astype(np.int64)
+    nstp, njac = sd[0].sum(), sd[4].sum()
+    flops = float(njac * fl["per_step"] + nstp * fl["per_attempt"])
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        pt.copy_(hp, non_blocking=True)
+        vt.copy_(hv, non_blocking=True)
+        out, _ = aqchem_kinetics(pt, vt)
+        hout.copy_(out, non_blocking=True)
+        torch.cuda.synchronize(dev)
+    e2e_s = (time.perf_counter() - t0) / steps
+    dev_ms = float(np.mean(ms))
+    res = {"ncell": ncell, "ms_per_call": dev_ms, "value": ncell / (dev_ms * 1e-3),
+           "achieved_tflops": flops / (dev_ms * 1e-3) / 1e12, "flops_per_call": flops,
+           "steps_per_cell": float(sd[1].mean()), "max_steps_per_cell": int(sd[1].max()),
+           "failed_cells": int((sd[8] != 1).sum()),
+           "e2e": {"value": ncell / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": int(hp.numel() + hv.numel()) * 8,
+                   "d2h_bytes_per_step": int(hout.numel()) * 8}}
+    if threads > 0:                                   # CPU baseline leg: the oracle on a sample
+        sys.path.insert(0, str(ROOT / "oracle"))
+        from kmt2 import KMT2Oracle
+        o = KMT2Oracle()
+        nsample = min(ncell, 4000 * threads)             # a few seconds of host time
+        t0 = time.perf_counter()
+        vr, _, sr, _ = o.cells(p[:nsample], v[:nsample], threads=threads)
+        wall = time.perf_counter() - t0
+        got = out[:, :nsample].cpu().numpy().T
+        same = (sd[0, :nsample] == sr[:, 0]) & (sd[1, :nsample] == sr[:, 1])
+        big = np.abs(vr) > 1e-6 * np.abs(vr).max(axis=1, keepdims=True)
+        rel = np.where(big, np.abs(got - vr) / np.maximum(np.abs(vr), 1e-300), 0.0).max(axis=1)
+        res["cpu"] = {"value": nsample / wall, "cells": nsample, "wall_s": wall}
+        res["parity"] = {"cells": nsample, "same_steps": float(same.mean()),
+                         "max_rel_same_steps": float(rel[same].max()) if same.any() else None,
+                         "max_rel": float(rel.max())}
+    return res
+
+
 def barrier(dist):
     if dist is not None:
         import torch.distributed as tdist
@@ -461,6 +531,9 @@ def main():
     ap.add_argument("--adjoint-dims", default="100x100x35", help="grid of the adjoint window, NCOLSxNROWSxNLAYS")
     ap.add_argument("--only-adjoint", action="store_true",
                     help="time only the adjoint window and print its own line (for profiling)")
+    ap.add_argument("--only-aqchem", action="store_true",
+                    help="time only the KMT2 aqueous kinetics kernel and print its own line")
+    ap.add_argument("--aqchem-cells", type=int, default=200000, help="cloudy cells per KMT2 call")
     ap.add_argument("--solver", default="ros3", choices=["ros3", "ebi", "gear"],
                     help="solver of the timed CHEM calls (the metric is quoted for ros3)")
     a = ap.parse_args()
@@ -512,6 +585,28 @@ def main():
                               "higher_is_better": False, "dtype": "f64", "data": "synthetic", "adjoint": r}))
         return 0
     peak_tf, _ = _lib.fp64_peak(device)
+    if a.only_aqchem:
+        thr = 0 if (a.no_cpu or rank != 0) else host_threads()
+        r = run_aqchem(device, a.aqchem_cells, min(a.steps, 5), max(a.warmup, 3), thr)
+        if rank == 0:
+            line = {"metric": "KMT2 aqueous chemistry: cloudy cells integrated over their cloud time per second",
+                    "value": r["value"], "unit": "cells/s", "n_gpus": 1, "steps": min(a.steps, 5),
+                    "warmup": max(a.warmup, 3), "ms_per_step": r["ms_per_call"], "higher_is_better": True,
+                    "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                    "data": "synthetic (seeded; cmaq_gb300/synthetic.py: make_cloud_cells)",
+                    "config": {"workload": f"{r['ncell']} cloudy cells, KMT2 aqueous mechanism "
+                                           "(CCTM/src/cloud/acm_ae7_kmt2), TAUCLD 600-3600 s",
+                               "l2": f"inputs of {r['ncell'] * 176 * 8 / 1e6:.0f} MB per call, larger than the "
+                                     "129 MB L2, plus a 1 GB workspace"},
+                    "roofline": {"bound": "fp64", "achieved": r["achieved_tflops"], "peak": peak_tf,
+                                 "unit": "TFLOP/s", "frac": r["achieved_tflops"] / peak_tf, "traffic": None,
+                                 "peak_source": "measured live (cmaqchem_diag_fp64_peak)"},
+                    "e2e": r["e2e"], "gpu_launches": min(a.steps, 5), "aqchem": r}
+            if "cpu" in r:
+                line["cpu_baseline"] = {"value": r["cpu"]["value"], "unit": "cells/s", "cores": host_threads(),
+                                        "kind": "port", "sample": f"{r['cpu']['cells']} cells"}
+            print(json.dumps(line))
+        return 0
     issue = {f"{k}_lanes": _lib.fp64_issue(device, k) for k in (1, 32)}
 
     tuned = None if a.no_autotune else run_autotune(a.workload, 2018 + rank, device)
