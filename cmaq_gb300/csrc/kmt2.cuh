@@ -56,12 +56,6 @@ struct Cell {   // aqchem_Global of one cell
 };
 
 // ----------------------------------------------------------------------------- rate laws
-// HLCONST with EFFECTIVE = .FALSE. (hlconst.F:509-511), REAL(4) throughout
-KQ_HD inline float kq_hlconst(float a, float e, float temp)
-{
-    const float tfac = (298.0f - temp) / (298.0f * temp);
-    return a * expf(e * tfac);
-}
 
 // Schwartz (1986) mass-transfer coefficient of KMTF / KMTB (aqchem_Initialize.F90:53-104);
 // PI is a REAL(4) literal there
@@ -187,6 +181,41 @@ KQ_HD inline void kq_ionic(Cell& c, const double* v, long long s)
     c.gm2 = gm2 > 1.0e-30 ? gm2 : 1.0e-30;
 }
 
+// exp(t) by t = n ln2 + r (Cody-Waite split of ln 2, |r| <= ln2/2) and a Taylor series to
+// r^13, with IEEE operations, fma, rint and ldexp only: the same bits on host and device.
+KQ_HD inline double kq_exp(double t)
+{
+    const double ln2_hi = 0x1.62e42fee00000p-1, ln2_lo = 0x1.a39ef35793c76p-33;
+    if (t > 709.0) return INFINITY;
+    if (t < -745.0) return 0.0;
+    const double n = rint(t * 0x1.71547652b82fep+0);
+    const double r = fma(-n, ln2_lo, fma(-n, ln2_hi, t));
+    double e = 0x1.6124613a86d09p-33;
+    e = fma(e, r, 0x1.1eed8eff8d898p-29);
+    e = fma(e, r, 0x1.ae64567f544e4p-26);
+    e = fma(e, r, 0x1.27e4fb7789f5cp-22);
+    e = fma(e, r, 0x1.71de3a556c734p-19);
+    e = fma(e, r, 0x1.a01a01a01a01ap-16);
+    e = fma(e, r, 0x1.a01a01a01a01ap-13);
+    e = fma(e, r, 0x1.6c16c16c16c17p-10);
+    e = fma(e, r, 0x1.1111111111111p-7);
+    e = fma(e, r, 0x1.5555555555555p-5);
+    e = fma(e, r, 0x1.5555555555555p-3);
+    e = fma(e, r, 0.5);
+    e = fma(e, r, 1.0);
+    e = fma(e, r, 1.0);
+    return ldexp(e, (int)n);
+}
+
+// HLCONST with EFFECTIVE = .FALSE. (hlconst.F:509-511), REAL(4) throughout; its EXP is
+// kq_exp rounded to float (libm's and CUDA's expf differ by up to 2 float ulps, 1e-7
+// relative, which would move the gas / aqueous partitioning by as much)
+KQ_HD inline float kq_hlconst(float a, float e, float temp)
+{
+    const float tfac = (298.0f - temp) / (298.0f * temp);
+    return a * (float)kq_exp((double)(e * tfac));
+}
+
 // x**y for x >= 0, y > 0 from series with IEEE +, -, *, /, fma, frexp/ldexp and rint only,
 // identical on host and device (the routine of the Gear kernels, gear.cuh: gpow; libm
 // and CUDA pow differ by ulps, which move step-size decisions): log by 2 atanh(s) to
@@ -217,26 +246,7 @@ KQ_HD inline double kq_pow(double x, double y)
     p = fma(p, z, 1.0);
     const double ln2_hi = 0x1.62e42fee00000p-1, ln2_lo = 0x1.a39ef35793c76p-33;
     const double lx = fma((double)k, ln2_hi, fma((double)k, ln2_lo, (2.0 * u) * p));
-    const double t = y * lx;
-    if (t > 709.0) return INFINITY;
-    if (t < -745.0) return 0.0;
-    const double n = rint(t * 0x1.71547652b82fep+0);
-    const double r = fma(-n, ln2_lo, fma(-n, ln2_hi, t));
-    double e = 0x1.6124613a86d09p-33;
-    e = fma(e, r, 0x1.1eed8eff8d898p-29);
-    e = fma(e, r, 0x1.ae64567f544e4p-26);
-    e = fma(e, r, 0x1.27e4fb7789f5cp-22);
-    e = fma(e, r, 0x1.71de3a556c734p-19);
-    e = fma(e, r, 0x1.a01a01a01a01ap-16);
-    e = fma(e, r, 0x1.a01a01a01a01ap-13);
-    e = fma(e, r, 0x1.6c16c16c16c17p-10);
-    e = fma(e, r, 0x1.1111111111111p-7);
-    e = fma(e, r, 0x1.5555555555555p-5);
-    e = fma(e, r, 0x1.5555555555555p-3);
-    e = fma(e, r, 0.5);
-    e = fma(e, r, 1.0);
-    e = fma(e, r, 1.0);
-    return ldexp(e, (int)n);
+    return kq_exp(y * lx);
 }
 
 #include "gen/kmt2_aq.cuh"

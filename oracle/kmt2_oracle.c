@@ -28,7 +28,7 @@
  * literals and REAL(4) intermediates where the reference has them, no contraction of
  * a*b+c (built with -ffp-contract=off; the reference's build flags decide that for
  * the Fortran, which cannot be compiled here).  The step-size factor Err**(1/3) uses
- * the portable pow of portable_pow.h.
+ * the portable pow of portable_pow.h and HLCONST's REAL(4) EXP its portable exp.
  */
 #include <float.h>
 #include <math.h>
@@ -76,11 +76,14 @@ static const double KQ_PHI = 6.0221413e17;   /* aqchem_Global.F90: PHI */
 static const double KQ_DAQ = 1.0e-9;         /* aqchem_Global.F90: DAQ */
 
 /* ------------------------------------------------------------------ Henry's law */
-/* hlconst.F:509-511 with EFFECTIVE = .FALSE.: REAL(4) throughout. */
+/* hlconst.F:509-511 with EFFECTIVE = .FALSE.: REAL(4) throughout.  The REAL(4) EXP is
+ * the portable exp rounded to float: libm's and CUDA's expf differ by up to 2 float ulps
+ * (1e-7 relative, which moves the gas / aqueous partitioning by as much), so oracle and
+ * device share this routine; it is within one float ulp of the exact value. */
 static float kq_hlconst(float a, float e, float temp)
 {
     const float tfac = (298.0f - temp) / (298.0f * temp);
-    return a * expf(e * tfac);
+    return a * (float)portable_exp((double)(e * tfac));
 }
 
 /* ------------------------------------------------------------------ rate laws */

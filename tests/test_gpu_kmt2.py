@@ -2,9 +2,11 @@
 against the CPU oracle, through the C ABI (cmaqchem_kmt2_solve_device).
 
 The device code equals the oracle bit for bit when built for the host
-(tests/test_kmt2_host.py); on the GPU only CUDA's exp / pow / expf differ from libm by
-ulps.  Those move the rate constants in their last bits, so a cell takes the oracle's
-step sequence unless an accept / reject decision falls within rounding of its threshold.
+(tests/test_kmt2_host.py); on the GPU only CUDA's double exp / pow differ from libm by
+ulps (the REAL(4) Henry's law constants use a portable exp on both sides, because float
+expf differs by up to 2 float ulps).  The double ulps move the rate constants in their
+last bits, so a cell takes the oracle's step sequence unless an accept / reject decision
+falls within rounding of its threshold.
 Tolerances: at least 90 % of the cells with the oracle's step counts, relative 1e-8 on
 those cells' species above 1e-6 of the cell's largest; every cell finished and within
 5e-2 (the reference's RTOL is 1e-2) of the oracle.
