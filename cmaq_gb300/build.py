@@ -69,7 +69,8 @@ def lib_path(variant: str = "default") -> Path:
 
 
 def build(jobs: int | None = None, verbose: bool = False, variant: str = "default") -> Path:
-    """Build one register-cap variant (``r255`` is the default library)."""
+    """Build one variant of ``VARIANTS`` (``default``: generated functions capped at 128
+    registers with L2 prefetch, 16 resident warps per SM)."""
     if variant not in VARIANTS:
         raise ValueError(f"unknown variant {variant}")
     out_dir = BUILD if variant == "default" else BUILD / variant
