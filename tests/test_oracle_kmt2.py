@@ -360,3 +360,24 @@ def test_sunlit_and_dark_cells(o, cells):
     p, v = cells
     assert (p[:, P_COSZEN] > 0).any() and (p[:, P_COSZEN] <= 0).any()
     assert (p[:, P_PRCRATE] > 0).any() and (p[:, P_PRCRATE] == 0).any()
+
+
+def test_manifest_flop_counts_match_the_generated_code():
+    """The benchmark's algorithmic FLOPs (cmaq_gb300/mechs/kmt2/manifest.json) are the
+    binary +, -, *, / of the generated straight-line routines (unary minus is not counted;
+    the decomposition's count adds the diagonal shift of ros_PrepareMatrix, one add per
+    species)."""
+    import json
+    import re
+    man = json.loads((ROOT / "cmaq_gb300" / "mechs" / "kmt2" / "manifest.json").read_text())
+    src = (ROOT / "oracle" / "gen" / "kmt2_aq_unrolled.c").read_text()
+    counts = {}
+    for name in ("fun", "jac", "decomp", "solve"):
+        body = src.split(f"kqu_{name}(", 1)[1].split("\n}\n", 1)[0]
+        body = re.sub(r"fabs\([^)]*\) < DBL_MIN", "", body)
+        counts[name] = len(re.findall(r" [-+*/] ", body))
+    fl = man["flops"]
+    assert counts["fun"] == fl["fun"] and counts["jac"] == fl["jac"] and counts["solve"] == fl["solve"]
+    assert counts["decomp"] + man["nvar"] == fl["decomp"]
+    assert fl["per_attempt"] == fl["decomp"] + 4 * fl["solve"] + 2 * fl["fun"] + fl["vector"]
+    assert man["species"][:2] and len(man["species"]) == man["nvar"] + man["nfix"]
