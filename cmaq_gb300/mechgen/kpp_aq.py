@@ -291,7 +291,8 @@ def _henry(kmt_text: str, hl_text: str, names: list[str]):
     table = {}
     for m in re.finditer(r"DATA\s+SUBNAME\(\s*\d+\),\s*A\(\s*\d+\),\s*E\(\s*\d+\)\s*/\s*'([^']*)'\s*,\s*([^,]+),\s*([^/]+)/",
                          hl_text):
-        table[m.group(1).strip()] = (float(np.float32(float(m.group(2)))), float(np.float32(float(m.group(3)))))
+        # the first entry of a name, as HLCONST's search (hlconst.F:491-497)
+        table.setdefault(m.group(1).strip(), (float(np.float32(float(m.group(2)))), float(np.float32(float(m.group(3))))))
     chars = {m.group(1): m.group(2).strip() for m in
              re.finditer(r"CHARACTER\(\s*16\s*\),\s*SAVE\s*::\s*(\w+)\s*=\s*'([^']*)'", kmt_text)}
     out = []
