@@ -481,1547 +481,1029 @@ KQ_HD inline void kq_add_diagonal(double* g, double x, long long s)
     g[737 * s] = g[737 * s] + x;
 }
 
-KQ_HD KQ_NOINLINE void kqu_fun(const double* v, const double* f, const double* r, double* vdot, long long s)
+KQ_HD KQ_NOINLINE void kqu_fun_0(const double* v, const double* f, const double* r, double* vdot, long long s)
 {
-    const double a0 = r[0 * s] * v[99 * s];
-    const double a1 = r[1 * s] * v[85 * s];
-    const double a2 = r[2 * s] * v[86 * s];
-    const double a3 = r[3 * s] * v[87 * s];
-    const double a4 = r[4 * s] * v[84 * s];
-    const double a5 = r[5 * s] * v[88 * s];
-    const double a6 = r[6 * s] * v[89 * s];
-    const double a7 = r[7 * s] * v[90 * s];
-    const double a8 = r[8 * s] * v[91 * s];
-    const double a9 = r[9 * s] * v[92 * s];
-    const double a10 = r[10 * s] * v[93 * s];
-    const double a11 = r[11 * s] * v[94 * s];
-    const double a12 = r[12 * s] * v[81 * s];
-    const double a13 = r[13 * s] * v[95 * s];
-    const double a14 = r[14 * s] * v[73 * s];
-    const double a15 = r[15 * s] * v[96 * s];
-    const double a16 = r[16 * s] * v[144 * s];
-    const double a17 = r[17 * s] * v[106 * s];
-    const double a18 = r[18 * s] * v[124 * s];
-    const double a19 = r[19 * s] * v[107 * s];
-    const double a20 = r[20 * s] * v[145 * s];
-    const double a21 = r[21 * s] * v[157 * s];
-    const double a22 = r[22 * s] * v[141 * s];
-    const double a23 = r[23 * s] * v[120 * s];
-    const double a24 = r[24 * s] * v[121 * s];
-    const double a25 = r[25 * s] * v[110 * s];
-    const double a26 = r[26 * s] * v[105 * s];
-    const double a27 = r[27 * s] * v[112 * s];
-    const double a28 = r[28 * s] * v[154 * s];
-    const double a29 = r[29 * s] * v[158 * s];
-    const double a30 = r[30 * s] * v[125 * s];
-    const double a31 = r[31 * s] * v[149 * s];
-    const double a32 = r[32 * s] * v[0 * s];
-    const double a33 = r[33 * s] * v[1 * s];
-    const double a34 = r[34 * s] * v[2 * s];
-    const double a35 = r[35 * s] * v[3 * s];
-    const double a36 = r[36 * s] * v[4 * s];
-    const double a37 = r[37 * s] * v[5 * s];
-    const double a38 = r[38 * s] * v[6 * s];
-    const double a39 = r[39 * s] * v[7 * s];
-    const double a40 = r[40 * s] * v[144 * s];
-    const double a41 = r[41 * s] * v[156 * s];
-    const double a42 = r[42 * s] * v[106 * s];
-    const double a43 = r[43 * s] * v[124 * s];
-    const double a44 = r[44 * s] * v[114 * s];
-    const double a45 = r[45 * s] * v[107 * s];
-    const double a46 = r[46 * s] * v[141 * s];
-    const double a47 = r[47 * s] * v[110 * s];
-    const double a48 = r[48 * s] * f[0 * s];
-    const double a49 = r[49 * s] * v[109 * s];
-    const double a50 = r[50 * s] * v[123 * s];
-    const double a51 = r[51 * s] * v[154 * s];
-    const double a52 = r[52 * s] * v[125 * s];
-    const double a53 = r[53 * s] * v[149 * s];
-    const double a54 = r[54 * s] * v[155 * s] * v[156 * s];
-    const double a55 = r[55 * s] * v[155 * s] * v[159 * s];
-    const double a56 = r[56 * s] * v[146 * s] * v[155 * s];
-    const double a57 = r[57 * s] * v[114 * s] * v[155 * s];
-    const double a58 = r[58 * s] * v[113 * s] * v[155 * s];
-    const double a59 = r[59 * s] * v[108 * s] * v[152 * s];
-    const double a60 = r[60 * s] * v[137 * s] * v[155 * s];
-    const double a61 = r[61 * s] * v[111 * s] * v[155 * s];
-    const double a62 = r[62 * s] * v[152 * s] * v[155 * s];
-    const double a63 = r[63 * s] * v[123 * s] * v[155 * s];
-    const double a64 = r[64 * s] * v[153 * s] * v[155 * s];
-    const double a65 = r[65 * s] * v[150 * s] * v[155 * s];
-    const double a66 = r[66 * s] * v[151 * s] * v[155 * s];
-    const double a67 = r[67 * s] * v[129 * s] * v[155 * s];
-    const double a68 = r[68 * s] * v[145 * s] * v[155 * s] * v[156 * s];
-    const double a69 = r[69 * s] * v[144 * s] * v[157 * s];
-    const double a70 = r[70 * s] * v[156 * s] * v[157 * s];
-    const double a71 = r[71 * s] * v[157 * s] * v[159 * s];
-    const double a72 = r[72 * s] * v[13 * s] * v[144 * s];
-    const double a73 = r[73 * s] * v[13 * s] * v[156 * s];
-    const double a74 = r[74 * s] * v[13 * s] * v[159 * s];
-    const double a75 = r[75 * s] * v[12 * s] * v[144 * s];
-    const double a76 = r[76 * s] * v[12 * s] * v[156 * s];
-    const double a77 = r[77 * s] * v[12 * s] * v[159 * s];
-    const double a78 = r[78 * s] * v[12 * s] * v[13 * s] * v[144 * s];
-    const double a79 = r[79 * s] * v[12 * s] * v[13 * s] * v[156 * s];
-    const double a80 = r[80 * s] * v[12 * s] * v[13 * s] * v[159 * s];
-    const double a81 = r[81 * s] * v[120 * s] * v[155 * s] * v[156 * s];
-    const double a82 = r[82 * s] * v[121 * s] * v[155 * s] * v[156 * s];
-    const double a83 = r[83 * s] * v[121 * s] * v[156 * s];
-    const double a84 = r[84 * s] * v[154 * s] * v[154 * s];
-    const double a85 = r[85 * s] * v[150 * s] * v[154 * s];
-    const double a86 = r[86 * s] * v[150 * s] * v[157 * s];
-    const double a87 = r[87 * s] * v[144 * s] * v[158 * s];
-    const double a88 = r[88 * s] * v[156 * s] * v[158 * s];
-    const double a89 = r[89 * s] * v[158 * s] * v[159 * s];
-    const double a90 = r[90 * s] * v[149 * s] * v[156 * s];
-    const double a91 = r[91 * s] * v[129 * s];
-    const double a92 = r[92 * s] * v[151 * s] * v[157 * s];
-    const double a93 = r[93 * s] * v[151 * s] * v[160 * s];
-    const double a94 = r[94 * s] * v[125 * s] * v[160 * s];
-    const double a95 = r[95 * s] * v[144 * s];
-    const double a96 = r[96 * s] * v[106 * s];
-    const double a97 = r[97 * s] * v[124 * s];
-    const double a98 = r[98 * s] * v[107 * s];
-    const double a99 = r[99 * s] * v[145 * s];
-    const double a100 = r[100 * s] * v[157 * s];
-    const double a101 = r[101 * s] * v[141 * s];
-    const double a102 = r[102 * s] * v[120 * s];
-    const double a103 = r[103 * s] * v[121 * s];
-    const double a104 = r[104 * s] * v[109 * s];
-    const double a105 = r[105 * s] * v[110 * s];
-    const double a106 = r[106 * s] * v[105 * s];
-    const double a107 = r[107 * s] * v[112 * s];
-    const double a108 = r[108 * s] * v[153 * s];
-    const double a109 = r[109 * s] * v[146 * s];
-    const double a110 = r[110 * s] * v[108 * s];
-    const double a111 = r[111 * s] * v[111 * s];
-    const double a112 = r[112 * s] * v[8 * s];
-    const double a113 = r[113 * s] * v[9 * s];
-    const double a114 = r[114 * s] * v[10 * s];
-    const double a115 = r[115 * s] * v[11 * s];
-    const double a116 = r[116 * s] * v[14 * s];
-    const double a117 = r[117 * s] * v[15 * s];
-    const double a118 = r[118 * s] * v[16 * s];
-    const double a119 = r[119 * s] * v[17 * s];
-    const double a120 = r[120 * s] * v[12 * s];
-    const double a121 = r[121 * s] * v[13 * s];
-    const double a122 = r[122 * s] * v[155 * s];
-    const double a123 = r[123 * s] * v[152 * s];
-    const double a124 = r[124 * s] * v[156 * s];
-    const double a125 = r[125 * s] * v[159 * s];
-    const double a126 = r[126 * s] * v[114 * s];
-    const double a127 = r[127 * s] * v[113 * s];
-    const double a128 = r[128 * s] * v[137 * s];
-    const double a129 = r[129 * s] * v[123 * s];
-    const double a130 = r[130 * s] * v[150 * s];
-    const double a131 = r[131 * s] * v[154 * s];
-    const double a132 = r[132 * s] * v[158 * s];
-    const double a133 = r[133 * s] * v[125 * s];
-    const double a134 = r[134 * s] * v[151 * s];
-    const double a135 = r[135 * s] * v[129 * s];
-    const double a136 = r[136 * s] * v[149 * s];
-    const double a137 = r[137 * s] * f[1 * s];
-    const double a138 = r[138 * s] * v[160 * s];
-    const double a139 = r[139 * s] * v[160 * s];
-    const double a140 = r[140 * s] * v[100 * s];
-    const double a141 = r[141 * s] * v[74 * s];
-    const double a142 = r[142 * s] * v[76 * s];
-    const double a143 = r[143 * s] * v[115 * s];
-    const double a144 = r[144 * s] * v[75 * s];
-    const double a145 = r[145 * s] * v[77 * s];
-    const double a146 = r[146 * s] * v[115 * s] * f[0 * s];
-    const double a147 = r[147 * s] * v[115 * s] * v[153 * s];
-    const double a148 = r[148 * s] * v[101 * s] * v[115 * s];
-    const double a149 = r[149 * s] * v[102 * s] * v[115 * s];
-    const double a150 = r[150 * s] * v[115 * s] * f[0 * s];
-    const double a151 = r[151 * s] * v[115 * s] * v[153 * s];
-    const double a152 = r[152 * s] * v[115 * s] * v[146 * s];
-    const double a153 = r[153 * s] * v[75 * s] * f[0 * s];
-    const double a154 = r[154 * s] * v[75 * s] * v[153 * s];
-    const double a155 = r[155 * s] * v[77 * s] * f[0 * s];
-    const double a156 = r[156 * s] * v[77 * s] * v[153 * s];
-    const double a157 = r[157 * s] * v[115 * s];
-    const double a158 = r[158 * s] * v[101 * s];
-    const double a159 = r[159 * s] * v[102 * s];
-    const double a160 = r[160 * s] * v[55 * s];
-    const double a161 = r[161 * s] * v[75 * s];
-    const double a162 = r[162 * s] * v[77 * s];
-    const double a163 = r[163 * s] * v[59 * s];
-    const double a164 = r[164 * s] * v[61 * s];
-    const double a165 = r[165 * s] * v[52 * s];
-    const double a166 = r[166 * s] * v[78 * s];
-    const double a167 = r[167 * s] * v[79 * s];
-    const double a168 = r[168 * s] * v[80 * s];
-    const double a169 = r[169 * s] * v[83 * s];
-    const double a170 = r[170 * s] * v[82 * s];
-    const double a171 = r[171 * s] * v[104 * s];
-    const double a172 = r[172 * s] * v[134 * s];
-    const double a173 = r[173 * s] * v[143 * s];
-    const double a174 = r[174 * s] * v[118 * s];
-    const double a175 = r[175 * s] * v[133 * s];
-    const double a176 = r[176 * s] * v[136 * s];
-    const double a177 = r[177 * s] * v[128 * s];
-    const double a178 = r[178 * s] * v[131 * s];
-    const double a179 = r[179 * s] * v[133 * s];
-    const double a180 = r[180 * s] * v[138 * s];
-    const double a181 = r[181 * s] * v[134 * s];
-    const double a182 = r[182 * s] * v[140 * s] * v[155 * s];
-    const double a183 = r[183 * s] * v[131 * s] * v[155 * s];
-    const double a184 = r[184 * s] * v[130 * s] * v[155 * s];
-    const double a185 = r[185 * s] * v[132 * s] * v[155 * s];
-    const double a186 = r[186 * s] * v[139 * s] * v[155 * s];
-    const double a187 = r[187 * s] * v[135 * s] * v[155 * s];
-    const double a188 = r[188 * s] * v[143 * s] * f[0 * s];
-    const double a189 = r[189 * s] * v[148 * s];
-    const double a190 = r[190 * s] * v[118 * s] * f[0 * s];
-    const double a191 = r[191 * s] * v[116 * s];
-    const double a192 = r[192 * s] * v[145 * s];
-    const double a193 = r[193 * s] * v[104 * s] * v[160 * s];
-    const double a194 = r[194 * s] * v[104 * s] * v[160 * s];
-    const double a195 = r[195 * s] * v[138 * s] * v[160 * s];
-    const double a196 = r[196 * s] * v[139 * s] * v[160 * s];
-    const double a197 = r[197 * s] * v[105 * s] * v[160 * s];
-    const double a198 = r[198 * s] * v[136 * s] * v[160 * s];
-    const double a199 = r[199 * s] * v[140 * s] * v[160 * s];
-    const double a200 = r[200 * s] * v[128 * s] * v[160 * s];
-    const double a201 = r[201 * s] * v[131 * s] * v[160 * s];
-    const double a202 = r[202 * s] * v[130 * s] * v[160 * s];
-    const double a203 = r[203 * s] * v[112 * s] * v[160 * s];
-    const double a204 = r[204 * s] * v[133 * s] * v[160 * s];
-    const double a205 = r[205 * s] * v[132 * s] * v[160 * s];
-    const double a206 = r[206 * s] * v[134 * s] * v[160 * s];
-    const double a207 = r[207 * s] * v[135 * s] * v[160 * s];
-    const double a208 = r[208 * s] * v[148 * s] * v[160 * s];
-    const double a209 = r[209 * s] * v[141 * s] * v[160 * s];
-    const double a210 = r[210 * s] * v[116 * s] * v[160 * s];
-    const double a211 = r[211 * s] * v[136 * s];
-    const double a212 = r[212 * s] * v[140 * s];
-    const double a213 = r[213 * s] * v[128 * s];
-    const double a214 = r[214 * s] * v[131 * s];
-    const double a215 = r[215 * s] * v[130 * s];
-    const double a216 = r[216 * s] * v[133 * s];
-    const double a217 = r[217 * s] * v[132 * s];
-    const double a218 = r[218 * s] * v[134 * s];
-    const double a219 = r[219 * s] * v[135 * s];
-    const double a220 = r[220 * s] * v[148 * s];
-    const double a221 = r[221 * s] * v[104 * s];
-    const double a222 = r[222 * s] * v[138 * s];
-    const double a223 = r[223 * s] * v[139 * s];
-    const double a224 = r[224 * s] * v[143 * s];
-    const double a225 = r[225 * s] * v[118 * s];
-    const double a226 = r[226 * s] * v[116 * s];
-    const double a227 = r[227 * s] * v[97 * s];
-    const double a228 = r[228 * s] * v[98 * s];
-    const double a229 = r[229 * s] * v[126 * s];
-    const double a230 = r[230 * s] * v[119 * s];
-    const double a231 = r[231 * s] * v[146 * s];
-    const double a232 = r[232 * s] * v[160 * s] * v[160 * s];
-    const double a233 = r[233 * s] * v[154 * s] * v[160 * s];
-    const double a234 = r[234 * s] * v[150 * s] * v[160 * s];
-    const double a235 = r[235 * s] * v[145 * s] * v[160 * s];
-    const double a236 = r[236 * s] * v[156 * s] * v[160 * s];
-    const double a237 = r[237 * s] * v[154 * s] * v[158 * s];
-    const double a238 = r[238 * s] * v[150 * s] * v[158 * s];
-    const double a239 = r[239 * s] * v[149 * s];
-    const double a240 = r[240 * s] * v[126 * s] * v[153 * s];
-    const double a241 = r[241 * s] * v[126 * s] * v[156 * s];
-    const double a242 = r[242 * s] * v[103 * s] * f[2 * s];
-    const double a243 = r[243 * s] * v[142 * s] * v[154 * s];
-    const double a244 = r[244 * s] * v[142 * s] * v[142 * s];
-    const double a245 = r[245 * s] * v[127 * s] * v[155 * s] * v[156 * s];
-    const double a246 = r[246 * s] * v[122 * s] * f[0 * s];
-    const double a247 = r[247 * s] * v[119 * s] * v[119 * s];
-    const double a248 = r[248 * s] * v[119 * s] * v[156 * s];
-    const double a249 = r[249 * s] * v[137 * s] * v[160 * s];
-    const double a250 = r[250 * s] * v[143 * s] * v[156 * s];
-    const double a251 = r[251 * s] * v[143 * s] * v[159 * s];
-    const double a252 = r[252 * s] * v[147 * s];
-    const double a253 = r[253 * s] * v[147 * s] * v[152 * s];
-    const double a254 = r[254 * s] * v[147 * s] * v[160 * s];
-    const double a255 = r[255 * s] * v[118 * s] * v[156 * s];
-    const double a256 = r[256 * s] * v[118 * s] * v[159 * s];
-    const double a257 = r[257 * s] * v[117 * s];
-    const double a258 = r[258 * s] * v[117 * s] * v[152 * s];
-    const double a259 = r[259 * s] * v[117 * s] * v[160 * s];
-    const double a260 = r[260 * s] * v[126 * s];
-    const double a261 = r[261 * s] * v[119 * s];
-    const double a262 = r[262 * s] * v[122 * s];
-    const double a263 = r[263 * s] * v[103 * s];
-    const double a264 = r[264 * s] * v[147 * s];
-    const double a265 = r[265 * s] * v[142 * s];
-    const double a266 = r[266 * s] * v[127 * s];
-    const double a267 = r[267 * s] * v[21 * s];
-    const double a268 = r[268 * s] * v[117 * s];
-    vdot[0 * s] = 0.0 - a32;
-    vdot[1 * s] = 0.0 - a33;
-    vdot[2 * s] = 0.0 - a34;
-    vdot[3 * s] = 0.0 - a35;
-    vdot[4 * s] = 0.0 - a36;
-    vdot[5 * s] = 0.0 - a37;
-    vdot[6 * s] = 0.0 - a38;
-    vdot[7 * s] = 0.0 - a39;
-    vdot[8 * s] = 0.0 + a39 - a112;
-    vdot[9 * s] = 0.0 + a37 - a113;
-    vdot[10 * s] = 0.0 - a114;
-    vdot[11 * s] = 0.0 + a38 - a115;
-    vdot[12 * s] = 0.0 - a120;
-    vdot[13 * s] = 0.0 - a121;
-    vdot[14 * s] = 0.0 - a116;
-    vdot[15 * s] = 0.0 - a117;
-    vdot[16 * s] = 0.0 - a118;
-    vdot[17 * s] = 0.0 + a35 - a119;
-    vdot[18 * s] = 0.0 + a95 + a124 + a125 + a262 + a263 + a264 + a265 + a266;
-    vdot[19 * s] = 0.0 + a96;
-    vdot[20 * s] = 0.0 + a97 + a126 + a127 + a267;
-    vdot[21 * s] = 0.0 + a201 + a202 - a267;
-    vdot[22 * s] = 0.0 + a98;
-    vdot[23 * s] = 0.0 + a99;
-    vdot[24 * s] = 0.0 + a100;
-    vdot[25 * s] = 0.0 + a101 + a128;
-    vdot[26 * s] = 0.0 + a102;
-    vdot[27 * s] = 0.0 + a103;
-    vdot[28 * s] = 0.0 + a104 + a108 + a129;
-    vdot[29 * s] = 0.0 + a105;
-    vdot[30 * s] = 0.0 + a106;
-    vdot[31 * s] = 0.0 + a107;
-    vdot[32 * s] = 0.0 + a139;
-    vdot[33 * s] = 0.0 + a109;
-    vdot[34 * s] = 0.0 + a110;
-    vdot[35 * s] = 0.0 + a111;
-    vdot[36 * s] = 0.0 + a112;
-    vdot[37 * s] = 0.0 + a120;
-    vdot[38 * s] = 0.0 + a121;
-    vdot[39 * s] = 0.0 + a113;
-    vdot[40 * s] = 0.0 + a114;
-    vdot[41 * s] = 0.0 + a115;
-    vdot[42 * s] = 0.0 + a122;
-    vdot[43 * s] = 0.0 + a116;
-    vdot[44 * s] = 0.0 + a117;
-    vdot[45 * s] = 0.0 + a118;
-    vdot[46 * s] = 0.0 + a119;
-    vdot[47 * s] = 0.0 + a132;
-    vdot[48 * s] = 0.0 + a133 + a134;
-    vdot[49 * s] = 0.0 + a135 + a136;
-    vdot[50 * s] = 0.0 + a157;
-    vdot[51 * s] = 0.0 + a158 + a165;
-    vdot[52 * s] = 0.0 + a150 + a151 + a152 - a165;
-    vdot[53 * s] = 0.0 + a159;
-    vdot[54 * s] = 0.0 + a160;
-    vdot[55 * s] = 0.0 + a148 + a149 - a160;
-    vdot[56 * s] = 0.0 + a161;
-    vdot[57 * s] = 0.0 + a162;
-    vdot[58 * s] = 0.0 + a163;
-    vdot[59 * s] = 0.0 + a153 + a155 - a163;
-    vdot[60 * s] = 0.0 + a164;
-    vdot[61 * s] = 0.0 + a154 + a156 - a164;
-    vdot[62 * s] = 0.0 + a211 + a212;
-    vdot[63 * s] = 0.0 + a213 + a214 + a215;
-    vdot[64 * s] = 0.0 + a216 + a217;
-    vdot[65 * s] = 0.0 + a218 + a219;
-    vdot[66 * s] = 0.0 + a220 + a224 + a264;
-    vdot[67 * s] = 0.0 + a130 + a131;
-    vdot[68 * s] = 0.0 + a221;
-    vdot[69 * s] = 0.0 + a222 + a223;
-    vdot[70 * s] = 0.0 + a225 + a226 + a268;
-    vdot[71 * s] = 0.0 + a260;
-    vdot[72 * s] = 0.0 + a261;
-    vdot[73 * s] = 0.0 - a14 + a30;
-    vdot[74 * s] = 0.0 - a141 + a144;
-    vdot[75 * s] = 0.0 + a141 - a144 - a153 - a154 - a161;
-    vdot[76 * s] = 0.0 - a142 + a145;
-    vdot[77 * s] = 0.0 + a142 - a145 - a155 - a156 - a162;
-    vdot[78 * s] = 0.0 - a166 + a171;
-    vdot[79 * s] = 0.0 - a167 + a172;
-    vdot[80 * s] = 0.0 - a168 + a173;
-    vdot[81 * s] = 0.0 - a12 + a28;
-    vdot[82 * s] = 0.0 - a170 + a175;
-    vdot[83 * s] = 0.0 - a169 + a174;
-    vdot[84 * s] = 0.0 - a4 + a20;
-    vdot[85 * s] = 0.0 - a1 + a17;
-    vdot[86 * s] = 0.0 - a2 + a18;
-    vdot[87 * s] = 0.0 - a3 + a19;
-    vdot[88 * s] = 0.0 - a5 + a21;
-    vdot[89 * s] = 0.0 - a6 + a22;
-    vdot[90 * s] = 0.0 - a7 + a23;
-    vdot[91 * s] = 0.0 - a8 + a24;
-    vdot[92 * s] = 0.0 - a9 + a25;
-    vdot[93 * s] = 0.0 - a10 + a26;
-    vdot[94 * s] = 0.0 - a11 + a27;
-    vdot[95 * s] = 0.0 - a13 + a29;
-    vdot[96 * s] = 0.0 - a15 + a31;
-    vdot[97 * s] = 0.0 - a227 + a229;
-    vdot[98 * s] = 0.0 - a228 + a230;
-    vdot[99 * s] = 0.0 - a0 + a16;
-    vdot[100 * s] = 0.0 - a140 + a143;
-    vdot[101 * s] = 0.0 + a146 - a148 - a158;
-    vdot[102 * s] = 0.0 + a147 - a149 - a159;
-    vdot[103 * s] = 0.0 + a236 + a241 - a242 + a248 - a263;
-    vdot[104 * s] = 0.0 + a166 - a171 - a193 - a194 - a221;
-    vdot[105 * s] = 0.0 + a10 - a26 - a106 + a194 - a197;
-    vdot[106 * s] = 0.0 + a1 - a17 - a42 + a56 - a96;
-    vdot[107 * s] = 0.0 + a3 - a19 - a45 + a59 - a98;
-    vdot[108 * s] = 0.0 + a33 + a45 - a59 - a110;
-    vdot[109 * s] = 0.0 - a49 + a63 - a104;
-    vdot[110 * s] = 0.0 + a9 - a25 - a47 + a61 - a105;
-    vdot[111 * s] = 0.0 + a34 + a47 - a61 - a111;
-    vdot[112 * s] = 0.0 + a11 - a27 - a107 - a203;
-    vdot[113 * s] = 0.0 + a44 - a58 - a127;
-    vdot[114 * s] = 0.0 + a43 - a44 - a57 + a58 - a126;
-    vdot[115 * s] = 0.0 + a140 - a143 - a146 - a147 - a148 - a149 - a150 - a151 - a152 - a157;
-    vdot[116 * s] = 0.0 + a190 - a191 - a210 - a226 + a258;
-    vdot[117 * s] = 0.0 + a255 + a256 - a257 - a258 - a259 - a268;
-    vdot[118 * s] = 0.0 + a169 - a174 - a190 + a191 - a225 - a255 - a256 + a257;
-    vdot[119 * s] = 0.0 + a228 - a230 + -0x1.0000000000000p+1 * a247 - a248 - a261;
-    vdot[120 * s] = 0.0 + a7 - a23 - a81 - a102 + a248;
-    vdot[121 * s] = 0.0 + a8 - a24 - a82 - a83 - a103;
-    vdot[122 * s] = 0.0 + a240 + 0x1.0000000000000p+1 * a244 - a246 - a262;
-    vdot[123 * s] = 0.0 + a49 - a50 - a63 + a64 - a129 + a246;
-    vdot[124 * s] = 0.0 + a2 - a18 - a43 + a57 - a97 + 0x1.0000000000000p+1 * a200 + a201 + a202 + a204 + a205 + a209 + a249;
-    vdot[125 * s] = 0.0 + a14 - a30 - a52 + a66 - a94 - a133;
-    vdot[126 * s] = 0.0 + a227 - a229 - a240 - a241 - a260;
-    vdot[127 * s] = 0.0 + a243 - a245 - a266;
-    vdot[128 * s] = 0.0 - a177 + a183 + a198 - a200 - a213;
-    vdot[129 * s] = 0.0 + a53 - a67 - a91 - a135 + a238;
-    vdot[130 * s] = 0.0 + a178 - a184 - a202 - a215;
-    vdot[131 * s] = 0.0 + a177 - a178 - a183 + a184 + a199 - a201 - a214;
-    vdot[132 * s] = 0.0 + a179 - a185 + 0x1.d70a3e0000000p-1 * a203 - a205 - a217;
-    vdot[133 * s] = 0.0 + a170 - a175 - a179 + a185 - a204 - a216;
-    vdot[134 * s] = 0.0 + a167 - a172 - a181 + a187 + a204 - a206 - a218;
-    vdot[135 * s] = 0.0 + a181 - a187 + a205 - a207 - a219;
-    vdot[136 * s] = 0.0 - a176 + a182 + a197 - a198 + 0x1.b333340000000p-1 * a206 - a211;
-    vdot[137 * s] = 0.0 + a46 - a60 - a128 - a249;
-    vdot[138 * s] = 0.0 - a180 + a186 + a193 - a195 - a222;
-    vdot[139 * s] = 0.0 + a180 - a186 - a196 - a223;
-    vdot[140 * s] = 0.0 + a176 - a182 + a195 + a196 - a199 + 0x1.47ae140000000p-4 * a203 + 0x1.b333340000000p-1 * a207 - a212;
-    vdot[141 * s] = 0.0 + a6 - a22 - a46 + a60 - a101 + a208 - a209 + a254;
-    vdot[142 * s] = 0.0 + a242 - a243 + -0x1.0000000000000p+1 * a244 - a265;
-    vdot[143 * s] = 0.0 + a168 - a173 - a188 + a189 - a224 + 0x1.0000000000000p+1 * a247 - a250 - a251 + a252;
-    vdot[144 * s] = 0.0 + a0 - a16 - a40 + a54 - a69 - a72 - a75 - a78 - a87 - a95;
-    vdot[145 * s] = 0.0 + a4 - a20 - a68 + a84 + a85 - a99 - a192 + a232 - a235;
-    vdot[146 * s] = 0.0 + a32 + a42 - a56 + a90 + a92 - a109 - a152 - a231 + a240 + a241;
-    vdot[147 * s] = 0.0 + a250 + a251 - a252 - a253 - a254 - a264;
-    vdot[148 * s] = 0.0 + a188 - a189 + 0x1.3333340000000p-3 * a206 + 0x1.3333340000000p-3 * a207 - a208 - a220 + a253;
-    vdot[149 * s] = 0.0 + a15 - a31 - a53 + a67 - a90 - a136 + a237 - a239;
-    vdot[150 * s] = 0.0 + a51 - a65 - a85 - a86 - a130 - a234 - a238;
-    vdot[151 * s] = 0.0 + a52 - a66 + 0x1.0000000000000p+1 * a87 + 0x1.0000000000000p+1 * a88 + 0x1.0000000000000p+1 * a89 + a91 - a92 - a93 - a134;
-    vdot[152 * s] = 0.0 + a45 + a48 - a59 - a62 + a85 + a86 + a93 - a123 + a202 + a231 + a234 + a249 + a251 - a253;
-    vdot[153 * s] = 0.0 + a36 + a50 - a64 + a68 + a69 + a70 + a71 + a72 + a73 + a74 + a75 + a76 + a77 + a78 + a79 + a80 + a81 + a82 + a83 + a87 + a88 + a89 + a90 - a108 - a147 - a151 - a154 - a156 - a240 + 0x1.0000000000000p+1 * a245;
-    vdot[154 * s] = 0.0 + a12 - a28 - a51 + a65 + -0x1.0000000000000p+1 * a84 - a85 - a131 + a193 + a194 + a195 + a196 + a197 + a198 + a199 + a203 + a204 + a205 + a208 + a209 - a233 + a235 - a237 + a239 - a243 + 0x1.0000000000000p+1 * a247 + a249 + a254;
-    vdot[155 * s] = 0.0 + a40 + a41 + a42 + a43 + a44 + a46 + a47 + a48 + a49 + a50 + a51 + a52 + a53 - a54 - a55 - a56 - a57 - a58 - a60 - a61 - a62 - a63 - a64 - a65 - a66 - a67 + a68 + 0x1.0000000000000p+1 * a69 + a70 + 0x1.0000000000000p+1 * a72 + a73 + 0x1.0000000000000p+1 * a75 + a76 + 0x1.0000000000000p+1 * a78 + a79 + a81 + a82 + a83 + 0x1.0000000000000p+2 * a87 + 0x1.8000000000000p+1 * a88 + 0x1.0000000000000p+1 * a89 + 0x1.0000000000000p+1 * a90 - a122 + a176 + a177 + a178 + a179 + a180 + a181 - a182 - a183 - a184 - a185 - a186 - a187 + a195 + a241 + 0x1.0000000000000p+1 * a245;
-    vdot[156 * s] = 0.0 + a40 - a41 - a54 + a55 - a68 - a70 - a73 - a76 - a79 - a81 - a82 - a83 - a88 - a90 - a124 - a236 - a241 - a245 - a248 - a250 + a252 + a254;
-    vdot[157 * s] = 0.0 + a5 - a21 - a69 - a70 - a71 - a86 - a92 - a100;
-    vdot[158 * s] = 0.0 + a13 - a29 + -0x1.0000000000000p+1 * a87 + -0x1.0000000000000p+1 * a88 + -0x1.0000000000000p+1 * a89 + a93 + a94 - a132 + a231 - a237 - a238 + a239;
-    vdot[159 * s] = 0.0 + a41 - a55 - a71 - a74 - a77 - a80 - a89 - a125 - a251 + a253;
-    vdot[160 * s] = 0.0 + a86 - a93 - a94 + a137 - a138 - a139 + 0x1.0000000000000p+1 * a192 - a193 - a194 - a195 - a196 - a197 - a198 - a199 + -0x1.0000000000000p+1 * a200 - a201 - a202 - a203 - a204 - a205 - a206 - a207 - a208 - a209 + a231 + -0x1.0000000000000p+1 * a232 - a233 - a234 - a235 - a236 + a246 - a249 - a254;
+    vdot[0 * s] = 0.0 - (r[32 * s] * v[0 * s]);
+    vdot[1 * s] = 0.0 - (r[33 * s] * v[1 * s]);
+    vdot[2 * s] = 0.0 - (r[34 * s] * v[2 * s]);
+    vdot[3 * s] = 0.0 - (r[35 * s] * v[3 * s]);
+    vdot[4 * s] = 0.0 - (r[36 * s] * v[4 * s]);
+    vdot[5 * s] = 0.0 - (r[37 * s] * v[5 * s]);
+    vdot[6 * s] = 0.0 - (r[38 * s] * v[6 * s]);
+    vdot[7 * s] = 0.0 - (r[39 * s] * v[7 * s]);
+    vdot[8 * s] = 0.0 + (r[39 * s] * v[7 * s]) - (r[112 * s] * v[8 * s]);
+    vdot[9 * s] = 0.0 + (r[37 * s] * v[5 * s]) - (r[113 * s] * v[9 * s]);
+    vdot[10 * s] = 0.0 - (r[114 * s] * v[10 * s]);
+    vdot[11 * s] = 0.0 + (r[38 * s] * v[6 * s]) - (r[115 * s] * v[11 * s]);
+    vdot[12 * s] = 0.0 - (r[120 * s] * v[12 * s]);
+    vdot[13 * s] = 0.0 - (r[121 * s] * v[13 * s]);
+    vdot[14 * s] = 0.0 - (r[116 * s] * v[14 * s]);
+    vdot[15 * s] = 0.0 - (r[117 * s] * v[15 * s]);
+    vdot[16 * s] = 0.0 - (r[118 * s] * v[16 * s]);
+    vdot[17 * s] = 0.0 + (r[35 * s] * v[3 * s]) - (r[119 * s] * v[17 * s]);
+    vdot[18 * s] = 0.0 + (r[95 * s] * v[144 * s]) + (r[124 * s] * v[156 * s]) + (r[125 * s] * v[159 * s]) + (r[262 * s] * v[122 * s]) + (r[263 * s] * v[103 * s]) + (r[264 * s] * v[147 * s]) + (r[265 * s] * v[142 * s]) + (r[266 * s] * v[127 * s]);
+    vdot[19 * s] = 0.0 + (r[96 * s] * v[106 * s]);
+    vdot[20 * s] = 0.0 + (r[97 * s] * v[124 * s]) + (r[126 * s] * v[114 * s]) + (r[127 * s] * v[113 * s]) + (r[267 * s] * v[21 * s]);
+    vdot[21 * s] = 0.0 + (r[201 * s] * v[131 * s] * v[160 * s]) + (r[202 * s] * v[130 * s] * v[160 * s]) - (r[267 * s] * v[21 * s]);
+    vdot[22 * s] = 0.0 + (r[98 * s] * v[107 * s]);
+    vdot[23 * s] = 0.0 + (r[99 * s] * v[145 * s]);
+    vdot[24 * s] = 0.0 + (r[100 * s] * v[157 * s]);
+    vdot[25 * s] = 0.0 + (r[101 * s] * v[141 * s]) + (r[128 * s] * v[137 * s]);
+    vdot[26 * s] = 0.0 + (r[102 * s] * v[120 * s]);
+    vdot[27 * s] = 0.0 + (r[103 * s] * v[121 * s]);
+    vdot[28 * s] = 0.0 + (r[104 * s] * v[109 * s]) + (r[108 * s] * v[153 * s]) + (r[129 * s] * v[123 * s]);
+    vdot[29 * s] = 0.0 + (r[105 * s] * v[110 * s]);
+    vdot[30 * s] = 0.0 + (r[106 * s] * v[105 * s]);
+    vdot[31 * s] = 0.0 + (r[107 * s] * v[112 * s]);
+    vdot[32 * s] = 0.0 + (r[139 * s] * v[160 * s]);
+    vdot[33 * s] = 0.0 + (r[109 * s] * v[146 * s]);
+    vdot[34 * s] = 0.0 + (r[110 * s] * v[108 * s]);
+    vdot[35 * s] = 0.0 + (r[111 * s] * v[111 * s]);
+    vdot[36 * s] = 0.0 + (r[112 * s] * v[8 * s]);
+    vdot[37 * s] = 0.0 + (r[120 * s] * v[12 * s]);
+    vdot[38 * s] = 0.0 + (r[121 * s] * v[13 * s]);
+    vdot[39 * s] = 0.0 + (r[113 * s] * v[9 * s]);
+    vdot[40 * s] = 0.0 + (r[114 * s] * v[10 * s]);
+    vdot[41 * s] = 0.0 + (r[115 * s] * v[11 * s]);
+    vdot[42 * s] = 0.0 + (r[122 * s] * v[155 * s]);
+    vdot[43 * s] = 0.0 + (r[116 * s] * v[14 * s]);
+    vdot[44 * s] = 0.0 + (r[117 * s] * v[15 * s]);
+    vdot[45 * s] = 0.0 + (r[118 * s] * v[16 * s]);
+    vdot[46 * s] = 0.0 + (r[119 * s] * v[17 * s]);
+    vdot[47 * s] = 0.0 + (r[132 * s] * v[158 * s]);
+    vdot[48 * s] = 0.0 + (r[133 * s] * v[125 * s]) + (r[134 * s] * v[151 * s]);
+    vdot[49 * s] = 0.0 + (r[135 * s] * v[129 * s]) + (r[136 * s] * v[149 * s]);
+    vdot[50 * s] = 0.0 + (r[157 * s] * v[115 * s]);
+    vdot[51 * s] = 0.0 + (r[158 * s] * v[101 * s]) + (r[165 * s] * v[52 * s]);
+    vdot[52 * s] = 0.0 + (r[150 * s] * v[115 * s] * f[0 * s]) + (r[151 * s] * v[115 * s] * v[153 * s]) + (r[152 * s] * v[115 * s] * v[146 * s]) - (r[165 * s] * v[52 * s]);
+    vdot[53 * s] = 0.0 + (r[159 * s] * v[102 * s]);
+    vdot[54 * s] = 0.0 + (r[160 * s] * v[55 * s]);
+    vdot[55 * s] = 0.0 + (r[148 * s] * v[101 * s] * v[115 * s]) + (r[149 * s] * v[102 * s] * v[115 * s]) - (r[160 * s] * v[55 * s]);
+    vdot[56 * s] = 0.0 + (r[161 * s] * v[75 * s]);
+    vdot[57 * s] = 0.0 + (r[162 * s] * v[77 * s]);
+    vdot[58 * s] = 0.0 + (r[163 * s] * v[59 * s]);
+    vdot[59 * s] = 0.0 + (r[153 * s] * v[75 * s] * f[0 * s]) + (r[155 * s] * v[77 * s] * f[0 * s]) - (r[163 * s] * v[59 * s]);
+    vdot[60 * s] = 0.0 + (r[164 * s] * v[61 * s]);
+    vdot[61 * s] = 0.0 + (r[154 * s] * v[75 * s] * v[153 * s]) + (r[156 * s] * v[77 * s] * v[153 * s]) - (r[164 * s] * v[61 * s]);
 }
 
-KQ_HD KQ_NOINLINE void kqu_jac(const double* v, const double* f, const double* r, double* jvs, long long s)
+KQ_HD KQ_NOINLINE void kqu_fun_1(const double* v, const double* f, const double* r, double* vdot, long long s)
 {
-    const double b0 = r[0 * s];
-    const double b1 = r[1 * s];
-    const double b2 = r[2 * s];
-    const double b3 = r[3 * s];
-    const double b4 = r[4 * s];
-    const double b5 = r[5 * s];
-    const double b6 = r[6 * s];
-    const double b7 = r[7 * s];
-    const double b8 = r[8 * s];
-    const double b9 = r[9 * s];
-    const double b10 = r[10 * s];
-    const double b11 = r[11 * s];
-    const double b12 = r[12 * s];
-    const double b13 = r[13 * s];
-    const double b14 = r[14 * s];
-    const double b15 = r[15 * s];
-    const double b16 = r[16 * s];
-    const double b17 = r[17 * s];
-    const double b18 = r[18 * s];
-    const double b19 = r[19 * s];
-    const double b20 = r[20 * s];
-    const double b21 = r[21 * s];
-    const double b22 = r[22 * s];
-    const double b23 = r[23 * s];
-    const double b24 = r[24 * s];
-    const double b25 = r[25 * s];
-    const double b26 = r[26 * s];
-    const double b27 = r[27 * s];
-    const double b28 = r[28 * s];
-    const double b29 = r[29 * s];
-    const double b30 = r[30 * s];
-    const double b31 = r[31 * s];
-    const double b32 = r[32 * s];
-    const double b33 = r[33 * s];
-    const double b34 = r[34 * s];
-    const double b35 = r[35 * s];
-    const double b36 = r[36 * s];
-    const double b37 = r[37 * s];
-    const double b38 = r[38 * s];
-    const double b39 = r[39 * s];
-    const double b40 = r[40 * s];
-    const double b41 = r[41 * s];
-    const double b42 = r[42 * s];
-    const double b43 = r[43 * s];
-    const double b44 = r[44 * s];
-    const double b45 = r[45 * s];
-    const double b46 = r[46 * s];
-    const double b47 = r[47 * s];
-    const double b48 = r[49 * s];
-    const double b49 = r[50 * s];
-    const double b50 = r[51 * s];
-    const double b51 = r[52 * s];
-    const double b52 = r[53 * s];
-    const double b53 = r[54 * s] * v[156 * s];
-    const double b54 = r[54 * s] * v[155 * s];
-    const double b55 = r[55 * s] * v[159 * s];
-    const double b56 = r[55 * s] * v[155 * s];
-    const double b57 = r[56 * s] * v[155 * s];
-    const double b58 = r[56 * s] * v[146 * s];
-    const double b59 = r[57 * s] * v[155 * s];
-    const double b60 = r[57 * s] * v[114 * s];
-    const double b61 = r[58 * s] * v[155 * s];
-    const double b62 = r[58 * s] * v[113 * s];
-    const double b63 = r[59 * s] * v[152 * s];
-    const double b64 = r[59 * s] * v[108 * s];
-    const double b65 = r[60 * s] * v[155 * s];
-    const double b66 = r[60 * s] * v[137 * s];
-    const double b67 = r[61 * s] * v[155 * s];
-    const double b68 = r[61 * s] * v[111 * s];
-    const double b69 = r[62 * s] * v[155 * s];
-    const double b70 = r[62 * s] * v[152 * s];
-    const double b71 = r[63 * s] * v[155 * s];
-    const double b72 = r[63 * s] * v[123 * s];
-    const double b73 = r[64 * s] * v[155 * s];
-    const double b74 = r[64 * s] * v[153 * s];
-    const double b75 = r[65 * s] * v[155 * s];
-    const double b76 = r[65 * s] * v[150 * s];
-    const double b77 = r[66 * s] * v[155 * s];
-    const double b78 = r[66 * s] * v[151 * s];
-    const double b79 = r[67 * s] * v[155 * s];
-    const double b80 = r[67 * s] * v[129 * s];
-    const double b81 = r[68 * s] * v[155 * s] * v[156 * s];
-    const double b82 = r[68 * s] * v[145 * s] * v[156 * s];
-    const double b83 = r[68 * s] * v[145 * s] * v[155 * s];
-    const double b84 = r[69 * s] * v[157 * s];
-    const double b85 = r[69 * s] * v[144 * s];
-    const double b86 = r[70 * s] * v[157 * s];
-    const double b87 = r[70 * s] * v[156 * s];
-    const double b88 = r[71 * s] * v[159 * s];
-    const double b89 = r[71 * s] * v[157 * s];
-    const double b90 = r[72 * s] * v[144 * s];
-    const double b91 = r[72 * s] * v[13 * s];
-    const double b92 = r[73 * s] * v[156 * s];
-    const double b93 = r[73 * s] * v[13 * s];
-    const double b94 = r[74 * s] * v[159 * s];
-    const double b95 = r[74 * s] * v[13 * s];
-    const double b96 = r[75 * s] * v[144 * s];
-    const double b97 = r[75 * s] * v[12 * s];
-    const double b98 = r[76 * s] * v[156 * s];
-    const double b99 = r[76 * s] * v[12 * s];
-    const double b100 = r[77 * s] * v[159 * s];
-    const double b101 = r[77 * s] * v[12 * s];
-    const double b102 = r[78 * s] * v[13 * s] * v[144 * s];
-    const double b103 = r[78 * s] * v[12 * s] * v[144 * s];
-    const double b104 = r[78 * s] * v[12 * s] * v[13 * s];
-    const double b105 = r[79 * s] * v[13 * s] * v[156 * s];
-    const double b106 = r[79 * s] * v[12 * s] * v[156 * s];
-    const double b107 = r[79 * s] * v[12 * s] * v[13 * s];
-    const double b108 = r[80 * s] * v[13 * s] * v[159 * s];
-    const double b109 = r[80 * s] * v[12 * s] * v[159 * s];
-    const double b110 = r[80 * s] * v[12 * s] * v[13 * s];
-    const double b111 = r[81 * s] * v[155 * s] * v[156 * s];
-    const double b112 = r[81 * s] * v[120 * s] * v[156 * s];
-    const double b113 = r[81 * s] * v[120 * s] * v[155 * s];
-    const double b114 = r[82 * s] * v[155 * s] * v[156 * s];
-    const double b115 = r[82 * s] * v[121 * s] * v[156 * s];
-    const double b116 = r[82 * s] * v[121 * s] * v[155 * s];
-    const double b117 = r[83 * s] * v[156 * s];
-    const double b118 = r[83 * s] * v[121 * s];
-    const double b119 = r[84 * s] * 0x1.0000000000000p+1 * v[154 * s];
-    const double b120 = r[85 * s] * v[154 * s];
-    const double b121 = r[85 * s] * v[150 * s];
-    const double b122 = r[86 * s] * v[157 * s];
-    const double b123 = r[86 * s] * v[150 * s];
-    const double b124 = r[87 * s] * v[158 * s];
-    const double b125 = r[87 * s] * v[144 * s];
-    const double b126 = r[88 * s] * v[158 * s];
-    const double b127 = r[88 * s] * v[156 * s];
-    const double b128 = r[89 * s] * v[159 * s];
-    const double b129 = r[89 * s] * v[158 * s];
-    const double b130 = r[90 * s] * v[156 * s];
-    const double b131 = r[90 * s] * v[149 * s];
-    const double b132 = r[91 * s];
-    const double b133 = r[92 * s] * v[157 * s];
-    const double b134 = r[92 * s] * v[151 * s];
-    const double b135 = r[93 * s] * v[160 * s];
-    const double b136 = r[93 * s] * v[151 * s];
-    const double b137 = r[94 * s] * v[160 * s];
-    const double b138 = r[94 * s] * v[125 * s];
-    const double b139 = r[95 * s];
-    const double b140 = r[96 * s];
-    const double b141 = r[97 * s];
-    const double b142 = r[98 * s];
-    const double b143 = r[99 * s];
-    const double b144 = r[100 * s];
-    const double b145 = r[101 * s];
-    const double b146 = r[102 * s];
-    const double b147 = r[103 * s];
-    const double b148 = r[104 * s];
-    const double b149 = r[105 * s];
-    const double b150 = r[106 * s];
-    const double b151 = r[107 * s];
-    const double b152 = r[108 * s];
-    const double b153 = r[109 * s];
-    const double b154 = r[110 * s];
-    const double b155 = r[111 * s];
-    const double b156 = r[112 * s];
-    const double b157 = r[113 * s];
-    const double b158 = r[114 * s];
-    const double b159 = r[115 * s];
-    const double b160 = r[116 * s];
-    const double b161 = r[117 * s];
-    const double b162 = r[118 * s];
-    const double b163 = r[119 * s];
-    const double b164 = r[120 * s];
-    const double b165 = r[121 * s];
-    const double b166 = r[122 * s];
-    const double b167 = r[123 * s];
-    const double b168 = r[124 * s];
-    const double b169 = r[125 * s];
-    const double b170 = r[126 * s];
-    const double b171 = r[127 * s];
-    const double b172 = r[128 * s];
-    const double b173 = r[129 * s];
-    const double b174 = r[130 * s];
-    const double b175 = r[131 * s];
-    const double b176 = r[132 * s];
-    const double b177 = r[133 * s];
-    const double b178 = r[134 * s];
-    const double b179 = r[135 * s];
-    const double b180 = r[136 * s];
-    const double b181 = r[138 * s];
-    const double b182 = r[139 * s];
-    const double b183 = r[140 * s];
-    const double b184 = r[141 * s];
-    const double b185 = r[142 * s];
-    const double b186 = r[143 * s];
-    const double b187 = r[144 * s];
-    const double b188 = r[145 * s];
-    const double b189 = r[146 * s] * f[0 * s];
-    const double b190 = r[147 * s] * v[153 * s];
-    const double b191 = r[147 * s] * v[115 * s];
-    const double b192 = r[148 * s] * v[115 * s];
-    const double b193 = r[148 * s] * v[101 * s];
-    const double b194 = r[149 * s] * v[115 * s];
-    const double b195 = r[149 * s] * v[102 * s];
-    const double b196 = r[150 * s] * f[0 * s];
-    const double b197 = r[151 * s] * v[153 * s];
-    const double b198 = r[151 * s] * v[115 * s];
-    const double b199 = r[152 * s] * v[146 * s];
-    const double b200 = r[152 * s] * v[115 * s];
-    const double b201 = r[153 * s] * f[0 * s];
-    const double b202 = r[154 * s] * v[153 * s];
-    const double b203 = r[154 * s] * v[75 * s];
-    const double b204 = r[155 * s] * f[0 * s];
-    const double b205 = r[156 * s] * v[153 * s];
-    const double b206 = r[156 * s] * v[77 * s];
-    const double b207 = r[157 * s];
-    const double b208 = r[158 * s];
-    const double b209 = r[159 * s];
-    const double b210 = r[160 * s];
-    const double b211 = r[161 * s];
-    const double b212 = r[162 * s];
-    const double b213 = r[163 * s];
-    const double b214 = r[164 * s];
-    const double b215 = r[165 * s];
-    const double b216 = r[166 * s];
-    const double b217 = r[167 * s];
-    const double b218 = r[168 * s];
-    const double b219 = r[169 * s];
-    const double b220 = r[170 * s];
-    const double b221 = r[171 * s];
-    const double b222 = r[172 * s];
-    const double b223 = r[173 * s];
-    const double b224 = r[174 * s];
-    const double b225 = r[175 * s];
-    const double b226 = r[176 * s];
-    const double b227 = r[177 * s];
-    const double b228 = r[178 * s];
-    const double b229 = r[179 * s];
-    const double b230 = r[180 * s];
-    const double b231 = r[181 * s];
-    const double b232 = r[182 * s] * v[155 * s];
-    const double b233 = r[182 * s] * v[140 * s];
-    const double b234 = r[183 * s] * v[155 * s];
-    const double b235 = r[183 * s] * v[131 * s];
-    const double b236 = r[184 * s] * v[155 * s];
-    const double b237 = r[184 * s] * v[130 * s];
-    const double b238 = r[185 * s] * v[155 * s];
-    const double b239 = r[185 * s] * v[132 * s];
-    const double b240 = r[186 * s] * v[155 * s];
-    const double b241 = r[186 * s] * v[139 * s];
-    const double b242 = r[187 * s] * v[155 * s];
-    const double b243 = r[187 * s] * v[135 * s];
-    const double b244 = r[188 * s] * f[0 * s];
-    const double b245 = r[189 * s];
-    const double b246 = r[190 * s] * f[0 * s];
-    const double b247 = r[191 * s];
-    const double b248 = r[192 * s];
-    const double b249 = r[193 * s] * v[160 * s];
-    const double b250 = r[193 * s] * v[104 * s];
-    const double b251 = r[194 * s] * v[160 * s];
-    const double b252 = r[194 * s] * v[104 * s];
-    const double b253 = r[195 * s] * v[160 * s];
-    const double b254 = r[195 * s] * v[138 * s];
-    const double b255 = r[196 * s] * v[160 * s];
-    const double b256 = r[196 * s] * v[139 * s];
-    const double b257 = r[197 * s] * v[160 * s];
-    const double b258 = r[197 * s] * v[105 * s];
-    const double b259 = r[198 * s] * v[160 * s];
-    const double b260 = r[198 * s] * v[136 * s];
-    const double b261 = r[199 * s] * v[160 * s];
-    const double b262 = r[199 * s] * v[140 * s];
-    const double b263 = r[200 * s] * v[160 * s];
-    const double b264 = r[200 * s] * v[128 * s];
-    const double b265 = r[201 * s] * v[160 * s];
-    const double b266 = r[201 * s] * v[131 * s];
-    const double b267 = r[202 * s] * v[160 * s];
-    const double b268 = r[202 * s] * v[130 * s];
-    const double b269 = r[203 * s] * v[160 * s];
-    const double b270 = r[203 * s] * v[112 * s];
-    const double b271 = r[204 * s] * v[160 * s];
-    const double b272 = r[204 * s] * v[133 * s];
-    const double b273 = r[205 * s] * v[160 * s];
-    const double b274 = r[205 * s] * v[132 * s];
-    const double b275 = r[206 * s] * v[160 * s];
-    const double b276 = r[206 * s] * v[134 * s];
-    const double b277 = r[207 * s] * v[160 * s];
-    const double b278 = r[207 * s] * v[135 * s];
-    const double b279 = r[208 * s] * v[160 * s];
-    const double b280 = r[208 * s] * v[148 * s];
-    const double b281 = r[209 * s] * v[160 * s];
-    const double b282 = r[209 * s] * v[141 * s];
-    const double b283 = r[210 * s] * v[160 * s];
-    const double b284 = r[210 * s] * v[116 * s];
-    const double b285 = r[211 * s];
-    const double b286 = r[212 * s];
-    const double b287 = r[213 * s];
-    const double b288 = r[214 * s];
-    const double b289 = r[215 * s];
-    const double b290 = r[216 * s];
-    const double b291 = r[217 * s];
-    const double b292 = r[218 * s];
-    const double b293 = r[219 * s];
-    const double b294 = r[220 * s];
-    const double b295 = r[221 * s];
-    const double b296 = r[222 * s];
-    const double b297 = r[223 * s];
-    const double b298 = r[224 * s];
-    const double b299 = r[225 * s];
-    const double b300 = r[226 * s];
-    const double b301 = r[227 * s];
-    const double b302 = r[228 * s];
-    const double b303 = r[229 * s];
-    const double b304 = r[230 * s];
-    const double b305 = r[231 * s];
-    const double b306 = r[232 * s] * 0x1.0000000000000p+1 * v[160 * s];
-    const double b307 = r[233 * s] * v[160 * s];
-    const double b308 = r[233 * s] * v[154 * s];
-    const double b309 = r[234 * s] * v[160 * s];
-    const double b310 = r[234 * s] * v[150 * s];
-    const double b311 = r[235 * s] * v[160 * s];
-    const double b312 = r[235 * s] * v[145 * s];
-    const double b313 = r[236 * s] * v[160 * s];
-    const double b314 = r[236 * s] * v[156 * s];
-    const double b315 = r[237 * s] * v[158 * s];
-    const double b316 = r[237 * s] * v[154 * s];
-    const double b317 = r[238 * s] * v[158 * s];
-    const double b318 = r[238 * s] * v[150 * s];
-    const double b319 = r[239 * s];
-    const double b320 = r[240 * s] * v[153 * s];
-    const double b321 = r[240 * s] * v[126 * s];
-    const double b322 = r[241 * s] * v[156 * s];
-    const double b323 = r[241 * s] * v[126 * s];
-    const double b324 = r[242 * s] * f[2 * s];
-    const double b325 = r[243 * s] * v[154 * s];
-    const double b326 = r[243 * s] * v[142 * s];
-    const double b327 = r[244 * s] * 0x1.0000000000000p+1 * v[142 * s];
-    const double b328 = r[245 * s] * v[155 * s] * v[156 * s];
-    const double b329 = r[245 * s] * v[127 * s] * v[156 * s];
-    const double b330 = r[245 * s] * v[127 * s] * v[155 * s];
-    const double b331 = r[246 * s] * f[0 * s];
-    const double b332 = r[247 * s] * 0x1.0000000000000p+1 * v[119 * s];
-    const double b333 = r[248 * s] * v[156 * s];
-    const double b334 = r[248 * s] * v[119 * s];
-    const double b335 = r[249 * s] * v[160 * s];
-    const double b336 = r[249 * s] * v[137 * s];
-    const double b337 = r[250 * s] * v[156 * s];
-    const double b338 = r[250 * s] * v[143 * s];
-    const double b339 = r[251 * s] * v[159 * s];
-    const double b340 = r[251 * s] * v[143 * s];
-    const double b341 = r[252 * s];
-    const double b342 = r[253 * s] * v[152 * s];
-    const double b343 = r[253 * s] * v[147 * s];
-    const double b344 = r[254 * s] * v[160 * s];
-    const double b345 = r[254 * s] * v[147 * s];
-    const double b346 = r[255 * s] * v[156 * s];
-    const double b347 = r[255 * s] * v[118 * s];
-    const double b348 = r[256 * s] * v[159 * s];
-    const double b349 = r[256 * s] * v[118 * s];
-    const double b350 = r[257 * s];
-    const double b351 = r[258 * s] * v[152 * s];
-    const double b352 = r[258 * s] * v[117 * s];
-    const double b353 = r[259 * s] * v[160 * s];
-    const double b354 = r[259 * s] * v[117 * s];
-    const double b355 = r[260 * s];
-    const double b356 = r[261 * s];
-    const double b357 = r[262 * s];
-    const double b358 = r[263 * s];
-    const double b359 = r[264 * s];
-    const double b360 = r[265 * s];
-    const double b361 = r[266 * s];
-    const double b362 = r[267 * s];
-    const double b363 = r[268 * s];
-    jvs[0 * s] = 0.0 - b32;
-    jvs[1 * s] = 0.0 - b33;
-    jvs[2 * s] = 0.0 - b34;
-    jvs[3 * s] = 0.0 - b35;
-    jvs[4 * s] = 0.0 - b36;
-    jvs[5 * s] = 0.0 - b37;
-    jvs[6 * s] = 0.0 - b38;
-    jvs[7 * s] = 0.0 - b39;
-    jvs[8 * s] = 0.0 + b39;
-    jvs[9 * s] = 0.0 - b156;
-    jvs[10 * s] = 0.0 + b37;
-    jvs[11 * s] = 0.0 - b157;
-    jvs[12 * s] = 0.0 - b158;
-    jvs[13 * s] = 0.0 + b38;
-    jvs[14 * s] = 0.0 - b159;
-    jvs[15 * s] = 0.0 - b164;
-    jvs[16 * s] = 0.0 - b165;
-    jvs[17 * s] = 0.0 - b160;
-    jvs[18 * s] = 0.0 - b161;
-    jvs[19 * s] = 0.0 - b162;
-    jvs[20 * s] = 0.0 + b35;
-    jvs[21 * s] = 0.0 - b163;
+    vdot[62 * s] = 0.0 + (r[211 * s] * v[136 * s]) + (r[212 * s] * v[140 * s]);
+    vdot[63 * s] = 0.0 + (r[213 * s] * v[128 * s]) + (r[214 * s] * v[131 * s]) + (r[215 * s] * v[130 * s]);
+    vdot[64 * s] = 0.0 + (r[216 * s] * v[133 * s]) + (r[217 * s] * v[132 * s]);
+    vdot[65 * s] = 0.0 + (r[218 * s] * v[134 * s]) + (r[219 * s] * v[135 * s]);
+    vdot[66 * s] = 0.0 + (r[220 * s] * v[148 * s]) + (r[224 * s] * v[143 * s]) + (r[264 * s] * v[147 * s]);
+    vdot[67 * s] = 0.0 + (r[130 * s] * v[150 * s]) + (r[131 * s] * v[154 * s]);
+    vdot[68 * s] = 0.0 + (r[221 * s] * v[104 * s]);
+    vdot[69 * s] = 0.0 + (r[222 * s] * v[138 * s]) + (r[223 * s] * v[139 * s]);
+    vdot[70 * s] = 0.0 + (r[225 * s] * v[118 * s]) + (r[226 * s] * v[116 * s]) + (r[268 * s] * v[117 * s]);
+    vdot[71 * s] = 0.0 + (r[260 * s] * v[126 * s]);
+    vdot[72 * s] = 0.0 + (r[261 * s] * v[119 * s]);
+    vdot[73 * s] = 0.0 - (r[14 * s] * v[73 * s]) + (r[30 * s] * v[125 * s]);
+    vdot[74 * s] = 0.0 - (r[141 * s] * v[74 * s]) + (r[144 * s] * v[75 * s]);
+    vdot[75 * s] = 0.0 + (r[141 * s] * v[74 * s]) - (r[144 * s] * v[75 * s]) - (r[153 * s] * v[75 * s] * f[0 * s]) - (r[154 * s] * v[75 * s] * v[153 * s]) - (r[161 * s] * v[75 * s]);
+    vdot[76 * s] = 0.0 - (r[142 * s] * v[76 * s]) + (r[145 * s] * v[77 * s]);
+    vdot[77 * s] = 0.0 + (r[142 * s] * v[76 * s]) - (r[145 * s] * v[77 * s]) - (r[155 * s] * v[77 * s] * f[0 * s]) - (r[156 * s] * v[77 * s] * v[153 * s]) - (r[162 * s] * v[77 * s]);
+    vdot[78 * s] = 0.0 - (r[166 * s] * v[78 * s]) + (r[171 * s] * v[104 * s]);
+    vdot[79 * s] = 0.0 - (r[167 * s] * v[79 * s]) + (r[172 * s] * v[134 * s]);
+    vdot[80 * s] = 0.0 - (r[168 * s] * v[80 * s]) + (r[173 * s] * v[143 * s]);
+    vdot[81 * s] = 0.0 - (r[12 * s] * v[81 * s]) + (r[28 * s] * v[154 * s]);
+    vdot[82 * s] = 0.0 - (r[170 * s] * v[82 * s]) + (r[175 * s] * v[133 * s]);
+    vdot[83 * s] = 0.0 - (r[169 * s] * v[83 * s]) + (r[174 * s] * v[118 * s]);
+    vdot[84 * s] = 0.0 - (r[4 * s] * v[84 * s]) + (r[20 * s] * v[145 * s]);
+    vdot[85 * s] = 0.0 - (r[1 * s] * v[85 * s]) + (r[17 * s] * v[106 * s]);
+    vdot[86 * s] = 0.0 - (r[2 * s] * v[86 * s]) + (r[18 * s] * v[124 * s]);
+    vdot[87 * s] = 0.0 - (r[3 * s] * v[87 * s]) + (r[19 * s] * v[107 * s]);
+    vdot[88 * s] = 0.0 - (r[5 * s] * v[88 * s]) + (r[21 * s] * v[157 * s]);
+    vdot[89 * s] = 0.0 - (r[6 * s] * v[89 * s]) + (r[22 * s] * v[141 * s]);
+    vdot[90 * s] = 0.0 - (r[7 * s] * v[90 * s]) + (r[23 * s] * v[120 * s]);
+    vdot[91 * s] = 0.0 - (r[8 * s] * v[91 * s]) + (r[24 * s] * v[121 * s]);
+    vdot[92 * s] = 0.0 - (r[9 * s] * v[92 * s]) + (r[25 * s] * v[110 * s]);
+    vdot[93 * s] = 0.0 - (r[10 * s] * v[93 * s]) + (r[26 * s] * v[105 * s]);
+    vdot[94 * s] = 0.0 - (r[11 * s] * v[94 * s]) + (r[27 * s] * v[112 * s]);
+    vdot[95 * s] = 0.0 - (r[13 * s] * v[95 * s]) + (r[29 * s] * v[158 * s]);
+    vdot[96 * s] = 0.0 - (r[15 * s] * v[96 * s]) + (r[31 * s] * v[149 * s]);
+    vdot[97 * s] = 0.0 - (r[227 * s] * v[97 * s]) + (r[229 * s] * v[126 * s]);
+    vdot[98 * s] = 0.0 - (r[228 * s] * v[98 * s]) + (r[230 * s] * v[119 * s]);
+    vdot[99 * s] = 0.0 - (r[0 * s] * v[99 * s]) + (r[16 * s] * v[144 * s]);
+    vdot[100 * s] = 0.0 - (r[140 * s] * v[100 * s]) + (r[143 * s] * v[115 * s]);
+    vdot[101 * s] = 0.0 + (r[146 * s] * v[115 * s] * f[0 * s]) - (r[148 * s] * v[101 * s] * v[115 * s]) - (r[158 * s] * v[101 * s]);
+    vdot[102 * s] = 0.0 + (r[147 * s] * v[115 * s] * v[153 * s]) - (r[149 * s] * v[102 * s] * v[115 * s]) - (r[159 * s] * v[102 * s]);
+}
+
+KQ_HD KQ_NOINLINE void kqu_fun_2(const double* v, const double* f, const double* r, double* vdot, long long s)
+{
+    vdot[103 * s] = 0.0 + (r[236 * s] * v[156 * s] * v[160 * s]) + (r[241 * s] * v[126 * s] * v[156 * s]) - (r[242 * s] * v[103 * s] * f[2 * s]) + (r[248 * s] * v[119 * s] * v[156 * s]) - (r[263 * s] * v[103 * s]);
+    vdot[104 * s] = 0.0 + (r[166 * s] * v[78 * s]) - (r[171 * s] * v[104 * s]) - (r[193 * s] * v[104 * s] * v[160 * s]) - (r[194 * s] * v[104 * s] * v[160 * s]) - (r[221 * s] * v[104 * s]);
+    vdot[105 * s] = 0.0 + (r[10 * s] * v[93 * s]) - (r[26 * s] * v[105 * s]) - (r[106 * s] * v[105 * s]) + (r[194 * s] * v[104 * s] * v[160 * s]) - (r[197 * s] * v[105 * s] * v[160 * s]);
+    vdot[106 * s] = 0.0 + (r[1 * s] * v[85 * s]) - (r[17 * s] * v[106 * s]) - (r[42 * s] * v[106 * s]) + (r[56 * s] * v[146 * s] * v[155 * s]) - (r[96 * s] * v[106 * s]);
+    vdot[107 * s] = 0.0 + (r[3 * s] * v[87 * s]) - (r[19 * s] * v[107 * s]) - (r[45 * s] * v[107 * s]) + (r[59 * s] * v[108 * s] * v[152 * s]) - (r[98 * s] * v[107 * s]);
+    vdot[108 * s] = 0.0 + (r[33 * s] * v[1 * s]) + (r[45 * s] * v[107 * s]) - (r[59 * s] * v[108 * s] * v[152 * s]) - (r[110 * s] * v[108 * s]);
+    vdot[109 * s] = 0.0 - (r[49 * s] * v[109 * s]) + (r[63 * s] * v[123 * s] * v[155 * s]) - (r[104 * s] * v[109 * s]);
+    vdot[110 * s] = 0.0 + (r[9 * s] * v[92 * s]) - (r[25 * s] * v[110 * s]) - (r[47 * s] * v[110 * s]) + (r[61 * s] * v[111 * s] * v[155 * s]) - (r[105 * s] * v[110 * s]);
+    vdot[111 * s] = 0.0 + (r[34 * s] * v[2 * s]) + (r[47 * s] * v[110 * s]) - (r[61 * s] * v[111 * s] * v[155 * s]) - (r[111 * s] * v[111 * s]);
+    vdot[112 * s] = 0.0 + (r[11 * s] * v[94 * s]) - (r[27 * s] * v[112 * s]) - (r[107 * s] * v[112 * s]) - (r[203 * s] * v[112 * s] * v[160 * s]);
+    vdot[113 * s] = 0.0 + (r[44 * s] * v[114 * s]) - (r[58 * s] * v[113 * s] * v[155 * s]) - (r[127 * s] * v[113 * s]);
+    vdot[114 * s] = 0.0 + (r[43 * s] * v[124 * s]) - (r[44 * s] * v[114 * s]) - (r[57 * s] * v[114 * s] * v[155 * s]) + (r[58 * s] * v[113 * s] * v[155 * s]) - (r[126 * s] * v[114 * s]);
+    vdot[115 * s] = 0.0 + (r[140 * s] * v[100 * s]) - (r[143 * s] * v[115 * s]) - (r[146 * s] * v[115 * s] * f[0 * s]) - (r[147 * s] * v[115 * s] * v[153 * s]) - (r[148 * s] * v[101 * s] * v[115 * s]) - (r[149 * s] * v[102 * s] * v[115 * s]) - (r[150 * s] * v[115 * s] * f[0 * s]) - (r[151 * s] * v[115 * s] * v[153 * s]) - (r[152 * s] * v[115 * s] * v[146 * s]) - (r[157 * s] * v[115 * s]);
+    vdot[116 * s] = 0.0 + (r[190 * s] * v[118 * s] * f[0 * s]) - (r[191 * s] * v[116 * s]) - (r[210 * s] * v[116 * s] * v[160 * s]) - (r[226 * s] * v[116 * s]) + (r[258 * s] * v[117 * s] * v[152 * s]);
+    vdot[117 * s] = 0.0 + (r[255 * s] * v[118 * s] * v[156 * s]) + (r[256 * s] * v[118 * s] * v[159 * s]) - (r[257 * s] * v[117 * s]) - (r[258 * s] * v[117 * s] * v[152 * s]) - (r[259 * s] * v[117 * s] * v[160 * s]) - (r[268 * s] * v[117 * s]);
+    vdot[118 * s] = 0.0 + (r[169 * s] * v[83 * s]) - (r[174 * s] * v[118 * s]) - (r[190 * s] * v[118 * s] * f[0 * s]) + (r[191 * s] * v[116 * s]) - (r[225 * s] * v[118 * s]) - (r[255 * s] * v[118 * s] * v[156 * s]) - (r[256 * s] * v[118 * s] * v[159 * s]) + (r[257 * s] * v[117 * s]);
+}
+
+KQ_HD KQ_NOINLINE void kqu_fun_3(const double* v, const double* f, const double* r, double* vdot, long long s)
+{
+    vdot[119 * s] = 0.0 + (r[228 * s] * v[98 * s]) - (r[230 * s] * v[119 * s]) + -0x1.0000000000000p+1 * (r[247 * s] * v[119 * s] * v[119 * s]) - (r[248 * s] * v[119 * s] * v[156 * s]) - (r[261 * s] * v[119 * s]);
+    vdot[120 * s] = 0.0 + (r[7 * s] * v[90 * s]) - (r[23 * s] * v[120 * s]) - (r[81 * s] * v[120 * s] * v[155 * s] * v[156 * s]) - (r[102 * s] * v[120 * s]) + (r[248 * s] * v[119 * s] * v[156 * s]);
+    vdot[121 * s] = 0.0 + (r[8 * s] * v[91 * s]) - (r[24 * s] * v[121 * s]) - (r[82 * s] * v[121 * s] * v[155 * s] * v[156 * s]) - (r[83 * s] * v[121 * s] * v[156 * s]) - (r[103 * s] * v[121 * s]);
+    vdot[122 * s] = 0.0 + (r[240 * s] * v[126 * s] * v[153 * s]) + 0x1.0000000000000p+1 * (r[244 * s] * v[142 * s] * v[142 * s]) - (r[246 * s] * v[122 * s] * f[0 * s]) - (r[262 * s] * v[122 * s]);
+    vdot[123 * s] = 0.0 + (r[49 * s] * v[109 * s]) - (r[50 * s] * v[123 * s]) - (r[63 * s] * v[123 * s] * v[155 * s]) + (r[64 * s] * v[153 * s] * v[155 * s]) - (r[129 * s] * v[123 * s]) + (r[246 * s] * v[122 * s] * f[0 * s]);
+    vdot[124 * s] = 0.0 + (r[2 * s] * v[86 * s]) - (r[18 * s] * v[124 * s]) - (r[43 * s] * v[124 * s]) + (r[57 * s] * v[114 * s] * v[155 * s]) - (r[97 * s] * v[124 * s]) + 0x1.0000000000000p+1 * (r[200 * s] * v[128 * s] * v[160 * s]) + (r[201 * s] * v[131 * s] * v[160 * s]) + (r[202 * s] * v[130 * s] * v[160 * s]) + (r[204 * s] * v[133 * s] * v[160 * s]) + (r[205 * s] * v[132 * s] * v[160 * s]) + (r[209 * s] * v[141 * s] * v[160 * s]) + (r[249 * s] * v[137 * s] * v[160 * s]);
+    vdot[125 * s] = 0.0 + (r[14 * s] * v[73 * s]) - (r[30 * s] * v[125 * s]) - (r[52 * s] * v[125 * s]) + (r[66 * s] * v[151 * s] * v[155 * s]) - (r[94 * s] * v[125 * s] * v[160 * s]) - (r[133 * s] * v[125 * s]);
+    vdot[126 * s] = 0.0 + (r[227 * s] * v[97 * s]) - (r[229 * s] * v[126 * s]) - (r[240 * s] * v[126 * s] * v[153 * s]) - (r[241 * s] * v[126 * s] * v[156 * s]) - (r[260 * s] * v[126 * s]);
+    vdot[127 * s] = 0.0 + (r[243 * s] * v[142 * s] * v[154 * s]) - (r[245 * s] * v[127 * s] * v[155 * s] * v[156 * s]) - (r[266 * s] * v[127 * s]);
+    vdot[128 * s] = 0.0 - (r[177 * s] * v[128 * s]) + (r[183 * s] * v[131 * s] * v[155 * s]) + (r[198 * s] * v[136 * s] * v[160 * s]) - (r[200 * s] * v[128 * s] * v[160 * s]) - (r[213 * s] * v[128 * s]);
+    vdot[129 * s] = 0.0 + (r[53 * s] * v[149 * s]) - (r[67 * s] * v[129 * s] * v[155 * s]) - (r[91 * s] * v[129 * s]) - (r[135 * s] * v[129 * s]) + (r[238 * s] * v[150 * s] * v[158 * s]);
+    vdot[130 * s] = 0.0 + (r[178 * s] * v[131 * s]) - (r[184 * s] * v[130 * s] * v[155 * s]) - (r[202 * s] * v[130 * s] * v[160 * s]) - (r[215 * s] * v[130 * s]);
+    vdot[131 * s] = 0.0 + (r[177 * s] * v[128 * s]) - (r[178 * s] * v[131 * s]) - (r[183 * s] * v[131 * s] * v[155 * s]) + (r[184 * s] * v[130 * s] * v[155 * s]) + (r[199 * s] * v[140 * s] * v[160 * s]) - (r[201 * s] * v[131 * s] * v[160 * s]) - (r[214 * s] * v[131 * s]);
+    vdot[132 * s] = 0.0 + (r[179 * s] * v[133 * s]) - (r[185 * s] * v[132 * s] * v[155 * s]) + 0x1.d70a3e0000000p-1 * (r[203 * s] * v[112 * s] * v[160 * s]) - (r[205 * s] * v[132 * s] * v[160 * s]) - (r[217 * s] * v[132 * s]);
+}
+
+KQ_HD KQ_NOINLINE void kqu_fun_4(const double* v, const double* f, const double* r, double* vdot, long long s)
+{
+    vdot[133 * s] = 0.0 + (r[170 * s] * v[82 * s]) - (r[175 * s] * v[133 * s]) - (r[179 * s] * v[133 * s]) + (r[185 * s] * v[132 * s] * v[155 * s]) - (r[204 * s] * v[133 * s] * v[160 * s]) - (r[216 * s] * v[133 * s]);
+    vdot[134 * s] = 0.0 + (r[167 * s] * v[79 * s]) - (r[172 * s] * v[134 * s]) - (r[181 * s] * v[134 * s]) + (r[187 * s] * v[135 * s] * v[155 * s]) + (r[204 * s] * v[133 * s] * v[160 * s]) - (r[206 * s] * v[134 * s] * v[160 * s]) - (r[218 * s] * v[134 * s]);
+    vdot[135 * s] = 0.0 + (r[181 * s] * v[134 * s]) - (r[187 * s] * v[135 * s] * v[155 * s]) + (r[205 * s] * v[132 * s] * v[160 * s]) - (r[207 * s] * v[135 * s] * v[160 * s]) - (r[219 * s] * v[135 * s]);
+    vdot[136 * s] = 0.0 - (r[176 * s] * v[136 * s]) + (r[182 * s] * v[140 * s] * v[155 * s]) + (r[197 * s] * v[105 * s] * v[160 * s]) - (r[198 * s] * v[136 * s] * v[160 * s]) + 0x1.b333340000000p-1 * (r[206 * s] * v[134 * s] * v[160 * s]) - (r[211 * s] * v[136 * s]);
+    vdot[137 * s] = 0.0 + (r[46 * s] * v[141 * s]) - (r[60 * s] * v[137 * s] * v[155 * s]) - (r[128 * s] * v[137 * s]) - (r[249 * s] * v[137 * s] * v[160 * s]);
+    vdot[138 * s] = 0.0 - (r[180 * s] * v[138 * s]) + (r[186 * s] * v[139 * s] * v[155 * s]) + (r[193 * s] * v[104 * s] * v[160 * s]) - (r[195 * s] * v[138 * s] * v[160 * s]) - (r[222 * s] * v[138 * s]);
+    vdot[139 * s] = 0.0 + (r[180 * s] * v[138 * s]) - (r[186 * s] * v[139 * s] * v[155 * s]) - (r[196 * s] * v[139 * s] * v[160 * s]) - (r[223 * s] * v[139 * s]);
+    vdot[140 * s] = 0.0 + (r[176 * s] * v[136 * s]) - (r[182 * s] * v[140 * s] * v[155 * s]) + (r[195 * s] * v[138 * s] * v[160 * s]) + (r[196 * s] * v[139 * s] * v[160 * s]) - (r[199 * s] * v[140 * s] * v[160 * s]) + 0x1.47ae140000000p-4 * (r[203 * s] * v[112 * s] * v[160 * s]) + 0x1.b333340000000p-1 * (r[207 * s] * v[135 * s] * v[160 * s]) - (r[212 * s] * v[140 * s]);
+    vdot[141 * s] = 0.0 + (r[6 * s] * v[89 * s]) - (r[22 * s] * v[141 * s]) - (r[46 * s] * v[141 * s]) + (r[60 * s] * v[137 * s] * v[155 * s]) - (r[101 * s] * v[141 * s]) + (r[208 * s] * v[148 * s] * v[160 * s]) - (r[209 * s] * v[141 * s] * v[160 * s]) + (r[254 * s] * v[147 * s] * v[160 * s]);
+    vdot[142 * s] = 0.0 + (r[242 * s] * v[103 * s] * f[2 * s]) - (r[243 * s] * v[142 * s] * v[154 * s]) + -0x1.0000000000000p+1 * (r[244 * s] * v[142 * s] * v[142 * s]) - (r[265 * s] * v[142 * s]);
+    vdot[143 * s] = 0.0 + (r[168 * s] * v[80 * s]) - (r[173 * s] * v[143 * s]) - (r[188 * s] * v[143 * s] * f[0 * s]) + (r[189 * s] * v[148 * s]) - (r[224 * s] * v[143 * s]) + 0x1.0000000000000p+1 * (r[247 * s] * v[119 * s] * v[119 * s]) - (r[250 * s] * v[143 * s] * v[156 * s]) - (r[251 * s] * v[143 * s] * v[159 * s]) + (r[252 * s] * v[147 * s]);
+    vdot[144 * s] = 0.0 + (r[0 * s] * v[99 * s]) - (r[16 * s] * v[144 * s]) - (r[40 * s] * v[144 * s]) + (r[54 * s] * v[155 * s] * v[156 * s]) - (r[69 * s] * v[144 * s] * v[157 * s]) - (r[72 * s] * v[13 * s] * v[144 * s]) - (r[75 * s] * v[12 * s] * v[144 * s]) - (r[78 * s] * v[12 * s] * v[13 * s] * v[144 * s]) - (r[87 * s] * v[144 * s] * v[158 * s]) - (r[95 * s] * v[144 * s]);
+}
+
+KQ_HD KQ_NOINLINE void kqu_fun_5(const double* v, const double* f, const double* r, double* vdot, long long s)
+{
+    vdot[145 * s] = 0.0 + (r[4 * s] * v[84 * s]) - (r[20 * s] * v[145 * s]) - (r[68 * s] * v[145 * s] * v[155 * s] * v[156 * s]) + (r[84 * s] * v[154 * s] * v[154 * s]) + (r[85 * s] * v[150 * s] * v[154 * s]) - (r[99 * s] * v[145 * s]) - (r[192 * s] * v[145 * s]) + (r[232 * s] * v[160 * s] * v[160 * s]) - (r[235 * s] * v[145 * s] * v[160 * s]);
+    vdot[146 * s] = 0.0 + (r[32 * s] * v[0 * s]) + (r[42 * s] * v[106 * s]) - (r[56 * s] * v[146 * s] * v[155 * s]) + (r[90 * s] * v[149 * s] * v[156 * s]) + (r[92 * s] * v[151 * s] * v[157 * s]) - (r[109 * s] * v[146 * s]) - (r[152 * s] * v[115 * s] * v[146 * s]) - (r[231 * s] * v[146 * s]) + (r[240 * s] * v[126 * s] * v[153 * s]) + (r[241 * s] * v[126 * s] * v[156 * s]);
+    vdot[147 * s] = 0.0 + (r[250 * s] * v[143 * s] * v[156 * s]) + (r[251 * s] * v[143 * s] * v[159 * s]) - (r[252 * s] * v[147 * s]) - (r[253 * s] * v[147 * s] * v[152 * s]) - (r[254 * s] * v[147 * s] * v[160 * s]) - (r[264 * s] * v[147 * s]);
+    vdot[148 * s] = 0.0 + (r[188 * s] * v[143 * s] * f[0 * s]) - (r[189 * s] * v[148 * s]) + 0x1.3333340000000p-3 * (r[206 * s] * v[134 * s] * v[160 * s]) + 0x1.3333340000000p-3 * (r[207 * s] * v[135 * s] * v[160 * s]) - (r[208 * s] * v[148 * s] * v[160 * s]) - (r[220 * s] * v[148 * s]) + (r[253 * s] * v[147 * s] * v[152 * s]);
+    vdot[149 * s] = 0.0 + (r[15 * s] * v[96 * s]) - (r[31 * s] * v[149 * s]) - (r[53 * s] * v[149 * s]) + (r[67 * s] * v[129 * s] * v[155 * s]) - (r[90 * s] * v[149 * s] * v[156 * s]) - (r[136 * s] * v[149 * s]) + (r[237 * s] * v[154 * s] * v[158 * s]) - (r[239 * s] * v[149 * s]);
+    vdot[150 * s] = 0.0 + (r[51 * s] * v[154 * s]) - (r[65 * s] * v[150 * s] * v[155 * s]) - (r[85 * s] * v[150 * s] * v[154 * s]) - (r[86 * s] * v[150 * s] * v[157 * s]) - (r[130 * s] * v[150 * s]) - (r[234 * s] * v[150 * s] * v[160 * s]) - (r[238 * s] * v[150 * s] * v[158 * s]);
+    vdot[151 * s] = 0.0 + (r[52 * s] * v[125 * s]) - (r[66 * s] * v[151 * s] * v[155 * s]) + 0x1.0000000000000p+1 * (r[87 * s] * v[144 * s] * v[158 * s]) + 0x1.0000000000000p+1 * (r[88 * s] * v[156 * s] * v[158 * s]) + 0x1.0000000000000p+1 * (r[89 * s] * v[158 * s] * v[159 * s]) + (r[91 * s] * v[129 * s]) - (r[92 * s] * v[151 * s] * v[157 * s]) - (r[93 * s] * v[151 * s] * v[160 * s]) - (r[134 * s] * v[151 * s]);
+    vdot[152 * s] = 0.0 + (r[45 * s] * v[107 * s]) + (r[48 * s] * f[0 * s]) - (r[59 * s] * v[108 * s] * v[152 * s]) - (r[62 * s] * v[152 * s] * v[155 * s]) + (r[85 * s] * v[150 * s] * v[154 * s]) + (r[86 * s] * v[150 * s] * v[157 * s]) + (r[93 * s] * v[151 * s] * v[160 * s]) - (r[123 * s] * v[152 * s]) + (r[202 * s] * v[130 * s] * v[160 * s]) + (r[231 * s] * v[146 * s]) + (r[234 * s] * v[150 * s] * v[160 * s]) + (r[249 * s] * v[137 * s] * v[160 * s]) + (r[251 * s] * v[143 * s] * v[159 * s]) - (r[253 * s] * v[147 * s] * v[152 * s]);
+}
+
+KQ_HD KQ_NOINLINE void kqu_fun_6(const double* v, const double* f, const double* r, double* vdot, long long s)
+{
+    vdot[153 * s] = 0.0 + (r[36 * s] * v[4 * s]) + (r[50 * s] * v[123 * s]) - (r[64 * s] * v[153 * s] * v[155 * s]) + (r[68 * s] * v[145 * s] * v[155 * s] * v[156 * s]) + (r[69 * s] * v[144 * s] * v[157 * s]) + (r[70 * s] * v[156 * s] * v[157 * s]) + (r[71 * s] * v[157 * s] * v[159 * s]) + (r[72 * s] * v[13 * s] * v[144 * s]) + (r[73 * s] * v[13 * s] * v[156 * s]) + (r[74 * s] * v[13 * s] * v[159 * s]) + (r[75 * s] * v[12 * s] * v[144 * s]) + (r[76 * s] * v[12 * s] * v[156 * s]) + (r[77 * s] * v[12 * s] * v[159 * s]) + (r[78 * s] * v[12 * s] * v[13 * s] * v[144 * s]) + (r[79 * s] * v[12 * s] * v[13 * s] * v[156 * s]) + (r[80 * s] * v[12 * s] * v[13 * s] * v[159 * s]) + (r[81 * s] * v[120 * s] * v[155 * s] * v[156 * s]) + (r[82 * s] * v[121 * s] * v[155 * s] * v[156 * s]) + (r[83 * s] * v[121 * s] * v[156 * s]) + (r[87 * s] * v[144 * s] * v[158 * s]) + (r[88 * s] * v[156 * s] * v[158 * s]) + (r[89 * s] * v[158 * s] * v[159 * s]) + (r[90 * s] * v[149 * s] * v[156 * s]) - (r[108 * s] * v[153 * s]) - (r[147 * s] * v[115 * s] * v[153 * s]) - (r[151 * s] * v[115 * s] * v[153 * s]) - (r[154 * s] * v[75 * s] * v[153 * s]) - (r[156 * s] * v[77 * s] * v[153 * s]) - (r[240 * s] * v[126 * s] * v[153 * s]) + 0x1.0000000000000p+1 * (r[245 * s] * v[127 * s] * v[155 * s] * v[156 * s]);
+    vdot[154 * s] = 0.0 + (r[12 * s] * v[81 * s]) - (r[28 * s] * v[154 * s]) - (r[51 * s] * v[154 * s]) + (r[65 * s] * v[150 * s] * v[155 * s]) + -0x1.0000000000000p+1 * (r[84 * s] * v[154 * s] * v[154 * s]) - (r[85 * s] * v[150 * s] * v[154 * s]) - (r[131 * s] * v[154 * s]) + (r[193 * s] * v[104 * s] * v[160 * s]) + (r[194 * s] * v[104 * s] * v[160 * s]) + (r[195 * s] * v[138 * s] * v[160 * s]) + (r[196 * s] * v[139 * s] * v[160 * s]) + (r[197 * s] * v[105 * s] * v[160 * s]) + (r[198 * s] * v[136 * s] * v[160 * s]) + (r[199 * s] * v[140 * s] * v[160 * s]) + (r[203 * s] * v[112 * s] * v[160 * s]) + (r[204 * s] * v[133 * s] * v[160 * s]) + (r[205 * s] * v[132 * s] * v[160 * s]) + (r[208 * s] * v[148 * s] * v[160 * s]) + (r[209 * s] * v[141 * s] * v[160 * s]) - (r[233 * s] * v[154 * s] * v[160 * s]) + (r[235 * s] * v[145 * s] * v[160 * s]) - (r[237 * s] * v[154 * s] * v[158 * s]) + (r[239 * s] * v[149 * s]) - (r[243 * s] * v[142 * s] * v[154 * s]) + 0x1.0000000000000p+1 * (r[247 * s] * v[119 * s] * v[119 * s]) + (r[249 * s] * v[137 * s] * v[160 * s]) + (r[254 * s] * v[147 * s] * v[160 * s]);
+}
+
+KQ_HD KQ_NOINLINE void kqu_fun_7(const double* v, const double* f, const double* r, double* vdot, long long s)
+{
+    vdot[155 * s] = 0.0 + (r[40 * s] * v[144 * s]) + (r[41 * s] * v[156 * s]) + (r[42 * s] * v[106 * s]) + (r[43 * s] * v[124 * s]) + (r[44 * s] * v[114 * s]) + (r[46 * s] * v[141 * s]) + (r[47 * s] * v[110 * s]) + (r[48 * s] * f[0 * s]) + (r[49 * s] * v[109 * s]) + (r[50 * s] * v[123 * s]) + (r[51 * s] * v[154 * s]) + (r[52 * s] * v[125 * s]) + (r[53 * s] * v[149 * s]) - (r[54 * s] * v[155 * s] * v[156 * s]) - (r[55 * s] * v[155 * s] * v[159 * s]) - (r[56 * s] * v[146 * s] * v[155 * s]) - (r[57 * s] * v[114 * s] * v[155 * s]) - (r[58 * s] * v[113 * s] * v[155 * s]) - (r[60 * s] * v[137 * s] * v[155 * s]) - (r[61 * s] * v[111 * s] * v[155 * s]) - (r[62 * s] * v[152 * s] * v[155 * s]) - (r[63 * s] * v[123 * s] * v[155 * s]) - (r[64 * s] * v[153 * s] * v[155 * s]) - (r[65 * s] * v[150 * s] * v[155 * s]) - (r[66 * s] * v[151 * s] * v[155 * s]) - (r[67 * s] * v[129 * s] * v[155 * s]) + (r[68 * s] * v[145 * s] * v[155 * s] * v[156 * s]) + 0x1.0000000000000p+1 * (r[69 * s] * v[144 * s] * v[157 * s]) + (r[70 * s] * v[156 * s] * v[157 * s]) + 0x1.0000000000000p+1 * (r[72 * s] * v[13 * s] * v[144 * s]) + (r[73 * s] * v[13 * s] * v[156 * s]) + 0x1.0000000000000p+1 * (r[75 * s] * v[12 * s] * v[144 * s]) + (r[76 * s] * v[12 * s] * v[156 * s]) + 0x1.0000000000000p+1 * (r[78 * s] * v[12 * s] * v[13 * s] * v[144 * s]) + (r[79 * s] * v[12 * s] * v[13 * s] * v[156 * s]) + (r[81 * s] * v[120 * s] * v[155 * s] * v[156 * s]) + (r[82 * s] * v[121 * s] * v[155 * s] * v[156 * s]) + (r[83 * s] * v[121 * s] * v[156 * s]) + 0x1.0000000000000p+2 * (r[87 * s] * v[144 * s] * v[158 * s]) + 0x1.8000000000000p+1 * (r[88 * s] * v[156 * s] * v[158 * s]) + 0x1.0000000000000p+1 * (r[89 * s] * v[158 * s] * v[159 * s]) + 0x1.0000000000000p+1 * (r[90 * s] * v[149 * s] * v[156 * s]) - (r[122 * s] * v[155 * s]) + (r[176 * s] * v[136 * s]) + (r[177 * s] * v[128 * s]) + (r[178 * s] * v[131 * s]) + (r[179 * s] * v[133 * s]) + (r[180 * s] * v[138 * s]) + (r[181 * s] * v[134 * s]) - (r[182 * s] * v[140 * s] * v[155 * s]) - (r[183 * s] * v[131 * s] * v[155 * s]) - (r[184 * s] * v[130 * s] * v[155 * s]) - (r[185 * s] * v[132 * s] * v[155 * s]) - (r[186 * s] * v[139 * s] * v[155 * s]) - (r[187 * s] * v[135 * s] * v[155 * s]) + (r[195 * s] * v[138 * s] * v[160 * s]) + (r[241 * s] * v[126 * s] * v[156 * s]) + 0x1.0000000000000p+1 * (r[245 * s] * v[127 * s] * v[155 * s] * v[156 * s]);
+}
+
+KQ_HD KQ_NOINLINE void kqu_fun_8(const double* v, const double* f, const double* r, double* vdot, long long s)
+{
+    vdot[156 * s] = 0.0 + (r[40 * s] * v[144 * s]) - (r[41 * s] * v[156 * s]) - (r[54 * s] * v[155 * s] * v[156 * s]) + (r[55 * s] * v[155 * s] * v[159 * s]) - (r[68 * s] * v[145 * s] * v[155 * s] * v[156 * s]) - (r[70 * s] * v[156 * s] * v[157 * s]) - (r[73 * s] * v[13 * s] * v[156 * s]) - (r[76 * s] * v[12 * s] * v[156 * s]) - (r[79 * s] * v[12 * s] * v[13 * s] * v[156 * s]) - (r[81 * s] * v[120 * s] * v[155 * s] * v[156 * s]) - (r[82 * s] * v[121 * s] * v[155 * s] * v[156 * s]) - (r[83 * s] * v[121 * s] * v[156 * s]) - (r[88 * s] * v[156 * s] * v[158 * s]) - (r[90 * s] * v[149 * s] * v[156 * s]) - (r[124 * s] * v[156 * s]) - (r[236 * s] * v[156 * s] * v[160 * s]) - (r[241 * s] * v[126 * s] * v[156 * s]) - (r[245 * s] * v[127 * s] * v[155 * s] * v[156 * s]) - (r[248 * s] * v[119 * s] * v[156 * s]) - (r[250 * s] * v[143 * s] * v[156 * s]) + (r[252 * s] * v[147 * s]) + (r[254 * s] * v[147 * s] * v[160 * s]);
+    vdot[157 * s] = 0.0 + (r[5 * s] * v[88 * s]) - (r[21 * s] * v[157 * s]) - (r[69 * s] * v[144 * s] * v[157 * s]) - (r[70 * s] * v[156 * s] * v[157 * s]) - (r[71 * s] * v[157 * s] * v[159 * s]) - (r[86 * s] * v[150 * s] * v[157 * s]) - (r[92 * s] * v[151 * s] * v[157 * s]) - (r[100 * s] * v[157 * s]);
+    vdot[158 * s] = 0.0 + (r[13 * s] * v[95 * s]) - (r[29 * s] * v[158 * s]) + -0x1.0000000000000p+1 * (r[87 * s] * v[144 * s] * v[158 * s]) + -0x1.0000000000000p+1 * (r[88 * s] * v[156 * s] * v[158 * s]) + -0x1.0000000000000p+1 * (r[89 * s] * v[158 * s] * v[159 * s]) + (r[93 * s] * v[151 * s] * v[160 * s]) + (r[94 * s] * v[125 * s] * v[160 * s]) - (r[132 * s] * v[158 * s]) + (r[231 * s] * v[146 * s]) - (r[237 * s] * v[154 * s] * v[158 * s]) - (r[238 * s] * v[150 * s] * v[158 * s]) + (r[239 * s] * v[149 * s]);
+    vdot[159 * s] = 0.0 + (r[41 * s] * v[156 * s]) - (r[55 * s] * v[155 * s] * v[159 * s]) - (r[71 * s] * v[157 * s] * v[159 * s]) - (r[74 * s] * v[13 * s] * v[159 * s]) - (r[77 * s] * v[12 * s] * v[159 * s]) - (r[80 * s] * v[12 * s] * v[13 * s] * v[159 * s]) - (r[89 * s] * v[158 * s] * v[159 * s]) - (r[125 * s] * v[159 * s]) - (r[251 * s] * v[143 * s] * v[159 * s]) + (r[253 * s] * v[147 * s] * v[152 * s]);
+}
+
+KQ_HD KQ_NOINLINE void kqu_fun_9(const double* v, const double* f, const double* r, double* vdot, long long s)
+{
+    vdot[160 * s] = 0.0 + (r[86 * s] * v[150 * s] * v[157 * s]) - (r[93 * s] * v[151 * s] * v[160 * s]) - (r[94 * s] * v[125 * s] * v[160 * s]) + (r[137 * s] * f[1 * s]) - (r[138 * s] * v[160 * s]) - (r[139 * s] * v[160 * s]) + 0x1.0000000000000p+1 * (r[192 * s] * v[145 * s]) - (r[193 * s] * v[104 * s] * v[160 * s]) - (r[194 * s] * v[104 * s] * v[160 * s]) - (r[195 * s] * v[138 * s] * v[160 * s]) - (r[196 * s] * v[139 * s] * v[160 * s]) - (r[197 * s] * v[105 * s] * v[160 * s]) - (r[198 * s] * v[136 * s] * v[160 * s]) - (r[199 * s] * v[140 * s] * v[160 * s]) + -0x1.0000000000000p+1 * (r[200 * s] * v[128 * s] * v[160 * s]) - (r[201 * s] * v[131 * s] * v[160 * s]) - (r[202 * s] * v[130 * s] * v[160 * s]) - (r[203 * s] * v[112 * s] * v[160 * s]) - (r[204 * s] * v[133 * s] * v[160 * s]) - (r[205 * s] * v[132 * s] * v[160 * s]) - (r[206 * s] * v[134 * s] * v[160 * s]) - (r[207 * s] * v[135 * s] * v[160 * s]) - (r[208 * s] * v[148 * s] * v[160 * s]) - (r[209 * s] * v[141 * s] * v[160 * s]) + (r[231 * s] * v[146 * s]) + -0x1.0000000000000p+1 * (r[232 * s] * v[160 * s] * v[160 * s]) - (r[233 * s] * v[154 * s] * v[160 * s]) - (r[234 * s] * v[150 * s] * v[160 * s]) - (r[235 * s] * v[145 * s] * v[160 * s]) - (r[236 * s] * v[156 * s] * v[160 * s]) + (r[246 * s] * v[122 * s] * f[0 * s]) - (r[249 * s] * v[137 * s] * v[160 * s]) - (r[254 * s] * v[147 * s] * v[160 * s]);
+}
+
+KQ_HD inline void kqu_fun(const double* v, const double* f, const double* r, double* vdot, long long s)
+{
+    kqu_fun_0(v, f, r, vdot, s);
+    kqu_fun_1(v, f, r, vdot, s);
+    kqu_fun_2(v, f, r, vdot, s);
+    kqu_fun_3(v, f, r, vdot, s);
+    kqu_fun_4(v, f, r, vdot, s);
+    kqu_fun_5(v, f, r, vdot, s);
+    kqu_fun_6(v, f, r, vdot, s);
+    kqu_fun_7(v, f, r, vdot, s);
+    kqu_fun_8(v, f, r, vdot, s);
+    kqu_fun_9(v, f, r, vdot, s);
+}
+
+KQ_HD KQ_NOINLINE void kqu_jac_0(const double* v, const double* f, const double* r, double* jvs, long long s)
+{
+    jvs[0 * s] = 0.0 - (r[32 * s]);
+    jvs[1 * s] = 0.0 - (r[33 * s]);
+    jvs[2 * s] = 0.0 - (r[34 * s]);
+    jvs[3 * s] = 0.0 - (r[35 * s]);
+    jvs[4 * s] = 0.0 - (r[36 * s]);
+    jvs[5 * s] = 0.0 - (r[37 * s]);
+    jvs[6 * s] = 0.0 - (r[38 * s]);
+    jvs[7 * s] = 0.0 - (r[39 * s]);
+    jvs[8 * s] = 0.0 + (r[39 * s]);
+    jvs[9 * s] = 0.0 - (r[112 * s]);
+    jvs[10 * s] = 0.0 + (r[37 * s]);
+    jvs[11 * s] = 0.0 - (r[113 * s]);
+    jvs[12 * s] = 0.0 - (r[114 * s]);
+    jvs[13 * s] = 0.0 + (r[38 * s]);
+    jvs[14 * s] = 0.0 - (r[115 * s]);
+    jvs[15 * s] = 0.0 - (r[120 * s]);
+    jvs[16 * s] = 0.0 - (r[121 * s]);
+    jvs[17 * s] = 0.0 - (r[116 * s]);
+    jvs[18 * s] = 0.0 - (r[117 * s]);
+    jvs[19 * s] = 0.0 - (r[118 * s]);
+    jvs[20 * s] = 0.0 + (r[35 * s]);
+    jvs[21 * s] = 0.0 - (r[119 * s]);
     jvs[22 * s] = 0.0;
-    jvs[23 * s] = 0.0 + b358;
-    jvs[24 * s] = 0.0 + b357;
-    jvs[25 * s] = 0.0 + b361;
-    jvs[26 * s] = 0.0 + b360;
-    jvs[27 * s] = 0.0 + b139;
-    jvs[28 * s] = 0.0 + b359;
-    jvs[29 * s] = 0.0 + b168;
-    jvs[30 * s] = 0.0 + b169;
+    jvs[23 * s] = 0.0 + (r[263 * s]);
+    jvs[24 * s] = 0.0 + (r[262 * s]);
+    jvs[25 * s] = 0.0 + (r[266 * s]);
+    jvs[26 * s] = 0.0 + (r[265 * s]);
+    jvs[27 * s] = 0.0 + (r[95 * s]);
+    jvs[28 * s] = 0.0 + (r[264 * s]);
+    jvs[29 * s] = 0.0 + (r[124 * s]);
+    jvs[30 * s] = 0.0 + (r[125 * s]);
     jvs[31 * s] = 0.0;
-    jvs[32 * s] = 0.0 + b140;
+    jvs[32 * s] = 0.0 + (r[96 * s]);
     jvs[33 * s] = 0.0;
-    jvs[34 * s] = 0.0 + b362;
-    jvs[35 * s] = 0.0 + b171;
-    jvs[36 * s] = 0.0 + b170;
-    jvs[37 * s] = 0.0 + b141;
-    jvs[38 * s] = 0.0 - b362;
-    jvs[39 * s] = 0.0 + b267;
-    jvs[40 * s] = 0.0 + b265;
-    jvs[41 * s] = 0.0 + b266 + b268;
+    jvs[34 * s] = 0.0 + (r[267 * s]);
+    jvs[35 * s] = 0.0 + (r[127 * s]);
+    jvs[36 * s] = 0.0 + (r[126 * s]);
+    jvs[37 * s] = 0.0 + (r[97 * s]);
+    jvs[38 * s] = 0.0 - (r[267 * s]);
+    jvs[39 * s] = 0.0 + (r[202 * s] * v[160 * s]);
+    jvs[40 * s] = 0.0 + (r[201 * s] * v[160 * s]);
+    jvs[41 * s] = 0.0 + (r[201 * s] * v[131 * s]) + (r[202 * s] * v[130 * s]);
     jvs[42 * s] = 0.0;
-    jvs[43 * s] = 0.0 + b142;
+    jvs[43 * s] = 0.0 + (r[98 * s]);
     jvs[44 * s] = 0.0;
-    jvs[45 * s] = 0.0 + b143;
+    jvs[45 * s] = 0.0 + (r[99 * s]);
     jvs[46 * s] = 0.0;
-    jvs[47 * s] = 0.0 + b144;
+    jvs[47 * s] = 0.0 + (r[100 * s]);
     jvs[48 * s] = 0.0;
-    jvs[49 * s] = 0.0 + b172;
-    jvs[50 * s] = 0.0 + b145;
+    jvs[49 * s] = 0.0 + (r[128 * s]);
+    jvs[50 * s] = 0.0 + (r[101 * s]);
     jvs[51 * s] = 0.0;
-    jvs[52 * s] = 0.0 + b146;
+    jvs[52 * s] = 0.0 + (r[102 * s]);
     jvs[53 * s] = 0.0;
-    jvs[54 * s] = 0.0 + b147;
+    jvs[54 * s] = 0.0 + (r[103 * s]);
     jvs[55 * s] = 0.0;
-    jvs[56 * s] = 0.0 + b148;
-    jvs[57 * s] = 0.0 + b173;
-    jvs[58 * s] = 0.0 + b152;
+    jvs[56 * s] = 0.0 + (r[104 * s]);
+    jvs[57 * s] = 0.0 + (r[129 * s]);
+    jvs[58 * s] = 0.0 + (r[108 * s]);
     jvs[59 * s] = 0.0;
-    jvs[60 * s] = 0.0 + b149;
+    jvs[60 * s] = 0.0 + (r[105 * s]);
     jvs[61 * s] = 0.0;
-    jvs[62 * s] = 0.0 + b150;
+    jvs[62 * s] = 0.0 + (r[106 * s]);
     jvs[63 * s] = 0.0;
-    jvs[64 * s] = 0.0 + b151;
+    jvs[64 * s] = 0.0 + (r[107 * s]);
     jvs[65 * s] = 0.0;
-    jvs[66 * s] = 0.0 + b182;
+    jvs[66 * s] = 0.0 + (r[139 * s]);
     jvs[67 * s] = 0.0;
-    jvs[68 * s] = 0.0 + b153;
+    jvs[68 * s] = 0.0 + (r[109 * s]);
     jvs[69 * s] = 0.0;
-    jvs[70 * s] = 0.0 + b154;
+    jvs[70 * s] = 0.0 + (r[110 * s]);
     jvs[71 * s] = 0.0;
-    jvs[72 * s] = 0.0 + b155;
-    jvs[73 * s] = 0.0 + b156;
+    jvs[72 * s] = 0.0 + (r[111 * s]);
+    jvs[73 * s] = 0.0 + (r[112 * s]);
     jvs[74 * s] = 0.0;
-    jvs[75 * s] = 0.0 + b164;
+    jvs[75 * s] = 0.0 + (r[120 * s]);
     jvs[76 * s] = 0.0;
-    jvs[77 * s] = 0.0 + b165;
+    jvs[77 * s] = 0.0 + (r[121 * s]);
     jvs[78 * s] = 0.0;
-    jvs[79 * s] = 0.0 + b157;
+    jvs[79 * s] = 0.0 + (r[113 * s]);
     jvs[80 * s] = 0.0;
-    jvs[81 * s] = 0.0 + b158;
+    jvs[81 * s] = 0.0 + (r[114 * s]);
     jvs[82 * s] = 0.0;
-    jvs[83 * s] = 0.0 + b159;
+    jvs[83 * s] = 0.0 + (r[115 * s]);
     jvs[84 * s] = 0.0;
     jvs[85 * s] = 0.0;
-    jvs[86 * s] = 0.0 + b166;
-    jvs[87 * s] = 0.0 + b160;
+    jvs[86 * s] = 0.0 + (r[122 * s]);
+    jvs[87 * s] = 0.0 + (r[116 * s]);
     jvs[88 * s] = 0.0;
-    jvs[89 * s] = 0.0 + b161;
+    jvs[89 * s] = 0.0 + (r[117 * s]);
     jvs[90 * s] = 0.0;
-    jvs[91 * s] = 0.0 + b162;
+    jvs[91 * s] = 0.0 + (r[118 * s]);
     jvs[92 * s] = 0.0;
-    jvs[93 * s] = 0.0 + b163;
+    jvs[93 * s] = 0.0 + (r[119 * s]);
     jvs[94 * s] = 0.0;
     jvs[95 * s] = 0.0;
-    jvs[96 * s] = 0.0 + b176;
+    jvs[96 * s] = 0.0 + (r[132 * s]);
     jvs[97 * s] = 0.0;
-    jvs[98 * s] = 0.0 + b177;
-    jvs[99 * s] = 0.0 + b178;
+    jvs[98 * s] = 0.0 + (r[133 * s]);
+    jvs[99 * s] = 0.0 + (r[134 * s]);
     jvs[100 * s] = 0.0;
-    jvs[101 * s] = 0.0 + b179;
-    jvs[102 * s] = 0.0 + b180;
+    jvs[101 * s] = 0.0 + (r[135 * s]);
+    jvs[102 * s] = 0.0 + (r[136 * s]);
     jvs[103 * s] = 0.0;
-    jvs[104 * s] = 0.0 + b207;
+    jvs[104 * s] = 0.0 + (r[157 * s]);
     jvs[105 * s] = 0.0;
-    jvs[106 * s] = 0.0 + b215;
-    jvs[107 * s] = 0.0 + b208;
-    jvs[108 * s] = 0.0 - b215;
-    jvs[109 * s] = 0.0 + b196 + b197 + b199;
-    jvs[110 * s] = 0.0 + b200;
-    jvs[111 * s] = 0.0 + b198;
+    jvs[106 * s] = 0.0 + (r[165 * s]);
+    jvs[107 * s] = 0.0 + (r[158 * s]);
+    jvs[108 * s] = 0.0 - (r[165 * s]);
+    jvs[109 * s] = 0.0 + (r[150 * s] * f[0 * s]) + (r[151 * s] * v[153 * s]) + (r[152 * s] * v[146 * s]);
+    jvs[110 * s] = 0.0 + (r[152 * s] * v[115 * s]);
+}
+
+KQ_HD KQ_NOINLINE void kqu_jac_1(const double* v, const double* f, const double* r, double* jvs, long long s)
+{
+    jvs[111 * s] = 0.0 + (r[151 * s] * v[115 * s]);
     jvs[112 * s] = 0.0;
-    jvs[113 * s] = 0.0 + b209;
+    jvs[113 * s] = 0.0 + (r[159 * s]);
     jvs[114 * s] = 0.0;
-    jvs[115 * s] = 0.0 + b210;
-    jvs[116 * s] = 0.0 - b210;
-    jvs[117 * s] = 0.0 + b192;
-    jvs[118 * s] = 0.0 + b194;
-    jvs[119 * s] = 0.0 + b193 + b195;
+    jvs[115 * s] = 0.0 + (r[160 * s]);
+    jvs[116 * s] = 0.0 - (r[160 * s]);
+    jvs[117 * s] = 0.0 + (r[148 * s] * v[115 * s]);
+    jvs[118 * s] = 0.0 + (r[149 * s] * v[115 * s]);
+    jvs[119 * s] = 0.0 + (r[148 * s] * v[101 * s]) + (r[149 * s] * v[102 * s]);
     jvs[120 * s] = 0.0;
-    jvs[121 * s] = 0.0 + b211;
+    jvs[121 * s] = 0.0 + (r[161 * s]);
     jvs[122 * s] = 0.0;
-    jvs[123 * s] = 0.0 + b212;
+    jvs[123 * s] = 0.0 + (r[162 * s]);
     jvs[124 * s] = 0.0;
-    jvs[125 * s] = 0.0 + b213;
-    jvs[126 * s] = 0.0 - b213;
-    jvs[127 * s] = 0.0 + b201;
-    jvs[128 * s] = 0.0 + b204;
+    jvs[125 * s] = 0.0 + (r[163 * s]);
+    jvs[126 * s] = 0.0 - (r[163 * s]);
+    jvs[127 * s] = 0.0 + (r[153 * s] * f[0 * s]);
+    jvs[128 * s] = 0.0 + (r[155 * s] * f[0 * s]);
     jvs[129 * s] = 0.0;
-    jvs[130 * s] = 0.0 + b214;
-    jvs[131 * s] = 0.0 - b214;
-    jvs[132 * s] = 0.0 + b202;
-    jvs[133 * s] = 0.0 + b205;
-    jvs[134 * s] = 0.0 + b203 + b206;
+    jvs[130 * s] = 0.0 + (r[164 * s]);
+    jvs[131 * s] = 0.0 - (r[164 * s]);
+    jvs[132 * s] = 0.0 + (r[154 * s] * v[153 * s]);
+    jvs[133 * s] = 0.0 + (r[156 * s] * v[153 * s]);
+    jvs[134 * s] = 0.0 + (r[154 * s] * v[75 * s]) + (r[156 * s] * v[77 * s]);
     jvs[135 * s] = 0.0;
-    jvs[136 * s] = 0.0 + b285;
-    jvs[137 * s] = 0.0 + b286;
+    jvs[136 * s] = 0.0 + (r[211 * s]);
+    jvs[137 * s] = 0.0 + (r[212 * s]);
     jvs[138 * s] = 0.0;
-    jvs[139 * s] = 0.0 + b287;
-    jvs[140 * s] = 0.0 + b289;
-    jvs[141 * s] = 0.0 + b288;
+    jvs[139 * s] = 0.0 + (r[213 * s]);
+    jvs[140 * s] = 0.0 + (r[215 * s]);
+    jvs[141 * s] = 0.0 + (r[214 * s]);
     jvs[142 * s] = 0.0;
-    jvs[143 * s] = 0.0 + b291;
-    jvs[144 * s] = 0.0 + b290;
+    jvs[143 * s] = 0.0 + (r[217 * s]);
+    jvs[144 * s] = 0.0 + (r[216 * s]);
     jvs[145 * s] = 0.0;
-    jvs[146 * s] = 0.0 + b292;
-    jvs[147 * s] = 0.0 + b293;
+    jvs[146 * s] = 0.0 + (r[218 * s]);
+    jvs[147 * s] = 0.0 + (r[219 * s]);
     jvs[148 * s] = 0.0;
-    jvs[149 * s] = 0.0 + b298;
-    jvs[150 * s] = 0.0 + b359;
-    jvs[151 * s] = 0.0 + b294;
+    jvs[149 * s] = 0.0 + (r[224 * s]);
+    jvs[150 * s] = 0.0 + (r[264 * s]);
+    jvs[151 * s] = 0.0 + (r[220 * s]);
     jvs[152 * s] = 0.0;
-    jvs[153 * s] = 0.0 + b174;
-    jvs[154 * s] = 0.0 + b175;
+    jvs[153 * s] = 0.0 + (r[130 * s]);
+    jvs[154 * s] = 0.0 + (r[131 * s]);
     jvs[155 * s] = 0.0;
-    jvs[156 * s] = 0.0 + b295;
+    jvs[156 * s] = 0.0 + (r[221 * s]);
     jvs[157 * s] = 0.0;
-    jvs[158 * s] = 0.0 + b296;
-    jvs[159 * s] = 0.0 + b297;
+    jvs[158 * s] = 0.0 + (r[222 * s]);
+    jvs[159 * s] = 0.0 + (r[223 * s]);
     jvs[160 * s] = 0.0;
-    jvs[161 * s] = 0.0 + b300;
-    jvs[162 * s] = 0.0 + b363;
-    jvs[163 * s] = 0.0 + b299;
+    jvs[161 * s] = 0.0 + (r[226 * s]);
+    jvs[162 * s] = 0.0 + (r[268 * s]);
+    jvs[163 * s] = 0.0 + (r[225 * s]);
     jvs[164 * s] = 0.0;
-    jvs[165 * s] = 0.0 + b355;
+    jvs[165 * s] = 0.0 + (r[260 * s]);
     jvs[166 * s] = 0.0;
-    jvs[167 * s] = 0.0 + b356;
-    jvs[168 * s] = 0.0 - b14;
-    jvs[169 * s] = 0.0 + b30;
-    jvs[170 * s] = 0.0 - b184;
-    jvs[171 * s] = 0.0 + b187;
-    jvs[172 * s] = 0.0 + b184;
-    jvs[173 * s] = 0.0 - b187 - b201 - b202 - b211;
-    jvs[174 * s] = 0.0 - b203;
-    jvs[175 * s] = 0.0 - b185;
-    jvs[176 * s] = 0.0 + b188;
-    jvs[177 * s] = 0.0 + b185;
-    jvs[178 * s] = 0.0 - b188 - b204 - b205 - b212;
-    jvs[179 * s] = 0.0 - b206;
-    jvs[180 * s] = 0.0 - b216;
-    jvs[181 * s] = 0.0 + b221;
-    jvs[182 * s] = 0.0 - b217;
-    jvs[183 * s] = 0.0 + b222;
-    jvs[184 * s] = 0.0 - b218;
-    jvs[185 * s] = 0.0 + b223;
-    jvs[186 * s] = 0.0 - b12;
-    jvs[187 * s] = 0.0 + b28;
-    jvs[188 * s] = 0.0 - b220;
-    jvs[189 * s] = 0.0 + b225;
-    jvs[190 * s] = 0.0 - b219;
-    jvs[191 * s] = 0.0 + b224;
-    jvs[192 * s] = 0.0 - b4;
-    jvs[193 * s] = 0.0 + b20;
-    jvs[194 * s] = 0.0 - b1;
-    jvs[195 * s] = 0.0 + b17;
-    jvs[196 * s] = 0.0 - b2;
-    jvs[197 * s] = 0.0 + b18;
-    jvs[198 * s] = 0.0 - b3;
-    jvs[199 * s] = 0.0 + b19;
-    jvs[200 * s] = 0.0 - b5;
-    jvs[201 * s] = 0.0 + b21;
-    jvs[202 * s] = 0.0 - b6;
-    jvs[203 * s] = 0.0 + b22;
-    jvs[204 * s] = 0.0 - b7;
-    jvs[205 * s] = 0.0 + b23;
-    jvs[206 * s] = 0.0 - b8;
-    jvs[207 * s] = 0.0 + b24;
-    jvs[208 * s] = 0.0 - b9;
-    jvs[209 * s] = 0.0 + b25;
-    jvs[210 * s] = 0.0 - b10;
-    jvs[211 * s] = 0.0 + b26;
-    jvs[212 * s] = 0.0 - b11;
-    jvs[213 * s] = 0.0 + b27;
-    jvs[214 * s] = 0.0 - b13;
-    jvs[215 * s] = 0.0 + b29;
-    jvs[216 * s] = 0.0 - b15;
-    jvs[217 * s] = 0.0 + b31;
-    jvs[218 * s] = 0.0 - b301;
-    jvs[219 * s] = 0.0 + b303;
-    jvs[220 * s] = 0.0 - b302;
-    jvs[221 * s] = 0.0 + b304;
-    jvs[222 * s] = 0.0 - b0;
-    jvs[223 * s] = 0.0 + b16;
-    jvs[224 * s] = 0.0 - b183;
-    jvs[225 * s] = 0.0 + b186;
-    jvs[226 * s] = 0.0 - b192 - b208;
-    jvs[227 * s] = 0.0 + b189 - b193;
-    jvs[228 * s] = 0.0 - b194 - b209;
-    jvs[229 * s] = 0.0 + b190 - b195;
-    jvs[230 * s] = 0.0 + b191;
-    jvs[231 * s] = 0.0 - b324 - b358;
-    jvs[232 * s] = 0.0 + b333;
-    jvs[233 * s] = 0.0 + b322;
-    jvs[234 * s] = 0.0 + b313 + b323 + b334;
-    jvs[235 * s] = 0.0 + b314;
-    jvs[236 * s] = 0.0 + b216;
-    jvs[237 * s] = 0.0 - b221 - b249 - b251 - b295;
-    jvs[238 * s] = 0.0 - b250 - b252;
-    jvs[239 * s] = 0.0 + b10;
-    jvs[240 * s] = 0.0 + b251;
-    jvs[241 * s] = 0.0 - b26 - b150 - b257;
-    jvs[242 * s] = 0.0 + b252 - b258;
-    jvs[243 * s] = 0.0 + b1;
-    jvs[244 * s] = 0.0 - b17 - b42 - b140;
-    jvs[245 * s] = 0.0 + b57;
-    jvs[246 * s] = 0.0 + b58;
-    jvs[247 * s] = 0.0 + b3;
-    jvs[248 * s] = 0.0 - b19 - b45 - b142;
-    jvs[249 * s] = 0.0 + b63;
-    jvs[250 * s] = 0.0 + b64;
-    jvs[251 * s] = 0.0 + b33;
-    jvs[252 * s] = 0.0 + b45;
-    jvs[253 * s] = 0.0 - b63 - b154;
-    jvs[254 * s] = 0.0 - b64;
-    jvs[255 * s] = 0.0 - b48 - b148;
-    jvs[256 * s] = 0.0 + b71;
-    jvs[257 * s] = 0.0 + b72;
-    jvs[258 * s] = 0.0 + b9;
-    jvs[259 * s] = 0.0 - b25 - b47 - b149;
-    jvs[260 * s] = 0.0 + b67;
-    jvs[261 * s] = 0.0 + b68;
-    jvs[262 * s] = 0.0 + b34;
-    jvs[263 * s] = 0.0 + b47;
-    jvs[264 * s] = 0.0 - b67 - b155;
-    jvs[265 * s] = 0.0 - b68;
-    jvs[266 * s] = 0.0 + b11;
-    jvs[267 * s] = 0.0 - b27 - b151 - b269;
-    jvs[268 * s] = 0.0 - b270;
-    jvs[269 * s] = 0.0 - b61 - b171;
-    jvs[270 * s] = 0.0 + b44;
-    jvs[271 * s] = 0.0 - b62;
-    jvs[272 * s] = 0.0 + b61;
-    jvs[273 * s] = 0.0 - b44 - b59 - b170;
-    jvs[274 * s] = 0.0 + b43;
-    jvs[275 * s] = 0.0 - b60 + b62;
-    jvs[276 * s] = 0.0 + b183;
-    jvs[277 * s] = 0.0 - b192;
-    jvs[278 * s] = 0.0 - b194;
-    jvs[279 * s] = 0.0 - b186 - b189 - b190 - b193 - b195 - b196 - b197 - b199 - b207;
-    jvs[280 * s] = 0.0 - b200;
-    jvs[281 * s] = 0.0 - b191 - b198;
-    jvs[282 * s] = 0.0 - b247 - b283 - b300;
-    jvs[283 * s] = 0.0 + b351;
-    jvs[284 * s] = 0.0 + b246;
-    jvs[285 * s] = 0.0 + b352;
-    jvs[286 * s] = 0.0 - b284;
-    jvs[287 * s] = 0.0 - b350 - b351 - b353 - b363;
-    jvs[288 * s] = 0.0 + b346 + b348;
-    jvs[289 * s] = 0.0 - b352;
-    jvs[290 * s] = 0.0 + b347;
-    jvs[291 * s] = 0.0 + b349;
-    jvs[292 * s] = 0.0 - b354;
-    jvs[293 * s] = 0.0 + b219;
-    jvs[294 * s] = 0.0 + b247;
-    jvs[295 * s] = 0.0 + b350;
-    jvs[296 * s] = 0.0 - b224 - b246 - b299 - b346 - b348;
+    jvs[167 * s] = 0.0 + (r[261 * s]);
+    jvs[168 * s] = 0.0 - (r[14 * s]);
+    jvs[169 * s] = 0.0 + (r[30 * s]);
+    jvs[170 * s] = 0.0 - (r[141 * s]);
+    jvs[171 * s] = 0.0 + (r[144 * s]);
+    jvs[172 * s] = 0.0 + (r[141 * s]);
+    jvs[173 * s] = 0.0 - (r[144 * s]) - (r[153 * s] * f[0 * s]) - (r[154 * s] * v[153 * s]) - (r[161 * s]);
+    jvs[174 * s] = 0.0 - (r[154 * s] * v[75 * s]);
+    jvs[175 * s] = 0.0 - (r[142 * s]);
+    jvs[176 * s] = 0.0 + (r[145 * s]);
+    jvs[177 * s] = 0.0 + (r[142 * s]);
+    jvs[178 * s] = 0.0 - (r[145 * s]) - (r[155 * s] * f[0 * s]) - (r[156 * s] * v[153 * s]) - (r[162 * s]);
+    jvs[179 * s] = 0.0 - (r[156 * s] * v[77 * s]);
+    jvs[180 * s] = 0.0 - (r[166 * s]);
+    jvs[181 * s] = 0.0 + (r[171 * s]);
+    jvs[182 * s] = 0.0 - (r[167 * s]);
+    jvs[183 * s] = 0.0 + (r[172 * s]);
+    jvs[184 * s] = 0.0 - (r[168 * s]);
+    jvs[185 * s] = 0.0 + (r[173 * s]);
+    jvs[186 * s] = 0.0 - (r[12 * s]);
+    jvs[187 * s] = 0.0 + (r[28 * s]);
+    jvs[188 * s] = 0.0 - (r[170 * s]);
+    jvs[189 * s] = 0.0 + (r[175 * s]);
+    jvs[190 * s] = 0.0 - (r[169 * s]);
+    jvs[191 * s] = 0.0 + (r[174 * s]);
+    jvs[192 * s] = 0.0 - (r[4 * s]);
+    jvs[193 * s] = 0.0 + (r[20 * s]);
+    jvs[194 * s] = 0.0 - (r[1 * s]);
+    jvs[195 * s] = 0.0 + (r[17 * s]);
+    jvs[196 * s] = 0.0 - (r[2 * s]);
+    jvs[197 * s] = 0.0 + (r[18 * s]);
+    jvs[198 * s] = 0.0 - (r[3 * s]);
+    jvs[199 * s] = 0.0 + (r[19 * s]);
+    jvs[200 * s] = 0.0 - (r[5 * s]);
+    jvs[201 * s] = 0.0 + (r[21 * s]);
+    jvs[202 * s] = 0.0 - (r[6 * s]);
+    jvs[203 * s] = 0.0 + (r[22 * s]);
+    jvs[204 * s] = 0.0 - (r[7 * s]);
+    jvs[205 * s] = 0.0 + (r[23 * s]);
+    jvs[206 * s] = 0.0 - (r[8 * s]);
+}
+
+KQ_HD KQ_NOINLINE void kqu_jac_2(const double* v, const double* f, const double* r, double* jvs, long long s)
+{
+    jvs[207 * s] = 0.0 + (r[24 * s]);
+    jvs[208 * s] = 0.0 - (r[9 * s]);
+    jvs[209 * s] = 0.0 + (r[25 * s]);
+    jvs[210 * s] = 0.0 - (r[10 * s]);
+    jvs[211 * s] = 0.0 + (r[26 * s]);
+    jvs[212 * s] = 0.0 - (r[11 * s]);
+    jvs[213 * s] = 0.0 + (r[27 * s]);
+    jvs[214 * s] = 0.0 - (r[13 * s]);
+    jvs[215 * s] = 0.0 + (r[29 * s]);
+    jvs[216 * s] = 0.0 - (r[15 * s]);
+    jvs[217 * s] = 0.0 + (r[31 * s]);
+    jvs[218 * s] = 0.0 - (r[227 * s]);
+    jvs[219 * s] = 0.0 + (r[229 * s]);
+    jvs[220 * s] = 0.0 - (r[228 * s]);
+    jvs[221 * s] = 0.0 + (r[230 * s]);
+    jvs[222 * s] = 0.0 - (r[0 * s]);
+    jvs[223 * s] = 0.0 + (r[16 * s]);
+    jvs[224 * s] = 0.0 - (r[140 * s]);
+    jvs[225 * s] = 0.0 + (r[143 * s]);
+    jvs[226 * s] = 0.0 - (r[148 * s] * v[115 * s]) - (r[158 * s]);
+    jvs[227 * s] = 0.0 + (r[146 * s] * f[0 * s]) - (r[148 * s] * v[101 * s]);
+    jvs[228 * s] = 0.0 - (r[149 * s] * v[115 * s]) - (r[159 * s]);
+    jvs[229 * s] = 0.0 + (r[147 * s] * v[153 * s]) - (r[149 * s] * v[102 * s]);
+    jvs[230 * s] = 0.0 + (r[147 * s] * v[115 * s]);
+    jvs[231 * s] = 0.0 - (r[242 * s] * f[2 * s]) - (r[263 * s]);
+    jvs[232 * s] = 0.0 + (r[248 * s] * v[156 * s]);
+    jvs[233 * s] = 0.0 + (r[241 * s] * v[156 * s]);
+    jvs[234 * s] = 0.0 + (r[236 * s] * v[160 * s]) + (r[241 * s] * v[126 * s]) + (r[248 * s] * v[119 * s]);
+    jvs[235 * s] = 0.0 + (r[236 * s] * v[156 * s]);
+    jvs[236 * s] = 0.0 + (r[166 * s]);
+    jvs[237 * s] = 0.0 - (r[171 * s]) - (r[193 * s] * v[160 * s]) - (r[194 * s] * v[160 * s]) - (r[221 * s]);
+    jvs[238 * s] = 0.0 - (r[193 * s] * v[104 * s]) - (r[194 * s] * v[104 * s]);
+    jvs[239 * s] = 0.0 + (r[10 * s]);
+    jvs[240 * s] = 0.0 + (r[194 * s] * v[160 * s]);
+    jvs[241 * s] = 0.0 - (r[26 * s]) - (r[106 * s]) - (r[197 * s] * v[160 * s]);
+    jvs[242 * s] = 0.0 + (r[194 * s] * v[104 * s]) - (r[197 * s] * v[105 * s]);
+    jvs[243 * s] = 0.0 + (r[1 * s]);
+    jvs[244 * s] = 0.0 - (r[17 * s]) - (r[42 * s]) - (r[96 * s]);
+    jvs[245 * s] = 0.0 + (r[56 * s] * v[155 * s]);
+    jvs[246 * s] = 0.0 + (r[56 * s] * v[146 * s]);
+    jvs[247 * s] = 0.0 + (r[3 * s]);
+    jvs[248 * s] = 0.0 - (r[19 * s]) - (r[45 * s]) - (r[98 * s]);
+    jvs[249 * s] = 0.0 + (r[59 * s] * v[152 * s]);
+    jvs[250 * s] = 0.0 + (r[59 * s] * v[108 * s]);
+    jvs[251 * s] = 0.0 + (r[33 * s]);
+    jvs[252 * s] = 0.0 + (r[45 * s]);
+    jvs[253 * s] = 0.0 - (r[59 * s] * v[152 * s]) - (r[110 * s]);
+    jvs[254 * s] = 0.0 - (r[59 * s] * v[108 * s]);
+    jvs[255 * s] = 0.0 - (r[49 * s]) - (r[104 * s]);
+    jvs[256 * s] = 0.0 + (r[63 * s] * v[155 * s]);
+    jvs[257 * s] = 0.0 + (r[63 * s] * v[123 * s]);
+    jvs[258 * s] = 0.0 + (r[9 * s]);
+    jvs[259 * s] = 0.0 - (r[25 * s]) - (r[47 * s]) - (r[105 * s]);
+    jvs[260 * s] = 0.0 + (r[61 * s] * v[155 * s]);
+    jvs[261 * s] = 0.0 + (r[61 * s] * v[111 * s]);
+    jvs[262 * s] = 0.0 + (r[34 * s]);
+    jvs[263 * s] = 0.0 + (r[47 * s]);
+    jvs[264 * s] = 0.0 - (r[61 * s] * v[155 * s]) - (r[111 * s]);
+    jvs[265 * s] = 0.0 - (r[61 * s] * v[111 * s]);
+    jvs[266 * s] = 0.0 + (r[11 * s]);
+    jvs[267 * s] = 0.0 - (r[27 * s]) - (r[107 * s]) - (r[203 * s] * v[160 * s]);
+    jvs[268 * s] = 0.0 - (r[203 * s] * v[112 * s]);
+    jvs[269 * s] = 0.0 - (r[58 * s] * v[155 * s]) - (r[127 * s]);
+    jvs[270 * s] = 0.0 + (r[44 * s]);
+    jvs[271 * s] = 0.0 - (r[58 * s] * v[113 * s]);
+    jvs[272 * s] = 0.0 + (r[58 * s] * v[155 * s]);
+}
+
+KQ_HD KQ_NOINLINE void kqu_jac_3(const double* v, const double* f, const double* r, double* jvs, long long s)
+{
+    jvs[273 * s] = 0.0 - (r[44 * s]) - (r[57 * s] * v[155 * s]) - (r[126 * s]);
+    jvs[274 * s] = 0.0 + (r[43 * s]);
+    jvs[275 * s] = 0.0 - (r[57 * s] * v[114 * s]) + (r[58 * s] * v[113 * s]);
+    jvs[276 * s] = 0.0 + (r[140 * s]);
+    jvs[277 * s] = 0.0 - (r[148 * s] * v[115 * s]);
+    jvs[278 * s] = 0.0 - (r[149 * s] * v[115 * s]);
+    jvs[279 * s] = 0.0 - (r[143 * s]) - (r[146 * s] * f[0 * s]) - (r[147 * s] * v[153 * s]) - (r[148 * s] * v[101 * s]) - (r[149 * s] * v[102 * s]) - (r[150 * s] * f[0 * s]) - (r[151 * s] * v[153 * s]) - (r[152 * s] * v[146 * s]) - (r[157 * s]);
+    jvs[280 * s] = 0.0 - (r[152 * s] * v[115 * s]);
+    jvs[281 * s] = 0.0 - (r[147 * s] * v[115 * s]) - (r[151 * s] * v[115 * s]);
+    jvs[282 * s] = 0.0 - (r[191 * s]) - (r[210 * s] * v[160 * s]) - (r[226 * s]);
+    jvs[283 * s] = 0.0 + (r[258 * s] * v[152 * s]);
+    jvs[284 * s] = 0.0 + (r[190 * s] * f[0 * s]);
+    jvs[285 * s] = 0.0 + (r[258 * s] * v[117 * s]);
+    jvs[286 * s] = 0.0 - (r[210 * s] * v[116 * s]);
+    jvs[287 * s] = 0.0 - (r[257 * s]) - (r[258 * s] * v[152 * s]) - (r[259 * s] * v[160 * s]) - (r[268 * s]);
+    jvs[288 * s] = 0.0 + (r[255 * s] * v[156 * s]) + (r[256 * s] * v[159 * s]);
+    jvs[289 * s] = 0.0 - (r[258 * s] * v[117 * s]);
+    jvs[290 * s] = 0.0 + (r[255 * s] * v[118 * s]);
+    jvs[291 * s] = 0.0 + (r[256 * s] * v[118 * s]);
+    jvs[292 * s] = 0.0 - (r[259 * s] * v[117 * s]);
+    jvs[293 * s] = 0.0 + (r[169 * s]);
+    jvs[294 * s] = 0.0 + (r[191 * s]);
+    jvs[295 * s] = 0.0 + (r[257 * s]);
+    jvs[296 * s] = 0.0 - (r[174 * s]) - (r[190 * s] * f[0 * s]) - (r[225 * s]) - (r[255 * s] * v[156 * s]) - (r[256 * s] * v[159 * s]);
     jvs[297 * s] = 0.0;
-    jvs[298 * s] = 0.0 - b347;
-    jvs[299 * s] = 0.0 - b349;
+    jvs[298 * s] = 0.0 - (r[255 * s] * v[118 * s]);
+    jvs[299 * s] = 0.0 - (r[256 * s] * v[118 * s]);
     jvs[300 * s] = 0.0;
-    jvs[301 * s] = 0.0 + b302;
-    jvs[302 * s] = 0.0 - b304 + -0x1.0000000000000p+1 * b332 - b333 - b356;
-    jvs[303 * s] = 0.0 - b334;
-    jvs[304 * s] = 0.0 + b7;
-    jvs[305 * s] = 0.0 + b333;
-    jvs[306 * s] = 0.0 - b23 - b111 - b146;
-    jvs[307 * s] = 0.0 - b112;
-    jvs[308 * s] = 0.0 - b113 + b334;
-    jvs[309 * s] = 0.0 + b8;
-    jvs[310 * s] = 0.0 - b24 - b114 - b117 - b147;
-    jvs[311 * s] = 0.0 - b115;
-    jvs[312 * s] = 0.0 - b116 - b118;
-    jvs[313 * s] = 0.0 - b331 - b357;
-    jvs[314 * s] = 0.0 + b320;
-    jvs[315 * s] = 0.0 + 0x1.0000000000000p+1 * b327;
-    jvs[316 * s] = 0.0 + b321;
-    jvs[317 * s] = 0.0 + b48;
-    jvs[318 * s] = 0.0 + b331;
-    jvs[319 * s] = 0.0 - b49 - b71 - b173;
+    jvs[301 * s] = 0.0 + (r[228 * s]);
+    jvs[302 * s] = 0.0 - (r[230 * s]) + -0x1.0000000000000p+1 * (r[247 * s] * 0x1.0000000000000p+1 * v[119 * s]) - (r[248 * s] * v[156 * s]) - (r[261 * s]);
+    jvs[303 * s] = 0.0 - (r[248 * s] * v[119 * s]);
+    jvs[304 * s] = 0.0 + (r[7 * s]);
+    jvs[305 * s] = 0.0 + (r[248 * s] * v[156 * s]);
+    jvs[306 * s] = 0.0 - (r[23 * s]) - (r[81 * s] * v[155 * s] * v[156 * s]) - (r[102 * s]);
+    jvs[307 * s] = 0.0 - (r[81 * s] * v[120 * s] * v[156 * s]);
+    jvs[308 * s] = 0.0 - (r[81 * s] * v[120 * s] * v[155 * s]) + (r[248 * s] * v[119 * s]);
+    jvs[309 * s] = 0.0 + (r[8 * s]);
+    jvs[310 * s] = 0.0 - (r[24 * s]) - (r[82 * s] * v[155 * s] * v[156 * s]) - (r[83 * s] * v[156 * s]) - (r[103 * s]);
+    jvs[311 * s] = 0.0 - (r[82 * s] * v[121 * s] * v[156 * s]);
+    jvs[312 * s] = 0.0 - (r[82 * s] * v[121 * s] * v[155 * s]) - (r[83 * s] * v[121 * s]);
+    jvs[313 * s] = 0.0 - (r[246 * s] * f[0 * s]) - (r[262 * s]);
+    jvs[314 * s] = 0.0 + (r[240 * s] * v[153 * s]);
+    jvs[315 * s] = 0.0 + 0x1.0000000000000p+1 * (r[244 * s] * 0x1.0000000000000p+1 * v[142 * s]);
+    jvs[316 * s] = 0.0 + (r[240 * s] * v[126 * s]);
+    jvs[317 * s] = 0.0 + (r[49 * s]);
+    jvs[318 * s] = 0.0 + (r[246 * s] * f[0 * s]);
+    jvs[319 * s] = 0.0 - (r[50 * s]) - (r[63 * s] * v[155 * s]) - (r[129 * s]);
     jvs[320 * s] = 0.0;
     jvs[321 * s] = 0.0;
-    jvs[322 * s] = 0.0 + b73;
-    jvs[323 * s] = 0.0 - b72 + b74;
-    jvs[324 * s] = 0.0 + b2;
-    jvs[325 * s] = 0.0 + b59;
-    jvs[326 * s] = 0.0 - b18 - b43 - b141;
-    jvs[327 * s] = 0.0 + 0x1.0000000000000p+1 * b263;
-    jvs[328 * s] = 0.0 + b267;
-    jvs[329 * s] = 0.0 + b265;
-    jvs[330 * s] = 0.0 + b273;
-    jvs[331 * s] = 0.0 + b271;
-    jvs[332 * s] = 0.0 + b335;
-    jvs[333 * s] = 0.0 + b281;
-    jvs[334 * s] = 0.0 + b60;
-    jvs[335 * s] = 0.0 + 0x1.0000000000000p+1 * b264 + b266 + b268 + b272 + b274 + b282 + b336;
-    jvs[336 * s] = 0.0 + b14;
-    jvs[337 * s] = 0.0 - b30 - b51 - b137 - b177;
-    jvs[338 * s] = 0.0 + b77;
-    jvs[339 * s] = 0.0 + b78;
-    jvs[340 * s] = 0.0 - b138;
-    jvs[341 * s] = 0.0 + b301;
-    jvs[342 * s] = 0.0 - b303 - b320 - b322 - b355;
-    jvs[343 * s] = 0.0 - b321;
-    jvs[344 * s] = 0.0 - b323;
-    jvs[345 * s] = 0.0 - b328 - b361;
-    jvs[346 * s] = 0.0 + b325;
-    jvs[347 * s] = 0.0 + b326;
-    jvs[348 * s] = 0.0 - b329;
-    jvs[349 * s] = 0.0 - b330;
-    jvs[350 * s] = 0.0 - b227 - b263 - b287;
-    jvs[351 * s] = 0.0 + b234;
-    jvs[352 * s] = 0.0 + b259;
-    jvs[353 * s] = 0.0 + b235;
-    jvs[354 * s] = 0.0 + b260 - b264;
-    jvs[355 * s] = 0.0 - b79 - b132 - b179;
-    jvs[356 * s] = 0.0 + b52;
-    jvs[357 * s] = 0.0 + b317;
-    jvs[358 * s] = 0.0 - b80;
-    jvs[359 * s] = 0.0 + b318;
-    jvs[360 * s] = 0.0 - b236 - b267 - b289;
-    jvs[361 * s] = 0.0 + b228;
-    jvs[362 * s] = 0.0 - b237;
-    jvs[363 * s] = 0.0 - b268;
-    jvs[364 * s] = 0.0 + b227;
-    jvs[365 * s] = 0.0 + b236;
-    jvs[366 * s] = 0.0 - b228 - b234 - b265 - b288;
+    jvs[322 * s] = 0.0 + (r[64 * s] * v[155 * s]);
+    jvs[323 * s] = 0.0 - (r[63 * s] * v[123 * s]) + (r[64 * s] * v[153 * s]);
+    jvs[324 * s] = 0.0 + (r[2 * s]);
+    jvs[325 * s] = 0.0 + (r[57 * s] * v[155 * s]);
+}
+
+KQ_HD KQ_NOINLINE void kqu_jac_4(const double* v, const double* f, const double* r, double* jvs, long long s)
+{
+    jvs[326 * s] = 0.0 - (r[18 * s]) - (r[43 * s]) - (r[97 * s]);
+    jvs[327 * s] = 0.0 + 0x1.0000000000000p+1 * (r[200 * s] * v[160 * s]);
+    jvs[328 * s] = 0.0 + (r[202 * s] * v[160 * s]);
+    jvs[329 * s] = 0.0 + (r[201 * s] * v[160 * s]);
+    jvs[330 * s] = 0.0 + (r[205 * s] * v[160 * s]);
+    jvs[331 * s] = 0.0 + (r[204 * s] * v[160 * s]);
+    jvs[332 * s] = 0.0 + (r[249 * s] * v[160 * s]);
+    jvs[333 * s] = 0.0 + (r[209 * s] * v[160 * s]);
+    jvs[334 * s] = 0.0 + (r[57 * s] * v[114 * s]);
+    jvs[335 * s] = 0.0 + 0x1.0000000000000p+1 * (r[200 * s] * v[128 * s]) + (r[201 * s] * v[131 * s]) + (r[202 * s] * v[130 * s]) + (r[204 * s] * v[133 * s]) + (r[205 * s] * v[132 * s]) + (r[209 * s] * v[141 * s]) + (r[249 * s] * v[137 * s]);
+    jvs[336 * s] = 0.0 + (r[14 * s]);
+    jvs[337 * s] = 0.0 - (r[30 * s]) - (r[52 * s]) - (r[94 * s] * v[160 * s]) - (r[133 * s]);
+    jvs[338 * s] = 0.0 + (r[66 * s] * v[155 * s]);
+    jvs[339 * s] = 0.0 + (r[66 * s] * v[151 * s]);
+    jvs[340 * s] = 0.0 - (r[94 * s] * v[125 * s]);
+    jvs[341 * s] = 0.0 + (r[227 * s]);
+    jvs[342 * s] = 0.0 - (r[229 * s]) - (r[240 * s] * v[153 * s]) - (r[241 * s] * v[156 * s]) - (r[260 * s]);
+    jvs[343 * s] = 0.0 - (r[240 * s] * v[126 * s]);
+    jvs[344 * s] = 0.0 - (r[241 * s] * v[126 * s]);
+    jvs[345 * s] = 0.0 - (r[245 * s] * v[155 * s] * v[156 * s]) - (r[266 * s]);
+    jvs[346 * s] = 0.0 + (r[243 * s] * v[154 * s]);
+    jvs[347 * s] = 0.0 + (r[243 * s] * v[142 * s]);
+    jvs[348 * s] = 0.0 - (r[245 * s] * v[127 * s] * v[156 * s]);
+    jvs[349 * s] = 0.0 - (r[245 * s] * v[127 * s] * v[155 * s]);
+    jvs[350 * s] = 0.0 - (r[177 * s]) - (r[200 * s] * v[160 * s]) - (r[213 * s]);
+    jvs[351 * s] = 0.0 + (r[183 * s] * v[155 * s]);
+    jvs[352 * s] = 0.0 + (r[198 * s] * v[160 * s]);
+    jvs[353 * s] = 0.0 + (r[183 * s] * v[131 * s]);
+    jvs[354 * s] = 0.0 + (r[198 * s] * v[136 * s]) - (r[200 * s] * v[128 * s]);
+    jvs[355 * s] = 0.0 - (r[67 * s] * v[155 * s]) - (r[91 * s]) - (r[135 * s]);
+    jvs[356 * s] = 0.0 + (r[53 * s]);
+    jvs[357 * s] = 0.0 + (r[238 * s] * v[158 * s]);
+    jvs[358 * s] = 0.0 - (r[67 * s] * v[129 * s]);
+    jvs[359 * s] = 0.0 + (r[238 * s] * v[150 * s]);
+    jvs[360 * s] = 0.0 - (r[184 * s] * v[155 * s]) - (r[202 * s] * v[160 * s]) - (r[215 * s]);
+    jvs[361 * s] = 0.0 + (r[178 * s]);
+    jvs[362 * s] = 0.0 - (r[184 * s] * v[130 * s]);
+    jvs[363 * s] = 0.0 - (r[202 * s] * v[130 * s]);
+    jvs[364 * s] = 0.0 + (r[177 * s]);
+    jvs[365 * s] = 0.0 + (r[184 * s] * v[155 * s]);
+    jvs[366 * s] = 0.0 - (r[178 * s]) - (r[183 * s] * v[155 * s]) - (r[201 * s] * v[160 * s]) - (r[214 * s]);
     jvs[367 * s] = 0.0;
-    jvs[368 * s] = 0.0 + b261;
-    jvs[369 * s] = 0.0 - b235 + b237;
-    jvs[370 * s] = 0.0 + b262 - b266;
-    jvs[371 * s] = 0.0 + 0x1.d70a3e0000000p-1 * b269;
-    jvs[372 * s] = 0.0 - b238 - b273 - b291;
-    jvs[373 * s] = 0.0 + b229;
-    jvs[374 * s] = 0.0 - b239;
-    jvs[375 * s] = 0.0 + 0x1.d70a3e0000000p-1 * b270 - b274;
-    jvs[376 * s] = 0.0 + b220;
-    jvs[377 * s] = 0.0 + b238;
-    jvs[378 * s] = 0.0 - b225 - b229 - b271 - b290;
-    jvs[379 * s] = 0.0 + b239;
-    jvs[380 * s] = 0.0 - b272;
-    jvs[381 * s] = 0.0 + b217;
-    jvs[382 * s] = 0.0 + b271;
-    jvs[383 * s] = 0.0 - b222 - b231 - b275 - b292;
-    jvs[384 * s] = 0.0 + b242;
-    jvs[385 * s] = 0.0 + b243;
-    jvs[386 * s] = 0.0 + b272 - b276;
-    jvs[387 * s] = 0.0 + b273;
+    jvs[368 * s] = 0.0 + (r[199 * s] * v[160 * s]);
+    jvs[369 * s] = 0.0 - (r[183 * s] * v[131 * s]) + (r[184 * s] * v[130 * s]);
+    jvs[370 * s] = 0.0 + (r[199 * s] * v[140 * s]) - (r[201 * s] * v[131 * s]);
+    jvs[371 * s] = 0.0 + 0x1.d70a3e0000000p-1 * (r[203 * s] * v[160 * s]);
+    jvs[372 * s] = 0.0 - (r[185 * s] * v[155 * s]) - (r[205 * s] * v[160 * s]) - (r[217 * s]);
+    jvs[373 * s] = 0.0 + (r[179 * s]);
+    jvs[374 * s] = 0.0 - (r[185 * s] * v[132 * s]);
+    jvs[375 * s] = 0.0 + 0x1.d70a3e0000000p-1 * (r[203 * s] * v[112 * s]) - (r[205 * s] * v[132 * s]);
+    jvs[376 * s] = 0.0 + (r[170 * s]);
+    jvs[377 * s] = 0.0 + (r[185 * s] * v[155 * s]);
+    jvs[378 * s] = 0.0 - (r[175 * s]) - (r[179 * s]) - (r[204 * s] * v[160 * s]) - (r[216 * s]);
+}
+
+KQ_HD KQ_NOINLINE void kqu_jac_5(const double* v, const double* f, const double* r, double* jvs, long long s)
+{
+    jvs[379 * s] = 0.0 + (r[185 * s] * v[132 * s]);
+    jvs[380 * s] = 0.0 - (r[204 * s] * v[133 * s]);
+    jvs[381 * s] = 0.0 + (r[167 * s]);
+    jvs[382 * s] = 0.0 + (r[204 * s] * v[160 * s]);
+    jvs[383 * s] = 0.0 - (r[172 * s]) - (r[181 * s]) - (r[206 * s] * v[160 * s]) - (r[218 * s]);
+    jvs[384 * s] = 0.0 + (r[187 * s] * v[155 * s]);
+    jvs[385 * s] = 0.0 + (r[187 * s] * v[135 * s]);
+    jvs[386 * s] = 0.0 + (r[204 * s] * v[133 * s]) - (r[206 * s] * v[134 * s]);
+    jvs[387 * s] = 0.0 + (r[205 * s] * v[160 * s]);
     jvs[388 * s] = 0.0;
-    jvs[389 * s] = 0.0 + b231;
-    jvs[390 * s] = 0.0 - b242 - b277 - b293;
-    jvs[391 * s] = 0.0 - b243;
-    jvs[392 * s] = 0.0 + b274 - b278;
-    jvs[393 * s] = 0.0 + b257;
-    jvs[394 * s] = 0.0 + 0x1.b333340000000p-1 * b275;
+    jvs[389 * s] = 0.0 + (r[181 * s]);
+    jvs[390 * s] = 0.0 - (r[187 * s] * v[155 * s]) - (r[207 * s] * v[160 * s]) - (r[219 * s]);
+    jvs[391 * s] = 0.0 - (r[187 * s] * v[135 * s]);
+    jvs[392 * s] = 0.0 + (r[205 * s] * v[132 * s]) - (r[207 * s] * v[135 * s]);
+    jvs[393 * s] = 0.0 + (r[197 * s] * v[160 * s]);
+    jvs[394 * s] = 0.0 + 0x1.b333340000000p-1 * (r[206 * s] * v[160 * s]);
     jvs[395 * s] = 0.0;
-    jvs[396 * s] = 0.0 - b226 - b259 - b285;
-    jvs[397 * s] = 0.0 + b232;
-    jvs[398 * s] = 0.0 + b233;
-    jvs[399 * s] = 0.0 + b258 - b260 + 0x1.b333340000000p-1 * b276;
-    jvs[400 * s] = 0.0 - b65 - b172 - b335;
-    jvs[401 * s] = 0.0 + b46;
-    jvs[402 * s] = 0.0 - b66;
-    jvs[403 * s] = 0.0 - b336;
-    jvs[404 * s] = 0.0 + b249;
-    jvs[405 * s] = 0.0 - b230 - b253 - b296;
-    jvs[406 * s] = 0.0 + b240;
-    jvs[407 * s] = 0.0 + b241;
-    jvs[408 * s] = 0.0 + b250 - b254;
-    jvs[409 * s] = 0.0 + b230;
-    jvs[410 * s] = 0.0 - b240 - b255 - b297;
-    jvs[411 * s] = 0.0 - b241;
-    jvs[412 * s] = 0.0 - b256;
-    jvs[413 * s] = 0.0 + 0x1.47ae140000000p-4 * b269;
-    jvs[414 * s] = 0.0 + 0x1.b333340000000p-1 * b277;
-    jvs[415 * s] = 0.0 + b226;
-    jvs[416 * s] = 0.0 + b253;
-    jvs[417 * s] = 0.0 + b255;
-    jvs[418 * s] = 0.0 - b232 - b261 - b286;
-    jvs[419 * s] = 0.0 - b233;
-    jvs[420 * s] = 0.0 + b254 + b256 - b262 + 0x1.47ae140000000p-4 * b270 + 0x1.b333340000000p-1 * b278;
-    jvs[421 * s] = 0.0 + b6;
-    jvs[422 * s] = 0.0 + b65;
-    jvs[423 * s] = 0.0 - b22 - b46 - b145 - b281;
-    jvs[424 * s] = 0.0 + b344;
-    jvs[425 * s] = 0.0 + b279;
-    jvs[426 * s] = 0.0 + b66;
-    jvs[427 * s] = 0.0 + b280 - b282 + b345;
-    jvs[428 * s] = 0.0 + b324;
+    jvs[396 * s] = 0.0 - (r[176 * s]) - (r[198 * s] * v[160 * s]) - (r[211 * s]);
+    jvs[397 * s] = 0.0 + (r[182 * s] * v[155 * s]);
+    jvs[398 * s] = 0.0 + (r[182 * s] * v[140 * s]);
+    jvs[399 * s] = 0.0 + (r[197 * s] * v[105 * s]) - (r[198 * s] * v[136 * s]) + 0x1.b333340000000p-1 * (r[206 * s] * v[134 * s]);
+    jvs[400 * s] = 0.0 - (r[60 * s] * v[155 * s]) - (r[128 * s]) - (r[249 * s] * v[160 * s]);
+    jvs[401 * s] = 0.0 + (r[46 * s]);
+    jvs[402 * s] = 0.0 - (r[60 * s] * v[137 * s]);
+    jvs[403 * s] = 0.0 - (r[249 * s] * v[137 * s]);
+    jvs[404 * s] = 0.0 + (r[193 * s] * v[160 * s]);
+    jvs[405 * s] = 0.0 - (r[180 * s]) - (r[195 * s] * v[160 * s]) - (r[222 * s]);
+    jvs[406 * s] = 0.0 + (r[186 * s] * v[155 * s]);
+    jvs[407 * s] = 0.0 + (r[186 * s] * v[139 * s]);
+    jvs[408 * s] = 0.0 + (r[193 * s] * v[104 * s]) - (r[195 * s] * v[138 * s]);
+    jvs[409 * s] = 0.0 + (r[180 * s]);
+    jvs[410 * s] = 0.0 - (r[186 * s] * v[155 * s]) - (r[196 * s] * v[160 * s]) - (r[223 * s]);
+    jvs[411 * s] = 0.0 - (r[186 * s] * v[139 * s]);
+    jvs[412 * s] = 0.0 - (r[196 * s] * v[139 * s]);
+    jvs[413 * s] = 0.0 + 0x1.47ae140000000p-4 * (r[203 * s] * v[160 * s]);
+    jvs[414 * s] = 0.0 + 0x1.b333340000000p-1 * (r[207 * s] * v[160 * s]);
+    jvs[415 * s] = 0.0 + (r[176 * s]);
+    jvs[416 * s] = 0.0 + (r[195 * s] * v[160 * s]);
+    jvs[417 * s] = 0.0 + (r[196 * s] * v[160 * s]);
+    jvs[418 * s] = 0.0 - (r[182 * s] * v[155 * s]) - (r[199 * s] * v[160 * s]) - (r[212 * s]);
+    jvs[419 * s] = 0.0 - (r[182 * s] * v[140 * s]);
+    jvs[420 * s] = 0.0 + (r[195 * s] * v[138 * s]) + (r[196 * s] * v[139 * s]) - (r[199 * s] * v[140 * s]) + 0x1.47ae140000000p-4 * (r[203 * s] * v[112 * s]) + 0x1.b333340000000p-1 * (r[207 * s] * v[135 * s]);
+    jvs[421 * s] = 0.0 + (r[6 * s]);
+    jvs[422 * s] = 0.0 + (r[60 * s] * v[155 * s]);
+    jvs[423 * s] = 0.0 - (r[22 * s]) - (r[46 * s]) - (r[101 * s]) - (r[209 * s] * v[160 * s]);
+    jvs[424 * s] = 0.0 + (r[254 * s] * v[160 * s]);
+    jvs[425 * s] = 0.0 + (r[208 * s] * v[160 * s]);
+    jvs[426 * s] = 0.0 + (r[60 * s] * v[137 * s]);
+    jvs[427 * s] = 0.0 + (r[208 * s] * v[148 * s]) - (r[209 * s] * v[141 * s]) + (r[254 * s] * v[147 * s]);
+    jvs[428 * s] = 0.0 + (r[242 * s] * f[2 * s]);
     jvs[429 * s] = 0.0;
     jvs[430 * s] = 0.0;
-    jvs[431 * s] = 0.0 - b325 + -0x1.0000000000000p+1 * b327 - b360;
+    jvs[431 * s] = 0.0 - (r[243 * s] * v[154 * s]) + -0x1.0000000000000p+1 * (r[244 * s] * 0x1.0000000000000p+1 * v[142 * s]) - (r[265 * s]);
     jvs[432 * s] = 0.0;
-    jvs[433 * s] = 0.0 - b326;
+    jvs[433 * s] = 0.0 - (r[243 * s] * v[142 * s]);
     jvs[434 * s] = 0.0;
     jvs[435 * s] = 0.0;
-    jvs[436 * s] = 0.0 + b218;
-    jvs[437 * s] = 0.0 + 0x1.0000000000000p+1 * b332;
-    jvs[438 * s] = 0.0 - b223 - b244 - b298 - b337 - b339;
-    jvs[439 * s] = 0.0 + b341;
-    jvs[440 * s] = 0.0 + b245;
-    jvs[441 * s] = 0.0 - b338;
-    jvs[442 * s] = 0.0 - b340;
-    jvs[443 * s] = 0.0 - b96 - b102;
-    jvs[444 * s] = 0.0 - b90 - b103;
-    jvs[445 * s] = 0.0 + b0;
-    jvs[446 * s] = 0.0 - b16 - b40 - b84 - b91 - b97 - b104 - b124 - b139;
-    jvs[447 * s] = 0.0 + b53;
-    jvs[448 * s] = 0.0 + b54;
-    jvs[449 * s] = 0.0 - b85;
-    jvs[450 * s] = 0.0 - b125;
-    jvs[451 * s] = 0.0 + b4;
-    jvs[452 * s] = 0.0 - b20 - b81 - b143 - b248 - b311;
-    jvs[453 * s] = 0.0 + b120;
-    jvs[454 * s] = 0.0 + b119 + b121;
-    jvs[455 * s] = 0.0 - b82;
-    jvs[456 * s] = 0.0 - b83;
-    jvs[457 * s] = 0.0 + b306 - b312;
-    jvs[458 * s] = 0.0 + b32;
-    jvs[459 * s] = 0.0 + b42;
-    jvs[460 * s] = 0.0 - b199;
-    jvs[461 * s] = 0.0 + b320 + b322;
-    jvs[462 * s] = 0.0 - b57 - b153 - b200 - b305;
-    jvs[463 * s] = 0.0 + b130;
-    jvs[464 * s] = 0.0 + b133;
-    jvs[465 * s] = 0.0 + b321;
-    jvs[466 * s] = 0.0 - b58;
-    jvs[467 * s] = 0.0 + b131 + b323;
-    jvs[468 * s] = 0.0 + b134;
-    jvs[469 * s] = 0.0 + b337 + b339;
-    jvs[470 * s] = 0.0 - b341 - b342 - b344 - b359;
+    jvs[436 * s] = 0.0 + (r[168 * s]);
+}
+
+KQ_HD KQ_NOINLINE void kqu_jac_6(const double* v, const double* f, const double* r, double* jvs, long long s)
+{
+    jvs[437 * s] = 0.0 + 0x1.0000000000000p+1 * (r[247 * s] * 0x1.0000000000000p+1 * v[119 * s]);
+    jvs[438 * s] = 0.0 - (r[173 * s]) - (r[188 * s] * f[0 * s]) - (r[224 * s]) - (r[250 * s] * v[156 * s]) - (r[251 * s] * v[159 * s]);
+    jvs[439 * s] = 0.0 + (r[252 * s]);
+    jvs[440 * s] = 0.0 + (r[189 * s]);
+    jvs[441 * s] = 0.0 - (r[250 * s] * v[143 * s]);
+    jvs[442 * s] = 0.0 - (r[251 * s] * v[143 * s]);
+    jvs[443 * s] = 0.0 - (r[75 * s] * v[144 * s]) - (r[78 * s] * v[13 * s] * v[144 * s]);
+    jvs[444 * s] = 0.0 - (r[72 * s] * v[144 * s]) - (r[78 * s] * v[12 * s] * v[144 * s]);
+    jvs[445 * s] = 0.0 + (r[0 * s]);
+    jvs[446 * s] = 0.0 - (r[16 * s]) - (r[40 * s]) - (r[69 * s] * v[157 * s]) - (r[72 * s] * v[13 * s]) - (r[75 * s] * v[12 * s]) - (r[78 * s] * v[12 * s] * v[13 * s]) - (r[87 * s] * v[158 * s]) - (r[95 * s]);
+    jvs[447 * s] = 0.0 + (r[54 * s] * v[156 * s]);
+    jvs[448 * s] = 0.0 + (r[54 * s] * v[155 * s]);
+    jvs[449 * s] = 0.0 - (r[69 * s] * v[144 * s]);
+    jvs[450 * s] = 0.0 - (r[87 * s] * v[144 * s]);
+    jvs[451 * s] = 0.0 + (r[4 * s]);
+    jvs[452 * s] = 0.0 - (r[20 * s]) - (r[68 * s] * v[155 * s] * v[156 * s]) - (r[99 * s]) - (r[192 * s]) - (r[235 * s] * v[160 * s]);
+    jvs[453 * s] = 0.0 + (r[85 * s] * v[154 * s]);
+    jvs[454 * s] = 0.0 + (r[84 * s] * 0x1.0000000000000p+1 * v[154 * s]) + (r[85 * s] * v[150 * s]);
+    jvs[455 * s] = 0.0 - (r[68 * s] * v[145 * s] * v[156 * s]);
+    jvs[456 * s] = 0.0 - (r[68 * s] * v[145 * s] * v[155 * s]);
+    jvs[457 * s] = 0.0 + (r[232 * s] * 0x1.0000000000000p+1 * v[160 * s]) - (r[235 * s] * v[145 * s]);
+    jvs[458 * s] = 0.0 + (r[32 * s]);
+    jvs[459 * s] = 0.0 + (r[42 * s]);
+    jvs[460 * s] = 0.0 - (r[152 * s] * v[146 * s]);
+    jvs[461 * s] = 0.0 + (r[240 * s] * v[153 * s]) + (r[241 * s] * v[156 * s]);
+    jvs[462 * s] = 0.0 - (r[56 * s] * v[155 * s]) - (r[109 * s]) - (r[152 * s] * v[115 * s]) - (r[231 * s]);
+    jvs[463 * s] = 0.0 + (r[90 * s] * v[156 * s]);
+    jvs[464 * s] = 0.0 + (r[92 * s] * v[157 * s]);
+    jvs[465 * s] = 0.0 + (r[240 * s] * v[126 * s]);
+    jvs[466 * s] = 0.0 - (r[56 * s] * v[146 * s]);
+    jvs[467 * s] = 0.0 + (r[90 * s] * v[149 * s]) + (r[241 * s] * v[126 * s]);
+    jvs[468 * s] = 0.0 + (r[92 * s] * v[151 * s]);
+    jvs[469 * s] = 0.0 + (r[250 * s] * v[156 * s]) + (r[251 * s] * v[159 * s]);
+    jvs[470 * s] = 0.0 - (r[252 * s]) - (r[253 * s] * v[152 * s]) - (r[254 * s] * v[160 * s]) - (r[264 * s]);
     jvs[471 * s] = 0.0;
-    jvs[472 * s] = 0.0 - b343;
-    jvs[473 * s] = 0.0 + b338;
-    jvs[474 * s] = 0.0 + b340;
-    jvs[475 * s] = 0.0 - b345;
-    jvs[476 * s] = 0.0 + 0x1.3333340000000p-3 * b275;
-    jvs[477 * s] = 0.0 + 0x1.3333340000000p-3 * b277;
-    jvs[478 * s] = 0.0 + b244;
-    jvs[479 * s] = 0.0 + b342;
-    jvs[480 * s] = 0.0 - b245 - b279 - b294;
-    jvs[481 * s] = 0.0 + b343;
+    jvs[472 * s] = 0.0 - (r[253 * s] * v[147 * s]);
+    jvs[473 * s] = 0.0 + (r[250 * s] * v[143 * s]);
+    jvs[474 * s] = 0.0 + (r[251 * s] * v[143 * s]);
+    jvs[475 * s] = 0.0 - (r[254 * s] * v[147 * s]);
+    jvs[476 * s] = 0.0 + 0x1.3333340000000p-3 * (r[206 * s] * v[160 * s]);
+    jvs[477 * s] = 0.0 + 0x1.3333340000000p-3 * (r[207 * s] * v[160 * s]);
+    jvs[478 * s] = 0.0 + (r[188 * s] * f[0 * s]);
+    jvs[479 * s] = 0.0 + (r[253 * s] * v[152 * s]);
+    jvs[480 * s] = 0.0 - (r[189 * s]) - (r[208 * s] * v[160 * s]) - (r[220 * s]);
+    jvs[481 * s] = 0.0 + (r[253 * s] * v[147 * s]);
     jvs[482 * s] = 0.0;
     jvs[483 * s] = 0.0;
     jvs[484 * s] = 0.0;
-    jvs[485 * s] = 0.0 + 0x1.3333340000000p-3 * b276 + 0x1.3333340000000p-3 * b278 - b280;
-    jvs[486 * s] = 0.0 + b15;
-    jvs[487 * s] = 0.0 + b79;
-    jvs[488 * s] = 0.0 - b31 - b52 - b130 - b180 - b319;
+    jvs[485 * s] = 0.0 + 0x1.3333340000000p-3 * (r[206 * s] * v[134 * s]) + 0x1.3333340000000p-3 * (r[207 * s] * v[135 * s]) - (r[208 * s] * v[148 * s]);
+    jvs[486 * s] = 0.0 + (r[15 * s]);
+    jvs[487 * s] = 0.0 + (r[67 * s] * v[155 * s]);
+}
+
+KQ_HD KQ_NOINLINE void kqu_jac_7(const double* v, const double* f, const double* r, double* jvs, long long s)
+{
+    jvs[488 * s] = 0.0 - (r[31 * s]) - (r[53 * s]) - (r[90 * s] * v[156 * s]) - (r[136 * s]) - (r[239 * s]);
     jvs[489 * s] = 0.0;
-    jvs[490 * s] = 0.0 + b315;
-    jvs[491 * s] = 0.0 + b80;
-    jvs[492 * s] = 0.0 - b131;
-    jvs[493 * s] = 0.0 + b316;
-    jvs[494 * s] = 0.0 - b75 - b120 - b122 - b174 - b309 - b317;
-    jvs[495 * s] = 0.0 + b50 - b121;
-    jvs[496 * s] = 0.0 - b76;
-    jvs[497 * s] = 0.0 - b123;
-    jvs[498 * s] = 0.0 - b318;
-    jvs[499 * s] = 0.0 - b310;
-    jvs[500 * s] = 0.0 + b51;
-    jvs[501 * s] = 0.0 + b132;
-    jvs[502 * s] = 0.0 + 0x1.0000000000000p+1 * b124;
+    jvs[490 * s] = 0.0 + (r[237 * s] * v[158 * s]);
+    jvs[491 * s] = 0.0 + (r[67 * s] * v[129 * s]);
+    jvs[492 * s] = 0.0 - (r[90 * s] * v[149 * s]);
+    jvs[493 * s] = 0.0 + (r[237 * s] * v[154 * s]);
+    jvs[494 * s] = 0.0 - (r[65 * s] * v[155 * s]) - (r[85 * s] * v[154 * s]) - (r[86 * s] * v[157 * s]) - (r[130 * s]) - (r[234 * s] * v[160 * s]) - (r[238 * s] * v[158 * s]);
+    jvs[495 * s] = 0.0 + (r[51 * s]) - (r[85 * s] * v[150 * s]);
+    jvs[496 * s] = 0.0 - (r[65 * s] * v[150 * s]);
+    jvs[497 * s] = 0.0 - (r[86 * s] * v[150 * s]);
+    jvs[498 * s] = 0.0 - (r[238 * s] * v[150 * s]);
+    jvs[499 * s] = 0.0 - (r[234 * s] * v[150 * s]);
+    jvs[500 * s] = 0.0 + (r[52 * s]);
+    jvs[501 * s] = 0.0 + (r[91 * s]);
+    jvs[502 * s] = 0.0 + 0x1.0000000000000p+1 * (r[87 * s] * v[158 * s]);
     jvs[503 * s] = 0.0;
     jvs[504 * s] = 0.0;
-    jvs[505 * s] = 0.0 - b77 - b133 - b135 - b178;
+    jvs[505 * s] = 0.0 - (r[66 * s] * v[155 * s]) - (r[92 * s] * v[157 * s]) - (r[93 * s] * v[160 * s]) - (r[134 * s]);
     jvs[506 * s] = 0.0;
-    jvs[507 * s] = 0.0 - b78;
-    jvs[508 * s] = 0.0 + 0x1.0000000000000p+1 * b126;
-    jvs[509 * s] = 0.0 - b134;
-    jvs[510 * s] = 0.0 + 0x1.0000000000000p+1 * b125 + 0x1.0000000000000p+1 * b127 + 0x1.0000000000000p+1 * b128;
-    jvs[511 * s] = 0.0 + 0x1.0000000000000p+1 * b129;
-    jvs[512 * s] = 0.0 - b136;
-    jvs[513 * s] = 0.0 + b45;
-    jvs[514 * s] = 0.0 - b63;
-    jvs[515 * s] = 0.0 + b267;
+    jvs[507 * s] = 0.0 - (r[66 * s] * v[151 * s]);
+    jvs[508 * s] = 0.0 + 0x1.0000000000000p+1 * (r[88 * s] * v[158 * s]);
+    jvs[509 * s] = 0.0 - (r[92 * s] * v[151 * s]);
+    jvs[510 * s] = 0.0 + 0x1.0000000000000p+1 * (r[87 * s] * v[144 * s]) + 0x1.0000000000000p+1 * (r[88 * s] * v[156 * s]) + 0x1.0000000000000p+1 * (r[89 * s] * v[159 * s]);
+    jvs[511 * s] = 0.0 + 0x1.0000000000000p+1 * (r[89 * s] * v[158 * s]);
+    jvs[512 * s] = 0.0 - (r[93 * s] * v[151 * s]);
+    jvs[513 * s] = 0.0 + (r[45 * s]);
+    jvs[514 * s] = 0.0 - (r[59 * s] * v[152 * s]);
+    jvs[515 * s] = 0.0 + (r[202 * s] * v[160 * s]);
     jvs[516 * s] = 0.0;
     jvs[517 * s] = 0.0;
-    jvs[518 * s] = 0.0 + b335;
+    jvs[518 * s] = 0.0 + (r[249 * s] * v[160 * s]);
     jvs[519 * s] = 0.0;
     jvs[520 * s] = 0.0;
-    jvs[521 * s] = 0.0 + b339;
-    jvs[522 * s] = 0.0 + b305;
-    jvs[523 * s] = 0.0 - b342;
+    jvs[521 * s] = 0.0 + (r[251 * s] * v[159 * s]);
+    jvs[522 * s] = 0.0 + (r[231 * s]);
+    jvs[523 * s] = 0.0 - (r[253 * s] * v[152 * s]);
     jvs[524 * s] = 0.0;
     jvs[525 * s] = 0.0;
-    jvs[526 * s] = 0.0 + b120 + b122 + b309;
-    jvs[527 * s] = 0.0 + b135;
-    jvs[528 * s] = 0.0 - b64 - b69 - b167 - b343;
+    jvs[526 * s] = 0.0 + (r[85 * s] * v[154 * s]) + (r[86 * s] * v[157 * s]) + (r[234 * s] * v[160 * s]);
+    jvs[527 * s] = 0.0 + (r[93 * s] * v[160 * s]);
+    jvs[528 * s] = 0.0 - (r[59 * s] * v[108 * s]) - (r[62 * s] * v[155 * s]) - (r[123 * s]) - (r[253 * s] * v[147 * s]);
     jvs[529 * s] = 0.0;
-    jvs[530 * s] = 0.0 + b121;
-    jvs[531 * s] = 0.0 - b70;
+    jvs[530 * s] = 0.0 + (r[85 * s] * v[150 * s]);
+    jvs[531 * s] = 0.0 - (r[62 * s] * v[152 * s]);
     jvs[532 * s] = 0.0;
-    jvs[533 * s] = 0.0 + b123;
+    jvs[533 * s] = 0.0 + (r[86 * s] * v[150 * s]);
     jvs[534 * s] = 0.0;
-    jvs[535 * s] = 0.0 + b340;
-    jvs[536 * s] = 0.0 + b136 + b268 + b310 + b336;
-    jvs[537 * s] = 0.0 + b36;
-    jvs[538 * s] = 0.0 + b96 + b98 + b100 + b102 + b105 + b108;
-    jvs[539 * s] = 0.0 + b90 + b92 + b94 + b103 + b106 + b109;
-    jvs[540 * s] = 0.0 - b202;
-    jvs[541 * s] = 0.0 - b205;
-    jvs[542 * s] = 0.0 - b190 - b197;
-    jvs[543 * s] = 0.0 + b111;
-    jvs[544 * s] = 0.0 + b114 + b117;
-    jvs[545 * s] = 0.0 + b49;
-    jvs[546 * s] = 0.0 - b320;
-    jvs[547 * s] = 0.0 + 0x1.0000000000000p+1 * b328;
+    jvs[535 * s] = 0.0 + (r[251 * s] * v[143 * s]);
+    jvs[536 * s] = 0.0 + (r[93 * s] * v[151 * s]) + (r[202 * s] * v[130 * s]) + (r[234 * s] * v[150 * s]) + (r[249 * s] * v[137 * s]);
+    jvs[537 * s] = 0.0 + (r[36 * s]);
+    jvs[538 * s] = 0.0 + (r[75 * s] * v[144 * s]) + (r[76 * s] * v[156 * s]) + (r[77 * s] * v[159 * s]) + (r[78 * s] * v[13 * s] * v[144 * s]) + (r[79 * s] * v[13 * s] * v[156 * s]) + (r[80 * s] * v[13 * s] * v[159 * s]);
+    jvs[539 * s] = 0.0 + (r[72 * s] * v[144 * s]) + (r[73 * s] * v[156 * s]) + (r[74 * s] * v[159 * s]) + (r[78 * s] * v[12 * s] * v[144 * s]) + (r[79 * s] * v[12 * s] * v[156 * s]) + (r[80 * s] * v[12 * s] * v[159 * s]);
+    jvs[540 * s] = 0.0 - (r[154 * s] * v[153 * s]);
+    jvs[541 * s] = 0.0 - (r[156 * s] * v[153 * s]);
+    jvs[542 * s] = 0.0 - (r[147 * s] * v[153 * s]) - (r[151 * s] * v[153 * s]);
+}
+
+KQ_HD KQ_NOINLINE void kqu_jac_8(const double* v, const double* f, const double* r, double* jvs, long long s)
+{
+    jvs[543 * s] = 0.0 + (r[81 * s] * v[155 * s] * v[156 * s]);
+    jvs[544 * s] = 0.0 + (r[82 * s] * v[155 * s] * v[156 * s]) + (r[83 * s] * v[156 * s]);
+    jvs[545 * s] = 0.0 + (r[50 * s]);
+    jvs[546 * s] = 0.0 - (r[240 * s] * v[153 * s]);
+    jvs[547 * s] = 0.0 + 0x1.0000000000000p+1 * (r[245 * s] * v[155 * s] * v[156 * s]);
     jvs[548 * s] = 0.0;
-    jvs[549 * s] = 0.0 + b84 + b91 + b97 + b104 + b124;
-    jvs[550 * s] = 0.0 + b81;
+    jvs[549 * s] = 0.0 + (r[69 * s] * v[157 * s]) + (r[72 * s] * v[13 * s]) + (r[75 * s] * v[12 * s]) + (r[78 * s] * v[12 * s] * v[13 * s]) + (r[87 * s] * v[158 * s]);
+    jvs[550 * s] = 0.0 + (r[68 * s] * v[155 * s] * v[156 * s]);
     jvs[551 * s] = 0.0;
-    jvs[552 * s] = 0.0 + b130;
+    jvs[552 * s] = 0.0 + (r[90 * s] * v[156 * s]);
     jvs[553 * s] = 0.0;
     jvs[554 * s] = 0.0;
-    jvs[555 * s] = 0.0 - b73 - b152 - b191 - b198 - b203 - b206 - b321;
+    jvs[555 * s] = 0.0 - (r[64 * s] * v[155 * s]) - (r[108 * s]) - (r[147 * s] * v[115 * s]) - (r[151 * s] * v[115 * s]) - (r[154 * s] * v[75 * s]) - (r[156 * s] * v[77 * s]) - (r[240 * s] * v[126 * s]);
     jvs[556 * s] = 0.0;
-    jvs[557 * s] = 0.0 - b74 + b82 + b112 + b115 + 0x1.0000000000000p+1 * b329;
-    jvs[558 * s] = 0.0 + b83 + b86 + b93 + b99 + b107 + b113 + b116 + b118 + b126 + b131 + 0x1.0000000000000p+1 * b330;
-    jvs[559 * s] = 0.0 + b85 + b87 + b88;
-    jvs[560 * s] = 0.0 + b125 + b127 + b128;
-    jvs[561 * s] = 0.0 + b89 + b95 + b101 + b110 + b129;
+    jvs[557 * s] = 0.0 - (r[64 * s] * v[153 * s]) + (r[68 * s] * v[145 * s] * v[156 * s]) + (r[81 * s] * v[120 * s] * v[156 * s]) + (r[82 * s] * v[121 * s] * v[156 * s]) + 0x1.0000000000000p+1 * (r[245 * s] * v[127 * s] * v[156 * s]);
+    jvs[558 * s] = 0.0 + (r[68 * s] * v[145 * s] * v[155 * s]) + (r[70 * s] * v[157 * s]) + (r[73 * s] * v[13 * s]) + (r[76 * s] * v[12 * s]) + (r[79 * s] * v[12 * s] * v[13 * s]) + (r[81 * s] * v[120 * s] * v[155 * s]) + (r[82 * s] * v[121 * s] * v[155 * s]) + (r[83 * s] * v[121 * s]) + (r[88 * s] * v[158 * s]) + (r[90 * s] * v[149 * s]) + 0x1.0000000000000p+1 * (r[245 * s] * v[127 * s] * v[155 * s]);
+    jvs[559 * s] = 0.0 + (r[69 * s] * v[144 * s]) + (r[70 * s] * v[156 * s]) + (r[71 * s] * v[159 * s]);
+    jvs[560 * s] = 0.0 + (r[87 * s] * v[144 * s]) + (r[88 * s] * v[156 * s]) + (r[89 * s] * v[159 * s]);
+    jvs[561 * s] = 0.0 + (r[71 * s] * v[157 * s]) + (r[74 * s] * v[13 * s]) + (r[77 * s] * v[12 * s]) + (r[80 * s] * v[12 * s] * v[13 * s]) + (r[89 * s] * v[158 * s]);
     jvs[562 * s] = 0.0;
-    jvs[563 * s] = 0.0 + b12;
-    jvs[564 * s] = 0.0 + b249 + b251;
-    jvs[565 * s] = 0.0 + b257;
-    jvs[566 * s] = 0.0 + b269;
-    jvs[567 * s] = 0.0 + 0x1.0000000000000p+1 * b332;
-    jvs[568 * s] = 0.0 + b273;
-    jvs[569 * s] = 0.0 + b271;
-    jvs[570 * s] = 0.0 + b259;
-    jvs[571 * s] = 0.0 + b335;
-    jvs[572 * s] = 0.0 + b253;
-    jvs[573 * s] = 0.0 + b255;
-    jvs[574 * s] = 0.0 + b261;
-    jvs[575 * s] = 0.0 + b281;
-    jvs[576 * s] = 0.0 - b325;
-    jvs[577 * s] = 0.0 + b311;
-    jvs[578 * s] = 0.0 + b344;
-    jvs[579 * s] = 0.0 + b279;
-    jvs[580 * s] = 0.0 + b319;
-    jvs[581 * s] = 0.0 + b75 - b120;
+    jvs[563 * s] = 0.0 + (r[12 * s]);
+    jvs[564 * s] = 0.0 + (r[193 * s] * v[160 * s]) + (r[194 * s] * v[160 * s]);
+    jvs[565 * s] = 0.0 + (r[197 * s] * v[160 * s]);
+    jvs[566 * s] = 0.0 + (r[203 * s] * v[160 * s]);
+    jvs[567 * s] = 0.0 + 0x1.0000000000000p+1 * (r[247 * s] * 0x1.0000000000000p+1 * v[119 * s]);
+    jvs[568 * s] = 0.0 + (r[205 * s] * v[160 * s]);
+    jvs[569 * s] = 0.0 + (r[204 * s] * v[160 * s]);
+    jvs[570 * s] = 0.0 + (r[198 * s] * v[160 * s]);
+    jvs[571 * s] = 0.0 + (r[249 * s] * v[160 * s]);
+    jvs[572 * s] = 0.0 + (r[195 * s] * v[160 * s]);
+    jvs[573 * s] = 0.0 + (r[196 * s] * v[160 * s]);
+    jvs[574 * s] = 0.0 + (r[199 * s] * v[160 * s]);
+    jvs[575 * s] = 0.0 + (r[209 * s] * v[160 * s]);
+    jvs[576 * s] = 0.0 - (r[243 * s] * v[154 * s]);
+    jvs[577 * s] = 0.0 + (r[235 * s] * v[160 * s]);
+    jvs[578 * s] = 0.0 + (r[254 * s] * v[160 * s]);
+    jvs[579 * s] = 0.0 + (r[208 * s] * v[160 * s]);
+    jvs[580 * s] = 0.0 + (r[239 * s]);
+    jvs[581 * s] = 0.0 + (r[65 * s] * v[155 * s]) - (r[85 * s] * v[154 * s]);
     jvs[582 * s] = 0.0;
     jvs[583 * s] = 0.0;
-    jvs[584 * s] = 0.0 - b28 - b50 + -0x1.0000000000000p+1 * b119 - b121 - b175 - b307 - b315 - b326;
-    jvs[585 * s] = 0.0 + b76;
+}
+
+KQ_HD KQ_NOINLINE void kqu_jac_9(const double* v, const double* f, const double* r, double* jvs, long long s)
+{
+    jvs[584 * s] = 0.0 - (r[28 * s]) - (r[51 * s]) + -0x1.0000000000000p+1 * (r[84 * s] * 0x1.0000000000000p+1 * v[154 * s]) - (r[85 * s] * v[150 * s]) - (r[131 * s]) - (r[233 * s] * v[160 * s]) - (r[237 * s] * v[158 * s]) - (r[243 * s] * v[142 * s]);
+    jvs[585 * s] = 0.0 + (r[65 * s] * v[150 * s]);
     jvs[586 * s] = 0.0;
     jvs[587 * s] = 0.0;
-    jvs[588 * s] = 0.0 - b316;
+    jvs[588 * s] = 0.0 - (r[237 * s] * v[154 * s]);
     jvs[589 * s] = 0.0;
-    jvs[590 * s] = 0.0 + b250 + b252 + b254 + b256 + b258 + b260 + b262 + b270 + b272 + b274 + b280 + b282 - b308 + b312 + b336 + b345;
-    jvs[591 * s] = 0.0 + 0x1.0000000000000p+1 * b96 + b98 + 0x1.0000000000000p+1 * b102 + b105;
-    jvs[592 * s] = 0.0 + 0x1.0000000000000p+1 * b90 + b92 + 0x1.0000000000000p+1 * b103 + b106;
-    jvs[593 * s] = 0.0 + b42;
-    jvs[594 * s] = 0.0 + b48;
-    jvs[595 * s] = 0.0 + b47;
-    jvs[596 * s] = 0.0 - b67;
-    jvs[597 * s] = 0.0 - b61;
-    jvs[598 * s] = 0.0 + b44 - b59;
-    jvs[599 * s] = 0.0 + b111;
-    jvs[600 * s] = 0.0 + b114 + b117;
-    jvs[601 * s] = 0.0 + b49 - b71;
-    jvs[602 * s] = 0.0 + b43;
-    jvs[603 * s] = 0.0 + b51;
-    jvs[604 * s] = 0.0 + b322;
-    jvs[605 * s] = 0.0 + 0x1.0000000000000p+1 * b328;
-    jvs[606 * s] = 0.0 + b227;
-    jvs[607 * s] = 0.0 - b79;
-    jvs[608 * s] = 0.0 - b236;
-    jvs[609 * s] = 0.0 + b228 - b234;
-    jvs[610 * s] = 0.0 - b238;
-    jvs[611 * s] = 0.0 + b229;
-    jvs[612 * s] = 0.0 + b231;
-    jvs[613 * s] = 0.0 - b242;
-    jvs[614 * s] = 0.0 + b226;
-    jvs[615 * s] = 0.0 - b65;
-    jvs[616 * s] = 0.0 + b230 + b253;
-    jvs[617 * s] = 0.0 - b240;
-    jvs[618 * s] = 0.0 - b232;
-    jvs[619 * s] = 0.0 + b46;
+    jvs[590 * s] = 0.0 + (r[193 * s] * v[104 * s]) + (r[194 * s] * v[104 * s]) + (r[195 * s] * v[138 * s]) + (r[196 * s] * v[139 * s]) + (r[197 * s] * v[105 * s]) + (r[198 * s] * v[136 * s]) + (r[199 * s] * v[140 * s]) + (r[203 * s] * v[112 * s]) + (r[204 * s] * v[133 * s]) + (r[205 * s] * v[132 * s]) + (r[208 * s] * v[148 * s]) + (r[209 * s] * v[141 * s]) - (r[233 * s] * v[154 * s]) + (r[235 * s] * v[145 * s]) + (r[249 * s] * v[137 * s]) + (r[254 * s] * v[147 * s]);
+    jvs[591 * s] = 0.0 + 0x1.0000000000000p+1 * (r[75 * s] * v[144 * s]) + (r[76 * s] * v[156 * s]) + 0x1.0000000000000p+1 * (r[78 * s] * v[13 * s] * v[144 * s]) + (r[79 * s] * v[13 * s] * v[156 * s]);
+    jvs[592 * s] = 0.0 + 0x1.0000000000000p+1 * (r[72 * s] * v[144 * s]) + (r[73 * s] * v[156 * s]) + 0x1.0000000000000p+1 * (r[78 * s] * v[12 * s] * v[144 * s]) + (r[79 * s] * v[12 * s] * v[156 * s]);
+    jvs[593 * s] = 0.0 + (r[42 * s]);
+    jvs[594 * s] = 0.0 + (r[49 * s]);
+    jvs[595 * s] = 0.0 + (r[47 * s]);
+    jvs[596 * s] = 0.0 - (r[61 * s] * v[155 * s]);
+    jvs[597 * s] = 0.0 - (r[58 * s] * v[155 * s]);
+    jvs[598 * s] = 0.0 + (r[44 * s]) - (r[57 * s] * v[155 * s]);
+    jvs[599 * s] = 0.0 + (r[81 * s] * v[155 * s] * v[156 * s]);
+    jvs[600 * s] = 0.0 + (r[82 * s] * v[155 * s] * v[156 * s]) + (r[83 * s] * v[156 * s]);
+    jvs[601 * s] = 0.0 + (r[50 * s]) - (r[63 * s] * v[155 * s]);
+    jvs[602 * s] = 0.0 + (r[43 * s]);
+    jvs[603 * s] = 0.0 + (r[52 * s]);
+    jvs[604 * s] = 0.0 + (r[241 * s] * v[156 * s]);
+    jvs[605 * s] = 0.0 + 0x1.0000000000000p+1 * (r[245 * s] * v[155 * s] * v[156 * s]);
+    jvs[606 * s] = 0.0 + (r[177 * s]);
+    jvs[607 * s] = 0.0 - (r[67 * s] * v[155 * s]);
+    jvs[608 * s] = 0.0 - (r[184 * s] * v[155 * s]);
+    jvs[609 * s] = 0.0 + (r[178 * s]) - (r[183 * s] * v[155 * s]);
+    jvs[610 * s] = 0.0 - (r[185 * s] * v[155 * s]);
+    jvs[611 * s] = 0.0 + (r[179 * s]);
+    jvs[612 * s] = 0.0 + (r[181 * s]);
+    jvs[613 * s] = 0.0 - (r[187 * s] * v[155 * s]);
+    jvs[614 * s] = 0.0 + (r[176 * s]);
+    jvs[615 * s] = 0.0 - (r[60 * s] * v[155 * s]);
+    jvs[616 * s] = 0.0 + (r[180 * s]) + (r[195 * s] * v[160 * s]);
+    jvs[617 * s] = 0.0 - (r[186 * s] * v[155 * s]);
+    jvs[618 * s] = 0.0 - (r[182 * s] * v[155 * s]);
+    jvs[619 * s] = 0.0 + (r[46 * s]);
     jvs[620 * s] = 0.0;
-    jvs[621 * s] = 0.0 + b40 + 0x1.0000000000000p+1 * b84 + 0x1.0000000000000p+1 * b91 + 0x1.0000000000000p+1 * b97 + 0x1.0000000000000p+1 * b104 + 0x1.0000000000000p+2 * b124;
-    jvs[622 * s] = 0.0 + b81;
-    jvs[623 * s] = 0.0 - b57;
+    jvs[621 * s] = 0.0 + (r[40 * s]) + 0x1.0000000000000p+1 * (r[69 * s] * v[157 * s]) + 0x1.0000000000000p+1 * (r[72 * s] * v[13 * s]) + 0x1.0000000000000p+1 * (r[75 * s] * v[12 * s]) + 0x1.0000000000000p+1 * (r[78 * s] * v[12 * s] * v[13 * s]) + 0x1.0000000000000p+2 * (r[87 * s] * v[158 * s]);
+    jvs[622 * s] = 0.0 + (r[68 * s] * v[155 * s] * v[156 * s]);
+    jvs[623 * s] = 0.0 - (r[56 * s] * v[155 * s]);
     jvs[624 * s] = 0.0;
     jvs[625 * s] = 0.0;
-    jvs[626 * s] = 0.0 + b52 + 0x1.0000000000000p+1 * b130;
-    jvs[627 * s] = 0.0 - b75;
-    jvs[628 * s] = 0.0 - b77;
-    jvs[629 * s] = 0.0 - b69;
-    jvs[630 * s] = 0.0 - b73;
-    jvs[631 * s] = 0.0 + b50;
-    jvs[632 * s] = 0.0 - b53 - b55 - b58 - b60 - b62 - b66 - b68 - b70 - b72 - b74 - b76 - b78 - b80 + b82 + b112 + b115 - b166 - b233 - b235 - b237 - b239 - b241 - b243 + 0x1.0000000000000p+1 * b329;
-    jvs[633 * s] = 0.0 + b41 - b54 + b83 + b86 + b93 + b99 + b107 + b113 + b116 + b118 + 0x1.8000000000000p+1 * b126 + 0x1.0000000000000p+1 * b131 + b323 + 0x1.0000000000000p+1 * b330;
-    jvs[634 * s] = 0.0 + 0x1.0000000000000p+1 * b85 + b87;
-    jvs[635 * s] = 0.0 + 0x1.0000000000000p+2 * b125 + 0x1.8000000000000p+1 * b127 + 0x1.0000000000000p+1 * b128;
-    jvs[636 * s] = 0.0 - b56 + 0x1.0000000000000p+1 * b129;
-    jvs[637 * s] = 0.0 + b254;
-    jvs[638 * s] = 0.0 - b98 - b105;
-    jvs[639 * s] = 0.0 - b92 - b106;
-    jvs[640 * s] = 0.0 - b333;
-    jvs[641 * s] = 0.0 - b111;
-    jvs[642 * s] = 0.0 - b114 - b117;
-    jvs[643 * s] = 0.0 - b322;
-    jvs[644 * s] = 0.0 - b328;
+    jvs[626 * s] = 0.0 + (r[53 * s]) + 0x1.0000000000000p+1 * (r[90 * s] * v[156 * s]);
+    jvs[627 * s] = 0.0 - (r[65 * s] * v[155 * s]);
+    jvs[628 * s] = 0.0 - (r[66 * s] * v[155 * s]);
+    jvs[629 * s] = 0.0 - (r[62 * s] * v[155 * s]);
+    jvs[630 * s] = 0.0 - (r[64 * s] * v[155 * s]);
+    jvs[631 * s] = 0.0 + (r[51 * s]);
+}
+
+KQ_HD KQ_NOINLINE void kqu_jac_10(const double* v, const double* f, const double* r, double* jvs, long long s)
+{
+    jvs[632 * s] = 0.0 - (r[54 * s] * v[156 * s]) - (r[55 * s] * v[159 * s]) - (r[56 * s] * v[146 * s]) - (r[57 * s] * v[114 * s]) - (r[58 * s] * v[113 * s]) - (r[60 * s] * v[137 * s]) - (r[61 * s] * v[111 * s]) - (r[62 * s] * v[152 * s]) - (r[63 * s] * v[123 * s]) - (r[64 * s] * v[153 * s]) - (r[65 * s] * v[150 * s]) - (r[66 * s] * v[151 * s]) - (r[67 * s] * v[129 * s]) + (r[68 * s] * v[145 * s] * v[156 * s]) + (r[81 * s] * v[120 * s] * v[156 * s]) + (r[82 * s] * v[121 * s] * v[156 * s]) - (r[122 * s]) - (r[182 * s] * v[140 * s]) - (r[183 * s] * v[131 * s]) - (r[184 * s] * v[130 * s]) - (r[185 * s] * v[132 * s]) - (r[186 * s] * v[139 * s]) - (r[187 * s] * v[135 * s]) + 0x1.0000000000000p+1 * (r[245 * s] * v[127 * s] * v[156 * s]);
+    jvs[633 * s] = 0.0 + (r[41 * s]) - (r[54 * s] * v[155 * s]) + (r[68 * s] * v[145 * s] * v[155 * s]) + (r[70 * s] * v[157 * s]) + (r[73 * s] * v[13 * s]) + (r[76 * s] * v[12 * s]) + (r[79 * s] * v[12 * s] * v[13 * s]) + (r[81 * s] * v[120 * s] * v[155 * s]) + (r[82 * s] * v[121 * s] * v[155 * s]) + (r[83 * s] * v[121 * s]) + 0x1.8000000000000p+1 * (r[88 * s] * v[158 * s]) + 0x1.0000000000000p+1 * (r[90 * s] * v[149 * s]) + (r[241 * s] * v[126 * s]) + 0x1.0000000000000p+1 * (r[245 * s] * v[127 * s] * v[155 * s]);
+    jvs[634 * s] = 0.0 + 0x1.0000000000000p+1 * (r[69 * s] * v[144 * s]) + (r[70 * s] * v[156 * s]);
+    jvs[635 * s] = 0.0 + 0x1.0000000000000p+2 * (r[87 * s] * v[144 * s]) + 0x1.8000000000000p+1 * (r[88 * s] * v[156 * s]) + 0x1.0000000000000p+1 * (r[89 * s] * v[159 * s]);
+    jvs[636 * s] = 0.0 - (r[55 * s] * v[155 * s]) + 0x1.0000000000000p+1 * (r[89 * s] * v[158 * s]);
+    jvs[637 * s] = 0.0 + (r[195 * s] * v[138 * s]);
+    jvs[638 * s] = 0.0 - (r[76 * s] * v[156 * s]) - (r[79 * s] * v[13 * s] * v[156 * s]);
+    jvs[639 * s] = 0.0 - (r[73 * s] * v[156 * s]) - (r[79 * s] * v[12 * s] * v[156 * s]);
+    jvs[640 * s] = 0.0 - (r[248 * s] * v[156 * s]);
+    jvs[641 * s] = 0.0 - (r[81 * s] * v[155 * s] * v[156 * s]);
+    jvs[642 * s] = 0.0 - (r[82 * s] * v[155 * s] * v[156 * s]) - (r[83 * s] * v[156 * s]);
+    jvs[643 * s] = 0.0 - (r[241 * s] * v[156 * s]);
+    jvs[644 * s] = 0.0 - (r[245 * s] * v[155 * s] * v[156 * s]);
     jvs[645 * s] = 0.0;
-    jvs[646 * s] = 0.0 - b337;
-    jvs[647 * s] = 0.0 + b40;
-    jvs[648 * s] = 0.0 - b81;
-    jvs[649 * s] = 0.0 + b341 + b344;
+    jvs[646 * s] = 0.0 - (r[250 * s] * v[156 * s]);
+    jvs[647 * s] = 0.0 + (r[40 * s]);
+    jvs[648 * s] = 0.0 - (r[68 * s] * v[155 * s] * v[156 * s]);
+    jvs[649 * s] = 0.0 + (r[252 * s]) + (r[254 * s] * v[160 * s]);
     jvs[650 * s] = 0.0;
-    jvs[651 * s] = 0.0 - b130;
+    jvs[651 * s] = 0.0 - (r[90 * s] * v[156 * s]);
     jvs[652 * s] = 0.0;
     jvs[653 * s] = 0.0;
     jvs[654 * s] = 0.0;
     jvs[655 * s] = 0.0;
-    jvs[656 * s] = 0.0 - b53 + b55 - b82 - b112 - b115 - b329;
-    jvs[657 * s] = 0.0 - b41 - b54 - b83 - b86 - b93 - b99 - b107 - b113 - b116 - b118 - b126 - b131 - b168 - b313 - b323 - b330 - b334 - b338;
-    jvs[658 * s] = 0.0 - b87;
-    jvs[659 * s] = 0.0 - b127;
-    jvs[660 * s] = 0.0 + b56;
-    jvs[661 * s] = 0.0 - b314 + b345;
-    jvs[662 * s] = 0.0 + b5;
-    jvs[663 * s] = 0.0 - b84;
-    jvs[664 * s] = 0.0 - b122;
-    jvs[665 * s] = 0.0 - b133;
-    jvs[666 * s] = 0.0;
-    jvs[667 * s] = 0.0;
-    jvs[668 * s] = 0.0 - b86;
-    jvs[669 * s] = 0.0 - b21 - b85 - b87 - b88 - b123 - b134 - b144;
-    jvs[670 * s] = 0.0;
-    jvs[671 * s] = 0.0 - b89;
-    jvs[672 * s] = 0.0;
-    jvs[673 * s] = 0.0 + b13;
-    jvs[674 * s] = 0.0 + b137;
-    jvs[675 * s] = 0.0 + -0x1.0000000000000p+1 * b124;
-    jvs[676 * s] = 0.0 + b305;
-    jvs[677 * s] = 0.0 + b319;
-    jvs[678 * s] = 0.0 - b317;
-    jvs[679 * s] = 0.0 + b135;
-    jvs[680 * s] = 0.0;
-    jvs[681 * s] = 0.0 - b315;
-    jvs[682 * s] = 0.0;
-    jvs[683 * s] = 0.0 + -0x1.0000000000000p+1 * b126;
-    jvs[684 * s] = 0.0;
-    jvs[685 * s] = 0.0 - b29 + -0x1.0000000000000p+1 * b125 + -0x1.0000000000000p+1 * b127 + -0x1.0000000000000p+1 * b128 - b176 - b316 - b318;
-    jvs[686 * s] = 0.0 + -0x1.0000000000000p+1 * b129;
-    jvs[687 * s] = 0.0 + b136 + b138;
-    jvs[688 * s] = 0.0 - b100 - b108;
-    jvs[689 * s] = 0.0 - b94 - b109;
-    jvs[690 * s] = 0.0 - b339;
-    jvs[691 * s] = 0.0 + b342;
-    jvs[692 * s] = 0.0;
-    jvs[693 * s] = 0.0 + b343;
-    jvs[694 * s] = 0.0;
-    jvs[695 * s] = 0.0;
-    jvs[696 * s] = 0.0 - b55;
-    jvs[697 * s] = 0.0 + b41;
-    jvs[698 * s] = 0.0 - b88;
-    jvs[699 * s] = 0.0 - b128;
-    jvs[700 * s] = 0.0 - b56 - b89 - b95 - b101 - b110 - b129 - b169 - b340;
-    jvs[701 * s] = 0.0;
-    jvs[702 * s] = 0.0 - b249 - b251;
-    jvs[703 * s] = 0.0 - b257;
-    jvs[704 * s] = 0.0 - b269;
-    jvs[705 * s] = 0.0 + b331;
-    jvs[706 * s] = 0.0 - b137;
-    jvs[707 * s] = 0.0;
-    jvs[708 * s] = 0.0 + -0x1.0000000000000p+1 * b263;
-    jvs[709 * s] = 0.0 - b267;
-    jvs[710 * s] = 0.0 - b265;
-    jvs[711 * s] = 0.0 - b273;
-    jvs[712 * s] = 0.0 - b271;
-    jvs[713 * s] = 0.0 - b275;
-    jvs[714 * s] = 0.0 - b277;
-    jvs[715 * s] = 0.0 - b259;
-    jvs[716 * s] = 0.0 - b335;
-    jvs[717 * s] = 0.0 - b253;
-    jvs[718 * s] = 0.0 - b255;
-    jvs[719 * s] = 0.0 - b261;
-    jvs[720 * s] = 0.0 - b281;
-    jvs[721 * s] = 0.0;
-    jvs[722 * s] = 0.0 + 0x1.0000000000000p+1 * b248 - b311;
-    jvs[723 * s] = 0.0 + b305;
-    jvs[724 * s] = 0.0 - b344;
-    jvs[725 * s] = 0.0 - b279;
-    jvs[726 * s] = 0.0;
-    jvs[727 * s] = 0.0 + b122 - b309;
-    jvs[728 * s] = 0.0 - b135;
-    jvs[729 * s] = 0.0;
-    jvs[730 * s] = 0.0;
-    jvs[731 * s] = 0.0 - b307;
-    jvs[732 * s] = 0.0;
-    jvs[733 * s] = 0.0 - b313;
-    jvs[734 * s] = 0.0 + b123;
-    jvs[735 * s] = 0.0;
-    jvs[736 * s] = 0.0;
-    jvs[737 * s] = 0.0 - b136 - b138 - b181 - b182 - b250 - b252 - b254 - b256 - b258 - b260 - b262 + -0x1.0000000000000p+1 * b264 - b266 - b268 - b270 - b272 - b274 - b276 - b278 - b280 - b282 + -0x1.0000000000000p+1 * b306 - b308 - b310 - b312 - b314 - b336 - b345;
+    jvs[656 * s] = 0.0 - (r[54 * s] * v[156 * s]) + (r[55 * s] * v[159 * s]) - (r[68 * s] * v[145 * s] * v[156 * s]) - (r[81 * s] * v[120 * s] * v[156 * s]) - (r[82 * s] * v[121 * s] * v[156 * s]) - (r[245 * s] * v[127 * s] * v[156 * s]);
 }
 
-KQ_HD KQ_NOINLINE int kqu_decomp(double* jvs, long long s)
+KQ_HD KQ_NOINLINE void kqu_jac_11(const double* v, const double* f, const double* r, double* jvs, long long s)
+{
+    jvs[657 * s] = 0.0 - (r[41 * s]) - (r[54 * s] * v[155 * s]) - (r[68 * s] * v[145 * s] * v[155 * s]) - (r[70 * s] * v[157 * s]) - (r[73 * s] * v[13 * s]) - (r[76 * s] * v[12 * s]) - (r[79 * s] * v[12 * s] * v[13 * s]) - (r[81 * s] * v[120 * s] * v[155 * s]) - (r[82 * s] * v[121 * s] * v[155 * s]) - (r[83 * s] * v[121 * s]) - (r[88 * s] * v[158 * s]) - (r[90 * s] * v[149 * s]) - (r[124 * s]) - (r[236 * s] * v[160 * s]) - (r[241 * s] * v[126 * s]) - (r[245 * s] * v[127 * s] * v[155 * s]) - (r[248 * s] * v[119 * s]) - (r[250 * s] * v[143 * s]);
+    jvs[658 * s] = 0.0 - (r[70 * s] * v[156 * s]);
+    jvs[659 * s] = 0.0 - (r[88 * s] * v[156 * s]);
+    jvs[660 * s] = 0.0 + (r[55 * s] * v[155 * s]);
+    jvs[661 * s] = 0.0 - (r[236 * s] * v[156 * s]) + (r[254 * s] * v[147 * s]);
+    jvs[662 * s] = 0.0 + (r[5 * s]);
+    jvs[663 * s] = 0.0 - (r[69 * s] * v[157 * s]);
+    jvs[664 * s] = 0.0 - (r[86 * s] * v[157 * s]);
+    jvs[665 * s] = 0.0 - (r[92 * s] * v[157 * s]);
+    jvs[666 * s] = 0.0;
+    jvs[667 * s] = 0.0;
+    jvs[668 * s] = 0.0 - (r[70 * s] * v[157 * s]);
+    jvs[669 * s] = 0.0 - (r[21 * s]) - (r[69 * s] * v[144 * s]) - (r[70 * s] * v[156 * s]) - (r[71 * s] * v[159 * s]) - (r[86 * s] * v[150 * s]) - (r[92 * s] * v[151 * s]) - (r[100 * s]);
+    jvs[670 * s] = 0.0;
+    jvs[671 * s] = 0.0 - (r[71 * s] * v[157 * s]);
+    jvs[672 * s] = 0.0;
+    jvs[673 * s] = 0.0 + (r[13 * s]);
+    jvs[674 * s] = 0.0 + (r[94 * s] * v[160 * s]);
+    jvs[675 * s] = 0.0 + -0x1.0000000000000p+1 * (r[87 * s] * v[158 * s]);
+    jvs[676 * s] = 0.0 + (r[231 * s]);
+    jvs[677 * s] = 0.0 + (r[239 * s]);
+    jvs[678 * s] = 0.0 - (r[238 * s] * v[158 * s]);
+    jvs[679 * s] = 0.0 + (r[93 * s] * v[160 * s]);
+    jvs[680 * s] = 0.0;
+    jvs[681 * s] = 0.0 - (r[237 * s] * v[158 * s]);
+    jvs[682 * s] = 0.0;
+    jvs[683 * s] = 0.0 + -0x1.0000000000000p+1 * (r[88 * s] * v[158 * s]);
+    jvs[684 * s] = 0.0;
+    jvs[685 * s] = 0.0 - (r[29 * s]) + -0x1.0000000000000p+1 * (r[87 * s] * v[144 * s]) + -0x1.0000000000000p+1 * (r[88 * s] * v[156 * s]) + -0x1.0000000000000p+1 * (r[89 * s] * v[159 * s]) - (r[132 * s]) - (r[237 * s] * v[154 * s]) - (r[238 * s] * v[150 * s]);
+    jvs[686 * s] = 0.0 + -0x1.0000000000000p+1 * (r[89 * s] * v[158 * s]);
+    jvs[687 * s] = 0.0 + (r[93 * s] * v[151 * s]) + (r[94 * s] * v[125 * s]);
+    jvs[688 * s] = 0.0 - (r[77 * s] * v[159 * s]) - (r[80 * s] * v[13 * s] * v[159 * s]);
+    jvs[689 * s] = 0.0 - (r[74 * s] * v[159 * s]) - (r[80 * s] * v[12 * s] * v[159 * s]);
+    jvs[690 * s] = 0.0 - (r[251 * s] * v[159 * s]);
+    jvs[691 * s] = 0.0 + (r[253 * s] * v[152 * s]);
+    jvs[692 * s] = 0.0;
+    jvs[693 * s] = 0.0 + (r[253 * s] * v[147 * s]);
+    jvs[694 * s] = 0.0;
+    jvs[695 * s] = 0.0;
+    jvs[696 * s] = 0.0 - (r[55 * s] * v[159 * s]);
+    jvs[697 * s] = 0.0 + (r[41 * s]);
+    jvs[698 * s] = 0.0 - (r[71 * s] * v[159 * s]);
+    jvs[699 * s] = 0.0 - (r[89 * s] * v[159 * s]);
+    jvs[700 * s] = 0.0 - (r[55 * s] * v[155 * s]) - (r[71 * s] * v[157 * s]) - (r[74 * s] * v[13 * s]) - (r[77 * s] * v[12 * s]) - (r[80 * s] * v[12 * s] * v[13 * s]) - (r[89 * s] * v[158 * s]) - (r[125 * s]) - (r[251 * s] * v[143 * s]);
+    jvs[701 * s] = 0.0;
+    jvs[702 * s] = 0.0 - (r[193 * s] * v[160 * s]) - (r[194 * s] * v[160 * s]);
+    jvs[703 * s] = 0.0 - (r[197 * s] * v[160 * s]);
+    jvs[704 * s] = 0.0 - (r[203 * s] * v[160 * s]);
+}
+
+KQ_HD KQ_NOINLINE void kqu_jac_12(const double* v, const double* f, const double* r, double* jvs, long long s)
+{
+    jvs[705 * s] = 0.0 + (r[246 * s] * f[0 * s]);
+    jvs[706 * s] = 0.0 - (r[94 * s] * v[160 * s]);
+    jvs[707 * s] = 0.0;
+    jvs[708 * s] = 0.0 + -0x1.0000000000000p+1 * (r[200 * s] * v[160 * s]);
+    jvs[709 * s] = 0.0 - (r[202 * s] * v[160 * s]);
+    jvs[710 * s] = 0.0 - (r[201 * s] * v[160 * s]);
+    jvs[711 * s] = 0.0 - (r[205 * s] * v[160 * s]);
+    jvs[712 * s] = 0.0 - (r[204 * s] * v[160 * s]);
+    jvs[713 * s] = 0.0 - (r[206 * s] * v[160 * s]);
+    jvs[714 * s] = 0.0 - (r[207 * s] * v[160 * s]);
+    jvs[715 * s] = 0.0 - (r[198 * s] * v[160 * s]);
+    jvs[716 * s] = 0.0 - (r[249 * s] * v[160 * s]);
+    jvs[717 * s] = 0.0 - (r[195 * s] * v[160 * s]);
+    jvs[718 * s] = 0.0 - (r[196 * s] * v[160 * s]);
+    jvs[719 * s] = 0.0 - (r[199 * s] * v[160 * s]);
+    jvs[720 * s] = 0.0 - (r[209 * s] * v[160 * s]);
+    jvs[721 * s] = 0.0;
+    jvs[722 * s] = 0.0 + 0x1.0000000000000p+1 * (r[192 * s]) - (r[235 * s] * v[160 * s]);
+    jvs[723 * s] = 0.0 + (r[231 * s]);
+    jvs[724 * s] = 0.0 - (r[254 * s] * v[160 * s]);
+    jvs[725 * s] = 0.0 - (r[208 * s] * v[160 * s]);
+    jvs[726 * s] = 0.0;
+    jvs[727 * s] = 0.0 + (r[86 * s] * v[157 * s]) - (r[234 * s] * v[160 * s]);
+    jvs[728 * s] = 0.0 - (r[93 * s] * v[160 * s]);
+    jvs[729 * s] = 0.0;
+    jvs[730 * s] = 0.0;
+    jvs[731 * s] = 0.0 - (r[233 * s] * v[160 * s]);
+    jvs[732 * s] = 0.0;
+    jvs[733 * s] = 0.0 - (r[236 * s] * v[160 * s]);
+    jvs[734 * s] = 0.0 + (r[86 * s] * v[150 * s]);
+    jvs[735 * s] = 0.0;
+    jvs[736 * s] = 0.0;
+    jvs[737 * s] = 0.0 - (r[93 * s] * v[151 * s]) - (r[94 * s] * v[125 * s]) - (r[138 * s]) - (r[139 * s]) - (r[193 * s] * v[104 * s]) - (r[194 * s] * v[104 * s]) - (r[195 * s] * v[138 * s]) - (r[196 * s] * v[139 * s]) - (r[197 * s] * v[105 * s]) - (r[198 * s] * v[136 * s]) - (r[199 * s] * v[140 * s]) + -0x1.0000000000000p+1 * (r[200 * s] * v[128 * s]) - (r[201 * s] * v[131 * s]) - (r[202 * s] * v[130 * s]) - (r[203 * s] * v[112 * s]) - (r[204 * s] * v[133 * s]) - (r[205 * s] * v[132 * s]) - (r[206 * s] * v[134 * s]) - (r[207 * s] * v[135 * s]) - (r[208 * s] * v[148 * s]) - (r[209 * s] * v[141 * s]) + -0x1.0000000000000p+1 * (r[232 * s] * 0x1.0000000000000p+1 * v[160 * s]) - (r[233 * s] * v[154 * s]) - (r[234 * s] * v[150 * s]) - (r[235 * s] * v[145 * s]) - (r[236 * s] * v[156 * s]) - (r[249 * s] * v[137 * s]) - (r[254 * s] * v[147 * s]);
+}
+
+KQ_HD inline void kqu_jac(const double* v, const double* f, const double* r, double* jvs, long long s)
+{
+    kqu_jac_0(v, f, r, jvs, s);
+    kqu_jac_1(v, f, r, jvs, s);
+    kqu_jac_2(v, f, r, jvs, s);
+    kqu_jac_3(v, f, r, jvs, s);
+    kqu_jac_4(v, f, r, jvs, s);
+    kqu_jac_5(v, f, r, jvs, s);
+    kqu_jac_6(v, f, r, jvs, s);
+    kqu_jac_7(v, f, r, jvs, s);
+    kqu_jac_8(v, f, r, jvs, s);
+    kqu_jac_9(v, f, r, jvs, s);
+    kqu_jac_10(v, f, r, jvs, s);
+    kqu_jac_11(v, f, r, jvs, s);
+    kqu_jac_12(v, f, r, jvs, s);
+}
+
+KQ_HD KQ_NOINLINE int kqu_decomp_0(double* jvs, long long s)
 {
     if (fabs(jvs[0 * s]) < DBL_MIN) return 1;
     if (fabs(jvs[1 * s]) < DBL_MIN) return 2;
@@ -2255,6 +1737,11 @@ KQ_HD KQ_NOINLINE int kqu_decomp(double* jvs, long long s)
       jvs[310 * s] = jvs[310 * s] + a * jvs[207 * s];
     }
     if (fabs(jvs[313 * s]) < DBL_MIN) return 123;
+    return 0;
+}
+
+KQ_HD KQ_NOINLINE int kqu_decomp_1(double* jvs, long long s)
+{
     if (fabs(jvs[319 * s]) < DBL_MIN) return 124;
     { const double a = -jvs[317 * s] / jvs[255 * s]; jvs[317 * s] = -a;
       jvs[319 * s] = jvs[319 * s] + a * jvs[256 * s];
@@ -2477,6 +1964,11 @@ KQ_HD KQ_NOINLINE int kqu_decomp(double* jvs, long long s)
       jvs[493 * s] = jvs[493 * s] + a * jvs[359 * s];
     }
     if (fabs(jvs[494 * s]) < DBL_MIN) return 151;
+    return 0;
+}
+
+KQ_HD KQ_NOINLINE int kqu_decomp_2(double* jvs, long long s)
+{
     if (fabs(jvs[505 * s]) < DBL_MIN) return 152;
     { const double a = -jvs[500 * s] / jvs[337 * s]; jvs[500 * s] = -a;
       jvs[505 * s] = jvs[505 * s] + a * jvs[338 * s];
@@ -2690,6 +2182,11 @@ KQ_HD KQ_NOINLINE int kqu_decomp(double* jvs, long long s)
       jvs[561 * s] = jvs[561 * s] + a * jvs[511 * s];
       jvs[562 * s] = jvs[562 * s] + a * jvs[512 * s];
     }
+    return 0;
+}
+
+KQ_HD KQ_NOINLINE int kqu_decomp_3(double* jvs, long long s)
+{
     if (fabs(jvs[584 * s]) < DBL_MIN) return 155;
     { const double a = -jvs[563 * s] / jvs[186 * s]; jvs[563 * s] = -a;
       jvs[584 * s] = jvs[584 * s] + a * jvs[187 * s];
@@ -2804,6 +2301,11 @@ KQ_HD KQ_NOINLINE int kqu_decomp(double* jvs, long long s)
       jvs[589 * s] = jvs[589 * s] + a * jvs[561 * s];
       jvs[590 * s] = jvs[590 * s] + a * jvs[562 * s];
     }
+    return 0;
+}
+
+KQ_HD KQ_NOINLINE int kqu_decomp_4(double* jvs, long long s)
+{
     if (fabs(jvs[632 * s]) < DBL_MIN) return 156;
     { const double a = -jvs[591 * s] / jvs[15 * s]; jvs[591 * s] = -a;
     }
@@ -3033,6 +2535,11 @@ KQ_HD KQ_NOINLINE int kqu_decomp(double* jvs, long long s)
       jvs[636 * s] = jvs[636 * s] + a * jvs[589 * s];
       jvs[637 * s] = jvs[637 * s] + a * jvs[590 * s];
     }
+    return 0;
+}
+
+KQ_HD KQ_NOINLINE int kqu_decomp_5(double* jvs, long long s)
+{
     if (fabs(jvs[657 * s]) < DBL_MIN) return 157;
     { const double a = -jvs[638 * s] / jvs[15 * s]; jvs[638 * s] = -a;
     }
@@ -3193,6 +2700,11 @@ KQ_HD KQ_NOINLINE int kqu_decomp(double* jvs, long long s)
       jvs[671 * s] = jvs[671 * s] + a * jvs[660 * s];
       jvs[672 * s] = jvs[672 * s] + a * jvs[661 * s];
     }
+    return 0;
+}
+
+KQ_HD KQ_NOINLINE int kqu_decomp_6(double* jvs, long long s)
+{
     if (fabs(jvs[685 * s]) < DBL_MIN) return 159;
     { const double a = -jvs[673 * s] / jvs[214 * s]; jvs[673 * s] = -a;
       jvs[685 * s] = jvs[685 * s] + a * jvs[215 * s];
@@ -3348,6 +2860,11 @@ KQ_HD KQ_NOINLINE int kqu_decomp(double* jvs, long long s)
       jvs[700 * s] = jvs[700 * s] + a * jvs[686 * s];
       jvs[701 * s] = jvs[701 * s] + a * jvs[687 * s];
     }
+    return 0;
+}
+
+KQ_HD KQ_NOINLINE int kqu_decomp_7(double* jvs, long long s)
+{
     if (fabs(jvs[737 * s]) < DBL_MIN) return 161;
     { const double a = -jvs[702 * s] / jvs[237 * s]; jvs[702 * s] = -a;
       jvs[737 * s] = jvs[737 * s] + a * jvs[238 * s];
@@ -3549,7 +3066,21 @@ KQ_HD KQ_NOINLINE int kqu_decomp(double* jvs, long long s)
     return 0;
 }
 
-KQ_HD KQ_NOINLINE void kqu_solve(const double* jvs, double* x, long long s)
+KQ_HD inline int kqu_decomp(double* jvs, long long s)
+{
+    int rc;
+    if ((rc = kqu_decomp_0(jvs, s)) != 0) return rc;
+    if ((rc = kqu_decomp_1(jvs, s)) != 0) return rc;
+    if ((rc = kqu_decomp_2(jvs, s)) != 0) return rc;
+    if ((rc = kqu_decomp_3(jvs, s)) != 0) return rc;
+    if ((rc = kqu_decomp_4(jvs, s)) != 0) return rc;
+    if ((rc = kqu_decomp_5(jvs, s)) != 0) return rc;
+    if ((rc = kqu_decomp_6(jvs, s)) != 0) return rc;
+    if ((rc = kqu_decomp_7(jvs, s)) != 0) return rc;
+    return 0;
+}
+
+KQ_HD KQ_NOINLINE void kqu_solve_f0(const double* jvs, double* x, long long s)
 {
     x[8 * s] = x[8 * s] - jvs[8 * s] * x[7 * s];
     x[9 * s] = x[9 * s] - jvs[10 * s] * x[5 * s];
@@ -3593,6 +3124,10 @@ KQ_HD KQ_NOINLINE void kqu_solve(const double* jvs, double* x, long long s)
     x[136 * s] = x[136 * s] - jvs[393 * s] * x[105 * s] - jvs[394 * s] * x[134 * s] - jvs[395 * s] * x[135 * s];
     x[138 * s] = x[138 * s] - jvs[404 * s] * x[104 * s];
     x[139 * s] = x[139 * s] - jvs[409 * s] * x[138 * s];
+}
+
+KQ_HD KQ_NOINLINE void kqu_solve_f1(const double* jvs, double* x, long long s)
+{
     x[140 * s] = x[140 * s] - jvs[413 * s] * x[112 * s] - jvs[414 * s] * x[135 * s] - jvs[415 * s] * x[136 * s] - jvs[416 * s] * x[138 * s] - jvs[417 * s] * x[139 * s];
     x[141 * s] = x[141 * s] - jvs[421 * s] * x[89 * s] - jvs[422 * s] * x[137 * s];
     x[142 * s] = x[142 * s] - jvs[428 * s] * x[103 * s] - jvs[429 * s] * x[119 * s] - jvs[430 * s] * x[126 * s];
@@ -3612,7 +3147,15 @@ KQ_HD KQ_NOINLINE void kqu_solve(const double* jvs, double* x, long long s)
     x[157 * s] = x[157 * s] - jvs[662 * s] * x[88 * s] - jvs[663 * s] * x[144 * s] - jvs[664 * s] * x[150 * s] - jvs[665 * s] * x[151 * s] - jvs[666 * s] * x[154 * s] - jvs[667 * s] * x[155 * s] - jvs[668 * s] * x[156 * s];
     x[158 * s] = x[158 * s] - jvs[673 * s] * x[95 * s] - jvs[674 * s] * x[125 * s] - jvs[675 * s] * x[144 * s] - jvs[676 * s] * x[146 * s] - jvs[677 * s] * x[149 * s] - jvs[678 * s] * x[150 * s] - jvs[679 * s] * x[151 * s] - jvs[680 * s] * x[153 * s] - jvs[681 * s] * x[154 * s] - jvs[682 * s] * x[155 * s] - jvs[683 * s] * x[156 * s] - jvs[684 * s] * x[157 * s];
     x[159 * s] = x[159 * s] - jvs[688 * s] * x[12 * s] - jvs[689 * s] * x[13 * s] - jvs[690 * s] * x[143 * s] - jvs[691 * s] * x[147 * s] - jvs[692 * s] * x[148 * s] - jvs[693 * s] * x[152 * s] - jvs[694 * s] * x[153 * s] - jvs[695 * s] * x[154 * s] - jvs[696 * s] * x[155 * s] - jvs[697 * s] * x[156 * s] - jvs[698 * s] * x[157 * s] - jvs[699 * s] * x[158 * s];
+}
+
+KQ_HD KQ_NOINLINE void kqu_solve_f2(const double* jvs, double* x, long long s)
+{
     x[160 * s] = x[160 * s] - jvs[702 * s] * x[104 * s] - jvs[703 * s] * x[105 * s] - jvs[704 * s] * x[112 * s] - jvs[705 * s] * x[122 * s] - jvs[706 * s] * x[125 * s] - jvs[707 * s] * x[126 * s] - jvs[708 * s] * x[128 * s] - jvs[709 * s] * x[130 * s] - jvs[710 * s] * x[131 * s] - jvs[711 * s] * x[132 * s] - jvs[712 * s] * x[133 * s] - jvs[713 * s] * x[134 * s] - jvs[714 * s] * x[135 * s] - jvs[715 * s] * x[136 * s] - jvs[716 * s] * x[137 * s] - jvs[717 * s] * x[138 * s] - jvs[718 * s] * x[139 * s] - jvs[719 * s] * x[140 * s] - jvs[720 * s] * x[141 * s] - jvs[721 * s] * x[142 * s] - jvs[722 * s] * x[145 * s] - jvs[723 * s] * x[146 * s] - jvs[724 * s] * x[147 * s] - jvs[725 * s] * x[148 * s] - jvs[726 * s] * x[149 * s] - jvs[727 * s] * x[150 * s] - jvs[728 * s] * x[151 * s] - jvs[729 * s] * x[152 * s] - jvs[730 * s] * x[153 * s] - jvs[731 * s] * x[154 * s] - jvs[732 * s] * x[155 * s] - jvs[733 * s] * x[156 * s] - jvs[734 * s] * x[157 * s] - jvs[735 * s] * x[158 * s] - jvs[736 * s] * x[159 * s];
+}
+
+KQ_HD KQ_NOINLINE void kqu_solve_b0(const double* jvs, double* x, long long s)
+{
     x[160 * s] = (x[160 * s]) / jvs[737 * s];
     x[159 * s] = (x[159 * s] - jvs[701 * s] * x[160 * s]) / jvs[700 * s];
     x[158 * s] = (x[158 * s] - jvs[686 * s] * x[159 * s] - jvs[687 * s] * x[160 * s]) / jvs[685 * s];
@@ -3655,6 +3198,10 @@ KQ_HD KQ_NOINLINE void kqu_solve(const double* jvs, double* x, long long s)
     x[121 * s] = (x[121 * s] - jvs[311 * s] * x[155 * s] - jvs[312 * s] * x[156 * s]) / jvs[310 * s];
     x[120 * s] = (x[120 * s] - jvs[307 * s] * x[155 * s] - jvs[308 * s] * x[156 * s]) / jvs[306 * s];
     x[119 * s] = (x[119 * s] - jvs[303 * s] * x[156 * s]) / jvs[302 * s];
+}
+
+KQ_HD KQ_NOINLINE void kqu_solve_b1(const double* jvs, double* x, long long s)
+{
     x[118 * s] = (x[118 * s] - jvs[297 * s] * x[152 * s] - jvs[298 * s] * x[156 * s] - jvs[299 * s] * x[159 * s] - jvs[300 * s] * x[160 * s]) / jvs[296 * s];
     x[117 * s] = (x[117 * s] - jvs[288 * s] * x[118 * s] - jvs[289 * s] * x[152 * s] - jvs[290 * s] * x[156 * s] - jvs[291 * s] * x[159 * s] - jvs[292 * s] * x[160 * s]) / jvs[287 * s];
     x[116 * s] = (x[116 * s] - jvs[283 * s] * x[117 * s] - jvs[284 * s] * x[118 * s] - jvs[285 * s] * x[152 * s] - jvs[286 * s] * x[160 * s]) / jvs[282 * s];
@@ -3739,6 +3286,10 @@ KQ_HD KQ_NOINLINE void kqu_solve(const double* jvs, double* x, long long s)
     x[37 * s] = (x[37 * s]) / jvs[76 * s];
     x[36 * s] = (x[36 * s]) / jvs[74 * s];
     x[35 * s] = (x[35 * s] - jvs[72 * s] * x[111 * s]) / jvs[71 * s];
+}
+
+KQ_HD KQ_NOINLINE void kqu_solve_b2(const double* jvs, double* x, long long s)
+{
     x[34 * s] = (x[34 * s] - jvs[70 * s] * x[108 * s]) / jvs[69 * s];
     x[33 * s] = (x[33 * s] - jvs[68 * s] * x[146 * s]) / jvs[67 * s];
     x[32 * s] = (x[32 * s] - jvs[66 * s] * x[160 * s]) / jvs[65 * s];
@@ -3774,4 +3325,14 @@ KQ_HD KQ_NOINLINE void kqu_solve(const double* jvs, double* x, long long s)
     x[2 * s] = (x[2 * s]) / jvs[2 * s];
     x[1 * s] = (x[1 * s]) / jvs[1 * s];
     x[0 * s] = (x[0 * s]) / jvs[0 * s];
+}
+
+KQ_HD inline void kqu_solve(const double* jvs, double* x, long long s)
+{
+    kqu_solve_f0(jvs, x, s);
+    kqu_solve_f1(jvs, x, s);
+    kqu_solve_f2(jvs, x, s);
+    kqu_solve_b0(jvs, x, s);
+    kqu_solve_b1(jvs, x, s);
+    kqu_solve_b2(jvs, x, s);
 }

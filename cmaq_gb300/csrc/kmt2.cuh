@@ -162,7 +162,7 @@ KQ_HD inline double kq_kiepox(const Cell& c, const double* v, const double* f, l
 
 // ionic strength and activity coefficients (aqchem_Rates.F90:423-452), terms in the
 // reference's order (L_HMSMIN twice, as there)
-KQ_HD inline void kq_ionic(Cell& c, const double* v, long long s)
+KQ_HD KQ_NOINLINE void kq_ionic(Cell& c, const double* v, long long s)
 {
 #define V(n) v[(n) * s]
     const double sum = V(L_HPLUS) + V(L_NH4PLUS) + V(L_OHMIN) + V(L_HCO3MIN) + V(L_O2MIN) + V(L_NO2MIN)
@@ -255,7 +255,7 @@ KQ_HD inline double kq_pow(double x, double y)
 // AQCHEM before the integration; y, f, r are the lane's workspace arrays.  Returns 0, or
 // -1 for the reference's MET DATA ERROR (aqchem_kmt.F90:427-431), -2 for its initial pH
 // error (aqchem_Initialize.F90:476-481).
-KQ_HD inline int kq_setup(Cell& c, const double* p, long long n, const double* vmix, double* y, double* f, double* r,
+KQ_HD KQ_NOINLINE int kq_setup(Cell& c, const double* p, long long n, const double* vmix, double* y, double* f, double* r,
                           long long s)
 {
     const float temp2 = (float)p[P_TEMP2 * n], pres_pa = (float)p[P_PRES_PA * n];

@@ -21,8 +21,8 @@ evaluation code (``oracle/kmt2_oracle.c``) walks:
 
 and, for the device code, ``cmaq_gb300/csrc/gen/kmt2_aq_consts.cuh`` (sizes, species
 indices) and ``cmaq_gb300/csrc/gen/kmt2_aq.cuh`` (Henry's law constants, rate constants,
-tolerances, f, J, LU factorisation and solve as strided straight-line code; the rate-law
-functions they call are in ``csrc/kmt2.cuh``).  ``oracle/gen/kmt2_aq_unrolled.c`` holds
+tolerances, f, J, LU factorisation and solve as strided straight-line code in functions
+of about 200 operations; the rate-law functions they call are in ``csrc/kmt2.cuh``).  ``oracle/gen/kmt2_aq_unrolled.c`` holds
 the same straight-line f, J, LU and solve for the oracle's bit-for-bit check, and
 ``cmaq_gb300/mechs/kmt2/manifest.json`` the species names and the FLOP counts of those
 routines (the benchmark's algorithmic work per step).
@@ -580,12 +580,107 @@ def device_source(k: KppMech) -> str:
     out.append("KQ_HD inline void kq_add_diagonal(double* g, double x, long long s)\n{")
     out += [f"    g[{d} * s] = g[{d} * s] + x;" for d in k.lu_diag[:-1]]
     out.append("}\n")
-    body = unrolled_routines(k, qual="KQ_HD KQ_NOINLINE", acc=lambda name, i: f"{name}[{i} * s]")
-    for fn in ("kqu_fun(const double* v, const double* f, const double* r, double* vdot)",
-               "kqu_jac(const double* v, const double* f, const double* r, double* jvs)",
-               "kqu_decomp(double* jvs)", "kqu_solve(const double* jvs, double* x)"):
-        body = body.replace(fn, fn[:-1] + ", long long s)")
-    out.append(body)
+    out.append(device_routines(k))
+    return "\n".join(out)
+
+
+DEVICE_CHUNK_OPS = 200   # LU updates / solve terms per generated device function (bounds register spills)
+
+
+def device_routines(k: KppMech, chunk_ops: int = DEVICE_CHUNK_OPS) -> str:
+    """The straight-line f, J, LU and solve of ``unrolled_routines`` for the device:
+    strided accesses; every tendency and Jacobian entry computed from its products
+    inline (no hundreds of live temporaries; each product is formed from the same
+    operands in the same order, so the bits are those of the oracle's routines); the LU
+    factorisation and the two triangular solves split at row boundaries into functions of
+    about ``chunk_ops`` operations."""
+    acc = lambda name, i: f"{name}[{i} * s]"
+    n = k.nvar
+    q = "KQ_HD KQ_NOINLINE"
+    out = []
+    prod = lambda rx: " * ".join([acc("r", rx)] + [_factor(x, n, acc) for x in k.factors[rx]])
+    def chunked(name, args, call_args, items, cost, line):
+        groups, cur, ops = [], [], 0
+        for it in items:
+            if cur and ops + cost(it) > chunk_ops:
+                groups.append(cur)
+                cur, ops = [], 0
+            cur.append(it)
+            ops += cost(it)
+        if cur:
+            groups.append(cur)
+        for gi, g in enumerate(groups):
+            out.append(f"{q} void {name}_{gi}({args})\n{{")
+            out.extend(line(it) for it in g)
+            out.append("}\n")
+        out.append(f"KQ_HD inline void {name}({args})\n{{")
+        out.extend(f"    {name}_{gi}({call_args});" for gi in range(len(groups)))
+        out.append("}\n")
+
+    fargs = "const double* v, const double* f, const double* r, double* vdot, long long s"
+    chunked("kqu_fun", fargs, "v, f, r, vdot, s", range(n),
+            lambda i: sum(1 + len(k.factors[rx]) for _, rx in k.vdot[i]),
+            lambda i: f"    {acc('vdot', i)} = 0.0" + "".join(_term(c, f"({prod(rx)})") for c, rx in k.vdot[i]) + ";")
+    bprod = lambda b: " * ".join([acc("r", k.blist[b][0])] + ([c_dbl(float(k.blist[b][1]))] if k.blist[b][1] > 1 else [])
+                                 + [_factor(x, n, acc) for x in k.blist[b][2]])
+    jargs = "const double* v, const double* f, const double* r, double* jvs, long long s"
+    chunked("kqu_jac", jargs, "v, f, r, jvs, s", range(len(k.jvs)),
+            lambda e: sum(1 + len(k.blist[b][2]) for _, b in k.jvs[e]) + 1,
+            lambda e: f"    {acc('jvs', e)} = 0.0" + "".join(_term(c, f"({bprod(b)})") for c, b in k.jvs[e]) + ";")
+    pos = {(k.lu_irow[e], k.lu_icol[e]): e for e in range(len(k.lu_irow))}
+
+    def row_cost(row):
+        return sum(1 + k.lu_crow[k.lu_icol[kk] + 1] - k.lu_diag[k.lu_icol[kk]] - 1
+                   for kk in range(k.lu_crow[row], k.lu_diag[row])) + 1
+
+    def split(rows, cost):
+        groups, cur, acc_ops = [], [], 0
+        for row in rows:
+            if cur and acc_ops + cost(row) > chunk_ops:
+                groups.append(cur)
+                cur, acc_ops = [], 0
+            cur.append(row)
+            acc_ops += cost(row)
+        if cur:
+            groups.append(cur)
+        return groups
+
+    dgroups = split(range(n), row_cost)
+    for gi, rows in enumerate(dgroups):
+        out.append(f"{q} int kqu_decomp_{gi}(double* jvs, long long s)\n{{")
+        for row in rows:
+            out.append(f"    if (fabs({acc('jvs', k.lu_diag[row])}) < DBL_MIN) return {row + 1};")
+            for kk in range(k.lu_crow[row], k.lu_diag[row]):
+                j = k.lu_icol[kk]
+                out.append(f"    {{ const double a = -{acc('jvs', kk)} / {acc('jvs', k.lu_diag[j])}; {acc('jvs', kk)} = -a;")
+                for jj in range(k.lu_diag[j] + 1, k.lu_crow[j + 1]):
+                    qq = pos[(row, k.lu_icol[jj])]
+                    out.append(f"      {acc('jvs', qq)} = {acc('jvs', qq)} + a * {acc('jvs', jj)};")
+                out.append("    }")
+        out.append("    return 0;\n}\n")
+    out.append(f"KQ_HD inline int kqu_decomp(double* jvs, long long s)\n{{\n    int rc;")
+    out += [f"    if ((rc = kqu_decomp_{gi}(jvs, s)) != 0) return rc;" for gi in range(len(dgroups))]
+    out.append("    return 0;\n}\n")
+    fgroups = split(range(n), lambda row: k.lu_diag[row] - k.lu_crow[row] + 1)
+    bgroups = split(range(n - 1, -1, -1), lambda row: k.lu_crow[row + 1] - k.lu_diag[row])
+    for gi, rows in enumerate(fgroups):
+        out.append(f"{q} void kqu_solve_f{gi}(const double* jvs, double* x, long long s)\n{{")
+        for row in rows:
+            terms = "".join(f" - {acc('jvs', kk)} * {acc('x', k.lu_icol[kk])}" for kk in range(k.lu_crow[row], k.lu_diag[row]))
+            if terms:
+                out.append(f"    {acc('x', row)} = {acc('x', row)}{terms};")
+        out.append("}\n")
+    for gi, rows in enumerate(bgroups):
+        out.append(f"{q} void kqu_solve_b{gi}(const double* jvs, double* x, long long s)\n{{")
+        for row in rows:
+            terms = "".join(f" - {acc('jvs', kk)} * {acc('x', k.lu_icol[kk])}"
+                            for kk in range(k.lu_diag[row] + 1, k.lu_crow[row + 1]))
+            out.append(f"    {acc('x', row)} = ({acc('x', row)}{terms}) / {acc('jvs', k.lu_diag[row])};")
+        out.append("}\n")
+    out.append(f"KQ_HD inline void kqu_solve(const double* jvs, double* x, long long s)\n{{")
+    out += [f"    kqu_solve_f{gi}(jvs, x, s);" for gi in range(len(fgroups))]
+    out += [f"    kqu_solve_b{gi}(jvs, x, s);" for gi in range(len(bgroups))]
+    out.append("}\n")
     return "\n".join(out)
 
 
