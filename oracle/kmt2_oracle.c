@@ -461,12 +461,13 @@ static double kq_error_norm(const double* y, const double* ynew, const double* y
 }
 
 typedef struct {
-    double a[KQ_NREACT], b[KQ_NB];
     double jac0[KQ_LU_NONZERO], ghimj[KQ_LU_NONZERO];
     double ynew[KQ_NVAR], fcn0[KQ_NVAR], fcn[KQ_NVAR], k[4][KQ_NVAR], yerr[KQ_NVAR];
 } KqWork;
 
 /* ros_Integrator with Rodas3, autonomous (ICNTRL(1) = 1), vector tolerances, the
+ * straight-line f, J, LU and solve (the form of the reference's KPP-generated code, and
+ * bit for bit the table-driven routines' results; tests hold them equal), the
  * reference's defaults: Hmin = 0, Hmax = |Tend - Tstart|, Hstart = 1e-5, FacMin 0.2,
  * FacMax 6, FacRej 0.1, FacSafe 0.9, 200000 steps.  The rate constants follow the
  * accepted state: Fun and Jac call Update_RCONST, which reads the module's VAR, the
@@ -489,9 +490,9 @@ static int kq_ros_integrator(KqState* s, double* y, double tstart, double tend, 
         if ((t + 0.1 * h) == t || h <= roundoff) return -7;
         h = fmin(h, fabs(tend - t));
         kq_update_rconst(s, y);
-        kq_fun(y, s->fix, s->rconst, w->a, w->fcn0);
+        kqu_fun(y, s->fix, s->rconst, w->fcn0);
         st[KQS_NFUN]++;
-        kq_jac(y, s->fix, s->rconst, w->b, w->jac0);
+        kqu_jac(y, s->fix, s->rconst, w->jac0);
         st[KQS_NJAC]++;
         for (;;) {
             /* ros_PrepareMatrix */
@@ -500,7 +501,7 @@ static int kq_ros_integrator(KqState* s, double* y, double tstart, double tend, 
                 for (int i = 0; i < KQ_LU_NONZERO; ++i) w->ghimj[i] = -w->jac0[i];
                 const double ghinv = 1.0 / (h * RD3_GAMMA[0]);
                 for (int i = 0; i < KQ_NVAR; ++i) w->ghimj[kq_lu_diag[i]] = w->ghimj[kq_lu_diag[i]] + ghinv;
-                const int ising = kq_decomp(w->ghimj);
+                const int ising = kqu_decomp(w->ghimj);
                 st[KQS_NDEC]++;
                 if (ising == 0) break;
                 st[KQS_NSNG]++;
@@ -513,12 +514,12 @@ static int kq_ros_integrator(KqState* s, double* y, double tstart, double tend, 
                 } else if (RD3_NEWF[s_]) {
                     memcpy(w->ynew, y, sizeof(w->ynew));
                     for (int j = 0; j < s_; ++j) kq_waxpy(RD3_A[s_ * (s_ - 1) / 2 + j], w->k[j], w->ynew);
-                    kq_fun(w->ynew, s->fix, s->rconst, w->a, w->fcn);
+                    kqu_fun(w->ynew, s->fix, s->rconst, w->fcn);
                     st[KQS_NFUN]++;
                 }
                 memcpy(w->k[s_], w->fcn, sizeof(w->fcn));
                 for (int j = 0; j < s_; ++j) kq_waxpy(RD3_C[s_ * (s_ - 1) / 2 + j] / h, w->k[j], w->k[s_]);
-                kq_solve(w->ghimj, w->k[s_]);
+                kqu_solve(w->ghimj, w->k[s_]);
                 st[KQS_NSOL]++;
             }
             memcpy(w->ynew, y, sizeof(w->ynew));
