@@ -27,3 +27,45 @@ def pytest_collection_modifyitems(config, items):
     for it in items:
         if "gpu" in it.keywords:
             it.add_marker(skip)
+
+
+@pytest.fixture(scope="session")
+def kmt2_harness(tmp_path_factory):
+    """tests/kmt2_host_harness.cpp (the KMT2 device code built for the host) compiled with
+    g++ under AddressSanitizer and UndefinedBehaviorSanitizer; skipped without g++."""
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no C++ compiler")
+    exe = tmp_path_factory.mktemp("kmt2") / "kmt2_host_harness"
+    cmd = [gxx, "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-fsanitize=address,undefined",
+           "-fno-sanitize-recover=all", "-o", str(exe), str(ROOT / "tests" / "kmt2_host_harness.cpp")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0 and "sanitize" in r.stderr:
+        pytest.skip("sanitizer runtime not available")
+    assert r.returncode == 0, r.stderr[-3000:]
+    return exe
+
+
+def run_kmt2_harness(exe, params_t, var_mix_t, nlanes, workdir):
+    """Run the host build on [element][cell] arrays; returns var_out [161][n], fix_out
+    [4][n], stats [10][n], the number of failed cells and the per-lane workspace size."""
+    import os
+    import subprocess
+    import numpy as np
+    n = params_t.shape[1]
+    inp, out = workdir / "in.bin", workdir / "out.bin"
+    np.concatenate([params_t.ravel(), var_mix_t.ravel()]).astype(np.float64).tofile(inp)
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=1:abort_on_error=0", UBSAN_OPTIONS="halt_on_error=1")
+    r = subprocess.run([str(exe), str(inp), str(out), str(n), str(nlanes)], capture_output=True, text=True,
+                       timeout=600, env=env)
+    assert r.returncode == 0, r.stderr[-3000:]
+    assert "runtime error" not in r.stderr, r.stderr[-3000:]
+    raw = out.read_bytes()
+    nv, nf = 161 * n, 4 * n
+    var = np.frombuffer(raw[:8 * nv], np.float64).reshape(161, n)
+    fix = np.frombuffer(raw[8 * nv:8 * (nv + nf)], np.float64).reshape(4, n)
+    st = np.frombuffer(raw[8 * (nv + nf):], np.int32).reshape(10, n)
+    nfail, ws_elems = map(int, r.stdout.split())
+    return var, fix, st, nfail, ws_elems
