@@ -381,3 +381,42 @@ def test_manifest_flop_counts_match_the_generated_code():
     assert counts["decomp"] + man["nvar"] == fl["decomp"]
     assert fl["per_attempt"] == fl["decomp"] + 4 * fl["solve"] + 2 * fl["fun"] + fl["vector"]
     assert man["species"][:2] and len(man["species"]) == man["nvar"] + man["nfix"]
+
+
+@pytest.mark.skipif(not KMT2_DIR.exists(), reason="CMAQ sources not available")
+def test_generator_check_catches_a_wrong_derivation():
+    """The generator's comparison with Jac_SP rejects a Jacobian with one coefficient
+    changed; the LU structure derived from the Jacobian pattern, fill-in included, is
+    JacobianSP's."""
+    from cmaq_gb300.mechgen import kpp_aq as K
+    text = (KMT2_DIR / "aqchem_Function.F90").read_text()
+    factors, vdot = K._function(text, 161, 269)
+    blist, entries = K._derive_jacobian(factors, vdot, 161)
+    lu = K._symbolic_lu(set(entries), 161)
+    jac_text = (KMT2_DIR / "aqchem_Jacobian.F90").read_text()
+    K._check_reference_jacobian(jac_text, 161, factors, blist, lu, entries)   # the derivation passes
+    key = next(kk for kk, v in entries.items() if v)
+    bad = dict(entries)
+    bad[key] = [(2.0 * entries[key][0][0], entries[key][0][1])] + entries[key][1:]
+    with pytest.raises(ValueError, match="Jac_SP"):
+        K._check_reference_jacobian(jac_text, 161, factors, blist, lu, bad)
+    pattern = set(entries)
+    fill = sorted(set(zip(lu[0], lu[1])) - pattern)
+    assert fill, "the mechanism has fill-in"
+    sp = (KMT2_DIR / "aqchem_JacobianSP.F90").read_text()
+    assert [v - 1 for v in K._int_array(sp, "LU_IROW")] == lu[0]
+    assert [v - 1 for v in K._int_array(sp, "LU_ICOL")] == lu[1]
+
+
+def test_cloud_cell_inputs_are_seeded_and_in_range():
+    from cmaq_gb300.synthetic import KMT2_PARAMS, make_cloud_cells
+    a = make_cloud_cells(50, seed=4)
+    b = make_cloud_cells(50, seed=4)
+    c = make_cloud_cells(50, seed=5)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and not np.array_equal(a[1], c[1])
+    p, v = a
+    col = {k: i for i, k in enumerate(KMT2_PARAMS)}
+    assert ((p[:, col["temp2"]] >= 268) & (p[:, col["temp2"]] <= 298)).all()
+    assert (p[:, col["wcavg"]] <= p[:, col["wtavg"]]).all()
+    assert np.array_equal(p[:, col["temp2"]], p[:, col["temp2"]].astype(np.float32))   # REAL arguments
+    assert (v >= 0).all() and (v.max(axis=1) > 3e-4).all()                             # CO2 present
