@@ -26,12 +26,12 @@ KQ_HD inline void kq_henry(Cell& c, float t2)
     c.henry[17] = (double)kq_hlconst((float)0x1.c9c3800000000p+24, (float)0x0.0p+0, t2);   // HIEPOX
     c.henry[18] = (double)kq_hlconst((float)0x1.d4c0000000000p+16, (float)0x0.0p+0, t2);   // HMAE
     c.henry[19] = (double)kq_hlconst((float)0x1.d4c0000000000p+16, (float)0x0.0p+0, t2);   // HHMML
-    c.henry[20] = 0x1.4050000000000p+15 * exp(0x1.1f80000000000p+12 * ((298.0 - (double)t2) / (298.0 * (double)t2)));   // GCOLH
+    c.henry[20] = 0x1.4050000000000p+15 * kq_exp(0x1.1f80000000000p+12 * ((298.0 - (double)t2) / (298.0 * (double)t2)));   // GCOLH
     c.henry[21] = (double)kq_hlconst((float)0x1.0040000000000p+12, (float)0x1.89c0000000000p+12, t2);   // CCOOHH
     c.henry[22] = 0x1.4000000000000p+1;   // HCHOH
     c.henry[23] = (double)kq_hlconst((float)0x1.24f8000000000p+18, (float)0x1.4500000000000p+12, t2);   // PYRACH
     c.henry[24] = (double)kq_hlconst((float)0x1.3333340000000p-1, (float)0x0.0p+0, t2);   // NO3H
-    c.henry[25] = 0x1.599999999999ap+1 * exp(0x1.fb80000000000p+10 * ((298.0 - (double)t2) / (298.0 * (double)t2)));   // CH3O2H
+    c.henry[25] = 0x1.599999999999ap+1 * kq_exp(0x1.fb80000000000p+10 * ((298.0 - (double)t2) / (298.0 * (double)t2)));   // CH3O2H
 }
 
 KQ_HD KQ_NOINLINE void kq_rates_once(const Cell& c, const double* v, const double* f, double* r, long long s)

@@ -17,9 +17,11 @@
 //
 // The same operations in the same order as the reference's Fortran (REAL(4) literals
 // and REAL(4) intermediates kept, no contraction of a*b+c: the library is compiled with
-// -fmad=false).  One cell's arrays live in a lane-interleaved FP64 workspace (element
-// i of a lane at ws[i * s]); inputs and outputs are [element][cell] with stride n.
-// The header compiles as plain C++ too, so the host can run exactly this code.
+// -fmad=false), with exp and x**y by portable series routines (kq_exp, kq_pow) that
+// give the same bits on the host and on the device.  One cell's arrays live in a
+// lane-interleaved FP64 workspace (element i of a lane at ws[i * s]); inputs and
+// outputs are [element][cell] with stride n.  The header compiles as plain C++ too, so
+// the host can run exactly this code.
 #pragma once
 
 #include <float.h>
@@ -55,6 +57,78 @@ struct Cell {   // aqchem_Global of one cell
     double henry[NHENRY];
 };
 
+// ----------------------------------------------------------------------------- portable exp and pow
+// Every exp and x**y of the kinetic core goes through these two routines, on the host
+// and on the device alike, so that the GPU reproduces the oracle bit for bit (CUDA's
+// double exp and pow differ from libm's by ulps, and Rodas3's accept / reject decisions
+// amplify one ulp in a rate constant to 1e-5 in the final state).
+
+// exp(t) by t = n ln2 + r (Cody-Waite split of ln 2, |r| <= ln2/2) and a Taylor series to
+// r^13, with IEEE operations, fma, rint and ldexp only: the same bits on host and device.
+KQ_HD inline double kq_exp(double t)
+{
+    const double ln2_hi = 0x1.62e42fee00000p-1, ln2_lo = 0x1.a39ef35793c76p-33;
+    if (t > 709.0) return INFINITY;
+    if (t < -745.0) return 0.0;
+    const double n = rint(t * 0x1.71547652b82fep+0);
+    const double r = fma(-n, ln2_lo, fma(-n, ln2_hi, t));
+    double e = 0x1.6124613a86d09p-33;
+    e = fma(e, r, 0x1.1eed8eff8d898p-29);
+    e = fma(e, r, 0x1.ae64567f544e4p-26);
+    e = fma(e, r, 0x1.27e4fb7789f5cp-22);
+    e = fma(e, r, 0x1.71de3a556c734p-19);
+    e = fma(e, r, 0x1.a01a01a01a01ap-16);
+    e = fma(e, r, 0x1.a01a01a01a01ap-13);
+    e = fma(e, r, 0x1.6c16c16c16c17p-10);
+    e = fma(e, r, 0x1.1111111111111p-7);
+    e = fma(e, r, 0x1.5555555555555p-5);
+    e = fma(e, r, 0x1.5555555555555p-3);
+    e = fma(e, r, 0.5);
+    e = fma(e, r, 1.0);
+    e = fma(e, r, 1.0);
+    return ldexp(e, (int)n);
+}
+
+// x**y for x >= 0, y > 0 from series with IEEE +, -, *, /, fma, frexp/ldexp and rint only,
+// identical on host and device (the routine of the Gear kernels, gear.cuh: gpow; libm
+// and CUDA pow differ by ulps, which move step-size decisions): log by 2 atanh(s) to
+// s^23 after x = m 2^k, exp by Taylor to r^13 after a Cody-Waite reduction by ln 2.
+KQ_HD inline double kq_pow(double x, double y)
+{
+    if (!(x > 0.0)) return x == 0.0 ? 0.0 : x;
+    if (isinf(x)) return x;
+    int k;
+    double m = frexp(x, &k);
+    if (m < 0x1.6a09e667f3bcdp-1) {
+        m = m * 2.0;
+        k = k - 1;
+    }
+    const double u = (m - 1.0) / (m + 1.0);
+    const double z = u * u;
+    double p = 0x1.642c8590b2164p-5;
+    p = fma(p, z, 0x1.8618618618618p-5);
+    p = fma(p, z, 0x1.af286bca1af28p-5);
+    p = fma(p, z, 0x1.e1e1e1e1e1e1ep-5);
+    p = fma(p, z, 0x1.1111111111111p-4);
+    p = fma(p, z, 0x1.3b13b13b13b14p-4);
+    p = fma(p, z, 0x1.745d1745d1746p-4);
+    p = fma(p, z, 0x1.c71c71c71c71cp-4);
+    p = fma(p, z, 0x1.2492492492492p-3);
+    p = fma(p, z, 0x1.999999999999ap-3);
+    p = fma(p, z, 0x1.5555555555555p-2);
+    p = fma(p, z, 1.0);
+    const double ln2_hi = 0x1.62e42fee00000p-1, ln2_lo = 0x1.a39ef35793c76p-33;
+    const double lx = fma((double)k, ln2_hi, fma((double)k, ln2_lo, (2.0 * u) * p));
+    return kq_exp(y * lx);
+}
+
+// x**y of the rate laws (metal inhibition, activity coefficients): the portable pow, NaN
+// for x < 0 as Fortran's real power of a negative base gives
+KQ_HD inline double kq_rpow(double x, double y)
+{
+    return x < 0.0 ? NAN : kq_pow(x, y);
+}
+
 // ----------------------------------------------------------------------------- rate laws
 
 // Schwartz (1986) mass-transfer coefficient of KMTF / KMTB (aqchem_Initialize.F90:53-104);
@@ -78,19 +152,19 @@ KQ_HD inline double kq_kmtb(const Cell& c, double hl, double accom, double dg, d
 // aqchem_Initialize.F90:106-117
 KQ_HD inline double kq_hydf(const Cell& c, double kf, double dh)
 {
-    const double k = kf * exp(dh * c.delinvt);
+    const double k = kf * kq_exp(dh * c.delinvt);
     return k * c.phi2;
 }
 // aqchem_Initialize.F90:132-152 (a negative J: the COSZEN estimate scaled by PHOTO)
 KQ_HD inline double kq_kphot(const Cell& c, double maxc, double jval)
 {
     if (!(jval < 0.0)) return jval;
-    return c.czen > 0.001 ? c.photo * 2.718281828 * maxc * exp(-1.0 / c.czen) : 0.0;
+    return c.czen > 0.001 ? c.photo * 2.718281828 * maxc * kq_exp(-1.0 / c.czen) : 0.0;
 }
 // aqchem_Rates.F90:146-158
 KQ_HD inline double kq_disf(const Cell& c, double keq, double dh, double kb, int g1)
 {
-    const double k = kb * (keq * exp(dh * c.delinvt));
+    const double k = kb * (keq * kq_exp(dh * c.delinvt));
     return g1 == 1 ? k * c.gm1 : k;
 }
 // aqchem_Rates.F90:160-174
@@ -108,7 +182,7 @@ KQ_HD inline double kq_diffusion_factor(const Cell& c, double krate)
     const double q1 = krate < 0.0 ? 0.0 : c.ddiam / 2.0 * sqrt(krate / 1.0e-9);
     if (!(q1 > 1.0e-3)) return 1.0;
     if (q1 > 100.0) return 3.0 / q1;
-    const double e2 = exp(2.0 * q1);
+    const double e2 = kq_exp(2.0 * q1);
     const double coth = (e2 + 1.0) / (e2 - 1.0);
     const double q = 3.0 * ((coth / q1) - (1.0 / (q1 * q1)));
     return q > 1.0 ? 1.0 : q;
@@ -118,18 +192,18 @@ KQ_HD inline double kq_krxn(const Cell& c, const double* v, long long s, double 
                             int metal)
 {
     const double phi2 = c.phi2;
-    double k = kr * exp(dh * c.delinvt);
+    double k = kr * kq_exp(dh * c.delinvt);
     if (rtype == 1) k = (k / (1.0 + 13.0 * v[L_HPLUS * s] * phi2)) * phi2;
     else if (rtype == 3) k = k * phi2;
     else if (rtype == 4) k = k / phi2;
     if (metal > 0) {
         const double s6 = (v[L_H2SO4 * s] + v[L_HSO4MIN * s] + v[L_SO4MIN2 * s]) * phi2;
-        k = k / (1.0 + 75.0 * pow(s6, 0.67));
+        k = k / (1.0 + 75.0 * kq_rpow(s6, 0.67));
     }
     if (qy >= 1) {
-        const double k1 = 2.4e+4 * exp(0.0 * c.delinvt);
-        const double k2 = 3.7e+5 * exp(-5530.88 * c.delinvt);
-        const double k3 = 1.5e+9 * exp(-5280.56 * c.delinvt);
+        const double k1 = 2.4e+4 * kq_exp(0.0 * c.delinvt);
+        const double k2 = 3.7e+5 * kq_exp(-5530.88 * c.delinvt);
+        const double k3 = 1.5e+9 * kq_exp(-5280.56 * c.delinvt);
         const double kt = (k1 * v[L_SO2 * s] + k2 * v[L_HSO3MIN * s] + k3 * v[L_SO3MIN2 * s]) * phi2;
         k = k * kq_diffusion_factor(c, kt);
     }
@@ -176,35 +250,9 @@ KQ_HD KQ_NOINLINE void kq_ionic(Cell& c, const double* v, long long s)
 #undef V
     c.stion = 0.5 * sum * c.phi2;
     const double lg1 = -0.509 * (sqrt(c.stion) / (1.0 + sqrt(c.stion)) - 0.2 * c.stion);
-    c.gm1 = pow(10.0, lg1);
-    const double gm2 = pow(10.0, lg1 * 4.0);
+    c.gm1 = kq_rpow(10.0, lg1);
+    const double gm2 = kq_rpow(10.0, lg1 * 4.0);
     c.gm2 = gm2 > 1.0e-30 ? gm2 : 1.0e-30;
-}
-
-// exp(t) by t = n ln2 + r (Cody-Waite split of ln 2, |r| <= ln2/2) and a Taylor series to
-// r^13, with IEEE operations, fma, rint and ldexp only: the same bits on host and device.
-KQ_HD inline double kq_exp(double t)
-{
-    const double ln2_hi = 0x1.62e42fee00000p-1, ln2_lo = 0x1.a39ef35793c76p-33;
-    if (t > 709.0) return INFINITY;
-    if (t < -745.0) return 0.0;
-    const double n = rint(t * 0x1.71547652b82fep+0);
-    const double r = fma(-n, ln2_lo, fma(-n, ln2_hi, t));
-    double e = 0x1.6124613a86d09p-33;
-    e = fma(e, r, 0x1.1eed8eff8d898p-29);
-    e = fma(e, r, 0x1.ae64567f544e4p-26);
-    e = fma(e, r, 0x1.27e4fb7789f5cp-22);
-    e = fma(e, r, 0x1.71de3a556c734p-19);
-    e = fma(e, r, 0x1.a01a01a01a01ap-16);
-    e = fma(e, r, 0x1.a01a01a01a01ap-13);
-    e = fma(e, r, 0x1.6c16c16c16c17p-10);
-    e = fma(e, r, 0x1.1111111111111p-7);
-    e = fma(e, r, 0x1.5555555555555p-5);
-    e = fma(e, r, 0x1.5555555555555p-3);
-    e = fma(e, r, 0.5);
-    e = fma(e, r, 1.0);
-    e = fma(e, r, 1.0);
-    return ldexp(e, (int)n);
 }
 
 // HLCONST with EFFECTIVE = .FALSE. (hlconst.F:509-511), REAL(4) throughout; its EXP is
@@ -214,39 +262,6 @@ KQ_HD inline float kq_hlconst(float a, float e, float temp)
 {
     const float tfac = (298.0f - temp) / (298.0f * temp);
     return a * (float)kq_exp((double)(e * tfac));
-}
-
-// x**y for x >= 0, y > 0 from series with IEEE +, -, *, /, fma, frexp/ldexp and rint only,
-// identical on host and device (the routine of the Gear kernels, gear.cuh: gpow; libm
-// and CUDA pow differ by ulps, which move step-size decisions): log by 2 atanh(s) to
-// s^23 after x = m 2^k, exp by Taylor to r^13 after a Cody-Waite reduction by ln 2.
-KQ_HD inline double kq_pow(double x, double y)
-{
-    if (!(x > 0.0)) return x == 0.0 ? 0.0 : x;
-    if (isinf(x)) return x;
-    int k;
-    double m = frexp(x, &k);
-    if (m < 0x1.6a09e667f3bcdp-1) {
-        m = m * 2.0;
-        k = k - 1;
-    }
-    const double u = (m - 1.0) / (m + 1.0);
-    const double z = u * u;
-    double p = 0x1.642c8590b2164p-5;
-    p = fma(p, z, 0x1.8618618618618p-5);
-    p = fma(p, z, 0x1.af286bca1af28p-5);
-    p = fma(p, z, 0x1.e1e1e1e1e1e1ep-5);
-    p = fma(p, z, 0x1.1111111111111p-4);
-    p = fma(p, z, 0x1.3b13b13b13b14p-4);
-    p = fma(p, z, 0x1.745d1745d1746p-4);
-    p = fma(p, z, 0x1.c71c71c71c71cp-4);
-    p = fma(p, z, 0x1.2492492492492p-3);
-    p = fma(p, z, 0x1.999999999999ap-3);
-    p = fma(p, z, 0x1.5555555555555p-2);
-    p = fma(p, z, 1.0);
-    const double ln2_hi = 0x1.62e42fee00000p-1, ln2_lo = 0x1.a39ef35793c76p-33;
-    const double lx = fma((double)k, ln2_hi, fma((double)k, ln2_lo, (2.0 * u) * p));
-    return kq_exp(y * lx);
 }
 
 #include "gen/kmt2_aq.cuh"
@@ -289,8 +304,8 @@ KQ_HD KQ_NOINLINE int kq_setup(Cell& c, const double* p, long long n, const doub
     for (int i = 0; i < NFIX; ++i) f[i * s] = c.cfactor * 0.0;
     f[L_H2O * s] = 55.5 * c.invphi2;
     f[G_HO * s] = p[P_HO * n] * c.cfactor;
-    f[L_O2 * s] = (double)0.21f * c.press * 1.3e-3 * exp(1500.0 * c.delinvt) * c.invphi2;
-    const double kw = 1.00e-14 * exp(-6.955e+03 * c.delinvt);
+    f[L_O2 * s] = (double)0.21f * c.press * 1.3e-3 * kq_exp(1500.0 * c.delinvt) * c.invphi2;
+    const double kw = 1.00e-14 * kq_exp(-6.955e+03 * c.delinvt);
     double pos = 2.0 * (y[L_CAPLUS2 * s] + y[L_MGPLUS2 * s]) + y[L_NAPLUS * s] + y[L_KPLUS * s] + y[L_NH4PLUS * s];
     double neg = 2.0 * (y[L_SO4MIN2 * s] + y[L_OXLACMIN2 * s]) + y[L_NO3MIN * s] + y[L_CLMIN * s];
     pos = pos * c.phi2;
@@ -433,8 +448,9 @@ KQ_HD inline int kq_integrate(Cell& c, double* ws, long long s, double tstart, d
 }
 
 // One cloudy cell: set-up, AQCHEM's integration loop, the state (molec/cm3) to vout and
-// the fixed species to fout (if given); statistics to st[S_* * n].  Returns 0 when the
-// integration finished.
+// the fixed species to fout (if given); statistics to st[S_* * n].  A cell whose set-up
+// fails (IERR -101, -102) gets NaN in vout and fout.  Returns 0 when the integration
+// finished.
 KQ_HD inline int kq_cell(const double* p, const double* vmix, double* vout, double* fout, int* st_out, long long n,
                          double* ws, long long s)
 {
@@ -444,8 +460,11 @@ KQ_HD inline int kq_cell(const double* p, const double* vmix, double* vout, doub
     double* y = ws + W_Y * s;
     double* f = ws + W_F * s;
     int ierr = kq_setup(c, p, n, vmix, y, f, ws + W_R * s, s);
-    if (ierr != 0) {
+    if (ierr != 0) {   // no state to return: NaN marks the cell's outputs
         ierr -= 100;
+        for (int i = 0; i < NVAR; ++i) vout[i * n] = NAN;
+        if (fout)
+            for (int i = 0; i < NFIX; ++i) fout[i * n] = NAN;
     } else {
         double t = 0.0;
         ierr = 1;

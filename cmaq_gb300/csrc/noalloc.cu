@@ -47,7 +47,9 @@ int noalloc_fail(const std::string& msg)
     return -1;
 }
 
-// Device address of the scratch array on `device` (current), looked up once per device.
+// Device address of the scratch array on `device` (current), looked up once per device
+// and kept until the process exits (a cudaDeviceReset would leave it stale; the header
+// tells callers not to call again after one).
 cudaError_t scratch_on(int device, double** out)
 {
     std::lock_guard<std::mutex> lock(g_setup_mutex);

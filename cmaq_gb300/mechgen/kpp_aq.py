@@ -554,7 +554,7 @@ def device_source(k: KppMech) -> str:
         if kind == "hlconst":
             out.append(f"    c.henry[{h}] = (double)kq_hlconst((float){c_dbl(a)}, (float){c_dbl(e)}, t2);   // {name}")
         elif kind == "exp":
-            out.append(f"    c.henry[{h}] = {c_dbl(a)} * exp({c_dbl(e)} * ((298.0 - (double)t2) / (298.0 * (double)t2)));"
+            out.append(f"    c.henry[{h}] = {c_dbl(a)} * kq_exp({c_dbl(e)} * ((298.0 - (double)t2) / (298.0 * (double)t2)));"
                        f"   // {name}")
         else:
             out.append(f"    c.henry[{h}] = {c_dbl(a)};   // {name}")

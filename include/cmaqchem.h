@@ -16,7 +16,7 @@
  * AEROSOL_CHEMISTRY (rbdriver.F:409, 499-511).
  *
  * Array layouts are the reference's Fortran layouts, so a Fortran caller passes
- * its arrays unchanged (see the ISO_C_BINDING shim in INTEGRATION.md):
+ * its arrays unchanged (the ISO_C_BINDING drop-in chem_gpu.F beside this header):
  *     conc    CONC(NCOLS, NROWS, NLAYS, NSPCSD)   REAL(4)
  *     ta, qv, dens, pres  (NCOLS, NROWS, NLAYS)   REAL(4)  K, kg/kg, kg/m3, Pa
  *     seaice, ocean_szone (NCOLS, NROWS)          REAL(4)  fractions
@@ -233,10 +233,12 @@ void cmaqchem_destroy(cmaqchem_handle* h);
  * the caller passes the device arrays y, rki, night and (optionally) status exactly as
  * for cmaqchem_ros3_solve_device.  The first call on a device, with that device current,
  * looks up the array's device address; make that first call before any stream capture.
- * All calls share the array: calls whose kernels overlap on the GPU race and must be
- * serialised by the caller.  ncell above CMAQCHEM_NOALLOC_MAX_CELLS is rejected, as is a
- * mechanism whose per-block workspace does not fit the array.  Runs on the current
- * device, returns 0 or -1 (text from cmaqchem_last_error). */
+ * The address is kept for the life of the process, so a cudaDeviceReset leaves it stale:
+ * do not call this entry point again after resetting the device.  All calls share the
+ * array: calls whose kernels overlap on the GPU race and must be serialised by the
+ * caller.  ncell above CMAQCHEM_NOALLOC_MAX_CELLS is rejected, as is a mechanism whose
+ * per-block workspace does not fit the array.  Runs on the current device and
+ * synchronises `stream` before it returns 0, or -1 (text from cmaqchem_last_error). */
 #define CMAQCHEM_NOALLOC_SCRATCH_BYTES (64ull << 20)
 #define CMAQCHEM_NOALLOC_MAX_CELLS (1ll << 31)
 int cmaqchem_ros3_solve_noalloc(const char* mechanism, long long ncell, double* y, const double* rki,
@@ -256,7 +258,8 @@ int cmaqchem_ros3_solve_noalloc(const char* mechanism, long long ncell, double* 
  *   var_mix [CMAQCHEM_KMT2_NVAR][ncell]: the KPP state as Initialize maps GAS and AEROSOL
  *           (aqchem_Initialize.F90:308-421, mol/molV; L_HPLUS and L_OHMIN are recomputed);
  *   var_out [CMAQCHEM_KMT2_NVAR][ncell]: the state at TAUCLD (molec/cm3, KPP's units);
- *   fix_out [CMAQCHEM_KMT2_NFIX][ncell] or NULL: the fixed species;
+ *           NaN for a cell whose set-up failed (IERR -101 or -102);
+ *   fix_out [CMAQCHEM_KMT2_NFIX][ncell] or NULL: the fixed species (NaN as var_out);
  *   stats   [CMAQCHEM_KMT2_NSTAT][ncell] int: steps, accepted, rejected, f and J evaluations,
  *           factorisations, solves, singular factorisations, IERR (1 = success; < 0: the
  *           reference's ros_ErrorMsg codes, -101 / -102 for its MET DATA and initial pH

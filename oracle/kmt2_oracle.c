@@ -27,8 +27,11 @@
  * Arithmetic follows the reference's Fortran: the same operation order, REAL(4)
  * literals and REAL(4) intermediates where the reference has them, no contraction of
  * a*b+c (built with -ffp-contract=off; the reference's build flags decide that for
- * the Fortran, which cannot be compiled here).  The step-size factor Err**(1/3) uses
- * the portable pow of portable_pow.h and HLCONST's REAL(4) EXP its portable exp.
+ * the Fortran, which cannot be compiled here).  Every EXP and ** (the rate laws,
+ * HLCONST's REAL(4) EXP, the activity coefficients, the step-size factor Err**(1/3))
+ * uses the portable exp and pow of portable_pow.h, which the device code restates
+ * operation for operation: libm's and CUDA's exp and pow differ by ulps, and Rodas3's
+ * accept / reject decisions amplify one ulp in a rate constant to 1e-5 in the state.
  */
 #include <float.h>
 #include <math.h>
@@ -38,6 +41,10 @@
 #include "gen/kmt2_aq.c"
 #include "gen/kmt2_aq_unrolled.c"
 #include "portable_pow.h"
+
+/* x**y of the rate laws: the portable pow, NaN for x < 0 (Fortran's real power of a
+ * negative base) */
+static double kq_rpow(double x, double y) { return x < 0.0 ? NAN : portable_pow(x, y); }
 
 /* per-cell parameters: the AQCHEM arguments the kinetic core reads */
 enum {
@@ -111,14 +118,14 @@ static double kq_kmtb(const KqState* s, double hl, double accom, double dg, doub
 /* aqchem_Initialize.F90:106-117 */
 static double kq_hydf(const KqState* s, double kf, double dh)
 {
-    double v = kf * exp(dh * s->delinvt);
+    double v = kf * portable_exp(dh * s->delinvt);
     return v * s->phi2;
 }
 /* aqchem_Initialize.F90:132-152 */
 static double kq_kphot(const KqState* s, double maxc, double jval)
 {
     if (jval < 0.0) {
-        if (s->czen > 0.001) return s->photo * 2.718281828 * maxc * exp(-1.0 / s->czen);
+        if (s->czen > 0.001) return s->photo * 2.718281828 * maxc * portable_exp(-1.0 / s->czen);
         return 0.0;
     }
     return jval;
@@ -127,7 +134,7 @@ static double kq_kphot(const KqState* s, double maxc, double jval)
 /* aqchem_Rates.F90:146-158 */
 static double kq_disf(const KqState* s, double keq, double dh, double kb, int g1)
 {
-    double v = kb * (keq * exp(dh * s->delinvt));
+    double v = kb * (keq * portable_exp(dh * s->delinvt));
     if (g1 == 1) v = v * s->gm1;
     return v;
 }
@@ -149,7 +156,7 @@ static double kq_diffusion_q(const KqState* s, double krate)
     double q;
     if (q1 > 1.0e-3) {
         if (q1 <= 100.0) {
-            const double e2 = exp(2.0 * q1);
+            const double e2 = portable_exp(2.0 * q1);
             const double cothq = (e2 + 1.0) / (e2 - 1.0);
             q = 3.0 * ((cothq / q1) - (1.0 / (q1 * q1)));
             if (q > 1.0) q = 1.0;
@@ -165,16 +172,16 @@ static double kq_diffusion_q(const KqState* s, double krate)
 static double kq_krxn(const KqState* s, const double* var, double kr, double dh, int rtype, int qy, int metal)
 {
     const double phi2 = s->phi2;
-    const double sviinh = 1.0 + 75.0 * pow((var[KQ_L_H2SO4] + var[KQ_L_HSO4MIN] + var[KQ_L_SO4MIN2]) * phi2, 0.67);
-    double k = kr * exp(dh * s->delinvt);
+    const double sviinh = 1.0 + 75.0 * kq_rpow((var[KQ_L_H2SO4] + var[KQ_L_HSO4MIN] + var[KQ_L_SO4MIN2]) * phi2, 0.67);
+    double k = kr * portable_exp(dh * s->delinvt);
     if (rtype == 1) k = (k / (1.0 + 13.0 * var[KQ_L_HPLUS] * phi2)) * phi2;
     else if (rtype == 3) k = k * phi2;
     else if (rtype == 4) k = k / phi2;
     if (metal > 0) k = k / sviinh;
     if (qy >= 1) {
-        const double ko31 = 2.4e+4 * exp(0.0 * s->delinvt);
-        const double ko32 = 3.7e+5 * exp(-5530.88 * s->delinvt);
-        const double ko33 = 1.5e+9 * exp(-5280.56 * s->delinvt);
+        const double ko31 = 2.4e+4 * portable_exp(0.0 * s->delinvt);
+        const double ko32 = 3.7e+5 * portable_exp(-5530.88 * s->delinvt);
+        const double ko33 = 1.5e+9 * portable_exp(-5280.56 * s->delinvt);
         const double ko3t = (ko31 * var[KQ_L_SO2] + ko32 * var[KQ_L_HSO3MIN] + ko33 * var[KQ_L_SO3MIN2]) * phi2;
         k = k * kq_diffusion_q(s, ko3t);
     }
@@ -239,8 +246,8 @@ static void kq_ionic(KqState* s, const double* v)
     const double rs = sqrt(s->stion);
     const double gm1log = -0.509 * (rs / (1.0 + sqrt(s->stion)) - 0.2 * s->stion);
     const double gm2log = gm1log * 4.0;
-    s->gm1 = pow(10.0, gm1log);
-    const double gm2 = pow(10.0, gm2log);
+    s->gm1 = kq_rpow(10.0, gm1log);
+    const double gm2 = kq_rpow(10.0, gm2log);
     s->gm2 = gm2 > 1.0e-30 ? gm2 : 1.0e-30;
 }
 
@@ -293,7 +300,7 @@ static int kq_setup(const double* p, const double* var_mix, KqState* s, double* 
         if (kq_henry_kind[h] == 0)
             s->henry[h] = (double)kq_hlconst((float)kq_henry_a[h], (float)kq_henry_e[h], temp2);
         else if (kq_henry_kind[h] == 1)
-            s->henry[h] = kq_henry_a[h] * exp(kq_henry_e[h] * ((298.0 - (double)temp2) / (298.0 * (double)temp2)));
+            s->henry[h] = kq_henry_a[h] * portable_exp(kq_henry_e[h] * ((298.0 - (double)temp2) / (298.0 * (double)temp2)));
         else
             s->henry[h] = kq_henry_a[h];
     }
@@ -329,8 +336,8 @@ static int kq_setup(const double* p, const double* var_mix, KqState* s, double* 
     for (int i = 0; i < KQ_NFIX; ++i) s->fix[i] = s->cfactor * 0.0;
     s->fix[KQ_L_H2O] = 55.5 * s->invphi2;
     s->fix[KQ_G_HO] = p[KQP_HO] * s->cfactor;
-    s->fix[KQ_L_O2] = (double)0.21f * s->press * 1.3e-3 * exp(1500.0 * s->delinvt) * s->invphi2;
-    const double kw = 1.00e-14 * exp(-6.955e+03 * s->delinvt);
+    s->fix[KQ_L_O2] = (double)0.21f * s->press * 1.3e-3 * portable_exp(1500.0 * s->delinvt) * s->invphi2;
+    const double kw = 1.00e-14 * portable_exp(-6.955e+03 * s->delinvt);
     double sumpos = 2.0 * (var[KQ_L_CAPLUS2] + var[KQ_L_MGPLUS2]) + var[KQ_L_NAPLUS] + var[KQ_L_KPLUS]
                   + var[KQ_L_NH4PLUS];
     double sumneg = 2.0 * (var[KQ_L_SO4MIN2] + var[KQ_L_OXLACMIN2]) + var[KQ_L_NO3MIN] + var[KQ_L_CLMIN];
@@ -562,7 +569,10 @@ static int kq_cell(const double* p, const double* var_mix, double* var_out, doub
     KqState s;
     memset(st, 0, sizeof(int) * KQ_NSTAT);
     int rc = kq_setup(p, var_mix, &s, var_out);
-    if (rc != 0) {
+    if (rc != 0) {   /* no state to return: NaN marks the cell's outputs */
+        for (int i = 0; i < KQ_NVAR; ++i) var_out[i] = NAN;
+        if (fix_out)
+            for (int i = 0; i < KQ_NFIX; ++i) fix_out[i] = NAN;
         st[KQS_IERR] = rc - 100;
         return 1;
     }

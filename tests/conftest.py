@@ -8,6 +8,15 @@ sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "oracle"))
 
 
+def cmaq_root() -> Path:
+    """The CMAQ source tree the generator checks read: $CMAQ_ROOT, else a checkout named
+    ``reference`` beside this repository.  Tests that need it skip when neither holds
+    ``CCTM``."""
+    import os
+    env = os.environ.get("CMAQ_ROOT")
+    return Path(env) if env else ROOT.parent / "reference"
+
+
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU and the built libcmaqchem.so")
 

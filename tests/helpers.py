@@ -90,3 +90,58 @@ def writeback(g: GridInputs, o, y):
             v = (np.float64(F32(1.0) / fwd) * dens) * v
         out[g.cgrid_index[s] - 1] = v.astype(F32)
     return out.reshape(g.conc.shape)
+
+
+def _fma(a: float, b: float, c: float) -> float:
+    """a * b + c rounded once (exact rational arithmetic, then one round to nearest)."""
+    from fractions import Fraction
+    return float(Fraction(a) * Fraction(b) + Fraction(c))
+
+
+_h = float.fromhex
+_EXP_SERIES = [_h("0x1.6124613a86d09p-33"), _h("0x1.1eed8eff8d898p-29"), _h("0x1.ae64567f544e4p-26"), _h("0x1.27e4fb7789f5cp-22"),
+               _h("0x1.71de3a556c734p-19"), _h("0x1.a01a01a01a01ap-16"), _h("0x1.a01a01a01a01ap-13"), _h("0x1.6c16c16c16c17p-10"),
+               _h("0x1.1111111111111p-7"), _h("0x1.5555555555555p-5"), _h("0x1.5555555555555p-3"), 0.5, 1.0, 1.0]
+_LOG_SERIES = [_h("0x1.642c8590b2164p-5"), _h("0x1.8618618618618p-5"), _h("0x1.af286bca1af28p-5"), _h("0x1.e1e1e1e1e1e1ep-5"),
+               _h("0x1.1111111111111p-4"), _h("0x1.3b13b13b13b14p-4"), _h("0x1.745d1745d1746p-4"), _h("0x1.c71c71c71c71cp-4"),
+               _h("0x1.2492492492492p-3"), _h("0x1.999999999999ap-3"), _h("0x1.5555555555555p-2"), 1.0]
+_LN2_HI, _LN2_LO = _h("0x1.62e42fee00000p-1"), _h("0x1.a39ef35793c76p-33")
+
+
+def portable_exp(t: float) -> float:
+    """exp(t) of the oracle's portable series (t = n ln2 + r, Cody-Waite split of ln 2,
+    Taylor series to r^13), restated in Python with exact fused multiply-adds: the bits
+    the oracle and the device code compute."""
+    import math
+    t = float(t)
+    if t > 709.0:
+        return math.inf
+    if t < -745.0:
+        return 0.0
+    n = float(round(t * _h("0x1.71547652b82fep+0")))   # round half to even, as rint
+    r = _fma(-n, _LN2_LO, _fma(-n, _LN2_HI, t))
+    e = _EXP_SERIES[0]
+    for c in _EXP_SERIES[1:]:
+        e = _fma(e, r, c)
+    return math.ldexp(e, int(n))
+
+
+def portable_pow(x: float, y: float) -> float:
+    """x**y of the oracle's portable series (log by 2 atanh(s) to s^23 after x = m 2^k),
+    restated in Python like portable_exp."""
+    import math
+    x, y = float(x), float(y)
+    if not x > 0.0:
+        return 0.0 if x == 0.0 else x
+    if math.isinf(x):
+        return x
+    m, k = math.frexp(x)
+    if m < _h("0x1.6a09e667f3bcdp-1"):
+        m, k = m * 2.0, k - 1
+    s = (m - 1.0) / (m + 1.0)
+    z = s * s
+    p = _LOG_SERIES[0]
+    for c in _LOG_SERIES[1:]:
+        p = _fma(p, z, c)
+    lx = _fma(float(k), _LN2_HI, _fma(float(k), _LN2_LO, (2.0 * s) * p))
+    return portable_exp(y * lx)

@@ -11,13 +11,13 @@ generator emits, against the symbolic LU of the mechanism:
 * forward / backward substitution levels respect the row dependencies;
 * every species' derivative sum is assigned to exactly one lane.
 """
-import os
 import re
 from pathlib import Path
 
 import pytest
+from conftest import cmaq_root  # noqa: E402
 
-CMAQ = Path(os.environ.get("CMAQ_ROOT", "/root/reference"))
+CMAQ = cmaq_root()
 pytestmark = pytest.mark.skipif(not (CMAQ / "CCTM").exists(), reason="needs the CMAQ sources")
 
 

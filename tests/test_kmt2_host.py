@@ -4,8 +4,8 @@ kmt2.cuh is host/device code: tests/kmt2_host_harness.cpp compiles it with g++ u
 AddressSanitizer and UndefinedBehaviorSanitizer and runs the kernel's lane loop over the
 cells serially (same interleaved workspace, same [element][cell] arrays), so these CPU
 tests check the product's arithmetic bit for bit against the oracle (same libm on both
-sides) and every array index for the sizes below.  On the GPU only CUDA's double exp /
-pow differ (tests/test_gpu_kmt2.py).
+sides, exp and pow by the portable series of both) and every array index for the sizes
+below.  tests/test_gpu_kmt2.py holds the GPU to the same bits.
 """
 import sys
 from pathlib import Path
@@ -57,3 +57,4 @@ def test_switches_and_failed_cells(kmt2_harness, o, tmp_path):
     assert np.array_equal(st, sr)
     good = np.arange(len(p)) != 3
     assert np.array_equal(var[good], vr[good])
+    assert np.isnan(var[3]).all() and np.isnan(vr[3]).all()     # a failed set-up leaves NaN, not stale memory

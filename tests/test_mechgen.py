@@ -1,16 +1,16 @@
 """Mechanism generator: parsed sizes, symbolic LU, rate-program coverage, reproducibility."""
 import ctypes as C
 import filecmp
-import os
 from pathlib import Path
 
 import numpy as np
 import pytest
 
 from cmaq_gb300.synthetic import manifest
+from conftest import cmaq_root  # noqa: E402
 
 ROOT = Path(__file__).resolve().parents[1]
-CMAQ = Path(os.environ.get("CMAQ_ROOT", "/root/reference"))
+CMAQ = cmaq_root()
 
 
 @pytest.mark.parametrize("mech,ns,nr,iarray,nnzj", [

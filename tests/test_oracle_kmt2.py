@@ -6,7 +6,8 @@ What pins the restatement to the reference, without a Fortran compiler to run it
   (test_generator_matches_the_reference, skipped without the CMAQ sources);
 * rate laws, Henry's law constants, the set-up's unit conversions and the initial
   charge balance against formulas restated here from the reference text, to the last
-  bit where the operation order is the same;
+  bit where the operation order is the same (EXP and ** by the portable series both
+  the oracle and the device code use, restated in tests/helpers.py);
 * J against finite differences of f, the sparse LU against a dense solve;
 * Rodas3 with the reference's tolerances against the same integration with RTOL
   scaled down (convergence), and the reference's step statistics' invariants.
@@ -18,12 +19,15 @@ from pathlib import Path
 import numpy as np
 import pytest
 
+from helpers import portable_exp as pexp, portable_pow as ppow
+
 ROOT = Path(__file__).resolve().parents[1]
 sys.path.insert(0, str(ROOT / "oracle"))
 from kmt2 import (KMT2Oracle, P_AIRM, P_ALFA3, P_COSZEN, P_HO, P_ISPC8, P_JH2O2, P_MTPYRAC,  # noqa: E402
                   P_PRCRATE, P_PRES_PA, P_TAUCLD, P_TEMP2, P_WCAVG, P_WTAVG, STATS)
+from conftest import cmaq_root  # noqa: E402
 
-CMAQ = Path(os.environ.get("CMAQ_ROOT", "/root/reference"))
+CMAQ = cmaq_root()
 KMT2_DIR = CMAQ / "CCTM" / "src" / "cloud" / "acm_ae7_kmt2"
 S = {n: i for i, n in enumerate(STATS)}
 
@@ -77,7 +81,7 @@ def test_henry_constants(o, cells):
         assert abs(henry[0] - float(so2)) <= float(np.spacing(so2))     # SO2H, the first one used
         assert henry[0] == float(np.float32(henry[0]))                  # a REAL(4) value
         td = float(t)
-        gcol = 4.1e4 * np.exp(4.6e3 * ((298.0 - td) / (298.0 * td)))
+        gcol = 4.1e4 * pexp(4.6e3 * ((298.0 - td) / (298.0 * td)))
         assert gcol in henry
         assert 2.5 in henry
 
@@ -98,7 +102,7 @@ def test_setup_units_and_charge_balance(o, cells):
         delinvt = (298.0 - t) / (298.0 * t)
         assert fix[ix["L_H2O"] - o.nvar] == 55.5 * (1.0 / phi2)
         assert fix[ix["G_HO"] - o.nvar] == p[c, P_HO] * cfactor
-        o2 = float(np.float32(0.21)) * (pres / 101325.0) * 1.3e-3 * np.exp(1500.0 * delinvt) * (1.0 / phi2)
+        o2 = float(np.float32(0.21)) * (pres / 101325.0) * 1.3e-3 * pexp(1500.0 * delinvt) * (1.0 / phi2)
         assert fix[ix["L_O2"] - o.nvar] == o2
         kept = [i for i in range(o.nvar) if o.names[i] not in ("L_HPLUS", "L_OHMIN")]
         assert np.array_equal(var[kept], cfactor * v[c, kept])
@@ -106,7 +110,7 @@ def test_setup_units_and_charge_balance(o, cells):
             + var[ix["L_NH4PLUS"]]
         neg = 2.0 * (var[ix["L_SO4MIN2"]] + var[ix["L_OXLACMIN2"]]) + var[ix["L_NO3MIN"]] + var[ix["L_CLMIN"]]
         h, oh = var[ix["L_HPLUS"]] * phi2, var[ix["L_OHMIN"]] * phi2
-        kw = 1.0e-14 * np.exp(-6.955e3 * delinvt)
+        kw = 1.0e-14 * pexp(-6.955e3 * delinvt)
         assert abs((h + pos * phi2) - (oh + neg * phi2)) <= 1e-9 * (h + pos * phi2)
         assert abs(h * oh / kw - 1.0) < 1e-12
 
@@ -145,7 +149,7 @@ def test_rate_laws_set_once(o, cells):
         lwc = float(_f32(p[c, P_WCAVG]))
         assert rc[0] == _kmt(t, 0.11, 1.28e-5, 64.064) * lwc / 1000.0           # RCONST(1)
         assert rc[16] == _kmt(t, 0.11, 1.28e-5, 64.064) / (0.08206 * t * henry[0])  # RCONST(17), SO2H
-        assert rc[188] == 1.8e-1 * np.exp(4.03e3 * sc["delinvt"]) * sc["phi2"]    # RCONST(189) HYDF
+        assert rc[188] == 1.8e-1 * pexp(4.03e3 * sc["delinvt"]) * sc["phi2"]      # RCONST(189) HYDF
         assert rc[189] == 5.1e-3                                                 # RCONST(190)
         assert rc[91] == 1.1                                                     # RCONST(92)
         assert rc[192] == p[c, P_JH2O2]                                          # RCONST(193) KPHOT(J)
@@ -178,19 +182,20 @@ def test_rate_laws_refreshed_from_the_state(o, cells):
                       + x("L_CAPLUS2") + x("L_MGPLUS2")) + 9.0 * x("L_FEPLUS3"))
         stion = 0.5 * s * phi2
         assert sc["stion"] == stion
-        gm1 = 10.0 ** (-0.509 * (np.sqrt(stion) / (1.0 + np.sqrt(stion)) - 0.2 * stion))
-        assert abs(sc["gm1"] / gm1 - 1) < 1e-15
+        lg1 = -0.509 * (np.sqrt(stion) / (1.0 + np.sqrt(stion)) - 0.2 * stion)
+        assert sc["gm1"] == ppow(10.0, lg1)
+        assert abs(sc["gm1"] / 10.0 ** lg1 - 1) < 1e-15
         gm1, gm2 = sc["gm1"], sc["gm2"]
-        assert rc[40] == 2.0e8 * (1.39e-2 * np.exp(1.87e3 * d))                 # DISF(.., 0)
-        assert rc[41] == 5.0e10 * (6.72e-8 * np.exp(3.55e2 * d)) * gm1          # DISF(.., 1)
+        assert rc[40] == 2.0e8 * (1.39e-2 * pexp(1.87e3 * d))                   # DISF(.., 0)
+        assert rc[41] == 5.0e10 * (6.72e-8 * pexp(3.55e2 * d)) * gm1            # DISF(.., 1)
         assert rc[54] == 2.0e8 * gm1 * gm1 * phi2                               # DISB(2.0D8, 2)
         assert rc[55] == 5.0e10 * gm1 * gm2 * phi2                              # DISB(5.0D10, 1)
-        k = 7.45e7 * np.exp(-4756.08 * d)                                       # KRXN(.., 1, 0, 0)
+        k = 7.45e7 * pexp(-4756.08 * d)                                         # KRXN(.., 1, 0, 0)
         assert rc[68] == (k / (1.0 + 13.0 * x("L_HPLUS") * phi2)) * phi2 * phi2
-        k = 750.0 * np.exp(0.0 * d)                                             # KRXN(750, 0, 0, 0, 1)
-        svi = 1.0 + 75.0 * ((x("L_H2SO4") + x("L_HSO4MIN") + x("L_SO4MIN2")) * phi2) ** 0.67
-        assert abs(rc[72] / ((k / svi) * phi2) - 1) < 1e-15
-        assert rc[239] == 2.6e-2 * np.exp(0.0 * d) / phi2 * phi2                # KRXN(.., 4, 0, 0)
+        k = 750.0 * pexp(0.0 * d)                                               # KRXN(750, 0, 0, 0, 1)
+        svi = 1.0 + 75.0 * ppow((x("L_H2SO4") + x("L_HSO4MIN") + x("L_SO4MIN2")) * phi2, 0.67)
+        assert rc[72] == (k / svi) * phi2
+        assert rc[239] == 2.6e-2 * pexp(0.0 * d) / phi2 * phi2                  # KRXN(.., 4, 0, 0)
         assert rc[146] == 0.0 and rc[153] == 0.0                                # KIEPOX TYPE >= 1 off
         assert rc[150] > 0.0                                                    # KIEPOX TYPE 0 on (ISPC8 = 0)
 
