@@ -54,6 +54,8 @@ sys.path.insert(0, str(ROOT))
 METRIC = "ROS3 CB6r5 grid-cells/s per 1-h chem step"
 UNIT = "grid-cells/s per 1-h chem step"
 RTOL, ATOL = 1.0e-3, 1.0e-9
+# tight tolerance of the accuracy block and its timing leg (DTMIN lowered to 1e-14 min)
+TIGHT_RTOL, TIGHT_ATOL = 1.0e-5, 1.0e-14
 TSTEP = (10000, 500, 500)          # TSTEP(3) HHMMSS: output 1 h, sync 5 min
 STEPS_PER_HOUR = 12
 
@@ -77,7 +79,7 @@ class ClockSampler:
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,utilization.gpu")
 
     def __init__(self, device: int):
         self.device = device
@@ -107,7 +109,7 @@ class ClockSampler:
     def summary(self) -> dict:
         if not self.path or not os.path.exists(self.path):
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
-        sm, smax, reasons = [], None, set()
+        sm, busy, smax, reasons = [], [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in open(self.path):
             p = [x.strip() for x in line.split(",")]
@@ -118,12 +120,19 @@ class ClockSampler:
                 smax = float(p[2])
             except ValueError:
                 continue
+            try:
+                if len(p) > 9 and float(p[9]) >= 50.0:
+                    busy.append(sm[-1])
+            except ValueError:
+                pass
             for nm, v in zip(names, p[5:9]):
                 if v.lower() == "active":
                     reasons.add(nm)
         os.unlink(self.path)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "samples": len(sm),
-                "reasons": sorted(reasons)}
+        # the median over samples with the GPU busy (utilization >= 50 %), else over all
+        use = busy if busy else sm
+        return {"sm_mhz": statistics.median(use) if use else None, "sm_max_mhz": smax, "samples": len(sm),
+                "samples_under_load": len(busy), "reasons": sorted(reasons)}
 
 
 def make_inputs(workload: str, seed: int):
@@ -138,19 +147,26 @@ def flops_of(st: dict, info) -> float:
 
 
 def run_device(g, schedule: str, steps: int, warmup: int, dist, device: int, sample_clocks: bool,
-               tuned: dict | None = None, graph: bool = False, solver: str = "ros3"):
+               tuned: dict | None = None, graph: bool = False, solver: str = "ros3", rtol: float = RTOL,
+               atol: float = ATOL, dtmin_exp: int | None = None):
     """K timed CHEM calls on device-resident arrays from the initial state.  graph: the K
-    calls are replayed from one captured CUDA graph (cmaqchem_steps_device)."""
+    calls are replayed from one captured CUDA graph (cmaqchem_steps_device), as three
+    replays (the first call, the rest of the first hour, the calls after it) whose
+    statistics are kept apart.  The warm-up calls repeat the first call; the work queue's
+    step-count history is cleared after them, so the timed first call is queued as a fresh
+    run's first call (grid order), and later calls by the previous call's step counts."""
     import torch
     from cmaq_gb300.chem import ChemSolver
     dev = {k: torch.from_numpy(np.ascontiguousarray(getattr(g, k))).to(f"cuda:{device}")
            for k in ("conc", "ta", "qv", "dens", "pres", "seaice", "ocean_szone", "rj", "khetero")}
     conc0 = dev["conc"].clone()
     s = ChemSolver(g.mech, ncols=g.ncols, nrows=g.nrows, nlays=g.nlays, nspcsd=g.nspcsd, cgrid_index=g.cgrid_index,
-                   rtol=RTOL, atol=ATOL, schedule=schedule, device=device, solver=solver,
+                   rtol=rtol, atol=atol, schedule=schedule, device=device, solver=solver,
                    variant=(tuned or {}).get("variant", "default"))
     if tuned:
         s.set_tuning(block_warps=tuned["block_warps"], lockstep=tuned["lockstep"])
+    if dtmin_exp is not None:
+        s.set_tuning(ros3_dtmin_exp=dtmin_exp)
     stream = torch.cuda.current_stream(device)
     args = [dev[k] for k in ("conc", "ta", "qv", "dens", "pres", "seaice", "ocean_szone", "rj", "khetero")]
     # every warm-up step is the hour's first CHEM call from the initial state, so the queue
@@ -162,9 +178,12 @@ def run_device(g, schedule: str, steps: int, warmup: int, dist, device: int, sam
         else:
             s.step(*args, tstep=TSTEP, stream=stream)
     dev["conc"].copy_(conc0)
+    if schedule == "queue":
+        s.set_tuning(queue_history=0)
     torch.cuda.synchronize(device)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     stats = []
+    parts = [n for n in (1, min(steps, STEPS_PER_HOUR) - 1, steps - STEPS_PER_HOUR) if n > 0]
     clocks = ClockSampler(device) if sample_clocks else None
     if clocks:
         clocks.__enter__()
@@ -173,7 +192,8 @@ def run_device(g, schedule: str, steps: int, warmup: int, dist, device: int, sam
     t0 = time.perf_counter()
     ev0.record(stream)
     if graph:
-        stats.append(s.steps(steps, *args, tstep=TSTEP, stream=stream))
+        for n in parts:
+            stats.append(s.steps(n, *args, tstep=TSTEP, stream=stream))
     else:
         for _ in range(steps):
             stats.append(s.step(*args, tstep=TSTEP, stream=stream))
@@ -187,7 +207,105 @@ def run_device(g, schedule: str, steps: int, warmup: int, dist, device: int, sam
     s.close()
     del dev, conc0
     torch.cuda.empty_cache()
-    return {"ms_total": ms, "wall_s": wall, "stats": stats, "clocks": clocks.summary() if clocks else None}
+    return {"ms_total": ms, "wall_s": wall, "stats": stats, "calls": parts if graph else [1] * steps,
+            "clocks": clocks.summary() if clocks else None}
+
+
+def split_calls(r: dict, ncell: int) -> dict:
+    """First call and first hour of a run_device result: device time and step attempts."""
+    out, done, ms, att = {}, 0, 0.0, 0
+    for n, st in zip(r["calls"], r["stats"]):
+        done += n
+        ms += st["device_ms"]
+        att += st["accepted_steps"] + st["rejected_steps"]
+        if done == 1:
+            out["first_call_ms"] = ms
+            out["first_call_attempts_per_cell"] = att / ncell
+        if done == STEPS_PER_HOUR:
+            out["first_hour"] = {"value": ncell / (ms * 1e-3), "ms_per_step": ms / done,
+                                 "step_attempts_per_cell": att / ncell / done}
+    return out
+
+
+def fp64_peak_record(device: int) -> dict:
+    """The FP64 roofline's denominators: (1) independent FMA chains on every SM for about a
+    second, three times, with the SM clock sampled meanwhile (best TFLOP/s); (2) the
+    clock-derived rate 2 FMA per clock per SM (a one-warp clock64 probe measures one FP64
+    warp instruction per 64 cycles per SM sub-partition, 4 x 32 / 64 = 2) x 2 FLOP x SMs x
+    SM clock."""
+    import torch
+    from cmaq_gb300 import _lib
+    nsm = torch.cuda.get_device_properties(device).multi_processor_count
+    _lib.fp64_peak(device)
+    with ClockSampler(device) as ck:
+        runs = [_lib.fp64_peak_long(device, 1000.0) for _ in range(3)]
+    c = ck.summary()
+    best = max(r[0] for r in runs)
+    return {"measured_tflops": best, "kernel_ms": [r[1] for r in runs], "measured_sm_mhz": c.get("sm_mhz"),
+            "measured_clock_samples": c.get("samples_under_load"), "measured_reasons": c.get("reasons"),
+            "sms": nsm, "fma_per_clk_per_sm": 2.0,
+            "measured_fma_per_clk_per_sm": None if not c.get("sm_mhz") else
+            best * 1e12 / 2.0 / nsm / (c["sm_mhz"] * 1e6)}
+
+
+def clock_peak(rec: dict, sm_mhz: float | None) -> float | None:
+    """2 FMA/clk/SM x 2 FLOP x SMs x clock, in TFLOP/s."""
+    if not sm_mhz:
+        return None
+    return rec["fma_per_clk_per_sm"] * 2.0 * rec["sms"] * sm_mhz * 1e6 / 1e12
+
+
+def run_accuracy(g, device: int, tuned, threads: int, tight_tol=(1.0e-5, 1.0e-14), col_step: int = 46,
+                 row_step: int = 50) -> dict:
+    """Accuracy of the batched GPU kernel after one simulated hour (12 CHEM calls) on a
+    sample of the workload grid (every col_step-th column and row_step-th row, all layers),
+    against the oracle's tight solution (rtol 1e-8, atol 1e-18 ppmV, DTMIN lowered to 1e-14
+    min), on species above 1e-10 ppmV of the REAL(4) CGRID output: at the headline
+    tolerance and at a tight one (DTMIN lowered to 1e-14 there too)."""
+    import torch
+    from cmaq_gb300.chem import ChemSolver
+    from cmaq_gb300.synthetic import subgrid
+    sys.path.insert(0, str(ROOT / "oracle"))
+    from oracle import Oracle
+    sub = subgrid(g, col_step, row_step, 1)
+    o = Oracle(sub.mech)
+    t0 = time.perf_counter()
+    truth = sub.conc.copy()
+    with o.tight():
+        for _ in range(STEPS_PER_HOUR):
+            truth, tot = o.chem(sub, blksize=1, rtol=1.0e-8, atol=1.0e-18, threads=threads, conc=truth)
+            if tot["rc"] != 0:
+                return {"error": "the tight oracle solution failed"}
+    truth_s = time.perf_counter() - t0
+    idx = np.unique(sub.cgrid_index - 1)
+    tr = truth[idx].astype(np.float64)
+    mask = tr > 1.0e-10
+
+    def gpu_hour(rtol, atol, dtmin_exp):
+        dev = {k: torch.from_numpy(np.ascontiguousarray(getattr(sub, k))).to(f"cuda:{device}")
+               for k in ("conc", "ta", "qv", "dens", "pres", "seaice", "ocean_szone", "rj", "khetero")}
+        sv = ChemSolver(sub.mech, ncols=sub.ncols, nrows=sub.nrows, nlays=sub.nlays, nspcsd=sub.nspcsd,
+                        cgrid_index=sub.cgrid_index, rtol=rtol, atol=atol, schedule="queue", device=device)
+        if tuned:
+            sv.set_tuning(block_warps=tuned["block_warps"], lockstep=tuned["lockstep"])
+        if dtmin_exp is not None:
+            sv.set_tuning(ros3_dtmin_exp=dtmin_exp)
+        failed = 0
+        for _ in range(STEPS_PER_HOUR):
+            failed += sv.step(*[dev[k] for k in ("conc", "ta", "qv", "dens", "pres", "seaice", "ocean_szone", "rj",
+                                                 "khetero")], tstep=TSTEP)["failed_cells"]
+        sv.close()
+        got = dev["conc"].cpu().numpy()[idx].astype(np.float64)
+        rel = np.abs(got[mask] - tr[mask]) / tr[mask]
+        return {"rtol": rtol, "atol": atol, "max": float(rel.max()), "p99_9": float(np.quantile(rel, 0.999)),
+                "median": float(np.median(rel)), "failed_cells": int(failed)}
+
+    return {"sample": f"{sub.ncols}x{sub.nrows}x{sub.nlays} ({sub.ncell} cells): every {col_step}th column and "
+                      f"{row_step}th row of the workload grid, all layers",
+            "truth": "oracle (ROS3 per cell) rtol 1e-8, atol 1e-18 ppmV, DTMIN 1e-14 min",
+            "species": f"CGRID species above 1e-10 ppmV after the hour ({int(mask.sum())} values)",
+            "truth_s": truth_s, "headline": gpu_hour(RTOL, ATOL, None),
+            "tight": dict(gpu_hour(tight_tol[0], tight_tol[1], -14), dtmin_min=1.0e-14)}
 
 
 def run_e2e(g, steps: int, warmup: int, dist, device: int):
@@ -212,6 +330,7 @@ def run_e2e(g, steps: int, warmup: int, dist, device: int):
         h["conc"][...] = conc0
         s.step(*args, tstep=TSTEP)
     h["conc"][...] = conc0
+    s.set_tuning(queue_history=0)        # the timed first call is queued as a fresh run's
     # the call copies the mechanism's CGRID planes (not all NSPCSD) and the other inputs
     plane = h["conc"].nbytes // g.nspcsd
     nplanes = len(set(int(c) for c in g.cgrid_index))
@@ -279,12 +398,21 @@ def run_adjoint(device: int, nsync: int = STEPS_PER_HOUR, dims=(100, 100, 35)) -
         emis.grad = None
     fwd, bwd = times[-1]
     s.close()
+    del w, a, y, emis, logk, y0, rki, night
+    torch.cuda.empty_cache()
+    # the same cells' hour through the batched CHEM kernel (no tape): the forward a user
+    # would run without gradients
+    b = run_device(g, "queue", nsync, 1, None, device, sample_clocks=False, graph=True)
+    bfwd = b["ms_total"]
     return {"workload": f"cb6r5_ae7_aq {dims[0]}x{dims[1]}x{dims[2]} ({n} cells), {nsync} x 5-min steps, solver level "
                         "(rates from CALC_RCONST of the grid, fixed over the hour)",
             "loss": "sum of O3 over the surface layer at the end of the hour",
             "gradients": "initial concentrations, 349 log rate multipliers, emission tendencies",
             "forward_ms": fwd, "backward_ms": bwd, "backward_over_forward": bwd / fwd,
-            "total_over_forward": (fwd + bwd) / fwd}
+            "total_over_forward": (fwd + bwd) / fwd,
+            "batched_forward_ms": bfwd, "total_over_batched_forward": (fwd + bwd) / bfwd,
+            "forward_note": "forward_ms records the tape (accepted steps' states and sizes); batched_forward_ms is "
+                            "the same cells' hour through the batched CHEM kernel without a tape"}
 
 
 def run_skewed(device: int, steps: int, tuned) -> dict:
@@ -301,6 +429,29 @@ def run_skewed(device: int, steps: int, tuned) -> dict:
                         f"10x NOx/VOC, {steps} x 5-min CHEM calls from the initial state",
             "batched_value": bv, "plain_value": pv, "batched_over_plain": bv / pv,
             "step_attempts_per_cell": att}
+
+
+def run_tight(g, device: int, steps: int, tuned, info, tol, peak_rec) -> dict:
+    """The workload grid at the tight tolerance of the accuracy block (DTMIN lowered to
+    1e-14 min): batched (graph-replayed) and plain, the first `steps` calls from the
+    initial state, with the batched kernel's FP64 rate."""
+    b = run_device(g, "queue", steps, 1, None, device, sample_clocks=True, tuned=tuned, graph=True,
+                   rtol=tol[0], atol=tol[1], dtmin_exp=-14)
+    p = run_device(g, "static", steps, 1, None, device, sample_clocks=False, rtol=tol[0], atol=tol[1],
+                   dtmin_exp=-14)
+    bv = g.ncell / (STEPS_PER_HOUR * b["ms_total"] / steps / 1e3)
+    pv = g.ncell / (STEPS_PER_HOUR * p["ms_total"] / steps / 1e3)
+    fl = sum(flops_of(st, info) for st in b["stats"])
+    dev_ms = sum(st["device_ms"] for st in b["stats"])
+    ach = fl / (dev_ms * 1e-3) / 1e12
+    cp = clock_peak(peak_rec, (b["clocks"] or {}).get("sm_mhz"))
+    peak = max(x for x in (peak_rec["measured_tflops"], cp) if x)
+    att = sum(st["accepted_steps"] + st["rejected_steps"] for st in b["stats"]) / g.ncell / steps
+    return {"workload": f"cb6r5_ae7_aq {g.ncols}x{g.nrows}x{g.nlays} ({g.ncell} cells), the hour's first {steps} x "
+                        f"5-min CHEM calls, rtol {tol[0]:g}, atol {tol[1]:g} ppmV, DTMIN 1e-14 min",
+            "batched_value": bv, "plain_value": pv, "batched_over_plain": bv / pv,
+            "step_attempts_per_cell": att, "achieved_tflops": ach, "roofline_frac": ach / peak,
+            "failed_cells": int(sum(st["failed_cells"] for st in b["stats"])), "clocks": b["clocks"]}
 
 
 def run_cracmm2(device: int, steps: int) -> dict:
@@ -355,16 +506,20 @@ def run_cracmm2(device: int, steps: int) -> dict:
     return out
 
 
-def run_ebi(device: int, steps: int) -> dict:
-    """EBI (HRSOLVER) against batched ROS3 on one 100x100x10 grid of the same distributions."""
+def run_ebi(device: int, steps: int, g=None) -> dict:
+    """EBI (HRSOLVER) CHEM calls on the workload grid (the CONUS grid of the headline line
+    unless g is given), K calls from the initial state; ROS3 on the same grid is the
+    headline's batched arm."""
     from cmaq_gb300.synthetic import make_grid
-    g = make_grid(seed=2018, ncols=100, nrows=100, nlays=10)
-    out = {"workload": f"cb6r5_ae7_aq 100x100x10 ({g.ncell} cells), {steps} x 5-min CHEM calls"}
-    for solver in ("ebi", "ros3"):
-        r = run_device(g, "queue", steps, 1, None, device, sample_clocks=False, solver=solver)
-        out[f"{solver}_ms_per_step"] = r["ms_total"] / steps
-        out[f"{solver}_value"] = g.ncell / (STEPS_PER_HOUR * r["ms_total"] / steps / 1e3)
-    return out
+    if g is None:
+        g = make_grid(seed=2018, ncols=100, nrows=100, nlays=10)
+    r = run_device(g, "queue", steps, 1, None, device, sample_clocks=False, solver="ebi")
+    att = sum(st["accepted_steps"] for st in r["stats"]) / g.ncell / steps
+    return {"workload": f"cb6r5_ae7_aq {g.ncols}x{g.nrows}x{g.nlays} ({g.ncell} cells), {steps} x 5-min EBI CHEM "
+                        "calls from the initial state",
+            "ebi_ms_per_step": r["ms_total"] / steps,
+            "ebi_value": g.ncell / (STEPS_PER_HOUR * r["ms_total"] / steps / 1e3),
+            "ebi_iterations_per_cell_and_call": att, **{"ebi_" + k: v for k, v in split_calls(r, g.ncell).items()}}
 
 
 def run_gear(device: int, steps: int) -> dict:
@@ -383,6 +538,14 @@ def run_gear(device: int, steps: int) -> dict:
             out["gear_steps_per_cell"] = sum(st["accepted_steps"] for st in r["stats"]) / g.ncell / steps
             out["gear_failures_per_cell"] = sum(st["rejected_steps"] for st in r["stats"]) / g.ncell / steps
     return out
+
+
+def aqchem_roofline(r: dict, peak_rec: dict | None) -> dict:
+    """FP64 roofline of the KMT2 kernel against the measured FMA-chain rate."""
+    pk = None if peak_rec is None else peak_rec["measured_tflops"]
+    return {"bound": "fp64", "achieved": r["achieved_tflops"], "peak": pk, "unit": "TFLOP/s",
+            "frac": None if not pk else r["achieved_tflops"] / pk, "traffic": None,
+            "peak_source": "measured live (cmaqchem_diag_fp64_peak_long)"}
 
 
 def run_aqchem(device: int, ncell: int, steps: int, warmup: int, threads: int) -> dict:
@@ -414,8 +577,10 @@ def run_aqchem(device: int, ncell: int, steps: int, warmup: int, threads: int) -
         torch.cuda.synchronize(dev)
         ms.append(ev[0].elapsed_time(ev[1]))
     sd = st.cpu().numpy().astype(np.int64)
-    nstp, njac = sd[0].sum(), sd[4].sum()
-    flops = float(njac * fl["per_step"] + nstp * fl["per_attempt"])
+    # each routine's operation count times its own counter: f, J, factorisations (with the
+    # repeats after a singular one), solves, and the vector work of every attempt
+    flops = float(sd[3].sum() * fl["fun"] + sd[4].sum() * fl["jac"] + sd[5].sum() * fl["decomp"]
+                  + sd[6].sum() * fl["solve"] + sd[0].sum() * fl["vector"])
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     for _ in range(steps):
@@ -441,12 +606,12 @@ def run_aqchem(device: int, ncell: int, steps: int, warmup: int, threads: int) -
         vr, _, sr, _ = o.cells(p[:nsample], v[:nsample], threads=threads)
         wall = time.perf_counter() - t0
         got = out[:, :nsample].cpu().numpy().T
-        same = (sd[0, :nsample] == sr[:, 0]) & (sd[1, :nsample] == sr[:, 1])
+        same = (sd[:, :nsample].T == sr).all(axis=1)
         big = np.abs(vr) > 1e-6 * np.abs(vr).max(axis=1, keepdims=True)
         rel = np.where(big, np.abs(got - vr) / np.maximum(np.abs(vr), 1e-300), 0.0).max(axis=1)
         res["cpu"] = {"value": nsample / wall, "cells": nsample, "wall_s": wall}
         res["parity"] = {"cells": nsample, "same_steps": float(same.mean()),
-                         "max_rel_same_steps": float(rel[same].max()) if same.any() else None,
+                         "bit_equal_cells": float(((got == vr).all(axis=1) & same).mean()),
                          "max_rel": float(rel.max())}
     return res
 
@@ -526,8 +691,14 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-ebi", action="store_true")
     ap.add_argument("--no-gear", action="store_true")
-    ap.add_argument("--all-configs", action="store_true",
-                    help="also time the skewed-stiffness CONUS grid and CRACMM2 on 1M cells (about 5 more minutes)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="only the headline arms (batched, plain, e2e, CPU baseline)")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the skewed-stiffness CONUS grid and CRACMM2 on 1M cells")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the accuracy block and the tight-tolerance leg")
+    ap.add_argument("--no-aqchem", action="store_true", help="skip the KMT2 aqueous kinetics leg")
+    ap.add_argument("--tight-steps", type=int, default=2,
+                    help="CHEM calls of the tight-tolerance leg on the workload grid (0: skip)")
     ap.add_argument("--adjoint-dims", default="100x100x35", help="grid of the adjoint window, NCOLSxNROWSxNLAYS")
     ap.add_argument("--only-adjoint", action="store_true",
                     help="time only the adjoint window and print its own line (for profiling)")
@@ -584,7 +755,7 @@ def main():
                               "warmup": 1, "ms_per_step": (r["forward_ms"] + r["backward_ms"]) / a.steps,
                               "higher_is_better": False, "dtype": "f64", "data": "synthetic", "adjoint": r}))
         return 0
-    peak_tf, _ = _lib.fp64_peak(device)
+    peak_rec = fp64_peak_record(device) if rank == 0 or world == 1 else None
     if a.only_aqchem:
         thr = 0 if (a.no_cpu or rank != 0) else host_threads()
         r = run_aqchem(device, a.aqchem_cells, min(a.steps, 5), max(a.warmup, 3), thr)
@@ -598,9 +769,7 @@ def main():
                                            "(CCTM/src/cloud/acm_ae7_kmt2), TAUCLD 600-3600 s",
                                "l2": f"inputs of {r['ncell'] * 176 * 8 / 1e6:.0f} MB per call, larger than the "
                                      "129 MB L2, plus a 1 GB workspace"},
-                    "roofline": {"bound": "fp64", "achieved": r["achieved_tflops"], "peak": peak_tf,
-                                 "unit": "TFLOP/s", "frac": r["achieved_tflops"] / peak_tf, "traffic": None,
-                                 "peak_source": "measured live (cmaqchem_diag_fp64_peak)"},
+                    "roofline": aqchem_roofline(r, peak_rec),
                     "e2e": r["e2e"], "gpu_launches": min(a.steps, 5), "aqchem": r}
             if "cpu" in r:
                 line["cpu_baseline"] = {"value": r["cpu"]["value"], "unit": "cells/s", "cores": host_threads(),
@@ -620,6 +789,7 @@ def main():
     dev_ms = sum(s["device_ms"] for s in batched["stats"])
     achieved_tf = fl / (dev_ms * 1e-3) / 1e12
     attempts = sum(s["accepted_steps"] + s["rejected_steps"] for s in batched["stats"])
+    calls = split_calls(batched, ncell)
 
     plain = None
     if not a.no_plain:
@@ -628,7 +798,7 @@ def main():
         p_fl = sum(flops_of(s, info) for s in p["stats"])
         p_dev = sum(s["device_ms"] for s in p["stats"])
         plain = {"value": world * ncell / (STEPS_PER_HOUR * p_ms / 1e3), "ms_per_step": p_ms,
-                 "achieved_tflops": p_fl / (p_dev * 1e-3) / 1e12}
+                 "achieved_tflops": p_fl / (p_dev * 1e-3) / 1e12, **split_calls(p, ncell)}
 
     e2e = None
     if not a.no_e2e:
@@ -656,25 +826,49 @@ def main():
                "gear_sample": None if rg is None else
                f"{rg['cells']} cells x {rg['steps']} SMVGEAR CHEM calls (BLKSIZE 50 + reordering), {thr} threads"}
 
-    adjoint = None if (a.no_adjoint or rank != 0) else run_adjoint(device, STEPS_PER_HOUR, adims)
-    ebi = None if (a.no_ebi or rank != 0) else run_ebi(device, a.steps)
-    gear = None if (a.no_gear or rank != 0) else run_gear(device, a.steps)
-    skewed = run_skewed(device, a.steps, tuned) if (a.all_configs and rank == 0) else None
-    cracmm2 = run_cracmm2(device, a.steps) if (a.all_configs and rank == 0) else None
+    extras = rank == 0 and not a.no_extras
+    tight_tol = (TIGHT_RTOL, TIGHT_ATOL)
+    legs_s = {}
+
+    def leg(name, on, fn):
+        if not on:
+            return None
+        t0 = time.perf_counter()
+        out = fn()
+        legs_s[name] = round(time.perf_counter() - t0, 1)
+        return out
+    accuracy = leg("accuracy", extras and not a.no_accuracy,
+                   lambda: run_accuracy(g, device, tuned, host_threads(), tight_tol))
+    tight = leg("tight", extras and not a.no_accuracy and a.tight_steps > 0,
+                lambda: run_tight(g, device, a.tight_steps, tuned, info, tight_tol, peak_rec))
+    ebi = leg("ebi", extras and not a.no_ebi, lambda: run_ebi(device, STEPS_PER_HOUR, g))
+    adjoint = leg("adjoint", extras and not a.no_adjoint, lambda: run_adjoint(device, STEPS_PER_HOUR, adims))
+    gear = leg("gear", extras and not a.no_gear, lambda: run_gear(device, a.steps))
+    skewed = leg("skewed", extras and not a.no_configs, lambda: run_skewed(device, STEPS_PER_HOUR, tuned))
+    cracmm2 = leg("cracmm2", extras and not a.no_configs, lambda: run_cracmm2(device, STEPS_PER_HOUR))
+    aqchem = leg("aqchem", extras and not a.no_aqchem,
+                 lambda: run_aqchem(device, a.aqchem_cells, 3, 3, 0 if a.no_cpu else host_threads()))
+    if aqchem is not None:
+        aqchem["roofline"] = aqchem_roofline(aqchem, peak_rec)
 
     traffic = traffic_note = None
     tfile = ROOT / "profiles" / "traffic_per_step.json"
     if tfile.exists():
         try:
             t = json.loads(tfile.read_text()).get(a.workload)
-            traffic = None if t is None else float(t["bytes_per_launch"])
-            traffic_note = None if t is None else t["source"]
+            if t is not None:
+                # DRAM bytes per cell-attempt from the ncu capture, times this run's attempts per call
+                traffic = float(t["bytes_per_cell_attempt"]) * attempts / a.steps
+                traffic_note = t["source"]
         except Exception:
             traffic = None
     if rank == 0:
         launches_per_step = 4   # queue ordering (hist, scan, scatter) + solve, replayed from one graph
         if a.solver != "ros3":   # EBI iterations and Gear steps have no ROS3 FLOP count
             achieved_tf = None
+        bclk = (batched["clocks"] or {}).get("sm_mhz")
+        cpk = clock_peak(peak_rec, bclk)
+        peak_tf = max(x for x in (peak_rec["measured_tflops"], cpk) if x)
         line = {
             "metric": METRIC if a.solver == "ros3" else METRIC.replace("ROS3", a.solver.upper()), "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -683,31 +877,44 @@ def main():
                                    f"{a.steps} x 5-min CHEM calls from the initial state, rtol 1e-3, atol 1e-9 ppmV",
                        "schedule": "batched (persistent, work queue ordered by previous step counts; "
                                    "the calls replayed from one captured CUDA graph)",
+                       "queue": "cold at the first timed call: the warm-up calls' step counts are cleared, so "
+                                "it is queued in grid order like a fresh run's first call",
                        "tuned": None if tuned is None else {k: tuned[k] for k in
                                                             ("variant", "lockstep", "block_warps", "sample",
                                                              "tuning_s")},
                        "cells": ncell, "step_attempts_per_cell": attempts / ncell / a.steps,
                        "l2": "inputs larger than L2 (CGRID %.1f GB); no flush" % (g.conc.nbytes / 1e9),
                        "parallelism": f"replicas x{world} (own grid per GPU)"},
+            **calls,
             "roofline": None if achieved_tf is None else {
                          "bound": "fp64", "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
                          "frac": achieved_tf / peak_tf, "traffic": traffic, "traffic_source": traffic_note,
+                         "traffic_per": "one CHEM call (launch) of this run: DRAM bytes per cell-attempt x this run's "
+                                        "attempts per call",
                          "dram_gbs_from_traffic": None if traffic is None else traffic / (ms_step * 1e-3) / 1e9,
-                         "peak_source": "measured live: FP64 FMA-chain kernel (no FP64 figure in "
+                         "peak_source": "the larger of the measured FP64 FMA-chain rate and the clock-derived "
+                                        "rate at the timed region's median SM clock (no FP64 figure in "
                                         "MEASURED_PEAKS.json)",
+                         "peak_measured": peak_rec, "peak_clock_derived": cpk, "timed_sm_mhz": bclk,
+                         "frac_of_measured": achieved_tf / peak_rec["measured_tflops"],
+                         "frac_of_clock_derived": None if not cpk else achieved_tf / cpk,
                          "flops": "algorithmic FLOPs of the reference's ROS3 step per attempt x attempts",
                          "fp64_chain_cycles_per_fma": issue},
             "plain": plain,
             "batched_over_plain": None if plain is None else value / plain["value"],
+            "accuracy": accuracy,
+            "tight": tight,
             "adjoint": adjoint,
             "ebi": ebi,
             "gear": gear,
             "skewed": skewed,
             "cracmm2": cracmm2,
+            "aqchem": aqchem,
             "e2e": e2e,
             "cpu_baseline": cpu,
             "clocks": batched["clocks"],
             "gpu_launches": launches_per_step * a.steps,
+            "extra_legs_s": legs_s,
         }
         print(json.dumps(line))
     if dist is not None:

@@ -74,6 +74,7 @@ def lib(variant: str = "default") -> C.CDLL:
     L.cmaqchem_last_error.argtypes = [C.c_char_p, C.c_size_t]
     L.cmaqchem_diag_fp64_peak.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.cmaqchem_diag_fp64_issue.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double)]
+    L.cmaqchem_diag_fp64_peak_long.argtypes = [C.c_int, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.cmaqchem_diag_set_tuning.argtypes = [vp, C.c_char_p, C.c_int]
     L.cmaqchem_kmt2_workspace_doubles.argtypes = [C.c_longlong]
     L.cmaqchem_kmt2_workspace_doubles.restype = C.c_longlong
@@ -85,6 +86,14 @@ def fp64_peak(device: int = 0) -> tuple[float, float]:
     """Measured FP64 FMA throughput (TFLOP/s) and kernel time (ms) of `device`."""
     tf, ms = C.c_double(), C.c_double()
     if lib().cmaqchem_diag_fp64_peak(device, C.byref(tf), C.byref(ms)) != 0:
+        raise ChemError("FP64 peak measurement failed")
+    return tf.value, ms.value
+
+
+def fp64_peak_long(device: int = 0, target_ms: float = 1000.0) -> tuple[float, float]:
+    """Measured FP64 FMA throughput (TFLOP/s) of a kernel of about target_ms, and its time (ms)."""
+    tf, ms = C.c_double(), C.c_double()
+    if lib().cmaqchem_diag_fp64_peak_long(device, C.c_double(target_ms), C.byref(tf), C.byref(ms)) != 0:
         raise ChemError("FP64 peak measurement failed")
     return tf.value, ms.value
 

@@ -93,6 +93,7 @@ struct cmaqchem_handle {
     bool have_history = false;
     // tuning knobs (cmaqchem_diag_set_tuning)
     int use_night = 1;
+    double dtmin = ros3::DTMIN;   // ROS3 minimum step (rbsolver.F:105), lowered only by a tuning knob
     int q_sync = 1;          // work-queue kernel: barriers between attempt phases
     int q_wpb = 8;           // work-queue kernel: warps per block
     int q_nblocks = 0;
@@ -265,7 +266,7 @@ chem::GridArgs grid_args(cmaqchem_handle* h, float* conc, const float* ta, const
     a.rj = rj;
     a.khet = khet;
     a.chemstep = chemstep;
-    a.tol = ros3::Tol{h->cfg.rtol, h->cfg.atol, h->rnspec};
+    a.tol = ros3::Tol{h->cfg.rtol, h->cfg.atol, h->rnspec, h->dtmin};
     a.ws = h->d_ws;
     a.max_iter = h->max_iter;
     a.cell_status = h->d_status;
@@ -461,6 +462,20 @@ extern "C" int cmaqchem_diag_set_tuning(cmaqchem_handle* h, const char* key, int
         h->ebi_warp = value != 0;
         if (h->graph_exec) CK(cudaGraphExecDestroy(h->graph_exec));
         h->graph_exec = nullptr;
+        return 0;
+    } else if (strcmp(key, "ros3_dtmin_exp") == 0) {
+        // ROS3 minimum step 10^value min (the reference's DTMIN is 1e-8, value -8)
+        if (value < -30 || value > -2) return fail("ros3_dtmin_exp must be in [-30, -2]");
+        h->dtmin = pow(10.0, (double)value);
+        if (h->graph_exec) CK(cudaGraphExecDestroy(h->graph_exec));
+        h->graph_exec = nullptr;
+        return 0;
+    } else if (strcmp(key, "queue_history") == 0) {
+        // 0: forget the previous call's step counts, so the next call starts with the work
+        // queue of a fresh run's first call (cells in grid order)
+        if (value != 0) return fail("queue_history takes 0 (clear)");
+        if (h->d_steps) CK(cudaMemset(h->d_steps, 0, sizeof(int) * h->ncell));
+        h->have_history = false;
         return 0;
     } else if (strcmp(key, "host_chunks") == 0) {
         if (value < 1 || value > MAX_E2E_CHUNKS) return fail("host_chunks must be 1 .. 16");
@@ -779,7 +794,7 @@ extern "C" int cmaqchem_ros3_solve_device(cmaqchem_handle* h, long long ncell, d
     a.night = night;
     a.ncell = ncell;
     a.chemstep = chemstep_min;
-    a.tol = ros3::Tol{h->cfg.rtol, h->cfg.atol, h->rnspec};
+    a.tol = ros3::Tol{h->cfg.rtol, h->cfg.atol, h->rnspec, h->dtmin};
     a.ws = h->d_ws;
     a.max_iter = h->max_iter;
     a.cell_status = status;
@@ -929,7 +944,7 @@ adj::Args adj_args(cmaqchem_handle* h, long long ncell, const double* rki, const
     adj::Args a{};
     a.ncell = ncell;
     a.chemstep = chemstep;
-    a.tol = ros3::Tol{h->cfg.rtol, h->cfg.atol, h->rnspec};
+    a.tol = ros3::Tol{h->cfg.rtol, h->cfg.atol, h->rnspec, h->dtmin};
     a.max_iter = h->max_iter;
     a.ws = h->d_adj_ws;
     a.rki = rki;

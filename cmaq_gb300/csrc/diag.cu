@@ -66,14 +66,16 @@ extern "C" int cmaqchem_diag_fp64_issue(int device, int active_lanes, double* cy
     return 0;
 }
 
-extern "C" int cmaqchem_diag_fp64_peak(int device, double* tflops, double* ms)
+namespace {
+
+int fp64_peak_iters(int device, int iters, double* tflops, double* ms)
 {
     if (cudaSetDevice(device) != cudaSuccess) return -1;
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
     double* sink = nullptr;
     if (cudaMalloc(&sink, 1024 * sizeof(double)) != cudaSuccess) return -1;
-    const int threads = 256, blocks = nsm * 8, iters = 4096;
+    const int threads = 256, blocks = nsm * 8;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -92,4 +94,21 @@ extern "C" int cmaqchem_diag_fp64_peak(int device, double* tflops, double* ms)
     if (tflops) *tflops = flops / (t * 1.0e-3) / 1.0e12;
     if (ms) *ms = t;
     return 0;
+}
+
+}  // namespace
+
+extern "C" int cmaqchem_diag_fp64_peak(int device, double* tflops, double* ms)
+{
+    return fp64_peak_iters(device, 4096, tflops, ms);
+}
+
+extern "C" int cmaqchem_diag_fp64_peak_long(int device, double target_ms, double* tflops, double* ms)
+{
+    if (!(target_ms > 0.0)) return -1;
+    double t = 0.0;
+    if (fp64_peak_iters(device, 4096, nullptr, &t) != 0 || !(t > 0.0)) return -1;   // rate at 4096 links
+    double scale = (target_ms < 10.0 ? 10.0 : (target_ms > 5000.0 ? 5000.0 : target_ms)) / t;
+    const double iters = 4096.0 * scale;
+    return fp64_peak_iters(device, iters > 1.0e9 ? 1000000000 : (iters < 64.0 ? 64 : (int)iters), tflops, ms);
 }

@@ -42,6 +42,7 @@ constexpr int ST_NONFINITE = 4;      // an accepted solution held a non-finite v
 
 struct Tol {
     double rtol, atol, rnspec;
+    double dtmin = DTMIN;   // the reference's DTMIN; lowered only for tight accuracy runs
 };
 
 struct CellStats {
@@ -200,14 +201,14 @@ __device__ void attempt_phased(double* __restrict__ ws, CellState& s, double che
         s.have_f0 = false;
         s.tnow = tend;
         dtfac = s.lpass ? fmax(FACMIN, fmin(dtfac, FACMAX)) : fmax(FACMIN, fmin(dtfac, FACONE));
-        s.dt = fmin(DTMAX, fmax(DTMIN, dtfac * dt));
+        s.dt = fmin(DTMAX, fmax(tol.dtmin, dtfac * dt));
         s.lpass = true;
     } else {
         if (s.st.nfails == 0 && s.tnow == 0.0) s.st.nbad_starts++;
         s.st.nfails++;
         s.dt = FACMIN * dt;
         s.lpass = false;
-        if (s.dt < DTMIN) s.st.status |= ST_DT_UNDERFLOW;
+        if (s.dt < tol.dtmin) s.st.status |= ST_DT_UNDERFLOW;
     }
 }
 

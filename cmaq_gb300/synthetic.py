@@ -154,6 +154,22 @@ def make_grid(mech: str = "cb6r5_ae7_aq", ncols: int = 20, nrows: int = 20, nlay
                       seed=seed)
 
 
+def subgrid(g: GridInputs, col_step: int = 1, row_step: int = 1, lay_step: int = 1) -> GridInputs:
+    """Every col_step-th column, row_step-th row and lay_step-th layer of a grid, with the
+    same per-cell inputs: a sample of a large grid whose cells integrate exactly as they do
+    inside it (chemistry couples no cells)."""
+    c, r, lv = slice(None, None, col_step), slice(None, None, row_step), slice(None, None, lay_step)
+    conc = np.ascontiguousarray(g.conc[:, lv, r, c])
+    _, nlays, nrows, ncols = conc.shape
+    return GridInputs(mech=g.mech, ncols=ncols, nrows=nrows, nlays=nlays, nspcsd=g.nspcsd, conc=conc,
+                      ta=np.ascontiguousarray(g.ta[lv, r, c]), qv=np.ascontiguousarray(g.qv[lv, r, c]),
+                      dens=np.ascontiguousarray(g.dens[lv, r, c]), pres=np.ascontiguousarray(g.pres[lv, r, c]),
+                      seaice=np.ascontiguousarray(g.seaice[r, c]),
+                      ocean_szone=np.ascontiguousarray(g.ocean_szone[r, c]),
+                      rj=np.ascontiguousarray(g.rj[:, lv, r, c]), khetero=np.ascontiguousarray(g.khetero[lv, r, c]),
+                      cgrid_index=g.cgrid_index, seed=g.seed)
+
+
 # --- configurations of the chemistry benchmark (CB6r5 unless stated)
 CONFIGS = {
     "cpu4k": dict(ncols=20, nrows=20, nlays=10),                        # 4,000 cells

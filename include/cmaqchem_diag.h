@@ -13,6 +13,10 @@ extern "C" {
  * on every SM: TFLOP/s (an FMA counts 2) and the kernel time in ms. */
 int cmaqchem_diag_fp64_peak(int device, double* tflops, double* ms);
 
+/* The same measurement with a kernel of about target_ms milliseconds (clamped to
+ * 10-5000 ms), long enough for a clock sampler to record the SM clock it ran at. */
+int cmaqchem_diag_fp64_peak_long(int device, double target_ms, double* tflops, double* ms);
+
 /* Clock cycles per link of a dependent FP64 FMA chain run by one warp with active_lanes
  * (1-32) lanes active: the latency a cell's sequential FP64 work pays per operation. */
 int cmaqchem_diag_fp64_issue(int device, int active_lanes, double* cycles_per_instruction);
@@ -26,6 +30,10 @@ int cmaqchem_diag_fp64_issue(int device, int active_lanes, double* cycles_per_in
  * 0 (default): as many as fit) and "adjoint_tape_mb" (device memory for the adjoint's
  * step tape; a synchronisation step whose tape is larger is processed in batches of
  * consecutive cells; 0 (default): the largest step's tape, halved until it fits) and
+ * "ros3_dtmin_exp" (ROS3's minimum step is 10^value minutes; default -8, the reference's
+ * DTMIN; a lower value lets tight tolerances pass the initial radical transient) and
+ * "queue_history" (0: clear the step counts the work queue is ordered by, so that the next
+ * call is queued as a fresh run's first call) and
  * "host_chunks" (1-16, default 4: cmaqchem_step moves the grid in that many chunks of
  * consecutive cells so that copies overlap the integration of the previous chunk) and
  * "ebi_warp" (EBI solver: 1 (default) one cell per warp with its state in shared memory,

@@ -54,8 +54,12 @@ def test_run_aqchem_bookkeeping_on_the_host(kmt2_harness, tmp_path, monkeypatch)
     assert 20 < r["steps_per_cell"] < 100
     fl = bench_manifest_flops()
     assert r["flops_per_call"] > 40 * 20 * fl["per_attempt"]
+    # each routine's count times its own counter: four solves per attempt, f at stages 3 and 4
+    # plus once per accepted step, one J per accepted step, at least one factorisation per attempt
+    per_cell = 20 * (fl["decomp"] + 4 * fl["solve"] + 2 * fl["fun"] + fl["vector"])
+    assert r["flops_per_call"] > 40 * per_cell
     assert r["e2e"]["h2d_bytes_per_step"] == 40 * (15 + 161) * 8 and r["e2e"]["d2h_bytes_per_step"] == 40 * 161 * 8
-    assert r["parity"] == {"cells": 40, "same_steps": 1.0, "max_rel_same_steps": 0.0, "max_rel": 0.0}
+    assert r["parity"] == {"cells": 40, "same_steps": 1.0, "bit_equal_cells": 1.0, "max_rel": 0.0}
     assert r["cpu"]["cells"] == 40 and r["cpu"]["value"] > 0
 
 
