@@ -55,7 +55,7 @@ METRIC = "ROS3 CB6r5 grid-cells/s per 1-h chem step"
 UNIT = "grid-cells/s per 1-h chem step"
 RTOL, ATOL = 1.0e-3, 1.0e-9
 # tight tolerance of the accuracy block and its timing leg (DTMIN lowered to 1e-14 min)
-TIGHT_RTOL, TIGHT_ATOL = 1.0e-5, 1.0e-14
+TIGHT_RTOL, TIGHT_ATOL = 3.0e-7, 1.0e-16
 TSTEP = (10000, 500, 500)          # TSTEP(3) HHMMSS: output 1 h, sync 5 min
 STEPS_PER_HOUR = 12
 
@@ -255,25 +255,27 @@ def clock_peak(rec: dict, sm_mhz: float | None) -> float | None:
     return rec["fma_per_clk_per_sm"] * 2.0 * rec["sms"] * sm_mhz * 1e6 / 1e12
 
 
-def run_accuracy(g, device: int, tuned, threads: int, tight_tol=(1.0e-5, 1.0e-14), col_step: int = 46,
-                 row_step: int = 50) -> dict:
+def run_accuracy(g, device: int, tuned, threads: int, tight_tol=(TIGHT_RTOL, TIGHT_ATOL), col_step: int = 46,
+                 row_step: int = 50, lay_step: int = 2) -> dict:
     """Accuracy of the batched GPU kernel after one simulated hour (12 CHEM calls) on a
-    sample of the workload grid (every col_step-th column and row_step-th row, all layers),
-    against the oracle's tight solution (rtol 1e-8, atol 1e-18 ppmV, DTMIN lowered to 1e-14
-    min), on species above 1e-10 ppmV of the REAL(4) CGRID output: at the headline
-    tolerance and at a tight one (DTMIN lowered to 1e-14 there too)."""
+    sample of the workload grid (every col_step-th column, row_step-th row and lay_step-th
+    layer), against the oracle's tight solution (rtol 1e-8, atol 1e-16 ppmV, DTMIN lowered to
+    1e-14 min; within 4e-6 of a solution at rtol 1e-9, atol 1e-17 on such a sample), on
+    species above 1e-10 ppmV of the REAL(4) CGRID output: at the headline tolerance and at
+    the tight one (DTMIN lowered to 1e-14 there too)."""
     import torch
     from cmaq_gb300.chem import ChemSolver
     from cmaq_gb300.synthetic import subgrid
     sys.path.insert(0, str(ROOT / "oracle"))
     from oracle import Oracle
-    sub = subgrid(g, col_step, row_step, 1)
+    sub = subgrid(g, col_step, row_step, lay_step)
     o = Oracle(sub.mech)
     t0 = time.perf_counter()
     truth = sub.conc.copy()
     with o.tight():
         for _ in range(STEPS_PER_HOUR):
-            truth, tot = o.chem(sub, blksize=1, rtol=1.0e-8, atol=1.0e-18, threads=threads, conc=truth)
+            truth, tot = o.chem(sub, blksize=1, rtol=1.0e-8, atol=1.0e-16, threads=threads, conc=truth,
+                                max_iter=10000000)
             if tot["rc"] != 0:
                 return {"error": "the tight oracle solution failed"}
     truth_s = time.perf_counter() - t0
@@ -300,9 +302,9 @@ def run_accuracy(g, device: int, tuned, threads: int, tight_tol=(1.0e-5, 1.0e-14
         return {"rtol": rtol, "atol": atol, "max": float(rel.max()), "p99_9": float(np.quantile(rel, 0.999)),
                 "median": float(np.median(rel)), "failed_cells": int(failed)}
 
-    return {"sample": f"{sub.ncols}x{sub.nrows}x{sub.nlays} ({sub.ncell} cells): every {col_step}th column and "
-                      f"{row_step}th row of the workload grid, all layers",
-            "truth": "oracle (ROS3 per cell) rtol 1e-8, atol 1e-18 ppmV, DTMIN 1e-14 min",
+    return {"sample": f"{sub.ncols}x{sub.nrows}x{sub.nlays} ({sub.ncell} cells): every {col_step}th column, "
+                      f"{row_step}th row and {lay_step}th layer of the workload grid",
+            "truth": "oracle (ROS3 per cell) rtol 1e-8, atol 1e-16 ppmV, DTMIN 1e-14 min",
             "species": f"CGRID species above 1e-10 ppmV after the hour ({int(mask.sum())} values)",
             "truth_s": truth_s, "headline": gpu_hour(RTOL, ATOL, None),
             "tight": dict(gpu_hour(tight_tol[0], tight_tol[1], -14), dtmin_min=1.0e-14)}
@@ -836,6 +838,7 @@ def main():
         t0 = time.perf_counter()
         out = fn()
         legs_s[name] = round(time.perf_counter() - t0, 1)
+        print(f"[bench] {name}: {legs_s[name]} s", file=sys.stderr, flush=True)
         return out
     accuracy = leg("accuracy", extras and not a.no_accuracy,
                    lambda: run_accuracy(g, device, tuned, host_threads(), tight_tol))

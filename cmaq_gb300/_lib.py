@@ -76,9 +76,11 @@ def lib(variant: str = "default") -> C.CDLL:
     L.cmaqchem_diag_fp64_issue.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double)]
     L.cmaqchem_diag_fp64_peak_long.argtypes = [C.c_int, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.cmaqchem_diag_set_tuning.argtypes = [vp, C.c_char_p, C.c_int]
+    L.cmaqchem_diag_phase_cycles.argtypes = [C.c_int, C.POINTER(C.c_ulonglong), C.c_int]
     L.cmaqchem_kmt2_workspace_doubles.argtypes = [C.c_longlong]
     L.cmaqchem_kmt2_workspace_doubles.restype = C.c_longlong
     L.cmaqchem_kmt2_solve_device.argtypes = [C.c_longlong, vp, vp, vp, vp, vp, vp, C.c_longlong, vp]
+    L.cmaqchem_kmt2_solve.argtypes = [C.c_longlong, vp, vp, vp, vp, vp, C.c_int]
     return L
 
 

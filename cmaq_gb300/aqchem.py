@@ -56,3 +56,23 @@ def aqchem_kinetics(params: torch.Tensor, var_mix: torch.Tensor, *, lanes: int |
         _lib.check(L.cmaqchem_kmt2_solve_device(n, _ptr(params), _ptr(var_mix), _ptr(var_out), _ptr(fix_out),
                                                 _ptr(stats), _ptr(ws), ws.numel(), C.c_void_p(s.cuda_stream)))
     return (var_out, fix_out, stats) if with_fix else (var_out, stats)
+
+
+def aqchem_kinetics_host(params, var_mix, *, device: int = 0, with_fix: bool = False):
+    """The same integration on host numpy arrays, params [15][n] and var_mix [161][n]
+    float64, through the host-array entry point (cmaqchem_kmt2_solve): returns numpy
+    (var_out, stats) or (var_out, fix_out, stats)."""
+    import numpy as np
+    params = np.ascontiguousarray(params, dtype=np.float64)
+    var_mix = np.ascontiguousarray(var_mix, dtype=np.float64)
+    if params.ndim != 2 or params.shape[0] != NPARAM or var_mix.shape != (NVAR, params.shape[1]):
+        raise ValueError(f"params must be ({NPARAM}, n) and var_mix ({NVAR}, n)")
+    n = params.shape[1]
+    var_out = np.empty((NVAR, n))
+    fix_out = np.empty((NFIX, n)) if with_fix else None
+    stats = np.zeros((len(STATS), n), dtype=np.int32)
+    if n:
+        L = _lib.lib()
+        p = lambda a: None if a is None else C.c_void_p(a.ctypes.data)
+        _lib.check(L.cmaqchem_kmt2_solve(n, p(params), p(var_mix), p(var_out), p(fix_out), p(stats), int(device)))
+    return (var_out, fix_out, stats) if with_fix else (var_out, stats)

@@ -35,7 +35,14 @@ VARIANTS = {"default": (GEN_DEFAULT, ["-DCHEM_QUEUE_WARPS_PER_SM=16"]),
             "full255": ([], [Q8]), "pf255": (["-DCHEM_USE_PREFETCH"], [Q8]),
             "r168": ([], ["-maxrregcount=168"]),
             "r128": ([], ["-maxrregcount=128", "-DCHEM_QUEUE_WARPS_PER_SM=16"]),
-            "lucs": ([], ["-DCHEM_LDLU(p)=__ldcs(p)", Q8])}
+            "lucs": ([], ["-DCHEM_LDLU(p)=__ldcs(p)", Q8]),
+            # the default build with clock counters between the attempt's phase barriers
+            "phases": (GEN_DEFAULT, ["-DCHEM_QUEUE_WARPS_PER_SM=16", "-DCHEM_PHASE_TIMING"]),
+            # 1/U(i,i) by the correctly rounded reciprocal (same bits); L1 prefetch of the next row
+            "rcp": (GEN_DEFAULT + ["-DCHEM_RCP(x)=__drcp_rn(x)"], ["-DCHEM_QUEUE_WARPS_PER_SM=16"]),
+            "pfl1": (GEN_DEFAULT + ["-DCHEM_USE_PREFETCH_L1"], ["-DCHEM_QUEUE_WARPS_PER_SM=16"]),
+            "rcp_pfl1": (GEN_DEFAULT + ["-DCHEM_RCP(x)=__drcp_rn(x)", "-DCHEM_USE_PREFETCH_L1"],
+                         ["-DCHEM_QUEUE_WARPS_PER_SM=16"])}
 
 
 def _is_generated_math(src: Path) -> bool:

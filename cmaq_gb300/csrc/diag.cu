@@ -5,6 +5,11 @@
 
 #include "../../include/cmaqchem_diag.h"
 
+#ifdef CHEM_PHASE_TIMING
+// clock cycles per phase of the lock-stepped ROS3 attempt (ros3.cuh: CHEM_PHASE_MARK)
+__device__ unsigned long long g_chem_phase_cycles[8];
+#endif
+
 namespace {
 
 constexpr int CHAINS = 8;
@@ -111,4 +116,23 @@ extern "C" int cmaqchem_diag_fp64_peak_long(int device, double target_ms, double
     double scale = (target_ms < 10.0 ? 10.0 : (target_ms > 5000.0 ? 5000.0 : target_ms)) / t;
     const double iters = 4096.0 * scale;
     return fp64_peak_iters(device, iters > 1.0e9 ? 1000000000 : (iters < 64.0 ? 64 : (int)iters), tflops, ms);
+}
+
+extern "C" int cmaqchem_diag_phase_cycles(int device, unsigned long long* out, int reset)
+{
+#ifdef CHEM_PHASE_TIMING
+    if (cudaSetDevice(device) != cudaSuccess) return -1;
+    if (out && cudaMemcpyFromSymbol(out, g_chem_phase_cycles, 8 * sizeof(unsigned long long)) != cudaSuccess)
+        return -1;
+    if (reset) {
+        const unsigned long long z[8] = {};
+        if (cudaMemcpyToSymbol(g_chem_phase_cycles, z, sizeof(z)) != cudaSuccess) return -1;
+    }
+    return 0;
+#else
+    (void)device;
+    (void)out;
+    (void)reset;
+    return -1;
+#endif
 }

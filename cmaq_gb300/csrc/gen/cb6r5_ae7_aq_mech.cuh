@@ -19,6 +19,21 @@ __device__ __forceinline__ void chem_prefetch_l2(const double* p)
 #else
 #define CHEM_PREFETCH(p) ((void)0)
 #endif
+// L1 prefetch of the entries the next row reads (build variant 'pfl1'); off by default
+#ifdef CHEM_USE_PREFETCH_L1
+__device__ __forceinline__ void chem_prefetch_l1(const double* p)
+{
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(__cvta_generic_to_global(p)));
+}
+#define CHEM_PREFETCH_L1(p) chem_prefetch_l1(p)
+#else
+#define CHEM_PREFETCH_L1(p) ((void)0)
+#endif
+// 1/U(i,i): IEEE division by default; a build may use the correctly rounded
+// reciprocal __drcp_rn, which gives the same bits
+#ifndef CHEM_RCP
+#define CHEM_RCP(x) (1.0 / (x))
+#endif
 namespace mech_cb6r5_ae7_aq {
 constexpr const char* NAME = "cb6r5_ae7_aq";
 constexpr int NSPEC = 149;

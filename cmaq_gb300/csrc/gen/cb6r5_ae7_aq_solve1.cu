@@ -10,6 +10,7 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
     double* __restrict__ b = ws + rhs * 32;
     (void)vd;
     {
+      CHEM_PREFETCH_L1(ws + 77664);
       double x = b[0];
       b[0] = x;
     }
@@ -84,6 +85,7 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       b[544] = x;
     }
     {
+      CHEM_PREFETCH_L1(ws + 77696);
       double x = b[576];
       b[576] = x;
     }
@@ -110,6 +112,7 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       b[736] = x;
     }
     {
+      CHEM_PREFETCH_L1(ws + 77728);
       double x = b[768];
       b[768] = x;
     }
@@ -128,6 +131,7 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       b[864] = x;
     }
     {
+      CHEM_PREFETCH_L1(ws + 77760);
       double x = b[896];
       b[896] = x;
     }
@@ -170,6 +174,7 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       b[1184] = x;
     }
     {
+      CHEM_PREFETCH_L1(ws + 77792);
       double x = b[1216];
       b[1216] = x;
     }
@@ -181,6 +186,8 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       b[1248] = x;
     }
     {
+      CHEM_PREFETCH_L1(ws + 77824);
+      CHEM_PREFETCH_L1(ws + 77856);
       double x = b[1280];
       b[1280] = x;
     }
@@ -197,11 +204,17 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 77984);
       CHEM_PREFETCH(ws + 78016);
       CHEM_PREFETCH(ws + 78048);
+      CHEM_PREFETCH_L1(ws + 77888);
+      CHEM_PREFETCH_L1(ws + 77920);
+      CHEM_PREFETCH_L1(ws + 77952);
       double x = b[1344];
       b[1344] = x;
     }
     {
       CHEM_PREFETCH(ws + 78080);
+      CHEM_PREFETCH_L1(ws + 77984);
+      CHEM_PREFETCH_L1(ws + 78016);
+      CHEM_PREFETCH_L1(ws + 78048);
       double x = b[1376];
       x = fma(-CHEM_LDLU(lu + 256), b[64], x);
       x = fma(-CHEM_LDLU(lu + 288), b[96], x);
@@ -210,6 +223,7 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
     }
     {
       CHEM_PREFETCH(ws + 78112);
+      CHEM_PREFETCH_L1(ws + 78080);
       double x = b[1408];
       x = fma(-CHEM_LDLU(lu + 352), b[160], x);
       x = fma(-CHEM_LDLU(lu + 384), b[192], x);
@@ -217,6 +231,7 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       b[1408] = x;
     }
     {
+      CHEM_PREFETCH_L1(ws + 78112);
       double x = b[1440];
       x = fma(-CHEM_LDLU(lu + 448), b[704], x);
       b[1440] = x;
@@ -264,6 +279,7 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       b[1760] = x;
     }
     {
+      CHEM_PREFETCH_L1(ws + 78144);
       double x = b[1792];
       b[1792] = x;
     }
@@ -277,10 +293,14 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 78208);
       CHEM_PREFETCH(ws + 78240);
       CHEM_PREFETCH(ws + 78272);
+      CHEM_PREFETCH_L1(ws + 78176);
       double x = b[1856];
       b[1856] = x;
     }
     {
+      CHEM_PREFETCH_L1(ws + 78208);
+      CHEM_PREFETCH_L1(ws + 78240);
+      CHEM_PREFETCH_L1(ws + 78272);
       double x = b[1888];
       x = fma(-CHEM_LDLU(lu + 544), b[1856], x);
       b[1888] = x;
@@ -306,6 +326,7 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       b[2016] = x;
     }
     {
+      CHEM_PREFETCH_L1(ws + 78304);
       double x = b[2048];
       b[2048] = x;
     }
@@ -316,6 +337,7 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       b[2080] = x;
     }
     {
+      CHEM_PREFETCH_L1(ws + 78336);
       double x = b[2112];
       b[2112] = x;
     }
@@ -327,16 +349,19 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
     }
     {
       CHEM_PREFETCH(ws + 78400);
+      CHEM_PREFETCH_L1(ws + 78368);
       double x = b[2176];
       b[2176] = x;
     }
     {
       CHEM_PREFETCH(ws + 78432);
+      CHEM_PREFETCH_L1(ws + 78400);
       double x = b[2208];
       x = fma(-CHEM_LDLU(lu + 736), b[2016], x);
       b[2208] = x;
     }
     {
+      CHEM_PREFETCH_L1(ws + 78432);
       double x = b[2240];
       x = fma(-CHEM_LDLU(lu + 768), b[2144], x);
       b[2240] = x;
@@ -368,6 +393,7 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       b[2432] = x;
     }
     {
+      CHEM_PREFETCH_L1(ws + 78464);
       double x = b[2464];
       b[2464] = x;
     }
@@ -384,6 +410,7 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 78624);
       CHEM_PREFETCH(ws + 78656);
       CHEM_PREFETCH(ws + 78688);
+      CHEM_PREFETCH_L1(ws + 78496);
       double x = b[2528];
       b[2528] = x;
     }
@@ -391,11 +418,20 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 78720);
       CHEM_PREFETCH(ws + 78752);
       CHEM_PREFETCH(ws + 78784);
+      CHEM_PREFETCH_L1(ws + 78528);
+      CHEM_PREFETCH_L1(ws + 78560);
+      CHEM_PREFETCH_L1(ws + 78592);
+      CHEM_PREFETCH_L1(ws + 78624);
+      CHEM_PREFETCH_L1(ws + 78656);
+      CHEM_PREFETCH_L1(ws + 78688);
       double x = b[2560];
       x = fma(-CHEM_LDLU(lu + 864), b[1152], x);
       b[2560] = x;
     }
     {
+      CHEM_PREFETCH_L1(ws + 78720);
+      CHEM_PREFETCH_L1(ws + 78752);
+      CHEM_PREFETCH_L1(ws + 78784);
       double x = b[2592];
       x = fma(-CHEM_LDLU(lu + 896), b[480], x);
       x = fma(-CHEM_LDLU(lu + 928), b[512], x);
@@ -426,6 +462,8 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 78880);
       CHEM_PREFETCH(ws + 78912);
       CHEM_PREFETCH(ws + 78944);
+      CHEM_PREFETCH_L1(ws + 78816);
+      CHEM_PREFETCH_L1(ws + 78848);
       double x = b[2720];
       b[2720] = x;
     }
@@ -434,6 +472,9 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 79008);
       CHEM_PREFETCH(ws + 79040);
       CHEM_PREFETCH(ws + 79072);
+      CHEM_PREFETCH_L1(ws + 78880);
+      CHEM_PREFETCH_L1(ws + 78912);
+      CHEM_PREFETCH_L1(ws + 78944);
       double x = b[2752];
       x = fma(-CHEM_LDLU(lu + 1184), b[1504], x);
       x = fma(-CHEM_LDLU(lu + 1216), b[2304], x);
@@ -441,6 +482,10 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
     }
     {
       CHEM_PREFETCH(ws + 79104);
+      CHEM_PREFETCH_L1(ws + 78976);
+      CHEM_PREFETCH_L1(ws + 79008);
+      CHEM_PREFETCH_L1(ws + 79040);
+      CHEM_PREFETCH_L1(ws + 79072);
       double x = b[2784];
       x = fma(-CHEM_LDLU(lu + 1248), b[1504], x);
       x = fma(-CHEM_LDLU(lu + 1280), b[2304], x);
@@ -448,6 +493,7 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       b[2784] = x;
     }
     {
+      CHEM_PREFETCH_L1(ws + 79104);
       double x = b[2816];
       x = fma(-CHEM_LDLU(lu + 1344), b[1504], x);
       x = fma(-CHEM_LDLU(lu + 1376), b[2304], x);
@@ -467,11 +513,13 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
     }
     {
       CHEM_PREFETCH(ws + 79168);
+      CHEM_PREFETCH_L1(ws + 79136);
       double x = b[2912];
       b[2912] = x;
     }
     {
       CHEM_PREFETCH(ws + 79200);
+      CHEM_PREFETCH_L1(ws + 79168);
       double x = b[2944];
       x = fma(-CHEM_LDLU(lu + 1504), b[1088], x);
       b[2944] = x;
@@ -479,6 +527,7 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
     {
       CHEM_PREFETCH(ws + 79232);
       CHEM_PREFETCH(ws + 79264);
+      CHEM_PREFETCH_L1(ws + 79200);
       double x = b[2976];
       x = fma(-CHEM_LDLU(lu + 1536), b[2400], x);
       b[2976] = x;
@@ -489,12 +538,19 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 79360);
       CHEM_PREFETCH(ws + 79392);
       CHEM_PREFETCH(ws + 79424);
+      CHEM_PREFETCH_L1(ws + 79232);
+      CHEM_PREFETCH_L1(ws + 79264);
       double x = b[3008];
       x = fma(-CHEM_LDLU(lu + 1568), b[1184], x);
       b[3008] = x;
     }
     {
       CHEM_PREFETCH(ws + 79456);
+      CHEM_PREFETCH_L1(ws + 79296);
+      CHEM_PREFETCH_L1(ws + 79328);
+      CHEM_PREFETCH_L1(ws + 79360);
+      CHEM_PREFETCH_L1(ws + 79392);
+      CHEM_PREFETCH_L1(ws + 79424);
       double x = b[3040];
       x = fma(-CHEM_LDLU(lu + 1600), b[1184], x);
       x = fma(-CHEM_LDLU(lu + 1632), b[3008], x);
@@ -502,6 +558,7 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
     }
     {
       CHEM_PREFETCH(ws + 79488);
+      CHEM_PREFETCH_L1(ws + 79456);
       double x = b[3072];
       x = fma(-CHEM_LDLU(lu + 1664), b[448], x);
       x = fma(-CHEM_LDLU(lu + 1696), b[2144], x);
@@ -515,6 +572,7 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 79552);
       CHEM_PREFETCH(ws + 79584);
       CHEM_PREFETCH(ws + 79616);
+      CHEM_PREFETCH_L1(ws + 79488);
       double x = b[3104];
       x = fma(-CHEM_LDLU(lu + 1824), b[384], x);
       b[3104] = x;
@@ -525,6 +583,10 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 79712);
       CHEM_PREFETCH(ws + 79744);
       CHEM_PREFETCH(ws + 79776);
+      CHEM_PREFETCH_L1(ws + 79520);
+      CHEM_PREFETCH_L1(ws + 79552);
+      CHEM_PREFETCH_L1(ws + 79584);
+      CHEM_PREFETCH_L1(ws + 79616);
       double x = b[3136];
       x = fma(-CHEM_LDLU(lu + 1856), b[1664], x);
       b[3136] = x;
@@ -533,6 +595,11 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 79808);
       CHEM_PREFETCH(ws + 79840);
       CHEM_PREFETCH(ws + 79872);
+      CHEM_PREFETCH_L1(ws + 79648);
+      CHEM_PREFETCH_L1(ws + 79680);
+      CHEM_PREFETCH_L1(ws + 79712);
+      CHEM_PREFETCH_L1(ws + 79744);
+      CHEM_PREFETCH_L1(ws + 79776);
       double x = b[3168];
       x = fma(-CHEM_LDLU(lu + 1888), b[2752], x);
       x = fma(-CHEM_LDLU(lu + 1920), b[2784], x);
@@ -546,6 +613,9 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 79968);
       CHEM_PREFETCH(ws + 80000);
       CHEM_PREFETCH(ws + 80032);
+      CHEM_PREFETCH_L1(ws + 79808);
+      CHEM_PREFETCH_L1(ws + 79840);
+      CHEM_PREFETCH_L1(ws + 79872);
       double x = b[3200];
       x = fma(-CHEM_LDLU(lu + 2016), b[2752], x);
       x = fma(-CHEM_LDLU(lu + 2048), b[2784], x);
@@ -557,6 +627,11 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
     {
       CHEM_PREFETCH(ws + 80064);
       CHEM_PREFETCH(ws + 80096);
+      CHEM_PREFETCH_L1(ws + 79904);
+      CHEM_PREFETCH_L1(ws + 79936);
+      CHEM_PREFETCH_L1(ws + 79968);
+      CHEM_PREFETCH_L1(ws + 80000);
+      CHEM_PREFETCH_L1(ws + 80032);
       double x = b[3232];
       x = fma(-CHEM_LDLU(lu + 2176), b[2528], x);
       x = fma(-CHEM_LDLU(lu + 2208), b[2656], x);
@@ -566,6 +641,8 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
     {
       CHEM_PREFETCH(ws + 80128);
       CHEM_PREFETCH(ws + 80160);
+      CHEM_PREFETCH_L1(ws + 80064);
+      CHEM_PREFETCH_L1(ws + 80096);
       double x = b[3264];
       x = fma(-CHEM_LDLU(lu + 2272), b[448], x);
       x = fma(-CHEM_LDLU(lu + 2304), b[2144], x);
@@ -576,6 +653,8 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
     }
     {
       CHEM_PREFETCH(ws + 80192);
+      CHEM_PREFETCH_L1(ws + 80128);
+      CHEM_PREFETCH_L1(ws + 80160);
       double x = b[3296];
       x = fma(-CHEM_LDLU(lu + 2432), b[1056], x);
       x = fma(-CHEM_LDLU(lu + 2464), b[1664], x);
@@ -586,6 +665,7 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 80256);
       CHEM_PREFETCH(ws + 80288);
       CHEM_PREFETCH(ws + 80320);
+      CHEM_PREFETCH_L1(ws + 80192);
       double x = b[3328];
       x = fma(-CHEM_LDLU(lu + 2496), b[1760], x);
       x = fma(-CHEM_LDLU(lu + 2528), b[2176], x);
@@ -594,6 +674,10 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
     {
       CHEM_PREFETCH(ws + 80352);
       CHEM_PREFETCH(ws + 80384);
+      CHEM_PREFETCH_L1(ws + 80224);
+      CHEM_PREFETCH_L1(ws + 80256);
+      CHEM_PREFETCH_L1(ws + 80288);
+      CHEM_PREFETCH_L1(ws + 80320);
       double x = b[3360];
       x = fma(-CHEM_LDLU(lu + 2560), b[2848], x);
       b[3360] = x;
@@ -602,6 +686,8 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 80416);
       CHEM_PREFETCH(ws + 80448);
       CHEM_PREFETCH(ws + 80480);
+      CHEM_PREFETCH_L1(ws + 80352);
+      CHEM_PREFETCH_L1(ws + 80384);
       double x = b[3392];
       x = fma(-CHEM_LDLU(lu + 2592), b[896], x);
       x = fma(-CHEM_LDLU(lu + 2624), b[928], x);
@@ -611,6 +697,9 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
     }
     {
       CHEM_PREFETCH(ws + 80512);
+      CHEM_PREFETCH_L1(ws + 80416);
+      CHEM_PREFETCH_L1(ws + 80448);
+      CHEM_PREFETCH_L1(ws + 80480);
       double x = b[3424];
       x = fma(-CHEM_LDLU(lu + 2720), b[1664], x);
       x = fma(-CHEM_LDLU(lu + 2752), b[2528], x);
@@ -618,6 +707,7 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
     }
     {
       CHEM_PREFETCH(ws + 80544);
+      CHEM_PREFETCH_L1(ws + 80512);
       double x = b[3456];
       x = fma(-CHEM_LDLU(lu + 2784), b[3008], x);
       x = fma(-CHEM_LDLU(lu + 2816), b[3136], x);
@@ -628,6 +718,7 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 80576);
       CHEM_PREFETCH(ws + 80608);
       CHEM_PREFETCH(ws + 80640);
+      CHEM_PREFETCH_L1(ws + 80544);
       double x = b[3488];
       x = fma(-CHEM_LDLU(lu + 2880), b[1088], x);
       b[3488] = x;
@@ -635,6 +726,9 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
     {
       CHEM_PREFETCH(ws + 80672);
       CHEM_PREFETCH(ws + 80704);
+      CHEM_PREFETCH_L1(ws + 80576);
+      CHEM_PREFETCH_L1(ws + 80608);
+      CHEM_PREFETCH_L1(ws + 80640);
       double x = b[3520];
       x = fma(-CHEM_LDLU(lu + 2912), b[2016], x);
       b[3520] = x;
@@ -645,6 +739,8 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 80800);
       CHEM_PREFETCH(ws + 80832);
       CHEM_PREFETCH(ws + 80864);
+      CHEM_PREFETCH_L1(ws + 80672);
+      CHEM_PREFETCH_L1(ws + 80704);
       double x = b[3552];
       x = fma(-CHEM_LDLU(lu + 2944), b[1632], x);
       x = fma(-CHEM_LDLU(lu + 2976), b[3136], x);
@@ -658,6 +754,11 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 80992);
       CHEM_PREFETCH(ws + 81024);
       CHEM_PREFETCH(ws + 81056);
+      CHEM_PREFETCH_L1(ws + 80736);
+      CHEM_PREFETCH_L1(ws + 80768);
+      CHEM_PREFETCH_L1(ws + 80800);
+      CHEM_PREFETCH_L1(ws + 80832);
+      CHEM_PREFETCH_L1(ws + 80864);
       double x = b[3584];
       x = fma(-CHEM_LDLU(lu + 3040), b[1120], x);
       x = fma(-CHEM_LDLU(lu + 3072), b[1152], x);
@@ -672,6 +773,12 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 81248);
       CHEM_PREFETCH(ws + 81280);
       CHEM_PREFETCH(ws + 81312);
+      CHEM_PREFETCH_L1(ws + 80896);
+      CHEM_PREFETCH_L1(ws + 80928);
+      CHEM_PREFETCH_L1(ws + 80960);
+      CHEM_PREFETCH_L1(ws + 80992);
+      CHEM_PREFETCH_L1(ws + 81024);
+      CHEM_PREFETCH_L1(ws + 81056);
       double x = b[3616];
       x = fma(-CHEM_LDLU(lu + 3104), b[384], x);
       x = fma(-CHEM_LDLU(lu + 3136), b[1088], x);
@@ -690,6 +797,14 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 81536);
       CHEM_PREFETCH(ws + 81568);
       CHEM_PREFETCH(ws + 81600);
+      CHEM_PREFETCH_L1(ws + 81088);
+      CHEM_PREFETCH_L1(ws + 81120);
+      CHEM_PREFETCH_L1(ws + 81152);
+      CHEM_PREFETCH_L1(ws + 81184);
+      CHEM_PREFETCH_L1(ws + 81216);
+      CHEM_PREFETCH_L1(ws + 81248);
+      CHEM_PREFETCH_L1(ws + 81280);
+      CHEM_PREFETCH_L1(ws + 81312);
       double x = b[3648];
       x = fma(-CHEM_LDLU(lu + 3264), b[960], x);
       x = fma(-CHEM_LDLU(lu + 3296), b[1984], x);
@@ -702,6 +817,15 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
     {
       CHEM_PREFETCH(ws + 81632);
       CHEM_PREFETCH(ws + 81664);
+      CHEM_PREFETCH_L1(ws + 81344);
+      CHEM_PREFETCH_L1(ws + 81376);
+      CHEM_PREFETCH_L1(ws + 81408);
+      CHEM_PREFETCH_L1(ws + 81440);
+      CHEM_PREFETCH_L1(ws + 81472);
+      CHEM_PREFETCH_L1(ws + 81504);
+      CHEM_PREFETCH_L1(ws + 81536);
+      CHEM_PREFETCH_L1(ws + 81568);
+      CHEM_PREFETCH_L1(ws + 81600);
       double x = b[3680];
       x = fma(-CHEM_LDLU(lu + 3456), b[1504], x);
       x = fma(-CHEM_LDLU(lu + 3488), b[2304], x);
@@ -721,6 +845,8 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 81824);
       CHEM_PREFETCH(ws + 81856);
       CHEM_PREFETCH(ws + 81888);
+      CHEM_PREFETCH_L1(ws + 81632);
+      CHEM_PREFETCH_L1(ws + 81664);
       double x = b[3712];
       x = fma(-CHEM_LDLU(lu + 3712), b[1504], x);
       x = fma(-CHEM_LDLU(lu + 3744), b[2304], x);
@@ -738,6 +864,13 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 81952);
       CHEM_PREFETCH(ws + 81984);
       CHEM_PREFETCH(ws + 82016);
+      CHEM_PREFETCH_L1(ws + 81696);
+      CHEM_PREFETCH_L1(ws + 81728);
+      CHEM_PREFETCH_L1(ws + 81760);
+      CHEM_PREFETCH_L1(ws + 81792);
+      CHEM_PREFETCH_L1(ws + 81824);
+      CHEM_PREFETCH_L1(ws + 81856);
+      CHEM_PREFETCH_L1(ws + 81888);
       double x = b[3744];
       x = fma(-CHEM_LDLU(lu + 4000), b[1792], x);
       x = fma(-CHEM_LDLU(lu + 4032), b[3616], x);
@@ -749,6 +882,10 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 82112);
       CHEM_PREFETCH(ws + 82144);
       CHEM_PREFETCH(ws + 82176);
+      CHEM_PREFETCH_L1(ws + 81920);
+      CHEM_PREFETCH_L1(ws + 81952);
+      CHEM_PREFETCH_L1(ws + 81984);
+      CHEM_PREFETCH_L1(ws + 82016);
       double x = b[3776];
       x = fma(-CHEM_LDLU(lu + 4064), b[352], x);
       x = fma(-CHEM_LDLU(lu + 4096), b[1632], x);
@@ -763,6 +900,11 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 82208);
       CHEM_PREFETCH(ws + 82240);
       CHEM_PREFETCH(ws + 82272);
+      CHEM_PREFETCH_L1(ws + 82048);
+      CHEM_PREFETCH_L1(ws + 82080);
+      CHEM_PREFETCH_L1(ws + 82112);
+      CHEM_PREFETCH_L1(ws + 82144);
+      CHEM_PREFETCH_L1(ws + 82176);
       double x = b[3808];
       x = fma(-CHEM_LDLU(lu + 4288), b[1120], x);
       x = fma(-CHEM_LDLU(lu + 4320), b[1152], x);
@@ -777,6 +919,9 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 82400);
       CHEM_PREFETCH(ws + 82432);
       CHEM_PREFETCH(ws + 82464);
+      CHEM_PREFETCH_L1(ws + 82208);
+      CHEM_PREFETCH_L1(ws + 82240);
+      CHEM_PREFETCH_L1(ws + 82272);
       double x = b[3840];
       x = fma(-CHEM_LDLU(lu + 4416), b[864], x);
       x = fma(-CHEM_LDLU(lu + 4448), b[1632], x);
@@ -793,6 +938,12 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 82624);
       CHEM_PREFETCH(ws + 82656);
       CHEM_PREFETCH(ws + 82688);
+      CHEM_PREFETCH_L1(ws + 82304);
+      CHEM_PREFETCH_L1(ws + 82336);
+      CHEM_PREFETCH_L1(ws + 82368);
+      CHEM_PREFETCH_L1(ws + 82400);
+      CHEM_PREFETCH_L1(ws + 82432);
+      CHEM_PREFETCH_L1(ws + 82464);
       double x = b[3872];
       x = fma(-CHEM_LDLU(lu + 4576), b[1024], x);
       x = fma(-CHEM_LDLU(lu + 4608), b[2528], x);
@@ -810,6 +961,13 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 82944);
       CHEM_PREFETCH(ws + 82976);
       CHEM_PREFETCH(ws + 83008);
+      CHEM_PREFETCH_L1(ws + 82496);
+      CHEM_PREFETCH_L1(ws + 82528);
+      CHEM_PREFETCH_L1(ws + 82560);
+      CHEM_PREFETCH_L1(ws + 82592);
+      CHEM_PREFETCH_L1(ws + 82624);
+      CHEM_PREFETCH_L1(ws + 82656);
+      CHEM_PREFETCH_L1(ws + 82688);
       double x = b[3904];
       x = fma(-CHEM_LDLU(lu + 4672), b[3136], x);
       x = fma(-CHEM_LDLU(lu + 4704), b[3296], x);
@@ -830,6 +988,16 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 83264);
       CHEM_PREFETCH(ws + 83296);
       CHEM_PREFETCH(ws + 83328);
+      CHEM_PREFETCH_L1(ws + 82720);
+      CHEM_PREFETCH_L1(ws + 82752);
+      CHEM_PREFETCH_L1(ws + 82784);
+      CHEM_PREFETCH_L1(ws + 82816);
+      CHEM_PREFETCH_L1(ws + 82848);
+      CHEM_PREFETCH_L1(ws + 82880);
+      CHEM_PREFETCH_L1(ws + 82912);
+      CHEM_PREFETCH_L1(ws + 82944);
+      CHEM_PREFETCH_L1(ws + 82976);
+      CHEM_PREFETCH_L1(ws + 83008);
       double x = b[3936];
       x = fma(-CHEM_LDLU(lu + 4864), b[384], x);
       x = fma(-CHEM_LDLU(lu + 4896), b[1088], x);
@@ -858,6 +1026,16 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 83808);
       CHEM_PREFETCH(ws + 83840);
       CHEM_PREFETCH(ws + 83872);
+      CHEM_PREFETCH_L1(ws + 83040);
+      CHEM_PREFETCH_L1(ws + 83072);
+      CHEM_PREFETCH_L1(ws + 83104);
+      CHEM_PREFETCH_L1(ws + 83136);
+      CHEM_PREFETCH_L1(ws + 83168);
+      CHEM_PREFETCH_L1(ws + 83200);
+      CHEM_PREFETCH_L1(ws + 83232);
+      CHEM_PREFETCH_L1(ws + 83264);
+      CHEM_PREFETCH_L1(ws + 83296);
+      CHEM_PREFETCH_L1(ws + 83328);
       double x = b[3968];
       x = fma(-CHEM_LDLU(lu + 5088), b[832], x);
       x = fma(-CHEM_LDLU(lu + 5120), b[864], x);
@@ -886,6 +1064,23 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 84256);
       CHEM_PREFETCH(ws + 84288);
       CHEM_PREFETCH(ws + 84320);
+      CHEM_PREFETCH_L1(ws + 83360);
+      CHEM_PREFETCH_L1(ws + 83392);
+      CHEM_PREFETCH_L1(ws + 83424);
+      CHEM_PREFETCH_L1(ws + 83456);
+      CHEM_PREFETCH_L1(ws + 83488);
+      CHEM_PREFETCH_L1(ws + 83520);
+      CHEM_PREFETCH_L1(ws + 83552);
+      CHEM_PREFETCH_L1(ws + 83584);
+      CHEM_PREFETCH_L1(ws + 83616);
+      CHEM_PREFETCH_L1(ws + 83648);
+      CHEM_PREFETCH_L1(ws + 83680);
+      CHEM_PREFETCH_L1(ws + 83712);
+      CHEM_PREFETCH_L1(ws + 83744);
+      CHEM_PREFETCH_L1(ws + 83776);
+      CHEM_PREFETCH_L1(ws + 83808);
+      CHEM_PREFETCH_L1(ws + 83840);
+      CHEM_PREFETCH_L1(ws + 83872);
       double x = b[4000];
       x = fma(-CHEM_LDLU(lu + 5408), b[3136], x);
       x = fma(-CHEM_LDLU(lu + 5440), b[3296], x);
@@ -908,6 +1103,20 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 84512);
       CHEM_PREFETCH(ws + 84544);
       CHEM_PREFETCH(ws + 84576);
+      CHEM_PREFETCH_L1(ws + 83904);
+      CHEM_PREFETCH_L1(ws + 83936);
+      CHEM_PREFETCH_L1(ws + 83968);
+      CHEM_PREFETCH_L1(ws + 84000);
+      CHEM_PREFETCH_L1(ws + 84032);
+      CHEM_PREFETCH_L1(ws + 84064);
+      CHEM_PREFETCH_L1(ws + 84096);
+      CHEM_PREFETCH_L1(ws + 84128);
+      CHEM_PREFETCH_L1(ws + 84160);
+      CHEM_PREFETCH_L1(ws + 84192);
+      CHEM_PREFETCH_L1(ws + 84224);
+      CHEM_PREFETCH_L1(ws + 84256);
+      CHEM_PREFETCH_L1(ws + 84288);
+      CHEM_PREFETCH_L1(ws + 84320);
       double x = b[4032];
       x = fma(-CHEM_LDLU(lu + 5728), b[1632], x);
       x = fma(-CHEM_LDLU(lu + 5760), b[1792], x);
@@ -941,6 +1150,14 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 84896);
       CHEM_PREFETCH(ws + 84928);
       CHEM_PREFETCH(ws + 84960);
+      CHEM_PREFETCH_L1(ws + 84352);
+      CHEM_PREFETCH_L1(ws + 84384);
+      CHEM_PREFETCH_L1(ws + 84416);
+      CHEM_PREFETCH_L1(ws + 84448);
+      CHEM_PREFETCH_L1(ws + 84480);
+      CHEM_PREFETCH_L1(ws + 84512);
+      CHEM_PREFETCH_L1(ws + 84544);
+      CHEM_PREFETCH_L1(ws + 84576);
       double x = b[4064];
       x = fma(-CHEM_LDLU(lu + 6272), b[928], x);
       x = fma(-CHEM_LDLU(lu + 6304), b[960], x);
@@ -973,6 +1190,18 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 85344);
       CHEM_PREFETCH(ws + 85376);
       CHEM_PREFETCH(ws + 85408);
+      CHEM_PREFETCH_L1(ws + 84608);
+      CHEM_PREFETCH_L1(ws + 84640);
+      CHEM_PREFETCH_L1(ws + 84672);
+      CHEM_PREFETCH_L1(ws + 84704);
+      CHEM_PREFETCH_L1(ws + 84736);
+      CHEM_PREFETCH_L1(ws + 84768);
+      CHEM_PREFETCH_L1(ws + 84800);
+      CHEM_PREFETCH_L1(ws + 84832);
+      CHEM_PREFETCH_L1(ws + 84864);
+      CHEM_PREFETCH_L1(ws + 84896);
+      CHEM_PREFETCH_L1(ws + 84928);
+      CHEM_PREFETCH_L1(ws + 84960);
       double x = b[4096];
       x = fma(-CHEM_LDLU(lu + 6720), b[1952], x);
       x = fma(-CHEM_LDLU(lu + 6752), b[2048], x);
@@ -1005,6 +1234,20 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 85984);
       CHEM_PREFETCH(ws + 86016);
       CHEM_PREFETCH(ws + 86048);
+      CHEM_PREFETCH_L1(ws + 84992);
+      CHEM_PREFETCH_L1(ws + 85024);
+      CHEM_PREFETCH_L1(ws + 85056);
+      CHEM_PREFETCH_L1(ws + 85088);
+      CHEM_PREFETCH_L1(ws + 85120);
+      CHEM_PREFETCH_L1(ws + 85152);
+      CHEM_PREFETCH_L1(ws + 85184);
+      CHEM_PREFETCH_L1(ws + 85216);
+      CHEM_PREFETCH_L1(ws + 85248);
+      CHEM_PREFETCH_L1(ws + 85280);
+      CHEM_PREFETCH_L1(ws + 85312);
+      CHEM_PREFETCH_L1(ws + 85344);
+      CHEM_PREFETCH_L1(ws + 85376);
+      CHEM_PREFETCH_L1(ws + 85408);
       double x = b[4128];
       x = fma(-CHEM_LDLU(lu + 6976), b[832], x);
       x = fma(-CHEM_LDLU(lu + 7008), b[864], x);
@@ -1034,6 +1277,26 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 86400);
       CHEM_PREFETCH(ws + 86432);
       CHEM_PREFETCH(ws + 86464);
+      CHEM_PREFETCH_L1(ws + 85440);
+      CHEM_PREFETCH_L1(ws + 85472);
+      CHEM_PREFETCH_L1(ws + 85504);
+      CHEM_PREFETCH_L1(ws + 85536);
+      CHEM_PREFETCH_L1(ws + 85568);
+      CHEM_PREFETCH_L1(ws + 85600);
+      CHEM_PREFETCH_L1(ws + 85632);
+      CHEM_PREFETCH_L1(ws + 85664);
+      CHEM_PREFETCH_L1(ws + 85696);
+      CHEM_PREFETCH_L1(ws + 85728);
+      CHEM_PREFETCH_L1(ws + 85760);
+      CHEM_PREFETCH_L1(ws + 85792);
+      CHEM_PREFETCH_L1(ws + 85824);
+      CHEM_PREFETCH_L1(ws + 85856);
+      CHEM_PREFETCH_L1(ws + 85888);
+      CHEM_PREFETCH_L1(ws + 85920);
+      CHEM_PREFETCH_L1(ws + 85952);
+      CHEM_PREFETCH_L1(ws + 85984);
+      CHEM_PREFETCH_L1(ws + 86016);
+      CHEM_PREFETCH_L1(ws + 86048);
       double x = b[4160];
       x = fma(-CHEM_LDLU(lu + 7360), b[672], x);
       x = fma(-CHEM_LDLU(lu + 7392), b[2048], x);
@@ -1069,6 +1332,19 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 86944);
       CHEM_PREFETCH(ws + 86976);
       CHEM_PREFETCH(ws + 87008);
+      CHEM_PREFETCH_L1(ws + 86080);
+      CHEM_PREFETCH_L1(ws + 86112);
+      CHEM_PREFETCH_L1(ws + 86144);
+      CHEM_PREFETCH_L1(ws + 86176);
+      CHEM_PREFETCH_L1(ws + 86208);
+      CHEM_PREFETCH_L1(ws + 86240);
+      CHEM_PREFETCH_L1(ws + 86272);
+      CHEM_PREFETCH_L1(ws + 86304);
+      CHEM_PREFETCH_L1(ws + 86336);
+      CHEM_PREFETCH_L1(ws + 86368);
+      CHEM_PREFETCH_L1(ws + 86400);
+      CHEM_PREFETCH_L1(ws + 86432);
+      CHEM_PREFETCH_L1(ws + 86464);
       double x = b[4192];
       x = fma(-CHEM_LDLU(lu + 7808), b[1024], x);
       x = fma(-CHEM_LDLU(lu + 7840), b[1216], x);
@@ -1110,6 +1386,23 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 87488);
       CHEM_PREFETCH(ws + 87520);
       CHEM_PREFETCH(ws + 87552);
+      CHEM_PREFETCH_L1(ws + 86496);
+      CHEM_PREFETCH_L1(ws + 86528);
+      CHEM_PREFETCH_L1(ws + 86560);
+      CHEM_PREFETCH_L1(ws + 86592);
+      CHEM_PREFETCH_L1(ws + 86624);
+      CHEM_PREFETCH_L1(ws + 86656);
+      CHEM_PREFETCH_L1(ws + 86688);
+      CHEM_PREFETCH_L1(ws + 86720);
+      CHEM_PREFETCH_L1(ws + 86752);
+      CHEM_PREFETCH_L1(ws + 86784);
+      CHEM_PREFETCH_L1(ws + 86816);
+      CHEM_PREFETCH_L1(ws + 86848);
+      CHEM_PREFETCH_L1(ws + 86880);
+      CHEM_PREFETCH_L1(ws + 86912);
+      CHEM_PREFETCH_L1(ws + 86944);
+      CHEM_PREFETCH_L1(ws + 86976);
+      CHEM_PREFETCH_L1(ws + 87008);
       double x = b[4224];
       x = fma(-CHEM_LDLU(lu + 8448), b[928], x);
       x = fma(-CHEM_LDLU(lu + 8480), b[960], x);
@@ -1148,6 +1441,23 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 88160);
       CHEM_PREFETCH(ws + 88192);
       CHEM_PREFETCH(ws + 88224);
+      CHEM_PREFETCH_L1(ws + 87040);
+      CHEM_PREFETCH_L1(ws + 87072);
+      CHEM_PREFETCH_L1(ws + 87104);
+      CHEM_PREFETCH_L1(ws + 87136);
+      CHEM_PREFETCH_L1(ws + 87168);
+      CHEM_PREFETCH_L1(ws + 87200);
+      CHEM_PREFETCH_L1(ws + 87232);
+      CHEM_PREFETCH_L1(ws + 87264);
+      CHEM_PREFETCH_L1(ws + 87296);
+      CHEM_PREFETCH_L1(ws + 87328);
+      CHEM_PREFETCH_L1(ws + 87360);
+      CHEM_PREFETCH_L1(ws + 87392);
+      CHEM_PREFETCH_L1(ws + 87424);
+      CHEM_PREFETCH_L1(ws + 87456);
+      CHEM_PREFETCH_L1(ws + 87488);
+      CHEM_PREFETCH_L1(ws + 87520);
+      CHEM_PREFETCH_L1(ws + 87552);
       double x = b[4256];
       x = fma(-CHEM_LDLU(lu + 8864), b[352], x);
       x = fma(-CHEM_LDLU(lu + 8896), b[1792], x);
@@ -1189,6 +1499,27 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 88800);
       CHEM_PREFETCH(ws + 88832);
       CHEM_PREFETCH(ws + 88864);
+      CHEM_PREFETCH_L1(ws + 87584);
+      CHEM_PREFETCH_L1(ws + 87616);
+      CHEM_PREFETCH_L1(ws + 87648);
+      CHEM_PREFETCH_L1(ws + 87680);
+      CHEM_PREFETCH_L1(ws + 87712);
+      CHEM_PREFETCH_L1(ws + 87744);
+      CHEM_PREFETCH_L1(ws + 87776);
+      CHEM_PREFETCH_L1(ws + 87808);
+      CHEM_PREFETCH_L1(ws + 87840);
+      CHEM_PREFETCH_L1(ws + 87872);
+      CHEM_PREFETCH_L1(ws + 87904);
+      CHEM_PREFETCH_L1(ws + 87936);
+      CHEM_PREFETCH_L1(ws + 87968);
+      CHEM_PREFETCH_L1(ws + 88000);
+      CHEM_PREFETCH_L1(ws + 88032);
+      CHEM_PREFETCH_L1(ws + 88064);
+      CHEM_PREFETCH_L1(ws + 88096);
+      CHEM_PREFETCH_L1(ws + 88128);
+      CHEM_PREFETCH_L1(ws + 88160);
+      CHEM_PREFETCH_L1(ws + 88192);
+      CHEM_PREFETCH_L1(ws + 88224);
       double x = b[4288];
       x = fma(-CHEM_LDLU(lu + 9408), b[832], x);
       x = fma(-CHEM_LDLU(lu + 9440), b[896], x);
@@ -1232,6 +1563,26 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 89504);
       CHEM_PREFETCH(ws + 89536);
       CHEM_PREFETCH(ws + 89568);
+      CHEM_PREFETCH_L1(ws + 88256);
+      CHEM_PREFETCH_L1(ws + 88288);
+      CHEM_PREFETCH_L1(ws + 88320);
+      CHEM_PREFETCH_L1(ws + 88352);
+      CHEM_PREFETCH_L1(ws + 88384);
+      CHEM_PREFETCH_L1(ws + 88416);
+      CHEM_PREFETCH_L1(ws + 88448);
+      CHEM_PREFETCH_L1(ws + 88480);
+      CHEM_PREFETCH_L1(ws + 88512);
+      CHEM_PREFETCH_L1(ws + 88544);
+      CHEM_PREFETCH_L1(ws + 88576);
+      CHEM_PREFETCH_L1(ws + 88608);
+      CHEM_PREFETCH_L1(ws + 88640);
+      CHEM_PREFETCH_L1(ws + 88672);
+      CHEM_PREFETCH_L1(ws + 88704);
+      CHEM_PREFETCH_L1(ws + 88736);
+      CHEM_PREFETCH_L1(ws + 88768);
+      CHEM_PREFETCH_L1(ws + 88800);
+      CHEM_PREFETCH_L1(ws + 88832);
+      CHEM_PREFETCH_L1(ws + 88864);
       double x = b[4320];
       x = fma(-CHEM_LDLU(lu + 9952), b[1856], x);
       x = fma(-CHEM_LDLU(lu + 9984), b[2048], x);
@@ -1277,6 +1628,28 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 90144);
       CHEM_PREFETCH(ws + 90176);
       CHEM_PREFETCH(ws + 90208);
+      CHEM_PREFETCH_L1(ws + 88896);
+      CHEM_PREFETCH_L1(ws + 88928);
+      CHEM_PREFETCH_L1(ws + 88960);
+      CHEM_PREFETCH_L1(ws + 88992);
+      CHEM_PREFETCH_L1(ws + 89024);
+      CHEM_PREFETCH_L1(ws + 89056);
+      CHEM_PREFETCH_L1(ws + 89088);
+      CHEM_PREFETCH_L1(ws + 89120);
+      CHEM_PREFETCH_L1(ws + 89152);
+      CHEM_PREFETCH_L1(ws + 89184);
+      CHEM_PREFETCH_L1(ws + 89216);
+      CHEM_PREFETCH_L1(ws + 89248);
+      CHEM_PREFETCH_L1(ws + 89280);
+      CHEM_PREFETCH_L1(ws + 89312);
+      CHEM_PREFETCH_L1(ws + 89344);
+      CHEM_PREFETCH_L1(ws + 89376);
+      CHEM_PREFETCH_L1(ws + 89408);
+      CHEM_PREFETCH_L1(ws + 89440);
+      CHEM_PREFETCH_L1(ws + 89472);
+      CHEM_PREFETCH_L1(ws + 89504);
+      CHEM_PREFETCH_L1(ws + 89536);
+      CHEM_PREFETCH_L1(ws + 89568);
       double x = b[4352];
       x = fma(-CHEM_LDLU(lu + 10624), b[1632], x);
       x = fma(-CHEM_LDLU(lu + 10656), b[1984], x);
@@ -1324,6 +1697,26 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 90880);
       CHEM_PREFETCH(ws + 90912);
       CHEM_PREFETCH(ws + 90944);
+      CHEM_PREFETCH_L1(ws + 89600);
+      CHEM_PREFETCH_L1(ws + 89632);
+      CHEM_PREFETCH_L1(ws + 89664);
+      CHEM_PREFETCH_L1(ws + 89696);
+      CHEM_PREFETCH_L1(ws + 89728);
+      CHEM_PREFETCH_L1(ws + 89760);
+      CHEM_PREFETCH_L1(ws + 89792);
+      CHEM_PREFETCH_L1(ws + 89824);
+      CHEM_PREFETCH_L1(ws + 89856);
+      CHEM_PREFETCH_L1(ws + 89888);
+      CHEM_PREFETCH_L1(ws + 89920);
+      CHEM_PREFETCH_L1(ws + 89952);
+      CHEM_PREFETCH_L1(ws + 89984);
+      CHEM_PREFETCH_L1(ws + 90016);
+      CHEM_PREFETCH_L1(ws + 90048);
+      CHEM_PREFETCH_L1(ws + 90080);
+      CHEM_PREFETCH_L1(ws + 90112);
+      CHEM_PREFETCH_L1(ws + 90144);
+      CHEM_PREFETCH_L1(ws + 90176);
+      CHEM_PREFETCH_L1(ws + 90208);
       double x = b[4384];
       x = fma(-CHEM_LDLU(lu + 11264), b[1728], x);
       x = fma(-CHEM_LDLU(lu + 11296), b[2144], x);
@@ -1373,6 +1766,29 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 91616);
       CHEM_PREFETCH(ws + 91648);
       CHEM_PREFETCH(ws + 91680);
+      CHEM_PREFETCH_L1(ws + 90240);
+      CHEM_PREFETCH_L1(ws + 90272);
+      CHEM_PREFETCH_L1(ws + 90304);
+      CHEM_PREFETCH_L1(ws + 90336);
+      CHEM_PREFETCH_L1(ws + 90368);
+      CHEM_PREFETCH_L1(ws + 90400);
+      CHEM_PREFETCH_L1(ws + 90432);
+      CHEM_PREFETCH_L1(ws + 90464);
+      CHEM_PREFETCH_L1(ws + 90496);
+      CHEM_PREFETCH_L1(ws + 90528);
+      CHEM_PREFETCH_L1(ws + 90560);
+      CHEM_PREFETCH_L1(ws + 90592);
+      CHEM_PREFETCH_L1(ws + 90624);
+      CHEM_PREFETCH_L1(ws + 90656);
+      CHEM_PREFETCH_L1(ws + 90688);
+      CHEM_PREFETCH_L1(ws + 90720);
+      CHEM_PREFETCH_L1(ws + 90752);
+      CHEM_PREFETCH_L1(ws + 90784);
+      CHEM_PREFETCH_L1(ws + 90816);
+      CHEM_PREFETCH_L1(ws + 90848);
+      CHEM_PREFETCH_L1(ws + 90880);
+      CHEM_PREFETCH_L1(ws + 90912);
+      CHEM_PREFETCH_L1(ws + 90944);
       double x = b[4416];
       x = fma(-CHEM_LDLU(lu + 11968), b[416], x);
       x = fma(-CHEM_LDLU(lu + 12000), b[2016], x);
@@ -1423,6 +1839,29 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 92448);
       CHEM_PREFETCH(ws + 92480);
       CHEM_PREFETCH(ws + 92512);
+      CHEM_PREFETCH_L1(ws + 90976);
+      CHEM_PREFETCH_L1(ws + 91008);
+      CHEM_PREFETCH_L1(ws + 91040);
+      CHEM_PREFETCH_L1(ws + 91072);
+      CHEM_PREFETCH_L1(ws + 91104);
+      CHEM_PREFETCH_L1(ws + 91136);
+      CHEM_PREFETCH_L1(ws + 91168);
+      CHEM_PREFETCH_L1(ws + 91200);
+      CHEM_PREFETCH_L1(ws + 91232);
+      CHEM_PREFETCH_L1(ws + 91264);
+      CHEM_PREFETCH_L1(ws + 91296);
+      CHEM_PREFETCH_L1(ws + 91328);
+      CHEM_PREFETCH_L1(ws + 91360);
+      CHEM_PREFETCH_L1(ws + 91392);
+      CHEM_PREFETCH_L1(ws + 91424);
+      CHEM_PREFETCH_L1(ws + 91456);
+      CHEM_PREFETCH_L1(ws + 91488);
+      CHEM_PREFETCH_L1(ws + 91520);
+      CHEM_PREFETCH_L1(ws + 91552);
+      CHEM_PREFETCH_L1(ws + 91584);
+      CHEM_PREFETCH_L1(ws + 91616);
+      CHEM_PREFETCH_L1(ws + 91648);
+      CHEM_PREFETCH_L1(ws + 91680);
       double x = b[4448];
       x = fma(-CHEM_LDLU(lu + 12608), b[1344], x);
       x = fma(-CHEM_LDLU(lu + 12640), b[2688], x);
@@ -1484,6 +1923,32 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 93536);
       CHEM_PREFETCH(ws + 93568);
       CHEM_PREFETCH(ws + 93600);
+      CHEM_PREFETCH_L1(ws + 91712);
+      CHEM_PREFETCH_L1(ws + 91744);
+      CHEM_PREFETCH_L1(ws + 91776);
+      CHEM_PREFETCH_L1(ws + 91808);
+      CHEM_PREFETCH_L1(ws + 91840);
+      CHEM_PREFETCH_L1(ws + 91872);
+      CHEM_PREFETCH_L1(ws + 91904);
+      CHEM_PREFETCH_L1(ws + 91936);
+      CHEM_PREFETCH_L1(ws + 91968);
+      CHEM_PREFETCH_L1(ws + 92000);
+      CHEM_PREFETCH_L1(ws + 92032);
+      CHEM_PREFETCH_L1(ws + 92064);
+      CHEM_PREFETCH_L1(ws + 92096);
+      CHEM_PREFETCH_L1(ws + 92128);
+      CHEM_PREFETCH_L1(ws + 92160);
+      CHEM_PREFETCH_L1(ws + 92192);
+      CHEM_PREFETCH_L1(ws + 92224);
+      CHEM_PREFETCH_L1(ws + 92256);
+      CHEM_PREFETCH_L1(ws + 92288);
+      CHEM_PREFETCH_L1(ws + 92320);
+      CHEM_PREFETCH_L1(ws + 92352);
+      CHEM_PREFETCH_L1(ws + 92384);
+      CHEM_PREFETCH_L1(ws + 92416);
+      CHEM_PREFETCH_L1(ws + 92448);
+      CHEM_PREFETCH_L1(ws + 92480);
+      CHEM_PREFETCH_L1(ws + 92512);
       double x = b[4480];
       x = fma(-CHEM_LDLU(lu + 13344), b[352], x);
       x = fma(-CHEM_LDLU(lu + 13376), b[1792], x);
@@ -1545,6 +2010,40 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 94624);
       CHEM_PREFETCH(ws + 94656);
       CHEM_PREFETCH(ws + 94688);
+      CHEM_PREFETCH_L1(ws + 92544);
+      CHEM_PREFETCH_L1(ws + 92576);
+      CHEM_PREFETCH_L1(ws + 92608);
+      CHEM_PREFETCH_L1(ws + 92640);
+      CHEM_PREFETCH_L1(ws + 92672);
+      CHEM_PREFETCH_L1(ws + 92704);
+      CHEM_PREFETCH_L1(ws + 92736);
+      CHEM_PREFETCH_L1(ws + 92768);
+      CHEM_PREFETCH_L1(ws + 92800);
+      CHEM_PREFETCH_L1(ws + 92832);
+      CHEM_PREFETCH_L1(ws + 92864);
+      CHEM_PREFETCH_L1(ws + 92896);
+      CHEM_PREFETCH_L1(ws + 92928);
+      CHEM_PREFETCH_L1(ws + 92960);
+      CHEM_PREFETCH_L1(ws + 92992);
+      CHEM_PREFETCH_L1(ws + 93024);
+      CHEM_PREFETCH_L1(ws + 93056);
+      CHEM_PREFETCH_L1(ws + 93088);
+      CHEM_PREFETCH_L1(ws + 93120);
+      CHEM_PREFETCH_L1(ws + 93152);
+      CHEM_PREFETCH_L1(ws + 93184);
+      CHEM_PREFETCH_L1(ws + 93216);
+      CHEM_PREFETCH_L1(ws + 93248);
+      CHEM_PREFETCH_L1(ws + 93280);
+      CHEM_PREFETCH_L1(ws + 93312);
+      CHEM_PREFETCH_L1(ws + 93344);
+      CHEM_PREFETCH_L1(ws + 93376);
+      CHEM_PREFETCH_L1(ws + 93408);
+      CHEM_PREFETCH_L1(ws + 93440);
+      CHEM_PREFETCH_L1(ws + 93472);
+      CHEM_PREFETCH_L1(ws + 93504);
+      CHEM_PREFETCH_L1(ws + 93536);
+      CHEM_PREFETCH_L1(ws + 93568);
+      CHEM_PREFETCH_L1(ws + 93600);
       double x = b[4512];
       x = fma(-CHEM_LDLU(lu + 14080), b[864], x);
       x = fma(-CHEM_LDLU(lu + 14112), b[1632], x);
@@ -1614,6 +2113,40 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 95872);
       CHEM_PREFETCH(ws + 95904);
       CHEM_PREFETCH(ws + 95936);
+      CHEM_PREFETCH_L1(ws + 93632);
+      CHEM_PREFETCH_L1(ws + 93664);
+      CHEM_PREFETCH_L1(ws + 93696);
+      CHEM_PREFETCH_L1(ws + 93728);
+      CHEM_PREFETCH_L1(ws + 93760);
+      CHEM_PREFETCH_L1(ws + 93792);
+      CHEM_PREFETCH_L1(ws + 93824);
+      CHEM_PREFETCH_L1(ws + 93856);
+      CHEM_PREFETCH_L1(ws + 93888);
+      CHEM_PREFETCH_L1(ws + 93920);
+      CHEM_PREFETCH_L1(ws + 93952);
+      CHEM_PREFETCH_L1(ws + 93984);
+      CHEM_PREFETCH_L1(ws + 94016);
+      CHEM_PREFETCH_L1(ws + 94048);
+      CHEM_PREFETCH_L1(ws + 94080);
+      CHEM_PREFETCH_L1(ws + 94112);
+      CHEM_PREFETCH_L1(ws + 94144);
+      CHEM_PREFETCH_L1(ws + 94176);
+      CHEM_PREFETCH_L1(ws + 94208);
+      CHEM_PREFETCH_L1(ws + 94240);
+      CHEM_PREFETCH_L1(ws + 94272);
+      CHEM_PREFETCH_L1(ws + 94304);
+      CHEM_PREFETCH_L1(ws + 94336);
+      CHEM_PREFETCH_L1(ws + 94368);
+      CHEM_PREFETCH_L1(ws + 94400);
+      CHEM_PREFETCH_L1(ws + 94432);
+      CHEM_PREFETCH_L1(ws + 94464);
+      CHEM_PREFETCH_L1(ws + 94496);
+      CHEM_PREFETCH_L1(ws + 94528);
+      CHEM_PREFETCH_L1(ws + 94560);
+      CHEM_PREFETCH_L1(ws + 94592);
+      CHEM_PREFETCH_L1(ws + 94624);
+      CHEM_PREFETCH_L1(ws + 94656);
+      CHEM_PREFETCH_L1(ws + 94688);
       double x = b[4544];
       x = fma(-CHEM_LDLU(lu + 14912), b[832], x);
       x = fma(-CHEM_LDLU(lu + 14944), b[864], x);
@@ -1695,6 +2228,45 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 97248);
       CHEM_PREFETCH(ws + 97280);
       CHEM_PREFETCH(ws + 97312);
+      CHEM_PREFETCH_L1(ws + 94720);
+      CHEM_PREFETCH_L1(ws + 94752);
+      CHEM_PREFETCH_L1(ws + 94784);
+      CHEM_PREFETCH_L1(ws + 94816);
+      CHEM_PREFETCH_L1(ws + 94848);
+      CHEM_PREFETCH_L1(ws + 94880);
+      CHEM_PREFETCH_L1(ws + 94912);
+      CHEM_PREFETCH_L1(ws + 94944);
+      CHEM_PREFETCH_L1(ws + 94976);
+      CHEM_PREFETCH_L1(ws + 95008);
+      CHEM_PREFETCH_L1(ws + 95040);
+      CHEM_PREFETCH_L1(ws + 95072);
+      CHEM_PREFETCH_L1(ws + 95104);
+      CHEM_PREFETCH_L1(ws + 95136);
+      CHEM_PREFETCH_L1(ws + 95168);
+      CHEM_PREFETCH_L1(ws + 95200);
+      CHEM_PREFETCH_L1(ws + 95232);
+      CHEM_PREFETCH_L1(ws + 95264);
+      CHEM_PREFETCH_L1(ws + 95296);
+      CHEM_PREFETCH_L1(ws + 95328);
+      CHEM_PREFETCH_L1(ws + 95360);
+      CHEM_PREFETCH_L1(ws + 95392);
+      CHEM_PREFETCH_L1(ws + 95424);
+      CHEM_PREFETCH_L1(ws + 95456);
+      CHEM_PREFETCH_L1(ws + 95488);
+      CHEM_PREFETCH_L1(ws + 95520);
+      CHEM_PREFETCH_L1(ws + 95552);
+      CHEM_PREFETCH_L1(ws + 95584);
+      CHEM_PREFETCH_L1(ws + 95616);
+      CHEM_PREFETCH_L1(ws + 95648);
+      CHEM_PREFETCH_L1(ws + 95680);
+      CHEM_PREFETCH_L1(ws + 95712);
+      CHEM_PREFETCH_L1(ws + 95744);
+      CHEM_PREFETCH_L1(ws + 95776);
+      CHEM_PREFETCH_L1(ws + 95808);
+      CHEM_PREFETCH_L1(ws + 95840);
+      CHEM_PREFETCH_L1(ws + 95872);
+      CHEM_PREFETCH_L1(ws + 95904);
+      CHEM_PREFETCH_L1(ws + 95936);
       double x = b[4576];
       x = fma(-CHEM_LDLU(lu + 16000), b[832], x);
       x = fma(-CHEM_LDLU(lu + 16032), b[864], x);
@@ -1784,6 +2356,49 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 98880);
       CHEM_PREFETCH(ws + 98912);
       CHEM_PREFETCH(ws + 98944);
+      CHEM_PREFETCH_L1(ws + 95968);
+      CHEM_PREFETCH_L1(ws + 96000);
+      CHEM_PREFETCH_L1(ws + 96032);
+      CHEM_PREFETCH_L1(ws + 96064);
+      CHEM_PREFETCH_L1(ws + 96096);
+      CHEM_PREFETCH_L1(ws + 96128);
+      CHEM_PREFETCH_L1(ws + 96160);
+      CHEM_PREFETCH_L1(ws + 96192);
+      CHEM_PREFETCH_L1(ws + 96224);
+      CHEM_PREFETCH_L1(ws + 96256);
+      CHEM_PREFETCH_L1(ws + 96288);
+      CHEM_PREFETCH_L1(ws + 96320);
+      CHEM_PREFETCH_L1(ws + 96352);
+      CHEM_PREFETCH_L1(ws + 96384);
+      CHEM_PREFETCH_L1(ws + 96416);
+      CHEM_PREFETCH_L1(ws + 96448);
+      CHEM_PREFETCH_L1(ws + 96480);
+      CHEM_PREFETCH_L1(ws + 96512);
+      CHEM_PREFETCH_L1(ws + 96544);
+      CHEM_PREFETCH_L1(ws + 96576);
+      CHEM_PREFETCH_L1(ws + 96608);
+      CHEM_PREFETCH_L1(ws + 96640);
+      CHEM_PREFETCH_L1(ws + 96672);
+      CHEM_PREFETCH_L1(ws + 96704);
+      CHEM_PREFETCH_L1(ws + 96736);
+      CHEM_PREFETCH_L1(ws + 96768);
+      CHEM_PREFETCH_L1(ws + 96800);
+      CHEM_PREFETCH_L1(ws + 96832);
+      CHEM_PREFETCH_L1(ws + 96864);
+      CHEM_PREFETCH_L1(ws + 96896);
+      CHEM_PREFETCH_L1(ws + 96928);
+      CHEM_PREFETCH_L1(ws + 96960);
+      CHEM_PREFETCH_L1(ws + 96992);
+      CHEM_PREFETCH_L1(ws + 97024);
+      CHEM_PREFETCH_L1(ws + 97056);
+      CHEM_PREFETCH_L1(ws + 97088);
+      CHEM_PREFETCH_L1(ws + 97120);
+      CHEM_PREFETCH_L1(ws + 97152);
+      CHEM_PREFETCH_L1(ws + 97184);
+      CHEM_PREFETCH_L1(ws + 97216);
+      CHEM_PREFETCH_L1(ws + 97248);
+      CHEM_PREFETCH_L1(ws + 97280);
+      CHEM_PREFETCH_L1(ws + 97312);
       double x = b[4608];
       x = fma(-CHEM_LDLU(lu + 17088), b[960], x);
       x = fma(-CHEM_LDLU(lu + 17120), b[1280], x);
@@ -1880,6 +2495,57 @@ __device__ __noinline__ void solve_1_0(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 100576);
       CHEM_PREFETCH(ws + 100608);
       CHEM_PREFETCH(ws + 100640);
+      CHEM_PREFETCH_L1(ws + 97344);
+      CHEM_PREFETCH_L1(ws + 97376);
+      CHEM_PREFETCH_L1(ws + 97408);
+      CHEM_PREFETCH_L1(ws + 97440);
+      CHEM_PREFETCH_L1(ws + 97472);
+      CHEM_PREFETCH_L1(ws + 97504);
+      CHEM_PREFETCH_L1(ws + 97536);
+      CHEM_PREFETCH_L1(ws + 97568);
+      CHEM_PREFETCH_L1(ws + 97600);
+      CHEM_PREFETCH_L1(ws + 97632);
+      CHEM_PREFETCH_L1(ws + 97664);
+      CHEM_PREFETCH_L1(ws + 97696);
+      CHEM_PREFETCH_L1(ws + 97728);
+      CHEM_PREFETCH_L1(ws + 97760);
+      CHEM_PREFETCH_L1(ws + 97792);
+      CHEM_PREFETCH_L1(ws + 97824);
+      CHEM_PREFETCH_L1(ws + 97856);
+      CHEM_PREFETCH_L1(ws + 97888);
+      CHEM_PREFETCH_L1(ws + 97920);
+      CHEM_PREFETCH_L1(ws + 97952);
+      CHEM_PREFETCH_L1(ws + 97984);
+      CHEM_PREFETCH_L1(ws + 98016);
+      CHEM_PREFETCH_L1(ws + 98048);
+      CHEM_PREFETCH_L1(ws + 98080);
+      CHEM_PREFETCH_L1(ws + 98112);
+      CHEM_PREFETCH_L1(ws + 98144);
+      CHEM_PREFETCH_L1(ws + 98176);
+      CHEM_PREFETCH_L1(ws + 98208);
+      CHEM_PREFETCH_L1(ws + 98240);
+      CHEM_PREFETCH_L1(ws + 98272);
+      CHEM_PREFETCH_L1(ws + 98304);
+      CHEM_PREFETCH_L1(ws + 98336);
+      CHEM_PREFETCH_L1(ws + 98368);
+      CHEM_PREFETCH_L1(ws + 98400);
+      CHEM_PREFETCH_L1(ws + 98432);
+      CHEM_PREFETCH_L1(ws + 98464);
+      CHEM_PREFETCH_L1(ws + 98496);
+      CHEM_PREFETCH_L1(ws + 98528);
+      CHEM_PREFETCH_L1(ws + 98560);
+      CHEM_PREFETCH_L1(ws + 98592);
+      CHEM_PREFETCH_L1(ws + 98624);
+      CHEM_PREFETCH_L1(ws + 98656);
+      CHEM_PREFETCH_L1(ws + 98688);
+      CHEM_PREFETCH_L1(ws + 98720);
+      CHEM_PREFETCH_L1(ws + 98752);
+      CHEM_PREFETCH_L1(ws + 98784);
+      CHEM_PREFETCH_L1(ws + 98816);
+      CHEM_PREFETCH_L1(ws + 98848);
+      CHEM_PREFETCH_L1(ws + 98880);
+      CHEM_PREFETCH_L1(ws + 98912);
+      CHEM_PREFETCH_L1(ws + 98944);
       double x = b[4640];
       x = fma(-CHEM_LDLU(lu + 18336), b[1024], x);
       x = fma(-CHEM_LDLU(lu + 18368), b[1280], x);
@@ -2030,6 +2696,59 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 103648);
       CHEM_PREFETCH(ws + 103680);
       CHEM_PREFETCH(ws + 103712);
+      CHEM_PREFETCH_L1(ws + 98976);
+      CHEM_PREFETCH_L1(ws + 99008);
+      CHEM_PREFETCH_L1(ws + 99040);
+      CHEM_PREFETCH_L1(ws + 99072);
+      CHEM_PREFETCH_L1(ws + 99104);
+      CHEM_PREFETCH_L1(ws + 99136);
+      CHEM_PREFETCH_L1(ws + 99168);
+      CHEM_PREFETCH_L1(ws + 99200);
+      CHEM_PREFETCH_L1(ws + 99232);
+      CHEM_PREFETCH_L1(ws + 99264);
+      CHEM_PREFETCH_L1(ws + 99296);
+      CHEM_PREFETCH_L1(ws + 99328);
+      CHEM_PREFETCH_L1(ws + 99360);
+      CHEM_PREFETCH_L1(ws + 99392);
+      CHEM_PREFETCH_L1(ws + 99424);
+      CHEM_PREFETCH_L1(ws + 99456);
+      CHEM_PREFETCH_L1(ws + 99488);
+      CHEM_PREFETCH_L1(ws + 99520);
+      CHEM_PREFETCH_L1(ws + 99552);
+      CHEM_PREFETCH_L1(ws + 99584);
+      CHEM_PREFETCH_L1(ws + 99616);
+      CHEM_PREFETCH_L1(ws + 99648);
+      CHEM_PREFETCH_L1(ws + 99680);
+      CHEM_PREFETCH_L1(ws + 99712);
+      CHEM_PREFETCH_L1(ws + 99744);
+      CHEM_PREFETCH_L1(ws + 99776);
+      CHEM_PREFETCH_L1(ws + 99808);
+      CHEM_PREFETCH_L1(ws + 99840);
+      CHEM_PREFETCH_L1(ws + 99872);
+      CHEM_PREFETCH_L1(ws + 99904);
+      CHEM_PREFETCH_L1(ws + 99936);
+      CHEM_PREFETCH_L1(ws + 99968);
+      CHEM_PREFETCH_L1(ws + 100000);
+      CHEM_PREFETCH_L1(ws + 100032);
+      CHEM_PREFETCH_L1(ws + 100064);
+      CHEM_PREFETCH_L1(ws + 100096);
+      CHEM_PREFETCH_L1(ws + 100128);
+      CHEM_PREFETCH_L1(ws + 100160);
+      CHEM_PREFETCH_L1(ws + 100192);
+      CHEM_PREFETCH_L1(ws + 100224);
+      CHEM_PREFETCH_L1(ws + 100256);
+      CHEM_PREFETCH_L1(ws + 100288);
+      CHEM_PREFETCH_L1(ws + 100320);
+      CHEM_PREFETCH_L1(ws + 100352);
+      CHEM_PREFETCH_L1(ws + 100384);
+      CHEM_PREFETCH_L1(ws + 100416);
+      CHEM_PREFETCH_L1(ws + 100448);
+      CHEM_PREFETCH_L1(ws + 100480);
+      CHEM_PREFETCH_L1(ws + 100512);
+      CHEM_PREFETCH_L1(ws + 100544);
+      CHEM_PREFETCH_L1(ws + 100576);
+      CHEM_PREFETCH_L1(ws + 100608);
+      CHEM_PREFETCH_L1(ws + 100640);
       double x = b[4672];
       x = fma(-CHEM_LDLU(lu + 19712), b[384], x);
       x = fma(-CHEM_LDLU(lu + 19744), b[416], x);
@@ -2086,6 +2805,102 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
     }
     {
       CHEM_PREFETCH(ws + 136448);
+      CHEM_PREFETCH_L1(ws + 100672);
+      CHEM_PREFETCH_L1(ws + 100704);
+      CHEM_PREFETCH_L1(ws + 100736);
+      CHEM_PREFETCH_L1(ws + 100768);
+      CHEM_PREFETCH_L1(ws + 100800);
+      CHEM_PREFETCH_L1(ws + 100832);
+      CHEM_PREFETCH_L1(ws + 100864);
+      CHEM_PREFETCH_L1(ws + 100896);
+      CHEM_PREFETCH_L1(ws + 100928);
+      CHEM_PREFETCH_L1(ws + 100960);
+      CHEM_PREFETCH_L1(ws + 100992);
+      CHEM_PREFETCH_L1(ws + 101024);
+      CHEM_PREFETCH_L1(ws + 101056);
+      CHEM_PREFETCH_L1(ws + 101088);
+      CHEM_PREFETCH_L1(ws + 101120);
+      CHEM_PREFETCH_L1(ws + 101152);
+      CHEM_PREFETCH_L1(ws + 101184);
+      CHEM_PREFETCH_L1(ws + 101216);
+      CHEM_PREFETCH_L1(ws + 101248);
+      CHEM_PREFETCH_L1(ws + 101280);
+      CHEM_PREFETCH_L1(ws + 101312);
+      CHEM_PREFETCH_L1(ws + 101344);
+      CHEM_PREFETCH_L1(ws + 101376);
+      CHEM_PREFETCH_L1(ws + 101408);
+      CHEM_PREFETCH_L1(ws + 101440);
+      CHEM_PREFETCH_L1(ws + 101472);
+      CHEM_PREFETCH_L1(ws + 101504);
+      CHEM_PREFETCH_L1(ws + 101536);
+      CHEM_PREFETCH_L1(ws + 101568);
+      CHEM_PREFETCH_L1(ws + 101600);
+      CHEM_PREFETCH_L1(ws + 101632);
+      CHEM_PREFETCH_L1(ws + 101664);
+      CHEM_PREFETCH_L1(ws + 101696);
+      CHEM_PREFETCH_L1(ws + 101728);
+      CHEM_PREFETCH_L1(ws + 101760);
+      CHEM_PREFETCH_L1(ws + 101792);
+      CHEM_PREFETCH_L1(ws + 101824);
+      CHEM_PREFETCH_L1(ws + 101856);
+      CHEM_PREFETCH_L1(ws + 101888);
+      CHEM_PREFETCH_L1(ws + 101920);
+      CHEM_PREFETCH_L1(ws + 101952);
+      CHEM_PREFETCH_L1(ws + 101984);
+      CHEM_PREFETCH_L1(ws + 102016);
+      CHEM_PREFETCH_L1(ws + 102048);
+      CHEM_PREFETCH_L1(ws + 102080);
+      CHEM_PREFETCH_L1(ws + 102112);
+      CHEM_PREFETCH_L1(ws + 102144);
+      CHEM_PREFETCH_L1(ws + 102176);
+      CHEM_PREFETCH_L1(ws + 102208);
+      CHEM_PREFETCH_L1(ws + 102240);
+      CHEM_PREFETCH_L1(ws + 102272);
+      CHEM_PREFETCH_L1(ws + 102304);
+      CHEM_PREFETCH_L1(ws + 102336);
+      CHEM_PREFETCH_L1(ws + 102368);
+      CHEM_PREFETCH_L1(ws + 102400);
+      CHEM_PREFETCH_L1(ws + 102432);
+      CHEM_PREFETCH_L1(ws + 102464);
+      CHEM_PREFETCH_L1(ws + 102496);
+      CHEM_PREFETCH_L1(ws + 102528);
+      CHEM_PREFETCH_L1(ws + 102560);
+      CHEM_PREFETCH_L1(ws + 102592);
+      CHEM_PREFETCH_L1(ws + 102624);
+      CHEM_PREFETCH_L1(ws + 102656);
+      CHEM_PREFETCH_L1(ws + 102688);
+      CHEM_PREFETCH_L1(ws + 102720);
+      CHEM_PREFETCH_L1(ws + 102752);
+      CHEM_PREFETCH_L1(ws + 102784);
+      CHEM_PREFETCH_L1(ws + 102816);
+      CHEM_PREFETCH_L1(ws + 102848);
+      CHEM_PREFETCH_L1(ws + 102880);
+      CHEM_PREFETCH_L1(ws + 102912);
+      CHEM_PREFETCH_L1(ws + 102944);
+      CHEM_PREFETCH_L1(ws + 102976);
+      CHEM_PREFETCH_L1(ws + 103008);
+      CHEM_PREFETCH_L1(ws + 103040);
+      CHEM_PREFETCH_L1(ws + 103072);
+      CHEM_PREFETCH_L1(ws + 103104);
+      CHEM_PREFETCH_L1(ws + 103136);
+      CHEM_PREFETCH_L1(ws + 103168);
+      CHEM_PREFETCH_L1(ws + 103200);
+      CHEM_PREFETCH_L1(ws + 103232);
+      CHEM_PREFETCH_L1(ws + 103264);
+      CHEM_PREFETCH_L1(ws + 103296);
+      CHEM_PREFETCH_L1(ws + 103328);
+      CHEM_PREFETCH_L1(ws + 103360);
+      CHEM_PREFETCH_L1(ws + 103392);
+      CHEM_PREFETCH_L1(ws + 103424);
+      CHEM_PREFETCH_L1(ws + 103456);
+      CHEM_PREFETCH_L1(ws + 103488);
+      CHEM_PREFETCH_L1(ws + 103520);
+      CHEM_PREFETCH_L1(ws + 103552);
+      CHEM_PREFETCH_L1(ws + 103584);
+      CHEM_PREFETCH_L1(ws + 103616);
+      CHEM_PREFETCH_L1(ws + 103648);
+      CHEM_PREFETCH_L1(ws + 103680);
+      CHEM_PREFETCH_L1(ws + 103712);
       double x = b[4704];
       x = fma(-CHEM_LDLU(lu + 21344), b[352], x);
       x = fma(-CHEM_LDLU(lu + 21376), b[384], x);
@@ -2145,6 +2960,7 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
     {
       CHEM_PREFETCH(ws + 103744);
       CHEM_PREFETCH(ws + 136416);
+      CHEM_PREFETCH_L1(ws + 136448);
       double x = b[4736];
       x = fma(-CHEM_LDLU(lu + 23040), b[352], x);
       x = fma(-CHEM_LDLU(lu + 23072), b[384], x);
@@ -2248,6 +3064,8 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 103776);
       CHEM_PREFETCH(ws + 103808);
       CHEM_PREFETCH(ws + 136384);
+      CHEM_PREFETCH_L1(ws + 103744);
+      CHEM_PREFETCH_L1(ws + 136416);
       double x = b[4736];
       b[4736] = x * CHEM_LDLU(vd + 4736);
     }
@@ -2256,6 +3074,9 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 103872);
       CHEM_PREFETCH(ws + 103904);
       CHEM_PREFETCH(ws + 136352);
+      CHEM_PREFETCH_L1(ws + 103776);
+      CHEM_PREFETCH_L1(ws + 103808);
+      CHEM_PREFETCH_L1(ws + 136384);
       double x = b[4704];
       x = fma(-CHEM_LDLU(lu + 26112), b[4736], x);
       b[4704] = x * CHEM_LDLU(vd + 4704);
@@ -2266,6 +3087,10 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 104000);
       CHEM_PREFETCH(ws + 104032);
       CHEM_PREFETCH(ws + 136320);
+      CHEM_PREFETCH_L1(ws + 103840);
+      CHEM_PREFETCH_L1(ws + 103872);
+      CHEM_PREFETCH_L1(ws + 103904);
+      CHEM_PREFETCH_L1(ws + 136352);
       double x = b[4672];
       x = fma(-CHEM_LDLU(lu + 26144), b[4704], x);
       x = fma(-CHEM_LDLU(lu + 26176), b[4736], x);
@@ -2278,6 +3103,11 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 104160);
       CHEM_PREFETCH(ws + 104192);
       CHEM_PREFETCH(ws + 136288);
+      CHEM_PREFETCH_L1(ws + 103936);
+      CHEM_PREFETCH_L1(ws + 103968);
+      CHEM_PREFETCH_L1(ws + 104000);
+      CHEM_PREFETCH_L1(ws + 104032);
+      CHEM_PREFETCH_L1(ws + 136320);
       double x = b[4640];
       x = fma(-CHEM_LDLU(lu + 26208), b[4672], x);
       x = fma(-CHEM_LDLU(lu + 26240), b[4704], x);
@@ -2292,6 +3122,12 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 104352);
       CHEM_PREFETCH(ws + 104384);
       CHEM_PREFETCH(ws + 136256);
+      CHEM_PREFETCH_L1(ws + 104064);
+      CHEM_PREFETCH_L1(ws + 104096);
+      CHEM_PREFETCH_L1(ws + 104128);
+      CHEM_PREFETCH_L1(ws + 104160);
+      CHEM_PREFETCH_L1(ws + 104192);
+      CHEM_PREFETCH_L1(ws + 136288);
       double x = b[4608];
       x = fma(-CHEM_LDLU(lu + 26304), b[4640], x);
       x = fma(-CHEM_LDLU(lu + 26336), b[4672], x);
@@ -2308,6 +3144,13 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 104576);
       CHEM_PREFETCH(ws + 104608);
       CHEM_PREFETCH(ws + 136224);
+      CHEM_PREFETCH_L1(ws + 104224);
+      CHEM_PREFETCH_L1(ws + 104256);
+      CHEM_PREFETCH_L1(ws + 104288);
+      CHEM_PREFETCH_L1(ws + 104320);
+      CHEM_PREFETCH_L1(ws + 104352);
+      CHEM_PREFETCH_L1(ws + 104384);
+      CHEM_PREFETCH_L1(ws + 136256);
       double x = b[4576];
       x = fma(-CHEM_LDLU(lu + 26432), b[4608], x);
       x = fma(-CHEM_LDLU(lu + 26464), b[4640], x);
@@ -2326,6 +3169,14 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 104832);
       CHEM_PREFETCH(ws + 104864);
       CHEM_PREFETCH(ws + 136192);
+      CHEM_PREFETCH_L1(ws + 104416);
+      CHEM_PREFETCH_L1(ws + 104448);
+      CHEM_PREFETCH_L1(ws + 104480);
+      CHEM_PREFETCH_L1(ws + 104512);
+      CHEM_PREFETCH_L1(ws + 104544);
+      CHEM_PREFETCH_L1(ws + 104576);
+      CHEM_PREFETCH_L1(ws + 104608);
+      CHEM_PREFETCH_L1(ws + 136224);
       double x = b[4544];
       x = fma(-CHEM_LDLU(lu + 26592), b[4576], x);
       x = fma(-CHEM_LDLU(lu + 26624), b[4608], x);
@@ -2345,6 +3196,15 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 105088);
       CHEM_PREFETCH(ws + 105120);
       CHEM_PREFETCH(ws + 136160);
+      CHEM_PREFETCH_L1(ws + 104640);
+      CHEM_PREFETCH_L1(ws + 104672);
+      CHEM_PREFETCH_L1(ws + 104704);
+      CHEM_PREFETCH_L1(ws + 104736);
+      CHEM_PREFETCH_L1(ws + 104768);
+      CHEM_PREFETCH_L1(ws + 104800);
+      CHEM_PREFETCH_L1(ws + 104832);
+      CHEM_PREFETCH_L1(ws + 104864);
+      CHEM_PREFETCH_L1(ws + 136192);
       double x = b[4512];
       x = fma(-CHEM_LDLU(lu + 26784), b[4544], x);
       x = fma(-CHEM_LDLU(lu + 26816), b[4576], x);
@@ -2366,6 +3226,15 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 105376);
       CHEM_PREFETCH(ws + 105408);
       CHEM_PREFETCH(ws + 136128);
+      CHEM_PREFETCH_L1(ws + 104896);
+      CHEM_PREFETCH_L1(ws + 104928);
+      CHEM_PREFETCH_L1(ws + 104960);
+      CHEM_PREFETCH_L1(ws + 104992);
+      CHEM_PREFETCH_L1(ws + 105024);
+      CHEM_PREFETCH_L1(ws + 105056);
+      CHEM_PREFETCH_L1(ws + 105088);
+      CHEM_PREFETCH_L1(ws + 105120);
+      CHEM_PREFETCH_L1(ws + 136160);
       double x = b[4480];
       x = fma(-CHEM_LDLU(lu + 27008), b[4512], x);
       x = fma(-CHEM_LDLU(lu + 27040), b[4544], x);
@@ -2389,6 +3258,16 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 105696);
       CHEM_PREFETCH(ws + 105728);
       CHEM_PREFETCH(ws + 136096);
+      CHEM_PREFETCH_L1(ws + 105152);
+      CHEM_PREFETCH_L1(ws + 105184);
+      CHEM_PREFETCH_L1(ws + 105216);
+      CHEM_PREFETCH_L1(ws + 105248);
+      CHEM_PREFETCH_L1(ws + 105280);
+      CHEM_PREFETCH_L1(ws + 105312);
+      CHEM_PREFETCH_L1(ws + 105344);
+      CHEM_PREFETCH_L1(ws + 105376);
+      CHEM_PREFETCH_L1(ws + 105408);
+      CHEM_PREFETCH_L1(ws + 136128);
       double x = b[4448];
       x = fma(-CHEM_LDLU(lu + 27264), b[4512], x);
       x = fma(-CHEM_LDLU(lu + 27296), b[4544], x);
@@ -2412,6 +3291,17 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 106016);
       CHEM_PREFETCH(ws + 106048);
       CHEM_PREFETCH(ws + 136064);
+      CHEM_PREFETCH_L1(ws + 105440);
+      CHEM_PREFETCH_L1(ws + 105472);
+      CHEM_PREFETCH_L1(ws + 105504);
+      CHEM_PREFETCH_L1(ws + 105536);
+      CHEM_PREFETCH_L1(ws + 105568);
+      CHEM_PREFETCH_L1(ws + 105600);
+      CHEM_PREFETCH_L1(ws + 105632);
+      CHEM_PREFETCH_L1(ws + 105664);
+      CHEM_PREFETCH_L1(ws + 105696);
+      CHEM_PREFETCH_L1(ws + 105728);
+      CHEM_PREFETCH_L1(ws + 136096);
       double x = b[4416];
       x = fma(-CHEM_LDLU(lu + 27520), b[4448], x);
       x = fma(-CHEM_LDLU(lu + 27552), b[4512], x);
@@ -2436,6 +3326,17 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 106336);
       CHEM_PREFETCH(ws + 106368);
       CHEM_PREFETCH(ws + 136032);
+      CHEM_PREFETCH_L1(ws + 105760);
+      CHEM_PREFETCH_L1(ws + 105792);
+      CHEM_PREFETCH_L1(ws + 105824);
+      CHEM_PREFETCH_L1(ws + 105856);
+      CHEM_PREFETCH_L1(ws + 105888);
+      CHEM_PREFETCH_L1(ws + 105920);
+      CHEM_PREFETCH_L1(ws + 105952);
+      CHEM_PREFETCH_L1(ws + 105984);
+      CHEM_PREFETCH_L1(ws + 106016);
+      CHEM_PREFETCH_L1(ws + 106048);
+      CHEM_PREFETCH_L1(ws + 136064);
       double x = b[4384];
       x = fma(-CHEM_LDLU(lu + 27808), b[4416], x);
       x = fma(-CHEM_LDLU(lu + 27840), b[4448], x);
@@ -2464,6 +3365,17 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 106752);
       CHEM_PREFETCH(ws + 106784);
       CHEM_PREFETCH(ws + 136000);
+      CHEM_PREFETCH_L1(ws + 106080);
+      CHEM_PREFETCH_L1(ws + 106112);
+      CHEM_PREFETCH_L1(ws + 106144);
+      CHEM_PREFETCH_L1(ws + 106176);
+      CHEM_PREFETCH_L1(ws + 106208);
+      CHEM_PREFETCH_L1(ws + 106240);
+      CHEM_PREFETCH_L1(ws + 106272);
+      CHEM_PREFETCH_L1(ws + 106304);
+      CHEM_PREFETCH_L1(ws + 106336);
+      CHEM_PREFETCH_L1(ws + 106368);
+      CHEM_PREFETCH_L1(ws + 136032);
       double x = b[4352];
       x = fma(-CHEM_LDLU(lu + 28128), b[4384], x);
       x = fma(-CHEM_LDLU(lu + 28160), b[4416], x);
@@ -2490,6 +3402,20 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 107104);
       CHEM_PREFETCH(ws + 107136);
       CHEM_PREFETCH(ws + 135968);
+      CHEM_PREFETCH_L1(ws + 106400);
+      CHEM_PREFETCH_L1(ws + 106432);
+      CHEM_PREFETCH_L1(ws + 106464);
+      CHEM_PREFETCH_L1(ws + 106496);
+      CHEM_PREFETCH_L1(ws + 106528);
+      CHEM_PREFETCH_L1(ws + 106560);
+      CHEM_PREFETCH_L1(ws + 106592);
+      CHEM_PREFETCH_L1(ws + 106624);
+      CHEM_PREFETCH_L1(ws + 106656);
+      CHEM_PREFETCH_L1(ws + 106688);
+      CHEM_PREFETCH_L1(ws + 106720);
+      CHEM_PREFETCH_L1(ws + 106752);
+      CHEM_PREFETCH_L1(ws + 106784);
+      CHEM_PREFETCH_L1(ws + 136000);
       double x = b[4320];
       x = fma(-CHEM_LDLU(lu + 28448), b[4384], x);
       x = fma(-CHEM_LDLU(lu + 28480), b[4416], x);
@@ -2516,6 +3442,18 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 107456);
       CHEM_PREFETCH(ws + 107488);
       CHEM_PREFETCH(ws + 135936);
+      CHEM_PREFETCH_L1(ws + 106816);
+      CHEM_PREFETCH_L1(ws + 106848);
+      CHEM_PREFETCH_L1(ws + 106880);
+      CHEM_PREFETCH_L1(ws + 106912);
+      CHEM_PREFETCH_L1(ws + 106944);
+      CHEM_PREFETCH_L1(ws + 106976);
+      CHEM_PREFETCH_L1(ws + 107008);
+      CHEM_PREFETCH_L1(ws + 107040);
+      CHEM_PREFETCH_L1(ws + 107072);
+      CHEM_PREFETCH_L1(ws + 107104);
+      CHEM_PREFETCH_L1(ws + 107136);
+      CHEM_PREFETCH_L1(ws + 135968);
       double x = b[4288];
       x = fma(-CHEM_LDLU(lu + 28768), b[4320], x);
       x = fma(-CHEM_LDLU(lu + 28800), b[4352], x);
@@ -2548,6 +3486,18 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 107904);
       CHEM_PREFETCH(ws + 107936);
       CHEM_PREFETCH(ws + 135904);
+      CHEM_PREFETCH_L1(ws + 107168);
+      CHEM_PREFETCH_L1(ws + 107200);
+      CHEM_PREFETCH_L1(ws + 107232);
+      CHEM_PREFETCH_L1(ws + 107264);
+      CHEM_PREFETCH_L1(ws + 107296);
+      CHEM_PREFETCH_L1(ws + 107328);
+      CHEM_PREFETCH_L1(ws + 107360);
+      CHEM_PREFETCH_L1(ws + 107392);
+      CHEM_PREFETCH_L1(ws + 107424);
+      CHEM_PREFETCH_L1(ws + 107456);
+      CHEM_PREFETCH_L1(ws + 107488);
+      CHEM_PREFETCH_L1(ws + 135936);
       double x = b[4256];
       x = fma(-CHEM_LDLU(lu + 29184), b[4320], x);
       x = fma(-CHEM_LDLU(lu + 29216), b[4384], x);
@@ -2576,6 +3526,21 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 108288);
       CHEM_PREFETCH(ws + 108320);
       CHEM_PREFETCH(ws + 135872);
+      CHEM_PREFETCH_L1(ws + 107520);
+      CHEM_PREFETCH_L1(ws + 107552);
+      CHEM_PREFETCH_L1(ws + 107584);
+      CHEM_PREFETCH_L1(ws + 107616);
+      CHEM_PREFETCH_L1(ws + 107648);
+      CHEM_PREFETCH_L1(ws + 107680);
+      CHEM_PREFETCH_L1(ws + 107712);
+      CHEM_PREFETCH_L1(ws + 107744);
+      CHEM_PREFETCH_L1(ws + 107776);
+      CHEM_PREFETCH_L1(ws + 107808);
+      CHEM_PREFETCH_L1(ws + 107840);
+      CHEM_PREFETCH_L1(ws + 107872);
+      CHEM_PREFETCH_L1(ws + 107904);
+      CHEM_PREFETCH_L1(ws + 107936);
+      CHEM_PREFETCH_L1(ws + 135904);
       double x = b[4224];
       x = fma(-CHEM_LDLU(lu + 29536), b[4320], x);
       x = fma(-CHEM_LDLU(lu + 29568), b[4384], x);
@@ -2603,6 +3568,19 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 108640);
       CHEM_PREFETCH(ws + 108672);
       CHEM_PREFETCH(ws + 135840);
+      CHEM_PREFETCH_L1(ws + 107968);
+      CHEM_PREFETCH_L1(ws + 108000);
+      CHEM_PREFETCH_L1(ws + 108032);
+      CHEM_PREFETCH_L1(ws + 108064);
+      CHEM_PREFETCH_L1(ws + 108096);
+      CHEM_PREFETCH_L1(ws + 108128);
+      CHEM_PREFETCH_L1(ws + 108160);
+      CHEM_PREFETCH_L1(ws + 108192);
+      CHEM_PREFETCH_L1(ws + 108224);
+      CHEM_PREFETCH_L1(ws + 108256);
+      CHEM_PREFETCH_L1(ws + 108288);
+      CHEM_PREFETCH_L1(ws + 108320);
+      CHEM_PREFETCH_L1(ws + 135872);
       double x = b[4192];
       x = fma(-CHEM_LDLU(lu + 29888), b[4224], x);
       x = fma(-CHEM_LDLU(lu + 29920), b[4256], x);
@@ -2633,6 +3611,18 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 108992);
       CHEM_PREFETCH(ws + 109024);
       CHEM_PREFETCH(ws + 135808);
+      CHEM_PREFETCH_L1(ws + 108352);
+      CHEM_PREFETCH_L1(ws + 108384);
+      CHEM_PREFETCH_L1(ws + 108416);
+      CHEM_PREFETCH_L1(ws + 108448);
+      CHEM_PREFETCH_L1(ws + 108480);
+      CHEM_PREFETCH_L1(ws + 108512);
+      CHEM_PREFETCH_L1(ws + 108544);
+      CHEM_PREFETCH_L1(ws + 108576);
+      CHEM_PREFETCH_L1(ws + 108608);
+      CHEM_PREFETCH_L1(ws + 108640);
+      CHEM_PREFETCH_L1(ws + 108672);
+      CHEM_PREFETCH_L1(ws + 135840);
       double x = b[4160];
       x = fma(-CHEM_LDLU(lu + 30336), b[4224], x);
       x = fma(-CHEM_LDLU(lu + 30368), b[4320], x);
@@ -2661,6 +3651,18 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 109344);
       CHEM_PREFETCH(ws + 109376);
       CHEM_PREFETCH(ws + 135776);
+      CHEM_PREFETCH_L1(ws + 108704);
+      CHEM_PREFETCH_L1(ws + 108736);
+      CHEM_PREFETCH_L1(ws + 108768);
+      CHEM_PREFETCH_L1(ws + 108800);
+      CHEM_PREFETCH_L1(ws + 108832);
+      CHEM_PREFETCH_L1(ws + 108864);
+      CHEM_PREFETCH_L1(ws + 108896);
+      CHEM_PREFETCH_L1(ws + 108928);
+      CHEM_PREFETCH_L1(ws + 108960);
+      CHEM_PREFETCH_L1(ws + 108992);
+      CHEM_PREFETCH_L1(ws + 109024);
+      CHEM_PREFETCH_L1(ws + 135808);
       double x = b[4128];
       x = fma(-CHEM_LDLU(lu + 30720), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 30752), b[4224], x);
@@ -2689,6 +3691,18 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 109728);
       CHEM_PREFETCH(ws + 109760);
       CHEM_PREFETCH(ws + 135744);
+      CHEM_PREFETCH_L1(ws + 109056);
+      CHEM_PREFETCH_L1(ws + 109088);
+      CHEM_PREFETCH_L1(ws + 109120);
+      CHEM_PREFETCH_L1(ws + 109152);
+      CHEM_PREFETCH_L1(ws + 109184);
+      CHEM_PREFETCH_L1(ws + 109216);
+      CHEM_PREFETCH_L1(ws + 109248);
+      CHEM_PREFETCH_L1(ws + 109280);
+      CHEM_PREFETCH_L1(ws + 109312);
+      CHEM_PREFETCH_L1(ws + 109344);
+      CHEM_PREFETCH_L1(ws + 109376);
+      CHEM_PREFETCH_L1(ws + 135776);
       double x = b[4096];
       x = fma(-CHEM_LDLU(lu + 31072), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 31104), b[4224], x);
@@ -2715,6 +3729,19 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 110048);
       CHEM_PREFETCH(ws + 110080);
       CHEM_PREFETCH(ws + 135712);
+      CHEM_PREFETCH_L1(ws + 109408);
+      CHEM_PREFETCH_L1(ws + 109440);
+      CHEM_PREFETCH_L1(ws + 109472);
+      CHEM_PREFETCH_L1(ws + 109504);
+      CHEM_PREFETCH_L1(ws + 109536);
+      CHEM_PREFETCH_L1(ws + 109568);
+      CHEM_PREFETCH_L1(ws + 109600);
+      CHEM_PREFETCH_L1(ws + 109632);
+      CHEM_PREFETCH_L1(ws + 109664);
+      CHEM_PREFETCH_L1(ws + 109696);
+      CHEM_PREFETCH_L1(ws + 109728);
+      CHEM_PREFETCH_L1(ws + 109760);
+      CHEM_PREFETCH_L1(ws + 135744);
       double x = b[4064];
       x = fma(-CHEM_LDLU(lu + 31424), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 31456), b[4224], x);
@@ -2745,6 +3772,17 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 110496);
       CHEM_PREFETCH(ws + 110528);
       CHEM_PREFETCH(ws + 135680);
+      CHEM_PREFETCH_L1(ws + 109792);
+      CHEM_PREFETCH_L1(ws + 109824);
+      CHEM_PREFETCH_L1(ws + 109856);
+      CHEM_PREFETCH_L1(ws + 109888);
+      CHEM_PREFETCH_L1(ws + 109920);
+      CHEM_PREFETCH_L1(ws + 109952);
+      CHEM_PREFETCH_L1(ws + 109984);
+      CHEM_PREFETCH_L1(ws + 110016);
+      CHEM_PREFETCH_L1(ws + 110048);
+      CHEM_PREFETCH_L1(ws + 110080);
+      CHEM_PREFETCH_L1(ws + 135712);
       double x = b[4032];
       x = fma(-CHEM_LDLU(lu + 31776), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 31808), b[4224], x);
@@ -2771,6 +3809,21 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 110784);
       CHEM_PREFETCH(ws + 110816);
       CHEM_PREFETCH(ws + 135648);
+      CHEM_PREFETCH_L1(ws + 110112);
+      CHEM_PREFETCH_L1(ws + 110144);
+      CHEM_PREFETCH_L1(ws + 110176);
+      CHEM_PREFETCH_L1(ws + 110208);
+      CHEM_PREFETCH_L1(ws + 110240);
+      CHEM_PREFETCH_L1(ws + 110272);
+      CHEM_PREFETCH_L1(ws + 110304);
+      CHEM_PREFETCH_L1(ws + 110336);
+      CHEM_PREFETCH_L1(ws + 110368);
+      CHEM_PREFETCH_L1(ws + 110400);
+      CHEM_PREFETCH_L1(ws + 110432);
+      CHEM_PREFETCH_L1(ws + 110464);
+      CHEM_PREFETCH_L1(ws + 110496);
+      CHEM_PREFETCH_L1(ws + 110528);
+      CHEM_PREFETCH_L1(ws + 135680);
       double x = b[4000];
       x = fma(-CHEM_LDLU(lu + 32160), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 32192), b[4320], x);
@@ -2802,6 +3855,16 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 111296);
       CHEM_PREFETCH(ws + 111328);
       CHEM_PREFETCH(ws + 135616);
+      CHEM_PREFETCH_L1(ws + 110560);
+      CHEM_PREFETCH_L1(ws + 110592);
+      CHEM_PREFETCH_L1(ws + 110624);
+      CHEM_PREFETCH_L1(ws + 110656);
+      CHEM_PREFETCH_L1(ws + 110688);
+      CHEM_PREFETCH_L1(ws + 110720);
+      CHEM_PREFETCH_L1(ws + 110752);
+      CHEM_PREFETCH_L1(ws + 110784);
+      CHEM_PREFETCH_L1(ws + 110816);
+      CHEM_PREFETCH_L1(ws + 135648);
       double x = b[3968];
       x = fma(-CHEM_LDLU(lu + 32480), b[4064], x);
       x = fma(-CHEM_LDLU(lu + 32512), b[4128], x);
@@ -2830,6 +3893,23 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 111584);
       CHEM_PREFETCH(ws + 111616);
       CHEM_PREFETCH(ws + 135584);
+      CHEM_PREFETCH_L1(ws + 110848);
+      CHEM_PREFETCH_L1(ws + 110880);
+      CHEM_PREFETCH_L1(ws + 110912);
+      CHEM_PREFETCH_L1(ws + 110944);
+      CHEM_PREFETCH_L1(ws + 110976);
+      CHEM_PREFETCH_L1(ws + 111008);
+      CHEM_PREFETCH_L1(ws + 111040);
+      CHEM_PREFETCH_L1(ws + 111072);
+      CHEM_PREFETCH_L1(ws + 111104);
+      CHEM_PREFETCH_L1(ws + 111136);
+      CHEM_PREFETCH_L1(ws + 111168);
+      CHEM_PREFETCH_L1(ws + 111200);
+      CHEM_PREFETCH_L1(ws + 111232);
+      CHEM_PREFETCH_L1(ws + 111264);
+      CHEM_PREFETCH_L1(ws + 111296);
+      CHEM_PREFETCH_L1(ws + 111328);
+      CHEM_PREFETCH_L1(ws + 135616);
       double x = b[3936];
       x = fma(-CHEM_LDLU(lu + 32928), b[4320], x);
       x = fma(-CHEM_LDLU(lu + 32960), b[4384], x);
@@ -2854,6 +3934,16 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 111904);
       CHEM_PREFETCH(ws + 111936);
       CHEM_PREFETCH(ws + 135552);
+      CHEM_PREFETCH_L1(ws + 111360);
+      CHEM_PREFETCH_L1(ws + 111392);
+      CHEM_PREFETCH_L1(ws + 111424);
+      CHEM_PREFETCH_L1(ws + 111456);
+      CHEM_PREFETCH_L1(ws + 111488);
+      CHEM_PREFETCH_L1(ws + 111520);
+      CHEM_PREFETCH_L1(ws + 111552);
+      CHEM_PREFETCH_L1(ws + 111584);
+      CHEM_PREFETCH_L1(ws + 111616);
+      CHEM_PREFETCH_L1(ws + 135584);
       double x = b[3904];
       x = fma(-CHEM_LDLU(lu + 33216), b[3936], x);
       x = fma(-CHEM_LDLU(lu + 33248), b[4096], x);
@@ -2883,6 +3973,17 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 112160);
       CHEM_PREFETCH(ws + 112192);
       CHEM_PREFETCH(ws + 135520);
+      CHEM_PREFETCH_L1(ws + 111648);
+      CHEM_PREFETCH_L1(ws + 111680);
+      CHEM_PREFETCH_L1(ws + 111712);
+      CHEM_PREFETCH_L1(ws + 111744);
+      CHEM_PREFETCH_L1(ws + 111776);
+      CHEM_PREFETCH_L1(ws + 111808);
+      CHEM_PREFETCH_L1(ws + 111840);
+      CHEM_PREFETCH_L1(ws + 111872);
+      CHEM_PREFETCH_L1(ws + 111904);
+      CHEM_PREFETCH_L1(ws + 111936);
+      CHEM_PREFETCH_L1(ws + 135552);
       double x = b[3872];
       x = fma(-CHEM_LDLU(lu + 33728), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 33760), b[4320], x);
@@ -2908,6 +4009,15 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 112512);
       CHEM_PREFETCH(ws + 112544);
       CHEM_PREFETCH(ws + 135488);
+      CHEM_PREFETCH_L1(ws + 111968);
+      CHEM_PREFETCH_L1(ws + 112000);
+      CHEM_PREFETCH_L1(ws + 112032);
+      CHEM_PREFETCH_L1(ws + 112064);
+      CHEM_PREFETCH_L1(ws + 112096);
+      CHEM_PREFETCH_L1(ws + 112128);
+      CHEM_PREFETCH_L1(ws + 112160);
+      CHEM_PREFETCH_L1(ws + 112192);
+      CHEM_PREFETCH_L1(ws + 135520);
       double x = b[3840];
       x = fma(-CHEM_LDLU(lu + 34016), b[3872], x);
       x = fma(-CHEM_LDLU(lu + 34048), b[4160], x);
@@ -2933,6 +4043,18 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 112832);
       CHEM_PREFETCH(ws + 112864);
       CHEM_PREFETCH(ws + 135456);
+      CHEM_PREFETCH_L1(ws + 112224);
+      CHEM_PREFETCH_L1(ws + 112256);
+      CHEM_PREFETCH_L1(ws + 112288);
+      CHEM_PREFETCH_L1(ws + 112320);
+      CHEM_PREFETCH_L1(ws + 112352);
+      CHEM_PREFETCH_L1(ws + 112384);
+      CHEM_PREFETCH_L1(ws + 112416);
+      CHEM_PREFETCH_L1(ws + 112448);
+      CHEM_PREFETCH_L1(ws + 112480);
+      CHEM_PREFETCH_L1(ws + 112512);
+      CHEM_PREFETCH_L1(ws + 112544);
+      CHEM_PREFETCH_L1(ws + 135488);
       double x = b[3808];
       x = fma(-CHEM_LDLU(lu + 34336), b[4320], x);
       x = fma(-CHEM_LDLU(lu + 34368), b[4384], x);
@@ -2947,6 +4069,17 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
     {
       CHEM_PREFETCH(ws + 112896);
       CHEM_PREFETCH(ws + 135424);
+      CHEM_PREFETCH_L1(ws + 112576);
+      CHEM_PREFETCH_L1(ws + 112608);
+      CHEM_PREFETCH_L1(ws + 112640);
+      CHEM_PREFETCH_L1(ws + 112672);
+      CHEM_PREFETCH_L1(ws + 112704);
+      CHEM_PREFETCH_L1(ws + 112736);
+      CHEM_PREFETCH_L1(ws + 112768);
+      CHEM_PREFETCH_L1(ws + 112800);
+      CHEM_PREFETCH_L1(ws + 112832);
+      CHEM_PREFETCH_L1(ws + 112864);
+      CHEM_PREFETCH_L1(ws + 135456);
       double x = b[3776];
       x = fma(-CHEM_LDLU(lu + 34592), b[3872], x);
       x = fma(-CHEM_LDLU(lu + 34624), b[4160], x);
@@ -2965,6 +4098,8 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 112928);
       CHEM_PREFETCH(ws + 112960);
       CHEM_PREFETCH(ws + 135392);
+      CHEM_PREFETCH_L1(ws + 112896);
+      CHEM_PREFETCH_L1(ws + 135424);
       double x = b[3744];
       x = fma(-CHEM_LDLU(lu + 34944), b[3872], x);
       x = fma(-CHEM_LDLU(lu + 34976), b[3936], x);
@@ -2992,6 +4127,9 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 113312);
       CHEM_PREFETCH(ws + 113344);
       CHEM_PREFETCH(ws + 135360);
+      CHEM_PREFETCH_L1(ws + 112928);
+      CHEM_PREFETCH_L1(ws + 112960);
+      CHEM_PREFETCH_L1(ws + 135392);
       double x = b[3712];
       x = fma(-CHEM_LDLU(lu + 35264), b[4736], x);
       b[3712] = x * CHEM_LDLU(vd + 3712);
@@ -3003,6 +4141,19 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 113472);
       CHEM_PREFETCH(ws + 113504);
       CHEM_PREFETCH(ws + 135328);
+      CHEM_PREFETCH_L1(ws + 112992);
+      CHEM_PREFETCH_L1(ws + 113024);
+      CHEM_PREFETCH_L1(ws + 113056);
+      CHEM_PREFETCH_L1(ws + 113088);
+      CHEM_PREFETCH_L1(ws + 113120);
+      CHEM_PREFETCH_L1(ws + 113152);
+      CHEM_PREFETCH_L1(ws + 113184);
+      CHEM_PREFETCH_L1(ws + 113216);
+      CHEM_PREFETCH_L1(ws + 113248);
+      CHEM_PREFETCH_L1(ws + 113280);
+      CHEM_PREFETCH_L1(ws + 113312);
+      CHEM_PREFETCH_L1(ws + 113344);
+      CHEM_PREFETCH_L1(ws + 135360);
       double x = b[3680];
       x = fma(-CHEM_LDLU(lu + 35296), b[3712], x);
       x = fma(-CHEM_LDLU(lu + 35328), b[4736], x);
@@ -3016,6 +4167,12 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 113664);
       CHEM_PREFETCH(ws + 113696);
       CHEM_PREFETCH(ws + 135296);
+      CHEM_PREFETCH_L1(ws + 113376);
+      CHEM_PREFETCH_L1(ws + 113408);
+      CHEM_PREFETCH_L1(ws + 113440);
+      CHEM_PREFETCH_L1(ws + 113472);
+      CHEM_PREFETCH_L1(ws + 113504);
+      CHEM_PREFETCH_L1(ws + 135328);
       double x = b[3648];
       x = fma(-CHEM_LDLU(lu + 35360), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 35392), b[4224], x);
@@ -3042,6 +4199,13 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 113952);
       CHEM_PREFETCH(ws + 113984);
       CHEM_PREFETCH(ws + 135264);
+      CHEM_PREFETCH_L1(ws + 113536);
+      CHEM_PREFETCH_L1(ws + 113568);
+      CHEM_PREFETCH_L1(ws + 113600);
+      CHEM_PREFETCH_L1(ws + 113632);
+      CHEM_PREFETCH_L1(ws + 113664);
+      CHEM_PREFETCH_L1(ws + 113696);
+      CHEM_PREFETCH_L1(ws + 135296);
       double x = b[3616];
       x = fma(-CHEM_LDLU(lu + 35744), b[4544], x);
       x = fma(-CHEM_LDLU(lu + 35776), b[4608], x);
@@ -3060,6 +4224,16 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 114208);
       CHEM_PREFETCH(ws + 114240);
       CHEM_PREFETCH(ws + 135232);
+      CHEM_PREFETCH_L1(ws + 113728);
+      CHEM_PREFETCH_L1(ws + 113760);
+      CHEM_PREFETCH_L1(ws + 113792);
+      CHEM_PREFETCH_L1(ws + 113824);
+      CHEM_PREFETCH_L1(ws + 113856);
+      CHEM_PREFETCH_L1(ws + 113888);
+      CHEM_PREFETCH_L1(ws + 113920);
+      CHEM_PREFETCH_L1(ws + 113952);
+      CHEM_PREFETCH_L1(ws + 113984);
+      CHEM_PREFETCH_L1(ws + 135264);
       double x = b[3584];
       x = fma(-CHEM_LDLU(lu + 35904), b[4384], x);
       x = fma(-CHEM_LDLU(lu + 35936), b[4448], x);
@@ -3077,6 +4251,15 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 114400);
       CHEM_PREFETCH(ws + 114432);
       CHEM_PREFETCH(ws + 135200);
+      CHEM_PREFETCH_L1(ws + 114016);
+      CHEM_PREFETCH_L1(ws + 114048);
+      CHEM_PREFETCH_L1(ws + 114080);
+      CHEM_PREFETCH_L1(ws + 114112);
+      CHEM_PREFETCH_L1(ws + 114144);
+      CHEM_PREFETCH_L1(ws + 114176);
+      CHEM_PREFETCH_L1(ws + 114208);
+      CHEM_PREFETCH_L1(ws + 114240);
+      CHEM_PREFETCH_L1(ws + 135232);
       double x = b[3552];
       x = fma(-CHEM_LDLU(lu + 36096), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 36128), b[4320], x);
@@ -3102,6 +4285,13 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 114752);
       CHEM_PREFETCH(ws + 114784);
       CHEM_PREFETCH(ws + 135168);
+      CHEM_PREFETCH_L1(ws + 114272);
+      CHEM_PREFETCH_L1(ws + 114304);
+      CHEM_PREFETCH_L1(ws + 114336);
+      CHEM_PREFETCH_L1(ws + 114368);
+      CHEM_PREFETCH_L1(ws + 114400);
+      CHEM_PREFETCH_L1(ws + 114432);
+      CHEM_PREFETCH_L1(ws + 135200);
       double x = b[3520];
       x = fma(-CHEM_LDLU(lu + 36384), b[4320], x);
       x = fma(-CHEM_LDLU(lu + 36416), b[4384], x);
@@ -3124,6 +4314,18 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 115040);
       CHEM_PREFETCH(ws + 115072);
       CHEM_PREFETCH(ws + 135136);
+      CHEM_PREFETCH_L1(ws + 114464);
+      CHEM_PREFETCH_L1(ws + 114496);
+      CHEM_PREFETCH_L1(ws + 114528);
+      CHEM_PREFETCH_L1(ws + 114560);
+      CHEM_PREFETCH_L1(ws + 114592);
+      CHEM_PREFETCH_L1(ws + 114624);
+      CHEM_PREFETCH_L1(ws + 114656);
+      CHEM_PREFETCH_L1(ws + 114688);
+      CHEM_PREFETCH_L1(ws + 114720);
+      CHEM_PREFETCH_L1(ws + 114752);
+      CHEM_PREFETCH_L1(ws + 114784);
+      CHEM_PREFETCH_L1(ws + 135168);
       double x = b[3488];
       x = fma(-CHEM_LDLU(lu + 36640), b[4384], x);
       x = fma(-CHEM_LDLU(lu + 36672), b[4448], x);
@@ -3141,6 +4343,16 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 115232);
       CHEM_PREFETCH(ws + 115264);
       CHEM_PREFETCH(ws + 135104);
+      CHEM_PREFETCH_L1(ws + 114816);
+      CHEM_PREFETCH_L1(ws + 114848);
+      CHEM_PREFETCH_L1(ws + 114880);
+      CHEM_PREFETCH_L1(ws + 114912);
+      CHEM_PREFETCH_L1(ws + 114944);
+      CHEM_PREFETCH_L1(ws + 114976);
+      CHEM_PREFETCH_L1(ws + 115008);
+      CHEM_PREFETCH_L1(ws + 115040);
+      CHEM_PREFETCH_L1(ws + 115072);
+      CHEM_PREFETCH_L1(ws + 135136);
       double x = b[3456];
       x = fma(-CHEM_LDLU(lu + 36832), b[3520], x);
       x = fma(-CHEM_LDLU(lu + 36864), b[3552], x);
@@ -3165,6 +4377,13 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 115488);
       CHEM_PREFETCH(ws + 115520);
       CHEM_PREFETCH(ws + 135072);
+      CHEM_PREFETCH_L1(ws + 115104);
+      CHEM_PREFETCH_L1(ws + 115136);
+      CHEM_PREFETCH_L1(ws + 115168);
+      CHEM_PREFETCH_L1(ws + 115200);
+      CHEM_PREFETCH_L1(ws + 115232);
+      CHEM_PREFETCH_L1(ws + 115264);
+      CHEM_PREFETCH_L1(ws + 135104);
       double x = b[3424];
       x = fma(-CHEM_LDLU(lu + 37184), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 37216), b[4320], x);
@@ -3184,6 +4403,15 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 115648);
       CHEM_PREFETCH(ws + 115680);
       CHEM_PREFETCH(ws + 135040);
+      CHEM_PREFETCH_L1(ws + 115296);
+      CHEM_PREFETCH_L1(ws + 115328);
+      CHEM_PREFETCH_L1(ws + 115360);
+      CHEM_PREFETCH_L1(ws + 115392);
+      CHEM_PREFETCH_L1(ws + 115424);
+      CHEM_PREFETCH_L1(ws + 115456);
+      CHEM_PREFETCH_L1(ws + 115488);
+      CHEM_PREFETCH_L1(ws + 115520);
+      CHEM_PREFETCH_L1(ws + 135072);
       double x = b[3392];
       x = fma(-CHEM_LDLU(lu + 37472), b[3872], x);
       x = fma(-CHEM_LDLU(lu + 37504), b[4224], x);
@@ -3201,6 +4429,12 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 115840);
       CHEM_PREFETCH(ws + 115872);
       CHEM_PREFETCH(ws + 135008);
+      CHEM_PREFETCH_L1(ws + 115552);
+      CHEM_PREFETCH_L1(ws + 115584);
+      CHEM_PREFETCH_L1(ws + 115616);
+      CHEM_PREFETCH_L1(ws + 115648);
+      CHEM_PREFETCH_L1(ws + 115680);
+      CHEM_PREFETCH_L1(ws + 135040);
       double x = b[3360];
       x = fma(-CHEM_LDLU(lu + 37664), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 37696), b[4320], x);
@@ -3218,6 +4452,13 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 115968);
       CHEM_PREFETCH(ws + 116000);
       CHEM_PREFETCH(ws + 134976);
+      CHEM_PREFETCH_L1(ws + 115712);
+      CHEM_PREFETCH_L1(ws + 115744);
+      CHEM_PREFETCH_L1(ws + 115776);
+      CHEM_PREFETCH_L1(ws + 115808);
+      CHEM_PREFETCH_L1(ws + 115840);
+      CHEM_PREFETCH_L1(ws + 115872);
+      CHEM_PREFETCH_L1(ws + 135008);
       double x = b[3328];
       x = fma(-CHEM_LDLU(lu + 37920), b[3616], x);
       x = fma(-CHEM_LDLU(lu + 37952), b[4608], x);
@@ -3236,6 +4477,11 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 116224);
       CHEM_PREFETCH(ws + 116256);
       CHEM_PREFETCH(ws + 134944);
+      CHEM_PREFETCH_L1(ws + 115904);
+      CHEM_PREFETCH_L1(ws + 115936);
+      CHEM_PREFETCH_L1(ws + 115968);
+      CHEM_PREFETCH_L1(ws + 116000);
+      CHEM_PREFETCH_L1(ws + 134976);
       double x = b[3296];
       x = fma(-CHEM_LDLU(lu + 38080), b[3424], x);
       x = fma(-CHEM_LDLU(lu + 38112), b[4384], x);
@@ -3250,6 +4496,15 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 116320);
       CHEM_PREFETCH(ws + 116352);
       CHEM_PREFETCH(ws + 134912);
+      CHEM_PREFETCH_L1(ws + 116032);
+      CHEM_PREFETCH_L1(ws + 116064);
+      CHEM_PREFETCH_L1(ws + 116096);
+      CHEM_PREFETCH_L1(ws + 116128);
+      CHEM_PREFETCH_L1(ws + 116160);
+      CHEM_PREFETCH_L1(ws + 116192);
+      CHEM_PREFETCH_L1(ws + 116224);
+      CHEM_PREFETCH_L1(ws + 116256);
+      CHEM_PREFETCH_L1(ws + 134944);
       double x = b[3264];
       x = fma(-CHEM_LDLU(lu + 38272), b[4384], x);
       x = fma(-CHEM_LDLU(lu + 38304), b[4544], x);
@@ -3263,6 +4518,10 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 116448);
       CHEM_PREFETCH(ws + 116480);
       CHEM_PREFETCH(ws + 134880);
+      CHEM_PREFETCH_L1(ws + 116288);
+      CHEM_PREFETCH_L1(ws + 116320);
+      CHEM_PREFETCH_L1(ws + 116352);
+      CHEM_PREFETCH_L1(ws + 134912);
       double x = b[3232];
       x = fma(-CHEM_LDLU(lu + 38400), b[3424], x);
       x = fma(-CHEM_LDLU(lu + 38432), b[3552], x);
@@ -3283,6 +4542,11 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 116672);
       CHEM_PREFETCH(ws + 116704);
       CHEM_PREFETCH(ws + 134848);
+      CHEM_PREFETCH_L1(ws + 116384);
+      CHEM_PREFETCH_L1(ws + 116416);
+      CHEM_PREFETCH_L1(ws + 116448);
+      CHEM_PREFETCH_L1(ws + 116480);
+      CHEM_PREFETCH_L1(ws + 134880);
       double x = b[3200];
       x = fma(-CHEM_LDLU(lu + 38656), b[3680], x);
       x = fma(-CHEM_LDLU(lu + 38688), b[3712], x);
@@ -3296,6 +4560,14 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 116832);
       CHEM_PREFETCH(ws + 116864);
       CHEM_PREFETCH(ws + 134816);
+      CHEM_PREFETCH_L1(ws + 116512);
+      CHEM_PREFETCH_L1(ws + 116544);
+      CHEM_PREFETCH_L1(ws + 116576);
+      CHEM_PREFETCH_L1(ws + 116608);
+      CHEM_PREFETCH_L1(ws + 116640);
+      CHEM_PREFETCH_L1(ws + 116672);
+      CHEM_PREFETCH_L1(ws + 116704);
+      CHEM_PREFETCH_L1(ws + 134848);
       double x = b[3168];
       x = fma(-CHEM_LDLU(lu + 38752), b[3200], x);
       x = fma(-CHEM_LDLU(lu + 38784), b[3680], x);
@@ -3309,6 +4581,12 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 116960);
       CHEM_PREFETCH(ws + 116992);
       CHEM_PREFETCH(ws + 134784);
+      CHEM_PREFETCH_L1(ws + 116736);
+      CHEM_PREFETCH_L1(ws + 116768);
+      CHEM_PREFETCH_L1(ws + 116800);
+      CHEM_PREFETCH_L1(ws + 116832);
+      CHEM_PREFETCH_L1(ws + 116864);
+      CHEM_PREFETCH_L1(ws + 134816);
       double x = b[3136];
       x = fma(-CHEM_LDLU(lu + 38880), b[3424], x);
       x = fma(-CHEM_LDLU(lu + 38912), b[4160], x);
@@ -3326,6 +4604,11 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 117120);
       CHEM_PREFETCH(ws + 117152);
       CHEM_PREFETCH(ws + 134752);
+      CHEM_PREFETCH_L1(ws + 116896);
+      CHEM_PREFETCH_L1(ws + 116928);
+      CHEM_PREFETCH_L1(ws + 116960);
+      CHEM_PREFETCH_L1(ws + 116992);
+      CHEM_PREFETCH_L1(ws + 134784);
       double x = b[3104];
       x = fma(-CHEM_LDLU(lu + 39104), b[4384], x);
       x = fma(-CHEM_LDLU(lu + 39136), b[4448], x);
@@ -3341,6 +4624,12 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 117280);
       CHEM_PREFETCH(ws + 117312);
       CHEM_PREFETCH(ws + 134720);
+      CHEM_PREFETCH_L1(ws + 117024);
+      CHEM_PREFETCH_L1(ws + 117056);
+      CHEM_PREFETCH_L1(ws + 117088);
+      CHEM_PREFETCH_L1(ws + 117120);
+      CHEM_PREFETCH_L1(ws + 117152);
+      CHEM_PREFETCH_L1(ws + 134752);
       double x = b[3072];
       x = fma(-CHEM_LDLU(lu + 39264), b[4384], x);
       x = fma(-CHEM_LDLU(lu + 39296), b[4544], x);
@@ -3354,6 +4643,12 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 117408);
       CHEM_PREFETCH(ws + 117440);
       CHEM_PREFETCH(ws + 134688);
+      CHEM_PREFETCH_L1(ws + 117184);
+      CHEM_PREFETCH_L1(ws + 117216);
+      CHEM_PREFETCH_L1(ws + 117248);
+      CHEM_PREFETCH_L1(ws + 117280);
+      CHEM_PREFETCH_L1(ws + 117312);
+      CHEM_PREFETCH_L1(ws + 134720);
       double x = b[3040];
       x = fma(-CHEM_LDLU(lu + 39392), b[3456], x);
       x = fma(-CHEM_LDLU(lu + 39424), b[3520], x);
@@ -3368,6 +4663,11 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 117536);
       CHEM_PREFETCH(ws + 117568);
       CHEM_PREFETCH(ws + 134656);
+      CHEM_PREFETCH_L1(ws + 117344);
+      CHEM_PREFETCH_L1(ws + 117376);
+      CHEM_PREFETCH_L1(ws + 117408);
+      CHEM_PREFETCH_L1(ws + 117440);
+      CHEM_PREFETCH_L1(ws + 134688);
       double x = b[3008];
       x = fma(-CHEM_LDLU(lu + 39552), b[3456], x);
       x = fma(-CHEM_LDLU(lu + 39584), b[3520], x);
@@ -3383,6 +4683,11 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 117696);
       CHEM_PREFETCH(ws + 117728);
       CHEM_PREFETCH(ws + 134624);
+      CHEM_PREFETCH_L1(ws + 117472);
+      CHEM_PREFETCH_L1(ws + 117504);
+      CHEM_PREFETCH_L1(ws + 117536);
+      CHEM_PREFETCH_L1(ws + 117568);
+      CHEM_PREFETCH_L1(ws + 134656);
       double x = b[2976];
       x = fma(-CHEM_LDLU(lu + 39712), b[4320], x);
       x = fma(-CHEM_LDLU(lu + 39744), b[4544], x);
@@ -3397,6 +4702,12 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 117856);
       CHEM_PREFETCH(ws + 117888);
       CHEM_PREFETCH(ws + 134592);
+      CHEM_PREFETCH_L1(ws + 117600);
+      CHEM_PREFETCH_L1(ws + 117632);
+      CHEM_PREFETCH_L1(ws + 117664);
+      CHEM_PREFETCH_L1(ws + 117696);
+      CHEM_PREFETCH_L1(ws + 117728);
+      CHEM_PREFETCH_L1(ws + 134624);
       double x = b[2944];
       x = fma(-CHEM_LDLU(lu + 39840), b[4384], x);
       x = fma(-CHEM_LDLU(lu + 39872), b[4544], x);
@@ -3413,6 +4724,12 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 118080);
       CHEM_PREFETCH(ws + 118112);
       CHEM_PREFETCH(ws + 134560);
+      CHEM_PREFETCH_L1(ws + 117760);
+      CHEM_PREFETCH_L1(ws + 117792);
+      CHEM_PREFETCH_L1(ws + 117824);
+      CHEM_PREFETCH_L1(ws + 117856);
+      CHEM_PREFETCH_L1(ws + 117888);
+      CHEM_PREFETCH_L1(ws + 134592);
       double x = b[2912];
       x = fma(-CHEM_LDLU(lu + 39968), b[3168], x);
       x = fma(-CHEM_LDLU(lu + 40000), b[3200], x);
@@ -3424,6 +4741,14 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
     {
       CHEM_PREFETCH(ws + 118144);
       CHEM_PREFETCH(ws + 134528);
+      CHEM_PREFETCH_L1(ws + 117920);
+      CHEM_PREFETCH_L1(ws + 117952);
+      CHEM_PREFETCH_L1(ws + 117984);
+      CHEM_PREFETCH_L1(ws + 118016);
+      CHEM_PREFETCH_L1(ws + 118048);
+      CHEM_PREFETCH_L1(ws + 118080);
+      CHEM_PREFETCH_L1(ws + 118112);
+      CHEM_PREFETCH_L1(ws + 134560);
       double x = b[2880];
       x = fma(-CHEM_LDLU(lu + 40128), b[4288], x);
       x = fma(-CHEM_LDLU(lu + 40160), b[4352], x);
@@ -3436,6 +4761,8 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 118176);
       CHEM_PREFETCH(ws + 118208);
       CHEM_PREFETCH(ws + 134496);
+      CHEM_PREFETCH_L1(ws + 118144);
+      CHEM_PREFETCH_L1(ws + 134528);
       double x = b[2848];
       x = fma(-CHEM_LDLU(lu + 40288), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 40320), b[4320], x);
@@ -3451,6 +4778,9 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 118272);
       CHEM_PREFETCH(ws + 118304);
       CHEM_PREFETCH(ws + 134464);
+      CHEM_PREFETCH_L1(ws + 118176);
+      CHEM_PREFETCH_L1(ws + 118208);
+      CHEM_PREFETCH_L1(ws + 134496);
       double x = b[2816];
       x = fma(-CHEM_LDLU(lu + 40512), b[4736], x);
       b[2816] = x * CHEM_LDLU(vd + 2816);
@@ -3461,6 +4791,10 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 118400);
       CHEM_PREFETCH(ws + 118432);
       CHEM_PREFETCH(ws + 134432);
+      CHEM_PREFETCH_L1(ws + 118240);
+      CHEM_PREFETCH_L1(ws + 118272);
+      CHEM_PREFETCH_L1(ws + 118304);
+      CHEM_PREFETCH_L1(ws + 134464);
       double x = b[2784];
       x = fma(-CHEM_LDLU(lu + 40544), b[2816], x);
       x = fma(-CHEM_LDLU(lu + 40576), b[4736], x);
@@ -3473,6 +4807,11 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 118560);
       CHEM_PREFETCH(ws + 118592);
       CHEM_PREFETCH(ws + 134400);
+      CHEM_PREFETCH_L1(ws + 118336);
+      CHEM_PREFETCH_L1(ws + 118368);
+      CHEM_PREFETCH_L1(ws + 118400);
+      CHEM_PREFETCH_L1(ws + 118432);
+      CHEM_PREFETCH_L1(ws + 134432);
       double x = b[2752];
       x = fma(-CHEM_LDLU(lu + 40608), b[2784], x);
       x = fma(-CHEM_LDLU(lu + 40640), b[2816], x);
@@ -3486,6 +4825,12 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 118720);
       CHEM_PREFETCH(ws + 118752);
       CHEM_PREFETCH(ws + 134368);
+      CHEM_PREFETCH_L1(ws + 118464);
+      CHEM_PREFETCH_L1(ws + 118496);
+      CHEM_PREFETCH_L1(ws + 118528);
+      CHEM_PREFETCH_L1(ws + 118560);
+      CHEM_PREFETCH_L1(ws + 118592);
+      CHEM_PREFETCH_L1(ws + 134400);
       double x = b[2720];
       x = fma(-CHEM_LDLU(lu + 40704), b[4416], x);
       x = fma(-CHEM_LDLU(lu + 40736), b[4544], x);
@@ -3500,6 +4845,12 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 118880);
       CHEM_PREFETCH(ws + 118912);
       CHEM_PREFETCH(ws + 134336);
+      CHEM_PREFETCH_L1(ws + 118624);
+      CHEM_PREFETCH_L1(ws + 118656);
+      CHEM_PREFETCH_L1(ws + 118688);
+      CHEM_PREFETCH_L1(ws + 118720);
+      CHEM_PREFETCH_L1(ws + 118752);
+      CHEM_PREFETCH_L1(ws + 134368);
       double x = b[2688];
       x = fma(-CHEM_LDLU(lu + 40832), b[3744], x);
       x = fma(-CHEM_LDLU(lu + 40864), b[4096], x);
@@ -3512,6 +4863,12 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 118944);
       CHEM_PREFETCH(ws + 118976);
       CHEM_PREFETCH(ws + 134304);
+      CHEM_PREFETCH_L1(ws + 118784);
+      CHEM_PREFETCH_L1(ws + 118816);
+      CHEM_PREFETCH_L1(ws + 118848);
+      CHEM_PREFETCH_L1(ws + 118880);
+      CHEM_PREFETCH_L1(ws + 118912);
+      CHEM_PREFETCH_L1(ws + 134336);
       double x = b[2656];
       x = fma(-CHEM_LDLU(lu + 40992), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 41024), b[4320], x);
@@ -3526,6 +4883,9 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 119072);
       CHEM_PREFETCH(ws + 119104);
       CHEM_PREFETCH(ws + 134272);
+      CHEM_PREFETCH_L1(ws + 118944);
+      CHEM_PREFETCH_L1(ws + 118976);
+      CHEM_PREFETCH_L1(ws + 134304);
       double x = b[2624];
       x = fma(-CHEM_LDLU(lu + 41152), b[2944], x);
       x = fma(-CHEM_LDLU(lu + 41184), b[4384], x);
@@ -3541,6 +4901,11 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 119232);
       CHEM_PREFETCH(ws + 119264);
       CHEM_PREFETCH(ws + 134240);
+      CHEM_PREFETCH_L1(ws + 119008);
+      CHEM_PREFETCH_L1(ws + 119040);
+      CHEM_PREFETCH_L1(ws + 119072);
+      CHEM_PREFETCH_L1(ws + 119104);
+      CHEM_PREFETCH_L1(ws + 134272);
       double x = b[2592];
       x = fma(-CHEM_LDLU(lu + 41312), b[4608], x);
       x = fma(-CHEM_LDLU(lu + 41344), b[4640], x);
@@ -3552,6 +4917,12 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 119360);
       CHEM_PREFETCH(ws + 119392);
       CHEM_PREFETCH(ws + 134208);
+      CHEM_PREFETCH_L1(ws + 119136);
+      CHEM_PREFETCH_L1(ws + 119168);
+      CHEM_PREFETCH_L1(ws + 119200);
+      CHEM_PREFETCH_L1(ws + 119232);
+      CHEM_PREFETCH_L1(ws + 119264);
+      CHEM_PREFETCH_L1(ws + 134240);
       double x = b[2560];
       x = fma(-CHEM_LDLU(lu + 41376), b[4384], x);
       x = fma(-CHEM_LDLU(lu + 41408), b[4544], x);
@@ -3564,6 +4935,11 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 119456);
       CHEM_PREFETCH(ws + 119488);
       CHEM_PREFETCH(ws + 134176);
+      CHEM_PREFETCH_L1(ws + 119296);
+      CHEM_PREFETCH_L1(ws + 119328);
+      CHEM_PREFETCH_L1(ws + 119360);
+      CHEM_PREFETCH_L1(ws + 119392);
+      CHEM_PREFETCH_L1(ws + 134208);
       double x = b[2528];
       x = fma(-CHEM_LDLU(lu + 41504), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 41536), b[4320], x);
@@ -3578,6 +4954,10 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 119584);
       CHEM_PREFETCH(ws + 119616);
       CHEM_PREFETCH(ws + 134144);
+      CHEM_PREFETCH_L1(ws + 119424);
+      CHEM_PREFETCH_L1(ws + 119456);
+      CHEM_PREFETCH_L1(ws + 119488);
+      CHEM_PREFETCH_L1(ws + 134176);
       double x = b[2496];
       x = fma(-CHEM_LDLU(lu + 41664), b[4384], x);
       x = fma(-CHEM_LDLU(lu + 41696), b[4544], x);
@@ -3591,6 +4971,11 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 119712);
       CHEM_PREFETCH(ws + 119744);
       CHEM_PREFETCH(ws + 134112);
+      CHEM_PREFETCH_L1(ws + 119520);
+      CHEM_PREFETCH_L1(ws + 119552);
+      CHEM_PREFETCH_L1(ws + 119584);
+      CHEM_PREFETCH_L1(ws + 119616);
+      CHEM_PREFETCH_L1(ws + 134144);
       double x = b[2464];
       x = fma(-CHEM_LDLU(lu + 41792), b[4384], x);
       x = fma(-CHEM_LDLU(lu + 41824), b[4608], x);
@@ -3603,6 +4988,11 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 119840);
       CHEM_PREFETCH(ws + 119872);
       CHEM_PREFETCH(ws + 134080);
+      CHEM_PREFETCH_L1(ws + 119648);
+      CHEM_PREFETCH_L1(ws + 119680);
+      CHEM_PREFETCH_L1(ws + 119712);
+      CHEM_PREFETCH_L1(ws + 119744);
+      CHEM_PREFETCH_L1(ws + 134112);
       double x = b[2432];
       x = fma(-CHEM_LDLU(lu + 41888), b[4320], x);
       x = fma(-CHEM_LDLU(lu + 41920), b[4544], x);
@@ -3616,6 +5006,11 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 119968);
       CHEM_PREFETCH(ws + 120000);
       CHEM_PREFETCH(ws + 134048);
+      CHEM_PREFETCH_L1(ws + 119776);
+      CHEM_PREFETCH_L1(ws + 119808);
+      CHEM_PREFETCH_L1(ws + 119840);
+      CHEM_PREFETCH_L1(ws + 119872);
+      CHEM_PREFETCH_L1(ws + 134080);
       double x = b[2400];
       x = fma(-CHEM_LDLU(lu + 42016), b[4320], x);
       x = fma(-CHEM_LDLU(lu + 42048), b[4544], x);
@@ -3629,6 +5024,11 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 120096);
       CHEM_PREFETCH(ws + 120128);
       CHEM_PREFETCH(ws + 134016);
+      CHEM_PREFETCH_L1(ws + 119904);
+      CHEM_PREFETCH_L1(ws + 119936);
+      CHEM_PREFETCH_L1(ws + 119968);
+      CHEM_PREFETCH_L1(ws + 120000);
+      CHEM_PREFETCH_L1(ws + 134048);
       double x = b[2368];
       x = fma(-CHEM_LDLU(lu + 42144), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 42176), b[4544], x);
@@ -3643,6 +5043,11 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 120256);
       CHEM_PREFETCH(ws + 120288);
       CHEM_PREFETCH(ws + 133984);
+      CHEM_PREFETCH_L1(ws + 120032);
+      CHEM_PREFETCH_L1(ws + 120064);
+      CHEM_PREFETCH_L1(ws + 120096);
+      CHEM_PREFETCH_L1(ws + 120128);
+      CHEM_PREFETCH_L1(ws + 134016);
       double x = b[2336];
       x = fma(-CHEM_LDLU(lu + 42272), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 42304), b[4544], x);
@@ -3658,6 +5063,12 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 120448);
       CHEM_PREFETCH(ws + 120480);
       CHEM_PREFETCH(ws + 133952);
+      CHEM_PREFETCH_L1(ws + 120160);
+      CHEM_PREFETCH_L1(ws + 120192);
+      CHEM_PREFETCH_L1(ws + 120224);
+      CHEM_PREFETCH_L1(ws + 120256);
+      CHEM_PREFETCH_L1(ws + 120288);
+      CHEM_PREFETCH_L1(ws + 133984);
       double x = b[2304];
       x = fma(-CHEM_LDLU(lu + 42400), b[2752], x);
       x = fma(-CHEM_LDLU(lu + 42432), b[2784], x);
@@ -3670,6 +5081,13 @@ __device__ __noinline__ void solve_1_1(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 120544);
       CHEM_PREFETCH(ws + 120576);
       CHEM_PREFETCH(ws + 133920);
+      CHEM_PREFETCH_L1(ws + 120320);
+      CHEM_PREFETCH_L1(ws + 120352);
+      CHEM_PREFETCH_L1(ws + 120384);
+      CHEM_PREFETCH_L1(ws + 120416);
+      CHEM_PREFETCH_L1(ws + 120448);
+      CHEM_PREFETCH_L1(ws + 120480);
+      CHEM_PREFETCH_L1(ws + 133952);
       double x = b[2272];
       x = fma(-CHEM_LDLU(lu + 42528), b[4384], x);
       x = fma(-CHEM_LDLU(lu + 42560), b[4416], x);
@@ -3691,6 +5109,10 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 120672);
       CHEM_PREFETCH(ws + 120704);
       CHEM_PREFETCH(ws + 133888);
+      CHEM_PREFETCH_L1(ws + 120512);
+      CHEM_PREFETCH_L1(ws + 120544);
+      CHEM_PREFETCH_L1(ws + 120576);
+      CHEM_PREFETCH_L1(ws + 133920);
       double x = b[2240];
       x = fma(-CHEM_LDLU(lu + 42688), b[2496], x);
       x = fma(-CHEM_LDLU(lu + 42720), b[2560], x);
@@ -3705,6 +5127,11 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 120768);
       CHEM_PREFETCH(ws + 120800);
       CHEM_PREFETCH(ws + 133856);
+      CHEM_PREFETCH_L1(ws + 120608);
+      CHEM_PREFETCH_L1(ws + 120640);
+      CHEM_PREFETCH_L1(ws + 120672);
+      CHEM_PREFETCH_L1(ws + 120704);
+      CHEM_PREFETCH_L1(ws + 133888);
       double x = b[2208];
       x = fma(-CHEM_LDLU(lu + 42880), b[4544], x);
       x = fma(-CHEM_LDLU(lu + 42912), b[4640], x);
@@ -3717,6 +5144,10 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 120896);
       CHEM_PREFETCH(ws + 120928);
       CHEM_PREFETCH(ws + 133824);
+      CHEM_PREFETCH_L1(ws + 120736);
+      CHEM_PREFETCH_L1(ws + 120768);
+      CHEM_PREFETCH_L1(ws + 120800);
+      CHEM_PREFETCH_L1(ws + 133856);
       double x = b[2176];
       x = fma(-CHEM_LDLU(lu + 42976), b[3328], x);
       x = fma(-CHEM_LDLU(lu + 43008), b[4608], x);
@@ -3731,6 +5162,11 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 121056);
       CHEM_PREFETCH(ws + 121088);
       CHEM_PREFETCH(ws + 133792);
+      CHEM_PREFETCH_L1(ws + 120832);
+      CHEM_PREFETCH_L1(ws + 120864);
+      CHEM_PREFETCH_L1(ws + 120896);
+      CHEM_PREFETCH_L1(ws + 120928);
+      CHEM_PREFETCH_L1(ws + 133824);
       double x = b[2144];
       x = fma(-CHEM_LDLU(lu + 43104), b[4384], x);
       x = fma(-CHEM_LDLU(lu + 43136), b[4704], x);
@@ -3743,6 +5179,12 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 121184);
       CHEM_PREFETCH(ws + 121216);
       CHEM_PREFETCH(ws + 133760);
+      CHEM_PREFETCH_L1(ws + 120960);
+      CHEM_PREFETCH_L1(ws + 120992);
+      CHEM_PREFETCH_L1(ws + 121024);
+      CHEM_PREFETCH_L1(ws + 121056);
+      CHEM_PREFETCH_L1(ws + 121088);
+      CHEM_PREFETCH_L1(ws + 133792);
       double x = b[2112];
       x = fma(-CHEM_LDLU(lu + 43200), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 43232), b[4320], x);
@@ -3755,6 +5197,11 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 121280);
       CHEM_PREFETCH(ws + 121312);
       CHEM_PREFETCH(ws + 133728);
+      CHEM_PREFETCH_L1(ws + 121120);
+      CHEM_PREFETCH_L1(ws + 121152);
+      CHEM_PREFETCH_L1(ws + 121184);
+      CHEM_PREFETCH_L1(ws + 121216);
+      CHEM_PREFETCH_L1(ws + 133760);
       double x = b[2080];
       x = fma(-CHEM_LDLU(lu + 43328), b[2112], x);
       x = fma(-CHEM_LDLU(lu + 43360), b[4160], x);
@@ -3768,6 +5215,10 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 121376);
       CHEM_PREFETCH(ws + 121408);
       CHEM_PREFETCH(ws + 133696);
+      CHEM_PREFETCH_L1(ws + 121248);
+      CHEM_PREFETCH_L1(ws + 121280);
+      CHEM_PREFETCH_L1(ws + 121312);
+      CHEM_PREFETCH_L1(ws + 133728);
       double x = b[2048];
       x = fma(-CHEM_LDLU(lu + 43488), b[4160], x);
       x = fma(-CHEM_LDLU(lu + 43520), b[4320], x);
@@ -3780,6 +5231,10 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 121472);
       CHEM_PREFETCH(ws + 121504);
       CHEM_PREFETCH(ws + 133664);
+      CHEM_PREFETCH_L1(ws + 121344);
+      CHEM_PREFETCH_L1(ws + 121376);
+      CHEM_PREFETCH_L1(ws + 121408);
+      CHEM_PREFETCH_L1(ws + 133696);
       double x = b[2016];
       x = fma(-CHEM_LDLU(lu + 43616), b[4544], x);
       x = fma(-CHEM_LDLU(lu + 43648), b[4640], x);
@@ -3790,6 +5245,10 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 121536);
       CHEM_PREFETCH(ws + 121568);
       CHEM_PREFETCH(ws + 133632);
+      CHEM_PREFETCH_L1(ws + 121440);
+      CHEM_PREFETCH_L1(ws + 121472);
+      CHEM_PREFETCH_L1(ws + 121504);
+      CHEM_PREFETCH_L1(ws + 133664);
       double x = b[1984];
       x = fma(-CHEM_LDLU(lu + 43712), b[4224], x);
       x = fma(-CHEM_LDLU(lu + 43744), b[4544], x);
@@ -3801,6 +5260,9 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 121632);
       CHEM_PREFETCH(ws + 121664);
       CHEM_PREFETCH(ws + 133600);
+      CHEM_PREFETCH_L1(ws + 121536);
+      CHEM_PREFETCH_L1(ws + 121568);
+      CHEM_PREFETCH_L1(ws + 133632);
       double x = b[1952];
       x = fma(-CHEM_LDLU(lu + 43808), b[4096], x);
       x = fma(-CHEM_LDLU(lu + 43840), b[4608], x);
@@ -3812,6 +5274,10 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 121728);
       CHEM_PREFETCH(ws + 121760);
       CHEM_PREFETCH(ws + 133568);
+      CHEM_PREFETCH_L1(ws + 121600);
+      CHEM_PREFETCH_L1(ws + 121632);
+      CHEM_PREFETCH_L1(ws + 121664);
+      CHEM_PREFETCH_L1(ws + 133600);
       double x = b[1920];
       x = fma(-CHEM_LDLU(lu + 43904), b[4608], x);
       x = fma(-CHEM_LDLU(lu + 43936), b[4640], x);
@@ -3822,6 +5288,10 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 121824);
       CHEM_PREFETCH(ws + 121856);
       CHEM_PREFETCH(ws + 133536);
+      CHEM_PREFETCH_L1(ws + 121696);
+      CHEM_PREFETCH_L1(ws + 121728);
+      CHEM_PREFETCH_L1(ws + 121760);
+      CHEM_PREFETCH_L1(ws + 133568);
       double x = b[1888];
       x = fma(-CHEM_LDLU(lu + 43968), b[4320], x);
       x = fma(-CHEM_LDLU(lu + 44000), b[4640], x);
@@ -3833,6 +5303,10 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 121920);
       CHEM_PREFETCH(ws + 121952);
       CHEM_PREFETCH(ws + 133504);
+      CHEM_PREFETCH_L1(ws + 121792);
+      CHEM_PREFETCH_L1(ws + 121824);
+      CHEM_PREFETCH_L1(ws + 121856);
+      CHEM_PREFETCH_L1(ws + 133536);
       double x = b[1856];
       x = fma(-CHEM_LDLU(lu + 44064), b[4320], x);
       x = fma(-CHEM_LDLU(lu + 44096), b[4640], x);
@@ -3844,6 +5318,10 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 122016);
       CHEM_PREFETCH(ws + 122048);
       CHEM_PREFETCH(ws + 133472);
+      CHEM_PREFETCH_L1(ws + 121888);
+      CHEM_PREFETCH_L1(ws + 121920);
+      CHEM_PREFETCH_L1(ws + 121952);
+      CHEM_PREFETCH_L1(ws + 133504);
       double x = b[1824];
       x = fma(-CHEM_LDLU(lu + 44160), b[3520], x);
       x = fma(-CHEM_LDLU(lu + 44192), b[4608], x);
@@ -3855,6 +5333,10 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 122112);
       CHEM_PREFETCH(ws + 122144);
       CHEM_PREFETCH(ws + 133440);
+      CHEM_PREFETCH_L1(ws + 121984);
+      CHEM_PREFETCH_L1(ws + 122016);
+      CHEM_PREFETCH_L1(ws + 122048);
+      CHEM_PREFETCH_L1(ws + 133472);
       double x = b[1792];
       x = fma(-CHEM_LDLU(lu + 44256), b[3744], x);
       x = fma(-CHEM_LDLU(lu + 44288), b[4608], x);
@@ -3866,6 +5348,10 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 122208);
       CHEM_PREFETCH(ws + 122240);
       CHEM_PREFETCH(ws + 133408);
+      CHEM_PREFETCH_L1(ws + 122080);
+      CHEM_PREFETCH_L1(ws + 122112);
+      CHEM_PREFETCH_L1(ws + 122144);
+      CHEM_PREFETCH_L1(ws + 133440);
       double x = b[1760];
       x = fma(-CHEM_LDLU(lu + 44352), b[3616], x);
       x = fma(-CHEM_LDLU(lu + 44384), b[4640], x);
@@ -3877,6 +5363,10 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 122304);
       CHEM_PREFETCH(ws + 122336);
       CHEM_PREFETCH(ws + 133376);
+      CHEM_PREFETCH_L1(ws + 122176);
+      CHEM_PREFETCH_L1(ws + 122208);
+      CHEM_PREFETCH_L1(ws + 122240);
+      CHEM_PREFETCH_L1(ws + 133408);
       double x = b[1728];
       x = fma(-CHEM_LDLU(lu + 44448), b[4384], x);
       x = fma(-CHEM_LDLU(lu + 44480), b[4512], x);
@@ -3888,6 +5378,10 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 122400);
       CHEM_PREFETCH(ws + 122432);
       CHEM_PREFETCH(ws + 133344);
+      CHEM_PREFETCH_L1(ws + 122272);
+      CHEM_PREFETCH_L1(ws + 122304);
+      CHEM_PREFETCH_L1(ws + 122336);
+      CHEM_PREFETCH_L1(ws + 133376);
       double x = b[1696];
       x = fma(-CHEM_LDLU(lu + 44544), b[4608], x);
       x = fma(-CHEM_LDLU(lu + 44576), b[4704], x);
@@ -3899,6 +5393,10 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 122496);
       CHEM_PREFETCH(ws + 122528);
       CHEM_PREFETCH(ws + 133312);
+      CHEM_PREFETCH_L1(ws + 122368);
+      CHEM_PREFETCH_L1(ws + 122400);
+      CHEM_PREFETCH_L1(ws + 122432);
+      CHEM_PREFETCH_L1(ws + 133344);
       double x = b[1664];
       x = fma(-CHEM_LDLU(lu + 44640), b[3424], x);
       x = fma(-CHEM_LDLU(lu + 44672), b[4704], x);
@@ -3910,6 +5408,10 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 122592);
       CHEM_PREFETCH(ws + 122624);
       CHEM_PREFETCH(ws + 133280);
+      CHEM_PREFETCH_L1(ws + 122464);
+      CHEM_PREFETCH_L1(ws + 122496);
+      CHEM_PREFETCH_L1(ws + 122528);
+      CHEM_PREFETCH_L1(ws + 133312);
       double x = b[1632];
       x = fma(-CHEM_LDLU(lu + 44736), b[3424], x);
       x = fma(-CHEM_LDLU(lu + 44768), b[4384], x);
@@ -3920,6 +5422,10 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 122656);
       CHEM_PREFETCH(ws + 122688);
       CHEM_PREFETCH(ws + 133248);
+      CHEM_PREFETCH_L1(ws + 122560);
+      CHEM_PREFETCH_L1(ws + 122592);
+      CHEM_PREFETCH_L1(ws + 122624);
+      CHEM_PREFETCH_L1(ws + 133280);
       double x = b[1600];
       x = fma(-CHEM_LDLU(lu + 44832), b[2016], x);
       x = fma(-CHEM_LDLU(lu + 44864), b[4544], x);
@@ -3930,6 +5436,9 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 122720);
       CHEM_PREFETCH(ws + 122752);
       CHEM_PREFETCH(ws + 133216);
+      CHEM_PREFETCH_L1(ws + 122656);
+      CHEM_PREFETCH_L1(ws + 122688);
+      CHEM_PREFETCH_L1(ws + 133248);
       double x = b[1568];
       x = fma(-CHEM_LDLU(lu + 44928), b[3008], x);
       x = fma(-CHEM_LDLU(lu + 44960), b[4320], x);
@@ -3939,6 +5448,9 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
     {
       CHEM_PREFETCH(ws + 122784);
       CHEM_PREFETCH(ws + 133184);
+      CHEM_PREFETCH_L1(ws + 122720);
+      CHEM_PREFETCH_L1(ws + 122752);
+      CHEM_PREFETCH_L1(ws + 133216);
       double x = b[1536];
       x = fma(-CHEM_LDLU(lu + 45024), b[4544], x);
       x = fma(-CHEM_LDLU(lu + 45056), b[4736], x);
@@ -3947,6 +5459,8 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
     {
       CHEM_PREFETCH(ws + 122816);
       CHEM_PREFETCH(ws + 133152);
+      CHEM_PREFETCH_L1(ws + 122784);
+      CHEM_PREFETCH_L1(ws + 133184);
       double x = b[1504];
       x = fma(-CHEM_LDLU(lu + 45088), b[2752], x);
       x = fma(-CHEM_LDLU(lu + 45120), b[4736], x);
@@ -3954,12 +5468,15 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
     }
     {
       CHEM_PREFETCH(ws + 133120);
+      CHEM_PREFETCH_L1(ws + 122816);
+      CHEM_PREFETCH_L1(ws + 133152);
       double x = b[1472];
       x = fma(-CHEM_LDLU(lu + 45152), b[4736], x);
       b[1472] = x * CHEM_LDLU(vd + 1472);
     }
     {
       CHEM_PREFETCH(ws + 133088);
+      CHEM_PREFETCH_L1(ws + 133120);
       double x = b[1440];
       x = fma(-CHEM_LDLU(lu + 45184), b[4736], x);
       b[1440] = x * CHEM_LDLU(vd + 1440);
@@ -3968,6 +5485,7 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 122848);
       CHEM_PREFETCH(ws + 122880);
       CHEM_PREFETCH(ws + 133056);
+      CHEM_PREFETCH_L1(ws + 133088);
       double x = b[1408];
       b[1408] = x * CHEM_LDLU(vd + 1408);
     }
@@ -3975,6 +5493,9 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 122912);
       CHEM_PREFETCH(ws + 122944);
       CHEM_PREFETCH(ws + 133024);
+      CHEM_PREFETCH_L1(ws + 122848);
+      CHEM_PREFETCH_L1(ws + 122880);
+      CHEM_PREFETCH_L1(ws + 133056);
       double x = b[1376];
       b[1376] = x * CHEM_LDLU(vd + 1376);
     }
@@ -3982,6 +5503,9 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 122976);
       CHEM_PREFETCH(ws + 123008);
       CHEM_PREFETCH(ws + 132992);
+      CHEM_PREFETCH_L1(ws + 122912);
+      CHEM_PREFETCH_L1(ws + 122944);
+      CHEM_PREFETCH_L1(ws + 133024);
       double x = b[1344];
       x = fma(-CHEM_LDLU(lu + 45216), b[4448], x);
       x = fma(-CHEM_LDLU(lu + 45248), b[4608], x);
@@ -3990,6 +5514,9 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
     {
       CHEM_PREFETCH(ws + 123040);
       CHEM_PREFETCH(ws + 132960);
+      CHEM_PREFETCH_L1(ws + 122976);
+      CHEM_PREFETCH_L1(ws + 123008);
+      CHEM_PREFETCH_L1(ws + 132992);
       double x = b[1312];
       x = fma(-CHEM_LDLU(lu + 45280), b[1664], x);
       x = fma(-CHEM_LDLU(lu + 45312), b[4736], x);
@@ -3999,6 +5526,8 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 123072);
       CHEM_PREFETCH(ws + 123104);
       CHEM_PREFETCH(ws + 132928);
+      CHEM_PREFETCH_L1(ws + 123040);
+      CHEM_PREFETCH_L1(ws + 132960);
       double x = b[1280];
       x = fma(-CHEM_LDLU(lu + 45344), b[4608], x);
       x = fma(-CHEM_LDLU(lu + 45376), b[4640], x);
@@ -4008,6 +5537,9 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 123136);
       CHEM_PREFETCH(ws + 123168);
       CHEM_PREFETCH(ws + 132896);
+      CHEM_PREFETCH_L1(ws + 123072);
+      CHEM_PREFETCH_L1(ws + 123104);
+      CHEM_PREFETCH_L1(ws + 132928);
       double x = b[1248];
       x = fma(-CHEM_LDLU(lu + 45408), b[1280], x);
       b[1248] = x * CHEM_LDLU(vd + 1248);
@@ -4016,6 +5548,9 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 123200);
       CHEM_PREFETCH(ws + 123232);
       CHEM_PREFETCH(ws + 132864);
+      CHEM_PREFETCH_L1(ws + 123136);
+      CHEM_PREFETCH_L1(ws + 123168);
+      CHEM_PREFETCH_L1(ws + 132896);
       double x = b[1216];
       x = fma(-CHEM_LDLU(lu + 45440), b[3520], x);
       x = fma(-CHEM_LDLU(lu + 45472), b[4608], x);
@@ -4025,6 +5560,9 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 123264);
       CHEM_PREFETCH(ws + 123296);
       CHEM_PREFETCH(ws + 132832);
+      CHEM_PREFETCH_L1(ws + 123200);
+      CHEM_PREFETCH_L1(ws + 123232);
+      CHEM_PREFETCH_L1(ws + 132864);
       double x = b[1184];
       x = fma(-CHEM_LDLU(lu + 45504), b[3008], x);
       x = fma(-CHEM_LDLU(lu + 45536), b[3520], x);
@@ -4034,6 +5572,9 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 123328);
       CHEM_PREFETCH(ws + 123360);
       CHEM_PREFETCH(ws + 132800);
+      CHEM_PREFETCH_L1(ws + 123264);
+      CHEM_PREFETCH_L1(ws + 123296);
+      CHEM_PREFETCH_L1(ws + 132832);
       double x = b[1152];
       x = fma(-CHEM_LDLU(lu + 45568), b[4544], x);
       x = fma(-CHEM_LDLU(lu + 45600), b[4736], x);
@@ -4043,6 +5584,9 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 123392);
       CHEM_PREFETCH(ws + 123424);
       CHEM_PREFETCH(ws + 132768);
+      CHEM_PREFETCH_L1(ws + 123328);
+      CHEM_PREFETCH_L1(ws + 123360);
+      CHEM_PREFETCH_L1(ws + 132800);
       double x = b[1120];
       x = fma(-CHEM_LDLU(lu + 45632), b[4544], x);
       x = fma(-CHEM_LDLU(lu + 45664), b[4736], x);
@@ -4052,6 +5596,9 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 123456);
       CHEM_PREFETCH(ws + 123488);
       CHEM_PREFETCH(ws + 132736);
+      CHEM_PREFETCH_L1(ws + 123392);
+      CHEM_PREFETCH_L1(ws + 123424);
+      CHEM_PREFETCH_L1(ws + 132768);
       double x = b[1088];
       x = fma(-CHEM_LDLU(lu + 45696), b[4544], x);
       x = fma(-CHEM_LDLU(lu + 45728), b[4736], x);
@@ -4062,6 +5609,9 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 123552);
       CHEM_PREFETCH(ws + 123584);
       CHEM_PREFETCH(ws + 132704);
+      CHEM_PREFETCH_L1(ws + 123456);
+      CHEM_PREFETCH_L1(ws + 123488);
+      CHEM_PREFETCH_L1(ws + 132736);
       double x = b[1056];
       x = fma(-CHEM_LDLU(lu + 45760), b[1664], x);
       x = fma(-CHEM_LDLU(lu + 45792), b[4736], x);
@@ -4071,6 +5621,10 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 123616);
       CHEM_PREFETCH(ws + 123648);
       CHEM_PREFETCH(ws + 132672);
+      CHEM_PREFETCH_L1(ws + 123520);
+      CHEM_PREFETCH_L1(ws + 123552);
+      CHEM_PREFETCH_L1(ws + 123584);
+      CHEM_PREFETCH_L1(ws + 132704);
       double x = b[1024];
       x = fma(-CHEM_LDLU(lu + 45824), b[3424], x);
       x = fma(-CHEM_LDLU(lu + 45856), b[4640], x);
@@ -4080,6 +5634,9 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 123680);
       CHEM_PREFETCH(ws + 123712);
       CHEM_PREFETCH(ws + 132640);
+      CHEM_PREFETCH_L1(ws + 123616);
+      CHEM_PREFETCH_L1(ws + 123648);
+      CHEM_PREFETCH_L1(ws + 132672);
       double x = b[992];
       x = fma(-CHEM_LDLU(lu + 45888), b[2528], x);
       x = fma(-CHEM_LDLU(lu + 45920), b[4640], x);
@@ -4090,6 +5647,9 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 123744);
       CHEM_PREFETCH(ws + 123776);
       CHEM_PREFETCH(ws + 132608);
+      CHEM_PREFETCH_L1(ws + 123680);
+      CHEM_PREFETCH_L1(ws + 123712);
+      CHEM_PREFETCH_L1(ws + 132640);
       double x = b[960];
       x = fma(-CHEM_LDLU(lu + 45984), b[1984], x);
       x = fma(-CHEM_LDLU(lu + 46016), b[4608], x);
@@ -4099,6 +5659,9 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 123808);
       CHEM_PREFETCH(ws + 123840);
       CHEM_PREFETCH(ws + 132576);
+      CHEM_PREFETCH_L1(ws + 123744);
+      CHEM_PREFETCH_L1(ws + 123776);
+      CHEM_PREFETCH_L1(ws + 132608);
       double x = b[928];
       x = fma(-CHEM_LDLU(lu + 46048), b[4544], x);
       x = fma(-CHEM_LDLU(lu + 46080), b[4736], x);
@@ -4108,6 +5671,9 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 123872);
       CHEM_PREFETCH(ws + 123904);
       CHEM_PREFETCH(ws + 132544);
+      CHEM_PREFETCH_L1(ws + 123808);
+      CHEM_PREFETCH_L1(ws + 123840);
+      CHEM_PREFETCH_L1(ws + 132576);
       double x = b[896];
       x = fma(-CHEM_LDLU(lu + 46112), b[4544], x);
       x = fma(-CHEM_LDLU(lu + 46144), b[4736], x);
@@ -4116,6 +5682,9 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
     {
       CHEM_PREFETCH(ws + 123936);
       CHEM_PREFETCH(ws + 132512);
+      CHEM_PREFETCH_L1(ws + 123872);
+      CHEM_PREFETCH_L1(ws + 123904);
+      CHEM_PREFETCH_L1(ws + 132544);
       double x = b[864];
       x = fma(-CHEM_LDLU(lu + 46176), b[4544], x);
       x = fma(-CHEM_LDLU(lu + 46208), b[4736], x);
@@ -4124,6 +5693,8 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
     {
       CHEM_PREFETCH(ws + 123968);
       CHEM_PREFETCH(ws + 132480);
+      CHEM_PREFETCH_L1(ws + 123936);
+      CHEM_PREFETCH_L1(ws + 132512);
       double x = b[832];
       x = fma(-CHEM_LDLU(lu + 46240), b[4544], x);
       x = fma(-CHEM_LDLU(lu + 46272), b[4736], x);
@@ -4132,6 +5703,8 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
     {
       CHEM_PREFETCH(ws + 124000);
       CHEM_PREFETCH(ws + 132448);
+      CHEM_PREFETCH_L1(ws + 123968);
+      CHEM_PREFETCH_L1(ws + 132480);
       double x = b[800];
       x = fma(-CHEM_LDLU(lu + 46304), b[4736], x);
       b[800] = x * CHEM_LDLU(vd + 800);
@@ -4139,12 +5712,16 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
     {
       CHEM_PREFETCH(ws + 124032);
       CHEM_PREFETCH(ws + 132416);
+      CHEM_PREFETCH_L1(ws + 124000);
+      CHEM_PREFETCH_L1(ws + 132448);
       double x = b[768];
       x = fma(-CHEM_LDLU(lu + 46336), b[4736], x);
       b[768] = x * CHEM_LDLU(vd + 768);
     }
     {
       CHEM_PREFETCH(ws + 132384);
+      CHEM_PREFETCH_L1(ws + 124032);
+      CHEM_PREFETCH_L1(ws + 132416);
       double x = b[736];
       x = fma(-CHEM_LDLU(lu + 46368), b[4736], x);
       b[736] = x * CHEM_LDLU(vd + 736);
@@ -4153,6 +5730,7 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 124064);
       CHEM_PREFETCH(ws + 124096);
       CHEM_PREFETCH(ws + 132352);
+      CHEM_PREFETCH_L1(ws + 132384);
       double x = b[704];
       x = fma(-CHEM_LDLU(lu + 46400), b[4736], x);
       b[704] = x * CHEM_LDLU(vd + 704);
@@ -4160,12 +5738,17 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
     {
       CHEM_PREFETCH(ws + 124128);
       CHEM_PREFETCH(ws + 132320);
+      CHEM_PREFETCH_L1(ws + 124064);
+      CHEM_PREFETCH_L1(ws + 124096);
+      CHEM_PREFETCH_L1(ws + 132352);
       double x = b[672];
       b[672] = x * CHEM_LDLU(vd + 672);
     }
     {
       CHEM_PREFETCH(ws + 124160);
       CHEM_PREFETCH(ws + 132288);
+      CHEM_PREFETCH_L1(ws + 124128);
+      CHEM_PREFETCH_L1(ws + 132320);
       double x = b[640];
       x = fma(-CHEM_LDLU(lu + 46432), b[4000], x);
       x = fma(-CHEM_LDLU(lu + 46464), b[4256], x);
@@ -4174,6 +5757,8 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
     {
       CHEM_PREFETCH(ws + 124192);
       CHEM_PREFETCH(ws + 132256);
+      CHEM_PREFETCH_L1(ws + 124160);
+      CHEM_PREFETCH_L1(ws + 132288);
       double x = b[608];
       x = fma(-CHEM_LDLU(lu + 46496), b[1312], x);
       b[608] = x * CHEM_LDLU(vd + 608);
@@ -4181,6 +5766,8 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
     {
       CHEM_PREFETCH(ws + 124224);
       CHEM_PREFETCH(ws + 132224);
+      CHEM_PREFETCH_L1(ws + 124192);
+      CHEM_PREFETCH_L1(ws + 132256);
       double x = b[576];
       x = fma(-CHEM_LDLU(lu + 46528), b[1312], x);
       b[576] = x * CHEM_LDLU(vd + 576);
@@ -4188,6 +5775,8 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
     {
       CHEM_PREFETCH(ws + 124256);
       CHEM_PREFETCH(ws + 132192);
+      CHEM_PREFETCH_L1(ws + 124224);
+      CHEM_PREFETCH_L1(ws + 132224);
       double x = b[544];
       x = fma(-CHEM_LDLU(lu + 46560), b[1248], x);
       b[544] = x * CHEM_LDLU(vd + 544);
@@ -4195,6 +5784,8 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
     {
       CHEM_PREFETCH(ws + 124288);
       CHEM_PREFETCH(ws + 132160);
+      CHEM_PREFETCH_L1(ws + 124256);
+      CHEM_PREFETCH_L1(ws + 132192);
       double x = b[512];
       x = fma(-CHEM_LDLU(lu + 46592), b[1920], x);
       b[512] = x * CHEM_LDLU(vd + 512);
@@ -4202,6 +5793,8 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
     {
       CHEM_PREFETCH(ws + 124320);
       CHEM_PREFETCH(ws + 132128);
+      CHEM_PREFETCH_L1(ws + 124288);
+      CHEM_PREFETCH_L1(ws + 132160);
       double x = b[480];
       x = fma(-CHEM_LDLU(lu + 46624), b[1920], x);
       b[480] = x * CHEM_LDLU(vd + 480);
@@ -4209,6 +5802,8 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
     {
       CHEM_PREFETCH(ws + 124352);
       CHEM_PREFETCH(ws + 132096);
+      CHEM_PREFETCH_L1(ws + 124320);
+      CHEM_PREFETCH_L1(ws + 132128);
       double x = b[448];
       x = fma(-CHEM_LDLU(lu + 46656), b[4736], x);
       b[448] = x * CHEM_LDLU(vd + 448);
@@ -4216,6 +5811,8 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
     {
       CHEM_PREFETCH(ws + 124384);
       CHEM_PREFETCH(ws + 132064);
+      CHEM_PREFETCH_L1(ws + 124352);
+      CHEM_PREFETCH_L1(ws + 132096);
       double x = b[416];
       x = fma(-CHEM_LDLU(lu + 46688), b[4736], x);
       b[416] = x * CHEM_LDLU(vd + 416);
@@ -4223,6 +5820,8 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
     {
       CHEM_PREFETCH(ws + 124416);
       CHEM_PREFETCH(ws + 132032);
+      CHEM_PREFETCH_L1(ws + 124384);
+      CHEM_PREFETCH_L1(ws + 132064);
       double x = b[384];
       x = fma(-CHEM_LDLU(lu + 46720), b[4736], x);
       b[384] = x * CHEM_LDLU(vd + 384);
@@ -4231,6 +5830,8 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 124448);
       CHEM_PREFETCH(ws + 124480);
       CHEM_PREFETCH(ws + 132000);
+      CHEM_PREFETCH_L1(ws + 124416);
+      CHEM_PREFETCH_L1(ws + 132032);
       double x = b[352];
       x = fma(-CHEM_LDLU(lu + 46752), b[4736], x);
       b[352] = x * CHEM_LDLU(vd + 352);
@@ -4239,12 +5840,18 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
       CHEM_PREFETCH(ws + 124512);
       CHEM_PREFETCH(ws + 124544);
       CHEM_PREFETCH(ws + 131968);
+      CHEM_PREFETCH_L1(ws + 124448);
+      CHEM_PREFETCH_L1(ws + 124480);
+      CHEM_PREFETCH_L1(ws + 132000);
       double x = b[320];
       x = fma(-CHEM_LDLU(lu + 46784), b[960], x);
       b[320] = x * CHEM_LDLU(vd + 320);
     }
     {
       CHEM_PREFETCH(ws + 131936);
+      CHEM_PREFETCH_L1(ws + 124512);
+      CHEM_PREFETCH_L1(ws + 124544);
+      CHEM_PREFETCH_L1(ws + 131968);
       double x = b[288];
       x = fma(-CHEM_LDLU(lu + 46816), b[2208], x);
       x = fma(-CHEM_LDLU(lu + 46848), b[4736], x);
@@ -4252,6 +5859,7 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
     }
     {
       CHEM_PREFETCH(ws + 131904);
+      CHEM_PREFETCH_L1(ws + 131936);
       double x = b[256];
       x = fma(-CHEM_LDLU(lu + 46880), b[2208], x);
       x = fma(-CHEM_LDLU(lu + 46912), b[4736], x);
@@ -4259,35 +5867,42 @@ __device__ __noinline__ void solve_1_2(double* __restrict__ ws, int rhs)
     }
     {
       CHEM_PREFETCH(ws + 131872);
+      CHEM_PREFETCH_L1(ws + 131904);
       double x = b[224];
       b[224] = x * CHEM_LDLU(vd + 224);
     }
     {
       CHEM_PREFETCH(ws + 131840);
+      CHEM_PREFETCH_L1(ws + 131872);
       double x = b[192];
       b[192] = x * CHEM_LDLU(vd + 192);
     }
     {
       CHEM_PREFETCH(ws + 131808);
+      CHEM_PREFETCH_L1(ws + 131840);
       double x = b[160];
       b[160] = x * CHEM_LDLU(vd + 160);
     }
     {
       CHEM_PREFETCH(ws + 131776);
+      CHEM_PREFETCH_L1(ws + 131808);
       double x = b[128];
       b[128] = x * CHEM_LDLU(vd + 128);
     }
     {
       CHEM_PREFETCH(ws + 131744);
+      CHEM_PREFETCH_L1(ws + 131776);
       double x = b[96];
       b[96] = x * CHEM_LDLU(vd + 96);
     }
     {
       CHEM_PREFETCH(ws + 131712);
+      CHEM_PREFETCH_L1(ws + 131744);
       double x = b[64];
       b[64] = x * CHEM_LDLU(vd + 64);
     }
     {
+      CHEM_PREFETCH_L1(ws + 131712);
       double x = b[32];
       b[32] = x * CHEM_LDLU(vd + 32);
     }

@@ -9,6 +9,7 @@
 // singular factorisation, 16 passes), so every thread ends.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <string>
 
 #include "../../include/cmaqchem.h"
@@ -22,6 +23,7 @@ static_assert(kmt2::NPARAM == CMAQCHEM_KMT2_NPARAM && kmt2::NSTAT == CMAQCHEM_KM
 namespace {
 
 constexpr int KMT2_THREADS = 128;
+constexpr long long KMT2_LANES_PER_SM = 256;   // two 128-thread blocks per SM
 
 struct Kmt2Args {
     const double* params;
@@ -76,4 +78,44 @@ extern "C" int cmaqchem_kmt2_solve_device(long long ncell, const double* params,
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return fail(std::string("k_kmt2_cells: ") + cudaGetErrorString(e));
     return 0;
+}
+
+// Host-array form for callers without device arrays (a Fortran cloud module): the same
+// [element][cell] layouts in host memory; device buffers are allocated for the call and
+// freed before it returns, the copies are synchronous.
+extern "C" int cmaqchem_kmt2_solve(long long ncell, const double* params, const double* var_mix, double* var_out,
+                                   double* fix_out, int* stats, int device)
+{
+    if (ncell < 0) return fail("ncell must be >= 0");
+    if (ncell == 0) return 0;
+    if (!params || !var_mix || !var_out || !stats) return fail("null array argument");
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return fail(std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+    const long long lanes = std::min<long long>(ncell, (long long)(nsm > 0 ? nsm : 1) * KMT2_LANES_PER_SM);
+    const size_t n = (size_t)ncell;
+    const size_t bytes[6] = {sizeof(double) * kmt2::NPARAM * n, sizeof(double) * kmt2::NVAR * n,
+                             sizeof(double) * kmt2::NVAR * n, fix_out ? sizeof(double) * kmt2::NFIX * n : 0,
+                             sizeof(int) * kmt2::NSTAT * n,
+                             sizeof(double) * (size_t)cmaqchem_kmt2_workspace_doubles(lanes)};
+    void* d[6] = {};
+    int rc = 0;
+    for (int i = 0; i < 6 && rc == 0; ++i)
+        if (bytes[i] && (e = cudaMalloc(&d[i], bytes[i])) != cudaSuccess)
+            rc = fail(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    if (rc == 0 && ((e = cudaMemcpy(d[0], params, bytes[0], cudaMemcpyHostToDevice)) != cudaSuccess ||
+                    (e = cudaMemcpy(d[1], var_mix, bytes[1], cudaMemcpyHostToDevice)) != cudaSuccess))
+        rc = fail(std::string("copy to the device: ") + cudaGetErrorString(e));
+    if (rc == 0)
+        rc = cmaqchem_kmt2_solve_device(ncell, (const double*)d[0], (const double*)d[1], (double*)d[2],
+                                        (double*)d[3], (int*)d[4], (double*)d[5], (long long)(bytes[5] / sizeof(double)),
+                                        nullptr);
+    if (rc == 0 && ((e = cudaMemcpy(var_out, d[2], bytes[2], cudaMemcpyDeviceToHost)) != cudaSuccess ||
+                    (e = cudaMemcpy(stats, d[4], bytes[4], cudaMemcpyDeviceToHost)) != cudaSuccess ||
+                    (fix_out && (e = cudaMemcpy(fix_out, d[3], bytes[3], cudaMemcpyDeviceToHost)) != cudaSuccess)))
+        rc = fail(std::string("copy to the host: ") + cudaGetErrorString(e));
+    for (void* q : d)
+        if (q) cudaFree(q);
+    return rc;
 }

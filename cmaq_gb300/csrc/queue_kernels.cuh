@@ -46,6 +46,7 @@ __global__ void __launch_bounds__(WPB * 32, CHEM_QUEUE_WARPS_PER_SM / WPB > 0 ? 
     const long long warp = (long long)blockIdx.x * WPB + (threadIdx.x >> 5);
     double* ws = warp_ws<M>(a.ws, warp);
     ros3::CellState s;
+    s.tmark = clock64();
     long long cell = -1;
     bool sun = false;
     bool drained = false;
@@ -79,6 +80,7 @@ __global__ void __launch_bounds__(WPB * 32, CHEM_QUEUE_WARPS_PER_SM / WPB > 0 ? 
         if (LOCKSTEP) {
             if (!__syncthreads_or(busy)) break;
             night = __syncthreads_and(!busy || !sun) && a.use_night;
+            CHEM_PHASE_MARK(s, 6);
         } else {
             if (!__any_sync(0xffffffffu, busy)) break;
             night = __all_sync(0xffffffffu, !busy || !sun) && a.use_night;

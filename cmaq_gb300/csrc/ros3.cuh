@@ -59,7 +59,26 @@ struct CellState {
     bool lpass, have_f0;
     bool yave;          // accumulate the time integral of Y in ws[OFF_YAVE] (DDM-3D)
     CellStats st;
+    long long tmark;    // phase-timing builds: clock at the last phase barrier (thread 0)
 };
+
+#ifdef CHEM_PHASE_TIMING
+// Diagnostic build: thread 0 of each block adds the clock cycles between consecutive
+// phase barriers of the lock-stepped attempt to g_chem_phase_cycles[phase] (diag.cu);
+// slot 7 counts the block's attempts.
+extern __device__ unsigned long long g_chem_phase_cycles[8];
+#define CHEM_PHASE_MARK(s, i)                                                                  \
+    do {                                                                                       \
+        if (threadIdx.x == 0) {                                                                \
+            const long long t_ = clock64();                                                    \
+            atomicAdd(&g_chem_phase_cycles[i], (unsigned long long)(t_ - (s).tmark));          \
+            (s).tmark = t_;                                                                    \
+            if ((i) == 0) atomicAdd(&g_chem_phase_cycles[7], 1ull);                             \
+        }                                                                                      \
+    } while (0)
+#else
+#define CHEM_PHASE_MARK(s, i) ((void)0)
+#endif
 
 __device__ __forceinline__ void start(CellState& s)
 {
@@ -131,6 +150,7 @@ __device__ void attempt_phased(double* __restrict__ ws, CellState& s, double che
         if (night) M::explic_1(ws); else M::explic_0(ws);
     }
     if (SYNC) __syncthreads();
+    if (SYNC) CHEM_PHASE_MARK(s, 0);
     if (SYNC == 2) {
         if (night) M::jacdecomp_1_sync(ws, gdtinv, go); else M::jacdecomp_0_sync(ws, gdtinv, go);
     } else {
@@ -139,10 +159,12 @@ __device__ void attempt_phased(double* __restrict__ ws, CellState& s, double che
         }
         if (SYNC) __syncthreads();
     }
+    if (SYNC) CHEM_PHASE_MARK(s, 1);
     if (go) {   // stage 1
         for (int n = 0; n < M::NSPEC; ++n) ws[(M::OFF_K1 + n) * 32] = -ws[(M::OFF_F0 + n) * 32];
     }
     solve_phase<M, SYNC>(ws, M::OFF_K1, night, go);
+    if (SYNC) CHEM_PHASE_MARK(s, 2);
     if (go) {   // stage 2
         for (int n = 0; n < M::NSPEC; ++n)
             ws[(M::OFF_YP + n) * 32] = ws[(M::OFF_Y + n) * 32] + ws[(M::OFF_K1 + n) * 32];
@@ -153,7 +175,9 @@ __device__ void attempt_phased(double* __restrict__ ws, CellState& s, double che
             ws[(M::OFF_K2 + n) * 32] = fma(-x1, ws[(M::OFF_K1 + n) * 32], -ws[(M::OFF_YDOT + n) * 32]);
     }
     if (SYNC) __syncthreads();
+    if (SYNC) CHEM_PHASE_MARK(s, 3);
     solve_phase<M, SYNC>(ws, M::OFF_K2, night, go);
+    if (SYNC) CHEM_PHASE_MARK(s, 4);
     if (go) {   // stage 3
         const double x1 = C31 * dtinv;
         const double x2 = C32 * dtinv;
@@ -163,6 +187,7 @@ __device__ void attempt_phased(double* __restrict__ ws, CellState& s, double che
         }
     }
     solve_phase<M, SYNC>(ws, M::OFF_K3, night, go);
+    if (SYNC) CHEM_PHASE_MARK(s, 5);
     if (!go) return;
     // solution and error estimate
     double err = 0.0;

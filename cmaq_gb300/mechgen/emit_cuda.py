@@ -198,6 +198,21 @@ def cuda_sources(m: Mechanism, prog: RateProgram, sp: SparseMech, mech: str, src
                   "#else",
                   "#define CHEM_PREFETCH(p) ((void)0)",
                   "#endif",
+                  "// L1 prefetch of the entries the next row reads (build variant 'pfl1'); off by default",
+                  "#ifdef CHEM_USE_PREFETCH_L1",
+                  "__device__ __forceinline__ void chem_prefetch_l1(const double* p)",
+                  "{",
+                  '    asm volatile("prefetch.global.L1 [%0];" ::"l"(__cvta_generic_to_global(p)));',
+                  "}",
+                  "#define CHEM_PREFETCH_L1(p) chem_prefetch_l1(p)",
+                  "#else",
+                  "#define CHEM_PREFETCH_L1(p) ((void)0)",
+                  "#endif",
+                  "// 1/U(i,i): IEEE division by default; a build may use the correctly rounded",
+                  "// reciprocal __drcp_rn, which gives the same bits",
+                  "#ifndef CHEM_RCP",
+                  "#define CHEM_RCP(x) (1.0 / (x))",
+                  "#endif",
                   f"namespace {ns_name} {{", f'constexpr const char* NAME = "{mech}";']
     consts = (("NSPEC", ns), ("NRXNS", nr), ("ISCHAN", n), ("NPHOTAB", m.nphotab),
               ("NHETERO", m.nhetero), ("WS_ELEMS", lay.total), ("OFF_Y", lay.y), ("OFF_YP", lay.yp),
@@ -558,6 +573,8 @@ def _jacdecomp_chunks(m: Mechanism, sp: SparseMech, lay: Layout, d: int, gear: b
         o = [f"    {{ // row {i}"]
         if i + PREFETCH_AHEAD < n:
             o.extend(f"      CHEM_PREFETCH(ws + {e * 32});" for e in reads[i + PREFETCH_AHEAD])
+        if i + 1 < n:
+            o.extend(f"      CHEM_PREFETCH_L1(ws + {e * 32});" for e in reads[i + 1])
         nops = 0
         for j in cols:
             st = jpt[(i, j)]
@@ -604,7 +621,7 @@ def _jacdecomp_chunks(m: Mechanism, sp: SparseMech, lay: Layout, d: int, gear: b
                 nops += 1
         for (st_ij, j) in upper:
             o.append(f"      lu[{st_ij * 32}] = a{j};")
-        o.append(f"      vd[{i * 32}] = 1.0 / a{i};")
+        o.append(f"      vd[{i * 32}] = CHEM_RCP(a{i});")
         o.append("    }")
         rows_code.append((nops + len(cols), o))
     # group rows into chunks
@@ -640,12 +657,15 @@ def _solve_chunks(sp: SparseMech, lay: Layout, d: int) -> list[list[str]]:
     # rows in sweep order with the LU elements each reads
     sweep = [("L", i, [lay.lu + st for (st, _) in sp.lower[d][i]]) for i in range(n)]
     sweep += [("U", i, [lay.lu + st for (st, _) in sp.upper[d][i]] + [lay.vdiag + i]) for i in range(n - 1, -1, -1)]
-    ahead = {}
+    ahead, next1 = {}, {}
     for q in range(len(sweep) - PREFETCH_AHEAD):
         ahead[(sweep[q][0], sweep[q][1])] = sweep[q + PREFETCH_AHEAD][2]
+    for q in range(len(sweep) - 1):
+        next1[(sweep[q][0], sweep[q][1])] = sweep[q + 1][2]
 
     def pf(kind, i):
-        return [f"      CHEM_PREFETCH(ws + {e * 32});" for e in ahead.get((kind, i), [])]
+        return ([f"      CHEM_PREFETCH(ws + {e * 32});" for e in ahead.get((kind, i), [])]
+                + [f"      CHEM_PREFETCH_L1(ws + {e * 32});" for e in next1.get((kind, i), [])])
     pieces = []
     for i in range(n):
         o = ["    {"] + pf("L", i) + [f"      double x = b[{i * 32}];"]

@@ -270,6 +270,12 @@ int cmaqchem_ros3_solve_noalloc(const char* mechanism, long long ncell, double* 
 #define CMAQCHEM_KMT2_NPARAM 15
 #define CMAQCHEM_KMT2_NSTAT 10
 long long cmaqchem_kmt2_workspace_doubles(long long nlanes);
+/* The same integration on host arrays (same [element][cell] layouts; a Fortran caller
+ * passes PARAMS(N, 15), VAR_MIX(N, 161), VAR_OUT(N, 161), FIX_OUT(N, 4) or NULL, STATS(N, 10))
+ * on `device`: device buffers and the workspace are allocated for the call, the copies
+ * are synchronous.  Returns 0 or -1. */
+int cmaqchem_kmt2_solve(long long ncell, const double* params, const double* var_mix, double* var_out,
+                        double* fix_out, int* stats, int device);
 int cmaqchem_kmt2_solve_device(long long ncell, const double* params, const double* var_mix, double* var_out,
                                double* fix_out, int* stats, double* workspace, long long workspace_doubles,
                                void* stream);

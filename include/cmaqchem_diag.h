@@ -17,6 +17,14 @@ int cmaqchem_diag_fp64_peak(int device, double* tflops, double* ms);
  * 10-5000 ms), long enough for a clock sampler to record the SM clock it ran at. */
 int cmaqchem_diag_fp64_peak_long(int device, double target_ms, double* tflops, double* ms);
 
+/* Phase-timing builds (CHEM_PHASE_TIMING): clock cycles thread 0 of each block of the
+ * lock-stepped work-queue kernel spent in each phase of a ROS3 attempt, summed over blocks:
+ * out[0] f(Y) and the partial-derivative products, [1] Jacobian and LU, [2] stage 1 solve,
+ * [3] stage 2's f, [4] stage 2 solve, [5] stage 3 solve, [6] error estimate, step update and
+ * the refill of finished lanes; out[7] the number of block-attempts.  reset != 0 zeroes the
+ * counters after reading.  Returns -1 in other builds. */
+int cmaqchem_diag_phase_cycles(int device, unsigned long long* out, int reset);
+
 /* Clock cycles per link of a dependent FP64 FMA chain run by one warp with active_lanes
  * (1-32) lanes active: the latency a cell's sequential FP64 work pays per operation. */
 int cmaqchem_diag_fp64_issue(int device, int active_lanes, double* cycles_per_instruction);

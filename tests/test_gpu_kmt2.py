@@ -92,3 +92,14 @@ def test_kmt2_rejects_bad_arguments():
     rc = L.cmaqchem_kmt2_solve_device(2, C.c_void_p(x.data_ptr()), C.c_void_p(x.data_ptr()), C.c_void_p(x.data_ptr()),
                                       None, C.c_void_p(ws.data_ptr()), C.c_void_p(ws.data_ptr()), ws.numel(), None)
     assert rc == -1 and "workspace" in _lib.last_error()
+
+
+def test_kmt2_host_array_entry_equals_the_device_entry(o):
+    """cmaqchem_kmt2_solve (host arrays, copies inside the call) gives the device entry's bits."""
+    from cmaq_gb300.aqchem import aqchem_kinetics_host
+    p, v = o.synthetic_cells(37, seed=35)
+    var, fix, st = _gpu(p, v)
+    hv, hf, hs = aqchem_kinetics_host(p.T, v.T, with_fix=True)
+    assert np.array_equal(hv.T, var) and np.array_equal(hf.T, fix) and np.array_equal(hs.T, st)
+    empty = aqchem_kinetics_host(np.zeros((15, 0)), np.zeros((161, 0)))
+    assert empty[0].shape == (161, 0)
