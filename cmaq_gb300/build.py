@@ -42,7 +42,10 @@ VARIANTS = {"default": (GEN_DEFAULT, ["-DCHEM_QUEUE_WARPS_PER_SM=16"]),
             "rcp": (GEN_DEFAULT + ["-DCHEM_RCP(x)=__drcp_rn(x)"], ["-DCHEM_QUEUE_WARPS_PER_SM=16"]),
             "pfl1": (GEN_DEFAULT + ["-DCHEM_USE_PREFETCH_L1"], ["-DCHEM_QUEUE_WARPS_PER_SM=16"]),
             "rcp_pfl1": (GEN_DEFAULT + ["-DCHEM_RCP(x)=__drcp_rn(x)", "-DCHEM_USE_PREFETCH_L1"],
-                         ["-DCHEM_QUEUE_WARPS_PER_SM=16"])}
+                         ["-DCHEM_QUEUE_WARPS_PER_SM=16"]),
+            # more resident warps for lower register caps (20 warps: 4-warp blocks; 24: 8-warp blocks)
+            "r96w20": (["-maxrregcount=96", "-DCHEM_USE_PREFETCH"], ["-DCHEM_QUEUE_WARPS_PER_SM=20"]),
+            "r80w24": (["-maxrregcount=80", "-DCHEM_USE_PREFETCH"], ["-DCHEM_QUEUE_WARPS_PER_SM=24"])}
 
 
 def _is_generated_math(src: Path) -> bool:
