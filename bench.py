@@ -227,12 +227,18 @@ def split_calls(r: dict, ncell: int) -> dict:
     return out
 
 
+FP64_SHAPES = [(0, 8, 256, 8), (0, 16, 256, 4), (0, 4, 256, 8), (0, 1, 1024, 2), (0, 8, 128, 2),
+               (0, 8, 32, 4), (1, 8, 256, 8), (2, 8, 256, 8)]   # (op, chains, threads, blocks per SM)
+
+
 def fp64_peak_record(device: int) -> dict:
-    """The FP64 roofline's denominators: (1) independent FMA chains on every SM for about a
-    second, three times, with the SM clock sampled meanwhile (best TFLOP/s); (2) the
-    clock-derived rate 2 FMA per clock per SM (a one-warp clock64 probe measures one FP64
-    warp instruction per 64 cycles per SM sub-partition, 4 x 32 / 64 = 2) x 2 FLOP x SMs x
-    SM clock."""
+    """The FP64 roofline's denominator: (1) independent FMA chains on every SM for about a
+    second, three times, with the SM clock sampled meanwhile (best TFLOP/s); (2) the FP64
+    pipe's rate in lane operations per clock per SM over a sweep of kernel shapes (1-16
+    chains per thread, 4-64 warps per SM, fma / mul / add), whose saturated value times 2 FLOP
+    x SMs x the timed region's SM clock is the clock-derived peak; (3) for reference, the rate
+    a one-warp clock64 probe implies (one FP64 warp instruction per 64 cycles per SM
+    sub-partition: 4 x 32 / 64 = 2 per clock per SM), which no kernel shape reaches."""
     import torch
     from cmaq_gb300 import _lib
     nsm = torch.cuda.get_device_properties(device).multi_processor_count
@@ -241,18 +247,23 @@ def fp64_peak_record(device: int) -> dict:
         runs = [_lib.fp64_peak_long(device, 1000.0) for _ in range(3)]
     c = ck.summary()
     best = max(r[0] for r in runs)
+    sweep = {f"op{o}_ch{ch}_t{t}_b{b}": _lib.fp64_rate(device, o, ch, t, b) for o, ch, t, b in FP64_SHAPES}
     return {"measured_tflops": best, "kernel_ms": [r[1] for r in runs], "measured_sm_mhz": c.get("sm_mhz"),
             "measured_clock_samples": c.get("samples_under_load"), "measured_reasons": c.get("reasons"),
-            "sms": nsm, "fma_per_clk_per_sm": 2.0,
+            "sms": nsm, "fp64_ops_per_clk_per_sm": sweep,
+            "saturated_ops_per_clk_per_sm": max(sweep.values()),
             "measured_fma_per_clk_per_sm": None if not c.get("sm_mhz") else
-            best * 1e12 / 2.0 / nsm / (c["sm_mhz"] * 1e6)}
+            best * 1e12 / 2.0 / nsm / (c["sm_mhz"] * 1e6),
+            "issue_probe_ops_per_clk_per_sm": 2.0}
 
 
-def clock_peak(rec: dict, sm_mhz: float | None) -> float | None:
-    """2 FMA/clk/SM x 2 FLOP x SMs x clock, in TFLOP/s."""
+def clock_peak(rec: dict, sm_mhz: float | None, per_clk: float | None = None) -> float | None:
+    """FP64 ops per clock per SM (default: the saturated rate of the sweep) x 2 FLOP x SMs x
+    clock, in TFLOP/s."""
     if not sm_mhz:
         return None
-    return rec["fma_per_clk_per_sm"] * 2.0 * rec["sms"] * sm_mhz * 1e6 / 1e12
+    r = rec["saturated_ops_per_clk_per_sm"] if per_clk is None else per_clk
+    return r * 2.0 * rec["sms"] * sm_mhz * 1e6 / 1e12
 
 
 def run_accuracy(g, device: int, tuned, threads: int, tight_tol=(TIGHT_RTOL, TIGHT_ATOL), col_step: int = 46,
@@ -876,6 +887,7 @@ def main():
             achieved_tf = None
         bclk = (batched["clocks"] or {}).get("sm_mhz")
         cpk = clock_peak(peak_rec, bclk)
+        ipk = clock_peak(peak_rec, bclk, peak_rec["issue_probe_ops_per_clk_per_sm"])
         peak_tf = max(x for x in (peak_rec["measured_tflops"], cpk) if x)
         line = {
             "metric": METRIC if a.solver == "ros3" else METRIC.replace("ROS3", a.solver.upper()), "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
@@ -901,11 +913,14 @@ def main():
                                         "attempts per call",
                          "dram_gbs_from_traffic": None if traffic is None else traffic / (ms_step * 1e-3) / 1e9,
                          "peak_source": "the larger of the measured FP64 FMA-chain rate and the clock-derived "
-                                        "rate at the timed region's median SM clock (no FP64 figure in "
-                                        "MEASURED_PEAKS.json)",
+                                        "rate (the saturated FP64 ops per clock per SM of a sweep of kernel "
+                                        "shapes, at the timed region's median SM clock); no FP64 figure in "
+                                        "MEASURED_PEAKS.json",
                          "peak_measured": peak_rec, "peak_clock_derived": cpk, "timed_sm_mhz": bclk,
                          "frac_of_measured": achieved_tf / peak_rec["measured_tflops"],
                          "frac_of_clock_derived": None if not cpk else achieved_tf / cpk,
+                         "issue_probe_peak": ipk,
+                         "frac_of_issue_probe_peak": None if not ipk else achieved_tf / ipk,
                          "flops": "algorithmic FLOPs of the reference's ROS3 step per attempt x attempts",
                          "fp64_chain_cycles_per_fma": issue},
             "plain": plain,

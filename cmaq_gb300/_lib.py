@@ -76,6 +76,7 @@ def lib(variant: str = "default") -> C.CDLL:
     L.cmaqchem_diag_fp64_issue.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double)]
     L.cmaqchem_diag_fp64_peak_long.argtypes = [C.c_int, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.cmaqchem_diag_set_tuning.argtypes = [vp, C.c_char_p, C.c_int]
+    L.cmaqchem_diag_fp64_rate.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.cmaqchem_diag_phase_cycles.argtypes = [C.c_int, C.POINTER(C.c_ulonglong), C.c_int]
     L.cmaqchem_kmt2_workspace_doubles.argtypes = [C.c_longlong]
     L.cmaqchem_kmt2_workspace_doubles.restype = C.c_longlong
@@ -98,6 +99,15 @@ def fp64_peak_long(device: int = 0, target_ms: float = 1000.0) -> tuple[float, f
     if lib().cmaqchem_diag_fp64_peak_long(device, C.c_double(target_ms), C.byref(tf), C.byref(ms)) != 0:
         raise ChemError("FP64 peak measurement failed")
     return tf.value, ms.value
+
+
+def fp64_rate(device: int = 0, op: int = 0, chains: int = 8, threads: int = 256, blocks_per_sm: int = 8) -> float:
+    """FP64 lane operations per clock per SM (at the maximum SM clock) of one kernel shape
+    (op 0 fma, 1 mul, 2 add; independent chains per thread; threads; blocks per SM)."""
+    r, ms = C.c_double(), C.c_double()
+    if lib().cmaqchem_diag_fp64_rate(device, op, chains, threads, blocks_per_sm, C.byref(r), C.byref(ms)) != 0:
+        raise ChemError("FP64 rate measurement failed")
+    return r.value
 
 
 def fp64_issue(device: int = 0, active_lanes: int = 1) -> float:

@@ -136,3 +136,82 @@ extern "C" int cmaqchem_diag_phase_cycles(int device, unsigned long long* out, i
     return -1;
 #endif
 }
+
+namespace {
+
+// `chains` independent FP64 chains per thread of one kind: 0 a*b+c (DFMA), 1 a*b, 2 a+c.
+template <int CH, int OP>
+__global__ void k_fp64_kind(int iters, double b, double c, double* sink)
+{
+    double a[CH];
+#pragma unroll
+    for (int k = 0; k < CH; ++k) a[k] = (double)(threadIdx.x + k) * 1.0e-3;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < CH; ++k) {
+            if (OP == 0) a[k] = fma(a[k], b, c);
+            else if (OP == 1) a[k] = a[k] * b;
+            else a[k] = a[k] + c;
+        }
+    }
+    double t = 0.0;
+#pragma unroll
+    for (int k = 0; k < CH; ++k) t += a[k];
+    if (t == -1.2345e300) sink[threadIdx.x] = t;
+}
+
+template <int CH>
+cudaError_t launch_kind(int op, int blocks, int threads, int iters, double* sink)
+{
+    if (op == 0) k_fp64_kind<CH, 0><<<blocks, threads>>>(iters, 0.999999, 1.0e-7, sink);
+    else if (op == 1) k_fp64_kind<CH, 1><<<blocks, threads>>>(iters, 0.999999, 1.0e-7, sink);
+    else k_fp64_kind<CH, 2><<<blocks, threads>>>(iters, 0.999999, 1.0e-7, sink);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_chains(int chains, int op, int blocks, int threads, int iters, double* sink)
+{
+    switch (chains) {
+    case 1: return launch_kind<1>(op, blocks, threads, iters, sink);
+    case 2: return launch_kind<2>(op, blocks, threads, iters, sink);
+    case 4: return launch_kind<4>(op, blocks, threads, iters, sink);
+    case 8: return launch_kind<8>(op, blocks, threads, iters, sink);
+    default: return launch_kind<16>(op, blocks, threads, iters, sink);
+    }
+}
+
+}  // namespace
+
+extern "C" int cmaqchem_diag_fp64_rate(int device, int op, int chains, int threads, int blocks_per_sm,
+                                       double* ops_per_clk_per_sm, double* ms)
+{
+    if (op < 0 || op > 2 || (chains != 1 && chains != 2 && chains != 4 && chains != 8 && chains != 16)) return -1;
+    if (threads < 32 || threads > 1024 || threads % 32 != 0 || blocks_per_sm < 1 || blocks_per_sm > 32) return -1;
+    if (!ops_per_clk_per_sm) return -1;
+    if (cudaSetDevice(device) != cudaSuccess) return -1;
+    int nsm = 0, khz = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+    cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, device);
+    double* sink = nullptr;
+    if (cudaMalloc(&sink, 1024 * sizeof(double)) != cudaSuccess) return -1;
+    const int blocks = nsm * blocks_per_sm, iters = 32768 / chains;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaError_t err = launch_chains(chains, op, blocks, threads, 64, sink);   // warm-up
+    cudaEventRecord(e0);
+    if (err == cudaSuccess) err = launch_chains(chains, op, blocks, threads, iters, sink);
+    cudaEventRecord(e1);
+    if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+    float t = 0.0f;
+    cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(sink);
+    if (err != cudaSuccess || !(t > 0.0f)) return -1;
+    // lane operations per second / SMs / the device's maximum SM clock
+    const double ops = (double)chains * iters * threads * blocks;
+    *ops_per_clk_per_sm = ops / (t * 1.0e-3) / nsm / (khz * 1.0e3);
+    if (ms) *ms = t;
+    return 0;
+}

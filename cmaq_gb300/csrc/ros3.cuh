@@ -11,6 +11,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#ifdef CHEM_PHASE_TIMING
+extern __device__ unsigned long long g_chem_phase_cycles[8];
+#endif
+
 namespace ros3 {
 
 constexpr double GAM = 0.43586652150845899941601945119356;
@@ -64,16 +68,15 @@ struct CellState {
 
 #ifdef CHEM_PHASE_TIMING
 // Diagnostic build: thread 0 of each block adds the clock cycles between consecutive
-// phase barriers of the lock-stepped attempt to g_chem_phase_cycles[phase] (diag.cu);
-// slot 7 counts the block's attempts.
-extern __device__ unsigned long long g_chem_phase_cycles[8];
+// phase barriers of the lock-stepped attempt to g_chem_phase_cycles[phase] (diag.cu,
+// global namespace); slot 7 counts the block's attempts.
 #define CHEM_PHASE_MARK(s, i)                                                                  \
     do {                                                                                       \
         if (threadIdx.x == 0) {                                                                \
             const long long t_ = clock64();                                                    \
-            atomicAdd(&g_chem_phase_cycles[i], (unsigned long long)(t_ - (s).tmark));          \
+            atomicAdd(&::g_chem_phase_cycles[i], (unsigned long long)(t_ - (s).tmark));        \
             (s).tmark = t_;                                                                    \
-            if ((i) == 0) atomicAdd(&g_chem_phase_cycles[7], 1ull);                             \
+            if ((i) == 0) atomicAdd(&::g_chem_phase_cycles[7], 1ull);                           \
         }                                                                                      \
     } while (0)
 #else

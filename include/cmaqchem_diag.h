@@ -25,6 +25,13 @@ int cmaqchem_diag_fp64_peak_long(int device, double target_ms, double* tflops, d
  * counters after reading.  Returns -1 in other builds. */
 int cmaqchem_diag_phase_cycles(int device, unsigned long long* out, int reset);
 
+/* FP64 lane operations per clock per SM, at the device's maximum SM clock, of `chains`
+ * (1, 2, 4, 8 or 16) independent chains per thread of one kind (op 0: a*b+c, 1: a*b,
+ * 2: a+c), `threads` per block and `blocks_per_sm` blocks per SM; ms: the kernel time.
+ * The saturated value over the launch shapes is the FP64 pipe's rate. */
+int cmaqchem_diag_fp64_rate(int device, int op, int chains, int threads, int blocks_per_sm,
+                            double* ops_per_clk_per_sm, double* ms);
+
 /* Clock cycles per link of a dependent FP64 FMA chain run by one warp with active_lanes
  * (1-32) lanes active: the latency a cell's sequential FP64 work pays per operation. */
 int cmaqchem_diag_fp64_issue(int device, int active_lanes, double* cycles_per_instruction);

@@ -564,7 +564,8 @@ static int kq_ros_integrator(KqState* s, double* y, double tstart, double tend, 
 /* One cell: set-up, then aqchem_kmt.F90:531-543 (INTEGRATE from T to T + DT while
  * T < TEND; at most 16 passes where the reference would loop on).  var_out gets the
  * state in molec/cm3, fix_out the fixed species. */
-static int kq_cell(const double* p, const double* var_mix, double* var_out, double* fix_out, int* st, KqWork* w)
+static int kq_cell_state(const double* p, const double* var_mix, double* var_out, double* fix_out, int* st,
+                         KqWork* w, KqState* sp)
 {
     KqState s;
     memset(st, 0, sizeof(int) * KQ_NSTAT);
@@ -592,7 +593,433 @@ static int kq_cell(const double* p, const double* var_mix, double* var_out, doub
     }
     if (fix_out) memcpy(fix_out, s.fix, sizeof(s.fix));
     st[KQS_IERR] = ierr;
+    if (sp) *sp = s;
     return ierr == 1 ? 0 : 1;
+}
+
+static int kq_cell(const double* p, const double* var_mix, double* var_out, double* fix_out, int* st, KqWork* w)
+{
+    return kq_cell_state(p, var_mix, var_out, fix_out, st, w, NULL);
+}
+
+/* ------------------------------------------------------------------ the whole AQCHEM */
+/* AQCHEM's GAS array in AQ_DATA.F's srggas order (29 species, mol/molV) */
+enum { KG_SO2 = 0, KG_HNO3, KG_N2O5, KG_CO2, KG_NH3, KG_H2O2, KG_O3, KG_FOA, KG_MHP, KG_PAA, KG_H2SO4, KG_HCL,
+       KG_GLY, KG_MGLY, KG_HO, KG_IEPOX, KG_IMAE, KG_IHMML, KG_HO2, KG_NO2, KG_HONO, KG_HNO4, KG_GCOL, KG_CCOOH,
+       KG_HCHO, KG_NO3RAD, KG_CH3O2, KG_HCHOP, KG_PYRUV, KG_NGAS };
+/* positions of the aerosol surrogates AQCHEM reads or writes in the caller's AEROSOL(NAER,
+ * NMODES) list (AQ_DATA.F's LSO4, LNH4, ...); element (i, mode) is aer[i + naer * mode] */
+enum { KA_SO4 = 0, KA_NH4, KA_NO3, KA_CL, KA_NA, KA_EC, KA_POA, KA_PRI, KA_SOA, KA_NUM, KA_SOILC, KA_SEASC,
+       KA_ANTHC, KA_CAACC, KA_MGACC, KA_KACC, KA_FEACC, KA_MNACC, KA_ORGC, KA_TRACER_AKN, KA_TRACER_ACC,
+       KA_TRACER_COR, KA_PHG_AKN, KA_PHG_ACC, KA_PHG_COR, KA_IETET, KA_IEOS, KA_DIMER, KA_IMGA, KA_IMOS,
+       KA_ISO3, KA_NIDX };
+enum { KM_AKN = 0, KM_ACC, KM_COR };
+/* coarse crustal factors of aqchem_kmt.F90:329-365 (computed once by the caller) */
+enum { KF_SOIL_FE = 0, KF_CORS_FE, KF_SOIL_MN, KF_CORS_MN, KF_SEAS_NA, KF_SOIL_NA, KF_CORS_NA, KF_SEAS_MG,
+       KF_SOIL_MG, KF_CORS_MG, KF_SEAS_CA, KF_SOIL_CA, KF_CORS_CA, KF_SEAS_K, KF_SOIL_K, KF_CORS_K, KF_N };
+/* per-cell scalar outputs: HPWDEP, BETASO4, FRACTR, FRACPOA, FRACPRI, FRACSOA, and the four
+ * mass-balance percentages AQCHEM checks (S, N without NH3, NH3/NH4, Cl) */
+enum { KO_HPWDEP = 0, KO_BETASO4, KO_FRACTR, KO_FRACPOA, KO_FRACPRI, KO_FRACSOA, KO_MBAL, KO_N = KO_MBAL + 4 };
+
+/* REAL(4) EXP of the redistribution (EXP of a REAL product): the portable exp rounded to float */
+static double kq_fexp(float x) { return (double)(float)portable_exp((double)x); }
+
+/* AQCHEM (aqchem_kmt.F90:21-978) for one cloudy cell: the fractions and mass-balance start
+ * (:434-507), Initialize's mapping of GAS / AEROSOL into the KPP state (aqchem_Initialize.F90:
+ * 290-421), the set-up and integration of the kinetic core (kq_cell_state), and the
+ * redistribution into GAS, AEROSOL, GASWDEP, AERWDEP (:546-976).  gas [KG_NGAS], aer
+ * [naer * 3] in and out; gwd [KG_NGAS], awd [naer * 3], out [KO_N] out.  The GAS value of HO
+ * replaces the HO parameter.  Returns 0, or 1 when the integration or the set-up failed
+ * (set-up: every output NaN, where the reference stops the run). */
+static int kq_aqchem_cell(const double* p, double* gas, double* aer, int naer, const int* ai, const double* fac,
+                          double* gwd, double* awd, double* out, int* st, KqWork* w)
+{
+#define AER(k, m) aer[ai[k] + naer * (m)]
+#define AWD(k, m) awd[ai[k] + naer * (m)]
+    double pp[KQ_NPARAM];
+    memcpy(pp, p, sizeof(pp));
+    pp[KQP_HO] = gas[KG_HO];
+    const float taucld = (float)p[KQP_TAUCLD], alfa0 = (float)p[KQP_ALFA0], alfa3 = (float)p[KQP_ALFA3];
+    const float coszen = (float)p[KQP_COSZEN];
+    const int ispc8 = (int)p[KQP_ISPC8], mtpyrac = (int)p[KQP_MTPYRAC];
+    /* aqchem_kmt.F90:434-477: fractional weights */
+    double totnit = gas[KG_HNO3] + AER(KA_NO3, KM_ACC);
+    const double fhno3 = totnit > 0.0 ? gas[KG_HNO3] / totnit : 1.0;
+    const double fno3acc = AER(KA_NO3, KM_ACC) + AER(KA_NO3, KM_COR) > 0.0
+                               ? AER(KA_NO3, KM_ACC) / (AER(KA_NO3, KM_ACC) + AER(KA_NO3, KM_COR)) : 1.0;
+    double totamm = gas[KG_NH3] + AER(KA_NH4, KM_ACC);
+    const double fnh3 = totamm > 0.0 ? gas[KG_NH3] / totamm : 1.0;
+    const double fnh4acc = AER(KA_NH4, KM_ACC) + AER(KA_NH4, KM_COR) > 0.0
+                               ? AER(KA_NH4, KM_ACC) / (AER(KA_NH4, KM_ACC) + AER(KA_NH4, KM_COR)) : 1.0;
+    const double totcl = gas[KG_HCL] + AER(KA_CL, KM_ACC);
+    const double fhcl = totcl > 0.0 ? gas[KG_HCL] / totcl : 1.0;
+    const double fclacc = AER(KA_CL, KM_ACC) + AER(KA_CL, KM_COR) > 0.0
+                              ? AER(KA_CL, KM_ACC) / (AER(KA_CL, KM_ACC) + AER(KA_CL, KM_COR)) : 1.0;
+    (void)fhcl;
+    const int dark = coszen <= 0.0f;
+    /* :486-498: mass balance at the start */
+    const double w_s = (double)32.06f, w_n = (double)14.007f, w_cl = (double)35.5f;
+    double startm[4];
+    startm[0] = (gas[KG_SO2] + gas[KG_H2SO4]) * w_s;
+    startm[1] = (gas[KG_HNO3] + 2 * gas[KG_N2O5] + gas[KG_NO2] + gas[KG_HONO] + gas[KG_HNO4] + gas[KG_NO3RAD]) * w_n;
+    startm[2] = gas[KG_NH3] * w_n;
+    startm[3] = gas[KG_HCL] * w_cl;
+    for (int m = 0; m < 3; ++m) {
+        startm[0] = startm[0] + AER(KA_SO4, m) * w_s;
+        startm[1] = startm[1] + AER(KA_NO3, m) * w_n;
+        startm[2] = startm[2] + AER(KA_NH4, m) * w_n;
+        startm[3] = startm[3] + AER(KA_CL, m) * w_cl;
+    }
+    const double poaiinit = AER(KA_POA, KM_AKN), priiinit = AER(KA_PRI, KM_AKN);
+    const double traciinit = AER(KA_TRACER_AKN, KM_AKN), soaiinit = AER(KA_SOA, KM_AKN);
+    /* aqchem_Initialize.F90:290-421: the KPP state in mol/molV */
+    const double fe_iii = dark ? 0.9 : 0.1, mn_ii = 1.0, fe_sol = 0.1, mn_sol = 0.5;
+    double v[KQ_NVAR];
+    for (int i = 0; i < KQ_NVAR; ++i) v[i] = 0.0;
+    v[KQ_G_SO2] = gas[KG_SO2];
+    v[KQ_G_HNO3] = gas[KG_HNO3] + 2.0 * gas[KG_N2O5];
+    v[KQ_G_CO2] = gas[KG_CO2];
+    v[KQ_G_NH3] = gas[KG_NH3];
+    v[KQ_G_H2O2] = gas[KG_H2O2];
+    v[KQ_G_O3] = gas[KG_O3];
+    v[KQ_G_HCOOH] = gas[KG_FOA];
+    v[KQ_G_MHP] = gas[KG_MHP];
+    v[KQ_G_PAA] = gas[KG_PAA];
+    v[KQ_G_HCL] = gas[KG_HCL];
+    v[KQ_G_GLY] = gas[KG_GLY];
+    v[KQ_G_MGLY] = gas[KG_MGLY];
+    v[KQ_G_IEPOX] = gas[KG_IEPOX];
+    if (ispc8 > 0) {
+        v[KQ_G_IMAE] = gas[KG_IMAE];
+        v[KQ_G_IHMML] = gas[KG_IHMML];
+    }
+    v[KQ_G_NO2] = gas[KG_NO2];
+    v[KQ_G_HONO] = gas[KG_HONO];
+    v[KQ_G_HNO4] = gas[KG_HNO4];
+    v[KQ_G_NO3] = gas[KG_NO3RAD];
+    v[KQ_G_CH3O2] = gas[KG_CH3O2];
+    v[KQ_G_GCOL] = gas[KG_GCOL];
+    v[KQ_G_CCOOH] = gas[KG_CCOOH];
+    v[KQ_G_HCHO] = gas[KG_HCHO];
+    v[KQ_G_HO2] = gas[KG_HO2];
+    v[KQ_G_HCHOP] = gas[KG_HCHOP];
+    if (mtpyrac > 0) v[KQ_G_PYRAC] = gas[KG_PYRUV];
+    v[KQ_A_NO3AKN] = AER(KA_NO3, KM_AKN);
+    v[KQ_A_NH4AKN] = AER(KA_NH4, KM_AKN);
+    v[KQ_A_CLAKN] = AER(KA_CL, KM_AKN);
+    v[KQ_A_NAAKN] = AER(KA_NA, KM_AKN);
+    v[KQ_A_SO4AKN] = AER(KA_SO4, KM_AKN);
+    v[KQ_A_PECAKN] = AER(KA_EC, KM_AKN);
+    v[KQ_A_POAAKN] = AER(KA_POA, KM_AKN);
+    v[KQ_A_PRIAKN] = AER(KA_PRI, KM_AKN);
+    v[KQ_L_SO4MIN2] = AER(KA_SO4, KM_ACC) + AER(KA_SO4, KM_COR);
+    v[KQ_L_NO3MIN] = AER(KA_NO3, KM_ACC) + AER(KA_NO3, KM_COR);
+    v[KQ_L_NH4PLUS] = AER(KA_NH4, KM_ACC) + AER(KA_NH4, KM_COR);
+    v[KQ_L_CLMIN] = AER(KA_CL, KM_ACC) + AER(KA_CL, KM_COR);
+    v[KQ_L_PRIACC] = AER(KA_PRI, KM_ACC);
+    v[KQ_L_NAPLUS] = AER(KA_NA, KM_ACC);
+    v[KQ_L_CAPLUS2] = AER(KA_CAACC, KM_ACC);
+    v[KQ_L_MGPLUS2] = AER(KA_MGACC, KM_ACC);
+    v[KQ_L_KPLUS] = AER(KA_KACC, KM_ACC);
+    v[KQ_L_PECACC] = AER(KA_EC, KM_ACC);
+    v[KQ_L_ORGC] = (double)0.2f * AER(KA_ORGC, KM_ACC);
+    v[KQ_L_OXLACMIN2] = (double)0.8f * AER(KA_ORGC, KM_ACC) / (double)(90.03f / 177.0f);
+    v[KQ_L_POAACC] = AER(KA_POA, KM_ACC);
+    if (ispc8 > 0) {
+        v[KQ_L_IETET] = AER(KA_IETET, KM_ACC);
+        v[KQ_L_IEOS] = AER(KA_IEOS, KM_ACC);
+        v[KQ_L_DIMER] = AER(KA_DIMER, KM_ACC);
+        v[KQ_L_IMGA] = AER(KA_IMGA, KM_ACC);
+        v[KQ_L_IMOS] = AER(KA_IMOS, KM_ACC);
+    } else {
+        v[KQ_L_ISO3] = AER(KA_ISO3, KM_ACC);
+    }
+    v[KQ_L_SO4MIN2] = v[KQ_L_SO4MIN2] + gas[KG_H2SO4];
+    const double soilc = AER(KA_SOILC, KM_COR), anthc = AER(KA_ANTHC, KM_COR), seasc = AER(KA_SEASC, KM_COR);
+    double fecor = fac[KF_SOIL_FE] * soilc + fac[KF_CORS_FE] * anthc;
+    double mncor = fac[KF_SOIL_MN] * soilc + fac[KF_CORS_MN] * anthc;
+    double nacor = fac[KF_SEAS_NA] * seasc + fac[KF_SOIL_NA] * soilc + fac[KF_CORS_NA] * anthc;
+    double mgcor = fac[KF_SEAS_MG] * seasc + fac[KF_SOIL_MG] * soilc + fac[KF_CORS_MG] * anthc;
+    double cacor = fac[KF_SEAS_CA] * seasc + fac[KF_SOIL_CA] * soilc + fac[KF_CORS_CA] * anthc;
+    double kcor = fac[KF_SEAS_K] * seasc + fac[KF_SOIL_K] * soilc + fac[KF_CORS_K] * anthc;
+    v[KQ_L_NAPLUS] = v[KQ_L_NAPLUS] + nacor;
+    v[KQ_L_CAPLUS2] = v[KQ_L_CAPLUS2] + cacor;
+    v[KQ_L_MGPLUS2] = v[KQ_L_MGPLUS2] + mgcor;
+    v[KQ_L_KPLUS] = v[KQ_L_KPLUS] + kcor;
+    v[KQ_L_FEPLUS3] = fe_sol * fe_iii * (AER(KA_FEACC, KM_ACC) + fecor);
+    v[KQ_L_MNPLUS2] = mn_sol * mn_ii * (AER(KA_MNACC, KM_ACC) + mncor);
+    /* the kinetic core */
+    double var[KQ_NVAR];
+    KqState s;
+    const int fail = kq_cell_state(pp, v, var, NULL, st, w, &s);
+    if (st[KQS_IERR] <= -101) {   /* set-up failed: the reference stops the run */
+        for (int i = 0; i < KG_NGAS; ++i) gas[i] = gwd[i] = NAN;
+        for (int i = 0; i < naer * 3; ++i) aer[i] = awd[i] = NAN;
+        for (int i = 0; i < KO_N; ++i) out[i] = NAN;
+        return 1;
+    }
+    const double* fixv = s.fix;
+    /* :546-976: redistribution */
+    for (int i = 0; i < KG_NGAS; ++i) gwd[i] = 0.0;
+    for (int i = 0; i < naer * 3; ++i) awd[i] = 0.0;
+    const float temp2 = (float)p[KQP_TEMP2], airm = (float)p[KQP_AIRM], pres_pa = (float)p[KQP_PRES_PA];
+    const double cthk1 = (double)(airm * temp2) * 0.08206 / ((double)pres_pa / 101325.0 * 1000.0);
+    const double cfactor = s.cfactor, invcfac = 1.0 / cfactor;
+    const double wfactor = (double)(float)p[KQP_WCAVG] * cthk1 * s.phi2;
+    const double expwet = portable_exp(-s.wetfac * (double)taucld);
+    const double ex0 = kq_fexp(-alfa0 * taucld), ex3 = kq_fexp(-alfa3 * taucld);
+    AER(KA_NO3, KM_AKN) = var[KQ_A_NO3AKN] * invcfac;
+    AER(KA_NH4, KM_AKN) = var[KQ_A_NH4AKN] * invcfac;
+    AER(KA_CL, KM_AKN) = var[KQ_A_CLAKN] * invcfac;
+    AER(KA_NA, KM_AKN) = var[KQ_A_NAAKN] * invcfac;
+    AER(KA_SO4, KM_AKN) = var[KQ_A_SO4AKN] * invcfac;
+    AER(KA_EC, KM_AKN) = var[KQ_A_PECAKN] * invcfac;
+    AER(KA_POA, KM_AKN) = var[KQ_A_POAAKN] * invcfac;
+    AER(KA_PRI, KM_AKN) = var[KQ_A_PRIAKN] * invcfac;
+    AER(KA_NUM, KM_AKN) = AER(KA_NUM, KM_AKN) * ex0;
+    AER(KA_TRACER_ACC, KM_ACC) = AER(KA_TRACER_ACC, KM_ACC) + AER(KA_TRACER_AKN, KM_AKN) * (1.0 - ex3);
+    AER(KA_PHG_ACC, KM_ACC) = AER(KA_PHG_ACC, KM_ACC) + AER(KA_PHG_AKN, KM_AKN) * (1.0 - ex3);
+    AER(KA_TRACER_AKN, KM_AKN) = AER(KA_TRACER_AKN, KM_AKN) * ex3;
+    AER(KA_PHG_AKN, KM_AKN) = AER(KA_PHG_AKN, KM_AKN) * ex3;
+    AWD(KA_TRACER_ACC, KM_ACC) = AER(KA_TRACER_ACC, KM_ACC) * (1.0 - expwet) * cfactor;
+    AWD(KA_PHG_ACC, KM_ACC) = AER(KA_PHG_ACC, KM_ACC) * (1.0 - expwet) * cfactor;
+    AWD(KA_TRACER_COR, KM_COR) = AER(KA_TRACER_COR, KM_COR) * (1.0 - expwet) * cfactor;
+    AWD(KA_PHG_COR, KM_COR) = AER(KA_PHG_COR, KM_COR) * (1.0 - expwet) * cfactor;
+    AER(KA_TRACER_ACC, KM_ACC) = AER(KA_TRACER_ACC, KM_ACC) * expwet;
+    AER(KA_PHG_ACC, KM_ACC) = AER(KA_PHG_ACC, KM_ACC) * expwet;
+    AER(KA_TRACER_COR, KM_COR) = AER(KA_TRACER_COR, KM_COR) * expwet;
+    AER(KA_PHG_COR, KM_COR) = AER(KA_PHG_COR, KM_COR) * expwet;
+    AER(KA_SOA, KM_ACC) = AER(KA_SOA, KM_ACC) + AER(KA_SOA, KM_AKN) * (1.0 - ex3);
+    AER(KA_SOA, KM_AKN) = AER(KA_SOA, KM_AKN) * ex3;
+    AWD(KA_SOA, KM_ACC) = AER(KA_SOA, KM_ACC) * (1.0 - expwet) * cfactor;
+    AER(KA_SOA, KM_ACC) = AER(KA_SOA, KM_ACC) * expwet;
+    AWD(KA_SOILC, KM_COR) = AER(KA_SOILC, KM_COR) * (1.0 - expwet) * cfactor;
+    AWD(KA_SEASC, KM_COR) = AER(KA_SEASC, KM_COR) * (1.0 - expwet) * cfactor;
+    AWD(KA_ANTHC, KM_COR) = AER(KA_ANTHC, KM_COR) * (1.0 - expwet) * cfactor;
+    AWD(KA_SO4, KM_COR) = AER(KA_SO4, KM_COR) * (1.0 - expwet) * cfactor;
+    AWD(KA_NH4, KM_COR) = AER(KA_NH4, KM_COR) * (1.0 - expwet) * cfactor;
+    AWD(KA_NO3, KM_COR) = AER(KA_NO3, KM_COR) * (1.0 - expwet) * cfactor;
+    AWD(KA_CL, KM_COR) = AER(KA_CL, KM_COR) * (1.0 - expwet) * cfactor;
+    AER(KA_NUM, KM_COR) = AER(KA_NUM, KM_COR) * expwet;
+    AER(KA_SOILC, KM_COR) = AER(KA_SOILC, KM_COR) * expwet;
+    AER(KA_SEASC, KM_COR) = AER(KA_SEASC, KM_COR) * expwet;
+    AER(KA_ANTHC, KM_COR) = AER(KA_ANTHC, KM_COR) * expwet;
+    AER(KA_SO4, KM_COR) = AER(KA_SO4, KM_COR) * expwet;
+    AER(KA_NH4, KM_COR) = AER(KA_NH4, KM_COR) * expwet;
+    AER(KA_NO3, KM_COR) = AER(KA_NO3, KM_COR) * expwet;
+    AER(KA_CL, KM_COR) = AER(KA_CL, KM_COR) * expwet;
+    const double wsoil = AWD(KA_SOILC, KM_COR), wanth = AWD(KA_ANTHC, KM_COR), wseas = AWD(KA_SEASC, KM_COR);
+    const double wdfecor = fac[KF_SOIL_FE] * wsoil + fac[KF_CORS_FE] * wanth;
+    const double wdmncor = fac[KF_SOIL_MN] * wsoil + fac[KF_CORS_MN] * wanth;
+    const double wdnacor = fac[KF_SEAS_NA] * wseas + fac[KF_SOIL_NA] * wsoil + fac[KF_CORS_NA] * wanth;
+    const double wdmgcor = fac[KF_SEAS_MG] * wseas + fac[KF_SOIL_MG] * wsoil + fac[KF_CORS_MG] * wanth;
+    const double wdcacor = fac[KF_SEAS_CA] * wseas + fac[KF_SOIL_CA] * wsoil + fac[KF_CORS_CA] * wanth;
+    const double wdkcor = fac[KF_SEAS_K] * wseas + fac[KF_SOIL_K] * wsoil + fac[KF_CORS_K] * wanth;
+    AWD(KA_FEACC, KM_ACC) = fmax((var[KQ_WD_FEPLUS3] / fe_iii / fe_sol) - wdfecor, 0.0);
+    AWD(KA_MNACC, KM_ACC) = fmax((var[KQ_WD_MNPLUS2] / mn_ii / mn_sol) - wdmncor, 0.0);
+    AWD(KA_NA, KM_ACC) = fmax(var[KQ_WD_NAPLUS] - wdnacor, 0.0);
+    AWD(KA_CAACC, KM_ACC) = fmax(var[KQ_WD_CAPLUS2] - wdcacor, 0.0);
+    AWD(KA_MGACC, KM_ACC) = fmax(var[KQ_WD_MGPLUS2] - wdmgcor, 0.0);
+    AWD(KA_KACC, KM_ACC) = fmax(var[KQ_WD_KPLUS] - wdkcor, 0.0);
+    AWD(KA_SO4, KM_ACC) = fmax(var[KQ_WD_H2SO4] - AWD(KA_SO4, KM_COR), 0.0);
+    AWD(KA_NH4, KM_ACC) = fmax(var[KQ_WD_NH4PLUS] - AWD(KA_NH4, KM_COR), 0.0);
+    AWD(KA_NO3, KM_ACC) = fmax(var[KQ_WD_NO3MIN] - AWD(KA_NO3, KM_COR), 0.0);
+    AWD(KA_CL, KM_ACC) = fmax(var[KQ_WD_CLMIN] - AWD(KA_CL, KM_COR), 0.0);
+    AWD(KA_PRI, KM_ACC) = var[KQ_WD_PRIACC];
+    AWD(KA_EC, KM_ACC) = var[KQ_WD_PECACC];
+    AWD(KA_ORGC, KM_ACC) = var[KQ_WD_ORGC];
+    AWD(KA_POA, KM_ACC) = var[KQ_WD_POAACC];
+    if (ispc8 > 0) {
+        AWD(KA_IETET, KM_ACC) = var[KQ_WD_IETET];
+        AWD(KA_IEOS, KM_ACC) = var[KQ_WD_IEOS];
+        AWD(KA_DIMER, KM_ACC) = var[KQ_WD_DIMER];
+        AWD(KA_IMGA, KM_ACC) = var[KQ_WD_IMGA];
+        AWD(KA_IMOS, KM_ACC) = var[KQ_WD_IMOS];
+    } else {
+        AWD(KA_ISO3, KM_ACC) = var[KQ_WD_IETET];
+    }
+    if (AWD(KA_NH4, KM_COR) > var[KQ_WD_NH4PLUS]) {
+        AWD(KA_NH4, KM_COR) = (1.0 - fnh4acc) * var[KQ_WD_NH4PLUS];
+        AWD(KA_NH4, KM_ACC) = fnh4acc * var[KQ_WD_NH4PLUS];
+        AER(KA_NH4, KM_COR) = (1.0 - fnh4acc) * (var[KQ_L_NH4OH] + var[KQ_L_NH4PLUS]) * invcfac;
+    }
+    if (AWD(KA_NO3, KM_COR) > var[KQ_WD_NO3MIN]) {
+        AWD(KA_NO3, KM_COR) = (1.0 - fno3acc) * var[KQ_WD_NO3MIN];
+        AWD(KA_NO3, KM_ACC) = fno3acc * var[KQ_WD_NO3MIN];
+        AER(KA_NO3, KM_COR) = (1.0 - fno3acc) * (var[KQ_L_HNO3] + var[KQ_L_NO3MIN]) * invcfac;
+    }
+    if (AWD(KA_CL, KM_COR) > var[KQ_WD_CLMIN]) {
+        AWD(KA_CL, KM_COR) = (1.0 - fclacc) * var[KQ_WD_CLMIN];
+        AWD(KA_CL, KM_ACC) = fclacc * var[KQ_WD_CLMIN];
+        AER(KA_CL, KM_COR) = (1.0 - fclacc) * var[KQ_L_CLMIN] * invcfac;
+    }
+    AER(KA_PRI, KM_ACC) = var[KQ_L_PRIACC] * invcfac;
+    AER(KA_EC, KM_ACC) = var[KQ_L_PECACC] * invcfac;
+    AER(KA_ORGC, KM_ACC) = var[KQ_L_ORGC] * invcfac;
+    AER(KA_POA, KM_ACC) = var[KQ_L_POAACC] * invcfac;
+    out[KO_FRACTR] = AER(KA_TRACER_ACC, KM_ACC) > 0.0
+        ? fmin(((traciinit - AER(KA_TRACER_AKN, KM_AKN)) * expwet) / AER(KA_TRACER_ACC, KM_ACC), 1.0) : 0.0;
+    out[KO_FRACPOA] = AER(KA_POA, KM_ACC) > 0.0
+        ? fmin(((poaiinit - AER(KA_POA, KM_AKN)) * expwet) / AER(KA_POA, KM_ACC), 1.0) : 0.0;
+    out[KO_FRACPRI] = AER(KA_PRI, KM_ACC) > 0.0
+        ? fmin(((priiinit - AER(KA_PRI, KM_AKN)) * expwet) / AER(KA_PRI, KM_ACC), 1.0) : 0.0;
+    out[KO_FRACSOA] = AER(KA_SOA, KM_ACC) > 0.0
+        ? fmin(((soaiinit - AER(KA_SOA, KM_AKN)) * expwet) / AER(KA_SOA, KM_ACC), 1.0) : 0.0;
+    if (ispc8 > 0) {
+        AER(KA_IETET, KM_ACC) = var[KQ_L_IETET] * invcfac;
+        AER(KA_IEOS, KM_ACC) = var[KQ_L_IEOS] * invcfac;
+        AER(KA_DIMER, KM_ACC) = var[KQ_L_DIMER] * invcfac;
+        AER(KA_IMGA, KM_ACC) = var[KQ_L_IMGA] * invcfac;
+        AER(KA_IMOS, KM_ACC) = var[KQ_L_IMOS] * invcfac;
+    } else {
+        AER(KA_ISO3, KM_ACC) = (var[KQ_L_ISO3]) * invcfac;
+    }
+    const double soilc2 = AER(KA_SOILC, KM_COR), anthc2 = AER(KA_ANTHC, KM_COR), seasc2 = AER(KA_SEASC, KM_COR);
+    fecor = fac[KF_SOIL_FE] * soilc2 + fac[KF_CORS_FE] * anthc2;
+    mncor = fac[KF_SOIL_MN] * soilc2 + fac[KF_CORS_MN] * anthc2;
+    nacor = fac[KF_SEAS_NA] * seasc2 + fac[KF_SOIL_NA] * soilc2 + fac[KF_CORS_NA] * anthc2;
+    mgcor = fac[KF_SEAS_MG] * seasc2 + fac[KF_SOIL_MG] * soilc2 + fac[KF_CORS_MG] * anthc2;
+    cacor = fac[KF_SEAS_CA] * seasc2 + fac[KF_SOIL_CA] * soilc2 + fac[KF_CORS_CA] * anthc2;
+    kcor = fac[KF_SEAS_K] * seasc2 + fac[KF_SOIL_K] * soilc2 + fac[KF_CORS_K] * anthc2;
+    AER(KA_FEACC, KM_ACC) = fmax((var[KQ_L_FEPLUS3] / fe_iii / fe_sol - fecor * cfactor) * invcfac, 0.0);
+    AER(KA_MNACC, KM_ACC) = fmax((var[KQ_L_MNPLUS2] / mn_ii / mn_sol - mncor * cfactor) * invcfac, 0.0);
+    AER(KA_NA, KM_ACC) = fmax((var[KQ_L_NAPLUS] - nacor * cfactor) * invcfac, 0.0);
+    AER(KA_CAACC, KM_ACC) = fmax((var[KQ_L_CAPLUS2] - cacor * cfactor) * invcfac, 0.0);
+    AER(KA_MGACC, KM_ACC) = fmax((var[KQ_L_MGPLUS2] - mgcor * cfactor) * invcfac, 0.0);
+    AER(KA_KACC, KM_ACC) = fmax((var[KQ_L_KPLUS] - kcor * cfactor) * invcfac, 0.0);
+    AER(KA_SO4, KM_ACC) = fmax(((var[KQ_L_H2SO4] + var[KQ_L_SO4MIN2] + var[KQ_L_HSO4MIN]) * invcfac)
+                               - AER(KA_SO4, KM_COR), 0.0);
+    AER(KA_CL, KM_ACC) = fmax((var[KQ_L_CLMIN] * invcfac) - AER(KA_CL, KM_COR), 0.0);
+    totamm = var[KQ_G_NH3] + var[KQ_L_NH4OH] + var[KQ_L_NH4PLUS] - AER(KA_NH4, KM_COR) * cfactor;
+    totnit = var[KQ_G_HNO3] + var[KQ_L_HNO3] + var[KQ_L_NO3MIN] - AER(KA_NO3, KM_COR) * cfactor;
+    totamm = fmax(totamm, 0.0);
+    totnit = fmax(totnit, 0.0);
+    AER(KA_NO3, KM_ACC) = ((1.0 - fhno3) * totnit) * invcfac;
+    AER(KA_NH4, KM_ACC) = ((1.0 - fnh3) * totamm) * invcfac;
+    const double oliggly = 0.0 * 3.3e-1, oligmgly = 0.0 * 1.9e-1;   /* OLIG = 0 (aqchem_kmt.F90:412) */
+    gas[KG_SO2] = (var[KQ_G_SO2] + var[KQ_L_SO2] + var[KQ_L_HSO3MIN] + var[KQ_L_SO3MIN2] + var[KQ_L_HMSMIN]
+                   + var[KQ_L_SO3MIN] + var[KQ_L_SO5MIN] + var[KQ_L_HSO5MIN] + var[KQ_L_SO4MIN]) * invcfac;
+    gas[KG_N2O5] = 0.0;
+    gas[KG_CO2] = (var[KQ_G_CO2] + var[KQ_L_H2CO3] + var[KQ_L_HCO3MIN] + var[KQ_L_CO3MIN2] + var[KQ_L_CO2MIN])
+                  * invcfac;
+    gas[KG_H2O2] = (var[KQ_G_H2O2] + var[KQ_L_H2O2]) * invcfac;
+    gas[KG_O3] = (var[KQ_G_O3] + var[KQ_L_O3]) * invcfac;
+    gas[KG_FOA] = (var[KQ_G_HCOOH] + var[KQ_L_HCOOH] + var[KQ_L_HCOOMIN]) * invcfac;
+    gas[KG_MHP] = (var[KQ_G_MHP] + var[KQ_L_MHP]) * invcfac;
+    gas[KG_PAA] = (var[KQ_G_PAA] + var[KQ_L_PAA]) * invcfac;
+    gas[KG_H2SO4] = 0.0;
+    gas[KG_HCL] = (var[KQ_G_HCL] + var[KQ_L_HCL]) * invcfac;
+    gas[KG_GLY] = (var[KQ_G_GLY] + var[KQ_L_GLY] * (1.0 - oliggly)) * invcfac;
+    gas[KG_MGLY] = (var[KQ_G_MGLY] + var[KQ_L_MGLY] * (1.0 - oligmgly)) * invcfac;
+    gas[KG_HNO3] = (fhno3 * totnit) * invcfac;
+    gas[KG_NH3] = (fnh3 * totamm) * invcfac;
+    gas[KG_HO] = (fixv[KQ_G_HO - KQ_NVAR]) * invcfac;
+    gas[KG_IEPOX] = (var[KQ_G_IEPOX] + var[KQ_L_IEPOX]) * invcfac;
+    if (ispc8 > 0) {
+        gas[KG_IMAE] = (var[KQ_G_IMAE] + var[KQ_L_IMAE]) * invcfac;
+        gas[KG_IHMML] = (var[KQ_G_IHMML] + var[KQ_L_IHMML]) * invcfac;
+    }
+    gas[KG_HO2] = (var[KQ_G_HO2] + var[KQ_L_HO2] + var[KQ_L_O2MIN]) * invcfac;
+    gas[KG_NO2] = (var[KQ_G_NO2] + var[KQ_L_NO2]) * invcfac;
+    gas[KG_HONO] = (var[KQ_G_HONO] + var[KQ_L_HONO] + var[KQ_L_NO2MIN]) * invcfac;
+    gas[KG_HNO4] = (var[KQ_G_HNO4] + var[KQ_L_HNO4] + var[KQ_L_NO4MIN]) * invcfac;
+    gas[KG_NO3RAD] = (var[KQ_G_NO3] + var[KQ_L_NO3]) * invcfac;
+    gas[KG_CH3O2] = (var[KQ_G_CH3O2] + var[KQ_L_CH3O2]) * invcfac;
+    gas[KG_CCOOH] = (var[KQ_G_CCOOH] + var[KQ_L_CCOOH] + var[KQ_L_CCOOHMIN]) * invcfac;
+    gas[KG_HCHO] = (var[KQ_G_HCHO] + var[KQ_L_CH2OHYD] + var[KQ_L_HCHO] + var[KQ_L_HMSMIN]) * invcfac;
+    gas[KG_GCOL] = (var[KQ_G_GCOL] + var[KQ_L_GCOL]) * invcfac;
+    gas[KG_HCHOP] = (var[KQ_G_HCHOP] + var[KQ_L_CH2OHYDP] + var[KQ_L_HCHOP] + var[KQ_L_HMSMINP]) * invcfac;
+    gwd[KG_SO2] = var[KQ_WD_SO2];
+    gwd[KG_HNO3] = var[KQ_WD_HNO3];
+    gwd[KG_N2O5] = 0.0;
+    gwd[KG_CO2] = var[KQ_WD_CO2];
+    gwd[KG_NH3] = var[KQ_WD_NH4OH];
+    gwd[KG_H2O2] = var[KQ_WD_H2O2];
+    gwd[KG_O3] = var[KQ_WD_O3];
+    gwd[KG_FOA] = var[KQ_WD_HCOOH];
+    gwd[KG_MHP] = var[KQ_WD_MHP];
+    gwd[KG_PAA] = var[KQ_WD_PAA];
+    gwd[KG_H2SO4] = 0.0;
+    gwd[KG_HCL] = var[KQ_WD_HCL];
+    gwd[KG_GLY] = var[KQ_WD_GLY] * (1.0 - oliggly);
+    gwd[KG_MGLY] = var[KQ_WD_MGLY] * (1.0 - oligmgly);
+    gwd[KG_HO] = var[KQ_WD_HO];
+    gwd[KG_IEPOX] = var[KQ_WD_IEPOX];
+    if (ispc8 > 0) {
+        gwd[KG_IMAE] = var[KQ_WD_IMAE];
+        gwd[KG_IHMML] = var[KQ_WD_IHMML];
+    }
+    gwd[KG_NO2] = var[KQ_WD_NO2];
+    gwd[KG_HONO] = var[KQ_WD_HONO];
+    gwd[KG_HNO4] = var[KQ_WD_HNO4];
+    gwd[KG_NO3RAD] = var[KQ_WD_NO3];
+    gwd[KG_CH3O2] = var[KQ_WD_CH3O2];
+    gwd[KG_GCOL] = var[KQ_WD_GCOL];
+    gwd[KG_CCOOH] = var[KQ_WD_CCOOH];
+    gwd[KG_HCHO] = var[KQ_WD_CH2OHYD];
+    gwd[KG_HO2] = var[KQ_WD_HO2];
+    gwd[KG_HCHOP] = var[KQ_WD_CH2OHYDP];
+    double apyrac = 0.0, wdpyrac = 0.0;
+    if (mtpyrac > 0) {
+        gas[KG_PYRUV] = (var[KQ_G_PYRAC] + var[KQ_L_PYRAC]) * invcfac;
+        gwd[KG_PYRUV] = var[KQ_WD_PYRAC];
+        wdpyrac = 0.0;
+        apyrac = var[KQ_L_PYRACMIN];
+    } else {
+        wdpyrac = var[KQ_WD_PYRAC];
+        apyrac = var[KQ_L_PYRAC] + var[KQ_L_PYRACMIN];
+    }
+    const double r7404 = (double)(74.04f / 177.0f), r9003 = (double)(90.03f / 177.0f);
+    const double r8806 = (double)(88.06f / 177.0f), r7605 = (double)(76.05f / 177.0f);
+    const double r5804 = (double)(58.04f / 177.0f), r7206 = (double)(72.06f / 177.0f);
+    AER(KA_ORGC, KM_ACC) = (var[KQ_L_ORGC] + (r7404 * var[KQ_L_GLYAC]) + (r9003 * var[KQ_L_OXLAC])
+                            + (r9003 * var[KQ_L_OXLACMIN]) + (r9003 * var[KQ_L_OXLACMIN2]) + (r8806 * apyrac)
+                            + (r7605 * var[KQ_L_GCOLAC]) + (r7404 * var[KQ_L_GLYACMIN])
+                            + (r7605 * var[KQ_L_GCOLACMIN])
+                            + r5804 * oliggly * var[KQ_L_GLY] + r7206 * oligmgly * var[KQ_L_MGLY]) * invcfac;
+    AWD(KA_ORGC, KM_ACC) = var[KQ_WD_ORGC] + (r7404 * var[KQ_WD_GLYAC]) + (r9003 * var[KQ_WD_OXLAC])
+                           + (r8806 * wdpyrac) + (r7605 * var[KQ_WD_GCOLAC])
+                           + r5804 * oliggly * var[KQ_WD_GLY] + r7206 * oligmgly * var[KQ_WD_MGLY];
+    for (int i = 0; i < KG_NGAS; ++i) gwd[i] = gwd[i] * wfactor;
+    for (int i = 0; i < naer * 3; ++i) awd[i] = awd[i] * wfactor;
+    for (int i = 0; i < KG_NGAS; ++i) {
+        if (gas[i] < 0.0) gas[i] = 0.0;
+        if (gwd[i] < 0.0) gwd[i] = 0.0;
+    }
+    for (int i = 0; i < naer * 3; ++i) {
+        if (aer[i] < 0.0) aer[i] = 0.0;
+        if (awd[i] < 0.0) awd[i] = 0.0;
+    }
+    out[KO_HPWDEP] = (double)(float)(var[KQ_WD_HPLUS] * wfactor);   /* HPWDEP is REAL */
+    const double depsum = AWD(KA_SO4, KM_ACC) / wfactor;
+    const double betaso4 = AER(KA_SO4, KM_ACC) * cfactor + depsum > 0.0
+                               ? depsum / (AER(KA_SO4, KM_ACC) * cfactor + depsum) / (double)taucld : 0.0;
+    out[KO_BETASO4] = betaso4;
+    AER(KA_NUM, KM_ACC) = AER(KA_NUM, KM_ACC) * portable_exp(-betaso4 * (double)taucld);
+    /* :919-973: mass balance at the end */
+    double endm[4];
+    endm[0] = (gas[KG_SO2] + gas[KG_H2SO4] + (gwd[KG_SO2] + gwd[KG_H2SO4]) / wfactor / cfactor) * w_s;
+    endm[1] = (gas[KG_HNO3] + 2 * gas[KG_N2O5] + gas[KG_NO2] + gas[KG_HONO] + gas[KG_HNO4] + gas[KG_NO3RAD]
+               + (gwd[KG_HNO3] + gwd[KG_NO2] + gwd[KG_HONO] + gwd[KG_HNO4] + gwd[KG_NO3RAD]) / wfactor / cfactor)
+              * w_n;
+    endm[2] = (gas[KG_NH3] + gwd[KG_NH3] / wfactor / cfactor) * w_n;
+    endm[3] = (gas[KG_HCL] + gwd[KG_HCL] / wfactor / cfactor) * w_cl;
+    for (int m = 0; m < 3; ++m) {
+        endm[0] = endm[0] + AER(KA_SO4, m) * w_s;
+        endm[1] = endm[1] + AER(KA_NO3, m) * w_n;
+        endm[2] = endm[2] + AER(KA_NH4, m) * w_n;
+        endm[3] = endm[3] + AER(KA_CL, m) * w_cl;
+    }
+    for (int m = 0; m < 3; ++m) {
+        endm[0] = endm[0] + (AWD(KA_SO4, m) / wfactor / cfactor) * w_s;
+        endm[1] = endm[1] + (AWD(KA_NO3, m) / wfactor / cfactor) * w_n;
+        endm[2] = endm[2] + (AWD(KA_NH4, m) / wfactor / cfactor) * w_n;
+        endm[3] = endm[3] + (AWD(KA_CL, m) / wfactor / cfactor) * w_cl;
+    }
+    for (int i = 0; i < 4; ++i) out[KO_MBAL + i] = startm[i] > 0.0 ? 100 * (startm[i] - endm[i]) / startm[i] : 0.0;
+    return fail;
+#undef AER
+#undef AWD
 }
 
 /* ------------------------------------------------------------------ exports */
@@ -694,6 +1121,27 @@ int oracle_kq_cells(long long ncell, const double* params, const double* var_mix
         for (long long c = 0; c < ncell; ++c)
             nfail += kq_cell(&params[c * KQ_NPARAM], &var_mix[c * KQ_NVAR], &var_out[c * KQ_NVAR],
                              fix_out ? &fix_out[c * KQ_NFIX] : NULL, &stats[c * KQ_NSTAT], &w);
+    }
+    return nfail;
+}
+
+/* AQCHEM for ncell cells: params [ncell][KQ_NPARAM]; gas [ncell][29] and aer [ncell][naer * 3]
+ * in and out; aer_index [31] positions of the surrogates in the caller's aerosol list;
+ * factors [16]; gas_wdep [ncell][29], aer_wdep [ncell][naer * 3], out [ncell][10], stats
+ * [ncell][KQ_NSTAT] out.  Returns the number of cells that did not finish. */
+int oracle_kq_aqchem_cells(long long ncell, const double* params, double* gas, double* aer, int naer,
+                           const int* aer_index, const double* factors, double* gas_wdep, double* aer_wdep,
+                           double* out, int* stats, int threads)
+{
+    int nfail = 0;
+#pragma omp parallel num_threads(threads > 0 ? threads : 1) reduction(+ : nfail)
+    {
+        static __thread KqWork w;
+#pragma omp for schedule(dynamic, 1)
+        for (long long c = 0; c < ncell; ++c)
+            nfail += kq_aqchem_cell(&params[c * KQ_NPARAM], &gas[c * KG_NGAS], &aer[c * naer * 3], naer, aer_index,
+                                    factors, &gas_wdep[c * KG_NGAS], &aer_wdep[c * naer * 3], &out[c * KO_N],
+                                    &stats[c * KQ_NSTAT], &w);
     }
     return nfail;
 }

@@ -12,10 +12,12 @@ grid, checked two ways on the GPU:
   CCTM/src/ddm3d/DDM3D_CHEM.F:155-511), for NOx and VOC emissions over an hour that
   follows a 1-hour spin-up.  Emissions enter between the chemistry calls, as VDIFF adds
   them (E * DT into CGRID, and DT into the emitted species' row of SENGRID for the
-  parameter); the adjoint side chains twelve one-step windows with the same injection.
-  DDM-3D's once-per-step Crank-Nicolson update is an approximation of its own (the CPU
-  oracle measured 4e-5 to 1.4e-3 against the adjoint for these parameters); tolerance
-  2e-2.
+  parameter); the adjoint side chains one-step windows with the same injection.  DDM-3D
+  linearises each synchronisation step once, at the step's time-averaged concentrations
+  (a Crank-Nicolson-type update), so a pulse of emitted NO that reacts away within the
+  step is followed less accurately the longer the step: measured 3.8 % for the NO
+  parameter with 5-minute steps; the test uses 1-minute steps (TSTEP(2) = 000100, 60
+  CHEM calls) and a tolerance of 2e-2.
 """
 import numpy as np
 import pytest
@@ -91,8 +93,10 @@ def test_emission_gradients_match_gpu_ddm3d():
     names = [sp["name"] for sp in manifest(sub.mech)["species"]]
     emitted = ["NO", "NO2"] + [v for v in ("FORM", "ISOP") if v in names]
     slots = [int(sub.cgrid_index[names.index(v)]) - 1 for v in emitted]
-    dt = 5.0                                                    # minutes per synchronisation step
-    e_rate = 2e-6                                               # ppm/min of each emitted species
+    dt = 1.0                                                    # minutes per synchronisation step
+    nstep = 60
+    tstep = (10000, 100, 100)                                   # TSTEP(2) = 000100: one minute
+    e_rate = 1e-6                                               # ppm/min of each emitted species
     dev = {k: torch.from_numpy(np.ascontiguousarray(getattr(sub, k))).cuda()
            for k in ("conc", "ta", "qv", "dens", "pres", "seaice", "ocean_szone", "rj", "khetero")}
     args = [dev[k] for k in ("conc", "ta", "qv", "dens", "pres", "seaice", "ocean_szone", "rj", "khetero")]
@@ -105,15 +109,15 @@ def test_emission_gradients_match_gpu_ddm3d():
     # DDM-3D on the GPU: parameter p = the emission rate of species emitted[p] in every cell
     nparam = len(emitted)
     sen = torch.zeros((sub.nspcsd, nparam) + tuple(dev["conc"].shape[1:]), dtype=torch.float32, device="cuda")
-    for _ in range(12):
+    for _ in range(nstep):
         for p, slot in enumerate(slots):
             dev["conc"][slot] += e_rate * dt                    # VDIFF adds E * DT
             sen[slot, p] += dt                                  # and DT to the parameter's own species
-        s.step_ddm(sen, *args)
+        s.step_ddm(sen, *args, tstep=tstep)
     io3_slot = int(sub.cgrid_index[names.index("O3")]) - 1
     ddm = sen[io3_slot].reshape(nparam, -1).sum(dim=1).double().cpu().numpy()
     s.close()
-    # the adjoint of the same hour: twelve one-step windows, the injection before each
+    # the adjoint of the same hour: one-step windows, the injection before each
     n = sub.ncell
     ss = ChemSolver(sub.mech, ncols=n, nrows=1, nlays=1, nspcsd=sub.nspcsd, rtol=1e-3, atol=1e-9)
     gs = ChemSolver(sub.mech, ncols=sub.ncols, nrows=sub.nrows, nlays=sub.nlays, nspcsd=sub.nspcsd,
@@ -123,7 +127,7 @@ def test_emission_gradients_match_gpu_ddm3d():
     rows = [ss.iold2new[names.index(v)] for v in emitted]
     rate = torch.full((nparam,), e_rate, dtype=torch.float64, device="cuda", requires_grad=True)
     y = y1
-    for _ in range(12):
+    for _ in range(nstep):
         inj = torch.zeros_like(y1)
         inj = inj.index_put((torch.tensor(rows, device="cuda"),), (rate * dt)[:, None].expand(nparam, n),
                             accumulate=True)
@@ -131,5 +135,5 @@ def test_emission_gradients_match_gpu_ddm3d():
     y[ss.iold2new[names.index("O3")]].sum().backward()
     adj = rate.grad.cpu().numpy()
     ss.close()
-    for p in range(nparam):
-        assert abs(adj[p] - ddm[p]) <= 2e-2 * abs(adj[p]), (emitted[p], adj[p], ddm[p])
+    rel = np.abs(adj - ddm) / np.abs(adj)
+    assert (rel <= 2e-2).all(), list(zip(emitted, adj, ddm, rel))
