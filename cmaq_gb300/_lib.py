@@ -82,6 +82,7 @@ def lib(variant: str = "default") -> C.CDLL:
     L.cmaqchem_kmt2_workspace_doubles.restype = C.c_longlong
     L.cmaqchem_kmt2_solve_device.argtypes = [C.c_longlong, vp, vp, vp, vp, vp, vp, C.c_longlong, vp]
     L.cmaqchem_kmt2_solve.argtypes = [C.c_longlong, vp, vp, vp, vp, vp, C.c_int]
+    L.cmaqchem_aqchem_device.argtypes = [C.c_longlong, vp, vp, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, C.c_longlong, vp]
     return L
 
 

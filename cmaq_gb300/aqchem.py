@@ -76,3 +76,50 @@ def aqchem_kinetics_host(params, var_mix, *, device: int = 0, with_fix: bool = F
         p = lambda a: None if a is None else C.c_void_p(a.ctypes.data)
         _lib.check(L.cmaqchem_kmt2_solve(n, p(params), p(var_mix), p(var_out), p(fix_out), p(stats), int(device)))
     return (var_out, fix_out, stats) if with_fix else (var_out, stats)
+
+
+NGAS, NSURROGATE, NFACTOR, NOUT = 29, 31, 16, 10
+OUTS = ("hpwdep", "betaso4", "fractr", "fracpoa", "fracpri", "fracsoa", "mbal_s", "mbal_n", "mbal_nh4", "mbal_cl")
+
+
+def aqchem(params: torch.Tensor, gas: torch.Tensor, aerosol: torch.Tensor, aer_index, factors, *,
+           lanes: int | None = None, stream: torch.cuda.Stream | None = None):
+    """The whole AQCHEM (mapping of GAS and AEROSOL into the KPP state, the kinetic core,
+    redistribution; include/cmaqchem.h: cmaqchem_aqchem_device) for n cloudy cells.
+    ``params`` [15][n], ``gas`` [29][n] and ``aerosol`` [naer * 3][n] float64 CUDA tensors
+    (gas and aerosol are updated in place, as AQCHEM's INOUT arguments); ``aer_index`` the
+    31 rows of AQCHEM's surrogates in the aerosol list, ``factors`` the 16 coarse crustal
+    factors (the manifest's ``crustal_factors`` for the repository's mechanism).  Returns
+    (gas_wdep [29][n], aer_wdep [naer * 3][n], out [10][n] (``OUTS``), stats [10][n])."""
+    import numpy as np
+    for name, t, rows in (("params", params, NPARAM), ("gas", gas, NGAS), ("aerosol", aerosol, None)):
+        ok = t.is_cuda and t.dtype == torch.float64 and t.dim() == 2 and t.is_contiguous()
+        if not ok or (rows is not None and t.shape[0] != rows):
+            raise ValueError(f"{name} must be a contiguous float64 CUDA tensor of shape ({rows or 'naer*3'}, n)")
+    n = params.shape[1]
+    if gas.shape[1] != n or aerosol.shape[1] != n or aerosol.shape[0] % 3:
+        raise ValueError("params, gas and aerosol must describe the same cells; aerosol has naer * 3 rows")
+    naer = aerosol.shape[0] // 3
+    idx = np.ascontiguousarray(aer_index, dtype=np.int32)
+    fac = np.ascontiguousarray(factors, dtype=np.float64)
+    if idx.shape != (NSURROGATE,) or fac.shape != (NFACTOR,):
+        raise ValueError(f"aer_index needs {NSURROGATE} entries and factors {NFACTOR}")
+    dev = params.device
+    gwd = torch.empty_like(gas)
+    awd = torch.empty_like(aerosol)
+    out = torch.empty((NOUT, n), dtype=torch.float64, device=dev)
+    stats = torch.zeros((len(STATS), n), dtype=torch.int32, device=dev)
+    if n == 0:
+        return gwd, awd, out, stats
+    L = _lib.lib()
+    if lanes is None:
+        lanes = torch.cuda.get_device_properties(dev).multi_processor_count * LANES_PER_SM
+    lanes = max(1, min(int(lanes), n))
+    ws = torch.empty(L.cmaqchem_kmt2_workspace_doubles(lanes), dtype=torch.float64, device=dev)
+    s = stream or torch.cuda.current_stream(dev)
+    with torch.cuda.device(dev):
+        _lib.check(L.cmaqchem_aqchem_device(n, _ptr(params), _ptr(gas), _ptr(aerosol), naer,
+                                            C.c_void_p(idx.ctypes.data), C.c_void_p(fac.ctypes.data), _ptr(gwd),
+                                            _ptr(awd), _ptr(out), _ptr(stats), _ptr(ws), ws.numel(),
+                                            C.c_void_p(s.cuda_stream)))
+    return gwd, awd, out, stats

@@ -19,6 +19,8 @@ __attribute__((visibility("hidden"))) void cmaqchem_set_error(const std::string&
 
 static_assert(kmt2::NVAR == CMAQCHEM_KMT2_NVAR && kmt2::NFIX == CMAQCHEM_KMT2_NFIX, "KMT2 sizes");
 static_assert(kmt2::NPARAM == CMAQCHEM_KMT2_NPARAM && kmt2::NSTAT == CMAQCHEM_KMT2_NSTAT, "KMT2 layout");
+static_assert(kmt2::KG_NGAS == CMAQCHEM_AQ_NGAS && kmt2::KA_NIDX == CMAQCHEM_AQ_NSURROGATE, "AQCHEM layout");
+static_assert(kmt2::KF_N == CMAQCHEM_AQ_NFACTOR && kmt2::KO_N == CMAQCHEM_AQ_NOUT, "AQCHEM layout");
 
 namespace {
 
@@ -44,6 +46,32 @@ __global__ void __launch_bounds__(KMT2_THREADS) k_kmt2_cells(Kmt2Args a)
     for (long long c = lane; c < a.ncell; c += a.nlanes)
         kmt2::kq_cell(a.params + c, a.var_mix + c, a.var_out + c, a.fix_out ? a.fix_out + c : nullptr, a.stats + c,
                       a.ncell, ws, a.nlanes);
+}
+
+struct AqchemArgs {
+    const double* params;
+    double* gas;
+    double* aer;
+    double* gas_wdep;
+    double* aer_wdep;
+    double* out;
+    int* stats;
+    double* ws;
+    long long ncell;
+    long long nlanes;
+    int naer;
+    int ai[kmt2::KA_NIDX];
+    double fac[kmt2::KF_N];
+};
+
+__global__ void __launch_bounds__(KMT2_THREADS) k_aqchem_cells(AqchemArgs a)
+{
+    const long long lane = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (lane >= a.nlanes) return;
+    double* ws = a.ws + lane;
+    for (long long c = lane; c < a.ncell; c += a.nlanes)
+        kmt2::kq_aqchem_cell(a.params + c, a.gas + c, a.aer + c, a.naer, a.ai, a.fac, a.gas_wdep + c, a.aer_wdep + c,
+                             a.out + c, a.stats + c, a.ncell, ws, a.nlanes);
 }
 
 int fail(const std::string& msg)
@@ -118,4 +146,47 @@ extern "C" int cmaqchem_kmt2_solve(long long ncell, const double* params, const 
     for (void* q : d)
         if (q) cudaFree(q);
     return rc;
+}
+
+// The whole AQCHEM for a batch of cloudy cells: GAS / AEROSOL in, the KPP state, the kinetic
+// core, GAS / AEROSOL / wet deposition out (include/cmaqchem.h: cmaqchem_aqchem_device).
+extern "C" int cmaqchem_aqchem_device(long long ncell, const double* params, double* gas, double* aerosol, int naer,
+                                      const int* aer_index, const double* factors, double* gas_wdep,
+                                      double* aer_wdep, double* out, int* stats, double* workspace,
+                                      long long workspace_doubles, void* stream)
+{
+    if (ncell < 0) return fail("ncell must be >= 0");
+    if (ncell == 0) return 0;
+    if (!params || !gas || !aerosol || !aer_index || !factors || !gas_wdep || !aer_wdep || !out || !stats ||
+        !workspace)
+        return fail("null array argument");
+    if (naer < 1) return fail("naer must be >= 1");
+    AqchemArgs a{};
+    for (int i = 0; i < kmt2::KA_NIDX; ++i) {
+        if (aer_index[i] < 0 || aer_index[i] >= naer) return fail("aer_index entry outside [0, naer)");
+        a.ai[i] = aer_index[i];
+    }
+    for (int i = 0; i < kmt2::KF_N; ++i) a.fac[i] = factors[i];
+    long long nlanes = workspace_doubles / kmt2::WS_ELEMS;
+    if (nlanes < 1) return fail("workspace smaller than one lane (cmaqchem_kmt2_workspace_doubles(1) doubles)");
+    if (nlanes > ncell) nlanes = ncell;
+    const long long blocks = (nlanes + KMT2_THREADS - 1) / KMT2_THREADS;
+    if (blocks > 0x7fffffffLL) return fail("too many lanes");
+    a.params = params;
+    a.gas = gas;
+    a.aer = aerosol;
+    a.gas_wdep = gas_wdep;
+    a.aer_wdep = aer_wdep;
+    a.out = out;
+    a.stats = stats;
+    a.ws = workspace;
+    a.ncell = ncell;
+    a.nlanes = nlanes;
+    a.naer = naer;
+    cudaStream_t s = (cudaStream_t)stream;
+    k_aqchem_cells<<<(unsigned)blocks, KMT2_THREADS, 0, s>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail(std::string("k_aqchem_cells: ") + cudaGetErrorString(e));
+    return 0;
 }

@@ -267,11 +267,12 @@ KQ_HD inline float kq_hlconst(float a, float e, float temp)
 #include "gen/kmt2_aq.cuh"
 
 // ----------------------------------------------------------------------------- set-up
-// AQCHEM before the integration; y, f, r are the lane's workspace arrays.  Returns 0, or
-// -1 for the reference's MET DATA ERROR (aqchem_kmt.F90:427-431), -2 for its initial pH
-// error (aqchem_Initialize.F90:476-481).
-KQ_HD KQ_NOINLINE int kq_setup(Cell& c, const double* p, long long n, const double* vmix, double* y, double* f, double* r,
-                          long long s)
+// AQCHEM before the integration; y, f, r are the lane's workspace arrays, vmix (stride vn)
+// the KPP state as Initialize maps it, ho the gas-phase OH.  Returns 0, or -1 for the
+// reference's MET DATA ERROR (aqchem_kmt.F90:427-431), -2 for its initial pH error
+// (aqchem_Initialize.F90:476-481).
+KQ_HD KQ_NOINLINE int kq_setup(Cell& c, const double* p, long long n, const double* vmix, long long vn, double ho,
+                               double* y, double* f, double* r, long long s)
 {
     const float temp2 = (float)p[P_TEMP2 * n], pres_pa = (float)p[P_PRES_PA * n];
     const float taucld = (float)p[P_TAUCLD * n], prcrate = (float)p[P_PRCRATE * n];
@@ -300,10 +301,10 @@ KQ_HD KQ_NOINLINE int kq_setup(Cell& c, const double* p, long long n, const doub
     c.invphi2 = 1.0 / c.phi2;
     c.czen = (double)(float)p[P_COSZEN * n];
     c.cfactor = (double)pres_pa / (c.temp_kpp * (double)8.314510f) * 6.0221413e17;
-    for (int i = 0; i < NVAR; ++i) y[i * s] = c.cfactor * vmix[i * n];
+    for (int i = 0; i < NVAR; ++i) y[i * s] = c.cfactor * vmix[i * vn];
     for (int i = 0; i < NFIX; ++i) f[i * s] = c.cfactor * 0.0;
     f[L_H2O * s] = 55.5 * c.invphi2;
-    f[G_HO * s] = p[P_HO * n] * c.cfactor;
+    f[G_HO * s] = ho * c.cfactor;
     f[L_O2 * s] = (double)0.21f * c.press * 1.3e-3 * kq_exp(1500.0 * c.delinvt) * c.invphi2;
     const double kw = 1.00e-14 * kq_exp(-6.955e+03 * c.delinvt);
     double pos = 2.0 * (y[L_CAPLUS2 * s] + y[L_MGPLUS2 * s]) + y[L_NAPLUS * s] + y[L_KPLUS * s] + y[L_NH4PLUS * s];
@@ -447,24 +448,16 @@ KQ_HD inline int kq_integrate(Cell& c, double* ws, long long s, double tstart, d
     return 1;
 }
 
-// One cloudy cell: set-up, AQCHEM's integration loop, the state (molec/cm3) to vout and
-// the fixed species to fout (if given); statistics to st[S_* * n].  A cell whose set-up
-// fails (IERR -101, -102) gets NaN in vout and fout.  Returns 0 when the integration
-// finished.
-KQ_HD inline int kq_cell(const double* p, const double* vmix, double* vout, double* fout, int* st_out, long long n,
-                         double* ws, long long s)
+// The kinetic core of one cell: set-up and AQCHEM's integration loop (aqchem_kmt.F90:
+// 529-543, at most 16 passes); the state stays in the workspace (Y, F).  Statistics to
+// st[S_*]; returns IERR (1 = success, -101 / -102 for a failed set-up).
+KQ_HD inline int kq_core(Cell& c, const double* p, long long n, const double* vmix, long long vn, double ho,
+                         double* ws, long long s, long long* st)
 {
-    Cell c;
-    long long st[NSTAT];
     for (int i = 0; i < NSTAT; ++i) st[i] = 0;
-    double* y = ws + W_Y * s;
-    double* f = ws + W_F * s;
-    int ierr = kq_setup(c, p, n, vmix, y, f, ws + W_R * s, s);
-    if (ierr != 0) {   // no state to return: NaN marks the cell's outputs
+    int ierr = kq_setup(c, p, n, vmix, vn, ho, ws + W_Y * s, ws + W_F * s, ws + W_R * s, s);
+    if (ierr != 0) {
         ierr -= 100;
-        for (int i = 0; i < NVAR; ++i) vout[i * n] = NAN;
-        if (fout)
-            for (int i = 0; i < NFIX; ++i) fout[i * n] = NAN;
     } else {
         double t = 0.0;
         ierr = 1;
@@ -479,13 +472,455 @@ KQ_HD inline int kq_cell(const double* p, const double* vmix, double* vout, doub
             t = texit;
             if (ierr < 0 && texit <= 0.0) break;
         }
+    }
+    st[S_IERR] = ierr;
+    return ierr;
+}
+
+// One cloudy cell: set-up, AQCHEM's integration loop, the state (molec/cm3) to vout and
+// the fixed species to fout (if given); statistics to st[S_* * n].  A cell whose set-up
+// fails (IERR -101, -102) gets NaN in vout and fout.  Returns 0 when the integration
+// finished.
+KQ_HD inline int kq_cell(const double* p, const double* vmix, double* vout, double* fout, int* st_out, long long n,
+                         double* ws, long long s)
+{
+    Cell c;
+    long long st[NSTAT];
+    const int ierr = kq_core(c, p, n, vmix, n, p[P_HO * n], ws, s, st);
+    const double* y = ws + W_Y * s;
+    const double* f = ws + W_F * s;
+    if (ierr <= -101) {   // no state to return: NaN marks the cell's outputs
+        for (int i = 0; i < NVAR; ++i) vout[i * n] = NAN;
+        if (fout)
+            for (int i = 0; i < NFIX; ++i) fout[i * n] = NAN;
+    } else {
         for (int i = 0; i < NVAR; ++i) vout[i * n] = y[i * s];
         if (fout)
             for (int i = 0; i < NFIX; ++i) fout[i * n] = f[i * s];
     }
-    st[S_IERR] = ierr;
     for (int i = 0; i < NSTAT; ++i) st_out[i * n] = (int)st[i];
     return ierr == 1 ? 0 : 1;
+}
+
+// ----------------------------------------------------------------------------- the whole AQCHEM
+// AQCHEM's GAS array in AQ_DATA.F's srggas order (29 species, mol/molV)
+enum { KG_SO2 = 0, KG_HNO3, KG_N2O5, KG_CO2, KG_NH3, KG_H2O2, KG_O3, KG_FOA, KG_MHP, KG_PAA, KG_H2SO4, KG_HCL,
+       KG_GLY, KG_MGLY, KG_HO, KG_IEPOX, KG_IMAE, KG_IHMML, KG_HO2, KG_NO2, KG_HONO, KG_HNO4, KG_GCOL, KG_CCOOH,
+       KG_HCHO, KG_NO3RAD, KG_CH3O2, KG_HCHOP, KG_PYRUV, KG_NGAS };
+// positions (in the caller's AEROSOL(NAER, NMODES) list) of the surrogates AQCHEM reads or
+// writes: AQ_DATA.F's LSO4, LNH4, ...; element (i, mode) is aer[(i + naer * mode) * n]
+enum { KA_SO4 = 0, KA_NH4, KA_NO3, KA_CL, KA_NA, KA_EC, KA_POA, KA_PRI, KA_SOA, KA_NUM, KA_SOILC, KA_SEASC,
+       KA_ANTHC, KA_CAACC, KA_MGACC, KA_KACC, KA_FEACC, KA_MNACC, KA_ORGC, KA_TRACER_AKN, KA_TRACER_ACC,
+       KA_TRACER_COR, KA_PHG_AKN, KA_PHG_ACC, KA_PHG_COR, KA_IETET, KA_IEOS, KA_DIMER, KA_IMGA, KA_IMOS,
+       KA_ISO3, KA_NIDX };
+enum { KM_AKN = 0, KM_ACC, KM_COR };
+// coarse crustal factors of aqchem_kmt.F90:329-365 (computed once by the caller)
+enum { KF_SOIL_FE = 0, KF_CORS_FE, KF_SOIL_MN, KF_CORS_MN, KF_SEAS_NA, KF_SOIL_NA, KF_CORS_NA, KF_SEAS_MG,
+       KF_SOIL_MG, KF_CORS_MG, KF_SEAS_CA, KF_SOIL_CA, KF_CORS_CA, KF_SEAS_K, KF_SOIL_K, KF_CORS_K, KF_N };
+// per-cell scalar outputs: HPWDEP, BETASO4, FRACTR, FRACPOA, FRACPRI, FRACSOA and the four
+// mass-balance percentages AQCHEM checks (S, N without NH3, NH3 / NH4, Cl)
+enum { KO_HPWDEP = 0, KO_BETASO4, KO_FRACTR, KO_FRACPOA, KO_FRACPRI, KO_FRACSOA, KO_MBAL, KO_N = KO_MBAL + 4 };
+
+// REAL(4) EXP of the redistribution (EXP of a REAL product): the portable exp rounded to float
+KQ_HD inline double kq_fexp(float x) { return (double)(float)kq_exp((double)x); }
+
+// AQCHEM (aqchem_kmt.F90:21-978) for one cloudy cell: the fractions and mass-balance start
+// (:434-507), Initialize's mapping of GAS / AEROSOL into the KPP state (aqchem_Initialize.F90:
+// 290-421, into the workspace's YNEW), the kinetic core (kq_core), and the redistribution
+// into GAS, AEROSOL, GASWDEP, AERWDEP (:546-976).  gas [KG_NGAS] and aer [naer * 3] (stride
+// n) in and out; gwd, awd, out [KO_N], st_out [NSTAT] out.  GAS's HO is the OH the
+// set-up reads (the parameter row is not).  Returns 0, or 1 when the integration or the
+// set-up failed (set-up: every output NaN, where the reference stops the run).
+KQ_HD inline int kq_aqchem_cell(const double* p, double* gas, double* aer, int naer, const int* ai,
+                                const double* fac, double* gwd, double* awd, double* out, int* st_out, long long n,
+                                double* ws, long long s)
+{
+#define AER(k, m) aer[(long long)(ai[k] + naer * (m)) * n]
+#define AWD(k, m) awd[(long long)(ai[k] + naer * (m)) * n]
+    const double ho = gas[KG_HO * n];
+    const float taucld = (float)p[P_TAUCLD * n], alfa0 = (float)p[P_ALFA0 * n], alfa3 = (float)p[P_ALFA3 * n];
+    const float coszen = (float)p[P_COSZEN * n];
+    const int ispc8 = (int)p[P_ISPC8 * n], mtpyrac = (int)p[P_MTPYRAC * n];
+    /* aqchem_kmt.F90:434-477: fractional weights */
+    double totnit = gas[KG_HNO3 * n] + AER(KA_NO3, KM_ACC);
+    const double fhno3 = totnit > 0.0 ? gas[KG_HNO3 * n] / totnit : 1.0;
+    const double fno3acc = AER(KA_NO3, KM_ACC) + AER(KA_NO3, KM_COR) > 0.0
+                               ? AER(KA_NO3, KM_ACC) / (AER(KA_NO3, KM_ACC) + AER(KA_NO3, KM_COR)) : 1.0;
+    double totamm = gas[KG_NH3 * n] + AER(KA_NH4, KM_ACC);
+    const double fnh3 = totamm > 0.0 ? gas[KG_NH3 * n] / totamm : 1.0;
+    const double fnh4acc = AER(KA_NH4, KM_ACC) + AER(KA_NH4, KM_COR) > 0.0
+                               ? AER(KA_NH4, KM_ACC) / (AER(KA_NH4, KM_ACC) + AER(KA_NH4, KM_COR)) : 1.0;
+    const double totcl = gas[KG_HCL * n] + AER(KA_CL, KM_ACC);
+    const double fhcl = totcl > 0.0 ? gas[KG_HCL * n] / totcl : 1.0;
+    const double fclacc = AER(KA_CL, KM_ACC) + AER(KA_CL, KM_COR) > 0.0
+                              ? AER(KA_CL, KM_ACC) / (AER(KA_CL, KM_ACC) + AER(KA_CL, KM_COR)) : 1.0;
+    (void)fhcl;
+    const int dark = coszen <= 0.0f;
+    /* :486-498: mass balance at the start */
+    const double w_s = (double)32.06f, w_n = (double)14.007f, w_cl = (double)35.5f;
+    double startm[4];
+    startm[0] = (gas[KG_SO2 * n] + gas[KG_H2SO4 * n]) * w_s;
+    startm[1] = (gas[KG_HNO3 * n] + 2 * gas[KG_N2O5 * n] + gas[KG_NO2 * n] + gas[KG_HONO * n] + gas[KG_HNO4 * n] + gas[KG_NO3RAD * n]) * w_n;
+    startm[2] = gas[KG_NH3 * n] * w_n;
+    startm[3] = gas[KG_HCL * n] * w_cl;
+    for (int m = 0; m < 3; ++m) {
+        startm[0] = startm[0] + AER(KA_SO4, m) * w_s;
+        startm[1] = startm[1] + AER(KA_NO3, m) * w_n;
+        startm[2] = startm[2] + AER(KA_NH4, m) * w_n;
+        startm[3] = startm[3] + AER(KA_CL, m) * w_cl;
+    }
+    const double poaiinit = AER(KA_POA, KM_AKN), priiinit = AER(KA_PRI, KM_AKN);
+    const double traciinit = AER(KA_TRACER_AKN, KM_AKN), soaiinit = AER(KA_SOA, KM_AKN);
+    /* aqchem_Initialize.F90:290-421: the KPP state in mol/molV */
+    const double fe_iii = dark ? 0.9 : 0.1, mn_ii = 1.0, fe_sol = 0.1, mn_sol = 0.5;
+    double* v = ws + W_YNEW * s;   // Initialize's VAR before the unit conversion
+    for (int i = 0; i < NVAR; ++i) v[i * s] = 0.0;
+    v[G_SO2 * s] = gas[KG_SO2 * n];
+    v[G_HNO3 * s] = gas[KG_HNO3 * n] + 2.0 * gas[KG_N2O5 * n];
+    v[G_CO2 * s] = gas[KG_CO2 * n];
+    v[G_NH3 * s] = gas[KG_NH3 * n];
+    v[G_H2O2 * s] = gas[KG_H2O2 * n];
+    v[G_O3 * s] = gas[KG_O3 * n];
+    v[G_HCOOH * s] = gas[KG_FOA * n];
+    v[G_MHP * s] = gas[KG_MHP * n];
+    v[G_PAA * s] = gas[KG_PAA * n];
+    v[G_HCL * s] = gas[KG_HCL * n];
+    v[G_GLY * s] = gas[KG_GLY * n];
+    v[G_MGLY * s] = gas[KG_MGLY * n];
+    v[G_IEPOX * s] = gas[KG_IEPOX * n];
+    if (ispc8 > 0) {
+        v[G_IMAE * s] = gas[KG_IMAE * n];
+        v[G_IHMML * s] = gas[KG_IHMML * n];
+    }
+    v[G_NO2 * s] = gas[KG_NO2 * n];
+    v[G_HONO * s] = gas[KG_HONO * n];
+    v[G_HNO4 * s] = gas[KG_HNO4 * n];
+    v[G_NO3 * s] = gas[KG_NO3RAD * n];
+    v[G_CH3O2 * s] = gas[KG_CH3O2 * n];
+    v[G_GCOL * s] = gas[KG_GCOL * n];
+    v[G_CCOOH * s] = gas[KG_CCOOH * n];
+    v[G_HCHO * s] = gas[KG_HCHO * n];
+    v[G_HO2 * s] = gas[KG_HO2 * n];
+    v[G_HCHOP * s] = gas[KG_HCHOP * n];
+    if (mtpyrac > 0) v[G_PYRAC * s] = gas[KG_PYRUV * n];
+    v[A_NO3AKN * s] = AER(KA_NO3, KM_AKN);
+    v[A_NH4AKN * s] = AER(KA_NH4, KM_AKN);
+    v[A_CLAKN * s] = AER(KA_CL, KM_AKN);
+    v[A_NAAKN * s] = AER(KA_NA, KM_AKN);
+    v[A_SO4AKN * s] = AER(KA_SO4, KM_AKN);
+    v[A_PECAKN * s] = AER(KA_EC, KM_AKN);
+    v[A_POAAKN * s] = AER(KA_POA, KM_AKN);
+    v[A_PRIAKN * s] = AER(KA_PRI, KM_AKN);
+    v[L_SO4MIN2 * s] = AER(KA_SO4, KM_ACC) + AER(KA_SO4, KM_COR);
+    v[L_NO3MIN * s] = AER(KA_NO3, KM_ACC) + AER(KA_NO3, KM_COR);
+    v[L_NH4PLUS * s] = AER(KA_NH4, KM_ACC) + AER(KA_NH4, KM_COR);
+    v[L_CLMIN * s] = AER(KA_CL, KM_ACC) + AER(KA_CL, KM_COR);
+    v[L_PRIACC * s] = AER(KA_PRI, KM_ACC);
+    v[L_NAPLUS * s] = AER(KA_NA, KM_ACC);
+    v[L_CAPLUS2 * s] = AER(KA_CAACC, KM_ACC);
+    v[L_MGPLUS2 * s] = AER(KA_MGACC, KM_ACC);
+    v[L_KPLUS * s] = AER(KA_KACC, KM_ACC);
+    v[L_PECACC * s] = AER(KA_EC, KM_ACC);
+    v[L_ORGC * s] = (double)0.2f * AER(KA_ORGC, KM_ACC);
+    v[L_OXLACMIN2 * s] = (double)0.8f * AER(KA_ORGC, KM_ACC) / (double)(90.03f / 177.0f);
+    v[L_POAACC * s] = AER(KA_POA, KM_ACC);
+    if (ispc8 > 0) {
+        v[L_IETET * s] = AER(KA_IETET, KM_ACC);
+        v[L_IEOS * s] = AER(KA_IEOS, KM_ACC);
+        v[L_DIMER * s] = AER(KA_DIMER, KM_ACC);
+        v[L_IMGA * s] = AER(KA_IMGA, KM_ACC);
+        v[L_IMOS * s] = AER(KA_IMOS, KM_ACC);
+    } else {
+        v[L_ISO3 * s] = AER(KA_ISO3, KM_ACC);
+    }
+    v[L_SO4MIN2 * s] = v[L_SO4MIN2 * s] + gas[KG_H2SO4 * n];
+    const double soilc = AER(KA_SOILC, KM_COR), anthc = AER(KA_ANTHC, KM_COR), seasc = AER(KA_SEASC, KM_COR);
+    double fecor = fac[KF_SOIL_FE] * soilc + fac[KF_CORS_FE] * anthc;
+    double mncor = fac[KF_SOIL_MN] * soilc + fac[KF_CORS_MN] * anthc;
+    double nacor = fac[KF_SEAS_NA] * seasc + fac[KF_SOIL_NA] * soilc + fac[KF_CORS_NA] * anthc;
+    double mgcor = fac[KF_SEAS_MG] * seasc + fac[KF_SOIL_MG] * soilc + fac[KF_CORS_MG] * anthc;
+    double cacor = fac[KF_SEAS_CA] * seasc + fac[KF_SOIL_CA] * soilc + fac[KF_CORS_CA] * anthc;
+    double kcor = fac[KF_SEAS_K] * seasc + fac[KF_SOIL_K] * soilc + fac[KF_CORS_K] * anthc;
+    v[L_NAPLUS * s] = v[L_NAPLUS * s] + nacor;
+    v[L_CAPLUS2 * s] = v[L_CAPLUS2 * s] + cacor;
+    v[L_MGPLUS2 * s] = v[L_MGPLUS2 * s] + mgcor;
+    v[L_KPLUS * s] = v[L_KPLUS * s] + kcor;
+    v[L_FEPLUS3 * s] = fe_sol * fe_iii * (AER(KA_FEACC, KM_ACC) + fecor);
+    v[L_MNPLUS2 * s] = mn_sol * mn_ii * (AER(KA_MNACC, KM_ACC) + mncor);
+    /* the kinetic core */
+    Cell c;
+    long long st[NSTAT];
+    const int ierr = kq_core(c, p, n, v, s, ho, ws, s, st);
+    for (int i = 0; i < NSTAT; ++i) st_out[i * n] = (int)st[i];
+    if (ierr <= -101) {   /* set-up failed: the reference stops the run */
+        for (int i = 0; i < KG_NGAS; ++i) gas[i * n] = gwd[i * n] = NAN;
+        for (int i = 0; i < naer * 3; ++i) aer[i * n] = awd[i * n] = NAN;
+        for (int i = 0; i < KO_N; ++i) out[i * n] = NAN;
+        return 1;
+    }
+    const double* y = ws + W_Y * s;
+    const double* f = ws + W_F * s;
+    /* :546-976: redistribution */
+    for (int i = 0; i < KG_NGAS; ++i) gwd[i * n] = 0.0;
+    for (int i = 0; i < naer * 3; ++i) awd[i * n] = 0.0;
+    const float temp2 = (float)p[P_TEMP2 * n], airm = (float)p[P_AIRM * n], pres_pa = (float)p[P_PRES_PA * n];
+    const double cthk1 = (double)(airm * temp2) * 0.08206 / ((double)pres_pa / 101325.0 * 1000.0);
+    const double cfactor = c.cfactor, invcfac = 1.0 / cfactor;
+    const double wfactor = (double)(float)p[P_WCAVG * n] * cthk1 * c.phi2;
+    const double expwet = kq_exp(-c.wetfac * (double)taucld);
+    const double ex0 = kq_fexp(-alfa0 * taucld), ex3 = kq_fexp(-alfa3 * taucld);
+    AER(KA_NO3, KM_AKN) = y[A_NO3AKN * s] * invcfac;
+    AER(KA_NH4, KM_AKN) = y[A_NH4AKN * s] * invcfac;
+    AER(KA_CL, KM_AKN) = y[A_CLAKN * s] * invcfac;
+    AER(KA_NA, KM_AKN) = y[A_NAAKN * s] * invcfac;
+    AER(KA_SO4, KM_AKN) = y[A_SO4AKN * s] * invcfac;
+    AER(KA_EC, KM_AKN) = y[A_PECAKN * s] * invcfac;
+    AER(KA_POA, KM_AKN) = y[A_POAAKN * s] * invcfac;
+    AER(KA_PRI, KM_AKN) = y[A_PRIAKN * s] * invcfac;
+    AER(KA_NUM, KM_AKN) = AER(KA_NUM, KM_AKN) * ex0;
+    AER(KA_TRACER_ACC, KM_ACC) = AER(KA_TRACER_ACC, KM_ACC) + AER(KA_TRACER_AKN, KM_AKN) * (1.0 - ex3);
+    AER(KA_PHG_ACC, KM_ACC) = AER(KA_PHG_ACC, KM_ACC) + AER(KA_PHG_AKN, KM_AKN) * (1.0 - ex3);
+    AER(KA_TRACER_AKN, KM_AKN) = AER(KA_TRACER_AKN, KM_AKN) * ex3;
+    AER(KA_PHG_AKN, KM_AKN) = AER(KA_PHG_AKN, KM_AKN) * ex3;
+    AWD(KA_TRACER_ACC, KM_ACC) = AER(KA_TRACER_ACC, KM_ACC) * (1.0 - expwet) * cfactor;
+    AWD(KA_PHG_ACC, KM_ACC) = AER(KA_PHG_ACC, KM_ACC) * (1.0 - expwet) * cfactor;
+    AWD(KA_TRACER_COR, KM_COR) = AER(KA_TRACER_COR, KM_COR) * (1.0 - expwet) * cfactor;
+    AWD(KA_PHG_COR, KM_COR) = AER(KA_PHG_COR, KM_COR) * (1.0 - expwet) * cfactor;
+    AER(KA_TRACER_ACC, KM_ACC) = AER(KA_TRACER_ACC, KM_ACC) * expwet;
+    AER(KA_PHG_ACC, KM_ACC) = AER(KA_PHG_ACC, KM_ACC) * expwet;
+    AER(KA_TRACER_COR, KM_COR) = AER(KA_TRACER_COR, KM_COR) * expwet;
+    AER(KA_PHG_COR, KM_COR) = AER(KA_PHG_COR, KM_COR) * expwet;
+    AER(KA_SOA, KM_ACC) = AER(KA_SOA, KM_ACC) + AER(KA_SOA, KM_AKN) * (1.0 - ex3);
+    AER(KA_SOA, KM_AKN) = AER(KA_SOA, KM_AKN) * ex3;
+    AWD(KA_SOA, KM_ACC) = AER(KA_SOA, KM_ACC) * (1.0 - expwet) * cfactor;
+    AER(KA_SOA, KM_ACC) = AER(KA_SOA, KM_ACC) * expwet;
+    AWD(KA_SOILC, KM_COR) = AER(KA_SOILC, KM_COR) * (1.0 - expwet) * cfactor;
+    AWD(KA_SEASC, KM_COR) = AER(KA_SEASC, KM_COR) * (1.0 - expwet) * cfactor;
+    AWD(KA_ANTHC, KM_COR) = AER(KA_ANTHC, KM_COR) * (1.0 - expwet) * cfactor;
+    AWD(KA_SO4, KM_COR) = AER(KA_SO4, KM_COR) * (1.0 - expwet) * cfactor;
+    AWD(KA_NH4, KM_COR) = AER(KA_NH4, KM_COR) * (1.0 - expwet) * cfactor;
+    AWD(KA_NO3, KM_COR) = AER(KA_NO3, KM_COR) * (1.0 - expwet) * cfactor;
+    AWD(KA_CL, KM_COR) = AER(KA_CL, KM_COR) * (1.0 - expwet) * cfactor;
+    AER(KA_NUM, KM_COR) = AER(KA_NUM, KM_COR) * expwet;
+    AER(KA_SOILC, KM_COR) = AER(KA_SOILC, KM_COR) * expwet;
+    AER(KA_SEASC, KM_COR) = AER(KA_SEASC, KM_COR) * expwet;
+    AER(KA_ANTHC, KM_COR) = AER(KA_ANTHC, KM_COR) * expwet;
+    AER(KA_SO4, KM_COR) = AER(KA_SO4, KM_COR) * expwet;
+    AER(KA_NH4, KM_COR) = AER(KA_NH4, KM_COR) * expwet;
+    AER(KA_NO3, KM_COR) = AER(KA_NO3, KM_COR) * expwet;
+    AER(KA_CL, KM_COR) = AER(KA_CL, KM_COR) * expwet;
+    const double wsoil = AWD(KA_SOILC, KM_COR), wanth = AWD(KA_ANTHC, KM_COR), wseas = AWD(KA_SEASC, KM_COR);
+    const double wdfecor = fac[KF_SOIL_FE] * wsoil + fac[KF_CORS_FE] * wanth;
+    const double wdmncor = fac[KF_SOIL_MN] * wsoil + fac[KF_CORS_MN] * wanth;
+    const double wdnacor = fac[KF_SEAS_NA] * wseas + fac[KF_SOIL_NA] * wsoil + fac[KF_CORS_NA] * wanth;
+    const double wdmgcor = fac[KF_SEAS_MG] * wseas + fac[KF_SOIL_MG] * wsoil + fac[KF_CORS_MG] * wanth;
+    const double wdcacor = fac[KF_SEAS_CA] * wseas + fac[KF_SOIL_CA] * wsoil + fac[KF_CORS_CA] * wanth;
+    const double wdkcor = fac[KF_SEAS_K] * wseas + fac[KF_SOIL_K] * wsoil + fac[KF_CORS_K] * wanth;
+    AWD(KA_FEACC, KM_ACC) = fmax((y[WD_FEPLUS3 * s] / fe_iii / fe_sol) - wdfecor, 0.0);
+    AWD(KA_MNACC, KM_ACC) = fmax((y[WD_MNPLUS2 * s] / mn_ii / mn_sol) - wdmncor, 0.0);
+    AWD(KA_NA, KM_ACC) = fmax(y[WD_NAPLUS * s] - wdnacor, 0.0);
+    AWD(KA_CAACC, KM_ACC) = fmax(y[WD_CAPLUS2 * s] - wdcacor, 0.0);
+    AWD(KA_MGACC, KM_ACC) = fmax(y[WD_MGPLUS2 * s] - wdmgcor, 0.0);
+    AWD(KA_KACC, KM_ACC) = fmax(y[WD_KPLUS * s] - wdkcor, 0.0);
+    AWD(KA_SO4, KM_ACC) = fmax(y[WD_H2SO4 * s] - AWD(KA_SO4, KM_COR), 0.0);
+    AWD(KA_NH4, KM_ACC) = fmax(y[WD_NH4PLUS * s] - AWD(KA_NH4, KM_COR), 0.0);
+    AWD(KA_NO3, KM_ACC) = fmax(y[WD_NO3MIN * s] - AWD(KA_NO3, KM_COR), 0.0);
+    AWD(KA_CL, KM_ACC) = fmax(y[WD_CLMIN * s] - AWD(KA_CL, KM_COR), 0.0);
+    AWD(KA_PRI, KM_ACC) = y[WD_PRIACC * s];
+    AWD(KA_EC, KM_ACC) = y[WD_PECACC * s];
+    AWD(KA_ORGC, KM_ACC) = y[WD_ORGC * s];
+    AWD(KA_POA, KM_ACC) = y[WD_POAACC * s];
+    if (ispc8 > 0) {
+        AWD(KA_IETET, KM_ACC) = y[WD_IETET * s];
+        AWD(KA_IEOS, KM_ACC) = y[WD_IEOS * s];
+        AWD(KA_DIMER, KM_ACC) = y[WD_DIMER * s];
+        AWD(KA_IMGA, KM_ACC) = y[WD_IMGA * s];
+        AWD(KA_IMOS, KM_ACC) = y[WD_IMOS * s];
+    } else {
+        AWD(KA_ISO3, KM_ACC) = y[WD_IETET * s];
+    }
+    if (AWD(KA_NH4, KM_COR) > y[WD_NH4PLUS * s]) {
+        AWD(KA_NH4, KM_COR) = (1.0 - fnh4acc) * y[WD_NH4PLUS * s];
+        AWD(KA_NH4, KM_ACC) = fnh4acc * y[WD_NH4PLUS * s];
+        AER(KA_NH4, KM_COR) = (1.0 - fnh4acc) * (y[L_NH4OH * s] + y[L_NH4PLUS * s]) * invcfac;
+    }
+    if (AWD(KA_NO3, KM_COR) > y[WD_NO3MIN * s]) {
+        AWD(KA_NO3, KM_COR) = (1.0 - fno3acc) * y[WD_NO3MIN * s];
+        AWD(KA_NO3, KM_ACC) = fno3acc * y[WD_NO3MIN * s];
+        AER(KA_NO3, KM_COR) = (1.0 - fno3acc) * (y[L_HNO3 * s] + y[L_NO3MIN * s]) * invcfac;
+    }
+    if (AWD(KA_CL, KM_COR) > y[WD_CLMIN * s]) {
+        AWD(KA_CL, KM_COR) = (1.0 - fclacc) * y[WD_CLMIN * s];
+        AWD(KA_CL, KM_ACC) = fclacc * y[WD_CLMIN * s];
+        AER(KA_CL, KM_COR) = (1.0 - fclacc) * y[L_CLMIN * s] * invcfac;
+    }
+    AER(KA_PRI, KM_ACC) = y[L_PRIACC * s] * invcfac;
+    AER(KA_EC, KM_ACC) = y[L_PECACC * s] * invcfac;
+    AER(KA_ORGC, KM_ACC) = y[L_ORGC * s] * invcfac;
+    AER(KA_POA, KM_ACC) = y[L_POAACC * s] * invcfac;
+    out[(KO_FRACTR) * n] = AER(KA_TRACER_ACC, KM_ACC) > 0.0
+        ? fmin(((traciinit - AER(KA_TRACER_AKN, KM_AKN)) * expwet) / AER(KA_TRACER_ACC, KM_ACC), 1.0) : 0.0;
+    out[(KO_FRACPOA) * n] = AER(KA_POA, KM_ACC) > 0.0
+        ? fmin(((poaiinit - AER(KA_POA, KM_AKN)) * expwet) / AER(KA_POA, KM_ACC), 1.0) : 0.0;
+    out[(KO_FRACPRI) * n] = AER(KA_PRI, KM_ACC) > 0.0
+        ? fmin(((priiinit - AER(KA_PRI, KM_AKN)) * expwet) / AER(KA_PRI, KM_ACC), 1.0) : 0.0;
+    out[(KO_FRACSOA) * n] = AER(KA_SOA, KM_ACC) > 0.0
+        ? fmin(((soaiinit - AER(KA_SOA, KM_AKN)) * expwet) / AER(KA_SOA, KM_ACC), 1.0) : 0.0;
+    if (ispc8 > 0) {
+        AER(KA_IETET, KM_ACC) = y[L_IETET * s] * invcfac;
+        AER(KA_IEOS, KM_ACC) = y[L_IEOS * s] * invcfac;
+        AER(KA_DIMER, KM_ACC) = y[L_DIMER * s] * invcfac;
+        AER(KA_IMGA, KM_ACC) = y[L_IMGA * s] * invcfac;
+        AER(KA_IMOS, KM_ACC) = y[L_IMOS * s] * invcfac;
+    } else {
+        AER(KA_ISO3, KM_ACC) = (y[L_ISO3 * s]) * invcfac;
+    }
+    const double soilc2 = AER(KA_SOILC, KM_COR), anthc2 = AER(KA_ANTHC, KM_COR), seasc2 = AER(KA_SEASC, KM_COR);
+    fecor = fac[KF_SOIL_FE] * soilc2 + fac[KF_CORS_FE] * anthc2;
+    mncor = fac[KF_SOIL_MN] * soilc2 + fac[KF_CORS_MN] * anthc2;
+    nacor = fac[KF_SEAS_NA] * seasc2 + fac[KF_SOIL_NA] * soilc2 + fac[KF_CORS_NA] * anthc2;
+    mgcor = fac[KF_SEAS_MG] * seasc2 + fac[KF_SOIL_MG] * soilc2 + fac[KF_CORS_MG] * anthc2;
+    cacor = fac[KF_SEAS_CA] * seasc2 + fac[KF_SOIL_CA] * soilc2 + fac[KF_CORS_CA] * anthc2;
+    kcor = fac[KF_SEAS_K] * seasc2 + fac[KF_SOIL_K] * soilc2 + fac[KF_CORS_K] * anthc2;
+    AER(KA_FEACC, KM_ACC) = fmax((y[L_FEPLUS3 * s] / fe_iii / fe_sol - fecor * cfactor) * invcfac, 0.0);
+    AER(KA_MNACC, KM_ACC) = fmax((y[L_MNPLUS2 * s] / mn_ii / mn_sol - mncor * cfactor) * invcfac, 0.0);
+    AER(KA_NA, KM_ACC) = fmax((y[L_NAPLUS * s] - nacor * cfactor) * invcfac, 0.0);
+    AER(KA_CAACC, KM_ACC) = fmax((y[L_CAPLUS2 * s] - cacor * cfactor) * invcfac, 0.0);
+    AER(KA_MGACC, KM_ACC) = fmax((y[L_MGPLUS2 * s] - mgcor * cfactor) * invcfac, 0.0);
+    AER(KA_KACC, KM_ACC) = fmax((y[L_KPLUS * s] - kcor * cfactor) * invcfac, 0.0);
+    AER(KA_SO4, KM_ACC) = fmax(((y[L_H2SO4 * s] + y[L_SO4MIN2 * s] + y[L_HSO4MIN * s]) * invcfac)
+                               - AER(KA_SO4, KM_COR), 0.0);
+    AER(KA_CL, KM_ACC) = fmax((y[L_CLMIN * s] * invcfac) - AER(KA_CL, KM_COR), 0.0);
+    totamm = y[G_NH3 * s] + y[L_NH4OH * s] + y[L_NH4PLUS * s] - AER(KA_NH4, KM_COR) * cfactor;
+    totnit = y[G_HNO3 * s] + y[L_HNO3 * s] + y[L_NO3MIN * s] - AER(KA_NO3, KM_COR) * cfactor;
+    totamm = fmax(totamm, 0.0);
+    totnit = fmax(totnit, 0.0);
+    AER(KA_NO3, KM_ACC) = ((1.0 - fhno3) * totnit) * invcfac;
+    AER(KA_NH4, KM_ACC) = ((1.0 - fnh3) * totamm) * invcfac;
+    const double oliggly = 0.0 * 3.3e-1, oligmgly = 0.0 * 1.9e-1;   /* OLIG = 0 (aqchem_kmt.F90:412) */
+    gas[KG_SO2 * n] = (y[G_SO2 * s] + y[L_SO2 * s] + y[L_HSO3MIN * s] + y[L_SO3MIN2 * s] + y[L_HMSMIN * s]
+                   + y[L_SO3MIN * s] + y[L_SO5MIN * s] + y[L_HSO5MIN * s] + y[L_SO4MIN * s]) * invcfac;
+    gas[KG_N2O5 * n] = 0.0;
+    gas[KG_CO2 * n] = (y[G_CO2 * s] + y[L_H2CO3 * s] + y[L_HCO3MIN * s] + y[L_CO3MIN2 * s] + y[L_CO2MIN * s])
+                  * invcfac;
+    gas[KG_H2O2 * n] = (y[G_H2O2 * s] + y[L_H2O2 * s]) * invcfac;
+    gas[KG_O3 * n] = (y[G_O3 * s] + y[L_O3 * s]) * invcfac;
+    gas[KG_FOA * n] = (y[G_HCOOH * s] + y[L_HCOOH * s] + y[L_HCOOMIN * s]) * invcfac;
+    gas[KG_MHP * n] = (y[G_MHP * s] + y[L_MHP * s]) * invcfac;
+    gas[KG_PAA * n] = (y[G_PAA * s] + y[L_PAA * s]) * invcfac;
+    gas[KG_H2SO4 * n] = 0.0;
+    gas[KG_HCL * n] = (y[G_HCL * s] + y[L_HCL * s]) * invcfac;
+    gas[KG_GLY * n] = (y[G_GLY * s] + y[L_GLY * s] * (1.0 - oliggly)) * invcfac;
+    gas[KG_MGLY * n] = (y[G_MGLY * s] + y[L_MGLY * s] * (1.0 - oligmgly)) * invcfac;
+    gas[KG_HNO3 * n] = (fhno3 * totnit) * invcfac;
+    gas[KG_NH3 * n] = (fnh3 * totamm) * invcfac;
+    gas[KG_HO * n] = (f[G_HO * s]) * invcfac;
+    gas[KG_IEPOX * n] = (y[G_IEPOX * s] + y[L_IEPOX * s]) * invcfac;
+    if (ispc8 > 0) {
+        gas[KG_IMAE * n] = (y[G_IMAE * s] + y[L_IMAE * s]) * invcfac;
+        gas[KG_IHMML * n] = (y[G_IHMML * s] + y[L_IHMML * s]) * invcfac;
+    }
+    gas[KG_HO2 * n] = (y[G_HO2 * s] + y[L_HO2 * s] + y[L_O2MIN * s]) * invcfac;
+    gas[KG_NO2 * n] = (y[G_NO2 * s] + y[L_NO2 * s]) * invcfac;
+    gas[KG_HONO * n] = (y[G_HONO * s] + y[L_HONO * s] + y[L_NO2MIN * s]) * invcfac;
+    gas[KG_HNO4 * n] = (y[G_HNO4 * s] + y[L_HNO4 * s] + y[L_NO4MIN * s]) * invcfac;
+    gas[KG_NO3RAD * n] = (y[G_NO3 * s] + y[L_NO3 * s]) * invcfac;
+    gas[KG_CH3O2 * n] = (y[G_CH3O2 * s] + y[L_CH3O2 * s]) * invcfac;
+    gas[KG_CCOOH * n] = (y[G_CCOOH * s] + y[L_CCOOH * s] + y[L_CCOOHMIN * s]) * invcfac;
+    gas[KG_HCHO * n] = (y[G_HCHO * s] + y[L_CH2OHYD * s] + y[L_HCHO * s] + y[L_HMSMIN * s]) * invcfac;
+    gas[KG_GCOL * n] = (y[G_GCOL * s] + y[L_GCOL * s]) * invcfac;
+    gas[KG_HCHOP * n] = (y[G_HCHOP * s] + y[L_CH2OHYDP * s] + y[L_HCHOP * s] + y[L_HMSMINP * s]) * invcfac;
+    gwd[KG_SO2 * n] = y[WD_SO2 * s];
+    gwd[KG_HNO3 * n] = y[WD_HNO3 * s];
+    gwd[KG_N2O5 * n] = 0.0;
+    gwd[KG_CO2 * n] = y[WD_CO2 * s];
+    gwd[KG_NH3 * n] = y[WD_NH4OH * s];
+    gwd[KG_H2O2 * n] = y[WD_H2O2 * s];
+    gwd[KG_O3 * n] = y[WD_O3 * s];
+    gwd[KG_FOA * n] = y[WD_HCOOH * s];
+    gwd[KG_MHP * n] = y[WD_MHP * s];
+    gwd[KG_PAA * n] = y[WD_PAA * s];
+    gwd[KG_H2SO4 * n] = 0.0;
+    gwd[KG_HCL * n] = y[WD_HCL * s];
+    gwd[KG_GLY * n] = y[WD_GLY * s] * (1.0 - oliggly);
+    gwd[KG_MGLY * n] = y[WD_MGLY * s] * (1.0 - oligmgly);
+    gwd[KG_HO * n] = y[WD_HO * s];
+    gwd[KG_IEPOX * n] = y[WD_IEPOX * s];
+    if (ispc8 > 0) {
+        gwd[KG_IMAE * n] = y[WD_IMAE * s];
+        gwd[KG_IHMML * n] = y[WD_IHMML * s];
+    }
+    gwd[KG_NO2 * n] = y[WD_NO2 * s];
+    gwd[KG_HONO * n] = y[WD_HONO * s];
+    gwd[KG_HNO4 * n] = y[WD_HNO4 * s];
+    gwd[KG_NO3RAD * n] = y[WD_NO3 * s];
+    gwd[KG_CH3O2 * n] = y[WD_CH3O2 * s];
+    gwd[KG_GCOL * n] = y[WD_GCOL * s];
+    gwd[KG_CCOOH * n] = y[WD_CCOOH * s];
+    gwd[KG_HCHO * n] = y[WD_CH2OHYD * s];
+    gwd[KG_HO2 * n] = y[WD_HO2 * s];
+    gwd[KG_HCHOP * n] = y[WD_CH2OHYDP * s];
+    double apyrac = 0.0, wdpyrac = 0.0;
+    if (mtpyrac > 0) {
+        gas[KG_PYRUV * n] = (y[G_PYRAC * s] + y[L_PYRAC * s]) * invcfac;
+        gwd[KG_PYRUV * n] = y[WD_PYRAC * s];
+        wdpyrac = 0.0;
+        apyrac = y[L_PYRACMIN * s];
+    } else {
+        wdpyrac = y[WD_PYRAC * s];
+        apyrac = y[L_PYRAC * s] + y[L_PYRACMIN * s];
+    }
+    const double r7404 = (double)(74.04f / 177.0f), r9003 = (double)(90.03f / 177.0f);
+    const double r8806 = (double)(88.06f / 177.0f), r7605 = (double)(76.05f / 177.0f);
+    const double r5804 = (double)(58.04f / 177.0f), r7206 = (double)(72.06f / 177.0f);
+    AER(KA_ORGC, KM_ACC) = (y[L_ORGC * s] + (r7404 * y[L_GLYAC * s]) + (r9003 * y[L_OXLAC * s])
+                            + (r9003 * y[L_OXLACMIN * s]) + (r9003 * y[L_OXLACMIN2 * s]) + (r8806 * apyrac)
+                            + (r7605 * y[L_GCOLAC * s]) + (r7404 * y[L_GLYACMIN * s])
+                            + (r7605 * y[L_GCOLACMIN * s])
+                            + r5804 * oliggly * y[L_GLY * s] + r7206 * oligmgly * y[L_MGLY * s]) * invcfac;
+    AWD(KA_ORGC, KM_ACC) = y[WD_ORGC * s] + (r7404 * y[WD_GLYAC * s]) + (r9003 * y[WD_OXLAC * s])
+                           + (r8806 * wdpyrac) + (r7605 * y[WD_GCOLAC * s])
+                           + r5804 * oliggly * y[WD_GLY * s] + r7206 * oligmgly * y[WD_MGLY * s];
+    for (int i = 0; i < KG_NGAS; ++i) gwd[i * n] = gwd[i * n] * wfactor;
+    for (int i = 0; i < naer * 3; ++i) awd[i * n] = awd[i * n] * wfactor;
+    for (int i = 0; i < KG_NGAS; ++i) {
+        if (gas[i * n] < 0.0) gas[i * n] = 0.0;
+        if (gwd[i * n] < 0.0) gwd[i * n] = 0.0;
+    }
+    for (int i = 0; i < naer * 3; ++i) {
+        if (aer[i * n] < 0.0) aer[i * n] = 0.0;
+        if (awd[i * n] < 0.0) awd[i * n] = 0.0;
+    }
+    out[(KO_HPWDEP) * n] = (double)(float)(y[WD_HPLUS * s] * wfactor);   /* HPWDEP is REAL */
+    const double depsum = AWD(KA_SO4, KM_ACC) / wfactor;
+    const double betaso4 = AER(KA_SO4, KM_ACC) * cfactor + depsum > 0.0
+                               ? depsum / (AER(KA_SO4, KM_ACC) * cfactor + depsum) / (double)taucld : 0.0;
+    out[(KO_BETASO4) * n] = betaso4;
+    AER(KA_NUM, KM_ACC) = AER(KA_NUM, KM_ACC) * kq_exp(-betaso4 * (double)taucld);
+    /* :919-973: mass balance at the end */
+    double endm[4];
+    endm[0] = (gas[KG_SO2 * n] + gas[KG_H2SO4 * n] + (gwd[KG_SO2 * n] + gwd[KG_H2SO4 * n]) / wfactor / cfactor) * w_s;
+    endm[1] = (gas[KG_HNO3 * n] + 2 * gas[KG_N2O5 * n] + gas[KG_NO2 * n] + gas[KG_HONO * n] + gas[KG_HNO4 * n] + gas[KG_NO3RAD * n]
+               + (gwd[KG_HNO3 * n] + gwd[KG_NO2 * n] + gwd[KG_HONO * n] + gwd[KG_HNO4 * n] + gwd[KG_NO3RAD * n]) / wfactor / cfactor)
+              * w_n;
+    endm[2] = (gas[KG_NH3 * n] + gwd[KG_NH3 * n] / wfactor / cfactor) * w_n;
+    endm[3] = (gas[KG_HCL * n] + gwd[KG_HCL * n] / wfactor / cfactor) * w_cl;
+    for (int m = 0; m < 3; ++m) {
+        endm[0] = endm[0] + AER(KA_SO4, m) * w_s;
+        endm[1] = endm[1] + AER(KA_NO3, m) * w_n;
+        endm[2] = endm[2] + AER(KA_NH4, m) * w_n;
+        endm[3] = endm[3] + AER(KA_CL, m) * w_cl;
+    }
+    for (int m = 0; m < 3; ++m) {
+        endm[0] = endm[0] + (AWD(KA_SO4, m) / wfactor / cfactor) * w_s;
+        endm[1] = endm[1] + (AWD(KA_NO3, m) / wfactor / cfactor) * w_n;
+        endm[2] = endm[2] + (AWD(KA_NH4, m) / wfactor / cfactor) * w_n;
+        endm[3] = endm[3] + (AWD(KA_CL, m) / wfactor / cfactor) * w_cl;
+    }
+    for (int i = 0; i < 4; ++i) out[(KO_MBAL + i) * n] = startm[i] > 0.0 ? 100 * (startm[i] - endm[i]) / startm[i] : 0.0;
+    return ierr == 1 ? 0 : 1;
+#undef AER
+#undef AWD
 }
 
 }  // namespace kmt2

@@ -701,9 +701,74 @@ def flop_counts(k: KppMech) -> dict:
             "per_step": fun + jac, "per_attempt": decomp + 4 * solve + 2 * fun + vector}
 
 
-def manifest(k: KppMech) -> dict:
-    return {"mechanism": "kmt2 (CCTM/src/cloud/acm_ae7_kmt2)", "nvar": k.nvar, "nfix": k.nfix, "nreact": k.nreact,
-            "lu_nonzero": len(k.lu_irow), "species": k.names, "flops": flop_counts(k)}
+# AQCHEM's GAS array (CCTM/src/cloud/acm_ae7_kmt2/AQ_DATA.F: srggas, in that order)
+AQ_GAS = ("SO2", "HNO3", "N2O5", "CO2", "NH3", "H2O2", "O3", "FOA", "MHP", "PAA", "H2SO4", "HCL", "GLY", "MGLY",
+          "HO", "IEPOX", "IMAE", "IHMML", "HO2", "NO2", "HONO", "HNO4", "GCOL", "CCOOH", "HCHO", "NO3RAD", "CH3O2",
+          "HCHOP", "PYRUV")
+# the aerosol surrogates AQCHEM reads or writes (AQ_DATA.F's LSO4, LNH4, ... used in aqchem_kmt.F90 and
+# aqchem_Initialize.F90), in the order of the library's surrogate-position array
+AQ_AEROSOL = ("SO4", "NH4", "NO3", "CL", "NA", "EC", "POA", "PRI", "SOA", "NUM", "SOILC", "SEASC", "ANTHC",
+              "CAACC", "MGACC", "KACC", "FEACC", "MNACC", "ORGC", "TRACER_AKN", "TRACER_ACC", "TRACER_COR",
+              "PHG_AKN", "PHG_ACC", "PHG_COR", "IETET", "IEOS", "DIMER", "IMGA", "IMOS", "ISO3")
+# the coarse crustal factors of aqchem_kmt.F90:329-365: (name, AERO_DATA factor, bulk species, element, renorm)
+CRUSTAL = (("SOIL_FE_FAC", "asoil_fe_fac", "ASOIL", "AFE", "asoil_renorm"),
+           ("CORS_FE_FAC", "acors_fe_fac", "ACORS", "AFE", "acorsem_renorm"),
+           ("SOIL_MN_FAC", "asoil_mn_fac", "ASOIL", "AMN", "asoil_renorm"),
+           ("CORS_MN_FAC", "acors_mn_fac", "ACORS", "AMN", "acorsem_renorm"),
+           ("SEAS_NA_FAC", "ascat_na_fac", "ASEACAT", "ANA", None),
+           ("SOIL_NA_FAC", "asoil_na_fac", "ASOIL", "ANA", "asoil_renorm"),
+           ("CORS_NA_FAC", "acors_na_fac", "ACORS", "ANA", "acorsem_renorm"),
+           ("SEAS_MG_FAC", "ascat_mg_fac", "ASEACAT", "AMG", None),
+           ("SOIL_MG_FAC", "asoil_mg_fac", "ASOIL", "AMG", "asoil_renorm"),
+           ("CORS_MG_FAC", "acors_mg_fac", "ACORS", "AMG", "acorsem_renorm"),
+           ("SEAS_CA_FAC", "ascat_ca_fac", "ASEACAT", "ACA", None),
+           ("SOIL_CA_FAC", "asoil_ca_fac", "ASOIL", "ACA", "asoil_renorm"),
+           ("CORS_CA_FAC", "acors_ca_fac", "ACORS", "ACA", "acorsem_renorm"),
+           ("SEAS_K_FAC", "ascat_k_fac", "ASEACAT", "AK", None),
+           ("SOIL_K_FAC", "asoil_k_fac", "ASOIL", "AK", "asoil_renorm"),
+           ("CORS_K_FAC", "acors_k_fac", "ACORS", "AK", "acorsem_renorm"))
+
+
+def crustal_factors(cmaq_root: str, mech: str = "cb6r5_ae7_aq") -> list[float]:
+    """AQCHEM's first-call coarse crustal factors (aqchem_kmt.F90:329-365): AERO_DATA's
+    REAL(8) speciation factors and renormalisations (CCTM/src/aero/aero6/AERO_DATA.F:591-627)
+    times the ratio of the REAL(4) molecular weights of the mechanism's AE namelist
+    (MECHS/<mech>/AE_<mech>.nml), in the reference's operation order."""
+    import numpy as np
+    root = Path(cmaq_root) / "CCTM" / "src"
+    text = (root / "aero" / "aero6" / "AERO_DATA.F").read_text()
+    const = {}
+    for m in re.finditer(r"Real\(\s*8\s*\),\s*Parameter\s*::\s*(\w+)\s*=\s*([^!\n]+(?:\n\s*&[^!\n]+)*)", text):
+        expr = re.sub(r"\n\s*&", " ", m.group(2)).strip()
+        const[m.group(1).lower()] = expr
+    def value(name):
+        expr = const[name]
+        terms = re.findall(r"([+-]?)\s*([0-9.]+D[+-]?[0-9]+|[0-9.]+|[a-z_0-9]+)", expr.replace(" ", ""))
+        acc = None
+        for sign, tok in terms:
+            v = value(tok.lower()) if re.match(r"[a-z_]", tok) else float(tok.replace("D", "e"))
+            acc = v if acc is None else (acc - v if sign == "-" else acc + v)
+        return acc
+    nml = (root / "MECHS" / mech / f"AE_{mech}.nml").read_text()
+    mw = {m.group(1): float(np.float32(float(m.group(2))))
+          for m in re.finditer(r"^'(\w+)'\s*,\s*([0-9.]+)", nml, flags=re.M)}
+    out = []
+    for _, fac, bulk, elem, renorm in CRUSTAL:
+        v = value(fac) * mw[bulk] / mw[elem]
+        if renorm:
+            v = v / value(renorm)
+        out.append(v)
+    return out
+
+
+def manifest(k: KppMech, cmaq_root: str | None = None) -> dict:
+    m = {"mechanism": "kmt2 (CCTM/src/cloud/acm_ae7_kmt2)", "nvar": k.nvar, "nfix": k.nfix, "nreact": k.nreact,
+         "lu_nonzero": len(k.lu_irow), "species": k.names, "flops": flop_counts(k)}
+    if cmaq_root:
+        m["aqchem"] = {"gas": list(AQ_GAS), "aerosol_surrogates": list(AQ_AEROSOL),
+                       "crustal_factor_names": [c[0] for c in CRUSTAL],
+                       "crustal_factors": crustal_factors(cmaq_root)}
+    return m
 
 
 def unrolled_source(k: KppMech) -> str:
@@ -725,7 +790,7 @@ def write_outputs(cmaq_root: str) -> KppMech:
     (cdir / "kmt2_aq.cuh").write_text(device_source(k))
     mdir = REPO / "cmaq_gb300" / "mechs" / "kmt2"
     mdir.mkdir(parents=True, exist_ok=True)
-    (mdir / "manifest.json").write_text(json.dumps(manifest(k), indent=1) + "\n")
+    (mdir / "manifest.json").write_text(json.dumps(manifest(k, cmaq_root), indent=1) + "\n")
     return k
 
 

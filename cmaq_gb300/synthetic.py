@@ -272,3 +272,56 @@ def make_cloud_cells(n: int, seed: int = 0, ispc8: int = 0, mtpyrac: int = 0):
     for name, (lo, hi) in ranges.items():
         v[:, index[name]] = 10 ** rng.uniform(lo, hi, n)
     return p, v
+
+
+# log10 ranges of AQCHEM's GAS and AEROSOL inputs (mol/molV; the aerosol numbers per mol of air)
+_GAS_RANGES = {"SO2": (-9.5, -8), "HNO3": (-10.5, -9), "N2O5": (-12, -10.5), "CO2": (-3.45, -3.35),
+               "NH3": (-10.5, -8.5), "H2O2": (-10, -8.7), "O3": (-7.6, -7.2), "FOA": (-10.5, -9), "MHP": (-10.5, -9),
+               "PAA": (-11, -10), "H2SO4": (-12, -10.5), "HCL": (-11.5, -10), "GLY": (-11.5, -10),
+               "MGLY": (-11.5, -10), "HO": (-14.5, -12.5), "IEPOX": (-11, -9.5), "HO2": (-12, -10.7),
+               "NO2": (-10, -8), "HONO": (-11.5, -10), "HNO4": (-12, -10.5), "GCOL": (-12, -10.5),
+               "CCOOH": (-10.5, -9), "HCHO": (-9.5, -8.5), "NO3RAD": (-13.5, -12), "CH3O2": (-12.5, -11),
+               "HCHOP": (-13, -11)}
+_AER_RANGES = {  # (surrogate, mode 0 Aitken / 1 accumulation / 2 coarse)
+    ("NO3", 0): (-13, -11.5), ("NH4", 0): (-12.5, -11), ("CL", 0): (-14, -12.5), ("NA", 0): (-14, -12.5),
+    ("SO4", 0): (-12.5, -11), ("EC", 0): (-13, -11.5), ("POA", 0): (-12.5, -11), ("PRI", 0): (-13, -11.5),
+    ("SOA", 0): (-13, -11.5), ("NUM", 0): (10, 12), ("TRACER_AKN", 0): (-14, -12), ("PHG_AKN", 0): (-15, -13),
+    ("SO4", 1): (-10, -9), ("NO3", 1): (-10.5, -9.3), ("NH4", 1): (-9.8, -8.8), ("CL", 1): (-12, -10.5),
+    ("PRI", 1): (-11.5, -10), ("NA", 1): (-12, -10.5), ("CAACC", 1): (-12.5, -11), ("MGACC", 1): (-13, -11.5),
+    ("KACC", 1): (-13, -11.5), ("EC", 1): (-11.5, -10.5), ("ORGC", 1): (-12, -10.5), ("POA", 1): (-11, -9.8),
+    ("FEACC", 1): (-13.5, -12), ("MNACC", 1): (-14.5, -13), ("SOA", 1): (-11, -9.8), ("NUM", 1): (9, 11),
+    ("TRACER_ACC", 1): (-13, -11.5), ("PHG_ACC", 1): (-14, -12.5),
+    ("SO4", 2): (-11.5, -10), ("NO3", 2): (-11.5, -10.5), ("NH4", 2): (-11, -10), ("CL", 2): (-11.5, -10.5),
+    ("SOILC", 2): (-11, -9.5), ("SEASC", 2): (-11.5, -10), ("ANTHC", 2): (-11, -9.5), ("NUM", 2): (7, 9),
+    ("TRACER_COR", 2): (-13.5, -12), ("PHG_COR", 2): (-14.5, -13)}
+
+
+def make_cloud_columns(n: int, seed: int = 0, ispc8: int = 0, mtpyrac: int = 0):
+    """Seeded inputs of the whole AQCHEM (mapping, kinetics, redistribution) for n cloudy
+    cells: params [n][15] as ``make_cloud_cells`` draws them (the HO row is not read: GAS
+    carries HO), gas [n][29] in AQ_DATA's order, aerosol [n][31 * 3] (surrogate i of mode m
+    at i + 31 * m, the surrogates in the order of the manifest's ``aerosol_surrogates``),
+    the identity surrogate positions [31] and the coarse crustal factors [16] of the
+    manifest."""
+    man = kmt2_manifest()["aqchem"]
+    gas_names, aer_names = man["gas"], man["aerosol_surrogates"]
+    p, _ = make_cloud_cells(n, seed=seed, ispc8=ispc8, mtpyrac=mtpyrac)
+    rng = np.random.default_rng(seed + 7919)
+    g = np.zeros((n, len(gas_names)))
+    ranges = dict(_GAS_RANGES)
+    if ispc8:
+        ranges.update({"IMAE": (-12, -10.5), "IHMML": (-12, -10.5)})
+    if mtpyrac:
+        ranges["PYRUV"] = (-12, -10.5)
+    for name, (lo, hi) in ranges.items():
+        g[:, gas_names.index(name)] = 10 ** rng.uniform(lo, hi, n)
+    na = len(aer_names)
+    a = np.zeros((n, na * 3))
+    ar = dict(_AER_RANGES)
+    if ispc8:
+        ar.update({(k, 1): (-12.5, -11) for k in ("IETET", "IEOS", "DIMER", "IMGA", "IMOS")})
+    else:
+        ar[("ISO3", 1)] = (-12, -10.5)
+    for (name, mode), (lo, hi) in ar.items():
+        a[:, aer_names.index(name) + na * mode] = 10 ** rng.uniform(lo, hi, n)
+    return p, g, a, np.arange(na, dtype=np.int32), np.array(man["crustal_factors"])

@@ -280,6 +280,42 @@ int cmaqchem_kmt2_solve_device(long long ncell, const double* params, const doub
                                double* fix_out, int* stats, double* workspace, long long workspace_doubles,
                                void* stream);
 
+/* The whole KMT2 AQCHEM (CCTM/src/cloud/acm_ae7_kmt2/aqchem_kmt.F90:21-978) for ncell cloudy
+ * cells: the fractional weights and mass-balance start, Initialize's mapping of GAS and
+ * AEROSOL into the KPP state (aqchem_Initialize.F90:290-421), the kinetic core of
+ * cmaqchem_kmt2_solve_device, and the redistribution into GAS, AEROSOL, GASWDEP and AERWDEP
+ * (aqchem_kmt.F90:546-976).  Device arrays, [element][cell]:
+ *   params   [CMAQCHEM_KMT2_NPARAM][ncell] as for cmaqchem_kmt2_solve_device (the HO row is
+ *            not read: GAS carries HO);
+ *   gas      [CMAQCHEM_AQ_NGAS][ncell] in and out, AQ_DATA.F's order: SO2, HNO3, N2O5, CO2,
+ *            NH3, H2O2, O3, FOA, MHP, PAA, H2SO4, HCL, GLY, MGLY, HO, IEPOX, IMAE, IHMML,
+ *            HO2, NO2, HONO, HNO4, GCOL, CCOOH, HCHO, NO3RAD, CH3O2, HCHOP, PYRUV (mol/molV);
+ *   aerosol  [naer * 3][ncell] in and out: AEROSOL(NAER, NMODES) flattened, surrogate i of
+ *            mode m (0 Aitken, 1 accumulation, 2 coarse) at row i + naer * m;
+ *   aer_index [CMAQCHEM_AQ_NSURROGATE] (host array): rows of AQCHEM's surrogates in the
+ *            caller's aerosol list, in the order SO4, NH4, NO3, CL, NA, EC, POA, PRI, SOA,
+ *            NUM, SOILC, SEASC, ANTHC, CAACC, MGACC, KACC, FEACC, MNACC, ORGC, TRACER_AKN,
+ *            TRACER_ACC, TRACER_COR, PHG_AKN, PHG_ACC, PHG_COR, IETET, IEOS, DIMER, IMGA,
+ *            IMOS, ISO3 (AQ_DATA.F's LSO4 ... LISO3, 0-based);
+ *   factors  [CMAQCHEM_AQ_NFACTOR] (host array): the coarse crustal factors AQCHEM computes on
+ *            its first call (aqchem_kmt.F90:329-365), SOIL_FE, CORS_FE, SOIL_MN, CORS_MN,
+ *            SEAS_NA, SOIL_NA, CORS_NA, SEAS_MG, SOIL_MG, CORS_MG, SEAS_CA, SOIL_CA, CORS_CA,
+ *            SEAS_K, SOIL_K, CORS_K;
+ *   gas_wdep [CMAQCHEM_AQ_NGAS][ncell], aer_wdep [naer * 3][ncell] out (mm mol/L);
+ *   out      [CMAQCHEM_AQ_NOUT][ncell] out: HPWDEP, BETASO4, FRACTR, FRACPOA, FRACPRI,
+ *            FRACSOA, and the four mass-balance percentages AQCHEM checks (S, N without
+ *            NH3, NH3/NH4, Cl), whose magnitude above 0.5 makes the reference warn;
+ *   stats    [CMAQCHEM_KMT2_NSTAT][ncell] int as for cmaqchem_kmt2_solve_device.
+ * A cell whose set-up fails gets NaN in every output.  The workspace is that of
+ * cmaqchem_kmt2_solve_device.  Synchronises the stream; returns 0 or -1. */
+#define CMAQCHEM_AQ_NGAS 29
+#define CMAQCHEM_AQ_NSURROGATE 31
+#define CMAQCHEM_AQ_NFACTOR 16
+#define CMAQCHEM_AQ_NOUT 10
+int cmaqchem_aqchem_device(long long ncell, const double* params, double* gas, double* aerosol, int naer,
+                           const int* aer_index, const double* factors, double* gas_wdep, double* aer_wdep,
+                           double* out, int* stats, double* workspace, long long workspace_doubles, void* stream);
+
 /* Text of the last error of the calling thread; returns its length. */
 int cmaqchem_last_error(char* buf, size_t len);
 

@@ -60,6 +60,7 @@ def load() -> C.CDLL:
     lib.oracle_kq_set_rtol_scale.argtypes = [C.c_double]
     lib.oracle_kq_set_rtol_scale.restype = None
     lib.oracle_kq_cells.argtypes = [C.c_longlong, dp, dp, dp, dp, ip, C.c_int]
+    lib.oracle_kq_aqchem_cells.argtypes = [C.c_longlong, dp, dp, dp, C.c_int, ip, dp, dp, dp, dp, ip, C.c_int]
     return lib
 
 
@@ -151,6 +152,27 @@ class KMT2Oracle:
             self.lib.oracle_kq_set_rtol_scale(1.0)
         return var, fix, st, nfail
 
+    def aqchem(self, params, gas, aerosol, aer_index, factors, threads: int = 0):
+        """The whole AQCHEM per cell (mapping, kinetic core, redistribution): params [n][15],
+        gas [n][29], aerosol [n][naer * 3] (element (i, mode) at i + naer * mode), aer_index
+        [31] positions of AQCHEM's surrogates in the aerosol list, factors [16] coarse
+        crustal factors.  Returns (gas, aerosol, gas_wdep, aer_wdep, out [n][10], stats,
+        nfail); out: HPWDEP, BETASO4, FRACTR, FRACPOA, FRACPRI, FRACSOA, MBAL(1:4)."""
+        params = np.ascontiguousarray(params, np.float64)
+        g = np.array(gas, np.float64, order="C", copy=True)
+        a = np.array(aerosol, np.float64, order="C", copy=True)
+        n = params.shape[0]
+        naer = a.shape[1] // 3
+        idx = np.ascontiguousarray(aer_index, np.int32)
+        fac = np.ascontiguousarray(factors, np.float64)
+        gw, aw = np.zeros_like(g), np.zeros_like(a)
+        out = np.zeros((n, 10))
+        st = np.zeros((n, self.nstat), np.int32)
+        threads = threads or min(16, max(1, __import__("os").cpu_count() or 1))
+        nfail = self.lib.oracle_kq_aqchem_cells(n, _p(params), _p(g), _p(a), naer, _p(idx, C.c_int), _p(fac),
+                                                _p(gw), _p(aw), _p(out), _p(st, C.c_int), threads)
+        return g, a, gw, aw, out, st, nfail
+
     # ------------------------------------------------------------------ synthetic cells
     def synthetic_cells(self, n: int, seed: int = 0, ispc8: int = 0, mtpyrac: int = 0):
         """Seeded cloudy cells (cmaq_gb300.synthetic.make_cloud_cells: the benchmark's
@@ -161,3 +183,13 @@ class KMT2Oracle:
             sys.path.insert(0, root)
         from cmaq_gb300.synthetic import make_cloud_cells
         return make_cloud_cells(n, seed=seed, ispc8=ispc8, mtpyrac=mtpyrac)
+
+    def synthetic_columns(self, n: int, seed: int = 0, ispc8: int = 0, mtpyrac: int = 0):
+        """Seeded AQCHEM inputs (cmaq_gb300.synthetic.make_cloud_columns): params [n][15],
+        gas [n][29], aerosol [n][31 * 3], aer_index [31], factors [16]."""
+        import sys
+        root = str(HERE.parent)
+        if root not in sys.path:
+            sys.path.insert(0, root)
+        from cmaq_gb300.synthetic import make_cloud_columns
+        return make_cloud_columns(n, seed=seed, ispc8=ispc8, mtpyrac=mtpyrac)

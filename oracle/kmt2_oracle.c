@@ -913,7 +913,7 @@ static int kq_aqchem_cell(const double* p, double* gas, double* aer, int naer, c
     gas[KG_MGLY] = (var[KQ_G_MGLY] + var[KQ_L_MGLY] * (1.0 - oligmgly)) * invcfac;
     gas[KG_HNO3] = (fhno3 * totnit) * invcfac;
     gas[KG_NH3] = (fnh3 * totamm) * invcfac;
-    gas[KG_HO] = (fixv[KQ_G_HO - KQ_NVAR]) * invcfac;
+    gas[KG_HO] = (fixv[KQ_G_HO]) * invcfac;
     gas[KG_IEPOX] = (var[KQ_G_IEPOX] + var[KQ_L_IEPOX]) * invcfac;
     if (ispc8 > 0) {
         gas[KG_IMAE] = (var[KQ_G_IMAE] + var[KQ_L_IMAE]) * invcfac;

@@ -78,3 +78,31 @@ def run_kmt2_harness(exe, params_t, var_mix_t, nlanes, workdir):
     st = np.frombuffer(raw[8 * (nv + nf):], np.int32).reshape(10, n)
     nfail, ws_elems = map(int, r.stdout.split())
     return var, fix, st, nfail, ws_elems
+
+
+def run_aqchem_harness(exe, params_t, gas_t, aer_t, aer_index, factors, nlanes, workdir):
+    """The whole AQCHEM of the host build on [element][cell] arrays; returns gas, aerosol,
+    gas_wdep, aer_wdep, out [10][n], stats [10][n] ([element][cell]) and the failed cells."""
+    import os
+    import subprocess
+    import numpy as np
+    n = params_t.shape[1]
+    naer = aer_t.shape[0] // 3
+    inp, out = workdir / "aq_in.bin", workdir / "aq_out.bin"
+    with open(inp, "wb") as f:
+        np.concatenate([params_t.ravel(), gas_t.ravel(), aer_t.ravel(), np.asarray(factors, np.float64)]).astype(
+            np.float64).tofile(f)
+        np.asarray(aer_index, np.int32).tofile(f)
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=1:abort_on_error=0", UBSAN_OPTIONS="halt_on_error=1")
+    r = subprocess.run([str(exe), "aqchem", str(inp), str(out), str(n), str(nlanes), str(naer)], capture_output=True,
+                       text=True, timeout=600, env=env)
+    assert r.returncode == 0, r.stderr[-3000:]
+    assert "runtime error" not in r.stderr, r.stderr[-3000:]
+    raw = np.fromfile(out, dtype=np.uint8)
+    ng, na = 29 * n, naer * 3 * n
+    d = raw[:8 * (2 * ng + 2 * na + 10 * n)].view(np.float64)
+    g, a = d[:ng].reshape(29, n), d[ng:ng + na].reshape(naer * 3, n)
+    gw, aw = d[ng + na:2 * ng + na].reshape(29, n), d[2 * ng + na:2 * ng + 2 * na].reshape(naer * 3, n)
+    o = d[2 * ng + 2 * na:].reshape(10, n)
+    st = raw[8 * (2 * ng + 2 * na + 10 * n):].view(np.int32).reshape(10, n)
+    return g, a, gw, aw, o, st, int(r.stdout.split()[0])

@@ -9,13 +9,67 @@
 //   kmt2_host_harness <in> <out> ncell nlanes
 //   in:  params [NPARAM][ncell], var_mix [NVAR][ncell]          (doubles)
 //   out: var_out [NVAR][ncell], fix_out [NFIX][ncell] (doubles), stats [NSTAT][ncell] (int32)
+//
+//   kmt2_host_harness aqchem <in> <out> ncell nlanes naer       (the whole AQCHEM, kq_aqchem_cell)
+//   in:  params [NPARAM][ncell], gas [29][ncell], aerosol [naer*3][ncell], factors [16] (doubles),
+//        aer_index [31] (int32)
+//   out: gas, aerosol, gas_wdep, aer_wdep, out [10][ncell] (doubles), stats [NSTAT][ncell] (int32)
 #include <stdio.h>
 #include <stdlib.h>
+#include <string.h>
 
 #include "../cmaq_gb300/csrc/kmt2.cuh"
 
+static int run_aqchem(int argc, char** argv)
+{
+    if (argc != 7) return 2;
+    const long long ncell = atoll(argv[4]), nlanes = atoll(argv[5]);
+    const int naer = atoi(argv[6]);
+    if (ncell <= 0 || nlanes <= 0 || naer <= 0) return 2;
+    const size_t ng = (size_t)kmt2::KG_NGAS * ncell, na = (size_t)naer * 3 * ncell;
+    const size_t nd = (size_t)kmt2::NPARAM * ncell + ng + na + kmt2::KF_N;
+    double* in = (double*)malloc(sizeof(double) * nd);
+    int aidx[kmt2::KA_NIDX];
+    FILE* fi = fopen(argv[2], "rb");
+    if (!fi || fread(in, sizeof(double), nd, fi) != nd || fread(aidx, sizeof(int), kmt2::KA_NIDX, fi) != kmt2::KA_NIDX)
+        return 3;
+    fclose(fi);
+    const double* params = in;
+    double* gas = in + (size_t)kmt2::NPARAM * ncell;
+    double* aer = gas + ng;
+    const double* fac = aer + na;
+    double* gwd = (double*)calloc(ng, sizeof(double));
+    double* awd = (double*)calloc(na, sizeof(double));
+    double* out = (double*)calloc((size_t)kmt2::KO_N * ncell, sizeof(double));
+    int* st = (int*)calloc((size_t)kmt2::NSTAT * ncell, sizeof(int));
+    double* ws = (double*)malloc(sizeof(double) * kmt2::WS_ELEMS * nlanes);
+    int nfail = 0;
+    for (long long lane = 0; lane < nlanes; ++lane)
+        for (long long c = lane; c < ncell; c += nlanes)
+            nfail += kmt2::kq_aqchem_cell(params + c, gas + c, aer + c, naer, aidx, fac, gwd + c, awd + c, out + c,
+                                          st + c, ncell, ws + lane, nlanes);
+    FILE* fo = fopen(argv[3], "wb");
+    if (!fo) return 4;
+    fwrite(gas, sizeof(double), ng, fo);
+    fwrite(aer, sizeof(double), na, fo);
+    fwrite(gwd, sizeof(double), ng, fo);
+    fwrite(awd, sizeof(double), na, fo);
+    fwrite(out, sizeof(double), (size_t)kmt2::KO_N * ncell, fo);
+    fwrite(st, sizeof(int), (size_t)kmt2::NSTAT * ncell, fo);
+    fclose(fo);
+    free(in);
+    free(gwd);
+    free(awd);
+    free(out);
+    free(st);
+    free(ws);
+    printf("%d %d\n", nfail, kmt2::WS_ELEMS);
+    return 0;
+}
+
 int main(int argc, char** argv)
 {
+    if (argc > 1 && strcmp(argv[1], "aqchem") == 0) return run_aqchem(argc, argv);
     if (argc != 5) return 2;
     const long long ncell = atoll(argv[3]), nlanes = atoll(argv[4]);
     if (ncell <= 0 || nlanes <= 0) return 2;

@@ -103,3 +103,28 @@ def test_kmt2_host_array_entry_equals_the_device_entry(o):
     assert np.array_equal(hv.T, var) and np.array_equal(hf.T, fix) and np.array_equal(hs.T, st)
     empty = aqchem_kinetics_host(np.zeros((15, 0)), np.zeros((161, 0)))
     assert empty[0].shape == (161, 0)
+
+
+@pytest.mark.parametrize("seed,ispc8,mtpyrac", [(41, 0, 0), (42, 1, 1)])
+def test_whole_aqchem_equals_the_oracle(o, seed, ispc8, mtpyrac):
+    """cmaqchem_aqchem_device (mapping, kinetic core, redistribution) against the oracle's
+    restatement: every output bit for bit, with AQCHEM's surrogates at shuffled rows of the
+    aerosol list and a failed set-up among the cells."""
+    import torch
+    from cmaq_gb300.aqchem import aqchem
+    p, g, a, idx, fac = o.synthetic_columns(150, seed=seed, ispc8=ispc8, mtpyrac=mtpyrac)
+    naer = len(idx)
+    perm = np.random.default_rng(seed).permutation(naer)
+    a2 = np.zeros_like(a)
+    for m in range(3):
+        a2[:, perm + naer * m] = a[:, np.arange(naer) + naer * m]
+    p[7, P_TEMP2] = 0.0
+    rg, ra, rgw, raw_, ro, rs, rnf = o.aqchem(p, g, a2, perm, fac)
+    t = lambda x: torch.from_numpy(np.ascontiguousarray(x.T)).cuda()
+    pg, gg, ga = t(p), t(g), t(a2)
+    gwd, awd, out, st = aqchem(pg, gg, ga, perm, fac)
+    torch.cuda.synchronize()
+    assert np.array_equal(st.cpu().numpy().T, rs)
+    for got, ref in ((gg, rg), (ga, ra), (gwd, rgw), (awd, raw_), (out, ro)):
+        assert np.array_equal(got.cpu().numpy().T, ref, equal_nan=True)
+    assert np.isnan(rg[7]).all() and np.abs(ro[np.arange(150) != 7, 6:10]).max() < 1e-2

@@ -17,7 +17,7 @@ ROOT = Path(__file__).resolve().parents[1]
 sys.path.insert(0, str(ROOT / "oracle"))
 from kmt2 import KMT2Oracle, P_TEMP2, STATS  # noqa: E402
 
-from conftest import run_kmt2_harness  # noqa: E402
+from conftest import run_aqchem_harness, run_kmt2_harness  # noqa: E402
 
 
 @pytest.fixture(scope="module")
@@ -58,3 +58,25 @@ def test_switches_and_failed_cells(kmt2_harness, o, tmp_path):
     good = np.arange(len(p)) != 3
     assert np.array_equal(var[good], vr[good])
     assert np.isnan(var[3]).all() and np.isnan(vr[3]).all()     # a failed set-up leaves NaN, not stale memory
+
+
+@pytest.mark.parametrize("ncell,nlanes,ispc8,mtpyrac", [(23, 5, 0, 0), (9, 9, 1, 1)])
+def test_whole_aqchem_device_code_equals_the_oracle(kmt2_harness, o, tmp_path, ncell, nlanes, ispc8, mtpyrac):
+    """kq_aqchem_cell (mapping, kinetic core, redistribution) built for the host against the
+    oracle's restatement: every output bit for bit, with a shuffled surrogate order (the
+    positions array maps AQCHEM's surrogates into the caller's aerosol list) and a failed
+    set-up next to good cells."""
+    p, g, a, idx, fac = o.synthetic_columns(ncell, seed=200 + ncell, ispc8=ispc8, mtpyrac=mtpyrac)
+    naer = len(idx)
+    perm = np.random.default_rng(1).permutation(naer)          # surrogate k lives at row perm[k]
+    a2 = np.zeros_like(a)
+    for m in range(3):
+        a2[:, perm + naer * m] = a[:, np.arange(naer) + naer * m]
+    p[2, P_TEMP2] = 0.0
+    hg, ha, hgw, haw, ho, hs, hnf = run_aqchem_harness(kmt2_harness, p.T, g.T, a2.T, perm, fac, nlanes, tmp_path)
+    rg, ra, rgw, raw_, ro, rs, rnf = o.aqchem(p, g, a2, perm, fac)
+    assert hnf == rnf >= 1
+    assert np.array_equal(hs.T, rs)
+    for h, r in ((hg, rg), (ha, ra), (hgw, rgw), (haw, raw_), (ho, ro)):
+        assert np.array_equal(h.T, r, equal_nan=True)
+    assert np.isnan(rg[2]).all() and np.isfinite(rg[np.arange(ncell) != 2]).all()

@@ -425,3 +425,99 @@ def test_cloud_cell_inputs_are_seeded_and_in_range():
     assert (p[:, col["wcavg"]] <= p[:, col["wtavg"]]).all()
     assert np.array_equal(p[:, col["temp2"]], p[:, col["temp2"]].astype(np.float32))   # REAL arguments
     assert (v >= 0).all() and (v.max(axis=1) > 3e-4).all()                             # CO2 present
+
+
+# ----------------------------------------------------------------------------- the whole AQCHEM
+def _aq_names():
+    from cmaq_gb300.synthetic import kmt2_manifest
+    m = kmt2_manifest()["aqchem"]
+    return m["gas"], m["aerosol_surrogates"]
+
+
+def _map_in(o, p, g, a):
+    """Initialize's mapping of GAS and AEROSOL into the KPP state (aqchem_Initialize.F90:
+    290-421), restated from the reference text for one cell."""
+    gn, an = _aq_names()
+    na = len(an)
+    G = lambda s: g[gn.index(s)]
+    A = lambda s, m: a[an.index(s) + na * m]
+    f32 = lambda x: float(np.float32(x))
+    v = np.zeros(o.nvar)
+    x = o.index
+    ispc8, mtpyrac = int(p[P_ISPC8]), int(p[P_MTPYRAC])
+    for kpp, gas in (("G_SO2", "SO2"), ("G_CO2", "CO2"), ("G_NH3", "NH3"), ("G_H2O2", "H2O2"), ("G_O3", "O3"),
+                     ("G_HCOOH", "FOA"), ("G_MHP", "MHP"), ("G_PAA", "PAA"), ("G_HCL", "HCL"), ("G_GLY", "GLY"),
+                     ("G_MGLY", "MGLY"), ("G_IEPOX", "IEPOX"), ("G_NO2", "NO2"), ("G_HONO", "HONO"),
+                     ("G_HNO4", "HNO4"), ("G_NO3", "NO3RAD"), ("G_CH3O2", "CH3O2"), ("G_GCOL", "GCOL"),
+                     ("G_CCOOH", "CCOOH"), ("G_HCHO", "HCHO"), ("G_HO2", "HO2"), ("G_HCHOP", "HCHOP")):
+        v[x[kpp]] = G(gas)
+    v[x["G_HNO3"]] = G("HNO3") + 2.0 * G("N2O5")
+    if ispc8:
+        v[x["G_IMAE"]], v[x["G_IHMML"]] = G("IMAE"), G("IHMML")
+    if mtpyrac:
+        v[x["G_PYRAC"]] = G("PYRUV")
+    for kpp, s in (("A_NO3AKN", "NO3"), ("A_NH4AKN", "NH4"), ("A_CLAKN", "CL"), ("A_NAAKN", "NA"),
+                   ("A_SO4AKN", "SO4"), ("A_PECAKN", "EC"), ("A_POAAKN", "POA"), ("A_PRIAKN", "PRI")):
+        v[x[kpp]] = A(s, 0)
+    for kpp, s in (("L_SO4MIN2", "SO4"), ("L_NO3MIN", "NO3"), ("L_NH4PLUS", "NH4"), ("L_CLMIN", "CL")):
+        v[x[kpp]] = A(s, 1) + A(s, 2)
+    for kpp, s in (("L_PRIACC", "PRI"), ("L_NAPLUS", "NA"), ("L_CAPLUS2", "CAACC"), ("L_MGPLUS2", "MGACC"),
+                   ("L_KPLUS", "KACC"), ("L_PECACC", "EC"), ("L_POAACC", "POA")):
+        v[x[kpp]] = A(s, 1)
+    v[x["L_ORGC"]] = f32(0.2) * A("ORGC", 1)
+    v[x["L_OXLACMIN2"]] = f32(0.8) * A("ORGC", 1) / f32(np.float32(90.03) / np.float32(177.0))
+    if ispc8:
+        for s in ("IETET", "IEOS", "DIMER", "IMGA", "IMOS"):
+            v[x["L_" + s]] = A(s, 1)
+    else:
+        v[x["L_ISO3"]] = A("ISO3", 1)
+    v[x["L_SO4MIN2"]] = v[x["L_SO4MIN2"]] + G("H2SO4")
+    return v
+
+
+def test_whole_aqchem_conserves_mass_like_the_reference_checks(o):
+    """aqchem_kmt.F90:919-973 warns when S, N (without NH3), NH3/NH4 or Cl change by more than
+    0.5 % between the inputs and GAS + AEROSOL + wet deposition; the restatement stays far
+    inside that on seeded cells, every output is non-negative, N2O5 and H2SO4 end at zero
+    (moved to HNO3 and sulfate), and the scavenged fractions lie in [0, 1]."""
+    for ispc8, mtpyrac in ((0, 0), (1, 1)):
+        p, g, a, idx, fac = o.synthetic_columns(40, seed=61 + ispc8, ispc8=ispc8, mtpyrac=mtpyrac)
+        g2, a2, gw, aw, out, st, nf = o.aqchem(p, g, a, idx, fac)
+        assert nf == 0 and (st[:, S["ierr"]] == 1).all()
+        assert np.abs(out[:, 6:10]).max() < 1e-2                     # percent
+        assert (g2 >= 0).all() and (a2 >= 0).all() and (gw >= 0).all() and (aw >= 0).all()
+        gn, _ = _aq_names()
+        assert (g2[:, gn.index("N2O5")] == 0).all() and (g2[:, gn.index("H2SO4")] == 0).all()
+        assert ((out[:, 2:6] >= 0) & (out[:, 2:6] <= 1)).all()
+        assert (out[:, 1] >= 0).all()                                # BETASO4
+
+
+def test_whole_aqchem_maps_into_the_kinetic_core_and_back(o):
+    """The state AQCHEM hands the kinetic core is Initialize's mapping (restated here from
+    the reference text), with GAS's HO as the fixed OH: the kinetic core on that state gives
+    the same final state, so GAS(O3) = (G_O3 + L_O3) / CFACTOR and GAS(H2O2) = (G_H2O2 +
+    L_H2O2) / CFACTOR (aqchem_kmt.F90:785-786) to the last bit."""
+    p, g, a, idx, fac = o.synthetic_columns(6, seed=71)
+    g2, a2, gw, aw, out, st, nf = o.aqchem(p, g, a, idx, fac)
+    gn, an = _aq_names()
+    ix = o.index
+    for c in range(6):
+        v = _map_in(o, p[c], g[c], a[c])
+        na = len(an)
+        fe_iii = 0.9 if np.float32(p[c, P_COSZEN]) <= 0 else 0.1
+        soil, anth, seas = a[c, an.index("SOILC") + 2 * na], a[c, an.index("ANTHC") + 2 * na], a[c, an.index("SEASC") + 2 * na]
+        # coarse crustal cations (aqchem_Initialize.F90:392-421)
+        v[ix["L_NAPLUS"]] += fac[4] * seas + fac[5] * soil + fac[6] * anth
+        v[ix["L_CAPLUS2"]] += fac[10] * seas + fac[11] * soil + fac[12] * anth
+        v[ix["L_MGPLUS2"]] += fac[7] * seas + fac[8] * soil + fac[9] * anth
+        v[ix["L_KPLUS"]] += fac[13] * seas + fac[14] * soil + fac[15] * anth
+        v[ix["L_FEPLUS3"]] = 0.1 * fe_iii * (a[c, an.index("FEACC") + na] + (fac[0] * soil + fac[1] * anth))
+        v[ix["L_MNPLUS2"]] = 0.5 * 1.0 * (a[c, an.index("MNACC") + na] + (fac[2] * soil + fac[3] * anth))
+        pc = p[c].copy()
+        pc[P_HO] = g[c, gn.index("HO")]
+        var, fix, stc, nfc = o.cells(pc[None], v[None])
+        _, _, _, _, sc = o.setup(pc, v)
+        inv = 1.0 / sc["cfactor"]
+        assert g2[c, gn.index("O3")] == (var[0, ix["G_O3"]] + var[0, ix["L_O3"]]) * inv
+        assert g2[c, gn.index("H2O2")] == (var[0, ix["G_H2O2"]] + var[0, ix["L_H2O2"]]) * inv
+        assert np.array_equal(stc[0], st[c])
