@@ -45,7 +45,11 @@ VARIANTS = {"default": (GEN_DEFAULT, ["-DCHEM_QUEUE_WARPS_PER_SM=16"]),
                          ["-DCHEM_QUEUE_WARPS_PER_SM=16"]),
             # more resident warps for lower register caps (20 warps: 4-warp blocks; 24: 8-warp blocks)
             "r96w20": (["-maxrregcount=96", "-DCHEM_USE_PREFETCH"], ["-DCHEM_QUEUE_WARPS_PER_SM=20"]),
-            "r80w24": (["-maxrregcount=80", "-DCHEM_USE_PREFETCH"], ["-DCHEM_QUEUE_WARPS_PER_SM=24"])}
+            "r80w24": (["-maxrregcount=80", "-DCHEM_USE_PREFETCH"], ["-DCHEM_QUEUE_WARPS_PER_SM=24"]),
+            "r80w24rcp": (["-maxrregcount=80", "-DCHEM_USE_PREFETCH", "-DCHEM_RCP(x)=__drcp_rn(x)"],
+                          ["-DCHEM_QUEUE_WARPS_PER_SM=24"]),
+            "r72w28": (["-maxrregcount=72", "-DCHEM_USE_PREFETCH"], ["-DCHEM_QUEUE_WARPS_PER_SM=28"]),
+            "r64w32": (["-maxrregcount=64", "-DCHEM_USE_PREFETCH"], ["-DCHEM_QUEUE_WARPS_PER_SM=32"])}
 
 
 def _is_generated_math(src: Path) -> bool:

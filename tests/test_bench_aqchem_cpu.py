@@ -49,7 +49,7 @@ def test_run_aqchem_bookkeeping_on_the_host(kmt2_harness, tmp_path, monkeypatch)
                         else to(self, *a, **k))
     sys.path.insert(0, str(ROOT))
     import bench
-    r = bench.run_aqchem(0, 40, 2, 1, 2)
+    r = bench.run_aqchem(0, 40, 2, 1, 2, whole=False)
     assert r["ncell"] == 40 and r["failed_cells"] == 0 and r["value"] > 0
     assert 20 < r["steps_per_cell"] < 100
     fl = bench_manifest_flops()
