@@ -94,6 +94,12 @@ struct cmaqchem_handle {
     // tuning knobs (cmaqchem_diag_set_tuning)
     int use_night = 1;
     double dtmin = ros3::DTMIN;   // ROS3 minimum step (rbsolver.F:105), lowered only by a tuning knob
+    // rate-constant pass of the work-queue ROS3 call: CALC_RCONST of every cell by whole warps
+    // before the solver kernel, which then gathers the rates instead of evaluating them in
+    // the few lanes it refills at a time (same numbers); allocated at set-up when it fits
+    int rconst_pass = 1;
+    double* d_rki_all = nullptr;
+    uint8_t* d_sun_all = nullptr;
     int q_sync = 1;          // work-queue kernel: barriers between attempt phases
     int q_wpb = 8;           // work-queue kernel: warps per block
     int q_nblocks = 0;
@@ -157,7 +163,7 @@ void free_handle(cmaqchem_handle* h)
                     h->s_qv, h->s_dens, h->s_pres, h->s_seaice, h->s_osz, h->s_rj, h->s_khet,
                     h->d_adj_ws, h->d_tape_y, h->d_tape_h, h->d_tape_off, h->d_tiles, h->d_tape_tot,
                     h->d_adj_order, h->d_adj_status, h->d_adj_counters, h->d_yave, h->d_gear_coef,
-                    h->d_ebi_def, h->d_ebi_ndef};
+                    h->d_ebi_def, h->d_ebi_ndef, h->d_rki_all, h->d_sun_all};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
@@ -417,6 +423,24 @@ extern "C" int cmaqchem_init(const cmaqchem_cfg* cfg, cmaqchem_handle** out)
         CK(cudaMalloc(&h->d_hist, sizeof(unsigned int) * chem::QUEUE_BINS));
         CK(cudaMalloc(&h->d_cursor, sizeof(unsigned long long) * chem::QUEUE_BINS));
         CK(cudaMalloc(&h->d_head, sizeof(unsigned long long)));
+        if (cfg->solver == CMAQCHEM_SOLVER_ROS3 && cfg->schedule == CMAQCHEM_SCHED_QUEUE) {
+            // the rate-constant pass's arrays, when they leave a quarter of the free memory
+            const size_t bytes = sizeof(double) * (size_t)m->nrxns * h->ncell;
+            size_t free_b = 0, total_b = 0;
+            CK(cudaMemGetInfo(&free_b, &total_b));
+            if (bytes + h->ncell < free_b - free_b / 4 && cudaMalloc(&h->d_rki_all, bytes) == cudaSuccess &&
+                cudaMalloc(&h->d_sun_all, h->ncell) == cudaSuccess) {
+                h->rconst_pass = 1;
+            } else {
+                cudaGetLastError();   // a failed allocation leaves the pass off, not an error
+                if (h->d_rki_all) cudaFree(h->d_rki_all);
+                h->d_rki_all = nullptr;
+                h->d_sun_all = nullptr;
+                h->rconst_pass = 0;
+            }
+        } else {
+            h->rconst_pass = 0;
+        }
         CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
         CK(cudaEventCreate(&h->ev0));
         CK(cudaEventCreate(&h->ev1));
@@ -467,6 +491,13 @@ extern "C" int cmaqchem_diag_set_tuning(cmaqchem_handle* h, const char* key, int
         // ROS3 minimum step 10^value min (the reference's DTMIN is 1e-8, value -8)
         if (value < -30 || value > -2) return fail("ros3_dtmin_exp must be in [-30, -2]");
         h->dtmin = pow(10.0, (double)value);
+        if (h->graph_exec) CK(cudaGraphExecDestroy(h->graph_exec));
+        h->graph_exec = nullptr;
+        return 0;
+    } else if (strcmp(key, "rconst_pass") == 0) {
+        // 1: the work-queue ROS3 call evaluates CALC_RCONST in a pass of whole warps first
+        // (when its arrays were allocated at set-up); 0: in the refilled lanes; same numbers
+        h->rconst_pass = value != 0;
         if (h->graph_exec) CK(cudaGraphExecDestroy(h->graph_exec));
         h->graph_exec = nullptr;
         return 0;
@@ -551,6 +582,12 @@ static int enqueue_step(cmaqchem_handle* h, const chem::GridArgs& a, int itmstep
             } else {
                 CK(h->ops->chem_ebi(a, q, e, h->nblocks, s));
             }
+        } else if (h->rconst_pass && h->d_rki_all) {
+            CK(h->ops->rconst_pass(a, c0, c1, h->d_rki_all, h->d_sun_all, h->nblocks, s));
+            chem::GridArgs ap = a;
+            ap.rki_all = h->d_rki_all;
+            ap.sun_all = h->d_sun_all;
+            CK(h->ops->chem_queue(ap, q, h->q_sync, h->q_wpb, h->q_nblocks, s));
         } else {
             CK(h->ops->chem_queue(a, q, h->q_sync, h->q_wpb, h->q_nblocks, s));
         }

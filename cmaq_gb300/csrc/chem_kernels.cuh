@@ -59,6 +59,9 @@ struct GridArgs {
                                    //      step attempts of sunlit cells
     int use_night;                 // 1: all-dark warps use the night pattern; 0: day pattern always
     double* yave;                  // [ischan][ncell] time-averaged Y of the call (DDM-3D), or nullptr
+    const double* rki_all;         // [nrxns][ncell] rate constants of the call's cells from k_rconst_pass, or
+                                   // nullptr (gather_cell evaluates CALC_RCONST itself)
+    const uint8_t* sun_all;        // [ncell] sunlight flags of the same pass
 };
 
 // DDM-3D: the cell's time-averaged concentrations (rbsolver.F:592-595) to a.yave
@@ -105,6 +108,24 @@ __device__ bool gather_cell(const GridArgs& a, long long c, double* __restrict__
     for (int k = 0; k < M::NHETERO; ++k) hetv[k] = a.khet[(size_t)c * M::NHETERO + k];
     M::rconst(ws, temp, press, h2o, seawater, sun ? 1 : 0, rjv, hetv);
     return sun;
+}
+
+// Gather one cell into ws: concentrations as gather_cell, and the rate constants from the
+// call's rate-constant pass when there is one (the same numbers, computed by whole warps
+// over consecutive cells instead of by the few lanes a work queue refills at a time).
+template <class M>
+__device__ bool gather_cell_pass(const GridArgs& a, long long c, double* __restrict__ ws)
+{
+    if (!a.rki_all) return gather_cell<M>(a, c, ws);
+    const float densf = a.dens[c];
+    const float svol = __fdiv_rn(1.0f, densf);
+    for (int s = 0; s < M::ISCHAN; ++s) {
+        const float conc = a.cgrid[(size_t)a.cgrid_index[s] * a.ncell + c];
+        const float v = a.convert[s] ? __fmul_rn(__fmul_rn(a.fwd_conv[s], svol), conc) : conc;
+        ws[(M::OFF_Y + M::iold2new(s)) * 32] = (double)fmaxf(v, CONCMIN_F);
+    }
+    for (int r = 0; r < M::NRXNS; ++r) ws[(M::OFF_RKI + r) * 32] = a.rki_all[(size_t)r * a.ncell + c];
+    return a.sun_all[c] != 0;
 }
 
 template <class M>
@@ -213,6 +234,25 @@ __global__ void __launch_bounds__(THREADS_PER_BLOCK, 1) k_ros3_solve(SolveArgs a
             if (a.cell_status) a.cell_status[c] = st.status;
             if (a.cell_nsteps) a.cell_nsteps[c] = st.nsteps;
             if (a.cell_nfails) a.cell_nfails[c] = st.nfails;
+        }
+    }
+}
+
+// The rate-constant pass of a CHEM call: CALC_RCONST of cells [c0, c1) by whole warps in grid
+// order into rki[nrxns][ncell] and sunlit[ncell], for gather_cell_pass.
+template <class M>
+__global__ void __launch_bounds__(THREADS_PER_BLOCK, 1) k_rconst_pass(GridArgs a, long long c0, long long c1,
+                                                                      double* rki, uint8_t* sunlit)
+{
+    const long long nwarps = (long long)gridDim.x * WARPS_PER_BLOCK;
+    const long long warp = (long long)blockIdx.x * WARPS_PER_BLOCK + (threadIdx.x >> 5);
+    double* ws = warp_ws<M>(a.ws, warp);
+    for (long long base = c0 + warp * 32; base < c1; base += nwarps * 32) {
+        const long long c = base + (threadIdx.x & 31);
+        if (c < c1) {
+            const bool sun = gather_cell<M>(a, c, ws);
+            for (int r = 0; r < M::NRXNS; ++r) rki[(size_t)r * a.ncell + c] = ws[(M::OFF_RKI + r) * 32];
+            sunlit[c] = sun ? 1 : 0;
         }
     }
 }

@@ -39,6 +39,8 @@ struct MechOps {
     cudaError_t (*adj_occupancy)(int* forward_bps, int* reverse_bps);
     cudaError_t (*ddm_update)(const chem::GridArgs&, const chem::DdmArgs&, int nblocks, cudaStream_t);
     cudaError_t (*rconst)(const chem::GridArgs&, double* rki, uint8_t* sunlit, int nblocks, cudaStream_t);
+    cudaError_t (*rconst_pass)(const chem::GridArgs&, long long c0, long long c1, double* rki, uint8_t* sunlit,
+                               int nblocks, cudaStream_t);
     cudaError_t (*occupancy)(int* blocks_per_sm);
     int gear_ws_elems;
     // grid: one Gear CHEM call on GridArgs; otherwise the solver-level entry on GearArgs' arrays
@@ -164,6 +166,12 @@ struct MechOps {
         chem::k_rconst<T_><<<nb, chem::THREADS_PER_BLOCK, 0, s>>>(a, rki, sun);                     \
         return cudaGetLastError();                                                                  \
     }                                                                                               \
+    cudaError_t rconst_pass_(const chem::GridArgs& a, long long c0, long long c1, double* rki, uint8_t* sun, \
+                             int nb, cudaStream_t s)                                                \
+    {                                                                                               \
+        chem::k_rconst_pass<T_><<<nb, chem::THREADS_PER_BLOCK, 0, s>>>(a, c0, c1, rki, sun);        \
+        return cudaGetLastError();                                                                  \
+    }                                                                                               \
     cudaError_t gear_(const chem::GridArgs& a, const chem::QueueArgs& q, const chem::GearArgs& g, bool grid, \
                       int nb, cudaStream_t s)                                                       \
     {                                                                                               \
@@ -231,5 +239,5 @@ struct MechOps {
                                    solve_, chem_ebi_, ebi_solve_, chem_ebi_warp_, ebi_warp_occupancy_, \
                                    T_::EBI_DELTAT,                                                  \
                                    T_::ADJ_WS_ELEMS, adj_forward_, adj_reverse_, adj_occupancy_, ddm_update_,     \
-                                   rconst_, occupancy_, T_::GEAR_WS_ELEMS, gear_, gear_occupancy_,   \
+                                   rconst_, rconst_pass_, occupancy_, T_::GEAR_WS_ELEMS, gear_, gear_occupancy_, \
                                    gear_warp_, gear_warp_occupancy_};

@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(WPB * 32, CHEM_QUEUE_WARPS_PER_SM / WPB > 0 ? 
                     const unsigned long long pos = base + __popc(need & ((1u << lane) - 1u));
                     if (pos < queue_len(q, a.ncell)) {
                         cell = q.cell0 + (q.order ? q.order[pos] : (long long)pos);
-                        sun = gather_cell<M>(a, cell, ws);
+                        sun = gather_cell_pass<M>(a, cell, ws);
                         ros3::start(s);
                         if (a.yave) {
                             s.yave = true;

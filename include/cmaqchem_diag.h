@@ -47,6 +47,10 @@ int cmaqchem_diag_fp64_issue(int device, int active_lanes, double* cycles_per_in
  * consecutive cells; 0 (default): the largest step's tape, halved until it fits) and
  * "ros3_dtmin_exp" (ROS3's minimum step is 10^value minutes; default -8, the reference's
  * DTMIN; a lower value lets tight tolerances pass the initial radical transient) and
+ * "rconst_pass" (1, default when its arrays fit at set-up: the work-queue ROS3 call
+ * evaluates CALC_RCONST of every cell in a pass of whole warps before the solver kernel,
+ * which gathers the rates; 0: the solver kernel evaluates them in the lanes it refills;
+ * same results) and
  * "queue_history" (0: clear the step counts the work queue is ordered by, so that the next
  * call is queued as a fresh run's first call) and
  * "host_chunks" (1-16, default 4: cmaqchem_step moves the grid in that many chunks of
