@@ -80,6 +80,8 @@ def lib(variant: str = "default") -> C.CDLL:
     L.cmaqchem_diag_phase_cycles.argtypes = [C.c_int, C.POINTER(C.c_ulonglong), C.c_int]
     L.cmaqchem_kmt2_workspace_doubles.argtypes = [C.c_longlong]
     L.cmaqchem_kmt2_workspace_doubles.restype = C.c_longlong
+    L.cmaqchem_kmt2_default_lanes.argtypes = [C.c_int]
+    L.cmaqchem_kmt2_default_lanes.restype = C.c_longlong
     L.cmaqchem_kmt2_solve_device.argtypes = [C.c_longlong, vp, vp, vp, vp, vp, vp, C.c_longlong, vp]
     L.cmaqchem_kmt2_solve.argtypes = [C.c_longlong, vp, vp, vp, vp, vp, C.c_int]
     L.cmaqchem_aqchem_device.argtypes = [C.c_longlong, vp, vp, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, C.c_longlong, vp]

@@ -22,7 +22,6 @@ NVAR, NFIX, NPARAM = 161, 4, 15
 PARAMS = ("temp2", "pres_pa", "taucld", "prcrate", "wcavg", "wtavg", "airm", "alfa0", "alfa3", "coszen", "jh2o2",
           "ho", "ispc8", "mtpyrac", "photo")
 STATS = ("nstp", "nacc", "nrej", "nfun", "njac", "ndec", "nsol", "nsng", "ierr", "npass")
-LANES_PER_SM = 256   # two 128-thread blocks of 255 registers each fit an SM
 
 
 def _ptr(t: torch.Tensor | None):
@@ -30,10 +29,12 @@ def _ptr(t: torch.Tensor | None):
 
 
 def aqchem_kinetics(params: torch.Tensor, var_mix: torch.Tensor, *, lanes: int | None = None, with_fix: bool = False,
-                    stream: torch.cuda.Stream | None = None):
+                    stream: torch.cuda.Stream | None = None, variant: str = "default"):
     """Integrate n cloudy cells over their TAUCLD; returns (var_out, stats) or, with
-    with_fix, (var_out, fix_out, stats).  ``lanes`` caps the cells integrated at once
-    (the workspace holds 25.6 KB per lane); by default 256 per SM."""
+    with_fix, (var_out, fix_out, stats).  ``lanes`` is the number of threads that take
+    cells from the call's queue (the workspace holds 23 KB per lane); by default as
+    many as the device holds resident (cmaqchem_kmt2_default_lanes).  ``variant``: a
+    library build of ``cmaq_gb300.build`` (same bits in all)."""
     for name, t, rows in (("params", params, NPARAM), ("var_mix", var_mix, NVAR)):
         if not (t.is_cuda and t.dtype == torch.float64 and t.dim() == 2 and t.shape[0] == rows and t.is_contiguous()):
             raise ValueError(f"{name} must be a contiguous float64 CUDA tensor of shape ({rows}, n)")
@@ -46,9 +47,11 @@ def aqchem_kinetics(params: torch.Tensor, var_mix: torch.Tensor, *, lanes: int |
     stats = torch.zeros((len(STATS), n), dtype=torch.int32, device=dev)
     if n == 0:
         return (var_out, fix_out, stats) if with_fix else (var_out, stats)
-    L = _lib.lib()
+    L = _lib.lib(variant)
     if lanes is None:
-        lanes = torch.cuda.get_device_properties(dev).multi_processor_count * LANES_PER_SM
+        lanes = L.cmaqchem_kmt2_default_lanes(dev.index if dev.index is not None else torch.cuda.current_device())
+        if lanes < 1:
+            raise _lib.ChemError(_lib.last_error())
     lanes = max(1, min(int(lanes), n))
     ws = torch.empty(L.cmaqchem_kmt2_workspace_doubles(lanes), dtype=torch.float64, device=dev)
     s = stream or torch.cuda.current_stream(dev)
@@ -83,7 +86,7 @@ OUTS = ("hpwdep", "betaso4", "fractr", "fracpoa", "fracpri", "fracsoa", "mbal_s"
 
 
 def aqchem(params: torch.Tensor, gas: torch.Tensor, aerosol: torch.Tensor, aer_index, factors, *,
-           lanes: int | None = None, stream: torch.cuda.Stream | None = None):
+           lanes: int | None = None, stream: torch.cuda.Stream | None = None, variant: str = "default"):
     """The whole AQCHEM (mapping of GAS and AEROSOL into the KPP state, the kinetic core,
     redistribution; include/cmaqchem.h: cmaqchem_aqchem_device) for n cloudy cells.
     ``params`` [15][n], ``gas`` [29][n] and ``aerosol`` [naer * 3][n] float64 CUDA tensors
@@ -111,9 +114,11 @@ def aqchem(params: torch.Tensor, gas: torch.Tensor, aerosol: torch.Tensor, aer_i
     stats = torch.zeros((len(STATS), n), dtype=torch.int32, device=dev)
     if n == 0:
         return gwd, awd, out, stats
-    L = _lib.lib()
+    L = _lib.lib(variant)
     if lanes is None:
-        lanes = torch.cuda.get_device_properties(dev).multi_processor_count * LANES_PER_SM
+        lanes = L.cmaqchem_kmt2_default_lanes(dev.index if dev.index is not None else torch.cuda.current_device())
+        if lanes < 1:
+            raise _lib.ChemError(_lib.last_error())
     lanes = max(1, min(int(lanes), n))
     ws = torch.empty(L.cmaqchem_kmt2_workspace_doubles(lanes), dtype=torch.float64, device=dev)
     s = stream or torch.cuda.current_stream(dev)
@@ -123,3 +128,58 @@ def aqchem(params: torch.Tensor, gas: torch.Tensor, aerosol: torch.Tensor, aer_i
                                             _ptr(awd), _ptr(out), _ptr(stats), _ptr(ws), ws.numel(),
                                             C.c_void_p(s.cuda_stream)))
     return gwd, awd, out, stats
+
+
+def sweep(ncell: int, specs, reps: int = 2, seed: int = 2018) -> dict:
+    """Launch-shape sweep of the kinetic core: for each spec "variant:lanes_per_sm" (a
+    build of ``cmaq_gb300.build`` and the lanes per SM of the call) the device time of one
+    call on ``ncell`` seeded cloudy cells (median of 3, after one untimed call), the FP64
+    rate from the routines' operation counts, and whether the state equals the first
+    spec's bit for bit."""
+    import numpy as np
+    from .synthetic import kmt2_manifest, make_cloud_cells
+    fl = kmt2_manifest()["flops"]
+    p, v = make_cloud_cells(ncell, seed=seed)
+    pt = torch.from_numpy(np.ascontiguousarray(p.T)).cuda()
+    vt = torch.from_numpy(np.ascontiguousarray(v.T)).cuda()
+    nsm = torch.cuda.get_device_properties(pt.device).multi_processor_count
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ref, out = None, {}
+    for rep in range(reps):
+        for spec in specs:
+            variant, lps = spec.split(":")
+            lanes = min(ncell, nsm * int(lps))
+            aqchem_kinetics(pt, vt, lanes=lanes, variant=variant)
+            ms = []
+            for _ in range(3):
+                ev[0].record()
+                var, st = aqchem_kinetics(pt, vt, lanes=lanes, variant=variant)
+                ev[1].record()
+                torch.cuda.synchronize()
+                ms.append(ev[0].elapsed_time(ev[1]))
+            sd = st.cpu().numpy().astype(np.int64)
+            flops = float(sd[3].sum() * fl["fun"] + sd[4].sum() * fl["jac"] + sd[5].sum() * fl["decomp"]
+                          + sd[6].sum() * fl["solve"] + sd[0].sum() * fl["vector"])
+            vo = var.cpu().numpy()
+            ref = vo.copy() if ref is None else ref
+            m = float(np.median(ms))
+            r = {"ms": m, "cells_per_s": ncell / m * 1e3, "tflops": flops / m / 1e9,
+                 "same_bits": bool(np.array_equal(vo, ref, equal_nan=True))}
+            out.setdefault(spec, []).append(r)
+            print(f"rep {rep} {spec}: {m:.1f} ms ({ncell} cells, {lanes} lanes), {r['cells_per_s']:.0f} cells/s, "
+                  f"{r['tflops']:.4f} TFLOP/s, same bits: {r['same_bits']}", flush=True)
+    return out
+
+
+if __name__ == "__main__":
+    import argparse
+    from . import build as cbuild
+    ap = argparse.ArgumentParser(description="launch-shape sweep of the KMT2 kinetic core (see sweep())")
+    ap.add_argument("specs", help="comma-separated variant:lanes_per_sm, e.g. default:512,kq3:384")
+    ap.add_argument("--cells", type=int, default=200000)
+    ap.add_argument("--reps", type=int, default=2)
+    a = ap.parse_args()
+    specs = a.specs.split(",")
+    for v in dict.fromkeys(sp.split(":")[0] for sp in specs):
+        cbuild.build(variant=v)
+    sweep(a.cells, specs, a.reps)

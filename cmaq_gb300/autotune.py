@@ -8,9 +8,10 @@ of a sample of the grid for each candidate:
 
 * cells per block: 64, 128 or 256 (``block_warps`` 2, 4, 8; one cell per thread);
 * register cap and prefetch: library variants of ``cmaq_gb300.build`` (the default
-  library caps the generated functions at 128 registers for 16 warps per SM and
-  prefetches workspace rows; ``g168`` 168 registers and 12 warps; ``nopf`` 168 without
-  the prefetch; ``full255`` no cap (8 warps); ``r168`` caps every function);
+  library caps the generated functions at 80 registers for 24 warps per SM and
+  prefetches workspace rows; ``w16`` 128 registers and 16 warps; ``g168`` 168 registers
+  and 12 warps; ``nopf`` 168 without the prefetch; ``full255`` no cap (8 warps);
+  ``r168`` caps every function);
 * queue granularity: whether the block's warps pass barriers between the phases of
   each step attempt (``lockstep`` 1), also between the generated chunks of the LU
   and the solves (2), or run free (0, 256-cell blocks only); a lane always refills
@@ -45,7 +46,7 @@ class Candidate:
         return {"block_warps": self.block_warps, "lockstep": self.lockstep}
 
 
-def candidates(variants=("default", "g168", "nopf", "full255", "r168")) -> list[Candidate]:
+def candidates(variants=("default", "w16", "g168", "nopf", "full255", "r168")) -> list[Candidate]:
     out = []
     for v in variants:
         out.append(Candidate(v, 0, 8))
@@ -129,3 +130,67 @@ def tuned_solver(g, result: dict, **kw) -> ChemSolver:
                    schedule="queue", variant=result["variant"], **kw)
     s.set_tuning(block_warps=result["block_warps"], lockstep=result["lockstep"])
     return s
+
+
+def sweep(g, specs, ncalls: int = 12, reps: int = 2, verbose: bool = True) -> dict:
+    """Launch-shape sweep: for each spec "variant:block_warps:lockstep:rconst_pass" (later
+    fields optional; defaults 8, 1, 1) the device time of ``ncalls`` graph-replayed CHEM
+    calls of grid ``g`` after one call from the initial state (the queue history is then
+    cleared, so every spec starts from the same queue order), ``reps`` times, with the
+    FP64 rate and whether the final concentrations equal the first spec's bit for bit."""
+    import torch
+    from . import _lib
+    info, _ = _lib.mech_info(g.mech)
+    dev = {k: torch.from_numpy(np.ascontiguousarray(getattr(g, k))).cuda() for k in KEYS}
+    conc0 = dev["conc"].clone()
+    args = [dev[k] for k in KEYS]
+    ref, out = None, {}
+    for rep in range(reps):
+        for spec in specs:
+            f = spec.split(":")
+            knobs = dict(zip(("block_warps", "lockstep", "rconst_pass"), (int(x) for x in f[1:])))
+            knobs = {"block_warps": 8, "lockstep": 1, "rconst_pass": 1, **knobs}
+            s = ChemSolver(g.mech, ncols=g.ncols, nrows=g.nrows, nlays=g.nlays, nspcsd=g.nspcsd,
+                           cgrid_index=g.cgrid_index, rtol=1e-3, atol=1e-9, schedule="queue", variant=f[0])
+            try:
+                s.set_tuning(**knobs)
+                dev["conc"].copy_(conc0)
+                s.steps(1, *args)
+                dev["conc"].copy_(conc0)
+                s.set_tuning(queue_history=0)
+                st = s.steps(ncalls, *args)
+                torch.cuda.synchronize()
+            finally:
+                s.close()
+            conc = dev["conc"].cpu().numpy()
+            ref = conc.copy() if ref is None else ref
+            att = st["accepted_steps"] + st["rejected_steps"]
+            sun = st["sunlit_attempts"]
+            tf = (sun * info.flops_step_day + (att - sun) * info.flops_step_night) / (st["device_ms"] * 1e-3) / 1e12
+            r = {"ms": st["device_ms"], "tflops": tf, "same_bits": bool(np.array_equal(conc, ref)),
+                 "attempts_per_cell_and_call": att / g.ncell / ncalls}
+            out.setdefault(spec, []).append(r)
+            if verbose:
+                print(f"rep {rep} {spec}: {r['ms']:.0f} ms for {ncalls} calls, {r['tflops']:.4f} TFLOP/s, "
+                      f"{r['attempts_per_cell_and_call']:.2f} attempts/cell/call, same bits: {r['same_bits']}",
+                      flush=True)
+    return out
+
+
+if __name__ == "__main__":
+    import argparse
+    from . import build as cbuild
+    from .synthetic import make_grid
+    ap = argparse.ArgumentParser(description="launch-shape sweep of the batched ROS3 kernel (see sweep())")
+    ap.add_argument("specs", help="comma-separated variant:block_warps:lockstep:rconst_pass")
+    ap.add_argument("--grid", default="459x299x8", help="COLSxROWSxLAYS of the seeded grid")
+    ap.add_argument("--mech", default="cb6r5_ae7_aq")
+    ap.add_argument("--calls", type=int, default=12)
+    ap.add_argument("--reps", type=int, default=2)
+    a = ap.parse_args()
+    specs = a.specs.split(",")
+    for v in dict.fromkeys(sp.split(":")[0] for sp in specs):
+        cbuild.build(variant=v)
+    nc, nr, nl = map(int, a.grid.split("x"))
+    sweep(make_grid(mech=a.mech, ncols=nc, nrows=nr, nlays=nl, seed=2018), specs, a.calls, a.reps)
+

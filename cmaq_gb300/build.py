@@ -23,33 +23,36 @@ BUILD = PKG / "_build"
 LIB = BUILD / "libcmaqchem.so"
 # Build variants the autotuner can choose from: name -> (extra nvcc flags of the generated
 # mechanism code, extra flags of every translation unit).  The default library caps the
-# generated LU / solve / rate / adjoint functions at 128 registers and turns on their L2
-# prefetch a few rows ahead, and the work-queue kernel carries launch bounds for 16
+# generated LU / solve / rate / adjoint functions at 80 registers and turns on their L2
+# prefetch a few rows ahead, and the work-queue kernel carries launch bounds for 24
 # resident warps per SM; this measured fastest (see the launch-shape sweep in profiles/).
 # The EBI routines and the kernels' own code are not capped.
-GEN_DEFAULT = ["-maxrregcount=128", "-DCHEM_USE_PREFETCH"]
-Q8 = "-DCHEM_QUEUE_WARPS_PER_SM=8"
-VARIANTS = {"default": (GEN_DEFAULT, ["-DCHEM_QUEUE_WARPS_PER_SM=16"]),
+GEN_DEFAULT = ["-maxrregcount=80", "-DCHEM_USE_PREFETCH"]
+Q_DEFAULT = "-DCHEM_QUEUE_WARPS_PER_SM=24"
+GEN128 = ["-maxrregcount=128", "-DCHEM_USE_PREFETCH"]
+Q8, Q16 = "-DCHEM_QUEUE_WARPS_PER_SM=8", "-DCHEM_QUEUE_WARPS_PER_SM=16"
+VARIANTS = {"default": (GEN_DEFAULT, [Q_DEFAULT]),
+            "w16": (GEN128, [Q16]),   # 128 registers, 16 warps per SM
             "g168": (["-maxrregcount=168", "-DCHEM_USE_PREFETCH"], []),
             "nopf": (["-maxrregcount=168"], []),
             "full255": ([], [Q8]), "pf255": (["-DCHEM_USE_PREFETCH"], [Q8]),
             "r168": ([], ["-maxrregcount=168"]),
-            "r128": ([], ["-maxrregcount=128", "-DCHEM_QUEUE_WARPS_PER_SM=16"]),
+            "r128": ([], ["-maxrregcount=128", Q16]),
             "lucs": ([], ["-DCHEM_LDLU(p)=__ldcs(p)", Q8]),
             # the default build with clock counters between the attempt's phase barriers
-            "phases": (GEN_DEFAULT, ["-DCHEM_QUEUE_WARPS_PER_SM=16", "-DCHEM_PHASE_TIMING"]),
+            "phases": (GEN_DEFAULT, [Q_DEFAULT, "-DCHEM_PHASE_TIMING"]),
             # 1/U(i,i) by the correctly rounded reciprocal (same bits); L1 prefetch of the next row
-            "rcp": (GEN_DEFAULT + ["-DCHEM_RCP(x)=__drcp_rn(x)"], ["-DCHEM_QUEUE_WARPS_PER_SM=16"]),
-            "pfl1": (GEN_DEFAULT + ["-DCHEM_USE_PREFETCH_L1"], ["-DCHEM_QUEUE_WARPS_PER_SM=16"]),
-            "rcp_pfl1": (GEN_DEFAULT + ["-DCHEM_RCP(x)=__drcp_rn(x)", "-DCHEM_USE_PREFETCH_L1"],
-                         ["-DCHEM_QUEUE_WARPS_PER_SM=16"]),
-            # more resident warps for lower register caps (20 warps: 4-warp blocks; 24: 8-warp blocks)
+            "rcp": (GEN_DEFAULT + ["-DCHEM_RCP(x)=__drcp_rn(x)"], [Q_DEFAULT]),
+            "pfl1": (GEN_DEFAULT + ["-DCHEM_USE_PREFETCH_L1"], [Q_DEFAULT]),
+            # other register caps with as many resident warps as they allow
             "r96w20": (["-maxrregcount=96", "-DCHEM_USE_PREFETCH"], ["-DCHEM_QUEUE_WARPS_PER_SM=20"]),
-            "r80w24": (["-maxrregcount=80", "-DCHEM_USE_PREFETCH"], ["-DCHEM_QUEUE_WARPS_PER_SM=24"]),
-            "r80w24rcp": (["-maxrregcount=80", "-DCHEM_USE_PREFETCH", "-DCHEM_RCP(x)=__drcp_rn(x)"],
-                          ["-DCHEM_QUEUE_WARPS_PER_SM=24"]),
             "r72w28": (["-maxrregcount=72", "-DCHEM_USE_PREFETCH"], ["-DCHEM_QUEUE_WARPS_PER_SM=28"]),
-            "r64w32": (["-maxrregcount=64", "-DCHEM_USE_PREFETCH"], ["-DCHEM_QUEUE_WARPS_PER_SM=32"])}
+            "r64w32": (["-maxrregcount=64", "-DCHEM_USE_PREFETCH"], ["-DCHEM_QUEUE_WARPS_PER_SM=32"]),
+            # KMT2 kernels built for 2 or 3 resident 128-lane blocks per SM (255 / 168 registers;
+            # the default is 4, 128 registers), or without the block barriers between phases
+            "kq2": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_MIN_BLOCKS=2"]),
+            "kq3": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_MIN_BLOCKS=3"]),
+            "kqfree": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_LOCKSTEP=0"])}
 
 
 def _is_generated_math(src: Path) -> bool:
@@ -83,8 +86,8 @@ def lib_path(variant: str = "default") -> Path:
 
 
 def build(jobs: int | None = None, verbose: bool = False, variant: str = "default") -> Path:
-    """Build one variant of ``VARIANTS`` (``default``: generated functions capped at 128
-    registers with L2 prefetch, 16 resident warps per SM)."""
+    """Build one variant of ``VARIANTS`` (``default``: generated functions capped at 80
+    registers with L2 prefetch, 24 resident warps per SM)."""
     if variant not in VARIANTS:
         raise ValueError(f"unknown variant {variant}")
     out_dir = BUILD if variant == "default" else BUILD / variant

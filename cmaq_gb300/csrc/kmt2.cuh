@@ -19,7 +19,7 @@
 // and REAL(4) intermediates kept, no contraction of a*b+c: the library is compiled with
 // -fmad=false), with exp and x**y by portable series routines (kq_exp, kq_pow) that
 // give the same bits on the host and on the device.  One cell's arrays live in a
-// lane-interleaved FP64 workspace (element i of a lane at ws[i * s]); inputs and
+// lane-interleaved FP64 workspace (element i of a lane at ws[i * KQ_S]); inputs and
 // outputs are [element][cell] with stride n.  The header compiles as plain C++ too, so
 // the host can run exactly this code.
 #pragma once
@@ -39,15 +39,19 @@ namespace kmt2 {
 
 #include "gen/kmt2_aq_consts.cuh"
 
+// The workspace holds a warp's 32 lanes side by side: element i of a lane at ws[i * KQ_S]
+// (ws pointing at the lane's first element), so a warp's access to one element reads 256
+// consecutive bytes and every offset is a constant.
+constexpr long long KQ_S = 32;
+
 // per-cell parameters, [KQ_NPARAM][ncell] (include/cmaqchem.h: CMAQCHEM_KMT2_*)
 enum { P_TEMP2 = 0, P_PRES_PA, P_TAUCLD, P_PRCRATE, P_WCAVG, P_WTAVG, P_AIRM, P_ALFA0, P_ALFA3, P_COSZEN,
        P_JH2O2, P_HO, P_ISPC8, P_MTPYRAC, P_PHOTO, NPARAM };
 // per-cell statistics, [NSTAT][ncell]
 enum { S_NSTP = 0, S_NACC, S_NREJ, S_NFUN, S_NJAC, S_NDEC, S_NSOL, S_NSNG, S_IERR, S_NKRON, NSTAT };
-// workspace layout of one lane (elements)
-constexpr int W_Y = 0, W_YNEW = NVAR, W_FCN0 = 2 * NVAR, W_FCN = 3 * NVAR, W_K = 4 * NVAR, W_YERR = 8 * NVAR,
-              W_JAC0 = 9 * NVAR, W_GHIMJ = W_JAC0 + LU_NONZERO, W_R = W_GHIMJ + LU_NONZERO, W_F = W_R + NREACT,
-              WS_ELEMS = W_F + NFIX;
+// workspace layout of one lane (elements): Y, YNEW, FCN0, K1-K4, JAC0, GHIMJ, the rates, FIX
+constexpr int W_Y = 0, W_YNEW = NVAR, W_FCN0 = 2 * NVAR, W_K = 3 * NVAR, W_JAC0 = 7 * NVAR,
+              W_GHIMJ = W_JAC0 + LU_NONZERO, W_R = W_GHIMJ + LU_NONZERO, W_F = W_R + NREACT, WS_ELEMS = W_F + NFIX;
 
 struct Cell {   // aqchem_Global of one cell
     double temp_kpp, press, lwc, lwcfrac, delinvt, phi2, invphi2, ddiam;
@@ -188,44 +192,44 @@ KQ_HD inline double kq_diffusion_factor(const Cell& c, double krate)
     return q > 1.0 ? 1.0 : q;
 }
 // aqchem_Rates.F90:176-249
-KQ_HD inline double kq_krxn(const Cell& c, const double* v, long long s, double kr, double dh, int rtype, int qy,
+KQ_HD inline double kq_krxn(const Cell& c, const double* v, double kr, double dh, int rtype, int qy,
                             int metal)
 {
     const double phi2 = c.phi2;
     double k = kr * kq_exp(dh * c.delinvt);
-    if (rtype == 1) k = (k / (1.0 + 13.0 * v[L_HPLUS * s] * phi2)) * phi2;
+    if (rtype == 1) k = (k / (1.0 + 13.0 * v[L_HPLUS * KQ_S] * phi2)) * phi2;
     else if (rtype == 3) k = k * phi2;
     else if (rtype == 4) k = k / phi2;
     if (metal > 0) {
-        const double s6 = (v[L_H2SO4 * s] + v[L_HSO4MIN * s] + v[L_SO4MIN2 * s]) * phi2;
+        const double s6 = (v[L_H2SO4 * KQ_S] + v[L_HSO4MIN * KQ_S] + v[L_SO4MIN2 * KQ_S]) * phi2;
         k = k / (1.0 + 75.0 * kq_rpow(s6, 0.67));
     }
     if (qy >= 1) {
         const double k1 = 2.4e+4 * kq_exp(0.0 * c.delinvt);
         const double k2 = 3.7e+5 * kq_exp(-5530.88 * c.delinvt);
         const double k3 = 1.5e+9 * kq_exp(-5280.56 * c.delinvt);
-        const double kt = (k1 * v[L_SO2 * s] + k2 * v[L_HSO3MIN * s] + k3 * v[L_SO3MIN2 * s]) * phi2;
+        const double kt = (k1 * v[L_SO2 * KQ_S] + k2 * v[L_HSO3MIN * KQ_S] + k3 * v[L_SO3MIN2 * KQ_S]) * phi2;
         k = k * kq_diffusion_factor(c, kt);
     }
     return k * phi2;
 }
 // aqchem_Rates.F90:251-362
-KQ_HD inline double kq_kiepox(const Cell& c, const double* v, const double* f, long long s, double kh, double khso4,
+KQ_HD inline double kq_kiepox(const Cell& c, const double* v, const double* f, double kh, double khso4,
                               int type)
 {
     const double phi2 = c.phi2;
     if (c.ispc8 <= 0 ? type > 0 : type < 1) return 0.0;
-    const double h = v[L_HPLUS * s], hso4 = v[L_HSO4MIN * s], so4 = v[L_SO4MIN2 * s];
+    const double h = v[L_HPLUS * KQ_S], hso4 = v[L_HSO4MIN * KQ_S], so4 = v[L_SO4MIN2 * KQ_S];
     double kiepox = kh * h * phi2 + khso4 * hso4 * phi2;
-    double kt = (9.0e-4 * h * phi2 + 1.31e-5 * hso4 * phi2) * f[L_H2O * s] * phi2;
+    double kt = (9.0e-4 * h * phi2 + 1.31e-5 * hso4 * phi2) * f[L_H2O * KQ_S] * phi2;
     if (type <= 1) {
         kt = kt + (8.83e-3 * h * phi2 + 2.92e-6 * hso4 * phi2) * so4 * phi2;
         const double kn = 2.0e-4 * h * phi2 + 2.92e-6 * hso4 * phi2;
         if (c.ispc8 <= 0) {
-            kt = kt + kn * v[L_NO3MIN * s] * phi2;
+            kt = kt + kn * v[L_NO3MIN * KQ_S] * phi2;
         } else {
-            kt = kt + kn * v[L_IETET * s] * phi2;
-            kt = kt + kn * v[L_IEOS * s] * phi2;
+            kt = kt + kn * v[L_IETET * KQ_S] * phi2;
+            kt = kt + kn * v[L_IEOS * KQ_S] * phi2;
         }
     } else {
         kt = kt + (2.0e-4 * h * phi2 + 2.92e-6 * hso4 * phi2) * so4 * phi2;
@@ -236,9 +240,9 @@ KQ_HD inline double kq_kiepox(const Cell& c, const double* v, const double* f, l
 
 // ionic strength and activity coefficients (aqchem_Rates.F90:423-452), terms in the
 // reference's order (L_HMSMIN twice, as there)
-KQ_HD KQ_NOINLINE void kq_ionic(Cell& c, const double* v, long long s)
+KQ_HD KQ_NOINLINE void kq_ionic(Cell& c, const double* v)
 {
-#define V(n) v[(n) * s]
+#define V(n) v[(n) * KQ_S]
     const double sum = V(L_HPLUS) + V(L_NH4PLUS) + V(L_OHMIN) + V(L_HCO3MIN) + V(L_O2MIN) + V(L_NO2MIN)
                      + V(L_NO4MIN) + V(L_GLYACMIN) + V(L_OXLACMIN) + V(L_PYRACMIN) + V(L_GCOLACMIN) + V(L_CCOOHMIN)
                      + V(L_HSO3MIN) + V(L_HCOOMIN) + V(L_NO3MIN) + V(L_HSO4MIN) + V(L_HMSMIN) + V(L_NAPLUS)
@@ -272,7 +276,7 @@ KQ_HD inline float kq_hlconst(float a, float e, float temp)
 // reference's MET DATA ERROR (aqchem_kmt.F90:427-431), -2 for its initial pH error
 // (aqchem_Initialize.F90:476-481).
 KQ_HD KQ_NOINLINE int kq_setup(Cell& c, const double* p, long long n, const double* vmix, long long vn, double ho,
-                               double* y, double* f, double* r, long long s)
+                               double* y, double* f, double* r)
 {
     const float temp2 = (float)p[P_TEMP2 * n], pres_pa = (float)p[P_PRES_PA * n];
     const float taucld = (float)p[P_TAUCLD * n], prcrate = (float)p[P_PRCRATE * n];
@@ -301,205 +305,294 @@ KQ_HD KQ_NOINLINE int kq_setup(Cell& c, const double* p, long long n, const doub
     c.invphi2 = 1.0 / c.phi2;
     c.czen = (double)(float)p[P_COSZEN * n];
     c.cfactor = (double)pres_pa / (c.temp_kpp * (double)8.314510f) * 6.0221413e17;
-    for (int i = 0; i < NVAR; ++i) y[i * s] = c.cfactor * vmix[i * vn];
-    for (int i = 0; i < NFIX; ++i) f[i * s] = c.cfactor * 0.0;
-    f[L_H2O * s] = 55.5 * c.invphi2;
-    f[G_HO * s] = ho * c.cfactor;
-    f[L_O2 * s] = (double)0.21f * c.press * 1.3e-3 * kq_exp(1500.0 * c.delinvt) * c.invphi2;
+    for (int i = 0; i < NVAR; ++i) y[i * KQ_S] = c.cfactor * vmix[i * vn];
+    for (int i = 0; i < NFIX; ++i) f[i * KQ_S] = c.cfactor * 0.0;
+    f[L_H2O * KQ_S] = 55.5 * c.invphi2;
+    f[G_HO * KQ_S] = ho * c.cfactor;
+    f[L_O2 * KQ_S] = (double)0.21f * c.press * 1.3e-3 * kq_exp(1500.0 * c.delinvt) * c.invphi2;
     const double kw = 1.00e-14 * kq_exp(-6.955e+03 * c.delinvt);
-    double pos = 2.0 * (y[L_CAPLUS2 * s] + y[L_MGPLUS2 * s]) + y[L_NAPLUS * s] + y[L_KPLUS * s] + y[L_NH4PLUS * s];
-    double neg = 2.0 * (y[L_SO4MIN2 * s] + y[L_OXLACMIN2 * s]) + y[L_NO3MIN * s] + y[L_CLMIN * s];
+    double pos = 2.0 * (y[L_CAPLUS2 * KQ_S] + y[L_MGPLUS2 * KQ_S]) + y[L_NAPLUS * KQ_S] + y[L_KPLUS * KQ_S] + y[L_NH4PLUS * KQ_S];
+    double neg = 2.0 * (y[L_SO4MIN2 * KQ_S] + y[L_OXLACMIN2 * KQ_S]) + y[L_NO3MIN * KQ_S] + y[L_CLMIN * KQ_S];
     pos = pos * c.phi2;
     neg = neg * c.phi2;
     const double chg = pos - neg;
     const double oh = (chg + sqrt(chg * chg + 4.0 * kw)) * 0.5;
     if (!(oh > 0.0)) return -2;
-    y[L_OHMIN * s] = oh * c.invphi2;
-    y[L_HPLUS * s] = (kw / oh) * c.invphi2;
-    kq_rates_once(c, y, f, r, s);
+    y[L_OHMIN * KQ_S] = oh * c.invphi2;
+    y[L_HPLUS * KQ_S] = (kw / oh) * c.invphi2;
+    kq_rates_once(c, y, f, r);
     return 0;
 }
 
-KQ_HD inline void kq_axpy(double a, const double* x, double* y, long long s)   // WAXPY: y += a x, a = 0 skipped
-{
-    if (a == 0.0) return;
-    for (int i = 0; i < NVAR; ++i) y[i * s] = y[i * s] + a * x[i * s];
-}
-KQ_HD inline void kq_copy(const double* x, double* y, long long s)
-{
-    for (int i = 0; i < NVAR; ++i) y[i * s] = x[i * s];
-}
-
-// ros_ErrorNorm (aqchem_Integrator.F90:694-724)
-KQ_HD inline double kq_error_norm(const double* y, const double* ynew, const double* yerr, long long s)
+// ros_ErrorNorm (aqchem_Integrator.F90:694-724) of Rodas3's error estimate, which is K4
+// (E = 0, 0, 0, 1: YERR = 0 + 1 * K4)
+KQ_HD inline double kq_error_norm(const double* y, const double* ynew, const double* k4)
 {
     double err = 0.0;
     for (int i = 0; i < NVAR; ++i) {
-        const double ymax = fmax(fabs(y[i * s]), fabs(ynew[i * s]));
-        const double q = yerr[i * s] / (kq_atol(i) + kq_rtol(i) * ymax);
+        const double ymax = fmax(fabs(y[i * KQ_S]), fabs(ynew[i * KQ_S]));
+        const double q = (0.0 + k4[i * KQ_S]) / (kq_atol(i) + kq_rtol(i) * ymax);
         err = err + q * q;
     }
     err = sqrt(err / (double)NVAR);
     return err > 1.0e-10 ? err : 1.0e-10;
 }
 
-// One INTEGRATE call: ros_Integrator with Rodas3 (aqchem_Integrator.F90:485-690, 1070-1134),
-// its four stages written out with Rodas3's coefficients (A = 2, 0, 2, 0, 1; C = 4, 1, -1,
-// 1, -1, -8/3; M = 2, 0, 1, 1; E = 0, 0, 0, 1; gamma_1 = 1/2; new f at stages 3 and 4).
-// Returns IERR (1 = success); *texit is the time of the last accepted step (0 if none).
-KQ_HD inline int kq_integrate(Cell& c, double* ws, long long s, double tstart, double tend, double* texit,
-                              long long* st)
-{
-    double* y = ws + W_Y * s;
-    double* ynew = ws + W_YNEW * s;
-    double* fcn0 = ws + W_FCN0 * s;
-    double* fcn = ws + W_FCN * s;
-    double* k1 = ws + W_K * s;
-    double* k2 = k1 + NVAR * s;
-    double* k3 = k2 + NVAR * s;
-    double* k4 = k3 + NVAR * s;
-    double* yerr = ws + W_YERR * s;
-    double* jac0 = ws + W_JAC0 * s;
-    double* ghimj = ws + W_GHIMJ * s;
-    double* r = ws + W_R * s;
-    const double* f = ws + W_F * s;
-    const double roundoff = DBL_EPSILON, hmax = fabs(tend - tstart);
-    long long nstp = 0, nacc = 0;
-    double t = tstart, h = fmin(1.0e-5, hmax);
-    *texit = 0.0;
-    if (fabs(h) <= 10.0 * roundoff) h = 1.0e-5;
-    bool reject_last = false, reject_more = false;
-    while (fabs(t - tend) >= roundoff) {
-        if (nstp > 200000) return -6;
-        if ((t + 0.1 * h) == t || h <= roundoff) return -7;
-        h = fmin(h, fabs(tend - t));
-        kq_ionic(c, y, s);
-        kq_rates_update(c, y, f, r, s);
-        kqu_fun(y, f, r, fcn0, s);
-        st[S_NFUN]++;
-        kqu_jac(y, f, r, jac0, s);
-        st[S_NJAC]++;
-        for (;;) {
-            int nsing = 0;
-            for (;;) {                                           // ros_PrepareMatrix
-                for (int i = 0; i < LU_NONZERO; ++i) ghimj[i * s] = -jac0[i * s];
-                const double ghinv = 1.0 / (h * 0.5);
-                kq_add_diagonal(ghimj, ghinv, s);
-                const int ising = kqu_decomp(ghimj, s);
-                st[S_NDEC]++;
-                if (ising == 0) break;
-                st[S_NSNG]++;
-                if (++nsing > 5) return -8;
-                h = h * 0.5;
-            }
-            kq_copy(fcn0, k1, s);                                // stage 1
-            kqu_solve(ghimj, k1, s);
-            kq_copy(fcn0, k2, s);                                // stage 2 (no new f)
-            kq_axpy(4.0 / h, k1, k2, s);
-            kqu_solve(ghimj, k2, s);
-            kq_copy(y, ynew, s);                                 // stage 3
-            kq_axpy(2.0, k1, ynew, s);
-            kqu_fun(ynew, f, r, fcn, s);
-            st[S_NFUN]++;
-            kq_copy(fcn, k3, s);
-            kq_axpy(1.0 / h, k1, k3, s);
-            kq_axpy(-1.0 / h, k2, k3, s);
-            kqu_solve(ghimj, k3, s);
-            kq_copy(y, ynew, s);                                 // stage 4
-            kq_axpy(2.0, k1, ynew, s);
-            kq_axpy(1.0, k3, ynew, s);
-            kqu_fun(ynew, f, r, fcn, s);
-            st[S_NFUN]++;
-            kq_copy(fcn, k4, s);
-            kq_axpy(1.0 / h, k1, k4, s);
-            kq_axpy(-1.0 / h, k2, k4, s);
-            kq_axpy(-(8.0 / 3.0) / h, k3, k4, s);
-            kqu_solve(ghimj, k4, s);
-            st[S_NSOL] += 4;
-            kq_copy(y, ynew, s);                                 // new state and error
-            kq_axpy(2.0, k1, ynew, s);
-            kq_axpy(1.0, k3, ynew, s);
-            kq_axpy(1.0, k4, ynew, s);
-            for (int i = 0; i < NVAR; ++i) yerr[i * s] = 0.0;
-            kq_axpy(1.0, k4, yerr, s);
-            const double err = kq_error_norm(y, ynew, yerr, s);
-            double hnew = h * fmin(6.0, fmax(0.2, 0.9 / kq_pow(err, 1.0 / 3.0)));
-            nstp++;
-            st[S_NSTP]++;
-            if (err <= 1.0) {                                    // accept (Hmin = 0)
-                nacc++;
-                st[S_NACC]++;
-                kq_copy(ynew, y, s);
-                t = t + h;
-                hnew = fmax(0.0, fmin(hnew, hmax));
-                if (reject_last) hnew = fmin(hnew, h);
-                *texit = t;
-                reject_last = reject_more = false;
-                h = hnew;
-                break;
-            }
-            if (reject_more) hnew = h * 0.1;                     // reject
-            reject_more = reject_last;
-            reject_last = true;
-            h = hnew;
-            if (nacc >= 1) st[S_NREJ]++;
-        }
-    }
-    return 1;
-}
+// AQCHEM's integration loop (aqchem_kmt.F90:529-543: INTEGRATE called while T < TEND, at
+// most 16 times) around KPP's ros_Integrator with Rodas3 (aqchem_Integrator.F90:485-690,
+// 1070-1134), unrolled into one Rodas3 attempt per call of kq_advance.  A lane keeps its
+// cell's loop variables in a Lane between calls, so that a warp's lanes can each be at a
+// different step of a different cell and a lane whose cell ends takes the next one; the
+// operations of a cell, and their order, are those of the two nested loops.  Rodas3's four
+// stages are written out with its coefficients (A = 2, 0, 2, 0, 1; C = 4, 1, -1, 1, -1,
+// -8/3; M = 2, 0, 1, 1; E = 0, 0, 0, 1; gamma_1 = 1/2; new f at stages 3 and 4).
+enum { KL_PASS = 0, KL_STEP, KL_ATTEMPT, KL_DONE };
+struct Lane {
+    double tc;                       // AQCHEM's T: where the next INTEGRATE call starts
+    double t, tend, hmax, h, texit;  // ros_Integrator's T, Tend, Hmax, H and the last accepted T
+    long long nstp, nacc;            // its step counters (per INTEGRATE call)
+    int phase, ierr;
+    bool reject_last, reject_more;
+};
 
-// The kinetic core of one cell: set-up and AQCHEM's integration loop (aqchem_kmt.F90:
-// 529-543, at most 16 passes); the state stays in the workspace (Y, F).  Statistics to
-// st[S_*]; returns IERR (1 = success, -101 / -102 for a failed set-up).
-KQ_HD inline int kq_core(Cell& c, const double* p, long long n, const double* vmix, long long vn, double ho,
-                         double* ws, long long s, long long* st)
+// A cell's kinetic core is kq_begin, then kq_advance until it returns true; the state stays
+// in the workspace (Y, F).
+//
+// kq_begin: statistics cleared, the set-up, the first INTEGRATE call pending.  A failed set-up
+// (-1, -2) leaves the lane done with IERR -101 / -102.  Returns the set-up's status.
+KQ_HD inline int kq_begin(Cell& c, Lane& L, const double* p, long long n, const double* vmix, long long vn, double ho,
+                          double* ws, long long* st)
 {
     for (int i = 0; i < NSTAT; ++i) st[i] = 0;
-    int ierr = kq_setup(c, p, n, vmix, vn, ho, ws + W_Y * s, ws + W_F * s, ws + W_R * s, s);
-    if (ierr != 0) {
-        ierr -= 100;
-    } else {
-        double t = 0.0;
-        ierr = 1;
-        while (t < c.tend) {
-            if (st[S_NKRON] >= 16) {
-                ierr = -100;
-                break;
-            }
-            st[S_NKRON]++;
-            double texit = 0.0;
-            ierr = kq_integrate(c, ws, s, t, t + c.dt, &texit, st);
-            t = texit;
-            if (ierr < 0 && texit <= 0.0) break;
-        }
-    }
-    st[S_IERR] = ierr;
-    return ierr;
+    const int e = kq_setup(c, p, n, vmix, vn, ho, ws + W_Y * KQ_S, ws + W_F * KQ_S, ws + W_R * KQ_S);
+    L.tc = 0.0;
+    L.ierr = e != 0 ? e - 100 : 1;
+    L.phase = e != 0 ? KL_DONE : KL_PASS;
+    return e;
 }
 
-// One cloudy cell: set-up, AQCHEM's integration loop, the state (molec/cm3) to vout and
-// the fixed species to fout (if given); statistics to st[S_* * n].  A cell whose set-up
-// fails (IERR -101, -102) gets NaN in vout and fout.  Returns 0 when the integration
-// finished.
-KQ_HD inline int kq_cell(const double* p, const double* vmix, double* vout, double* fout, int* st_out, long long n,
-                         double* ws, long long s)
+// the return of an INTEGRATE call with status ierr: AQCHEM's T becomes the last accepted time,
+// and a call that failed without an accepted step ends the loop
+KQ_HD inline void kq_return(Lane& L, int ierr)
 {
-    Cell c;
-    long long st[NSTAT];
-    const int ierr = kq_core(c, p, n, vmix, n, p[P_HO * n], ws, s, st);
-    const double* y = ws + W_Y * s;
-    const double* f = ws + W_F * s;
-    if (ierr <= -101) {   // no state to return: NaN marks the cell's outputs
-        for (int i = 0; i < NVAR; ++i) vout[i * n] = NAN;
-        if (fout)
-            for (int i = 0; i < NFIX; ++i) fout[i * n] = NAN;
-    } else {
-        for (int i = 0; i < NVAR; ++i) vout[i * n] = y[i * s];
-        if (fout)
-            for (int i = 0; i < NFIX; ++i) fout[i * n] = f[i * s];
+    L.ierr = ierr;
+    L.tc = L.texit;
+    L.phase = (ierr < 0 && L.texit <= 0.0) ? KL_DONE : KL_PASS;
+}
+
+// The phases of one pass of a lane, in order: kq_next (the INTEGRATE calls' and steps'
+// transitions up to the next attempt: a new step's rates, f and J), kq_prepare (ros_
+// PrepareMatrix), kq_stages12, kq_stage3f, kq_stage3s, kq_stage4f, kq_stage4s (Rodas3's
+// stages, solves apart from the f evaluations so that each phase runs one routine) and
+// kq_decide (error norm, accept or reject).  A kernel may put a block barrier between
+// phases, so that its warps run the same routine at the same time; kq_advance runs them
+// back to back.  Rodas3's stages, each vector formed in one pass (ros_Integrator's stage
+// loop and WAXPY calls, a zero multiplier skipped as WAXPY does): K1 = FCN0; K2 = FCN0 +
+// (4/h) K1; YNEW = Y + 2 K1 -> K3 = f(YNEW) + (1/h) K1 - (1/h) K2; YNEW + K3 -> K4 =
+// f(YNEW) + (1/h) K1 - (1/h) K2 - (8/3/h) K3; YNEW + K4 is the new state (M = 2, 0, 1, 1:
+// stage 4's Y + 2 K1 + K3 is stage 3's YNEW + K3, bit for bit).
+
+// Moves the lane to its next attempt.  Returns true when the cell is finished: L.ierr is
+// IERR (1 = success, -6 / -7 / -8 from ros_Integrator, -100 for 16 calls, -101 / -102 for a
+// failed set-up), also in st[S_IERR].  Each pass of the loop moves the lane on by one
+// phase, at most 16 INTEGRATE calls.
+KQ_HD inline bool kq_next(Cell& c, Lane& L, double* ws, long long* st)
+{
+    double* y = ws + W_Y * KQ_S;
+    const double roundoff = DBL_EPSILON;
+    for (;;) {
+        if (L.phase == KL_DONE) {
+            st[S_IERR] = L.ierr;
+            return true;
+        }
+        if (L.phase == KL_ATTEMPT) return false;
+        if (L.phase == KL_PASS) {        // AQCHEM's loop head, then ros_Integrator's entry
+            if (!(L.tc < c.tend)) {
+                L.phase = KL_DONE;
+                continue;
+            }
+            if (st[S_NKRON] >= 16) {
+                L.ierr = -100;
+                L.phase = KL_DONE;
+                continue;
+            }
+            st[S_NKRON]++;
+            const double tstart = L.tc;
+            L.tend = tstart + c.dt;
+            L.hmax = fabs(L.tend - tstart);
+            L.nstp = L.nacc = 0;
+            L.t = tstart;
+            L.h = fmin(1.0e-5, L.hmax);
+            L.texit = 0.0;
+            if (fabs(L.h) <= 10.0 * roundoff) L.h = 1.0e-5;
+            L.reject_last = L.reject_more = false;
+            L.phase = KL_STEP;
+        }
+        // KL_STEP: a new step, rates, f and J at the accepted state
+        if (!(fabs(L.t - L.tend) >= roundoff)) {
+            kq_return(L, 1);
+            continue;
+        }
+        if (L.nstp > 200000) {
+            kq_return(L, -6);
+            continue;
+        }
+        if ((L.t + 0.1 * L.h) == L.t || L.h <= roundoff) {
+            kq_return(L, -7);
+            continue;
+        }
+        L.h = fmin(L.h, fabs(L.tend - L.t));
+        double* r = ws + W_R * KQ_S;
+        const double* f = ws + W_F * KQ_S;
+        kq_ionic(c, y);
+        kq_rates_update(c, y, f, r);
+        kqu_fun(y, f, r, ws + W_FCN0 * KQ_S);
+        st[S_NFUN]++;
+        kqu_jac(y, f, r, ws + W_JAC0 * KQ_S);
+        st[S_NJAC]++;
+        L.phase = KL_ATTEMPT;
+        return false;
     }
-    for (int i = 0; i < NSTAT; ++i) st_out[i * n] = (int)st[i];
-    return ierr == 1 ? 0 : 1;
+}
+
+// ros_PrepareMatrix: GHIMJ = 1/(h gamma) - JAC0 factorised, h halved after a singular
+// factorisation; after 5 halvings the INTEGRATE call returns -8 and this returns false
+// (the lane's next pass starts at kq_next)
+KQ_HD inline bool kq_prepare(Lane& L, double* ws, long long* st)
+{
+    const double* jac0 = ws + W_JAC0 * KQ_S;
+    double* ghimj = ws + W_GHIMJ * KQ_S;
+    int nsing = 0;
+    for (;;) {
+        for (int i = 0; i < LU_NONZERO; ++i) ghimj[i * KQ_S] = -jac0[i * KQ_S];
+        const double ghinv = 1.0 / (L.h * 0.5);
+        kq_add_diagonal(ghimj, ghinv);
+        const int ising = kqu_decomp(ghimj);
+        st[S_NDEC]++;
+        if (ising == 0) return true;
+        st[S_NSNG]++;
+        if (++nsing > 5) {
+            kq_return(L, -8);
+            return false;
+        }
+        L.h = L.h * 0.5;
+    }
+}
+
+// stages 1 and 2: K1, K2 and stage 3's YNEW
+KQ_HD inline void kq_stages12(const Lane& L, double* ws)
+{
+    const double* y = ws + W_Y * KQ_S;
+    double* ynew = ws + W_YNEW * KQ_S;
+    const double* fcn0 = ws + W_FCN0 * KQ_S;
+    double* k1 = ws + W_K * KQ_S;
+    double* k2 = k1 + NVAR * KQ_S;
+    const double* ghimj = ws + W_GHIMJ * KQ_S;
+    const double c21 = 4.0 / L.h;
+    for (int i = 0; i < NVAR; ++i) k1[i * KQ_S] = fcn0[i * KQ_S];
+    kqu_solve(ghimj, k1);
+    for (int i = 0; i < NVAR; ++i) {
+        double t = fcn0[i * KQ_S];
+        if (c21 != 0.0) t = t + c21 * k1[i * KQ_S];
+        k2[i * KQ_S] = t;
+    }
+    kqu_solve(ghimj, k2);
+    for (int i = 0; i < NVAR; ++i) ynew[i * KQ_S] = y[i * KQ_S] + 2.0 * k1[i * KQ_S];
+}
+
+// stage 3 (k = 3) or 4 (k = 4): f(YNEW) into Kk
+KQ_HD inline void kq_stage_f(double* ws, int k, long long* st)
+{
+    const double* r = ws + W_R * KQ_S;
+    const double* f = ws + W_F * KQ_S;
+    kqu_fun(ws + W_YNEW * KQ_S, f, r, ws + (W_K + (k - 1) * NVAR) * KQ_S);
+    st[S_NFUN]++;
+}
+
+// stage 3's K3 from f(YNEW), solved, and stage 4's YNEW
+KQ_HD inline void kq_stage3s(const Lane& L, double* ws)
+{
+    double* ynew = ws + W_YNEW * KQ_S;
+    const double* k1 = ws + W_K * KQ_S;
+    const double* k2 = k1 + NVAR * KQ_S;
+    double* k3 = ws + (W_K + 2 * NVAR) * KQ_S;
+    const double c31 = 1.0 / L.h, c32 = -1.0 / L.h;
+    for (int i = 0; i < NVAR; ++i) {
+        double t = k3[i * KQ_S];
+        if (c31 != 0.0) t = t + c31 * k1[i * KQ_S];
+        if (c32 != 0.0) t = t + c32 * k2[i * KQ_S];
+        k3[i * KQ_S] = t;
+    }
+    kqu_solve(ws + W_GHIMJ * KQ_S, k3);
+    for (int i = 0; i < NVAR; ++i) ynew[i * KQ_S] = ynew[i * KQ_S] + k3[i * KQ_S];
+}
+
+// stage 4's K4 from f(YNEW), solved, and the new state
+KQ_HD inline void kq_stage4s(const Lane& L, double* ws, long long* st)
+{
+    double* ynew = ws + W_YNEW * KQ_S;
+    const double* k1 = ws + W_K * KQ_S;
+    const double* k2 = k1 + NVAR * KQ_S;
+    const double* k3 = k2 + NVAR * KQ_S;
+    double* k4 = ws + (W_K + 3 * NVAR) * KQ_S;
+    const double c31 = 1.0 / L.h, c32 = -1.0 / L.h, c43 = -(8.0 / 3.0) / L.h;
+    for (int i = 0; i < NVAR; ++i) {
+        double t = k4[i * KQ_S];
+        if (c31 != 0.0) t = t + c31 * k1[i * KQ_S];
+        if (c32 != 0.0) t = t + c32 * k2[i * KQ_S];
+        if (c43 != 0.0) t = t + c43 * k3[i * KQ_S];
+        k4[i * KQ_S] = t;
+    }
+    kqu_solve(ws + W_GHIMJ * KQ_S, k4);
+    st[S_NSOL] += 4;
+    for (int i = 0; i < NVAR; ++i) ynew[i * KQ_S] = ynew[i * KQ_S] + k4[i * KQ_S];
+}
+
+// the error norm and ros_Integrator's accept / reject decision (Hmin = 0)
+KQ_HD inline void kq_decide(Lane& L, double* ws, long long* st)
+{
+    double* y = ws + W_Y * KQ_S;
+    const double* ynew = ws + W_YNEW * KQ_S;
+    const double h = L.h;
+    const double err = kq_error_norm(y, ynew, ws + (W_K + 3 * NVAR) * KQ_S);
+    double hnew = h * fmin(6.0, fmax(0.2, 0.9 / kq_pow(err, 1.0 / 3.0)));
+    L.nstp++;
+    st[S_NSTP]++;
+    if (err <= 1.0) {                    // accept
+        L.nacc++;
+        st[S_NACC]++;
+        for (int i = 0; i < NVAR; ++i) y[i * KQ_S] = ynew[i * KQ_S];
+        L.t = L.t + h;
+        hnew = fmax(0.0, fmin(hnew, L.hmax));
+        if (L.reject_last) hnew = fmin(hnew, h);
+        L.texit = L.t;
+        L.reject_last = L.reject_more = false;
+        L.h = hnew;
+        L.phase = KL_STEP;
+        return;
+    }
+    if (L.reject_more) hnew = h * 0.1;   // reject: the next attempt reuses f and J
+    L.reject_more = L.reject_last;
+    L.reject_last = true;
+    L.h = hnew;
+    if (L.nacc >= 1) st[S_NREJ]++;
+}
+
+// Runs the cell up to the end of its next Rodas3 attempt (the phases back to back).
+// Returns true when the cell is finished (as kq_next).
+KQ_HD inline bool kq_advance(Cell& c, Lane& L, double* ws, long long* st)
+{
+    for (;;) {
+        if (kq_next(c, L, ws, st)) return true;
+        if (!kq_prepare(L, ws, st)) continue;
+        kq_stages12(L, ws);
+        kq_stage_f(ws, 3, st);
+        kq_stage3s(L, ws);
+        kq_stage_f(ws, 4, st);
+        kq_stage4s(L, ws, st);
+        kq_decide(L, ws, st);
+        return false;
+    }
 }
 
 // ----------------------------------------------------------------------------- the whole AQCHEM
@@ -524,20 +617,103 @@ enum { KO_HPWDEP = 0, KO_BETASO4, KO_FRACTR, KO_FRACPOA, KO_FRACPRI, KO_FRACSOA,
 // REAL(4) EXP of the redistribution (EXP of a REAL product): the portable exp rounded to float
 KQ_HD inline double kq_fexp(float x) { return (double)(float)kq_exp((double)x); }
 
-// AQCHEM (aqchem_kmt.F90:21-978) for one cloudy cell: the fractions and mass-balance start
-// (:434-507), Initialize's mapping of GAS / AEROSOL into the KPP state (aqchem_Initialize.F90:
-// 290-421, into the workspace's YNEW), the kinetic core (kq_core), and the redistribution
-// into GAS, AEROSOL, GASWDEP, AERWDEP (:546-976).  gas [KG_NGAS] and aer [naer * 3] (stride
-// n) in and out; gwd, awd, out [KO_N], st_out [NSTAT] out.  GAS's HO is the OH the
-// set-up reads (the parameter row is not).  Returns 0, or 1 when the integration or the
-// set-up failed (set-up: every output NaN, where the reference stops the run).
-KQ_HD inline int kq_aqchem_cell(const double* p, double* gas, double* aer, int naer, const int* ai,
-                                const double* fac, double* gwd, double* awd, double* out, int* st_out, long long n,
-                                double* ws, long long s)
-{
 #define AER(k, m) aer[(long long)(ai[k] + naer * (m)) * n]
 #define AWD(k, m) awd[(long long)(ai[k] + naer * (m)) * n]
-    const double ho = gas[KG_HO * n];
+
+// Initialize's mapping of AQCHEM's GAS / AEROSOL into the KPP state in mol/molV
+// (aqchem_Initialize.F90:290-421), into the workspace's YNEW, which the set-up reads
+KQ_HD inline void kq_aq_map(const double* p, const double* gas, const double* aer, int naer, const int* ai,
+                            const double* fac, long long n, double* ws)
+{
+    const float coszen = (float)p[P_COSZEN * n];
+    const int ispc8 = (int)p[P_ISPC8 * n], mtpyrac = (int)p[P_MTPYRAC * n];
+    const int dark = coszen <= 0.0f;
+    const double fe_iii = dark ? 0.9 : 0.1, mn_ii = 1.0, fe_sol = 0.1, mn_sol = 0.5;
+    double* v = ws + W_YNEW * KQ_S;   // Initialize's VAR before the unit conversion
+    for (int i = 0; i < NVAR; ++i) v[i * KQ_S] = 0.0;
+    v[G_SO2 * KQ_S] = gas[KG_SO2 * n];
+    v[G_HNO3 * KQ_S] = gas[KG_HNO3 * n] + 2.0 * gas[KG_N2O5 * n];
+    v[G_CO2 * KQ_S] = gas[KG_CO2 * n];
+    v[G_NH3 * KQ_S] = gas[KG_NH3 * n];
+    v[G_H2O2 * KQ_S] = gas[KG_H2O2 * n];
+    v[G_O3 * KQ_S] = gas[KG_O3 * n];
+    v[G_HCOOH * KQ_S] = gas[KG_FOA * n];
+    v[G_MHP * KQ_S] = gas[KG_MHP * n];
+    v[G_PAA * KQ_S] = gas[KG_PAA * n];
+    v[G_HCL * KQ_S] = gas[KG_HCL * n];
+    v[G_GLY * KQ_S] = gas[KG_GLY * n];
+    v[G_MGLY * KQ_S] = gas[KG_MGLY * n];
+    v[G_IEPOX * KQ_S] = gas[KG_IEPOX * n];
+    if (ispc8 > 0) {
+        v[G_IMAE * KQ_S] = gas[KG_IMAE * n];
+        v[G_IHMML * KQ_S] = gas[KG_IHMML * n];
+    }
+    v[G_NO2 * KQ_S] = gas[KG_NO2 * n];
+    v[G_HONO * KQ_S] = gas[KG_HONO * n];
+    v[G_HNO4 * KQ_S] = gas[KG_HNO4 * n];
+    v[G_NO3 * KQ_S] = gas[KG_NO3RAD * n];
+    v[G_CH3O2 * KQ_S] = gas[KG_CH3O2 * n];
+    v[G_GCOL * KQ_S] = gas[KG_GCOL * n];
+    v[G_CCOOH * KQ_S] = gas[KG_CCOOH * n];
+    v[G_HCHO * KQ_S] = gas[KG_HCHO * n];
+    v[G_HO2 * KQ_S] = gas[KG_HO2 * n];
+    v[G_HCHOP * KQ_S] = gas[KG_HCHOP * n];
+    if (mtpyrac > 0) v[G_PYRAC * KQ_S] = gas[KG_PYRUV * n];
+    v[A_NO3AKN * KQ_S] = AER(KA_NO3, KM_AKN);
+    v[A_NH4AKN * KQ_S] = AER(KA_NH4, KM_AKN);
+    v[A_CLAKN * KQ_S] = AER(KA_CL, KM_AKN);
+    v[A_NAAKN * KQ_S] = AER(KA_NA, KM_AKN);
+    v[A_SO4AKN * KQ_S] = AER(KA_SO4, KM_AKN);
+    v[A_PECAKN * KQ_S] = AER(KA_EC, KM_AKN);
+    v[A_POAAKN * KQ_S] = AER(KA_POA, KM_AKN);
+    v[A_PRIAKN * KQ_S] = AER(KA_PRI, KM_AKN);
+    v[L_SO4MIN2 * KQ_S] = AER(KA_SO4, KM_ACC) + AER(KA_SO4, KM_COR);
+    v[L_NO3MIN * KQ_S] = AER(KA_NO3, KM_ACC) + AER(KA_NO3, KM_COR);
+    v[L_NH4PLUS * KQ_S] = AER(KA_NH4, KM_ACC) + AER(KA_NH4, KM_COR);
+    v[L_CLMIN * KQ_S] = AER(KA_CL, KM_ACC) + AER(KA_CL, KM_COR);
+    v[L_PRIACC * KQ_S] = AER(KA_PRI, KM_ACC);
+    v[L_NAPLUS * KQ_S] = AER(KA_NA, KM_ACC);
+    v[L_CAPLUS2 * KQ_S] = AER(KA_CAACC, KM_ACC);
+    v[L_MGPLUS2 * KQ_S] = AER(KA_MGACC, KM_ACC);
+    v[L_KPLUS * KQ_S] = AER(KA_KACC, KM_ACC);
+    v[L_PECACC * KQ_S] = AER(KA_EC, KM_ACC);
+    v[L_ORGC * KQ_S] = (double)0.2f * AER(KA_ORGC, KM_ACC);
+    v[L_OXLACMIN2 * KQ_S] = (double)0.8f * AER(KA_ORGC, KM_ACC) / (double)(90.03f / 177.0f);
+    v[L_POAACC * KQ_S] = AER(KA_POA, KM_ACC);
+    if (ispc8 > 0) {
+        v[L_IETET * KQ_S] = AER(KA_IETET, KM_ACC);
+        v[L_IEOS * KQ_S] = AER(KA_IEOS, KM_ACC);
+        v[L_DIMER * KQ_S] = AER(KA_DIMER, KM_ACC);
+        v[L_IMGA * KQ_S] = AER(KA_IMGA, KM_ACC);
+        v[L_IMOS * KQ_S] = AER(KA_IMOS, KM_ACC);
+    } else {
+        v[L_ISO3 * KQ_S] = AER(KA_ISO3, KM_ACC);
+    }
+    v[L_SO4MIN2 * KQ_S] = v[L_SO4MIN2 * KQ_S] + gas[KG_H2SO4 * n];
+    const double soilc = AER(KA_SOILC, KM_COR), anthc = AER(KA_ANTHC, KM_COR), seasc = AER(KA_SEASC, KM_COR);
+    double fecor = fac[KF_SOIL_FE] * soilc + fac[KF_CORS_FE] * anthc;
+    double mncor = fac[KF_SOIL_MN] * soilc + fac[KF_CORS_MN] * anthc;
+    double nacor = fac[KF_SEAS_NA] * seasc + fac[KF_SOIL_NA] * soilc + fac[KF_CORS_NA] * anthc;
+    double mgcor = fac[KF_SEAS_MG] * seasc + fac[KF_SOIL_MG] * soilc + fac[KF_CORS_MG] * anthc;
+    double cacor = fac[KF_SEAS_CA] * seasc + fac[KF_SOIL_CA] * soilc + fac[KF_CORS_CA] * anthc;
+    double kcor = fac[KF_SEAS_K] * seasc + fac[KF_SOIL_K] * soilc + fac[KF_CORS_K] * anthc;
+    v[L_NAPLUS * KQ_S] = v[L_NAPLUS * KQ_S] + nacor;
+    v[L_CAPLUS2 * KQ_S] = v[L_CAPLUS2 * KQ_S] + cacor;
+    v[L_MGPLUS2 * KQ_S] = v[L_MGPLUS2 * KQ_S] + mgcor;
+    v[L_KPLUS * KQ_S] = v[L_KPLUS * KQ_S] + kcor;
+    v[L_FEPLUS3 * KQ_S] = fe_sol * fe_iii * (AER(KA_FEACC, KM_ACC) + fecor);
+    v[L_MNPLUS2 * KQ_S] = mn_sol * mn_ii * (AER(KA_MNACC, KM_ACC) + mncor);
+}
+
+// AQCHEM after the kinetic core (c, ierr, st: the lane's at the end): the fractional weights and the
+// mass-balance start (aqchem_kmt.F90:434-507) from gas / aer as they came in, then the
+// redistribution into GAS, AEROSOL, GASWDEP, AERWDEP (:546-976).  A failed set-up (IERR
+// -101, -102) gives NaN in every output, where the reference stops the run.  Returns 0, or
+// 1 when the integration or the set-up failed.
+KQ_HD inline int kq_aq_finish(const Cell& c, int ierr, const long long* st, const double* p, double* gas, double* aer,
+                              int naer, const int* ai, const double* fac, double* gwd, double* awd, double* out,
+                              int* st_out, long long n, const double* ws)
+{
     const float taucld = (float)p[P_TAUCLD * n], alfa0 = (float)p[P_ALFA0 * n], alfa3 = (float)p[P_ALFA3 * n];
     const float coszen = (float)p[P_COSZEN * n];
     const int ispc8 = (int)p[P_ISPC8 * n], mtpyrac = (int)p[P_MTPYRAC * n];
@@ -571,86 +747,7 @@ KQ_HD inline int kq_aqchem_cell(const double* p, double* gas, double* aer, int n
     }
     const double poaiinit = AER(KA_POA, KM_AKN), priiinit = AER(KA_PRI, KM_AKN);
     const double traciinit = AER(KA_TRACER_AKN, KM_AKN), soaiinit = AER(KA_SOA, KM_AKN);
-    /* aqchem_Initialize.F90:290-421: the KPP state in mol/molV */
     const double fe_iii = dark ? 0.9 : 0.1, mn_ii = 1.0, fe_sol = 0.1, mn_sol = 0.5;
-    double* v = ws + W_YNEW * s;   // Initialize's VAR before the unit conversion
-    for (int i = 0; i < NVAR; ++i) v[i * s] = 0.0;
-    v[G_SO2 * s] = gas[KG_SO2 * n];
-    v[G_HNO3 * s] = gas[KG_HNO3 * n] + 2.0 * gas[KG_N2O5 * n];
-    v[G_CO2 * s] = gas[KG_CO2 * n];
-    v[G_NH3 * s] = gas[KG_NH3 * n];
-    v[G_H2O2 * s] = gas[KG_H2O2 * n];
-    v[G_O3 * s] = gas[KG_O3 * n];
-    v[G_HCOOH * s] = gas[KG_FOA * n];
-    v[G_MHP * s] = gas[KG_MHP * n];
-    v[G_PAA * s] = gas[KG_PAA * n];
-    v[G_HCL * s] = gas[KG_HCL * n];
-    v[G_GLY * s] = gas[KG_GLY * n];
-    v[G_MGLY * s] = gas[KG_MGLY * n];
-    v[G_IEPOX * s] = gas[KG_IEPOX * n];
-    if (ispc8 > 0) {
-        v[G_IMAE * s] = gas[KG_IMAE * n];
-        v[G_IHMML * s] = gas[KG_IHMML * n];
-    }
-    v[G_NO2 * s] = gas[KG_NO2 * n];
-    v[G_HONO * s] = gas[KG_HONO * n];
-    v[G_HNO4 * s] = gas[KG_HNO4 * n];
-    v[G_NO3 * s] = gas[KG_NO3RAD * n];
-    v[G_CH3O2 * s] = gas[KG_CH3O2 * n];
-    v[G_GCOL * s] = gas[KG_GCOL * n];
-    v[G_CCOOH * s] = gas[KG_CCOOH * n];
-    v[G_HCHO * s] = gas[KG_HCHO * n];
-    v[G_HO2 * s] = gas[KG_HO2 * n];
-    v[G_HCHOP * s] = gas[KG_HCHOP * n];
-    if (mtpyrac > 0) v[G_PYRAC * s] = gas[KG_PYRUV * n];
-    v[A_NO3AKN * s] = AER(KA_NO3, KM_AKN);
-    v[A_NH4AKN * s] = AER(KA_NH4, KM_AKN);
-    v[A_CLAKN * s] = AER(KA_CL, KM_AKN);
-    v[A_NAAKN * s] = AER(KA_NA, KM_AKN);
-    v[A_SO4AKN * s] = AER(KA_SO4, KM_AKN);
-    v[A_PECAKN * s] = AER(KA_EC, KM_AKN);
-    v[A_POAAKN * s] = AER(KA_POA, KM_AKN);
-    v[A_PRIAKN * s] = AER(KA_PRI, KM_AKN);
-    v[L_SO4MIN2 * s] = AER(KA_SO4, KM_ACC) + AER(KA_SO4, KM_COR);
-    v[L_NO3MIN * s] = AER(KA_NO3, KM_ACC) + AER(KA_NO3, KM_COR);
-    v[L_NH4PLUS * s] = AER(KA_NH4, KM_ACC) + AER(KA_NH4, KM_COR);
-    v[L_CLMIN * s] = AER(KA_CL, KM_ACC) + AER(KA_CL, KM_COR);
-    v[L_PRIACC * s] = AER(KA_PRI, KM_ACC);
-    v[L_NAPLUS * s] = AER(KA_NA, KM_ACC);
-    v[L_CAPLUS2 * s] = AER(KA_CAACC, KM_ACC);
-    v[L_MGPLUS2 * s] = AER(KA_MGACC, KM_ACC);
-    v[L_KPLUS * s] = AER(KA_KACC, KM_ACC);
-    v[L_PECACC * s] = AER(KA_EC, KM_ACC);
-    v[L_ORGC * s] = (double)0.2f * AER(KA_ORGC, KM_ACC);
-    v[L_OXLACMIN2 * s] = (double)0.8f * AER(KA_ORGC, KM_ACC) / (double)(90.03f / 177.0f);
-    v[L_POAACC * s] = AER(KA_POA, KM_ACC);
-    if (ispc8 > 0) {
-        v[L_IETET * s] = AER(KA_IETET, KM_ACC);
-        v[L_IEOS * s] = AER(KA_IEOS, KM_ACC);
-        v[L_DIMER * s] = AER(KA_DIMER, KM_ACC);
-        v[L_IMGA * s] = AER(KA_IMGA, KM_ACC);
-        v[L_IMOS * s] = AER(KA_IMOS, KM_ACC);
-    } else {
-        v[L_ISO3 * s] = AER(KA_ISO3, KM_ACC);
-    }
-    v[L_SO4MIN2 * s] = v[L_SO4MIN2 * s] + gas[KG_H2SO4 * n];
-    const double soilc = AER(KA_SOILC, KM_COR), anthc = AER(KA_ANTHC, KM_COR), seasc = AER(KA_SEASC, KM_COR);
-    double fecor = fac[KF_SOIL_FE] * soilc + fac[KF_CORS_FE] * anthc;
-    double mncor = fac[KF_SOIL_MN] * soilc + fac[KF_CORS_MN] * anthc;
-    double nacor = fac[KF_SEAS_NA] * seasc + fac[KF_SOIL_NA] * soilc + fac[KF_CORS_NA] * anthc;
-    double mgcor = fac[KF_SEAS_MG] * seasc + fac[KF_SOIL_MG] * soilc + fac[KF_CORS_MG] * anthc;
-    double cacor = fac[KF_SEAS_CA] * seasc + fac[KF_SOIL_CA] * soilc + fac[KF_CORS_CA] * anthc;
-    double kcor = fac[KF_SEAS_K] * seasc + fac[KF_SOIL_K] * soilc + fac[KF_CORS_K] * anthc;
-    v[L_NAPLUS * s] = v[L_NAPLUS * s] + nacor;
-    v[L_CAPLUS2 * s] = v[L_CAPLUS2 * s] + cacor;
-    v[L_MGPLUS2 * s] = v[L_MGPLUS2 * s] + mgcor;
-    v[L_KPLUS * s] = v[L_KPLUS * s] + kcor;
-    v[L_FEPLUS3 * s] = fe_sol * fe_iii * (AER(KA_FEACC, KM_ACC) + fecor);
-    v[L_MNPLUS2 * s] = mn_sol * mn_ii * (AER(KA_MNACC, KM_ACC) + mncor);
-    /* the kinetic core */
-    Cell c;
-    long long st[NSTAT];
-    const int ierr = kq_core(c, p, n, v, s, ho, ws, s, st);
     for (int i = 0; i < NSTAT; ++i) st_out[i * n] = (int)st[i];
     if (ierr <= -101) {   /* set-up failed: the reference stops the run */
         for (int i = 0; i < KG_NGAS; ++i) gas[i * n] = gwd[i * n] = NAN;
@@ -658,8 +755,8 @@ KQ_HD inline int kq_aqchem_cell(const double* p, double* gas, double* aer, int n
         for (int i = 0; i < KO_N; ++i) out[i * n] = NAN;
         return 1;
     }
-    const double* y = ws + W_Y * s;
-    const double* f = ws + W_F * s;
+    const double* y = ws + W_Y * KQ_S;
+    const double* f = ws + W_F * KQ_S;
     /* :546-976: redistribution */
     for (int i = 0; i < KG_NGAS; ++i) gwd[i * n] = 0.0;
     for (int i = 0; i < naer * 3; ++i) awd[i * n] = 0.0;
@@ -669,14 +766,14 @@ KQ_HD inline int kq_aqchem_cell(const double* p, double* gas, double* aer, int n
     const double wfactor = (double)(float)p[P_WCAVG * n] * cthk1 * c.phi2;
     const double expwet = kq_exp(-c.wetfac * (double)taucld);
     const double ex0 = kq_fexp(-alfa0 * taucld), ex3 = kq_fexp(-alfa3 * taucld);
-    AER(KA_NO3, KM_AKN) = y[A_NO3AKN * s] * invcfac;
-    AER(KA_NH4, KM_AKN) = y[A_NH4AKN * s] * invcfac;
-    AER(KA_CL, KM_AKN) = y[A_CLAKN * s] * invcfac;
-    AER(KA_NA, KM_AKN) = y[A_NAAKN * s] * invcfac;
-    AER(KA_SO4, KM_AKN) = y[A_SO4AKN * s] * invcfac;
-    AER(KA_EC, KM_AKN) = y[A_PECAKN * s] * invcfac;
-    AER(KA_POA, KM_AKN) = y[A_POAAKN * s] * invcfac;
-    AER(KA_PRI, KM_AKN) = y[A_PRIAKN * s] * invcfac;
+    AER(KA_NO3, KM_AKN) = y[A_NO3AKN * KQ_S] * invcfac;
+    AER(KA_NH4, KM_AKN) = y[A_NH4AKN * KQ_S] * invcfac;
+    AER(KA_CL, KM_AKN) = y[A_CLAKN * KQ_S] * invcfac;
+    AER(KA_NA, KM_AKN) = y[A_NAAKN * KQ_S] * invcfac;
+    AER(KA_SO4, KM_AKN) = y[A_SO4AKN * KQ_S] * invcfac;
+    AER(KA_EC, KM_AKN) = y[A_PECAKN * KQ_S] * invcfac;
+    AER(KA_POA, KM_AKN) = y[A_POAAKN * KQ_S] * invcfac;
+    AER(KA_PRI, KM_AKN) = y[A_PRIAKN * KQ_S] * invcfac;
     AER(KA_NUM, KM_AKN) = AER(KA_NUM, KM_AKN) * ex0;
     AER(KA_TRACER_ACC, KM_ACC) = AER(KA_TRACER_ACC, KM_ACC) + AER(KA_TRACER_AKN, KM_AKN) * (1.0 - ex3);
     AER(KA_PHG_ACC, KM_ACC) = AER(KA_PHG_ACC, KM_ACC) + AER(KA_PHG_AKN, KM_AKN) * (1.0 - ex3);
@@ -716,48 +813,48 @@ KQ_HD inline int kq_aqchem_cell(const double* p, double* gas, double* aer, int n
     const double wdmgcor = fac[KF_SEAS_MG] * wseas + fac[KF_SOIL_MG] * wsoil + fac[KF_CORS_MG] * wanth;
     const double wdcacor = fac[KF_SEAS_CA] * wseas + fac[KF_SOIL_CA] * wsoil + fac[KF_CORS_CA] * wanth;
     const double wdkcor = fac[KF_SEAS_K] * wseas + fac[KF_SOIL_K] * wsoil + fac[KF_CORS_K] * wanth;
-    AWD(KA_FEACC, KM_ACC) = fmax((y[WD_FEPLUS3 * s] / fe_iii / fe_sol) - wdfecor, 0.0);
-    AWD(KA_MNACC, KM_ACC) = fmax((y[WD_MNPLUS2 * s] / mn_ii / mn_sol) - wdmncor, 0.0);
-    AWD(KA_NA, KM_ACC) = fmax(y[WD_NAPLUS * s] - wdnacor, 0.0);
-    AWD(KA_CAACC, KM_ACC) = fmax(y[WD_CAPLUS2 * s] - wdcacor, 0.0);
-    AWD(KA_MGACC, KM_ACC) = fmax(y[WD_MGPLUS2 * s] - wdmgcor, 0.0);
-    AWD(KA_KACC, KM_ACC) = fmax(y[WD_KPLUS * s] - wdkcor, 0.0);
-    AWD(KA_SO4, KM_ACC) = fmax(y[WD_H2SO4 * s] - AWD(KA_SO4, KM_COR), 0.0);
-    AWD(KA_NH4, KM_ACC) = fmax(y[WD_NH4PLUS * s] - AWD(KA_NH4, KM_COR), 0.0);
-    AWD(KA_NO3, KM_ACC) = fmax(y[WD_NO3MIN * s] - AWD(KA_NO3, KM_COR), 0.0);
-    AWD(KA_CL, KM_ACC) = fmax(y[WD_CLMIN * s] - AWD(KA_CL, KM_COR), 0.0);
-    AWD(KA_PRI, KM_ACC) = y[WD_PRIACC * s];
-    AWD(KA_EC, KM_ACC) = y[WD_PECACC * s];
-    AWD(KA_ORGC, KM_ACC) = y[WD_ORGC * s];
-    AWD(KA_POA, KM_ACC) = y[WD_POAACC * s];
+    AWD(KA_FEACC, KM_ACC) = fmax((y[WD_FEPLUS3 * KQ_S] / fe_iii / fe_sol) - wdfecor, 0.0);
+    AWD(KA_MNACC, KM_ACC) = fmax((y[WD_MNPLUS2 * KQ_S] / mn_ii / mn_sol) - wdmncor, 0.0);
+    AWD(KA_NA, KM_ACC) = fmax(y[WD_NAPLUS * KQ_S] - wdnacor, 0.0);
+    AWD(KA_CAACC, KM_ACC) = fmax(y[WD_CAPLUS2 * KQ_S] - wdcacor, 0.0);
+    AWD(KA_MGACC, KM_ACC) = fmax(y[WD_MGPLUS2 * KQ_S] - wdmgcor, 0.0);
+    AWD(KA_KACC, KM_ACC) = fmax(y[WD_KPLUS * KQ_S] - wdkcor, 0.0);
+    AWD(KA_SO4, KM_ACC) = fmax(y[WD_H2SO4 * KQ_S] - AWD(KA_SO4, KM_COR), 0.0);
+    AWD(KA_NH4, KM_ACC) = fmax(y[WD_NH4PLUS * KQ_S] - AWD(KA_NH4, KM_COR), 0.0);
+    AWD(KA_NO3, KM_ACC) = fmax(y[WD_NO3MIN * KQ_S] - AWD(KA_NO3, KM_COR), 0.0);
+    AWD(KA_CL, KM_ACC) = fmax(y[WD_CLMIN * KQ_S] - AWD(KA_CL, KM_COR), 0.0);
+    AWD(KA_PRI, KM_ACC) = y[WD_PRIACC * KQ_S];
+    AWD(KA_EC, KM_ACC) = y[WD_PECACC * KQ_S];
+    AWD(KA_ORGC, KM_ACC) = y[WD_ORGC * KQ_S];
+    AWD(KA_POA, KM_ACC) = y[WD_POAACC * KQ_S];
     if (ispc8 > 0) {
-        AWD(KA_IETET, KM_ACC) = y[WD_IETET * s];
-        AWD(KA_IEOS, KM_ACC) = y[WD_IEOS * s];
-        AWD(KA_DIMER, KM_ACC) = y[WD_DIMER * s];
-        AWD(KA_IMGA, KM_ACC) = y[WD_IMGA * s];
-        AWD(KA_IMOS, KM_ACC) = y[WD_IMOS * s];
+        AWD(KA_IETET, KM_ACC) = y[WD_IETET * KQ_S];
+        AWD(KA_IEOS, KM_ACC) = y[WD_IEOS * KQ_S];
+        AWD(KA_DIMER, KM_ACC) = y[WD_DIMER * KQ_S];
+        AWD(KA_IMGA, KM_ACC) = y[WD_IMGA * KQ_S];
+        AWD(KA_IMOS, KM_ACC) = y[WD_IMOS * KQ_S];
     } else {
-        AWD(KA_ISO3, KM_ACC) = y[WD_IETET * s];
+        AWD(KA_ISO3, KM_ACC) = y[WD_IETET * KQ_S];
     }
-    if (AWD(KA_NH4, KM_COR) > y[WD_NH4PLUS * s]) {
-        AWD(KA_NH4, KM_COR) = (1.0 - fnh4acc) * y[WD_NH4PLUS * s];
-        AWD(KA_NH4, KM_ACC) = fnh4acc * y[WD_NH4PLUS * s];
-        AER(KA_NH4, KM_COR) = (1.0 - fnh4acc) * (y[L_NH4OH * s] + y[L_NH4PLUS * s]) * invcfac;
+    if (AWD(KA_NH4, KM_COR) > y[WD_NH4PLUS * KQ_S]) {
+        AWD(KA_NH4, KM_COR) = (1.0 - fnh4acc) * y[WD_NH4PLUS * KQ_S];
+        AWD(KA_NH4, KM_ACC) = fnh4acc * y[WD_NH4PLUS * KQ_S];
+        AER(KA_NH4, KM_COR) = (1.0 - fnh4acc) * (y[L_NH4OH * KQ_S] + y[L_NH4PLUS * KQ_S]) * invcfac;
     }
-    if (AWD(KA_NO3, KM_COR) > y[WD_NO3MIN * s]) {
-        AWD(KA_NO3, KM_COR) = (1.0 - fno3acc) * y[WD_NO3MIN * s];
-        AWD(KA_NO3, KM_ACC) = fno3acc * y[WD_NO3MIN * s];
-        AER(KA_NO3, KM_COR) = (1.0 - fno3acc) * (y[L_HNO3 * s] + y[L_NO3MIN * s]) * invcfac;
+    if (AWD(KA_NO3, KM_COR) > y[WD_NO3MIN * KQ_S]) {
+        AWD(KA_NO3, KM_COR) = (1.0 - fno3acc) * y[WD_NO3MIN * KQ_S];
+        AWD(KA_NO3, KM_ACC) = fno3acc * y[WD_NO3MIN * KQ_S];
+        AER(KA_NO3, KM_COR) = (1.0 - fno3acc) * (y[L_HNO3 * KQ_S] + y[L_NO3MIN * KQ_S]) * invcfac;
     }
-    if (AWD(KA_CL, KM_COR) > y[WD_CLMIN * s]) {
-        AWD(KA_CL, KM_COR) = (1.0 - fclacc) * y[WD_CLMIN * s];
-        AWD(KA_CL, KM_ACC) = fclacc * y[WD_CLMIN * s];
-        AER(KA_CL, KM_COR) = (1.0 - fclacc) * y[L_CLMIN * s] * invcfac;
+    if (AWD(KA_CL, KM_COR) > y[WD_CLMIN * KQ_S]) {
+        AWD(KA_CL, KM_COR) = (1.0 - fclacc) * y[WD_CLMIN * KQ_S];
+        AWD(KA_CL, KM_ACC) = fclacc * y[WD_CLMIN * KQ_S];
+        AER(KA_CL, KM_COR) = (1.0 - fclacc) * y[L_CLMIN * KQ_S] * invcfac;
     }
-    AER(KA_PRI, KM_ACC) = y[L_PRIACC * s] * invcfac;
-    AER(KA_EC, KM_ACC) = y[L_PECACC * s] * invcfac;
-    AER(KA_ORGC, KM_ACC) = y[L_ORGC * s] * invcfac;
-    AER(KA_POA, KM_ACC) = y[L_POAACC * s] * invcfac;
+    AER(KA_PRI, KM_ACC) = y[L_PRIACC * KQ_S] * invcfac;
+    AER(KA_EC, KM_ACC) = y[L_PECACC * KQ_S] * invcfac;
+    AER(KA_ORGC, KM_ACC) = y[L_ORGC * KQ_S] * invcfac;
+    AER(KA_POA, KM_ACC) = y[L_POAACC * KQ_S] * invcfac;
     out[(KO_FRACTR) * n] = AER(KA_TRACER_ACC, KM_ACC) > 0.0
         ? fmin(((traciinit - AER(KA_TRACER_AKN, KM_AKN)) * expwet) / AER(KA_TRACER_ACC, KM_ACC), 1.0) : 0.0;
     out[(KO_FRACPOA) * n] = AER(KA_POA, KM_ACC) > 0.0
@@ -767,120 +864,120 @@ KQ_HD inline int kq_aqchem_cell(const double* p, double* gas, double* aer, int n
     out[(KO_FRACSOA) * n] = AER(KA_SOA, KM_ACC) > 0.0
         ? fmin(((soaiinit - AER(KA_SOA, KM_AKN)) * expwet) / AER(KA_SOA, KM_ACC), 1.0) : 0.0;
     if (ispc8 > 0) {
-        AER(KA_IETET, KM_ACC) = y[L_IETET * s] * invcfac;
-        AER(KA_IEOS, KM_ACC) = y[L_IEOS * s] * invcfac;
-        AER(KA_DIMER, KM_ACC) = y[L_DIMER * s] * invcfac;
-        AER(KA_IMGA, KM_ACC) = y[L_IMGA * s] * invcfac;
-        AER(KA_IMOS, KM_ACC) = y[L_IMOS * s] * invcfac;
+        AER(KA_IETET, KM_ACC) = y[L_IETET * KQ_S] * invcfac;
+        AER(KA_IEOS, KM_ACC) = y[L_IEOS * KQ_S] * invcfac;
+        AER(KA_DIMER, KM_ACC) = y[L_DIMER * KQ_S] * invcfac;
+        AER(KA_IMGA, KM_ACC) = y[L_IMGA * KQ_S] * invcfac;
+        AER(KA_IMOS, KM_ACC) = y[L_IMOS * KQ_S] * invcfac;
     } else {
-        AER(KA_ISO3, KM_ACC) = (y[L_ISO3 * s]) * invcfac;
+        AER(KA_ISO3, KM_ACC) = (y[L_ISO3 * KQ_S]) * invcfac;
     }
     const double soilc2 = AER(KA_SOILC, KM_COR), anthc2 = AER(KA_ANTHC, KM_COR), seasc2 = AER(KA_SEASC, KM_COR);
-    fecor = fac[KF_SOIL_FE] * soilc2 + fac[KF_CORS_FE] * anthc2;
-    mncor = fac[KF_SOIL_MN] * soilc2 + fac[KF_CORS_MN] * anthc2;
-    nacor = fac[KF_SEAS_NA] * seasc2 + fac[KF_SOIL_NA] * soilc2 + fac[KF_CORS_NA] * anthc2;
-    mgcor = fac[KF_SEAS_MG] * seasc2 + fac[KF_SOIL_MG] * soilc2 + fac[KF_CORS_MG] * anthc2;
-    cacor = fac[KF_SEAS_CA] * seasc2 + fac[KF_SOIL_CA] * soilc2 + fac[KF_CORS_CA] * anthc2;
-    kcor = fac[KF_SEAS_K] * seasc2 + fac[KF_SOIL_K] * soilc2 + fac[KF_CORS_K] * anthc2;
-    AER(KA_FEACC, KM_ACC) = fmax((y[L_FEPLUS3 * s] / fe_iii / fe_sol - fecor * cfactor) * invcfac, 0.0);
-    AER(KA_MNACC, KM_ACC) = fmax((y[L_MNPLUS2 * s] / mn_ii / mn_sol - mncor * cfactor) * invcfac, 0.0);
-    AER(KA_NA, KM_ACC) = fmax((y[L_NAPLUS * s] - nacor * cfactor) * invcfac, 0.0);
-    AER(KA_CAACC, KM_ACC) = fmax((y[L_CAPLUS2 * s] - cacor * cfactor) * invcfac, 0.0);
-    AER(KA_MGACC, KM_ACC) = fmax((y[L_MGPLUS2 * s] - mgcor * cfactor) * invcfac, 0.0);
-    AER(KA_KACC, KM_ACC) = fmax((y[L_KPLUS * s] - kcor * cfactor) * invcfac, 0.0);
-    AER(KA_SO4, KM_ACC) = fmax(((y[L_H2SO4 * s] + y[L_SO4MIN2 * s] + y[L_HSO4MIN * s]) * invcfac)
+    const double fecor = fac[KF_SOIL_FE] * soilc2 + fac[KF_CORS_FE] * anthc2;
+    const double mncor = fac[KF_SOIL_MN] * soilc2 + fac[KF_CORS_MN] * anthc2;
+    const double nacor = fac[KF_SEAS_NA] * seasc2 + fac[KF_SOIL_NA] * soilc2 + fac[KF_CORS_NA] * anthc2;
+    const double mgcor = fac[KF_SEAS_MG] * seasc2 + fac[KF_SOIL_MG] * soilc2 + fac[KF_CORS_MG] * anthc2;
+    const double cacor = fac[KF_SEAS_CA] * seasc2 + fac[KF_SOIL_CA] * soilc2 + fac[KF_CORS_CA] * anthc2;
+    const double kcor = fac[KF_SEAS_K] * seasc2 + fac[KF_SOIL_K] * soilc2 + fac[KF_CORS_K] * anthc2;
+    AER(KA_FEACC, KM_ACC) = fmax((y[L_FEPLUS3 * KQ_S] / fe_iii / fe_sol - fecor * cfactor) * invcfac, 0.0);
+    AER(KA_MNACC, KM_ACC) = fmax((y[L_MNPLUS2 * KQ_S] / mn_ii / mn_sol - mncor * cfactor) * invcfac, 0.0);
+    AER(KA_NA, KM_ACC) = fmax((y[L_NAPLUS * KQ_S] - nacor * cfactor) * invcfac, 0.0);
+    AER(KA_CAACC, KM_ACC) = fmax((y[L_CAPLUS2 * KQ_S] - cacor * cfactor) * invcfac, 0.0);
+    AER(KA_MGACC, KM_ACC) = fmax((y[L_MGPLUS2 * KQ_S] - mgcor * cfactor) * invcfac, 0.0);
+    AER(KA_KACC, KM_ACC) = fmax((y[L_KPLUS * KQ_S] - kcor * cfactor) * invcfac, 0.0);
+    AER(KA_SO4, KM_ACC) = fmax(((y[L_H2SO4 * KQ_S] + y[L_SO4MIN2 * KQ_S] + y[L_HSO4MIN * KQ_S]) * invcfac)
                                - AER(KA_SO4, KM_COR), 0.0);
-    AER(KA_CL, KM_ACC) = fmax((y[L_CLMIN * s] * invcfac) - AER(KA_CL, KM_COR), 0.0);
-    totamm = y[G_NH3 * s] + y[L_NH4OH * s] + y[L_NH4PLUS * s] - AER(KA_NH4, KM_COR) * cfactor;
-    totnit = y[G_HNO3 * s] + y[L_HNO3 * s] + y[L_NO3MIN * s] - AER(KA_NO3, KM_COR) * cfactor;
+    AER(KA_CL, KM_ACC) = fmax((y[L_CLMIN * KQ_S] * invcfac) - AER(KA_CL, KM_COR), 0.0);
+    totamm = y[G_NH3 * KQ_S] + y[L_NH4OH * KQ_S] + y[L_NH4PLUS * KQ_S] - AER(KA_NH4, KM_COR) * cfactor;
+    totnit = y[G_HNO3 * KQ_S] + y[L_HNO3 * KQ_S] + y[L_NO3MIN * KQ_S] - AER(KA_NO3, KM_COR) * cfactor;
     totamm = fmax(totamm, 0.0);
     totnit = fmax(totnit, 0.0);
     AER(KA_NO3, KM_ACC) = ((1.0 - fhno3) * totnit) * invcfac;
     AER(KA_NH4, KM_ACC) = ((1.0 - fnh3) * totamm) * invcfac;
     const double oliggly = 0.0 * 3.3e-1, oligmgly = 0.0 * 1.9e-1;   /* OLIG = 0 (aqchem_kmt.F90:412) */
-    gas[KG_SO2 * n] = (y[G_SO2 * s] + y[L_SO2 * s] + y[L_HSO3MIN * s] + y[L_SO3MIN2 * s] + y[L_HMSMIN * s]
-                   + y[L_SO3MIN * s] + y[L_SO5MIN * s] + y[L_HSO5MIN * s] + y[L_SO4MIN * s]) * invcfac;
+    gas[KG_SO2 * n] = (y[G_SO2 * KQ_S] + y[L_SO2 * KQ_S] + y[L_HSO3MIN * KQ_S] + y[L_SO3MIN2 * KQ_S] + y[L_HMSMIN * KQ_S]
+                   + y[L_SO3MIN * KQ_S] + y[L_SO5MIN * KQ_S] + y[L_HSO5MIN * KQ_S] + y[L_SO4MIN * KQ_S]) * invcfac;
     gas[KG_N2O5 * n] = 0.0;
-    gas[KG_CO2 * n] = (y[G_CO2 * s] + y[L_H2CO3 * s] + y[L_HCO3MIN * s] + y[L_CO3MIN2 * s] + y[L_CO2MIN * s])
+    gas[KG_CO2 * n] = (y[G_CO2 * KQ_S] + y[L_H2CO3 * KQ_S] + y[L_HCO3MIN * KQ_S] + y[L_CO3MIN2 * KQ_S] + y[L_CO2MIN * KQ_S])
                   * invcfac;
-    gas[KG_H2O2 * n] = (y[G_H2O2 * s] + y[L_H2O2 * s]) * invcfac;
-    gas[KG_O3 * n] = (y[G_O3 * s] + y[L_O3 * s]) * invcfac;
-    gas[KG_FOA * n] = (y[G_HCOOH * s] + y[L_HCOOH * s] + y[L_HCOOMIN * s]) * invcfac;
-    gas[KG_MHP * n] = (y[G_MHP * s] + y[L_MHP * s]) * invcfac;
-    gas[KG_PAA * n] = (y[G_PAA * s] + y[L_PAA * s]) * invcfac;
+    gas[KG_H2O2 * n] = (y[G_H2O2 * KQ_S] + y[L_H2O2 * KQ_S]) * invcfac;
+    gas[KG_O3 * n] = (y[G_O3 * KQ_S] + y[L_O3 * KQ_S]) * invcfac;
+    gas[KG_FOA * n] = (y[G_HCOOH * KQ_S] + y[L_HCOOH * KQ_S] + y[L_HCOOMIN * KQ_S]) * invcfac;
+    gas[KG_MHP * n] = (y[G_MHP * KQ_S] + y[L_MHP * KQ_S]) * invcfac;
+    gas[KG_PAA * n] = (y[G_PAA * KQ_S] + y[L_PAA * KQ_S]) * invcfac;
     gas[KG_H2SO4 * n] = 0.0;
-    gas[KG_HCL * n] = (y[G_HCL * s] + y[L_HCL * s]) * invcfac;
-    gas[KG_GLY * n] = (y[G_GLY * s] + y[L_GLY * s] * (1.0 - oliggly)) * invcfac;
-    gas[KG_MGLY * n] = (y[G_MGLY * s] + y[L_MGLY * s] * (1.0 - oligmgly)) * invcfac;
+    gas[KG_HCL * n] = (y[G_HCL * KQ_S] + y[L_HCL * KQ_S]) * invcfac;
+    gas[KG_GLY * n] = (y[G_GLY * KQ_S] + y[L_GLY * KQ_S] * (1.0 - oliggly)) * invcfac;
+    gas[KG_MGLY * n] = (y[G_MGLY * KQ_S] + y[L_MGLY * KQ_S] * (1.0 - oligmgly)) * invcfac;
     gas[KG_HNO3 * n] = (fhno3 * totnit) * invcfac;
     gas[KG_NH3 * n] = (fnh3 * totamm) * invcfac;
-    gas[KG_HO * n] = (f[G_HO * s]) * invcfac;
-    gas[KG_IEPOX * n] = (y[G_IEPOX * s] + y[L_IEPOX * s]) * invcfac;
+    gas[KG_HO * n] = (f[G_HO * KQ_S]) * invcfac;
+    gas[KG_IEPOX * n] = (y[G_IEPOX * KQ_S] + y[L_IEPOX * KQ_S]) * invcfac;
     if (ispc8 > 0) {
-        gas[KG_IMAE * n] = (y[G_IMAE * s] + y[L_IMAE * s]) * invcfac;
-        gas[KG_IHMML * n] = (y[G_IHMML * s] + y[L_IHMML * s]) * invcfac;
+        gas[KG_IMAE * n] = (y[G_IMAE * KQ_S] + y[L_IMAE * KQ_S]) * invcfac;
+        gas[KG_IHMML * n] = (y[G_IHMML * KQ_S] + y[L_IHMML * KQ_S]) * invcfac;
     }
-    gas[KG_HO2 * n] = (y[G_HO2 * s] + y[L_HO2 * s] + y[L_O2MIN * s]) * invcfac;
-    gas[KG_NO2 * n] = (y[G_NO2 * s] + y[L_NO2 * s]) * invcfac;
-    gas[KG_HONO * n] = (y[G_HONO * s] + y[L_HONO * s] + y[L_NO2MIN * s]) * invcfac;
-    gas[KG_HNO4 * n] = (y[G_HNO4 * s] + y[L_HNO4 * s] + y[L_NO4MIN * s]) * invcfac;
-    gas[KG_NO3RAD * n] = (y[G_NO3 * s] + y[L_NO3 * s]) * invcfac;
-    gas[KG_CH3O2 * n] = (y[G_CH3O2 * s] + y[L_CH3O2 * s]) * invcfac;
-    gas[KG_CCOOH * n] = (y[G_CCOOH * s] + y[L_CCOOH * s] + y[L_CCOOHMIN * s]) * invcfac;
-    gas[KG_HCHO * n] = (y[G_HCHO * s] + y[L_CH2OHYD * s] + y[L_HCHO * s] + y[L_HMSMIN * s]) * invcfac;
-    gas[KG_GCOL * n] = (y[G_GCOL * s] + y[L_GCOL * s]) * invcfac;
-    gas[KG_HCHOP * n] = (y[G_HCHOP * s] + y[L_CH2OHYDP * s] + y[L_HCHOP * s] + y[L_HMSMINP * s]) * invcfac;
-    gwd[KG_SO2 * n] = y[WD_SO2 * s];
-    gwd[KG_HNO3 * n] = y[WD_HNO3 * s];
+    gas[KG_HO2 * n] = (y[G_HO2 * KQ_S] + y[L_HO2 * KQ_S] + y[L_O2MIN * KQ_S]) * invcfac;
+    gas[KG_NO2 * n] = (y[G_NO2 * KQ_S] + y[L_NO2 * KQ_S]) * invcfac;
+    gas[KG_HONO * n] = (y[G_HONO * KQ_S] + y[L_HONO * KQ_S] + y[L_NO2MIN * KQ_S]) * invcfac;
+    gas[KG_HNO4 * n] = (y[G_HNO4 * KQ_S] + y[L_HNO4 * KQ_S] + y[L_NO4MIN * KQ_S]) * invcfac;
+    gas[KG_NO3RAD * n] = (y[G_NO3 * KQ_S] + y[L_NO3 * KQ_S]) * invcfac;
+    gas[KG_CH3O2 * n] = (y[G_CH3O2 * KQ_S] + y[L_CH3O2 * KQ_S]) * invcfac;
+    gas[KG_CCOOH * n] = (y[G_CCOOH * KQ_S] + y[L_CCOOH * KQ_S] + y[L_CCOOHMIN * KQ_S]) * invcfac;
+    gas[KG_HCHO * n] = (y[G_HCHO * KQ_S] + y[L_CH2OHYD * KQ_S] + y[L_HCHO * KQ_S] + y[L_HMSMIN * KQ_S]) * invcfac;
+    gas[KG_GCOL * n] = (y[G_GCOL * KQ_S] + y[L_GCOL * KQ_S]) * invcfac;
+    gas[KG_HCHOP * n] = (y[G_HCHOP * KQ_S] + y[L_CH2OHYDP * KQ_S] + y[L_HCHOP * KQ_S] + y[L_HMSMINP * KQ_S]) * invcfac;
+    gwd[KG_SO2 * n] = y[WD_SO2 * KQ_S];
+    gwd[KG_HNO3 * n] = y[WD_HNO3 * KQ_S];
     gwd[KG_N2O5 * n] = 0.0;
-    gwd[KG_CO2 * n] = y[WD_CO2 * s];
-    gwd[KG_NH3 * n] = y[WD_NH4OH * s];
-    gwd[KG_H2O2 * n] = y[WD_H2O2 * s];
-    gwd[KG_O3 * n] = y[WD_O3 * s];
-    gwd[KG_FOA * n] = y[WD_HCOOH * s];
-    gwd[KG_MHP * n] = y[WD_MHP * s];
-    gwd[KG_PAA * n] = y[WD_PAA * s];
+    gwd[KG_CO2 * n] = y[WD_CO2 * KQ_S];
+    gwd[KG_NH3 * n] = y[WD_NH4OH * KQ_S];
+    gwd[KG_H2O2 * n] = y[WD_H2O2 * KQ_S];
+    gwd[KG_O3 * n] = y[WD_O3 * KQ_S];
+    gwd[KG_FOA * n] = y[WD_HCOOH * KQ_S];
+    gwd[KG_MHP * n] = y[WD_MHP * KQ_S];
+    gwd[KG_PAA * n] = y[WD_PAA * KQ_S];
     gwd[KG_H2SO4 * n] = 0.0;
-    gwd[KG_HCL * n] = y[WD_HCL * s];
-    gwd[KG_GLY * n] = y[WD_GLY * s] * (1.0 - oliggly);
-    gwd[KG_MGLY * n] = y[WD_MGLY * s] * (1.0 - oligmgly);
-    gwd[KG_HO * n] = y[WD_HO * s];
-    gwd[KG_IEPOX * n] = y[WD_IEPOX * s];
+    gwd[KG_HCL * n] = y[WD_HCL * KQ_S];
+    gwd[KG_GLY * n] = y[WD_GLY * KQ_S] * (1.0 - oliggly);
+    gwd[KG_MGLY * n] = y[WD_MGLY * KQ_S] * (1.0 - oligmgly);
+    gwd[KG_HO * n] = y[WD_HO * KQ_S];
+    gwd[KG_IEPOX * n] = y[WD_IEPOX * KQ_S];
     if (ispc8 > 0) {
-        gwd[KG_IMAE * n] = y[WD_IMAE * s];
-        gwd[KG_IHMML * n] = y[WD_IHMML * s];
+        gwd[KG_IMAE * n] = y[WD_IMAE * KQ_S];
+        gwd[KG_IHMML * n] = y[WD_IHMML * KQ_S];
     }
-    gwd[KG_NO2 * n] = y[WD_NO2 * s];
-    gwd[KG_HONO * n] = y[WD_HONO * s];
-    gwd[KG_HNO4 * n] = y[WD_HNO4 * s];
-    gwd[KG_NO3RAD * n] = y[WD_NO3 * s];
-    gwd[KG_CH3O2 * n] = y[WD_CH3O2 * s];
-    gwd[KG_GCOL * n] = y[WD_GCOL * s];
-    gwd[KG_CCOOH * n] = y[WD_CCOOH * s];
-    gwd[KG_HCHO * n] = y[WD_CH2OHYD * s];
-    gwd[KG_HO2 * n] = y[WD_HO2 * s];
-    gwd[KG_HCHOP * n] = y[WD_CH2OHYDP * s];
+    gwd[KG_NO2 * n] = y[WD_NO2 * KQ_S];
+    gwd[KG_HONO * n] = y[WD_HONO * KQ_S];
+    gwd[KG_HNO4 * n] = y[WD_HNO4 * KQ_S];
+    gwd[KG_NO3RAD * n] = y[WD_NO3 * KQ_S];
+    gwd[KG_CH3O2 * n] = y[WD_CH3O2 * KQ_S];
+    gwd[KG_GCOL * n] = y[WD_GCOL * KQ_S];
+    gwd[KG_CCOOH * n] = y[WD_CCOOH * KQ_S];
+    gwd[KG_HCHO * n] = y[WD_CH2OHYD * KQ_S];
+    gwd[KG_HO2 * n] = y[WD_HO2 * KQ_S];
+    gwd[KG_HCHOP * n] = y[WD_CH2OHYDP * KQ_S];
     double apyrac = 0.0, wdpyrac = 0.0;
     if (mtpyrac > 0) {
-        gas[KG_PYRUV * n] = (y[G_PYRAC * s] + y[L_PYRAC * s]) * invcfac;
-        gwd[KG_PYRUV * n] = y[WD_PYRAC * s];
+        gas[KG_PYRUV * n] = (y[G_PYRAC * KQ_S] + y[L_PYRAC * KQ_S]) * invcfac;
+        gwd[KG_PYRUV * n] = y[WD_PYRAC * KQ_S];
         wdpyrac = 0.0;
-        apyrac = y[L_PYRACMIN * s];
+        apyrac = y[L_PYRACMIN * KQ_S];
     } else {
-        wdpyrac = y[WD_PYRAC * s];
-        apyrac = y[L_PYRAC * s] + y[L_PYRACMIN * s];
+        wdpyrac = y[WD_PYRAC * KQ_S];
+        apyrac = y[L_PYRAC * KQ_S] + y[L_PYRACMIN * KQ_S];
     }
     const double r7404 = (double)(74.04f / 177.0f), r9003 = (double)(90.03f / 177.0f);
     const double r8806 = (double)(88.06f / 177.0f), r7605 = (double)(76.05f / 177.0f);
     const double r5804 = (double)(58.04f / 177.0f), r7206 = (double)(72.06f / 177.0f);
-    AER(KA_ORGC, KM_ACC) = (y[L_ORGC * s] + (r7404 * y[L_GLYAC * s]) + (r9003 * y[L_OXLAC * s])
-                            + (r9003 * y[L_OXLACMIN * s]) + (r9003 * y[L_OXLACMIN2 * s]) + (r8806 * apyrac)
-                            + (r7605 * y[L_GCOLAC * s]) + (r7404 * y[L_GLYACMIN * s])
-                            + (r7605 * y[L_GCOLACMIN * s])
-                            + r5804 * oliggly * y[L_GLY * s] + r7206 * oligmgly * y[L_MGLY * s]) * invcfac;
-    AWD(KA_ORGC, KM_ACC) = y[WD_ORGC * s] + (r7404 * y[WD_GLYAC * s]) + (r9003 * y[WD_OXLAC * s])
-                           + (r8806 * wdpyrac) + (r7605 * y[WD_GCOLAC * s])
-                           + r5804 * oliggly * y[WD_GLY * s] + r7206 * oligmgly * y[WD_MGLY * s];
+    AER(KA_ORGC, KM_ACC) = (y[L_ORGC * KQ_S] + (r7404 * y[L_GLYAC * KQ_S]) + (r9003 * y[L_OXLAC * KQ_S])
+                            + (r9003 * y[L_OXLACMIN * KQ_S]) + (r9003 * y[L_OXLACMIN2 * KQ_S]) + (r8806 * apyrac)
+                            + (r7605 * y[L_GCOLAC * KQ_S]) + (r7404 * y[L_GLYACMIN * KQ_S])
+                            + (r7605 * y[L_GCOLACMIN * KQ_S])
+                            + r5804 * oliggly * y[L_GLY * KQ_S] + r7206 * oligmgly * y[L_MGLY * KQ_S]) * invcfac;
+    AWD(KA_ORGC, KM_ACC) = y[WD_ORGC * KQ_S] + (r7404 * y[WD_GLYAC * KQ_S]) + (r9003 * y[WD_OXLAC * KQ_S])
+                           + (r8806 * wdpyrac) + (r7605 * y[WD_GCOLAC * KQ_S])
+                           + r5804 * oliggly * y[WD_GLY * KQ_S] + r7206 * oligmgly * y[WD_MGLY * KQ_S];
     for (int i = 0; i < KG_NGAS; ++i) gwd[i * n] = gwd[i * n] * wfactor;
     for (int i = 0; i < naer * 3; ++i) awd[i * n] = awd[i * n] * wfactor;
     for (int i = 0; i < KG_NGAS; ++i) {
@@ -891,7 +988,7 @@ KQ_HD inline int kq_aqchem_cell(const double* p, double* gas, double* aer, int n
         if (aer[i * n] < 0.0) aer[i * n] = 0.0;
         if (awd[i * n] < 0.0) awd[i * n] = 0.0;
     }
-    out[(KO_HPWDEP) * n] = (double)(float)(y[WD_HPLUS * s] * wfactor);   /* HPWDEP is REAL */
+    out[(KO_HPWDEP) * n] = (double)(float)(y[WD_HPLUS * KQ_S] * wfactor);   /* HPWDEP is REAL */
     const double depsum = AWD(KA_SO4, KM_ACC) / wfactor;
     const double betaso4 = AER(KA_SO4, KM_ACC) * cfactor + depsum > 0.0
                                ? depsum / (AER(KA_SO4, KM_ACC) * cfactor + depsum) / (double)taucld : 0.0;
@@ -919,8 +1016,9 @@ KQ_HD inline int kq_aqchem_cell(const double* p, double* gas, double* aer, int n
     }
     for (int i = 0; i < 4; ++i) out[(KO_MBAL + i) * n] = startm[i] > 0.0 ? 100 * (startm[i] - endm[i]) / startm[i] : 0.0;
     return ierr == 1 ? 0 : 1;
+}
+
 #undef AER
 #undef AWD
-}
 
 }  // namespace kmt2

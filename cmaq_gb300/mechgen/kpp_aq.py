@@ -521,9 +521,9 @@ def _rate_call(kind: str, a: list[float]) -> str:
     if kind == "DISB":
         return f"kq_disb(c, {d(a[0])}, {int(a[1])})"
     if kind == "KRXN":
-        return f"kq_krxn(c, v, s, {d(a[0])}, {d(a[1])}, {int(a[2])}, {int(a[3])}, {int(a[4])})"
+        return f"kq_krxn(c, v, {d(a[0])}, {d(a[1])}, {int(a[2])}, {int(a[3])}, {int(a[4])})"
     if kind == "KIEPOX":
-        return f"kq_kiepox(c, v, f, s, {d(a[0])}, {d(a[1])}, {int(a[2])})"
+        return f"kq_kiepox(c, v, f, {d(a[0])}, {d(a[1])}, {int(a[2])})"
     if kind == "KMTF":
         return f"kq_kmtf(c, {d(a[0])}, {d(a[1])}, {d(a[2])})"
     if kind == "KMTB":
@@ -543,7 +543,8 @@ def device_source(k: KppMech) -> str:
     """Strided straight-line routines for the device code (``namespace kmt2``, after the
     rate-law functions of csrc/kmt2.cuh): Henry's law constants, the rate constants set
     once and refreshed, RTOL, f, J, LU factorisation and solve.  Arrays live in a
-    lane-interleaved workspace: element i of a lane at ``p[i * s]``."""
+    lane-interleaved workspace: element i of a lane at ``p[i * KQ_S]`` (KQ_S, the lanes
+    of a warp, is a constant of csrc/kmt2.cuh)."""
     out = ["// Generated by cmaq_gb300/mechgen/kpp_aq.py from CCTM/src/cloud/acm_ae7_kmt2: Henry's law",
            "// constants (aqchem_kmt.F90:371-396), rate constants (aqchem_Initialize.F90:491-636,",
            "// aqchem_Rates.F90:456-579), tolerances, Fun, Jac_SP, KppDecomp, KppSolve as straight-line",
@@ -560,7 +561,7 @@ def device_source(k: KppMech) -> str:
             out.append(f"    c.henry[{h}] = {c_dbl(a)};   // {name}")
     out.append("}\n")
     for fn, upd in (("kq_rates_once", False), ("kq_rates_update", True)):
-        out.append(f"KQ_HD KQ_NOINLINE void {fn}(const Cell& c, const double* v, const double* f, double* r, long long s)\n{{")
+        out.append(f"KQ_HD KQ_NOINLINE void {fn}(const Cell& c, const double* v, const double* f, double* r)\n{{")
         if not upd:
             out.append("    (void)v;\n    (void)f;")
         for rx, (kind, args, refreshed, mt) in enumerate(k.rates):
@@ -569,7 +570,7 @@ def device_source(k: KppMech) -> str:
             call = _rate_call(kind, args)
             if mt:
                 call = f"(double)c.mtpyrac * {call}"
-            out.append(f"    r[{rx} * s] = {call};")
+            out.append(f"    r[{rx} * KQ_S] = {call};")
         out.append("}\n")
     special = sorted({i for i in range(k.nvar) if k.rtol[i] != k.rtol[0]})
     assert len(set(k.atol)) == 1 and len({k.rtol[i] for i in special}) <= 1
@@ -577,8 +578,8 @@ def device_source(k: KppMech) -> str:
     alt = c_dbl(k.rtol[special[0]]) if special else c_dbl(k.rtol[0])
     out.append(f"KQ_HD inline double kq_rtol(int i) {{ return ({cond}) ? {alt} : {c_dbl(k.rtol[0])}; }}")
     out.append(f"KQ_HD inline double kq_atol(int) {{ return {c_dbl(k.atol[0])}; }}\n")
-    out.append("KQ_HD inline void kq_add_diagonal(double* g, double x, long long s)\n{")
-    out += [f"    g[{d} * s] = g[{d} * s] + x;" for d in k.lu_diag[:-1]]
+    out.append("KQ_HD inline void kq_add_diagonal(double* g, double x)\n{")
+    out += [f"    g[{d} * KQ_S] = g[{d} * KQ_S] + x;" for d in k.lu_diag[:-1]]
     out.append("}\n")
     out.append(device_routines(k))
     return "\n".join(out)
@@ -594,7 +595,7 @@ def device_routines(k: KppMech, chunk_ops: int = DEVICE_CHUNK_OPS) -> str:
     operands in the same order, so the bits are those of the oracle's routines); the LU
     factorisation and the two triangular solves split at row boundaries into functions of
     about ``chunk_ops`` operations."""
-    acc = lambda name, i: f"{name}[{i} * s]"
+    acc = lambda name, i: f"{name}[{i} * KQ_S]"
     n = k.nvar
     q = "KQ_HD KQ_NOINLINE"
     out = []
@@ -617,14 +618,14 @@ def device_routines(k: KppMech, chunk_ops: int = DEVICE_CHUNK_OPS) -> str:
         out.extend(f"    {name}_{gi}({call_args});" for gi in range(len(groups)))
         out.append("}\n")
 
-    fargs = "const double* v, const double* f, const double* r, double* vdot, long long s"
-    chunked("kqu_fun", fargs, "v, f, r, vdot, s", range(n),
+    fargs = "const double* v, const double* f, const double* r, double* vdot"
+    chunked("kqu_fun", fargs, "v, f, r, vdot", range(n),
             lambda i: sum(1 + len(k.factors[rx]) for _, rx in k.vdot[i]),
             lambda i: f"    {acc('vdot', i)} = 0.0" + "".join(_term(c, f"({prod(rx)})") for c, rx in k.vdot[i]) + ";")
     bprod = lambda b: " * ".join([acc("r", k.blist[b][0])] + ([c_dbl(float(k.blist[b][1]))] if k.blist[b][1] > 1 else [])
                                  + [_factor(x, n, acc) for x in k.blist[b][2]])
-    jargs = "const double* v, const double* f, const double* r, double* jvs, long long s"
-    chunked("kqu_jac", jargs, "v, f, r, jvs, s", range(len(k.jvs)),
+    jargs = "const double* v, const double* f, const double* r, double* jvs"
+    chunked("kqu_jac", jargs, "v, f, r, jvs", range(len(k.jvs)),
             lambda e: sum(1 + len(k.blist[b][2]) for _, b in k.jvs[e]) + 1,
             lambda e: f"    {acc('jvs', e)} = 0.0" + "".join(_term(c, f"({bprod(b)})") for c, b in k.jvs[e]) + ";")
     pos = {(k.lu_irow[e], k.lu_icol[e]): e for e in range(len(k.lu_irow))}
@@ -647,7 +648,7 @@ def device_routines(k: KppMech, chunk_ops: int = DEVICE_CHUNK_OPS) -> str:
 
     dgroups = split(range(n), row_cost)
     for gi, rows in enumerate(dgroups):
-        out.append(f"{q} int kqu_decomp_{gi}(double* jvs, long long s)\n{{")
+        out.append(f"{q} int kqu_decomp_{gi}(double* jvs)\n{{")
         for row in rows:
             out.append(f"    if (fabs({acc('jvs', k.lu_diag[row])}) < DBL_MIN) return {row + 1};")
             for kk in range(k.lu_crow[row], k.lu_diag[row]):
@@ -658,28 +659,28 @@ def device_routines(k: KppMech, chunk_ops: int = DEVICE_CHUNK_OPS) -> str:
                     out.append(f"      {acc('jvs', qq)} = {acc('jvs', qq)} + a * {acc('jvs', jj)};")
                 out.append("    }")
         out.append("    return 0;\n}\n")
-    out.append(f"KQ_HD inline int kqu_decomp(double* jvs, long long s)\n{{\n    int rc;")
-    out += [f"    if ((rc = kqu_decomp_{gi}(jvs, s)) != 0) return rc;" for gi in range(len(dgroups))]
+    out.append(f"KQ_HD inline int kqu_decomp(double* jvs)\n{{\n    int rc;")
+    out += [f"    if ((rc = kqu_decomp_{gi}(jvs)) != 0) return rc;" for gi in range(len(dgroups))]
     out.append("    return 0;\n}\n")
     fgroups = split(range(n), lambda row: k.lu_diag[row] - k.lu_crow[row] + 1)
     bgroups = split(range(n - 1, -1, -1), lambda row: k.lu_crow[row + 1] - k.lu_diag[row])
     for gi, rows in enumerate(fgroups):
-        out.append(f"{q} void kqu_solve_f{gi}(const double* jvs, double* x, long long s)\n{{")
+        out.append(f"{q} void kqu_solve_f{gi}(const double* jvs, double* x)\n{{")
         for row in rows:
             terms = "".join(f" - {acc('jvs', kk)} * {acc('x', k.lu_icol[kk])}" for kk in range(k.lu_crow[row], k.lu_diag[row]))
             if terms:
                 out.append(f"    {acc('x', row)} = {acc('x', row)}{terms};")
         out.append("}\n")
     for gi, rows in enumerate(bgroups):
-        out.append(f"{q} void kqu_solve_b{gi}(const double* jvs, double* x, long long s)\n{{")
+        out.append(f"{q} void kqu_solve_b{gi}(const double* jvs, double* x)\n{{")
         for row in rows:
             terms = "".join(f" - {acc('jvs', kk)} * {acc('x', k.lu_icol[kk])}"
                             for kk in range(k.lu_diag[row] + 1, k.lu_crow[row + 1]))
             out.append(f"    {acc('x', row)} = ({acc('x', row)}{terms}) / {acc('jvs', k.lu_diag[row])};")
         out.append("}\n")
-    out.append(f"KQ_HD inline void kqu_solve(const double* jvs, double* x, long long s)\n{{")
-    out += [f"    kqu_solve_f{gi}(jvs, x, s);" for gi in range(len(fgroups))]
-    out += [f"    kqu_solve_b{gi}(jvs, x, s);" for gi in range(len(bgroups))]
+    out.append(f"KQ_HD inline void kqu_solve(const double* jvs, double* x)\n{{")
+    out += [f"    kqu_solve_f{gi}(jvs, x);" for gi in range(len(fgroups))]
+    out += [f"    kqu_solve_b{gi}(jvs, x);" for gi in range(len(bgroups))]
     out.append("}\n")
     return "\n".join(out)
 

@@ -247,10 +247,12 @@ int cmaqchem_ros3_solve_noalloc(const char* mechanism, long long ncell, double* 
 
 /* KMT2 aqueous cloud chemistry (CCTM/src/cloud/acm_ae7_kmt2): the kinetic core of AQCHEM
  * (aqchem_kmt.F90:371-543: Henry's law constants, Initialize, Update_RCONST and the KPP
- * Rodas3 integration over TAUCLD) for ncell cloudy cells on the current device, one cell
- * per thread.  No handle; the caller supplies a device workspace of at least
- * cmaqchem_kmt2_workspace_doubles(1) doubles, and workspace / cmaqchem_kmt2_workspace_doubles(1)
- * cells are integrated at a time.  Device arrays, [element][cell]:
+ * Rodas3 integration over TAUCLD) for ncell cloudy cells on the current device.  No
+ * handle; the caller supplies a device workspace of cmaqchem_kmt2_workspace_doubles(nlanes)
+ * doubles (nlanes >= 1): nlanes threads integrate the cells, each taking the next cell
+ * of a queue (a counter at the end of the workspace, cleared on `stream` by the call)
+ * when its cell ends, so one call's workspace serves any ncell.  Device arrays,
+ * [element][cell]:
  *   params  [CMAQCHEM_KMT2_NPARAM][ncell]: TEMP2 (K), PRES_PA (Pa), TAUCLD (s), PRCRATE (mm/h),
  *           WCAVG, WTAVG (kg/m3), AIRM (mol/m2), ALFA0, ALFA3 (1/s), COSZEN, JH2O2 (1/s),
  *           GAS(LHO) (mol/mol), ISPC8, MTPYRAC, PHOTO (0/1); AQCHEM's REAL arguments are read
@@ -270,6 +272,9 @@ int cmaqchem_ros3_solve_noalloc(const char* mechanism, long long ncell, double* 
 #define CMAQCHEM_KMT2_NPARAM 15
 #define CMAQCHEM_KMT2_NSTAT 10
 long long cmaqchem_kmt2_workspace_doubles(long long nlanes);
+/* The lanes that fill `device` (its SMs times the resident lanes per SM the kernels are
+ * built for), or -1 without such a device. */
+long long cmaqchem_kmt2_default_lanes(int device);
 /* The same integration on host arrays (same [element][cell] layouts; a Fortran caller
  * passes PARAMS(N, 15), VAR_MIX(N, 161), VAR_OUT(N, 161), FIX_OUT(N, 4) or NULL, STATS(N, 10))
  * on `device`: device buffers and the workspace are allocated for the call, the copies
@@ -307,7 +312,8 @@ int cmaqchem_kmt2_solve_device(long long ncell, const double* params, const doub
  *            NH3, NH3/NH4, Cl), whose magnitude above 0.5 makes the reference warn;
  *   stats    [CMAQCHEM_KMT2_NSTAT][ncell] int as for cmaqchem_kmt2_solve_device.
  * A cell whose set-up fails gets NaN in every output.  The workspace is that of
- * cmaqchem_kmt2_solve_device.  Synchronises the stream; returns 0 or -1. */
+ * cmaqchem_kmt2_solve_device (the mapped state lives in it between the mapping and the
+ * set-up).  Synchronises the stream; returns 0 or -1. */
 #define CMAQCHEM_AQ_NGAS 29
 #define CMAQCHEM_AQ_NSURROGATE 31
 #define CMAQCHEM_AQ_NFACTOR 16

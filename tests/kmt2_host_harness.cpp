@@ -1,16 +1,18 @@
 // Host build of the KMT2 device code (cmaq_gb300/csrc/kmt2.cuh) for the CPU tests.
 //
-// Runs the kernel's loop, lane by lane, over the cells: lane l integrates cells
-// l, l + nlanes, ... in its slice of the lane-interleaved workspace, exactly the
-// indexing of k_kmt2_cells (csrc/kmt2.cu), serially.  Built with AddressSanitizer by
-// tests/test_kmt2_host.py, so every workspace and array access of the device code is
-// bounds-checked for the sizes the test runs.
+// Runs the kernels' cell queue serially: lanes 0 .. nlanes-1, each with its slice of the
+// workspace (a warp's 32 lanes side by side, as on the device), take cells in lane order
+// from a counter, and every pass of
+// the loop advances each busy lane by one Rodas3 attempt (kmt2::kq_advance), as one pass
+// of k_kmt2_queue / k_aqchem_queue (csrc/kmt2.cu) does for a warp.  Built with
+// AddressSanitizer by tests/test_kmt2_host.py, so every workspace and array access of the
+// device code is bounds-checked for the sizes the test runs.
 //
 //   kmt2_host_harness <in> <out> ncell nlanes
 //   in:  params [NPARAM][ncell], var_mix [NVAR][ncell]          (doubles)
 //   out: var_out [NVAR][ncell], fix_out [NFIX][ncell] (doubles), stats [NSTAT][ncell] (int32)
 //
-//   kmt2_host_harness aqchem <in> <out> ncell nlanes naer       (the whole AQCHEM, kq_aqchem_cell)
+//   kmt2_host_harness aqchem <in> <out> ncell nlanes naer       (the whole AQCHEM)
 //   in:  params [NPARAM][ncell], gas [29][ncell], aerosol [naer*3][ncell], factors [16] (doubles),
 //        aer_index [31] (int32)
 //   out: gas, aerosol, gas_wdep, aer_wdep, out [10][ncell] (doubles), stats [NSTAT][ncell] (int32)
@@ -18,7 +20,56 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <vector>
+
 #include "../cmaq_gb300/csrc/kmt2.cuh"
+
+// lane l's workspace: warp l / 32's block, column l % 32 (csrc/kmt2.cu)
+static double* lane_ws(double* ws, long long l)
+{
+    return ws + (l / 32) * (kmt2::KQ_S * kmt2::WS_ELEMS) + l % 32;
+}
+
+// the workspace of nlanes lanes: whole warps
+static double* alloc_ws(long long nlanes)
+{
+    return (double*)malloc(sizeof(double) * kmt2::KQ_S * kmt2::WS_ELEMS * ((nlanes + 31) / 32));
+}
+
+struct Slot {   // a lane between attempts
+    kmt2::Cell c;
+    kmt2::Lane L;
+    long long st[kmt2::NSTAT];
+    long long cell = -1;
+};
+
+// The kernels' loop: begin(q, l) starts q.cell in lane l's slice, done(q, l) writes its
+// outputs when kq_advance has ended it.
+template <class Begin, class Done>
+static void run_queue(long long ncell, long long nlanes, double* ws, Begin begin, Done done)
+{
+    std::vector<Slot> lanes((size_t)nlanes);
+    long long next = 0;
+    for (;;) {
+        bool busy = false;
+        for (long long l = 0; l < nlanes; ++l) {
+            Slot& q = lanes[(size_t)l];
+            if (q.cell < 0 && next < ncell) {
+                q.cell = next++;
+                begin(q, l);
+            }
+            busy = busy || q.cell >= 0;
+        }
+        if (!busy) break;
+        for (long long l = 0; l < nlanes; ++l) {
+            Slot& q = lanes[(size_t)l];
+            if (q.cell >= 0 && kmt2::kq_advance(q.c, q.L, lane_ws(ws, l), q.st)) {
+                done(q, l);
+                q.cell = -1;
+            }
+        }
+    }
+}
 
 static int run_aqchem(int argc, char** argv)
 {
@@ -42,12 +93,23 @@ static int run_aqchem(int argc, char** argv)
     double* awd = (double*)calloc(na, sizeof(double));
     double* out = (double*)calloc((size_t)kmt2::KO_N * ncell, sizeof(double));
     int* st = (int*)calloc((size_t)kmt2::NSTAT * ncell, sizeof(int));
-    double* ws = (double*)malloc(sizeof(double) * kmt2::WS_ELEMS * nlanes);
+    double* ws = alloc_ws(nlanes);
     int nfail = 0;
-    for (long long lane = 0; lane < nlanes; ++lane)
-        for (long long c = lane; c < ncell; c += nlanes)
-            nfail += kmt2::kq_aqchem_cell(params + c, gas + c, aer + c, naer, aidx, fac, gwd + c, awd + c, out + c,
-                                          st + c, ncell, ws + lane, nlanes);
+    const long long n = ncell;
+    run_queue(
+        ncell, nlanes, ws,
+        [&](Slot& q, long long l) {
+            const long long c = q.cell;
+            double* w = lane_ws(ws, l);
+            kmt2::kq_aq_map(params + c, gas + c, aer + c, naer, aidx, fac, n, w);
+            kmt2::kq_begin(q.c, q.L, params + c, n, w + kmt2::W_YNEW * kmt2::KQ_S, kmt2::KQ_S, gas[kmt2::KG_HO * n + c],
+                           w, q.st);
+        },
+        [&](Slot& q, long long l) {
+            const long long c = q.cell;
+            nfail += kmt2::kq_aq_finish(q.c, q.L.ierr, q.st, params + c, gas + c, aer + c, naer, aidx, fac, gwd + c,
+                                        awd + c, out + c, st + c, n, lane_ws(ws, l));
+        });
     FILE* fo = fopen(argv[3], "wb");
     if (!fo) return 4;
     fwrite(gas, sizeof(double), ng, fo);
@@ -81,13 +143,27 @@ int main(int argc, char** argv)
     double* vout = (double*)calloc((size_t)kmt2::NVAR * ncell, sizeof(double));
     double* fout = (double*)calloc((size_t)kmt2::NFIX * ncell, sizeof(double));
     int* st = (int*)calloc((size_t)kmt2::NSTAT * ncell, sizeof(int));
-    double* ws = (double*)malloc(sizeof(double) * kmt2::WS_ELEMS * nlanes);
+    double* ws = alloc_ws(nlanes);
     const double* params = in;
     const double* vmix = in + (size_t)kmt2::NPARAM * ncell;
     int nfail = 0;
-    for (long long lane = 0; lane < nlanes; ++lane)
-        for (long long c = lane; c < ncell; c += nlanes)
-            nfail += kmt2::kq_cell(params + c, vmix + c, vout + c, fout + c, st + c, ncell, ws + lane, nlanes);
+    const long long n = ncell;
+    run_queue(
+        ncell, nlanes, ws,
+        [&](Slot& q, long long l) {
+            const long long c = q.cell;
+            kmt2::kq_begin(q.c, q.L, params + c, n, vmix + c, n, params[kmt2::P_HO * n + c], lane_ws(ws, l), q.st);
+        },
+        [&](Slot& q, long long l) {
+            const long long c = q.cell;
+            const double* y = lane_ws(ws, l) + kmt2::W_Y * kmt2::KQ_S;
+            const double* f = lane_ws(ws, l) + kmt2::W_F * kmt2::KQ_S;
+            const bool nan = q.L.ierr <= -101;   // failed set-up: no state to return
+            for (int i = 0; i < kmt2::NVAR; ++i) vout[i * n + c] = nan ? (double)NAN : y[i * kmt2::KQ_S];
+            for (int i = 0; i < kmt2::NFIX; ++i) fout[i * n + c] = nan ? (double)NAN : f[i * kmt2::KQ_S];
+            for (int i = 0; i < kmt2::NSTAT; ++i) st[i * n + c] = (int)q.st[i];
+            nfail += q.L.ierr == 1 ? 0 : 1;
+        });
     FILE* fo = fopen(argv[2], "wb");
     if (!fo) return 4;
     fwrite(vout, sizeof(double), (size_t)kmt2::NVAR * ncell, fo);

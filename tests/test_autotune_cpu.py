@@ -5,7 +5,7 @@ from cmaq_gb300.autotune import Candidate, cache_key, candidates
 def test_candidate_space():
     c = candidates(("default", "r168"))
     assert len(c) == 2 * 7
-    assert len(candidates()) == 5 * 7
+    assert len(candidates()) == 6 * 7
     assert Candidate("default", 0, 8) in c                  # free-running warps only with 8-warp blocks
     assert all(x.block_warps in (2, 4, 8) and x.lockstep in (0, 1, 2) for x in c)
     assert not any(x.lockstep == 0 and x.block_warps != 8 for x in c)

@@ -140,9 +140,11 @@ def test_kmt2_entry_checks_arguments_before_any_cuda_call():
     """cmaqchem_kmt2_* reject bad arguments on the host (no GPU needed)."""
     from cmaq_gb300 import _lib
     L = _lib.lib()
-    per_lane = L.cmaqchem_kmt2_workspace_doubles(1)
-    assert per_lane == 9 * 161 + 2 * 738 + 269 + 4
-    assert L.cmaqchem_kmt2_workspace_doubles(1000) == 1000 * per_lane
+    per_lane = 7 * 161 + 2 * 738 + 269 + 4
+    tail = L.cmaqchem_kmt2_workspace_doubles(1) - 32 * per_lane   # whole warps, then the queue's counter
+    assert 1 <= tail <= 64
+    assert L.cmaqchem_kmt2_workspace_doubles(32) == 32 * per_lane + tail
+    assert L.cmaqchem_kmt2_workspace_doubles(1000) == 1024 * per_lane + tail
     assert L.cmaqchem_kmt2_workspace_doubles(0) == 0
     assert L.cmaqchem_kmt2_solve_device(0, None, None, None, None, None, None, 0, None) == 0
     assert L.cmaqchem_kmt2_solve_device(-1, None, None, None, None, None, None, 0, None) == -1

@@ -1,8 +1,9 @@
 """The KMT2 device code (cmaq_gb300/csrc/kmt2.cuh), built for the host, against the oracle.
 
 kmt2.cuh is host/device code: tests/kmt2_host_harness.cpp compiles it with g++ under
-AddressSanitizer and UndefinedBehaviorSanitizer and runs the kernel's lane loop over the
-cells serially (same interleaved workspace, same [element][cell] arrays), so these CPU
+AddressSanitizer and UndefinedBehaviorSanitizer and runs the kernels' cell queue serially
+(one Rodas3 attempt per busy lane per pass, same interleaved workspace, same
+[element][cell] arrays), so these CPU
 tests check the product's arithmetic bit for bit against the oracle (same libm on both
 sides, exp and pow by the portable series of both) and every array index for the sizes
 below.  tests/test_gpu_kmt2.py holds the GPU to the same bits.
@@ -36,7 +37,7 @@ def test_device_code_equals_the_oracle(kmt2_harness, o, tmp_path, ncell, nlanes)
     var, fix, st, nfail, ws_elems = run(kmt2_harness, o, p, v, nlanes, tmp_path)
     vr, fr, sr, nf_r = o.cells(p, v)
     assert nfail == nf_r == 0
-    assert ws_elems == 9 * o.nvar + 2 * o.lu_nonzero + o.nreact + o.nfix
+    assert ws_elems == 7 * o.nvar + 2 * o.lu_nonzero + o.nreact + o.nfix
     assert np.array_equal(st, sr)
     assert np.array_equal(var, vr)
     assert np.array_equal(fix, fr)
@@ -62,7 +63,7 @@ def test_switches_and_failed_cells(kmt2_harness, o, tmp_path):
 
 @pytest.mark.parametrize("ncell,nlanes,ispc8,mtpyrac", [(23, 5, 0, 0), (9, 9, 1, 1)])
 def test_whole_aqchem_device_code_equals_the_oracle(kmt2_harness, o, tmp_path, ncell, nlanes, ispc8, mtpyrac):
-    """kq_aqchem_cell (mapping, kinetic core, redistribution) built for the host against the
+    """The whole AQCHEM (kq_aq_map, the queued kinetic core, kq_aq_finish) built for the host against the
     oracle's restatement: every output bit for bit, with a shuffled surrogate order (the
     positions array maps AQCHEM's surrogates into the caller's aerosol list) and a failed
     set-up next to good cells."""
