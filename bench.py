@@ -26,6 +26,8 @@ Arms and extras
   ``cracmm2``.
 * --impl reference: the reference algorithm (C oracle; the Fortran cannot be
   compiled here) on all host cores, bounded sample per step.
+* --only-hetchem: HETCHEM_RATES alone (cmaqchem_hetchem_rates_device) on the workload
+  grid's cells, its own line: cells/s, HBM roofline, end to end, the oracle on a sample.
 * --only-aqchem: the KMT2 aqueous kinetics kernel alone (cmaqchem_kmt2_solve_device) on
   --aqchem-cells seeded cloudy cells per call, with its own line: cells/s, FP64
   roofline, end to end through pinned host memory, the C oracle on a host sample and a
@@ -590,6 +592,69 @@ def run_aqchem_whole(dev, ncell: int, steps: int) -> dict:
             "max_abs_mass_balance_percent": float(np.abs(wo[6:10]).max())}
 
 
+def run_hetchem(device: int, ncell: int, steps: int, threads: int) -> dict:
+    """HETCHEM_RATES (cmaqchem_hetchem_rates_device): KHETERO of ncell seeded cells from
+    their CGRID aerosol block and met fields (cmaq_gb300/synthetic.py: make_aerosol_cells).
+    Device time by CUDA events around each call (inputs resident); end to end with the
+    aerosol block and met copied from pinned host memory and KHETERO copied back; the HBM
+    roofline of the call's algorithmic bytes (the block and met read once, KHETERO written
+    once); the oracle on a host sample for the baseline and a parity summary."""
+    import torch
+    from cmaq_gb300.hetchem import hetchem_rates, layout
+    from cmaq_gb300.synthetic import make_aerosol_cells
+    nae, _, nhet = layout()
+    ae, ta, p, q, d = make_aerosol_cells(ncell, seed=2018)
+    dev = torch.device(f"cuda:{device}")
+    host = [torch.from_numpy(x).pin_memory() for x in (ae, ta, p, q, d)]
+    dv = [x.to(dev) for x in host]
+    out = torch.empty((ncell, nhet), dtype=torch.float64, device=dev)
+    hout = torch.empty((ncell, nhet), dtype=torch.float64).pin_memory()
+    for _ in range(3):
+        hetchem_rates(*dv, out=out)
+    torch.cuda.synchronize(dev)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ms = []
+    for _ in range(steps):
+        ev[0].record()
+        hetchem_rates(*dv, out=out)
+        ev[1].record()
+        torch.cuda.synchronize(dev)
+        ms.append(ev[0].elapsed_time(ev[1]))
+    dev_ms = float(np.median(ms))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for hx, dx in zip(host, dv):
+            dx.copy_(hx, non_blocking=True)
+        hetchem_rates(*dv, out=out)
+        hout.copy_(out, non_blocking=True)
+        torch.cuda.synchronize(dev)
+    e2e_s = (time.perf_counter() - t0) / steps
+    nbytes = ncell * (nae * 4 + 16 + nhet * 8)
+    peak = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"] if (ROOT / "MEASURED_PEAKS.json").exists() else None
+    achieved = nbytes / (dev_ms * 1e-3) / 1e9
+    res = {"ncell": ncell, "ms_per_call": dev_ms, "value": ncell / (dev_ms * 1e-3),
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": None if not peak else achieved / peak, "traffic": None,
+                        "bytes_per_cell": nae * 4 + 16 + nhet * 8,
+                        "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth)"},
+           "e2e": {"value": ncell / e2e_s, "unit": "cells/s",
+                   "h2d_bytes_per_step": int(sum(x.numel() * x.element_size() for x in host)),
+                   "d2h_bytes_per_step": int(hout.numel() * 8)}}
+    if threads > 0:                                   # CPU baseline: the oracle on a sample
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import hetchem as het_oracle
+        nsample = min(ncell, 20000 * threads)
+        t0 = time.perf_counter()
+        want = het_oracle.rates(ae[:, :nsample], ta[:nsample], p[:nsample], q[:nsample], d[:nsample], threads=threads)
+        wall = time.perf_counter() - t0
+        got = out[:nsample].cpu().numpy()
+        rel = np.abs(got - want) / np.maximum(np.abs(want), 1e-300)
+        res["cpu"] = {"value": nsample / wall, "cells": nsample, "wall_s": wall, "threads": threads}
+        res["parity"] = {"cells": nsample, "max_rel_diff": float(rel.max()),
+                         "same_zero_pattern": bool(((got == 0) == (want == 0)).all())}
+    return res
+
+
 def run_aqchem(device: int, ncell: int, steps: int, warmup: int, threads: int, whole: bool = True) -> dict:
     """KMT2 aqueous kinetics (cmaqchem_kmt2_solve_device): one call integrates ncell seeded
     cloudy cells over their cloud time.  Device time by CUDA events around each call
@@ -743,6 +808,9 @@ def main():
                     help="skip the skewed-stiffness CONUS grid and CRACMM2 on 1M cells")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the accuracy block and the tight-tolerance leg")
     ap.add_argument("--no-aqchem", action="store_true", help="skip the KMT2 aqueous kinetics leg")
+    ap.add_argument("--no-hetchem", action="store_true", help="skip the HETCHEM_RATES leg")
+    ap.add_argument("--only-hetchem", action="store_true",
+                    help="only the HETCHEM_RATES kernel on the workload grid's cells, its own JSON line")
     ap.add_argument("--tight-steps", type=int, default=2,
                     help="CHEM calls of the tight-tolerance leg on the workload grid (0: skip)")
     ap.add_argument("--adjoint-dims", default="100x100x35", help="grid of the adjoint window, NCOLSxNROWSxNLAYS")
@@ -802,6 +870,26 @@ def main():
                               "higher_is_better": False, "dtype": "f64", "data": "synthetic", "adjoint": r}))
         return 0
     peak_rec = fp64_peak_record(device) if rank == 0 or world == 1 else None
+    if a.only_hetchem:
+        thr = 0 if (a.no_cpu or rank != 0) else host_threads()
+        dims = WORKLOADS[a.workload]
+        ncell = dims["ncols"] * dims["nrows"] * dims["nlays"]
+        r = run_hetchem(device, ncell, min(a.steps, 5), thr)
+        if rank == 0:
+            line = {"metric": "HETCHEM_RATES: grid cells of KHETERO per second", "value": r["value"],
+                    "unit": "cells/s", "n_gpus": 1, "steps": min(a.steps, 5), "warmup": 3,
+                    "ms_per_step": r["ms_per_call"], "higher_is_better": True, "scaling": "weak",
+                    "vs_baseline": None, "dtype": "f32+f64",
+                    "data": "synthetic (seeded; cmaq_gb300/synthetic.py: make_aerosol_cells)",
+                    "config": {"workload": f"{ncell} cells ({a.workload} grid), cb6r5_ae7_aq aerosol block "
+                                           "(84 rows) and met, 17 KHETERO",
+                               "l2": f"inputs of {ncell * 352 / 1e9:.1f} GB per call, larger than the 129 MB L2"},
+                    "roofline": r["roofline"], "e2e": r["e2e"], "gpu_launches": min(a.steps, 5), "hetchem": r}
+            if "cpu" in r:
+                line["cpu_baseline"] = {"value": r["cpu"]["value"], "unit": "cells/s", "cores": r["cpu"]["threads"],
+                                        "kind": "port", "sample": f"{r['cpu']['cells']} cells"}
+            print(json.dumps(line))
+        return 0
     if a.only_aqchem:
         thr = 0 if (a.no_cpu or rank != 0) else host_threads()
         r = run_aqchem(device, a.aqchem_cells, min(a.steps, 5), max(a.warmup, 3), thr)
@@ -893,6 +981,8 @@ def main():
     gear = leg("gear", extras and not a.no_gear, lambda: run_gear(device, a.steps))
     skewed = leg("skewed", extras and not a.no_configs, lambda: run_skewed(device, STEPS_PER_HOUR, tuned))
     cracmm2 = leg("cracmm2", extras and not a.no_configs, lambda: run_cracmm2(device, STEPS_PER_HOUR))
+    hetchem = leg("hetchem", extras and not a.no_hetchem,
+                  lambda: run_hetchem(device, g.ncell, 5, 0 if a.no_cpu else host_threads()))
     aqchem = leg("aqchem", extras and not a.no_aqchem,
                  lambda: run_aqchem(device, a.aqchem_cells, 3, 3, 0 if a.no_cpu else host_threads()))
     if aqchem is not None:
@@ -961,6 +1051,7 @@ def main():
             "skewed": skewed,
             "cracmm2": cracmm2,
             "aqchem": aqchem,
+            "hetchem": hetchem,
             "e2e": e2e,
             "cpu_baseline": cpu,
             "clocks": batched["clocks"],

@@ -85,6 +85,9 @@ def lib(variant: str = "default") -> C.CDLL:
     L.cmaqchem_kmt2_solve_device.argtypes = [C.c_longlong, vp, vp, vp, vp, vp, vp, C.c_longlong, vp]
     L.cmaqchem_kmt2_solve.argtypes = [C.c_longlong, vp, vp, vp, vp, vp, C.c_int]
     L.cmaqchem_aqchem_device.argtypes = [C.c_longlong, vp, vp, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, C.c_longlong, vp]
+    L.cmaqchem_hetchem_layout.argtypes = [C.c_char_p, ip, ip, ip]
+    L.cmaqchem_hetchem_rates_device.argtypes = [C.c_char_p, C.c_longlong, vp, vp, vp, vp, vp, vp, vp]
+    L.cmaqchem_hetchem_rates.argtypes = [C.c_char_p, C.c_longlong, vp, vp, vp, vp, vp, vp, C.c_int]
     return L
 
 

@@ -325,3 +325,59 @@ def make_cloud_columns(n: int, seed: int = 0, ispc8: int = 0, mtpyrac: int = 0):
     for (name, mode), (lo, hi) in ar.items():
         a[:, aer_names.index(name) + na * mode] = 10 ** rng.uniform(lo, hi, n)
     return p, g, a, np.arange(na, dtype=np.int32), np.array(man["crustal_factors"])
+
+
+def hetchem_tables(mech: str = "cb6r5_ae7_aq") -> dict:
+    return json.loads((Path(__file__).resolve().parent / "mechs" / mech / "hetchem.json").read_text())
+
+
+# log10 ranges (ug/m3) of the aerosol species' mass per mode (Aitken, accumulation, coarse)
+_AE_MASS = {"ASO4": ((-2.5, -0.5), (-1.0, 1.3), (-1.5, 0.5)), "ANO3": ((-3, -1), (-2.0, 1.0), (-2.0, 0.3)),
+            "ANH4": ((-3, -1), (-1.5, 0.9), (-2.0, 0.0)), "ACL": ((-4, -2), (-3.0, 0.3), (-3.0, 0.5)),
+            "ANA": ((-4, -2), (-3.0, 0.0), None), "AH2O": ((-3, -0.5), (-2.0, 1.7), (-2.0, 1.3)),
+            "AH3OP": ((-7, -5), (-6.0, -2.5), (-7.0, -4.0)), "AORGH2O": (None, (-3.0, 0.5), None),
+            "ASOIL": (None, None, (-1.0, 1.3)), "ACORS": (None, None, (-1.0, 1.3)), "ASEACAT": (None, None, (-2.0, 0.7))}
+_AE_DEFAULT = ((-3.5, -1.5), (-3.0, 0.3), (-2.5, 0.5))
+# number (#/m3) and geometric mean diameter (m) ranges, sigma_g, per mode
+_AE_NUM = ((9.0, 10.7), (8.0, 9.7), (4.5, 6.5))
+_AE_DG = ((0.01e-6, 0.04e-6), (0.08e-6, 0.3e-6), (1.0e-6, 4.0e-6))
+_AE_SG = (1.7, 2.0, 2.2)
+
+
+def make_aerosol_cells(n: int, seed: int = 0, mech: str = "cb6r5_ae7_aq"):
+    """Seeded inputs of HETCHEM_RATES for n grid cells: the CGRID aerosol block ae [NAE][n]
+    (float32; species mass log-uniform in the decades of ``_AE_MASS`` per mode, ug/m3; the
+    number per mode log-uniform, #/m3, and the surface area of a lognormal mode with a
+    geometric mean diameter in ``_AE_DG`` and sigma_g of ``_AE_SG``, m2/m3, as CGRID's
+    SRF rows hold it), and met [n] float32: temperature 230-310 K, pressure 200-1013 hPa,
+    relative humidity 2-100 % given as the water-vapour mass mixing ratio of the same
+    saturation formula, air density of the ideal gas.  Every tenth cell is clean (all
+    masses at 1e-6 of their draw)."""
+    t = hetchem_tables(mech)
+    rows = t["ae_rows"]
+    rng = np.random.default_rng(seed)
+    ae = np.zeros((len(rows), n), np.float32)
+    clean = np.where(np.arange(n) % 10 == 9, 1.0e-6, 1.0)
+    for s in t["species"]:
+        rng_s = _AE_MASS.get(s["bulkname"], _AE_DEFAULT)
+        for m in range(3):
+            r = s["row"][m]
+            if r < 0:
+                continue
+            lo, hi = rng_s[m] if rng_s[m] is not None else _AE_DEFAULT[m]
+            ae[r] = (10 ** rng.uniform(lo, hi, n) * clean).astype(np.float32)
+    for m in range(3):
+        num = 10 ** rng.uniform(*_AE_NUM[m], n)
+        dg = rng.uniform(*_AE_DG[m], n)
+        ae[t["num_rows"][m]] = num.astype(np.float32)
+        ae[t["srf_rows"][m]] = (np.pi * num * dg ** 2 * np.exp(2.0 * np.log(_AE_SG[m]) ** 2)).astype(np.float32)
+    ta = rng.uniform(230.0, 310.0, n)
+    pres = rng.uniform(20000.0, 101325.0, n)
+    rh = rng.uniform(0.02, 1.0, n)
+    esat = 610.94 * np.exp(17.625 * (ta - 273.15) / (ta - 273.15 + 243.04))
+    e = np.minimum(rh * esat, 0.5 * pres)
+    eps = 18.0153 / 28.9628
+    qv = eps * e / (pres - e)
+    dens = pres / (287.0 * ta)
+    f = lambda a: a.astype(np.float32)
+    return ae, f(ta), f(pres), f(qv), f(dens)

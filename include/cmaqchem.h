@@ -322,6 +322,28 @@ int cmaqchem_aqchem_device(long long ncell, const double* params, double* gas, d
                            const int* aer_index, const double* factors, double* gas_wdep, double* aer_wdep,
                            double* out, int* stats, double* workspace, long long workspace_doubles, void* stream);
 
+/* Heterogeneous rate constants KHETERO: HETCHEM_RATES (CCTM/src/aero/aero6/AEROSOL_CHEMISTRY.F:
+ * 282-1535, with HETCHEM_EXTRACT_AERO, extract_aero, calcmoments, getpar, N2O5_GAMMA,
+ * CALCISOPGAMMAS and PNCOM_LOSS) for ncell = NCOLS * NROWS * NLAYS grid cells, the step the
+ * reference runs before CHEM (rbdriver.F:409).  Device arrays:
+ *   ae       CONC(1, 1, 1, AE_STRT): the aerosol block of CGRID, nae rows of ncell REAL (ug/m3;
+ *            NUM* #/m3; SRF* m2/m3), the AE namelist's species expanded by mode;
+ *   ta, pres, qv, dens  (NCOLS, NROWS, NLAYS) REAL: K, Pa, kg/kg, kg/m3;
+ *   khetero  KHETERO(NHETERO, NCOLS, NROWS, NLAYS) REAL(8) out, the mechanism's HETERO order,
+ *            the array the CHEM entries take.
+ * cmaqchem_hetchem_layout gives the block's rows, its first row in the mechanism's CGRID
+ * (0-based) and NHETERO.  Only cb6r5_ae7_aq is built.  Synchronises the stream; returns 0 or
+ * -1.  cmaqchem_hetchem_rates takes host arrays (device buffers for the call). */
+#define CMAQCHEM_HET_CB6R5_NAE 84
+#define CMAQCHEM_HET_CB6R5_AE_FIRST 131
+#define CMAQCHEM_HET_CB6R5_NHETERO 17
+int cmaqchem_hetchem_layout(const char* mechanism, int* nae, int* ae_first, int* nhetero);
+int cmaqchem_hetchem_rates_device(const char* mechanism, long long ncell, const float* ae, const float* ta,
+                                  const float* pres, const float* qv, const float* dens, double* khetero,
+                                  void* stream);
+int cmaqchem_hetchem_rates(const char* mechanism, long long ncell, const float* ae, const float* ta,
+                           const float* pres, const float* qv, const float* dens, double* khetero, int device);
+
 /* Text of the last error of the calling thread; returns its length. */
 int cmaqchem_last_error(char* buf, size_t len);
 

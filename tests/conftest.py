@@ -57,6 +57,41 @@ def kmt2_harness(tmp_path_factory):
     return exe
 
 
+@pytest.fixture(scope="session")
+def hetchem_harness(tmp_path_factory):
+    """tests/hetchem_host_harness.cpp (the HETCHEM_RATES device code built for the host)
+    compiled with g++ under AddressSanitizer and UndefinedBehaviorSanitizer."""
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no C++ compiler")
+    exe = tmp_path_factory.mktemp("hetchem") / "hetchem_host_harness"
+    cmd = [gxx, "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-fsanitize=address,undefined",
+           "-fno-sanitize-recover=all", "-o", str(exe), str(ROOT / "tests" / "hetchem_host_harness.cpp")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0 and "sanitize" in r.stderr:
+        pytest.skip("sanitizer runtime not available")
+    assert r.returncode == 0, r.stderr[-3000:]
+    return exe
+
+
+def run_hetchem_harness(exe, ae, ta, pres, qv, dens, workdir):
+    """KHETERO [ncell][NHET] of the host build for the aerosol block ae [NAE][ncell] and met."""
+    import os
+    import subprocess
+    import numpy as np
+    n = ae.shape[1]
+    inp, out = workdir / "het_in.bin", workdir / "het_out.bin"
+    np.concatenate([np.asarray(ae, np.float32).ravel()] + [np.asarray(x, np.float32).ravel()
+                                                           for x in (ta, pres, qv, dens)]).tofile(inp)
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=1:abort_on_error=0", UBSAN_OPTIONS="halt_on_error=1")
+    r = subprocess.run([str(exe), str(inp), str(out), str(n)], capture_output=True, text=True, timeout=600, env=env)
+    assert r.returncode == 0, r.stderr[-3000:]
+    assert "runtime error" not in r.stderr, r.stderr[-3000:]
+    return np.fromfile(out, np.float64).reshape(n, -1)
+
+
 def run_kmt2_harness(exe, params_t, var_mix_t, nlanes, workdir):
     """Run the host build on [element][cell] arrays; returns var_out [161][n], fix_out
     [4][n], stats [10][n], the number of failed cells and the per-lane workspace size."""

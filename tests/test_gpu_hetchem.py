@@ -1,0 +1,74 @@
+"""GPU parity of the heterogeneous rate constants (HETCHEM_RATES, CCTM/src/aero/aero6/
+AEROSOL_CHEMISTRY.F) against the oracle, through the C ABI
+(cmaqchem_hetchem_rates_device, cmaqchem_hetchem_rates).
+
+The device code performs the oracle's IEEE operations in the same order (built with
+-fmad=false), but its exp, log, pow, tanh and log10 (float and double) are CUDA's, which
+differ from the host library's by an ulp or two.  The outputs are smooth functions of
+those values with no step-size amplification, so the bar is a relative difference of
+1e-5 per KHETERO entry (float intermediates carry 6e-8 per ulp) and the same zero
+pattern; tests/test_hetchem_host.py holds the same code, built for the host, to the
+oracle bit for bit.
+"""
+import numpy as np
+import pytest
+
+h = pytest.importorskip("hetchem")   # oracle/hetchem.py
+pytestmark = pytest.mark.gpu
+RTOL = 1e-5
+
+
+def _dev(*arrays):
+    import torch
+    return [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in arrays]
+
+
+def test_layout_matches_the_tables():
+    from cmaq_gb300.hetchem import layout
+    t = h.tables()
+    assert layout() == (len(t["ae_rows"]), t["ae_first"], len(t["hetero"]))
+    from cmaq_gb300 import _lib
+    with pytest.raises(_lib.ChemError):
+        layout("cracmm2")
+
+
+@pytest.mark.parametrize("n,seed", [(20000, 21), (777, 4)])
+def test_device_rates_match_the_oracle(n, seed):
+    import torch
+    from cmaq_gb300.hetchem import hetchem_rates
+    from cmaq_gb300.synthetic import make_aerosol_cells
+    ae, ta, p, q, d = make_aerosol_cells(n, seed=seed)
+    got = hetchem_rates(*_dev(ae, ta, p, q, d))
+    torch.cuda.synchronize()
+    got = got.cpu().numpy()
+    want = h.rates(ae, ta, p, q, d, threads=8)
+    assert np.isfinite(got).all()
+    assert ((got == 0) == (want == 0)).all()
+    rel = np.abs(got - want) / np.maximum(np.abs(want), 1e-300)
+    assert rel.max() <= RTOL, (rel.max(), np.unravel_index(rel.argmax(), rel.shape))
+
+
+def test_cgrid_view_and_host_entry_give_the_same_bits():
+    """The aerosol block read in place from a CGRID (CONC(1,1,1,AE_STRT) with the gas rows
+    before it), and the host-array entry, equal the compact device call bit for bit."""
+    import torch
+    from cmaq_gb300.hetchem import hetchem_rates, hetchem_rates_host, layout
+    from cmaq_gb300.synthetic import make_aerosol_cells
+    nae, first, _ = layout()
+    ae, ta, p, q, d = make_aerosol_cells(5000, seed=8)
+    cgrid = np.full((first + nae + 3, ae.shape[1]), -1.0, np.float32)
+    cgrid[first:first + nae] = ae
+    cg, tt, pt, qt, dt = _dev(cgrid, ta, p, q, d)
+    a = hetchem_rates(cg[first:first + nae], tt, pt, qt, dt).cpu().numpy()
+    b = hetchem_rates(*_dev(ae), tt, pt, qt, dt).cpu().numpy()
+    c = hetchem_rates_host(ae, ta, p, q, d)
+    torch.cuda.synchronize()
+    assert np.array_equal(a, b) and np.array_equal(b, c)
+
+
+def test_empty_call_and_bad_arguments():
+    from cmaq_gb300 import _lib
+    L = _lib.lib()
+    assert L.cmaqchem_hetchem_rates_device(b"cb6r5_ae7_aq", 0, None, None, None, None, None, None, None) == 0
+    assert L.cmaqchem_hetchem_rates_device(b"cb6r5_ae7_aq", 5, None, None, None, None, None, None, None) == -1
+    assert "null" in _lib.last_error()
