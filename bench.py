@@ -20,10 +20,14 @@ Arms and extras
   a bounded CPU sample of the reference algorithm (the C oracle, BLKSIZE 50 with the
   stiffness reordering) on the host cores -> ``cpu_baseline``; the differentiable
   1-hour window on 100x100x35 cells (forward and discrete-adjoint times) ->
-  ``adjoint``; EBI against ROS3 on a 100x100x10 grid -> ``ebi``; with --all-configs also
-  the CONUS grid with skewed stiffness (30 % plume columns), batched against plain ->
-  ``skewed``, and CRACMM2 on 200x200x25 cells, batched hour and adjoint window ->
-  ``cracmm2``.
+  ``adjoint``; EBI on the workload grid -> ``ebi``; SMVGEAR against ROS3 on 100x100x10
+  cells -> ``gear``; the accuracy block (GPU hour against the oracle's tight solution
+  on a sample of cells) -> ``accuracy``; the KMT2 aqueous kinetics on 200,000 cloudy
+  cells -> ``aqchem``; HETCHEM_RATES on the workload grid -> ``hetchem``.  With
+  --all-configs also the CONUS grid with skewed stiffness (30 % plume columns), batched
+  against plain -> ``skewed``, and CRACMM2 on 200x200x25 cells, batched hour and
+  adjoint window -> ``cracmm2``; with --tight-steps N the tight-tolerance timing leg
+  -> ``tight``.
 * --impl reference: the reference algorithm (C oracle; the Fortran cannot be
   compiled here) on all host cores, bounded sample per step.
 * --only-hetchem: HETCHEM_RATES alone (cmaqchem_hetchem_rates_device) on the workload
@@ -804,15 +808,16 @@ def main():
     ap.add_argument("--no-gear", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="only the headline arms (batched, plain, e2e, CPU baseline)")
-    ap.add_argument("--no-configs", action="store_true",
-                    help="skip the skewed-stiffness CONUS grid and CRACMM2 on 1M cells")
+    ap.add_argument("--all-configs", action="store_true",
+                    help="also the skewed-stiffness CONUS grid and CRACMM2 on 1M cells (about 5 minutes)")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the accuracy block and the tight-tolerance leg")
     ap.add_argument("--no-aqchem", action="store_true", help="skip the KMT2 aqueous kinetics leg")
     ap.add_argument("--no-hetchem", action="store_true", help="skip the HETCHEM_RATES leg")
     ap.add_argument("--only-hetchem", action="store_true",
                     help="only the HETCHEM_RATES kernel on the workload grid's cells, its own JSON line")
-    ap.add_argument("--tight-steps", type=int, default=2,
-                    help="CHEM calls of the tight-tolerance leg on the workload grid (0: skip)")
+    ap.add_argument("--tight-steps", type=int, default=0,
+                    help="CHEM calls of the tight-tolerance leg on every 7th layer of the workload grid "
+                         "(0: skip; 2 takes about 14 minutes)")
     ap.add_argument("--adjoint-dims", default="100x100x35", help="grid of the adjoint window, NCOLSxNROWSxNLAYS")
     ap.add_argument("--only-adjoint", action="store_true",
                     help="time only the adjoint window and print its own line (for profiling)")
@@ -869,7 +874,6 @@ def main():
                               "warmup": 1, "ms_per_step": (r["forward_ms"] + r["backward_ms"]) / a.steps,
                               "higher_is_better": False, "dtype": "f64", "data": "synthetic", "adjoint": r}))
         return 0
-    peak_rec = fp64_peak_record(device) if rank == 0 or world == 1 else None
     if a.only_hetchem:
         thr = 0 if (a.no_cpu or rank != 0) else host_threads()
         dims = WORKLOADS[a.workload]
@@ -890,6 +894,7 @@ def main():
                                         "kind": "port", "sample": f"{r['cpu']['cells']} cells"}
             print(json.dumps(line))
         return 0
+    peak_rec = fp64_peak_record(device) if rank == 0 or world == 1 else None
     if a.only_aqchem:
         thr = 0 if (a.no_cpu or rank != 0) else host_threads()
         r = run_aqchem(device, a.aqchem_cells, min(a.steps, 5), max(a.warmup, 3), thr)
@@ -979,8 +984,8 @@ def main():
     ebi = leg("ebi", extras and not a.no_ebi, lambda: run_ebi(device, STEPS_PER_HOUR, g))
     adjoint = leg("adjoint", extras and not a.no_adjoint, lambda: run_adjoint(device, STEPS_PER_HOUR, adims))
     gear = leg("gear", extras and not a.no_gear, lambda: run_gear(device, a.steps))
-    skewed = leg("skewed", extras and not a.no_configs, lambda: run_skewed(device, STEPS_PER_HOUR, tuned))
-    cracmm2 = leg("cracmm2", extras and not a.no_configs, lambda: run_cracmm2(device, STEPS_PER_HOUR))
+    skewed = leg("skewed", extras and a.all_configs, lambda: run_skewed(device, STEPS_PER_HOUR, tuned))
+    cracmm2 = leg("cracmm2", extras and a.all_configs, lambda: run_cracmm2(device, STEPS_PER_HOUR))
     hetchem = leg("hetchem", extras and not a.no_hetchem,
                   lambda: run_hetchem(device, g.ncell, 5, 0 if a.no_cpu else host_threads()))
     aqchem = leg("aqchem", extras and not a.no_aqchem,

@@ -52,7 +52,11 @@ VARIANTS = {"default": (GEN_DEFAULT, [Q_DEFAULT]),
             # the default is 4, 128 registers), or without the block barriers between phases
             "kq2": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_MIN_BLOCKS=2"]),
             "kq3": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_MIN_BLOCKS=3"]),
-            "kqfree": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_LOCKSTEP=0"])}
+            "kqfree": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_LOCKSTEP=0"]),
+            # KMT2 refill deferred until 8, 16 or 32 of a block's 128 lanes are idle
+            "kqr8": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_REFILL_MIN=8"]),
+            "kqr16": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_REFILL_MIN=16"]),
+            "kqr32": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_REFILL_MIN=32"])}
 
 
 def _is_generated_math(src: Path) -> bool:
@@ -63,6 +67,19 @@ def _is_generated_math(src: Path) -> bool:
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-rdc=true", "-fmad=false", "-lineinfo", "-Xcompiler", "-fPIC",
               "-Xptxas", "-O3"]
+
+
+# The default library's exceptions, measured slower at the 80-register cap: the adjoint's
+# own generated routines (called only by the adjoint kernels, launch-bounded for 16 warps
+# per SM) and everything of CRACMM2 (twice CB6r5's species: its queue kernel runs 16
+# warps per SM with its routines at 128 registers; 58,989 against 51,080 grid-cells/s).
+def _flags(src: Path, variant: str, gen_extra: list, all_extra: list) -> list:
+    if variant == "default":
+        if src.name.startswith("cracmm2_") or src.name == "mech_cracmm2.cu":
+            return [Q16] + (GEN128 if _is_generated_math(src) else [])
+        if _is_generated_math(src) and "_adj" in src.name:
+            return all_extra + GEN128
+    return all_extra + (gen_extra if _is_generated_math(src) else [])
 
 
 def _nvcc() -> str:
@@ -101,18 +118,22 @@ def build(jobs: int | None = None, verbose: bool = False, variant: str = "defaul
         rel = src.relative_to(CSRC).as_posix().replace("/", "__")
         obj = out_dir / (rel[:-3] + ".o")
         objs.append(obj)
-        if obj.exists() and obj.stat().st_mtime > max(src.stat().st_mtime, hdr_mtime):
+        stamp = obj.with_suffix(".flags")   # the flags the object was built with
+        flags = " ".join(_flags(src, variant, gen_extra, all_extra))
+        if (obj.exists() and obj.stat().st_mtime > max(src.stat().st_mtime, hdr_mtime) and stamp.exists()
+                and stamp.read_text() == flags):
             continue
         todo.append((src, obj))
 
     def compile_one(item):
         src, obj = item
-        extra = all_extra + (gen_extra if _is_generated_math(src) else [])
+        extra = _flags(src, variant, gen_extra, all_extra)
         cmd = [nvcc, *ARCH, *NVCC_FLAGS, *extra, "-I", str(CSRC), "-c", str(src), "-o", str(obj) + ".tmp"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {src.name}:\n{r.stderr[-4000:]}")
         os.replace(str(obj) + ".tmp", obj)
+        obj.with_suffix(".flags").write_text(" ".join(extra))
         if verbose:
             print("compiled", src.name, flush=True)
 

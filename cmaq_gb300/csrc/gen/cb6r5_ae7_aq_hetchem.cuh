@@ -26,6 +26,7 @@ struct HetTables {
     float density[NSPC];
     float molwt[NSPC];
     float min_conc[NSPC][3];
+    double m3fac[NSPC];   // REAL( 1.0E-9 * f6pi / density, 8 ), the factor of the moment sums
     int charge[NSPC];
     unsigned char tracer[NSPC], no_m2wet[NSPC], om[NSPC];
     short row[NSPC][3];   // row in the aerosol block per mode, -1: missing
@@ -39,6 +40,7 @@ struct HetTables {
     {{1800.0f, 1800.0f, 2200.0f, 1800.0f, 2200.0f, 2200.0f, 2200.0f, 2200.0f, 1400.0f, 1400.0f, 2200.0f, 2200.0f, 2200.0f, 2200.0f, 2200.0f, 2200.0f, 2200.0f, 1000.0f, 1000.0f, 1000.0f, 1400.0f, 1400.0f, 1400.0f, 1400.0f, 1400.0f, 1400.0f, 1400.0f, 2600.0f, 2200.0f, 2200.0f, 1400.0f, 1400.0f, 1400.0f, 1400.0f, 1400.0f, 1400.0f, 1400.0f, 1400.0f, 1400.0f, 1400.0f, 1400.0f, 1400.0f, 1400.0f, 1400.0f, 1400.0f, 1400.0f, 1400.0f, 1400.0f, 1400.0f, 1400.0f, 1400.0f, 1400.0f, 1400.0f, 1400.0f}, \
      {96.0f, 62.0f, 35.5f, 18.0f, 23.0f, 24.3f, 39.1f, 40.1f, 220.0f, 220.0f, 12.0f, 55.8f, 200.0f, 27.0f, 28.1f, 47.9f, 54.9f, 18.0f, 18.0f, 19.0f, 132.0f, 133.0f, 168.2f, 273.0f, 206.0f, 248.0f, 177.0f, 100.0f, 100.0f, 23.75f, 231.0f, 168.0f, 300.0f, 200.0f, 186.0f, 184.0f, 170.0f, 168.0f, 66.4f, 218.0f, 230.0f, 241.0f, 253.0f, 266.0f, 136.0f, 136.0f, 135.0f, 135.0f, 134.0f, 170.0f, 198.0f, 179.0f, 169.0f, 158.0f}, \
      {{1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}, {1e-23f, 1e-23f, 1e-23f}}, \
+     {1.0610328804797065e-12, 1.0610328804797065e-12, 8.681178063733863e-13, 1.0610328804797065e-12, 8.681178063733863e-13, 8.681178063733863e-13, 8.681178063733863e-13, 8.681178063733863e-13, 1.3641851320453369e-12, 1.3641851320453369e-12, 8.681178063733863e-13, 8.681178063733863e-13, 8.681178063733863e-13, 8.681178063733863e-13, 8.681178063733863e-13, 8.681178063733863e-13, 8.681178063733863e-13, 1.909859206547515e-12, 1.909859206547515e-12, 1.909859206547515e-12, 1.3641851320453369e-12, 1.3641851320453369e-12, 1.3641851320453369e-12, 1.3641851320453369e-12, 1.3641851320453369e-12, 1.3641851320453369e-12, 1.3641851320453369e-12, 7.345612291174974e-13, 8.681178063733863e-13, 8.681178063733863e-13, 1.3641851320453369e-12, 1.3641851320453369e-12, 1.3641851320453369e-12, 1.3641851320453369e-12, 1.3641851320453369e-12, 1.3641851320453369e-12, 1.3641851320453369e-12, 1.3641851320453369e-12, 1.3641851320453369e-12, 1.3641851320453369e-12, 1.3641851320453369e-12, 1.3641851320453369e-12, 1.3641851320453369e-12, 1.3641851320453369e-12, 1.3641851320453369e-12, 1.3641851320453369e-12, 1.3641851320453369e-12, 1.3641851320453369e-12, 1.3641851320453369e-12, 1.3641851320453369e-12, 1.3641851320453369e-12, 1.3641851320453369e-12, 1.3641851320453369e-12, 1.3641851320453369e-12}, \
      {-2, -1, -1, 1, 1, 2, 1, 2, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0}, \
      {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0}, \
      {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0}, \

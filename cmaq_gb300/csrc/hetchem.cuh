@@ -76,29 +76,22 @@ HC_HD inline void het_extract(const HetTables& T, const float* ae, long long n, 
         m0[m] = fmaxf(ae[T.num_row[m] * n], CONMIN);
         m2[m] = fmaxf(ae[T.srf_row[m] * n] / PI, CONMIN);
     }
-    for (int m = 0; m < 3; ++m) {                                       // calcmoments( .true. )
+    // calcmoments( .true. ), then getpar( FIXED_sg = F ): both sum the mode's wet third
+    // moment over the same species in the same order (the species' factor REAL( 1.0E-9 *
+    // f6pi / density, 8 ) from the tables), so the sum is formed once
+    for (int m = 0; m < 3; ++m) {
         const float initial_m2 = m2[m];
         const float initial_m3 = fmaxf(m3[m], CONMIN);
         double wetsum = 0.0;
         for (int s = 0; s < NSPC; ++s) {
             if (T.tracer[s] || missing(T, s, m)) continue;
-            const double factor = (double)(1.0e-9f * F6PI / T.density[s]);
-            wetsum = wetsum + factor * (double)a.conc[s][m];
+            wetsum = wetsum + T.m3fac[s] * (double)a.conc[s][m];
         }
         m3[m] = fmaxf((float)wetsum, CONMIN);
         m2[m] = initial_m2 * powf((float)wetsum / initial_m3, (float)(2.0 / 3.0));
     }
-    const double minl2sg = (double)(logf(MIN_SIGMA_G) * logf(MIN_SIGMA_G));   // getpar( FIXED_sg = F )
+    const double minl2sg = (double)(logf(MIN_SIGMA_G) * logf(MIN_SIGMA_G));
     const double maxl2sg = (double)(logf(MAX_SIGMA_G) * logf(MAX_SIGMA_G));
-    for (int m = 0; m < 3; ++m) {
-        double sum_m3 = 0.0;
-        for (int s = 0; s < NSPC; ++s) {
-            if (T.tracer[s] || missing(T, s, m)) continue;
-            const double factor = (double)(1.0e-9f * F6PI / T.density[s]);
-            sum_m3 = sum_m3 + factor * (double)a.conc[s][m];
-        }
-        m3[m] = fmaxf((float)sum_m3, CONMIN);
-    }
     for (int m = 0; m < 3; ++m) {
         const double xfsum = (1.0 / 3.0) * log((double)m0[m]) + (2.0 / 3.0) * log((double)m3[m]);
         double l2sg = xfsum - log((double)m2[m]);

@@ -72,9 +72,13 @@ __device__ __forceinline__ long long take_cell(bool need, unsigned long long* ne
 // with a block barrier between phases (KMT2_LOCKSTEP), so that the block's warps run the
 // same generated routine at the same time and share its instruction-cache lines; finish
 // (cell, c, L, st) writes a finished cell.  The block leaves the loop when, after a
-// refill, none of its lanes holds a cell (the queue is empty).
+// refill, none of its lanes holds a cell (the queue is empty); a refill pass runs only
+// when KMT2_REFILL_MIN of the block's lanes are idle or none is busy.
 #ifndef KMT2_LOCKSTEP
 #define KMT2_LOCKSTEP 1
+#endif
+#ifndef KMT2_REFILL_MIN
+#define KMT2_REFILL_MIN 1
 #endif
 #if KMT2_LOCKSTEP
 #define KMT2_PHASE_BARRIER() __syncthreads()
@@ -91,7 +95,11 @@ __device__ __forceinline__ void kmt2_queue_loop(bool has_ws, double* ws, unsigne
     long long cell = -1;
     bool drained = !has_ws;
     for (;;) {
-        const bool need = cell < 0 && !drained;
+        // refill when KMT2_REFILL_MIN lanes of the block are idle (or none is busy), so that
+        // the set-up of new cells runs for several lanes at once
+        const int nidle = __syncthreads_count(cell < 0 && !drained);
+        const int nbusy = __syncthreads_count(cell >= 0);
+        const bool need = cell < 0 && !drained && (nidle >= KMT2_REFILL_MIN || nbusy == 0);
         const long long got = take_cell(need, next, ncell);
         if (need) {
             if (got < 0) {

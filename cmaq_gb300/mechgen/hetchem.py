@@ -191,6 +191,14 @@ def tables(cmaq: str | Path, mech: str = "cb6r5_ae7_aq") -> dict:
             "henry_iepox": list(henry(cmaq, "IEPOX"))}
 
 
+def _m3fac(density: float) -> float:
+    """REAL( 1.0E-9 * f6pi / density, 8 ) with f6pi = 6.0 / PI, each operation in float
+    as the reference's REAL arithmetic rounds it."""
+    import numpy as np
+    f6pi = np.float32(6.0) / np.float32(3.14159265)
+    return float(np.float32(np.float32(1.0e-9) * f6pi) / np.float32(density))
+
+
 def _c_float(v: float) -> str:
     return repr(float(v)) + "f"
 
@@ -224,6 +232,7 @@ def device_header(t: dict) -> str:
           f"{_c_float(t['henry_iepox'][1])};", ""]
     o.append("struct HetTables {")
     o += ["    float density[NSPC];", "    float molwt[NSPC];", "    float min_conc[NSPC][3];",
+          "    double m3fac[NSPC];   // REAL( 1.0E-9 * f6pi / density, 8 ), the factor of the moment sums",
           "    int charge[NSPC];", "    unsigned char tracer[NSPC], no_m2wet[NSPC], om[NSPC];",
           "    short row[NSPC][3];   // row in the aerosol block per mode, -1: missing",
           "    short num_row[3], srf_row[3];",
@@ -235,6 +244,7 @@ def device_header(t: dict) -> str:
     o.append("    {" + vec([s["density"] for s in sp], _c_float) + ", \\")
     o.append("     " + vec([s["molwt"] for s in sp], _c_float) + ", \\")
     o.append("     {" + ", ".join(vec(s["min_conc"], _c_float) for s in sp) + "}, \\")
+    o.append("     " + vec([_m3fac(s["density"]) for s in sp], _c_double) + ", \\")
     o.append("     " + vec([s["charge"] for s in sp], str) + ", \\")
     for key in ("tracer", "no_m2wet", "om"):
         o.append("     " + vec([int(s[key]) for s in sp], str) + ", \\")
