@@ -367,14 +367,23 @@ def run_e2e(g, steps: int, warmup: int, dist, device: int):
 
 def run_autotune(workload: str, seed: int, device: int) -> dict:
     """Launch-shape autotuning on a layer slice of the workload grid (same columns and
-    distributions, 4 layers), 2 timed CHEM calls per candidate."""
+    distributions, 4 layers), 2 timed CHEM calls per candidate, over the default library
+    (80 registers, 24 warps per SM) and the w16 build (128 registers, 16 warps), which is
+    built here if missing."""
+    from cmaq_gb300 import build as cbuild
     from cmaq_gb300.autotune import tune
     from cmaq_gb300.synthetic import make_grid
     dims = dict(WORKLOADS[workload])
     dims["nlays"] = min(4, dims["nlays"])
     g = make_grid(seed=seed, **dims)
     t0 = time.perf_counter()
-    res = tune(g, nsteps=2)
+    variants = ["default"]
+    try:
+        cbuild.build(variant="w16")
+        variants.append("w16")
+    except Exception as e:   # no nvcc: the default library alone
+        print(f"[bench] w16 build skipped: {e}", file=sys.stderr)
+    res = tune(g, nsteps=2, variants=variants)
     res["tuning_s"] = time.perf_counter() - t0
     res["sample"] = f"{g.ncols}x{g.nrows}x{g.nlays} ({g.ncell} cells)"
     return res
@@ -652,10 +661,13 @@ def run_hetchem(device: int, ncell: int, steps: int, threads: int) -> dict:
         want = het_oracle.rates(ae[:, :nsample], ta[:nsample], p[:nsample], q[:nsample], d[:nsample], threads=threads)
         wall = time.perf_counter() - t0
         got = out[:nsample].cpu().numpy()
-        rel = np.abs(got - want) / np.maximum(np.abs(want), 1e-300)
+        rel = np.where(got == want, 0.0, np.abs(got - want) / np.maximum(np.abs(want), 1e-300))
+        switch = [het_oracle.tables()["hetero"].index(x) for x in ("HETERO_IEPOX", "HETERO_IEPOXOS", "HETERO_TETROL")]
+        rest = np.delete(rel, switch, axis=1)
         res["cpu"] = {"value": nsample / wall, "cells": nsample, "wall_s": wall, "threads": threads}
-        res["parity"] = {"cells": nsample, "max_rel_diff": float(rel.max()),
-                         "same_zero_pattern": bool(((got == 0) == (want == 0)).all())}
+        res["parity"] = {"cells": nsample, "max_rel_diff_off_switch": float(rest.max()),
+                         "cells_on_the_iepox_switch": int((rel[:, switch] > 1e-5).any(axis=1).sum()),
+                         "note": "CALCISOPGAMMAS' q / TANH( q ) > 1 switch flips with an ulp of TANH for tiny q"}
     return res
 
 

@@ -53,9 +53,10 @@ VARIANTS = {"default": (GEN_DEFAULT, [Q_DEFAULT]),
             "kq2": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_MIN_BLOCKS=2"]),
             "kq3": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_MIN_BLOCKS=3"]),
             "kqfree": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_LOCKSTEP=0"]),
-            # KMT2 refill deferred until 8, 16 or 32 of a block's 128 lanes are idle
+            # KMT2 refill as soon as a lane is idle, or deferred until 8 or 32 of a block's 128
+            # lanes are (the default waits for 16)
+            "kqr1": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_REFILL_MIN=1"]),
             "kqr8": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_REFILL_MIN=8"]),
-            "kqr16": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_REFILL_MIN=16"]),
             "kqr32": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_REFILL_MIN=32"])}
 
 
@@ -109,6 +110,13 @@ def build(jobs: int | None = None, verbose: bool = False, variant: str = "defaul
         raise ValueError(f"unknown variant {variant}")
     out_dir = BUILD if variant == "default" else BUILD / variant
     out_dir.mkdir(parents=True, exist_ok=True)
+    import fcntl
+    with open(out_dir / ".lock", "w") as lock:      # one builder at a time (ranks of a torchrun job)
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        return _build_locked(out_dir, variant, jobs, verbose)
+
+
+def _build_locked(out_dir: Path, variant: str, jobs: int | None, verbose: bool) -> Path:
     lib = lib_path(variant)
     gen_extra, all_extra = (list(x) for x in VARIANTS[variant])
     nvcc = _nvcc()

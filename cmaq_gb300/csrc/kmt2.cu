@@ -78,7 +78,7 @@ __device__ __forceinline__ long long take_cell(bool need, unsigned long long* ne
 #define KMT2_LOCKSTEP 1
 #endif
 #ifndef KMT2_REFILL_MIN
-#define KMT2_REFILL_MIN 1
+#define KMT2_REFILL_MIN 16
 #endif
 #if KMT2_LOCKSTEP
 #define KMT2_PHASE_BARRIER() __syncthreads()

@@ -45,6 +45,8 @@ def load() -> C.CDLL:
     lib.oracle_het_pncom_loss.restype = C.c_double
     lib.oracle_het_moments.argtypes = [fp, C.c_longlong, dp, dp, dp]
     lib.oracle_het_moments.restype = None
+    lib.oracle_het_isop_q.argtypes = [fp, C.c_longlong, C.c_double]
+    lib.oracle_het_isop_q.restype = C.c_double
     return lib
 
 
@@ -74,6 +76,8 @@ def cell_piece(name: str, ae_col, *args):
         return L.oracle_het_n2o5_gamma(p, 1, *args)
     if name == "crystalized":
         return bool(L.oracle_het_crystalized(p, 1, *args))
+    if name == "isop_q":
+        return L.oracle_het_isop_q(p, 1, *args)
     if name == "moments":
         m2, m3, de = (np.zeros(3) for _ in range(3))
         dp = C.POINTER(C.c_double)

@@ -274,9 +274,17 @@ static double pncom_loss(float poc, float pncom)
     return 0.0;
 }
 
-/* CALCISOPGAMMAS for the IEPOX parent (NUMVOC = 1 for this mechanism's pair table) */
+/* CALCISOPGAMMAS for the IEPOX parent (NUMVOC = 1 for this mechanism's pair table); *q_out
+ * (if given) receives the diffuso-reactive parameter q */
+static void calcisopgammas_q(const HoState* s, double radius, double temperature, double cfactor_iepox,
+                             double* gammaiepox, double* kpiepox, double* ftet, double* fos, double* q_out);
 static void calcisopgammas(const HoState* s, double radius, double temperature, double cfactor_iepox,
                            double* gammaiepox, double* kpiepox, double* ftet, double* fos)
+{
+    calcisopgammas_q(s, radius, temperature, cfactor_iepox, gammaiepox, kpiepox, ftet, fos, NULL);
+}
+static void calcisopgammas_q(const HoState* s, double radius, double temperature, double cfactor_iepox,
+                             double* gammaiepox, double* kpiepox, double* ftet, double* fos, double* q_out)
 {
     const double inv_alpha = 1.0 / 0.02, diffusivity = 1.0e-9, RgasLatmmolK = 0.08206;
     double acidmolconc[2];
@@ -313,6 +321,7 @@ static void calcisopgammas(const HoState* s, double radius, double temperature, 
     const float tfac = (298.0f - temp) / (298.0f * temp);   /* HLCONST, EFFECTIVE = .FALSE. */
     const double heff = (double)(ho_hl_iepox_a * expf(ho_hl_iepox_e * tfac));
     const double q = radius * sqrt(kparticle / diffusivity);
+    if (q_out) *q_out = q;
     if (q / tanh(q) > 1.0) {
         const double nu = cfactor_iepox * sqrt(temperature);
         const double denom = (inv_alpha + nu * radius
@@ -502,4 +511,15 @@ void oracle_het_moments(const float* conc, long long stride, double* wet_m2, dou
         wet_m3[n] = s.wet_m3[n];
         de_wet[n] = s.de_wet[n];
     }
+}
+/* CALCISOPGAMMAS' diffuso-reactive parameter q of one cell (its switch q / TANH( q ) > 1
+ * decides whether the epoxide uptake is on) */
+double oracle_het_isop_q(const float* conc, long long stride, double temp)
+{
+    HoState s;
+    hetchem_extract_aero(&s, conc, stride);
+    double g, kp, ft, fo, q = 0.0;
+    calcisopgammas_q(&s, 0.5 * s.de_wet[1], temp, sqrt(8.0e3 * (double)RGASUNIV_F / (ho_mw_iepox * DPI_D)), &g,
+                     &kp, &ft, &fo, &q);
+    return q;
 }

@@ -6,9 +6,13 @@ The device code performs the oracle's IEEE operations in the same order (built w
 -fmad=false), but its exp, log, pow, tanh and log10 (float and double) are CUDA's, which
 differ from the host library's by an ulp or two.  The outputs are smooth functions of
 those values with no step-size amplification, so the bar is a relative difference of
-1e-5 per KHETERO entry (float intermediates carry 6e-8 per ulp) and the same zero
-pattern; tests/test_hetchem_host.py holds the same code, built for the host, to the
-oracle bit for bit.
+1e-5 per KHETERO entry (float intermediates carry 6e-8 per ulp) — except at one switch of
+the reference itself: CALCISOPGAMMAS turns the epoxide uptake on where q / TANH( q ) >
+1.0 (AEROSOL_CHEMISTRY.F:2517), which in floating point is 1.0 for q below about 2e-8,
+so for tiny q an ulp of TANH decides whether IEPOX, IEPOXOS and TETROL are zero or not.
+Cells that differ only there, with the oracle's q below 1e-6, are counted and allowed;
+every other entry must meet the bar.  tests/test_hetchem_host.py holds the same code,
+built for the host, to the oracle bit for bit.
 """
 import numpy as np
 import pytest
@@ -43,9 +47,16 @@ def test_device_rates_match_the_oracle(n, seed):
     got = got.cpu().numpy()
     want = h.rates(ae, ta, p, q, d, threads=8)
     assert np.isfinite(got).all()
-    assert ((got == 0) == (want == 0)).all()
-    rel = np.abs(got - want) / np.maximum(np.abs(want), 1e-300)
-    assert rel.max() <= RTOL, (rel.max(), np.unravel_index(rel.argmax(), rel.shape))
+    t = h.tables()
+    switch = [t["hetero"].index(x) for x in ("HETERO_IEPOX", "HETERO_IEPOXOS", "HETERO_TETROL")]
+    rel = np.where(got == want, 0.0, np.abs(got - want) / np.maximum(np.abs(want), 1e-300))
+    bad = rel > RTOL
+    others = np.delete(bad, switch, axis=1)
+    assert not others.any(), [(int(c), t["hetero"][j], got[c, j], want[c, j]) for c, j in np.argwhere(bad)[:8]]
+    flips = np.nonzero(bad.any(axis=1))[0]
+    qs = np.array([h.cell_piece("isop_q", ae[:, c], float(ta[c])) for c in flips])
+    assert (qs < 1e-6).all(), list(zip(flips[qs >= 1e-6][:5], qs[qs >= 1e-6][:5]))
+    print(f"{len(flips)} of {n} cells on the q / TANH( q ) switch")
 
 
 def test_cgrid_view_and_host_entry_give_the_same_bits():
