@@ -23,11 +23,11 @@ Arms and extras
   ``adjoint``; EBI on the workload grid -> ``ebi``; SMVGEAR against ROS3 on 100x100x10
   cells -> ``gear``; the accuracy block (GPU hour against the oracle's tight solution
   on a sample of cells) -> ``accuracy``; the KMT2 aqueous kinetics on 200,000 cloudy
-  cells -> ``aqchem``; HETCHEM_RATES on the workload grid -> ``hetchem``.  With
-  --all-configs also the CONUS grid with skewed stiffness (30 % plume columns), batched
-  against plain -> ``skewed``, and CRACMM2 on 200x200x25 cells, batched hour and
-  adjoint window -> ``cracmm2``; with --tight-steps N the tight-tolerance timing leg
-  -> ``tight``.
+  cells -> ``aqchem``; HETCHEM_RATES on the workload grid -> ``hetchem``; the CONUS grid
+  with skewed stiffness (30 % plume columns), batched against plain -> ``skewed``;
+  CRACMM2 on 200x200x25 cells, batched hour and adjoint window -> ``cracmm2``; the
+  tight-tolerance timing leg (rtol 3e-7 on every 7th layer, --tight-steps calls) ->
+  ``tight``.  The whole default run takes about half an hour.
 * --impl reference: the reference algorithm (C oracle; the Fortran cannot be
   compiled here) on all host cores, bounded sample per step.
 * --only-hetchem: HETCHEM_RATES alone (cmaqchem_hetchem_rates_device) on the workload
@@ -820,16 +820,17 @@ def main():
     ap.add_argument("--no-gear", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="only the headline arms (batched, plain, e2e, CPU baseline)")
-    ap.add_argument("--all-configs", action="store_true",
-                    help="also the skewed-stiffness CONUS grid and CRACMM2 on 1M cells (about 5 minutes)")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the skewed-stiffness CONUS grid and CRACMM2 on 1M cells (about 5 minutes)")
+    ap.add_argument("--all-configs", action="store_true", help="accepted for compatibility: the configs run by default")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the accuracy block and the tight-tolerance leg")
     ap.add_argument("--no-aqchem", action="store_true", help="skip the KMT2 aqueous kinetics leg")
     ap.add_argument("--no-hetchem", action="store_true", help="skip the HETCHEM_RATES leg")
     ap.add_argument("--only-hetchem", action="store_true",
                     help="only the HETCHEM_RATES kernel on the workload grid's cells, its own JSON line")
-    ap.add_argument("--tight-steps", type=int, default=0,
+    ap.add_argument("--tight-steps", type=int, default=2,
                     help="CHEM calls of the tight-tolerance leg on every 7th layer of the workload grid "
-                         "(0: skip; 2 takes about 14 minutes)")
+                         "(0: skip; 2 take about 14 minutes)")
     ap.add_argument("--adjoint-dims", default="100x100x35", help="grid of the adjoint window, NCOLSxNROWSxNLAYS")
     ap.add_argument("--only-adjoint", action="store_true",
                     help="time only the adjoint window and print its own line (for profiling)")
@@ -996,8 +997,8 @@ def main():
     ebi = leg("ebi", extras and not a.no_ebi, lambda: run_ebi(device, STEPS_PER_HOUR, g))
     adjoint = leg("adjoint", extras and not a.no_adjoint, lambda: run_adjoint(device, STEPS_PER_HOUR, adims))
     gear = leg("gear", extras and not a.no_gear, lambda: run_gear(device, a.steps))
-    skewed = leg("skewed", extras and a.all_configs, lambda: run_skewed(device, STEPS_PER_HOUR, tuned))
-    cracmm2 = leg("cracmm2", extras and a.all_configs, lambda: run_cracmm2(device, STEPS_PER_HOUR))
+    skewed = leg("skewed", extras and not a.no_configs, lambda: run_skewed(device, STEPS_PER_HOUR, tuned))
+    cracmm2 = leg("cracmm2", extras and not a.no_configs, lambda: run_cracmm2(device, STEPS_PER_HOUR))
     hetchem = leg("hetchem", extras and not a.no_hetchem,
                   lambda: run_hetchem(device, g.ncell, 5, 0 if a.no_cpu else host_threads()))
     aqchem = leg("aqchem", extras and not a.no_aqchem,
