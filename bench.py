@@ -69,6 +69,7 @@ WORKLOADS = {
     "conus": dict(ncols=459, nrows=299, nlays=35),
     "conus_skewed": dict(ncols=459, nrows=299, nlays=35, plume_fraction=0.3),
     "small": dict(ncols=100, nrows=100, nlays=10),
+    "conus4": dict(ncols=459, nrows=299, nlays=4),   # a 4-layer slice of the CONUS grid (profiling)
     "cpu4k": dict(ncols=20, nrows=20, nlays=10),
 }
 

@@ -73,7 +73,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-rdc=true", "-fmad=false", "-lineinfo", "-Xc
 # The default library's exceptions, measured slower at the 80-register cap: the adjoint's
 # own generated routines (called only by the adjoint kernels, launch-bounded for 16 warps
 # per SM) and everything of CRACMM2 (twice CB6r5's species: its queue kernel runs 16
-# warps per SM with its routines at 128 registers; 58,989 against 51,080 grid-cells/s).
+# warps per SM with its routines at 128 registers; 56,097 against 51,080 grid-cells/s).
 def _flags(src: Path, variant: str, gen_extra: list, all_extra: list) -> list:
     if variant == "default":
         if src.name.startswith("cracmm2_") or src.name == "mech_cracmm2.cu":

@@ -6,13 +6,15 @@ The device code performs the oracle's IEEE operations in the same order (built w
 -fmad=false), but its exp, log, pow, tanh and log10 (float and double) are CUDA's, which
 differ from the host library's by an ulp or two.  The outputs are smooth functions of
 those values with no step-size amplification, so the bar is a relative difference of
-1e-5 per KHETERO entry (float intermediates carry 6e-8 per ulp) — except at one switch of
-the reference itself: CALCISOPGAMMAS turns the epoxide uptake on where q / TANH( q ) >
-1.0 (AEROSOL_CHEMISTRY.F:2517), which in floating point is 1.0 for q below about 2e-8,
-so for tiny q an ulp of TANH decides whether IEPOX, IEPOXOS and TETROL are zero or not.
-Cells that differ only there, with the oracle's q below 1e-6, are counted and allowed;
-every other entry must meet the bar.  tests/test_hetchem_host.py holds the same code,
-built for the host, to the oracle bit for bit.
+1e-5 per KHETERO entry (float intermediates carry 6e-8 per ulp) — except where the
+reference's own arithmetic is ill-conditioned: CALCISOPGAMMAS forms the IEPOX uptake
+coefficient from q / TANH( q ) - 1 (AEROSOL_CHEMISTRY.F:2517-2526), about q^2 / 3, a
+difference of two numbers next to 1, so an ulp of TANH moves IEPOX, IEPOXOS and TETROL
+by up to 2^-52 / (q^2 / 3) relative, and for q below about 2e-7 decides whether they
+are zero at all (the switch q / TANH( q ) > 1).  Those three labels are held to that
+bound with the oracle's q of each cell; every other entry must meet 1e-5.
+tests/test_hetchem_host.py holds the same code, built for the host, to the oracle bit
+for bit.
 """
 import numpy as np
 import pytest
@@ -51,12 +53,19 @@ def test_device_rates_match_the_oracle(n, seed):
     switch = [t["hetero"].index(x) for x in ("HETERO_IEPOX", "HETERO_IEPOXOS", "HETERO_TETROL")]
     rel = np.where(got == want, 0.0, np.abs(got - want) / np.maximum(np.abs(want), 1e-300))
     bad = rel > RTOL
-    others = np.delete(bad, switch, axis=1)
-    assert not others.any(), [(int(c), t["hetero"][j], got[c, j], want[c, j]) for c, j in np.argwhere(bad)[:8]]
-    flips = np.nonzero(bad.any(axis=1))[0]
-    qs = np.array([h.cell_piece("isop_q", ae[:, c], float(ta[c])) for c in flips])
-    assert (qs < 1e-6).all(), list(zip(flips[qs >= 1e-6][:5], qs[qs >= 1e-6][:5]))
-    print(f"{len(flips)} of {n} cells on the q / TANH( q ) switch")
+    bad[:, switch] = False
+    assert not bad.any(), [(int(c), t["hetero"][j], got[c, j], want[c, j]) for c, j in np.argwhere(bad)[:8]]
+    qs = np.array([h.cell_piece("isop_q", ae[:, c], float(ta[c])) for c in range(n)])
+    cond = np.maximum(qs * qs / 3.0, 1e-300)            # q / tanh(q) - 1
+    eps = 2.0 ** -52
+    allowed = RTOL + 16.0 * eps / cond
+    flip = (got[:, switch] == 0) != (want[:, switch] == 0)
+    assert (~flip.any(axis=1) | (cond < 64.0 * eps)).all(), qs[flip.any(axis=1)][:5]
+    rs = np.where(flip, 0.0, rel[:, switch])
+    worst = (rs / allowed[:, None]).max()
+    assert worst <= 1.0, worst
+    print(f"{int(flip.any(axis=1).sum())} of {n} cells on the q / TANH( q ) switch; "
+          f"IEPOX-family error at most {worst:.2f} of its conditioning bound")
 
 
 def test_cgrid_view_and_host_entry_give_the_same_bits():
