@@ -10,6 +10,9 @@ is exchanged, so the split changes no per-cell result.
   remainders going to the leading subdomains.
 * :func:`balanced_ranges` -- contiguous cell ranges of near-equal cost from per-cell
   costs (e.g. the previous call's step attempts), for uneven stiffness.
+* :func:`reduce_shard_gradient` -- the one exchange of a sharded run: the gradient of a
+  parameter every rank shares (the adjoint window's per-reaction log rate multipliers, or
+  a scalar loss) summed over the ranks.
 """
 from __future__ import annotations
 
@@ -62,3 +65,21 @@ def sub_grid(g, cols: slice, rows: slice):
                    ocean_szone=np.ascontiguousarray(g.ocean_szone[rows, cols]),
                    rj=np.ascontiguousarray(g.rj[:, :, rows, cols]),
                    khetero=np.ascontiguousarray(g.khetero[:, rows, cols, :]))
+
+
+def reduce_shard_gradient(grad, group=None):
+    """Sum, over the ranks of ``group``, of a gradient that every rank computed for its own
+    cells; in place, and returned.  A parameter shared by all cells (``log_k`` of the
+    adjoint window) gets one contribution per cell, so the whole domain's gradient is the
+    sum of the subdomains'.  One all-reduce of the flat tensor (349 doubles for CB6r5's
+    log-k, 531 for CRACMM2's) on the tensor's device: NCCL for GPU tensors, gloo for CPU
+    ones.  Without an initialised process group, or with one rank, it returns ``grad``."""
+    import torch.distributed as dist
+    if grad is None or not dist.is_available() or not dist.is_initialized():
+        return grad
+    if dist.get_world_size(group) == 1:
+        return grad
+    if not grad.is_contiguous():
+        raise ValueError("reduce_shard_gradient: the gradient must be contiguous")
+    dist.all_reduce(grad, op=dist.ReduceOp.SUM, group=group)
+    return grad
