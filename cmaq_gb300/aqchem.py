@@ -180,6 +180,6 @@ if __name__ == "__main__":
     ap.add_argument("--reps", type=int, default=2)
     a = ap.parse_args()
     specs = a.specs.split(",")
-    for v in dict.fromkeys(sp.split(":")[0] for sp in specs):
+    for v in dict.fromkeys(["default"] + [sp.split(":")[0] for sp in specs]):   # variants share its objects
         cbuild.build(variant=v)
     sweep(a.cells, specs, a.reps)

@@ -57,7 +57,12 @@ VARIANTS = {"default": (GEN_DEFAULT, [Q_DEFAULT]),
             # lanes are (the default waits for 16)
             "kqr1": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_REFILL_MIN=1"]),
             "kqr8": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_REFILL_MIN=8"]),
-            "kqr32": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_REFILL_MIN=32"])}
+            "kqr32": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_REFILL_MIN=32"]),
+            # KMT2 staging passes when 16 or 32 of a block's 128 staging slots are empty (the
+            # default waits for 64), or only when lanes wait for a cell (129: never by count)
+            "kqs16": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_STAGE_MIN=16"]),
+            "kqs32": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_STAGE_MIN=32"]),
+            "kqsoff": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_STAGE_MIN=129"])}
 
 
 def _is_generated_math(src: Path) -> bool:
@@ -74,8 +79,13 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-rdc=true", "-fmad=false", "-lineinfo", "-Xc
 # own generated routines (called only by the adjoint kernels, launch-bounded for 16 warps
 # per SM) and everything of CRACMM2 (twice CB6r5's species: its queue kernel runs 16
 # warps per SM with its routines at 128 registers; 56,097 against 51,080 grid-cells/s).
+# The KMT2 kernels' own switches (-DKMT2_*) reach kmt2.cu only, so that a KMT2 variant
+# shares every other object with the default build.
 def _flags(src: Path, variant: str, gen_extra: list, all_extra: list) -> list:
-    if variant == "default":
+    own = [f for f in all_extra if not f.startswith("-DKMT2_")]
+    if src.name != "kmt2.cu":
+        all_extra = own
+    if variant == "default" or (gen_extra == GEN_DEFAULT and own == [Q_DEFAULT]):
         if src.name.startswith("cracmm2_") or src.name == "mech_cracmm2.cu":
             return [Q16] + (GEN128 if _is_generated_math(src) else [])
         if _is_generated_math(src) and "_adj" in src.name:
@@ -116,8 +126,15 @@ def build(jobs: int | None = None, verbose: bool = False, variant: str = "defaul
         return _build_locked(out_dir, variant, jobs, verbose)
 
 
+def _fresh(obj: Path, src_mtime: float, flags: str) -> bool:
+    """obj is newer than its sources and was built with flags."""
+    stamp = obj.with_suffix(".flags")
+    return obj.exists() and obj.stat().st_mtime > src_mtime and stamp.exists() and stamp.read_text() == flags
+
+
 def _build_locked(out_dir: Path, variant: str, jobs: int | None, verbose: bool) -> Path:
     lib = lib_path(variant)
+    todo_link = False
     gen_extra, all_extra = (list(x) for x in VARIANTS[variant])
     nvcc = _nvcc()
     hdr_mtime = max(p.stat().st_mtime for p in _headers())
@@ -128,8 +145,13 @@ def _build_locked(out_dir: Path, variant: str, jobs: int | None, verbose: bool) 
         objs.append(obj)
         stamp = obj.with_suffix(".flags")   # the flags the object was built with
         flags = " ".join(_flags(src, variant, gen_extra, all_extra))
-        if (obj.exists() and obj.stat().st_mtime > max(src.stat().st_mtime, hdr_mtime) and stamp.exists()
-                and stamp.read_text() == flags):
+        if _fresh(obj, max(src.stat().st_mtime, hdr_mtime), flags):
+            continue
+        shared = BUILD / obj.name   # the default build's object, when its flags are the same
+        if out_dir != BUILD and _fresh(shared, max(src.stat().st_mtime, hdr_mtime), flags):
+            shutil.copy2(shared, obj)
+            stamp.write_text(flags)
+            todo_link = True
             continue
         todo.append((src, obj))
 
@@ -148,7 +170,7 @@ def _build_locked(out_dir: Path, variant: str, jobs: int | None, verbose: bool) 
     if todo:
         with ThreadPoolExecutor(max_workers=jobs or os.cpu_count() or 4) as ex:
             list(ex.map(compile_one, todo))
-    if todo or not lib.exists():
+    if todo or todo_link or not lib.exists():
         cmd = [nvcc, *ARCH, "-shared", "-rdc=true", *[str(o) for o in objs], "-o", str(lib) + ".tmp"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
