@@ -57,12 +57,7 @@ VARIANTS = {"default": (GEN_DEFAULT, [Q_DEFAULT]),
             # lanes are (the default waits for 16)
             "kqr1": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_REFILL_MIN=1"]),
             "kqr8": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_REFILL_MIN=8"]),
-            "kqr32": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_REFILL_MIN=32"]),
-            # KMT2 staging passes when 16 or 32 of a block's 128 staging slots are empty (the
-            # default waits for 64), or only when lanes wait for a cell (129: never by count)
-            "kqs16": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_STAGE_MIN=16"]),
-            "kqs32": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_STAGE_MIN=32"]),
-            "kqsoff": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_STAGE_MIN=129"])}
+            "kqr32": (GEN_DEFAULT, [Q_DEFAULT, "-DKMT2_REFILL_MIN=32"])}
 
 
 def _is_generated_math(src: Path) -> bool:
@@ -105,7 +100,7 @@ def sources() -> list[Path]:
 
 
 def _headers() -> list[Path]:
-    return (sorted(CSRC.glob("*.cuh")) + sorted((CSRC / "gen").glob("*.cuh"))
+    return (sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + sorted((CSRC / "gen").glob("*.cuh"))
             + sorted((PKG.parent / "include").glob("*.h")))
 
 

@@ -9,7 +9,7 @@ def _flags(name, variant):
 
 
 def test_kmt2_switches_reach_kmt2_only():
-    for v in ("kq3", "kqfree", "kqr8", "kqs32", "kqsoff"):
+    for v in ("kq2", "kq3", "kqfree", "kqr1", "kqr8", "kqr32"):
         assert any(f.startswith("-DKMT2_") for f in _flags("kmt2.cu", v))
         for name in ("chem_capi.cu", "gen/cb6r5_ae7_aq_rates.cu", "gen/cracmm2_rates.cu", "hetchem.cu"):
             assert _flags(name, v) == _flags(name, "default"), (v, name)
