@@ -23,7 +23,8 @@ Arms and extras
   ``adjoint``; EBI on the workload grid -> ``ebi``; SMVGEAR against ROS3 on 100x100x10
   cells -> ``gear``; the accuracy block (GPU hour against the oracle's tight solution
   on a sample of cells) -> ``accuracy``; the KMT2 aqueous kinetics on 200,000 cloudy
-  cells -> ``aqchem``; HETCHEM_RATES on the workload grid -> ``hetchem``; the CONUS grid
+  cells -> ``aqchem``; HETCHEM_RATES on the workload grid -> ``hetchem`` (CRACMM2's on
+  1,000,000 cells -> ``hetchem.cracmm2``); the CONUS grid
   with skewed stiffness (30 % plume columns), batched against plain -> ``skewed``;
   CRACMM2 on 200x200x25 cells, batched hour and adjoint window -> ``cracmm2``; the
   tight-tolerance timing leg (rtol 3e-7 on every 7th layer, --tight-steps calls) ->
@@ -606,9 +607,10 @@ def run_aqchem_whole(dev, ncell: int, steps: int) -> dict:
             "max_abs_mass_balance_percent": float(np.abs(wo[6:10]).max())}
 
 
-def run_hetchem(device: int, ncell: int, steps: int, threads: int) -> dict:
-    """HETCHEM_RATES (cmaqchem_hetchem_rates_device): KHETERO of ncell seeded cells from
-    their CGRID aerosol block and met fields (cmaq_gb300/synthetic.py: make_aerosol_cells).
+def run_hetchem(device: int, ncell: int, steps: int, threads: int, mech: str = "cb6r5_ae7_aq") -> dict:
+    """HETCHEM_RATES (cmaqchem_hetchem_rates_device) of mechanism ``mech``: KHETERO of ncell
+    seeded cells from their CGRID aerosol block and met fields (cmaq_gb300/synthetic.py:
+    make_aerosol_cells).
     Device time by CUDA events around each call (inputs resident); end to end with the
     aerosol block and met copied from pinned host memory and KHETERO copied back; the HBM
     roofline of the call's algorithmic bytes (the block and met read once, KHETERO written
@@ -616,21 +618,21 @@ def run_hetchem(device: int, ncell: int, steps: int, threads: int) -> dict:
     import torch
     from cmaq_gb300.hetchem import hetchem_rates, layout
     from cmaq_gb300.synthetic import make_aerosol_cells
-    nae, _, nhet = layout()
-    ae, ta, p, q, d = make_aerosol_cells(ncell, seed=2018)
+    nae, _, nhet = layout(mech)
+    ae, ta, p, q, d = make_aerosol_cells(ncell, seed=2018, mech=mech)
     dev = torch.device(f"cuda:{device}")
     host = [torch.from_numpy(x).pin_memory() for x in (ae, ta, p, q, d)]
     dv = [x.to(dev) for x in host]
-    out = hetchem_rates(*dv)
+    out = hetchem_rates(*dv, mechanism=mech)
     hout = torch.empty((ncell, nhet), dtype=torch.float64).pin_memory()
     for _ in range(2):
-        hetchem_rates(*dv, out=out)
+        hetchem_rates(*dv, mechanism=mech, out=out)
     torch.cuda.synchronize(dev)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
     ms = []
     for _ in range(steps):
         ev[0].record()
-        hetchem_rates(*dv, out=out)
+        hetchem_rates(*dv, mechanism=mech, out=out)
         ev[1].record()
         torch.cuda.synchronize(dev)
         ms.append(ev[0].elapsed_time(ev[1]))
@@ -639,14 +641,14 @@ def run_hetchem(device: int, ncell: int, steps: int, threads: int) -> dict:
     for _ in range(steps):
         for hx, dx in zip(host, dv):
             dx.copy_(hx, non_blocking=True)
-        hetchem_rates(*dv, out=out)
+        hetchem_rates(*dv, mechanism=mech, out=out)
         hout.copy_(out, non_blocking=True)
         torch.cuda.synchronize(dev)
     e2e_s = (time.perf_counter() - t0) / steps
     nbytes = ncell * (nae * 4 + 16 + nhet * 8)
     peak = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"] if (ROOT / "MEASURED_PEAKS.json").exists() else None
     achieved = nbytes / (dev_ms * 1e-3) / 1e9
-    res = {"ncell": ncell, "ms_per_call": dev_ms, "value": ncell / (dev_ms * 1e-3),
+    res = {"mechanism": mech, "ncell": ncell, "ms_per_call": dev_ms, "value": ncell / (dev_ms * 1e-3),
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": None if not peak else achieved / peak, "traffic": None,
                         "bytes_per_cell": nae * 4 + 16 + nhet * 8,
@@ -659,11 +661,13 @@ def run_hetchem(device: int, ncell: int, steps: int, threads: int) -> dict:
         import hetchem as het_oracle
         nsample = min(ncell, 20000 * threads)
         t0 = time.perf_counter()
-        want = het_oracle.rates(ae[:, :nsample], ta[:nsample], p[:nsample], q[:nsample], d[:nsample], threads=threads)
+        want = het_oracle.rates(ae[:, :nsample], ta[:nsample], p[:nsample], q[:nsample], d[:nsample], threads=threads,
+                                mech=mech)
         wall = time.perf_counter() - t0
         got = out[:nsample].cpu().numpy()
         rel = np.where(got == want, 0.0, np.abs(got - want) / np.maximum(np.abs(want), 1e-300))
-        switch = [het_oracle.tables()["hetero"].index(x) for x in ("HETERO_IEPOX", "HETERO_IEPOXOS", "HETERO_TETROL")]
+        switch = [j for j, x in enumerate(het_oracle.tables(mech)["hetero"])
+                  if x in ("HETERO_IEPOX", "HETERO_IEPOXOS", "HETERO_TETROL", "HETERO_ISO3NOSJ", "HETERO_ISO3OSJ")]
         rest = np.delete(rel, switch, axis=1)
         res["cpu"] = {"value": nsample / wall, "cells": nsample, "wall_s": wall, "threads": threads}
         res["parity"] = {"cells": nsample, "max_rel_diff_off_switch": float(rest.max()),
@@ -719,7 +723,7 @@ def run_aqchem(device: int, ncell: int, steps: int, warmup: int, threads: int, w
     res_whole = None
     if whole:
         res_whole = run_aqchem_whole(dev, ncell, steps)
-    res = {"ncell": ncell, "ms_per_call": dev_ms, "value": ncell / (dev_ms * 1e-3), "whole_aqchem": res_whole,
+    res = {"mechanism": mech, "ncell": ncell, "ms_per_call": dev_ms, "value": ncell / (dev_ms * 1e-3), "whole_aqchem": res_whole,
            "achieved_tflops": flops / (dev_ms * 1e-3) / 1e12, "flops_per_call": flops,
            "steps_per_cell": float(sd[1].mean()), "max_steps_per_cell": int(sd[1].max()),
            "failed_cells": int((sd[8] != 1).sum()),
@@ -1000,8 +1004,12 @@ def main():
     gear = leg("gear", extras and not a.no_gear, lambda: run_gear(device, a.steps))
     skewed = leg("skewed", extras and not a.no_configs, lambda: run_skewed(device, STEPS_PER_HOUR, tuned))
     cracmm2 = leg("cracmm2", extras and not a.no_configs, lambda: run_cracmm2(device, STEPS_PER_HOUR))
-    hetchem = leg("hetchem", extras and not a.no_hetchem,
-                  lambda: run_hetchem(device, g.ncell, 5, 0 if a.no_cpu else host_threads()))
+    def hetchem_both():
+        r = run_hetchem(device, g.ncell, 5, 0 if a.no_cpu else host_threads())
+        if not a.no_configs:                          # CRACMM2's tables on its 200x200x25 grid
+            r["cracmm2"] = run_hetchem(device, 1000000, 5, 0 if a.no_cpu else min(4, host_threads()), "cracmm2")
+        return r
+    hetchem = leg("hetchem", extras and not a.no_hetchem, hetchem_both)
     aqchem = leg("aqchem", extras and not a.no_aqchem,
                  lambda: run_aqchem(device, a.aqchem_cells, 3, 3, 0 if a.no_cpu else host_threads()))
     if aqchem is not None:

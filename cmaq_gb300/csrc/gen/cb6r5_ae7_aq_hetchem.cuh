@@ -1,5 +1,5 @@
 // Generated by cmaq_gb300/mechgen/hetchem.py from CCTM/src/aero/aero6 (AERO_DATA.F, AEROSOL_CHEMISTRY.F) and MECHS/cb6r5_ae7_aq.
-// Included inside namespace het by csrc/hetchem.cuh.  Do not edit.
+// Included inside the mechanism's namespace by csrc/hetchem.cuh.  Do not edit.
 #pragma once
 
 constexpr int NAE = 84;      // CGRID rows of the aerosol block
@@ -17,7 +17,7 @@ constexpr int I_AH3OP = 19;
 constexpr int I_APOC = 8;
 constexpr int I_APNCOM = 9;
 
-enum HetKind { K_N2O5IJ = 0, K_N2O5K = 1, K_H2NO3PAIJ = 2, K_H2NO3PBIJ = 3, K_H2NO3PAK = 4, K_H2NO3PBK = 5, K_NO2 = 6, K_IEPOX = 7, K_IEPOXOS = 8, K_TETROL = 9, K_GLY = 10, K_MGLY = 11, K_NTR2 = 12, K_CLNO3_WAI = 13, K_CLNO3_WAJ = 14, K_PNCOMLI = 15, K_PNCOMLJ = 16, K_NO3 = 17, K_HO2 = 18, K_N2O5I = 19, K_N2O5J = 20 };
+enum HetKind { K_N2O5IJ = 0, K_N2O5K = 1, K_H2NO3PAIJ = 2, K_H2NO3PBIJ = 3, K_H2NO3PAK = 4, K_H2NO3PBK = 5, K_NO2 = 6, K_IEPOX = 7, K_IEPOXOS = 8, K_TETROL = 9, K_GLY = 10, K_MGLY = 11, K_NTR2 = 12, K_CLNO3_WAI = 13, K_CLNO3_WAJ = 14, K_PNCOMLI = 15, K_PNCOMLJ = 16, K_NO3 = 17, K_HO2 = 18, K_N2O5I = 19, K_N2O5J = 20, K_ISO3NOSJ = 21, K_ISO3OSJ = 22 };
 
 constexpr double MW_IEPOX = 118.1, MW_NO3 = 62.0, MW_GLY = 58.0, MW_MGLY = 72.0, MW_HO2 = 33.0;
 constexpr float HL_IEPOX_A = 30000000.0f, HL_IEPOX_E = 0.0f;

@@ -1,12 +1,12 @@
 // C ABI of the heterogeneous rate constants (include/cmaqchem.h: cmaqchem_hetchem_*):
 // HETCHEM_RATES (CCTM/src/aero/aero6/AEROSOL_CHEMISTRY.F:282-1535) for every cell of a
-// grid, one cell per thread (hetchem.cuh).
+// grid, one cell per thread (hetchem.cuh), for the mechanisms of hetchem_table.h.
 //
 // The reference calls HETCHEM_RATES from the chemistry driver once per synchronisation
 // step before CHEM (rbdriver.F:409); KHETERO then feeds CALC_RCONST.  Here the kernel
 // reads the aerosol block of the caller's CGRID (CONC(:,:,:,AE_STRT:), REAL) and the met
 // fields in place and writes KHETERO(NHETERO, NCOLS, NROWS, NLAYS) (REAL(8)), the layout
-// the CHEM entries take.  Each thread holds its cell's aerosol state (54 species x 3
+// the CHEM entries take.  Each thread holds its cell's aerosol state (about 54 species x 3
 // modes) in local memory; the work per cell is a few thousand float and double
 // operations, so the kernel is bound by instruction issue, not by its 0.5 KB per cell
 // of DRAM traffic.
@@ -16,32 +16,11 @@
 #include <string>
 
 #include "../../include/cmaqchem.h"
-#include "hetchem.cuh"
+#include "hetchem_table.h"
 
 __attribute__((visibility("hidden"))) void cmaqchem_set_error(const std::string& msg);
 
-static_assert(het::NAE == CMAQCHEM_HET_CB6R5_NAE && het::NHET == CMAQCHEM_HET_CB6R5_NHETERO, "HETCHEM layout");
-static_assert(het::AE_FIRST == CMAQCHEM_HET_CB6R5_AE_FIRST, "HETCHEM layout");
-
-namespace het {
-__constant__ HetTables c_het = HET_TABLES_INIT;
-}
-
 namespace {
-
-constexpr int HET_THREADS = 128;
-
-__global__ void __launch_bounds__(HET_THREADS) k_hetchem_rates(const float* ae, long long ncell, const float* ta,
-                                                               const float* pres, const float* qv, const float* dens,
-                                                               double* khetero)
-{
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += stride) {
-        double k[het::NHET];
-        het::het_cell(het::c_het, ae + c, ncell, ta[c], pres[c], qv[c], dens[c], k);
-        for (int j = 0; j < het::NHET; ++j) khetero[c * het::NHET + j] = k[j];
-    }
-}
 
 int fail(const std::string& msg)
 {
@@ -49,22 +28,27 @@ int fail(const std::string& msg)
     return -1;
 }
 
-int check_mechanism(const char* mechanism)
+// the mechanism's entry, or null with the error set
+const HetMech* find_mechanism(const char* mechanism)
 {
-    if (!mechanism || std::strcmp(mechanism, "cb6r5_ae7_aq") != 0)
-        return fail(std::string("HETCHEM_RATES: mechanism '") + (mechanism ? mechanism : "(null)") +
-                    "' is not built (cb6r5_ae7_aq only)");
-    return 0;
+    static const HetMech table[] = {hetchem_mech_cb6r5_ae7_aq(), hetchem_mech_cracmm2()};
+    if (mechanism)
+        for (const HetMech& m : table)
+            if (std::strcmp(mechanism, m.name) == 0) return &m;
+    fail(std::string("HETCHEM_RATES: mechanism '") + (mechanism ? mechanism : "(null)") +
+         "' is not built (cb6r5_ae7_aq, cracmm2)");
+    return nullptr;
 }
 
 }  // namespace
 
 extern "C" int cmaqchem_hetchem_layout(const char* mechanism, int* nae, int* ae_first, int* nhetero)
 {
-    if (check_mechanism(mechanism) != 0) return -1;
-    if (nae) *nae = het::NAE;
-    if (ae_first) *ae_first = het::AE_FIRST;
-    if (nhetero) *nhetero = het::NHET;
+    const HetMech* m = find_mechanism(mechanism);
+    if (!m) return -1;
+    if (nae) *nae = m->nae;
+    if (ae_first) *ae_first = m->ae_first;
+    if (nhetero) *nhetero = m->nhet;
     return 0;
 }
 
@@ -72,19 +56,13 @@ extern "C" int cmaqchem_hetchem_rates_device(const char* mechanism, long long nc
                                              const float* ta, const float* pres, const float* qv, const float* dens,
                                              double* khetero, void* stream)
 {
-    if (check_mechanism(mechanism) != 0) return -1;
+    const HetMech* m = find_mechanism(mechanism);
+    if (!m) return -1;
     if (ncell < 0) return fail("ncell must be >= 0");
     if (ncell == 0) return 0;
     if (!ae || !ta || !pres || !qv || !dens || !khetero) return fail("null array argument");
-    int dev = 0, nsm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const long long want = (ncell + HET_THREADS - 1) / HET_THREADS;
-    const long long cap = (long long)(nsm > 0 ? nsm : 1) * 16;   // 16 blocks of 128 per SM, grid-stride beyond
-    const unsigned blocks = (unsigned)(want < cap ? want : cap);
     cudaStream_t s = (cudaStream_t)stream;
-    k_hetchem_rates<<<blocks, HET_THREADS, 0, s>>>(ae, ncell, ta, pres, qv, dens, khetero);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = m->launch(ncell, ae, ta, pres, qv, dens, khetero, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return fail(std::string("k_hetchem_rates: ") + cudaGetErrorString(e));
     return 0;
@@ -96,15 +74,16 @@ extern "C" int cmaqchem_hetchem_rates(const char* mechanism, long long ncell, co
                                       const float* pres, const float* qv, const float* dens, double* khetero,
                                       int device)
 {
-    if (check_mechanism(mechanism) != 0) return -1;
+    const HetMech* m = find_mechanism(mechanism);
+    if (!m) return -1;
     if (ncell < 0) return fail("ncell must be >= 0");
     if (ncell == 0) return 0;
     if (!ae || !ta || !pres || !qv || !dens || !khetero) return fail("null array argument");
     cudaError_t e = cudaSetDevice(device);
     if (e != cudaSuccess) return fail(std::string("cudaSetDevice: ") + cudaGetErrorString(e));
     const size_t n = (size_t)ncell;
-    const size_t bytes[6] = {sizeof(float) * het::NAE * n, sizeof(float) * n, sizeof(float) * n, sizeof(float) * n,
-                             sizeof(float) * n, sizeof(double) * het::NHET * n};
+    const size_t bytes[6] = {sizeof(float) * m->nae * n, sizeof(float) * n, sizeof(float) * n, sizeof(float) * n,
+                             sizeof(float) * n, sizeof(double) * m->nhet * n};
     const void* src[5] = {ae, ta, pres, qv, dens};
     void* d[6] = {};
     int rc = 0;

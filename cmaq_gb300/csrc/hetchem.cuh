@@ -14,9 +14,11 @@
 // The reference's REAL(4) and REAL(8) variables and literals are kept as float and double,
 // operation by operation, with the C math library's functions in place of Fortran's
 // intrinsics of the same kind.  The mechanism's tables (aerosol species, CGRID rows,
-// KHETERO labels, epoxide pairs) come from gen/<mech>_hetchem.cuh.  The sea-salt surface
-// area of HETCHEM_RATES feeds only the bromine and iodine rates of CB6R5M_AE7_AQ; the
-// mechanisms here have none, so it is not formed.
+// KHETERO labels, epoxide pairs) come from gen/<mech>_hetchem.cuh: a translation unit
+// includes this file for one mechanism, HET_NS naming the namespace that holds the code
+// and HET_GEN the generated header (CB6r5's, in namespace het, unless both are defined).
+// The sea-salt surface area of HETCHEM_RATES feeds only the bromine and iodine rates of
+// CB6R5M_AE7_AQ; the mechanisms here have none, so it is not formed.
 #pragma once
 
 #include <math.h>
@@ -27,9 +29,14 @@
 #define HC_HD
 #endif
 
-namespace het {
+#ifndef HET_NS
+#define HET_NS het
+#define HET_GEN "gen/cb6r5_ae7_aq_hetchem.cuh"
+#endif
 
-#include "gen/cb6r5_ae7_aq_hetchem.cuh"
+namespace HET_NS {
+
+#include HET_GEN
 
 // CONST.EXT and AEROMET_DATA (REAL(4) unless noted)
 constexpr float PI = 3.14159265f;
@@ -335,6 +342,8 @@ HC_HD inline void het_cell(const HetTables& T, const float* ae, long long n, flo
         case K_IEPOX: r = 60.0 * kiepox; break;
         case K_TETROL: r = 60.0 * AQUEOUS_FREQUENCY * ftet; break;
         case K_IEPOXOS: r = aso4j_ppm > 0.0 ? 60.0 * AQUEOUS_FREQUENCY * fos / aso4j_ppm : 0.0; break;
+        case K_ISO3NOSJ: r = 60.0 * AQUEOUS_FREQUENCY * ftet; break;   // CRACMM's non-sulfated IEPOX SOA
+        case K_ISO3OSJ: r = aso4j_ppm > 0.0 ? 60.0 * AQUEOUS_FREQUENCY * fos / aso4j_ppm : 0.0; break;
         case K_NO3: r = 60.0 * (kno3[0] + kno3[1]); break;
         case K_GLY: r = 60.0 * kgly[1]; break;
         case K_MGLY: r = 60.0 * kmgly[1]; break;
@@ -359,4 +368,4 @@ HC_HD inline void het_cell(const HetTables& T, const float* ae, long long n, flo
     }
 }
 
-}  // namespace het
+}  // namespace HET_NS

@@ -38,7 +38,8 @@ NUM_SUFFIX = ("ATKN", "ACC", "COR")
 IMPLEMENTED = ("HETERO_N2O5IJ", "HETERO_N2O5K", "HETERO_H2NO3PAIJ", "HETERO_H2NO3PBIJ", "HETERO_H2NO3PAK",
                "HETERO_H2NO3PBK", "HETERO_NO2", "HETERO_IEPOX", "HETERO_IEPOXOS", "HETERO_TETROL", "HETERO_GLY",
                "HETERO_MGLY", "HETERO_NTR2", "HETERO_CLNO3_WAI", "HETERO_CLNO3_WAJ", "HETERO_PNCOMLI",
-               "HETERO_PNCOMLJ", "HETERO_NO3", "HETERO_HO2", "HETERO_N2O5I", "HETERO_N2O5J")
+               "HETERO_PNCOMLJ", "HETERO_NO3", "HETERO_HO2", "HETERO_N2O5I", "HETERO_N2O5J", "HETERO_ISO3NOSJ",
+               "HETERO_ISO3OSJ")
 
 
 def _split_args(s: str) -> list[str]:
@@ -214,7 +215,7 @@ def device_header(t: dict) -> str:
     sp = t["species"]
     o = [f"// Generated by cmaq_gb300/mechgen/hetchem.py from CCTM/src/aero/aero6 (AERO_DATA.F, "
          f"AEROSOL_CHEMISTRY.F) and MECHS/{t['mechanism']}.",
-         "// Included inside namespace het by csrc/hetchem.cuh.  Do not edit.", "#pragma once", "",
+         "// Included inside the mechanism's namespace by csrc/hetchem.cuh.  Do not edit.", "#pragma once", "",
          f"constexpr int NAE = {len(t['ae_rows'])};      // CGRID rows of the aerosol block",
          f"constexpr int AE_FIRST = {t['ae_first']};  // its first row in the mechanism's CGRID (0-based)",
          f"constexpr int NSPC = {len(sp)};     // aerosol chemical species (map_aero order)",
@@ -290,7 +291,8 @@ def oracle_header(t: dict) -> str:
     o.append(arr("char* const", "ho_hetero", ['"' + h + '"' for h in t["hetero"]]))
     g = t["gas_molwt"]
     o.append(f"static const double ho_mw_iepox = {_c_double(g['IEPOX'])}, ho_mw_gly = {_c_double(g['GLY'])}, "
-             f"ho_mw_mgly = {_c_double(g['MGLY'])};")
+             f"ho_mw_mgly = {_c_double(g['MGLY'])}, ho_mw_no3 = {_c_double(g['NO3'])}, "
+             f"ho_mw_ho2 = {_c_double(g['HO2'])};")
     o.append(f"static const float ho_hl_iepox_a = {_c_float(t['henry_iepox'][0])}, ho_hl_iepox_e = "
              f"{_c_float(t['henry_iepox'][1])};")
     return "\n".join(o) + "\n"

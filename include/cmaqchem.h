@@ -332,11 +332,15 @@ int cmaqchem_aqchem_device(long long ncell, const double* params, double* gas, d
  *   khetero  KHETERO(NHETERO, NCOLS, NROWS, NLAYS) REAL(8) out, the mechanism's HETERO order,
  *            the array the CHEM entries take.
  * cmaqchem_hetchem_layout gives the block's rows, its first row in the mechanism's CGRID
- * (0-based) and NHETERO.  Only cb6r5_ae7_aq is built.  Synchronises the stream; returns 0 or
- * -1.  cmaqchem_hetchem_rates takes host arrays (device buffers for the call). */
+ * (0-based) and NHETERO.  Built for cb6r5_ae7_aq and cracmm2 (CRACMM's IEPOX pair table,
+ * the NO3 and HO2 uptake and the ISO3NOSJ / ISO3OSJ rates).  Synchronises the stream;
+ * returns 0 or -1.  cmaqchem_hetchem_rates takes host arrays (device buffers for the call). */
 #define CMAQCHEM_HET_CB6R5_NAE 84
 #define CMAQCHEM_HET_CB6R5_AE_FIRST 131
 #define CMAQCHEM_HET_CB6R5_NHETERO 17
+#define CMAQCHEM_HET_CRACMM2_NAE 90
+#define CMAQCHEM_HET_CRACMM2_AE_FIRST 184
+#define CMAQCHEM_HET_CRACMM2_NHETERO 9
 int cmaqchem_hetchem_layout(const char* mechanism, int* nae, int* ae_first, int* nhetero);
 int cmaqchem_hetchem_rates_device(const char* mechanism, long long ncell, const float* ae, const float* ta,
                                   const float* pres, const float* qv, const float* dens, double* khetero,

@@ -5,7 +5,8 @@
 Compiles ``oracle/ros3_oracle.c`` once per mechanism into
 ``oracle/_build/liboracle_<mech>.so`` with gcc, and ``oracle/kmt2_oracle.c`` (the
 KMT2 aqueous cloud chemistry, one mechanism) into ``oracle/_build/liboracle_kmt2.so``, and
-``oracle/hetchem_oracle.c`` (HETCHEM_RATES, cb6r5_ae7_aq) into ``oracle/_build/liboracle_hetchem.so``.  ``-ffp-contract=off`` keeps the
+``oracle/hetchem_oracle.c`` (HETCHEM_RATES) once per mechanism into
+``oracle/_build/liboracle_hetchem_<mech>.so``.  ``-ffp-contract=off`` keeps the
 compiler from fusing operations beyond the explicit ``fma`` calls; no
 ``-march`` flag, so the library builds the same on x86-64 and aarch64.
 
@@ -31,8 +32,8 @@ def kmt2_lib_path() -> Path:
     return HERE / "_build" / "liboracle_kmt2.so"
 
 
-def hetchem_lib_path() -> Path:
-    return HERE / "_build" / "liboracle_hetchem.so"
+def hetchem_lib_path(mech: str = "cb6r5_ae7_aq") -> Path:
+    return HERE / "_build" / f"liboracle_hetchem_{mech}.so"
 
 
 def _gcc(srcs, out: Path, defines=()):
@@ -63,10 +64,12 @@ def build(mechs=MECHS, force: bool = False) -> list[Path]:
              HERE / "portable_pow.h")
     if force or not kout.exists() or kout.stat().st_mtime <= max(p.stat().st_mtime for p in kdeps):
         procs.append((subprocess.Popen(_gcc([kdeps[0]], kout), cwd=HERE), kout))
-    hout = hetchem_lib_path()
-    hdeps = (HERE / "hetchem_oracle.c", HERE / "gen" / "cb6r5_ae7_aq_hetchem.h")
-    if force or not hout.exists() or hout.stat().st_mtime <= max(p.stat().st_mtime for p in hdeps):
-        procs.append((subprocess.Popen(_gcc([hdeps[0]], hout), cwd=HERE), hout))
+    for mech in MECHS:
+        hout = hetchem_lib_path(mech)
+        hdeps = (HERE / "hetchem_oracle.c", HERE / "gen" / f"{mech}_hetchem.h")
+        if force or not hout.exists() or hout.stat().st_mtime <= max(p.stat().st_mtime for p in hdeps):
+            cmd = _gcc([hdeps[0]], hout, (f'-DHO_TABLES="gen/{mech}_hetchem.h"',))
+            procs.append((subprocess.Popen(cmd, cwd=HERE), hout))
     for p, out in procs:
         if p.wait() != 0:
             raise RuntimeError(f"oracle build failed for {out.name}")

@@ -33,5 +33,5 @@ static const int ho_nuc_remove[] = {0, 2, 0, 0, 2, 0};
 static const int ho_nuc_os[] = {0, 1, 0, 0, 1, 0};
 static const double ho_nuc_kchem[] = {0.0009, 0.00883, 0.0002, 1.31e-05, 2.92e-06, 2.92e-06};
 static const char* const ho_hetero[] = {"HETERO_CLNO3_WAI", "HETERO_CLNO3_WAJ", "HETERO_NTR2", "HETERO_N2O5IJ", "HETERO_N2O5K", "HETERO_H2NO3PAIJ", "HETERO_H2NO3PAK", "HETERO_H2NO3PBIJ", "HETERO_H2NO3PBK", "HETERO_NO2", "HETERO_IEPOX", "HETERO_IEPOXOS", "HETERO_TETROL", "HETERO_GLY", "HETERO_MGLY", "HETERO_PNCOMLI", "HETERO_PNCOMLJ"};
-static const double ho_mw_iepox = 118.1, ho_mw_gly = 58.0, ho_mw_mgly = 72.0;
+static const double ho_mw_iepox = 118.1, ho_mw_gly = 58.0, ho_mw_mgly = 72.0, ho_mw_no3 = 62.0, ho_mw_ho2 = 33.0;
 static const float ho_hl_iepox_a = 30000000.0f, ho_hl_iepox_e = 0.0f;

@@ -1,8 +1,9 @@
 /* CPU oracle of CMAQ's heterogeneous rate constants KHETERO (test infrastructure).
  *
  * Restates, per grid cell, HETCHEM_RATES (CCTM/src/aero/aero6/AEROSOL_CHEMISTRY.F:282-1535)
- * for the mechanism of gen/<mech>_hetchem.h, with the aerosol-state routines it calls,
- * each as a function of the same name over a per-cell copy of the AERO_DATA module state:
+ * for the mechanism of gen/<mech>_hetchem.h (cb6r5_ae7_aq, cracmm2), with the aerosol-state
+ * routines it calls, each as a function of the same name over a per-cell copy of the
+ * AERO_DATA module state:
  *
  *   extract_aero     AERO_DATA.F:1296-1420 (minchk = .TRUE.)
  *   calcmoments      AERO_DATA.F:1575-1699 (both branches)
@@ -24,7 +25,12 @@
 #include <math.h>
 #include <string.h>
 
-#include "gen/cb6r5_ae7_aq_hetchem.h"
+/* the mechanism's tables: HO_TABLES names gen/<mech>_hetchem.h (oracle/build.py builds one
+ * library per mechanism) */
+#ifndef HO_TABLES
+#define HO_TABLES "gen/cb6r5_ae7_aq_hetchem.h"
+#endif
+#include HO_TABLES
 
 /* CONST.EXT, AEROMET_DATA, AERO_DATA parameters */
 static const float PI_F = 3.14159265f;
@@ -345,7 +351,7 @@ static void hetchem_rates_cell(const float* conc, long long stride, float temp, 
 {
     const double AQUEOUS_FREQUENCY = 1.0e+9, INV_SQRT_MWN2O5 = 9.62161363758323e-2;
     const double INV_SQRT_MWCLNO3 = 1.012739360000e-1, COEF1 = 7.24382926227485e10;
-    const double GAMMA_GLY = 2.9e-3;
+    const double GAMMA_GLY = 2.9e-3, GAMMA_NO3 = 1.0e-3, GAMMA_HO2 = 0.2;
     const double STD_DIFF_N2O5 = 0.0855e-4, STD_DIFF_CLNO3 = 0.1014e-4;
     const float GPKG = 1.0e+03f;
     const float CFACTOR = 8.0f * GPKG * RGASUNIV_F / PI_F;
@@ -362,6 +368,8 @@ static void hetchem_rates_cell(const float* conc, long long stride, float temp, 
     const double inv_mwaso4 = (double)(1.0f / ho_molwt[HO_ASO4]);
     const double cfactor_gly = sqrt(8.0e3 * (double)RGASUNIV_F / (ho_mw_gly * DPI_D));
     const double cfactor_mgly = sqrt(8.0e3 * (double)RGASUNIV_F / (ho_mw_mgly * DPI_D));
+    const double cfactor_no3 = sqrt(8.0e3 * (double)RGASUNIV_F / (ho_mw_no3 * DPI_D));
+    const double cfactor_ho2 = sqrt(8.0e3 * (double)RGASUNIV_F / (ho_mw_ho2 * DPI_D));
 
     HoState st;
     HoState* s = &st;
@@ -378,10 +386,12 @@ static void hetchem_rates_cell(const float* conc, long long stride, float temp, 
     const double cbar = cbar_coeff * INV_SQRT_MWN2O5;
     const double cbargly = cfactor_gly * sqrt(airtemp);
     const double cbarmgly = cfactor_mgly * sqrt(airtemp);
+    const double cbarno3 = cfactor_no3 * sqrt(airtemp);
+    const double cbarho2 = cfactor_ho2 * sqrt(airtemp);
     const double cbar_clno3 = cbar_coeff * INV_SQRT_MWCLNO3;
     const double inv_diffusivity = 1.0 / (STD_DIFF_N2O5 * adjust_diff);
     const double inv_diff_clno3 = 1.0 / (STD_DIFF_CLNO3 * adjust_diff);
-    double kn2o5[3], kgly[3], kmgly[3], cl_ppm[3], yield_clno2[3] = {0.0, 0.0, 0.0};
+    double kn2o5[3], kno3[3], kgly[3], kmgly[3], kho2[3], cl_ppm[3], yield_clno2[3] = {0.0, 0.0, 0.0};
     double yieldij = 0.0;
     for (int n = 0; n < 3; ++n) {
         double gamma;
@@ -389,10 +399,14 @@ static void hetchem_rates_cell(const float* conc, long long stride, float temp, 
         else gamma = n2o5_gamma(s, airtemp, airrh, 5);
         const double xxf = s->wet_m2[n] / (4.0 + 0.5 * s->de_wet[n] * gamma * cbar * inv_diffusivity);
         kn2o5[n] = gamma * xxf;
+        kno3[n] = GAMMA_NO3 * s->wet_m2[n] / (4.0 + 0.5 * s->de_wet[n] * GAMMA_NO3 * cbarno3 * inv_diffusivity)
+                * cbarno3 * DPI_D;
         kgly[n] = GAMMA_GLY * s->wet_m2[n] / (4.0 + 0.5 * s->de_wet[n] * GAMMA_GLY * cbargly * inv_diffusivity)
                 * cbargly * DPI_D;
         kmgly[n] = 0.09f * GAMMA_GLY * s->wet_m2[n]
                  / (4.0 + 0.5 * s->de_wet[n] * 0.09f * GAMMA_GLY * cbarmgly * inv_diffusivity) * cbarmgly * DPI_D;
+        kho2[n] = GAMMA_HO2 * s->wet_m2[n] / (4.0 + 0.5 * s->de_wet[n] * GAMMA_HO2 * cbarho2 * inv_diffusivity)
+                * cbarho2 * DPI_D;
         const float ah2o = s->aerospc_conc[HO_AH2O][n], acl = s->aerospc_conc[HO_ACL][n];
         cl_ppm[n] = ppm_factor * (acl * inv_mwcl);
         if (ah2o > 5.0e-01f && acl > 1.0e-04f) {
@@ -451,6 +465,14 @@ static void hetchem_rates_cell(const float* conc, long long stride, float temp, 
             k = 60.0 * AQUEOUS_FREQUENCY * fh2o;
         } else if (label_is(irate, "HETERO_IEPOXOS")) {
             k = aso4j_ppm > 0.0 ? 60.0 * AQUEOUS_FREQUENCY * fos / aso4j_ppm : 0.0;
+        } else if (label_is(irate, "HETERO_ISO3NOSJ")) {   /* CRACMM's IEPOX SOA */
+            k = 60.0 * AQUEOUS_FREQUENCY * fh2o;
+        } else if (label_is(irate, "HETERO_ISO3OSJ")) {
+            k = aso4j_ppm > 0.0 ? 60.0 * AQUEOUS_FREQUENCY * fos / aso4j_ppm : 0.0;
+        } else if (label_is(irate, "HETERO_NO3")) {
+            k = 60.0 * (kno3[0] + kno3[1]);
+        } else if (label_is(irate, "HETERO_HO2")) {
+            k = 60.0 * kho2[1];
         } else if (label_is(irate, "HETERO_GLY")) {
             k = 60.0 * kgly[1];
         } else if (label_is(irate, "HETERO_MGLY")) {

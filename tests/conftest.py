@@ -60,20 +60,28 @@ def kmt2_harness(tmp_path_factory):
 @pytest.fixture(scope="session")
 def hetchem_harness(tmp_path_factory):
     """tests/hetchem_host_harness.cpp (the HETCHEM_RATES device code built for the host)
-    compiled with g++ under AddressSanitizer and UndefinedBehaviorSanitizer."""
+    compiled with g++ under AddressSanitizer and UndefinedBehaviorSanitizer: a function of
+    the mechanism returning its executable (built once per mechanism)."""
     import shutil
     import subprocess
     gxx = shutil.which("g++")
     if gxx is None:
         pytest.skip("no C++ compiler")
-    exe = tmp_path_factory.mktemp("hetchem") / "hetchem_host_harness"
-    cmd = [gxx, "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-fsanitize=address,undefined",
-           "-fno-sanitize-recover=all", "-o", str(exe), str(ROOT / "tests" / "hetchem_host_harness.cpp")]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0 and "sanitize" in r.stderr:
-        pytest.skip("sanitizer runtime not available")
-    assert r.returncode == 0, r.stderr[-3000:]
-    return exe
+    built = {}
+
+    def get(mech="cb6r5_ae7_aq"):
+        if mech not in built:
+            exe = tmp_path_factory.mktemp("hetchem") / f"hetchem_host_harness_{mech}"
+            defs = [] if mech == "cb6r5_ae7_aq" else [f"-DHET_NS=het_{mech}", f'-DHET_GEN="gen/{mech}_hetchem.cuh"']
+            cmd = [gxx, "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-fsanitize=address,undefined",
+                   "-fno-sanitize-recover=all", *defs, "-o", str(exe), str(ROOT / "tests" / "hetchem_host_harness.cpp")]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0 and "sanitize" in r.stderr:
+                pytest.skip("sanitizer runtime not available")
+            assert r.returncode == 0, r.stderr[-3000:]
+            built[mech] = exe
+        return built[mech]
+    return get
 
 
 def run_hetchem_harness(exe, ae, ta, pres, qv, dens, workdir):

@@ -26,11 +26,12 @@ class _HostEvent:
         return (other.t - self.t) * 1e3
 
 
-def test_run_hetchem_bookkeeping_on_the_host(hetchem_harness, tmp_path, monkeypatch):
+@pytest.mark.parametrize("mech,nae,nhet", [("cb6r5_ae7_aq", 84, 17), ("cracmm2", 90, 9)])
+def test_run_hetchem_bookkeeping_on_the_host(hetchem_harness, tmp_path, monkeypatch, mech, nae, nhet):
     import cmaq_gb300.hetchem as het
 
     def host_rates(ae, ta, pres, qv, dens, *, mechanism="cb6r5_ae7_aq", out=None, stream=None):
-        k = torch.from_numpy(run_hetchem_harness(hetchem_harness, ae.numpy(), ta.numpy(), pres.numpy(), qv.numpy(),
+        k = torch.from_numpy(run_hetchem_harness(hetchem_harness(mechanism), ae.numpy(), ta.numpy(), pres.numpy(), qv.numpy(),
                                                  dens.numpy(), tmp_path).copy())
         if out is not None:
             out.copy_(k)
@@ -46,10 +47,10 @@ def test_run_hetchem_bookkeeping_on_the_host(hetchem_harness, tmp_path, monkeypa
                         else to(self, *a, **k))
     sys.path.insert(0, str(ROOT))
     import bench
-    r = bench.run_hetchem(0, 300, 2, 2)
-    assert r["ncell"] == 300 and r["value"] > 0
-    assert r["roofline"]["bound"] == "hbm" and r["roofline"]["bytes_per_cell"] == 84 * 4 + 16 + 17 * 8
-    assert r["e2e"]["h2d_bytes_per_step"] == 300 * (84 + 4) * 4 and r["e2e"]["d2h_bytes_per_step"] == 300 * 17 * 8
+    r = bench.run_hetchem(0, 300, 2, 2, mech)
+    assert r["ncell"] == 300 and r["value"] > 0 and r["mechanism"] == mech
+    assert r["roofline"]["bound"] == "hbm" and r["roofline"]["bytes_per_cell"] == nae * 4 + 16 + nhet * 8
+    assert r["e2e"]["h2d_bytes_per_step"] == 300 * (nae + 4) * 4 and r["e2e"]["d2h_bytes_per_step"] == 300 * nhet * 8
     assert r["parity"]["cells"] == 300 and r["parity"]["max_rel_diff_off_switch"] == 0.0
     assert r["parity"]["cells_on_the_iepox_switch"] == 0
     assert r["cpu"]["cells"] == 300 and r["cpu"]["value"] > 0

@@ -14,21 +14,32 @@ h = pytest.importorskip("hetchem")   # oracle/hetchem.py
 f32 = np.float32
 
 
-def test_tables_are_the_generators_output_on_the_reference():
+MECHS = ("cb6r5_ae7_aq", "cracmm2")
+
+
+@pytest.mark.parametrize("mech", MECHS)
+def test_tables_are_the_generators_output_on_the_reference(mech):
     root = cmaq_root()
     if not (root / "CCTM").exists():
         pytest.skip("CMAQ sources not present")
     from cmaq_gb300.mechgen.hetchem import tables
-    committed = json.loads((ROOT / "cmaq_gb300" / "mechs" / "cb6r5_ae7_aq" / "hetchem.json").read_text())
-    assert tables(root) == committed
+    committed = json.loads((ROOT / "cmaq_gb300" / "mechs" / mech / "hetchem.json").read_text())
+    assert tables(root, mech) == committed
 
 
-def test_aerosol_block_rows_match_the_mechanisms_cgrid_indices():
-    t = h.tables()
-    man = json.loads((ROOT / "cmaq_gb300" / "mechs" / "cb6r5_ae7_aq" / "manifest.json").read_text())
-    for s in man["species"]:
+@pytest.mark.parametrize("mech", MECHS)
+def test_aerosol_block_rows_match_the_mechanisms_cgrid_indices(mech):
+    t = h.tables(mech)
+    man = json.loads((ROOT / "cmaq_gb300" / "mechs" / mech / "manifest.json").read_text())
+    n = 0
+    for s in man["species"]:   # the aerosol species the gas mechanism reads or writes
         if s["type"] == "AE":
             assert t["ae_first"] + t["ae_rows"].index(s["name"]) == s["cgrid_index"], s["name"]
+            n += 1
+    assert n >= 1
+    assert t["hetero"] == man["hetero"]
+    if mech != "cb6r5_ae7_aq":
+        return
     assert t["ae_rows"][:6] == ["ASO4I", "ASO4J", "ASO4K", "ANH4I", "ANH4J", "ANH4K"]
     assert "NUMATKN" in t["ae_rows"] and "SRFCOR" in t["ae_rows"] and "ASEACAT" in t["ae_rows"]
     spc = {s["bulkname"]: s for s in t["species"]}
@@ -55,10 +66,10 @@ def test_pncom_loss(pncom):
     assert h.load().oracle_het_pncom_loss(1.0, pncom) == pncom_loss_py(1.0, pncom)
 
 
-def _column(**mass):
+def _column(mech="cb6r5_ae7_aq", **mass):
     """An aerosol column of the block: every species at 1e-3 ug/m3 per present mode, then
     the given 'NAMEmode' masses; number and surface area of typical modes."""
-    t = h.tables()
+    t = h.tables(mech)
     col = np.zeros(len(t["ae_rows"]), np.float32)
     for s in t["species"]:
         for r in s["row"]:
@@ -186,3 +197,50 @@ def test_uptake_rates_follow_the_kinetic_limit():
     g = 2.9e-3
     want = 60 * g * m2[1] / (4 + 0.5 * de[1] * g * cbar_gly / (0.0855e-4 * adj)) * cbar_gly * np.pi
     assert k[lab["HETERO_GLY"]] == pytest.approx(want, rel=1e-5)
+
+
+def test_cracmm2_no3_ho2_uptake_and_iepox_products():
+    """CRACMM2's own labels: NO3 on the Aitken and accumulation modes (gamma 1e-3) and HO2
+    on the accumulation mode (gamma 0.2), k = gamma S / (4 + D_e gamma cbar / (2 D)) cbar
+    pi (AEROSOL_CHEMISTRY.F:954-981, 1269-1279); ISO3NOSJ and ISO3OSJ split the IEPOX
+    uptake by CRACMM's pair table (:259-273): the sulfated fraction fos is the share of the
+    ASO4J pairs in sum(k_pair [nuc] [acid]) with H+ from AH3OPJ, HSO4- from the charge
+    balance and sulfate less the bisulfate, and ISO3NOSJ carries 1 - fos."""
+    mech = "cracmm2"
+    t = h.tables(mech)
+    col = _column(mech, ASO4J=4.0, AH2OJ=25.0, ANO3J=1.5, ANH4J=1.0, AH3OPJ=2e-4)
+    temp, pres, qv, dens = 290.0, 95000.0, 8e-3, 1.15
+    k = h.rates(col[:, None], np.array([temp]), np.array([pres]), np.array([qv]), np.array([dens]), mech=mech)[0]
+    m2, _, de = h.cell_piece("moments", col, mech=mech)
+    lab = {n: j for j, n in enumerate(t["hetero"])}
+    inv_d = 1.0 / (0.0855e-4 * (temp / 273.15) ** 1.75 * (101325.0 / pres))
+
+    def uptake(gamma, mw, m):
+        cbar = np.sqrt(8e3 * 8.314510 / (mw * np.pi)) * np.sqrt(temp)
+        return gamma * m2[m] / (4 + 0.5 * de[m] * gamma * cbar * inv_d) * cbar * np.pi
+
+    mw = t["gas_molwt"]
+    assert k[lab["HETERO_NO3"]] == pytest.approx(60 * (uptake(1e-3, mw["NO3"], 0) + uptake(1e-3, mw["NO3"], 1)),
+                                                 rel=1e-5)
+    assert k[lab["HETERO_HO2"]] == pytest.approx(60 * uptake(0.2, mw["HO2"], 1), rel=1e-5)
+    spc = t["species"]
+    conc = {s["bulkname"]: float(col[s["row"][1]]) for s in spc if s["row"][1] >= 0}
+    mwa = {s["bulkname"]: s["molwt"] for s in spc}
+    hplus = conc["AH3OP"] / mwa["AH3OP"] * 1e-6
+    charge = -sum(s["charge"] * conc[s["bulkname"]] / s["molwt"] for s in spc
+                  if s["row"][1] >= 0 and not s["tracer"])
+    acid = [hplus, max(charge * 1e-6 - hplus, 0.0)]
+    tot = os_ = 0.0
+    for p in t["nuc_pairs"]:
+        nuc = conc[p["nuc"][:-1]] / mwa[p["nuc"][:-1]] * 1e-6
+        if p["idx_remove"] >= 1:
+            nuc = max(nuc - acid[p["idx_remove"] - 1], 0.0)
+        kc = p["kchem"] * nuc * acid[p["idx_acid"] - 1]
+        tot += kc
+        os_ += kc if p["prod"] == "AISO3OSJ" else 0.0
+    fos = os_ / tot
+    assert {p["prod"] for p in t["nuc_pairs"]} == {"AISO3NOSJ", "AISO3OSJ"}
+    assert k[lab["HETERO_ISO3NOSJ"]] == pytest.approx(60 * 1e9 * (1 - fos), rel=1e-9)
+    aso4j_ppm = 1e-3 * (28.9628 / dens) * 4.0 / mwa["ASO4"]
+    assert k[lab["HETERO_ISO3OSJ"]] == pytest.approx(60 * 1e9 * fos / aso4j_ppm, rel=1e-6)
+    assert k[lab["HETERO_IEPOX"]] > 0
