@@ -723,7 +723,7 @@ def run_aqchem(device: int, ncell: int, steps: int, warmup: int, threads: int, w
     res_whole = None
     if whole:
         res_whole = run_aqchem_whole(dev, ncell, steps)
-    res = {"mechanism": mech, "ncell": ncell, "ms_per_call": dev_ms, "value": ncell / (dev_ms * 1e-3), "whole_aqchem": res_whole,
+    res = {"ncell": ncell, "ms_per_call": dev_ms, "value": ncell / (dev_ms * 1e-3), "whole_aqchem": res_whole,
            "achieved_tflops": flops / (dev_ms * 1e-3) / 1e12, "flops_per_call": flops,
            "steps_per_cell": float(sd[1].mean()), "max_steps_per_cell": int(sd[1].max()),
            "failed_cells": int((sd[8] != 1).sum()),
