@@ -44,6 +44,8 @@ VARIANTS = {"default": (GEN_DEFAULT, [Q_DEFAULT]),
             # 1/U(i,i) by the correctly rounded reciprocal (same bits); L1 prefetch of the next row
             "rcp": (GEN_DEFAULT + ["-DCHEM_RCP(x)=__drcp_rn(x)"], [Q_DEFAULT]),
             "pfl1": (GEN_DEFAULT + ["-DCHEM_USE_PREFETCH_L1"], [Q_DEFAULT]),
+            # the default build without the L2 prefetch of the next rows' workspace reads
+            "nopf80": (["-maxrregcount=80"], [Q_DEFAULT]),
             # other register caps with as many resident warps as they allow
             "r96w20": (["-maxrregcount=96", "-DCHEM_USE_PREFETCH"], ["-DCHEM_QUEUE_WARPS_PER_SM=20"]),
             "r72w28": (["-maxrregcount=72", "-DCHEM_USE_PREFETCH"], ["-DCHEM_QUEUE_WARPS_PER_SM=28"]),

@@ -125,6 +125,7 @@ struct cmaqchem_handle {
     double* s_khet = nullptr;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev_legacy = nullptr;   // orders the handle's stream after the legacy default stream
     // host-pointer path: copy stream and per-chunk events
     int e2e_chunks = 4;
     cudaStream_t copy_stream = nullptr, back_stream = nullptr;
@@ -174,6 +175,7 @@ void free_handle(cmaqchem_handle* h)
     if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
     if (h->back_stream) cudaStreamDestroy(h->back_stream);
     if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev_legacy) cudaEventDestroy(h->ev_legacy);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
@@ -188,6 +190,17 @@ int ensure_ws(cmaqchem_handle* h, size_t warps)
     CK(cudaMalloc(&h->d_ws, warps * (size_t)h->ws_elems * 32 * sizeof(double)));
     h->ws_warps = warps;
     return 0;
+}
+
+// The stream of a call: the caller's, or (stream null) the handle's own non-blocking
+// stream, ordered after the work already on the legacy default stream, where a caller
+// without a stream of its own (a PyTorch program on its default stream) wrote the inputs.
+cudaStream_t call_stream(cmaqchem_handle* h, void* stream)
+{
+    if (stream) return (cudaStream_t)stream;
+    if (cudaEventRecord(h->ev_legacy, cudaStreamLegacy) == cudaSuccess)
+        cudaStreamWaitEvent(h->stream, h->ev_legacy, 0);
+    return h->stream;
 }
 
 // Grid of the work-queue kernel for the handle's knobs: one persistent wave.
@@ -444,6 +457,10 @@ extern "C" int cmaqchem_init(const cmaqchem_cfg* cfg, cmaqchem_handle** out)
         CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
         CK(cudaEventCreate(&h->ev0));
         CK(cudaEventCreate(&h->ev1));
+        CK(cudaEventCreateWithFlags(&h->ev_legacy, cudaEventDisableTiming));
+        // the set-up memsets and copies above ran on the legacy default stream, which the
+        // handle's non-blocking stream does not wait for
+        CK(cudaDeviceSynchronize());
         return 0;
     };
     rc = setup();
@@ -504,8 +521,14 @@ extern "C" int cmaqchem_diag_set_tuning(cmaqchem_handle* h, const char* key, int
     } else if (strcmp(key, "queue_history") == 0) {
         // 0: forget the previous call's step counts, so the next call starts with the work
         // queue of a fresh run's first call (cells in grid order)
+        // (a set-up call: the device is idle before and after the clear, so no later call
+        // on any stream can sort its queue by a half-cleared count array)
         if (value != 0) return fail("queue_history takes 0 (clear)");
-        if (h->d_steps) CK(cudaMemset(h->d_steps, 0, sizeof(int) * h->ncell));
+        if (h->d_steps) {
+            CK(cudaDeviceSynchronize());
+            CK(cudaMemset(h->d_steps, 0, sizeof(int) * h->ncell));
+            CK(cudaDeviceSynchronize());
+        }
         h->have_history = false;
         return 0;
     } else if (strcmp(key, "host_chunks") == 0) {
@@ -642,7 +665,7 @@ extern "C" int cmaqchem_step_device(cmaqchem_handle* h, float* conc, const float
     (void)jdate;
     (void)jtime;
     if (!h) return fail("null handle");
-    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    cudaStream_t s = call_stream(h, stream);
     return step_device_impl(h, conc, ta, qv, dens, pres, seaice, ocean_szone, rj, khetero, tstep, s, stats);
 }
 
@@ -662,7 +685,7 @@ extern "C" int cmaqchem_step_ddm_device(cmaqchem_handle* h, float* conc, const f
     const int itmstep = hhmmss_to_sec(tstep[1]);
     if (itmstep <= 0) return fail("TSTEP(2) must be a positive HHMMSS interval");
     CK(cudaSetDevice(h->device));
-    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    cudaStream_t s = call_stream(h, stream);
     if (!h->d_yave) CK(cudaMalloc(&h->d_yave, sizeof(double) * h->ops->ischan * h->ncell));
     chem::GridArgs a = grid_args(h, conc, ta, qv, dens, pres, seaice, ocean_szone, rj, khetero,
                                  (double)itmstep / 60.0);
@@ -692,7 +715,7 @@ extern "C" int cmaqchem_steps_device(cmaqchem_handle* h, float* conc, const floa
     const int itmstep = hhmmss_to_sec(tstep[1]);
     if (itmstep <= 0) return fail("TSTEP(2) must be a positive HHMMSS interval");
     CK(cudaSetDevice(h->device));
-    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    cudaStream_t s = call_stream(h, stream);
     GraphKey key{{conc, ta, qv, dens, pres, seaice, ocean_szone, rj, khetero}, itmstep};
     if (!h->graph_exec || memcmp(&key, &h->graph_key, sizeof(key)) != 0) {
         if (h->graph_exec) CK(cudaGraphExecDestroy(h->graph_exec));
@@ -809,6 +832,7 @@ extern "C" int cmaqchem_cell_stats(cmaqchem_handle* h, int* status, int* attempt
 {
     if (!h) return fail("null handle");
     CK(cudaSetDevice(h->device));
+    CK(cudaDeviceSynchronize());   // the counts of calls still running on the handle's stream
     if (status) CK(cudaMemcpy(status, h->d_status, sizeof(int) * h->ncell, cudaMemcpyDeviceToHost));
     if (attempts) CK(cudaMemcpy(attempts, h->d_steps, sizeof(int) * h->ncell, cudaMemcpyDeviceToHost));
     return 0;
@@ -824,7 +848,7 @@ extern "C" int cmaqchem_ros3_solve_device(cmaqchem_handle* h, long long ncell, d
     if (!y || !rki || !night) return fail("null array argument");
     if (!(chemstep_min > 0.0)) return fail("chemstep must be positive");
     CK(cudaSetDevice(h->device));
-    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    cudaStream_t s = call_stream(h, stream);
     chem::SolveArgs a{};
     a.y = y;
     a.rki = rki;
@@ -851,7 +875,7 @@ extern "C" int cmaqchem_ebi_solve_device(cmaqchem_handle* h, long long ncell, do
     if (!yc || !rki) return fail("null array argument");
     if (tstep_sec <= 0) return fail("tstep_sec must be positive");
     CK(cudaSetDevice(h->device));
-    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    cudaStream_t s = call_stream(h, stream);
     chem::EbiSolveArgs a{};
     a.yc = yc;
     a.rki = rki;
@@ -877,7 +901,7 @@ extern "C" int cmaqchem_gear_solve_device(cmaqchem_handle* h, long long ncell, d
     if (!y || !rk || !night) return fail("null array argument");
     if (!(chemstep_min > 0.0)) return fail("chemstep must be positive");
     CK(cudaSetDevice(h->device));
-    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    cudaStream_t s = call_stream(h, stream);
     chem::GridArgs a{};
     a.ncell = ncell;
     a.chemstep = chemstep_min;
@@ -921,7 +945,7 @@ extern "C" int cmaqchem_rconst_device(cmaqchem_handle* h, const float* conc, con
     const void* ptrs[] = {conc, ta, qv, dens, pres, seaice, ocean_szone, rj, rki, khetero};
     if (check_ptrs(ptrs, h->ops->nhetero > 0 ? 10 : 9)) return -1;
     CK(cudaSetDevice(h->device));
-    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    cudaStream_t s = call_stream(h, stream);
     chem::GridArgs a = grid_args(h, const_cast<float*>(conc), ta, qv, dens, pres, seaice, ocean_szone, rj, khetero,
                                  1.0);
     CK(h->ops->rconst(a, rki, sunlit, h->nblocks, s));
@@ -1054,7 +1078,7 @@ extern "C" int cmaqchem_adj_forward(cmaqchem_handle* h, long long ncell, double*
 {
     if (adj_check(h, ncell, y, rki, night, nsync, chemstep_min, checkpoints, nsteps)) return -1;
     CK(cudaSetDevice(h->device));
-    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    cudaStream_t s = call_stream(h, stream);
     if (adj_setup(h, ncell)) return -1;
     CK(cudaMemsetAsync(h->d_adj_counters, 0, 3 * sizeof(unsigned long long), s));
     const TapePool pool = carve_pool(tape, tape_bytes, ncell, nsync, h->ops->ischan);
@@ -1103,7 +1127,7 @@ extern "C" int cmaqchem_adj_backward(cmaqchem_handle* h, long long ncell, double
     if (adj_check(h, ncell, lambda, rki, night, nsync, chemstep_min, checkpoints, nsteps)) return -1;
     if (!grad_logk) return fail("null array argument");
     CK(cudaSetDevice(h->device));
-    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    cudaStream_t s = call_stream(h, stream);
     if (adj_setup(h, ncell)) return -1;
     // steps whose tape the forward pass recorded completely skip the re-run
     const TapePool pool = carve_pool(const_cast<void*>(tape), tape_bytes, ncell, nsync, h->ops->ischan);

@@ -176,7 +176,9 @@ static __global__ void k_queue_scatter(const int* __restrict__ steps, long long 
         for (int i = threadIdx.x; i < QUEUE_BINS; i += blockDim.x)
             base[i] = cnt[i] ? atomicAdd(&cursor[i], (unsigned long long)cnt[i]) : 0ull;
         __syncthreads();
-        if (c < ncell) order[base[b] + rank] = (int)c;
+        // base + rank < ncell when the counts are the ones k_queue_hist saw; the check keeps a
+        // count array changed between the two kernels from writing past the order array
+        if (c < ncell && base[b] + rank < (unsigned long long)ncell) order[base[b] + rank] = (int)c;
         __syncthreads();
     }
 }
