@@ -23,11 +23,12 @@ BUILD = PKG / "_build"
 LIB = BUILD / "libcmaqchem.so"
 # Build variants the autotuner can choose from: name -> (extra nvcc flags of the generated
 # mechanism code, extra flags of every translation unit).  The default library caps the
-# generated LU / solve / rate / adjoint functions at 80 registers and turns on their L2
-# prefetch a few rows ahead, and the work-queue kernel carries launch bounds for 24
-# resident warps per SM; this measured fastest (see the launch-shape sweep in profiles/).
-# The EBI routines and the kernels' own code are not capped.
-GEN_DEFAULT = ["-maxrregcount=80", "-DCHEM_USE_PREFETCH"]
+# generated LU / solve / rate / adjoint functions at 80 registers without their L2 prefetch
+# of the next rows' workspace (with 24 resident warps per SM the prefetched lines were
+# evicted before use: 2.7 % slower, variant pf80), and the work-queue kernel carries launch
+# bounds for 24 resident warps per SM; this measured fastest (see the launch-shape sweep in
+# profiles/).  The EBI routines and the kernels' own code are not capped.
+GEN_DEFAULT = ["-maxrregcount=80"]
 Q_DEFAULT = "-DCHEM_QUEUE_WARPS_PER_SM=24"
 GEN128 = ["-maxrregcount=128", "-DCHEM_USE_PREFETCH"]
 Q8, Q16 = "-DCHEM_QUEUE_WARPS_PER_SM=8", "-DCHEM_QUEUE_WARPS_PER_SM=16"
@@ -44,8 +45,8 @@ VARIANTS = {"default": (GEN_DEFAULT, [Q_DEFAULT]),
             # 1/U(i,i) by the correctly rounded reciprocal (same bits); L1 prefetch of the next row
             "rcp": (GEN_DEFAULT + ["-DCHEM_RCP(x)=__drcp_rn(x)"], [Q_DEFAULT]),
             "pfl1": (GEN_DEFAULT + ["-DCHEM_USE_PREFETCH_L1"], [Q_DEFAULT]),
-            # the default build without the L2 prefetch of the next rows' workspace reads
-            "nopf80": (["-maxrregcount=80"], [Q_DEFAULT]),
+            # the default build with the L2 prefetch of the next rows' workspace reads
+            "pf80": (["-maxrregcount=80", "-DCHEM_USE_PREFETCH"], [Q_DEFAULT]),
             # other register caps with as many resident warps as they allow
             "r96w20": (["-maxrregcount=96", "-DCHEM_USE_PREFETCH"], ["-DCHEM_QUEUE_WARPS_PER_SM=20"]),
             "r72w28": (["-maxrregcount=72", "-DCHEM_USE_PREFETCH"], ["-DCHEM_QUEUE_WARPS_PER_SM=28"]),
