@@ -101,8 +101,11 @@ int cmaqchem_step(cmaqchem_handle* h, float* conc, const float* ta, const float*
                   const float* ocean_szone, const float* rj, const double* khetero,
                   int jdate, int jtime, const int tstep[3], cmaqchem_stats* stats);
 
-/* Same call on device-resident arrays (same layouts), enqueued on `stream`
- * (a cudaStream_t, NULL for the default stream); returns after the stream is idle. */
+/* Same call on device-resident arrays (same layouts), enqueued on `stream` (a
+ * cudaStream_t; NULL: the handle's own stream, which first waits for the work already on
+ * the legacy default stream, so inputs written there are complete).  The entries below
+ * that take a handle and a stream treat NULL the same way.  Returns after the stream is
+ * idle. */
 int cmaqchem_step_device(cmaqchem_handle* h, float* conc, const float* ta, const float* qv,
                          const float* dens, const float* pres, const float* seaice,
                          const float* ocean_szone, const float* rj, const double* khetero,
