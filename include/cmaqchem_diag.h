@@ -52,7 +52,7 @@ int cmaqchem_diag_fp64_issue(int device, int active_lanes, double* cycles_per_in
  * which gathers the rates; 0: the solver kernel evaluates them in the lanes it refills;
  * same results) and
  * "queue_history" (0: clear the step counts the work queue is ordered by, so that the next
- * call is queued as a fresh run's first call) and
+ * call is queued as a fresh run's first call; synchronises the device before and after) and
  * "host_chunks" (1-16, default 4: cmaqchem_step moves the grid in that many chunks of
  * consecutive cells so that copies overlap the integration of the previous chunk) and
  * "ebi_warp" (EBI solver: 1 (default) one cell per warp with its state in shared memory,
