@@ -84,6 +84,77 @@ def hetchem_harness(tmp_path_factory):
     return get
 
 
+@pytest.fixture(scope="session")
+def ros3_harness(tmp_path_factory):
+    """tests/ros3_host_harness.cpp with the mechanism's generated rate, LU and solve files
+    (the ROS3 device code built for the host) compiled by g++ under AddressSanitizer and
+    UndefinedBehaviorSanitizer, one object per file in parallel: a function of the
+    mechanism returning its executable (built once per mechanism)."""
+    import os
+    import shutil
+    import subprocess
+    from concurrent.futures import ThreadPoolExecutor
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no C++ compiler")
+    gen = ROOT / "cmaq_gb300" / "csrc" / "gen"
+    cuda_inc = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda")) / "include"
+    built = {}
+
+    def get(mech="cb6r5_ae7_aq"):
+        if mech in built:
+            return built[mech]
+        d = tmp_path_factory.mktemp(f"ros3_{mech}")
+        flags = ["-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-fsanitize=address,undefined",
+                 "-fno-sanitize-recover=all", "-I", str(cuda_inc), "-include", str(ROOT / "tests" / "cuda_host_shim.h"),
+                 f'-DMECH_HEADER="../cmaq_gb300/csrc/gen/{mech}_mech.cuh"', f"-DMECH_NS=mech_{mech}"]
+        srcs = ([ROOT / "tests" / "ros3_host_harness.cpp"] + sorted(gen.glob(f"{mech}_lu*.cu"))
+                + [gen / f"{mech}_solve0.cu", gen / f"{mech}_solve1.cu", gen / f"{mech}_rates.cu"])
+
+        def cc(src):
+            obj = d / (src.stem + ".o")
+            r = subprocess.run([gxx, *flags, "-x", "c++", "-c", str(src), "-o", str(obj)], capture_output=True,
+                               text=True)
+            return obj, r
+
+        with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+            res = list(ex.map(cc, srcs))
+        for _, r in res:
+            if r.returncode != 0 and "sanitize" in r.stderr:
+                pytest.skip("sanitizer runtime not available")
+            assert r.returncode == 0, r.stderr[-3000:]
+        exe = d / "ros3_host_harness"
+        r = subprocess.run([gxx, "-fsanitize=address,undefined", *[str(o) for o, _ in res], "-o", str(exe), "-lm"],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr[-3000:]
+        built[mech] = exe
+        return exe
+    return get
+
+
+def run_ros3_harness(exe, y0, rki, night, chemstep, rtol, atol, workdir):
+    """The host build's per-cell ROS3 over chemstep minutes: y [ISCHAN][n] (new species
+    order), rki [NRXNS][n], night [n]; returns (y, nsteps, nfails, status)."""
+    import os
+    import subprocess
+    import numpy as np
+    n = y0.shape[1]
+    inp, out = workdir / "ros3_in.bin", workdir / "ros3_out.bin"
+    np.concatenate([np.ascontiguousarray(y0, np.float64).view(np.uint8).ravel(),
+                    np.ascontiguousarray(rki, np.float64).view(np.uint8).ravel(),
+                    np.ascontiguousarray(night, np.uint8).ravel()]).tofile(inp)
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=1:abort_on_error=0", UBSAN_OPTIONS="halt_on_error=1")
+    r = subprocess.run([str(exe), str(inp), str(out), str(n), repr(float(chemstep)), repr(float(rtol)),
+                        repr(float(atol))], capture_output=True, text=True, timeout=900, env=env)
+    assert r.returncode == 0, r.stderr[-3000:]
+    assert "runtime error" not in r.stderr, r.stderr[-3000:]
+    raw = np.fromfile(out, np.uint8)
+    ny = y0.size * 8
+    y = raw[:ny].view(np.float64).reshape(y0.shape)
+    st = raw[ny:].view(np.int32).reshape(3, n)
+    return y, st[0], st[1], st[2]
+
+
 def run_hetchem_harness(exe, ae, ta, pres, qv, dens, workdir):
     """KHETERO [ncell][NHET] of the host build for the aerosol block ae [NAE][ncell] and met."""
     import os
