@@ -897,6 +897,8 @@ def main():
         dims = WORKLOADS[a.workload]
         ncell = dims["ncols"] * dims["nrows"] * dims["nlays"]
         r = run_hetchem(device, ncell, min(a.steps, 5), thr)
+        if not a.no_configs:                          # CRACMM2's tables on its 200x200x25 grid
+            r["cracmm2"] = run_hetchem(device, 1000000, min(a.steps, 5), min(thr, 4), "cracmm2")
         if rank == 0:
             line = {"metric": "HETCHEM_RATES: grid cells of KHETERO per second", "value": r["value"],
                     "unit": "cells/s", "n_gpus": 1, "steps": min(a.steps, 5), "warmup": 3,
