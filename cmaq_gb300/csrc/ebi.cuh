@@ -176,6 +176,9 @@ __device__ void iterate(double* __restrict__ ws, State& s, int max_iter, double*
 
 }  // namespace ebi
 
+// EBI_CELL_ONLY: the per-cell state machine above without the kernels below (the host
+// build of the CPU tests)
+#ifndef EBI_CELL_ONLY
 #include "chem_kernels.cuh"
 #include "queue_kernels.cuh"
 
@@ -614,3 +617,4 @@ __global__ void __launch_bounds__(EBIW_WPB * 32) k_chem_ebi_warp(GridArgs a, Que
 }
 
 }  // namespace chem
+#endif  // EBI_CELL_ONLY

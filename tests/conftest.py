@@ -84,12 +84,10 @@ def hetchem_harness(tmp_path_factory):
     return get
 
 
-@pytest.fixture(scope="session")
-def ros3_harness(tmp_path_factory):
-    """tests/ros3_host_harness.cpp with the mechanism's generated rate, LU and solve files
-    (the ROS3 device code built for the host) compiled by g++ under AddressSanitizer and
-    UndefinedBehaviorSanitizer, one object per file in parallel: a function of the
-    mechanism returning its executable (built once per mechanism)."""
+def _host_build(tmp_path_factory, name, mech, srcs):
+    """g++ build of a host harness with the mechanism's generated device files (csrc/gen)
+    under AddressSanitizer and UndefinedBehaviorSanitizer, one object per file in
+    parallel; CUDA qualifiers shimmed by tests/cuda_host_shim.h."""
     import os
     import shutil
     import subprocess
@@ -97,39 +95,82 @@ def ros3_harness(tmp_path_factory):
     gxx = shutil.which("g++")
     if gxx is None:
         pytest.skip("no C++ compiler")
-    gen = ROOT / "cmaq_gb300" / "csrc" / "gen"
+    d = tmp_path_factory.mktemp(f"{name}_{mech}")
     cuda_inc = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda")) / "include"
+    flags = ["-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-fsanitize=address,undefined",
+             "-fno-sanitize-recover=all", "-I", str(cuda_inc), "-include", str(ROOT / "tests" / "cuda_host_shim.h"),
+             f'-DMECH_HEADER="../cmaq_gb300/csrc/gen/{mech}_mech.cuh"', f"-DMECH_NS=mech_{mech}"]
+
+    def cc(src):
+        obj = d / (src.stem + ".o")
+        r = subprocess.run([gxx, *flags, "-x", "c++", "-c", str(src), "-o", str(obj)], capture_output=True, text=True)
+        return obj, r
+
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        res = list(ex.map(cc, srcs))
+    for _, r in res:
+        if r.returncode != 0 and "sanitize" in r.stderr:
+            pytest.skip("sanitizer runtime not available")
+        assert r.returncode == 0, r.stderr[-3000:]
+    exe = d / name
+    r = subprocess.run([gxx, "-fsanitize=address,undefined", *[str(o) for o, _ in res], "-o", str(exe), "-lm"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    return exe
+
+
+@pytest.fixture(scope="session")
+def ros3_harness(tmp_path_factory):
+    """tests/ros3_host_harness.cpp with the mechanism's generated rate, LU and solve files
+    (the ROS3 device code built for the host): a function of the mechanism returning its
+    executable (built once per mechanism)."""
+    gen = ROOT / "cmaq_gb300" / "csrc" / "gen"
     built = {}
 
     def get(mech="cb6r5_ae7_aq"):
-        if mech in built:
-            return built[mech]
-        d = tmp_path_factory.mktemp(f"ros3_{mech}")
-        flags = ["-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-fsanitize=address,undefined",
-                 "-fno-sanitize-recover=all", "-I", str(cuda_inc), "-include", str(ROOT / "tests" / "cuda_host_shim.h"),
-                 f'-DMECH_HEADER="../cmaq_gb300/csrc/gen/{mech}_mech.cuh"', f"-DMECH_NS=mech_{mech}"]
-        srcs = ([ROOT / "tests" / "ros3_host_harness.cpp"] + sorted(gen.glob(f"{mech}_lu*.cu"))
-                + [gen / f"{mech}_solve0.cu", gen / f"{mech}_solve1.cu", gen / f"{mech}_rates.cu"])
-
-        def cc(src):
-            obj = d / (src.stem + ".o")
-            r = subprocess.run([gxx, *flags, "-x", "c++", "-c", str(src), "-o", str(obj)], capture_output=True,
-                               text=True)
-            return obj, r
-
-        with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
-            res = list(ex.map(cc, srcs))
-        for _, r in res:
-            if r.returncode != 0 and "sanitize" in r.stderr:
-                pytest.skip("sanitizer runtime not available")
-            assert r.returncode == 0, r.stderr[-3000:]
-        exe = d / "ros3_host_harness"
-        r = subprocess.run([gxx, "-fsanitize=address,undefined", *[str(o) for o, _ in res], "-o", str(exe), "-lm"],
-                           capture_output=True, text=True)
-        assert r.returncode == 0, r.stderr[-3000:]
-        built[mech] = exe
-        return exe
+        if mech not in built:
+            srcs = ([ROOT / "tests" / "ros3_host_harness.cpp"] + sorted(gen.glob(f"{mech}_lu*.cu"))
+                    + [gen / f"{mech}_solve0.cu", gen / f"{mech}_solve1.cu", gen / f"{mech}_rates.cu"])
+            built[mech] = _host_build(tmp_path_factory, "ros3_host_harness", mech, srcs)
+        return built[mech]
     return get
+
+
+@pytest.fixture(scope="session")
+def ebi_harness(tmp_path_factory):
+    """tests/ebi_host_harness.cpp with the mechanism's generated EBI routines (the EBI
+    device code built for the host): a function of the mechanism returning its executable."""
+    gen = ROOT / "cmaq_gb300" / "csrc" / "gen"
+    built = {}
+
+    def get(mech="cb6r5_ae7_aq"):
+        if mech not in built:
+            srcs = [ROOT / "tests" / "ebi_host_harness.cpp", gen / f"{mech}_ebi.cu", gen / f"{mech}_rates.cu"]
+            built[mech] = _host_build(tmp_path_factory, "ebi_host_harness", mech, srcs)
+        return built[mech]
+    return get
+
+
+def run_ebi_harness(exe, yc0, rki, tstep_sec, workdir):
+    """The host build's HRSOLVER over tstep_sec: yc [NSPEC][n] (mechanism order), rki
+    [NRXNS][n]; returns (yc, status, iterations)."""
+    import os
+    import subprocess
+    import numpy as np
+    n = yc0.shape[1]
+    inp, out = workdir / "ebi_in.bin", workdir / "ebi_out.bin"
+    np.concatenate([np.ascontiguousarray(yc0, np.float64).view(np.uint8).ravel(),
+                    np.ascontiguousarray(rki, np.float64).view(np.uint8).ravel()]).tofile(inp)
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=1:abort_on_error=0", UBSAN_OPTIONS="halt_on_error=1")
+    r = subprocess.run([str(exe), str(inp), str(out), str(n), str(int(tstep_sec))], capture_output=True, text=True,
+                       timeout=900, env=env)
+    assert r.returncode == 0, r.stderr[-3000:]
+    assert "runtime error" not in r.stderr, r.stderr[-3000:]
+    raw = np.fromfile(out, np.uint8)
+    ny = yc0.size * 8
+    yc = raw[:ny].view(np.float64).reshape(yc0.shape)
+    st = raw[ny:].view(np.int32).reshape(2, n)
+    return yc, st[0], st[1]
 
 
 def run_ros3_harness(exe, y0, rki, night, chemstep, rtol, atol, workdir):
