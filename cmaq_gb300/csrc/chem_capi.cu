@@ -214,50 +214,9 @@ int configure_queue(cmaqchem_handle* h)
     return ensure_ws(h, (size_t)h->q_nblocks * h->q_wpb);
 }
 
-// Gear coefficients and tolerances: GRINIT / JSPARSE constants (grinit.F:163-171,
-// grsprse.F:682-720) and the OPTIMAL_ATOL_PPM levels (GRVARS.F:640-668); the same numbers
-// as the oracle's (REAL(4) expressions in REAL(4)).
-void gear_coefficients(double rtol, float max_atol, float min_atol, float conc_floor, int max_iter, gear::Coef* g)
-{
-    static const double pertst[3][7] = {{2.0, 4.5, 7.333, 10.42, 13.7, 17.15, 1.0},
-                                        {3.0, 6.0, 9.167, 12.5, 15.98, 1.0, 1.0},
-                                        {1.0, 1.0, 0.5, 0.1667, 0.04133, 0.008267, 1.0}};
-    *g = gear::Coef{};
-    for (int q = 0; q < 7; ++q) {
-        const int nqq = q + 1;
-        g->enqq1[q] = (double)(0.5f / (float)nqq);
-        g->enqq2[q] = (double)(0.5f / (float)(nqq + 1));
-        g->enqq3[q] = (double)(0.5f / (float)(nqq + 2));
-        g->conpst[q] = 1.0 / (pertst[0][q] * g->enqq3[q]);
-        g->conp15[q] = 1.5 * g->conpst[q];
-        for (int k = 0; k < 3; ++k) g->pertst[q][k] = pertst[k][q] * pertst[k][q];
-    }
-    // Nordsieck coefficients of the BDF formulas of order 1-6 (grsprse.F:698-720)
-    const double rows[6][7] = {{1.0, 1.0},
-                               {2.0 / 3.0, 1.0, 1.0 / 3.0},
-                               {6.0 / 11.0, 1.0, 6.0 / 11.0, 1.0 / 11.0},
-                               {12.0 / 25.0, 1.0, 0.70, 0.20, 0.02},
-                               {60.0 / 137.0, 1.0, 225.0 / 274.0, 85.0 / 274.0, 15.0 / 274.0, 1.0 / 274.0},
-                               {180.0 / 441.0, 1.0, 406.0 / 441.0, 735.0 / 1764.0, 175.0 / 1764.0, 21.0 / 1764.0,
-                                1.0 / 1764.0}};
-    for (int i = 0; i < 6; ++i)
-        for (int j = 0; j < 7; ++j) g->aset[i][j] = rows[i][j];
-    g->errmax = rtol;
-    g->ylow = (double)min_atol;
-    const double abhi = log10((double)max_atol), ablo = log10((double)min_atol);
-    g->atol_level[0] = pow(10.0, abhi);
-    g->atol_level[gear::NBINS] = pow(10.0, ablo);
-    for (int i = 2; i <= gear::NBINS; ++i) {
-        const double t = (abhi - ablo) * (double)(gear::NBINS - i + 1) / (double)gear::NBINS;
-        g->atol_level[i - 1] = pow(10.0, ablo + t);
-    }
-    g->atol_floor = (double)conc_floor;
-    g->max_iter = max_iter;
-}
-
 int upload_gear_coef(cmaqchem_handle* h)
 {
-    gear_coefficients(h->cfg.rtol, h->gear_max_atol, h->gear_min_atol, h->gear_floor, h->max_iter, &h->gear_coef);
+    gear::coefficients(h->cfg.rtol, h->gear_max_atol, h->gear_min_atol, h->gear_floor, h->max_iter, &h->gear_coef);
     if (!h->d_gear_coef) CK(cudaMalloc(&h->d_gear_coef, sizeof(gear::Coef)));
     CK(cudaMemcpy(h->d_gear_coef, &h->gear_coef, sizeof(gear::Coef), cudaMemcpyHostToDevice));
     return 0;

@@ -24,7 +24,11 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <math_constants.h>
+// GEAR_CELL_ONLY: the per-cell SMVGEAR code without the kernels at the end (the host
+// build of the CPU tests)
+#ifndef GEAR_CELL_ONLY
 #include "queue_kernels.cuh"
+#endif
 
 namespace gear {
 
@@ -50,6 +54,47 @@ struct Coef {
     double atol_floor;            // REAL(GEAR_CONC_FLOOR, 8)
     int max_iter;                 // cap on SUBFUN calls per cell and call (0: none)
 };
+
+// Gear coefficients and tolerances: GRINIT / JSPARSE constants (grinit.F:163-171,
+// grsprse.F:682-720) and the OPTIMAL_ATOL_PPM levels (GRVARS.F:640-668); the same numbers
+// as the oracle's (REAL(4) expressions in REAL(4)).
+inline void coefficients(double rtol, float max_atol, float min_atol, float conc_floor, int max_iter, Coef* g)
+{
+    static const double pertst[3][7] = {{2.0, 4.5, 7.333, 10.42, 13.7, 17.15, 1.0},
+                                        {3.0, 6.0, 9.167, 12.5, 15.98, 1.0, 1.0},
+                                        {1.0, 1.0, 0.5, 0.1667, 0.04133, 0.008267, 1.0}};
+    *g = Coef{};
+    for (int q = 0; q < 7; ++q) {
+        const int nqq = q + 1;
+        g->enqq1[q] = (double)(0.5f / (float)nqq);
+        g->enqq2[q] = (double)(0.5f / (float)(nqq + 1));
+        g->enqq3[q] = (double)(0.5f / (float)(nqq + 2));
+        g->conpst[q] = 1.0 / (pertst[0][q] * g->enqq3[q]);
+        g->conp15[q] = 1.5 * g->conpst[q];
+        for (int k = 0; k < 3; ++k) g->pertst[q][k] = pertst[k][q] * pertst[k][q];
+    }
+    // Nordsieck coefficients of the BDF formulas of order 1-6 (grsprse.F:698-720)
+    const double rows[6][7] = {{1.0, 1.0},
+                               {2.0 / 3.0, 1.0, 1.0 / 3.0},
+                               {6.0 / 11.0, 1.0, 6.0 / 11.0, 1.0 / 11.0},
+                               {12.0 / 25.0, 1.0, 0.70, 0.20, 0.02},
+                               {60.0 / 137.0, 1.0, 225.0 / 274.0, 85.0 / 274.0, 15.0 / 274.0, 1.0 / 274.0},
+                               {180.0 / 441.0, 1.0, 406.0 / 441.0, 735.0 / 1764.0, 175.0 / 1764.0, 21.0 / 1764.0,
+                                1.0 / 1764.0}};
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 7; ++j) g->aset[i][j] = rows[i][j];
+    g->errmax = rtol;
+    g->ylow = (double)min_atol;
+    const double abhi = log10((double)max_atol), ablo = log10((double)min_atol);
+    g->atol_level[0] = pow(10.0, abhi);
+    g->atol_level[NBINS] = pow(10.0, ablo);
+    for (int i = 2; i <= NBINS; ++i) {
+        const double t = (abhi - ablo) * (double)(NBINS - i + 1) / (double)NBINS;
+        g->atol_level[i - 1] = pow(10.0, ablo + t);
+    }
+    g->atol_floor = (double)conc_floor;
+    g->max_iter = max_iter;
+}
 
 enum { ST_OK = 0, ST_DT_UNDERFLOW = 1, ST_MAXITER = 2, ST_NONFINITE = 4 };
 enum { L_BEGIN = 0, L_INIT_POST = 1, L_ITER_POST = 2, L_DONE = 3 };
@@ -748,6 +793,7 @@ __device__ __forceinline__ void evaluate(double* __restrict__ ws, const State& s
 
 }  // namespace gear
 
+#ifndef GEAR_CELL_ONLY
 namespace chem {
 
 #ifndef GEAR_WARPS_PER_SM
@@ -940,3 +986,4 @@ __global__ void __launch_bounds__(32) k_gear_warp(GridArgs a, QueueArgs q, GearA
 }
 
 }  // namespace chem
+#endif  // GEAR_CELL_ONLY

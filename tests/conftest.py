@@ -151,6 +151,45 @@ def ebi_harness(tmp_path_factory):
     return get
 
 
+@pytest.fixture(scope="session")
+def gear_harness(tmp_path_factory):
+    """tests/gear_host_harness.cpp with the mechanism's generated f, PDERIV, LU and solve
+    routines and the cooperative kernel's tables (the SMVGEAR device code built for the
+    host): a function of the mechanism returning its executable."""
+    gen = ROOT / "cmaq_gb300" / "csrc" / "gen"
+    built = {}
+
+    def get(mech="cb6r5_ae7_aq"):
+        if mech not in built:
+            srcs = ([ROOT / "tests" / "gear_host_harness.cpp"] + sorted(gen.glob(f"{mech}_glu*.cu"))
+                    + [gen / f"{mech}_solve0.cu", gen / f"{mech}_rates.cu", gen / f"{mech}_gw_tables.cu"])
+            built[mech] = _host_build(tmp_path_factory, "gear_host_harness", mech, srcs)
+        return built[mech]
+    return get
+
+
+def run_gear_harness(exe, y0, rk, night, chemstep, rtol, max_atol, min_atol, conc_floor, workdir):
+    """The host build's SMVGEAR over chemstep minutes: y [NSPEC][n] (solver order), rk
+    [NRXNS][n], night [n]; returns (y, stats [n][8])."""
+    import os
+    import subprocess
+    import numpy as np
+    n = y0.shape[1]
+    inp, out = workdir / "gear_in.bin", workdir / "gear_out.bin"
+    np.concatenate([np.ascontiguousarray(y0, np.float64).view(np.uint8).ravel(),
+                    np.ascontiguousarray(rk, np.float64).view(np.uint8).ravel(),
+                    np.ascontiguousarray(night, np.uint8).ravel()]).tofile(inp)
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=1:abort_on_error=0", UBSAN_OPTIONS="halt_on_error=1")
+    r = subprocess.run([str(exe), str(inp), str(out), str(n), repr(float(chemstep)), repr(float(rtol)),
+                        repr(float(max_atol)), repr(float(min_atol)), repr(float(conc_floor))],
+                       capture_output=True, text=True, timeout=900, env=env)
+    assert r.returncode == 0, r.stderr[-3000:]
+    assert "runtime error" not in r.stderr, r.stderr[-3000:]
+    raw = np.fromfile(out, np.uint8)
+    ny = y0.size * 8
+    return raw[:ny].view(np.float64).reshape(y0.shape), raw[ny:].view(np.int32).reshape(n, 8)
+
+
 def run_ebi_harness(exe, yc0, rki, tstep_sec, workdir):
     """The host build's HRSOLVER over tstep_sec: yc [NSPEC][n] (mechanism order), rki
     [NRXNS][n]; returns (yc, status, iterations)."""
