@@ -426,7 +426,8 @@ def write_outputs(cmaq_root: str, mech: str, out_root: Path = REPO) -> dict:
     cdir = REPO_ / "cmaq_gb300" / "csrc" / "gen"
     cdir.mkdir(parents=True, exist_ok=True)
     for old in cdir.glob(f"{mech}_*"):
-        old.unlink()
+        if not old.name.endswith("_hetchem.cuh"):   # written by mechgen/hetchem.py
+            old.unlink()
     ebi_decl, ebi_tu = ebi_cuda_source(ebi, mech, m.nspec)
     for fname, text in cuda_sources(m, prog, sp, mech, src_hash, ebi_decl).items():
         (cdir / fname).write_text(text)
